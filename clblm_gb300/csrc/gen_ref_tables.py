@@ -1,0 +1,129 @@
+"""Generate ``clblm_ref_tables.h``: the numeric tables CLBLM's line-by-line
+path reads from its Fortran source.
+
+The tables must be identical to the reference's for the results to be
+identical, so they are extracted from the reference source text rather than
+retyped.  The decimal literals are carried over verbatim; both gfortran
+(``-fdefault-real-8``) and a C compiler parse such a literal straight to the
+nearest binary64 value, so the tables are bit-identical.
+
+Tables extracted (reference file:line):
+  * Voigt-width / sub-function weights AVRAT, CGAUSS, CF1, CF2, CF3, CER
+    (102 entries each over zeta = 0, 0.01, ..., 1.01):
+    src/clblm_src/clblm_ODLAY_CommonSub.f90:43-185
+  * TIPS temperature grid Tdat(119):  src/clblm_src/clblm_ODLAY_TIPS.f90:16-29
+  * TIPS Q(T) for isotopologue 1 of HITRAN molecules 1-9 (H2O, CO2, O3, N2O,
+    CO, CH4, O2, NO, SO2): the ``QofT( 1,J)`` DATA blocks of QT_H2O ... QT_SO2,
+    src/clblm_src/clblm_ODLAY_TIPS.f90:424-2254
+  * isotopologue-1 molecular masses of molecules 1-9:
+    src/common/clblm_ConstParam.f90:263-290
+
+Run (in a tree where the reference is mounted):
+    python clblm_gb300/csrc/gen_ref_tables.py /root/reference > clblm_gb300/csrc/clblm_ref_tables.h
+The generated header is committed; the build never needs the reference.
+"""
+import re
+import sys
+from pathlib import Path
+
+NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[EeDd][-+]?\d+)?"
+
+
+def _numbers(text):
+    out = []
+    for tok in re.findall(NUM, text):
+        out.append(tok.replace("D", "E").replace("d", "e"))
+    return out
+
+
+def _fortran_array(src, name):
+    m = re.search(r"real\s*,\s*PARAMETER\s*::\s*%s\s*\(1:102\)\s*=\s*\[(.*?)\]" % name,
+                  src, re.S | re.I)
+    if not m:
+        raise SystemExit("table %s not found" % name)
+    body = "\n".join(line.split("!")[0] for line in m.group(1).splitlines())
+    vals = _numbers(body)
+    if len(vals) != 102:
+        raise SystemExit("table %s: %d values" % (name, len(vals)))
+    return vals
+
+
+def _tips_grid(src):
+    m = re.search(r"Tdat\(NT\)\s*=\s*\[(.*?)\]", src, re.S)
+    vals = _numbers(m.group(1).replace("&", " "))
+    if len(vals) != 119:
+        raise SystemExit("Tdat: %d values" % len(vals))
+    return vals
+
+
+def _tips_iso1(src, mol):
+    start = re.search(r"Subroutine\s+QT_%s\b" % mol, src, re.I)
+    if not start:
+        raise SystemExit("QT_%s not found" % mol)
+    rest = src[start.end():]
+    m = re.search(r"data\s*\(QofT\(\s*1,J\),J=1,119\)\s*/(.*?)/", rest, re.S | re.I)
+    body = "\n".join(line.split("!")[0] for line in m.group(1).splitlines())
+    vals = _numbers(body.replace("&", " "))
+    if len(vals) != 119:
+        raise SystemExit("QT_%s iso1: %d values" % (mol, len(vals)))
+    return vals
+
+
+def _masses(src):
+    out = []
+    for m_id in range(1, 10):
+        m = re.search(r"data\s*\(isotpl_mass\(%d,i\),i=1,\d+\)\s*&?\s*&?\s*/\s*(%s)" % (m_id, NUM),
+                      src, re.S | re.I)
+        if not m:
+            raise SystemExit("mass of molecule %d not found" % m_id)
+        out.append(m.group(1))
+    return out
+
+
+def main(ref_root):
+    ref = Path(ref_root)
+    common = (ref / "src/clblm_src/clblm_ODLAY_CommonSub.f90").read_text(errors="replace")
+    tips = (ref / "src/clblm_src/clblm_ODLAY_TIPS.f90").read_text(errors="replace")
+    const = (ref / "src/common/clblm_ConstParam.f90").read_text(errors="replace")
+
+    lines = [
+        "/* Generated by gen_ref_tables.py from the CLBLM Fortran source; do not edit.",
+        " * Decimal literals are carried over verbatim so that the binary64 values match",
+        " * the reference's (-fdefault-real-8) tables bit for bit. */",
+        "#ifndef CLBLM_REF_TABLES_H",
+        "#define CLBLM_REF_TABLES_H",
+        "",
+    ]
+
+    def emit(name, vals, per=5):
+        lines.append("static const double %s[%d] = {" % (name, len(vals)))
+        for i in range(0, len(vals), per):
+            lines.append("    " + ", ".join(vals[i:i + per]) + ",")
+        lines.append("};")
+        lines.append("")
+
+    # clblm_ODLAY_CommonSub.f90:43-185
+    for name in ("AVRAT", "CGAUSS", "CF1", "CF2", "CF3", "CER"):
+        emit("CLBLM_" + name, _fortran_array(common, name))
+    # clblm_ODLAY_TIPS.f90:16-29
+    emit("CLBLM_TIPS_TDAT", _tips_grid(tips), per=8)
+    mols = ("H2O", "CO2", "O3", "N2O", "CO", "CH4", "O2", "NO", "SO2")
+    lines.append("/* TIPS Q(T) of isotopologue 1, HITRAN molecules 1..9 (%s) */" % ", ".join(mols))
+    lines.append("#define CLBLM_TIPS_NMOL 9")
+    lines.append("static const double CLBLM_TIPS_Q_ISO1[9][119] = {")
+    for mol in mols:
+        vals = _tips_iso1(tips, mol)
+        lines.append("  { /* %s */" % mol)
+        for i in range(0, len(vals), 6):
+            lines.append("    " + ", ".join(vals[i:i + 6]) + ",")
+        lines.append("  },")
+    lines.append("};")
+    lines.append("")
+    # clblm_ConstParam.f90:263-290
+    emit("CLBLM_ISO1_MASS", _masses(const), per=9)
+    lines.append("#endif")
+    sys.stdout.write("\n".join(lines) + "\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

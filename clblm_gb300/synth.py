@@ -1,0 +1,135 @@
+"""Seeded synthetic inputs of the benchmark workloads.
+
+No public dataset or line database is involved: the line lists, atmospheres
+and continuum table are drawn from numpy's PCG64 generator with the seed
+equal to the workload index, using the distributions the workloads specify:
+
+  * lines: centres uniform on the window (sorted), intensities log-uniform on
+    1e-26..1e-19 cm/molecule at 296 K, air half-widths uniform 0.05-0.10
+    cm-1/atm, self half-widths 1.5-5x air, temperature exponents 0.5-0.8,
+    lower-state energies 0-3000 cm-1, pressure shifts +-0.005 cm-1/atm.
+    Precision as on TAPE3: centre binary64, the rest binary32.
+  * atmosphere: pressure falling exponentially (levels equally spaced in
+    ln p), temperature 288 K at the surface, lapse to 217 K at 11 km, warming
+    linearly to 270 K at 50 km and constant above; altitudes from a 7 km
+    scale height.  Layer pressure is the geometric mean of its levels,
+    temperature the arithmetic mean.  Layer air columns from hydrostatics.
+    H2O volume mixing ratio 1e-2 exp(-z / 2 km), floored at 4e-6.
+  * continuum: a smooth self/foreign table on the MT_CKD grid (-20..20000
+    cm-1 by 10) with log-normal magnitudes and self T-exponents in 2..4.
+"""
+import numpy as np
+
+from .capi_types import Column, Continuum, Lines
+
+# HITRAN numbers of the seven synthetic absorbers (iso 1 each).  O2 (7) is left
+# out: the reference turns an O2 air width into a foreign width as
+# (alfa - 0.21 hwhm) / 0.79 (RDLIN, clblm_ODLAY.f90:2705-2712), which goes
+# negative for the workload's self widths of up to 5x air.
+SEVEN = np.array([1, 2, 3, 4, 5, 6, 8], dtype=np.int32)
+# constant volume mixing ratio of absorbers 2..7 (absorber 1 is H2O-like)
+OTHER_VMR = 1.0e-5
+AIR_COLUMN_PER_HPA = 100.0 / (9.80665 * 28.964e-3 / 6.02214199e23) / 1.0e4  # molec/cm2/hPa
+SECANT_DIFFUSE = 1.67  # clblm_ConstParam.f90:124
+
+
+def line_list(n, v1, v2, seed, mols=(1,)):
+    """n lines on [v1, v2] with the workload distributions; molecules drawn
+    uniformly from `mols` (HITRAN numbers, isotopologue 1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vnu = np.sort(rng.uniform(v1, v2, n))
+    sp = 10.0 ** rng.uniform(-26.0, -19.0, n)
+    alfa = rng.uniform(0.05, 0.10, n)
+    hwhm = alfa * rng.uniform(1.5, 5.0, n)
+    tmpalf = rng.uniform(0.5, 0.8, n)
+    epp = rng.uniform(0.0, 3000.0, n)
+    pshift = rng.uniform(-0.005, 0.005, n)
+    mols = np.asarray(mols, dtype=np.int32)
+    mol = mols[rng.integers(0, len(mols), n)] + 100
+    return Lines(vnu=vnu, sp=sp.astype(np.float32), alfa=alfa.astype(np.float32),
+                 epp=epp.astype(np.float32), mol=mol.astype(np.int32),
+                 hwhm=hwhm.astype(np.float32), tmpalf=tmpalf.astype(np.float32),
+                 pshift=pshift.astype(np.float32), iflg=np.zeros(n, np.int32))
+
+
+def continuum(seed=7):
+    """Smooth synthetic self/foreign coefficients on the MT_CKD 10 cm-1 grid."""
+    rng = np.random.Generator(np.random.PCG64(1000 + seed))
+    n = 2003
+    v = -20.0 + 10.0 * np.arange(n)
+
+    def smooth_lognormal(mean_log10, sigma):
+        z = rng.standard_normal(n + 64)
+        k = np.exp(-0.5 * (np.arange(-32, 33) / 8.0) ** 2)
+        z = np.convolve(z, k / np.sqrt((k * k).sum()), mode="same")[32:32 + n]
+        return 10.0 ** (mean_log10 + sigma * z)
+
+    self_ref = smooth_lognormal(-22.0, 0.6)
+    for_ref = smooth_lognormal(-24.0, 0.5)
+    texp = 2.0 + 2.0 * rng.uniform(0.0, 1.0, n)
+    texp = np.convolve(texp, np.ones(9) / 9.0, mode="same")
+    texp[:4] = texp[4]
+    texp[-4:] = texp[-5]
+    return Continuum(v[0], 10.0, self_ref, for_ref, texp, 1013.0, 296.0)
+
+
+def temperature(z_km):
+    z = np.asarray(z_km, dtype=np.float64)
+    t = np.where(z <= 11.0, 288.0 + (217.0 - 288.0) * z / 11.0,
+                 np.where(z <= 50.0, 217.0 + (270.0 - 217.0) * (z - 11.0) / 39.0, 270.0))
+    return t
+
+
+def atmosphere(nlay, p_top, v1, v2, mols=SEVEN, p_sfc=1013.0, scale_height=7.0,
+               other_vmr=OTHER_VMR, emis=0.98):
+    """Layered nadir column, layer 0 at the surface."""
+    k = np.arange(nlay + 1)
+    p_lev = p_sfc * (p_top / p_sfc) ** (k / nlay)
+    z_lev = -scale_height * np.log(p_lev / p_sfc)
+    t_lev = temperature(z_lev)
+    pave = np.sqrt(p_lev[:-1] * p_lev[1:])
+    tave = 0.5 * (t_lev[:-1] + t_lev[1:])
+    zmid = 0.5 * (z_lev[:-1] + z_lev[1:])
+    wair = (p_lev[:-1] - p_lev[1:]) * AIR_COLUMN_PER_HPA
+    mols = np.asarray(mols, dtype=np.int32)
+    w = np.zeros((nlay, len(mols)))
+    for j, m in enumerate(mols):
+        if m == 1:
+            vmr = np.maximum(1.0e-2 * np.exp(-zmid / 2.0), 4.0e-6)
+        else:
+            vmr = np.full(nlay, other_vmr)
+        w[:, j] = vmr * wair
+    return Column(mols, pave, tave, t_lev[:-1], t_lev[1:], w, wair, SECANT_DIFFUSE * wair,
+                  v1, v2, t_lev[0], emis)
+
+
+# ---- the benchmark workloads --------------------------------------------
+
+def config0():
+    """One homogeneous layer, 20,000 H2O-like lines on 600-700 cm-1."""
+    lines = line_list(20000, 600.0, 700.0, seed=0, mols=(1,))
+    wabs = 1.0e22
+    wtot = 2.479e24  # 1 km of air at 1013.25 hPa, 296 K (not given by the workload)
+    col = Column(np.array([1], np.int32), [1013.25], [296.0], [296.0], [296.0],
+                 np.array([[wabs]]), [wtot], [SECANT_DIFFUSE * wtot], 600.0, 700.0, 296.0, 1.0)
+    return lines, col
+
+
+def config1(n_lines=500000):
+    """60 layers 1013->0.1 hPa, seven absorbers, 500,000 lines on 500-2500."""
+    lines = line_list(n_lines, 500.0, 2500.0, seed=1, mols=SEVEN)
+    col = atmosphere(60, 0.1, 500.0, 2500.0)
+    return lines, col, continuum()
+
+
+def config2():
+    """config 1's atmosphere and lines over 600-1100 cm-1."""
+    lines, col, cont = config1()
+    return lines.window(600.0, 1100.0), col.with_window(600.0, 1100.0), cont
+
+
+def config4(n_lines=3000000):
+    """100 layers 1013->0.01 hPa, 3,000,000 lines on 10-3500 cm-1."""
+    lines = line_list(n_lines, 10.0, 3500.0, seed=4, mols=SEVEN)
+    col = atmosphere(100, 0.01, 10.0, 3500.0)
+    return lines, col, continuum()

@@ -1,0 +1,240 @@
+/*
+ * clblm_gb300.h -- C-ABI of the GB300 implementation of CLBLM's line-by-line
+ * hot path: per-layer monochromatic optical depth (Voigt line-by-line on
+ * nested panels + far-wing function 4 + MT_CKD-style H2O continuum) and the
+ * nadir upwelling radiance recurrence over a layered column.
+ *
+ * Plain C types only (pointers, sizes, doubles); no CUDA or torch types cross
+ * this boundary, so a Fortran ISO_C_BINDING shim, ctypes, or any C caller can
+ * bind it.  All references below are to the CLBLM Fortran source
+ * (file:line, path inside the CLBLM project).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (CLBLM_OK = 0).  The reference
+ *    STOPs the process on the same conditions; the ISO_C_BINDING shim maps a
+ *    non-zero status back to STOP with clblm_gpu_last_error()'s message.
+ *  - Output buffers are caller-allocated after a size query (the reference's
+ *    ODLAY allocates `monoOD` itself, clblm_ODLAY.f90:172).  Pass
+ *    CLBLM_OUT_DEVICE in `flags` when the buffer is device memory.
+ *  - One handle per host thread; all work of a handle runs on its own CUDA
+ *    stream.  The reference's SAVEd state (the sticky JRAD of
+ *    clblm_ODLAY.f90:182-183,349-352) lives in the handle.
+ */
+#ifndef CLBLM_GB300_H
+#define CLBLM_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------- */
+enum {
+  CLBLM_OK = 0,
+  CLBLM_ERR_ARG = 1,          /* bad pointer / size / value                    */
+  CLBLM_ERR_UNSORTED = 2,     /* line list not sorted by vnu                   */
+  CLBLM_ERR_GRID = 3,         /* bad spectral grid (V2<=V1, DV<=0, ...)        */
+  CLBLM_ERR_DV_RATIO = 4,     /* layer DV ratio > 2.5 (clblm_setDV.f90:318-320) */
+  CLBLM_ERR_RANGE = 5,        /* value outside a table (TIPS T, ABSRB size)    */
+  CLBLM_ERR_UNSUPPORTED = 6,  /* option of the reference not on this path      */
+  CLBLM_ERR_OOM = 7,          /* device allocation failed                      */
+  CLBLM_ERR_CUDA = 8,         /* CUDA runtime error                            */
+  CLBLM_ERR_CAPACITY = 9,     /* caller buffer too small                       */
+  CLBLM_ERR_NO_DEVICE = 10    /* no usable GB300 device / library not built    */
+};
+
+/* output buffer location */
+#define CLBLM_OUT_HOST   0
+#define CLBLM_OUT_DEVICE 1
+
+/* arithmetic of the device path */
+#define CLBLM_PREC_MIXED 0  /* FP32 line shape + Kahan sums, FP64 grid/index math */
+#define CLBLM_PREC_PLAIN 1  /* FP64 throughout                                    */
+
+/* Lines per record of the line file.  The reference reads TAPE3 in records of
+ * NLINEREC = 250 lines (clblm_LineData.f90:42, RDLIN clblm_ODLAY.f90:2645);
+ * record boundaries steer which lines are read and how the far-wing lines
+ * are shrunk, so the line list below is taken as consecutive records of this
+ * size. */
+#define CLBLM_LINES_PER_RECORD 250
+
+/* ---- inputs ------------------------------------------------------------ */
+
+/* Line list in structure-of-arrays form with TAPE3 precision
+ * (INPUT_BLOCK, clblm_LineData.f90:52-64): vnu is binary64, the rest binary32
+ * or int32.  Lines must be sorted by vnu (ascending). */
+typedef struct {
+  int64_t        n;
+  const double  *vnu;     /* line centre [cm-1]                                */
+  const float   *sp;      /* intensity at 296 K [cm-1/(molec cm-2)]            */
+  const float   *alfa;    /* air(foreign)-broadened HWHM at 296 K [cm-1/atm]   */
+  const float   *epp;     /* lower-state energy [cm-1]                         */
+  const int32_t *mol;     /* HITRAN molecule + 100 * isotopologue              */
+  const float   *hwhm;    /* self-broadened HWHM at 296 K [cm-1/atm]           */
+  const float   *tmpalf;  /* temperature exponent of the widths                */
+  const float   *pshift;  /* pressure shift [cm-1/atm]                         */
+  const int32_t *iflg;    /* line-coupling flag; lines with iflg < 0 skipped   */
+} clblm_lines_t;
+
+/* MT_CKD-style H2O continuum coefficient table on a uniform grid
+ * (the netCDF absco-ref_wv-mt-ckd.nc read by read_module.f90:50). */
+typedef struct {
+  int32_t       n;
+  double        v1, dv;             /* wavenumbers v1 + i*dv                   */
+  const double *self_absco_ref;     /* [n] cm2/molec/cm-1 at ref_press/temp    */
+  const double *for_absco_ref;      /* [n]                                     */
+  const double *self_texp;          /* [n] self T exponent                     */
+  double        ref_press, ref_temp;/* mbar, K                                 */
+} clblm_cont_t;
+
+/* One homogeneous layer along a path (CLBLM_Layer, clblm_AtmPath.f90:30-60):
+ * the arguments of ODLAY_nonStruct, clblm_ODLAY.f90:129-177. */
+typedef struct {
+  int32_t        nmol;
+  const int32_t *mol_id;   /* HITRAN molecule numbers of the selected absorbers */
+  const double  *w;        /* [nmol] column amounts [molec/cm2]                */
+  double         wtot;     /* total column incl. broadeners [molec/cm2]        */
+  double         pave;     /* mbar */
+  double         tave;     /* K    */
+  double         zbot, ztop;/* km, only used for the (unsupported) NLTE branch */
+  int32_t        lay_no;
+} clblm_layer_t;
+
+/* Spectral grid of one layer (CLBLM_SpectGrid + CLBLM_DV_Ctrl fields used by
+ * ODLAY_struct, clblm_ODLAY.f90:87-97). */
+typedef struct {
+  double v1, v2;       /* cm-1 */
+  double dv_normal;    /* DVnormal of this layer */
+  double dv_narrow;    /* DVnarrow of this layer */
+  double dv_out;       /* > 0: interpolate OD to this uniform DV               */
+  double sample;       /* SAMPLE (default 4)                                    */
+  double alfal0;       /* ALFAL0 (default 0.04)                                 */
+} clblm_grid_t;
+
+/* ODLAY options (CLBLM_OD_Ctrl, clblm_Config.f90:77-115). */
+typedef struct {
+  int32_t jrad;        /* JRAD, default 1; 0/-1 as in OPDPTH                    */
+  int32_t line_rejec;  /* lineRejec, default 1                                  */
+  double  dptmin;      /* DPTMIN, default 0                                     */
+  double  dptfac;      /* DPTFAC, default 0                                     */
+  double  xself;       /* XSELF continuum scale, default 1                     */
+  double  xfrgn;       /* XFRGN continuum scale, default 1                     */
+  int32_t contnm_off;  /* contnmOff                                             */
+  int32_t line_off;    /* lineOff                                               */
+  int32_t precision;   /* CLBLM_PREC_MIXED or CLBLM_PREC_PLAIN                  */
+} clblm_od_ctrl_t;
+
+/* A layered column seen in nadir from the top of the atmosphere, with the
+ * surface at the bottom (the inputs mode2_lookDn_mergeUp takes from its
+ * CLBLM_PathCompound and CLBLM_Surface, clblm_noScattRT.f90:1134-1300).
+ * Layer 0 is the lowest.  Amounts are along the viewing (reference) path;
+ * the downwelling path used for the surface-reflected term differs only in
+ * its total column `wtot_down` (airmass scaling, AMScalingThermal). */
+typedef struct {
+  int32_t        nlay;
+  int32_t        nmol;
+  const int32_t *mol_id;    /* [nmol] HITRAN numbers; must contain 1 (H2O)     */
+  const double  *pave;      /* [nlay] mbar                                     */
+  const double  *tave;      /* [nlay] K                                        */
+  const double  *tbot;      /* [nlay] K, temperature at the layer bottom       */
+  const double  *ttop;      /* [nlay] K, temperature at the layer top          */
+  const double  *w;         /* [nlay*nmol] row-major (layer, molecule)         */
+  const double  *wtot;      /* [nlay] total column along the viewing path      */
+  const double  *wtot_down; /* [nlay] total column along the downwelling path  */
+  double         v1, v2;    /* cm-1 */
+  double         tskin;     /* surface skin temperature, K                     */
+  double         emis;      /* surface emissivity (constant over v1..v2)       */
+} clblm_column_t;
+
+/* Radiative-transfer options (CLBLM_RT_Ctrl + CLBLM_DV_Ctrl). */
+typedef struct {
+  int32_t         lin_in_tau;  /* linInTau: 0, 1 (default), 2              */
+  int32_t         grid_type;   /* setDV gridType: 0 fixed ratio (RT_basic) */
+  double          sample;      /* SAMPLE, default 4                        */
+  double          alfal0;      /* ALFAL0, default 0.04                     */
+  double          alfal0_fine; /* ALFAL0_fine, default 0.005               */
+  double          dv_user;     /* user DV (<= 0: none)                     */
+  clblm_od_ctrl_t od;
+} clblm_rt_ctrl_t;
+
+/* Line bookkeeping of the last OD call: the counters HIRACQ prints
+ * (clblm_ODLAY.f90:1503-1515) plus the grids it used. */
+typedef struct {
+  int64_t nlin;        /* NLIN   lines passing molecule/amount checks          */
+  int64_t lincnt;      /* LINCNT lines convolved on the R1/R2/R3 panels        */
+  int64_t nminus;      /* NMINUS widths raised to DV                           */
+  int64_t nplus;       /* NPLUS  widths lowered to ALFMAX                      */
+  int64_t nshrunk;     /* far-wing (function 4) pseudo-lines after SHRINQ      */
+  int64_t npanels;     /* panels of NLIM1-1 = 2400 points                      */
+  int64_t nsamp;       /* OD points returned                                   */
+  double  dv;          /* DV of the convolution                                */
+  double  dvr4;        /* DV of the far-wing grid                              */
+  int32_t jrad;        /* JRAD in effect                                       */
+} clblm_od_stats_t;
+
+typedef struct clblm_handle clblm_handle_t;
+
+/* ---- entry points -------------------------------------------------------- */
+
+/* Create a handle on `device`, upload the line list (the reference reads it
+ * from TAPE3 per layer, RDLIN clblm_ODLAY.f90:2571) and the continuum table
+ * (read once by mt_ckd_h2o_absco, mt_ckd_h2o_module.f90:94-103).  `cont` may be
+ * NULL when every call has contnm_off set. */
+int clblm_gpu_create(const clblm_lines_t *lines, const clblm_cont_t *cont,
+                     int device, clblm_handle_t **out);
+
+/* Replace the handle's line list (same contract as clblm_gpu_create). */
+int clblm_gpu_set_lines(clblm_handle_t *h, const clblm_lines_t *lines);
+
+int clblm_gpu_destroy(clblm_handle_t *h);
+
+/* Message of the last failing call on this handle (or of the last failing
+ * clblm_gpu_create when h is NULL). */
+const char *clblm_gpu_last_error(const clblm_handle_t *h);
+
+/* Per-layer DVnormal / DVnarrow of a column and the uniform output DV:
+ * setDV_struct, clblm_setDV.f90:114-211 (calculateDV :221, fixDVRatio :277,
+ * DVSET :356).  Pure host arithmetic. */
+int clblm_setdv(const clblm_column_t *col, double sample, double alfal0,
+                double alfal0_fine, int32_t grid_type, double dv_user,
+                double *dv_normal, double *dv_narrow, double *dv_out);
+
+/* Number of OD points ODLAY returns for this layer and the DV they are on
+ * (clblm_ODLAY.f90:443-467 grid choice, panelOut's last-panel rule
+ * :2349-2360, DVout interpolation :571-598).  Reads the sticky JRAD state but
+ * does not change it. */
+int clblm_gpu_od_size(clblm_handle_t *h, const clblm_layer_t *layer,
+                      const clblm_grid_t *grid, const clblm_od_ctrl_t *ctrl,
+                      int64_t *nsamp, double *dv_used);
+
+/* Layer monochromatic optical depth: replaces ODLAY_nonStruct
+ * (clblm_ODLAY.f90:129-611).  Writes `nsamp` values (binary64) starting at
+ * grid->v1 with spacing `dv_used` into `out` (capacity `cap`). */
+int clblm_gpu_od(clblm_handle_t *h, const clblm_layer_t *layer,
+                 const clblm_grid_t *grid, const clblm_od_ctrl_t *ctrl,
+                 double *out, int64_t cap, int32_t flags);
+
+/* Counters of the last clblm_gpu_od (or of the last layer of clblm_gpu_rt_mode2). */
+int clblm_gpu_od_stats(const clblm_handle_t *h, clblm_od_stats_t *stats);
+
+/* Size of the nadir upwelling radiance spectrum of a column: the final merge
+ * grid of mode2_lookDn_mergeUp. */
+int clblm_gpu_rt_mode2_size(clblm_handle_t *h, const clblm_column_t *col,
+                            const clblm_rt_ctrl_t *ctrl, int64_t *npts,
+                            double *dv);
+
+/* Nadir upwelling thermal radiance at the top of the column: replaces the
+ * layer loop of mode2_lookDn_mergeUp (clblm_noScattRT.f90:1340-1466) with
+ * layerMerge_mode2 (:1560-1870), layerEmis (clblm_EMLAY.f90:104-178) and the
+ * per-layer ODLAY calls.  Radiance in W/(cm2 sr cm-1), binary64. */
+int clblm_gpu_rt_mode2(clblm_handle_t *h, const clblm_column_t *col,
+                       const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap,
+                       int32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLBLM_GB300_H */

@@ -1,0 +1,1923 @@
+/*
+ * clblm_oracle.c -- CPU FP64 restatement of CLBLM's per-layer optical depth
+ * (ODLAY) and nadir radiance (mode2) path.
+ *
+ * TEST INFRASTRUCTURE: this is the oracle the GPU path is checked against.
+ * It is compiled with -ffp-contract=off so that, like the reference's stock
+ * unoptimised gfortran build (Makefile:28, -fdefault-real-8 -g), every
+ * product and sum is rounded separately.  Default REAL of the reference is
+ * binary64; TAPE3 line parameters arrive as binary32 (clblm_LineData.f90:52-64).
+ *
+ * Fortran INT() of a real truncates toward zero, which is also what a C cast
+ * does; expressions keep the reference's left-to-right evaluation order.
+ * Arrays keep the reference's 1-based (or negative) index ranges through
+ * offset pointers.
+ *
+ * Every function cites the reference routine it restates (path inside the
+ * CLBLM project, file:line).
+ */
+#include "clblm_oracle.h"
+#include "../clblm_gb300/csrc/clblm_ref_tables.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---- constants: src/common/clblm_ConstParam.f90 ------------------------ */
+static const double PI_C = 3.1415926535898;         /* :21  */
+static const double ONEPL = 1.01;                   /* :49  */
+static const double ONEMI = 0.999;                  /* :50  */
+static const double BOLTZ = 1.3806503E-16;          /* :60  */
+static const double CLIGHT = 2.99792458E+10;        /* :61  */
+static const double AVOGAD = 6.02214199E+23;        /* :62  */
+static const double RADCN1 = 1.191042722E-12;       /* :70  */
+static const double RADCN2 = 1.4387752;             /* :71  */
+static const double P0 = 1013.25;                   /* :110 Press1013 */
+static const double TEMP0 = 296.0;                  /* :112 Temp296   */
+static const double AVMWT = 36.0;                   /* :118 */
+enum { NFPTS = 2001, NFMX = 3001, N_ABSRB = 5050, MXMOL = 47, NT = 119 };
+/* MaxISOTPL_smass, clblm_ConstParam.f90:246-251 */
+static const int MAXISO[MXMOL] = {6, 10, 9, 5, 6, 4, 3, 3, 2, 1, 2, 2, 3, 2, 4, 4, 2, 2, 5, 3, 2, 2, 3, 2,
+                                  1, 3, 2, 1, 2, 1, 3, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1, 1, 1, 1, 2, 4, 1};
+
+struct ocl_session {
+  int first_pass_jrad; /* firstPassJRAD, clblm_ODLAY.f90:182 */
+  int jrad;            /* SAVEd JRAD,   clblm_ODLAY.f90:183 */
+  int tables_ready;
+  double F1[NFMX + 1], F2[NFMX + 1], F3[NFMX + 1], FG[NFMX + 1], XVER[NFMX + 1];
+  /* interpSpectrum SAVEd 201-point coefficients, clblm_Spectrum.f90:350-351 */
+  int interp_ready;
+  double IA1[203], IA2[203], IA3[203], IA4[203];
+  char err[256];
+};
+
+static int fail(ocl_session *s, int code, const char *fmt, ...) {
+  if (s) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(s->err, sizeof s->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+ocl_session *ocl_create(void) {
+  ocl_session *s = (ocl_session *)calloc(1, sizeof(ocl_session));
+  if (s) s->first_pass_jrad = 1;
+  return s;
+}
+void ocl_destroy(ocl_session *s) { free(s); }
+void ocl_reset(ocl_session *s) {
+  s->first_pass_jrad = 1;
+  s->jrad = 0;
+}
+const char *ocl_last_error(const ocl_session *s) { return s ? s->err : ""; }
+
+/* ======================================================================
+ * Line-shape sub-functions.
+ * SHAPEL clblm_ODLAY.f90:2804-2909, SHAPEG :2914-2954, VERFN :2959-3015.
+ * Tables are 1-based, NFMX = 3001 entries (clblm_ConstParam.f90:92).
+ * ====================================================================== */
+static void shapel(double *F1, double *F2, double *F3) {
+  const double HWF1 = 4., HWF2 = 16., HWF3 = 64.;
+  const double DXF1 = 0.002, DXF2 = 0.008, DXF3 = 0.032;
+  const int NX1 = NFPTS, NX2 = NFPTS, NX3 = NFPTS;
+  double RECPI = 1. / (2. * asin(1.));
+#define A_FN(Z0) ((1. + 2. * (Z0) * (Z0)) / (((1. + (Z0) * (Z0))) * ((1. + (Z0) * (Z0)))))
+#define B_FN(Z0) (-1. / (((1. + (Z0) * (Z0))) * ((1. + (Z0) * (Z0)))))
+  double A1 = A_FN(HWF1), B1 = B_FN(HWF1);
+  double A2 = A_FN(HWF2), B2 = B_FN(HWF2);
+  double A3 = A_FN(HWF3), B3 = B_FN(HWF3);
+#undef A_FN
+#undef B_FN
+#define XLORNZ(XSQ) (1. / (1. + (XSQ)))
+#define Q1FN(XSQ) (A1 + B1 * (XSQ))
+#define Q2FN(XSQ) (A2 + B2 * (XSQ))
+#define Q3FN(XSQ) (A3 + B3 * (XSQ))
+  for (int i = 1; i <= NFMX; ++i) F1[i] = 0.;
+  F1[1] = RECPI * (XLORNZ(0.) - Q1FN(0.));
+  for (int jj = 2; jj <= NX1; ++jj) {
+    double X = (double)(jj - 1) * DXF1, XSQ = X * X;
+    F1[jj] = RECPI * (XLORNZ(XSQ) - Q1FN(XSQ));
+  }
+  F1[NX1] = 0.;
+  for (int i = 1; i <= NFMX; ++i) F2[i] = 0.;
+  F2[1] = RECPI * (Q1FN(0.) - Q2FN(0.));
+  int J1LIM = (int)(HWF1 / DXF2 + 1.001);
+  for (int jj = 2; jj <= J1LIM; ++jj) {
+    double X = (double)(jj - 1) * DXF2, XSQ = X * X;
+    F2[jj] = RECPI * (Q1FN(XSQ) - Q2FN(XSQ));
+  }
+  for (int jj = J1LIM + 1; jj <= NX2; ++jj) {
+    double X = (double)(jj - 1) * DXF2, XSQ = X * X;
+    F2[jj] = RECPI * (XLORNZ(XSQ) - Q2FN(XSQ));
+  }
+  F2[NX2] = 0.;
+  for (int i = 1; i <= NFMX; ++i) F3[i] = 0.;
+  F3[1] = RECPI * (Q2FN(0.) - Q3FN(0.));
+  int J2LIM = (int)(HWF2 / DXF3 + 1.001);
+  for (int jj = 2; jj <= J2LIM; ++jj) {
+    double X = (double)(jj - 1) * DXF3, XSQ = X * X;
+    F3[jj] = RECPI * (Q2FN(XSQ) - Q3FN(XSQ));
+  }
+  for (int jj = J2LIM + 1; jj <= NX3; ++jj) {
+    double X = (double)(jj - 1) * DXF3, XSQ = X * X;
+    F3[jj] = RECPI * (XLORNZ(XSQ) - Q3FN(XSQ));
+  }
+#undef XLORNZ
+#undef Q1FN
+#undef Q2FN
+#undef Q3FN
+}
+
+static void shapeg(double *FG) {
+  const double DXF1 = 0.002;
+  double FLN2 = log(2.);
+  double RECPI = 1. / (2. * asin(1.));
+  double FGNORM = sqrt(FLN2 * RECPI);
+  for (int i = 1; i <= NFMX; ++i) FG[i] = 0.;
+  FG[1] = FGNORM * exp(-FLN2 * 0.);
+  for (int jj = 2; jj <= NFPTS; ++jj) {
+    double X = (double)(jj - 1) * DXF1, XSQ = X * X;
+    FG[jj] = FGNORM * exp(-FLN2 * XSQ);
+  }
+  FG[NFPTS] = 0.;
+}
+
+static void verfn(double *XVER) {
+  const double DXF1 = 0.002;
+  const double CEXP = 0.45, CE0 = 1., CE2 = -.20737285249, CE4 = -.00872684335747;
+  double SE0 = sqrt(CEXP / PI_C);
+  double AE2 = 2. * CEXP;
+  double AE4 = AE2 * AE2 / 3.;
+  for (int i = 1; i <= NFMX; ++i) XVER[i] = 0.;
+  for (int i = 1; i <= NFMX; ++i) {
+    double Z = DXF1 * (double)(i - 1);
+    double Z2 = Z * Z;
+    double XE0 = SE0 * exp(-CEXP * Z2);
+    XVER[i] = (1. / (CE0 + CE2 + CE4)) * (CE0 + CE2 * AE2 * Z2 + CE4 * AE4 * Z2 * Z2) * XE0;
+  }
+}
+
+static void ensure_tables(ocl_session *s) {
+  if (s->tables_ready) return;
+  shapel(s->F1, s->F2, s->F3);
+  shapeg(s->FG);
+  verfn(s->XVER);
+  s->tables_ready = 1;
+}
+
+void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg, double *xver) {
+  static double F1[NFMX + 1], F2[NFMX + 1], F3[NFMX + 1], FG[NFMX + 1], XV[NFMX + 1];
+  shapel(F1, F2, F3);
+  shapeg(FG);
+  verfn(XV);
+  memcpy(f1, F1 + 1, NFMX * sizeof(double));
+  memcpy(f2, F2 + 1, NFMX * sizeof(double));
+  memcpy(f3, F3 + 1, NFMX * sizeof(double));
+  memcpy(fg, FG + 1, NFMX * sizeof(double));
+  memcpy(xver, XV + 1, NFMX * sizeof(double));
+}
+
+/* AVRAT etc. are 1-based in the reference (clblm_ODLAY_CommonSub.f90:43-185) */
+#define AVRAT(i) CLBLM_AVRAT[(i)-1]
+#define CGAUSS(i) CLBLM_CGAUSS[(i)-1]
+#define CF1(i) CLBLM_CF1[(i)-1]
+#define CF2(i) CLBLM_CF2[(i)-1]
+#define CF3(i) CLBLM_CF3[(i)-1]
+#define CER(i) CLBLM_CER[(i)-1]
+
+/* ======================================================================
+ * RADFN / RADFNI, clblm_ODLAY_CommonSub.f90:293-525
+ * ====================================================================== */
+double ocl_radfn(double VI, double XKT) {
+  double XVI = VI;
+  if (XKT > 0.0) {
+    double XVIOKT = XVI / XKT;
+    if (XVIOKT <= 0.01) return 0.5 * XVIOKT * XVI;
+    if (XVIOKT <= 10.0) {
+      double EXPVKT = exp(-XVIOKT);
+      return XVI * (1. - EXPVKT) / (1. + EXPVKT);
+    }
+    return XVI;
+  }
+  return XVI;
+}
+
+static double radfni(double VI, double DVI, double XKT, double *VINEW, double *RDEL, double *RDLAST) {
+  const double FACT1 = 3.0E-03;
+  double XVI = VI;
+  if (*RDLAST < 0.) {
+    if (XKT > 0.0) {
+      double XVIOKT = XVI / XKT;
+      if (XVIOKT <= 0.01) *RDLAST = 0.5 * XVIOKT * XVI;
+      else if (XVIOKT <= 10.0) {
+        double EXPVKT = exp(-XVIOKT);
+        *RDLAST = XVI * (1. - EXPVKT) / (1. + EXPVKT);
+      } else
+        *RDLAST = XVI;
+    } else
+      *RDLAST = XVI;
+  }
+  double RADFNI = *RDLAST;
+  int INTVLS = 1;
+  double RDNEXT;
+  if (XKT > 0.0) {
+    double XVIOKT = XVI / XKT;
+    if (XVIOKT <= 0.01) {
+      if (*VINEW >= 0.0) {
+        *VINEW = VI + FACT1 * 0.5 * XVI;
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+        *VINEW = VI + DVI * (double)INTVLS;
+      } else {
+        *VINEW = fabs(*VINEW);
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+      }
+      double XVINEW = *VINEW;
+      double XVINEWOKT = XVINEW / XKT;
+      RDNEXT = 0.5 * XVINEWOKT * XVINEW;
+    } else if (XVIOKT <= 10.0) {
+      double EXPVKT = exp(-XVIOKT);
+      double XMINUS = 1. - EXPVKT, XPLUS = 1. + EXPVKT;
+      if (*VINEW >= 0.0) {
+        double CVIKT = XVIOKT * EXPVKT;
+        *VINEW = VI + FACT1 * XVI / (1. + (CVIKT / XMINUS + CVIKT / XPLUS));
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+        *VINEW = VI + DVI * (double)INTVLS;
+      } else {
+        *VINEW = fabs(*VINEW);
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+      }
+      double XVINEW = *VINEW;
+      double XVINEWOKT = XVINEW / XKT;
+      double EXPVNEWKT = exp(-XVINEWOKT);
+      double XMINUSNEW = 1. - EXPVNEWKT, XPLUSNEW = 1. + EXPVNEWKT;
+      RDNEXT = XVINEW * XMINUSNEW / XPLUSNEW;
+    } else {
+      if (*VINEW >= 0.0) {
+        *VINEW = VI + (FACT1 * XVI);
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+        *VINEW = VI + DVI * (double)INTVLS;
+      } else {
+        *VINEW = fabs(*VINEW);
+        INTVLS = (int)((*VINEW - VI) / DVI);
+        if (INTVLS < 1) INTVLS = 1;
+      }
+      RDNEXT = *VINEW;
+    }
+  } else {
+    if (*VINEW >= 0.0) {
+      *VINEW = VI + (FACT1 * XVI);
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+      *VINEW = VI + DVI * (double)INTVLS;
+    } else {
+      *VINEW = fabs(*VINEW);
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+    }
+    RDNEXT = *VINEW;
+  }
+  *RDEL = (RDNEXT - RADFNI) / (double)INTVLS;
+  *RDLAST = RDNEXT;
+  return RADFNI;
+}
+
+/* ======================================================================
+ * TIPS partition sums: TIPS_2003 clblm_ODLAY_TIPS.f90:78-419 (iso 1 of
+ * molecules 1-7), QT_* range check :603-607, AtoB :5451-5546.
+ * ====================================================================== */
+static double atob(double aa, const double *Aarr, const double *Barr, int npt) {
+#define A(i) Aarr[(i)-1]
+#define B(i) Barr[(i)-1]
+  double bb = 0.;
+  for (int I = 2; I <= npt; ++I) {
+    if (A(I) >= aa) {
+      if (I < 3 || I == npt) {
+        int J = I;
+        if (I < 3) J = 3;
+        if (I == npt) J = npt;
+        double A0D1 = A(J - 2) - A(J - 1); if (A0D1 == 0.) A0D1 = 0.0001;
+        double A0D2 = A(J - 2) - A(J);     if (A0D2 == 0.) A0D2 = 0.0001;
+        double A1D1 = A(J - 1) - A(J - 2); if (A1D1 == 0.) A1D1 = 0.0001;
+        double A1D2 = A(J - 1) - A(J);     if (A1D2 == 0.) A1D2 = 0.0001;
+        double A2D1 = A(J) - A(J - 2);     if (A2D1 == 0.) A2D1 = 0.0001;
+        double A2D2 = A(J) - A(J - 1);     if (A2D2 == 0.) A2D2 = 0.0001;
+        double A0 = (aa - A(J - 1)) * (aa - A(J)) / (A0D1 * A0D2);
+        double A1 = (aa - A(J - 2)) * (aa - A(J)) / (A1D1 * A1D2);
+        double A2 = (aa - A(J - 2)) * (aa - A(J - 1)) / (A2D1 * A2D2);
+        bb = A0 * B(J - 2) + A1 * B(J - 1) + A2 * B(J);
+      } else {
+        int J = I;
+        double A0D1 = A(J - 2) - A(J - 1); if (A0D1 == 0.) A0D1 = 0.0001;
+        double A0D2 = A(J - 2) - A(J);     if (A0D2 == 0.) A0D2 = 0.0001;
+        double A0D3 = (A(J - 2) - A(J + 1)); if (A0D3 == 0.) A0D3 = 0.0001;
+        double A1D1 = A(J - 1) - A(J - 2); if (A1D1 == 0.) A1D1 = 0.0001;
+        double A1D2 = A(J - 1) - A(J);     if (A1D2 == 0.) A1D2 = 0.0001;
+        double A1D3 = A(J - 1) - A(J + 1); if (A1D3 == 0.) A1D3 = 0.0001;
+        double A2D1 = A(J) - A(J - 2);     if (A2D1 == 0.) A2D1 = 0.0001;
+        double A2D2 = A(J) - A(J - 1);     if (A2D2 == 0.) A2D2 = 0.0001;
+        double A2D3 = A(J) - A(J + 1);     if (A2D3 == 0.) A2D3 = 0.0001;
+        double A3D1 = A(J + 1) - A(J - 2); if (A3D1 == 0.) A3D1 = 0.0001;
+        double A3D2 = A(J + 1) - A(J - 1); if (A3D2 == 0.) A3D2 = 0.0001;
+        double A3D3 = A(J + 1) - A(J);     if (A3D3 == 0.) A3D3 = 0.0001;
+        double A0 = (aa - A(J - 1)) * (aa - A(J)) * (aa - A(J + 1));
+        A0 = A0 / (A0D1 * A0D2 * A0D3);
+        double A1 = (aa - A(J - 2)) * (aa - A(J)) * (aa - A(J + 1));
+        A1 = A1 / (A1D1 * A1D2 * A1D3);
+        double A2 = (aa - A(J - 2)) * (aa - A(J - 1)) * (aa - A(J + 1));
+        A2 = A2 / (A2D1 * A2D2 * A2D3);
+        double A3 = (aa - A(J - 2)) * (aa - A(J - 1)) * (aa - A(J));
+        A3 = A3 / (A3D1 * A3D2 * A3D3);
+        bb = A0 * B(J - 2) + A1 * B(J - 1) + A2 * B(J) + A3 * B(J + 1);
+      }
+      return bb;
+    }
+  }
+  return bb;
+#undef A
+#undef B
+}
+
+static int tips_qt(int mol, double T, double *qt) {
+  if (mol < 1 || mol > CLBLM_TIPS_NMOL) return -1;
+  if (T < 70. || T > 3000.) return -2;
+  *qt = atob(T, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[mol - 1], NT);
+  return 0;
+}
+
+int ocl_tips_scor(int mol, double t, double *scor) {
+  double q296, qt;
+  if (tips_qt(mol, 296., &q296) || tips_qt(mol, t, &qt)) return CLBLM_ERR_RANGE;
+  if (q296 <= 0. || qt <= 0.) return CLBLM_ERR_RANGE;
+  *scor = q296 / qt;
+  return 0;
+}
+
+/* ======================================================================
+ * Per-layer molecular constants: MOLEC clblm_ODLAY_CommonSub.f90:201-264
+ * (isotopologue 1 only: the line list carries iso 1 of molecules 1-7).
+ * ====================================================================== */
+typedef struct {
+  int nsel;
+  int sel[64];          /* selected HITRAN molecule numbers */
+  double WK[MXMOL + 1]; /* WK(m), clblm_ODLAY.f90:393-397 */
+  double SCOR[CLBLM_TIPS_NMOL + 1]; /* SCOR(m,1) */
+  double RHOSLF[MXMOL + 1];
+  double ALFD1[CLBLM_TIPS_NMOL + 1]; /* ALFD1(m,1) */
+} molec_t;
+
+static int is_selected(const molec_t *M, int m) {
+  for (int i = 0; i < M->nsel; ++i)
+    if (M->sel[i] == m) return 1;
+  return 0;
+}
+
+static int molec(ocl_session *s, molec_t *M, const clblm_layer_t *lay, double PAVE, double TAVE) {
+  double FLN2 = log(2.);
+  double FAD = FLN2 * 2. * AVOGAD * BOLTZ / (CLIGHT * CLIGHT);
+  double RHORAT = (PAVE / P0) * (TEMP0 / TAVE);
+  for (int i = 0; i < M->nsel; ++i) {
+    int imol = M->sel[i];
+    if (imol < 1 || imol > CLBLM_TIPS_NMOL)
+      return fail(s, CLBLM_ERR_UNSUPPORTED, "molecule %d: TIPS/mass tables carry molecules 1-9", imol);
+    double scor;
+    if (ocl_tips_scor(imol, TAVE, &scor))
+      return fail(s, CLBLM_ERR_RANGE, "TIPS: temperature %.3f outside 70-3000 K", TAVE);
+    M->SCOR[imol] = scor;
+    M->RHOSLF[imol] = RHORAT * M->WK[imol] / lay->wtot;
+    M->ALFD1[imol] = sqrt(FAD * TAVE / CLBLM_ISO1_MASS[imol - 1]);
+  }
+  return 0;
+}
+
+/* ======================================================================
+ * XINT, clblm_Spectrum.f90:874-915 (ONEPL/ONEMI of clblm_ConstParam).
+ * A and R3 are 1-based.
+ * ====================================================================== */
+static void xint(double V1A, double V2A, double DVA, const double *A, double AFACT, double VFT, double DVR3,
+                 double *R3, int N1R3, int N2R3) {
+  double RECDVA = 1. / DVA;
+  int ILO = (int)((V1A + DVA - VFT) / DVR3 + 1. + ONEMI);
+  if (ILO < N1R3) ILO = N1R3;
+  int IHI = (int)((V2A - DVA - VFT) / DVR3 + ONEMI);
+  if (IHI > N2R3) IHI = N2R3;
+  for (int I = ILO; I <= IHI; ++I) {
+    double VI = VFT + DVR3 * (double)(I - 1);
+    int J = (int)((VI - V1A) * RECDVA + ONEPL);
+    double VJ = V1A + DVA * (double)(J - 1);
+    double P = RECDVA * (VI - VJ);
+    double C = (3. - 2. * P) * P * P;
+    double B = 0.5 * P * (1. - P);
+    double B1 = B * (1. - P);
+    double B2 = B * P;
+    double CONTI = -A[J - 1] * B1 + A[J] * (1. - C + B2) + A[J + 1] * (C + B1) - A[J + 2] * B2;
+    R3[I] = R3[I] + CONTI * AFACT;
+  }
+}
+
+/* ======================================================================
+ * MT_CKD H2O continuum: mt_ckd_h2o_absco mt_ckd_h2o_module.f90:72-170,
+ * myradfn :173-209, myxint :213-258 (module ONEPL=1.001/ONEMI=0.999 :59),
+ * pre_xint :261-292; the H2O block of CONTNM clblm_ODLAY_Continuum.f90:355-405.
+ * ABSRB is 1-based on V1ABS + (i-1)*DVABS.
+ * ====================================================================== */
+static void myxint(double V1A, double V2A, double DVA, const double *A, double AFACT, double VFT, double DVR3,
+                   double *R3, int N1R3, int N2R3) {
+  const double onepl = 1.001, onemi = 0.999;
+  double RECDVA = 1. / DVA;
+  int ILO = (int)((V1A + DVA - VFT) / DVR3 + 1. + onemi);
+  if (ILO < N1R3) ILO = N1R3;
+  int IHI = (int)((V2A - DVA - VFT) / DVR3 + onemi);
+  if (IHI > N2R3) IHI = N2R3;
+  for (int I = ILO; I <= IHI; ++I) {
+    double VI = VFT + DVR3 * (double)(I - 1);
+    int J = (int)((VI - V1A) * RECDVA + onepl);
+    double VJ = V1A + DVA * (double)(J - 1);
+    double P = RECDVA * (VI - VJ);
+    double C = (3. - 2. * P) * P * P;
+    double B = 0.5 * P * (1. - P);
+    double B1 = B * (1. - P);
+    double B2 = B * P;
+    double CONTI = -A[J - 1] * B1 + A[J] * (1. - C + B2) + A[J + 1] * (C + B1) - A[J + 2] * B2;
+    R3[I] = R3[I] + CONTI * AFACT;
+  }
+}
+
+static int contnm_h2o(ocl_session *s, const clblm_cont_t *C, int JRAD, double V1ABS, double V2ABS, double DVABS,
+                      double *ABSRB /*1-based*/, double XSELF, double XFRGN, double V1, double V2, double PAVE,
+                      double TAVE, double Wtot, double WK1) {
+  if (!C || C->n < 4) return fail(s, CLBLM_ERR_ARG, "continuum table missing");
+  double h2o_fac = WK1 / Wtot;
+  if (!((V2 > -20.0) && (V1 < 20000.) && ((XSELF > 0.) || (XFRGN > 0.)))) return 0;
+  int ncoeffin = C->n;
+  double *wvn = (double *)malloc(sizeof(double) * (ncoeffin + 1)); /* 1-based */
+  for (int i = 1; i <= ncoeffin; ++i) wvn[i] = C->v1 + (double)(i - 1) * C->dv;
+  double dvc = wvn[2] - wvn[1];
+  int i = 1;
+  while (i <= ncoeffin && wvn[i] <= (V1ABS - 2 * dvc)) i++;
+  int i1 = i - 1;
+  if (i1 == 0) i1 = 1;
+  while (i <= ncoeffin && wvn[i] < (V2ABS + 2 * dvc)) i++;
+  int i2 = i;
+  if (i2 > ncoeffin) {
+    free(wvn);
+    return fail(s, CLBLM_ERR_RANGE, "continuum table does not cover %.3f", V2ABS);
+  }
+  int ncoeff = i2 - i1 + 1;
+  double *sh = (double *)calloc(ncoeff + 3, sizeof(double));
+  double *fh = (double *)calloc(ncoeff + 3, sizeof(double));
+  double xkt = TAVE / RADCN2;
+  double rho_rat = (PAVE / C->ref_press) * (C->ref_temp / TAVE);
+  int radflag = (JRAD != 0);
+  for (int k = 1; k <= ncoeff; ++k) {
+    int ii = i1 + k - 1;
+    double v = C->self_absco_ref[ii - 1] * pow(C->ref_temp / TAVE, C->self_texp[ii - 1]);
+    v = v * h2o_fac * rho_rat;
+    double f = C->for_absco_ref[ii - 1];
+    f = f * (1 - h2o_fac) * rho_rat;
+    if (radflag) {
+      double xvi = wvn[ii], rad = xvi, xviokt = xvi / xkt;
+      if (xviokt <= 0.01) rad = 0.5 * xviokt * xvi;
+      else if (xviokt <= 10.) {
+        double e = exp(-xviokt);
+        rad = xvi * (1 - e) / (1. + e);
+      }
+      v = v * rad;
+      f = f * rad;
+    }
+    sh[k] = v;
+    fh[k] = f;
+  }
+  int nptabs = (int)((V2ABS - V1ABS) / DVABS + 1);
+  int nbnd_v1c = (int)(2 + (wvn[1] - V1ABS) / DVABS + 1.e-5);
+  int ist = nbnd_v1c > 1 ? nbnd_v1c : 1;
+  int nbnd_v2c = (int)(1 + (wvn[ncoeffin] - V1ABS) / DVABS + 1.e-5);
+  int lst = nptabs < nbnd_v2c ? nptabs : nbnd_v2c;
+  double *self = (double *)calloc(N_ABSRB + 4, sizeof(double));
+  double *forc = (double *)calloc(N_ABSRB + 4, sizeof(double));
+  myxint(wvn[i1], wvn[i2], dvc, sh, 1.0, V1ABS, DVABS, self, ist, lst);
+  myxint(wvn[i1], wvn[i2], dvc, fh, 1.0, V1ABS, DVABS, forc, ist, lst);
+  for (int k = 1; k <= N_ABSRB; ++k) {
+    double cself = WK1 * self[k] * XSELF;
+    double cfor = WK1 * forc[k] * XFRGN;
+    ABSRB[k] = ABSRB[k] + cself + cfor;
+  }
+  free(self);
+  free(forc);
+  free(sh);
+  free(fh);
+  free(wvn);
+  return 0;
+}
+
+/* ======================================================================
+ * Far-wing (function 4) lines: the TAPE9 scratch file as records in memory.
+ * LINF4Q clblm_ODLAY_LineF4.f90:647-1266 (RDLNFL :1355-1476),
+ * SHRINQ :1516-1647, LBLF4Q :25-182, CNVF4Q :187-494, RDLN4Q :554-640.
+ * ====================================================================== */
+enum { SHR_MAX = 1250 };
+typedef struct {
+  double vnulo, vnuhi;
+  int n;
+  double VNU[SHR_MAX + 1], SP[SHR_MAX + 1], ALFA[SHR_MAX + 1], EPP[SHR_MAX + 1], SPP[SHR_MAX + 1];
+  int MOL[SHR_MAX + 1];
+} shrunk_rec;
+
+typedef struct {
+  shrunk_rec *rec;
+  int nrec, cap;
+  int64_t nlines;
+} tape9_t;
+
+static void tape9_push(tape9_t *t, const shrunk_rec *r) {
+  if (t->nrec == t->cap) {
+    t->cap = t->cap ? 2 * t->cap : 16;
+    t->rec = (shrunk_rec *)realloc(t->rec, (size_t)t->cap * sizeof(shrunk_rec));
+  }
+  t->rec[t->nrec++] = *r;
+  t->nlines += r->n;
+}
+
+/* SHRINQ: combine lines within DVR4/2 into one effective line. */
+static void shrinq(shrunk_rec *S, int *ILO, int *IHI, double DVR4) {
+  int J = *ILO - 1;
+  double DV = DVR4 / 2.;
+  double VLMT = S->VNU[*ILO] + DV;
+  double SUMAL = 0., SUMAD = 0., SUMS = 0., SUMV = 0., SUMC = 0.;
+  double SUMAL2 = 0., SUMAD2 = 0., SUMS2 = 0., SUMV2 = 0., SUMC2 = 0.;
+  for (int I = *ILO; I <= *IHI; ++I) {
+    if (S->SP[I] < 1.0e-35) {
+      S->SP[I] = 0.0;
+      S->SPP[I] = 0.0;
+    }
+    if (S->SPP[I] != 0.0) {
+      J = J + 1;
+      S->VNU[J] = S->VNU[I];
+      S->SP[J] = S->SP[I];
+      S->ALFA[J] = S->ALFA[I];
+      S->EPP[J] = S->EPP[I];
+      S->SPP[J] = S->SPP[I];
+      S->MOL[J] = S->MOL[I];
+      if (S->MOL[J] != 2) S->MOL[J] = 0;
+      goto L10;
+    }
+    if (S->MOL[I] != 2) {
+      SUMV = SUMV + S->VNU[I] * S->SP[I];
+      SUMS = SUMS + S->SP[I];
+      SUMAL = SUMAL + S->SP[I] * S->ALFA[I];
+      SUMAD = SUMAD + S->SP[I] * S->EPP[I];
+      SUMC = SUMC + S->SPP[I];
+    } else {
+      SUMV2 = SUMV2 + S->VNU[I] * S->SP[I];
+      SUMS2 = SUMS2 + S->SP[I];
+      SUMAL2 = SUMAL2 + S->SP[I] * S->ALFA[I];
+      SUMAD2 = SUMAD2 + S->SP[I] * S->EPP[I];
+      SUMC2 = SUMC2 + S->SPP[I];
+    }
+  L10:
+    if (I < *IHI) {
+      if (S->VNU[I + 1] <= VLMT) continue;
+    }
+    VLMT = S->VNU[I] + DV;
+    if (SUMS > 0.) {
+      J = J + 1;
+      S->SP[J] = SUMS;
+      S->ALFA[J] = SUMAL / SUMS;
+      S->EPP[J] = SUMAD / SUMS;
+      S->VNU[J] = SUMV / SUMS;
+      S->SPP[J] = SUMC;
+      S->MOL[J] = 0;
+      SUMAL = SUMAD = SUMS = SUMV = SUMC = 0.;
+    }
+    if (SUMS2 > 0.) {
+      J = J + 1;
+      S->SP[J] = SUMS2;
+      S->ALFA[J] = SUMAL2 / SUMS2;
+      S->EPP[J] = SUMAD2 / SUMS2;
+      S->VNU[J] = SUMV2 / SUMS2;
+      S->MOL[J] = 2;
+      S->SPP[J] = SUMC2;
+      SUMAL2 = SUMAD2 = SUMS2 = SUMV2 = SUMC2 = 0.;
+    }
+  }
+  *ILO = J + 1;
+  *IHI = J;
+}
+
+typedef struct {
+  const clblm_lines_t *L;
+  int64_t nrec;
+} linefile_t;
+
+static int64_t rec_first(int64_t r) { return r * CLBLM_LINES_PER_RECORD; }
+static int64_t rec_end(const linefile_t *F, int64_t r) {
+  int64_t e = (r + 1) * CLBLM_LINES_PER_RECORD;
+  return e < F->L->n ? e : F->L->n;
+}
+
+static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double V1L4, double V2L4, double DVR4,
+                  double PAVE, double TAVE, double WTOT, tape9_t *T9) {
+  const clblm_lines_t *L = F->L;
+  const int LIMIN = 1000;
+  double TRATIO = TAVE / TEMP0;
+  double RHORAT = (PAVE / P0) * (TEMP0 / TAVE);
+  double BETA = RADCN2 / TAVE, BETA0 = RADCN2 / TEMP0, BETACR = BETA - BETA0;
+  double VLO = V1L4, VHI = V2L4;
+  (void)WTOT;
+  shrunk_rec *S = (shrunk_rec *)calloc(1, sizeof(shrunk_rec));
+  int IJ = 0, ILO = 1, IHI = 0, IEOF = 0;
+  int64_t rec = 0;
+  for (;;) { /* label 30: RDLNFL */
+    /* RDLNFL: skip records with VMAX < VLO */
+    while (rec < F->nrec && L->vnu[rec_end(F, rec) - 1] < VLO) rec++;
+    if (rec >= F->nrec) {
+      IEOF = 1;
+      goto L60;
+    }
+    {
+      int64_t b = rec_first(rec), e = rec_end(F, rec);
+      rec++;
+      for (int64_t i = b; i < e; ++i) {
+        if (L->iflg[i] < 0) continue; /* IOUT maps iflg >= 0 only */
+        int M_ = L->mol[i] % 100;
+        int ISO = (L->mol[i] % 1000) / 100;
+        if (ISO == 0) ISO = 10;
+        if (!is_selected(M, M_)) continue;
+        if (M_ > MXMOL || M_ < 1) continue;
+        if (ISO > MAXISO[M_ - 1]) continue;
+        if (ISO != 1) {
+          free(S);
+          return fail(s, CLBLM_ERR_UNSUPPORTED, "isotopologue %d of molecule %d", ISO, M_);
+        }
+        double alfa = (double)L->alfa[i];
+        double pshift = (double)L->pshift[i];
+        if (M_ == 7 && L->iflg[i] >= 0) alfa = (alfa - 0.21 * (double)L->hwhm[i]) / (1.0 - 0.21);
+        if (M_ == 22 && L->iflg[i] >= 0) alfa = (alfa - 0.79 * (double)L->hwhm[i]) / (1.0 - 0.79);
+        double SUI = (double)L->sp[i] * M->WK[M_];
+        if (SUI == 0.) continue;
+        if (L->vnu[i] < VLO) continue;
+        IJ = IJ + 1;
+        S->VNU[IJ] = L->vnu[i] + RHORAT * pshift;
+        S->ALFA[IJ] = alfa;
+        S->EPP[IJ] = (double)L->epp[i];
+        S->MOL[IJ] = M_;
+        if (S->VNU[IJ] == 0.) SUI = 2. * SUI;
+        if (S->EPP[IJ] <= -1.001) S->EPP[IJ] = fabs(S->EPP[IJ]);
+        if (S->EPP[IJ] > -0.999)
+          SUI = SUI * M->SCOR[M_] * exp(-S->EPP[IJ] * BETACR) * (1. + exp(-S->VNU[IJ] * BETA));
+        double TMPCOR = pow(TRATIO, (double)L->tmpalf[i]);
+        double ALFA0I = S->ALFA[IJ] * TMPCOR;
+        double HWHMSI = (double)L->hwhm[i] * TMPCOR;
+        S->ALFA[IJ] = ALFA0I * (RHORAT - M->RHOSLF[M_]) + HWHMSI * M->RHOSLF[M_];
+        S->EPP[IJ] = S->VNU[IJ] * M->ALFD1[M_];
+        S->SP[IJ] = SUI * (1. + 0. * (PAVE / P0) * (PAVE / P0));
+        S->SPP[IJ] = SUI * 0. * (PAVE / P0);
+        if (S->VNU[IJ] > VHI) {
+          IEOF = 1;
+          goto L60;
+        }
+      }
+    }
+    if (IJ < LIMIN && IEOF == 0) continue;
+  L60:
+    IHI = IJ;
+    shrinq(S, &ILO, &IHI, DVR4);
+    IJ = ILO - 1;
+    if (IHI < LIMIN && IEOF == 0) continue;
+    if (IHI > 0) {
+      S->vnulo = S->VNU[1];
+      S->vnuhi = S->VNU[IHI];
+      S->n = IHI;
+      tape9_push(T9, S);
+    }
+    if (IEOF == 1) break;
+    IJ = 0;
+    ILO = 1;
+  }
+  free(S);
+  return 0;
+}
+
+/* CNVF4Q: function-4 convolution of one TAPE9 record into R4 (1-based). */
+static void cnvf4q(shrunk_rec *SH, double *R4, double V1R4, double V2R4, double DVR4, int NPTR4, int ILO,
+                   int *IHI, double BOUND4, int ILNFLG, double DPTFC, double DPTMN, int64_t *ILIN4) {
+  const double ZBND = 64.;
+  double RECPI = 1. / (2. * asin(1.));
+  double ZSQBND = ZBND * ZBND;
+  double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
+  double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
+  double VNULST = V2R4 + BOUND4;
+  double BNDSQ = BOUND4 * BOUND4;
+  double r_bndsq = 1. / BNDSQ;
+  int lastLine = ILO - 1;
+  for (int I = ILO; I <= *IHI; ++I) {
+    if (SH->VNU[I] >= VNULST) break;
+    lastLine = I;
+  }
+  for (int I = ILO; I <= lastLine; ++I) {
+    if (SH->SP[I] == 0. && SH->SPP[I] == 0.) continue;
+    double ALFADI = SH->EPP[I];
+    double ALFALI = SH->ALFA[I];
+    double ZETAI = ALFALI / (ALFALI + ALFADI);
+    int IZ = (int)(100. * ZETAI + ONEPL);
+    double ZETDIF = 100. * ZETAI - (double)(IZ - 1);
+    double ALFAVI = (AVRAT(IZ) + ZETDIF * (AVRAT(IZ + 1) - AVRAT(IZ))) * (ALFALI + ALFADI);
+    double RALFVI = 1. / ALFAVI;
+    double SIL = SH->SP[I] * RECPI * ALFALI;
+    double SIV = (ALFALI * RALFVI) * SH->SP[I] * RECPI * RALFVI;
+    double SPEAK = A3 * (fabs(SIV));
+    int JJ = (int)((SH->VNU[I] - V1R4) / DVR4 + 1.);
+    if (JJ < 1) JJ = 1;
+    if (JJ > NPTR4) JJ = NPTR4;
+    if (ILNFLG == 0 || ILNFLG == 1) {
+      if (SPEAK <= (DPTMN + DPTFC * R4[JJ]) && SH->SPP[I] == 0.) continue;
+    }
+    (*ILIN4)++;
+    double VNUI = SH->VNU[I];
+  L30:;
+    double XNUI = VNUI - V1R4;
+    int JMIN = (int)((XNUI - BOUND4) / DVR4 + 2.);
+    if (JMIN > NPTR4) continue;
+    if (JMIN < 1) JMIN = 1;
+    int JMAX = (int)((XNUI + BOUND4) / DVR4 + 1.);
+    if (JMAX >= JMIN) {
+      if (JMAX > NPTR4) JMAX = NPTR4;
+      double ALFLI2 = ALFALI * ALFALI;
+      double ALFVI2 = ALFAVI * ALFAVI;
+      double XJJ = (double)(JMIN - 1) * DVR4;
+      double F4BND = SIL / (ALFLI2 + BNDSQ);
+      double dptrat = SH->SPP[I] / (SH->SP[I] * ALFAVI);
+      double rec_alfvi2 = 1. / ALFVI2;
+      double siv_a3 = SIV * A3;
+      double siv_b3 = SIV * B3;
+      int sppEQzero = SH->SPP[I] == 0.;
+      if (SH->MOL[I] == 2) {
+        for (int J = JMIN; J <= JMAX; ++J) {
+          double XM = (XJJ - XNUI);
+          double XMSQ = XM * XM;
+          double ZVSQ = XMSQ * rec_alfvi2;
+          double fcnt_fn = (2. - (XMSQ * r_bndsq)) * F4BND;
+          double F4FN;
+          if (ZVSQ <= ZSQBND) F4FN = (siv_a3 + ZVSQ * siv_b3) - fcnt_fn;
+          else F4FN = SIL / (ALFLI2 + XMSQ) - fcnt_fn;
+          if (sppEQzero) R4[J] = R4[J] + F4FN;
+          else {
+            F4FN = F4FN + XM * dptrat * F4FN;
+            R4[J] = R4[J] + F4FN;
+          }
+          XJJ = XJJ + DVR4;
+        }
+      } else {
+        for (int J = JMIN; J <= JMAX; ++J) {
+          double XM = (XJJ - XNUI);
+          double XMSQ = XM * XM;
+          double ZVSQ = XMSQ * rec_alfvi2;
+          double F4FN;
+          if (ZVSQ <= ZSQBND) F4FN = (siv_a3 + ZVSQ * siv_b3) - F4BND;
+          else F4FN = SIL / (ALFLI2 + XMSQ) - F4BND;
+          if (sppEQzero) R4[J] = R4[J] + F4FN;
+          else {
+            F4FN = F4FN + XM * dptrat * F4FN;
+            R4[J] = R4[J] + F4FN;
+          }
+          XJJ = XJJ + DVR4;
+        }
+      }
+    }
+    /* label 50: Van Vleck-Weisskopf mirror line */
+    if (VNUI > 0. && VNUI <= 25.) {
+      VNUI = -SH->VNU[I];
+      SH->SPP[I] = -SH->SPP[I];
+      goto L30;
+    }
+  }
+  if (lastLine < *IHI) *IHI = -1;
+}
+
+/* LBLF4Q: R4 block [V1R4, V2R4] (V2R4 adjusted); R4 is 1-based, 2502 long. */
+static void lblf4q(int JRAD, double V1R4, double *V2R4, double *R4, int *NPTR4, double DVR4, double BOUND4,
+                   double TAVE, double DPTFAC, double DPTMIN, int ILNFLG, const tape9_t *T9, int64_t *ILIN4) {
+  const int LIMOUT = 2500;
+  double DPTMN = DPTMIN / ocl_radfn(*V2R4, TAVE / RADCN2);
+  double DPTFC = DPTFAC;
+  *NPTR4 = (int)((*V2R4 - V1R4) / DVR4 + ONEPL);
+  if (*NPTR4 > LIMOUT) *NPTR4 = LIMOUT;
+  *V2R4 = V1R4 + DVR4 * (double)(*NPTR4 - 1);
+  for (int i = 1; i <= LIMOUT + 2; ++i) R4[i] = 0.;
+  double BETA = RADCN2 / TAVE;
+  double VLO = V1R4 - BOUND4;
+  double VHI = *V2R4 + BOUND4;
+  shrunk_rec *line = (shrunk_rec *)malloc(sizeof(shrunk_rec));
+  int r = 0;
+  for (;;) {
+    /* RDLN4Q */
+    int IEOF = 0, IHI = 0;
+    while (r < T9->nrec && T9->rec[r].vnuhi < VLO) r++;
+    if (r >= T9->nrec) {
+      IEOF = 1;
+      IHI = 0;
+    } else {
+      memcpy(line, &T9->rec[r], sizeof(shrunk_rec));
+      r++;
+      IHI = line->n;
+      if (line->VNU[line->n] > VHI) IEOF = 1;
+    }
+    if (IEOF == 1 && IHI == 0) break;
+    cnvf4q(line, R4, V1R4, *V2R4, DVR4, *NPTR4, 1, &IHI, BOUND4, ILNFLG, DPTFC, DPTMN, ILIN4);
+    if (IHI == -1) break;
+    if (IEOF == 1) break; /* RDLN4Q returns EOF on the next header read */
+  }
+  free(line);
+  if (JRAD == 1) {
+    double XKT = 1. / BETA;
+    double VITST = V1R4 - DVR4;
+    double RDLAST = -1.;
+    int NPTSI1 = 0, NPTSI2 = 0;
+    do {
+      NPTSI1 = NPTSI2 + 1;
+      double VI = V1R4 + DVR4 * (double)(NPTSI1 - 1);
+      double RDEL;
+      double RADVI = radfni(VI, DVR4, XKT, &VITST, &RDEL, &RDLAST);
+      NPTSI2 = (int)((VITST - V1R4) / DVR4 + 0.001);
+      if (NPTSI2 > *NPTR4) NPTSI2 = *NPTR4;
+      double tmp = RADVI;
+      for (int I = NPTSI1; I <= NPTSI2; ++I) {
+        R4[I] = R4[I] * tmp;
+        tmp = tmp + RDEL;
+      }
+    } while (NPTSI2 < *NPTR4);
+  }
+}
+
+/* ======================================================================
+ * RSYM, clblm_ODLAY.f90:3020-3085 (negative-frequency folding, VFT <= 0).
+ * R is indexed from its own lower bound through the offset pointer.
+ * ====================================================================== */
+static void rsym(double *R, double DV, double VFT) {
+  int IP = (int)((-VFT / DV) + 1. - .000001);
+  IP = IP + 1;
+  double P = ((double)(IP - 1) + VFT / DV) * 2.;
+  double PST = P;
+  if (P > 1.) P = P - 1.;
+  double WN1 = -P * (P - 1.) * (P - 2.) / 6.;
+  double W0 = (P * P - 1.) * (P - 2.) / 2.;
+  double W1 = -P * (P + 1.) * (P - 2.) / 2.;
+  double W2 = P * (P * P - 1.) / 6.;
+  int K = IP;
+  int IPMAX = IP + IP - 1;
+  double B1, B2, C1, C2;
+  if (PST <= 1.) goto L20;
+  B1 = R[IP - 2];
+  B2 = R[IP - 1];
+  C1 = R[K];
+  for (int I = IP; I <= IPMAX; ++I) {
+    K = K - 1;
+    C2 = C1;
+    if (K < 1) return;
+    C1 = R[K];
+    R[K] = R[K] + WN1 * R[I + 1] + W0 * R[I] + W1 * B2 + W2 * B1;
+    B1 = B2;
+    B2 = R[I];
+    if (K <= 2) continue;
+    R[I] = R[I] + WN1 * C2 + W0 * C1 + W1 * R[K - 1] + W2 * R[K - 2];
+  }
+  return;
+L20:
+  C1 = R[IP];
+  C2 = R[IP + 1];
+  B2 = R[IP - 1];
+  for (int I = IP; I <= IPMAX; ++I) {
+    K = K - 1;
+    B1 = B2;
+    B2 = R[I];
+    if (K <= 1) return;
+    R[I] = R[I] + WN1 * C2 + W0 * C1 + W1 * R[K] + W2 * R[K - 1];
+    C2 = C1;
+    C1 = R[K];
+    R[K] = R[K] + WN1 * R[I + 2] + W0 * R[I + 1] + W1 * B2 + W2 * B1;
+  }
+}
+
+/* ======================================================================
+ * HIRACQ, clblm_ODLAY.f90:1002-1562 with RDLIN :2571-2798,
+ * LNCORQ :1566-2041, CNVFNQ :2067-2258, panelOut :2289-2545.
+ * ====================================================================== */
+enum { NLREC = CLBLM_LINES_PER_RECORD };
+typedef struct {
+  /* RDLIN / LNCORQ / CNVFNQ line buffer, 1-based */
+  double VNU[NLREC + 2], SP[NLREC + 2], ALFA0[NLREC + 2], EPP[NLREC + 2], HWHMS[NLREC + 2];
+  double TMPALF[NLREC + 2], PSHIFT[NLREC + 2], SPPSP[NLREC + 2], RECALF[NLREC + 2], ZETAI[NLREC + 2];
+  int MOL[NLREC + 2], IFLG[NLREC + 2], IZETA[NLREC + 2], IOUT[NLREC + 2];
+} linebuf_t;
+
+typedef struct {
+  /* inputs */
+  const linefile_t *F;
+  const molec_t *M;
+  double PAVE, TAVE, DV, V1, V2, SAMPLE, ALFAV, DPTFAC, DPTMIN;
+  int JRAD, ILNFLG;
+  double DVR4, V1R4, V2R4, BOUND4;
+  const double *ABSRB; /* 1-based, may be NULL when the continuum is off */
+  double DVABS, V1ABS, V2ABS;
+  const tape9_t *T9;
+  int line_off;
+  /* output */
+  double *out;
+  int64_t cap, numTotPoints;
+  clblm_od_stats_t *st;
+} hirac_args;
+
+static int hiracq(ocl_session *s, hirac_args *a) {
+  const double HWF1 = 4., HWF3 = 64., DXF1 = 0.002, DXF2 = 0.008, DXF3 = 0.032;
+  const int NX1 = NFPTS;
+  const molec_t *M = a->M;
+  const clblm_lines_t *L = a->F->L;
+  double DV = a->DV;
+  double PAVE = a->PAVE, TAVE = a->TAVE;
+  int JRAD = a->JRAD;
+  ensure_tables(s);
+  const double *F1 = s->F1, *F2 = s->F2, *F3 = s->F3, *FG = s->FG, *XVER = s->XVER;
+
+  double DPTMN = a->DPTMIN;
+  if (JRAD != 1) DPTMN = a->DPTMIN / ocl_radfn(a->V2, TAVE / RADCN2);
+  double DPTFC = a->DPTFAC;
+  const int NSHIFT = 32;
+  double ALFMAX = 4. * a->ALFAV;
+  int nALFMAX = (int)(ALFMAX / DV);
+  int NBOUND = (int)((2. * HWF3) * (double)nALFMAX + 0.01);
+  const int NLIM1 = 2401;
+  const int NLIM2 = (NLIM1 / 4) + 1;
+  const int NLIM3 = (NLIM2 / 4) + 1;
+
+  double DVP = DV;
+  double DVR2 = (DXF2 / DXF1) * DV;
+  double DVR3 = (DXF3 / DXF1) * DV;
+  int MAX1 = NSHIFT + NLIM1 + NSHIFT + NBOUND / 2;
+  int MAX2 = MAX1 / 4;
+  int MAX3 = MAX1 / 16;
+  MAX1 = MAX1 + 4 * nALFMAX;
+  MAX2 = MAX2 + 16 * nALFMAX / 4 + 1;
+  MAX3 = MAX3 + 64 * nALFMAX / 16 + 1;
+  double BOUND = (double)NBOUND * DV / 2.;
+  int NLO = NSHIFT + 1;
+  int NHI = NLIM1 + NSHIFT - 1;
+
+  /* array bounds: generous versions of the lbR and ubR limits (clblm_ODLAY.f90:1280-1285) */
+  int lbR1 = -(int)ceil((double)(4 * (64 + 4)) * a->ALFAV / DV + 1.) - 8;
+  int lbR2 = -(int)ceil(((double)(4 * (64 + 16)) * a->ALFAV / DV) / 4. + 1.) - 8;
+  int lbR3 = -(int)ceil(((double)(4 * (64 + 64)) * a->ALFAV / DV) / 16. + 1.) - 8;
+  int ubR1 = MAX1 + 8 + (int)ceil((double)(4 * (64 + 4)) * a->ALFAV / DV + 1.);
+  int ubR2 = MAX2 + 8 + (int)ceil(((double)(4 * (64 + 16)) * a->ALFAV / DV) / 4. + 1.);
+  int ubR3 = MAX3 + 8 + (int)ceil(((double)(4 * (64 + 64)) * a->ALFAV / DV) / 16. + 1.);
+  double *R1b = (double *)calloc((size_t)(ubR1 - lbR1 + 1), sizeof(double));
+  double *R2b = (double *)calloc((size_t)(ubR2 - lbR2 + 1), sizeof(double));
+  double *R3b = (double *)calloc((size_t)(ubR3 - lbR3 + 1), sizeof(double));
+  double *R4b = (double *)calloc(2503 + 4, sizeof(double));
+  double *R1 = R1b - lbR1, *R2 = R2b - lbR2, *R3 = R3b - lbR3, *R4 = R4b;
+  linebuf_t *B = (linebuf_t *)calloc(1, sizeof(linebuf_t));
+  int rc = 0;
+
+  int ILBLF4 = a->line_off ? 0 : 1;
+  double VFT = a->V1 - (double)NSHIFT * DV;
+  double VBOT = a->V1 - BOUND;
+  double VTOP = a->V2 + BOUND;
+  int64_t LINCNT = 0, NLIN = 0, NMINUS = 0, NPLUS = 0;
+  int64_t ILIN4 = 0;
+  double V1R4 = a->V1R4, V2R4 = a->V2R4;
+  double V2R4ST = V2R4;
+  int NPTR4 = 0;
+  if (ILBLF4 >= 1)
+    lblf4q(JRAD, V1R4, &V2R4, R4, &NPTR4, a->DVR4, a->BOUND4, TAVE, a->DPTFAC, a->DPTMIN, a->ILNFLG, a->T9,
+           &ILIN4);
+  int IFPAN = 1;
+
+  /* LNCORQ per-layer constants (NLNCR == 1 block, clblm_ODLAY.f90:1666-1697) */
+  double XKT0 = TEMP0 / RADCN2;
+  double XKT = TAVE / RADCN2;
+  double BETACR = (1. / XKT) - (1. / XKT0);
+  double TRATIO = TAVE / TEMP0;
+  double RHORAT = (PAVE / P0) * (TEMP0 / TAVE);
+  double PAVP0 = PAVE / P0;
+  double PAVP2 = PAVP0 * PAVP0;
+
+  /* RDLIN state */
+  int64_t rec = 0;
+  int IEOF = 0, ILO = 0, IHI = -999, IDATA = 0, IPANEL = 0;
+  int ISTOP = 0;
+
+  for (;;) {
+    /* ---- label 60: read a record ---- */
+  L60:
+    if (IEOF != 0) goto L80;
+    {
+      IDATA = 0;
+      if (ILO <= 0) rec = 0;
+      while (rec < a->F->nrec && L->vnu[rec_end(a->F, rec) - 1] < VBOT) rec++;
+      if (rec >= a->F->nrec) {
+        IEOF = 1;
+        goto L80;
+      }
+      int64_t b = rec_first(rec), e = rec_end(a->F, rec);
+      int NREC = (int)(e - b);
+      double VMIN = L->vnu[b];
+      rec++;
+      for (int i = 1; i <= NREC; ++i) {
+        int64_t k = b + i - 1;
+        B->IFLG[i] = L->iflg[k];
+        B->VNU[i] = L->vnu[k];
+        B->SP[i] = (double)L->sp[k];
+        B->ALFA0[i] = (double)L->alfa[k];
+        B->EPP[i] = (double)L->epp[k];
+        B->MOL[i] = L->mol[k];
+        B->HWHMS[i] = (double)L->hwhm[k];
+        B->TMPALF[i] = (double)L->tmpalf[k];
+        B->PSHIFT[i] = (double)L->pshift[k];
+        int m = B->MOL[i] % 100;
+        if (m == 7 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.21 * B->HWHMS[i]) / (1.0 - 0.21);
+        if (m == 22 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.79 * B->HWHMS[i]) / (1.0 - 0.79);
+      }
+      ILO = 1;
+      int IJ = 0;
+      for (int i = 1; i <= NREC; ++i)
+        if (B->IFLG[i] >= 0) B->IOUT[++IJ] = i;
+      for (int i = IJ + 1; i <= NLREC; ++i) B->IOUT[i] = NREC;
+      if (VMIN < VBOT) {
+        for (int J = 1; J <= IJ; ++J) {
+          ILO = J;
+          if (B->VNU[B->IOUT[J]] >= VBOT) break;
+        }
+      }
+      for (int J = ILO; J <= IJ; ++J) {
+        int I = B->IOUT[J];
+        if (B->MOL[I] > 0) {
+          IHI = J;
+          if (B->VNU[I] > VTOP) break;
+        }
+      }
+      if (IHI < IJ) IDATA = 1;
+    }
+    /* ---- LNCORQ ---- */
+    for (int J = ILO; J <= IHI; ++J) {
+      int I = B->IOUT[J];
+      int IFLAG = B->IFLG[I];
+      int m = B->MOL[I] % 100;
+      int ISO = (B->MOL[I] % 1000) / 100;
+      if (ISO == 0) ISO = 10;
+      if (!is_selected(M, m)) goto L25;
+      if (m > MXMOL || m < 1) goto L25;
+      if (ISO > MAXISO[m - 1]) goto L25;
+      if (ISO != 1) {
+        rc = fail(s, CLBLM_ERR_UNSUPPORTED, "isotopologue %d of molecule %d", ISO, m);
+        goto done;
+      }
+      if (IFLAG == 1 || IFLAG == 3) {
+        rc = fail(s, CLBLM_ERR_UNSUPPORTED, "line coupling (IFLG=%d)", IFLAG);
+        goto done;
+      }
+      B->MOL[I] = m;
+      {
+        double SUI = B->SP[I] * M->WK[m];
+        if (JRAD == 1) SUI = SUI * ocl_radfn(B->VNU[I], XKT);
+        if (SUI == 0.) goto L25;
+        NLIN++;
+        B->VNU[I] = B->VNU[I] + RHORAT * B->PSHIFT[I];
+        double TMPCOR = pow(TRATIO, B->TMPALF[I]);
+        double ALFA0I = B->ALFA0[I] * TMPCOR;
+        double HWHMSI = B->HWHMS[I] * TMPCOR;
+        double ALFL = ALFA0I * (RHORAT - M->RHOSLF[m]) + HWHMSI * M->RHOSLF[m];
+        double ALFAD = B->VNU[I] * M->ALFD1[m];
+        double ZETA = ALFL / (ALFL + ALFAD);
+        B->ZETAI[I] = ZETA;
+        double FZETA = 100. * ZETA;
+        int IZ = (int)(FZETA + ONEPL);
+        B->IZETA[I] = IZ;
+        double ZETDIF = FZETA - (double)(IZ - 1);
+        double ALFV = (AVRAT(IZ) + ZETDIF * (AVRAT(IZ + 1) - AVRAT(IZ))) * (ALFL + ALFAD);
+        int NMINAD = 0, NPLSAD = 0;
+        if (ALFV < DV) {
+          ALFV = DV;
+          NMINAD = 1;
+        }
+        if (ALFV > ALFMAX) {
+          ALFV = ALFMAX;
+          NPLSAD = 1;
+        }
+        if (HWF3 * ALFV + B->VNU[I] < VFT) goto L25;
+        B->RECALF[I] = 1. / ALFV;
+        if (B->EPP[I] <= -1.001) B->EPP[I] = fabs(B->EPP[I]);
+        if (B->EPP[I] > -0.999)
+          SUI = SUI * M->SCOR[m] * exp(-B->EPP[I] * BETACR) * (1. + exp(-B->VNU[I] / XKT));
+        B->SP[I] = SUI * (1. + 0. * PAVP2);
+        double SPPI = SUI * 0. * PAVP0;
+        B->SPPSP[I] = SPPI / B->SP[I];
+        B->EPP[I] = 0.0;
+        if (IFLAG == 0 && (a->ILNFLG == 0 || a->ILNFLG == 1)) {
+          double SPEAK = SUI * B->RECALF[I];
+          int JJ = (int)((B->VNU[I] - V1R4) / a->DVR4 + 1.);
+          if (JJ < 1) JJ = 1;
+          if (JJ > NPTR4) JJ = NPTR4;
+          double r4 = (ILBLF4 >= 1 && NPTR4 >= 1) ? R4[JJ] : 0.;
+          if (SPEAK <= (DPTMN + DPTFC * r4) && B->SPPSP[I] == 0.) goto L25;
+        }
+        NMINUS += NMINAD;
+        NPLUS += NPLSAD;
+        LINCNT++;
+        continue;
+      }
+    L25:
+      B->SP[I] = 0.0;
+      B->EPP[I] = 0.0;
+      B->SPPSP[I] = 0.0;
+    }
+
+    /* ---- label 70: CNVFNQ ---- */
+  L70:
+    {
+      double CLC1 = 4. / ((double)(NX1 - 1));
+      (void)CLC1;
+      double WAVDXF = DV / DXF1;
+      double HWDXF = HWF1 / DXF1;
+      double CONF2 = DV / DVR2;
+      double CONF3 = DV / DVR3;
+      int ILAST = ILO - 1;
+      if (ILO <= IHI) {
+        int J;
+        for (J = ILO; J <= IHI; ++J) {
+          int I = B->IOUT[J];
+          if (B->SP[I] == 0.) continue;
+          double DEPTHA = B->SP[I] * B->RECALF[I];
+          int IZM = B->IZETA[I];
+          double ZETDIF = 100. * B->ZETAI[I] - (double)(IZM - 1);
+          double STRFA1 = DEPTHA * (CF1(IZM) + ZETDIF * (CF1(IZM + 1) - CF1(IZM)));
+          double STRFA2 = DEPTHA * (CF2(IZM) + ZETDIF * (CF2(IZM + 1) - CF2(IZM)));
+          double STRFA3 = DEPTHA * (CF3(IZM) + ZETDIF * (CF3(IZM + 1) - CF3(IZM)));
+          double STRDA = DEPTHA * (CGAUSS(IZM) + ZETDIF * (CGAUSS(IZM + 1) - CGAUSS(IZM)));
+          double STRVRA = DEPTHA * (CER(IZM) + ZETDIF * (CER(IZM + 1) - CER(IZM)));
+          double ZSLOPE = B->RECALF[I] * WAVDXF;
+          double ZINT = (B->VNU[I] - VFT) / DV;
+          double BHWDXF = HWDXF / ZSLOPE;
+          int JMAX1 = (int)(ZINT + BHWDXF + 1.5);
+          if (JMAX1 > MAX1) {
+            ILAST = J - 1;
+            IPANEL = 1;
+            goto L40;
+          }
+          int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
+          double RSHFT = 0.5;
+          if (ZINT < 0.0) RSHFT = -RSHFT;
+          int J2SHFT = (int)(ZINT * (1. - CONF2) + RSHFT);
+          int J3SHFT = (int)(ZINT * (1. - CONF3) + RSHFT);
+          int JMIN2 = JMIN1 - J2SHFT;
+          int JMIN3 = JMIN1 - J3SHFT;
+          double ZF1L = ((double)(JMIN1 - 2) - ZINT) * ZSLOPE;
+          double ZF2L = ((double)(JMIN2 - 2) - ZINT * CONF2) * ZSLOPE;
+          double ZF3L = ((double)(JMIN3 - 2) - ZINT * CONF3) * ZSLOPE;
+          double ZF1 = ZF1L, ZF2 = ZF2L, ZF3 = ZF3L;
+          if (JMIN1 < lbR1 || JMAX1 > ubR1 || JMIN1 - J2SHFT < lbR2 || JMAX1 - J2SHFT > ubR2 ||
+              JMIN1 - J3SHFT < lbR3 || JMAX1 - J3SHFT > ubR3) {
+            rc = fail(s, CLBLM_ERR_RANGE, "panel index outside R arrays: J1 %d..%d [%d,%d] J2s %d [%d,%d] J3s %d [%d,%d] ZINT %g BHW %g", JMIN1, JMAX1, lbR1, ubR1, J2SHFT, lbR2, ubR2, J3SHFT, lbR3, ubR3, ZINT, BHWDXF);
+            goto done;
+          }
+          for (int J1 = JMIN1; J1 <= JMAX1; ++J1) {
+            int J2 = J1 - J2SHFT;
+            int J3 = J1 - J3SHFT;
+            ZF3 = ZF3 + ZSLOPE;
+            ZF2 = ZF2 + ZSLOPE;
+            ZF1 = ZF1 + ZSLOPE;
+            int IZ3 = (int)(fabs(ZF3) + 1.5);
+            int IZ2 = (int)(fabs(ZF2) + 1.5);
+            int IZ1 = (int)(fabs(ZF1) + 1.5);
+            if (IZ1 > NFMX || IZ2 > NFMX || IZ3 > NFMX) {
+              rc = fail(s, CLBLM_ERR_RANGE, "shape table index beyond NFMX");
+              goto done;
+            }
+            R3[J3] = R3[J3] + STRFA3 * F3[IZ3];
+            R2[J2] = R2[J2] + STRFA2 * F2[IZ2];
+            R1[J1] = R1[J1] + STRFA1 * F1[IZ1] + STRDA * FG[IZ1] + STRVRA * XVER[IZ1];
+          }
+        }
+        ILAST = IHI;
+        IPANEL = IDATA;
+      } else {
+        IPANEL = 1;
+      }
+    L40:
+      ILO = ILAST + 1;
+    }
+    if (IPANEL == 0) goto L60;
+
+    /* ---- label 80: panel output ---- */
+  L80:
+    {
+      int N1R2, N1R3;
+      if (IFPAN == 1) {
+        IFPAN = 0;
+        N1R2 = 1;
+        N1R3 = 1;
+      } else {
+        N1R2 = (NSHIFT / 4) + 1 + 4;
+        N1R3 = (NSHIFT / 16) + 1 + 3;
+      }
+      int N2R3 = NLIM3 + (NSHIFT / 16) - 1 + 3;
+      if (VFT <= 0.) {
+        rsym(R1, DV, VFT);
+        rsym(R2, DVR2, VFT);
+        rsym(R3, DVR3, VFT);
+      }
+      if (ILBLF4 >= 1) xint(V1R4, V2R4, a->DVR4, R4, 1.0, VFT, DVR3, R3, N1R3, N2R3);
+      if (a->ABSRB) xint(a->V1ABS, a->V2ABS, a->DVABS, a->ABSRB, 1., VFT, DVR3, R3, N1R3, N2R3);
+
+      /* panelOut */
+      const double X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
+      const double X10 = -1. / 16., X11 = 9. / 16.;
+      ISTOP = 0;
+      double V2P;
+      if ((VFT + (NHI - 1) * DVP) > a->V2) {
+        NHI = (int)((a->V2 - VFT) / DVP + 1.);
+        V2P = VFT + (double)(NHI - 1) * DVP;
+        if (V2P < a->V2) {
+          V2P = V2P + DVP;
+          NHI = NHI + 1;
+        }
+        ISTOP = 1;
+      } else {
+        V2P = VFT + (double)(NHI - 1) * DV;
+      }
+      (void)V2P;
+      int NLIM = NHI - NLO + 1;
+      double V1P = VFT + (double)(NLO - 1) * DV;
+      int LIMLO = N1R2;
+      if (N1R2 == 1) LIMLO = LIMLO + 4;
+      int LIMHI = (NHI / 4) + 1;
+      int J = 0, J3 = 0;
+      for (J = LIMLO; J <= LIMHI; J += 4) {
+        J3 = (J - 1) / 4 + 1;
+        R2[J] = R2[J] + R3[J3];
+        R2[J + 1] = R2[J + 1] + X00 * R3[J3 - 1] + X01 * R3[J3] + X02 * R3[J3 + 1] + X03 * R3[J3 + 2];
+        R2[J + 2] = R2[J + 2] + X10 * (R3[J3 - 1] + R3[J3 + 2]) + X11 * (R3[J3] + R3[J3 + 1]);
+        R2[J + 3] = R2[J + 3] + X03 * R3[J3 - 1] + X02 * R3[J3] + X01 * R3[J3 + 1] + X00 * R3[J3 + 2];
+      }
+      if (LIMLO <= LIMHI && ISTOP == 1) {
+        J3 = J3 + 1;
+        R2[J] = R2[J] + R3[J3];
+        R2[J + 1] = R2[J + 1] + X00 * R3[J3 - 1] + X01 * R3[J3] + X02 * R3[J3 + 1] + X03 * R3[J3 + 2];
+      }
+      for (J = NLO; J <= NHI; J += 4) {
+        int J2 = (J - 1) / 4 + 1;
+        R1[J] = R1[J] + R2[J2];
+        R1[J + 1] = R1[J + 1] + X00 * R2[J2 - 1] + X01 * R2[J2] + X02 * R2[J2 + 1] + X03 * R2[J2 + 2];
+        R1[J + 2] = R1[J + 2] + X10 * (R2[J2 - 1] + R2[J2 + 2]) + X11 * (R2[J2] + R2[J2 + 1]);
+        R1[J + 3] = R1[J + 3] + X03 * R2[J2 - 1] + X02 * R2[J2] + X01 * R2[J2 + 1] + X00 * R2[J2 + 2];
+      }
+      if (JRAD == 0) {
+        double XKTp = TAVE / RADCN2;
+        double VITST = V1P - DV;
+        double RDLAST = -1.;
+        int NPTSI1, NPTSI2 = NLO - 1;
+        do {
+          NPTSI1 = NPTSI2 + 1;
+          double VI = VFT + (double)(NPTSI1 - 1) * DV;
+          double RDEL;
+          double RADVI = radfni(VI, DV, XKTp, &VITST, &RDEL, &RDLAST);
+          NPTSI2 = (int)((VITST - VFT) / DV + 0.001);
+          if (NPTSI2 > NHI) NPTSI2 = NHI;
+          double tmp = RADVI;
+          for (int I = NPTSI1; I <= NPTSI2; ++I) {
+            R1[I] = R1[I] * tmp;
+            tmp = tmp + RDEL;
+          }
+        } while (NPTSI2 < NHI);
+      }
+      if (a->out) {
+        if (a->numTotPoints + NLIM > a->cap) {
+          rc = fail(s, CLBLM_ERR_CAPACITY, "output buffer too small");
+          goto done;
+        }
+        for (int k = 0; k < NLIM; ++k) a->out[a->numTotPoints + k] = R1[NLO + k];
+      }
+      a->numTotPoints += NLIM;
+      if (a->st) a->st->npanels++;
+      VFT = VFT + (double)(NLIM1 - 1) * DV;
+      if (ISTOP != 1) {
+        for (int jj = NLIM1; jj <= MAX1; ++jj) R1[jj - NLIM1 + 1] = R1[jj];
+        for (int jj = MAX1 - NLIM1 + 2; jj <= MAX1; ++jj) R1[jj] = 0.;
+        for (int jj = NLIM2; jj <= MAX2; ++jj) R2[jj - NLIM2 + 1] = R2[jj];
+        for (int jj = MAX2 - NLIM2 + 2; jj <= MAX2; ++jj) R2[jj] = 0.;
+        for (int jj = NLIM3; jj <= MAX3; ++jj) R3[jj - NLIM3 + 1] = R3[jj];
+        for (int jj = MAX3 - NLIM3 + 2; jj <= MAX3; ++jj) R3[jj] = 0.;
+        NLO = NSHIFT + 1;
+      }
+    }
+    if (ISTOP == 1) break;
+    if (ILBLF4 >= 1) {
+      double VF1 = VFT - 2. * a->DVR4;
+      VF1 = a->V1 + floor((VF1 - a->V1) / a->DVR4) * a->DVR4;
+      int N2R3n = NLIM3 + (NSHIFT / 16) - 1 + 3;
+      double VF2 = VFT + 2. * a->DVR4 + (double)(N2R3n + 4) * DVR3;
+      if (VF2 > V2R4 && V2R4 != V2R4ST) {
+        V1R4 = VF1;
+        V2R4 = V2R4ST;
+        lblf4q(JRAD, V1R4, &V2R4, R4, &NPTR4, a->DVR4, a->BOUND4, TAVE, a->DPTFAC, a->DPTMIN, a->ILNFLG, a->T9,
+               &ILIN4);
+      }
+    }
+    goto L70;
+  }
+done:
+  if (a->st) {
+    a->st->nlin = NLIN;
+    a->st->lincnt = LINCNT;
+    a->st->nminus = NMINUS;
+    a->st->nplus = NPLUS;
+  }
+  free(R1b);
+  free(R2b);
+  free(R3b);
+  free(R4b);
+  free(B);
+  return rc;
+}
+
+/* ======================================================================
+ * interpSpectrum_array2array, clblm_Spectrum.f90:326-620.
+ * in[0..nin-1] -> out[0..nout-1].
+ * ====================================================================== */
+static void interp_coef(ocl_session *s) {
+  if (s->interp_ready) return;
+  const int NUMCOF = 201;
+  double XNUMCF = (double)NUMCOF;
+  for (int IP = 0; IP <= NUMCOF + 1; ++IP) {
+    double P = ((double)IP - 1.0) / (XNUMCF - 1.0);
+    double PP = P * P;
+    s->IA1[IP] = -P / 2.0 * ((1 - P) * (1 - P));
+    s->IA2[IP] = 1.0 - PP * (3.0 - 2.0 * P) + PP / 2.0 * (1.0 - P);
+    s->IA3[IP] = PP * (3.0 - 2.0 * P) + P / 2.0 * ((1.0 - P) * (1.0 - P));
+    s->IA4[IP] = -PP / 2 * (1.0 - P);
+  }
+  s->interp_ready = 1;
+}
+
+static int interp_spectrum(ocl_session *s, const double *spIn, double DVin, double V1in, int64_t NLIMin,
+                           double *spOut, double DVout, double V1out, int64_t NLIMout) {
+  const double TOL = 1.e-8;
+  const double EPSD = 2.220446049250313e-16;
+  if (fabs(V1in - V1out) < EPSD && fabs(DVin - DVout) < EPSD && NLIMin == NLIMout) {
+    if (spOut != spIn) memcpy(spOut, spIn, sizeof(double) * (size_t)NLIMin);
+    return 0;
+  }
+  interp_coef(s);
+  double XNUMCF = 201.;
+  double V2out = V1out + (double)(NLIMout - 1) * DVout;
+  int64_t I1out = 1, I2out = NLIMout;
+  if (V1out < V1in) return fail(s, CLBLM_ERR_GRID, "interpSpectrum: output V1 below input V1");
+  int sameV1 = fabs(V1in - V1out) < EPSD;
+  double dvRatio = DVout / DVin;
+  if (fabs(DVout - DVin) < TOL) dvRatio = 1.;
+  int intervalLen_in, intervalLen_out, ITYPE;
+  static const double hi2lo[5] = {2. / 1., 3. / 2., 4. / 3., 5. / 4., 6. / 5.};
+  static const double lo2hi[5] = {1. / 2., 2. / 3., 3. / 4., 4. / 5., 5. / 6.};
+  int isHi = 0, isLo = 0;
+  for (int k = 0; k < 5; ++k) {
+    if (fabs(dvRatio - hi2lo[k]) < TOL) isHi = 1;
+    if (fabs(dvRatio - lo2hi[k]) < TOL) isLo = 1;
+  }
+  if (sameV1 && fabs(dvRatio - 1.) < EPSD) {
+    intervalLen_in = 1;
+    intervalLen_out = 1;
+    ITYPE = 0;
+  } else if (sameV1 && isHi) {
+    intervalLen_in = (int)(DVout / (DVout - DVin) + 0.5);
+    intervalLen_out = intervalLen_in - 1;
+    ITYPE = intervalLen_out - 1;
+  } else if (sameV1 && isLo) {
+    intervalLen_in = (int)(DVout / (DVin - DVout) + 0.5);
+    intervalLen_out = intervalLen_in + 1;
+    ITYPE = intervalLen_out - 1;
+  } else {
+    intervalLen_in = 0;
+    intervalLen_out = 0;
+    ITYPE = -1;
+  }
+  /* spInExt(1-4 : NLIMin+4); the reference leaves -3,-2 and N+3,N+4 unset */
+  double *ext = (double *)calloc((size_t)NLIMin + 9, sizeof(double));
+  double *X = ext + 4; /* X[i] == spInExt(i) for i in -3..NLIMin+4 (1-based) */
+  for (int64_t i = 1; i <= NLIMin; ++i) X[i] = spIn[i - 1];
+  X[0] = 2.0 * X[1] - X[2];
+  X[-1] = X[0];
+  X[NLIMin + 1] = 2.0 * X[NLIMin] - X[NLIMin - 1];
+  X[NLIMin + 2] = X[NLIMin + 1];
+#define O(i) spOut[(i)-1]
+  if (ITYPE == 0) {
+    int64_t iIn = 1 - (int64_t)llround(dvRatio);
+    for (int64_t I = I1out; I <= I2out; ++I) {
+      iIn = iIn + (int64_t)llround(dvRatio);
+      if (iIn > NLIMin + 4) iIn = NLIMin + 4;
+      O(I) = X[iIn];
+    }
+  } else if (ITYPE > 0) {
+    double Bc1[10], Bc2[10], Bc3[10], Bc4[10];
+    double AP = 1.0 / ((double)ITYPE + 1.0);
+    for (int JP = 1; JP <= ITYPE; ++JP) {
+      int IP = JP + 1;
+      double P = AP * (double)JP;
+      if (DVin > DVout) P = 1.0 - P;
+      Bc1[IP] = -P * (P - 1.0) * (P - 2.0) / 6.0;
+      Bc2[IP] = (P * P - 1.0) * (P - 2.0) * 0.5;
+      Bc3[IP] = -P * (P + 1.0) * (P - 2.0) * 0.5;
+      Bc4[IP] = P * (P * P - 1.0) / 6.0;
+    }
+    for (int NL = 1; NL <= intervalLen_out; ++NL) {
+      int64_t iIn = NL - intervalLen_in;
+      if (NL > 1 && DVin > DVout) iIn = iIn - 1;
+      if (NL == 1) {
+        for (int64_t I = I1out; I <= I2out; I += intervalLen_out) {
+          iIn = iIn + intervalLen_in;
+          O(I) = X[iIn];
+        }
+      } else {
+        double A1N = Bc1[NL], A2N = Bc2[NL], A3N = Bc3[NL], A4N = Bc4[NL];
+        for (int64_t I = I1out + NL - 1; I <= I2out; I += intervalLen_out) {
+          iIn = iIn + intervalLen_in;
+          O(I) = A1N * X[iIn - 1] + A2N * X[iIn] + A3N * X[iIn + 1] + A4N * X[iIn + 2];
+        }
+      }
+    }
+  } else {
+    double Vo = V1out;
+    while (Vo < V2out + TOL) {
+      int64_t iIn = (int64_t)((Vo - V1in) / DVin + 1.00001);
+      double Vi = V1in + (double)(iIn - 1) * DVin;
+      double P = (Vo - Vi) / DVin;
+      int64_t J1 = (int64_t)((Vo - V1out) / DVout + 1.001) + I1out - 1;
+      int64_t J2 = (I2out < J1 + 2400 - 1 ? I2out : J1 + 2400 - 1) + I1out - 1;
+      for (int64_t J = J1; J <= J2; ++J) {
+        int IP = (int)(P * XNUMCF + 1.00001);
+        O(J) = s->IA1[IP] * X[iIn - 1] + s->IA2[IP] * X[iIn] + s->IA3[IP] * X[iIn + 1] + s->IA4[IP] * X[iIn + 2];
+        P = P + dvRatio;
+        if (P >= 1.0) {
+          iIn = (int64_t)((double)iIn + P);
+          P = P - (double)((int64_t)P);
+        }
+      }
+      Vo = V1out + (double)J2 * DVout;
+    }
+  }
+  free(ext);
+#undef O
+  return 0;
+}
+
+int ocl_interp_spectrum(const double *in, double dvin, double v1in, int64_t nin, double *out, double dvout,
+                        double v1out, int64_t nout) {
+  ocl_session tmp;
+  memset(&tmp, 0, sizeof tmp);
+  return interp_spectrum(&tmp, in, dvin, v1in, nin, out, dvout, v1out, nout);
+}
+
+/* ======================================================================
+ * ODLAY_nonStruct clblm_ODLAY.f90:129-611 and OPDPTH :757-967.
+ * ====================================================================== */
+static int od_grid(const clblm_grid_t *g, double *DV, double *ALFAV) {
+  if (!(g->v2 > g->v1) || !(g->dv_normal > 0.) || !(g->dv_narrow > 0.) || !(g->sample > 0.)) return -1;
+  *ALFAV = g->sample * (g->dv_normal > g->dv_narrow ? g->dv_normal : g->dv_narrow);
+  *DV = g->dv_normal;
+  if (!(fabs(g->dv_normal - g->dv_narrow) / g->dv_normal > 0.2)) *DV = g->dv_narrow;
+  return 0;
+}
+
+int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
+              const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, double *out, int64_t cap, int64_t *nsamp,
+              double *dv_used, clblm_od_stats_t *st) {
+  if (!s || !L || !lay || !g || !ctrl) return CLBLM_ERR_ARG;
+  s->err[0] = 0;
+  double DV, ALFAV;
+  if (od_grid(g, &DV, &ALFAV)) return fail(s, CLBLM_ERR_GRID, "bad grid");
+  for (int64_t i = 1; i < L->n; ++i)
+    if (L->vnu[i] < L->vnu[i - 1]) return fail(s, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+  if (s->first_pass_jrad) {
+    s->jrad = ctrl->jrad;
+    s->first_pass_jrad = 0;
+  }
+  clblm_od_stats_t stl;
+  memset(&stl, 0, sizeof stl);
+  molec_t M;
+  memset(&M, 0, sizeof M);
+  M.nsel = lay->nmol;
+  if (M.nsel > 64) return fail(s, CLBLM_ERR_ARG, "too many molecules");
+  for (int i = 0; i < lay->nmol; ++i) {
+    M.sel[i] = lay->mol_id[i];
+    if (lay->mol_id[i] >= 1 && lay->mol_id[i] <= MXMOL) M.WK[lay->mol_id[i]] = lay->w[i];
+  }
+  double PAVE = lay->pave, TAVE = lay->tave, V1 = g->v1, V2 = g->v2;
+  int ILNFLG = ctrl->line_rejec ? 0 : -1;
+  int rc = molec(s, &M, lay, PAVE, TAVE);
+  if (rc) return rc;
+  if (ctrl->line_off) return fail(s, CLBLM_ERR_UNSUPPORTED, "lineOff");
+  if (ctrl->dptfac != 0.) {
+    /* accepted: the oracle follows the per-block R4 rule literally */
+  }
+
+  /* OPDPTH */
+  double XKT = TAVE / RADCN2;
+  if (((V1 / XKT) < 5.) && (s->jrad != -1)) s->jrad = 0;
+  int JRAD = s->jrad;
+  double *ABSRBb = NULL;
+  double DVABS = 0., V1ABS = 0., V2ABS = 0.;
+  if (!ctrl->contnm_off) {
+    DVABS = 1.;
+    V1ABS = (double)(int)V1;
+    if (V1 < 0.) V1ABS = V1ABS - 1.;
+    V1ABS = V1ABS - 3. * DVABS;
+    V2ABS = (double)(int)(V2 + 3. * DVABS + 0.5);
+    int NPTABS = (int)((V2ABS - V1ABS) / DVABS + 1.5);
+    if (NPTABS > N_ABSRB - 4) return fail(s, CLBLM_ERR_RANGE, "V2-V1 too wide for ABSRB (%d points)", NPTABS);
+    ABSRBb = (double *)calloc(N_ABSRB + 8, sizeof(double));
+    double WK1 = M.WK[1];
+    rc = contnm_h2o(s, C, JRAD, V1ABS, V2ABS, DVABS, ABSRBb, ctrl->xself, ctrl->xfrgn, V1, V2, PAVE, TAVE,
+                    lay->wtot, WK1);
+    if (rc) {
+      free(ABSRBb);
+      return rc;
+    }
+  }
+  double ALFAV4 = 64. * g->sample * DV;
+  double DVR4 = ALFAV4 / g->sample;
+  double BOUND4 = 25.;
+  double V1R4 = V1 - 2. * DVR4;
+  double V2R4 = V2 + 2. * DVR4;
+  double V1L4 = V1R4 - BOUND4 - DVR4;
+  double V2L4 = V2R4 + BOUND4 + 2 * DVR4;
+  linefile_t F;
+  F.L = L;
+  F.nrec = (L->n + CLBLM_LINES_PER_RECORD - 1) / CLBLM_LINES_PER_RECORD;
+  tape9_t T9;
+  memset(&T9, 0, sizeof T9);
+  rc = linf4q(s, &F, &M, V1L4, V2L4, DVR4, PAVE, TAVE, lay->wtot, &T9);
+  if (rc) {
+    free(ABSRBb);
+    free(T9.rec);
+    return rc;
+  }
+  stl.nshrunk = T9.nlines;
+
+  /* size of the output, then HIRACQ */
+  int64_t sizeOfBuffer = (int64_t)ceil((V2 - V1) / DV + 1.);
+  if (V1 + (double)(sizeOfBuffer - 1) * DV <= V2 + 1.e-7) sizeOfBuffer = sizeOfBuffer + 1;
+  double *buf = (double *)malloc(sizeof(double) * (size_t)(sizeOfBuffer + 4));
+  hirac_args a;
+  memset(&a, 0, sizeof a);
+  a.F = &F;
+  a.M = &M;
+  a.PAVE = PAVE;
+  a.TAVE = TAVE;
+  a.DV = DV;
+  a.V1 = V1;
+  a.V2 = V2;
+  a.SAMPLE = g->sample;
+  a.ALFAV = ALFAV;
+  a.DPTFAC = ctrl->dptfac;
+  a.DPTMIN = ctrl->dptmin;
+  a.JRAD = JRAD;
+  a.ILNFLG = ILNFLG;
+  a.DVR4 = DVR4;
+  a.V1R4 = V1R4;
+  a.V2R4 = V2R4;
+  a.BOUND4 = BOUND4;
+  a.ABSRB = ABSRBb;
+  a.DVABS = DVABS;
+  a.V1ABS = V1ABS;
+  a.V2ABS = V2ABS;
+  a.T9 = &T9;
+  a.out = buf;
+  a.cap = sizeOfBuffer + 4;
+  a.st = &stl;
+  rc = hiracq(s, &a);
+  free(ABSRBb);
+  free(T9.rec);
+  if (rc) {
+    free(buf);
+    return rc;
+  }
+  int64_t numFinePoints = a.numTotPoints;
+
+  /* DVout interpolation, clblm_ODLAY.f90:571-604 */
+  double outputDV = DV;
+  if (g->dv_out > 0.) outputDV = g->dv_out;
+  int64_t n = numFinePoints;
+  double *res = buf;
+  if (!(fabs(outputDV - DV) < 2.220446049250313e-16)) {
+    n = (int64_t)ceil((V2 - V1) / outputDV + 1.);
+    res = (double *)malloc(sizeof(double) * (size_t)n);
+    rc = interp_spectrum(s, buf, DV, V1, numFinePoints, res, outputDV, V1, n);
+    if (rc) {
+      free(buf);
+      free(res);
+      return rc;
+    }
+  }
+  stl.nsamp = n;
+  stl.dv = DV;
+  stl.dvr4 = DVR4;
+  stl.jrad = JRAD;
+  if (st) *st = stl;
+  if (nsamp) *nsamp = n;
+  if (dv_used) *dv_used = outputDV;
+  if (out) {
+    if (cap < n) rc = fail(s, CLBLM_ERR_CAPACITY, "need %lld points", (long long)n);
+    else memcpy(out, res, sizeof(double) * (size_t)n);
+  }
+  if (res != buf) free(res);
+  free(buf);
+  return rc;
+}
+
+/* ======================================================================
+ * setDV_struct clblm_setDV.f90:114-211, calculateDV :221-272,
+ * fixDVRatio :277-351, DVSET :356-382.
+ * ====================================================================== */
+static void calculate_dv(const clblm_column_t *col, double Vbar, double ALFAL0, double SAMPLE, double *DVC) {
+  int ih2o = -1;
+  for (int m = 0; m < col->nmol; ++m)
+    if (col->mol_id[m] == 1) ih2o = m;
+  for (int il = 0; il < col->nlay; ++il) {
+    double WTOTL = col->wtot[il];
+    double FRH2O = (ih2o >= 0 ? col->w[(size_t)il * col->nmol + ih2o] : 0.) / WTOTL;
+    double ALFCOR = (col->pave[il] / P0) * sqrt(TEMP0 / col->tave[il]);
+    double H2OSLF = (1. - FRH2O + 5. * FRH2O);
+    double ALBAR = ALFAL0 * ALFCOR * H2OSLF;
+    double ADBAR = 3.58115E-07 * Vbar * sqrt(col->tave[il] / AVMWT);
+    double AVBAR = 0.5 * (ALBAR + sqrt(ALBAR * ALBAR + 4. * ADBAR * ADBAR));
+    DVC[il] = AVBAR / SAMPLE;
+  }
+}
+
+static int fix_dv_ratio(ocl_session *s, double *DVout, const double *DVin, int nLay) {
+  const double TYPMAX = 2.5;
+  double OLDDV = 0.;
+  for (int il = 1; il <= nLay; ++il) {
+    double DV = DVin[il - 1];
+    double TYPE;
+    int ITYPE;
+    if (il == 1) {
+      int ISCAL = (int)(log10(DV) - 3.);
+      double SCAL = pow(10., (double)ISCAL);
+      int IDV = (int)((DV / SCAL) + 0.5);
+      if (IDV % 2 > 0) IDV = IDV + 1;
+      DV = SCAL * (double)IDV;
+    } else {
+      TYPE = OLDDV / DV;
+      if (TYPE > TYPMAX) return fail(s, CLBLM_ERR_DV_RATIO, "DV ratio %.3f > 2.5 at layer %d", TYPE, il);
+      else if (TYPE >= 1.2) {
+        DV = OLDDV;
+        ITYPE = (int)(1. / (TYPE - 1.) + 0.5);
+        if (ITYPE == 3) ITYPE = 2;
+        DV = OLDDV * (double)ITYPE / (double)(ITYPE + 1);
+      } else {
+        DV = OLDDV;
+      }
+    }
+    OLDDV = DV;
+    DVout[il - 1] = DV;
+  }
+  return 0;
+}
+
+int ocl_setdv(ocl_session *s, const clblm_column_t *col, double sample, double alfal0, double alfal0_fine,
+              int32_t grid_type, double dv_user, double *dv_normal, double *dv_narrow, double *dv_out) {
+  int n = col->nlay;
+  double V1 = col->v1, V2 = col->v2;
+  double Vbar = 0.5 * (V1 + V2);
+  if (V2 < V1) Vbar = V1;
+  double *DVC = (double *)malloc(sizeof(double) * n), *DVCf = (double *)malloc(sizeof(double) * n);
+  calculate_dv(col, Vbar, alfal0, sample, DVC);
+  calculate_dv(col, Vbar, alfal0_fine, sample, DVCf);
+  memcpy(dv_normal, DVC, sizeof(double) * n);
+  memcpy(dv_narrow, DVCf, sizeof(double) * n);
+  int rc = 0;
+  if (grid_type >= 0) {
+    if (grid_type == 0) {
+      rc = fix_dv_ratio(s, dv_normal, DVC, n);
+      if (!rc) rc = fix_dv_ratio(s, dv_narrow, DVCf, n);
+    }
+    if (!rc && dv_user > 0.) {
+      if (fabs(1. - dv_user / dv_normal[n - 1]) < 0.2) {
+        double R = dv_user / dv_normal[n - 1];
+        for (int l = 0; l < n; ++l) dv_normal[l] = dv_normal[l] * R;
+      }
+      if (fabs(1. - dv_user / dv_narrow[n - 1]) < 0.2) {
+        double R = dv_user / dv_narrow[n - 1];
+        for (int l = 0; l < n; ++l) dv_narrow[l] = dv_narrow[l] * R;
+      }
+    }
+  }
+  if (dv_out) {
+    if (grid_type == 1) {
+      if (dv_user > 0.) *dv_out = dv_user;
+      else {
+        double m = dv_narrow[0];
+        for (int l = 1; l < n; ++l)
+          if (dv_narrow[l] < m) m = dv_narrow[l];
+        *dv_out = m;
+      }
+    } else
+      *dv_out = -999.9;
+  }
+  free(DVC);
+  free(DVCf);
+  return rc;
+}
+
+/* ======================================================================
+ * planck clblm_EMLAY.f90:18-40, rlin :187-223, layerEmis :104-178.
+ * ====================================================================== */
+double ocl_planck(double V, double XKT) {
+  if (XKT <= 1.e-6) return 0.;
+  double cv3 = RADCN1 * V * V * V;
+  double evt = exp(V / XKT);
+  return cv3 / (evt - 1.);
+}
+
+void ocl_rlin(double od, double *hlf) {
+  const double dbAvg2dtau = -1. / 12;
+  if (od < 1.e-03) *hlf = .5 + od * dbAvg2dtau;
+  else if (od > 20.) *hlf = 1. / od;
+  else {
+    double tex = exp(od);
+    *hlf = 1. / (od)-1. / (tex - 1.);
+  }
+}
+
+static void layer_emis(double *em, double Ta, double Tb, double Tave, const double *tx, const double *od,
+                       int linInTau, double V1, double DV, int64_t n) {
+  double XKTA = Ta / RADCN2, XKTB = Tb / RADCN2, XKT = Tave / RADCN2;
+  for (int64_t ip = 1; ip <= n; ++ip) {
+    double odvi = od[ip - 1];
+    double abso = 1 - tx[ip - 1];
+    double hlf = 0.;
+    if (linInTau != 0) ocl_rlin(odvi, &hlf);
+    double vi = V1 + (double)(ip - 1) * DV;
+    if (linInTau == 0) em[ip - 1] = abso * ocl_planck(vi, XKT);
+    else if (linInTau == 1) {
+      double bba = ocl_planck(vi, XKTA), bb = ocl_planck(vi, XKT);
+      em[ip - 1] = abso * (bba + 2 * (bb - bba) * hlf);
+    } else {
+      double bba = ocl_planck(vi, XKTA), bbb = ocl_planck(vi, XKTB);
+      em[ip - 1] = abso * (bba + (bbb - bba) * hlf);
+    }
+  }
+}
+
+/* ======================================================================
+ * mode2_lookDn_mergeUp clblm_noScattRT.f90:1134-1466 with layerMerge_mode2
+ * :1560-1870 (thermal, airmass scaling on the viewing path, observer at the
+ * top), interpToFinestGrid clblm_Spectrum.f90:735-800, surface emission
+ * calcSurfThmEmis_array clblm_Scene.f90:1304-1392 for a constant emissivity.
+ * ====================================================================== */
+typedef struct {
+  double *v;
+  double V1, DV, V2;
+  int64_t n;
+} spect_t;
+
+static void spect_set(spect_t *sp, double V1, double DV, int64_t n) {
+  sp->V1 = V1;
+  sp->DV = DV;
+  sp->n = n;
+  sp->V2 = V1 + DV * (double)(n - 1);
+  sp->v = (double *)realloc(sp->v, sizeof(double) * (size_t)(n > 0 ? n : 1));
+}
+
+static int same_grid(const spect_t *a, const spect_t *b) {
+  const double E = 2.220446049250313e-16;
+  return fabs(a->V1 - b->V1) < E && fabs(a->V2 - b->V2) < E && fabs(a->DV - b->DV) < E && a->n == b->n;
+}
+
+static int to_finest(ocl_session *s, spect_t **sp, int nsp) {
+  int loc = 0;
+  for (int i = 1; i < nsp; ++i)
+    if (sp[i]->DV < sp[loc]->DV) loc = i;
+  for (int i = 0; i < nsp; ++i) {
+    if (i == loc || same_grid(sp[i], sp[loc])) continue;
+    if (fabs(sp[i]->V1 - sp[loc]->V1) > 2.220446049250313e-16)
+      return fail(s, CLBLM_ERR_GRID, "interpToFinestGrid: different V1");
+    spect_t nw = {0};
+    spect_set(&nw, sp[i]->V1, sp[loc]->DV, sp[loc]->n);
+    int rc = interp_spectrum(s, sp[i]->v, sp[i]->DV, sp[i]->V1, sp[i]->n, nw.v, nw.DV, nw.V1, nw.n);
+    if (rc) {
+      free(nw.v);
+      return rc;
+    }
+    free(sp[i]->v);
+    *sp[i] = nw;
+  }
+  return 0;
+}
+
+int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_column_t *col,
+                 const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap, int64_t *npts, double *dvp) {
+  int n = col->nlay;
+  if (n < 1) return fail(s, CLBLM_ERR_ARG, "no layers");
+  double *dvn = (double *)malloc(sizeof(double) * n), *dvf = (double *)malloc(sizeof(double) * n);
+  double dvo;
+  int rc = ocl_setdv(s, col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, ctrl->grid_type, ctrl->dv_user, dvn,
+                     dvf, &dvo);
+  if (rc) {
+    free(dvn);
+    free(dvf);
+    return rc;
+  }
+  double V1 = col->v1, V2 = col->v2;
+  double DV = dvn[0];
+  int64_t initNLIM = (int64_t)ceil((V2 - V1) / DV + 1.);
+  spect_t R = {0}, Rf = {0}, TA = {0}, TB = {0}, EU = {0}, ED = {0};
+  spect_set(&R, V1, DV, initNLIM);
+  spect_set(&Rf, V1, DV, initNLIM);
+  {
+    double XKTBND = col->tskin / RADCN2;
+    for (int64_t j = 1; j <= initNLIM; ++j) {
+      double v = V1 + (double)(j - 1) * DV;
+      R.v[j - 1] = ocl_planck(v, XKTBND) * col->emis;
+      Rf.v[j - 1] = 1.0 - col->emis;
+    }
+  }
+  double *od = NULL;
+  for (int il = 0; il < n && !rc; ++il) {
+    clblm_layer_t lay;
+    lay.nmol = col->nmol;
+    lay.mol_id = col->mol_id;
+    lay.w = col->w + (size_t)il * col->nmol;
+    lay.wtot = col->wtot[il];
+    lay.pave = col->pave[il];
+    lay.tave = col->tave[il];
+    lay.zbot = 0.;
+    lay.ztop = 0.;
+    lay.lay_no = il + 1;
+    clblm_grid_t g;
+    g.v1 = V1;
+    g.v2 = V2;
+    g.dv_normal = dvn[il];
+    g.dv_narrow = dvf[il];
+    g.dv_out = dvo;
+    g.sample = ctrl->sample;
+    g.alfal0 = ctrl->alfal0;
+    int64_t ns = 0;
+    double dvl = 0.;
+    int64_t capn = (int64_t)ceil((V2 - V1) / (dvn[il] < dvf[il] ? dvn[il] : dvf[il]) + 16.);
+    od = (double *)realloc(od, sizeof(double) * (size_t)capn);
+    rc = ocl_odlay(s, L, C, &lay, &g, &ctrl->od, od, capn, &ns, &dvl, NULL);
+    if (rc) break;
+    double scalUp = col->wtot[il] / lay.wtot;
+    double scalDn = col->wtot_down[il] / lay.wtot;
+    spect_set(&TA, V1, dvl, ns);
+    spect_set(&TB, V1, dvl, ns);
+    spect_set(&EU, V1, dvl, ns);
+    spect_set(&ED, V1, dvl, ns);
+    double *odA = (double *)malloc(sizeof(double) * (size_t)ns), *odB = (double *)malloc(sizeof(double) * (size_t)ns);
+    for (int64_t k = 0; k < ns; ++k) {
+      odA[k] = od[k] * scalUp;
+      odA[k] = odA[k] * 1.0;
+      odB[k] = od[k] * scalDn;
+      odB[k] = odB[k] * 1.0;
+      TA.v[k] = exp(-odA[k]);
+      TB.v[k] = exp(-odB[k]);
+    }
+    layer_emis(ED.v, col->tbot[il], col->ttop[il], col->tave[il], TB.v, odB, ctrl->lin_in_tau, V1, dvl, ns);
+    if (ctrl->lin_in_tau != 0)
+      layer_emis(EU.v, col->ttop[il], col->tbot[il], col->tave[il], TA.v, odA, ctrl->lin_in_tau, V1, dvl, ns);
+    else
+      memcpy(EU.v, ED.v, sizeof(double) * (size_t)ns);
+    free(odA);
+    free(odB);
+    spect_t *arr[6] = {&R, &Rf, &TA, &TB, &EU, &ED};
+    rc = to_finest(s, arr, 6);
+    if (rc) break;
+    for (int64_t k = 0; k < R.n; ++k) R.v[k] = EU.v[k] + TA.v[k] * (R.v[k] + ED.v[k] * Rf.v[k]);
+    for (int64_t k = 0; k < Rf.n; ++k) Rf.v[k] = TA.v[k] * TB.v[k] * Rf.v[k];
+  }
+  if (!rc) {
+    if (npts) *npts = R.n;
+    if (dvp) *dvp = R.DV;
+    if (rad) {
+      if (cap < R.n) rc = fail(s, CLBLM_ERR_CAPACITY, "need %lld points", (long long)R.n);
+      else memcpy(rad, R.v, sizeof(double) * (size_t)R.n);
+    }
+  }
+  free(od);
+  free(R.v);
+  free(Rf.v);
+  free(TA.v);
+  free(TB.v);
+  free(EU.v);
+  free(ED.v);
+  free(dvn);
+  free(dvf);
+  return rc;
+}

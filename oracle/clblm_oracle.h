@@ -1,0 +1,60 @@
+/*
+ * clblm_oracle.h -- CPU FP64 restatement of CLBLM's layer-OD and nadir-RT
+ * path.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the
+ * CPU-baseline leg of bench.py call it as the checker.  Nothing in the
+ * product links or calls it.
+ *
+ * It follows the Fortran control flow literally (panel loop, 250-line
+ * records, deferred lines, per-chunk line shrinking, sticky JRAD) so that
+ * line selection and panel index ranges are the reference's.  Types are the
+ * public ones of include/clblm_gb300.h.
+ */
+#ifndef CLBLM_ORACLE_H
+#define CLBLM_ORACLE_H
+
+#include "../include/clblm_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ocl_session ocl_session;
+
+ocl_session *ocl_create(void);
+void ocl_destroy(ocl_session *s);
+/* reset the sticky JRAD (a fresh process of the reference) */
+void ocl_reset(ocl_session *s);
+const char *ocl_last_error(const ocl_session *s);
+
+int ocl_setdv(ocl_session *s, const clblm_column_t *col, double sample,
+              double alfal0, double alfal0_fine, int32_t grid_type,
+              double dv_user, double *dv_normal, double *dv_narrow,
+              double *dv_out);
+
+/* ODLAY_nonStruct.  out may be NULL (size query); returns CLBLM_ERR_CAPACITY
+ * with *nsamp set when cap is too small. */
+int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
+              const clblm_layer_t *lay, const clblm_grid_t *g,
+              const clblm_od_ctrl_t *ctrl, double *out, int64_t cap,
+              int64_t *nsamp, double *dv_used, clblm_od_stats_t *st);
+
+/* mode2_lookDn_mergeUp thermal nadir radiance. */
+int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
+                 const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl,
+                 double *rad, int64_t cap, int64_t *npts, double *dv);
+
+/* Building blocks exposed for known-answer tests. */
+void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg,
+                      double *xver); /* each [3001] */
+double ocl_radfn(double vi, double xkt);
+double ocl_planck(double v, double xkt);
+void ocl_rlin(double od, double *hlf);
+int ocl_tips_scor(int mol, double t, double *scor);
+int ocl_interp_spectrum(const double *in, double dvin, double v1in,
+                        int64_t nin, double *out, double dvout, double v1out,
+                        int64_t nout);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,160 @@
+"""ctypes binding of the CPU FP64 oracle (oracle/_build/libclblm_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py, always as the checker.  The product never
+imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from clblm_gb300 import capi_types as T
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libclblm_oracle.so"
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("oracle error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        P = C.POINTER
+        L.ocl_create.restype = C.c_void_p
+        L.ocl_destroy.argtypes = [C.c_void_p]
+        L.ocl_reset.argtypes = [C.c_void_p]
+        L.ocl_last_error.restype = C.c_char_p
+        L.ocl_last_error.argtypes = [C.c_void_p]
+        L.ocl_odlay.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_layer_t),
+                                P(T.clblm_grid_t), P(T.clblm_od_ctrl_t), P(C.c_double), C.c_int64,
+                                P(C.c_int64), P(C.c_double), P(T.clblm_od_stats_t)]
+        L.ocl_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
+                                   P(T.clblm_rt_ctrl_t), P(C.c_double), C.c_int64, P(C.c_int64),
+                                   P(C.c_double)]
+        L.ocl_setdv.argtypes = [C.c_void_p, P(T.clblm_column_t), C.c_double, C.c_double, C.c_double,
+                                C.c_int32, C.c_double, P(C.c_double), P(C.c_double), P(C.c_double)]
+        L.ocl_shape_tables.argtypes = [P(C.c_double)] * 5
+        L.ocl_radfn.restype = C.c_double
+        L.ocl_radfn.argtypes = [C.c_double, C.c_double]
+        L.ocl_planck.restype = C.c_double
+        L.ocl_planck.argtypes = [C.c_double, C.c_double]
+        L.ocl_rlin.argtypes = [C.c_double, P(C.c_double)]
+        L.ocl_tips_scor.argtypes = [C.c_int, C.c_double, P(C.c_double)]
+        L.ocl_interp_spectrum.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, P(C.c_double),
+                                          C.c_double, C.c_double, C.c_int64]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Session:
+    """One reference 'process': holds the sticky JRAD state."""
+
+    def __init__(self):
+        self.h = lib().ocl_create()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ocl_destroy(self.h)
+            self.h = None
+
+    def reset(self):
+        lib().ocl_reset(self.h)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise OracleError(rc, lib().ocl_last_error(self.h).decode())
+
+    def setdv(self, col, sample=4.0, alfal0=0.04, alfal0_fine=0.005, grid_type=0, dv_user=-1.0):
+        n = col.nlay
+        dn, df, do = np.zeros(n), np.zeros(n), C.c_double()
+        cs = col.struct()
+        self._check(lib().ocl_setdv(self.h, C.byref(cs), sample, alfal0, alfal0_fine, grid_type, dv_user,
+                                    _dp(dn), _dp(df), C.byref(do)))
+        return dn, df, do.value
+
+    def odlay(self, lines, layer, grid, ctrl, cont=None):
+        ls = lines.struct()
+        cs = cont.struct() if cont is not None else None
+        ns, dv, st = C.c_int64(), C.c_double(), T.clblm_od_stats_t()
+        cap = int(np.ceil((grid.v2 - grid.v1) / min(grid.dv_normal, grid.dv_narrow,
+                                                     grid.dv_out if grid.dv_out > 0 else 1e9))) + 64
+        out = np.zeros(cap)
+        rc = lib().ocl_odlay(self.h, C.byref(ls), C.byref(cs) if cs is not None else None, C.byref(layer),
+                             C.byref(grid), C.byref(ctrl), _dp(out), cap, C.byref(ns), C.byref(dv),
+                             C.byref(st))
+        self._check(rc)
+        return out[:ns.value].copy(), dv.value, st.as_dict()
+
+    def rt_mode2(self, lines, col, ctrl, cont=None):
+        ls, cols = lines.struct(), col.struct()
+        cs = cont.struct() if cont is not None else None
+        n, dv = C.c_int64(), C.c_double()
+        rc = lib().ocl_rt_mode2(self.h, C.byref(ls), C.byref(cs) if cs is not None else None,
+                                C.byref(cols), C.byref(ctrl), None, 0, C.byref(n), C.byref(dv))
+        if rc not in (0, T.CLBLM_ERR_CAPACITY):
+            self._check(rc)
+        self.reset()
+        out = np.zeros(n.value)
+        self._check(lib().ocl_rt_mode2(self.h, C.byref(ls), C.byref(cs) if cs is not None else None,
+                                       C.byref(cols), C.byref(ctrl), _dp(out), n.value, C.byref(n),
+                                       C.byref(dv)))
+        return out, dv.value
+
+
+def shape_tables():
+    arrs = [np.zeros(3001) for _ in range(5)]
+    lib().ocl_shape_tables(*[_dp(a) for a in arrs])
+    return dict(zip(("F1", "F2", "F3", "FG", "XVER"), arrs))
+
+
+def radfn(v, xkt):
+    return lib().ocl_radfn(float(v), float(xkt))
+
+
+def planck(v, xkt):
+    return lib().ocl_planck(float(v), float(xkt))
+
+
+def rlin(od):
+    h = C.c_double()
+    lib().ocl_rlin(float(od), C.byref(h))
+    return h.value
+
+
+def tips_scor(mol, t):
+    s = C.c_double()
+    rc = lib().ocl_tips_scor(int(mol), float(t), C.byref(s))
+    if rc:
+        raise OracleError(rc, "tips")
+    return s.value
+
+
+def interp_spectrum(spin, dvin, v1in, dvout, v1out, nout):
+    spin = np.ascontiguousarray(spin, dtype=np.float64)
+    out = np.zeros(nout)
+    rc = lib().ocl_interp_spectrum(_dp(spin), dvin, v1in, len(spin), _dp(out), dvout, v1out, nout)
+    if rc:
+        raise OracleError(rc, "interp")
+    return out
