@@ -1,0 +1,305 @@
+"""Benchmark: nadir upwelling radiance of the 60-layer, 500,000-line,
+500-2500 cm-1 column (seven absorbers, synthetic continuum), i.e. per-layer
+line-by-line optical depth + far wings + continuum + the layer radiance merge.
+
+Metric: layer-spectral-points/s = sum over layers of the layer-grid points
+(what ODLAY returns per layer) / time of one full column.
+
+  value            mixed path (FP32 line shape, Kahan sums, FP64 index math),
+                   line list already resident on the device, radiance left on
+                   the device; timed with CUDA events on the library's stream
+  e2e              the same call through the C-ABI with host buffers: the line
+                   list is copied in from pinned host memory and the radiance
+                   copied back to pinned host memory inside every step
+  plain            the FP64 GPU path on the same column (reported beside)
+  cpu_baseline     the FP64 CPU restatement of the reference on a bounded
+                   sample of layers of the same column
+  --impl reference the reference's CPU path (the FP64 restatement, all host
+                   threads) on a bounded sample of the same workload
+
+Inputs are larger than L2 (the line list alone is 20 MB, the per-layer
+working set of a few layers exceeds 129 MB), so no extra L2 flush is done.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "layer-spectral-points/s"
+UNIT = "layer-points/s"
+WORKLOAD = "60-layer nadir radiance, 500000 lines (7 absorbers), 500-2500 cm-1, synthetic continuum"
+
+
+def layer_points(h, col, ctrl):
+    """Sum over layers of the points ODLAY returns on each layer grid."""
+    from clblm_gb300 import capi
+    from clblm_gb300 import capi_types as T
+    dn, df, do = capi.setDV(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, ctrl.grid_type, ctrl.dv_user)
+    tot = 0
+    for il in range(col.nlay):
+        g = T.grid_struct(col.v1, col.v2, dn[il], df[il], do, ctrl.sample, ctrl.alfal0)
+        n, _ = h.od_size(col.layer(il), g, ctrl.od)
+        tot += n
+    return tot
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                      "--query-gpu=" + self.Q, "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.splitlines()[0].split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def pinned_lines(lines):
+    """Copy of a line list whose arrays live in pinned host memory."""
+    import torch
+    from clblm_gb300.capi_types import Lines
+    arrs = {}
+    keep = []
+    for name, dt in Lines.FIELDS:
+        src = getattr(lines, name)
+        t = torch.empty(src.nbytes, dtype=torch.uint8, pin_memory=True)
+        a = t.numpy().view(dt)
+        a[:] = src
+        arrs[name] = a
+        keep.append(t)
+    pl = Lines(**arrs)
+    pl._pinned = keep
+    return pl
+
+
+CPU_LAYERS = list(range(28, 34))     # single-thread sample: 6 adjacent layers
+REF_LAYERS = list(range(20, 36))     # reference arm (all threads): 16 adjacent layers
+
+
+def cpu_sample_column(col, layers=CPU_LAYERS):
+    """Adjacent layers of the column (the reference STOPs on DV ratios > 2.5
+    between neighbouring layers, so the sample keeps them adjacent)."""
+    return col.sub(layers)
+
+
+def run_cpu(lines, col, cont, ctrl, threads, layers=CPU_LAYERS):
+    from oracle import oracle as O
+    s = O.Session()
+    sub = cpu_sample_column(col, layers)
+    t0 = time.perf_counter()
+    s.rt_mode2(lines, sub, ctrl, cont, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return sub, dt
+
+
+def sample_points(col, ctrl):
+    from clblm_gb300 import capi_types as T
+    from oracle import oracle as O
+    s = O.Session()
+    dn, df, do = s.setdv(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, ctrl.grid_type, ctrl.dv_user)
+    tot = 0
+    for il in range(col.nlay):
+        dv = dn[il] if abs(dn[il] - df[il]) / dn[il] > 0.2 else df[il]
+        # points ODLAY returns (panel rule); computed by the oracle's size query
+        g = T.grid_struct(col.v1, col.v2, dn[il], df[il], do, ctrl.sample, ctrl.alfal0)
+        n = int(np.ceil((col.v2 - col.v1) / dv + 1.0))
+        tot += n
+    return tot
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 GPU leg")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    from clblm_gb300 import synth
+    from clblm_gb300 import capi_types as T
+
+    lines, col, cont = synth.config1()
+    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_MIXED)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle as O
+        O.build()
+        threads = os.cpu_count() or 1
+        # each step: the reference path on the sample column (all host threads)
+        for _ in range(min(args.warmup, 1)):
+            run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), threads, REF_LAYERS)
+        times = []
+        sub = None
+        for _ in range(args.steps):
+            sub, dt = run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), threads, REF_LAYERS)
+            times.append(dt)
+        pts = sample_points(sub, ctrl)
+        v = pts / float(np.mean(times))
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "sample": "layers %d-%d of the column" % (REF_LAYERS[0], REF_LAYERS[-1])},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "layers %d-%d of the 60-layer column, full 500-2500 cm-1, OpenMP over layers"
+                                           % (REF_LAYERS[0], REF_LAYERS[-1])},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from clblm_gb300 import build as B
+    from clblm_gb300 import capi
+    B.build()
+    torch.cuda.set_device(0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    h = capi.Handle(lines, cont, device=torch.cuda.current_device())
+    npts, _ = h.rt_size(col, ctrl)
+    lp = layer_points(h, col, ctrl)
+    rad_dev = torch.empty(npts, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.ExternalStream(h.stream())
+
+    def step_dev(c=ctrl):
+        h.rt_mode2_device(col, c, rad_dev.data_ptr(), npts)
+
+    # warm-up (first calls grow the workspace)
+    for _ in range(max(3, args.warmup)):
+        step_dev()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks() as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_dev()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = lp * world / (ms * 1e-3)
+
+    # e2e through the C-ABI with host buffers
+    plines = pinned_lines(lines)
+    rad_host = torch.empty(npts, dtype=torch.float64, pin_memory=True).numpy()
+    h2d = plines.nbytes()
+    d2h = npts * 8
+    for _ in range(2):
+        h.set_lines(plines)
+        h.rt_mode2(col, ctrl, out=rad_host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h.set_lines(plines)
+        h.rt_mode2(col, ctrl, out=rad_host)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_value = lp * world / (e2e_ms * 1e-3)
+
+    # FP64 GPU path
+    plain = None
+    if not args.no_plain:
+        pctrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN)
+        step_dev(pctrl)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step_dev(pctrl)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1)
+        plain = {"value": lp / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms}
+        # radiance agreement of the mixed path with the FP64 GPU path
+        r64 = torch.empty_like(rad_dev)
+        h.rt_mode2_device(col, pctrl, r64.data_ptr(), npts)
+        step_dev()
+        torch.cuda.synchronize()
+        plain["max_rel_rad_diff_mixed_vs_plain"] = float(((rad_dev - r64).abs() / r64.abs()).max().item())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        sub, dt = run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), 1)
+        pts = sample_points(sub, ctrl)
+        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "layers %d-%d of the column, full 500-2500 cm-1, one thread (%.1f s)"
+                         % (CPU_LAYERS[0], CPU_LAYERS[-1], dt)}
+
+    roof = None
+    rf = ROOT / "profiles" / "roofline_live.json"
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 (mixed: FP32 line shape + Kahan, FP64 index math)",
+                "data": "synthetic (seeded, workload distributions)",
+                "config": {"workload": WORKLOAD, "layers": col.nlay, "lines": lines.n,
+                           "layer_points_per_step": lp, "radiance_points": npts,
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "l2": "inputs larger than L2, no flush"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": e2e_ms},
+                "plain_fp64": plain, "cpu_baseline": cpu, "roofline": roof, "clocks": clk.summary(),
+                "gpu_launches": None}
+        print(json.dumps(line))
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+"""ctypes binding of the GB300 C-ABI (libclblm_gb300.so, include/clblm_gb300.h)
+and a host-side mirror of the reference's interface for this path:
+
+  ODLAY(...)               -> clblm_gpu_od          (ODLAY_nonStruct, clblm_ODLAY.f90:129)
+  setDV(...)               -> clblm_setdv           (setDV_struct, clblm_setDV.f90:114)
+  mode2_lookDn_mergeUp(...)-> clblm_gpu_rt_mode2    (clblm_noScattRT.f90:1134)
+
+The library is loaded from the package directory; if it has not been built,
+or no CUDA device is usable, calls fail loudly (there is no CPU fallback).
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import capi_types as T
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libclblm_gb300.so"
+
+EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clblm_gpu_last_error",
+           "clblm_gpu_stream",
+           "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
+           "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2")
+
+
+class ClblmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("clblm error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libclblm_gb300.so (raises if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ClblmError(T.CLBLM_ERR_NO_DEVICE,
+                             "%s not built: run `python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+        L = C.CDLL(str(LIB_PATH))
+        P = C.POINTER
+        L.clblm_gpu_create.argtypes = [P(T.clblm_lines_t), P(T.clblm_cont_t), C.c_int, P(C.c_void_p)]
+        L.clblm_gpu_set_lines.argtypes = [C.c_void_p, P(T.clblm_lines_t)]
+        L.clblm_gpu_destroy.argtypes = [C.c_void_p]
+        L.clblm_gpu_last_error.argtypes = [C.c_void_p]
+        L.clblm_gpu_last_error.restype = C.c_char_p
+        L.clblm_gpu_stream.argtypes = [C.c_void_p]
+        L.clblm_gpu_stream.restype = C.c_void_p
+        L.clblm_setdv.argtypes = [P(T.clblm_column_t), C.c_double, C.c_double, C.c_double, C.c_int32,
+                                  C.c_double, P(C.c_double), P(C.c_double), P(C.c_double)]
+        L.clblm_gpu_od_size.argtypes = [C.c_void_p, P(T.clblm_layer_t), P(T.clblm_grid_t),
+                                        P(T.clblm_od_ctrl_t), P(C.c_int64), P(C.c_double)]
+        L.clblm_gpu_od.argtypes = [C.c_void_p, P(T.clblm_layer_t), P(T.clblm_grid_t), P(T.clblm_od_ctrl_t),
+                                   C.c_void_p, C.c_int64, C.c_int32]
+        L.clblm_gpu_od_stats.argtypes = [C.c_void_p, P(T.clblm_od_stats_t)]
+        L.clblm_gpu_rt_mode2_size.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t),
+                                              P(C.c_int64), P(C.c_double)]
+        L.clblm_gpu_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), C.c_void_p,
+                                         C.c_int64, C.c_int32]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Handle:
+    """A device-resident line list (+ continuum table) and the reference's
+    per-process state (the sticky JRAD)."""
+
+    def __init__(self, lines, cont=None, device=0):
+        self.lines = lines
+        self.cont = cont
+        ls = lines.struct()
+        cs = cont.struct() if cont is not None else None
+        h = C.c_void_p()
+        rc = lib().clblm_gpu_create(C.byref(ls), C.byref(cs) if cs is not None else None, device, C.byref(h))
+        if rc:
+            raise ClblmError(rc, lib().clblm_gpu_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().clblm_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise ClblmError(rc, lib().clblm_gpu_last_error(self.h).decode())
+
+    def stream(self):
+        """cudaStream_t of the handle (as an int)."""
+        return lib().clblm_gpu_stream(self.h)
+
+    def set_lines(self, lines):
+        self.lines = lines
+        ls = lines.struct()
+        self._check(lib().clblm_gpu_set_lines(self.h, C.byref(ls)))
+
+    def od_size(self, layer, grid, ctrl):
+        n, dv = C.c_int64(), C.c_double()
+        self._check(lib().clblm_gpu_od_size(self.h, C.byref(layer), C.byref(grid), C.byref(ctrl), C.byref(n),
+                                            C.byref(dv)))
+        return n.value, dv.value
+
+    def odlay(self, layer, grid, ctrl, out=None):
+        """Layer OD (binary64) on v1 + i*dv; returns (od, dv)."""
+        n, dv = self.od_size(layer, grid, ctrl)
+        if out is None:
+            out = np.empty(n)
+        self._check(lib().clblm_gpu_od(self.h, C.byref(layer), C.byref(grid), C.byref(ctrl),
+                                       out.ctypes.data_as(C.c_void_p), len(out), T.CLBLM_OUT_HOST))
+        return out[:n], dv
+
+    def od_device(self, layer, grid, ctrl, dptr, cap):
+        """Layer OD written to a device buffer (e.g. torch tensor data_ptr())."""
+        self._check(lib().clblm_gpu_od(self.h, C.byref(layer), C.byref(grid), C.byref(ctrl), C.c_void_p(dptr),
+                                       cap, T.CLBLM_OUT_DEVICE))
+
+    def stats(self):
+        s = T.clblm_od_stats_t()
+        self._check(lib().clblm_gpu_od_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def rt_size(self, col, ctrl):
+        n, dv = C.c_int64(), C.c_double()
+        cs = col.struct()
+        self._check(lib().clblm_gpu_rt_mode2_size(self.h, C.byref(cs), C.byref(ctrl), C.byref(n), C.byref(dv)))
+        return n.value, dv.value
+
+    def rt_mode2(self, col, ctrl, out=None):
+        """Nadir upwelling radiance at the top of `col`; returns (rad, dv)."""
+        n, dv = self.rt_size(col, ctrl)
+        if out is None:
+            out = np.empty(n)
+        cs = col.struct()
+        self._check(lib().clblm_gpu_rt_mode2(self.h, C.byref(cs), C.byref(ctrl), out.ctypes.data_as(C.c_void_p),
+                                             len(out), T.CLBLM_OUT_HOST))
+        return out[:n], dv
+
+    def rt_mode2_device(self, col, ctrl, dptr, cap):
+        cs = col.struct()
+        self._check(lib().clblm_gpu_rt_mode2(self.h, C.byref(cs), C.byref(ctrl), C.c_void_p(dptr), cap,
+                                             T.CLBLM_OUT_DEVICE))
+
+
+def setDV(col, sample=4.0, alfal0=0.04, alfal0_fine=0.005, grid_type=0, dv_user=-1.0):
+    """DVnormal, DVnarrow per layer and the output DV (setDV_struct)."""
+    n = col.nlay
+    dn, df, do = np.zeros(n), np.zeros(n), C.c_double()
+    cs = col.struct()
+    rc = lib().clblm_setdv(C.byref(cs), sample, alfal0, alfal0_fine, grid_type, dv_user, _dp(dn), _dp(df),
+                           C.byref(do))
+    if rc:
+        raise ClblmError(rc, "setDV")
+    return dn, df, do.value
+
+
+def ODLAY(handle, layer, grid, ctrl):
+    """monoOD, nSamp, DVout of ODLAY_nonStruct (clblm_ODLAY.f90:129-177)."""
+    od, dv = handle.odlay(layer, grid, ctrl)
+    return od, len(od), dv
+
+
+def mode2_lookDn_mergeUp(handle, col, ctrl):
+    """totalRadUp of mode2_lookDn_mergeUp (clblm_noScattRT.f90:1134)."""
+    return handle.rt_mode2(col, ctrl)

@@ -1,0 +1,100 @@
+// clblm_common.cuh -- constants, per-layer plan and per-line records shared by
+// the GB300 kernels of the layer optical-depth / radiance path.
+//
+// The per-layer plan holds every scalar the reference derives for a layer
+// (ODLAY_nonStruct / OPDPTH / HIRACQ, clblm_ODLAY.f90:129-1300) so that the
+// kernels can rebuild the reference's panel frames exactly: the panel origin
+// VFT of panel p, the array limits MAX1..MAX3, the far-wing grid, ...
+#pragma once
+#include <cstdint>
+
+namespace clblm {
+
+// ---- constants: src/common/clblm_ConstParam.f90 --------------------------
+constexpr double kONEPL = 1.01;     // :49
+constexpr double kONEMI = 0.999;    // :50
+constexpr double kRADCN1 = 1.191042722E-12;  // :70
+constexpr double kRADCN2 = 1.4387752;        // :71
+constexpr double kP0 = 1013.25;     // :110
+constexpr double kT0 = 296.0;       // :112
+constexpr int kNFPTS = 2001;        // :92
+constexpr int kNFMX = 3001;         // :92
+constexpr int kNABSRB = 5050;       // :95
+// HIRACQ panel constants, clblm_ODLAY.f90:1202-1227
+constexpr int kNSHIFT = 32;
+constexpr int kNLIM1 = 2401;
+constexpr int kNLIM2 = kNLIM1 / 4 + 1;   // 601
+constexpr int kNLIM3 = kNLIM2 / 4 + 1;   // 151
+constexpr int kPanelPts = kNLIM1 - 1;    // 2400 R1 points per panel
+constexpr int kPanelR2 = kNLIM2 - 1;     // 600
+constexpr int kPanelR3 = kNLIM3 - 1;     // 150
+constexpr double kHWF1 = 4., kHWF2 = 16., kHWF3 = 64.;
+constexpr double kDXF1 = 0.002, kDXF2 = 0.008, kDXF3 = 0.032;
+constexpr int kLIMOUT4 = 2500;           // clblm_ODLAY_LineF4.f90:86
+constexpr int kTIPSNMOL = 9;
+
+// Per-layer plan, filled on the host (exact FP64 restatement of the scalar
+// set-up of ODLAY_nonStruct, OPDPTH and HIRACQ) and read by the kernels.
+struct LayerPlan {
+  // grid
+  double v1, v2, dv, dvr2, dvr3, alfav, alfmax, bound, vbot, vtop, vft0;
+  double pave, tave, wtot, xkt, xkt0, betacr, tratio, rhorat, pavp0, pavp2;
+  double dptmn, dptfc;
+  int jrad, ilnflg, max1, max2, max3, nalfmax, nbound;
+  int npanels, nhi_last;          // panels and NHI of the last panel
+  int64_t nsamp;                  // R1 points output
+  // processed line range [line_lo, line_hi] (global indices, inclusive)
+  int64_t line_lo, line_hi;
+  int64_t first_rec_end;          // first line index after the first record read
+  // far wing
+  double dvr4, bound4, v1r4, v2r4st, v1l4, v2l4, beta, beta0, betacr4;
+  int64_t nptr4;                  // R4 points on the global far-wing grid
+  int nblk4;                      // LBLF4Q blocks of <= 2500 points along the panels
+  int64_t blk_off;                // this layer's block table: v1r4 / npt / m0 at blk_off + b
+                                  // (block of panel p at vft_off + p in the panel->block map)
+  int64_t f4_lo, f4_hi;           // LINF4Q line range [lo, hi)
+  // continuum (ABSRB on V1ABS + (i-1)*DVABS, 1-based)
+  int contnm;                     // 1: continuum on
+  double v1abs, v2abs, dvabs, xself, xfrgn, wk1, h2o_fac;
+  int nptabs;
+  // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
+  int sel[kTIPSNMOL + 1];
+  double wk[kTIPSNMOL + 1], scor[kTIPSNMOL + 1], rhoslf[kTIPSNMOL + 1], alfd1[kTIPSNMOL + 1];
+  // offsets of this layer's slices inside the shared per-call buffers
+  int64_t vft_off;     // VFT of panel p at vft_off + p
+  int64_t od_off;      // OD output
+  int64_t r4_off;      // R4 grid
+  int64_t abs_off;     // ABSRB (N_ABSRB + 8 per layer)
+};
+
+// Per accepted line, after LNCORQ (clblm_ODLAY.f90:1566-2041).
+struct LinePrep {
+  double vnu;      // shifted centre
+  double sp;       // SP(I) after the T correction
+  double recalf;   // 1 / ALFV
+  double zetai;
+  int iz;          // IZETA
+  int fpanel;      // first panel whose MAX1 fits the line (-1: rejected)
+};
+
+// One line's contribution on one of the three nested grids, in global
+// coordinates of that grid (index 0 at VFT of panel 0).
+struct GridRec {
+  int g_lo, g_hi;   // first / last global index touched (inclusive)
+  int q;            // panel the reference processes the line in
+  float zfl, zs;    // ZFkL and ZSLOPE (FP32 copies for the mixed path)
+  float a0, a1, a2; // strengths: R1 -> STRFA1, STRDA, STRVRA; R2/R3 -> STRFA2/3
+};
+// exact FP64 copies for the plain path and the mixed path's index fix-up
+struct GridRecD {
+  double zfl, zs, a0, a1, a2;
+};
+
+// Far-wing pseudo line after SHRINQ (LINE_SHRINK, clblm_LineData.f90:88-94).
+struct ShrunkLine {
+  double vnu, sp, alfa, alfd, spp;
+  int mol;
+  int pad;
+};
+
+}  // namespace clblm

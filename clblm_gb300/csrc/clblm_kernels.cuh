@@ -1,0 +1,88 @@
+// clblm_kernels.cuh -- device-side argument structs and kernel declarations
+// shared by prep.cu, panel.cu and the host runtime.
+#pragma once
+#include <cstdint>
+
+#include "clblm_common.cuh"
+
+namespace clblm {
+
+constexpr int kStatsPerLayer = 8;  // nlin, lincnt, nminus, nplus, bad, shrunk, -, -
+
+struct LineIn {
+  const double* vnu;
+  const float* sp;
+  const float* alfa;
+  const float* epp;
+  const int* mol;
+  const float* hwhm;
+  const float* tmpalf;
+  const float* pshift;
+  const int* iflg;
+  int64_t n;
+};
+
+struct ContIn {
+  int n;
+  double v1, dv;
+  const double* self_absco_ref;
+  const double* for_absco_ref;
+  const double* self_texp;
+  double ref_press, ref_temp;
+};
+
+// LINF4Q-corrected line (before SHRINQ)
+struct F4Prep {
+  double vnu, sp, alfa, alfd;
+  int mol, pass;
+};
+
+// shape tables in device global memory (loaded into shared memory per CTA)
+struct ShapeTabs {
+  const float4* t1f;   // {F1, FG, XVER, 0}
+  const float* t2f;    // F2
+  const float* t3f;    // F3
+  const double* t1d;   // F1, FG, XVER interleaved [3*NFMX]
+  const double* t2d;
+  const double* t3d;
+};
+
+// kernels of prep.cu (FP64, no FMA contraction)
+extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
+__global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const double* vft_all, LinePrep* out,
+                            int64_t out_stride, unsigned long long* stats);
+__global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,
+                                int nblk_stride);
+__global__ void k_scan_blocks(int* blockmax, int nblk_stride, const int64_t* nlines, int nlayers);
+__global__ void k_scan_apply(const LinePrep* prep, int64_t stride, const int64_t* nlines, const int* blockmax,
+                             int nblk_stride, int* qpanel);
+__global__ void k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
+                               const int* qpanel, int64_t stride, GridRec* rec, GridRecD* recd,
+                               const double* vnu_raw, unsigned long long* stats, double* alfvmax);
+__global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
+                               double shiftmax, int64_t* ranges, int64_t panel_stride);
+__global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);
+__global__ void k_f4_prep(const LayerPlan* plans, int layer0, LineIn lines, F4Prep* out, int64_t stride,
+                          unsigned long long* stats);
+__global__ void k_f4_count(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0, int64_t* blocksum,
+                           int nblk);
+__global__ void k_f4_blockscan(int64_t* blocksum, int nblk, const LayerPlan* plans, int layer0, int nlayers,
+                               int64_t* ntot);
+__global__ void k_f4_compact(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0,
+                             const int64_t* blocksum, int nblk, int64_t* cidx, long long* vbits, long long* lbits,
+                             int64_t* src, unsigned char* flags, int64_t* cut);
+__global__ void k_f4_walk(const LayerPlan* plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
+                          const int64_t* cidx, const long long* vbits, const long long* lbits,
+                          const unsigned char* flags, const int64_t* ntot, const int64_t* cut, int4* groups,
+                          int64_t* ngroups);
+__global__ void k_f4_groupsum(const LayerPlan* plans, int layer0, const F4Prep* prep, int64_t stride,
+                              const int64_t* src, const int4* groups, const int64_t* ngroups, ShrunkLine* out);
+struct F4Rec;
+struct F4RecD;
+__global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
+                              const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
+                              int64_t* nmirror);
+__global__ void k_f4_bounds(const F4Rec* rec, int64_t rstride, const int64_t* nrec, int layer0, int* pmax,
+                            int* smin);
+
+}  // namespace clblm

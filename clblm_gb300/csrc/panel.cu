@@ -1,0 +1,572 @@
+// panel.cu -- hot kernels of the layer optical depth and nadir radiance.
+//
+//   k_panel<Plain>   one CTA per (layer, panel of 2400 points): the three
+//                    nested Voigt sub-function grids R3 (16 DV), R2 (4 DV) and
+//                    R1 (DV) gathered from the per-line records (CNVFNQ,
+//                    clblm_ODLAY.f90:2067-2258), far-wing and continuum
+//                    interpolation into R3 (XINT, clblm_Spectrum.f90:874-915),
+//                    the R3->R2->R1 4-point interpolation and the radiation
+//                    term (panelOut, clblm_ODLAY.f90:2289-2493).
+//   k_f4_conv<Plain> far-wing function 4 on the DVR4 grid (CNVF4Q,
+//                    clblm_ODLAY_LineF4.f90:187-494), one thread per point.
+//   k_rt_layer<...>  one layer of the upward merge of mode2_lookDn_mergeUp
+//                    (layerMerge_mode2, clblm_noScattRT.f90:1704-1794) with
+//                    layerEmis (clblm_EMLAY.f90:104-178) and the
+//                    interpolation to the finest grid (interpSpectrum,
+//                    clblm_Spectrum.f90:326-620) folded into the load.
+//
+// Mixed path: table look-ups, products and sums in FP32 with Kahan-
+// compensated accumulation; every table index is the reference's FP64 index
+// (an FP32 index whose argument is within 1e-3 of a rounding boundary is
+// recomputed in FP64).  Plain path: FP64 throughout.
+#include <cuda_runtime.h>
+
+#include "clblm_common.cuh"
+#include "clblm_kernels.cuh"
+#include "clblm_panel.cuh"
+
+namespace clblm {
+
+// ---------------------------------------------------------------------------
+// accumulators
+struct KahanF {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = __fsub_rn(x, c);
+    float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return __fsub_rn(s, c); }
+};
+struct SumD {
+  double s = 0.;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+// FP32 table index IZ = INT(|ZF| + 1.5) with ZF = ZFL + k*ZSLOPE; falls back
+// to the FP64 record when the FP32 argument is too close to a boundary.
+__device__ __forceinline__ int table_index_mixed(int k, const GridRec& r, const GridRecD* rd) {
+  float zf = fmaf((float)k, r.zs, r.zfl);
+  float az = fabsf(zf);
+  float t = az + 12582913.0f;                  // 1.5*2^23 + 1: rounds |ZF|+1
+  int iz = __float_as_int(t) - 0x4B400000;     // rint(|ZF|) + 1
+  float d = az - (t - 12582913.0f);            // |ZF| - rint(|ZF|), exact
+  if (fabsf(d) > 0.499f) {
+    double zf64 = fma((double)k, rd->zs, rd->zfl);
+    iz = (int)(fabs(zf64) + 1.5);
+  }
+  return iz;
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory layout of k_panel
+template <bool Plain>
+struct PanelSmem;
+
+template <>
+struct PanelSmem<false> {
+  float4 t1[kNFMX];
+  float t2[kNFMX];
+  float t3[kNFMX];
+  float r3n[kR3Pts];     // R3 p-frame 0..160, lines of panels <= p
+  float r3o[8];          // R3 p-frame 0..7, lines of panels <= p-1
+  float r2[kR2Pts];      // R2 p-frame 0..615
+  int seg_start[kMaxSeg + 1];
+  double seg_v[kMaxSeg], seg_d[kMaxSeg];
+  int nseg;
+};
+template <>
+struct PanelSmem<true> {
+  double t1[3 * kNFMX];
+  double t2[kNFMX];
+  double t3[kNFMX];
+  double r3n[kR3Pts];
+  double r3o[8];
+  double r2[kR2Pts];
+  int seg_start[kMaxSeg + 1];
+  double seg_v[kMaxSeg], seg_d[kMaxSeg];
+  int nseg;
+};
+
+size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
+
+__device__ __forceinline__ int64_t lb_d(const double* a, int64_t lo, int64_t hi, double x) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// RADFNI, clblm_ODLAY_CommonSub.f90:379-508 (FP64)
+__device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, double* RDEL, double* RDLAST) {
+  const double FACT1 = 3.0E-03;
+  double XVI = VI;
+  if (*RDLAST < 0.) {
+    if (XKT > 0.0) {
+      double XVIOKT = XVI / XKT;
+      if (XVIOKT <= 0.01) *RDLAST = 0.5 * XVIOKT * XVI;
+      else if (XVIOKT <= 10.0) {
+        double E = exp(-XVIOKT);
+        *RDLAST = XVI * (1. - E) / (1. + E);
+      } else
+        *RDLAST = XVI;
+    } else
+      *RDLAST = XVI;
+  }
+  double RADFNI = *RDLAST;
+  int INTVLS = 1;
+  double RDNEXT;
+  if (XKT > 0.0) {
+    double XVIOKT = XVI / XKT;
+    if (XVIOKT <= 0.01) {
+      *VINEW = VI + FACT1 * 0.5 * XVI;
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+      *VINEW = VI + DVI * (double)INTVLS;
+      double XVINEW = *VINEW;
+      double XVINEWOKT = XVINEW / XKT;
+      RDNEXT = 0.5 * XVINEWOKT * XVINEW;
+    } else if (XVIOKT <= 10.0) {
+      double E = exp(-XVIOKT);
+      double XMINUS = 1. - E, XPLUS = 1. + E;
+      double CVIKT = XVIOKT * E;
+      *VINEW = VI + FACT1 * XVI / (1. + (CVIKT / XMINUS + CVIKT / XPLUS));
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+      *VINEW = VI + DVI * (double)INTVLS;
+      double XVINEW = *VINEW;
+      double XVINEWOKT = XVINEW / XKT;
+      double EN = exp(-XVINEWOKT);
+      RDNEXT = XVINEW * (1. - EN) / (1. + EN);
+    } else {
+      *VINEW = VI + (FACT1 * XVI);
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+      *VINEW = VI + DVI * (double)INTVLS;
+      RDNEXT = *VINEW;
+    }
+  } else {
+    *VINEW = VI + (FACT1 * XVI);
+    INTVLS = (int)((*VINEW - VI) / DVI);
+    if (INTVLS < 1) INTVLS = 1;
+    *VINEW = VI + DVI * (double)INTVLS;
+    RDNEXT = *VINEW;
+  }
+  *RDEL = (RDNEXT - RADFNI) / (double)INTVLS;
+  *RDLAST = RDNEXT;
+  return RADFNI;
+}
+
+// XINT weights of R3 point VI on the grid V1A + (J-1)*DVA (clblm_Spectrum.f90:874-915);
+// returns J and the four weights of A(J-1), A(J), A(J+1), A(J+2).
+__device__ __forceinline__ int xint_weights(double VI, double V1A, double DVA, double w[4]) {
+  double RECDVA = 1. / DVA;
+  int J = (int)((VI - V1A) * RECDVA + kONEPL);
+  double VJ = V1A + DVA * (double)(J - 1);
+  double P = RECDVA * (VI - VJ);
+  double C = (3. - 2. * P) * P * P;
+  double B = 0.5 * P * (1. - P);
+  double B1 = B * (1. - P);
+  double B2 = B * P;
+  w[0] = -B1;
+  w[1] = (1. - C + B2);
+  w[2] = (C + B1);
+  w[3] = -B2;
+  return J;
+}
+
+// JRAD = 1: LBLF4Q multiplies each R4 block by the piecewise-linear
+// radiation term RADFNI started at the block origin
+// (clblm_ODLAY_LineF4.f90:142-177); one thread per block.
+__global__ void k_r4_radfac(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ blk_v1,
+                            const int* __restrict__ blk_n, double* __restrict__ blk_fac) {
+  const LayerPlan& P = plans[blockIdx.y + layer0];
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= P.nblk4 || P.jrad != 1) return;
+  const double V1R4 = blk_v1[P.blk_off + b];
+  const int NPTR4 = blk_n[P.blk_off + b];
+  double* fac = blk_fac + (P.blk_off + b) * (int64_t)(kLIMOUT4 + 2);
+  const double XKT = 1. / (kRADCN2 / P.tave);
+  double VITST = V1R4 - P.dvr4;
+  double RDLAST = -1.;
+  int N1, N2 = 0;
+  do {
+    N1 = N2 + 1;
+    double VI = V1R4 + P.dvr4 * (double)(N1 - 1);
+    double RDEL;
+    double RADVI = radfni_d(VI, P.dvr4, XKT, &VITST, &RDEL, &RDLAST);
+    N2 = (int)((VITST - V1R4) / P.dvr4 + 0.001);
+    if (N2 > NPTR4) N2 = NPTR4;
+    double t = RADVI;
+    for (int I = N1; I <= N2; ++I) {
+      fac[I - 1] = t;
+      t = t + RDEL;
+    }
+  } while (N2 < NPTR4);
+}
+
+template <bool Plain>
+__global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PanelSmem<Plain>& S = *reinterpret_cast<PanelSmem<Plain>*>(smem_raw);
+
+  const int layer = blockIdx.y;
+  const LayerPlan& P = a.plans[layer + a.layer0];
+  const int p = blockIdx.x;
+  if (p >= P.npanels) return;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const double dv = P.dv;
+  const double* vft = a.vft_all + P.vft_off;
+  const double VFT = vft[p];
+  const bool last = (p == P.npanels - 1);
+  const int NHI = last ? P.nhi_last : (kNLIM1 + kNSHIFT - 1);
+
+  // ---- shape tables into shared memory ----
+  if constexpr (Plain) {
+    for (int i = tid; i < 3 * kNFMX; i += blockDim.x) S.t1[i] = a.tabs.t1d[i];
+    for (int i = tid; i < kNFMX; i += blockDim.x) {
+      S.t2[i] = a.tabs.t2d[i];
+      S.t3[i] = a.tabs.t3d[i];
+    }
+  } else {
+    for (int i = tid; i < kNFMX; i += blockDim.x) {
+      S.t1[i] = a.tabs.t1f[i];
+      S.t2[i] = a.tabs.t2f[i];
+      S.t3[i] = a.tabs.t3f[i];
+    }
+  }
+  // ---- radiation-term segments of this panel (panelOut, JRAD = 0) ----
+  if (tid == 0) {
+    int ns = 0;
+    if (P.jrad == 0) {
+      const int NLO = kNSHIFT + 1;
+      double XKT = P.tave / kRADCN2;
+      double V1P = VFT + (double)(NLO - 1) * dv;
+      double VITST = V1P - dv;
+      double RDLAST = -1.;
+      int N2 = NLO - 1;
+      do {
+        int N1 = N2 + 1;
+        double VI = VFT + (double)(N1 - 1) * dv;
+        double RDEL;
+        double RADVI = radfni_d(VI, dv, XKT, &VITST, &RDEL, &RDLAST);
+        N2 = (int)((VITST - VFT) / dv + 0.001);
+        if (N2 > NHI) N2 = NHI;
+        if (ns < kMaxSeg) {
+          S.seg_start[ns] = N1;
+          S.seg_v[ns] = RADVI;
+          S.seg_d[ns] = RDEL;
+        }
+        ns++;
+      } while (N2 < NHI);
+      if (ns > kMaxSeg) atomicOr(a.err, 1);
+      S.seg_start[min(ns, kMaxSeg)] = NHI + 1;
+    }
+    S.nseg = min(ns, kMaxSeg);
+  }
+  __syncthreads();
+
+  const int64_t nl = P.line_hi - P.line_lo + 1;
+  const double* vraw = a.vnu_raw + P.line_lo;
+  const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
+  const GridRec* rec2 = rec1 + a.stride;
+  const GridRec* rec3 = rec2 + a.stride;
+  const GridRecD* rd1 = a.recd + (int64_t)layer * a.stride * 3;
+  const GridRecD* rd2 = rd1 + a.stride;
+  const GridRecD* rd3 = rd2 + a.stride;
+  const int64_t* rg = a.ranges + ((int64_t)layer * a.panel_stride + p) * 6;
+  const double amax = a.alfvmax[layer + a.layer0];
+  const double shift = a.shiftmax * P.rhorat + 1e-9;
+
+  // ---- R3: line sums on p-frame points 0..160 (new) and 0..7 (old) ----
+  {
+    const double reach = 64. * amax + 48. * dv + shift;
+    for (int tile = warp; tile < (kR3Pts + 8 + 31) / 32; tile += kPanelThreads / 32) {
+      int idx = tile * 32 + lane;
+      bool old = idx >= kR3Pts;
+      int J3 = old ? idx - kR3Pts : idx;               // p-frame index
+      bool active = old ? (J3 < 8 && p > 0) : (J3 < kR3Pts);
+      int qmax = old ? p - 1 : p;
+      int g = kPanelR3 * p + J3 - 1;
+      // candidate lines of this tile
+      int J3a = tile * 32 - (old ? kR3Pts : 0), J3b = J3a + 31;
+      if (old) J3a = 0;
+      double vlo = P.vft0 + (double)(kPanelR3 * p + J3a - 1) * 16. * dv - reach;
+      double vhi = P.vft0 + (double)(kPanelR3 * p + J3b - 1) * 16. * dv + reach;
+      int64_t lo = lb_d(vraw, rg[4], rg[5], vlo), hi = lb_d(vraw, lo, rg[5], vhi);
+      Acc acc;
+      for (int64_t i = lo; i < hi; ++i) {
+        GridRec r = rec3[i];
+        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= qmax) {
+          int k = g - r.g_lo + 1;
+          if constexpr (Plain) {
+            GridRecD d = rd3[i];
+            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
+            if (iz <= kNFMX) acc.add(d.a0 * S.t3[iz - 1]);
+            else atomicOr(a.err, 2);
+          } else {
+            int iz = table_index_mixed(k, r, rd3 + i);
+            if (iz <= kNFMX) acc.add(r.a0 * S.t3[iz - 1]);
+            else atomicOr(a.err, 2);
+          }
+        }
+      }
+      if (active) {
+        // far wings (R4) and continuum (ABSRB) interpolated into R3
+        double VI = VFT + (16. * dv) * (double)(J3 - 1);
+        double extra = 0.;
+        if (P.nptr4 > 0) {
+          // the R4 block LBLF4Q held when XINT reached the point: this panel's
+          // for N1R3 = 6..155, the previous panel's for the carried points
+          // 1..5 (XINT'd there as 151..155)
+          const Real* R4 = reinterpret_cast<const Real*>(a.r4_all) + P.r4_off;  // global R4[m]
+          const int b = a.panel_blk[P.vft_off + ((p > 0 && J3 < 6) ? p - 1 : p)];
+          const double V1R4 = a.blk_v1[P.blk_off + b];
+          const int NPTR4 = a.blk_n[P.blk_off + b];
+          const int64_t m0 = a.blk_m0[P.blk_off + b];
+          const double V2R4 = V1R4 + P.dvr4 * (double)(NPTR4 - 1);
+          int ILO = (int)((V1R4 + P.dvr4 - VFT) / (16. * dv) + 1. + kONEMI);
+          int IHI = (int)((V2R4 - P.dvr4 - VFT) / (16. * dv) + kONEMI);
+          if (J3 >= ILO && J3 <= IHI) {
+            double w[4];
+            int J = xint_weights(VI, V1R4, P.dvr4, w);
+            const double* fac = a.blk_fac + (P.blk_off + b) * (int64_t)(kLIMOUT4 + 2);
+            for (int k = 0; k < 4; ++k) {
+              int jb = J - 1 + k;  // 1-based point of the block; zero past NPTR4
+              double v = 0.;
+              if (jb >= 1 && jb <= NPTR4 && m0 + jb - 1 < P.nptr4) {
+                v = (double)R4[m0 + jb - 1];
+                if (P.jrad == 1) v *= fac[jb - 1];
+              }
+              extra += v * w[k];
+            }
+          }
+        }
+        if (P.contnm) {
+          const double* AB = a.absrb_all + P.abs_off;  // 1-based
+          int ILO = (int)((P.v1abs + P.dvabs - VFT) / (16. * dv) + 1. + kONEMI);
+          int IHI = (int)((P.v2abs - P.dvabs - VFT) / (16. * dv) + kONEMI);
+          if (J3 >= ILO && J3 <= IHI) {
+            double w[4];
+            int J = xint_weights(VI, P.v1abs, P.dvabs, w);
+            extra += AB[J - 1] * w[0] + AB[J] * w[1] + AB[J + 1] * w[2] + AB[J + 2] * w[3];
+          }
+        }
+        acc.add((Real)extra);
+        if (old) S.r3o[J3] = acc.value();
+        else S.r3n[J3] = acc.value();
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- R2: line sums + R3 interpolation on p-frame points 5..615 ----
+  {
+    const Real X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
+    const Real X10 = -1. / 16., X11 = 9. / 16.;
+    const int LIMLO = (p == 0) ? 5 : 13;          // N1R2 (+4 in the first panel)
+    const int LIMHI = NHI / 4 + 1;
+    const int lastJg = LIMLO + ((LIMHI - LIMLO) / 4) * 4;  // last group start of the loop
+    const double reach = 16. * amax + 12. * dv + shift;
+    for (int tile = warp; tile * 32 < kR2Pts; tile += kPanelThreads / 32) {
+      int J = tile * 32 + lane;  // p-frame R2 index
+      bool active = J >= 5 && J < kR2Pts;
+      int g = kPanelR2 * p + J - 1;
+      double vlo = P.vft0 + (double)(kPanelR2 * p + tile * 32 - 1) * 4. * dv - reach;
+      double vhi = P.vft0 + (double)(kPanelR2 * p + tile * 32 + 30) * 4. * dv + reach;
+      int64_t lo = lb_d(vraw, rg[2], rg[3], vlo), hi = lb_d(vraw, lo, rg[3], vhi);
+      Acc acc;
+      for (int64_t i = lo; i < hi; ++i) {
+        GridRec r = rec2[i];
+        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= p) {
+          int k = g - r.g_lo + 1;
+          if constexpr (Plain) {
+            GridRecD d = rd2[i];
+            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
+            if (iz <= kNFMX) acc.add(d.a0 * S.t2[iz - 1]);
+            else atomicOr(a.err, 2);
+          } else {
+            int iz = table_index_mixed(k, r, rd2 + i);
+            if (iz <= kNFMX) acc.add(r.a0 * S.t2[iz - 1]);
+            else atomicOr(a.err, 2);
+          }
+        }
+      }
+      if (active) {
+        int off = (J - 1) & 3;
+        int Jg = J - off;
+        bool inloop = (LIMLO <= LIMHI) && Jg >= LIMLO && Jg <= LIMHI;
+        bool extra = last && (LIMLO <= LIMHI) && Jg == lastJg + 4 && off <= 1;
+        bool fromOld = (p > 0) && (Jg == 5 || Jg == 9);
+        Real v = 0;
+        if (inloop || extra || fromOld) {
+          const Real* R3 = fromOld ? S.r3o : S.r3n;
+          int J3 = (Jg - 1) / 4 + 1;
+          if (off == 0) v = R3[J3];
+          else if (off == 1) v = X00 * R3[J3 - 1] + X01 * R3[J3] + X02 * R3[J3 + 1] + X03 * R3[J3 + 2];
+          else if (off == 2) v = X10 * (R3[J3 - 1] + R3[J3 + 2]) + X11 * (R3[J3] + R3[J3 + 1]);
+          else v = X03 * R3[J3 - 1] + X02 * R3[J3] + X01 * R3[J3 + 1] + X00 * R3[J3 + 2];
+        }
+        acc.add(v);
+        S.r2[J] = acc.value();
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- R1: line sums + R2 interpolation + radiation term -> OD ----
+  {
+    const Real X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
+    const Real X10 = -1. / 16., X11 = 9. / 16.;
+    const double reach = 4. * amax + 3. * dv + shift;
+    Real* od = reinterpret_cast<Real*>(a.od_all) + P.od_off;
+    const int npts = NHI - kNSHIFT;  // output points of this panel
+    for (int tile = warp; tile * 32 < npts; tile += kPanelThreads / 32) {
+      int J = kNSHIFT + 1 + tile * 32 + lane;  // p-frame R1 index, 33..
+      bool active = J <= NHI;
+      int g = kPanelPts * p + J - 1;
+      double vlo = P.vft0 + (double)(kPanelPts * p + kNSHIFT + tile * 32) * dv - reach;
+      double vhi = P.vft0 + (double)(kPanelPts * p + kNSHIFT + tile * 32 + 31) * dv + reach;
+      int64_t lo = lb_d(vraw, rg[0], rg[1], vlo), hi = lb_d(vraw, lo, rg[1], vhi);
+      Acc acc;
+      for (int64_t i = lo; i < hi; ++i) {
+        GridRec r = rec1[i];
+        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= p) {
+          int k = g - r.g_lo + 1;
+          if constexpr (Plain) {
+            GridRecD d = rd1[i];
+            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
+            if (iz <= kNFMX) {
+              const double* T = S.t1 + 3 * (iz - 1);
+              acc.add(d.a0 * T[0] + d.a1 * T[1] + d.a2 * T[2]);
+            } else
+              atomicOr(a.err, 2);
+          } else {
+            int iz = table_index_mixed(k, r, rd1 + i);
+            if (iz <= kNFMX) {
+              float4 T = S.t1[iz - 1];
+              acc.add(fmaf(r.a0, T.x, fmaf(r.a1, T.y, r.a2 * T.z)));
+            } else
+              atomicOr(a.err, 2);
+          }
+        }
+      }
+      if (active) {
+        int off = (J - 33) & 3;
+        int Jg = J - off;
+        int J2 = (Jg - 1) / 4 + 1;
+        const Real* R2 = S.r2;
+        Real v;
+        if (off == 0) v = R2[J2];
+        else if (off == 1) v = X00 * R2[J2 - 1] + X01 * R2[J2] + X02 * R2[J2 + 1] + X03 * R2[J2 + 2];
+        else if (off == 2) v = X10 * (R2[J2 - 1] + R2[J2 + 2]) + X11 * (R2[J2] + R2[J2 + 1]);
+        else v = X03 * R2[J2 - 1] + X02 * R2[J2] + X01 * R2[J2 + 1] + X00 * R2[J2 + 2];
+        acc.add(v);
+        Real val = acc.value();
+        if (P.jrad == 0) {
+          // segment of J: largest s with seg_start[s] <= J
+          int s0 = 0, s1 = S.nseg;
+          while (s1 - s0 > 1) {
+            int m = (s0 + s1) >> 1;
+            if (S.seg_start[m] <= J) s0 = m;
+            else s1 = m;
+          }
+          double f = S.seg_v[s0] + (double)(J - S.seg_start[s0]) * S.seg_d[s0];
+          val = (Real)((double)val * f);
+        }
+        od[(int64_t)kPanelPts * p + (J - kNSHIFT - 1)] = val;
+      }
+    }
+  }
+}
+
+template __global__ void k_panel<false>(PanelArgs);
+template __global__ void k_panel<true>(PanelArgs);
+
+// ---------------------------------------------------------------------------
+// Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1, one thread per
+// point; the records overlapping point J = m+1 are the index range between the
+// first record whose running max of JMAX reaches J and the first record whose
+// running min of JMIN (from the right) exceeds J.
+template <bool Plain>
+__global__ void k_f4_conv(F4Args a) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
+  const int layer = blockIdx.y;
+  const LayerPlan& P = a.plans[layer + a.layer0];
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= P.nptr4 + 2) return;
+  if (m >= P.nptr4) {  // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94)
+    reinterpret_cast<Real*>(a.r4_all)[P.r4_off + m] = (Real)0;
+    return;
+  }
+  const int J = (int)m + 1;
+  const int64_t n = a.nrec[layer + a.layer0];
+  const int64_t nm = a.nmirror[layer + a.layer0];
+  const F4Rec* R = a.rec + (int64_t)layer * a.stride;
+  const F4RecD* D = a.recd + (int64_t)layer * a.stride;
+  const int* pm = a.pmax_jmax + (int64_t)layer * a.stride;
+  const int* sm = a.smin_jmin + (int64_t)layer * a.stride;
+  int64_t lo, hi;
+  {
+    int64_t l = 0, h = n;
+    while (l < h) {
+      int64_t mid = (l + h) >> 1;
+      if (pm[mid] < J) l = mid + 1;
+      else h = mid;
+    }
+    lo = l;
+    h = n;
+    while (l < h) {
+      int64_t mid = (l + h) >> 1;
+      if (sm[mid] <= J) l = mid + 1;
+      else h = mid;
+    }
+    hi = l;
+  }
+  const float dvr4f = (float)P.dvr4;
+  const double ZSQBND = 64. * 64.;
+  Acc acc;
+  auto one = [&](int64_t i) {
+    const F4Rec r = R[i];
+    if (J < r.jmin || J > r.jmax) return;
+    if constexpr (Plain) {
+      const F4RecD d = D[i];
+      double XM = (double)m * P.dvr4 - d.xnui;
+      double XMSQ = XM * XM;
+      double ZVSQ = XMSQ / d.alv2;
+      const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
+      const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
+      double fb = r.co2 ? (2. - XMSQ / (P.bound4 * P.bound4)) * d.fbnd : d.fbnd;
+      double F4FN;
+      if (ZVSQ <= ZSQBND) F4FN = (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
+      else F4FN = d.sil / (d.al2 + XMSQ) - fb;
+      acc.add(F4FN);
+    } else {
+      float xm = fmaf((float)(J - 1 - r.mc), dvr4f, r.x0);
+      float xmsq = xm * xm;
+      float zvsq = xmsq * r.ralv2;
+      float fb = r.co2 ? (2.f - xmsq * r.rbnd2) * r.fbnd : r.fbnd;
+      float f;
+      if (zvsq <= 4096.f) f = fmaf(zvsq, r.sb3, r.sa3) - fb;
+      else f = __fdividef(r.sil, r.al2 + xmsq) - fb;
+      acc.add(f);
+    }
+  };
+  for (int64_t i = lo; i < hi; ++i) one(i);
+  for (int64_t i = n; i < n + nm; ++i) one(i);
+  Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
+  R4[m] = (Real)acc.value();
+}
+
+template __global__ void k_f4_conv<false>(F4Args);
+template __global__ void k_f4_conv<true>(F4Args);
+
+}  // namespace clblm

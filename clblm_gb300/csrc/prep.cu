@@ -1,0 +1,955 @@
+// prep.cu -- FP64 per-line preparation kernels of the layer optical depth.
+//
+// Compiled with -fmad=false: like the reference's unoptimised build, every
+// double product and sum is rounded on its own, so the index arithmetic
+// (panel of a line, JMIN1/JMAX1, J2SHFT, J3SHFT) reproduces the Fortran's.
+//
+// Kernels (reference routine in brackets):
+//   k_line_prep      LNCORQ per line + first panel that fits the line
+//                    (clblm_ODLAY.f90:1566-2041, CNVFNQ deferral :2176-2181)
+//   k_scan_*         prefix maximum of the first-fit panel = the panel the
+//                    sequential reference convolves each line in
+//   k_line_records   CNVFNQ per-line set-up in the line's panel frame
+//                    (clblm_ODLAY.f90:2127-2166)
+//   k_continuum      mt_ckd_h2o_absco + CONTNM H2O block onto ABSRB
+//                    (mt_ckd_h2o_module.f90:72-170, clblm_ODLAY_Continuum.f90:355-405)
+//   k_f4_prep        LINF4Q per-line corrections (clblm_ODLAY_LineF4.f90:872-1171)
+//   k_f4_count/compact/walk/groupsum  the LINF4Q record loop with SHRINQ
+//                    (:959-1234, :1516-1647)
+#include "clblm_common.cuh"
+#include "clblm_kernels.cuh"
+#include "clblm_panel.cuh"
+
+namespace clblm {
+
+__constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
+// MaxISOTPL_smass, clblm_ConstParam.f90:246-251 (molecules 1..9)
+__constant__ int c_MAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
+
+__device__ __forceinline__ double radfn_d(double VI, double XKT) {
+  // RADFN, clblm_ODLAY_CommonSub.f90:293-323
+  double XVI = VI;
+  if (XKT > 0.0) {
+    double XVIOKT = XVI / XKT;
+    if (XVIOKT <= 0.01) return 0.5 * XVIOKT * XVI;
+    if (XVIOKT <= 10.0) {
+      double E = exp(-XVIOKT);
+      return XVI * (1. - E) / (1. + E);
+    }
+  }
+  return XVI;
+}
+
+// Does panel p (origin vft) take the line: JMAX1 <= MAX1 (CNVFNQ :2176-2181).
+__device__ __forceinline__ bool fits_panel(double vnu, double vft, double dv, double bhwdxf, int max1) {
+  double ZINT = (vnu - vft) / dv;
+  int JMAX1 = (int)(ZINT + bhwdxf + 1.5);
+  return JMAX1 <= max1;
+}
+
+__global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+                            const double* __restrict__ vft_all, LinePrep* __restrict__ out,
+                            int64_t out_stride, unsigned long long* __restrict__ stats) {
+  const LayerPlan& P = plans[blockIdx.y + layer0];
+  int64_t n = P.line_hi - P.line_lo + 1;
+  LinePrep* o = out + (int64_t)blockIdx.y * out_stride;
+  const double* vft = vft_all + P.vft_off;
+  unsigned long long nlin = 0, lincnt = 0, nminus = 0, nplus = 0, bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = P.line_lo + t;
+    LinePrep r;
+    r.vnu = 0.;
+    r.sp = 0.;
+    r.recalf = 0.;
+    r.zetai = 0.;
+    r.iz = 0;
+    r.fpanel = -1;
+    int iflg = lines.iflg[i];
+    int molf = lines.mol[i];
+    int m = molf % 100;
+    int iso = (molf % 1000) / 100;
+    if (iso == 0) iso = 10;
+    bool ok = iflg >= 0 && m >= 1 && m <= kTIPSNMOL && P.sel[m];
+    if (ok && iso > c_MAXISO[m]) ok = false;
+    if (ok && (iso != 1 || iflg == 1 || iflg == 3)) {
+      bad++;
+      ok = false;
+    }
+    double SUI = 0.;
+    if (ok) {
+      SUI = (double)lines.sp[i] * P.wk[m];
+      if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
+      if (SUI == 0.) ok = false;
+    }
+    if (ok) {
+      nlin++;
+      double alfa0 = (double)lines.alfa[i];
+      double hwhms = (double)lines.hwhm[i];
+      if (m == 7) alfa0 = (alfa0 - 0.21 * hwhms) / (1.0 - 0.21);
+      double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
+      double TMPCOR = pow(P.tratio, (double)lines.tmpalf[i]);
+      double ALFA0I = alfa0 * TMPCOR;
+      double HWHMSI = hwhms * TMPCOR;
+      double ALFL = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
+      double ALFAD = VNU * P.alfd1[m];
+      double ZETA = ALFL / (ALFL + ALFAD);
+      double FZETA = 100. * ZETA;
+      int IZ = (int)(FZETA + kONEPL);
+      if (!(IZ >= 1 && IZ <= 101)) {
+        bad++;
+        ok = false;
+      } else {
+        double ZETDIF = FZETA - (double)(IZ - 1);
+        double ALFV = (c_AVRAT[IZ - 1] + ZETDIF * (c_AVRAT[IZ] - c_AVRAT[IZ - 1])) * (ALFL + ALFAD);
+        int nmin = 0, npl = 0;
+        if (ALFV < P.dv) {
+          ALFV = P.dv;
+          nmin = 1;
+        }
+        if (ALFV > P.alfmax) {
+          ALFV = P.alfmax;
+          npl = 1;
+        }
+        // HWF3*ALFV + VNU < VFT: the line cannot reach the panel it is read
+        // in.  Lines of the first record are read with panel 0; k_line_records
+        // checks that no later line would be dropped at its own read panel.
+        if (kHWF3 * ALFV + VNU < vft[0]) ok = false;
+        if (ok) {
+          double RECALF = 1. / ALFV;
+          double EPP = (double)lines.epp[i];
+          if (EPP <= -1.001) EPP = fabs(EPP);
+          if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
+          double SP = SUI * (1. + 0. * P.pavp2);
+          if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
+            double SPEAK = SUI * RECALF;
+            if (SPEAK <= P.dptmn) ok = false;  // DPTFAC == 0 on this path
+          }
+          if (ok) {
+            lincnt++;
+            nminus += nmin;
+            nplus += npl;
+            r.vnu = VNU;
+            r.sp = SP;
+            r.recalf = RECALF;
+            r.zetai = ZETA;
+            r.iz = IZ;
+            // first panel p with JMAX1 <= MAX1
+            double WAVDXF = P.dv / kDXF1;
+            double HWDXF = kHWF1 / kDXF1;
+            double ZSLOPE = RECALF * WAVDXF;
+            double BHWDXF = HWDXF / ZSLOPE;
+            double est = ((VNU - vft[0]) / P.dv + BHWDXF + 1.5 - (double)P.max1) / (double)kPanelPts;
+            int p = est > 0. ? (int)est : 0;
+            if (p > P.npanels) p = P.npanels;
+            while (p > 0 && fits_panel(VNU, vft[p - 1], P.dv, BHWDXF, P.max1)) p--;
+            while (p < P.npanels && !fits_panel(VNU, vft[p], P.dv, BHWDXF, P.max1)) p++;
+            r.fpanel = p;  // == npanels: never convolved
+          }
+        }
+      }
+    }
+    o[t] = r;
+  }
+  // block reduction of the counters
+  __shared__ unsigned long long sh[5][32];
+  unsigned long long v[5] = {nlin, lincnt, nminus, nplus, bad};
+  for (int k = 0; k < 5; ++k) {
+    unsigned long long x = v[k];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long s = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[k][w];
+      if (s) atomicAdd(&stats[(blockIdx.y + layer0) * kStatsPerLayer + k], s);
+    }
+  }
+}
+
+// ---- prefix maximum of fpanel over a layer's line range -------------------
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blockmax(const LinePrep* __restrict__ prep, int64_t stride, const int64_t* __restrict__ nlines,
+                                int* __restrict__ blockmax, int nblk_stride) {
+  int layer = blockIdx.y;
+  int64_t n = nlines[layer];
+  int64_t base = (int64_t)blockIdx.x * kScanBlock;
+  int mx = -1;
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x) {
+    int64_t i = base + k;
+    if (i < n) mx = max(mx, prep[layer * stride + i].fpanel);
+  }
+  for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
+  __shared__ int sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = -1;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = max(m, sh[w]);
+    blockmax[layer * nblk_stride + blockIdx.x] = m;
+  }
+}
+
+// exclusive prefix max of the block maxima (one thread per layer; a few
+// thousand blocks at most)
+__global__ void k_scan_blocks(int* __restrict__ blockmax, int nblk_stride, const int64_t* __restrict__ nlines,
+                              int nlayers) {
+  int layer = blockIdx.x * blockDim.x + threadIdx.x;
+  if (layer >= nlayers) return;
+  int64_t n = nlines[layer];
+  int nb = (int)((n + kScanBlock - 1) / kScanBlock);
+  int run = -1;
+  for (int b = 0; b < nb; ++b) {
+    int v = blockmax[layer * nblk_stride + b];
+    blockmax[layer * nblk_stride + b] = run;
+    run = max(run, v);
+  }
+}
+
+// panel of each line = max(exclusive block prefix, inclusive in-block prefix)
+__global__ void k_scan_apply(const LinePrep* __restrict__ prep, int64_t stride, const int64_t* __restrict__ nlines,
+                             const int* __restrict__ blockmax, int nblk_stride, int* __restrict__ qpanel) {
+  int layer = blockIdx.y;
+  int64_t n = nlines[layer];
+  int64_t base = (int64_t)blockIdx.x * kScanBlock;
+  __shared__ int sh[kScanBlock];
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x) {
+    int64_t i = base + k;
+    sh[k] = i < n ? prep[layer * stride + i].fpanel : -1;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // each lane scans 32 entries, then a warp scan of the lane totals
+    int lane = threadIdx.x;
+    int run = -1;
+    for (int k = 0; k < kScanBlock / 32; ++k) {
+      int idx = lane * (kScanBlock / 32) + k;
+      run = max(run, sh[idx]);
+      sh[idx] = run;
+    }
+    int tot = run;
+    for (int off = 1; off < 32; off <<= 1) {
+      int o = __shfl_up_sync(0xffffffffu, tot, off);
+      if (lane >= off) tot = max(tot, o);
+    }
+    int excl = __shfl_up_sync(0xffffffffu, tot, 1);
+    if (lane == 0) excl = -1;
+    excl = max(excl, blockmax[layer * nblk_stride + blockIdx.x]);
+    for (int k = 0; k < kScanBlock / 32; ++k) {
+      int idx = lane * (kScanBlock / 32) + k;
+      sh[idx] = max(sh[idx], excl);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x) {
+    int64_t i = base + k;
+    if (i < n) qpanel[layer * stride + i] = sh[k];
+  }
+}
+
+// ---- CNVFNQ per-line set-up ----------------------------------------------
+__device__ __forceinline__ void interp_coef(const double* tab, int IZM, double ZETDIF, double DEPTHA, double* out) {
+  *out = DEPTHA * (tab[IZM - 1] + ZETDIF * (tab[IZM] - tab[IZM - 1]));
+}
+
+__global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vft_all,
+                               const LinePrep* __restrict__ prep, const int* __restrict__ qpanel, int64_t stride,
+                               GridRec* __restrict__ rec, GridRecD* __restrict__ recd,
+                               const double* __restrict__ vnu_raw, unsigned long long* __restrict__ stats,
+                               double* __restrict__ alfvmax) {
+  int layer = blockIdx.y;
+  const LayerPlan& P = plans[layer + layer0];
+  int64_t n = P.line_hi - P.line_lo + 1;
+  const double* vft = vft_all + P.vft_off;
+  double WAVDXF = P.dv / kDXF1;
+  double HWDXF = kHWF1 / kDXF1;
+  double DVR2 = (kDXF2 / kDXF1) * P.dv;
+  double DVR3 = (kDXF3 / kDXF1) * P.dv;
+  double CONF2 = P.dv / DVR2;
+  double CONF3 = P.dv / DVR3;
+  double amax = 0.;
+  unsigned long long bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const LinePrep lp = prep[layer * stride + t];
+    int q = qpanel[layer * stride + t];
+    GridRec g1, g2, g3;
+    g1.g_lo = g2.g_lo = g3.g_lo = 1;
+    g1.g_hi = g2.g_hi = g3.g_hi = 0;  // empty
+    g1.q = g2.q = g3.q = q;
+    g1.zfl = g2.zfl = g3.zfl = 0.f;
+    g1.zs = g2.zs = g3.zs = 0.f;
+    g1.a0 = g1.a1 = g1.a2 = g2.a0 = g2.a1 = g2.a2 = g3.a0 = g3.a1 = g3.a2 = 0.f;
+    GridRecD d1 = {0, 0, 0, 0, 0}, d2 = d1, d3 = d1;
+    if (lp.fpanel >= 0 && q < P.npanels) {
+      // a line of a later record is read in the panel the previous record
+      // ended in; dropping it there (HWF3*ALFV + VNU < VFT) is not modelled
+      int64_t gi = P.line_lo + t;
+      if (gi >= P.first_rec_end) {
+        int64_t rs = (gi / 250) * 250;  // first line of this line's record
+        int qr = 0;
+        if (rs - 1 >= P.line_lo) qr = max(0, qpanel[layer * stride + (rs - 1 - P.line_lo)]);
+        double alfv = 1. / lp.recalf;
+        if (qr > 0 && qr < P.npanels && kHWF3 * alfv + lp.vnu < vft[qr]) bad++;
+      }
+      double DEPTHA = lp.sp * lp.recalf;
+      int IZM = lp.iz;
+      double ZETDIF = 100. * lp.zetai - (double)(IZM - 1);
+      double STRFA1, STRFA2, STRFA3, STRDA, STRVRA;
+      interp_coef(c_CF1, IZM, ZETDIF, DEPTHA, &STRFA1);
+      interp_coef(c_CF2, IZM, ZETDIF, DEPTHA, &STRFA2);
+      interp_coef(c_CF3, IZM, ZETDIF, DEPTHA, &STRFA3);
+      interp_coef(c_CGAUSS, IZM, ZETDIF, DEPTHA, &STRDA);
+      interp_coef(c_CER, IZM, ZETDIF, DEPTHA, &STRVRA);
+      double ZSLOPE = lp.recalf * WAVDXF;
+      double ZINT = (lp.vnu - vft[q]) / P.dv;
+      double BHWDXF = HWDXF / ZSLOPE;
+      int JMAX1 = (int)(ZINT + BHWDXF + 1.5);
+      int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
+      double RSHFT = 0.5;
+      if (ZINT < 0.0) RSHFT = -RSHFT;
+      int J2SHFT = (int)(ZINT * (1. - CONF2) + RSHFT);
+      int J3SHFT = (int)(ZINT * (1. - CONF3) + RSHFT);
+      int JMIN2 = JMIN1 - J2SHFT;
+      int JMIN3 = JMIN1 - J3SHFT;
+      double ZF1L = ((double)(JMIN1 - 2) - ZINT) * ZSLOPE;
+      double ZF2L = ((double)(JMIN2 - 2) - ZINT * CONF2) * ZSLOPE;
+      double ZF3L = ((double)(JMIN3 - 2) - ZINT * CONF3) * ZSLOPE;
+      // global indices: grid k point J of panel q is kPanel_k * q + J - 1
+      g1.g_lo = kPanelPts * q + JMIN1 - 1;
+      g1.g_hi = kPanelPts * q + JMAX1 - 1;
+      g2.g_lo = kPanelR2 * q + JMIN2 - 1;
+      g2.g_hi = kPanelR2 * q + (JMAX1 - J2SHFT) - 1;
+      g3.g_lo = kPanelR3 * q + JMIN3 - 1;
+      g3.g_hi = kPanelR3 * q + (JMAX1 - J3SHFT) - 1;
+      g1.zfl = (float)ZF1L;
+      g2.zfl = (float)ZF2L;
+      g3.zfl = (float)ZF3L;
+      g1.zs = g2.zs = g3.zs = (float)ZSLOPE;
+      g1.a0 = (float)STRFA1;
+      g1.a1 = (float)STRDA;
+      g1.a2 = (float)STRVRA;
+      g2.a0 = (float)STRFA2;
+      g3.a0 = (float)STRFA3;
+      d1 = {ZF1L, ZSLOPE, STRFA1, STRDA, STRVRA};
+      d2 = {ZF2L, ZSLOPE, STRFA2, 0., 0.};
+      d3 = {ZF3L, ZSLOPE, STRFA3, 0., 0.};
+      amax = fmax(amax, 1. / lp.recalf);
+    }
+    int64_t o = (int64_t)layer * stride * 3;
+    rec[o + t] = g1;
+    rec[o + stride + t] = g2;
+    rec[o + 2 * stride + t] = g3;
+    recd[o + t] = d1;
+    recd[o + stride + t] = d2;
+    recd[o + 2 * stride + t] = d3;
+  }
+  for (int off = 16; off > 0; off >>= 1) amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, off));
+  unsigned long long b = bad;
+  for (int off = 16; off > 0; off >>= 1) b += __shfl_down_sync(0xffffffffu, b, off);
+  if ((threadIdx.x & 31) == 0) {
+    if (amax > 0.) atomicMax((unsigned long long*)&alfvmax[layer + layer0], (unsigned long long)__double_as_longlong(amax));
+    if (b) atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 4], b);
+  }
+}
+
+// ---- candidate line ranges of each panel on each grid ---------------------
+__device__ __forceinline__ int64_t lower_bound_d(const double* a, int64_t lo, int64_t hi, double x) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_panel_ranges(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vnu_raw,
+                               const double* __restrict__ alfvmax, double shiftmax, int64_t* __restrict__ ranges,
+                               int64_t panel_stride) {
+  int layer = blockIdx.y;
+  const LayerPlan& P = plans[layer + layer0];
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.npanels) return;
+  double a = alfvmax[layer + layer0];
+  double dv = P.dv;
+  double s = shiftmax * P.rhorat + 1e-9;
+  // grid 1: output points J = 33..2432 of panel p
+  double r1lo = P.vft0 + (double)(kPanelPts * p + 32) * dv, r1hi = P.vft0 + (double)(kPanelPts * p + 2431) * dv;
+  double reach1 = 4. * a + 3. * dv + s;
+  // grid 2: points J = 5..612 (4 DV)
+  double r2lo = P.vft0 + (double)(kPanelR2 * p + 4) * 4. * dv, r2hi = P.vft0 + (double)(kPanelR2 * p + 611) * 4. * dv;
+  double reach2 = 16. * a + 12. * dv + s;
+  // grid 3: points J = 0..160 (16 DV)
+  double r3lo = P.vft0 + (double)(kPanelR3 * p - 1) * 16. * dv, r3hi = P.vft0 + (double)(kPanelR3 * p + 159) * 16. * dv;
+  double reach3 = 64. * a + 48. * dv + s;
+  int64_t lo = P.line_lo, hi = P.line_hi + 1;
+  int64_t* r = ranges + ((int64_t)layer * panel_stride + p) * 6;
+  r[0] = lower_bound_d(vnu_raw, lo, hi, r1lo - reach1) - P.line_lo;
+  r[1] = lower_bound_d(vnu_raw, lo, hi, r1hi + reach1) - P.line_lo;
+  r[2] = lower_bound_d(vnu_raw, lo, hi, r2lo - reach2) - P.line_lo;
+  r[3] = lower_bound_d(vnu_raw, lo, hi, r2hi + reach2) - P.line_lo;
+  r[4] = lower_bound_d(vnu_raw, lo, hi, r3lo - reach3) - P.line_lo;
+  r[5] = lower_bound_d(vnu_raw, lo, hi, r3hi + reach3) - P.line_lo;
+}
+
+// ---- H2O continuum on the ABSRB grid -----------------------------------------
+// One thread per ABSRB point I (1-based).  The four table coefficients the
+// 4-point interpolation (myxint) needs are rebuilt per point exactly as
+// mt_ckd_h2o_absco builds sh2o_coeff/fh2o_coeff.
+__global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, ContIn cont, double* __restrict__ absrb_all) {
+  const LayerPlan& P = plans[blockIdx.y + layer0];
+  double* ABSRB = absrb_all + P.abs_off;  // ABSRB[I], I = 1..N_ABSRB
+  int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (I > kNABSRB + 7) return;
+  ABSRB[I] = 0.;
+  if (I == 1) ABSRB[0] = 0.;
+  if (I > kNABSRB) return;
+  if (!P.contnm) return;
+  if (!((P.v2 > -20.0) && (P.v1 < 20000.) && ((P.xself > 0.) || (P.xfrgn > 0.)))) return;
+  int ncoeffin = cont.n;
+  const double dvc = (cont.v1 + cont.dv) - cont.v1;
+  // i1, i2 bracket [V1ABS - 2 dvc, V2ABS + 2 dvc] (mt_ckd_h2o_module.f90:106-117)
+  int i = 1;
+  while (i <= ncoeffin && cont.v1 + (double)(i - 1) * cont.dv <= (P.v1abs - 2 * dvc)) i++;
+  int i1 = i - 1;
+  if (i1 == 0) i1 = 1;
+  while (i <= ncoeffin && cont.v1 + (double)(i - 1) * cont.dv < (P.v2abs + 2 * dvc)) i++;
+  int i2 = i;
+  double V1A = cont.v1 + (double)(i1 - 1) * cont.dv;
+  double V2A = cont.v1 + (double)(i2 - 1) * cont.dv;
+  int nptabs = (int)((P.v2abs - P.v1abs) / P.dvabs + 1);
+  double wvn1 = cont.v1, wvnN = cont.v1 + (double)(ncoeffin - 1) * cont.dv;
+  int nbnd_v1c = (int)(2 + (wvn1 - P.v1abs) / P.dvabs + 1.e-5);
+  int ist = nbnd_v1c > 1 ? nbnd_v1c : 1;
+  int nbnd_v2c = (int)(1 + (wvnN - P.v1abs) / P.dvabs + 1.e-5);
+  int lst = nptabs < nbnd_v2c ? nptabs : nbnd_v2c;
+  // myxint(V1A, V2A, dvc, coeff, 1.0, V1ABS, DVABS, out, ist, lst), module ONEPL/ONEMI
+  const double onepl = 1.001, onemi = 0.999;
+  double RECDVA = 1. / dvc;
+  int ILO = (int)((V1A + dvc - P.v1abs) / P.dvabs + 1. + onemi);
+  if (ILO < ist) ILO = ist;
+  int IHI = (int)((V2A - dvc - P.v1abs) / P.dvabs + onemi);
+  if (IHI > lst) IHI = lst;
+  if (I < ILO || I > IHI) return;
+  double xkt = P.tave / kRADCN2;
+  double rho_rat = (P.pave / cont.ref_press) * (cont.ref_temp / P.tave);
+  double VI = P.v1abs + P.dvabs * (double)(I - 1);
+  int J = (int)((VI - V1A) * RECDVA + onepl);
+  double VJ = V1A + dvc * (double)(J - 1);
+  double Pp = RECDVA * (VI - VJ);
+  double C = (3. - 2. * Pp) * Pp * Pp;
+  double B = 0.5 * Pp * (1. - Pp);
+  double B1 = B * (1. - Pp);
+  double B2 = B * Pp;
+  double sh[4], fh[4];
+  for (int k = 0; k < 4; ++k) {
+    int jj = J - 1 + k;       // 1-based index into the coefficient sub-array
+    int ii = i1 + jj - 1;     // 1-based table index
+    if (ii < 1 || ii > ncoeffin) {  // beyond the table: the reference reads outside its array
+      sh[k] = fh[k] = 0.;
+      continue;
+    }
+    double v = cont.self_absco_ref[ii - 1] * pow(cont.ref_temp / P.tave, cont.self_texp[ii - 1]);
+    v = v * P.h2o_fac * rho_rat;
+    double f = cont.for_absco_ref[ii - 1];
+    f = f * (1 - P.h2o_fac) * rho_rat;
+    if (P.jrad != 0) {
+      double xvi = cont.v1 + (double)(ii - 1) * cont.dv, rad = xvi, xviokt = xvi / xkt;
+      if (xviokt <= 0.01) rad = 0.5 * xviokt * xvi;
+      else if (xviokt <= 10.) {
+        double e = exp(-xviokt);
+        rad = xvi * (1 - e) / (1. + e);
+      }
+      v = v * rad;
+      f = f * rad;
+    }
+    sh[k] = v;
+    fh[k] = f;
+  }
+  double self = -sh[0] * B1 + sh[1] * (1. - C + B2) + sh[2] * (C + B1) - sh[3] * B2;
+  double forc = -fh[0] * B1 + fh[1] * (1. - C + B2) + fh[2] * (C + B1) - fh[3] * B2;
+  self = 0. + self * 1.0;
+  forc = 0. + forc * 1.0;
+  double cself = P.wk1 * self * P.xself;
+  double cfor = P.wk1 * forc * P.xfrgn;
+  ABSRB[I] = 0. + cself + cfor;
+}
+
+// ---- far-wing lines: LINF4Q per-line corrections --------------------------
+__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines, F4Prep* __restrict__ out,
+                          int64_t stride, unsigned long long* __restrict__ stats) {
+  const LayerPlan& P = plans[blockIdx.y + layer0];
+  int64_t n = P.f4_hi - P.f4_lo;
+  F4Prep* o = out + (int64_t)blockIdx.y * stride;
+  unsigned long long bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = P.f4_lo + t;
+    F4Prep r;
+    r.pass = 0;
+    r.vnu = r.sp = r.alfa = r.alfd = 0.;
+    r.mol = 0;
+    int iflg = lines.iflg[i];
+    int molf = lines.mol[i];
+    int m = molf % 100;
+    int iso = (molf % 1000) / 100;
+    if (iso == 0) iso = 10;
+    bool ok = iflg >= 0 && m >= 1 && m <= kTIPSNMOL && P.sel[m];
+    if (ok && iso > c_MAXISO[m]) ok = false;
+    if (ok && (iso != 1 || iflg == 1 || iflg == 3)) {
+      bad++;
+      ok = false;
+    }
+    if (ok) {
+      double SUI = (double)lines.sp[i] * P.wk[m];
+      if (SUI != 0. && !(lines.vnu[i] < P.v1l4)) {
+        double alfa = (double)lines.alfa[i];
+        double hwhm = (double)lines.hwhm[i];
+        if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
+        double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
+        double EPP = (double)lines.epp[i];
+        if (VNU == 0.) SUI = 2. * SUI;
+        if (EPP <= -1.001) EPP = fabs(EPP);
+        if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
+        double TMPCOR = pow(P.tratio, (double)lines.tmpalf[i]);
+        double ALFA0I = alfa * TMPCOR;
+        double HWHMSI = hwhm * TMPCOR;
+        r.alfa = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
+        r.alfd = VNU * P.alfd1[m];
+        r.sp = SUI * (1. + 0. * P.pavp2);
+        r.vnu = VNU;
+        r.mol = m;
+        r.pass = 1;
+      }
+    }
+    o[t] = r;
+  }
+  for (int off = 16; off > 0; off >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, off);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&stats[(blockIdx.y + layer0) * kStatsPerLayer + 4], bad);
+}
+
+// ---- LINF4Q record loop with SHRINQ, in parallel pieces -------------------
+// The reference appends the corrected lines of each 250-line record to a
+// buffer; when a record ends with >= 1000 entries the unshrunk tail is shrunk
+// (SHRINQ restarts its grouping at the tail's first line), and the buffer is
+// written out once it holds >= 1000 shrunk lines (clblm_ODLAY_LineF4.f90:959-
+// 1234).  A group ends at line e when the next line lies beyond VLMT, where
+// VLMT is the centre of the first line (at a restart) or of the previous
+// group's last line, plus DVR4/2 (:1516-1647).
+//
+// Pieces: (1) prefix count of the lines that enter the buffer, (2) compaction
+// with the integer image of each centre and of centre + DVR4/2 (positive
+// doubles order like their bit patterns), (3) one warp per layer replays the
+// record loop and finds group ends with ballots, (4) one thread per group
+// forms the group's sums in the reference's order.
+
+__global__ void k_f4_count(const F4Prep* __restrict__ prep, int64_t stride, const LayerPlan* __restrict__ plans,
+                           int layer0, int64_t* __restrict__ blocksum, int nblk) {
+  const int layer = blockIdx.y;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.f4_hi - P.f4_lo;
+  const int64_t base = (int64_t)blockIdx.x * 1024;
+  int c = 0;
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+    int64_t t = base + k;
+    if (t < n) c += prep[(int64_t)layer * stride + t].pass;
+  }
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+  __shared__ int sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += sh[w];
+    blocksum[(int64_t)layer * nblk + blockIdx.x] = tot;
+  }
+}
+
+__global__ void k_f4_blockscan(int64_t* __restrict__ blocksum, int nblk, const LayerPlan* __restrict__ plans,
+                               int layer0, int nlayers, int64_t* __restrict__ ntot) {
+  int layer = blockIdx.x * blockDim.x + threadIdx.x;
+  if (layer >= nlayers) return;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.f4_hi - P.f4_lo;
+  const int nb = (int)((n + 1 + 1023) / 1024);  // blocks covering t = 0..n
+  int64_t run = 0;
+  for (int b = 0; b < nb; ++b) {
+    int64_t v = blocksum[(int64_t)layer * nblk + b];
+    blocksum[(int64_t)layer * nblk + b] = run;
+    run += v;
+  }
+  ntot[layer] = run;
+}
+
+// cidx[t] = passing lines before t (t = 0..n, cidx[n] = total); the passing
+// lines are compacted into vbits / lbits (centre, centre + DVR4/2) and src.
+__global__ void k_f4_compact(const F4Prep* __restrict__ prep, int64_t stride, const LayerPlan* __restrict__ plans,
+                             int layer0, const int64_t* __restrict__ blocksum, int nblk, int64_t* __restrict__ cidx,
+                             long long* __restrict__ vbits, long long* __restrict__ lbits, int64_t* __restrict__ src,
+                             unsigned char* __restrict__ flags, int64_t* __restrict__ cut) {
+  const int layer = blockIdx.y;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.f4_hi - P.f4_lo;
+  const int64_t base = (int64_t)blockIdx.x * 1024;
+  __shared__ int sh[1024];
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+    int64_t t = base + k;
+    sh[k] = t < n ? prep[(int64_t)layer * stride + t].pass : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int lane = threadIdx.x, run = 0;
+    for (int k = 0; k < 32; ++k) {
+      int idx = lane * 32 + k;
+      int v = sh[idx];
+      sh[idx] = run;  // exclusive within the lane's 32
+      run += v;
+    }
+    int tot = run;
+    for (int off = 1; off < 32; off <<= 1) {
+      int o = __shfl_up_sync(0xffffffffu, tot, off);
+      if (lane >= off) tot += o;
+    }
+    int excl = tot - run;
+    for (int k = 0; k < 32; ++k) sh[lane * 32 + k] += excl;
+  }
+  __syncthreads();
+  const int64_t off0 = blocksum[(int64_t)layer * nblk + blockIdx.x];
+  const double half = P.dvr4 / 2.;
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+    int64_t t = base + k;
+    if (t > n) continue;
+    int64_t c = off0 + sh[k];
+    cidx[(int64_t)layer * (stride + 1) + t] = c;
+    if (t == n) continue;
+    const F4Prep& r = prep[(int64_t)layer * stride + t];
+    if (r.pass) {
+      vbits[(int64_t)layer * stride + c] = __double_as_longlong(r.vnu);
+      lbits[(int64_t)layer * stride + c] = __double_as_longlong(r.vnu + half);
+      src[(int64_t)layer * stride + c] = t;
+      // SHRINQ zeroes SP < 1e-35; a group emits a non-CO2 / CO2 line when
+      // its strength sum of that kind is positive
+      bool strong = !(r.sp < 1.0e-35);
+      flags[(int64_t)layer * stride + c] = (unsigned char)((strong && r.mol != 2 ? 1 : 0) | (strong && r.mol == 2 ? 2 : 0));
+      if (r.vnu > P.v2l4) atomicMin((unsigned long long*)&cut[layer], (unsigned long long)c);
+    }
+  }
+}
+
+// Group list of one layer: one warp replays the record loop.  Centres are
+// compared through their bit patterns (positive centres order like their
+// binary64 images; a non-positive centre is rejected on the host).  Each
+// group records its stream range and how many lines it emits (a non-CO2 line
+// when a non-CO2 member has SP >= 1e-35, a CO2 line likewise), which is what
+// the buffer arithmetic of the record loop counts.
+__global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total,
+                          int64_t stride, const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
+                          const long long* __restrict__ lbits, const unsigned char* __restrict__ flags,
+                          const int64_t* __restrict__ ntot, const int64_t* __restrict__ cut, int4* __restrict__ groups,
+                          int64_t* __restrict__ ngroups) {
+  const int layer = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (layer >= nlayers) return;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.f4_hi - P.f4_lo;
+  const int64_t* ci = cidx + (int64_t)layer * (stride + 1);
+  const long long* V = vbits + (int64_t)layer * stride;
+  const long long* Lm = lbits + (int64_t)layer * stride;
+  const unsigned char* F = flags + (int64_t)layer * stride;
+  int4* G = groups + (int64_t)layer * stride;
+  const int64_t total = ntot[layer];
+  const unsigned long long cutv = (unsigned long long)cut[layer];
+  const bool has_cut = cutv < (unsigned long long)total;
+  const int64_t send = has_cut ? (int64_t)cutv + 1 : total;  // stream ends after the first line above V2L4
+  const int64_t R = 250;
+  const int64_t nrec_total = (nlines_total + R - 1) / R;
+  int64_t rec = P.f4_lo / R;
+  int64_t IJ = 0, ILO = 1;  // 1-based buffer positions, as in LINF4Q
+  int64_t u0 = 0;           // stream index of the first unshrunk line
+  int64_t ng = 0, slot = 0;
+  int status = 0;
+  bool IEOF = false;
+  for (;;) {
+    if (rec >= nrec_total) {
+      IEOF = true;
+    } else {
+      int64_t tb = rec * R - P.f4_lo, te = tb + R;
+      rec++;
+      int64_t cb = ci[tb < 0 ? 0 : (tb > n ? n : tb)];
+      int64_t ce;
+      if (te <= n) ce = ci[te];
+      else if (rec * R >= nlines_total || (has_cut && send <= ci[n])) ce = ci[n];
+      else {  // lines beyond the prepared range would be needed
+        status = 2;
+        break;
+      }
+      if (cb < send && ce >= send) {
+        ce = send;
+        IEOF = true;
+      }
+      IJ += ce - cb;
+      if (IJ < 1000 && !IEOF) continue;
+    }
+    // SHRINQ over the unshrunk stream [u0, u1)
+    const int64_t u1 = u0 + (IJ - ILO + 1);
+    int64_t nemit = 0;
+    if (u1 > u0) {
+      int64_t cur = u0;
+      long long vlmt = Lm[u0];
+      int64_t base = cur;
+      long long vnext = 0, vme = 0;
+      unsigned char fme = 0;
+      bool loaded = false;
+      unsigned acc_nc = 0, acc_c2 = 0;
+      while (true) {
+        const int64_t e = base + lane;
+        if (!loaded) {
+          vme = e < u1 ? Lm[e] : 0;
+          vnext = (e + 1 < u1) ? V[e + 1] : 0;
+          fme = e < u1 ? F[e] : 0;
+          loaded = true;
+        }
+        bool inrange = e >= cur && e < u1;
+        bool pred = inrange && (e == u1 - 1 || vnext > vlmt);
+        unsigned m = __ballot_sync(0xffffffffu, pred);
+        int last_lane = m ? __ffs(m) - 1 : 31;
+        bool member = inrange && (lane <= last_lane);
+        acc_nc |= __ballot_sync(0xffffffffu, member && (fme & 1));
+        acc_c2 |= __ballot_sync(0xffffffffu, member && (fme & 2));
+        if (m == 0) {
+          base += 32;
+          loaded = false;
+          continue;
+        }
+        const int64_t eend = base + last_lane;
+        int k = (acc_nc ? 1 : 0) + (acc_c2 ? 1 : 0);
+        if (lane == 0 && ng < stride) G[ng] = make_int4((int)cur, (int)eend, (int)slot, (acc_nc ? 1 : 0) | (acc_c2 ? 2 : 0));
+        ng++;
+        slot += k;
+        nemit += k;
+        acc_nc = acc_c2 = 0;
+        if (eend == u1 - 1) break;
+        vlmt = __shfl_sync(0xffffffffu, vme, last_lane);
+        cur = eend + 1;
+        if (cur >= base + 32) {
+          base = cur;
+          loaded = false;
+        }
+      }
+    }
+    u0 = u1;
+    const int64_t J = ILO - 1 + nemit;
+    ILO = J + 1;
+    IJ = J;
+    if (J < 1000 && !IEOF) continue;
+    IJ = 0;
+    ILO = 1;
+    if (IEOF) break;
+  }
+  if (lane == 0) {
+    ngroups[2 * (layer + layer0)] = status ? -status : ng;
+    ngroups[2 * (layer + layer0) + 1] = slot;
+  }
+}
+
+// Sums of each group in the reference's order (SHRINQ :1563-1637): non-CO2
+// members into one pseudo-line, CO2 members into another, written to the
+// group's output slots.
+__global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, const F4Prep* __restrict__ prep,
+                              int64_t stride, const int64_t* __restrict__ src, const int4* __restrict__ groups,
+                              const int64_t* __restrict__ ngroups, ShrunkLine* __restrict__ out) {
+  const int layer = blockIdx.y;
+  const int64_t ng = ngroups[2 * (layer + layer0)];
+  const int4* G = groups + (int64_t)layer * stride;
+  const int64_t* S = src + (int64_t)layer * stride;
+  const F4Prep* pr = prep + (int64_t)layer * stride;
+  ShrunkLine* O = out + (int64_t)layer * stride;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
+    const int4 gr = G[g];
+    double SUMAL = 0., SUMAD = 0., SUMS = 0., SUMV = 0., SUMC = 0.;
+    double SUMAL2 = 0., SUMAD2 = 0., SUMS2 = 0., SUMV2 = 0., SUMC2 = 0.;
+    for (int u = gr.x; u <= gr.y; ++u) {
+      const F4Prep& r = pr[S[u]];
+      double sp = r.sp < 1.0e-35 ? 0.0 : r.sp;
+      if (r.mol != 2) {
+        SUMV = SUMV + r.vnu * sp;
+        SUMS = SUMS + sp;
+        SUMAL = SUMAL + sp * r.alfa;
+        SUMAD = SUMAD + sp * r.alfd;
+        SUMC = SUMC + 0.;
+      } else {
+        SUMV2 = SUMV2 + r.vnu * sp;
+        SUMS2 = SUMS2 + sp;
+        SUMAL2 = SUMAL2 + sp * r.alfa;
+        SUMAD2 = SUMAD2 + sp * r.alfd;
+        SUMC2 = SUMC2 + 0.;
+      }
+    }
+    int slot = gr.z;
+    if (SUMS > 0.) {
+      ShrunkLine L;
+      L.sp = SUMS;
+      L.alfa = SUMAL / SUMS;
+      L.alfd = SUMAD / SUMS;
+      L.vnu = SUMV / SUMS;
+      L.spp = SUMC;
+      L.mol = 0;
+      L.pad = 0;
+      O[slot++] = L;
+    }
+    if (SUMS2 > 0.) {
+      ShrunkLine L;
+      L.sp = SUMS2;
+      L.alfa = SUMAL2 / SUMS2;
+      L.alfd = SUMAD2 / SUMS2;
+      L.vnu = SUMV2 / SUMS2;
+      L.spp = SUMC2;
+      L.mol = 2;
+      L.pad = 0;
+      O[slot++] = L;
+    }
+  }
+}
+
+// CNVF4Q per-line set-up of each shrunk line (clblm_ODLAY_LineF4.f90:320-385):
+// Voigt width, the Lorentz/Voigt strengths and the point range JMIN..JMAX on
+// the global far-wing grid V1R4 + (J-1)*DVR4.  Lines at 0 < vnu <= 25 cm-1
+// also get a Van Vleck-Weisskopf mirror record at -vnu (:480-487), appended
+// after the direct records.
+__device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, F4Rec* r, F4RecD* d) {
+  const double ZSQBND = 64. * 64.;
+  const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
+  const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
+  const double RECPI = 1. / (2. * asin(1.));
+  double ALFADI = L.alfd, ALFALI = L.alfa;
+  double ZETAI = ALFALI / (ALFALI + ALFADI);
+  int IZ = (int)(100. * ZETAI + kONEPL);
+  double ZETDIF = 100. * ZETAI - (double)(IZ - 1);
+  double ALFAVI = (c_AVRAT[IZ - 1] + ZETDIF * (c_AVRAT[IZ] - c_AVRAT[IZ - 1])) * (ALFALI + ALFADI);
+  double RALFVI = 1. / ALFAVI;
+  double SIL = L.sp * RECPI * ALFALI;
+  double SIV = (ALFALI * RALFVI) * L.sp * RECPI * RALFVI;
+  double XNUI = VNUI - P.v1r4;
+  int JMIN = (int)((XNUI - P.bound4) / P.dvr4 + 2.);
+  if (JMIN < 1) JMIN = 1;
+  int JMAX = (int)((XNUI + P.bound4) / P.dvr4 + 1.);
+  if (JMAX > (int)P.nptr4) JMAX = (int)P.nptr4;
+  double ALFLI2 = ALFALI * ALFALI;
+  double ALFVI2 = ALFAVI * ALFAVI;
+  double BNDSQ = P.bound4 * P.bound4;
+  double F4BND = SIL / (ALFLI2 + BNDSQ);
+  r->jmin = JMIN;
+  r->jmax = JMAX;
+  // FP32 distances are taken from the grid point nearest the line centre, so
+  // that points near the centre do not lose digits to cancellation
+  r->mc = (int)floor(XNUI / P.dvr4 + 0.5);
+  r->co2 = (L.mol == 2);
+  r->x0 = (float)((double)r->mc * P.dvr4 - XNUI);
+  r->sil = (float)SIL;
+  r->sa3 = (float)(SIV * A3);
+  r->sb3 = (float)(SIV * B3);
+  r->fbnd = (float)F4BND;
+  r->al2 = (float)ALFLI2;
+  r->ralv2 = (float)(1. / ALFVI2);
+  r->rbnd2 = (float)(1. / BNDSQ);
+  d->xnui = XNUI;
+  d->sil = SIL;
+  d->siv = SIV;
+  d->fbnd = F4BND;
+  d->al2 = ALFLI2;
+  d->alv2 = ALFVI2;
+}
+
+__global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
+                              int64_t stride, const int64_t* __restrict__ nsh, F4Rec* __restrict__ rec,
+                              F4RecD* __restrict__ recd, int64_t rstride, int64_t* __restrict__ nrec,
+                              int64_t* __restrict__ nmirror) {
+  const int layer = blockIdx.y;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = nsh[2 * (layer + layer0)] < 0 ? 0 : nsh[2 * (layer + layer0) + 1];
+  const ShrunkLine* S = sh + (int64_t)layer * stride;
+  F4Rec* R = rec + (int64_t)layer * rstride;
+  F4RecD* D = recd + (int64_t)layer * rstride;
+  const double VNULST = P.v1r4 + P.dvr4 * (double)(P.nptr4 - 1) + P.bound4;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const ShrunkLine L = S[i];
+    F4Rec r;
+    F4RecD d;
+    f4_record(P, L, L.vnu, &r, &d);
+    // lines beyond the last point's reach, or without strength, add nothing
+    if (L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) {
+      r.jmin = 1 << 30;
+      r.jmax = -1;
+    }
+    R[i] = r;
+    D[i] = d;
+  }
+  // mirror lines: one thread per layer (at most the lines below 25 cm-1)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int64_t nm = 0;
+    for (int64_t i = 0; i < n && S[i].vnu <= 25. + 1.; ++i) {
+      const ShrunkLine L = S[i];
+      if (!(L.vnu > 0. && L.vnu <= 25.) || L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) continue;
+      F4Rec r;
+      F4RecD d;
+      f4_record(P, L, -L.vnu, &r, &d);
+      if (r.jmax >= r.jmin && n + nm < rstride) {
+        R[n + nm] = r;
+        D[n + nm] = d;
+        nm++;
+      }
+    }
+    nmirror[layer + layer0] = nm;
+    nrec[layer + layer0] = n;
+  }
+}
+
+// Per layer (one 1024-thread block): running max of jmax from the left and
+// running min of jmin from the right over the direct records, so that the
+// records overlapping a point form the contiguous index range found by two
+// binary searches.
+__global__ void k_f4_bounds(const F4Rec* __restrict__ rec, int64_t rstride, const int64_t* __restrict__ nrec,
+                            int layer0, int* __restrict__ pmax, int* __restrict__ smin) {
+  const int layer = blockIdx.x;
+  const int64_t n = nrec[layer + layer0];
+  const F4Rec* R = rec + (int64_t)layer * rstride;
+  int* pm = pmax + (int64_t)layer * rstride;
+  int* sm = smin + (int64_t)layer * rstride;
+  const int T = blockDim.x;
+  const int64_t chunk = (n + T - 1) / T;
+  const int64_t b = threadIdx.x * chunk, e = min(n, b + chunk);
+  __shared__ int shmax[1024], shmin[1024];
+  int mx = -1, mn = 1 << 30;
+  for (int64_t i = b; i < e; ++i) mx = max(mx, R[i].jmax);
+  for (int64_t i = b; i < e; ++i) mn = min(mn, R[i].jmin);
+  shmax[threadIdx.x] = mx;
+  shmin[threadIdx.x] = mn;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = -1;
+    for (int t = 0; t < T; ++t) {
+      int v = shmax[t];
+      shmax[t] = run;  // exclusive prefix max
+      run = max(run, v);
+    }
+    run = 1 << 30;
+    for (int t = T - 1; t >= 0; --t) {
+      int v = shmin[t];
+      shmin[t] = run;  // exclusive suffix min
+      run = min(run, v);
+    }
+  }
+  __syncthreads();
+  int run = shmax[threadIdx.x];
+  for (int64_t i = b; i < e; ++i) {
+    run = max(run, R[i].jmax);
+    pm[i] = run;
+  }
+  run = shmin[threadIdx.x];
+  for (int64_t i = e - 1; i >= b; --i) {
+    run = min(run, R[i].jmin);
+    sm[i] = run;
+  }
+}
+
+}  // namespace clblm

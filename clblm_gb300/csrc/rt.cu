@@ -1,0 +1,348 @@
+// rt.cu -- nadir upwelling radiance: one kernel launch per layer of the
+// upward merge of mode2_lookDn_mergeUp (clblm_noScattRT.f90:1340-1466).
+//
+// Per output point of the layer's merge grid:
+//   TxA = exp(-tau_A), TxB = exp(-tau_B)  with tau_A, tau_B the reference-path
+//     OD scaled to the viewing / downwelling paths (airmass scaling,
+//     layerMerge_mode2 :1627-1733),
+//   EmUp, EmDn = layerEmis(Ttop, Tbot, ...), layerEmis(Tbot, Ttop, ...)
+//     (clblm_EMLAY.f90:104-178, linear-in-tau weight rlin :187-223),
+//   R   <- EmUp + TxA * (R + EmDn * refl),    refl <- TxA * TxB * refl  (:1782-1794).
+// Spectra on a coarser grid are brought to the finest one with the
+// reference's interpSpectrum rules (clblm_Spectrum.f90:326-620), evaluated
+// per output point instead of materialising the interpolated arrays.
+#include <cuda_runtime.h>
+
+#include "clblm_common.cuh"
+#include "clblm_kernels.cuh"
+#include "clblm_panel.cuh"
+#include "clblm_rt.cuh"
+
+namespace clblm {
+
+// 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365)
+__constant__ double c_IA1[203], c_IA2[203], c_IA3[203], c_IA4[203];
+
+// Stencil of output point I (1-based) of grid (V1, dvout, nout) on the input
+// grid (V1, dvin, nin): up to four input indices and weights.
+struct Stencil {
+  int64_t i[4];
+  double w[4];
+  int n;
+};
+
+__device__ Stencil interp_stencil(const InterpSpec& s, int64_t I) {
+  Stencil st;
+  st.n = 0;
+  if (s.kind == 0) {  // same grid
+    st.i[0] = I;
+    st.w[0] = 1.;
+    st.n = 1;
+    return st;
+  }
+  if (s.itype == 0) {  // aligned copy (ratio 1 with a different length, or 2)
+    st.i[0] = I * s.nint_ratio - (s.nint_ratio - 1);
+    st.w[0] = 1.;
+    st.n = 1;
+    return st;
+  }
+  if (s.itype > 0) {  // fixed ratio n/(n+1) or (n+1)/n
+    int64_t g = (I - 1) / s.len_out;
+    int NL = (int)((I - 1) % s.len_out) + 1;
+    if (NL == 1) {
+      st.i[0] = 1 + g * s.len_in;
+      st.w[0] = 1.;
+      st.n = 1;
+      return st;
+    }
+    int64_t iIn = NL - s.len_in + (g + 1) * (int64_t)s.len_in;
+    if (s.dvin > s.dvout) iIn -= 1;
+    st.i[0] = iIn - 1;
+    st.i[1] = iIn;
+    st.i[2] = iIn + 1;
+    st.i[3] = iIn + 2;
+    st.w[0] = s.b1[NL];
+    st.w[1] = s.b2[NL];
+    st.w[2] = s.b3[NL];
+    st.w[3] = s.b4[NL];
+    st.n = 4;
+    return st;
+  }
+  // general ratio: (iIn, IP) replayed per output point by k_interp_map
+  int2 mp = s.map[I - 1];
+  int64_t iIn = mp.x;
+  int IP = mp.y;
+  st.i[0] = iIn - 1;
+  st.i[1] = iIn;
+  st.i[2] = iIn + 1;
+  st.i[3] = iIn + 2;
+  st.w[0] = c_IA1[IP];
+  st.w[1] = c_IA2[IP];
+  st.w[2] = c_IA3[IP];
+  st.w[3] = c_IA4[IP];
+  st.n = 4;
+  return st;
+}
+
+// The general-ratio branch of interpSpectrum (clblm_Spectrum.f90:528-565)
+// steps the phase P by DVout/DVin with a carry into iIn and restarts it from
+// the exact wavenumber every 2400 output points.  One thread per such block
+// replays the steps, so that the table index IP at grid coincidences (P just
+// below 1 or just past the carry) is the reference's.
+__global__ void k_interp_map(InterpSpec s, const int64_t* __restrict__ blk_j1, const double* __restrict__ blk_vo,
+                             int nblk, int64_t nout, int2* __restrict__ map) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblk) return;
+  const double Vo = blk_vo[b];
+  int64_t iIn = (int64_t)((Vo - s.v1) / s.dvin + 1.00001);
+  double Vi = s.v1 + (double)(iIn - 1) * s.dvin;
+  double P = (Vo - Vi) / s.dvin;
+  const int64_t J1 = blk_j1[b];
+  const int64_t J2 = min(nout, J1 + 2400 - 1);
+  for (int64_t J = J1; J <= J2; ++J) {
+    int IP = (int)(P * 201. + 1.00001);
+    map[J - 1] = make_int2((int)iIn, IP < 0 ? 0 : (IP > 202 ? 202 : IP));
+    P = P + s.ratio;
+    if (P >= 1.0) {
+      iIn = (int64_t)((double)iIn + P);
+      P = P - (double)((int64_t)P);
+    }
+  }
+}
+
+// value of spInExt(i) (1-based, extended by two points each side)
+template <typename F>
+__device__ __forceinline__ double ext_at(F f, int64_t n, int64_t i) {
+  if (i >= 1 && i <= n) return f(i);
+  if (i == 0 || i == -1) return 2.0 * f(1) - f(2);
+  if (i == n + 1 || i == n + 2) return 2.0 * f(n) - f(n - 1);
+  return 0.;
+}
+
+__device__ __forceinline__ double planck_d(double V, double XKT) {
+  if (XKT <= 1.e-6) return 0.;
+  double cv3 = kRADCN1 * V * V * V;
+  double evt = exp(V / XKT);
+  return cv3 / (evt - 1.);
+}
+
+__device__ __forceinline__ float planck_f(float x /* v/kT */, float cv3) { return cv3 / expm1f(x); }
+
+// rlin's weight with the small-tau branch extended by the series (mixed)
+__device__ __forceinline__ float hlf_f(float od) {
+  if (od < 0.1f) {
+    float o2 = od * od;
+    return 0.5f + od * (-1.f / 12.f + o2 * (1.f / 720.f - o2 * (1.f / 30240.f)));
+  }
+  if (od > 20.f) return 1.f / od;
+  return 1.f / od - 1.f / expm1f(od);
+}
+
+__device__ __forceinline__ double hlf_d(double od) {
+  const double dbAvg2dtau = -1. / 12;
+  if (od < 1.e-03) return .5 + od * dbAvg2dtau;
+  if (od > 20.) return 1. / od;
+  double tex = exp(od);
+  return 1. / (od)-1. / (tex - 1.);
+}
+
+// layer terms at OD-grid point i: TxA, TxB, EmUp, EmDn
+template <bool Plain>
+__device__ __forceinline__ void layer_terms(const RtLayerArgs& a, int64_t i, double out[4]) {
+  double od;
+  if constexpr (Plain) od = reinterpret_cast<const double*>(a.od)[i - 1];
+  else od = (double)reinterpret_cast<const float*>(a.od)[i - 1];
+  double v = a.v1 + (double)(i - 1) * a.dv_od;
+  if constexpr (Plain) {
+    double odA = od * a.scal_up;
+    odA = odA * 1.0;
+    double odB = od * a.scal_dn;
+    odB = odB * 1.0;
+    double TA = exp(-odA), TB = exp(-odB);
+    double XKTA_up = a.ttop / kRADCN2, XKTA_dn = a.tbot / kRADCN2, XKT = a.tave / kRADCN2;
+    double XKTB_up = a.tbot / kRADCN2, XKTB_dn = a.ttop / kRADCN2;
+    double EU, ED;
+    {  // down: Ta = Tbot, Tb = Ttop over path B
+      double abso = 1 - TB;
+      double hlf = a.lin_in_tau ? hlf_d(odB) : 0.;
+      if (a.lin_in_tau == 0) ED = abso * planck_d(v, XKT);
+      else if (a.lin_in_tau == 1) {
+        double bba = planck_d(v, XKTA_dn), bb = planck_d(v, XKT);
+        ED = abso * (bba + 2 * (bb - bba) * hlf);
+      } else {
+        double bba = planck_d(v, XKTA_dn), bbb = planck_d(v, XKTB_dn);
+        ED = abso * (bba + (bbb - bba) * hlf);
+      }
+    }
+    if (a.lin_in_tau == 0) EU = ED;
+    else {  // up: Ta = Ttop, Tb = Tbot over path A
+      double abso = 1 - TA;
+      double hlf = hlf_d(odA);
+      if (a.lin_in_tau == 1) {
+        double bba = planck_d(v, XKTA_up), bb = planck_d(v, XKT);
+        EU = abso * (bba + 2 * (bb - bba) * hlf);
+      } else {
+        double bba = planck_d(v, XKTA_up), bbb = planck_d(v, XKTB_up);
+        EU = abso * (bba + (bbb - bba) * hlf);
+      }
+    }
+    out[0] = TA;
+    out[1] = TB;
+    out[2] = EU;
+    out[3] = ED;
+  } else {
+    float odf = (float)od;
+    float odA = odf * (float)a.scal_up, odB = odf * (float)a.scal_dn;
+    float TA = expf(-odA), TB = expf(-odB);
+    float aA = -expm1f(-odA), aB = -expm1f(-odB);
+    float fi = (float)(i - 1);
+    float vf = fmaf(fi, a.vf1, a.vf0);
+    float cv3 = (float)kRADCN1 * vf * vf * vf;
+    float Bt = planck_f(fmaf(fi, a.xt1, a.xt0), cv3);
+    float Bb = planck_f(fmaf(fi, a.xb1, a.xb0), cv3);
+    float Ba = planck_f(fmaf(fi, a.xa1, a.xa0), cv3);
+    float EU, ED;
+    if (a.lin_in_tau == 0) {
+      ED = aB * Ba;
+      EU = ED;
+    } else if (a.lin_in_tau == 1) {
+      ED = aB * (Bb + 2.f * (Ba - Bb) * hlf_f(odB));
+      EU = aA * (Bt + 2.f * (Ba - Bt) * hlf_f(odA));
+    } else {
+      ED = aB * (Bb + (Bt - Bb) * hlf_f(odB));
+      EU = aA * (Bt + (Bb - Bt) * hlf_f(odA));
+    }
+    out[0] = TA;
+    out[1] = TB;
+    out[2] = EU;
+    out[3] = ED;
+  }
+}
+
+template <bool Plain>
+__global__ void k_rt_layer(RtLayerArgs a) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (I > a.n_out) return;
+  // merged radiance and reflectance at I
+  Real R = 0, F = 0;
+  {
+    Stencil st = interp_stencil(a.mr, I);
+    for (int k = 0; k < st.n; ++k) {
+      double r, f;
+      if (a.first) {
+        auto sr = [&](int64_t j) {
+          if constexpr (Plain) {
+            double v = a.v1 + (double)(j - 1) * a.mr.dvin;
+            return planck_d(v, a.tskin / kRADCN2) * a.emis;
+          } else {
+            float fj = (float)(j - 1);
+            float vf = fmaf(fj, (float)a.mr.dvin, (float)a.v1);
+            return (double)(planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * (float)a.emis);
+          }
+        };
+        auto sf = [&](int64_t j) { return 1.0 - a.emis; };
+        r = ext_at(sr, a.mr.nin, st.i[k]);
+        f = ext_at(sf, a.mr.nin, st.i[k]);
+      } else {
+        const Real* rin = reinterpret_cast<const Real*>(a.rad_in);
+        const Real* fin = reinterpret_cast<const Real*>(a.refl_in);
+        auto gr = [&](int64_t j) { return (double)rin[j - 1]; };
+        auto gf = [&](int64_t j) { return (double)fin[j - 1]; };
+        r = ext_at(gr, a.mr.nin, st.i[k]);
+        f = ext_at(gf, a.mr.nin, st.i[k]);
+      }
+      if (st.n == 1) {
+        R = (Real)r;
+        F = (Real)f;
+      } else {
+        R += (Real)st.w[k] * (Real)r;
+        F += (Real)st.w[k] * (Real)f;
+      }
+    }
+  }
+  double L[4];
+  {
+    Stencil st = interp_stencil(a.ly, I);
+    if (st.n == 1) {
+      int64_t j = st.i[0];
+      if (j >= 1 && j <= a.n_od) layer_terms<Plain>(a, j, L);
+      else {
+        double lo[4], hi[4];
+        int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
+        layer_terms<Plain>(a, jl, lo);
+        layer_terms<Plain>(a, jm, hi);
+        for (int c = 0; c < 4; ++c) L[c] = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2) ? 2.0 * lo[c] - hi[c] : 0.;
+      }
+    } else {
+      for (int c = 0; c < 4; ++c) L[c] = 0.;
+      for (int k = 0; k < 4; ++k) {
+        int64_t j = st.i[k];
+        double t[4];
+        if (j >= 1 && j <= a.n_od) layer_terms<Plain>(a, j, t);
+        else {
+          double lo[4], hi[4];
+          int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
+          layer_terms<Plain>(a, jl, lo);
+          layer_terms<Plain>(a, jm, hi);
+          for (int c = 0; c < 4; ++c)
+            t[c] = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2) ? 2.0 * lo[c] - hi[c] : 0.;
+        }
+        for (int c = 0; c < 4; ++c) L[c] += st.w[k] * t[c];
+      }
+    }
+  }
+  double TA = L[0], TB = L[1], EU = L[2], ED = L[3];
+  Real* rout = reinterpret_cast<Real*>(a.rad_out);
+  Real* fout = reinterpret_cast<Real*>(a.refl_out);
+  if constexpr (Plain) {
+    rout[I - 1] = EU + TA * (R + ED * F);
+    fout[I - 1] = TA * TB * F;
+  } else {
+    float r = (float)EU + (float)TA * ((float)R + (float)ED * (float)F);
+    rout[I - 1] = r;
+    fout[I - 1] = (float)TA * (float)TB * (float)F;
+  }
+}
+
+template __global__ void k_rt_layer<false>(RtLayerArgs);
+template __global__ void k_rt_layer<true>(RtLayerArgs);
+
+// DVout interpolation of a layer OD (ODLAY_nonStruct :582-598) and the
+// conversion of the device OD to binary64.
+template <bool Plain>
+__global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_out, double* out) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (I > n_out) return;
+  const Real* x = reinterpret_cast<const Real*>(od);
+  auto g = [&](int64_t j) { return (double)x[j - 1]; };
+  Stencil st = interp_stencil(s, I);
+  double v = 0.;
+  if (st.n == 1) v = ext_at(g, n_in, st.i[0]);
+  else
+    for (int k = 0; k < 4; ++k) v += st.w[k] * ext_at(g, n_in, st.i[k]);
+  out[I - 1] = v;
+}
+
+template __global__ void k_od_out<false>(const void*, int64_t, InterpSpec, int64_t, double*);
+template __global__ void k_od_out<true>(const void*, int64_t, InterpSpec, int64_t, double*);
+
+void rt_upload_interp_coef(cudaStream_t st) {
+  double a1[203], a2[203], a3[203], a4[203];
+  const double XNUMCF = 201.;
+  for (int IP = 0; IP <= 202; ++IP) {
+    double P = ((double)IP - 1.0) / (XNUMCF - 1.0);
+    double PP = P * P;
+    a1[IP] = -P / 2.0 * ((1 - P) * (1 - P));
+    a2[IP] = 1.0 - PP * (3.0 - 2.0 * P) + PP / 2.0 * (1.0 - P);
+    a3[IP] = PP * (3.0 - 2.0 * P) + P / 2.0 * ((1.0 - P) * (1.0 - P));
+    a4[IP] = -PP / 2 * (1.0 - P);
+  }
+  cudaMemcpyToSymbolAsync(c_IA1, a1, sizeof a1, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c_IA2, a2, sizeof a2, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c_IA3, a3, sizeof a3, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c_IA4, a4, sizeof a4, 0, cudaMemcpyHostToDevice, st);
+}
+
+}  // namespace clblm

@@ -1,0 +1,1370 @@
+// runtime.cu -- host side of the C-ABI (include/clblm_gb300.h): handles,
+// per-layer planning and the launch pipeline of the layer optical depth and
+// the nadir radiance.
+//
+// Planning restates, in FP64 on the host, the scalar set-up the reference
+// performs per layer before its loops (ODLAY_nonStruct clblm_ODLAY.f90:343-467,
+// OPDPTH :849-931, HIRACQ :1197-1345, the panel sequence of panelOut
+// :2349-2360 and :2496, the record logic of RDLIN :2571-2798) so that the
+// device kernels see the same panel origins, index limits and line ranges.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/clblm_gb300.h"
+#include "clblm_common.cuh"
+#include "clblm_kernels.cuh"
+#include "clblm_panel.cuh"
+#include "clblm_ref_tables.h"
+#include "clblm_rt.cuh"
+
+using namespace clblm;
+
+namespace {
+
+thread_local std::string g_create_err;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = n + n / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+}  // namespace
+
+struct clblm_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t nlines = 0;
+  DevBuf lines[9];
+  std::vector<double> h_vnu;
+  std::vector<int32_t> h_iflg, h_mol;
+  double shiftmax = 0.;
+  bool has_cont = false;
+  DevBuf cont_self, cont_for, cont_texp;
+  ContIn cont{};
+  DevBuf tabs;  // shape tables
+  ShapeTabs shape{};
+  bool first_pass_jrad = true;
+  int jrad = 0;
+  // workspace
+  DevBuf plans, vft, prep, qpanel, rec, recd, ranges, od, r4, absrb, stats, alfvmax, blockmax, nlines_d;
+  DevBuf f4prep, f4sh, f4nout, f4rec, f4recd, f4nrec, f4nmir, f4pm, f4sm, err;
+  DevBuf pblk, bv1, bn, bm0, bfac;
+  DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp;
+  DevBuf rt[4], outbuf, imap[2];
+  std::string errmsg;
+  clblm_od_stats_t last{};
+  int64_t launches = 0;  // kernels launched by the current call
+};
+
+namespace {
+
+int set_err(clblm_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->errmsg = buf;
+  else g_create_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(h, x)                                                                            \
+  do {                                                                                            \
+    cudaError_t e_ = (x);                                                                         \
+    if (e_ != cudaSuccess)                                                                        \
+      return set_err(h, e_ == cudaErrorMemoryAllocation ? CLBLM_ERR_OOM : CLBLM_ERR_CUDA, "%s: %s", \
+                     #x, cudaGetErrorString(e_));                                                 \
+  } while (0)
+
+// ---- constants (src/common/clblm_ConstParam.f90) ----
+const double kBOLTZ = 1.3806503E-16, kCLIGHT = 2.99792458E+10, kAVOGAD = 6.02214199E+23;
+const double kPI_C = 3.1415926535898;
+const int kMAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
+
+double radfn_h(double VI, double XKT) {  // RADFN, clblm_ODLAY_CommonSub.f90:293-323
+  double XVI = VI;
+  if (XKT > 0.0) {
+    double XVIOKT = XVI / XKT;
+    if (XVIOKT <= 0.01) return 0.5 * XVIOKT * XVI;
+    if (XVIOKT <= 10.0) {
+      double E = std::exp(-XVIOKT);
+      return XVI * (1. - E) / (1. + E);
+    }
+  }
+  return XVI;
+}
+
+// 3- or 4-point Lagrange interpolation of the TIPS table (AtoB,
+// clblm_ODLAY_TIPS.f90:5451-5546); identical divisors never occur in Tdat.
+double tips_interp(double T, const double* Tg, const double* Q, int npt) {
+  for (int I = 2; I <= npt; ++I) {
+    if (Tg[I - 1] >= T) {
+      auto A = [&](int k) { return Tg[k - 1]; };
+      auto B = [&](int k) { return Q[k - 1]; };
+      if (I < 3 || I == npt) {
+        int J = I < 3 ? 3 : (I == npt ? npt : I);
+        double A0 = (T - A(J - 1)) * (T - A(J)) / ((A(J - 2) - A(J - 1)) * (A(J - 2) - A(J)));
+        double A1 = (T - A(J - 2)) * (T - A(J)) / ((A(J - 1) - A(J - 2)) * (A(J - 1) - A(J)));
+        double A2 = (T - A(J - 2)) * (T - A(J - 1)) / ((A(J) - A(J - 2)) * (A(J) - A(J - 1)));
+        return A0 * B(J - 2) + A1 * B(J - 1) + A2 * B(J);
+      }
+      int J = I;
+      double A0 = (T - A(J - 1)) * (T - A(J)) * (T - A(J + 1));
+      A0 = A0 / ((A(J - 2) - A(J - 1)) * (A(J - 2) - A(J)) * (A(J - 2) - A(J + 1)));
+      double A1 = (T - A(J - 2)) * (T - A(J)) * (T - A(J + 1));
+      A1 = A1 / ((A(J - 1) - A(J - 2)) * (A(J - 1) - A(J)) * (A(J - 1) - A(J + 1)));
+      double A2 = (T - A(J - 2)) * (T - A(J - 1)) * (T - A(J + 1));
+      A2 = A2 / ((A(J) - A(J - 2)) * (A(J) - A(J - 1)) * (A(J) - A(J + 1)));
+      double A3 = (T - A(J - 2)) * (T - A(J - 1)) * (T - A(J));
+      A3 = A3 / ((A(J + 1) - A(J - 2)) * (A(J + 1) - A(J - 1)) * (A(J + 1) - A(J)));
+      return A0 * B(J - 2) + A1 * B(J - 1) + A2 * B(J) + A3 * B(J + 1);
+    }
+  }
+  return 0.;
+}
+
+// Line-shape sub-functions F1/F2/F3 (SHAPEL clblm_ODLAY.f90:2804-2909),
+// FG (SHAPEG :2914-2954) and XVER (VERFN :2959-3015) on 3001 points.
+void shape_tables(std::vector<double>& F1, std::vector<double>& F2, std::vector<double>& F3,
+                  std::vector<double>& FG, std::vector<double>& XV) {
+  const double HWF1 = 4., HWF2 = 16., HWF3 = 64., DXF1 = 0.002, DXF2 = 0.008, DXF3 = 0.032;
+  const int NX = kNFPTS, N = kNFMX;
+  F1.assign(N + 1, 0.);
+  F2.assign(N + 1, 0.);
+  F3.assign(N + 1, 0.);
+  FG.assign(N + 1, 0.);
+  XV.assign(N + 1, 0.);
+  const double RECPI = 1. / (2. * std::asin(1.));
+  auto Af = [](double z) { return (1. + 2. * z * z) / ((1. + z * z) * (1. + z * z)); };
+  auto Bf = [](double z) { return -1. / ((1. + z * z) * (1. + z * z)); };
+  const double A1 = Af(HWF1), B1 = Bf(HWF1), A2 = Af(HWF2), B2 = Bf(HWF2), A3 = Af(HWF3), B3 = Bf(HWF3);
+  auto lor = [](double xsq) { return 1. / (1. + xsq); };
+  F1[1] = RECPI * (lor(0.) - (A1 + B1 * 0.));
+  for (int j = 2; j <= NX; ++j) {
+    double X = (double)(j - 1) * DXF1, XSQ = X * X;
+    F1[j] = RECPI * (lor(XSQ) - (A1 + B1 * XSQ));
+  }
+  F1[NX] = 0.;
+  F2[1] = RECPI * ((A1 + B1 * 0.) - (A2 + B2 * 0.));
+  int J1LIM = (int)(HWF1 / DXF2 + 1.001);
+  for (int j = 2; j <= NX; ++j) {
+    double X = (double)(j - 1) * DXF2, XSQ = X * X;
+    F2[j] = j <= J1LIM ? RECPI * ((A1 + B1 * XSQ) - (A2 + B2 * XSQ)) : RECPI * (lor(XSQ) - (A2 + B2 * XSQ));
+  }
+  F2[NX] = 0.;
+  F3[1] = RECPI * ((A2 + B2 * 0.) - (A3 + B3 * 0.));
+  int J2LIM = (int)(HWF2 / DXF3 + 1.001);
+  for (int j = 2; j <= NX; ++j) {
+    double X = (double)(j - 1) * DXF3, XSQ = X * X;
+    F3[j] = j <= J2LIM ? RECPI * ((A2 + B2 * XSQ) - (A3 + B3 * XSQ)) : RECPI * (lor(XSQ) - (A3 + B3 * XSQ));
+  }
+  const double FLN2 = std::log(2.), FGNORM = std::sqrt(FLN2 * RECPI);
+  FG[1] = FGNORM * std::exp(-FLN2 * 0.);
+  for (int j = 2; j <= NX; ++j) {
+    double X = (double)(j - 1) * DXF1, XSQ = X * X;
+    FG[j] = FGNORM * std::exp(-FLN2 * XSQ);
+  }
+  FG[NX] = 0.;
+  const double CEXP = 0.45, CE0 = 1., CE2 = -.20737285249, CE4 = -.00872684335747;
+  const double SE0 = std::sqrt(CEXP / kPI_C), AE2 = 2. * CEXP, AE4 = AE2 * AE2 / 3.;
+  for (int i = 1; i <= N; ++i) {
+    double Z = DXF1 * (double)(i - 1), Z2 = Z * Z;
+    double XE0 = SE0 * std::exp(-CEXP * Z2);
+    XV[i] = (1. / (CE0 + CE2 + CE4)) * (CE0 + CE2 * AE2 * Z2 + CE4 * AE4 * Z2 * Z2) * XE0;
+  }
+}
+
+int upload_tables(clblm_handle* h) {
+  std::vector<double> F1, F2, F3, FG, XV;
+  shape_tables(F1, F2, F3, FG, XV);
+  const int N = kNFMX;
+  size_t bytes = N * sizeof(float4) + 2 * N * sizeof(float) + 5 * N * sizeof(double) + 1024;
+  CUDA_TRY(h, h->tabs.ensure(bytes));
+  std::vector<unsigned char> host(bytes, 0);
+  size_t off = 0;
+  auto put = [&](const void* src, size_t n) {
+    size_t o = (off + 255) & ~size_t(255);
+    std::memcpy(host.data() + o, src, n);
+    off = o + n;
+    return o;
+  };
+  std::vector<float4> t1f(N);
+  std::vector<float> t2f(N), t3f(N);
+  std::vector<double> t1d(3 * N), t2d(N), t3d(N);
+  for (int i = 0; i < N; ++i) {
+    t1f[i] = make_float4((float)F1[i + 1], (float)FG[i + 1], (float)XV[i + 1], 0.f);
+    t2f[i] = (float)F2[i + 1];
+    t3f[i] = (float)F3[i + 1];
+    t1d[3 * i] = F1[i + 1];
+    t1d[3 * i + 1] = FG[i + 1];
+    t1d[3 * i + 2] = XV[i + 1];
+    t2d[i] = F2[i + 1];
+    t3d[i] = F3[i + 1];
+  }
+  size_t o1 = put(t1f.data(), N * sizeof(float4));
+  size_t o2 = put(t2f.data(), N * sizeof(float));
+  size_t o3 = put(t3f.data(), N * sizeof(float));
+  size_t o4 = put(t1d.data(), 3 * N * sizeof(double));
+  size_t o5 = put(t2d.data(), N * sizeof(double));
+  size_t o6 = put(t3d.data(), N * sizeof(double));
+  if (off > h->tabs.bytes) return set_err(h, CLBLM_ERR_ARG, "table layout");
+  CUDA_TRY(h, cudaMemcpy(h->tabs.p, host.data(), off, cudaMemcpyHostToDevice));
+  unsigned char* b = h->tabs.as<unsigned char>();
+  h->shape.t1f = reinterpret_cast<const float4*>(b + o1);
+  h->shape.t2f = reinterpret_cast<const float*>(b + o2);
+  h->shape.t3f = reinterpret_cast<const float*>(b + o3);
+  h->shape.t1d = reinterpret_cast<const double*>(b + o4);
+  h->shape.t2d = reinterpret_cast<const double*>(b + o5);
+  h->shape.t3d = reinterpret_cast<const double*>(b + o6);
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_AVRAT, CLBLM_AVRAT, sizeof CLBLM_AVRAT));
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_CGAUSS, CLBLM_CGAUSS, sizeof CLBLM_CGAUSS));
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_CF1, CLBLM_CF1, sizeof CLBLM_CF1));
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_CF2, CLBLM_CF2, sizeof CLBLM_CF2));
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_CF3, CLBLM_CF3, sizeof CLBLM_CF3));
+  CUDA_TRY(h, cudaMemcpyToSymbol(c_CER, CLBLM_CER, sizeof CLBLM_CER));
+  rt_upload_interp_coef(h->stream);
+  return CLBLM_OK;
+}
+
+int load_lines(clblm_handle* h, const clblm_lines_t* L) {
+  if (!L || L->n < 0 || (L->n > 0 && (!L->vnu || !L->sp || !L->alfa || !L->epp || !L->mol || !L->hwhm ||
+                                      !L->tmpalf || !L->pshift || !L->iflg)))
+    return set_err(h, CLBLM_ERR_ARG, "bad line list");
+  for (int64_t i = 1; i < L->n; ++i)
+    if (L->vnu[i] < L->vnu[i - 1]) return set_err(h, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+  int64_t n = L->n;
+  h->nlines = n;
+  h->h_vnu.assign(L->vnu, L->vnu + n);
+  h->h_iflg.assign(L->iflg, L->iflg + n);
+  h->h_mol.assign(L->mol, L->mol + n);
+  double sm = 0.;
+  for (int64_t i = 0; i < n; ++i) sm = std::max(sm, std::fabs((double)L->pshift[i]));
+  h->shiftmax = sm;
+  const void* src[9] = {L->vnu, L->sp, L->alfa, L->epp, L->mol, L->hwhm, L->tmpalf, L->pshift, L->iflg};
+  size_t esz[9] = {8, 4, 4, 4, 4, 4, 4, 4, 4};
+  for (int k = 0; k < 9; ++k) {
+    CUDA_TRY(h, h->lines[k].ensure(std::max<size_t>(1, n * esz[k])));
+    if (n) CUDA_TRY(h, cudaMemcpyAsync(h->lines[k].p, src[k], n * esz[k], cudaMemcpyHostToDevice, h->stream));
+  }
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return CLBLM_OK;
+}
+
+LineIn line_in(const clblm_handle* h) {
+  LineIn li;
+  li.vnu = h->lines[0].as<const double>();
+  li.sp = h->lines[1].as<const float>();
+  li.alfa = h->lines[2].as<const float>();
+  li.epp = h->lines[3].as<const float>();
+  li.mol = h->lines[4].as<const int>();
+  li.hwhm = h->lines[5].as<const float>();
+  li.tmpalf = h->lines[6].as<const float>();
+  li.pshift = h->lines[7].as<const float>();
+  li.iflg = h->lines[8].as<const int>();
+  li.n = h->nlines;
+  return li;
+}
+
+// ---- per-layer plan ---------------------------------------------------------
+struct HostPlan {
+  LayerPlan P;
+  std::vector<double> vft;
+  std::vector<int> panel_blk;       // LBLF4Q block of each panel
+  std::vector<double> blk_v1;       // block origins V1R4
+  std::vector<int> blk_n;           // NPTR4 of each block
+  std::vector<int64_t> blk_m0;      // origin on the global far-wing grid
+  double dv_out;    // DV of the returned spectrum
+  int64_t n_out;    // points of the returned spectrum
+};
+
+int64_t lower_bound_h(const std::vector<double>& a, int64_t lo, int64_t hi, double x) {
+  return std::lower_bound(a.begin() + lo, a.begin() + hi, x) - a.begin();
+}
+
+// RDLIN's line range (clblm_ODLAY.f90:2624-2696 with the IHI/IDATA rule):
+// from the first line >= VBOT of the first record whose last line is >= VBOT,
+// to the first valid line above VTOP, continuing into the next record while
+// that line closes its record.
+void line_range(const clblm_handle* h, double VBOT, double VTOP, int64_t* lo, int64_t* hi, int64_t* first_end) {
+  const int64_t n = h->nlines, R = CLBLM_LINES_PER_RECORD;
+  int64_t nrec = (n + R - 1) / R;
+  int64_t rec = 0;
+  while (rec < nrec && h->h_vnu[std::min(n, (rec + 1) * R) - 1] < VBOT) rec++;
+  if (rec >= nrec) {
+    *lo = 0;
+    *hi = -1;
+    *first_end = 0;
+    return;
+  }
+  int64_t b = rec * R, e = std::min(n, b + R);
+  int64_t start = b;
+  // first valid (IFLG >= 0) line with vnu >= VBOT; the last valid line if none
+  {
+    int64_t last_valid = -1, found = -1;
+    for (int64_t i = b; i < e; ++i) {
+      if (h->h_iflg[i] < 0) continue;
+      last_valid = i;
+      if (h->h_vnu[b] < VBOT) {
+        if (h->h_vnu[i] >= VBOT) {
+          found = i;
+          break;
+        }
+      } else {
+        found = i;
+        break;
+      }
+    }
+    start = found >= 0 ? found : (last_valid >= 0 ? last_valid : b);
+  }
+  *lo = start;
+  *first_end = e;
+  // jump to the record holding the first line above VTOP
+  int64_t k = lower_bound_h(h->h_vnu, start, n, std::nextafter(VTOP, 1e300));  // first vnu > VTOP
+  int64_t r = std::max(rec, k / R);
+  if (k >= n) {
+    *hi = n - 1;
+    return;
+  }
+  for (;;) {
+    int64_t rb = r * R, re = std::min(n, rb + R);
+    int64_t from = (r == rec) ? start : rb;
+    int64_t ihi = -1, nvalid_after = 0;
+    bool hit = false;
+    for (int64_t i = from; i < re; ++i) {
+      if (h->h_iflg[i] < 0) continue;
+      if (hit) {
+        nvalid_after++;
+        continue;
+      }
+      if (h->h_mol[i] > 0) {
+        ihi = i;
+        if (h->h_vnu[i] > VTOP) hit = true;
+      }
+    }
+    if (ihi >= 0) *hi = ihi;
+    if (hit && nvalid_after > 0) return;       // IDATA = 1
+    if (re >= n) {
+      *hi = std::max<int64_t>(*hi, n - 1);
+      return;                                   // end of file
+    }
+    r++;
+  }
+}
+
+int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g, const clblm_od_ctrl_t* c,
+               int jrad_state, bool first_pass, HostPlan* hp, int* jrad_after) {
+  if (!lay || !g || !c) return set_err(h, CLBLM_ERR_ARG, "null argument");
+  if (!(g->v2 > g->v1) || !(g->dv_normal > 0.) || !(g->dv_narrow > 0.) || !(g->sample > 0.))
+    return set_err(h, CLBLM_ERR_GRID, "bad grid (v1 %.6f v2 %.6f dv %.3g/%.3g)", g->v1, g->v2, g->dv_normal,
+                   g->dv_narrow);
+  if (!(lay->pave > 0.) || !(lay->tave > 0.) || !(lay->wtot > 0.)) return set_err(h, CLBLM_ERR_ARG, "bad layer");
+  if (c->line_off) return set_err(h, CLBLM_ERR_UNSUPPORTED, "lineOff is not on this path");
+  if (c->dptmin != 0. || c->dptfac != 0.)
+    return set_err(h, CLBLM_ERR_UNSUPPORTED, "line rejection thresholds DPTMIN/DPTFAC != 0 are not on this path");
+  LayerPlan& P = hp->P;
+  std::memset(&P, 0, sizeof P);
+  const double V1 = g->v1, V2 = g->v2;
+  // grid choice, clblm_ODLAY.f90:443-457
+  double ALFAV = g->sample * std::max(g->dv_normal, g->dv_narrow);
+  double DV = g->dv_normal;
+  if (!(std::fabs(g->dv_normal - g->dv_narrow) / g->dv_normal > 0.2)) DV = g->dv_narrow;
+  // sticky JRAD, clblm_ODLAY.f90:349-352 and OPDPTH :877-878
+  int JRAD = first_pass ? c->jrad : jrad_state;
+  double XKT = lay->tave / kRADCN2;
+  if (((V1 / XKT) < 5.) && (JRAD != -1)) JRAD = 0;
+  *jrad_after = JRAD;
+  if (JRAD != 0 && JRAD != 1) return set_err(h, CLBLM_ERR_UNSUPPORTED, "JRAD=%d is not on this path", JRAD);
+  P.v1 = V1;
+  P.v2 = V2;
+  P.dv = DV;
+  P.dvr2 = (kDXF2 / kDXF1) * DV;
+  P.dvr3 = (kDXF3 / kDXF1) * DV;
+  P.alfav = ALFAV;
+  P.alfmax = 4. * ALFAV;
+  P.nalfmax = (int)(P.alfmax / DV);
+  P.nbound = (int)((2. * kHWF3) * (double)P.nalfmax + 0.01);
+  int MAX1 = kNSHIFT + kNLIM1 + kNSHIFT + P.nbound / 2;
+  int MAX2 = MAX1 / 4, MAX3 = MAX1 / 16;
+  P.max1 = MAX1 + 4 * P.nalfmax;
+  P.max2 = MAX2 + 16 * P.nalfmax / 4 + 1;
+  P.max3 = MAX3 + 64 * P.nalfmax / 16 + 1;
+  P.bound = (double)P.nbound * DV / 2.;
+  P.vft0 = V1 - (double)kNSHIFT * DV;
+  P.vbot = V1 - P.bound;
+  P.vtop = V2 + P.bound;
+  if (!(P.vft0 > 0.))
+    return set_err(h, CLBLM_ERR_UNSUPPORTED, "panels below 0 cm-1 (RSYM folding) are not on this path");
+  P.pave = lay->pave;
+  P.tave = lay->tave;
+  P.wtot = lay->wtot;
+  P.xkt = XKT;
+  P.xkt0 = kT0 / kRADCN2;
+  P.betacr = (1. / P.xkt) - (1. / P.xkt0);
+  P.tratio = lay->tave / kT0;
+  P.rhorat = (lay->pave / kP0) * (kT0 / lay->tave);
+  P.pavp0 = lay->pave / kP0;
+  P.pavp2 = P.pavp0 * P.pavp0;
+  P.jrad = JRAD;
+  P.ilnflg = c->line_rejec ? 0 : -1;
+  P.dptmn = c->dptmin;
+  if (JRAD != 1) P.dptmn = c->dptmin / radfn_h(V2, lay->tave / kRADCN2);
+  P.dptfc = c->dptfac;
+  // molecules: MOLEC clblm_ODLAY_CommonSub.f90:201-264 with TIPS_2003
+  const double FLN2 = std::log(2.);
+  const double FAD = FLN2 * 2. * kAVOGAD * kBOLTZ / (kCLIGHT * kCLIGHT);
+  for (int i = 0; i < lay->nmol; ++i) {
+    int m = lay->mol_id[i];
+    if (m < 1 || m > kTIPSNMOL)
+      return set_err(h, CLBLM_ERR_UNSUPPORTED, "molecule %d: the partition-sum tables carry molecules 1-9", m);
+    if (!(lay->tave >= 70. && lay->tave <= 3000.))
+      return set_err(h, CLBLM_ERR_RANGE, "TIPS: temperature %.3f K outside 70-3000 K", lay->tave);
+    P.sel[m] = 1;
+    P.wk[m] = lay->w[i];
+    double q296 = tips_interp(296., CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[m - 1], 119);
+    double qt = tips_interp(lay->tave, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[m - 1], 119);
+    P.scor[m] = q296 / qt;
+    P.rhoslf[m] = P.rhorat * P.wk[m] / lay->wtot;
+    P.alfd1[m] = std::sqrt(FAD * lay->tave / CLBLM_ISO1_MASS[m - 1]);
+  }
+  // panels: VFT advanced by 2400 DV until VFT + (NHI-1) DV > V2 (panelOut)
+  hp->vft.clear();
+  double VFT = P.vft0;
+  int64_t nsamp = 0;
+  const int NHI0 = kNLIM1 + kNSHIFT - 1;
+  for (;;) {
+    hp->vft.push_back(VFT);
+    if ((VFT + (NHI0 - 1) * DV) > V2) {
+      int NHI = (int)((V2 - VFT) / DV + 1.);
+      double V2P = VFT + (double)(NHI - 1) * DV;
+      if (V2P < V2) NHI = NHI + 1;
+      P.nhi_last = NHI;
+      nsamp += NHI - (kNSHIFT + 1) + 1;
+      break;
+    }
+    nsamp += NHI0 - (kNSHIFT + 1) + 1;
+    VFT = VFT + (double)(kNLIM1 - 1) * DV;
+    if (hp->vft.size() > (size_t)200000000) return set_err(h, CLBLM_ERR_GRID, "too many panels");
+  }
+  P.npanels = (int)hp->vft.size();
+  P.nsamp = nsamp;
+  line_range(h, P.vbot, P.vtop, &P.line_lo, &P.line_hi, &P.first_rec_end);
+  // far wings, OPDPTH :899-931
+  double ALFAV4 = 64. * g->sample * DV;
+  P.dvr4 = ALFAV4 / g->sample;
+  P.bound4 = 25.;
+  P.v1r4 = V1 - 2. * P.dvr4;
+  P.v2r4st = V2 + 2. * P.dvr4;
+  P.v1l4 = P.v1r4 - P.bound4 - P.dvr4;
+  P.v2l4 = P.v2r4st + P.bound4 + 2 * P.dvr4;
+  P.nptr4 = (int64_t)((P.v2r4st - P.v1r4) / P.dvr4 + kONEPL);
+  // LBLF4Q blocks: the first at V1R4; a new one starts after a panel when the
+  // next panel's reach VF2 passes the block's end (HIRACQ :1466-1497)
+  {
+    hp->panel_blk.assign(P.npanels, 0);
+    hp->blk_v1.clear();
+    hp->blk_n.clear();
+    hp->blk_m0.clear();
+    auto add_block = [&](double v1r4, int64_t m0) {
+      int n4 = (int)((P.v2r4st - v1r4) / P.dvr4 + kONEPL);
+      if (n4 > kLIMOUT4) n4 = kLIMOUT4;
+      hp->blk_v1.push_back(v1r4);
+      hp->blk_n.push_back(n4);
+      hp->blk_m0.push_back(m0);
+      return v1r4 + P.dvr4 * (double)(n4 - 1);  // adjusted V2R4
+    };
+    double v2r4 = add_block(P.v1r4, 0);
+    const int N2R3 = kNLIM3 + (kNSHIFT / 16) - 1 + 3;
+    for (int p = 0; p < P.npanels; ++p) {
+      hp->panel_blk[p] = (int)hp->blk_v1.size() - 1;
+      if (p + 1 >= P.npanels) break;
+      double VFTn = hp->vft[p + 1];
+      double VF1 = VFTn - 2. * P.dvr4;
+      double fl = std::floor((VF1 - V1) / P.dvr4);
+      VF1 = V1 + fl * P.dvr4;
+      double VF2 = VFTn + 2. * P.dvr4 + (double)(N2R3 + 4) * P.dvr3;
+      if (VF2 > v2r4 && v2r4 != P.v2r4st) v2r4 = add_block(VF1, (int64_t)fl + 2);
+    }
+    P.nblk4 = (int)hp->blk_v1.size();
+  }
+  P.beta = kRADCN2 / lay->tave;
+  P.beta0 = kRADCN2 / kT0;
+  P.betacr4 = P.beta - P.beta0;
+  P.f4_lo = lower_bound_h(h->h_vnu, 0, h->nlines, P.v1l4);
+  if (P.f4_lo < h->nlines && !(h->h_vnu[P.f4_lo] - h->shiftmax * P.rhorat > 0.))
+    return set_err(h, CLBLM_ERR_UNSUPPORTED, "line centres at or below 0 cm-1 are not on this path");
+  P.f4_hi = std::min<int64_t>(
+      h->nlines, lower_bound_h(h->h_vnu, P.f4_lo, h->nlines, P.v2l4 + h->shiftmax * P.rhorat + 1e-6) + 2 * 250);
+  // continuum grid, OPDPTH :880-896
+  P.contnm = c->contnm_off ? 0 : 1;
+  if (P.contnm) {
+    if (!h->has_cont) return set_err(h, CLBLM_ERR_ARG, "continuum requested but the handle has no table");
+    P.dvabs = 1.;
+    P.v1abs = (double)(int)V1;
+    if (V1 < 0.) P.v1abs = P.v1abs - 1.;
+    P.v1abs = P.v1abs - 3. * P.dvabs;
+    P.v2abs = (double)(int)(V2 + 3. * P.dvabs + 0.5);
+    P.nptabs = (int)((P.v2abs - P.v1abs) / P.dvabs + 1.5);
+    if (P.nptabs > kNABSRB - 4)
+      return set_err(h, CLBLM_ERR_RANGE, "V2-V1 too wide for the continuum grid (%d points)", P.nptabs);
+    P.xself = c->xself;
+    P.xfrgn = c->xfrgn;
+    P.wk1 = P.wk[1];
+    P.h2o_fac = P.wk[1] / lay->wtot;
+  }
+  // returned spectrum: DVout interpolation, clblm_ODLAY.f90:571-604
+  double outputDV = DV;
+  if (g->dv_out > 0.) outputDV = g->dv_out;
+  hp->dv_out = outputDV;
+  if (std::fabs(outputDV - DV) < 2.220446049250313e-16) hp->n_out = nsamp;
+  else hp->n_out = (int64_t)std::ceil((V2 - V1) / outputDV + 1.);
+  return CLBLM_OK;
+}
+
+// interpSpectrum's classification of an in->out grid pair (clblm_Spectrum.f90:368-497)
+InterpSpec interp_spec(double v1in, double dvin, int64_t nin, double v1out, double dvout, int64_t nout) {
+  InterpSpec s;
+  std::memset(&s, 0, sizeof s);
+  const double EPS = 2.220446049250313e-16, TOL = 1.e-8;
+  double v2in = v1in + dvin * (double)(nin - 1), v2out = v1out + dvout * (double)(nout - 1);
+  s.v1 = v1in;
+  s.dvin = dvin;
+  s.dvout = dvout;
+  s.nin = nin;
+  if (std::fabs(v1in - v1out) < EPS && std::fabs(v2in - v2out) < EPS && std::fabs(dvin - dvout) < EPS && nin == nout) {
+    s.kind = 0;
+    return s;
+  }
+  s.kind = 1;
+  bool sameV1 = std::fabs(v1in - v1out) < EPS;
+  double dvRatio = dvout / dvin;
+  if (std::fabs(dvout - dvin) < TOL) dvRatio = 1.;
+  s.ratio = dvRatio;
+  const double hi2lo[5] = {2. / 1., 3. / 2., 4. / 3., 5. / 4., 6. / 5.};
+  const double lo2hi[5] = {1. / 2., 2. / 3., 3. / 4., 4. / 5., 5. / 6.};
+  bool isHi = false, isLo = false;
+  for (int k = 0; k < 5; ++k) {
+    if (std::fabs(dvRatio - hi2lo[k]) < TOL) isHi = true;
+    if (std::fabs(dvRatio - lo2hi[k]) < TOL) isLo = true;
+  }
+  if (sameV1 && std::fabs(dvRatio - 1.) < EPS) {
+    s.len_in = s.len_out = 1;
+    s.itype = 0;
+  } else if (sameV1 && isHi) {
+    s.len_in = (int)(dvout / (dvout - dvin) + 0.5);
+    s.len_out = s.len_in - 1;
+    s.itype = s.len_out - 1;
+  } else if (sameV1 && isLo) {
+    s.len_in = (int)(dvout / (dvin - dvout) + 0.5);
+    s.len_out = s.len_in + 1;
+    s.itype = s.len_out - 1;
+  } else {
+    s.itype = -1;
+  }
+  s.nint_ratio = (int)std::llround(dvRatio);
+  if (s.itype > 0) {
+    double AP = 1.0 / ((double)s.itype + 1.0);
+    for (int JP = 1; JP <= s.itype && JP + 1 < 10; ++JP) {
+      int IP = JP + 1;
+      double P = AP * (double)JP;
+      if (dvin > dvout) P = 1.0 - P;
+      s.b1[IP] = -P * (P - 1.0) * (P - 2.0) / 6.0;
+      s.b2[IP] = (P * P - 1.0) * (P - 2.0) * 0.5;
+      s.b3[IP] = -P * (P + 1.0) * (P - 2.0) * 0.5;
+      s.b4[IP] = P * (P * P - 1.0) / 6.0;
+    }
+  }
+  return s;
+}
+
+// For a general-ratio spec: the block starts of interpSpectrum's outer loop
+// (exact FP64 replay on the host, a few thousand blocks at most) and the
+// per-point (iIn, IP) map built on the device into `buf`.
+int build_interp_map(clblm_handle* h, InterpSpec* s, int64_t nout, DevBuf* buf) {
+  if (s->kind == 0 || s->itype >= 0) return CLBLM_OK;
+  std::vector<int64_t> j1;
+  std::vector<double> vo;
+  const double TOL = 1.e-8;
+  double V2out = s->v1 + (double)(nout - 1) * s->dvout;
+  double Vo = s->v1;
+  while (Vo < V2out + TOL) {
+    int64_t J1 = (int64_t)((Vo - s->v1) / s->dvout + 1.001);
+    int64_t J2 = std::min<int64_t>(nout, J1 + 2400 - 1);
+    j1.push_back(J1);
+    vo.push_back(Vo);
+    Vo = s->v1 + (double)J2 * s->dvout;
+    if (j1.size() > (size_t)(nout / 2400 + 8)) return set_err(h, CLBLM_ERR_GRID, "interpolation blocks");
+  }
+  size_t nb = j1.size();
+  size_t need = sizeof(int2) * nout + 16 * (nb + 1) + 512;
+  CUDA_TRY(h, buf->ensure(need));
+  unsigned char* base = buf->as<unsigned char>();
+  int2* map = reinterpret_cast<int2*>(base);
+  size_t off = ((sizeof(int2) * nout) + 255) & ~size_t(255);
+  int64_t* dj1 = reinterpret_cast<int64_t*>(base + off);
+  double* dvo = reinterpret_cast<double*>(base + off + 8 * (nb + 1));
+  CUDA_TRY(h, cudaMemcpyAsync(dj1, j1.data(), 8 * nb, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(dvo, vo.data(), 8 * nb, cudaMemcpyHostToDevice, h->stream));
+  h->launches++;
+  k_interp_map<<<(unsigned)((nb + 63) / 64), 64, 0, h->stream>>>(*s, dj1, dvo, (int)nb, nout, map);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));  // host block tables go out of scope
+  s->map = map;
+  return CLBLM_OK;
+}
+
+// ---- device pipeline for a batch of layers ----------------------------------
+struct Batch {
+  std::vector<HostPlan>* hp;
+  int first, count;    // layers [first, first+count)
+  bool plain;
+};
+
+int64_t pad256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+// Runs the OD pipeline for `count` layers whose plans are already uploaded at
+// plans[first..]; OD of layer k lands at od + P.od_off (Real).
+int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t lstride,
+                 int64_t f4stride, int64_t pstride) {
+  cudaStream_t st = h->stream;
+  const LayerPlan* dplans = h->plans.as<const LayerPlan>();
+  LineIn li = line_in(h);
+  dim3 blk(256);
+  // continuum
+  h->launches++;
+  k_continuum<<<dim3((kNABSRB + 255) / 256, count), blk, 0, st>>>(dplans, first, h->cont, h->absrb.as<double>());
+  // far wings
+  h->launches++;
+  k_f4_prep<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
+      dplans, first, li, h->f4prep.as<F4Prep>(), f4stride, h->stats.as<unsigned long long>());
+  {
+    // LINF4Q record loop + SHRINQ: count, compact, walk, group sums
+    int nblk4 = (int)((f4stride + 1 + 1023) / 1024);
+    h->launches++;
+    k_f4_count<<<dim3(nblk4, count), 256, 0, st>>>(h->f4prep.as<F4Prep>(), f4stride, dplans, first,
+                                                   h->f4blk.as<int64_t>(), nblk4);
+    h->launches++;
+    k_f4_blockscan<<<(count + 63) / 64, 64, 0, st>>>(h->f4blk.as<int64_t>(), nblk4, dplans, first, count,
+                                                     h->f4ntot.as<int64_t>());
+    CUDA_TRY(h, cudaMemsetAsync(h->f4cut.p, 0xff, sizeof(int64_t) * count, st));
+    h->launches++;
+    k_f4_compact<<<dim3(nblk4, count), 256, 0, st>>>(h->f4prep.as<F4Prep>(), f4stride, dplans, first,
+                                                     h->f4blk.as<int64_t>(), nblk4, h->f4cidx.as<int64_t>(),
+                                                     h->f4vb.as<long long>(), h->f4lb.as<long long>(),
+                                                     h->f4src.as<int64_t>(), h->f4flag.as<unsigned char>(),
+                                                     h->f4cut.as<int64_t>());
+    h->launches++;
+    k_f4_walk<<<count, 32, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
+                                    h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4flag.as<unsigned char>(),
+                                    h->f4ntot.as<int64_t>(), h->f4cut.as<int64_t>(), h->f4grp.as<int4>(),
+                                    h->f4nout.as<int64_t>());
+    h->launches++;
+    k_f4_groupsum<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), 256, 0, st>>>(
+        dplans, first, h->f4prep.as<F4Prep>(), f4stride, h->f4src.as<int64_t>(), h->f4grp.as<int4>(),
+        h->f4nout.as<int64_t>(), h->f4sh.as<ShrunkLine>());
+  }
+  int64_t rstride = f4stride + 4096;
+  h->launches++;
+  k_f4_lineinit<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
+      dplans, first, h->f4sh.as<ShrunkLine>(), f4stride, h->f4nout.as<int64_t>(), h->f4rec.as<F4Rec>(),
+      h->f4recd.as<F4RecD>(), rstride, h->f4nrec.as<int64_t>(), h->f4nmir.as<int64_t>());
+  h->launches++;
+  k_f4_bounds<<<count, 1024, 0, st>>>(h->f4rec.as<F4Rec>(), rstride, h->f4nrec.as<int64_t>(), first,
+                                      h->f4pm.as<int>(), h->f4sm.as<int>());
+  {
+    int64_t maxr4 = 0;
+    for (int k = 0; k < count; ++k) maxr4 = std::max(maxr4, hps[first + k].P.nptr4);
+    F4Args fa;
+    fa.plans = dplans;
+    fa.layer0 = first;
+    fa.nrec = h->f4nrec.as<int64_t>();
+    fa.nmirror = h->f4nmir.as<int64_t>();
+    fa.rec = h->f4rec.as<F4Rec>();
+    fa.recd = h->f4recd.as<F4RecD>();
+    fa.stride = rstride;
+    fa.pmax_jmax = h->f4pm.as<int>();
+    fa.smin_jmin = h->f4sm.as<int>();
+    fa.r4_all = h->r4.p;
+    dim3 grid((unsigned)((maxr4 + 2 + 127) / 128), count);
+    h->launches++;
+    if (plain) k_f4_conv<true><<<grid, 128, 0, st>>>(fa);
+    else k_f4_conv<false><<<grid, 128, 0, st>>>(fa);
+  }
+  // line centres
+  h->launches++;
+  k_line_prep<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
+      dplans, first, li, h->vft.as<double>(), h->prep.as<LinePrep>(), lstride, h->stats.as<unsigned long long>());
+  int nblk = (int)((lstride + 1023) / 1024);
+  h->launches++;
+  k_scan_blockmax<<<dim3(nblk, count), 256, 0, st>>>(h->prep.as<LinePrep>(), lstride, h->nlines_d.as<int64_t>() + first,
+                                                      h->blockmax.as<int>(), nblk);
+  h->launches++;
+  k_scan_blocks<<<(count + 63) / 64, 64, 0, st>>>(h->blockmax.as<int>(), nblk, h->nlines_d.as<int64_t>() + first, count);
+  h->launches++;
+  k_scan_apply<<<dim3(nblk, count), 256, 0, st>>>(h->prep.as<LinePrep>(), lstride, h->nlines_d.as<int64_t>() + first,
+                                                   h->blockmax.as<int>(), nblk, h->qpanel.as<int>());
+  h->launches++;
+  k_line_records<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
+      dplans, first, h->vft.as<double>(), h->prep.as<LinePrep>(), h->qpanel.as<int>(), lstride, h->rec.as<GridRec>(),
+      h->recd.as<GridRecD>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(), h->alfvmax.as<double>());
+  int maxp = 0;
+  for (int k = 0; k < count; ++k) maxp = std::max(maxp, hps[first + k].P.npanels);
+  h->launches++;
+  k_panel_ranges<<<dim3((maxp + 127) / 128, count), 128, 0, st>>>(dplans, first, h->lines[0].as<double>(),
+                                                                   h->alfvmax.as<double>(), h->shiftmax,
+                                                                   h->ranges.as<int64_t>(), pstride);
+  PanelArgs pa;
+  pa.plans = dplans;
+  pa.layer0 = first;
+  pa.vft_all = h->vft.as<double>();
+  pa.rec = h->rec.as<GridRec>();
+  pa.recd = h->recd.as<GridRecD>();
+  pa.stride = lstride;
+  pa.ranges = h->ranges.as<int64_t>();
+  pa.panel_stride = pstride;
+  pa.vnu_raw = h->lines[0].as<double>();
+  pa.alfvmax = h->alfvmax.as<double>();
+  pa.shiftmax = h->shiftmax;
+  pa.r4_all = h->r4.p;
+  pa.absrb_all = h->absrb.as<double>();
+  pa.od_all = h->od.p;
+  pa.tabs = h->shape;
+  pa.panel_blk = h->pblk.as<int>();
+  pa.blk_v1 = h->bv1.as<double>();
+  pa.blk_n = h->bn.as<int>();
+  pa.blk_m0 = h->bm0.as<int64_t>();
+  pa.blk_fac = h->bfac.as<double>();
+  pa.err = h->err.as<int>();
+  {
+    int maxb = 1;
+    for (int k = 0; k < count; ++k) maxb = std::max(maxb, hps[first + k].P.nblk4);
+    h->launches++;
+    k_r4_radfac<<<dim3((maxb + 63) / 64, count), 64, 0, st>>>(dplans, first, h->bv1.as<double>(), h->bn.as<int>(),
+                                                            h->bfac.as<double>());
+  }
+  size_t smem = panel_smem_bytes(plain);
+  if (plain) {
+    CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    h->launches++;
+    k_panel<true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+  } else {
+    CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    h->launches++;
+    k_panel<false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+  }
+  CUDA_TRY(h, cudaGetLastError());
+  return CLBLM_OK;
+}
+
+// Sizes the workspace for layers [first, first+count) and uploads their plans.
+int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t* lstride,
+                  int64_t* f4stride, int64_t* pstride, int64_t* od_total) {
+  int64_t ls = 1, fs = 1, ps = 1, odt = 0, r4t = 0, vftt = 0;
+  for (int k = 0; k < count; ++k) {
+    LayerPlan& P = hps[first + k].P;
+    ls = std::max<int64_t>(ls, P.line_hi - P.line_lo + 1);
+    fs = std::max<int64_t>(fs, P.f4_hi - P.f4_lo);
+    ps = std::max<int64_t>(ps, P.npanels);
+  }
+  ls = pad256(ls);
+  fs = pad256(fs);
+  int nL = (int)hps.size();
+  // offsets of every layer's slices (all layers share the vft/plan arrays)
+  int64_t blkt = 0;
+  for (int k = 0; k < nL; ++k) {
+    LayerPlan& P = hps[k].P;
+    P.vft_off = vftt;
+    vftt += pad256((int64_t)hps[k].vft.size());
+    P.blk_off = blkt;
+    blkt += hps[k].blk_v1.size();
+  }
+  for (int k = 0; k < count; ++k) {
+    LayerPlan& P = hps[first + k].P;
+    P.od_off = odt;
+    odt += pad256(P.nsamp + 8);
+    P.r4_off = r4t;
+    r4t += pad256(P.nptr4 + 8);
+    P.abs_off = (int64_t)k * (kNABSRB + 8);
+  }
+  size_t real = plain ? 8 : 4;
+  CUDA_TRY(h, h->plans.ensure(sizeof(LayerPlan) * nL));
+  CUDA_TRY(h, h->vft.ensure(sizeof(double) * vftt));
+  CUDA_TRY(h, h->prep.ensure(sizeof(LinePrep) * ls * count));
+  CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * ls * count));
+  CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * ls * 3 * count));
+  CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * ls * 3 * count));
+  CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * ps * count));
+  CUDA_TRY(h, h->od.ensure(real * odt));
+  CUDA_TRY(h, h->r4.ensure(real * r4t));
+  CUDA_TRY(h, h->absrb.ensure(sizeof(double) * (kNABSRB + 8) * count));
+  CUDA_TRY(h, h->stats.ensure(sizeof(unsigned long long) * kStatsPerLayer * nL));
+  CUDA_TRY(h, h->alfvmax.ensure(sizeof(double) * nL));
+  CUDA_TRY(h, h->blockmax.ensure(sizeof(int) * ((ls + 1023) / 1024) * count));
+  CUDA_TRY(h, h->nlines_d.ensure(sizeof(int64_t) * nL));
+  CUDA_TRY(h, h->f4prep.ensure(sizeof(F4Prep) * fs * count));
+  CUDA_TRY(h, h->f4sh.ensure(sizeof(ShrunkLine) * fs * count));
+  CUDA_TRY(h, h->f4nout.ensure(sizeof(int64_t) * 2 * nL));
+  {
+    int64_t nblk4 = (fs + 1 + 1023) / 1024;
+    CUDA_TRY(h, h->f4blk.ensure(sizeof(int64_t) * nblk4 * count));
+    CUDA_TRY(h, h->f4ntot.ensure(sizeof(int64_t) * count));
+    CUDA_TRY(h, h->f4cidx.ensure(sizeof(int64_t) * (fs + 1) * count));
+    CUDA_TRY(h, h->f4vb.ensure(sizeof(long long) * fs * count));
+    CUDA_TRY(h, h->f4lb.ensure(sizeof(long long) * fs * count));
+    CUDA_TRY(h, h->f4src.ensure(sizeof(int64_t) * fs * count));
+    CUDA_TRY(h, h->f4flag.ensure(fs * count));
+    CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * count));
+    CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * fs * count));
+  }
+  CUDA_TRY(h, h->f4rec.ensure(sizeof(F4Rec) * (fs + 4096) * count));
+  CUDA_TRY(h, h->f4recd.ensure(sizeof(F4RecD) * (fs + 4096) * count));
+  CUDA_TRY(h, h->f4nrec.ensure(sizeof(int64_t) * nL));
+  CUDA_TRY(h, h->f4nmir.ensure(sizeof(int64_t) * nL));
+  CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (fs + 4096) * count));
+  CUDA_TRY(h, h->f4sm.ensure(sizeof(int) * (fs + 4096) * count));
+  CUDA_TRY(h, h->err.ensure(sizeof(int) * 4));
+  CUDA_TRY(h, h->pblk.ensure(sizeof(int) * vftt));
+  CUDA_TRY(h, h->bv1.ensure(sizeof(double) * (blkt + 1)));
+  CUDA_TRY(h, h->bn.ensure(sizeof(int) * (blkt + 1)));
+  CUDA_TRY(h, h->bm0.ensure(sizeof(int64_t) * (blkt + 1)));
+  CUDA_TRY(h, h->bfac.ensure(sizeof(double) * (kLIMOUT4 + 2) * (blkt + 1)));
+  {
+    std::vector<int> pb(vftt, 0), bn(blkt + 1, 0);
+    std::vector<double> bv(blkt + 1, 0.);
+    std::vector<int64_t> bm(blkt + 1, 0);
+    for (int k = 0; k < nL; ++k) {
+      const HostPlan& hp = hps[k];
+      std::copy(hp.panel_blk.begin(), hp.panel_blk.end(), pb.begin() + hp.P.vft_off);
+      std::copy(hp.blk_v1.begin(), hp.blk_v1.end(), bv.begin() + hp.P.blk_off);
+      std::copy(hp.blk_n.begin(), hp.blk_n.end(), bn.begin() + hp.P.blk_off);
+      std::copy(hp.blk_m0.begin(), hp.blk_m0.end(), bm.begin() + hp.P.blk_off);
+    }
+    cudaStream_t st0 = h->stream;
+    CUDA_TRY(h, cudaMemcpyAsync(h->pblk.p, pb.data(), sizeof(int) * vftt, cudaMemcpyHostToDevice, st0));
+    CUDA_TRY(h, cudaMemcpyAsync(h->bv1.p, bv.data(), sizeof(double) * (blkt + 1), cudaMemcpyHostToDevice, st0));
+    CUDA_TRY(h, cudaMemcpyAsync(h->bn.p, bn.data(), sizeof(int) * (blkt + 1), cudaMemcpyHostToDevice, st0));
+    CUDA_TRY(h, cudaMemcpyAsync(h->bm0.p, bm.data(), sizeof(int64_t) * (blkt + 1), cudaMemcpyHostToDevice, st0));
+    CUDA_TRY(h, cudaStreamSynchronize(st0));  // host vectors go out of scope
+  }
+  std::vector<LayerPlan> plans(nL);
+  std::vector<double> vft(vftt, 0.);
+  std::vector<int64_t> nl(nL, 0);
+  for (int k = 0; k < nL; ++k) {
+    plans[k] = hps[k].P;
+    std::copy(hps[k].vft.begin(), hps[k].vft.end(), vft.begin() + hps[k].P.vft_off);
+    nl[k] = hps[k].P.line_hi - hps[k].P.line_lo + 1;
+  }
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(h->plans.p, plans.data(), sizeof(LayerPlan) * nL, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->vft.p, vft.data(), sizeof(double) * vftt, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->nlines_d.p, nl.data(), sizeof(int64_t) * nL, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemsetAsync(h->stats.p, 0, sizeof(unsigned long long) * kStatsPerLayer * nL, st));
+  CUDA_TRY(h, cudaMemsetAsync(h->alfvmax.p, 0, sizeof(double) * nL, st));
+  CUDA_TRY(h, cudaMemsetAsync(h->err.p, 0, sizeof(int) * 4, st));
+  *lstride = ls;
+  *f4stride = fs;
+  *pstride = ps;
+  *od_total = odt;
+  return CLBLM_OK;
+}
+
+// Reads back the error flags and the counters of layers [first, first+count).
+int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, clblm_od_stats_t* last_stats) {
+  int err[4];
+  int nL = (int)hps.size();
+  std::vector<unsigned long long> stats(kStatsPerLayer * nL);
+  std::vector<int64_t> nout(2 * nL);
+  CUDA_TRY(h, cudaMemcpyAsync(err, h->err.p, sizeof err, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(stats.data(), h->stats.p, sizeof(unsigned long long) * stats.size(),
+                              cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(nout.data(), h->f4nout.p, sizeof(int64_t) * 2 * nL, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  CUDA_TRY(h, cudaGetLastError());
+  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "more than %d radiation-term segments in a panel", kMaxSeg);
+  if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
+  for (int k = first; k < first + count; ++k) {
+    const unsigned long long* s = &stats[k * kStatsPerLayer];
+    if (s[4]) return set_err(h, CLBLM_ERR_UNSUPPORTED, "layer %d: %llu lines need isotopologue/line-coupling/drop "
+                             "rules that are not on this path", k + 1, s[4]);
+    if (nout[2 * k] == -2)
+      return set_err(h, CLBLM_ERR_UNSUPPORTED, "far-wing line window: no line above V2L4 within the prepared range");
+  }
+  if (last_stats) {
+    int k = first + count - 1;
+    const unsigned long long* s = &stats[k * kStatsPerLayer];
+    const LayerPlan& P = hps[k].P;
+    last_stats->nlin = (int64_t)s[0];
+    last_stats->lincnt = (int64_t)s[1];
+    last_stats->nminus = (int64_t)s[2];
+    last_stats->nplus = (int64_t)s[3];
+    last_stats->nshrunk = nout[2 * k + 1];
+    last_stats->npanels = P.npanels;
+    last_stats->nsamp = hps[k].n_out;
+    last_stats->dv = P.dv;
+    last_stats->dvr4 = P.dvr4;
+    last_stats->jrad = P.jrad;
+  }
+  return CLBLM_OK;
+}
+
+int check_device(clblm_handle* h) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= h->device)
+    return set_err(h, CLBLM_ERR_NO_DEVICE, "no CUDA device %d", h->device);
+  return CLBLM_OK;
+}
+
+}  // namespace
+
+// =============================== C-ABI ======================================
+extern "C" {
+
+int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int device, clblm_handle_t** out) {
+  if (!out) return set_err(nullptr, CLBLM_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  clblm_handle* h = new clblm_handle();
+  h->device = device;
+  int rc = check_device(h);
+  if (rc) {
+    g_create_err = h->errmsg;
+    delete h;
+    return rc;
+  }
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_create_err = "cannot use CUDA device";
+    delete h;
+    return CLBLM_ERR_CUDA;
+  }
+  rc = upload_tables(h);
+  if (!rc) rc = load_lines(h, lines);
+  if (!rc && cont) {
+    if (cont->n < 4 || !cont->self_absco_ref || !cont->for_absco_ref || !cont->self_texp || !(cont->dv > 0.))
+      rc = set_err(h, CLBLM_ERR_ARG, "bad continuum table");
+    else {
+      size_t b = sizeof(double) * cont->n;
+      if (h->cont_self.ensure(b) || h->cont_for.ensure(b) || h->cont_texp.ensure(b)) rc = CLBLM_ERR_OOM;
+      else {
+        cudaMemcpy(h->cont_self.p, cont->self_absco_ref, b, cudaMemcpyHostToDevice);
+        cudaMemcpy(h->cont_for.p, cont->for_absco_ref, b, cudaMemcpyHostToDevice);
+        cudaMemcpy(h->cont_texp.p, cont->self_texp, b, cudaMemcpyHostToDevice);
+        h->cont.n = cont->n;
+        h->cont.v1 = cont->v1;
+        h->cont.dv = cont->dv;
+        h->cont.self_absco_ref = h->cont_self.as<double>();
+        h->cont.for_absco_ref = h->cont_for.as<double>();
+        h->cont.self_texp = h->cont_texp.as<double>();
+        h->cont.ref_press = cont->ref_press;
+        h->cont.ref_temp = cont->ref_temp;
+        h->has_cont = true;
+      }
+    }
+  }
+  if (rc) {
+    g_create_err = h->errmsg;
+    clblm_gpu_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return CLBLM_OK;
+}
+
+int clblm_gpu_set_lines(clblm_handle_t* h, const clblm_lines_t* lines) {
+  if (!h) return CLBLM_ERR_ARG;
+  cudaSetDevice(h->device);
+  return load_lines(h, lines);
+}
+
+int clblm_gpu_destroy(clblm_handle_t* h) {
+  if (!h) return CLBLM_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& b : h->lines) b.release();
+  DevBuf* bufs[] = {&h->cont_self, &h->cont_for, &h->cont_texp, &h->tabs,    &h->plans,  &h->vft,     &h->prep,
+                    &h->qpanel,    &h->rec,      &h->recd,      &h->ranges,  &h->od,     &h->r4,      &h->absrb,
+                    &h->stats,     &h->alfvmax,  &h->blockmax,  &h->nlines_d, &h->f4prep, &h->f4sh,
+                    &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
+                    &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
+                    &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
+                    &h->f4cut,     &h->f4grp};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& b : h->rt) b.release();
+  for (auto& b : h->imap) b.release();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CLBLM_OK;
+}
+
+const char* clblm_gpu_last_error(const clblm_handle_t* h) { return h ? h->errmsg.c_str() : g_create_err.c_str(); }
+
+void* clblm_gpu_stream(const clblm_handle_t* h) { return h ? (void*)h->stream : nullptr; }
+
+int clblm_setdv(const clblm_column_t* col, double sample, double alfal0, double alfal0_fine, int32_t grid_type,
+                double dv_user, double* dv_normal, double* dv_narrow, double* dv_out) {
+  if (!col || col->nlay < 1 || !dv_normal || !dv_narrow) return CLBLM_ERR_ARG;
+  const int n = col->nlay;
+  double V1 = col->v1, V2 = col->v2;
+  double Vbar = 0.5 * (V1 + V2);
+  if (V2 < V1) Vbar = V1;
+  int ih2o = -1;
+  for (int m = 0; m < col->nmol; ++m)
+    if (col->mol_id[m] == 1) ih2o = m;
+  // calculateDV, clblm_setDV.f90:221-272
+  auto calc = [&](double ALFAL0, double* DVC) {
+    for (int il = 0; il < n; ++il) {
+      double WTOTL = col->wtot[il];
+      double FRH2O = (ih2o >= 0 ? col->w[(size_t)il * col->nmol + ih2o] : 0.) / WTOTL;
+      double ALFCOR = (col->pave[il] / kP0) * std::sqrt(kT0 / col->tave[il]);
+      double H2OSLF = (1. - FRH2O + 5. * FRH2O);
+      double ALBAR = ALFAL0 * ALFCOR * H2OSLF;
+      double ADBAR = 3.58115E-07 * Vbar * std::sqrt(col->tave[il] / 36.0);
+      double AVBAR = 0.5 * (ALBAR + std::sqrt(ALBAR * ALBAR + 4. * ADBAR * ADBAR));
+      DVC[il] = AVBAR / sample;
+    }
+  };
+  // fixDVRatio, clblm_setDV.f90:277-351
+  auto fix = [&](double* DVo, const double* DVi) -> int {
+    double OLDDV = 0.;
+    for (int il = 1; il <= n; ++il) {
+      double DV = DVi[il - 1];
+      if (il == 1) {
+        int ISCAL = (int)(std::log10(DV) - 3.);
+        double SCAL = std::pow(10., (double)ISCAL);
+        int IDV = (int)((DV / SCAL) + 0.5);
+        if (IDV % 2 > 0) IDV = IDV + 1;
+        DV = SCAL * (double)IDV;
+      } else {
+        double TYPE = OLDDV / DV;
+        if (TYPE > 2.5) return CLBLM_ERR_DV_RATIO;
+        if (TYPE >= 1.2) {
+          int ITYPE = (int)(1. / (TYPE - 1.) + 0.5);
+          if (ITYPE == 3) ITYPE = 2;
+          DV = OLDDV * (double)ITYPE / (double)(ITYPE + 1);
+        } else {
+          DV = OLDDV;
+        }
+      }
+      OLDDV = DV;
+      DVo[il - 1] = DV;
+    }
+    return CLBLM_OK;
+  };
+  std::vector<double> dc(n), df(n);
+  calc(alfal0, dc.data());
+  calc(alfal0_fine, df.data());
+  std::copy(dc.begin(), dc.end(), dv_normal);
+  std::copy(df.begin(), df.end(), dv_narrow);
+  if (grid_type >= 0) {
+    if (grid_type == 0) {
+      int rc = fix(dv_normal, dc.data());
+      if (rc) return rc;
+      rc = fix(dv_narrow, df.data());
+      if (rc) return rc;
+    }
+    if (dv_user > 0.) {
+      if (std::fabs(1. - dv_user / dv_normal[n - 1]) < 0.2) {
+        double R = dv_user / dv_normal[n - 1];
+        for (int l = 0; l < n; ++l) dv_normal[l] = dv_normal[l] * R;
+      }
+      if (std::fabs(1. - dv_user / dv_narrow[n - 1]) < 0.2) {
+        double R = dv_user / dv_narrow[n - 1];
+        for (int l = 0; l < n; ++l) dv_narrow[l] = dv_narrow[l] * R;
+      }
+    }
+  }
+  if (dv_out) {
+    if (grid_type == 1) *dv_out = dv_user > 0. ? dv_user : *std::min_element(dv_narrow, dv_narrow + n);
+    else *dv_out = -999.9;
+  }
+  return CLBLM_OK;
+}
+
+int clblm_gpu_od_size(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid_t* grid,
+                      const clblm_od_ctrl_t* ctrl, int64_t* nsamp, double* dv_used) {
+  if (!h) return CLBLM_ERR_ARG;
+  HostPlan hp;
+  int jr;
+  int rc = plan_layer(h, layer, grid, ctrl, h->jrad, h->first_pass_jrad, &hp, &jr);
+  if (rc) return rc;
+  if (nsamp) *nsamp = hp.n_out;
+  if (dv_used) *dv_used = hp.dv_out;
+  return CLBLM_OK;
+}
+
+int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid_t* grid,
+                 const clblm_od_ctrl_t* ctrl, double* out, int64_t cap, int32_t flags) {
+  if (!h || !ctrl) return CLBLM_ERR_ARG;
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  std::vector<HostPlan> hps(1);
+  int jr;
+  int rc = plan_layer(h, layer, grid, ctrl, h->jrad, h->first_pass_jrad, &hps[0], &jr);
+  // the sticky JRAD is committed once the call gets past the grid checks,
+  // as the reference's SAVE is set before OPDPTH runs
+  if (rc == CLBLM_OK || rc == CLBLM_ERR_UNSUPPORTED) {
+    h->first_pass_jrad = false;
+    h->jrad = jr;
+  }
+  if (rc) return rc;
+  if (!out || cap < hps[0].n_out) return set_err(h, CLBLM_ERR_CAPACITY, "output needs %lld points", (long long)hps[0].n_out);
+  bool plain = ctrl->precision == CLBLM_PREC_PLAIN;
+  h->launches = 0;
+  int64_t ls, fs, ps, odt;
+  rc = prepare_batch(h, hps, 0, 1, plain, &ls, &fs, &ps, &odt);
+  if (rc) return rc;
+  rc = run_od_batch(h, hps, 0, 1, plain, ls, fs, ps);
+  if (rc) return rc;
+  const LayerPlan& P = hps[0].P;
+  int64_t n = hps[0].n_out;
+  double* dst = out;
+  if (flags != CLBLM_OUT_DEVICE) {
+    CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * n));
+    dst = h->outbuf.as<double>();
+  }
+  InterpSpec s = interp_spec(P.v1, P.dv, P.nsamp, P.v1, hps[0].dv_out, n);
+  rc = build_interp_map(h, &s, n, &h->imap[0]);
+  if (rc) return rc;
+  const void* od = plain ? (const void*)(h->od.as<double>() + P.od_off) : (const void*)(h->od.as<float>() + P.od_off);
+  h->launches++;
+  if (plain) k_od_out<true><<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(od, P.nsamp, s, n, dst);
+  else k_od_out<false><<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(od, P.nsamp, s, n, dst);
+  CUDA_TRY(h, cudaGetLastError());
+  if (flags != CLBLM_OUT_DEVICE)
+    CUDA_TRY(h, cudaMemcpyAsync(out, dst, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  rc = check_batch(h, hps, 0, 1, &h->last);
+  h->last.launches = h->launches;
+  return rc;
+}
+
+int clblm_gpu_od_stats(const clblm_handle_t* h, clblm_od_stats_t* stats) {
+  if (!h || !stats) return CLBLM_ERR_ARG;
+  *stats = h->last;
+  return CLBLM_OK;
+}
+
+}  // extern "C"
+
+// ---- nadir radiance ----------------------------------------------------------
+namespace {
+
+struct RtPlan {
+  std::vector<HostPlan> hps;
+  std::vector<clblm_layer_t> layers;
+  double dv0;
+  int64_t n0;
+  std::vector<double> grid_dv;   // merge grid after each layer
+  std::vector<int64_t> grid_n;
+  int jrad_after = 0;
+};
+
+int plan_column(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, RtPlan* rp) {
+  if (!col || !ctrl || col->nlay < 1) return set_err(h, CLBLM_ERR_ARG, "bad column");
+  const int n = col->nlay;
+  std::vector<double> dvn(n), dvf(n);
+  double dvo;
+  int rc = clblm_setdv(col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, ctrl->grid_type, ctrl->dv_user, dvn.data(),
+                       dvf.data(), &dvo);
+  if (rc == CLBLM_ERR_DV_RATIO) return set_err(h, rc, "layer DV ratio > 2.5");
+  if (rc) return set_err(h, rc, "setDV failed");
+  rp->hps.resize(n);
+  rp->layers.resize(n);
+  int jr = h->jrad;
+  bool fp = h->first_pass_jrad;
+  for (int il = 0; il < n; ++il) {
+    clblm_layer_t& L = rp->layers[il];
+    L.nmol = col->nmol;
+    L.mol_id = col->mol_id;
+    L.w = col->w + (size_t)il * col->nmol;
+    L.wtot = col->wtot[il];
+    L.pave = col->pave[il];
+    L.tave = col->tave[il];
+    L.zbot = L.ztop = 0.;
+    L.lay_no = il + 1;
+    clblm_grid_t g;
+    g.v1 = col->v1;
+    g.v2 = col->v2;
+    g.dv_normal = dvn[il];
+    g.dv_narrow = dvf[il];
+    g.dv_out = dvo;
+    g.sample = ctrl->sample;
+    g.alfal0 = ctrl->alfal0;
+    int jafter;
+    rc = plan_layer(h, &L, &g, &ctrl->od, jr, fp, &rp->hps[il], &jafter);
+    if (rc) return rc;
+    jr = jafter;
+    fp = false;
+  }
+  rp->jrad_after = jr;
+  rp->dv0 = dvn[0];
+  rp->n0 = (int64_t)std::ceil((col->v2 - col->v1) / rp->dv0 + 1.);
+  // merge grids: interpToFinestGrid (first minimum among merged, layer)
+  double gdv = rp->dv0;
+  int64_t gn = rp->n0;
+  rp->grid_dv.resize(n);
+  rp->grid_n.resize(n);
+  for (int il = 0; il < n; ++il) {
+    double ldv = rp->hps[il].dv_out;
+    int64_t ln = rp->hps[il].n_out;
+    if (ldv < gdv) {
+      gdv = ldv;
+      gn = ln;
+    }
+    rp->grid_dv[il] = gdv;
+    rp->grid_n[il] = gn;
+  }
+  return CLBLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clblm_gpu_rt_mode2_size(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl,
+                            int64_t* npts, double* dv) {
+  if (!h) return CLBLM_ERR_ARG;
+  RtPlan rp;
+  int rc = plan_column(h, col, ctrl, &rp);
+  if (rc) return rc;
+  if (npts) *npts = rp.grid_n.back();
+  if (dv) *dv = rp.grid_dv.back();
+  return CLBLM_OK;
+}
+
+int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, double* rad,
+                       int64_t cap, int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  if (!col || !col->tbot || !col->ttop || !col->wtot_down) return set_err(h, CLBLM_ERR_ARG, "bad column");
+  RtPlan rp;
+  int rc = plan_column(h, col, ctrl, &rp);
+  if (rc == CLBLM_OK || rc == CLBLM_ERR_UNSUPPORTED) {
+    h->first_pass_jrad = false;
+    h->jrad = rp.jrad_after;
+  }
+  if (rc) return rc;
+  const int n = col->nlay;
+  int64_t nfinal = rp.grid_n.back();
+  if (!rad || cap < nfinal) return set_err(h, CLBLM_ERR_CAPACITY, "radiance needs %lld points", (long long)nfinal);
+  bool plain = ctrl->od.precision == CLBLM_PREC_PLAIN;
+  h->launches = 0;
+  size_t real = plain ? 8 : 4;
+  int64_t maxn = rp.n0;
+  for (int il = 0; il < n; ++il) maxn = std::max(maxn, rp.grid_n[il]);
+  for (auto& b : h->rt) CUDA_TRY(h, b.ensure(real * (maxn + 8)));
+  // layers in batches sized to the workspace budget
+  const size_t budget = (size_t)24 << 30;
+  int cur = 0;  // ping-pong index of the merged spectra
+  for (int first = 0; first < n;) {
+    int count = 0;
+    size_t bytes = 0;
+    while (first + count < n) {
+      const LayerPlan& P = rp.hps[first + count].P;
+      size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
+                 (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+      if (count > 0 && bytes + b > budget) break;
+      bytes += b;
+      count++;
+    }
+    int64_t ls, fs, ps, odt;
+    rc = prepare_batch(h, rp.hps, first, count, plain, &ls, &fs, &ps, &odt);
+    if (rc) return rc;
+    rc = run_od_batch(h, rp.hps, first, count, plain, ls, fs, ps);
+    if (rc) return rc;
+    for (int il = first; il < first + count; ++il) {
+      const LayerPlan& P = rp.hps[il].P;
+      RtLayerArgs a;
+      std::memset(&a, 0, sizeof a);
+      double in_dv = il == 0 ? rp.dv0 : rp.grid_dv[il - 1];
+      int64_t in_n = il == 0 ? rp.n0 : rp.grid_n[il - 1];
+      a.n_out = rp.grid_n[il];
+      a.v1 = col->v1;
+      a.mr = interp_spec(col->v1, in_dv, in_n, col->v1, rp.grid_dv[il], rp.grid_n[il]);
+      rc = build_interp_map(h, &a.mr, a.n_out, &h->imap[0]);
+      if (rc) return rc;
+      // layer spectra on the OD grid (DV, nsamp) or the DVout grid
+      double odv = rp.hps[il].dv_out;
+      int64_t onn = rp.hps[il].n_out;
+      if (std::fabs(odv - P.dv) >= 2.220446049250313e-16)
+        return set_err(h, CLBLM_ERR_UNSUPPORTED, "uniform DVout grids in the radiance path are not on this path");
+      a.ly = interp_spec(col->v1, odv, onn, col->v1, rp.grid_dv[il], rp.grid_n[il]);
+      rc = build_interp_map(h, &a.ly, a.n_out, &h->imap[1]);
+      if (rc) return rc;
+      a.rad_in = h->rt[cur * 2].p;
+      a.refl_in = h->rt[cur * 2 + 1].p;
+      a.rad_out = h->rt[(1 - cur) * 2].p;
+      a.refl_out = h->rt[(1 - cur) * 2 + 1].p;
+      a.od = plain ? (const void*)(h->od.as<double>() + P.od_off) : (const void*)(h->od.as<float>() + P.od_off);
+      a.n_od = P.nsamp;
+      a.dv_od = P.dv;
+      a.scal_up = col->wtot[il] / col->wtot[il];
+      a.scal_dn = col->wtot_down[il] / col->wtot[il];
+      a.tbot = col->tbot[il];
+      a.ttop = col->ttop[il];
+      a.tave = col->tave[il];
+      a.lin_in_tau = ctrl->lin_in_tau;
+      a.first = il == 0;
+      a.tskin = col->tskin;
+      a.emis = col->emis;
+      a.xt0 = (float)(col->v1 * (kRADCN2 / col->ttop[il]));
+      a.xt1 = (float)(P.dv * (kRADCN2 / col->ttop[il]));
+      a.xb0 = (float)(col->v1 * (kRADCN2 / col->tbot[il]));
+      a.xb1 = (float)(P.dv * (kRADCN2 / col->tbot[il]));
+      a.xa0 = (float)(col->v1 * (kRADCN2 / col->tave[il]));
+      a.xa1 = (float)(P.dv * (kRADCN2 / col->tave[il]));
+      a.vf0 = (float)col->v1;
+      a.vf1 = (float)P.dv;
+      a.xs0 = (float)(col->v1 * (kRADCN2 / col->tskin));
+      a.xs1 = (float)(in_dv * (kRADCN2 / col->tskin));
+      unsigned grid = (unsigned)((a.n_out + 255) / 256);
+      h->launches++;
+      if (plain) k_rt_layer<true><<<grid, 256, 0, h->stream>>>(a);
+      else k_rt_layer<false><<<grid, 256, 0, h->stream>>>(a);
+      CUDA_TRY(h, cudaGetLastError());
+      cur = 1 - cur;
+    }
+    rc = check_batch(h, rp.hps, first, count, &h->last);
+    if (rc) return rc;
+    first += count;
+  }
+  // binary64 radiance out
+  CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * nfinal));
+  InterpSpec same;
+  std::memset(&same, 0, sizeof same);
+  same.kind = 0;
+  double* dst = flags == CLBLM_OUT_DEVICE ? rad : h->outbuf.as<double>();
+  h->launches++;
+  if (plain) k_od_out<true><<<(unsigned)((nfinal + 255) / 256), 256, 0, h->stream>>>(h->rt[cur * 2].p, nfinal, same, nfinal, dst);
+  else k_od_out<false><<<(unsigned)((nfinal + 255) / 256), 256, 0, h->stream>>>(h->rt[cur * 2].p, nfinal, same, nfinal, dst);
+  CUDA_TRY(h, cudaGetLastError());
+  if (flags != CLBLM_OUT_DEVICE)
+    CUDA_TRY(h, cudaMemcpyAsync(rad, dst, sizeof(double) * nfinal, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
+}  // extern "C"

@@ -172,6 +172,7 @@ typedef struct {
   double  dv;          /* DV of the convolution                                */
   double  dvr4;        /* DV of the far-wing grid                              */
   int32_t jrad;        /* JRAD in effect                                       */
+  int64_t launches;    /* device kernels launched by the last OD/radiance call */
 } clblm_od_stats_t;
 
 typedef struct clblm_handle clblm_handle_t;
@@ -215,6 +216,10 @@ int clblm_gpu_od_size(clblm_handle_t *h, const clblm_layer_t *layer,
 int clblm_gpu_od(clblm_handle_t *h, const clblm_layer_t *layer,
                  const clblm_grid_t *grid, const clblm_od_ctrl_t *ctrl,
                  double *out, int64_t cap, int32_t flags);
+
+/* The CUDA stream (a cudaStream_t) all work of the handle runs on, for
+ * callers that order their own work or time with events on it. */
+void *clblm_gpu_stream(const clblm_handle_t *h);
 
 /* Counters of the last clblm_gpu_od (or of the last layer of clblm_gpu_rt_mode2). */
 int clblm_gpu_od_stats(const clblm_handle_t *h, clblm_od_stats_t *stats);

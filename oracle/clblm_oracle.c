@@ -1493,6 +1493,23 @@ static int od_grid(const clblm_grid_t *g, double *DV, double *ALFAV) {
   return 0;
 }
 
+static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
+                      const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, int JRAD, double *out, int64_t cap,
+                      int64_t *nsamp, double *dv_used, clblm_od_stats_t *st);
+
+/* JRAD after this layer's OPDPTH: the first call takes odCtrl%JRAD, and
+ * OPDPTH sets it to 0 for good when V1/kT < 5 (clblm_ODLAY.f90:349-352, :877-878). */
+static int sticky_jrad(ocl_session *s, const clblm_layer_t *lay, const clblm_grid_t *g,
+                       const clblm_od_ctrl_t *ctrl) {
+  if (s->first_pass_jrad) {
+    s->jrad = ctrl->jrad;
+    s->first_pass_jrad = 0;
+  }
+  double XKT = lay->tave / RADCN2;
+  if (((g->v1 / XKT) < 5.) && (s->jrad != -1)) s->jrad = 0;
+  return s->jrad;
+}
+
 int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
               const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, double *out, int64_t cap, int64_t *nsamp,
               double *dv_used, clblm_od_stats_t *st) {
@@ -1502,10 +1519,15 @@ int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, con
   if (od_grid(g, &DV, &ALFAV)) return fail(s, CLBLM_ERR_GRID, "bad grid");
   for (int64_t i = 1; i < L->n; ++i)
     if (L->vnu[i] < L->vnu[i - 1]) return fail(s, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
-  if (s->first_pass_jrad) {
-    s->jrad = ctrl->jrad;
-    s->first_pass_jrad = 0;
-  }
+  int JRAD = sticky_jrad(s, lay, g, ctrl);
+  return odlay_core(s, L, C, lay, g, ctrl, JRAD, out, cap, nsamp, dv_used, st);
+}
+
+static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
+                      const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, int JRAD, double *out, int64_t cap,
+                      int64_t *nsamp, double *dv_used, clblm_od_stats_t *st) {
+  double DV, ALFAV;
+  if (od_grid(g, &DV, &ALFAV)) return fail(s, CLBLM_ERR_GRID, "bad grid");
   clblm_od_stats_t stl;
   memset(&stl, 0, sizeof stl);
   molec_t M;
@@ -1525,10 +1547,7 @@ int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, con
     /* accepted: the oracle follows the per-block R4 rule literally */
   }
 
-  /* OPDPTH */
-  double XKT = TAVE / RADCN2;
-  if (((V1 / XKT) < 5.) && (s->jrad != -1)) s->jrad = 0;
-  int JRAD = s->jrad;
+  /* OPDPTH (JRAD already reduced by its V1/kT < 5 rule) */
   double *ABSRBb = NULL;
   double DVABS = 0., V1ABS = 0., V2ABS = 0.;
   if (!ctrl->contnm_off) {
@@ -1821,8 +1840,9 @@ static int to_finest(ocl_session *s, spect_t **sp, int nsp) {
   return 0;
 }
 
-int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_column_t *col,
-                 const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap, int64_t *npts, double *dvp) {
+static int rt_mode2_impl(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
+                         const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap,
+                         int64_t *npts, double *dvp, int nthreads) {
   int n = col->nlay;
   if (n < 1) return fail(s, CLBLM_ERR_ARG, "no layers");
   double *dvn = (double *)malloc(sizeof(double) * n), *dvf = (double *)malloc(sizeof(double) * n);
@@ -1835,6 +1855,45 @@ int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, 
     return rc;
   }
   double V1 = col->v1, V2 = col->v2;
+  /* layers, grids and the sticky JRAD each layer's ODLAY call sees */
+  clblm_layer_t *lays = (clblm_layer_t *)calloc(n, sizeof(clblm_layer_t));
+  clblm_grid_t *gs = (clblm_grid_t *)calloc(n, sizeof(clblm_grid_t));
+  int *jr = (int *)calloc(n, sizeof(int));
+  double **ods = (double **)calloc(n, sizeof(double *));
+  int64_t *nss = (int64_t *)calloc(n, sizeof(int64_t));
+  double *dvls = (double *)calloc(n, sizeof(double));
+  int *rcs = (int *)calloc(n, sizeof(int));
+  for (int il = 0; il < n; ++il) {
+    clblm_layer_t *lay = &lays[il];
+    lay->nmol = col->nmol;
+    lay->mol_id = col->mol_id;
+    lay->w = col->w + (size_t)il * col->nmol;
+    lay->wtot = col->wtot[il];
+    lay->pave = col->pave[il];
+    lay->tave = col->tave[il];
+    lay->lay_no = il + 1;
+    clblm_grid_t *g = &gs[il];
+    g->v1 = V1;
+    g->v2 = V2;
+    g->dv_normal = dvn[il];
+    g->dv_narrow = dvf[il];
+    g->dv_out = dvo;
+    g->sample = ctrl->sample;
+    g->alfal0 = ctrl->alfal0;
+    jr[il] = sticky_jrad(s, lay, g, &ctrl->od);
+  }
+  ensure_tables(s);
+  interp_coef(s);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int il = 0; il < n; ++il) {
+    ocl_session loc = *s; /* tables and coefficients are read-only from here */
+    int64_t capn = (int64_t)ceil((V2 - V1) / (dvn[il] < dvf[il] ? dvn[il] : dvf[il]) + 16.);
+    ods[il] = (double *)malloc(sizeof(double) * (size_t)capn);
+    rcs[il] = odlay_core(&loc, L, C, &lays[il], &gs[il], &ctrl->od, jr[il], ods[il], capn, &nss[il], &dvls[il],
+                         NULL);
+    if (rcs[il]) memcpy(s->err, loc.err, sizeof s->err);
+  }
+  for (int il = 0; il < n && !rc; ++il) rc = rcs[il];
   double DV = dvn[0];
   int64_t initNLIM = (int64_t)ceil((V2 - V1) / DV + 1.);
   spect_t R = {0}, Rf = {0}, TA = {0}, TB = {0}, EU = {0}, ED = {0};
@@ -1848,34 +1907,12 @@ int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, 
       Rf.v[j - 1] = 1.0 - col->emis;
     }
   }
-  double *od = NULL;
   for (int il = 0; il < n && !rc; ++il) {
-    clblm_layer_t lay;
-    lay.nmol = col->nmol;
-    lay.mol_id = col->mol_id;
-    lay.w = col->w + (size_t)il * col->nmol;
-    lay.wtot = col->wtot[il];
-    lay.pave = col->pave[il];
-    lay.tave = col->tave[il];
-    lay.zbot = 0.;
-    lay.ztop = 0.;
-    lay.lay_no = il + 1;
-    clblm_grid_t g;
-    g.v1 = V1;
-    g.v2 = V2;
-    g.dv_normal = dvn[il];
-    g.dv_narrow = dvf[il];
-    g.dv_out = dvo;
-    g.sample = ctrl->sample;
-    g.alfal0 = ctrl->alfal0;
-    int64_t ns = 0;
-    double dvl = 0.;
-    int64_t capn = (int64_t)ceil((V2 - V1) / (dvn[il] < dvf[il] ? dvn[il] : dvf[il]) + 16.);
-    od = (double *)realloc(od, sizeof(double) * (size_t)capn);
-    rc = ocl_odlay(s, L, C, &lay, &g, &ctrl->od, od, capn, &ns, &dvl, NULL);
-    if (rc) break;
-    double scalUp = col->wtot[il] / lay.wtot;
-    double scalDn = col->wtot_down[il] / lay.wtot;
+    double *od = ods[il];
+    int64_t ns = nss[il];
+    double dvl = dvls[il];
+    double scalUp = col->wtot[il] / lays[il].wtot;
+    double scalDn = col->wtot_down[il] / lays[il].wtot;
     spect_set(&TA, V1, dvl, ns);
     spect_set(&TB, V1, dvl, ns);
     spect_set(&EU, V1, dvl, ns);
@@ -1910,7 +1947,14 @@ int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, 
       else memcpy(rad, R.v, sizeof(double) * (size_t)R.n);
     }
   }
-  free(od);
+  for (int il = 0; il < n; ++il) free(ods[il]);
+  free(ods);
+  free(nss);
+  free(dvls);
+  free(rcs);
+  free(jr);
+  free(gs);
+  free(lays);
   free(R.v);
   free(Rf.v);
   free(TA.v);
@@ -1920,4 +1964,15 @@ int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, 
   free(dvn);
   free(dvf);
   return rc;
+}
+
+int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_column_t *col,
+                 const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap, int64_t *npts, double *dvp) {
+  return rt_mode2_impl(s, L, C, col, ctrl, rad, cap, npts, dvp, 1);
+}
+
+int ocl_rt_mode2_par(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_column_t *col,
+                     const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap, int64_t *npts, double *dvp,
+                     int nthreads) {
+  return rt_mode2_impl(s, L, C, col, ctrl, rad, cap, npts, dvp, nthreads);
 }

@@ -43,6 +43,12 @@ int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
                  const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl,
                  double *rad, int64_t cap, int64_t *npts, double *dv);
 
+/* The same with the layer optical depths computed on `nthreads` OpenMP
+ * threads (the merge stays sequential): the CPU baseline. */
+int ocl_rt_mode2_par(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
+                     const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl, double *rad,
+                     int64_t cap, int64_t *npts, double *dv, int nthreads);
+
 /* Building blocks exposed for known-answer tests. */
 void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg,
                       double *xver); /* each [3001] */

@@ -49,6 +49,9 @@ def lib():
         L.ocl_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
                                    P(T.clblm_rt_ctrl_t), P(C.c_double), C.c_int64, P(C.c_int64),
                                    P(C.c_double)]
+        L.ocl_rt_mode2_par.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
+                                       P(T.clblm_rt_ctrl_t), P(C.c_double), C.c_int64, P(C.c_int64),
+                                       P(C.c_double), C.c_int]
         L.ocl_setdv.argtypes = [C.c_void_p, P(T.clblm_column_t), C.c_double, C.c_double, C.c_double,
                                 C.c_int32, C.c_double, P(C.c_double), P(C.c_double), P(C.c_double)]
         L.ocl_shape_tables.argtypes = [P(C.c_double)] * 5
@@ -107,20 +110,20 @@ class Session:
         self._check(rc)
         return out[:ns.value].copy(), dv.value, st.as_dict()
 
-    def rt_mode2(self, lines, col, ctrl, cont=None):
+    def rt_mode2(self, lines, col, ctrl, cont=None, nthreads=1, cap=None):
+        """Radiance of a fresh reference process (the sticky JRAD is reset)."""
         ls, cols = lines.struct(), col.struct()
         cs = cont.struct() if cont is not None else None
         n, dv = C.c_int64(), C.c_double()
-        rc = lib().ocl_rt_mode2(self.h, C.byref(ls), C.byref(cs) if cs is not None else None,
-                                C.byref(cols), C.byref(ctrl), None, 0, C.byref(n), C.byref(dv))
-        if rc not in (0, T.CLBLM_ERR_CAPACITY):
-            self._check(rc)
+        if cap is None:
+            dn, df, _ = self.setdv(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, ctrl.grid_type, ctrl.dv_user)
+            cap = int(np.ceil((col.v2 - col.v1) / min(dn.min(), df.min()))) + 64
+        out = np.zeros(cap)
         self.reset()
-        out = np.zeros(n.value)
-        self._check(lib().ocl_rt_mode2(self.h, C.byref(ls), C.byref(cs) if cs is not None else None,
-                                       C.byref(cols), C.byref(ctrl), _dp(out), n.value, C.byref(n),
-                                       C.byref(dv)))
-        return out, dv.value
+        self._check(lib().ocl_rt_mode2_par(self.h, C.byref(ls), C.byref(cs) if cs is not None else None,
+                                           C.byref(cols), C.byref(ctrl), _dp(out), cap, C.byref(n),
+                                           C.byref(dv), int(nthreads)))
+        return out[:n.value].copy(), dv.value
 
 
 def shape_tables():

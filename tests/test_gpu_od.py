@@ -1,0 +1,59 @@
+"""Layer optical depth on the GPU against the FP64 oracle (ODLAY_nonStruct)."""
+import numpy as np
+import pytest
+
+from clblm_gb300 import capi_types as T
+from clblm_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _layer_case(n_lines, v1, v2, seed, mols=(1,), pave=1013.25, tave=296.0, wabs=1e22, wtot=2.479e24):
+    lines = synth.line_list(n_lines, v1, v2, seed=seed, mols=mols)
+    mol = np.array(mols, np.int32)
+    w = np.full((1, len(mols)), wabs)
+    col = T.Column(mol, [pave], [tave], [tave], [tave], w, [wtot], [1.67 * wtot], v1, v2, tave, 1.0)
+    return lines, col
+
+
+def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision=T.CLBLM_PREC_MIXED):
+    dn, df, _ = gpu_lib.setDV(col)
+    lay = col.layer(0)
+    g = T.grid_struct(col.v1, col.v2, dn[0], df[0])
+    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off)
+    h = gpu_lib.Handle(lines, cont)
+    od, dv = h.odlay(lay, g, ctrl)
+    st = h.stats()
+    h.close()
+    ref, dvr, sr = oracle_mod.Session().odlay(lines, lay, g, ctrl, cont)
+    assert dv == dvr
+    assert len(od) == len(ref)
+    for k in ("nlin", "lincnt", "nminus", "nplus", "nshrunk", "npanels", "nsamp"):
+        assert st[k] == sr[k], (k, st[k], sr[k])
+    return od, ref
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+def test_config0_full(gpu_lib, oracle_mod, precision, tol):
+    lines, col = synth.config0()
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
+
+
+def test_continuum_and_seven_absorbers(gpu_lib, oracle_mod):
+    lines, col, cont = synth.config1(n_lines=20000)
+    lines = lines.window(900.0, 1000.0)
+    col = col.sub([5]).with_window(900.0, 1000.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= 1e-5, rel
+
+
+@pytest.mark.parametrize("layer", [0, 30, 59])
+def test_config1_layers_narrow_window(gpu_lib, oracle_mod, layer):
+    lines, col, cont = synth.config1(n_lines=50000)
+    col = col.sub([layer]).with_window(1000.0, 1040.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= 1e-5, rel
