@@ -2,7 +2,9 @@
 
 Translation units are compiled in parallel; prep.cu, whose FP64 index
 arithmetic must round every product and sum separately, is compiled with
---fmad=false.
+--fmad=false.  Host code is compiled with -ffp-contract=off everywhere: the
+planning arithmetic (panel and block bounds, grid restarts) must round like
+the reference's, and GCC on aarch64 would otherwise fuse a + b*c.
 """
 import os
 import shutil
@@ -33,8 +35,8 @@ def nvcc():
 
 def _compile(src, extra, verbose_ptxas=False):
     obj = BUILD / (Path(src).stem + ".o")
-    cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-rdc=true",
-           "-I", str(CSRC), "-I", str(HERE.parent / "include"), *extra, "-c", str(CSRC / src),
+    cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "-rdc=true", "-I", str(CSRC), "-I", str(HERE.parent / "include"), *extra, "-c", str(CSRC / src),
            "-o", str(obj)]
     if verbose_ptxas:
         cmd.insert(1, "-Xptxas=-v")

@@ -93,19 +93,21 @@ __global__ void k_interp_map(InterpSpec s, const int64_t* __restrict__ blk_j1, c
                              int nblk, int64_t nout, int2* __restrict__ map) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblk) return;
+  // every product and sum rounded on its own (no FMA contraction): a fused
+  // v1 + (iIn-1)*dvin moves P by ~1e-10 and flips the carry at coincidences
   const double Vo = blk_vo[b];
-  int64_t iIn = (int64_t)((Vo - s.v1) / s.dvin + 1.00001);
-  double Vi = s.v1 + (double)(iIn - 1) * s.dvin;
-  double P = (Vo - Vi) / s.dvin;
+  int64_t iIn = (int64_t)__dadd_rn(__ddiv_rn(__dadd_rn(Vo, -s.v1), s.dvin), 1.00001);
+  double Vi = __dadd_rn(s.v1, __dmul_rn((double)(iIn - 1), s.dvin));
+  double P = __ddiv_rn(__dadd_rn(Vo, -Vi), s.dvin);
   const int64_t J1 = blk_j1[b];
   const int64_t J2 = min(nout, J1 + 2400 - 1);
   for (int64_t J = J1; J <= J2; ++J) {
-    int IP = (int)(P * 201. + 1.00001);
+    int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
     map[J - 1] = make_int2((int)iIn, IP < 0 ? 0 : (IP > 202 ? 202 : IP));
-    P = P + s.ratio;
+    P = __dadd_rn(P, s.ratio);
     if (P >= 1.0) {
-      iIn = (int64_t)((double)iIn + P);
-      P = P - (double)((int64_t)P);
+      iIn = (int64_t)__dadd_rn((double)iIn, P);
+      P = __dadd_rn(P, -(double)((int64_t)P));
     }
   }
 }
