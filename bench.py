@@ -39,6 +39,22 @@ UNIT = "layer-points/s"
 WORKLOAD = "60-layer nadir radiance, 500000 lines (7 absorbers), 500-2500 cm-1, synthetic continuum"
 
 
+def max_over_ranks(ms, device):
+    """Slowest rank's time: every rank runs a full replica of the workload."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(points_per_replica, world, ms):
+    """Whole-job throughput of `world` replicas finishing within `ms`."""
+    return points_per_replica * world / (ms * 1e-3)
+
+
 def layer_points(h, col, ctrl):
     """Sum over layers of the points ODLAY returns on each layer grid."""
     from clblm_gb300 import capi
@@ -227,12 +243,8 @@ def main():
             step_dev()
         ev1.record(stream)
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = lp * world / (ms * 1e-3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, "cuda")
+    value = replica_value(lp, world, ms)
 
     # e2e through the C-ABI with host buffers
     plines = pinned_lines(lines)

@@ -3,6 +3,17 @@
  * (ODLAY) and nadir radiance (mode2) path.
  *
  * TEST INFRASTRUCTURE: this is the oracle the GPU path is checked against.
+ *
+ * PARITY UNPINNED.  The reference ships no tests, golden vectors or fixtures
+ * for this path, and its Fortran cannot be compiled or run beside this code,
+ * so nothing the reference itself computed pins this restatement.  What pins
+ * it is the reference's own data: the constant tables are extracted from its
+ * source at build time (clblm_gb300/csrc/gen_ref_tables.py), the MT_CKD
+ * table slice under tests/golden is read from its data file, and the
+ * known-answer tests under tests/ check the mathematics (line-shape
+ * normalisation, Planck and radiation-term limits, partition-sum ratio 1 at
+ * 296 K, exact interpolation of low-order polynomials).
+ *
  * It is compiled with -ffp-contract=off so that, like the reference's stock
  * unoptimised gfortran build (Makefile:28, -fdefault-real-8 -g), every
  * product and sum is rounded separately.  Default REAL of the reference is
@@ -1480,6 +1491,29 @@ int ocl_interp_spectrum(const double *in, double dvin, double v1in, int64_t nin,
   ocl_session tmp;
   memset(&tmp, 0, sizeof tmp);
   return interp_spectrum(&tmp, in, dvin, v1in, nin, out, dvout, v1out, nout);
+}
+
+/* The H2O continuum on OPDPTH's 1 cm-1 ABSRB grid (clblm_ODLAY.f90:880-896,
+ * CONTNM clblm_ODLAY_Continuum.f90:355-405): a known-answer helper that
+ * restates the set-up odlay_core performs before contnm_h2o. */
+int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double V1, double V2, double PAVE, double TAVE, double Wtot,
+                   double WK1, double xself, double xfrgn, double *absrb, double *v1abs, int *nptabs) {
+  ocl_session tmp;
+  memset(&tmp, 0, sizeof tmp);
+  double DVABS = 1.;
+  double V1ABS = (double)(int)V1;
+  if (V1 < 0.) V1ABS = V1ABS - 1.;
+  V1ABS = V1ABS - 3. * DVABS;
+  double V2ABS = (double)(int)(V2 + 3. * DVABS + 0.5);
+  int NPTABS = (int)((V2ABS - V1ABS) / DVABS + 1.5);
+  if (NPTABS > N_ABSRB - 4) return CLBLM_ERR_RANGE;
+  double *A = (double *)calloc(N_ABSRB + 8, sizeof(double));
+  int rc = contnm_h2o(&tmp, C, jrad, V1ABS, V2ABS, DVABS, A, xself, xfrgn, V1, V2, PAVE, TAVE, Wtot, WK1);
+  if (!rc) memcpy(absrb, A + 1, sizeof(double) * N_ABSRB);
+  free(A);
+  *v1abs = V1ABS;
+  *nptabs = NPTABS;
+  return rc;
 }
 
 /* ======================================================================

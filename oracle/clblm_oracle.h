@@ -56,6 +56,10 @@ double ocl_radfn(double vi, double xkt);
 double ocl_planck(double v, double xkt);
 void ocl_rlin(double od, double *hlf);
 int ocl_tips_scor(int mol, double t, double *scor);
+/* ABSRB(1..5050) of the H2O continuum on OPDPTH's 1 cm-1 grid starting at *v1abs */
+int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double v1, double v2, double pave,
+                   double tave, double wtot, double wk1, double xself, double xfrgn,
+                   double *absrb, double *v1abs, int *nptabs);
 int ocl_interp_spectrum(const double *in, double dvin, double v1in,
                         int64_t nin, double *out, double dvout, double v1out,
                         int64_t nout);

@@ -63,6 +63,8 @@ def lib():
         L.ocl_tips_scor.argtypes = [C.c_int, C.c_double, P(C.c_double)]
         L.ocl_interp_spectrum.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, P(C.c_double),
                                           C.c_double, C.c_double, C.c_int64]
+        L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
+                                                                                    P(C.c_double), P(C.c_int)]
         _lib = L
     return _lib
 
@@ -161,3 +163,18 @@ def interp_spectrum(spin, dvin, v1in, dvout, v1out, nout):
     if rc:
         raise OracleError(rc, "interp")
     return out
+
+
+N_ABSRB = 5050
+
+
+def contnm_h2o(cont, v1, v2, pave, tave, wtot, wk1, jrad=0, xself=1.0, xfrgn=1.0):
+    """(V1ABS, ABSRB[:NPTABS]) of the H2O continuum on OPDPTH's 1 cm-1 grid."""
+    out = np.zeros(N_ABSRB)
+    v1abs, npt = C.c_double(), C.c_int()
+    cs = cont.struct()
+    rc = lib().ocl_contnm_h2o(C.byref(cs), int(jrad), v1, v2, pave, tave, wtot, wk1, xself, xfrgn, _dp(out),
+                              C.byref(v1abs), C.byref(npt))
+    if rc:
+        raise OracleError(rc, "contnm_h2o")
+    return v1abs.value, out[:npt.value].copy()

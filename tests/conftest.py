@@ -25,3 +25,17 @@ def gpu_lib():
     B.build()
     from clblm_gb300 import capi
     return capi
+
+
+GOLDEN = ROOT / "tests" / "golden"
+
+
+@pytest.fixture(scope="session")
+def mtckd():
+    """The reference's MT_CKD H2O table, 0-3000 cm-1 (tests/golden)."""
+    import numpy as np
+    from clblm_gb300.capi_types import Continuum
+    z = np.load(GOLDEN / "mtckd_h2o_0_3000.npz")
+    wv = z["wavenumbers"]
+    return Continuum(wv[0], wv[1] - wv[0], z["self_absco_ref"], z["for_absco_ref"], z["self_texp"],
+                     float(z["ref_press"]), float(z["ref_temp"]))

@@ -57,3 +57,17 @@ def test_config1_layers_narrow_window(gpu_lib, oracle_mod, layer):
     od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0)
     rel = np.max(np.abs(od - ref) / np.abs(ref))
     assert rel <= 1e-5, rel
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+@pytest.mark.parametrize("layer", [0, 12])
+def test_reference_mtckd_table(gpu_lib, oracle_mod, mtckd, precision, tol, layer):
+    """The H2O continuum from the reference's own MT_CKD table (golden fixture)
+    on a water-rich lower layer, 1300-1400 cm-1 (the 6.3 um band wing).  A
+    sparse line list (500 lines on 500-2500 cm-1) leaves the continuum up to
+    99 % of the layer OD between lines."""
+    lines, col, _ = synth.config1(n_lines=500)
+    col = col.sub([layer]).with_window(1300.0, 1400.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=mtckd, contnm_off=0, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
