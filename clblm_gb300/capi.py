@@ -21,7 +21,9 @@ LIB_PATH = HERE / "libclblm_gb300.so"
 EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clblm_gpu_last_error",
            "clblm_gpu_stream",
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
-           "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2")
+           "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_interp_spectrum_noalloc")
+
+NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
 
 class ClblmError(RuntimeError):
@@ -60,6 +62,8 @@ def lib():
                                               P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), C.c_void_p,
                                          C.c_int64, C.c_int32]
+        L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
+                                                        C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
         _lib = L
     return _lib
 
@@ -175,3 +179,16 @@ def ODLAY(handle, layer, grid, ctrl):
 def mode2_lookDn_mergeUp(handle, col, ctrl):
     """totalRadUp of mode2_lookDn_mergeUp (clblm_noScattRT.f90:1134)."""
     return handle.rt_mode2(col, ctrl)
+
+
+def interp_spectrum_noalloc(d_in, nin, v1, dvin, d_out, nout, dvout, stream=0):
+    """Device spectrum (v1, dvin, nin) -> (v1, dvout, nout) with interpSpectrum's
+    rules, allocating no device memory (clblm_gpu_interp_spectrum_noalloc).
+
+    d_in, d_out: device addresses (e.g. torch tensor data_ptr()); stream: a
+    cudaStream_t as an int.  The work is queued, not waited for.  Calls share
+    one scratch array per device: order them on one stream."""
+    rc = lib().clblm_gpu_interp_spectrum_noalloc(C.c_void_p(d_in), nin, v1, dvin, C.c_void_p(d_out), nout,
+                                                 dvout, C.c_void_p(stream))
+    if rc:
+        raise ClblmError(rc, "clblm_gpu_interp_spectrum_noalloc")

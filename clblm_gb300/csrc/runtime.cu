@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1368,3 +1369,105 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
 }
 
 }  // extern "C"
+
+// ---- grid interpolation without device allocation ---------------------------
+//
+// For callers that cannot call cudaMalloc: a host model that hands its device
+// memory to the library only through a fixed pool it owns, code that runs
+// while another component is capturing or replaying work on the device, and
+// callers for which a failed allocation in mid-run is not an option.  The
+// per-point (iIn, IP) map of the general-ratio case, which the handle path
+// keeps in a workspace it allocates, lives here in one file-scope device
+// array that every GPU loading the library holds until the process exits.
+namespace {
+
+constexpr int64_t kNoAllocBlocks = CLBLM_NOALLOC_MAX_POINTS / 2400 + 8;
+constexpr size_t kNoAllocMapBytes = sizeof(int2) * (size_t)CLBLM_NOALLOC_MAX_POINTS;
+constexpr size_t kNoAllocBytes = kNoAllocMapBytes + 16 * (size_t)kNoAllocBlocks;
+static_assert(kNoAllocBytes == (size_t)CLBLM_NOALLOC_SCRATCH_BYTES, "scratch size of the header");
+
+// map[CLBLM_NOALLOC_MAX_POINTS] (int2), then the block starts J1 (int64) and
+// their wavenumbers Vo (double), kNoAllocBlocks of each
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices];
+
+// Once per device, with that device current: the device address of the
+// scratch array (its host-side name is only a stand-in) and the 201-point
+// interpolation coefficients in constant memory.
+cudaError_t noalloc_setup(int dev, unsigned char** ptr) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev]) {
+    *ptr = g_noalloc_ptr[dev];
+    return cudaSuccess;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  rt_upload_interp_coef(0);
+  e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) return e;
+  g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+  *ptr = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+bool is_device_pointer(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin, double v1, double dvin,
+                                                 double* d_out, int64_t nout, double dvout, void* stream) {
+  if (!d_in || !d_out || nin < 2 || nout < 1 || nin > INT32_MAX - 8) return CLBLM_ERR_ARG;
+  if (!(dvin > 0.) || !(dvout > 0.) || !std::isfinite(v1)) return CLBLM_ERR_GRID;
+  if (nout > CLBLM_NOALLOC_MAX_POINTS) return CLBLM_ERR_CAPACITY;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return CLBLM_ERR_NO_DEVICE;
+  if (!is_device_pointer(d_in) || !is_device_pointer(d_out)) return CLBLM_ERR_ARG;
+  unsigned char* base = nullptr;
+  if (noalloc_setup(dev, &base) != cudaSuccess) return CLBLM_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  InterpSpec s = interp_spec(v1, dvin, nin, v1, dvout, nout);
+  if (s.kind != 0 && s.itype < 0) {
+    // block starts of interpSpectrum's outer loop, as build_interp_map
+    int64_t j1[kNoAllocBlocks];
+    double vo[kNoAllocBlocks];
+    int nb = 0;
+    const double TOL = 1.e-8;
+    double V2out = v1 + (double)(nout - 1) * dvout;
+    double Vo = v1;
+    while (Vo < V2out + TOL) {
+      if (nb >= kNoAllocBlocks) return CLBLM_ERR_GRID;
+      int64_t J1 = (int64_t)((Vo - v1) / dvout + 1.001);
+      int64_t J2 = std::min<int64_t>(nout, J1 + 2400 - 1);
+      j1[nb] = J1;
+      vo[nb] = Vo;
+      ++nb;
+      Vo = v1 + (double)J2 * dvout;
+    }
+    int2* map = reinterpret_cast<int2*>(base);
+    // every map entry this call reads is written by it; zeroing first keeps
+    // an earlier call's entries out even so (a zero entry reads in bounds)
+    if (cudaMemsetAsync(map, 0, sizeof(int2) * (size_t)nout, st) != cudaSuccess) return CLBLM_ERR_CUDA;
+    int64_t* dj1 = reinterpret_cast<int64_t*>(base + kNoAllocMapBytes);
+    double* dvo = reinterpret_cast<double*>(base + kNoAllocMapBytes + 8 * (size_t)kNoAllocBlocks);
+    // the host tables are staged by the copies before they return
+    if (cudaMemcpyAsync(dj1, j1, 8 * (size_t)nb, cudaMemcpyHostToDevice, st) != cudaSuccess) return CLBLM_ERR_CUDA;
+    if (cudaMemcpyAsync(dvo, vo, 8 * (size_t)nb, cudaMemcpyHostToDevice, st) != cudaSuccess) return CLBLM_ERR_CUDA;
+    k_interp_map<<<(unsigned)((nb + 63) / 64), 64, 0, st>>>(s, dj1, dvo, nb, nout, map);
+    if (cudaGetLastError() != cudaSuccess) return CLBLM_ERR_CUDA;
+    s.map = map;
+  }
+  k_od_out<true><<<(unsigned)((nout + 255) / 256), 256, 0, st>>>(d_in, nin, s, nout, d_out);
+  if (cudaGetLastError() != cudaSuccess) return CLBLM_ERR_CUDA;
+  return CLBLM_OK;
+}

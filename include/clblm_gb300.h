@@ -238,6 +238,43 @@ int clblm_gpu_rt_mode2(clblm_handle_t *h, const clblm_column_t *col,
                        const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap,
                        int32_t flags);
 
+/* ---- grid interpolation that allocates nothing ----------------------------
+ *
+ * No counterpart in the reference.  Some callers cannot call cudaMalloc: a
+ * host model that owns all device memory through its own fixed pool, code
+ * that runs while another component captures or replays device work, or a
+ * caller for which an allocation failing in mid-run is not acceptable.  For
+ * them this entry point performs the step of clblm_gpu_od that maps a layer
+ * spectrum from its computation grid to a uniform output grid (the DVout
+ * interpolation of ODLAY_nonStruct, clblm_ODLAY.f90:582-598, with
+ * interpSpectrum's rules, clblm_Spectrum.f90:326-620) without allocating:
+ * the per-point interpolation map of a general grid ratio is kept in one
+ * file-scope device array of CLBLM_NOALLOC_SCRATCH_BYTES that every GPU
+ * which loads the library holds until the process exits.
+ *
+ *  - d_in: nin binary64 values on v1 + i*dvin; d_out: nout values on
+ *    v1 + i*dvout.  Both are device memory of the current device, passed by
+ *    the caller; host pointers are rejected (CLBLM_ERR_ARG).
+ *  - nout above CLBLM_NOALLOC_MAX_POINTS is rejected with
+ *    CLBLM_ERR_CAPACITY before any device work.
+ *  - The work is queued on `stream` (a cudaStream_t; NULL for the legacy
+ *    default stream); the call does not wait for it.
+ *  - The first call on a device sets up that device: it looks up the device
+ *    address of the scratch array, uploads the interpolation coefficients and
+ *    synchronizes the legacy default stream.  Make that first call before
+ *    any stream capture begins.
+ *  - Every call on a device shares the one scratch array: calls whose work
+ *    overlaps on the GPU (on different streams without ordering between
+ *    them) race and may return wrong values.  Order them on one stream.
+ *  - Calls no cudaMalloc, cudaFree or other allocating routine. */
+#define CLBLM_NOALLOC_MAX_POINTS (1 << 20)
+#define CLBLM_NOALLOC_SCRATCH_BYTES \
+  (8 * CLBLM_NOALLOC_MAX_POINTS + 16 * (CLBLM_NOALLOC_MAX_POINTS / 2400 + 8))
+int clblm_gpu_interp_spectrum_noalloc(const double *d_in, int64_t nin,
+                                      double v1, double dvin, double *d_out,
+                                      int64_t nout, double dvout,
+                                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif
