@@ -55,6 +55,58 @@ def replica_value(points_per_replica, world, ms):
     return points_per_replica * world / (ms * 1e-3)
 
 
+FLOP_CNVFNQ = 19   # per CNVFNQ inner step (R3, R2, R1 updates of one line at one point)
+FLOP_CNVF4Q = 9    # per CNVF4Q inner step (one far-wing record at one R4 point)
+
+
+def fp32_peak_tflops():
+    """Nominal FP32 FMA rate (152 SMs x 128 lanes x 2 FLOP) at the measured
+    maximum SM clock of the GB300s."""
+    mhz = 2070.0
+    try:
+        mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"])
+    except Exception:
+        pass
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12, mhz
+
+
+def load_traffic():
+    """DRAM bytes per algorithmic step of each line-shape kernel, from the ncu
+    capture summarised in profiles/ (None before one exists)."""
+    f = ROOT / "profiles" / "dram_traffic.json"
+    try:
+        return json.loads(f.read_text())
+    except Exception:
+        return {}
+
+
+def roofline(work, kt, steps, ms_step):
+    """Roofline of the dominant line-shape kernel: algorithmic FLOPs of one
+    launch (the call's step counts) over its CUDA-event time on the library's
+    stream, averaged over the timed steps."""
+    peak, mhz = fp32_peak_tflops()
+    traffic = load_traffic()
+    kernels = {
+        "k_f4_conv": (FLOP_CNVF4Q * work["cnvf4q_steps"], kt["ms_f4conv"] / steps, work["cnvf4q_steps"]),
+        "k_panel": (FLOP_CNVFNQ * work["cnvfnq_steps"], kt["ms_panel"] / steps, work["cnvfnq_steps"]),
+    }
+    out = {}
+    for name, (flop, ms, nstep) in kernels.items():
+        ach = flop / (ms * 1e-3) / 1e12 if ms > 0 else None
+        bps = traffic.get(name)
+        out[name] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                     "frac": ach / peak if ach else None,
+                     "traffic": bps * nstep if bps is not None else None,
+                     "ms_per_launch": ms, "share_of_step": ms / ms_step, "flop_per_launch": flop}
+    top = max(out, key=lambda k: out[k]["ms_per_launch"])
+    r = dict(out[top])
+    r["kernel"] = top
+    r["peak_source"] = ("nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x %.0f MHz (sm_max_mhz of "
+                        "MEASURED_PEAKS.json, which holds no FP32 figure)" % mhz)
+    r["others"] = {k: v for k, v in out.items() if k != top}
+    return r
+
+
 def layer_points(h, col, ctrl):
     """Sum over layers of the points ODLAY returns on each layer grid."""
     from clblm_gb300 import capi
@@ -236,13 +288,18 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kt = {"ms_panel": 0.0, "ms_f4conv": 0.0, "launches": 0}
     with Clocks() as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
             step_dev()
+            st = h.stats()  # host-side counters of the call just made (no device sync)
+            for k in kt:
+                kt[k] += st[k]
         ev1.record(stream)
         torch.cuda.synchronize()
+    work = h.stats()
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, "cuda")
     value = replica_value(lp, world, ms)
 
@@ -292,8 +349,7 @@ def main():
                "sample": "layers %d-%d of the column, full 500-2500 cm-1, one thread (%.1f s)"
                          % (CPU_LAYERS[0], CPU_LAYERS[-1], dt)}
 
-    roof = None
-    rf = ROOT / "profiles" / "roofline_live.json"
+    roof = roofline(work, kt, args.steps, ms)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -306,7 +362,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": e2e_ms},
                 "plain_fp64": plain, "cpu_baseline": cpu, "roofline": roof, "clocks": clk.summary(),
-                "gpu_launches": None}
+                "gpu_launches": int(kt["launches"])}
         print(json.dumps(line))
     h.close()
     if world > 1:

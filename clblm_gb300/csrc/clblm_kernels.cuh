@@ -7,7 +7,7 @@
 
 namespace clblm {
 
-constexpr int kStatsPerLayer = 8;  // nlin, lincnt, nminus, nplus, bad, shrunk, -, -
+constexpr int kStatsPerLayer = 8;  // nlin, lincnt, nminus, nplus, bad, CNVFNQ steps, CNVF4Q steps, -
 
 struct LineIn {
   const double* vnu;
@@ -81,7 +81,7 @@ struct F4Rec;
 struct F4RecD;
 __global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
-                              int64_t* nmirror);
+                              int64_t* nmirror, unsigned long long* stats);
 __global__ void k_f4_bounds(const F4Rec* rec, int64_t rstride, const int64_t* nrec, int layer0, int* pmax,
                             int* smin);
 

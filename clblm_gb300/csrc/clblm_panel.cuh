@@ -37,16 +37,22 @@ struct PanelArgs {
   int* err;
 };
 
-// far-wing pseudo-line prepared for the convolution (CNVF4Q per-line set-up)
+// far-wing pseudo-line prepared for the convolution (CNVF4Q per-line set-up),
+// FP32 form of the mixed path: 48 bytes, staged in shared memory in chunks
 struct F4Rec {
-  int jmin, jmax;   // global R4 points m+1 in [jmin, jmax]
-  int mc, co2;      // grid point nearest the line centre (m = J-1); CO2 variant
-  float x0;         // mc*DVR4 - XNUI, |x0| <= DVR4/2
-  float sil, sa3, sb3, fbnd, al2, ralv2, rbnd2;
+  int jmin, jmax;   // global R4 points J = m+1 in [jmin, jmax]
+  float mcf, x0;    // grid point m nearest the line centre (an integer, exact
+                    // in FP32) and mc*DVR4 - XNUI, |x0| <= DVR4/2
+  float sil, al2, ralv2, sa3;
+  float sb3, fb0, fb2, pad;  // pedestal fb0 - x^2 fb2 (CO2: 2 F4BND, F4BND/BOUND^2)
 };
+// FP64 form (the FP64 path), 64 bytes
 struct F4RecD {
+  int jmin, jmax, co2, pad;
   double xnui, sil, siv, fbnd, al2, alv2;
 };
+constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv
+constexpr int kF4Chunk = 256;    // records per shared-memory stage
 
 struct F4Args {
   const LayerPlan* plans;
@@ -59,31 +65,7 @@ struct F4Args {
   const int* pmax_jmax;     // running max of jmax
   const int* smin_jmin;     // running min (from the right) of jmin
   void* r4_all;
-};
-
-struct RtArgs {
-  int64_t n_out;            // points on the output grid of this layer
-  double v1, dv_out;        // output grid
-  // merged radiance / reflectance in (previous grid) and out
-  const void* rad_in;
-  const void* refl_in;
-  int64_t n_in;
-  double dv_in;
-  void* rad_out;
-  void* refl_out;
-  // this layer's optical depth on its own grid
-  const void* od;
-  int64_t n_od;
-  double dv_od;
-  double scal_up, scal_dn;
-  double tbot, ttop, tave;
-  int lin_in_tau;
-  // interpolation of the merged spectra (kind 0: same grid, 1: fixed ratio, 2: general)
-  int interp_mr;
-  int interp_od;
-  int first;                // 1: initialise rad_in/refl_in from the surface
-  double tskin, emis, dv_sfc;
-  int64_t n_sfc;
+  int* err;                 // bit 2: a shared-memory stage never arrived
 };
 
 size_t panel_smem_bytes(bool plain);

@@ -8,7 +8,8 @@
 //                    the R3->R2->R1 4-point interpolation and the radiation
 //                    term (panelOut, clblm_ODLAY.f90:2289-2493).
 //   k_f4_conv<Plain> far-wing function 4 on the DVR4 grid (CNVF4Q,
-//                    clblm_ODLAY_LineF4.f90:187-494), one thread per point.
+//                    clblm_ODLAY_LineF4.f90:187-494): one thread per point,
+//                    records streamed through shared memory by bulk copies.
 //   k_rt_layer<...>  one layer of the upward merge of mode2_lookDn_mergeUp
 //                    (layerMerge_mode2, clblm_noScattRT.f90:1704-1794) with
 //                    layerEmis (clblm_EMLAY.f90:104-178) and the
@@ -21,6 +22,7 @@
 // recomputed in FP64).  Plain path: FP64 throughout.
 #include <cuda_runtime.h>
 
+#include "clblm_bulk.cuh"
 #include "clblm_common.cuh"
 #include "clblm_kernels.cuh"
 #include "clblm_panel.cuh"
@@ -491,79 +493,169 @@ template __global__ void k_panel<false>(PanelArgs);
 template __global__ void k_panel<true>(PanelArgs);
 
 // ---------------------------------------------------------------------------
-// Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1, one thread per
-// point; the records overlapping point J = m+1 are the index range between the
-// first record whose running max of JMAX reaches J and the first record whose
-// running min of JMIN (from the right) exceeds J.
+// Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1 (CNVF4Q).
+//
+// One CTA per tile of kF4Tile consecutive points of one layer.  The records
+// that reach any point of the tile are one index range: from the first record
+// whose running max of JMAX reaches the tile's first point to the first one
+// whose running min of JMIN (from the right) passes its last point.  That
+// range streams through shared memory in chunks of kF4Chunk records, one bulk
+// copy per chunk into two alternating stages; every thread then evaluates all
+// records of the chunk at its own point.  The FP64 path adds the terms in the
+// reference's order (record order); the mixed path keeps four FP32 partial
+// sums per chunk (alternate records) and adds each chunk's total into a Kahan
+// sum.
 template <bool Plain>
-__global__ void k_f4_conv(F4Args a) {
+__global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
   using Real = typename std::conditional<Plain, double, float>::type;
-  using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
+  using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
+  constexpr uint32_t kStageBytes = sizeof(Rec) * kF4Chunk;
+  __shared__ __align__(128) Rec stage[2][kF4Chunk];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int64_t rng[2];
+
   const int layer = blockIdx.y;
   const LayerPlan& P = a.plans[layer + a.layer0];
-  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= P.nptr4 + 2) return;
-  if (m >= P.nptr4) {  // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94)
-    reinterpret_cast<Real*>(a.r4_all)[P.r4_off + m] = (Real)0;
-    return;
-  }
+  const int64_t m0 = (int64_t)blockIdx.x * kF4Tile;
+  if (m0 >= P.nptr4 + 2) return;  // whole CTA: no barrier has been set up yet
+  const int64_t m = m0 + threadIdx.x;
   const int J = (int)m + 1;
+  Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
   const int64_t n = a.nrec[layer + a.layer0];
   const int64_t nm = a.nmirror[layer + a.layer0];
-  const F4Rec* R = a.rec + (int64_t)layer * a.stride;
-  const F4RecD* D = a.recd + (int64_t)layer * a.stride;
-  const int* pm = a.pmax_jmax + (int64_t)layer * a.stride;
-  const int* sm = a.smin_jmin + (int64_t)layer * a.stride;
-  int64_t lo, hi;
-  {
+  const Rec* recs = reinterpret_cast<const Rec*>(Plain ? (const void*)a.recd : (const void*)a.rec) +
+                    (int64_t)layer * a.stride;
+
+  if (threadIdx.x == 0) {
+    const int* pm = a.pmax_jmax + (int64_t)layer * a.stride;
+    const int* sm = a.smin_jmin + (int64_t)layer * a.stride;
+    const int Jlo = (int)m0 + 1;
+    const int Jhi = (int)(m0 + kF4Tile < P.nptr4 ? m0 + kF4Tile : P.nptr4);
     int64_t l = 0, h = n;
-    while (l < h) {
+    while (l < h) {  // first record whose running max of JMAX reaches Jlo
       int64_t mid = (l + h) >> 1;
-      if (pm[mid] < J) l = mid + 1;
+      if (pm[mid] < Jlo) l = mid + 1;
       else h = mid;
     }
-    lo = l;
+    const int64_t lo = l;
     h = n;
-    while (l < h) {
+    while (l < h) {  // first record whose running min of JMIN exceeds Jhi
       int64_t mid = (l + h) >> 1;
-      if (sm[mid] <= J) l = mid + 1;
+      if (sm[mid] <= Jhi) l = mid + 1;
       else h = mid;
     }
-    hi = l;
+    rng[0] = lo;
+    rng[1] = (m0 >= P.nptr4) ? lo : l;  // tiles past NPTR4 need no records
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
   }
+  __syncthreads();
+  const int64_t lo = rng[0], hi = rng[1];
+  const int64_t nchunk = (hi - lo + kF4Chunk - 1) / kF4Chunk;
+  auto issue = [&](int64_t c) {  // thread 0: chunk c into stage c&1
+    const int64_t r0 = lo + c * kF4Chunk;
+    const int64_t nr = hi - r0 < kF4Chunk ? hi - r0 : (int64_t)kF4Chunk;
+    const uint32_t bytes = (uint32_t)(nr * (int64_t)sizeof(Rec));
+    mbar_arrive_expect_tx(&bar[c & 1], bytes);
+    bulk_g2s(&stage[c & 1][0], recs + r0, bytes, &bar[c & 1]);
+  };
+  if (threadIdx.x == 0 && nchunk > 0) issue(0);
+
+  const bool live = m < P.nptr4;
   const float dvr4f = (float)P.dvr4;
+  const float Jm1 = (float)(J - 1);  // exact: J < 2^24
   const double ZSQBND = 64. * 64.;
-  Acc acc;
-  auto one = [&](int64_t i) {
-    const F4Rec r = R[i];
-    if (J < r.jmin || J > r.jmax) return;
+  const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
+  const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
+  const double bnd2 = P.bound4 * P.bound4;
+  double accd = 0.;  // FP64 path
+  KahanF acck;       // mixed path: chunk totals
+  bool failed = false;
+  for (int64_t c = 0; c < nchunk; ++c) {
+    // the other stage was released by the barrier that closed chunk c-1
+    if (threadIdx.x == 0 && c + 1 < nchunk) issue(c + 1);
+    const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      if (threadIdx.x == 0) {
+        atomicOr(a.err, 4);
+        // let a copy still in flight land before the CTA leaves
+        if (c + 1 < nchunk) mbar_wait_bounded(&bar[(c + 1) & 1], (uint32_t)(((c + 1) >> 1) & 1));
+      }
+      break;
+    }
+    const Rec* S = stage[c & 1];
+    const int64_t left = hi - (lo + c * kF4Chunk);
+    const int cnt = (int)(left < kF4Chunk ? left : kF4Chunk);
+    if (live) {
+      if constexpr (Plain) {
+        for (int k = 0; k < cnt; ++k) {
+          const F4RecD& d = S[k];
+          if (J < d.jmin || J > d.jmax) continue;
+          double XM = (double)m * P.dvr4 - d.xnui;
+          double XMSQ = XM * XM;
+          double ZVSQ = XMSQ / d.alv2;
+          double fb = d.co2 ? (2. - XMSQ / bnd2) * d.fbnd : d.fbnd;
+          double F4FN;
+          if (ZVSQ <= ZSQBND) F4FN = (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
+          else F4FN = d.sil / (d.al2 + XMSQ) - fb;
+          accd += F4FN;
+        }
+      } else {
+        float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+        auto term = [&](const F4Rec& r) -> float {
+          float xm = fmaf(Jm1 - r.mcf, dvr4f, r.x0);
+          float xmsq = xm * xm;
+          float zvsq = xmsq * r.ralv2;
+          float fb = fmaf(-xmsq, r.fb2, r.fb0);
+          float f = zvsq <= 4096.f ? fmaf(zvsq, r.sb3, r.sa3) : __fdividef(r.sil, r.al2 + xmsq);
+          f -= fb;
+          return (J >= r.jmin && J <= r.jmax) ? f : 0.f;
+        };
+        int k = 0;
+        for (; k + 4 <= cnt; k += 4) {
+          p0 += term(S[k]);
+          p1 += term(S[k + 1]);
+          p2 += term(S[k + 2]);
+          p3 += term(S[k + 3]);
+        }
+        for (; k < cnt; ++k) p0 += term(S[k]);
+        acck.add((p0 + p1) + (p2 + p3));
+      }
+    }
+    __syncthreads();  // stage c&1 is free for chunk c+2
+  }
+  if (threadIdx.x == 0) {
+    mbar_inval(&bar[0]);
+    mbar_inval(&bar[1]);
+  }
+  if (failed || m >= P.nptr4 + 2) return;
+  if (!live) {  // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94)
+    R4[m] = (Real)0;
+    return;
+  }
+  // mirror records of lines below 25 cm-1 follow the direct ones
+  for (int64_t i = n; i < n + nm; ++i) {
+    const Rec& r = recs[i];
+    if (J < r.jmin || J > r.jmax) continue;
     if constexpr (Plain) {
-      const F4RecD d = D[i];
-      double XM = (double)m * P.dvr4 - d.xnui;
+      double XM = (double)m * P.dvr4 - r.xnui;
       double XMSQ = XM * XM;
-      double ZVSQ = XMSQ / d.alv2;
-      const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
-      const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
-      double fb = r.co2 ? (2. - XMSQ / (P.bound4 * P.bound4)) * d.fbnd : d.fbnd;
-      double F4FN;
-      if (ZVSQ <= ZSQBND) F4FN = (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
-      else F4FN = d.sil / (d.al2 + XMSQ) - fb;
-      acc.add(F4FN);
+      double ZVSQ = XMSQ / r.alv2;
+      double fb = r.co2 ? (2. - XMSQ / bnd2) * r.fbnd : r.fbnd;
+      accd += (ZVSQ <= ZSQBND) ? (r.siv * A3 + ZVSQ * (r.siv * B3)) - fb : r.sil / (r.al2 + XMSQ) - fb;
     } else {
-      float xm = fmaf((float)(J - 1 - r.mc), dvr4f, r.x0);
+      float xm = fmaf(Jm1 - r.mcf, dvr4f, r.x0);
       float xmsq = xm * xm;
       float zvsq = xmsq * r.ralv2;
-      float fb = r.co2 ? (2.f - xmsq * r.rbnd2) * r.fbnd : r.fbnd;
-      float f;
-      if (zvsq <= 4096.f) f = fmaf(zvsq, r.sb3, r.sa3) - fb;
-      else f = __fdividef(r.sil, r.al2 + xmsq) - fb;
-      acc.add(f);
+      float fb = fmaf(-xmsq, r.fb2, r.fb0);
+      float f = zvsq <= 4096.f ? fmaf(zvsq, r.sb3, r.sa3) : __fdividef(r.sil, r.al2 + xmsq);
+      acck.add(f - fb);
     }
-  };
-  for (int64_t i = lo; i < hi; ++i) one(i);
-  for (int64_t i = n; i < n + nm; ++i) one(i);
-  Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
-  R4[m] = (Real)acc.value();
+  }
+  if constexpr (Plain) R4[m] = accd;
+  else R4[m] = acck.value();
 }
 
 template __global__ void k_f4_conv<false>(F4Args);

@@ -271,6 +271,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
   double CONF3 = P.dv / DVR3;
   double amax = 0.;
   unsigned long long bad = 0;
+  unsigned long long steps = 0;  // CNVFNQ inner steps JMAX1-JMIN1+1 of the accepted lines
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
     const LinePrep lp = prep[layer * stride + t];
     int q = qpanel[layer * stride + t];
@@ -307,6 +308,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       double BHWDXF = HWDXF / ZSLOPE;
       int JMAX1 = (int)(ZINT + BHWDXF + 1.5);
       int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
+      if (JMAX1 >= JMIN1) steps += (unsigned long long)(JMAX1 - JMIN1 + 1);
       double RSHFT = 0.5;
       if (ZINT < 0.0) RSHFT = -RSHFT;
       int J2SHFT = (int)(ZINT * (1. - CONF2) + RSHFT);
@@ -348,9 +350,11 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
   for (int off = 16; off > 0; off >>= 1) amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, off));
   unsigned long long b = bad;
   for (int off = 16; off > 0; off >>= 1) b += __shfl_down_sync(0xffffffffu, b, off);
+  for (int off = 16; off > 0; off >>= 1) steps += __shfl_down_sync(0xffffffffu, steps, off);
   if ((threadIdx.x & 31) == 0) {
     if (amax > 0.) atomicMax((unsigned long long*)&alfvmax[layer + layer0], (unsigned long long)__double_as_longlong(amax));
     if (b) atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 4], b);
+    if (steps) atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 5], steps);
   }
 }
 
@@ -838,20 +842,25 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
   double ALFVI2 = ALFAVI * ALFAVI;
   double BNDSQ = P.bound4 * P.bound4;
   double F4BND = SIL / (ALFLI2 + BNDSQ);
-  r->jmin = JMIN;
-  r->jmax = JMAX;
+  const bool co2 = (L.mol == 2);
+  r->jmin = d->jmin = JMIN;
+  r->jmax = d->jmax = JMAX;
+  d->co2 = co2;
+  d->pad = 0;
   // FP32 distances are taken from the grid point nearest the line centre, so
   // that points near the centre do not lose digits to cancellation
-  r->mc = (int)floor(XNUI / P.dvr4 + 0.5);
-  r->co2 = (L.mol == 2);
-  r->x0 = (float)((double)r->mc * P.dvr4 - XNUI);
+  const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
+  r->mcf = (float)mc;
+  r->x0 = (float)((double)mc * P.dvr4 - XNUI);
   r->sil = (float)SIL;
-  r->sa3 = (float)(SIV * A3);
-  r->sb3 = (float)(SIV * B3);
-  r->fbnd = (float)F4BND;
   r->al2 = (float)ALFLI2;
   r->ralv2 = (float)(1. / ALFVI2);
-  r->rbnd2 = (float)(1. / BNDSQ);
+  r->sa3 = (float)(SIV * A3);
+  r->sb3 = (float)(SIV * B3);
+  // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
+  r->fb0 = (float)(co2 ? 2. * F4BND : F4BND);
+  r->fb2 = (float)(co2 ? F4BND / BNDSQ : 0.);
+  r->pad = 0.f;
   d->xnui = XNUI;
   d->sil = SIL;
   d->siv = SIV;
@@ -863,7 +872,7 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
 __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
                               int64_t stride, const int64_t* __restrict__ nsh, F4Rec* __restrict__ rec,
                               F4RecD* __restrict__ recd, int64_t rstride, int64_t* __restrict__ nrec,
-                              int64_t* __restrict__ nmirror) {
+                              int64_t* __restrict__ nmirror, unsigned long long* __restrict__ stats) {
   const int layer = blockIdx.y;
   const LayerPlan& P = plans[layer + layer0];
   const int64_t n = nsh[2 * (layer + layer0)] < 0 ? 0 : nsh[2 * (layer + layer0) + 1];
@@ -871,6 +880,7 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
   F4Rec* R = rec + (int64_t)layer * rstride;
   F4RecD* D = recd + (int64_t)layer * rstride;
   const double VNULST = P.v1r4 + P.dvr4 * (double)(P.nptr4 - 1) + P.bound4;
+  unsigned long long steps = 0;  // CNVF4Q inner steps (line, point) of these records
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const ShrunkLine L = S[i];
     F4Rec r;
@@ -878,12 +888,15 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     f4_record(P, L, L.vnu, &r, &d);
     // lines beyond the last point's reach, or without strength, add nothing
     if (L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) {
-      r.jmin = 1 << 30;
-      r.jmax = -1;
+      r.jmin = d.jmin = 1 << 30;
+      r.jmax = d.jmax = -1;
     }
+    if (r.jmax >= r.jmin) steps += (unsigned long long)(r.jmax - r.jmin + 1);
     R[i] = r;
     D[i] = d;
   }
+  for (int o = 16; o > 0; o >>= 1) steps += __shfl_down_sync(0xffffffffu, steps, o);
+  if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 6], steps);
   // mirror lines: one thread per layer (at most the lines below 25 cm-1)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     int64_t nm = 0;
@@ -897,6 +910,7 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
         R[n + nm] = r;
         D[n + nm] = d;
         nm++;
+        atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 6], (unsigned long long)(r.jmax - r.jmin + 1));
       }
     }
     nmirror[layer + layer0] = nm;

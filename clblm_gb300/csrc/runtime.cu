@@ -81,6 +81,15 @@ struct clblm_handle {
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
+  // per-call sums of the line-shape kernels' work and device time
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // f4 start/stop, panel start/stop
+  int64_t acc_fnq = 0, acc_f4q = 0;
+  double acc_ms_panel = 0., acc_ms_f4 = 0.;
+  void reset_call() {
+    launches = 0;
+    acc_fnq = acc_f4q = 0;
+    acc_ms_panel = acc_ms_f4 = 0.;
+  }
 };
 
 namespace {
@@ -694,7 +703,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   h->launches++;
   k_f4_lineinit<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
       dplans, first, h->f4sh.as<ShrunkLine>(), f4stride, h->f4nout.as<int64_t>(), h->f4rec.as<F4Rec>(),
-      h->f4recd.as<F4RecD>(), rstride, h->f4nrec.as<int64_t>(), h->f4nmir.as<int64_t>());
+      h->f4recd.as<F4RecD>(), rstride, h->f4nrec.as<int64_t>(), h->f4nmir.as<int64_t>(),
+      h->stats.as<unsigned long long>());
   h->launches++;
   k_f4_bounds<<<count, 1024, 0, st>>>(h->f4rec.as<F4Rec>(), rstride, h->f4nrec.as<int64_t>(), first,
                                       h->f4pm.as<int>(), h->f4sm.as<int>());
@@ -712,10 +722,13 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     fa.pmax_jmax = h->f4pm.as<int>();
     fa.smin_jmin = h->f4sm.as<int>();
     fa.r4_all = h->r4.p;
-    dim3 grid((unsigned)((maxr4 + 2 + 127) / 128), count);
+    fa.err = h->err.as<int>();
+    dim3 grid((unsigned)((maxr4 + 2 + kF4Tile - 1) / kF4Tile), count);
     h->launches++;
-    if (plain) k_f4_conv<true><<<grid, 128, 0, st>>>(fa);
-    else k_f4_conv<false><<<grid, 128, 0, st>>>(fa);
+    CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+    if (plain) k_f4_conv<true><<<grid, kF4Tile, 0, st>>>(fa);
+    else k_f4_conv<false><<<grid, kF4Tile, 0, st>>>(fa);
+    CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   }
   // line centres
   h->launches++;
@@ -773,12 +786,15 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   if (plain) {
     CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     h->launches++;
+    CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
     k_panel<true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
   } else {
     CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     h->launches++;
+    CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
     k_panel<false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
   }
+  CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
   CUDA_TRY(h, cudaGetLastError());
   return CLBLM_OK;
 }
@@ -909,6 +925,18 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
   CUDA_TRY(h, cudaGetLastError());
   if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "more than %d radiation-term segments in a panel", kMaxSeg);
   if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
+  if (err[0] & 4) return set_err(h, CLBLM_ERR_CUDA, "far-wing records: a shared-memory stage never arrived");
+  {
+    float t0 = 0.f, t1 = 0.f;
+    CUDA_TRY(h, cudaEventElapsedTime(&t0, h->ev[0], h->ev[1]));
+    CUDA_TRY(h, cudaEventElapsedTime(&t1, h->ev[2], h->ev[3]));
+    h->acc_ms_f4 += t0;
+    h->acc_ms_panel += t1;
+    for (int k = first; k < first + count; ++k) {
+      h->acc_fnq += (int64_t)stats[k * kStatsPerLayer + 5];
+      h->acc_f4q += (int64_t)stats[k * kStatsPerLayer + 6];
+    }
+  }
   for (int k = first; k < first + count; ++k) {
     const unsigned long long* s = &stats[k * kStatsPerLayer];
     if (s[4]) return set_err(h, CLBLM_ERR_UNSUPPORTED, "layer %d: %llu lines need isotopologue/line-coupling/drop "
@@ -930,6 +958,10 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
     last_stats->dv = P.dv;
     last_stats->dvr4 = P.dvr4;
     last_stats->jrad = P.jrad;
+    last_stats->cnvfnq_steps = h->acc_fnq;
+    last_stats->cnvf4q_steps = h->acc_f4q;
+    last_stats->ms_panel = h->acc_ms_panel;
+    last_stats->ms_f4conv = h->acc_ms_f4;
   }
   return CLBLM_OK;
 }
@@ -961,6 +993,13 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
     g_create_err = "cannot use CUDA device";
     delete h;
     return CLBLM_ERR_CUDA;
+  }
+  for (auto& e : h->ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      g_create_err = "cannot create CUDA events";
+      clblm_gpu_destroy(h);
+      return CLBLM_ERR_CUDA;
+    }
   }
   rc = upload_tables(h);
   if (!rc) rc = load_lines(h, lines);
@@ -1016,6 +1055,8 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
   for (auto& b : h->imap) b.release();
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CLBLM_OK;
@@ -1133,7 +1174,7 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
   if (rc) return rc;
   if (!out || cap < hps[0].n_out) return set_err(h, CLBLM_ERR_CAPACITY, "output needs %lld points", (long long)hps[0].n_out);
   bool plain = ctrl->precision == CLBLM_PREC_PLAIN;
-  h->launches = 0;
+  h->reset_call();
   int64_t ls, fs, ps, odt;
   rc = prepare_batch(h, hps, 0, 1, plain, &ls, &fs, &ps, &odt);
   if (rc) return rc;
@@ -1271,7 +1312,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
   int64_t nfinal = rp.grid_n.back();
   if (!rad || cap < nfinal) return set_err(h, CLBLM_ERR_CAPACITY, "radiance needs %lld points", (long long)nfinal);
   bool plain = ctrl->od.precision == CLBLM_PREC_PLAIN;
-  h->launches = 0;
+  h->reset_call();
   size_t real = plain ? 8 : 4;
   int64_t maxn = rp.n0;
   for (int il = 0; il < n; ++il) maxn = std::max(maxn, rp.grid_n[il]);

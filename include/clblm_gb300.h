@@ -173,6 +173,12 @@ typedef struct {
   double  dvr4;        /* DV of the far-wing grid                              */
   int32_t jrad;        /* JRAD in effect                                       */
   int64_t launches;    /* device kernels launched by the last OD/radiance call */
+  /* algorithmic work and device time of the two line-shape kernels, summed
+   * over every layer of the last OD/radiance call */
+  int64_t cnvfnq_steps; /* sum of JMAX1-JMIN1+1 over convolved lines (CNVFNQ)  */
+  int64_t cnvf4q_steps; /* sum of (far-wing record, R4 point) pairs (CNVF4Q)    */
+  double  ms_panel;     /* device time of the panel kernel (R1/R2/R3 + combine) */
+  double  ms_f4conv;    /* device time of the far-wing convolution kernel       */
 } clblm_od_stats_t;
 
 typedef struct clblm_handle clblm_handle_t;
