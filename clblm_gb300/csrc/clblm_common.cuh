@@ -79,7 +79,7 @@ struct LinePrep {
 
 // One line's contribution on one of the three nested grids, in global
 // coordinates of that grid (index 0 at VFT of panel 0).
-struct GridRec {
+struct __align__(16) GridRec {
   int g_lo, g_hi;   // first / last global index touched (inclusive)
   int q;            // panel the reference processes the line in
   float zfl, zs;    // ZFkL and ZSLOPE (FP32 copies for the mixed path)

@@ -82,6 +82,8 @@ struct F4RecD;
 __global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
                               int64_t* nmirror, unsigned long long* stats);
+__global__ void k_rec_bounds(const LayerPlan* plans, int layer0, const GridRec* rec, int64_t stride, int* pmax,
+                             int* smin);
 __global__ void k_f4_bounds(const F4Rec* rec, int64_t rstride, const int64_t* nrec, int layer0, int* pmax,
                             int* smin);
 

@@ -20,11 +20,8 @@ struct PanelArgs {
   const GridRec* rec;
   const GridRecD* recd;
   int64_t stride;
-  const int64_t* ranges;
+  const int64_t* ranges;     // per panel: candidate record windows of R1, R2, R3
   int64_t panel_stride;
-  const double* vnu_raw;
-  const double* alfvmax;
-  double shiftmax;
   const void* r4_all;
   const double* absrb_all;
   void* od_all;
@@ -34,6 +31,8 @@ struct PanelArgs {
   const int* blk_n;          // block length NPTR4
   const int64_t* blk_m0;     // block origin on the global far-wing grid
   const double* blk_fac;     // JRAD = 1: radiation term of each block point (2502 per block)
+  const int* pmax_g;         // per grid: running max of g_hi over the records
+  const int* smin_g;         // per grid: running min (from the right) of g_lo
   int* err;
 };
 

@@ -67,8 +67,19 @@ __device__ __forceinline__ int table_index_mixed(int k, const GridRec& r, const 
 template <bool Plain>
 struct PanelSmem;
 
+// 32-point tiles of the three grids: R1 p-frame points 33.., R2 0..615, R3 0..160
+constexpr int kTiles1 = kPanelPts / 32 + 1, kTiles2 = (kR2Pts + 31) / 32, kTiles3 = (kR3Pts + 31) / 32;
+constexpr int kPanelWarps = kPanelThreads / 32;
+
+// record index range [lo, hi) of every tile, and one 32-record staging
+// buffer per warp
+struct PanelTiles {
+  int lo1[kTiles1], hi1[kTiles1], lo2[kTiles2], hi2[kTiles2], lo3[kTiles3], hi3[kTiles3];
+  GridRec wrec[kPanelWarps][32];
+};
+
 template <>
-struct PanelSmem<false> {
+struct PanelSmem<false> : PanelTiles {
   float4 t1[kNFMX];
   float t2[kNFMX];
   float t3[kNFMX];
@@ -80,7 +91,8 @@ struct PanelSmem<false> {
   int nseg;
 };
 template <>
-struct PanelSmem<true> {
+struct PanelSmem<true> : PanelTiles {
+  GridRecD wrecd[kPanelWarps][32];
   double t1[3 * kNFMX];
   double t2[kNFMX];
   double t3[kNFMX];
@@ -93,15 +105,6 @@ struct PanelSmem<true> {
 };
 
 size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
-
-__device__ __forceinline__ int64_t lb_d(const double* a, int64_t lo, int64_t hi, double x) {
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if (a[mid] < x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
 
 // RADFNI, clblm_ODLAY_CommonSub.f90:379-508 (FP64)
 __device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, double* RDEL, double* RDLAST) {
@@ -211,6 +214,93 @@ __global__ void k_r4_radfac(const LayerPlan* __restrict__ plans, int layer0, con
   } while (N2 < NPTR4);
 }
 
+// Record ranges of the T tiles [G0 + 32t, G0 + 32t + 31] of one grid from the
+// running max of g_hi (pm) and min of g_lo (sm) over the panel's candidate
+// window [w0, w1): lo(t) = first record with pm >= G0 + 32t, hi(t) = first
+// record with sm > G0 + 32t + 31.  Every thread drops each record of the
+// window into the slot of the last tile it can reach / the last tile it is
+// past, and a suffix minimum over the tiles finishes both.
+__device__ __forceinline__ void tile_ranges_scatter(const int* __restrict__ pm, const int* __restrict__ sm,
+                                                    int64_t w0, int64_t w1, int G0, int T, int* lo, int* hi) {
+  for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
+    const int v = pm[i];
+    if (v >= G0) atomicMin(&lo[min((v - G0) >> 5, T - 1)], (int)i);
+    const int s = sm[i];
+    if (s - G0 > 31) atomicMin(&hi[min((s - G0) >> 5, T) - 1], (int)i);
+  }
+}
+__device__ __forceinline__ void tile_ranges_finish(int T, int* lo, int* hi) {
+  for (int t = T - 2; t >= 0; --t) {
+    lo[t] = min(lo[t], lo[t + 1]);
+    hi[t] = min(hi[t], hi[t + 1]);
+  }
+}
+
+// Sum over the records [lo, hi) of one grid at global point g of the lane:
+// the records pass through the warp's shared-memory buffer 32 at a time,
+// the next 32 already loaded into registers while the current ones are used.
+template <bool Plain, int GRID>
+__device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs& a, const GridRec* __restrict__ rec,
+                                            const GridRecD* __restrict__ recd, int64_t lo, int64_t hi, int g,
+                                            bool active, int qmax, typename std::conditional<Plain, SumD, KahanF>::type& acc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  GridRec* buf = S.wrec[warp];
+  GridRec nxt;
+  GridRecD nxtd;
+  if (lo + lane < hi) {
+    nxt = rec[lo + lane];
+    if constexpr (Plain) nxtd = recd[lo + lane];
+  }
+  for (int64_t base = lo; base < hi; base += 32) {
+    __syncwarp();
+    buf[lane] = nxt;
+    if constexpr (Plain) S.wrecd[warp][lane] = nxtd;
+    __syncwarp();
+    const int cnt = (int)(hi - base < 32 ? hi - base : 32);
+    if (base + 32 + lane < hi) {
+      nxt = rec[base + 32 + lane];
+      if constexpr (Plain) nxtd = recd[base + 32 + lane];
+    }
+    if (!active) continue;
+    for (int k = 0; k < cnt; ++k) {
+      const GridRec r = buf[k];
+      if (g < r.g_lo || g > r.g_hi || r.q > qmax) continue;
+      const int kk = g - r.g_lo + 1;
+      if constexpr (Plain) {
+        const GridRecD& d = S.wrecd[warp][k];
+        const int iz = (int)(fabs(fma((double)kk, d.zs, d.zfl)) + 1.5);
+        if (iz > kNFMX) {
+          atomicOr(a.err, 2);
+          continue;
+        }
+        if constexpr (GRID == 1) {
+          const double* T = S.t1 + 3 * (iz - 1);
+          acc.add(d.a0 * T[0] + d.a1 * T[1] + d.a2 * T[2]);
+        } else if constexpr (GRID == 2) {
+          acc.add(d.a0 * S.t2[iz - 1]);
+        } else {
+          acc.add(d.a0 * S.t3[iz - 1]);
+        }
+      } else {
+        const int iz = table_index_mixed(kk, r, recd + (base + k));
+        if (iz > kNFMX) {
+          atomicOr(a.err, 2);
+          continue;
+        }
+        if constexpr (GRID == 1) {
+          const float4 T = S.t1[iz - 1];
+          acc.add(fmaf(r.a0, T.x, fmaf(r.a1, T.y, r.a2 * T.z)));
+        } else if constexpr (GRID == 2) {
+          acc.add(r.a0 * S.t2[iz - 1]);
+        } else {
+          acc.add(r.a0 * S.t3[iz - 1]);
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
 template <bool Plain>
 __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
@@ -275,8 +365,6 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
   }
   __syncthreads();
 
-  const int64_t nl = P.line_hi - P.line_lo + 1;
-  const double* vraw = a.vnu_raw + P.line_lo;
   const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
   const GridRec* rec2 = rec1 + a.stride;
   const GridRec* rec3 = rec2 + a.stride;
@@ -284,87 +372,81 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
   const GridRecD* rd2 = rd1 + a.stride;
   const GridRecD* rd3 = rd2 + a.stride;
   const int64_t* rg = a.ranges + ((int64_t)layer * a.panel_stride + p) * 6;
-  const double amax = a.alfvmax[layer + a.layer0];
-  const double shift = a.shiftmax * P.rhorat + 1e-9;
+  const int* pm1 = a.pmax_g + (int64_t)layer * a.stride * 3;
+  const int* sm1 = a.smin_g + (int64_t)layer * a.stride * 3;
+
+  // ---- record range of every 32-point tile of the three grids ----
+  const int nT1 = (NHI - kNSHIFT + 31) / 32;
+  const int G01 = kPanelPts * p + kNSHIFT, G02 = kPanelR2 * p - 1, G03 = kPanelR3 * p - 1;
+  for (int t = tid; t < kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
+  for (int t = tid; t < kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
+  for (int t = tid; t < kTiles3; t += blockDim.x) S.lo3[t] = S.hi3[t] = (int)rg[5];
+  __syncthreads();
+  if (nT1 > 0) tile_ranges_scatter(pm1, sm1, rg[0], rg[1], G01, nT1, S.lo1, S.hi1);
+  tile_ranges_scatter(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, kTiles2, S.lo2, S.hi2);
+  tile_ranges_scatter(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, kTiles3, S.lo3, S.hi3);
+  __syncthreads();
+  if (tid == 0 && nT1 > 0) tile_ranges_finish(nT1, S.lo1, S.hi1);
+  if (tid == 32) tile_ranges_finish(kTiles2, S.lo2, S.hi2);
+  if (tid == 64) tile_ranges_finish(kTiles3, S.lo3, S.hi3);
+  __syncthreads();
 
   // ---- R3: line sums on p-frame points 0..160 (new) and 0..7 (old) ----
-  {
-    const double reach = 64. * amax + 48. * dv + shift;
-    for (int tile = warp; tile < (kR3Pts + 8 + 31) / 32; tile += kPanelThreads / 32) {
-      int idx = tile * 32 + lane;
-      bool old = idx >= kR3Pts;
-      int J3 = old ? idx - kR3Pts : idx;               // p-frame index
-      bool active = old ? (J3 < 8 && p > 0) : (J3 < kR3Pts);
-      int qmax = old ? p - 1 : p;
-      int g = kPanelR3 * p + J3 - 1;
-      // candidate lines of this tile
-      int J3a = tile * 32 - (old ? kR3Pts : 0), J3b = J3a + 31;
-      if (old) J3a = 0;
-      double vlo = P.vft0 + (double)(kPanelR3 * p + J3a - 1) * 16. * dv - reach;
-      double vhi = P.vft0 + (double)(kPanelR3 * p + J3b - 1) * 16. * dv + reach;
-      int64_t lo = lb_d(vraw, rg[4], rg[5], vlo), hi = lb_d(vraw, lo, rg[5], vhi);
-      Acc acc;
-      for (int64_t i = lo; i < hi; ++i) {
-        GridRec r = rec3[i];
-        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= qmax) {
-          int k = g - r.g_lo + 1;
-          if constexpr (Plain) {
-            GridRecD d = rd3[i];
-            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
-            if (iz <= kNFMX) acc.add(d.a0 * S.t3[iz - 1]);
-            else atomicOr(a.err, 2);
-          } else {
-            int iz = table_index_mixed(k, r, rd3 + i);
-            if (iz <= kNFMX) acc.add(r.a0 * S.t3[iz - 1]);
-            else atomicOr(a.err, 2);
-          }
-        }
-      }
-      if (active) {
-        // far wings (R4) and continuum (ABSRB) interpolated into R3
-        double VI = VFT + (16. * dv) * (double)(J3 - 1);
-        double extra = 0.;
-        if (P.nptr4 > 0) {
-          // the R4 block LBLF4Q held when XINT reached the point: this panel's
-          // for N1R3 = 6..155, the previous panel's for the carried points
-          // 1..5 (XINT'd there as 151..155)
-          const Real* R4 = reinterpret_cast<const Real*>(a.r4_all) + P.r4_off;  // global R4[m]
-          const int b = a.panel_blk[P.vft_off + ((p > 0 && J3 < 6) ? p - 1 : p)];
-          const double V1R4 = a.blk_v1[P.blk_off + b];
-          const int NPTR4 = a.blk_n[P.blk_off + b];
-          const int64_t m0 = a.blk_m0[P.blk_off + b];
-          const double V2R4 = V1R4 + P.dvr4 * (double)(NPTR4 - 1);
-          int ILO = (int)((V1R4 + P.dvr4 - VFT) / (16. * dv) + 1. + kONEMI);
-          int IHI = (int)((V2R4 - P.dvr4 - VFT) / (16. * dv) + kONEMI);
-          if (J3 >= ILO && J3 <= IHI) {
-            double w[4];
-            int J = xint_weights(VI, V1R4, P.dvr4, w);
-            const double* fac = a.blk_fac + (P.blk_off + b) * (int64_t)(kLIMOUT4 + 2);
-            for (int k = 0; k < 4; ++k) {
-              int jb = J - 1 + k;  // 1-based point of the block; zero past NPTR4
-              double v = 0.;
-              if (jb >= 1 && jb <= NPTR4 && m0 + jb - 1 < P.nptr4) {
-                v = (double)R4[m0 + jb - 1];
-                if (P.jrad == 1) v *= fac[jb - 1];
-              }
-              extra += v * w[k];
+  // units 0..kTiles3-1: 32 new points each; unit kTiles3: the 8 old points
+  for (int u = warp; u <= kTiles3; u += kPanelWarps) {
+    const bool old = (u == kTiles3);
+    const int J3 = old ? lane : u * 32 + lane;  // p-frame index
+    const bool active = old ? (J3 < 8 && p > 0) : (J3 < kR3Pts);
+    const int qmax = old ? p - 1 : p;
+    const int g = kPanelR3 * p + J3 - 1;
+    const int t = old ? 0 : u;
+    const int64_t lo = S.lo3[t], hi = max(S.lo3[t], S.hi3[t]);
+    Acc acc;
+    gather_grid<Plain, 3>(S, a, rec3, rd3, lo, hi, g, active, qmax, acc);
+    if (active) {
+      // far wings (R4) and continuum (ABSRB) interpolated into R3
+      double VI = VFT + (16. * dv) * (double)(J3 - 1);
+      double extra = 0.;
+      if (P.nptr4 > 0) {
+        // the R4 block LBLF4Q held when XINT reached the point: this panel's
+        // for N1R3 = 6..155, the previous panel's for the carried points
+        // 1..5 (XINT'd there as 151..155)
+        const Real* R4 = reinterpret_cast<const Real*>(a.r4_all) + P.r4_off;  // global R4[m]
+        const int b = a.panel_blk[P.vft_off + ((p > 0 && J3 < 6) ? p - 1 : p)];
+        const double V1R4 = a.blk_v1[P.blk_off + b];
+        const int NPTR4 = a.blk_n[P.blk_off + b];
+        const int64_t m0 = a.blk_m0[P.blk_off + b];
+        const double V2R4 = V1R4 + P.dvr4 * (double)(NPTR4 - 1);
+        int ILO = (int)((V1R4 + P.dvr4 - VFT) / (16. * dv) + 1. + kONEMI);
+        int IHI = (int)((V2R4 - P.dvr4 - VFT) / (16. * dv) + kONEMI);
+        if (J3 >= ILO && J3 <= IHI) {
+          double w[4];
+          int J = xint_weights(VI, V1R4, P.dvr4, w);
+          const double* fac = a.blk_fac + (P.blk_off + b) * (int64_t)(kLIMOUT4 + 2);
+          for (int k = 0; k < 4; ++k) {
+            int jb = J - 1 + k;  // 1-based point of the block; zero past NPTR4
+            double v = 0.;
+            if (jb >= 1 && jb <= NPTR4 && m0 + jb - 1 < P.nptr4) {
+              v = (double)R4[m0 + jb - 1];
+              if (P.jrad == 1) v *= fac[jb - 1];
             }
+            extra += v * w[k];
           }
         }
-        if (P.contnm) {
-          const double* AB = a.absrb_all + P.abs_off;  // 1-based
-          int ILO = (int)((P.v1abs + P.dvabs - VFT) / (16. * dv) + 1. + kONEMI);
-          int IHI = (int)((P.v2abs - P.dvabs - VFT) / (16. * dv) + kONEMI);
-          if (J3 >= ILO && J3 <= IHI) {
-            double w[4];
-            int J = xint_weights(VI, P.v1abs, P.dvabs, w);
-            extra += AB[J - 1] * w[0] + AB[J] * w[1] + AB[J + 1] * w[2] + AB[J + 2] * w[3];
-          }
-        }
-        acc.add((Real)extra);
-        if (old) S.r3o[J3] = acc.value();
-        else S.r3n[J3] = acc.value();
       }
+      if (P.contnm) {
+        const double* AB = a.absrb_all + P.abs_off;  // 1-based
+        int ILO = (int)((P.v1abs + P.dvabs - VFT) / (16. * dv) + 1. + kONEMI);
+        int IHI = (int)((P.v2abs - P.dvabs - VFT) / (16. * dv) + kONEMI);
+        if (J3 >= ILO && J3 <= IHI) {
+          double w[4];
+          int J = xint_weights(VI, P.v1abs, P.dvabs, w);
+          extra += AB[J - 1] * w[0] + AB[J] * w[1] + AB[J + 1] * w[2] + AB[J + 2] * w[3];
+        }
+      }
+      acc.add((Real)extra);
+      if (old) S.r3o[J3] = acc.value();
+      else S.r3n[J3] = acc.value();
     }
   }
   __syncthreads();
@@ -376,31 +458,12 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
     const int LIMLO = (p == 0) ? 5 : 13;          // N1R2 (+4 in the first panel)
     const int LIMHI = NHI / 4 + 1;
     const int lastJg = LIMLO + ((LIMHI - LIMLO) / 4) * 4;  // last group start of the loop
-    const double reach = 16. * amax + 12. * dv + shift;
-    for (int tile = warp; tile * 32 < kR2Pts; tile += kPanelThreads / 32) {
+    for (int tile = warp; tile < kTiles2; tile += kPanelWarps) {
       int J = tile * 32 + lane;  // p-frame R2 index
       bool active = J >= 5 && J < kR2Pts;
       int g = kPanelR2 * p + J - 1;
-      double vlo = P.vft0 + (double)(kPanelR2 * p + tile * 32 - 1) * 4. * dv - reach;
-      double vhi = P.vft0 + (double)(kPanelR2 * p + tile * 32 + 30) * 4. * dv + reach;
-      int64_t lo = lb_d(vraw, rg[2], rg[3], vlo), hi = lb_d(vraw, lo, rg[3], vhi);
       Acc acc;
-      for (int64_t i = lo; i < hi; ++i) {
-        GridRec r = rec2[i];
-        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= p) {
-          int k = g - r.g_lo + 1;
-          if constexpr (Plain) {
-            GridRecD d = rd2[i];
-            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
-            if (iz <= kNFMX) acc.add(d.a0 * S.t2[iz - 1]);
-            else atomicOr(a.err, 2);
-          } else {
-            int iz = table_index_mixed(k, r, rd2 + i);
-            if (iz <= kNFMX) acc.add(r.a0 * S.t2[iz - 1]);
-            else atomicOr(a.err, 2);
-          }
-        }
-      }
+      gather_grid<Plain, 2>(S, a, rec2, rd2, S.lo2[tile], max(S.lo2[tile], S.hi2[tile]), g, active, p, acc);
       if (active) {
         int off = (J - 1) & 3;
         int Jg = J - off;
@@ -427,39 +490,13 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
   {
     const Real X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
     const Real X10 = -1. / 16., X11 = 9. / 16.;
-    const double reach = 4. * amax + 3. * dv + shift;
     Real* od = reinterpret_cast<Real*>(a.od_all) + P.od_off;
-    const int npts = NHI - kNSHIFT;  // output points of this panel
-    for (int tile = warp; tile * 32 < npts; tile += kPanelThreads / 32) {
+    for (int tile = warp; tile < nT1; tile += kPanelWarps) {
       int J = kNSHIFT + 1 + tile * 32 + lane;  // p-frame R1 index, 33..
       bool active = J <= NHI;
       int g = kPanelPts * p + J - 1;
-      double vlo = P.vft0 + (double)(kPanelPts * p + kNSHIFT + tile * 32) * dv - reach;
-      double vhi = P.vft0 + (double)(kPanelPts * p + kNSHIFT + tile * 32 + 31) * dv + reach;
-      int64_t lo = lb_d(vraw, rg[0], rg[1], vlo), hi = lb_d(vraw, lo, rg[1], vhi);
       Acc acc;
-      for (int64_t i = lo; i < hi; ++i) {
-        GridRec r = rec1[i];
-        if (active && g >= r.g_lo && g <= r.g_hi && r.q <= p) {
-          int k = g - r.g_lo + 1;
-          if constexpr (Plain) {
-            GridRecD d = rd1[i];
-            int iz = (int)(fabs(fma((double)k, d.zs, d.zfl)) + 1.5);
-            if (iz <= kNFMX) {
-              const double* T = S.t1 + 3 * (iz - 1);
-              acc.add(d.a0 * T[0] + d.a1 * T[1] + d.a2 * T[2]);
-            } else
-              atomicOr(a.err, 2);
-          } else {
-            int iz = table_index_mixed(k, r, rd1 + i);
-            if (iz <= kNFMX) {
-              float4 T = S.t1[iz - 1];
-              acc.add(fmaf(r.a0, T.x, fmaf(r.a1, T.y, r.a2 * T.z)));
-            } else
-              atomicOr(a.err, 2);
-          }
-        }
-      }
+      gather_grid<Plain, 1>(S, a, rec1, rd1, S.lo1[tile], max(S.lo1[tile], S.hi1[tile]), g, active, p, acc);
       if (active) {
         int off = (J - 33) & 3;
         int Jg = J - off;

@@ -966,4 +966,60 @@ __global__ void k_f4_bounds(const F4Rec* __restrict__ rec, int64_t rstride, cons
   }
 }
 
+// Per (layer, grid): running max of g_hi from the left and running min of
+// g_lo from the right over the convolution records, so that the records that
+// touch a range [g0, g1] of grid points form the contiguous index range found
+// by two binary searches.  Empty records (g_hi < g_lo) touch nothing.
+__global__ void k_rec_bounds(const LayerPlan* __restrict__ plans, int layer0, const GridRec* __restrict__ rec,
+                             int64_t stride, int* __restrict__ pmax, int* __restrict__ smin) {
+  const int layer = blockIdx.x / 3, grid = blockIdx.x % 3;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.line_hi - P.line_lo + 1;
+  const int64_t o = ((int64_t)layer * 3 + grid) * stride;
+  const GridRec* R = rec + o;
+  int* pm = pmax + o;
+  int* sm = smin + o;
+  const int T = blockDim.x;
+  const int64_t chunk = (n + T - 1) / T;
+  const int64_t b = threadIdx.x * chunk, e = min(n, b + chunk);
+  __shared__ int shmax[1024], shmin[1024];
+  const int kNone = 0x7fffffff;
+  int mx = -1, mn = kNone;
+  for (int64_t i = b; i < e; ++i) {
+    const int lo = R[i].g_lo, hi = R[i].g_hi;
+    if (hi >= lo) {
+      mx = max(mx, hi);
+      mn = min(mn, lo);
+    }
+  }
+  shmax[threadIdx.x] = mx;
+  shmin[threadIdx.x] = mn;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = -1;
+    for (int t = 0; t < T; ++t) {
+      int v = shmax[t];
+      shmax[t] = run;  // exclusive prefix max
+      run = max(run, v);
+    }
+    run = kNone;
+    for (int t = T - 1; t >= 0; --t) {
+      int v = shmin[t];
+      shmin[t] = run;  // exclusive suffix min
+      run = min(run, v);
+    }
+  }
+  __syncthreads();
+  int run = shmax[threadIdx.x];
+  for (int64_t i = b; i < e; ++i) {
+    if (R[i].g_hi >= R[i].g_lo) run = max(run, R[i].g_hi);
+    pm[i] = run;
+  }
+  run = shmin[threadIdx.x];
+  for (int64_t i = e - 1; i >= b; --i) {
+    if (R[i].g_hi >= R[i].g_lo) run = min(run, R[i].g_lo);
+    sm[i] = run;
+  }
+}
+
 }  // namespace clblm

@@ -76,6 +76,7 @@ struct clblm_handle {
   DevBuf plans, vft, prep, qpanel, rec, recd, ranges, od, r4, absrb, stats, alfvmax, blockmax, nlines_d;
   DevBuf f4prep, f4sh, f4nout, f4rec, f4recd, f4nrec, f4nmir, f4pm, f4sm, err;
   DevBuf pblk, bv1, bn, bm0, bfac;
+  DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp;
   DevBuf rt[4], outbuf, imap[2];
   std::string errmsg;
@@ -747,6 +748,9 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   k_line_records<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
       dplans, first, h->vft.as<double>(), h->prep.as<LinePrep>(), h->qpanel.as<int>(), lstride, h->rec.as<GridRec>(),
       h->recd.as<GridRecD>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(), h->alfvmax.as<double>());
+  h->launches++;
+  k_rec_bounds<<<3 * count, 1024, 0, st>>>(dplans, first, h->rec.as<GridRec>(), lstride, h->gpm.as<int>(),
+                                           h->gsm.as<int>());
   int maxp = 0;
   for (int k = 0; k < count; ++k) maxp = std::max(maxp, hps[first + k].P.npanels);
   h->launches++;
@@ -762,9 +766,6 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.stride = lstride;
   pa.ranges = h->ranges.as<int64_t>();
   pa.panel_stride = pstride;
-  pa.vnu_raw = h->lines[0].as<double>();
-  pa.alfvmax = h->alfvmax.as<double>();
-  pa.shiftmax = h->shiftmax;
   pa.r4_all = h->r4.p;
   pa.absrb_all = h->absrb.as<double>();
   pa.od_all = h->od.p;
@@ -774,6 +775,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.blk_n = h->bn.as<int>();
   pa.blk_m0 = h->bm0.as<int64_t>();
   pa.blk_fac = h->bfac.as<double>();
+  pa.pmax_g = h->gpm.as<int>();
+  pa.smin_g = h->gsm.as<int>();
   pa.err = h->err.as<int>();
   {
     int maxb = 1;
@@ -836,6 +839,8 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
   CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * ls * count));
   CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * ls * 3 * count));
   CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * ls * 3 * count));
+  CUDA_TRY(h, h->gpm.ensure(sizeof(int) * ls * 3 * count));
+  CUDA_TRY(h, h->gsm.ensure(sizeof(int) * ls * 3 * count));
   CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * ps * count));
   CUDA_TRY(h, h->od.ensure(real * odt));
   CUDA_TRY(h, h->r4.ensure(real * r4t));
@@ -1051,7 +1056,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp};
+                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
   for (auto& b : h->imap) b.release();
