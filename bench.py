@@ -217,6 +217,30 @@ def sample_points(col, ctrl):
     return tot
 
 
+def profile_case(args):
+    """A bounded case for ncu captures of one kernel: the OD of one layer of the
+    60-layer column over a narrower window (the full line list stays on the
+    device: 20 MB; the layer's working set is a few hundred MB)."""
+    import torch
+    from clblm_gb300 import build as B
+    from clblm_gb300 import capi, synth
+    from clblm_gb300 import capi_types as T
+    B.build()
+    lines, col, cont = synth.config1()
+    c = col.sub([args.profile_layer]).with_window(*args.window)
+    dn, df, do = capi.setDV(c)
+    g = T.grid_struct(c.v1, c.v2, dn[0], df[0])
+    ctrl = T.od_ctrl(precision=T.CLBLM_PREC_PLAIN if args.plain else T.CLBLM_PREC_MIXED)
+    h = capi.Handle(lines, cont)
+    for _ in range(3):
+        od, dv = h.odlay(c.layer(0), g, ctrl)
+    torch.cuda.synchronize()
+    st = h.stats()
+    print("profile case: layer %d, %.1f-%.1f cm-1, %d points, dv %.3g, panel %.3f ms, f4 %.3f ms"
+          % (args.profile_layer, c.v1, c.v2, len(od), dv, st["ms_panel"], st["ms_f4conv"]))
+    h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,7 +249,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 GPU leg")
+    ap.add_argument("--profile-layer", type=int, default=None,
+                    help="profiling case: the OD of this one layer of the column, three calls, no JSON line")
+    ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
+                    help="spectral window of the profiling case (cm-1)")
+    ap.add_argument("--plain", action="store_true", help="profiling case in FP64")
     args = ap.parse_args()
+    if args.profile_layer is not None:
+        profile_case(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -546,7 +546,6 @@ template <bool Plain>
 __global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
-  constexpr uint32_t kStageBytes = sizeof(Rec) * kF4Chunk;
   __shared__ __align__(128) Rec stage[2][kF4Chunk];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ int64_t rng[2];

@@ -640,20 +640,66 @@ __global__ void k_f4_compact(const F4Prep* __restrict__ prep, int64_t stride, co
   }
 }
 
-// Group list of one layer: one warp replays the record loop.  Centres are
-// compared through their bit patterns (positive centres order like their
-// binary64 images; a non-positive centre is rejected on the host).  Each
-// group records its stream range and how many lines it emits (a non-CO2 line
-// when a non-CO2 member has SP >= 1e-35, a CO2 line likewise), which is what
-// the buffer arithmetic of the record loop counts.
-__global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total,
-                          int64_t stride, const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
-                          const long long* __restrict__ lbits, const unsigned char* __restrict__ flags,
-                          const int64_t* __restrict__ ntot, const int64_t* __restrict__ cut, int4* __restrict__ groups,
-                          int64_t* __restrict__ ngroups) {
-  const int layer = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+// Group list of one layer: one CTA replays LINF4Q's record loop (records of
+// 250 lines appended to a buffer until it holds 1000, then SHRINQ over the
+// lines not yet shrunk, clblm_ODLAY_LineF4.f90:1355-1476 and :1516-1647).
+// Centres are compared through their bit patterns (positive centres order
+// like their binary64 images; a non-positive centre is rejected on the host).
+//
+// Within one SHRINQ call a group that follows a group ending at line b has
+// the limit VLMT = VNU(b) + DVR4/2 and ends at the first line e > b whose
+// successor lies above VLMT.  That end is computed for every b in parallel;
+// one thread then follows the chain from the first group through shared
+// memory, and the groups' flags and output slots come from block scans.
+// Each group records its stream range and how many lines it emits (a
+// non-CO2 line when a non-CO2 member has SP >= 1e-35, a CO2 line likewise),
+// which is what the buffer arithmetic of the record loop counts.
+constexpr int kWalkThreads = 256;
+constexpr int kWalkMax = 1280;  // lines of one SHRINQ call: < 1000 + one 250-line record
+
+// exclusive block scan of one int per thread; returns the block total
+__device__ __forceinline__ int block_scan_excl(int v, int* warp_tot, int* out_excl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int w = 0; w < kWalkThreads / 32; ++w) {
+      int t = warp_tot[w];
+      warp_tot[w] = run;
+      run += t;
+    }
+    warp_tot[kWalkThreads / 32] = run;
+  }
+  __syncthreads();
+  *out_excl = warp_tot[warp] + x - v;
+  int total = warp_tot[kWalkThreads / 32];
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kWalkThreads)
+    k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
+              const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
+              const long long* __restrict__ lbits, const unsigned char* __restrict__ flags,
+              const int64_t* __restrict__ ntot, const int64_t* __restrict__ cut, int4* __restrict__ groups,
+              int64_t* __restrict__ ngroups) {
+  __shared__ long long sv[kWalkMax], sl[kWalkMax];
+  __shared__ short nxt[kWalkMax];          // group end following a group that ends at b
+  __shared__ short ends[kWalkMax];         // group ends of the call, in order
+  __shared__ unsigned char sf[kWalkMax];
+  __shared__ int warp_tot[kWalkThreads / 32 + 1];
+  __shared__ int sh_ng;
+  constexpr int kPer = kWalkMax / kWalkThreads;  // lines (or groups) per thread in the scans
+
+  const int layer = blockIdx.x;
   if (layer >= nlayers) return;
+  const int tid = threadIdx.x;
   const LayerPlan& P = plans[layer + layer0];
   const int64_t n = P.f4_hi - P.f4_lo;
   const int64_t* ci = cidx + (int64_t)layer * (stride + 1);
@@ -673,7 +719,7 @@ __global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int n
   int64_t ng = 0, slot = 0;
   int status = 0;
   bool IEOF = false;
-  for (;;) {
+  for (;;) {  // every thread runs the (uniform) record loop
     if (rec >= nrec_total) {
       IEOF = true;
     } else {
@@ -696,50 +742,73 @@ __global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int n
     }
     // SHRINQ over the unshrunk stream [u0, u1)
     const int64_t u1 = u0 + (IJ - ILO + 1);
+    const int m = (int)(u1 - u0);
+    if (m > kWalkMax) {
+      status = 3;
+      break;
+    }
     int64_t nemit = 0;
-    if (u1 > u0) {
-      int64_t cur = u0;
-      long long vlmt = Lm[u0];
-      int64_t base = cur;
-      long long vnext = 0, vme = 0;
-      unsigned char fme = 0;
-      bool loaded = false;
-      unsigned acc_nc = 0, acc_c2 = 0;
-      while (true) {
-        const int64_t e = base + lane;
-        if (!loaded) {
-          vme = e < u1 ? Lm[e] : 0;
-          vnext = (e + 1 < u1) ? V[e + 1] : 0;
-          fme = e < u1 ? F[e] : 0;
-          loaded = true;
+    if (m > 0) {
+      for (int i = tid; i < m; i += kWalkThreads) {
+        sv[i] = V[u0 + i];
+        sl[i] = Lm[u0 + i];
+        sf[i] = F[u0 + i];
+      }
+      __syncthreads();
+      // the end of the group that starts at b+1 with VLMT = VNU(b) + DVR4/2:
+      // the first e > b with VNU(e+1) > VLMT, or the last line
+      for (int b = tid; b < m; b += kWalkThreads) {
+        const long long lim = sl[b];
+        int j = b + 2;
+        while (j < m && sv[j] <= lim) ++j;
+        nxt[b] = (short)(j - 1 < m - 1 ? j - 1 : m - 1);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        // the first group starts at the first unshrunk line, VLMT = VNU(ILO) + DVR4/2
+        const long long lim = sl[0];
+        int j = 1;
+        while (j < m && sv[j] <= lim) ++j;
+        int e = j - 1;
+        int k = 0;
+        ends[k++] = (short)e;
+        while (e < m - 1) {
+          e = nxt[e];
+          ends[k++] = (short)e;
         }
-        bool inrange = e >= cur && e < u1;
-        bool pred = inrange && (e == u1 - 1 || vnext > vlmt);
-        unsigned m = __ballot_sync(0xffffffffu, pred);
-        int last_lane = m ? __ffs(m) - 1 : 31;
-        bool member = inrange && (lane <= last_lane);
-        acc_nc |= __ballot_sync(0xffffffffu, member && (fme & 1));
-        acc_c2 |= __ballot_sync(0xffffffffu, member && (fme & 2));
-        if (m == 0) {
-          base += 32;
-          loaded = false;
-          continue;
-        }
-        const int64_t eend = base + last_lane;
-        int k = (acc_nc ? 1 : 0) + (acc_c2 ? 1 : 0);
-        if (lane == 0 && ng < stride) G[ng] = make_int4((int)cur, (int)eend, (int)slot, (acc_nc ? 1 : 0) | (acc_c2 ? 2 : 0));
-        ng++;
-        slot += k;
-        nemit += k;
-        acc_nc = acc_c2 = 0;
-        if (eend == u1 - 1) break;
-        vlmt = __shfl_sync(0xffffffffu, vme, last_lane);
-        cur = eend + 1;
-        if (cur >= base + 32) {
-          base = cur;
-          loaded = false;
+        sh_ng = k;
+      }
+      __syncthreads();
+      const int gcount = sh_ng;
+      // which kinds each group emits: OR of its members' flags, then the
+      // output slots by a scan of the emitted counts
+      int kind[kPer], cnt = 0;
+      for (int q = 0; q < kPer; ++q) {
+        const int g = tid * kPer + q;
+        kind[q] = 0;
+        if (g < gcount) {
+          const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g];
+          int f = 0;
+          for (int i = s0; i <= s1; ++i) f |= sf[i];
+          kind[q] = f & 3;
+          cnt += (f & 1) + ((f >> 1) & 1);
         }
       }
+      int excl;
+      const int emitted = block_scan_excl(cnt, warp_tot, &excl);
+      int run = (int)slot + excl;
+      for (int q = 0; q < kPer; ++q) {
+        const int g = tid * kPer + q;
+        if (g < gcount) {
+          const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g];
+          if (ng + g < stride) G[ng + g] = make_int4((int)(u0 + s0), (int)(u0 + s1), run, kind[q]);
+          run += (kind[q] & 1) + ((kind[q] >> 1) & 1);
+        }
+      }
+      ng += gcount;
+      slot += emitted;
+      nemit = emitted;
+      __syncthreads();  // shared arrays are reused by the next call
     }
     u0 = u1;
     const int64_t J = ILO - 1 + nemit;
@@ -750,7 +819,7 @@ __global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int n
     ILO = 1;
     if (IEOF) break;
   }
-  if (lane == 0) {
+  if (tid == 0) {
     ngroups[2 * (layer + layer0)] = status ? -status : ng;
     ngroups[2 * (layer + layer0) + 1] = slot;
   }

@@ -691,7 +691,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
                                                      h->f4src.as<int64_t>(), h->f4flag.as<unsigned char>(),
                                                      h->f4cut.as<int64_t>());
     h->launches++;
-    k_f4_walk<<<count, 32, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
+    k_f4_walk<<<count, 256, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
                                     h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4flag.as<unsigned char>(),
                                     h->f4ntot.as<int64_t>(), h->f4cut.as<int64_t>(), h->f4grp.as<int4>(),
                                     h->f4nout.as<int64_t>());
@@ -948,6 +948,8 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
                              "rules that are not on this path", k + 1, s[4]);
     if (nout[2 * k] == -2)
       return set_err(h, CLBLM_ERR_UNSUPPORTED, "far-wing line window: no line above V2L4 within the prepared range");
+    if (nout[2 * k] < 0)
+      return set_err(h, CLBLM_ERR_RANGE, "far-wing lines: a SHRINQ call longer than the walk buffer");
   }
   if (last_stats) {
     int k = first + count - 1;
