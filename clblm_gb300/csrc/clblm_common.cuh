@@ -90,6 +90,12 @@ struct GridRecD {
   double zfl, zs, a0, a1, a2;
 };
 
+// low parts of ZFkL and ZSLOPE (FP64 value - FP32 value), for the
+// float-float table index near a rounding boundary (mixed path)
+struct GridRecLo {
+  float zfl_lo, zs_lo;
+};
+
 // Far-wing pseudo line after SHRINQ (LINE_SHRINK, clblm_LineData.f90:88-94).
 struct ShrunkLine {
   double vnu, sp, alfa, alfd, spp;

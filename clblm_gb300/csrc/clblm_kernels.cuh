@@ -58,7 +58,8 @@ __global__ void k_scan_apply(const LinePrep* prep, int64_t stride, const int64_t
                              int nblk_stride, int* qpanel);
 __global__ void k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
                                const int* qpanel, int64_t stride, GridRec* rec, GridRecD* recd,
-                               const double* vnu_raw, unsigned long long* stats, double* alfvmax);
+                               GridRecLo* reclo, const double* vnu_raw, unsigned long long* stats,
+                               double* alfvmax);
 __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
 __global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);

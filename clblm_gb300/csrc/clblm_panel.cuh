@@ -19,6 +19,7 @@ struct PanelArgs {
   const double* vft_all;
   const GridRec* rec;
   const GridRecD* recd;
+  const GridRecLo* reclo;
   int64_t stride;
   const int64_t* ranges;     // per panel: candidate record windows of R1, R2, R3
   int64_t panel_stride;

@@ -22,6 +22,8 @@
 // recomputed in FP64).  Plain path: FP64 throughout.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "clblm_bulk.cuh"
 #include "clblm_common.cuh"
 #include "clblm_kernels.cuh"
@@ -47,20 +49,52 @@ struct SumD {
   __device__ __forceinline__ double value() const { return s; }
 };
 
-// FP32 table index IZ = INT(|ZF| + 1.5) with ZF = ZFL + k*ZSLOPE; falls back
-// to the FP64 record when the FP32 argument is too close to a boundary.
-__device__ __forceinline__ int table_index_mixed(int k, const GridRec& r, const GridRecD* rd) {
+// FP32 table index IZ = INT(|ZF| + 1.5) with ZF = ZFL + k*ZSLOPE.  When the
+// FP32 argument lies within 1e-3 of a rounding boundary it is redone in
+// float-float (ZFL and ZSLOPE as hi + lo pairs, products and sums with their
+// exact errors, about 1e-8 absolute), and within 1e-7 of the boundary after
+// that, in FP64 from the record.
+__device__ __noinline__ int table_index_near_boundary(int k, float zfl, float zs, GridRecLo lo, const GridRecD* rd) {
+  const float kf = (float)k;
+  const float p = kf * zs;
+  const float pe = fmaf(kf, zs, -p);                // kf*zs = p + pe exactly
+  const float s = zfl + p;
+  const float bb = s - zfl;
+  const float se = (zfl - (s - bb)) + (p - bb);     // zfl + p = s + se exactly
+  const float tail = se + pe + fmaf(kf, lo.zs_lo, lo.zfl_lo);
+  const float a = fabsf(s), al = s < 0.f ? -tail : tail;
+  const float n = rintf(a);
+  const float dd = (a - n) + al;                    // |ZF| - n
+  if (fabsf(fabsf(dd) - 0.5f) < 1e-7f) {
+    const double zf64 = fma((double)k, rd->zs, rd->zfl);
+    return (int)(fabs(zf64) + 1.5);
+  }
+  return (int)n + 1 + (dd >= 0.5f ? 1 : (dd < -0.5f ? -1 : 0));
+}
+
+__device__ __forceinline__ int table_index_mixed(int k, const GridRec& r, GridRecLo lo, const GridRecD* rd,
+                                                 bool hit = true) {
   float zf = fmaf((float)k, r.zs, r.zfl);
   float az = fabsf(zf);
   float t = az + 12582913.0f;                  // 1.5*2^23 + 1: rounds |ZF|+1
   int iz = __float_as_int(t) - 0x4B400000;     // rint(|ZF|) + 1
   float d = az - (t - 12582913.0f);            // |ZF| - rint(|ZF|), exact
-  if (fabsf(d) > 0.499f) {
-    double zf64 = fma((double)k, rd->zs, rd->zfl);
-    iz = (int)(fabs(zf64) + 1.5);
-  }
+  if (hit && fabsf(d) > 0.499f) iz = table_index_near_boundary(k, r.zfl, r.zs, lo, rd);
   return iz;
 }
+
+// XINT set-up of one panel (clblm_Spectrum.f90:874-915 as called by HIRACQ,
+// clblm_ODLAY.f90:1451-1459): the R4 blocks in use (index 0: the previous
+// panel's, for the carried points 1..5; 1: this panel's), the R3 index
+// limits of both interpolations and the reciprocal spacings
+struct XintPanel {
+  double v1r4[2], recdva4, recdvab;
+  long long m0[2];
+  int nptr4[2], ilo4[2], ihi4[2], blk[2];
+  int iloab, ihiab;
+  int ab0, nab;  // mixed path: ABSRB(ab0 .. ab0+nab-1) staged as FP32 (nab = 0: read from global)
+};
+constexpr int kAbsStage = 64;
 
 // ---------------------------------------------------------------------------
 // shared-memory layout of k_panel
@@ -71,28 +105,34 @@ struct PanelSmem;
 constexpr int kTiles1 = kPanelPts / 32 + 1, kTiles2 = (kR2Pts + 31) / 32, kTiles3 = (kR3Pts + 31) / 32;
 constexpr int kPanelWarps = kPanelThreads / 32;
 
-// record index range [lo, hi) of every tile, and one 32-record staging
-// buffer per warp
+// record index range [lo, hi) of every tile, one 32-record staging buffer
+// per warp, and the panel's XINT set-up
+constexpr int kBatch = 16;  // records per staging batch of a warp
 struct PanelTiles {
   int lo1[kTiles1], hi1[kTiles1], lo2[kTiles2], hi2[kTiles2], lo3[kTiles3], hi3[kTiles3];
-  GridRec wrec[kPanelWarps][32];
+  GridRec wrec[kPanelWarps][kBatch];
+  XintPanel X;
 };
 
+// mixed path: under 74 KB, so that three CTAs share an SM
 template <>
 struct PanelSmem<false> : PanelTiles {
-  float4 t1[kNFMX];
+  GridRecLo wlo[kPanelWarps][kBatch];
+  float absf[kAbsStage];
+  float2 t1ab[kNFMX];    // R1 tables F1, FG
+  float t1c[kNFMX];      // R1 table XVER
   float t2[kNFMX];
   float t3[kNFMX];
   float r3n[kR3Pts];     // R3 p-frame 0..160, lines of panels <= p
   float r3o[8];          // R3 p-frame 0..7, lines of panels <= p-1
   float r2[kR2Pts];      // R2 p-frame 0..615
   int seg_start[kMaxSeg + 1];
-  double seg_v[kMaxSeg], seg_d[kMaxSeg];
+  float segf_v[kMaxSeg], segf_d[kMaxSeg];
   int nseg;
 };
 template <>
 struct PanelSmem<true> : PanelTiles {
-  GridRecD wrecd[kPanelWarps][32];
+  GridRecD wrecd[kPanelWarps][kBatch];
   double t1[3 * kNFMX];
   double t2[kNFMX];
   double t3[kNFMX];
@@ -168,8 +208,7 @@ __device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, dou
 
 // XINT weights of R3 point VI on the grid V1A + (J-1)*DVA (clblm_Spectrum.f90:874-915);
 // returns J and the four weights of A(J-1), A(J), A(J+1), A(J+2).
-__device__ __forceinline__ int xint_weights(double VI, double V1A, double DVA, double w[4]) {
-  double RECDVA = 1. / DVA;
+__device__ __forceinline__ int xint_weights(double VI, double V1A, double DVA, double RECDVA, double w[4]) {
   int J = (int)((VI - V1A) * RECDVA + kONEPL);
   double VJ = V1A + DVA * (double)(J - 1);
   double P = RECDVA * (VI - VJ);
@@ -182,6 +221,18 @@ __device__ __forceinline__ int xint_weights(double VI, double V1A, double DVA, d
   w[2] = (C + B1);
   w[3] = -B2;
   return J;
+}
+
+// the same weights in FP32 from the phase P (mixed path)
+__device__ __forceinline__ void xint_weights_f(float P, float w[4]) {
+  const float C = (3.f - 2.f * P) * P * P;
+  const float B = 0.5f * P * (1.f - P);
+  const float B1 = B * (1.f - P);
+  const float B2 = B * P;
+  w[0] = -B1;
+  w[1] = (1.f - C + B2);
+  w[2] = (C + B1);
+  w[3] = -B2;
 }
 
 // JRAD = 1: LBLF4Q multiplies each R4 block by the piecewise-linear
@@ -217,58 +268,96 @@ __global__ void k_r4_radfac(const LayerPlan* __restrict__ plans, int layer0, con
 // Record ranges of the T tiles [G0 + 32t, G0 + 32t + 31] of one grid from the
 // running max of g_hi (pm) and min of g_lo (sm) over the panel's candidate
 // window [w0, w1): lo(t) = first record with pm >= G0 + 32t, hi(t) = first
-// record with sm > G0 + 32t + 31.  Every thread drops each record of the
-// window into the slot of the last tile it can reach / the last tile it is
-// past, and a suffix minimum over the tiles finishes both.
-__device__ __forceinline__ void tile_ranges_scatter(const int* __restrict__ pm, const int* __restrict__ sm,
-                                                    int64_t w0, int64_t w1, int G0, int T, int* lo, int* hi) {
+// record with sm > G0 + 32t + 31 (w1 when there is none).  Both running
+// bounds are monotone, so each tile boundary is crossed by exactly one
+// record of the window (the first one for boundaries at or below its value),
+// and that record writes it.
+__device__ __forceinline__ long long floordiv32(long long x) { return x >> 5; }  // arithmetic shift: floor
+__device__ __forceinline__ void tile_ranges(const int* __restrict__ pm, const int* __restrict__ sm, int64_t w0,
+                                            int64_t w1, int G0, int T, int* lo, int* hi) {
+  const long long g0 = G0;
   for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
-    const int v = pm[i];
-    if (v >= G0) atomicMin(&lo[min((v - G0) >> 5, T - 1)], (int)i);
-    const int s = sm[i];
-    if (s - G0 > 31) atomicMin(&hi[min((s - G0) >> 5, T) - 1], (int)i);
-  }
-}
-__device__ __forceinline__ void tile_ranges_finish(int T, int* lo, int* hi) {
-  for (int t = T - 2; t >= 0; --t) {
-    lo[t] = min(lo[t], lo[t + 1]);
-    hi[t] = min(hi[t], hi[t + 1]);
+    // lo: tiles t with prev < G0 + 32 t <= cur
+    const long long cur = pm[i];
+    const long long prev = (i == w0) ? LLONG_MIN / 4 : (long long)pm[i - 1];
+    long long ta = (prev < g0) ? 0 : floordiv32(prev - g0) + 1;
+    long long tb = (cur < g0) ? -1 : min(floordiv32(cur - g0), (long long)T - 1);
+    for (long long t = ta; t <= tb; ++t) lo[t] = (int)i;
+    // hi: tiles t with prev <= G0 + 32 t + 31 < cur
+    const long long curs = sm[i];
+    const long long prevs = (i == w0) ? LLONG_MIN / 4 : (long long)sm[i - 1];
+    ta = (prevs - g0 - 31 <= 0) ? 0 : floordiv32(prevs - g0);
+    tb = (curs - g0 - 32 < 0) ? -1 : min(floordiv32(curs - g0 - 32), (long long)T - 1);
+    for (long long t = ta; t <= tb; ++t) hi[t] = (int)i;
   }
 }
 
+// Contribution of one record at global point g of the lane (mixed path):
+// zero unless the record's range holds g and its panel is at most qmax.
+template <int GRID>
+__device__ __forceinline__ float contrib_mixed(const PanelSmem<false>& S, const GridRec& r, GridRecLo lo,
+                                               const GridRecD* rd, int g, int qmax, int* err) {
+  bool hit = g >= r.g_lo && g <= r.g_hi && r.q <= qmax;
+  int iz = table_index_mixed(g - r.g_lo + 1, r, lo, rd, hit);
+  if (hit && iz > kNFMX) {
+    atomicOr(err, 2);
+    hit = false;
+  }
+  iz = hit ? iz : 1;
+  float v;
+  if constexpr (GRID == 1) {
+    const float2 ab = S.t1ab[iz - 1];
+    v = fmaf(r.a0, ab.x, fmaf(r.a1, ab.y, r.a2 * S.t1c[iz - 1]));
+  } else if constexpr (GRID == 2) {
+    v = r.a0 * S.t2[iz - 1];
+  } else {
+    v = r.a0 * S.t3[iz - 1];
+  }
+  return hit ? v : 0.f;
+}
+
 // Sum over the records [lo, hi) of one grid at global point g of the lane:
-// the records pass through the warp's shared-memory buffer 32 at a time,
-// the next 32 already loaded into registers while the current ones are used.
+// the records pass through the warp's shared-memory buffer kBatch at a time,
+// the next batch already loaded into registers while the current one is used.
+// The FP64 path adds record by record in record order; the mixed path adds
+// the records in pairs (one FP32 sum per pair into the Kahan sum).
 template <bool Plain, int GRID>
 __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs& a, const GridRec* __restrict__ rec,
-                                            const GridRecD* __restrict__ recd, int64_t lo, int64_t hi, int g,
-                                            bool active, int qmax, typename std::conditional<Plain, SumD, KahanF>::type& acc) {
+                                            const GridRecD* __restrict__ recd, const GridRecLo* __restrict__ reclo,
+                                            int64_t lo, int64_t hi, int g, bool active, int qmax,
+                                            typename std::conditional<Plain, SumD, KahanF>::type& acc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sl = lane & (kBatch - 1);
   GridRec* buf = S.wrec[warp];
   GridRec nxt;
   GridRecD nxtd;
-  if (lo + lane < hi) {
-    nxt = rec[lo + lane];
-    if constexpr (Plain) nxtd = recd[lo + lane];
+  GridRecLo nxtl;
+  if (lo + sl < hi) {
+    nxt = rec[lo + sl];
+    if constexpr (Plain) nxtd = recd[lo + sl];
+    else nxtl = reclo[lo + sl];
   }
-  for (int64_t base = lo; base < hi; base += 32) {
+  for (int64_t base = lo; base < hi; base += kBatch) {
     __syncwarp();
-    buf[lane] = nxt;
-    if constexpr (Plain) S.wrecd[warp][lane] = nxtd;
+    if (lane < kBatch) {
+      buf[lane] = nxt;
+      if constexpr (Plain) S.wrecd[warp][lane] = nxtd;
+      else S.wlo[warp][lane] = nxtl;
+    }
     __syncwarp();
-    const int cnt = (int)(hi - base < 32 ? hi - base : 32);
-    if (base + 32 + lane < hi) {
-      nxt = rec[base + 32 + lane];
-      if constexpr (Plain) nxtd = recd[base + 32 + lane];
+    const int cnt = (int)(hi - base < kBatch ? hi - base : kBatch);
+    if (base + kBatch + sl < hi) {
+      nxt = rec[base + kBatch + sl];
+      if constexpr (Plain) nxtd = recd[base + kBatch + sl];
+      else nxtl = reclo[base + kBatch + sl];
     }
     if (!active) continue;
-    for (int k = 0; k < cnt; ++k) {
-      const GridRec r = buf[k];
-      if (g < r.g_lo || g > r.g_hi || r.q > qmax) continue;
-      const int kk = g - r.g_lo + 1;
-      if constexpr (Plain) {
+    if constexpr (Plain) {
+      for (int k = 0; k < cnt; ++k) {
+        const GridRec r = buf[k];
+        if (g < r.g_lo || g > r.g_hi || r.q > qmax) continue;
         const GridRecD& d = S.wrecd[warp][k];
-        const int iz = (int)(fabs(fma((double)kk, d.zs, d.zfl)) + 1.5);
+        const int iz = (int)(fabs(fma((double)(g - r.g_lo + 1), d.zs, d.zfl)) + 1.5);
         if (iz > kNFMX) {
           atomicOr(a.err, 2);
           continue;
@@ -281,20 +370,13 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
         } else {
           acc.add(d.a0 * S.t3[iz - 1]);
         }
-      } else {
-        const int iz = table_index_mixed(kk, r, recd + (base + k));
-        if (iz > kNFMX) {
-          atomicOr(a.err, 2);
-          continue;
-        }
-        if constexpr (GRID == 1) {
-          const float4 T = S.t1[iz - 1];
-          acc.add(fmaf(r.a0, T.x, fmaf(r.a1, T.y, r.a2 * T.z)));
-        } else if constexpr (GRID == 2) {
-          acc.add(r.a0 * S.t2[iz - 1]);
-        } else {
-          acc.add(r.a0 * S.t3[iz - 1]);
-        }
+      }
+    } else {
+      for (int k = 0; k < cnt; k += 2) {
+        const int k1 = (k + 1 < cnt) ? k + 1 : k;
+        float v0 = contrib_mixed<GRID>(S, buf[k], S.wlo[warp][k], recd + (base + k), g, qmax, a.err);
+        float v1 = contrib_mixed<GRID>(S, buf[k1], S.wlo[warp][k1], recd + (base + k1), g, qmax, a.err);
+        acc.add(k1 != k ? v0 + v1 : v0);
       }
     }
   }
@@ -302,7 +384,7 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
 }
 
 template <bool Plain>
-__global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
+__global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -329,13 +411,84 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
     }
   } else {
     for (int i = tid; i < kNFMX; i += blockDim.x) {
-      S.t1[i] = a.tabs.t1f[i];
+      const float4 t = a.tabs.t1f[i];
+      S.t1ab[i] = make_float2(t.x, t.y);
+      S.t1c[i] = t.z;
       S.t2[i] = a.tabs.t2f[i];
       S.t3[i] = a.tabs.t3f[i];
     }
   }
-  // ---- radiation-term segments of this panel (panelOut, JRAD = 0) ----
-  if (tid == 0) {
+  __syncthreads();
+
+  const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
+  const GridRec* rec2 = rec1 + a.stride;
+  const GridRec* rec3 = rec2 + a.stride;
+  const GridRecD* rd1 = a.recd + (int64_t)layer * a.stride * 3;
+  const GridRecD* rd2 = rd1 + a.stride;
+  const GridRecD* rd3 = rd2 + a.stride;
+  const GridRecLo* rl1 = a.reclo + (int64_t)layer * a.stride * 3;
+  const GridRecLo* rl2 = rl1 + a.stride;
+  const GridRecLo* rl3 = rl2 + a.stride;
+  const int64_t* rg = a.ranges + ((int64_t)layer * a.panel_stride + p) * 6;
+  const int* pm1 = a.pmax_g + (int64_t)layer * a.stride * 3;
+  const int* sm1 = a.smin_g + (int64_t)layer * a.stride * 3;
+
+  // ---- record range of every 32-point tile of the three grids ----
+  const int nT1 = (NHI - kNSHIFT + 31) / 32;
+  const int G01 = kPanelPts * p + kNSHIFT, G02 = kPanelR2 * p - 1, G03 = kPanelR3 * p - 1;
+  for (int t = tid; t < kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
+  for (int t = tid; t < kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
+  for (int t = tid; t < kTiles3; t += blockDim.x) S.lo3[t] = S.hi3[t] = (int)rg[5];
+  if (tid == 0) {  // XINT set-up of the panel (once, in FP64)
+    XintPanel& X = S.X;
+    const double DVR3 = 16. * dv;
+    if (P.nptr4 > 0) {
+      X.recdva4 = 1. / P.dvr4;
+      for (int c = 0; c < 2; ++c) {
+        const int b = a.panel_blk[P.vft_off + ((c == 0 && p > 0) ? p - 1 : p)];
+        const double V1R4 = a.blk_v1[P.blk_off + b];
+        const int NPTR4 = a.blk_n[P.blk_off + b];
+        const double V2R4 = V1R4 + P.dvr4 * (double)(NPTR4 - 1);
+        X.blk[c] = b;
+        X.v1r4[c] = V1R4;
+        X.nptr4[c] = NPTR4;
+        X.m0[c] = a.blk_m0[P.blk_off + b];
+        X.ilo4[c] = (int)((V1R4 + P.dvr4 - VFT) / DVR3 + 1. + kONEMI);
+        X.ihi4[c] = (int)((V2R4 - P.dvr4 - VFT) / DVR3 + kONEMI);
+      }
+    }
+    X.nab = 0;
+    if (P.contnm) {
+      X.recdvab = 1. / P.dvabs;
+      X.iloab = (int)((P.v1abs + P.dvabs - VFT) / DVR3 + 1. + kONEMI);
+      X.ihiab = (int)((P.v2abs - P.dvabs - VFT) / DVR3 + kONEMI);
+      if constexpr (!Plain) {
+        const int j3a = max(X.iloab, 0), j3b = min(X.ihiab, kR3Pts - 1);
+        if (j3a <= j3b) {
+          const int Ja = (int)((VFT + DVR3 * (double)(j3a - 1) - P.v1abs) * X.recdvab + kONEPL);
+          const int Jb = (int)((VFT + DVR3 * (double)(j3b - 1) - P.v1abs) * X.recdvab + kONEPL);
+          if (Jb + 2 - (Ja - 1) + 1 <= kAbsStage) {
+            X.ab0 = Ja - 1;
+            X.nab = Jb + 2 - (Ja - 1) + 1;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if constexpr (!Plain) {  // ABSRB of the panel as FP32
+    const double* AB = a.absrb_all + P.abs_off;  // 1-based
+    for (int i = tid; i < S.X.nab; i += blockDim.x) S.absf[i] = (float)AB[S.X.ab0 + i];
+  }
+  if (nT1 > 0) tile_ranges(pm1, sm1, rg[0], rg[1], G01, nT1, S.lo1, S.hi1);
+  tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, kTiles2, S.lo2, S.hi2);
+  tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, kTiles3, S.lo3, S.hi3);
+  __syncthreads();
+
+  // ---- R3: line sums on p-frame points 0..160 (new) and 0..7 (old) ----
+  // units 0..kTiles3-1: 32 new points each; unit kTiles3: the 8 old points
+  static_assert(kTiles3 + 1 < kPanelWarps, "the last warp has no R3 unit");
+  if (warp == kPanelWarps - 1 && lane == 0) {  // idle in the R3 phase: radiation-term segments (panelOut, JRAD = 0)
     int ns = 0;
     if (P.jrad == 0) {
       const int NLO = kNSHIFT + 1;
@@ -353,8 +506,13 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
         if (N2 > NHI) N2 = NHI;
         if (ns < kMaxSeg) {
           S.seg_start[ns] = N1;
-          S.seg_v[ns] = RADVI;
-          S.seg_d[ns] = RDEL;
+          if constexpr (Plain) {
+            S.seg_v[ns] = RADVI;
+            S.seg_d[ns] = RDEL;
+          } else {
+            S.segf_v[ns] = (float)RADVI;
+            S.segf_d[ns] = (float)RDEL;
+          }
         }
         ns++;
       } while (N2 < NHI);
@@ -363,36 +521,6 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
     }
     S.nseg = min(ns, kMaxSeg);
   }
-  __syncthreads();
-
-  const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
-  const GridRec* rec2 = rec1 + a.stride;
-  const GridRec* rec3 = rec2 + a.stride;
-  const GridRecD* rd1 = a.recd + (int64_t)layer * a.stride * 3;
-  const GridRecD* rd2 = rd1 + a.stride;
-  const GridRecD* rd3 = rd2 + a.stride;
-  const int64_t* rg = a.ranges + ((int64_t)layer * a.panel_stride + p) * 6;
-  const int* pm1 = a.pmax_g + (int64_t)layer * a.stride * 3;
-  const int* sm1 = a.smin_g + (int64_t)layer * a.stride * 3;
-
-  // ---- record range of every 32-point tile of the three grids ----
-  const int nT1 = (NHI - kNSHIFT + 31) / 32;
-  const int G01 = kPanelPts * p + kNSHIFT, G02 = kPanelR2 * p - 1, G03 = kPanelR3 * p - 1;
-  for (int t = tid; t < kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
-  for (int t = tid; t < kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
-  for (int t = tid; t < kTiles3; t += blockDim.x) S.lo3[t] = S.hi3[t] = (int)rg[5];
-  __syncthreads();
-  if (nT1 > 0) tile_ranges_scatter(pm1, sm1, rg[0], rg[1], G01, nT1, S.lo1, S.hi1);
-  tile_ranges_scatter(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, kTiles2, S.lo2, S.hi2);
-  tile_ranges_scatter(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, kTiles3, S.lo3, S.hi3);
-  __syncthreads();
-  if (tid == 0 && nT1 > 0) tile_ranges_finish(nT1, S.lo1, S.hi1);
-  if (tid == 32) tile_ranges_finish(kTiles2, S.lo2, S.hi2);
-  if (tid == 64) tile_ranges_finish(kTiles3, S.lo3, S.hi3);
-  __syncthreads();
-
-  // ---- R3: line sums on p-frame points 0..160 (new) and 0..7 (old) ----
-  // units 0..kTiles3-1: 32 new points each; unit kTiles3: the 8 old points
   for (int u = warp; u <= kTiles3; u += kPanelWarps) {
     const bool old = (u == kTiles3);
     const int J3 = old ? lane : u * 32 + lane;  // p-frame index
@@ -402,49 +530,69 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
     const int t = old ? 0 : u;
     const int64_t lo = S.lo3[t], hi = max(S.lo3[t], S.hi3[t]);
     Acc acc;
-    gather_grid<Plain, 3>(S, a, rec3, rd3, lo, hi, g, active, qmax, acc);
+    gather_grid<Plain, 3>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
     if (active) {
-      // far wings (R4) and continuum (ABSRB) interpolated into R3
-      double VI = VFT + (16. * dv) * (double)(J3 - 1);
-      double extra = 0.;
-      if (P.nptr4 > 0) {
-        // the R4 block LBLF4Q held when XINT reached the point: this panel's
-        // for N1R3 = 6..155, the previous panel's for the carried points
-        // 1..5 (XINT'd there as 151..155)
-        const Real* R4 = reinterpret_cast<const Real*>(a.r4_all) + P.r4_off;  // global R4[m]
-        const int b = a.panel_blk[P.vft_off + ((p > 0 && J3 < 6) ? p - 1 : p)];
-        const double V1R4 = a.blk_v1[P.blk_off + b];
-        const int NPTR4 = a.blk_n[P.blk_off + b];
-        const int64_t m0 = a.blk_m0[P.blk_off + b];
-        const double V2R4 = V1R4 + P.dvr4 * (double)(NPTR4 - 1);
-        int ILO = (int)((V1R4 + P.dvr4 - VFT) / (16. * dv) + 1. + kONEMI);
-        int IHI = (int)((V2R4 - P.dvr4 - VFT) / (16. * dv) + kONEMI);
-        if (J3 >= ILO && J3 <= IHI) {
+      // far wings (R4) and continuum (ABSRB) interpolated into R3 (XINT).
+      // The R4 block LBLF4Q held when XINT reached the point: this panel's
+      // for N1R3 = 6..155, the previous panel's for the carried points 1..5
+      // (XINT'd there as 151..155).
+      const XintPanel& X = S.X;
+      const double VI = VFT + (16. * dv) * (double)(J3 - 1);
+      const int c = (p > 0 && J3 < 6) ? 0 : 1;
+      const Real* R4 = reinterpret_cast<const Real*>(a.r4_all) + P.r4_off;  // global R4[m]
+      const double* fac = a.blk_fac + (P.blk_off + X.blk[c]) * (int64_t)(kLIMOUT4 + 2);
+      const double* AB = a.absrb_all + P.abs_off;  // 1-based
+      Real extra = 0;
+      if constexpr (Plain) {
+        if (P.nptr4 > 0 && J3 >= X.ilo4[c] && J3 <= X.ihi4[c]) {
           double w[4];
-          int J = xint_weights(VI, V1R4, P.dvr4, w);
-          const double* fac = a.blk_fac + (P.blk_off + b) * (int64_t)(kLIMOUT4 + 2);
+          int J = xint_weights(VI, X.v1r4[c], P.dvr4, X.recdva4, w);
           for (int k = 0; k < 4; ++k) {
             int jb = J - 1 + k;  // 1-based point of the block; zero past NPTR4
             double v = 0.;
-            if (jb >= 1 && jb <= NPTR4 && m0 + jb - 1 < P.nptr4) {
-              v = (double)R4[m0 + jb - 1];
+            if (jb >= 1 && jb <= X.nptr4[c] && X.m0[c] + jb - 1 < P.nptr4) {
+              v = R4[X.m0[c] + jb - 1];
               if (P.jrad == 1) v *= fac[jb - 1];
             }
             extra += v * w[k];
           }
         }
-      }
-      if (P.contnm) {
-        const double* AB = a.absrb_all + P.abs_off;  // 1-based
-        int ILO = (int)((P.v1abs + P.dvabs - VFT) / (16. * dv) + 1. + kONEMI);
-        int IHI = (int)((P.v2abs - P.dvabs - VFT) / (16. * dv) + kONEMI);
-        if (J3 >= ILO && J3 <= IHI) {
+        if (P.contnm && J3 >= X.iloab && J3 <= X.ihiab) {
           double w[4];
-          int J = xint_weights(VI, P.v1abs, P.dvabs, w);
+          int J = xint_weights(VI, P.v1abs, P.dvabs, X.recdvab, w);
           extra += AB[J - 1] * w[0] + AB[J] * w[1] + AB[J + 1] * w[2] + AB[J + 2] * w[3];
         }
+      } else {
+        // FP64 only for the index and phase; weights and values in FP32
+        if (P.nptr4 > 0 && J3 >= X.ilo4[c] && J3 <= X.ihi4[c]) {
+          const double t = (VI - X.v1r4[c]) * X.recdva4;
+          const int J = (int)(t + kONEPL);
+          float w[4];
+          xint_weights_f((float)(t - (double)(J - 1)), w);
+          for (int k = 0; k < 4; ++k) {
+            int jb = J - 1 + k;
+            float v = 0.f;
+            if (jb >= 1 && jb <= X.nptr4[c] && X.m0[c] + jb - 1 < P.nptr4) {
+              v = R4[X.m0[c] + jb - 1];
+              if (P.jrad == 1) v *= (float)fac[jb - 1];
+            }
+            extra = fmaf(v, w[k], extra);
+          }
+        }
+        if (P.contnm && J3 >= X.iloab && J3 <= X.ihiab) {
+          const double t = (VI - P.v1abs) * X.recdvab;
+          const int J = (int)(t + kONEPL);
+          float w[4];
+          xint_weights_f((float)(t - (double)(J - 1)), w);
+          const int o = J - 1 - X.ab0;
+          if (X.nab > 0 && o >= 0 && o + 3 < X.nab) {
+            extra += S.absf[o] * w[0] + S.absf[o + 1] * w[1] + S.absf[o + 2] * w[2] + S.absf[o + 3] * w[3];
+          } else {
+            extra += (float)AB[J - 1] * w[0] + (float)AB[J] * w[1] + (float)AB[J + 1] * w[2] + (float)AB[J + 2] * w[3];
+          }
+        }
       }
-      acc.add((Real)extra);
+      acc.add(extra);
       if (old) S.r3o[J3] = acc.value();
       else S.r3n[J3] = acc.value();
     }
@@ -463,7 +611,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
       bool active = J >= 5 && J < kR2Pts;
       int g = kPanelR2 * p + J - 1;
       Acc acc;
-      gather_grid<Plain, 2>(S, a, rec2, rd2, S.lo2[tile], max(S.lo2[tile], S.hi2[tile]), g, active, p, acc);
+      gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[tile], max(S.lo2[tile], S.hi2[tile]), g, active, p, acc);
       if (active) {
         int off = (J - 1) & 3;
         int Jg = J - off;
@@ -496,7 +644,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
       bool active = J <= NHI;
       int g = kPanelPts * p + J - 1;
       Acc acc;
-      gather_grid<Plain, 1>(S, a, rec1, rd1, S.lo1[tile], max(S.lo1[tile], S.hi1[tile]), g, active, p, acc);
+      gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[tile], max(S.lo1[tile], S.hi1[tile]), g, active, p, acc);
       if (active) {
         int off = (J - 33) & 3;
         int Jg = J - off;
@@ -517,8 +665,12 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs a) {
             if (S.seg_start[m] <= J) s0 = m;
             else s1 = m;
           }
-          double f = S.seg_v[s0] + (double)(J - S.seg_start[s0]) * S.seg_d[s0];
-          val = (Real)((double)val * f);
+          if constexpr (Plain) {
+            double f = S.seg_v[s0] + (double)(J - S.seg_start[s0]) * S.seg_d[s0];
+            val = val * f;
+          } else {
+            val *= fmaf((float)(J - S.seg_start[s0]), S.segf_d[s0], S.segf_v[s0]);
+          }
         }
         od[(int64_t)kPanelPts * p + (J - kNSHIFT - 1)] = val;
       }

@@ -257,7 +257,8 @@ __device__ __forceinline__ void interp_coef(const double* tab, int IZM, double Z
 __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vft_all,
                                const LinePrep* __restrict__ prep, const int* __restrict__ qpanel, int64_t stride,
                                GridRec* __restrict__ rec, GridRecD* __restrict__ recd,
-                               const double* __restrict__ vnu_raw, unsigned long long* __restrict__ stats,
+                               GridRecLo* __restrict__ reclo, const double* __restrict__ vnu_raw,
+                               unsigned long long* __restrict__ stats,
                                double* __restrict__ alfvmax) {
   int layer = blockIdx.y;
   const LayerPlan& P = plans[layer + layer0];
@@ -283,6 +284,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
     g1.zs = g2.zs = g3.zs = 0.f;
     g1.a0 = g1.a1 = g1.a2 = g2.a0 = g2.a1 = g2.a2 = g3.a0 = g3.a1 = g3.a2 = 0.f;
     GridRecD d1 = {0, 0, 0, 0, 0}, d2 = d1, d3 = d1;
+    GridRecLo l1 = {0.f, 0.f}, l2 = l1, l3 = l1;
     if (lp.fpanel >= 0 && q < P.npanels) {
       // a line of a later record is read in the panel the previous record
       // ended in; dropping it there (HWF3*ALFV + VNU < VFT) is not modelled
@@ -337,6 +339,10 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       d1 = {ZF1L, ZSLOPE, STRFA1, STRDA, STRVRA};
       d2 = {ZF2L, ZSLOPE, STRFA2, 0., 0.};
       d3 = {ZF3L, ZSLOPE, STRFA3, 0., 0.};
+      const float zs_lo = (float)(ZSLOPE - (double)g1.zs);
+      l1 = {(float)(ZF1L - (double)g1.zfl), zs_lo};
+      l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
+      l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
       amax = fmax(amax, 1. / lp.recalf);
     }
     int64_t o = (int64_t)layer * stride * 3;
@@ -346,6 +352,9 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
     recd[o + t] = d1;
     recd[o + stride + t] = d2;
     recd[o + 2 * stride + t] = d3;
+    reclo[o + t] = l1;
+    reclo[o + stride + t] = l2;
+    reclo[o + 2 * stride + t] = l3;
   }
   for (int off = 16; off > 0; off >>= 1) amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, off));
   unsigned long long b = bad;

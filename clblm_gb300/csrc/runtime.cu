@@ -77,6 +77,7 @@ struct clblm_handle {
   DevBuf f4prep, f4sh, f4nout, f4rec, f4recd, f4nrec, f4nmir, f4pm, f4sm, err;
   DevBuf pblk, bv1, bn, bm0, bfac;
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
+  DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp;
   DevBuf rt[4], outbuf, imap[2];
   std::string errmsg;
@@ -117,7 +118,6 @@ int set_err(clblm_handle* h, int code, const char* fmt, ...) {
 // ---- constants (src/common/clblm_ConstParam.f90) ----
 const double kBOLTZ = 1.3806503E-16, kCLIGHT = 2.99792458E+10, kAVOGAD = 6.02214199E+23;
 const double kPI_C = 3.1415926535898;
-const int kMAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
 
 double radfn_h(double VI, double XKT) {  // RADFN, clblm_ODLAY_CommonSub.f90:293-323
   double XVI = VI;
@@ -747,7 +747,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   h->launches++;
   k_line_records<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
       dplans, first, h->vft.as<double>(), h->prep.as<LinePrep>(), h->qpanel.as<int>(), lstride, h->rec.as<GridRec>(),
-      h->recd.as<GridRecD>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(), h->alfvmax.as<double>());
+      h->recd.as<GridRecD>(), h->reclo.as<GridRecLo>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(),
+      h->alfvmax.as<double>());
   h->launches++;
   k_rec_bounds<<<3 * count, 1024, 0, st>>>(dplans, first, h->rec.as<GridRec>(), lstride, h->gpm.as<int>(),
                                            h->gsm.as<int>());
@@ -763,6 +764,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.vft_all = h->vft.as<double>();
   pa.rec = h->rec.as<GridRec>();
   pa.recd = h->recd.as<GridRecD>();
+  pa.reclo = h->reclo.as<GridRecLo>();
   pa.stride = lstride;
   pa.ranges = h->ranges.as<int64_t>();
   pa.panel_stride = pstride;
@@ -840,6 +842,7 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
   CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * ls * 3 * count));
   CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * ls * 3 * count));
   CUDA_TRY(h, h->gpm.ensure(sizeof(int) * ls * 3 * count));
+  CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * ls * 3 * count));
   CUDA_TRY(h, h->gsm.ensure(sizeof(int) * ls * 3 * count));
   CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * ps * count));
   CUDA_TRY(h, h->od.ensure(real * odt));
@@ -1058,7 +1061,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm};
+                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm,      &h->reclo};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
   for (auto& b : h->imap) b.release();
