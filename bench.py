@@ -241,6 +241,27 @@ def profile_case(args):
     h.close()
 
 
+def profile_column(args):
+    """A bounded radiance case for ncu captures: adjacent layers of the column
+    over the full window."""
+    import torch
+    from clblm_gb300 import build as B
+    from clblm_gb300 import capi, synth
+    from clblm_gb300 import capi_types as T
+    B.build()
+    lines, col, cont = synth.config1()
+    c = col.sub(list(range(*args.profile_column)))
+    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN if args.plain else T.CLBLM_PREC_MIXED)
+    h = capi.Handle(lines, cont)
+    for _ in range(2):
+        rad, dv = h.rt_mode2(c, ctrl)
+    torch.cuda.synchronize()
+    st = h.stats()
+    print("profile column: layers %d-%d, %d radiance points, %d launches per call"
+          % (args.profile_column[0], args.profile_column[1] - 1, len(rad), st["launches"]))
+    h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,9 +275,14 @@ def main():
     ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
                     help="spectral window of the profiling case (cm-1)")
     ap.add_argument("--plain", action="store_true", help="profiling case in FP64")
+    ap.add_argument("--profile-column", type=int, nargs=2, default=None, metavar=("FIRST", "LAST"),
+                    help="profiling case: the radiance of layers FIRST..LAST-1 of the column, two calls")
     args = ap.parse_args()
     if args.profile_layer is not None:
         profile_case(args)
+        return
+    if args.profile_column is not None:
+        profile_column(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))

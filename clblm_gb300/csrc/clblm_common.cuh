@@ -39,6 +39,8 @@ struct LayerPlan {
   // grid
   double v1, v2, dv, dvr2, dvr3, alfav, alfmax, bound, vbot, vtop, vft0;
   double pave, tave, wtot, xkt, xkt0, betacr, tratio, rhorat, pavp0, pavp2;
+  double ln_tratio;               // log(T/296): (T/296)^n = exp(n log(T/296))
+  int mixed;                      // 1: FP32 for strengths and shape coefficients
   double dptmn, dptfc;
   int jrad, ilnflg, max1, max2, max3, nalfmax, nbound;
   int npanels, nhi_last;          // panels and NHI of the last panel

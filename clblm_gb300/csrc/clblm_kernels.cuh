@@ -49,6 +49,8 @@ struct ShapeTabs {
 
 // kernels of prep.cu (FP64, no FMA contraction)
 extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
+// FP32 copies of CF1, CF2, CF3, CGAUSS, CER (mixed-path shape coefficients)
+extern __constant__ float c_SHAPEf[5][102];
 __global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const double* vft_all, LinePrep* out,
                             int64_t out_stride, unsigned long long* stats);
 __global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,

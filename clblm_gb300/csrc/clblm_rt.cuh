@@ -14,6 +14,7 @@ struct InterpSpec {
   int nint_ratio;   // NINT(dvRatio) for itype 0
   int len_in, len_out;
   double b1[10], b2[10], b3[10], b4[10];
+  float bf[4][10];  // FP32 copies of b1..b4 (mixed path)
   double v1, dvin, dvout, ratio;
   int64_t nin;
   const int2* map;  // itype < 0: (iIn, IP) of each output point, replayed by k_interp_map

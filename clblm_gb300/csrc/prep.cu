@@ -23,6 +23,7 @@
 namespace clblm {
 
 __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
+__constant__ float c_SHAPEf[5][102];
 // MaxISOTPL_smass, clblm_ConstParam.f90:246-251 (molecules 1..9)
 __constant__ int c_MAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
 
@@ -36,6 +37,18 @@ __device__ __forceinline__ double radfn_d(double VI, double XKT) {
       double E = exp(-XVIOKT);
       return XVI * (1. - E) / (1. + E);
     }
+  }
+  return XVI;
+}
+
+// RADFN in FP32 (mixed-path strengths): v tanh(v/2kT) with the same branches
+__device__ __forceinline__ float radfn_f(float XVI, float XKT) {
+  if (XKT <= 0.f) return XVI;
+  const float x = XVI / XKT;
+  if (x <= 0.01f) return 0.5f * x * XVI;
+  if (x <= 10.f) {
+    const float e = __expf(-x);
+    return XVI * (1.f - e) / (1.f + e);
   }
   return XVI;
 }
@@ -78,7 +91,6 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     double SUI = 0.;
     if (ok) {
       SUI = (double)lines.sp[i] * P.wk[m];
-      if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
       if (SUI == 0.) ok = false;
     }
     if (ok) {
@@ -87,7 +99,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
       double hwhms = (double)lines.hwhm[i];
       if (m == 7) alfa0 = (alfa0 - 0.21 * hwhms) / (1.0 - 0.21);
       double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
-      double TMPCOR = pow(P.tratio, (double)lines.tmpalf[i]);
+      double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
       double ALFL = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
@@ -118,7 +130,19 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
           double RECALF = 1. / ALFV;
           double EPP = (double)lines.epp[i];
           if (EPP <= -1.001) EPP = fabs(EPP);
-          if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
+          if (P.mixed) {
+            // strengths set no index: FP32 (RADFN when JRAD = 1, SCOR, the
+            // lower-state Boltzmann factor and the stimulated-emission term)
+            float sui = (float)SUI;
+            if (P.jrad == 1) sui *= radfn_f((float)lines.vnu[i], (float)P.xkt);
+            if (EPP > -0.999)
+              sui = sui * (float)P.scor[m] * __expf(-(float)EPP * (float)P.betacr) *
+                    (1.f + __expf(-(float)VNU / (float)P.xkt));
+            SUI = sui;
+          } else {
+            if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
+            if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
+          }
           double SP = SUI * (1. + 0. * P.pavp2);
           if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
             double SPEAK = SUI * RECALF;
@@ -300,11 +324,25 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       int IZM = lp.iz;
       double ZETDIF = 100. * lp.zetai - (double)(IZM - 1);
       double STRFA1, STRFA2, STRFA3, STRDA, STRVRA;
-      interp_coef(c_CF1, IZM, ZETDIF, DEPTHA, &STRFA1);
-      interp_coef(c_CF2, IZM, ZETDIF, DEPTHA, &STRFA2);
-      interp_coef(c_CF3, IZM, ZETDIF, DEPTHA, &STRFA3);
-      interp_coef(c_CGAUSS, IZM, ZETDIF, DEPTHA, &STRDA);
-      interp_coef(c_CER, IZM, ZETDIF, DEPTHA, &STRVRA);
+      if (P.mixed) {  // shape coefficients set no index: FP32
+        const float zd = (float)ZETDIF, de = (float)DEPTHA;
+        float c[5];
+        for (int q5 = 0; q5 < 5; ++q5) {
+          const float* T = c_SHAPEf[q5];
+          c[q5] = de * (T[IZM - 1] + zd * (T[IZM] - T[IZM - 1]));
+        }
+        STRFA1 = c[0];
+        STRFA2 = c[1];
+        STRFA3 = c[2];
+        STRDA = c[3];
+        STRVRA = c[4];
+      } else {
+        interp_coef(c_CF1, IZM, ZETDIF, DEPTHA, &STRFA1);
+        interp_coef(c_CF2, IZM, ZETDIF, DEPTHA, &STRFA2);
+        interp_coef(c_CF3, IZM, ZETDIF, DEPTHA, &STRFA3);
+        interp_coef(c_CGAUSS, IZM, ZETDIF, DEPTHA, &STRDA);
+        interp_coef(c_CER, IZM, ZETDIF, DEPTHA, &STRVRA);
+      }
       double ZSLOPE = lp.recalf * WAVDXF;
       double ZINT = (lp.vnu - vft[q]) / P.dv;
       double BHWDXF = HWDXF / ZSLOPE;
@@ -523,8 +561,14 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
         double EPP = (double)lines.epp[i];
         if (VNU == 0.) SUI = 2. * SUI;
         if (EPP <= -1.001) EPP = fabs(EPP);
-        if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
-        double TMPCOR = pow(P.tratio, (double)lines.tmpalf[i]);
+        if (EPP > -0.999) {
+          if (P.mixed)
+            SUI = (float)SUI * (float)P.scor[m] * __expf(-(float)EPP * (float)P.betacr4) *
+                  (1.f + __expf(-(float)VNU * (float)P.beta));
+          else
+            SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
+        }
+        double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
         double ALFA0I = alfa * TMPCOR;
         double HWHMSI = hwhm * TMPCOR;
         r.alfa = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];

@@ -20,19 +20,34 @@
 
 namespace clblm {
 
-// 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365)
+// 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365),
+// in FP64 and as FP32 copies for the mixed path
 __constant__ double c_IA1[203], c_IA2[203], c_IA3[203], c_IA4[203];
+__constant__ float c_IAf[4][203];
 
 // Stencil of output point I (1-based) of grid (V1, dvout, nout) on the input
-// grid (V1, dvin, nin): up to four input indices and weights.
+// grid (V1, dvin, nin): up to four input indices and weights of type W.
+template <typename W>
 struct Stencil {
   int64_t i[4];
-  double w[4];
+  W w[4];
   int n;
 };
 
-__device__ Stencil interp_stencil(const InterpSpec& s, int64_t I) {
-  Stencil st;
+template <typename W>
+__device__ __forceinline__ W ia_coef(int k, int IP) {
+  if constexpr (sizeof(W) == 8) return k == 0 ? c_IA1[IP] : k == 1 ? c_IA2[IP] : k == 2 ? c_IA3[IP] : c_IA4[IP];
+  else return c_IAf[k][IP];
+}
+template <typename W>
+__device__ __forceinline__ W b_coef(const InterpSpec& s, int k, int NL) {
+  if constexpr (sizeof(W) == 8) return k == 0 ? s.b1[NL] : k == 1 ? s.b2[NL] : k == 2 ? s.b3[NL] : s.b4[NL];
+  else return s.bf[k][NL];
+}
+
+template <typename W = double>
+__device__ Stencil<W> interp_stencil(const InterpSpec& s, int64_t I) {
+  Stencil<W> st;
   st.n = 0;
   if (s.kind == 0) {  // same grid
     st.i[0] = I;
@@ -61,10 +76,7 @@ __device__ Stencil interp_stencil(const InterpSpec& s, int64_t I) {
     st.i[1] = iIn;
     st.i[2] = iIn + 1;
     st.i[3] = iIn + 2;
-    st.w[0] = s.b1[NL];
-    st.w[1] = s.b2[NL];
-    st.w[2] = s.b3[NL];
-    st.w[3] = s.b4[NL];
+    for (int k = 0; k < 4; ++k) st.w[k] = b_coef<W>(s, k, NL);
     st.n = 4;
     return st;
   }
@@ -76,10 +88,7 @@ __device__ Stencil interp_stencil(const InterpSpec& s, int64_t I) {
   st.i[1] = iIn;
   st.i[2] = iIn + 1;
   st.i[3] = iIn + 2;
-  st.w[0] = c_IA1[IP];
-  st.w[1] = c_IA2[IP];
-  st.w[2] = c_IA3[IP];
-  st.w[3] = c_IA4[IP];
+  for (int k = 0; k < 4; ++k) st.w[k] = ia_coef<W>(k, IP);
   st.n = 4;
   return st;
 }
@@ -113,12 +122,12 @@ __global__ void k_interp_map(InterpSpec s, const int64_t* __restrict__ blk_j1, c
 }
 
 // value of spInExt(i) (1-based, extended by two points each side)
-template <typename F>
-__device__ __forceinline__ double ext_at(F f, int64_t n, int64_t i) {
+template <typename T, typename F>
+__device__ __forceinline__ T ext_at(F f, int64_t n, int64_t i) {
   if (i >= 1 && i <= n) return f(i);
-  if (i == 0 || i == -1) return 2.0 * f(1) - f(2);
-  if (i == n + 1 || i == n + 2) return 2.0 * f(n) - f(n - 1);
-  return 0.;
+  if (i == 0 || i == -1) return (T)2 * f(1) - f(2);
+  if (i == n + 1 || i == n + 2) return (T)2 * f(n) - f(n - 1);
+  return (T)0;
 }
 
 __device__ __forceinline__ double planck_d(double V, double XKT) {
@@ -149,76 +158,96 @@ __device__ __forceinline__ double hlf_d(double od) {
 }
 
 // layer terms at OD-grid point i: TxA, TxB, EmUp, EmDn
-template <bool Plain>
-__device__ __forceinline__ void layer_terms(const RtLayerArgs& a, int64_t i, double out[4]) {
-  double od;
-  if constexpr (Plain) od = reinterpret_cast<const double*>(a.od)[i - 1];
-  else od = (double)reinterpret_cast<const float*>(a.od)[i - 1];
-  double v = a.v1 + (double)(i - 1) * a.dv_od;
-  if constexpr (Plain) {
-    double odA = od * a.scal_up;
-    odA = odA * 1.0;
-    double odB = od * a.scal_dn;
-    odB = odB * 1.0;
-    double TA = exp(-odA), TB = exp(-odB);
-    double XKTA_up = a.ttop / kRADCN2, XKTA_dn = a.tbot / kRADCN2, XKT = a.tave / kRADCN2;
-    double XKTB_up = a.tbot / kRADCN2, XKTB_dn = a.ttop / kRADCN2;
-    double EU, ED;
-    {  // down: Ta = Tbot, Tb = Ttop over path B
-      double abso = 1 - TB;
-      double hlf = a.lin_in_tau ? hlf_d(odB) : 0.;
-      if (a.lin_in_tau == 0) ED = abso * planck_d(v, XKT);
-      else if (a.lin_in_tau == 1) {
-        double bba = planck_d(v, XKTA_dn), bb = planck_d(v, XKT);
-        ED = abso * (bba + 2 * (bb - bba) * hlf);
-      } else {
-        double bba = planck_d(v, XKTA_dn), bbb = planck_d(v, XKTB_dn);
-        ED = abso * (bba + (bbb - bba) * hlf);
-      }
-    }
-    if (a.lin_in_tau == 0) EU = ED;
-    else {  // up: Ta = Ttop, Tb = Tbot over path A
-      double abso = 1 - TA;
-      double hlf = hlf_d(odA);
-      if (a.lin_in_tau == 1) {
-        double bba = planck_d(v, XKTA_up), bb = planck_d(v, XKT);
-        EU = abso * (bba + 2 * (bb - bba) * hlf);
-      } else {
-        double bba = planck_d(v, XKTA_up), bbb = planck_d(v, XKTB_up);
-        EU = abso * (bba + (bbb - bba) * hlf);
-      }
-    }
-    out[0] = TA;
-    out[1] = TB;
-    out[2] = EU;
-    out[3] = ED;
-  } else {
-    float odf = (float)od;
-    float odA = odf * (float)a.scal_up, odB = odf * (float)a.scal_dn;
-    float TA = expf(-odA), TB = expf(-odB);
-    float aA = -expm1f(-odA), aB = -expm1f(-odB);
-    float fi = (float)(i - 1);
-    float vf = fmaf(fi, a.vf1, a.vf0);
-    float cv3 = (float)kRADCN1 * vf * vf * vf;
-    float Bt = planck_f(fmaf(fi, a.xt1, a.xt0), cv3);
-    float Bb = planck_f(fmaf(fi, a.xb1, a.xb0), cv3);
-    float Ba = planck_f(fmaf(fi, a.xa1, a.xa0), cv3);
-    float EU, ED;
-    if (a.lin_in_tau == 0) {
-      ED = aB * Ba;
-      EU = ED;
-    } else if (a.lin_in_tau == 1) {
-      ED = aB * (Bb + 2.f * (Ba - Bb) * hlf_f(odB));
-      EU = aA * (Bt + 2.f * (Ba - Bt) * hlf_f(odA));
+__device__ __forceinline__ void layer_terms_d(const RtLayerArgs& a, int64_t i, double out[4]) {
+  const double od = reinterpret_cast<const double*>(a.od)[i - 1];
+  const double v = a.v1 + (double)(i - 1) * a.dv_od;
+  double odA = od * a.scal_up;
+  odA = odA * 1.0;
+  double odB = od * a.scal_dn;
+  odB = odB * 1.0;
+  double TA = exp(-odA), TB = exp(-odB);
+  double XKTA_up = a.ttop / kRADCN2, XKTA_dn = a.tbot / kRADCN2, XKT = a.tave / kRADCN2;
+  double XKTB_up = a.tbot / kRADCN2, XKTB_dn = a.ttop / kRADCN2;
+  double EU, ED;
+  {  // down: Ta = Tbot, Tb = Ttop over path B
+    double abso = 1 - TB;
+    double hlf = a.lin_in_tau ? hlf_d(odB) : 0.;
+    if (a.lin_in_tau == 0) ED = abso * planck_d(v, XKT);
+    else if (a.lin_in_tau == 1) {
+      double bba = planck_d(v, XKTA_dn), bb = planck_d(v, XKT);
+      ED = abso * (bba + 2 * (bb - bba) * hlf);
     } else {
-      ED = aB * (Bb + (Bt - Bb) * hlf_f(odB));
-      EU = aA * (Bt + (Bb - Bt) * hlf_f(odA));
+      double bba = planck_d(v, XKTA_dn), bbb = planck_d(v, XKTB_dn);
+      ED = abso * (bba + (bbb - bba) * hlf);
     }
-    out[0] = TA;
-    out[1] = TB;
-    out[2] = EU;
-    out[3] = ED;
   }
+  if (a.lin_in_tau == 0) EU = ED;
+  else {  // up: Ta = Ttop, Tb = Tbot over path A
+    double abso = 1 - TA;
+    double hlf = hlf_d(odA);
+    if (a.lin_in_tau == 1) {
+      double bba = planck_d(v, XKTA_up), bb = planck_d(v, XKT);
+      EU = abso * (bba + 2 * (bb - bba) * hlf);
+    } else {
+      double bba = planck_d(v, XKTA_up), bbb = planck_d(v, XKTB_up);
+      EU = abso * (bba + (bbb - bba) * hlf);
+    }
+  }
+  out[0] = TA;
+  out[1] = TB;
+  out[2] = EU;
+  out[3] = ED;
+}
+
+__device__ __forceinline__ void layer_terms_f(const RtLayerArgs& a, int64_t i, float out[4]) {
+  const float odf = reinterpret_cast<const float*>(a.od)[i - 1];
+  const float odA = odf * (float)a.scal_up, odB = odf * (float)a.scal_dn;
+  const float TA = expf(-odA), TB = expf(-odB);
+  const float aA = -expm1f(-odA), aB = -expm1f(-odB);
+  const float fi = (float)(i - 1);
+  const float vf = fmaf(fi, a.vf1, a.vf0);
+  const float cv3 = (float)kRADCN1 * vf * vf * vf;
+  const float Bt = planck_f(fmaf(fi, a.xt1, a.xt0), cv3);
+  const float Bb = planck_f(fmaf(fi, a.xb1, a.xb0), cv3);
+  const float Ba = planck_f(fmaf(fi, a.xa1, a.xa0), cv3);
+  float EU, ED;
+  if (a.lin_in_tau == 0) {
+    ED = aB * Ba;
+    EU = ED;
+  } else if (a.lin_in_tau == 1) {
+    ED = aB * (Bb + 2.f * (Ba - Bb) * hlf_f(odB));
+    EU = aA * (Bt + 2.f * (Ba - Bt) * hlf_f(odA));
+  } else {
+    ED = aB * (Bb + (Bt - Bb) * hlf_f(odB));
+    EU = aA * (Bt + (Bb - Bt) * hlf_f(odA));
+  }
+  out[0] = TA;
+  out[1] = TB;
+  out[2] = EU;
+  out[3] = ED;
+}
+
+template <bool Plain>
+__device__ __forceinline__ void layer_terms(const RtLayerArgs& a, int64_t i,
+                                            typename std::conditional<Plain, double, float>::type out[4]) {
+  if constexpr (Plain) layer_terms_d(a, i, out);
+  else layer_terms_f(a, i, out);
+}
+
+// layer terms at OD-grid index j, with interpSpectrum's linear extension by
+// two points past either end
+template <bool Plain, typename Real>
+__device__ __forceinline__ void layer_terms_ext(const RtLayerArgs& a, int64_t j, Real t[4]) {
+  if (j >= 1 && j <= a.n_od) {
+    layer_terms<Plain>(a, j, t);
+    return;
+  }
+  Real lo[4], hi[4];
+  const int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
+  layer_terms<Plain>(a, jl, lo);
+  layer_terms<Plain>(a, jm, hi);
+  const bool ext = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2);
+  for (int c = 0; c < 4; ++c) t[c] = ext ? (Real)2 * lo[c] - hi[c] : (Real)0;
 }
 
 template <bool Plain>
@@ -229,82 +258,62 @@ __global__ void k_rt_layer(RtLayerArgs a) {
   // merged radiance and reflectance at I
   Real R = 0, F = 0;
   {
-    Stencil st = interp_stencil(a.mr, I);
-    for (int k = 0; k < st.n; ++k) {
-      double r, f;
+    const Stencil<Real> st = interp_stencil<Real>(a.mr, I);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (k >= st.n) break;
+      Real r, f;
       if (a.first) {
-        auto sr = [&](int64_t j) {
+        auto sr = [&](int64_t j) -> Real {
           if constexpr (Plain) {
             double v = a.v1 + (double)(j - 1) * a.mr.dvin;
             return planck_d(v, a.tskin / kRADCN2) * a.emis;
           } else {
             float fj = (float)(j - 1);
             float vf = fmaf(fj, (float)a.mr.dvin, (float)a.v1);
-            return (double)(planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * (float)a.emis);
+            return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * (float)a.emis;
           }
         };
-        auto sf = [&](int64_t j) { return 1.0 - a.emis; };
-        r = ext_at(sr, a.mr.nin, st.i[k]);
-        f = ext_at(sf, a.mr.nin, st.i[k]);
+        auto sf = [&](int64_t) -> Real { return (Real)(1.0 - a.emis); };
+        r = ext_at<Real>(sr, a.mr.nin, st.i[k]);
+        f = ext_at<Real>(sf, a.mr.nin, st.i[k]);
       } else {
         const Real* rin = reinterpret_cast<const Real*>(a.rad_in);
         const Real* fin = reinterpret_cast<const Real*>(a.refl_in);
-        auto gr = [&](int64_t j) { return (double)rin[j - 1]; };
-        auto gf = [&](int64_t j) { return (double)fin[j - 1]; };
-        r = ext_at(gr, a.mr.nin, st.i[k]);
-        f = ext_at(gf, a.mr.nin, st.i[k]);
+        auto gr = [&](int64_t j) -> Real { return rin[j - 1]; };
+        auto gf = [&](int64_t j) -> Real { return fin[j - 1]; };
+        r = ext_at<Real>(gr, a.mr.nin, st.i[k]);
+        f = ext_at<Real>(gf, a.mr.nin, st.i[k]);
       }
       if (st.n == 1) {
-        R = (Real)r;
-        F = (Real)f;
+        R = r;
+        F = f;
       } else {
-        R += (Real)st.w[k] * (Real)r;
-        F += (Real)st.w[k] * (Real)f;
+        R += st.w[k] * r;
+        F += st.w[k] * f;
       }
     }
   }
-  double L[4];
+  Real L[4];
   {
-    Stencil st = interp_stencil(a.ly, I);
+    const Stencil<Real> st = interp_stencil<Real>(a.ly, I);
     if (st.n == 1) {
-      int64_t j = st.i[0];
-      if (j >= 1 && j <= a.n_od) layer_terms<Plain>(a, j, L);
-      else {
-        double lo[4], hi[4];
-        int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
-        layer_terms<Plain>(a, jl, lo);
-        layer_terms<Plain>(a, jm, hi);
-        for (int c = 0; c < 4; ++c) L[c] = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2) ? 2.0 * lo[c] - hi[c] : 0.;
-      }
+      layer_terms_ext<Plain>(a, st.i[0], L);
     } else {
-      for (int c = 0; c < 4; ++c) L[c] = 0.;
+      for (int c = 0; c < 4; ++c) L[c] = 0;
+#pragma unroll
       for (int k = 0; k < 4; ++k) {
-        int64_t j = st.i[k];
-        double t[4];
-        if (j >= 1 && j <= a.n_od) layer_terms<Plain>(a, j, t);
-        else {
-          double lo[4], hi[4];
-          int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
-          layer_terms<Plain>(a, jl, lo);
-          layer_terms<Plain>(a, jm, hi);
-          for (int c = 0; c < 4; ++c)
-            t[c] = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2) ? 2.0 * lo[c] - hi[c] : 0.;
-        }
+        Real t[4];
+        layer_terms_ext<Plain>(a, st.i[k], t);
         for (int c = 0; c < 4; ++c) L[c] += st.w[k] * t[c];
       }
     }
   }
-  double TA = L[0], TB = L[1], EU = L[2], ED = L[3];
+  const Real TA = L[0], TB = L[1], EU = L[2], ED = L[3];
   Real* rout = reinterpret_cast<Real*>(a.rad_out);
   Real* fout = reinterpret_cast<Real*>(a.refl_out);
-  if constexpr (Plain) {
-    rout[I - 1] = EU + TA * (R + ED * F);
-    fout[I - 1] = TA * TB * F;
-  } else {
-    float r = (float)EU + (float)TA * ((float)R + (float)ED * (float)F);
-    rout[I - 1] = r;
-    fout[I - 1] = (float)TA * (float)TB * (float)F;
-  }
+  rout[I - 1] = EU + TA * (R + ED * F);
+  fout[I - 1] = TA * TB * F;
 }
 
 template __global__ void k_rt_layer<false>(RtLayerArgs);
@@ -319,11 +328,11 @@ __global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_o
   if (I > n_out) return;
   const Real* x = reinterpret_cast<const Real*>(od);
   auto g = [&](int64_t j) { return (double)x[j - 1]; };
-  Stencil st = interp_stencil(s, I);
+  const Stencil<double> st = interp_stencil<double>(s, I);
   double v = 0.;
-  if (st.n == 1) v = ext_at(g, n_in, st.i[0]);
+  if (st.n == 1) v = ext_at<double>(g, n_in, st.i[0]);
   else
-    for (int k = 0; k < 4; ++k) v += st.w[k] * ext_at(g, n_in, st.i[k]);
+    for (int k = 0; k < 4; ++k) v += st.w[k] * ext_at<double>(g, n_in, st.i[k]);
   out[I - 1] = v;
 }
 
@@ -345,6 +354,14 @@ void rt_upload_interp_coef(cudaStream_t st) {
   cudaMemcpyToSymbolAsync(c_IA2, a2, sizeof a2, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c_IA3, a3, sizeof a3, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c_IA4, a4, sizeof a4, 0, cudaMemcpyHostToDevice, st);
+  static float af[4][203];  // staged by the copy before it returns (pageable source)
+  for (int IP = 0; IP <= 202; ++IP) {
+    af[0][IP] = (float)a1[IP];
+    af[1][IP] = (float)a2[IP];
+    af[2][IP] = (float)a3[IP];
+    af[3][IP] = (float)a4[IP];
+  }
+  cudaMemcpyToSymbolAsync(c_IAf, af, sizeof af, 0, cudaMemcpyHostToDevice, st);
 }
 
 }  // namespace clblm

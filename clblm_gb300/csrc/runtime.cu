@@ -260,6 +260,13 @@ int upload_tables(clblm_handle* h) {
   CUDA_TRY(h, cudaMemcpyToSymbol(c_CF2, CLBLM_CF2, sizeof CLBLM_CF2));
   CUDA_TRY(h, cudaMemcpyToSymbol(c_CF3, CLBLM_CF3, sizeof CLBLM_CF3));
   CUDA_TRY(h, cudaMemcpyToSymbol(c_CER, CLBLM_CER, sizeof CLBLM_CER));
+  {
+    float sf[5][102];
+    const double* src[5] = {CLBLM_CF1, CLBLM_CF2, CLBLM_CF3, CLBLM_CGAUSS, CLBLM_CER};
+    for (int q = 0; q < 5; ++q)
+      for (int i = 0; i < 102; ++i) sf[q][i] = (float)src[q][i];
+    CUDA_TRY(h, cudaMemcpyToSymbol(c_SHAPEf, sf, sizeof sf));
+  }
   rt_upload_interp_coef(h->stream);
   return CLBLM_OK;
 }
@@ -439,6 +446,8 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.xkt0 = kT0 / kRADCN2;
   P.betacr = (1. / P.xkt) - (1. / P.xkt0);
   P.tratio = lay->tave / kT0;
+  P.ln_tratio = std::log(P.tratio);
+  P.mixed = c->precision == CLBLM_PREC_PLAIN ? 0 : 1;
   P.rhorat = (lay->pave / kP0) * (kT0 / lay->tave);
   P.pavp0 = lay->pave / kP0;
   P.pavp2 = P.pavp0 * P.pavp0;
@@ -609,6 +618,10 @@ InterpSpec interp_spec(double v1in, double dvin, int64_t nin, double v1out, doub
       s.b2[IP] = (P * P - 1.0) * (P - 2.0) * 0.5;
       s.b3[IP] = -P * (P + 1.0) * (P - 2.0) * 0.5;
       s.b4[IP] = P * (P * P - 1.0) / 6.0;
+      s.bf[0][IP] = (float)s.b1[IP];
+      s.bf[1][IP] = (float)s.b2[IP];
+      s.bf[2][IP] = (float)s.b3[IP];
+      s.bf[3][IP] = (float)s.b4[IP];
     }
   }
   return s;
