@@ -56,7 +56,8 @@ class clblm_grid_t(C.Structure):
 class clblm_od_ctrl_t(C.Structure):
     _fields_ = [("jrad", C.c_int32), ("line_rejec", C.c_int32), ("dptmin", C.c_double),
                 ("dptfac", C.c_double), ("xself", C.c_double), ("xfrgn", C.c_double),
-                ("contnm_off", C.c_int32), ("line_off", C.c_int32), ("precision", C.c_int32)]
+                ("contnm_off", C.c_int32), ("line_off", C.c_int32), ("precision", C.c_int32),
+                ("jac_mol", C.c_int32)]
 
 
 class clblm_column_t(C.Structure):
@@ -64,6 +65,33 @@ class clblm_column_t(C.Structure):
                 ("tave", _dp), ("tbot", _dp), ("ttop", _dp), ("w", _dp), ("wtot", _dp),
                 ("wtot_down", _dp), ("v1", C.c_double), ("v2", C.c_double),
                 ("tskin", C.c_double), ("emis", C.c_double)]
+
+
+class clblm_jac_t(C.Structure):
+    _fields_ = [("plev", _dp), ("qlev", _dp), ("jac_mol", C.c_int32), ("do_temp", C.c_int32)]
+
+
+class JacProfile:
+    """Level pressures and Jacobian-molecule mixing ratios (level 0 at the
+    surface) and the clblm_jac_t view of them."""
+
+    def __init__(self, plev, qlev, jac_mol=1, do_temp=1):
+        self.plev = np.ascontiguousarray(plev, dtype=np.float64)
+        self.qlev = np.ascontiguousarray(qlev, dtype=np.float64)
+        self.jac_mol, self.do_temp = int(jac_mol), int(do_temp)
+
+    def struct(self):
+        j = clblm_jac_t()
+        j.plev = _ptr(self.plev, C.c_double)
+        j.qlev = _ptr(self.qlev, C.c_double)
+        j.jac_mol, j.do_temp = self.jac_mol, self.do_temp
+        j._keep = self
+        return j
+
+    def sub(self, first, count):
+        """Levels of layers first .. first+count-1."""
+        return JacProfile(self.plev[first:first + count + 1], self.qlev[first:first + count + 1],
+                          self.jac_mol, self.do_temp)
 
 
 class clblm_rt_ctrl_t(C.Structure):
@@ -173,11 +201,11 @@ def grid_struct(v1, v2, dv_normal, dv_narrow, dv_out=-999.9, sample=4.0, alfal0=
 
 
 def od_ctrl(precision=CLBLM_PREC_MIXED, jrad=1, line_rejec=1, dptmin=0.0, dptfac=0.0,
-            xself=1.0, xfrgn=1.0, contnm_off=0, line_off=0):
+            xself=1.0, xfrgn=1.0, contnm_off=0, line_off=0, jac_mol=0):
     c = clblm_od_ctrl_t()
     c.jrad, c.line_rejec, c.dptmin, c.dptfac = jrad, line_rejec, dptmin, dptfac
     c.xself, c.xfrgn, c.contnm_off, c.line_off = xself, xfrgn, contnm_off, line_off
-    c.precision = precision
+    c.precision, c.jac_mol = precision, jac_mol
     return c
 
 

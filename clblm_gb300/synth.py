@@ -99,8 +99,18 @@ def atmosphere(nlay, p_top, v1, v2, mols=SEVEN, p_sfc=1013.0, scale_height=7.0,
         else:
             vmr = np.full(nlay, other_vmr)
         w[:, j] = vmr * wair
-    return Column(mols, pave, tave, t_lev[:-1], t_lev[1:], w, wair, SECANT_DIFFUSE * wair,
-                  v1, v2, t_lev[0], emis)
+    col = Column(mols, pave, tave, t_lev[:-1], t_lev[1:], w, wair, SECANT_DIFFUSE * wair,
+                 v1, v2, t_lev[0], emis)
+    col.p_lev = p_lev
+    col.q_h2o_lev = np.maximum(1.0e-2 * np.exp(-z_lev / 2.0), 4.0e-6)
+    return col
+
+
+def jac_profile(col, jac_mol=1, do_temp=1):
+    """Level pressures and H2O mixing ratios of a column made by atmosphere(),
+    as the Jacobian inputs (level 0 at the surface)."""
+    from .capi_types import JacProfile
+    return JacProfile(col.p_lev, col.q_h2o_lev, jac_mol=jac_mol, do_temp=do_temp)
 
 
 # ---- the benchmark workloads --------------------------------------------

@@ -124,6 +124,9 @@ typedef struct {
   int32_t contnm_off;  /* contnmOff                                             */
   int32_t line_off;    /* lineOff                                               */
   int32_t precision;   /* CLBLM_PREC_MIXED or CLBLM_PREC_PLAIN                  */
+  int32_t jac_mol;     /* HITRAN number whose continuum derivative term CONTNM
+                        * adds (icflg, clblm_ODLAY.f90:436-438,
+                        * clblm_ODLAY_Continuum.f90:394-401); 0: none          */
 } clblm_od_ctrl_t;
 
 /* A layered column seen in nadir from the top of the atmosphere, with the
@@ -147,6 +150,18 @@ typedef struct {
   double         tskin;     /* surface skin temperature, K                     */
   double         emis;      /* surface emissivity (constant over v1..v2)       */
 } clblm_column_t;
+
+/* Level profile for the Jacobians of noScattJacob (clblm_noScattJac.f90:20-339),
+ * nadir view from the top of the atmosphere.  Level 0 is the surface;
+ * layer l lies between levels l and l+1.  Level temperatures are the
+ * column's tbot[0..nlay-1] and ttop[nlay-1]. */
+typedef struct {
+  const double *plev;   /* [nlay+1] level pressure, mbar                       */
+  const double *qlev;   /* [nlay+1] volume mixing ratio of jac_mol at levels   */
+  int32_t jac_mol;      /* HITRAN number of the Jacobian molecule (1: H2O);
+                         * 0: no molecule Jacobian                              */
+  int32_t do_temp;      /* 1: level-temperature Jacobians                      */
+} clblm_jac_t;
 
 /* Radiative-transfer options (CLBLM_RT_Ctrl + CLBLM_DV_Ctrl). */
 typedef struct {
@@ -243,6 +258,32 @@ int clblm_gpu_rt_mode2_size(clblm_handle_t *h, const clblm_column_t *col,
 int clblm_gpu_rt_mode2(clblm_handle_t *h, const clblm_column_t *col,
                        const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap,
                        int32_t flags);
+
+/* Size of the Jacobian spectra: the uniform grid (gridType 1, DVout = the
+ * smallest DVnarrow or dv_user) over the 100000-point blocks of noScattJacob
+ * (clblm_noScattJac.f90:206-232). */
+int clblm_gpu_jac_size(clblm_handle_t *h, const clblm_column_t *col,
+                       const clblm_rt_ctrl_t *ctrl, const clblm_jac_t *jac,
+                       int64_t *npts, double *dv);
+
+/* Nadir upwelling radiance and its analytic Jacobians: replaces noScattJacob
+ * (clblm_noScattJac.f90:20-339) for the thermal, down-looking, airmass-scaled
+ * case with the viewing path as reference: the layer ODs of pathOD_up_dn_sun
+ * (:723-894), the per-point recurrence of Jacobians (:346-716), the layer to
+ * level maps of level2layer (:1208-1279) and the OD derivatives of
+ * drv_LevelTemp (:899-1065) and drv_LevelConc (:1069-1203).  Outputs
+ * (binary64, any may be NULL) on the grid of clblm_gpu_jac_size:
+ *   rad        [npts]            radiance, W/(cm2 sr cm-1)
+ *   dr_dtlev   [(nlay+1)*npts]   dR/dT of each level (level-major), per K
+ *   dr_dqlev   [(nlay+1)*npts]   dR/d ln q of each level for jac->jac_mol
+ *   dr_dtskin  [npts]            dR/dTskin
+ *   dr_demis   [npts]            dR/d emissivity
+ * `cap` is the capacity of each spectrum (>= npts). */
+int clblm_gpu_jac(clblm_handle_t *h, const clblm_column_t *col,
+                  const clblm_rt_ctrl_t *ctrl, const clblm_jac_t *jac,
+                  double *rad, double *dr_dtlev, double *dr_dqlev,
+                  double *dr_dtskin, double *dr_demis, int64_t cap,
+                  int32_t flags);
 
 /* ---- grid interpolation that allocates nothing ----------------------------
  *

@@ -464,7 +464,7 @@ static void myxint(double V1A, double V2A, double DVA, const double *A, double A
 
 static int contnm_h2o(ocl_session *s, const clblm_cont_t *C, int JRAD, double V1ABS, double V2ABS, double DVABS,
                       double *ABSRB /*1-based*/, double XSELF, double XFRGN, double V1, double V2, double PAVE,
-                      double TAVE, double Wtot, double WK1) {
+                      double TAVE, double Wtot, double WK1, int icflg) {
   if (!C || C->n < 4) return fail(s, CLBLM_ERR_ARG, "continuum table missing");
   double h2o_fac = WK1 / Wtot;
   if (!((V2 > -20.0) && (V1 < 20000.) && ((XSELF > 0.) || (XFRGN > 0.)))) return 0;
@@ -520,6 +520,11 @@ static int contnm_h2o(ocl_session *s, const clblm_cont_t *C, int JRAD, double V1
     double cself = WK1 * self[k] * XSELF;
     double cfor = WK1 * forc[k] * XFRGN;
     ABSRB[k] = ABSRB[k] + cself + cfor;
+    if (icflg == 1) { /* OD for the H2O Jacobian, clblm_ODLAY_Continuum.f90:394-401 */
+      double cfrgn_aj = (h2o_fac >= 1.0) ? 0. : WK1 * forc[k] * h2o_fac / (1.0 - h2o_fac);
+      double c = cself - cfrgn_aj;
+      ABSRB[k] = ABSRB[k] + c;
+    }
   }
   free(self);
   free(forc);
@@ -1508,7 +1513,7 @@ int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double V1, double V2, double
   int NPTABS = (int)((V2ABS - V1ABS) / DVABS + 1.5);
   if (NPTABS > N_ABSRB - 4) return CLBLM_ERR_RANGE;
   double *A = (double *)calloc(N_ABSRB + 8, sizeof(double));
-  int rc = contnm_h2o(&tmp, C, jrad, V1ABS, V2ABS, DVABS, A, xself, xfrgn, V1, V2, PAVE, TAVE, Wtot, WK1);
+  int rc = contnm_h2o(&tmp, C, jrad, V1ABS, V2ABS, DVABS, A, xself, xfrgn, V1, V2, PAVE, TAVE, Wtot, WK1, 0);
   if (!rc) memcpy(absrb, A + 1, sizeof(double) * N_ABSRB);
   free(A);
   *v1abs = V1ABS;
@@ -1595,7 +1600,7 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
     ABSRBb = (double *)calloc(N_ABSRB + 8, sizeof(double));
     double WK1 = M.WK[1];
     rc = contnm_h2o(s, C, JRAD, V1ABS, V2ABS, DVABS, ABSRBb, ctrl->xself, ctrl->xfrgn, V1, V2, PAVE, TAVE,
-                    lay->wtot, WK1);
+                    lay->wtot, WK1, ctrl->jac_mol);
     if (rc) {
       free(ABSRBb);
       return rc;
@@ -2009,4 +2014,435 @@ int ocl_rt_mode2_par(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t 
                      const clblm_rt_ctrl_t *ctrl, double *rad, int64_t cap, int64_t *npts, double *dvp,
                      int nthreads) {
   return rt_mode2_impl(s, L, C, col, ctrl, rad, cap, npts, dvp, nthreads);
+}
+
+/* ======================================================================
+ * Jacobians of the nadir thermal radiance: noScattJacob
+ * clblm_noScattJac.f90:20-339 for a down-looking observer above the top
+ * layer, no solar term, airmass scaling with the viewing path as reference
+ * (pathOD_up_dn_sun :723-894 with refPath = 1), no prebox smoothing.
+ * ====================================================================== */
+
+/* planckFnDrv clblm_EMLAY.f90:45-70 */
+static void planck_drv(double V, double T, double *B, double *dB) {
+  double XKT = T / RADCN2;
+  if (XKT <= 1.e-6) {
+    *B = 0.;
+    *dB = 0.;
+    return;
+  }
+  double cv3 = RADCN1 * V * V * V;
+  double evt = exp(V / XKT);
+  *B = cv3 / (evt - 1.);
+  *dB = *B * *B * (evt * V) / (RADCN2 * cv3 * XKT * XKT);
+}
+
+/* rlin with its derivative, clblm_EMLAY.f90:187-223 */
+static void rlin_d(double od, double *hlf, double *dhlf) {
+  const double dbAvg2dtau = -1. / 12;
+  double tex = 0.;
+  if (od < 1.e-03) *hlf = .5 + od * dbAvg2dtau;
+  else if (od > 20.) *hlf = 1. / od;
+  else {
+    tex = exp(od);
+    *hlf = 1. / (od)-1. / (tex - 1.);
+  }
+  if (od < 1.e-03) *dhlf = dbAvg2dtau;
+  else if (od > 20.) *dhlf = -1. / (od * od);
+  else *dhlf = -1. / (od * od) + tex / ((tex - 1) * (tex - 1));
+}
+
+/* level2layer clblm_noScattJac.f90:1208-1279 for one molecule; level l+1 is
+ * the top of layer l (arrays 0-based here). */
+static void level2layer(const double *Plev, const double *Tlev, const double *Tave, const double *QLev, int nLay,
+                        double *dT_dTup, double *dT_dTlo, double *dW_dQup, double *dW_dQlo) {
+  for (int l = 0; l < nLay; ++l) {
+    double Pup = Plev[l + 1], Plo = Plev[l];
+    double Tup = Tlev[l + 1], Tlo = Tlev[l];
+    double Tbar = Tave[l];
+    double rhoU = Pup / (Tup * 1.3806503E-19);
+    double rhoL = Plo / (Tlo * 1.3806503E-19);
+    double alpha = rhoU / rhoL;
+    double alphaT = -(Tup - Tlo) / log(alpha);
+    dT_dTlo[l] = ((Tbar - alphaT) / Tlo) * (rhoL / (rhoL - rhoU)) + (1.0 - alphaT / Tlo) / log(alpha);
+    dT_dTup[l] = ((Tbar - alphaT) / Tup) * (-rhoU / (rhoL - rhoU)) - (1.0 - alphaT / Tup) / log(alpha);
+    if (QLev) {
+      double denUp = QLev[l + 1], denLo = QLev[l];
+      if (denLo != 0.0) {
+        double ratU = denUp / rhoU, ratL = denLo / rhoL;
+        dW_dQlo[l] = (ratL / (ratL - alpha * ratU)) + 1.0 / log(alpha * ratU / ratL);
+        dW_dQup[l] = ((-alpha * ratU) / (ratL - alpha * ratU)) - 1.0 / log(alpha * ratU / ratL);
+      } else {
+        dW_dQlo[l] = 0.0;
+        dW_dQup[l] = 0.0;
+      }
+    }
+  }
+}
+
+/* Jacobians clblm_noScattJac.f90:346-716, down-looking branch with
+ * N1 = 1, N2 = nLay, obsLev = nLay + 1.  1-based through the macros; `w` is
+ * scratch of 8*(nLay+2) doubles. */
+static void jacobians_down(const double *viewOD_, const double *downOD_, const double *amfView_,
+                           const double *amfDown_, const double *Tlay_, const double *Tlev_, double Tsfc, double emis,
+                           double vn, int nLay, int linInTau, int doJacTemp, const double *dT_dTup_,
+                           const double *dT_dTlo_, double *dRad_dTlev_, double *dRad_dTau_, double *radp,
+                           double *dRad_dTsfcp, double *dRad_dEmisp, double *w) {
+#define viewOD(l) viewOD_[(l)-1]
+#define downOD(l) downOD_[(l)-1]
+#define amfView(l) amfView_[(l)-1]
+#define amfDown(l) amfDown_[(l)-1]
+#define dT_dTup(l) dT_dTup_[(l)-1]
+#define dT_dTlo(l) dT_dTlo_[(l)-1]
+#define dRad_dTlev(l) dRad_dTlev_[(l)-1]
+#define dRad_dTau(l) dRad_dTau_[(l)-1]
+  const int N1 = 1, N2 = nLay, obsLev = nLay + 1, M = nLay + 2;
+  double *Bbar = w, *dBbar = w + M, *Blev = w + 2 * M, *dBlev = w + 3 * M;
+  double *cumTxA = w + 4 * M, *cumTxB2 = w + 5 * M, *dRad_dT_up = w + 6 * M, *dRad_dT_dn = w + 7 * M;
+  double *dRad_dTbar = w + 8 * M;
+  double Bsfc, dBsfc;
+  if (linInTau != 0)
+    for (int lv = 1; lv <= N2 + 1; ++lv) planck_drv(vn, Tlev_[lv - 1], &Blev[lv], &dBlev[lv]);
+  for (int l = 1; l <= N2; ++l) planck_drv(vn, Tlay_[l - 1], &Bbar[l], &dBbar[l]);
+  planck_drv(vn, Tsfc, &Bsfc, &dBsfc);
+  double rad = 0.;
+  for (int l = N1; l <= N2; ++l) {
+    dRad_dTau(l) = 0.;
+    dRad_dTbar[l] = 0.;
+  }
+  for (int l = N1; l <= N2 + 1; ++l) {
+    dRad_dT_up[l] = 0.;
+    dRad_dT_dn[l] = 0.;
+    dRad_dTlev(l) = 0.;
+  }
+  double dRad_dEmis = 0., dRad_dTsfc = 0.;
+  int obsLay = obsLev;
+  /* 0- transmittance along the upwelling path from TOA down */
+  double cumODA = 0.;
+  for (int l = obsLev; l <= N2 + 1; ++l) cumTxA[l] = 1.;
+  for (int l = obsLay - 1; l >= N1; --l) {
+    cumODA = cumODA + viewOD(l);
+    cumTxA[l] = exp(-cumODA);
+  }
+  double totODUp = cumODA, totTxUp = cumTxA[N1];
+  double dbavgdb, dbavgdbdod, Blt, dTran;
+  /* 1- downwelling thermal radiance */
+  if (totTxUp > 1.e-06) {
+    cumTxB2[N1] = totTxUp;
+    double cumODB = 0.;
+    for (int l = N1; l <= N2; ++l) {
+      cumODB = cumODB + downOD(l);
+      cumTxB2[l + 1] = exp(-(totODUp + cumODB));
+    }
+    if (linInTau != 0) {
+      for (int l = N2; l >= N1; --l) {
+        dTran = cumTxB2[l] - cumTxB2[l + 1];
+        rlin_d(downOD(l), &dbavgdb, &dbavgdbdod);
+        if (linInTau == 2) {
+          Blt = Blev[l] + (Blev[l + 1] - Blev[l]) * dbavgdb;
+          dRad_dTau(l) = (cumTxB2[l + 1] * Blt - rad + dTran * dbavgdbdod * (Blev[l + 1] - Blev[l])) * amfDown(l);
+          if (doJacTemp) {
+            dRad_dT_dn[l + 1] = dRad_dT_dn[l + 1] + dTran * dBlev[l + 1] * dbavgdb;
+            dRad_dT_dn[l] = dTran * dBlev[l] * (1. - dbavgdb);
+            dRad_dTbar[l] = 0.0;
+          }
+        } else {
+          Blt = 2.0 * Bbar[l] * dbavgdb + Blev[l] * (1.0 - 2.0 * dbavgdb);
+          dRad_dTau(l) = (cumTxB2[l + 1] * Blt - rad + 2.0 * dTran * dbavgdbdod * (Bbar[l] - Blev[l])) * amfDown(l);
+          if (doJacTemp) {
+            dRad_dT_dn[l] = dTran * dBlev[l] * (1.0 - 2.0 * dbavgdb);
+            dRad_dTbar[l] = dTran * 2.0 * dBbar[l] * dbavgdb;
+          }
+        }
+        rad = rad + dTran * Blt;
+      }
+    } else {
+      for (int l = N2; l >= N1; --l) {
+        dTran = cumTxB2[l] - cumTxB2[l + 1];
+        dRad_dTau(l) = (cumTxB2[l + 1] * Bbar[l] - rad) * amfDown(l);
+        rad = rad + dTran * Bbar[l];
+        if (doJacTemp) dRad_dTbar[l] = dTran * dBbar[l];
+      }
+    }
+  }
+  /* 2- scaled by the surface reflectance */
+  double rsfc = (1. - emis);
+  for (int l = N1; l <= N2; ++l) {
+    dRad_dTau(l) = dRad_dTau(l) * rsfc;
+    if (doJacTemp) dRad_dTbar[l] = dRad_dTbar[l] * rsfc;
+  }
+  /* 3- surface terms */
+  dRad_dEmis = totTxUp * Bsfc - rad;
+  dRad_dTsfc = emis * totTxUp * dBsfc;
+  double sfcEmit = emis * totTxUp * Bsfc;
+  rad = rad * rsfc + sfcEmit;
+  /* 5- upwelling thermal radiance */
+  if (linInTau != 0) {
+    for (int l = N1; l <= obsLay - 1; ++l) {
+      dTran = cumTxA[l + 1] - cumTxA[l];
+      rlin_d(viewOD(l), &dbavgdb, &dbavgdbdod);
+      if (linInTau == 2) {
+        Blt = Blev[l + 1] * (1 - dbavgdb) + Blev[l] * dbavgdb;
+        dRad_dTau(l) = dRad_dTau(l) + (cumTxA[l] * Blt - rad + dTran * dbavgdbdod * (Blev[l] - Blev[l + 1])) * amfView(l);
+        if (doJacTemp) {
+          dRad_dT_up[l + 1] = dTran * dBlev[l + 1] * (1 - dbavgdb);
+          dRad_dT_up[l] = dRad_dT_up[l] + dTran * dBlev[l] * dbavgdb;
+        }
+      } else {
+        Blt = 2.0 * Bbar[l] * dbavgdb + Blev[l + 1] * (1.0 - 2.0 * dbavgdb);
+        dRad_dTau(l) =
+            dRad_dTau(l) + (cumTxA[l] * Blt - rad + dTran * dbavgdbdod * 2.0 * (Bbar[l] - Blev[l + 1])) * amfView(l);
+        if (doJacTemp) {
+          dRad_dT_up[l + 1] = dTran * dBlev[l + 1] * (1.0 - 2.0 * dbavgdb);
+          dRad_dTbar[l] = dRad_dTbar[l] + dTran * 2.0 * dBbar[l] * dbavgdb;
+        }
+      }
+      rad = rad + dTran * Blt;
+    }
+  } else {
+    for (int l = N1; l <= obsLay - 1; ++l) {
+      dTran = cumTxA[l + 1] - cumTxA[l];
+      dRad_dTau(l) = dRad_dTau(l) + (cumTxA[l] * Bbar[l] - rad) * amfView(l);
+      rad = rad + dTran * Bbar[l];
+      if (doJacTemp) dRad_dTbar[l] = dRad_dTbar[l] + dTran * dBbar[l];
+    }
+  }
+  /* emission terms of the level temperatures */
+  if (doJacTemp) {
+    if (linInTau != 0)
+      for (int lv = N1; lv <= N2 + 1; ++lv) dRad_dTlev(lv) = dRad_dT_up[lv] + dRad_dT_dn[lv] * rsfc;
+    if (linInTau == 0 || linInTau == 1) {
+      for (int l = N2; l >= N1; --l) {
+        dRad_dTlev(l + 1) = dRad_dTlev(l + 1) + dRad_dTbar[l] * dT_dTup(l);
+        dRad_dTlev(l) = dRad_dTlev(l) + dRad_dTbar[l] * dT_dTlo(l);
+      }
+    }
+  }
+  *radp = rad;
+  *dRad_dTsfcp = dRad_dTsfc;
+  *dRad_dEmisp = dRad_dEmis;
+#undef viewOD
+#undef downOD
+#undef amfView
+#undef amfDown
+#undef dT_dTup
+#undef dT_dTlo
+#undef dRad_dTlev
+#undef dRad_dTau
+}
+
+int ocl_jac_point(const double *viewOD, const double *downOD, const double *amfView, const double *amfDown,
+                  const double *Tlay, const double *Tlev, double Tsfc, double emis, double vn, int nLay, int linInTau,
+                  const double *dT_dTup, const double *dT_dTlo, double *dRad_dTlev, double *dRad_dTau, double *rad,
+                  double *dRad_dTsfc, double *dRad_dEmis) {
+  double *w = (double *)calloc((size_t)9 * (nLay + 2), sizeof(double));
+  if (!w) return CLBLM_ERR_OOM;
+  jacobians_down(viewOD, downOD, amfView, amfDown, Tlay, Tlev, Tsfc, emis, vn, nLay, linInTau, 1, dT_dTup, dT_dTlo,
+                 dRad_dTlev, dRad_dTau, rad, dRad_dTsfc, dRad_dEmis, w);
+  free(w);
+  return 0;
+}
+
+/* One ODLAY call of the Jacobian path: which layer, which perturbation. */
+enum { JV_BASE = 0, JV_TEMP = 1, JV_WTOT = 2, JV_MOL = 3 };
+
+int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_column_t *col,
+                  const clblm_rt_ctrl_t *ctrl, const clblm_jac_t *jac, double *rad, double *dtlev, double *dqlev,
+                  double *dtsfc, double *demis, int64_t cap, int64_t *npts, double *dvp, int nthreads) {
+  const int nLay = col->nlay, nmol = col->nmol;
+  if (nLay < 1 || !jac || !jac->plev) return fail(s, CLBLM_ERR_ARG, "bad Jacobian input");
+  if (ctrl->grid_type != 1) return fail(s, CLBLM_ERR_GRID, "noScattJacob: spectral grid is not uniform (gridType 1)");
+  int imol = -1;
+  if (jac->jac_mol > 0) {
+    for (int k = 0; k < nmol; ++k)
+      if (col->mol_id[k] == jac->jac_mol) imol = k;
+    if (imol < 0 || !jac->qlev) return fail(s, CLBLM_ERR_ARG, "invalid molecule for Jacobian calculation");
+  }
+  double *dvn = (double *)malloc(sizeof(double) * nLay), *dvf = (double *)malloc(sizeof(double) * nLay), DVB;
+  int rc = ocl_setdv(s, col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, 1, ctrl->dv_user, dvn, dvf, &DVB);
+  if (rc == 0 && !(DVB > 0.)) rc = fail(s, CLBLM_ERR_GRID, "noScattJacob: DVout not set");
+  /* level temperatures and the layer-to-level maps */
+  double *Tlev = (double *)malloc(sizeof(double) * (nLay + 1));
+  double *dT_dTup = (double *)calloc(nLay, sizeof(double)), *dT_dTlo = (double *)calloc(nLay, sizeof(double));
+  double *dW_dQup = (double *)calloc(nLay, sizeof(double)), *dW_dQlo = (double *)calloc(nLay, sizeof(double));
+  double *amfView = (double *)malloc(sizeof(double) * nLay), *amfDown = (double *)malloc(sizeof(double) * nLay);
+  for (int l = 0; l < nLay; ++l) {
+    Tlev[l] = col->tbot[l];
+    amfView[l] = col->wtot[l] / col->wtot[l];
+    amfDown[l] = col->wtot_down[l] / col->wtot[l];
+  }
+  Tlev[nLay] = col->ttop[nLay - 1];
+  level2layer(jac->plev, Tlev, col->tave, imol >= 0 ? jac->qlev : NULL, nLay, dT_dTup, dT_dTlo, dW_dQup, dW_dQlo);
+  /* per-job layers: the viewing-path layer, T+1, Wtot*1.01 and the molecule alone */
+  int nvar = 1 + (jac->do_temp ? 2 : 0) + (imol >= 0 ? 1 : 0);
+  clblm_layer_t *lays = (clblm_layer_t *)calloc((size_t)nvar * nLay, sizeof(clblm_layer_t));
+  double *wmol = (double *)calloc((size_t)nLay * nmol, sizeof(double));
+  int *vkind = (int *)calloc(nvar, sizeof(int));
+  {
+    int v = 0;
+    vkind[v++] = JV_BASE;
+    if (jac->do_temp) {
+      vkind[v++] = JV_TEMP;
+      vkind[v++] = JV_WTOT;
+    }
+    if (imol >= 0) vkind[v++] = JV_MOL;
+  }
+  for (int v = 0; v < nvar; ++v)
+    for (int il = 0; il < nLay; ++il) {
+      clblm_layer_t *lay = &lays[v * nLay + il];
+      lay->nmol = nmol;
+      lay->mol_id = col->mol_id;
+      lay->w = col->w + (size_t)il * nmol;
+      lay->wtot = col->wtot[il];
+      lay->pave = col->pave[il];
+      lay->tave = col->tave[il];
+      lay->lay_no = il + 1;
+      if (vkind[v] == JV_TEMP) lay->tave = col->tave[il] + 1.0;
+      if (vkind[v] == JV_WTOT) lay->wtot = col->wtot[il] + 0.01 * col->wtot[il];
+      if (vkind[v] == JV_MOL) {
+        double *wm = wmol + (size_t)il * nmol;
+        wm[imol] = col->w[(size_t)il * nmol + imol];
+        lay->w = wm;
+      }
+    }
+  clblm_od_ctrl_t octl = ctrl->od, octl_mol = ctrl->od;
+  octl_mol.jac_mol = jac->jac_mol;
+  int64_t total = 0;
+  double V1B = col->v1, V2B = V1B - DVB;
+  const int blockSize = 100000;
+  double *w9 = (double *)calloc((size_t)9 * (nLay + 2), sizeof(double));
+  double *dtl = (double *)malloc(sizeof(double) * (nLay + 1)), *dta = (double *)malloc(sizeof(double) * nLay);
+  double *vod = (double *)malloc(sizeof(double) * nLay), *dod = (double *)malloc(sizeof(double) * nLay);
+  while (rc == 0 && V2B < col->v2) {
+    V1B = V2B + DVB;
+    V2B = V1B + (double)(blockSize - 2) * DVB;
+    if (V2B > col->v2) V2B = col->v2;
+    /* the ODLAY calls in the reference's order: pathOD (il = 1..nLay), then
+     * per layer T+1 and Wtot, then per layer the molecule */
+    int njob = nvar * nLay;
+    int *jv = (int *)malloc(sizeof(int) * njob), *jl = (int *)malloc(sizeof(int) * njob);
+    int *jr = (int *)malloc(sizeof(int) * njob);
+    clblm_grid_t *gs = (clblm_grid_t *)calloc(njob, sizeof(clblm_grid_t));
+    int k = 0;
+    for (int il = 0; il < nLay; ++il) jv[k] = 0, jl[k++] = il;
+    if (jac->do_temp)
+      for (int il = 0; il < nLay; ++il) {
+        jv[k] = 1, jl[k++] = il;
+        jv[k] = 2, jl[k++] = il;
+      }
+    if (imol >= 0)
+      for (int il = 0; il < nLay; ++il) jv[k] = nvar - 1, jl[k++] = il;
+    for (int j = 0; j < njob; ++j) {
+      clblm_grid_t *g = &gs[j];
+      g->v1 = V1B;
+      g->v2 = V2B;
+      g->dv_normal = dvn[jl[j]];
+      g->dv_narrow = dvf[jl[j]];
+      g->dv_out = DVB;
+      g->sample = ctrl->sample;
+      g->alfal0 = ctrl->alfal0;
+      jr[j] = sticky_jrad(s, &lays[jv[j] * nLay + jl[j]], g, vkind[jv[j]] == JV_MOL ? &octl_mol : &octl);
+    }
+    ensure_tables(s);
+    interp_coef(s);
+    int64_t capb = (int64_t)ceil((V2B - V1B) / DVB) + 8;
+    double *ods = (double *)malloc(sizeof(double) * (size_t)njob * capb);
+    int64_t *nss = (int64_t *)calloc(njob, sizeof(int64_t));
+    int *rcs = (int *)calloc(njob, sizeof(int));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int j = 0; j < njob; ++j) {
+      ocl_session loc = *s;
+      double dvl;
+      rcs[j] = odlay_core(&loc, L, C, &lays[jv[j] * nLay + jl[j]], &gs[j],
+                          vkind[jv[j]] == JV_MOL ? &octl_mol : &octl, jr[j], ods + (size_t)j * capb, capb, &nss[j],
+                          &dvl, NULL);
+      if (rcs[j]) memcpy(s->err, loc.err, sizeof s->err);
+    }
+    for (int j = 0; j < njob && !rc; ++j) rc = rcs[j];
+    int64_t NLIM = nss[0];
+    for (int j = 0; j < njob && !rc; ++j)
+      if (nss[j] != NLIM) rc = fail(s, CLBLM_ERR_GRID, "Jacobian ODs of one block differ in length");
+    if (!rc && total + NLIM > cap) rc = fail(s, CLBLM_ERR_CAPACITY, "Jacobian spectra need more points");
+    if (!rc) {
+      V2B = V1B + (double)(NLIM - 1) * DVB;
+      /* OD of job (variant v, layer il) */
+#define OD(v, il, iv) ods[((size_t)((v)*nLay + (il)) * capb) + (iv)]
+      int vT = jac->do_temp ? 1 : -1, vW = jac->do_temp ? 2 : -1, vM = imol >= 0 ? nvar - 1 : -1;
+      for (int64_t iv = 0; iv < NLIM; ++iv) {
+        double vn = V1B + (double)iv * DVB;
+        for (int l = 0; l < nLay; ++l) {
+          vod[l] = OD(0, l, iv);
+          dod[l] = vod[l] * amfDown[l];
+        }
+        double r, dts, dem;
+        jacobians_down(vod, dod, amfView, amfDown, col->tave, Tlev, col->tskin, col->emis, vn, nLay,
+                       ctrl->lin_in_tau, jac->do_temp, dT_dTup, dT_dTlo, dtl, dta, &r, &dts, &dem, w9);
+        int64_t o = total + iv;
+        if (rad) rad[o] = r;
+        if (dtsfc) dtsfc[o] = dts;
+        if (demis) demis[o] = dem;
+        /* drv_LevelTemp :899-1065: level derivatives from the layer ones */
+        if (jac->do_temp && dtlev) {
+          double lo = 0.;
+          for (int il = 0; il < nLay; ++il) {
+            double m = OD(0, il, iv);
+            double dTau_dT = OD(vT, il, iv) - m;
+            double deltaW = 0.01 * col->wtot[il];
+            double dTau_dW = (OD(vW, il, iv) - m) / deltaW;
+            double fac = col->wtot[il] / col->tave[il];
+            dTau_dT = dTau_dT - dTau_dW * fac;
+            double dRaddT = dta[il] * dTau_dT;
+            double up = dRaddT * dT_dTup[il];
+            lo = lo + dRaddT * dT_dTlo[il] + dtl[il];
+            dtlev[(size_t)il * cap + o] = lo;
+            if (il == nLay - 1) dtlev[(size_t)nLay * cap + o] = up + dtl[il + 1];
+            lo = up;
+          }
+        }
+        /* drv_LevelConc :1069-1203 */
+        if (vM >= 0 && dqlev) {
+          double lo = 0.;
+          for (int il = 0; il < nLay; ++il) {
+            double dRad_dW = dta[il] * OD(vM, il, iv);
+            double up = dRad_dW * dW_dQup[il];
+            lo = lo + dRad_dW * dW_dQlo[il];
+            dqlev[(size_t)il * cap + o] = lo;
+            if (il == nLay - 1) dqlev[(size_t)nLay * cap + o] = up;
+            lo = up;
+          }
+        }
+      }
+#undef OD
+      total += NLIM;
+    }
+    free(ods);
+    free(nss);
+    free(rcs);
+    free(jv);
+    free(jl);
+    free(jr);
+    free(gs);
+  }
+  if (!rc) {
+    if (npts) *npts = total;
+    if (dvp) *dvp = DVB;
+  }
+  free(w9);
+  free(dtl);
+  free(dta);
+  free(vod);
+  free(dod);
+  free(lays);
+  free(wmol);
+  free(vkind);
+  free(Tlev);
+  free(dT_dTup);
+  free(dT_dTlo);
+  free(dW_dQup);
+  free(dW_dQlo);
+  free(amfView);
+  free(amfDown);
+  free(dvn);
+  free(dvf);
+  return rc;
 }

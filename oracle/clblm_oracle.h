@@ -49,6 +49,22 @@ int ocl_rt_mode2_par(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t 
                      const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl, double *rad,
                      int64_t cap, int64_t *npts, double *dv, int nthreads);
 
+/* noScattJacob (down-looking thermal nadir, airmass scaling, viewing path
+ * as reference): radiance and Jacobians on the uniform grid, level-major
+ * derivative arrays with row length `cap`.  ODs on `nthreads` threads. */
+int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
+                  const clblm_column_t *col, const clblm_rt_ctrl_t *ctrl,
+                  const clblm_jac_t *jac, double *rad, double *dtlev, double *dqlev,
+                  double *dtsfc, double *demis, int64_t cap, int64_t *npts, double *dv,
+                  int nthreads);
+/* The per-point recurrence of Jacobians (down-looking branch), for the
+ * finite-difference checks of the tests. */
+int ocl_jac_point(const double *viewOD, const double *downOD, const double *amfView,
+                  const double *amfDown, const double *Tlay, const double *Tlev, double Tsfc,
+                  double emis, double vn, int nLay, int linInTau, const double *dT_dTup,
+                  const double *dT_dTlo, double *dRad_dTlev, double *dRad_dTau, double *rad,
+                  double *dRad_dTsfc, double *dRad_dEmis);
+
 /* Building blocks exposed for known-answer tests. */
 void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg,
                       double *xver); /* each [3001] */

@@ -63,6 +63,10 @@ def lib():
         L.ocl_tips_scor.argtypes = [C.c_int, C.c_double, P(C.c_double)]
         L.ocl_interp_spectrum.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, P(C.c_double),
                                           C.c_double, C.c_double, C.c_int64]
+        L.ocl_jac_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
+                                    P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + [P(C.c_double)] * 5 + [
+                                    C.c_int64, P(C.c_int64), P(C.c_double), C.c_int]
+        L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
                                                                                     P(C.c_double), P(C.c_int)]
         _lib = L
@@ -126,6 +130,42 @@ class Session:
                                            C.byref(cols), C.byref(ctrl), _dp(out), cap, C.byref(n),
                                            C.byref(dv), int(nthreads)))
         return out[:n.value].copy(), dv.value
+
+
+def jac_mode2(session, lines, col, ctrl, jac, cont=None, nthreads=1, cap=None):
+    """noScattJacob on the uniform grid: dict of rad, dtlev [nlay+1, n],
+    dqlev [nlay+1, n], dtsfc, demis and the grid (v1, dv)."""
+    if cap is None:
+        dn, df, do = session.setdv(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, 1, ctrl.dv_user)
+        cap = int(np.ceil((col.v2 - col.v1) / do)) + 64
+    nl = col.nlay
+    rad, dts, dem = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+    dtl, dql = np.zeros((nl + 1, cap)), np.zeros((nl + 1, cap))
+    n, dv = C.c_int64(), C.c_double()
+    ls, cs, js = lines.struct(), col.struct(), jac.struct()
+    conts = cont.struct() if cont is not None else None
+    session.reset()
+    session._check(lib().ocl_jac_mode2(session.h, C.byref(ls), C.byref(conts) if conts is not None else None,
+                                       C.byref(cs), C.byref(ctrl), C.byref(js), _dp(rad), _dp(dtl), _dp(dql),
+                                       _dp(dts), _dp(dem), cap, C.byref(n), C.byref(dv), int(nthreads)))
+    k = n.value
+    return {"rad": rad[:k].copy(), "dtlev": dtl[:, :k].copy(), "dqlev": dql[:, :k].copy(), "dtsfc": dts[:k].copy(),
+            "demis": dem[:k].copy(), "v1": col.v1, "dv": dv.value}
+
+
+def jac_point(view_od, down_od, amf_view, amf_down, tlay, tlev, tsfc, emis, vn, lin_in_tau, dt_dtup, dt_dtlo):
+    """The per-point recurrence of Jacobians: (rad, dRad_dTau, dRad_dTlev, dRad_dTsfc, dRad_dEmis)."""
+    nl = len(view_od)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (view_od, down_od, amf_view, amf_down, tlay, tlev,
+                                                              dt_dtup, dt_dtlo)]
+    dtl, dta = np.zeros(nl + 1), np.zeros(nl)
+    r, ts, em = C.c_double(), C.c_double(), C.c_double()
+    rc = lib().ocl_jac_point(_dp(a[0]), _dp(a[1]), _dp(a[2]), _dp(a[3]), _dp(a[4]), _dp(a[5]), float(tsfc),
+                             float(emis), float(vn), nl, int(lin_in_tau), _dp(a[6]), _dp(a[7]), _dp(dtl), _dp(dta),
+                             C.byref(r), C.byref(ts), C.byref(em))
+    if rc:
+        raise OracleError(rc, "jac_point")
+    return r.value, dta, dtl, ts.value, em.value
 
 
 def shape_tables():

@@ -1,0 +1,66 @@
+"""The oracle's Jacobian recurrence (Jacobians, clblm_noScattJac.f90:346-716)
+against central finite differences of its own radiance (CPU only), and a
+small end-to-end run of noScattJacob."""
+import numpy as np
+import pytest
+
+
+def _column(nl, seed):
+    rng = np.random.default_rng(seed)
+    od = rng.uniform(0.01, 2.0, nl)
+    amf_down = rng.uniform(1.2, 2.0, nl)
+    tlev = np.linspace(288.0, 230.0, nl + 1) + rng.normal(0, 2, nl + 1)
+    tlay = 0.5 * (tlev[:-1] + tlev[1:]) + rng.normal(0, 0.5, nl)
+    return od, amf_down, tlev, tlay
+
+
+@pytest.mark.parametrize("lin_in_tau", [0, 1, 2])
+def test_recurrence_derivatives_match_central_differences(oracle_mod, lin_in_tau):
+    nl, vn, tsfc, emis = 6, 900.0, 290.0, 0.93
+    od, amfd, tlev, tlay = _column(nl, 3 + lin_in_tau)
+    amfv = np.ones(nl)
+    zero = np.zeros(nl)
+
+    def rad_of(tau, tl=tlev, ts=tsfc, em=emis):
+        return oracle_mod.jac_point(tau * amfv, tau * amfd, amfv, amfd, tlay, tl, ts, em, vn, lin_in_tau,
+                                    zero, zero)[0]
+
+    r, dta, dtl, dts, dem = oracle_mod.jac_point(od * amfv, od * amfd, amfv, amfd, tlay, tlev, tsfc, emis, vn,
+                                                 lin_in_tau, zero, zero)
+    assert r == pytest.approx(rad_of(od), rel=1e-15)
+    for l in range(nl):
+        h = 1e-5 * od[l]
+        p, m = od.copy(), od.copy()
+        p[l] += h
+        m[l] -= h
+        fd = (rad_of(p) - rad_of(m)) / (2 * h)
+        assert dta[l] == pytest.approx(fd, rel=1e-6, abs=1e-12 * abs(r)), (l, dta[l], fd)
+    if lin_in_tau != 0:  # level temperatures enter through the level Planck terms
+        for lv in range(nl + 1):
+            p, m = tlev.copy(), tlev.copy()
+            p[lv] += 1e-3
+            m[lv] -= 1e-3
+            fd = (rad_of(od, tl=p) - rad_of(od, tl=m)) / 2e-3
+            assert dtl[lv] == pytest.approx(fd, rel=1e-6, abs=1e-12 * abs(r)), (lv, dtl[lv], fd)
+    fd = (rad_of(od, ts=tsfc + 1e-3) - rad_of(od, ts=tsfc - 1e-3)) / 2e-3
+    assert dts == pytest.approx(fd, rel=1e-6)
+    fd = (rad_of(od, em=emis + 1e-6) - rad_of(od, em=emis - 1e-6)) / 2e-6
+    assert dem == pytest.approx(fd, rel=1e-6)
+
+
+def test_small_jacobian_run(oracle_mod, mtckd):
+    from clblm_gb300 import synth, capi_types as T
+    lines, col, cont = synth.config1(n_lines=20000)
+    # layers 10-12 (about 240-150 hPa): below the H2O floor, so the mixing
+    # ratio differs between levels (level2layer divides by its log ratio)
+    c = col.sub([10, 11, 12]).with_window(1000.0, 1004.0)
+    prof = synth.jac_profile(col).sub(10, 3)
+    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN, grid_type=1)
+    out = oracle_mod.jac_mode2(oracle_mod.Session(), lines, c, ctrl, prof, mtckd)
+    n = len(out["rad"])
+    assert n > 1000 and np.all(np.isfinite(out["rad"])) and np.all(out["rad"] > 0)
+    for k in ("dtlev", "dqlev"):
+        assert out[k].shape == (4, n) and np.all(np.isfinite(out[k]))
+    # a warmer surface and a warmer top level raise the upwelling radiance
+    assert np.all(out["dtsfc"] >= 0)
+    assert np.median(out["dtlev"][3]) > 0
