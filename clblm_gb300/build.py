@@ -22,6 +22,7 @@ UNITS = {
     "prep.cu": ["--fmad=false"],
     "panel.cu": [],
     "rt.cu": [],
+    "jac.cu": [],
     "runtime.cu": [],
 }
 

@@ -21,7 +21,8 @@ LIB_PATH = HERE / "libclblm_gb300.so"
 EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clblm_gpu_last_error",
            "clblm_gpu_stream",
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
-           "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_interp_spectrum_noalloc")
+           "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
+           "clblm_gpu_interp_spectrum_noalloc")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -62,6 +63,10 @@ def lib():
                                               P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), C.c_void_p,
                                          C.c_int64, C.c_int32]
+        L.clblm_gpu_jac_size.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t),
+                                         P(C.c_int64), P(C.c_double)]
+        L.clblm_gpu_jac.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + \
+            [C.c_void_p] * 5 + [C.c_int64, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
                                                         C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
         _lib = L
@@ -156,6 +161,48 @@ class Handle:
         cs = col.struct()
         self._check(lib().clblm_gpu_rt_mode2(self.h, C.byref(cs), C.byref(ctrl), C.c_void_p(dptr), cap,
                                              T.CLBLM_OUT_DEVICE))
+
+
+def _jac_methods():
+    def jac_size(self, col, ctrl, jac):
+        n, dv = C.c_int64(), C.c_double()
+        cs, js = col.struct(), jac.struct()
+        self._check(lib().clblm_gpu_jac_size(self.h, C.byref(cs), C.byref(ctrl), C.byref(js), C.byref(n),
+                                             C.byref(dv)))
+        return n.value, dv.value
+
+    def jac(self, col, ctrl, jac):
+        """Radiance and Jacobians (noScattJacob) on the uniform grid: dict of
+        rad, dtlev [nlay+1, n], dqlev [nlay+1, n], dtsfc, demis, v1, dv."""
+        n, dv = self.jac_size(col, ctrl, jac)
+        nl = col.nlay
+        out = {"rad": np.empty(n), "dtsfc": np.empty(n), "demis": np.empty(n),
+               "dtlev": np.empty((nl + 1, n)), "dqlev": np.empty((nl + 1, n))}
+        cs, js = col.struct(), jac.struct()
+        ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._check(lib().clblm_gpu_jac(self.h, C.byref(cs), C.byref(ctrl), C.byref(js), ptr(out["rad"]),
+                                        ptr(out["dtlev"]), ptr(out["dqlev"]), ptr(out["dtsfc"]), ptr(out["demis"]),
+                                        n, T.CLBLM_OUT_HOST))
+        out["v1"], out["dv"] = col.v1, dv
+        return out
+
+    def jac_device(self, col, ctrl, jac, rad=0, dtlev=0, dqlev=0, dtsfc=0, demis=0, cap=0):
+        """The same into device buffers (device addresses, level-major rows of `cap`)."""
+        cs, js = col.struct(), jac.struct()
+        self._check(lib().clblm_gpu_jac(self.h, C.byref(cs), C.byref(ctrl), C.byref(js), C.c_void_p(rad or None),
+                                        C.c_void_p(dtlev or None), C.c_void_p(dqlev or None),
+                                        C.c_void_p(dtsfc or None), C.c_void_p(demis or None), cap,
+                                        T.CLBLM_OUT_DEVICE))
+
+    return jac_size, jac, jac_device
+
+
+Handle.jac_size, Handle.jac, Handle.jac_device = _jac_methods()
+
+
+def noScattJacob(handle, col, ctrl, jac):
+    """Radiance and level Jacobians of a nadir column (clblm_noScattJac.f90:20)."""
+    return handle.jac(col, ctrl, jac)
 
 
 def setDV(col, sample=4.0, alfal0=0.04, alfal0_fine=0.005, grid_type=0, dv_user=-1.0):

@@ -57,6 +57,7 @@ struct LayerPlan {
   int64_t f4_lo, f4_hi;           // LINF4Q line range [lo, hi)
   // continuum (ABSRB on V1ABS + (i-1)*DVABS, 1-based)
   int contnm;                     // 1: continuum on
+  int jac_mol;                    // icflg: molecule whose continuum derivative term is added
   double v1abs, v2abs, dvabs, xself, xfrgn, wk1, h2o_fac;
   int nptabs;
   // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected

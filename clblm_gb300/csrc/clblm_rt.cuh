@@ -42,6 +42,79 @@ struct RtLayerArgs {
   float xs0, xs1;      // surface: v/kT_skin on the merged-input grid
 };
 
+// 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365),
+// in FP64 and as FP32 copies for the mixed path (defined in rt.cu)
+extern __constant__ double c_IA1[203], c_IA2[203], c_IA3[203], c_IA4[203];
+extern __constant__ float c_IAf[4][203];
+
+// Stencil of output point I (1-based) of grid (V1, dvout, nout) on the input
+// grid (V1, dvin, nin): up to four input indices and weights of type W.
+template <typename W>
+struct Stencil {
+  int64_t i[4];
+  W w[4];
+  int n;
+};
+
+template <typename W>
+__device__ __forceinline__ W ia_coef(int k, int IP) {
+  if constexpr (sizeof(W) == 8) return k == 0 ? c_IA1[IP] : k == 1 ? c_IA2[IP] : k == 2 ? c_IA3[IP] : c_IA4[IP];
+  else return c_IAf[k][IP];
+}
+template <typename W>
+__device__ __forceinline__ W b_coef(const InterpSpec& s, int k, int NL) {
+  if constexpr (sizeof(W) == 8) return k == 0 ? s.b1[NL] : k == 1 ? s.b2[NL] : k == 2 ? s.b3[NL] : s.b4[NL];
+  else return s.bf[k][NL];
+}
+
+template <typename W = double>
+__device__ __forceinline__ Stencil<W> interp_stencil(const InterpSpec& s, int64_t I) {
+  Stencil<W> st;
+  st.n = 0;
+  if (s.kind == 0) {  // same grid
+    st.i[0] = I;
+    st.w[0] = 1.;
+    st.n = 1;
+    return st;
+  }
+  if (s.itype == 0) {  // aligned copy (ratio 1 with a different length, or 2)
+    st.i[0] = I * s.nint_ratio - (s.nint_ratio - 1);
+    st.w[0] = 1.;
+    st.n = 1;
+    return st;
+  }
+  if (s.itype > 0) {  // fixed ratio n/(n+1) or (n+1)/n
+    int64_t g = (I - 1) / s.len_out;
+    int NL = (int)((I - 1) % s.len_out) + 1;
+    if (NL == 1) {
+      st.i[0] = 1 + g * s.len_in;
+      st.w[0] = 1.;
+      st.n = 1;
+      return st;
+    }
+    int64_t iIn = NL - s.len_in + (g + 1) * (int64_t)s.len_in;
+    if (s.dvin > s.dvout) iIn -= 1;
+    st.i[0] = iIn - 1;
+    st.i[1] = iIn;
+    st.i[2] = iIn + 1;
+    st.i[3] = iIn + 2;
+    for (int k = 0; k < 4; ++k) st.w[k] = b_coef<W>(s, k, NL);
+    st.n = 4;
+    return st;
+  }
+  // general ratio: (iIn, IP) replayed per output point by k_interp_map
+  int2 mp = s.map[I - 1];
+  int64_t iIn = mp.x;
+  int IP = mp.y;
+  st.i[0] = iIn - 1;
+  st.i[1] = iIn;
+  st.i[2] = iIn + 1;
+  st.i[3] = iIn + 2;
+  for (int k = 0; k < 4; ++k) st.w[k] = ia_coef<W>(k, IP);
+  st.n = 4;
+  return st;
+}
+
 void rt_upload_interp_coef(cudaStream_t st);
 __global__ void k_interp_map(InterpSpec s, const int64_t* blk_j1, const double* blk_vo, int nblk, int64_t nout,
                              int2* map);

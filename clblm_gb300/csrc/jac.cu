@@ -1,0 +1,286 @@
+// jac.cu -- Jacobians of the nadir thermal radiance (noScattJacob,
+// clblm_noScattJac.f90:20-339) on the GPU.
+//
+//   k_interp_map_jobs  (iIn, IP) maps of every layer OD of a block that needs
+//                      interpSpectrum's general-ratio branch (the DVout step of
+//                      ODLAY, clblm_ODLAY.f90:582-598)
+//   k_od_jobs          every layer OD of the block on the uniform grid, binary64
+//   k_jac<Plain>       one thread per spectral point: the down-looking
+//                      recurrence of Jacobians (:346-716) over the layers,
+//                      then the level-temperature derivatives of drv_LevelTemp
+//                      (:899-1065) and the molecule derivatives of
+//                      drv_LevelConc (:1069-1203)
+//
+// The per-point recurrence keeps its per-layer arrays in local memory
+// (at most kMaxJacLayers layers).  The mixed path runs it in FP32, the FP64
+// path in binary64 with the reference's operation order.
+#include <cuda_runtime.h>
+
+#include "clblm_common.cuh"
+#include "clblm_jac.cuh"
+#include "clblm_kernels.cuh"
+#include "clblm_panel.cuh"
+#include "clblm_rt.cuh"
+
+namespace clblm {
+
+__global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob, const int64_t* __restrict__ blk_j1,
+                                  const double* __restrict__ blk_vo, int nblk, int64_t nout) {
+  const int j = blockIdx.y;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njob || b >= nblk) return;
+  const InterpSpec& s = jobs[j].spec;
+  if (s.kind == 0 || s.itype >= 0) return;
+  int2* map = jobs[j].map;
+  const double Vo = blk_vo[b];
+  int64_t iIn = (int64_t)__dadd_rn(__ddiv_rn(__dadd_rn(Vo, -s.v1), s.dvin), 1.00001);
+  double Vi = __dadd_rn(s.v1, __dmul_rn((double)(iIn - 1), s.dvin));
+  double P = __ddiv_rn(__dadd_rn(Vo, -Vi), s.dvin);
+  const int64_t J1 = blk_j1[b];
+  const int64_t J2 = min(nout, J1 + 2400 - 1);
+  for (int64_t J = J1; J <= J2; ++J) {
+    int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
+    map[J - 1] = make_int2((int)iIn, IP < 0 ? 0 : (IP > 202 ? 202 : IP));
+    P = __dadd_rn(P, s.ratio);
+    if (P >= 1.0) {
+      iIn = (int64_t)__dadd_rn((double)iIn, P);
+      P = __dadd_rn(P, -(double)((int64_t)P));
+    }
+  }
+}
+
+// interpSpectrum's linear extension by two points past either end
+template <typename Real>
+__device__ __forceinline__ double od_ext(const Real* x, int64_t n, int64_t i) {
+  if (i >= 1 && i <= n) return (double)x[i - 1];
+  if (i == 0 || i == -1) return 2.0 * (double)x[0] - (double)x[1];
+  if (i == n + 1 || i == n + 2) return 2.0 * (double)x[n - 1] - (double)x[n - 2];
+  return 0.;
+}
+
+template <bool Plain>
+__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, int64_t nout, void* out) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  const int j = blockIdx.y;
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j >= njob || I > nout) return;
+  const JacJob& jb = jobs[j];
+  const Real* x = reinterpret_cast<const Real*>(od_all) + jb.od_off;
+  const Stencil<double> st = interp_stencil<double>(jb.spec, I);
+  double v = 0.;
+  if (st.n == 1) v = od_ext(x, jb.n_in, st.i[0]);
+  else
+    for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext(x, jb.n_in, st.i[k]);
+  reinterpret_cast<Real*>(out)[(int64_t)jb.slot * nout + (I - 1)] = (Real)v;
+}
+
+template __global__ void k_od_jobs<false>(const JacJob*, int, const void*, int64_t, void*);
+template __global__ void k_od_jobs<true>(const JacJob*, int, const void*, int64_t, void*);
+
+// ---- the per-point recurrence (Jacobians, down-looking branch) ------------
+template <typename Real>
+__device__ __forceinline__ Real dev_exp(Real x) {
+  if constexpr (sizeof(Real) == 8) return exp(x);
+  else return __expf(x);
+}
+
+// planckFnDrv, clblm_EMLAY.f90:45-70
+template <typename Real>
+__device__ __forceinline__ void planck_drv_t(double V, Real T, Real* B, Real* dB) {
+  const Real RC1 = (Real)kRADCN1, RC2 = (Real)kRADCN2;
+  Real XKT = T / RC2;
+  if (XKT <= (Real)1.e-6) {
+    *B = 0;
+    *dB = 0;
+    return;
+  }
+  const Real Vr = (Real)V;
+  Real cv3 = RC1 * Vr * Vr * Vr;
+  Real evt = dev_exp(Vr / XKT);
+  *B = cv3 / (evt - 1);
+  *dB = *B * *B * (evt * Vr) / (RC2 * cv3 * XKT * XKT);
+}
+
+// rlin with its derivative, clblm_EMLAY.f90:187-223
+template <typename Real>
+__device__ __forceinline__ void rlin_t(Real od, Real* hlf, Real* dhlf) {
+  const Real dbAvg2dtau = (Real)(-1. / 12);
+  if (od < (Real)1.e-03) {
+    *hlf = (Real)0.5 + od * dbAvg2dtau;
+    *dhlf = dbAvg2dtau;
+  } else if (od > (Real)20.) {
+    *hlf = 1 / od;
+    *dhlf = -1 / (od * od);
+  } else {
+    Real tex = dev_exp(od);
+    *hlf = 1 / (od)-1 / (tex - 1);
+    *dhlf = -1 / (od * od) + tex / ((tex - 1) * (tex - 1));
+  }
+}
+
+template <bool Plain>
+__global__ void __launch_bounds__(128) k_jac(JacArgs a) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  const int64_t iv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (iv >= a.nout) return;
+  const int N2 = a.nlay;
+  constexpr int M = kMaxJacLayers + 2;
+  Real viewOD[M], downOD[M], Bbar[M], dBbar[M], Blev[M], dBlev[M], cumTxA[M], cumTxB2[M];
+  Real dRad_dT_up[M], dRad_dT_dn[M], dRad_dTbar[M], dRad_dTau[M], dRad_dTlev[M];
+  const Real* jod = reinterpret_cast<const Real*>(a.jod);
+  const double vn = a.v1 + (double)iv * a.dv;
+  for (int l = 1; l <= N2; ++l) {
+    viewOD[l] = jod[(int64_t)(l - 1) * a.nout + iv];
+    downOD[l] = viewOD[l] * (Real)a.amf_down[l - 1];
+  }
+  if (a.lin_in_tau != 0)
+    for (int lv = 1; lv <= N2 + 1; ++lv) planck_drv_t<Real>(vn, (Real)a.tlev[lv - 1], &Blev[lv], &dBlev[lv]);
+  for (int l = 1; l <= N2; ++l) planck_drv_t<Real>(vn, (Real)a.tlay[l - 1], &Bbar[l], &dBbar[l]);
+  Real Bsfc, dBsfc;
+  planck_drv_t<Real>(vn, (Real)a.tsfc, &Bsfc, &dBsfc);
+  Real rad = 0;
+  for (int l = 1; l <= N2; ++l) dRad_dTau[l] = dRad_dTbar[l] = 0;
+  for (int l = 1; l <= N2 + 1; ++l) dRad_dT_up[l] = dRad_dT_dn[l] = dRad_dTlev[l] = 0;
+  const int obsLay = N2 + 1;
+  // 0- transmittance along the upwelling path from TOA down
+  Real cumODA = 0;
+  cumTxA[N2 + 1] = 1;
+  for (int l = obsLay - 1; l >= 1; --l) {
+    cumODA = cumODA + viewOD[l];
+    cumTxA[l] = dev_exp(-cumODA);
+  }
+  const Real totODUp = cumODA, totTxUp = cumTxA[1];
+  Real dbavgdb, dbavgdbdod, Blt, dTran;
+  const int lit = a.lin_in_tau;
+  const bool dT = a.do_temp != 0;
+  // 1- downwelling thermal radiance
+  if (totTxUp > (Real)1.e-06) {
+    cumTxB2[1] = totTxUp;
+    Real cumODB = 0;
+    for (int l = 1; l <= N2; ++l) {
+      cumODB = cumODB + downOD[l];
+      cumTxB2[l + 1] = dev_exp(-(totODUp + cumODB));
+    }
+    for (int l = N2; l >= 1; --l) {
+      dTran = cumTxB2[l] - cumTxB2[l + 1];
+      const Real amf = (Real)a.amf_down[l - 1];
+      if (lit != 0) {
+        rlin_t(downOD[l], &dbavgdb, &dbavgdbdod);
+        if (lit == 2) {
+          Blt = Blev[l] + (Blev[l + 1] - Blev[l]) * dbavgdb;
+          dRad_dTau[l] = (cumTxB2[l + 1] * Blt - rad + dTran * dbavgdbdod * (Blev[l + 1] - Blev[l])) * amf;
+          if (dT) {
+            dRad_dT_dn[l + 1] = dRad_dT_dn[l + 1] + dTran * dBlev[l + 1] * dbavgdb;
+            dRad_dT_dn[l] = dTran * dBlev[l] * (1 - dbavgdb);
+            dRad_dTbar[l] = 0;
+          }
+        } else {
+          Blt = 2 * Bbar[l] * dbavgdb + Blev[l] * (1 - 2 * dbavgdb);
+          dRad_dTau[l] = (cumTxB2[l + 1] * Blt - rad + 2 * dTran * dbavgdbdod * (Bbar[l] - Blev[l])) * amf;
+          if (dT) {
+            dRad_dT_dn[l] = dTran * dBlev[l] * (1 - 2 * dbavgdb);
+            dRad_dTbar[l] = dTran * 2 * dBbar[l] * dbavgdb;
+          }
+        }
+        rad = rad + dTran * Blt;
+      } else {
+        dRad_dTau[l] = (cumTxB2[l + 1] * Bbar[l] - rad) * amf;
+        rad = rad + dTran * Bbar[l];
+        if (dT) dRad_dTbar[l] = dTran * dBbar[l];
+      }
+    }
+  }
+  // 2- surface reflectance; 3- surface terms
+  const Real emis = (Real)a.emis, rsfc = 1 - emis;
+  for (int l = 1; l <= N2; ++l) {
+    dRad_dTau[l] = dRad_dTau[l] * rsfc;
+    if (dT) dRad_dTbar[l] = dRad_dTbar[l] * rsfc;
+  }
+  const Real dRad_dEmis = totTxUp * Bsfc - rad;
+  const Real dRad_dTsfc = emis * totTxUp * dBsfc;
+  rad = rad * rsfc + emis * totTxUp * Bsfc;
+  // 5- upwelling thermal radiance
+  for (int l = 1; l <= obsLay - 1; ++l) {
+    dTran = cumTxA[l + 1] - cumTxA[l];
+    if (lit != 0) {
+      rlin_t(viewOD[l], &dbavgdb, &dbavgdbdod);
+      if (lit == 2) {
+        Blt = Blev[l + 1] * (1 - dbavgdb) + Blev[l] * dbavgdb;
+        dRad_dTau[l] = dRad_dTau[l] + (cumTxA[l] * Blt - rad + dTran * dbavgdbdod * (Blev[l] - Blev[l + 1]));
+        if (dT) {
+          dRad_dT_up[l + 1] = dTran * dBlev[l + 1] * (1 - dbavgdb);
+          dRad_dT_up[l] = dRad_dT_up[l] + dTran * dBlev[l] * dbavgdb;
+        }
+      } else {
+        Blt = 2 * Bbar[l] * dbavgdb + Blev[l + 1] * (1 - 2 * dbavgdb);
+        dRad_dTau[l] = dRad_dTau[l] + (cumTxA[l] * Blt - rad + dTran * dbavgdbdod * 2 * (Bbar[l] - Blev[l + 1]));
+        if (dT) {
+          dRad_dT_up[l + 1] = dTran * dBlev[l + 1] * (1 - 2 * dbavgdb);
+          dRad_dTbar[l] = dRad_dTbar[l] + dTran * 2 * dBbar[l] * dbavgdb;
+        }
+      }
+      rad = rad + dTran * Blt;
+    } else {
+      dRad_dTau[l] = dRad_dTau[l] + (cumTxA[l] * Bbar[l] - rad);
+      rad = rad + dTran * Bbar[l];
+      if (dT) dRad_dTbar[l] = dRad_dTbar[l] + dTran * dBbar[l];
+    }
+  }
+  // (amfView = 1: the viewing path is the reference path)
+  if (dT) {
+    if (lit != 0)
+      for (int lv = 1; lv <= N2 + 1; ++lv) dRad_dTlev[lv] = dRad_dT_up[lv] + dRad_dT_dn[lv] * rsfc;
+    if (lit == 0 || lit == 1)
+      for (int l = N2; l >= 1; --l) {
+        dRad_dTlev[l + 1] = dRad_dTlev[l + 1] + dRad_dTbar[l] * (Real)a.dT_dTup[l - 1];
+        dRad_dTlev[l] = dRad_dTlev[l] + dRad_dTbar[l] * (Real)a.dT_dTlo[l - 1];
+      }
+  }
+  const int64_t o = a.off + iv;
+  if (a.rad) a.rad[o] = (double)rad;
+  if (a.dtsfc) a.dtsfc[o] = (double)dRad_dTsfc;
+  if (a.demis) a.demis[o] = (double)dRad_dEmis;
+  // drv_LevelTemp: dTau/dT = [tau(T+1) - tau(T)] - (Wtot/T) dTau/dWtot
+  if (dT && a.dtlev && a.vT >= 0) {
+    Real lo = 0;
+    for (int il = 0; il < N2; ++il) {
+      const Real m = jod[(int64_t)il * a.nout + iv];
+      const Real tp = jod[((int64_t)a.vT * N2 + il) * a.nout + iv];
+      const Real wp = jod[((int64_t)a.vW * N2 + il) * a.nout + iv];
+      Real dTau_dT;
+      if constexpr (Plain) {
+        dTau_dT = tp - m;
+        const double deltaW = 0.01 * a.wtot[il];
+        const double dTau_dW = (wp - m) / deltaW;
+        const double fac = a.wtot[il] / a.tlay[il];
+        dTau_dT = dTau_dT - dTau_dW * fac;
+      } else {
+        // (wp - m) / (0.01 Wtot) * (Wtot / T) = (wp - m) * 100 / T
+        dTau_dT = (tp - m) - (wp - m) * (100.f / (float)a.tlay[il]);
+      }
+      const Real dRaddT = dRad_dTau[il + 1] * dTau_dT;
+      const Real up = dRaddT * (Real)a.dT_dTup[il];
+      lo = lo + dRaddT * (Real)a.dT_dTlo[il] + dRad_dTlev[il + 1];
+      a.dtlev[(int64_t)il * a.ld + o] = (double)lo;
+      if (il == N2 - 1) a.dtlev[(int64_t)N2 * a.ld + o] = (double)(up + dRad_dTlev[il + 2]);
+      lo = up;
+    }
+  }
+  // drv_LevelConc: dTau/dln W = the OD of the molecule alone
+  if (a.dqlev && a.vM >= 0) {
+    Real lo = 0;
+    for (int il = 0; il < N2; ++il) {
+      const Real dRad_dW = dRad_dTau[il + 1] * jod[((int64_t)a.vM * N2 + il) * a.nout + iv];
+      const Real up = dRad_dW * (Real)a.dW_dQup[il];
+      lo = lo + dRad_dW * (Real)a.dW_dQlo[il];
+      a.dqlev[(int64_t)il * a.ld + o] = (double)lo;
+      if (il == N2 - 1) a.dqlev[(int64_t)N2 * a.ld + o] = (double)up;
+      lo = up;
+    }
+  }
+}
+
+template __global__ void k_jac<false>(JacArgs);
+template __global__ void k_jac<true>(JacArgs);
+
+}  // namespace clblm

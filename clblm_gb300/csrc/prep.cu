@@ -524,7 +524,13 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
   forc = 0. + forc * 1.0;
   double cself = P.wk1 * self * P.xself;
   double cfor = P.wk1 * forc * P.xfrgn;
-  ABSRB[I] = 0. + cself + cfor;
+  double ab = 0. + cself + cfor;
+  if (P.jac_mol == 1) {  // OD for the H2O Jacobian, clblm_ODLAY_Continuum.f90:394-401
+    double cfrgn_aj = (P.h2o_fac >= 1.0) ? 0. : P.wk1 * forc * P.h2o_fac / (1.0 - P.h2o_fac);
+    double c = cself - cfrgn_aj;
+    ab = ab + c;
+  }
+  ABSRB[I] = ab;
 }
 
 // ---- far-wing lines: LINF4Q per-line corrections --------------------------

@@ -23,6 +23,7 @@
 #include "clblm_kernels.cuh"
 #include "clblm_panel.cuh"
 #include "clblm_ref_tables.h"
+#include "clblm_jac.cuh"
 #include "clblm_rt.cuh"
 
 using namespace clblm;
@@ -78,6 +79,7 @@ struct clblm_handle {
   DevBuf pblk, bv1, bn, bm0, bfac;
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
   DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
+  DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp;
   DevBuf rt[4], outbuf, imap[2];
   std::string errmsg;
@@ -543,6 +545,7 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
       h->nlines, lower_bound_h(h->h_vnu, P.f4_lo, h->nlines, P.v2l4 + h->shiftmax * P.rhorat + 1e-6) + 2 * 250);
   // continuum grid, OPDPTH :880-896
   P.contnm = c->contnm_off ? 0 : 1;
+  P.jac_mol = c->jac_mol;
   if (P.contnm) {
     if (!h->has_cont) return set_err(h, CLBLM_ERR_ARG, "continuum requested but the handle has no table");
     P.dvabs = 1.;
@@ -1074,7 +1077,8 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm,      &h->reclo};
+                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
+                    &h->jblk};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
   for (auto& b : h->imap) b.release();
@@ -1535,3 +1539,368 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
   if (cudaGetLastError() != cudaSuccess) return CLBLM_ERR_CUDA;
   return CLBLM_OK;
 }
+
+// ---- Jacobians of the nadir radiance (noScattJacob) --------------------------
+namespace {
+
+// level2layer, clblm_noScattJac.f90:1208-1279, for one molecule (level l+1
+// is the top of layer l)
+void level2layer_h(const double* Plev, const double* Tlev, const double* Tave, const double* QLev, int nLay,
+                   double* dT_dTup, double* dT_dTlo, double* dW_dQup, double* dW_dQlo) {
+  for (int l = 0; l < nLay; ++l) {
+    const double Pup = Plev[l + 1], Plo = Plev[l], Tup = Tlev[l + 1], Tlo = Tlev[l], Tbar = Tave[l];
+    const double rhoU = Pup / (Tup * 1.3806503E-19);
+    const double rhoL = Plo / (Tlo * 1.3806503E-19);
+    const double alpha = rhoU / rhoL;
+    const double alphaT = -(Tup - Tlo) / std::log(alpha);
+    dT_dTlo[l] = ((Tbar - alphaT) / Tlo) * (rhoL / (rhoL - rhoU)) + (1.0 - alphaT / Tlo) / std::log(alpha);
+    dT_dTup[l] = ((Tbar - alphaT) / Tup) * (-rhoU / (rhoL - rhoU)) - (1.0 - alphaT / Tup) / std::log(alpha);
+    dW_dQup[l] = dW_dQlo[l] = 0.;
+    if (QLev && QLev[l] != 0.0) {
+      const double ratU = QLev[l + 1] / rhoU, ratL = QLev[l] / rhoL;
+      dW_dQlo[l] = (ratL / (ratL - alpha * ratU)) + 1.0 / std::log(alpha * ratU / ratL);
+      dW_dQup[l] = ((-alpha * ratU) / (ratL - alpha * ratU)) - 1.0 / std::log(alpha * ratU / ratL);
+    }
+  }
+}
+
+// The ODLAY calls of one Jacobian block, in the reference's order (which the
+// sticky JRAD depends on): the viewing-path layers (pathOD_up_dn_sun), then
+// per layer T+1 K and Wtot*1.01 (drv_LevelTemp), then per layer the
+// Jacobian molecule alone (drv_LevelConc).
+struct JacSetup {
+  int nvar = 1, vT = -1, vW = -1, vM = -1, imol = -1;
+  std::vector<int> job_var, job_lay;
+  std::vector<clblm_layer_t> lays;  // [variant * nlay + layer]
+  std::vector<double> wmol;         // amounts of the molecule-alone layers
+  double dvb = 0.;
+};
+
+int jac_setup(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac,
+              JacSetup* js, std::vector<double>* dvn, std::vector<double>* dvf) {
+  if (!col || !ctrl || !jac || !jac->plev || col->nlay < 1) return set_err(h, CLBLM_ERR_ARG, "bad Jacobian input");
+  if (!col->tbot || !col->ttop || !col->wtot_down) return set_err(h, CLBLM_ERR_ARG, "bad column");
+  if (col->nlay > kMaxJacLayers) return set_err(h, CLBLM_ERR_UNSUPPORTED, "more than %d layers", kMaxJacLayers);
+  if (ctrl->grid_type != 1)
+    return set_err(h, CLBLM_ERR_GRID, "noScattJacob: spectral grid is not uniform (gridType 1)");
+  const int nl = col->nlay, nmol = col->nmol;
+  if (jac->jac_mol > 0) {
+    for (int k = 0; k < nmol; ++k)
+      if (col->mol_id[k] == jac->jac_mol) js->imol = k;
+    if (js->imol < 0 || !jac->qlev) return set_err(h, CLBLM_ERR_ARG, "invalid molecule for Jacobian calculation");
+  }
+  dvn->resize(nl);
+  dvf->resize(nl);
+  int rc = clblm_setdv(col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, 1, ctrl->dv_user, dvn->data(),
+                       dvf->data(), &js->dvb);
+  if (rc == CLBLM_ERR_DV_RATIO) return set_err(h, rc, "layer DV ratio > 2.5");
+  if (rc) return set_err(h, rc, "setDV failed");
+  if (!(js->dvb > 0.)) return set_err(h, CLBLM_ERR_GRID, "noScattJacob: DVout not set");
+  js->nvar = 1;
+  if (jac->do_temp) {
+    js->vT = js->nvar++;
+    js->vW = js->nvar++;
+  }
+  if (js->imol >= 0) js->vM = js->nvar++;
+  js->lays.resize((size_t)js->nvar * nl);
+  js->wmol.assign((size_t)nl * nmol, 0.);
+  for (int v = 0; v < js->nvar; ++v)
+    for (int il = 0; il < nl; ++il) {
+      clblm_layer_t& L = js->lays[(size_t)v * nl + il];
+      L.nmol = nmol;
+      L.mol_id = col->mol_id;
+      L.w = col->w + (size_t)il * nmol;
+      L.wtot = col->wtot[il];
+      L.pave = col->pave[il];
+      L.tave = col->tave[il];
+      L.zbot = L.ztop = 0.;
+      L.lay_no = il + 1;
+      if (v == js->vT) L.tave = col->tave[il] + 1.0;
+      if (v == js->vW) L.wtot = col->wtot[il] + 0.01 * col->wtot[il];
+      if (v == js->vM) {
+        js->wmol[(size_t)il * nmol + js->imol] = col->w[(size_t)il * nmol + js->imol];
+        L.w = js->wmol.data() + (size_t)il * nmol;
+      }
+    }
+  js->job_var.clear();
+  js->job_lay.clear();
+  for (int il = 0; il < nl; ++il) js->job_var.push_back(0), js->job_lay.push_back(il);
+  if (jac->do_temp)
+    for (int il = 0; il < nl; ++il) {
+      js->job_var.push_back(js->vT), js->job_lay.push_back(il);
+      js->job_var.push_back(js->vW), js->job_lay.push_back(il);
+    }
+  if (js->vM >= 0)
+    for (int il = 0; il < nl; ++il) js->job_var.push_back(js->vM), js->job_lay.push_back(il);
+  return CLBLM_OK;
+}
+
+// plans of the jobs of the block [V1B, V2B]; returns the block's points
+int jac_plan_block(clblm_handle* h, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac, const JacSetup& js,
+                   const std::vector<double>& dvn, const std::vector<double>& dvf, double V1B, double V2B, int* jr,
+                   bool* fp, std::vector<HostPlan>* hps, int64_t* nlim) {
+  const int njob = (int)js.job_var.size();
+  const int nl = (int)dvn.size();
+  hps->assign(njob, HostPlan());
+  clblm_od_ctrl_t octl = ctrl->od, octl_mol = ctrl->od;
+  octl.jac_mol = 0;
+  octl_mol.jac_mol = jac->jac_mol;
+  for (int j = 0; j < njob; ++j) {
+    const int v = js.job_var[j], il = js.job_lay[j];
+    clblm_grid_t g;
+    g.v1 = V1B;
+    g.v2 = V2B;
+    g.dv_normal = dvn[il];
+    g.dv_narrow = dvf[il];
+    g.dv_out = js.dvb;
+    g.sample = ctrl->sample;
+    g.alfal0 = ctrl->alfal0;
+    int jafter;
+    int rc = plan_layer(h, &js.lays[(size_t)v * nl + il], &g, v == js.vM ? &octl_mol : &octl, *jr, *fp,
+                        &(*hps)[j], &jafter);
+    if (rc) return rc;
+    *jr = jafter;
+    *fp = false;
+  }
+  *nlim = (*hps)[0].n_out;
+  for (int j = 1; j < njob; ++j)
+    if ((*hps)[j].n_out != *nlim) return set_err(h, CLBLM_ERR_GRID, "Jacobian ODs of one block differ in length");
+  return CLBLM_OK;
+}
+
+// the blocks of noScattJacob (clblm_noScattJac.f90:206-232): V1B, V2B
+void jac_blocks(double v1, double v2, double dvb, std::vector<std::pair<double, double>>* blocks) {
+  const int blockSize = 100000;
+  double V1B = v1, V2B = V1B - dvb;
+  while (V2B < v2) {
+    V1B = V2B + dvb;
+    V2B = V1B + (double)(blockSize - 2) * dvb;
+    if (V2B > v2) V2B = v2;
+    blocks->push_back({V1B, V2B});
+    // the next block starts one DVB after the last point ODLAY returns
+    int64_t n = (int64_t)std::ceil((V2B - V1B) / dvb + 1.);
+    V2B = V1B + (double)(n - 1) * dvb;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int clblm_gpu_jac_size(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl,
+                       const clblm_jac_t* jac, int64_t* npts, double* dv) {
+  if (!h) return CLBLM_ERR_ARG;
+  JacSetup js;
+  std::vector<double> dvn, dvf;
+  int rc = jac_setup(h, col, ctrl, jac, &js, &dvn, &dvf);
+  if (rc) return rc;
+  std::vector<std::pair<double, double>> blocks;
+  jac_blocks(col->v1, col->v2, js.dvb, &blocks);
+  int64_t tot = 0;
+  for (auto& b : blocks) tot += (int64_t)std::ceil((b.second - b.first) / js.dvb + 1.);
+  if (npts) *npts = tot;
+  if (dv) *dv = js.dvb;
+  return CLBLM_OK;
+}
+
+int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac,
+                  double* rad, double* dr_dtlev, double* dr_dqlev, double* dr_dtskin, double* dr_demis, int64_t cap,
+                  int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  JacSetup js;
+  std::vector<double> dvn, dvf;
+  int rc = jac_setup(h, col, ctrl, jac, &js, &dvn, &dvf);
+  if (rc) return rc;
+  const int nl = col->nlay;
+  const bool plain = ctrl->od.precision == CLBLM_PREC_PLAIN;
+  const size_t real = plain ? 8 : 4;
+  std::vector<std::pair<double, double>> blocks;
+  jac_blocks(col->v1, col->v2, js.dvb, &blocks);
+  int64_t npts = 0;
+  for (auto& b : blocks) npts += (int64_t)std::ceil((b.second - b.first) / js.dvb + 1.);
+  if (cap < npts) return set_err(h, CLBLM_ERR_CAPACITY, "Jacobian spectra need %lld points", (long long)npts);
+  h->reset_call();
+  // layer and level profiles
+  std::vector<double> tlev(nl + 1), amfd(nl), dTu(nl), dTl(nl), dWu(nl), dWl(nl);
+  for (int l = 0; l < nl; ++l) {
+    tlev[l] = col->tbot[l];
+    amfd[l] = col->wtot_down[l] / col->wtot[l];
+  }
+  tlev[nl] = col->ttop[nl - 1];
+  level2layer_h(jac->plev, tlev.data(), col->tave, js.imol >= 0 ? jac->qlev : nullptr, nl, dTu.data(), dTl.data(),
+                dWu.data(), dWl.data());
+  std::vector<double> prof;  // tlay, tlev, amf_down, wtot, dT_dTup, dT_dTlo, dW_dQup, dW_dQlo
+  for (int l = 0; l < nl; ++l) prof.push_back(col->tave[l]);
+  prof.insert(prof.end(), tlev.begin(), tlev.end());
+  prof.insert(prof.end(), amfd.begin(), amfd.end());
+  for (int l = 0; l < nl; ++l) prof.push_back(col->wtot[l]);
+  for (auto* v : {&dTu, &dTl, &dWu, &dWl}) prof.insert(prof.end(), v->begin(), v->end());
+  CUDA_TRY(h, h->jprof.ensure(sizeof(double) * prof.size()));
+  CUDA_TRY(h, cudaMemcpy(h->jprof.p, prof.data(), sizeof(double) * prof.size(), cudaMemcpyHostToDevice));
+  const double* dprof = h->jprof.as<double>();
+  // outputs: straight into device buffers, or staged on the device
+  const bool dev = flags == CLBLM_OUT_DEVICE;
+  const int64_t ld = dev ? cap : npts;
+  double *o_rad = rad, *o_dtl = dr_dtlev, *o_dql = dr_dqlev, *o_dts = dr_dtskin, *o_dem = dr_demis;
+  if (!dev) {
+    size_t need = sizeof(double) * (size_t)npts * (3 + 2 * (size_t)(nl + 1));
+    CUDA_TRY(h, h->outbuf.ensure(need));
+    double* b = h->outbuf.as<double>();
+    o_rad = rad ? b : nullptr;
+    o_dts = dr_dtskin ? b + npts : nullptr;
+    o_dem = dr_demis ? b + 2 * npts : nullptr;
+    o_dtl = dr_dtlev ? b + 3 * npts : nullptr;
+    o_dql = dr_dqlev ? b + 3 * npts + (size_t)(nl + 1) * npts : nullptr;
+  }
+  int jr = h->jrad;
+  bool fp = h->first_pass_jrad;
+  int64_t total = 0;
+  const size_t budget = (size_t)24 << 30;
+  for (auto& blk : blocks) {
+    std::vector<HostPlan> hps;
+    int64_t nlim;
+    rc = jac_plan_block(h, ctrl, jac, js, dvn, dvf, blk.first, blk.second, &jr, &fp, &hps, &nlim);
+    if (rc) return rc;
+    const int njob = (int)hps.size();
+    // the block's ODs on the uniform grid, [variant][layer][point]
+    CUDA_TRY(h, h->jod.ensure(real * (size_t)js.nvar * nl * nlim));
+    CUDA_TRY(h, h->jmap.ensure(sizeof(int2) * (size_t)njob * nlim));
+    CUDA_TRY(h, h->jjobs.ensure(sizeof(JacJob) * (size_t)njob));
+    // output-grid blocks of interpSpectrum's general branch (shared by all jobs)
+    std::vector<int64_t> j1;
+    std::vector<double> vo;
+    {
+      const double TOL = 1.e-8;
+      const double V2out = blk.first + (double)(nlim - 1) * js.dvb;
+      double Vo = blk.first;
+      while (Vo < V2out + TOL) {
+        int64_t J1 = (int64_t)((Vo - blk.first) / js.dvb + 1.001);
+        int64_t J2 = std::min<int64_t>(nlim, J1 + 2400 - 1);
+        j1.push_back(J1);
+        vo.push_back(Vo);
+        Vo = blk.first + (double)J2 * js.dvb;
+        if (j1.size() > (size_t)(nlim / 2400 + 8)) return set_err(h, CLBLM_ERR_GRID, "interpolation blocks");
+      }
+    }
+    const int nbt = (int)j1.size();
+    CUDA_TRY(h, h->jblk.ensure(16 * (size_t)(nbt + 1)));
+    int64_t* dj1 = h->jblk.as<int64_t>();
+    double* dvo = reinterpret_cast<double*>(h->jblk.as<unsigned char>() + 8 * (size_t)(nbt + 1));
+    CUDA_TRY(h, cudaMemcpyAsync(dj1, j1.data(), 8 * (size_t)nbt, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(dvo, vo.data(), 8 * (size_t)nbt, cudaMemcpyHostToDevice, h->stream));
+    for (int first = 0; first < njob;) {
+      int count = 0;
+      size_t bytes = 0;
+      while (first + count < njob) {
+        const LayerPlan& P = hps[first + count].P;
+        size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
+                   (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+        if (count > 0 && bytes + b > budget) break;
+        bytes += b;
+        count++;
+      }
+      int64_t ls, fs, ps, odt;
+      rc = prepare_batch(h, hps, first, count, plain, &ls, &fs, &ps, &odt);
+      if (rc) return rc;
+      rc = run_od_batch(h, hps, first, count, plain, ls, fs, ps);
+      if (rc) return rc;
+      rc = check_batch(h, hps, first, count, &h->last);
+      if (rc) return rc;
+      std::vector<JacJob> jobs(count);
+      for (int k = 0; k < count; ++k) {
+        const int j = first + k;
+        const LayerPlan& P = hps[j].P;
+        JacJob& jb = jobs[k];
+        jb.spec = interp_spec(P.v1, P.dv, P.nsamp, blk.first, js.dvb, nlim);
+        jb.map = h->jmap.as<int2>() + (size_t)j * nlim;
+        jb.spec.map = jb.map;
+        jb.od_off = P.od_off;
+        jb.n_in = P.nsamp;
+        jb.slot = js.job_var[j] * nl + js.job_lay[j];
+      }
+      CUDA_TRY(h, cudaMemcpyAsync(h->jjobs.p, jobs.data(), sizeof(JacJob) * count, cudaMemcpyHostToDevice,
+                                  h->stream));
+      h->launches += 2;
+      k_interp_map_jobs<<<dim3((unsigned)((nbt + 63) / 64), count), 64, 0, h->stream>>>(
+          h->jjobs.as<JacJob>(), count, dj1, dvo, nbt, nlim);
+      {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_interp_map_jobs: %s", cudaGetErrorString(e));
+      }
+      if (plain)
+        k_od_jobs<true><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
+            h->jjobs.as<JacJob>(), count, h->od.p, nlim, h->jod.p);
+      else
+        k_od_jobs<false><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
+            h->jjobs.as<JacJob>(), count, h->od.p, nlim, h->jod.p);
+      {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_od_jobs: %s", cudaGetErrorString(e));
+      }
+      // the job table and the OD buffer are reused by the next batch
+      CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+      first += count;
+    }
+    JacArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.jod = h->jod.p;
+    a.nlay = nl;
+    a.vT = js.vT;
+    a.vW = js.vW;
+    a.vM = js.vM;
+    a.nout = nlim;
+    a.v1 = blk.first;
+    a.dv = js.dvb;
+    a.tlay = dprof;
+    a.tlev = dprof + nl;
+    a.amf_down = dprof + 2 * nl + 1;
+    a.wtot = dprof + 3 * nl + 1;
+    a.dT_dTup = dprof + 4 * nl + 1;
+    a.dT_dTlo = dprof + 5 * nl + 1;
+    a.dW_dQup = dprof + 6 * nl + 1;
+    a.dW_dQlo = dprof + 7 * nl + 1;
+    a.tsfc = col->tskin;
+    a.emis = col->emis;
+    a.lin_in_tau = ctrl->lin_in_tau;
+    a.do_temp = jac->do_temp;
+    a.rad = o_rad;
+    a.dtlev = o_dtl;
+    a.dqlev = o_dql;
+    a.dtsfc = o_dts;
+    a.demis = o_dem;
+    a.ld = ld;
+    a.off = total;
+    h->launches++;
+    if (plain) k_jac<true><<<(unsigned)((nlim + 127) / 128), 128, 0, h->stream>>>(a);
+    else k_jac<false><<<(unsigned)((nlim + 127) / 128), 128, 0, h->stream>>>(a);
+    {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_jac: %s", cudaGetErrorString(e));
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    total += nlim;
+  }
+  h->first_pass_jrad = fp;
+  h->jrad = jr;
+  if (!dev) {
+    auto row = [&](double* dst, const double* src) -> cudaError_t {
+      return dst && src ? cudaMemcpyAsync(dst, src, sizeof(double) * npts, cudaMemcpyDeviceToHost, h->stream)
+                        : cudaSuccess;
+    };
+    CUDA_TRY(h, row(rad, o_rad));
+    CUDA_TRY(h, row(dr_dtskin, o_dts));
+    CUDA_TRY(h, row(dr_demis, o_dem));
+    if (dr_dtlev && o_dtl)
+      CUDA_TRY(h, cudaMemcpy2DAsync(dr_dtlev, sizeof(double) * cap, o_dtl, sizeof(double) * npts,
+                                    sizeof(double) * npts, nl + 1, cudaMemcpyDeviceToHost, h->stream));
+    if (dr_dqlev && o_dql)
+      CUDA_TRY(h, cudaMemcpy2DAsync(dr_dqlev, sizeof(double) * cap, o_dql, sizeof(double) * npts,
+                                    sizeof(double) * npts, nl + 1, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  }
+  h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
+}  // extern "C"

@@ -2365,8 +2365,10 @@ int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
     if (!rc && total + NLIM > cap) rc = fail(s, CLBLM_ERR_CAPACITY, "Jacobian spectra need more points");
     if (!rc) {
       V2B = V1B + (double)(NLIM - 1) * DVB;
-      /* OD of job (variant v, layer il) */
-#define OD(v, il, iv) ods[((size_t)((v)*nLay + (il)) * capb) + (iv)]
+      /* OD of (variant v, layer il): the job that computed it */
+      int *jidx = (int *)malloc(sizeof(int) * (size_t)nvar * nLay);
+      for (int j = 0; j < njob; ++j) jidx[jv[j] * nLay + jl[j]] = j;
+#define OD(v, il, iv) ods[((size_t)jidx[(v)*nLay + (il)] * capb) + (iv)]
       int vT = jac->do_temp ? 1 : -1, vW = jac->do_temp ? 2 : -1, vM = imol >= 0 ? nvar - 1 : -1;
       for (int64_t iv = 0; iv < NLIM; ++iv) {
         double vn = V1B + (double)iv * DVB;
@@ -2413,6 +2415,7 @@ int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
         }
       }
 #undef OD
+      free(jidx);
       total += NLIM;
     }
     free(ods);
