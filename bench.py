@@ -217,6 +217,58 @@ def sample_points(col, ctrl):
     return tot
 
 
+def jacobian_leg(cont, steps):
+    """Radiance plus the level-temperature and ln q(H2O) Jacobians of every
+    level of the 60-layer column over 600-1100 cm-1 (the 120,000 lines of the
+    500,000-line list there), on the uniform grid of noScattJacob: mixed path
+    timed, FP64 path timed once, and their radiance and Jacobian agreement."""
+    import torch
+    from clblm_gb300 import capi, synth
+    from clblm_gb300 import capi_types as T
+    lines, col, _ = synth.config1()
+    lines, col = lines.window(600.0, 1100.0), col.with_window(600.0, 1100.0)
+    prof = synth.jac_profile(col)
+    h = capi.Handle(lines, cont)
+    res = {}
+    outs = {}
+    for name, prec, k in (("mixed", T.CLBLM_PREC_MIXED, steps), ("plain", T.CLBLM_PREC_PLAIN, 1)):
+        ctrl = T.rt_ctrl(precision=prec, grid_type=1)
+        n, dv = h.jac_size(col, ctrl, prof)
+        nl = col.nlay
+        o = {key: torch.empty(shape, dtype=torch.float64, device="cuda")
+             for key, shape in (("rad", n), ("dtlev", (nl + 1, n)), ("dqlev", (nl + 1, n)), ("dtsfc", n),
+                                ("demis", n))}
+        call = lambda: h.jac_device(col, ctrl, prof, o["rad"].data_ptr(), o["dtlev"].data_ptr(),
+                                    o["dqlev"].data_ptr(), o["dtsfc"].data_ptr(), o["demis"].data_ptr(), n)
+        call()  # warm-up (workspace growth)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            call()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / k
+        res[name] = {"ms_per_step": ms, "value": n * nl / (ms * 1e-3)}
+        outs[name] = {key: v.clone() for key, v in o.items()}
+        res["points"], res["dv"], res["layers"] = n, dv, nl
+    m, p = outs["mixed"], outs["plain"]
+    res["max_rel_rad_diff_mixed_vs_plain"] = float(((m["rad"] - p["rad"]).abs() / p["rad"].abs()).max())
+    for key in ("dtlev", "dqlev"):
+        # per level: max |mixed - FP64| over the level's largest |FP64| value;
+        # levels that are not finite in FP64 (level2layer's log ratio of equal
+        # mixing ratios) or identically zero are left out
+        scale = torch.nan_to_num(p[key], nan=0.0, posinf=0.0, neginf=0.0).abs().amax(dim=1)
+        ok = torch.isfinite(p[key]).all(dim=1) & (scale > 0)
+        d = (m[key] - p[key]).abs().amax(dim=1)
+        res["max_level_%s_diff_mixed_vs_plain" % key] = float((d[ok] / scale[ok]).max()) if ok.any() else None
+        res["levels_compared_%s" % key] = int(ok.sum())
+    res["unit"] = UNIT
+    res["workload"] = ("60-layer column, 120k lines, 600-1100 cm-1: radiance + dR/dT and dR/dln q(H2O) of all "
+                       "61 levels (noScattJacob, 100000-point blocks, uniform DV)")
+    res["speedup_mixed_vs_plain"] = res["plain"]["ms_per_step"] / res["mixed"]["ms_per_step"]
+    h.close()
+    return res
+
+
 def profile_case(args):
     """A bounded case for ncu captures of one kernel: the OD of one layer of the
     60-layer column over a narrower window (the full line list stays on the
@@ -270,6 +322,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 GPU leg")
+    ap.add_argument("--no-jac", action="store_true", help="skip the Jacobian leg (600-1100 cm-1)")
     ap.add_argument("--profile-layer", type=int, default=None,
                     help="profiling case: the OD of this one layer of the column, three calls, no JSON line")
     ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
@@ -407,6 +460,9 @@ def main():
                "sample": "layers %d-%d of the column, full 500-2500 cm-1, one thread (%.1f s)"
                          % (CPU_LAYERS[0], CPU_LAYERS[-1], dt)}
 
+    jacl = None
+    if not args.no_jac:
+        jacl = jacobian_leg(cont, max(1, min(args.steps, 3)))
     roof = roofline(work, kt, args.steps, ms)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -419,7 +475,8 @@ def main():
                            "l2": "inputs larger than L2, no flush"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": e2e_ms},
-                "plain_fp64": plain, "cpu_baseline": cpu, "roofline": roof, "clocks": clk.summary(),
+                "plain_fp64": plain, "jacobians": jacl, "cpu_baseline": cpu, "roofline": roof,
+                "clocks": clk.summary(),
                 "gpu_launches": int(kt["launches"])}
         print(json.dumps(line))
     h.close()

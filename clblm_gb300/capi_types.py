@@ -249,13 +249,23 @@ class Column:
         return layer_struct(self.mol_id, self.w[il], self.wtot[il], self.pave[il], self.tave[il],
                             lay_no=il + 1)
 
+    LEVEL_FIELDS = ("p_lev", "q_h2o_lev")  # optional level profiles ([nlay+1], level 0 at the bottom)
+
     def sub(self, layers):
         idx = np.asarray(layers)
-        return Column(self.mol_id, self.pave[idx], self.tave[idx], self.tbot[idx], self.ttop[idx],
-                      self.w[idx], self.wtot[idx], self.wtot_down[idx], self.v1, self.v2,
-                      self.tskin, self.emis)
+        c = Column(self.mol_id, self.pave[idx], self.tave[idx], self.tbot[idx], self.ttop[idx],
+                   self.w[idx], self.wtot[idx], self.wtot_down[idx], self.v1, self.v2,
+                   self.tskin, self.emis)
+        if len(idx) and np.all(np.diff(idx) == 1):  # contiguous layers keep their levels
+            for f in self.LEVEL_FIELDS:
+                if hasattr(self, f):
+                    setattr(c, f, getattr(self, f)[idx[0]:idx[-1] + 2])
+        return c
 
     def with_window(self, v1, v2):
         c = Column(self.mol_id, self.pave, self.tave, self.tbot, self.ttop, self.w, self.wtot,
                    self.wtot_down, v1, v2, self.tskin, self.emis)
+        for f in self.LEVEL_FIELDS:
+            if hasattr(self, f):
+                setattr(c, f, getattr(self, f))
         return c

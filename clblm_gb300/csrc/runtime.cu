@@ -1662,25 +1662,55 @@ int jac_plan_block(clblm_handle* h, const clblm_rt_ctrl_t* ctrl, const clblm_jac
     *jr = jafter;
     *fp = false;
   }
+  // the block length is the first layer's (clblm_noScattJac.f90:227); a layer
+  // on exactly DVout keeps its panel length (clblm_ODLAY.f90:562-580), of
+  // which the first nlim points are read
   *nlim = (*hps)[0].n_out;
+  // (a layer on exactly DVout can end one or two points short: the reference
+  // reads past its end; here the points take interpSpectrum's linear
+  // extension, which the OD gather applies)
   for (int j = 1; j < njob; ++j)
-    if ((*hps)[j].n_out != *nlim) return set_err(h, CLBLM_ERR_GRID, "Jacobian ODs of one block differ in length");
+    if ((*hps)[j].n_out < *nlim - 2 || (*hps)[j].n_out < 2)
+      return set_err(h, CLBLM_ERR_GRID, "a Jacobian OD of the block is shorter than the block");
   return CLBLM_OK;
 }
 
-// the blocks of noScattJacob (clblm_noScattJac.f90:206-232): V1B, V2B
-void jac_blocks(double v1, double v2, double dvb, std::vector<std::pair<double, double>>* blocks) {
+// The blocks of noScattJacob (clblm_noScattJac.f90:206-232): V1B, V2B and
+// the block length, which is the first layer's OD length (:227-229); the next
+// block starts one DVout after the block's last point.
+struct JacBlock {
+  double v1, v2;
+  int64_t n;
+};
+
+int jac_block_list(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const JacSetup& js,
+                   const std::vector<double>& dvn, const std::vector<double>& dvf, std::vector<JacBlock>* blocks) {
   const int blockSize = 100000;
-  double V1B = v1, V2B = V1B - dvb;
-  while (V2B < v2) {
+  const double dvb = js.dvb;
+  double V1B = col->v1, V2B = V1B - dvb;
+  clblm_od_ctrl_t octl = ctrl->od;
+  octl.jac_mol = 0;
+  while (V2B < col->v2) {
     V1B = V2B + dvb;
     V2B = V1B + (double)(blockSize - 2) * dvb;
-    if (V2B > v2) V2B = v2;
-    blocks->push_back({V1B, V2B});
-    // the next block starts one DVB after the last point ODLAY returns
-    int64_t n = (int64_t)std::ceil((V2B - V1B) / dvb + 1.);
-    V2B = V1B + (double)(n - 1) * dvb;
+    if (V2B > col->v2) V2B = col->v2;
+    clblm_grid_t g;
+    g.v1 = V1B;
+    g.v2 = V2B;
+    g.dv_normal = dvn[0];
+    g.dv_narrow = dvf[0];
+    g.dv_out = dvb;
+    g.sample = ctrl->sample;
+    g.alfal0 = ctrl->alfal0;
+    HostPlan hp;
+    int jafter;
+    int rc = plan_layer(h, &js.lays[0], &g, &octl, h->jrad, h->first_pass_jrad, &hp, &jafter);
+    if (rc) return rc;
+    blocks->push_back({V1B, V2B, hp.n_out});
+    V2B = V1B + (double)(hp.n_out - 1) * dvb;
+    if (blocks->size() > 100000) return set_err(h, CLBLM_ERR_GRID, "Jacobian blocks");
   }
+  return CLBLM_OK;
 }
 
 }  // namespace
@@ -1694,10 +1724,11 @@ int clblm_gpu_jac_size(clblm_handle_t* h, const clblm_column_t* col, const clblm
   std::vector<double> dvn, dvf;
   int rc = jac_setup(h, col, ctrl, jac, &js, &dvn, &dvf);
   if (rc) return rc;
-  std::vector<std::pair<double, double>> blocks;
-  jac_blocks(col->v1, col->v2, js.dvb, &blocks);
+  std::vector<JacBlock> blocks;
+  rc = jac_block_list(h, col, ctrl, js, dvn, dvf, &blocks);
+  if (rc) return rc;
   int64_t tot = 0;
-  for (auto& b : blocks) tot += (int64_t)std::ceil((b.second - b.first) / js.dvb + 1.);
+  for (auto& b : blocks) tot += b.n;
   if (npts) *npts = tot;
   if (dv) *dv = js.dvb;
   return CLBLM_OK;
@@ -1715,10 +1746,11 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
   const int nl = col->nlay;
   const bool plain = ctrl->od.precision == CLBLM_PREC_PLAIN;
   const size_t real = plain ? 8 : 4;
-  std::vector<std::pair<double, double>> blocks;
-  jac_blocks(col->v1, col->v2, js.dvb, &blocks);
+  std::vector<JacBlock> blocks;
+  rc = jac_block_list(h, col, ctrl, js, dvn, dvf, &blocks);
+  if (rc) return rc;
   int64_t npts = 0;
-  for (auto& b : blocks) npts += (int64_t)std::ceil((b.second - b.first) / js.dvb + 1.);
+  for (auto& b : blocks) npts += b.n;
   if (cap < npts) return set_err(h, CLBLM_ERR_CAPACITY, "Jacobian spectra need %lld points", (long long)npts);
   h->reset_call();
   // layer and level profiles
@@ -1760,8 +1792,9 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
   for (auto& blk : blocks) {
     std::vector<HostPlan> hps;
     int64_t nlim;
-    rc = jac_plan_block(h, ctrl, jac, js, dvn, dvf, blk.first, blk.second, &jr, &fp, &hps, &nlim);
+    rc = jac_plan_block(h, ctrl, jac, js, dvn, dvf, blk.v1, blk.v2, &jr, &fp, &hps, &nlim);
     if (rc) return rc;
+    if (nlim != blk.n) return set_err(h, CLBLM_ERR_GRID, "Jacobian block length changed");
     const int njob = (int)hps.size();
     // the block's ODs on the uniform grid, [variant][layer][point]
     CUDA_TRY(h, h->jod.ensure(real * (size_t)js.nvar * nl * nlim));
@@ -1772,14 +1805,14 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     std::vector<double> vo;
     {
       const double TOL = 1.e-8;
-      const double V2out = blk.first + (double)(nlim - 1) * js.dvb;
-      double Vo = blk.first;
+      const double V2out = blk.v1 + (double)(nlim - 1) * js.dvb;
+      double Vo = blk.v1;
       while (Vo < V2out + TOL) {
-        int64_t J1 = (int64_t)((Vo - blk.first) / js.dvb + 1.001);
+        int64_t J1 = (int64_t)((Vo - blk.v1) / js.dvb + 1.001);
         int64_t J2 = std::min<int64_t>(nlim, J1 + 2400 - 1);
         j1.push_back(J1);
         vo.push_back(Vo);
-        Vo = blk.first + (double)J2 * js.dvb;
+        Vo = blk.v1 + (double)J2 * js.dvb;
         if (j1.size() > (size_t)(nlim / 2400 + 8)) return set_err(h, CLBLM_ERR_GRID, "interpolation blocks");
       }
     }
@@ -1812,7 +1845,7 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
         const int j = first + k;
         const LayerPlan& P = hps[j].P;
         JacJob& jb = jobs[k];
-        jb.spec = interp_spec(P.v1, P.dv, P.nsamp, blk.first, js.dvb, nlim);
+        jb.spec = interp_spec(P.v1, P.dv, P.nsamp, blk.v1, js.dvb, nlim);
         jb.map = h->jmap.as<int2>() + (size_t)j * nlim;
         jb.spec.map = jb.map;
         jb.od_off = P.od_off;
@@ -1850,7 +1883,7 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     a.vW = js.vW;
     a.vM = js.vM;
     a.nout = nlim;
-    a.v1 = blk.first;
+    a.v1 = blk.v1;
     a.dv = js.dvb;
     a.tlay = dprof;
     a.tlev = dprof + nl;

@@ -2360,8 +2360,20 @@ int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
     }
     for (int j = 0; j < njob && !rc; ++j) rc = rcs[j];
     int64_t NLIM = nss[0];
-    for (int j = 0; j < njob && !rc; ++j)
-      if (nss[j] != NLIM) rc = fail(s, CLBLM_ERR_GRID, "Jacobian ODs of one block differ in length");
+    /* the block length is the first layer's (clblm_noScattJac.f90:227); a
+     * layer on exactly DVout keeps its panel length (clblm_ODLAY.f90:562-580),
+     * of which the first NLIM points are read */
+    for (int j = 0; j < njob && !rc; ++j) {
+      if (nss[j] < NLIM - 2 || nss[j] < 2) {
+        rc = fail(s, CLBLM_ERR_GRID, "a Jacobian OD of the block is shorter than the block");
+      } else if (nss[j] < NLIM) {
+        /* the reference reads past the end of this layer's OD here; the
+         * missing points take interpSpectrum's linear extension */
+        double *od = ods + (size_t)j * capb;
+        double ext = 2.0 * od[nss[j] - 1] - od[nss[j] - 2];
+        for (int64_t k = nss[j]; k < NLIM; ++k) od[k] = ext;
+      }
+    }
     if (!rc && total + NLIM > cap) rc = fail(s, CLBLM_ERR_CAPACITY, "Jacobian spectra need more points");
     if (!rc) {
       V2B = V1B + (double)(NLIM - 1) * DVB;
