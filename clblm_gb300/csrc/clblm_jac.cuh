@@ -19,6 +19,7 @@ struct JacJob {
   int64_t od_off;    // OD of the layer in the pipeline's OD buffer (Real)
   int64_t n_in;      // points of the layer OD
   int slot;
+  int build_map;     // 1: this job builds the map (other jobs of the layer read it)
 };
 
 struct JacArgs {

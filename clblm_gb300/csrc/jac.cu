@@ -30,7 +30,7 @@ __global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob, con
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= njob || b >= nblk) return;
   const InterpSpec& s = jobs[j].spec;
-  if (s.kind == 0 || s.itype >= 0) return;
+  if (!jobs[j].build_map) return;
   int2* map = jobs[j].map;
   const double Vo = blk_vo[b];
   int64_t iIn = (int64_t)__dadd_rn(__ddiv_rn(__dadd_rn(Vo, -s.v1), s.dvin), 1.00001);
@@ -51,11 +51,11 @@ __global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob, con
 
 // interpSpectrum's linear extension by two points past either end
 template <typename Real>
-__device__ __forceinline__ double od_ext(const Real* x, int64_t n, int64_t i) {
-  if (i >= 1 && i <= n) return (double)x[i - 1];
-  if (i == 0 || i == -1) return 2.0 * (double)x[0] - (double)x[1];
-  if (i == n + 1 || i == n + 2) return 2.0 * (double)x[n - 1] - (double)x[n - 2];
-  return 0.;
+__device__ __forceinline__ Real od_ext_t(const Real* x, int64_t n, int64_t i) {
+  if (i >= 1 && i <= n) return x[i - 1];
+  if (i == 0 || i == -1) return (Real)2 * x[0] - x[1];
+  if (i == n + 1 || i == n + 2) return (Real)2 * x[n - 1] - x[n - 2];
+  return (Real)0;
 }
 
 template <bool Plain>
@@ -66,12 +66,13 @@ __global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, int6
   if (j >= njob || I > nout) return;
   const JacJob& jb = jobs[j];
   const Real* x = reinterpret_cast<const Real*>(od_all) + jb.od_off;
-  const Stencil<double> st = interp_stencil<double>(jb.spec, I);
-  double v = 0.;
-  if (st.n == 1) v = od_ext(x, jb.n_in, st.i[0]);
+  const Stencil<Real> st = interp_stencil<Real>(jb.spec, I);  // FP32 weights in the mixed path
+  Real v = 0;
+  if (st.n == 1) v = od_ext_t(x, jb.n_in, st.i[0]);
   else
-    for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext(x, jb.n_in, st.i[k]);
-  reinterpret_cast<Real*>(out)[(int64_t)jb.slot * nout + (I - 1)] = (Real)v;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext_t(x, jb.n_in, st.i[k]);
+  reinterpret_cast<Real*>(out)[(int64_t)jb.slot * nout + (I - 1)] = v;
 }
 
 template __global__ void k_od_jobs<false>(const JacJob*, int, const void*, int64_t, void*);

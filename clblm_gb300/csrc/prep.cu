@@ -459,14 +459,27 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
   if (!P.contnm) return;
   if (!((P.v2 > -20.0) && (P.v1 < 20000.) && ((P.xself > 0.) || (P.xfrgn > 0.)))) return;
   int ncoeffin = cont.n;
+  if (I > (int)((P.v2abs - P.v1abs) / P.dvabs + 1)) return;  // beyond NPTABS: nothing to add
   const double dvc = (cont.v1 + cont.dv) - cont.v1;
-  // i1, i2 bracket [V1ABS - 2 dvc, V2ABS + 2 dvc] (mt_ckd_h2o_module.f90:106-117)
-  int i = 1;
-  while (i <= ncoeffin && cont.v1 + (double)(i - 1) * cont.dv <= (P.v1abs - 2 * dvc)) i++;
+  // i1, i2 bracket [V1ABS - 2 dvc, V2ABS + 2 dvc] (mt_ckd_h2o_module.f90:106-117):
+  // the reference's forward scans, as binary searches over the monotone grid
+  auto wvn = [&](int k) { return cont.v1 + (double)(k - 1) * cont.dv; };
+  int lo = 1, hi = ncoeffin + 1;  // first i with wvn(i) > V1ABS - 2 dvc
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (wvn(mid) <= (P.v1abs - 2 * dvc)) lo = mid + 1;
+    else hi = mid;
+  }
+  int i = lo;
   int i1 = i - 1;
   if (i1 == 0) i1 = 1;
-  while (i <= ncoeffin && cont.v1 + (double)(i - 1) * cont.dv < (P.v2abs + 2 * dvc)) i++;
-  int i2 = i;
+  hi = ncoeffin + 1;  // first i (from there) with wvn(i) >= V2ABS + 2 dvc
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (wvn(mid) < (P.v2abs + 2 * dvc)) lo = mid + 1;
+    else hi = mid;
+  }
+  int i2 = lo;
   double V1A = cont.v1 + (double)(i1 - 1) * cont.dv;
   double V2A = cont.v1 + (double)(i2 - 1) * cont.dv;
   int nptabs = (int)((P.v2abs - P.v1abs) / P.dvabs + 1);

@@ -1846,8 +1846,18 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
         const LayerPlan& P = hps[j].P;
         JacJob& jb = jobs[k];
         jb.spec = interp_spec(P.v1, P.dv, P.nsamp, blk.v1, js.dvb, nlim);
-        jb.map = h->jmap.as<int2>() + (size_t)j * nlim;
+        // the variants of a layer share its grid: one map per layer (built
+        // with the layer's first job), the others only read it
+        const int il = js.job_lay[j];
+        int owner = j;
+        for (int q = 0; q < j; ++q)
+          if (js.job_lay[q] == il && hps[q].P.dv == P.dv && hps[q].P.nsamp == P.nsamp) {
+            owner = q;
+            break;
+          }
+        jb.map = h->jmap.as<int2>() + (size_t)owner * nlim;
         jb.spec.map = jb.map;
+        jb.build_map = (owner == j && jb.spec.kind != 0 && jb.spec.itype < 0) ? 1 : 0;
         jb.od_off = P.od_off;
         jb.n_in = P.nsamp;
         jb.slot = js.job_var[j] * nl + js.job_lay[j];
