@@ -23,6 +23,7 @@ UNITS = {
     "panel.cu": [],
     "rt.cu": [],
     "jac.cu": [],
+    "tape3.cpp": [],
     "runtime.cu": [],
 }
 

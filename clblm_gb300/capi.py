@@ -22,7 +22,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_gpu_stream",
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
-           "clblm_gpu_interp_spectrum_noalloc")
+           "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -67,6 +67,8 @@ def lib():
                                          P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_jac.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + \
             [C.c_void_p] * 5 + [C.c_int64, C.c_int32]
+        L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
+                                       P(C.c_int64), C.c_char_p, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
                                                         C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
         _lib = L
@@ -203,6 +205,24 @@ Handle.jac_size, Handle.jac, Handle.jac_device = _jac_methods()
 def noScattJacob(handle, col, ctrl, jac):
     """Radiance and level Jacobians of a nadir column (clblm_noScattJac.f90:20)."""
     return handle.jac(col, ctrl, jac)
+
+
+def read_tape3(path, v1=-1e30, v2=1e30):
+    """Line list of an LNFL TAPE3 file (whole 250-line blocks meeting
+    [v1, v2]); host code, no device needed."""
+    err = C.create_string_buffer(512)
+    n = C.c_int64()
+    p = str(path).encode()
+    rc = lib().clblm_tape3_read(p, v1, v2, None, 0, C.byref(n), err, 512)
+    if rc:
+        raise ClblmError(rc, err.value.decode())
+    arrays = {name: np.empty(n.value, dtype=dt) for name, dt in T.Lines.FIELDS}
+    lines = T.Lines(**arrays)
+    ls = lines.struct()
+    rc = lib().clblm_tape3_read(p, v1, v2, C.byref(ls), n.value, C.byref(n), err, 512)
+    if rc:
+        raise ClblmError(rc, err.value.decode())
+    return lines
 
 
 def setDV(col, sample=4.0, alfal0=0.04, alfal0_fine=0.005, grid_type=0, dv_user=-1.0):

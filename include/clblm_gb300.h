@@ -285,6 +285,19 @@ int clblm_gpu_jac(clblm_handle_t *h, const clblm_column_t *col,
                   double *dr_dtskin, double *dr_demis, int64_t cap,
                   int32_t flags);
 
+/* Lines of an LNFL line file (TAPE3) as read by RDLIN (clblm_ODLAY.f90:
+ * 2645-2700) through CLBLM_LineData (clblm_LineData.f90:52-161): Fortran
+ * unformatted records (4-byte length markers), the file header, the optional
+ * negative-EPP record, then panel headers and 250-line blocks.  Whole blocks
+ * whose [VMIN, VMAX] misses [v1, v2] are skipped, so the line list keeps the
+ * file's 250-line records.  With lines == NULL or lines->vnu == NULL only the
+ * count is returned in *n_lines; otherwise the caller's arrays (capacity cap)
+ * are filled and lines->n is set.  Host code: needs no device.  On failure a
+ * message is written to errbuf (errlen bytes). */
+int clblm_tape3_read(const char *path, double v1, double v2,
+                     clblm_lines_t *lines, int64_t cap, int64_t *n_lines,
+                     char *errbuf, int32_t errlen);
+
 /* ---- grid interpolation that allocates nothing ----------------------------
  *
  * No counterpart in the reference.  Some callers cannot call cudaMalloc: a

@@ -71,3 +71,22 @@ def test_reference_mtckd_table(gpu_lib, oracle_mod, mtckd, precision, tol, layer
     od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=mtckd, contnm_off=0, precision=precision)
     rel = np.max(np.abs(od - ref) / np.abs(ref))
     assert rel <= tol, rel
+
+
+def test_od_from_tape3_file_is_identical(gpu_lib, tmp_path):
+    """Lines written as an LNFL TAPE3 file and read back by the library give
+    the same OD bit for bit."""
+    from clblm_gb300 import tape3
+    lines, col = _layer_case(6000, 600.0, 640.0, seed=21)
+    p = tmp_path / "TAPE3"
+    tape3.write_tape3(p, lines)
+    back = gpu_lib.read_tape3(p)
+    dn, df, _ = gpu_lib.setDV(col)
+    g = T.grid_struct(col.v1, col.v2, dn[0], df[0])
+    ctrl = T.od_ctrl(precision=T.CLBLM_PREC_MIXED, contnm_off=1)
+    h1, h2 = gpu_lib.Handle(lines), gpu_lib.Handle(back)
+    a, _ = h1.odlay(col.layer(0), g, ctrl)
+    b, _ = h2.odlay(col.layer(0), g, ctrl)
+    h1.close()
+    h2.close()
+    assert np.array_equal(a, b)
