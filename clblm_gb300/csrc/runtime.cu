@@ -87,6 +87,10 @@ struct clblm_handle {
   int64_t launches = 0;  // kernels launched by the current call
   // per-call sums of the line-shape kernels' work and device time
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // f4 start/stop, panel start/stop
+  // the far-wing chain runs on a second stream, forked from and joined back
+  // into `stream` within each OD batch
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int64_t acc_fnq = 0, acc_f4q = 0;
   double acc_ms_panel = 0., acc_ms_f4 = 0.;
   void reset_call() {
@@ -679,11 +683,14 @@ int64_t pad256(int64_t x) { return (x + 255) & ~int64_t(255); }
 // plans[first..]; OD of layer k lands at od + P.od_off (Real).
 int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t lstride,
                  int64_t f4stride, int64_t pstride) {
-  cudaStream_t st = h->stream;
   const LayerPlan* dplans = h->plans.as<const LayerPlan>();
   LineIn li = line_in(h);
   dim3 blk(256);
-  // continuum
+  // the continuum and the far-wing chain on the second stream, the line
+  // chain on the handle's stream; k_panel waits for both
+  CUDA_TRY(h, cudaEventRecord(h->fork_ev, h->stream));
+  CUDA_TRY(h, cudaStreamWaitEvent(h->stream2, h->fork_ev, 0));
+  cudaStream_t st = h->stream2;
   h->launches++;
   k_continuum<<<dim3((kNABSRB + 255) / 256, count), blk, 0, st>>>(dplans, first, h->cont, h->absrb.as<double>());
   // far wings
@@ -747,6 +754,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     else k_f4_conv<false><<<grid, kF4Tile, 0, st>>>(fa);
     CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   }
+  CUDA_TRY(h, cudaEventRecord(h->join_ev, st));
+  st = h->stream;
   // line centres
   h->launches++;
   k_line_prep<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
@@ -803,6 +812,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     k_r4_radfac<<<dim3((maxb + 63) / 64, count), 64, 0, st>>>(dplans, first, h->bv1.as<double>(), h->bn.as<int>(),
                                                             h->bfac.as<double>());
   }
+  CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
   size_t smem = panel_smem_bytes(plain);
   if (plain) {
     CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1027,6 +1037,13 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
       return CLBLM_ERR_CUDA;
     }
   }
+  if (cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    g_create_err = "cannot create the second stream";
+    clblm_gpu_destroy(h);
+    return CLBLM_ERR_CUDA;
+  }
   rc = upload_tables(h);
   if (!rc) rc = load_lines(h, lines);
   if (!rc && cont) {
@@ -1084,6 +1101,12 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   for (auto& b : h->imap) b.release();
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
+  if (h->stream2) {
+    cudaStreamSynchronize(h->stream2);
+    cudaStreamDestroy(h->stream2);
+  }
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CLBLM_OK;
