@@ -38,20 +38,27 @@ struct PanelArgs {
 };
 
 // far-wing pseudo-line prepared for the convolution (CNVF4Q per-line set-up),
-// FP32 form of the mixed path: 48 bytes, staged in shared memory in chunks
-struct F4Rec {
+// FP32 form of the mixed path: 80 bytes, staged in shared memory in chunks.
+// Every coefficient is stored twice, as the (x, y) operand pair of the
+// packed FP32x2 arithmetic that evaluates two points at once.
+struct __align__(16) F4Rec {
   int jmin, jmax;   // global R4 points J = m+1 in [jmin, jmax]
-  float mcf, x0;    // grid point m nearest the line centre (an integer, exact
-                    // in FP32) and mc*DVR4 - XNUI, |x0| <= DVR4/2
-  float sil, al2, ralv2, sa3;
-  float sb3, fb0, fb2, pad;  // pedestal fb0 - x^2 fb2 (CO2: 2 F4BND, F4BND/BOUND^2)
+  float2 nmc;       // -mc: the grid point m nearest the line centre (exact in FP32)
+  float2 x0;        // mc*DVR4 - XNUI, |x0| <= DVR4/2
+  float2 ralv2;     // 1 / ALFV^2
+  float2 nfb0, fb2; // minus the pedestal: -fb0 + x^2 fb2 (CO2: fb0 = 2 F4BND,
+                    // fb2 = F4BND/BOUND^2; else F4BND, 0)
+  float2 sa3, sb3;  // SIV*A3, SIV*B3
+  float2 al2, sil;  // ALFL^2, SIL
 };
+static_assert(sizeof(F4Rec) == 80, "far-wing record layout");
 // FP64 form (the FP64 path), 64 bytes
 struct F4RecD {
   int jmin, jmax, co2, pad;
   double xnui, sil, siv, fbnd, al2, alv2;
 };
-constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv
+constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv (two per thread)
+constexpr int kF4Threads = kF4Tile / 2;
 constexpr int kF4Chunk = 256;    // records per shared-memory stage
 
 struct F4Args {

@@ -8,8 +8,9 @@
 //                    the R3->R2->R1 4-point interpolation and the radiation
 //                    term (panelOut, clblm_ODLAY.f90:2289-2493).
 //   k_f4_conv<Plain> far-wing function 4 on the DVR4 grid (CNVF4Q,
-//                    clblm_ODLAY_LineF4.f90:187-494): one thread per point,
-//                    records streamed through shared memory by bulk copies.
+//                    clblm_ODLAY_LineF4.f90:187-494): two points per thread
+//                    (packed FP32x2 in the mixed path), records streamed
+//                    through shared memory by bulk copies.
 //   k_rt_layer<...>  one layer of the upward merge of mode2_lookDn_mergeUp
 //                    (layerMerge_mode2, clblm_noScattRT.f90:1704-1794) with
 //                    layerEmis (clblm_EMLAY.f90:104-178) and the
@@ -695,7 +696,7 @@ template __global__ void k_panel<true>(PanelArgs);
 // sums per chunk (alternate records) and adds each chunk's total into a Kahan
 // sum.
 template <bool Plain>
-__global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
+__global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
   __shared__ __align__(128) Rec stage[2][kF4Chunk];
@@ -706,8 +707,9 @@ __global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
   const LayerPlan& P = a.plans[layer + a.layer0];
   const int64_t m0 = (int64_t)blockIdx.x * kF4Tile;
   if (m0 >= P.nptr4 + 2) return;  // whole CTA: no barrier has been set up yet
-  const int64_t m = m0 + threadIdx.x;
-  const int J = (int)m + 1;
+  // the thread's two points: m0 + t and m0 + t + kF4Threads
+  const int64_t mA = m0 + threadIdx.x, mB = mA + kF4Threads;
+  const int JA = (int)mA + 1, JB = (int)mB + 1;
   Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
   const int64_t n = a.nrec[layer + a.layer0];
   const int64_t nm = a.nmirror[layer + a.layer0];
@@ -750,16 +752,46 @@ __global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
   };
   if (threadIdx.x == 0 && nchunk > 0) issue(0);
 
-  const bool live = m < P.nptr4;
+  const bool liveA = mA < P.nptr4, liveB = mB < P.nptr4;
+  const float2 Jm1 = make_float2((float)(JA - 1), (float)(JB - 1));  // exact: J < 2^24
   const float dvr4f = (float)P.dvr4;
-  const float Jm1 = (float)(J - 1);  // exact: J < 2^24
+  const float2 dvr4 = make_float2(dvr4f, dvr4f);
   const double ZSQBND = 64. * 64.;
   const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
   const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
   const double bnd2 = P.bound4 * P.bound4;
-  double accd = 0.;  // FP64 path
-  KahanF acck;       // mixed path: chunk totals
+  double accA = 0., accB = 0.;  // FP64 path
+  KahanF kA, kB;                // mixed path: chunk totals
   bool failed = false;
+  // FP64 term of record d at point m, in the reference's operations
+  auto term_d = [&](const F4RecD& d, int64_t m) -> double {
+    double XM = (double)m * P.dvr4 - d.xnui;
+    double XMSQ = XM * XM;
+    double ZVSQ = XMSQ / d.alv2;
+    double fb = d.co2 ? (2. - XMSQ / bnd2) * d.fbnd : d.fbnd;
+    if (ZVSQ <= ZSQBND) return (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
+    return d.sil / (d.al2 + XMSQ) - fb;
+  };
+  // FP32 terms of record r at both points (packed FP32x2), before the range test
+  auto shape_f = [&](const F4Rec& r) -> float2 {
+    const float2 xm = __ffma2_rn(__fadd2_rn(Jm1, r.nmc), dvr4, r.x0);
+    const float2 xmsq = __fmul2_rn(xm, xm);
+    const float2 zvsq = __fmul2_rn(xmsq, r.ralv2);
+    const float2 nfb = __ffma2_rn(xmsq, r.fb2, r.nfb0);
+    const float2 core = __ffma2_rn(zvsq, r.sb3, r.sa3);
+    const float2 den = __fadd2_rn(xmsq, r.al2);
+    float2 f = make_float2(zvsq.x <= 4096.f ? core.x : __fdividef(r.sil.x, den.x),
+                           zvsq.y <= 4096.f ? core.y : __fdividef(r.sil.y, den.y));
+    return __fadd2_rn(f, nfb);
+  };
+  auto term_f = [&](const F4Rec& r) -> float2 {
+    float2 f = shape_f(r);
+    f.x = (JA >= r.jmin && JA <= r.jmax) ? f.x : 0.f;
+    f.y = (JB >= r.jmin && JB <= r.jmax) ? f.y : 0.f;
+    return f;
+  };
+  const int tJlo = (int)m0 + 1;
+  const int tJhi = (int)(m0 + kF4Tile < P.nptr4 ? m0 + kF4Tile : P.nptr4);
   for (int64_t c = 0; c < nchunk; ++c) {
     // the other stage was released by the barrier that closed chunk c-1
     if (threadIdx.x == 0 && c + 1 < nchunk) issue(c + 1);
@@ -776,40 +808,38 @@ __global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
     const Rec* S = stage[c & 1];
     const int64_t left = hi - (lo + c * kF4Chunk);
     const int cnt = (int)(left < kF4Chunk ? left : kF4Chunk);
-    if (live) {
+    if (liveA) {
       if constexpr (Plain) {
         for (int k = 0; k < cnt; ++k) {
           const F4RecD& d = S[k];
-          if (J < d.jmin || J > d.jmax) continue;
-          double XM = (double)m * P.dvr4 - d.xnui;
-          double XMSQ = XM * XM;
-          double ZVSQ = XMSQ / d.alv2;
-          double fb = d.co2 ? (2. - XMSQ / bnd2) * d.fbnd : d.fbnd;
-          double F4FN;
-          if (ZVSQ <= ZSQBND) F4FN = (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
-          else F4FN = d.sil / (d.al2 + XMSQ) - fb;
-          accd += F4FN;
+          if (JA >= d.jmin && JA <= d.jmax) accA += term_d(d, mA);
+          if (liveB && JB >= d.jmin && JB <= d.jmax) accB += term_d(d, mB);
         }
-      } else {
-        float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-        auto term = [&](const F4Rec& r) -> float {
-          float xm = fmaf(Jm1 - r.mcf, dvr4f, r.x0);
-          float xmsq = xm * xm;
-          float zvsq = xmsq * r.ralv2;
-          float fb = fmaf(-xmsq, r.fb2, r.fb0);
-          float f = zvsq <= 4096.f ? fmaf(zvsq, r.sb3, r.sa3) : __fdividef(r.sil, r.al2 + xmsq);
-          f -= fb;
-          return (J >= r.jmin && J <= r.jmax) ? f : 0.f;
-        };
+      }
+    }
+    if constexpr (!Plain) {
+      // a chunk whose records all span the tile's live points needs no range test
+      bool cov = true;
+      for (int k = threadIdx.x; k < cnt; k += kF4Threads) cov &= (S[k].jmin <= tJlo && S[k].jmax >= tJhi);
+      const bool full = __syncthreads_and(cov);
+      if (liveA) {
+        float2 p0 = make_float2(0.f, 0.f), p1 = p0;
         int k = 0;
-        for (; k + 4 <= cnt; k += 4) {
-          p0 += term(S[k]);
-          p1 += term(S[k + 1]);
-          p2 += term(S[k + 2]);
-          p3 += term(S[k + 3]);
+        if (full) {
+          for (; k + 2 <= cnt; k += 2) {
+            p0 = __fadd2_rn(p0, shape_f(S[k]));
+            p1 = __fadd2_rn(p1, shape_f(S[k + 1]));
+          }
+        } else {
+          for (; k + 2 <= cnt; k += 2) {
+            p0 = __fadd2_rn(p0, term_f(S[k]));
+            p1 = __fadd2_rn(p1, term_f(S[k + 1]));
+          }
         }
-        for (; k < cnt; ++k) p0 += term(S[k]);
-        acck.add((p0 + p1) + (p2 + p3));
+        if (k < cnt) p0 = __fadd2_rn(p0, term_f(S[k]));
+        const float2 t = __fadd2_rn(p0, p1);
+        kA.add(t.x);
+        kB.add(t.y);
       }
     }
     __syncthreads();  // stage c&1 is free for chunk c+2
@@ -818,32 +848,36 @@ __global__ void __launch_bounds__(kF4Tile) k_f4_conv(F4Args a) {
     mbar_inval(&bar[0]);
     mbar_inval(&bar[1]);
   }
-  if (failed || m >= P.nptr4 + 2) return;
-  if (!live) {  // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94)
-    R4[m] = (Real)0;
-    return;
-  }
-  // mirror records of lines below 25 cm-1 follow the direct ones
-  for (int64_t i = n; i < n + nm; ++i) {
-    const Rec& r = recs[i];
-    if (J < r.jmin || J > r.jmax) continue;
+  if (failed) return;
+  // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94); mirror records of
+  // lines below 25 cm-1 follow the direct ones
+  const int64_t ms[2] = {mA, mB};
+  for (int q = 0; q < 2; ++q) {
+    const int64_t m = ms[q];
+    if (m >= P.nptr4 + 2) continue;
+    if (m >= P.nptr4) {
+      R4[m] = (Real)0;
+      continue;
+    }
+    const int J = (int)m + 1;
     if constexpr (Plain) {
-      double XM = (double)m * P.dvr4 - r.xnui;
-      double XMSQ = XM * XM;
-      double ZVSQ = XMSQ / r.alv2;
-      double fb = r.co2 ? (2. - XMSQ / bnd2) * r.fbnd : r.fbnd;
-      accd += (ZVSQ <= ZSQBND) ? (r.siv * A3 + ZVSQ * (r.siv * B3)) - fb : r.sil / (r.al2 + XMSQ) - fb;
+      double acc = q == 0 ? accA : accB;
+      for (int64_t i = n; i < n + nm; ++i) {
+        const F4RecD& d = recs[i];
+        if (J >= d.jmin && J <= d.jmax) acc += term_d(d, m);
+      }
+      R4[m] = acc;
     } else {
-      float xm = fmaf(Jm1 - r.mcf, dvr4f, r.x0);
-      float xmsq = xm * xm;
-      float zvsq = xmsq * r.ralv2;
-      float fb = fmaf(-xmsq, r.fb2, r.fb0);
-      float f = zvsq <= 4096.f ? fmaf(zvsq, r.sb3, r.sa3) : __fdividef(r.sil, r.al2 + xmsq);
-      acck.add(f - fb);
+      KahanF& acc = q == 0 ? kA : kB;
+      for (int64_t i = n; i < n + nm; ++i) {
+        const F4Rec& r = recs[i];
+        if (J < r.jmin || J > r.jmax) continue;
+        const float2 t = term_f(r);  // lane x is point A, lane y point B
+        acc.add(q == 0 ? t.x : t.y);
+      }
+      R4[m] = acc.value();
     }
   }
-  if constexpr (Plain) R4[m] = accd;
-  else R4[m] = acck.value();
 }
 
 template __global__ void k_f4_conv<false>(F4Args);

@@ -763,6 +763,7 @@ __global__ void __launch_bounds__(kWalkThreads)
               int64_t* __restrict__ ngroups) {
   __shared__ long long sv[kWalkMax], sl[kWalkMax];
   __shared__ short nxt[kWalkMax];          // group end following a group that ends at b
+  __shared__ short nxt2[kWalkMax], nxt3[kWalkMax], nxt4[kWalkMax];  // nxt applied 2, 3, 4 times
   __shared__ short ends[kWalkMax];         // group ends of the call, in order
   __shared__ unsigned char sf[kWalkMax];
   __shared__ int warp_tot[kWalkThreads / 32 + 1];
@@ -836,6 +837,15 @@ __global__ void __launch_bounds__(kWalkThreads)
         nxt[b] = (short)(j - 1 < m - 1 ? j - 1 : m - 1);
       }
       __syncthreads();
+      // powers of the map, so that the chain below advances four groups per
+      // step with independent loads (nxt(m-1) = m-1 keeps chains at the end)
+      for (int b = tid; b < m; b += kWalkThreads) nxt2[b] = nxt[nxt[b]];
+      __syncthreads();
+      for (int b = tid; b < m; b += kWalkThreads) {
+        nxt3[b] = nxt[nxt2[b]];
+        nxt4[b] = nxt2[nxt2[b]];
+      }
+      __syncthreads();
       if (tid == 0) {
         // the first group starts at the first unshrunk line, VLMT = VNU(ILO) + DVR4/2
         const long long lim = sl[0];
@@ -845,8 +855,15 @@ __global__ void __launch_bounds__(kWalkThreads)
         int k = 0;
         ends[k++] = (short)e;
         while (e < m - 1) {
-          e = nxt[e];
-          ends[k++] = (short)e;
+          const int a1 = nxt[e], a2 = nxt2[e], a3 = nxt3[e], a4 = nxt4[e];
+          ends[k++] = (short)a1;
+          if (a1 == m - 1) break;
+          ends[k++] = (short)a2;
+          if (a2 == m - 1) break;
+          ends[k++] = (short)a3;
+          if (a3 == m - 1) break;
+          ends[k++] = (short)a4;
+          e = a4;
         }
         sh_ng = k;
       }
@@ -991,17 +1008,17 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
   // FP32 distances are taken from the grid point nearest the line centre, so
   // that points near the centre do not lose digits to cancellation
   const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
-  r->mcf = (float)mc;
-  r->x0 = (float)((double)mc * P.dvr4 - XNUI);
-  r->sil = (float)SIL;
-  r->al2 = (float)ALFLI2;
-  r->ralv2 = (float)(1. / ALFVI2);
-  r->sa3 = (float)(SIV * A3);
-  r->sb3 = (float)(SIV * B3);
+  auto pair = [](double v) { return make_float2((float)v, (float)v); };
+  r->nmc = pair(-(double)mc);
+  r->x0 = pair((double)mc * P.dvr4 - XNUI);
+  r->sil = pair(SIL);
+  r->al2 = pair(ALFLI2);
+  r->ralv2 = pair(1. / ALFVI2);
+  r->sa3 = pair(SIV * A3);
+  r->sb3 = pair(SIV * B3);
   // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
-  r->fb0 = (float)(co2 ? 2. * F4BND : F4BND);
-  r->fb2 = (float)(co2 ? F4BND / BNDSQ : 0.);
-  r->pad = 0.f;
+  r->nfb0 = pair(co2 ? -2. * F4BND : -F4BND);
+  r->fb2 = pair(co2 ? F4BND / BNDSQ : 0.);
   d->xnui = XNUI;
   d->sil = SIL;
   d->siv = SIV;

@@ -750,8 +750,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     dim3 grid((unsigned)((maxr4 + 2 + kF4Tile - 1) / kF4Tile), count);
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-    if (plain) k_f4_conv<true><<<grid, kF4Tile, 0, st>>>(fa);
-    else k_f4_conv<false><<<grid, kF4Tile, 0, st>>>(fa);
+    if (plain) k_f4_conv<true><<<grid, kF4Threads, 0, st>>>(fa);
+    else k_f4_conv<false><<<grid, kF4Threads, 0, st>>>(fa);
     CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   }
   CUDA_TRY(h, cudaEventRecord(h->join_ev, st));
