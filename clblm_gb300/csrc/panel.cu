@@ -73,17 +73,6 @@ __device__ __noinline__ int table_index_near_boundary(int k, float zfl, float zs
   return (int)n + 1 + (dd >= 0.5f ? 1 : (dd < -0.5f ? -1 : 0));
 }
 
-__device__ __forceinline__ int table_index_mixed(int k, const GridRec& r, GridRecLo lo, const GridRecD* rd,
-                                                 bool hit = true) {
-  float zf = fmaf((float)k, r.zs, r.zfl);
-  float az = fabsf(zf);
-  float t = az + 12582913.0f;                  // 1.5*2^23 + 1: rounds |ZF|+1
-  int iz = __float_as_int(t) - 0x4B400000;     // rint(|ZF|) + 1
-  float d = az - (t - 12582913.0f);            // |ZF| - rint(|ZF|), exact
-  if (hit && fabsf(d) > 0.499f) iz = table_index_near_boundary(k, r.zfl, r.zs, lo, rd);
-  return iz;
-}
-
 // XINT set-up of one panel (clblm_Spectrum.f90:874-915 as called by HIRACQ,
 // clblm_ODLAY.f90:1451-1459): the R4 blocks in use (index 0: the previous
 // panel's, for the carried points 1..5; 1: this panel's), the R3 index
@@ -118,7 +107,6 @@ struct PanelTiles {
 // mixed path: under 74 KB, so that three CTAs share an SM
 template <>
 struct PanelSmem<false> : PanelTiles {
-  GridRecLo wlo[kPanelWarps][kBatch];
   float absf[kAbsStage];
   float2 t1ab[kNFMX];    // R1 tables F1, FG
   float t1c[kNFMX];      // R1 table XVER
@@ -293,35 +281,79 @@ __device__ __forceinline__ void tile_ranges(const int* __restrict__ pm, const in
   }
 }
 
-// Contribution of one record at global point g of the lane (mixed path):
-// zero unless the record's range holds g and its panel is at most qmax.
+// Table value of record r at table index iz (mixed path)
 template <int GRID>
-__device__ __forceinline__ float contrib_mixed(const PanelSmem<false>& S, const GridRec& r, GridRecLo lo,
-                                               const GridRecD* rd, int g, int qmax, int* err) {
-  bool hit = g >= r.g_lo && g <= r.g_hi && r.q <= qmax;
-  int iz = table_index_mixed(g - r.g_lo + 1, r, lo, rd, hit);
-  if (hit && iz > kNFMX) {
-    atomicOr(err, 2);
-    hit = false;
-  }
-  iz = hit ? iz : 1;
-  float v;
+__device__ __forceinline__ float table_term(const PanelSmem<false>& S, const GridRec& r, int iz) {
   if constexpr (GRID == 1) {
     const float2 ab = S.t1ab[iz - 1];
-    v = fmaf(r.a0, ab.x, fmaf(r.a1, ab.y, r.a2 * S.t1c[iz - 1]));
+    return fmaf(r.a0, ab.x, fmaf(r.a1, ab.y, r.a2 * S.t1c[iz - 1]));
   } else if constexpr (GRID == 2) {
-    v = r.a0 * S.t2[iz - 1];
+    return r.a0 * S.t2[iz - 1];
   } else {
-    v = r.a0 * S.t3[iz - 1];
+    return r.a0 * S.t3[iz - 1];
   }
+}
+
+// FP32 table index rint(|ZF|) + 1 = INT(|ZF| + 1.5) away from ties, and the
+// distance d = |ZF| - rint(|ZF|) (exact) that tells how near the rounding
+// boundary |d| = 0.5 the FP32 argument lies.  Always >= 1.
+__device__ __forceinline__ int fast_index(int k, const GridRec& r, float* d) {
+  const float az = fabsf(fmaf((float)k, r.zs, r.zfl));
+  const float t = az + 12582913.0f;            // 1.5*2^23 + 1: rounds |ZF| + 1
+  *d = az - (t - 12582913.0f);
+  return __float_as_int(t) - 0x4B400000;
+}
+
+// Contribution of one record at global point g of the lane (mixed path),
+// without branches: zero unless the record's range holds g and its panel is
+// at most qmax.  A hit whose FP32 index is within 1e-3 of a rounding
+// boundary, or beyond the tables, sets `bit` in *fix; the caller redoes those
+// terms with the reference's FP64 index.
+template <int GRID>
+__device__ __forceinline__ float term_fast(const PanelSmem<false>& S, const GridRec& r, int g, int qmax,
+                                           unsigned* fix, unsigned bit) {
+  const int kk = g - r.g_lo + 1;
+  const bool hit = kk >= 1 && g <= r.g_hi && r.q <= qmax;
+  float d;
+  int iz = fast_index(kk, r, &d);
+  *fix |= (hit && (fabsf(d) > 0.499f || iz > kNFMX)) ? bit : 0u;
+  iz = min(iz, kNFMX);
+  const float v = table_term<GRID>(S, r, iz);
   return hit ? v : 0.f;
+}
+
+// Correction of a batch sum for the terms flagged by term_fast: the term with
+// the FP64-exact index replaces the FP32-index one (both hits by construction)
+template <int GRID>
+__device__ __forceinline__ float fix_terms(const PanelSmem<false>& S, const GridRec* buf, int64_t base,
+                                        const GridRecLo* __restrict__ reclo, const GridRecD* __restrict__ recd,
+                                        int g, unsigned fix, int* err) {
+  float c = 0.f;
+  while (fix) {
+    const int k = __ffs(fix) - 1;
+    fix &= fix - 1;
+    const GridRec r = buf[k];
+    const int kk = g - r.g_lo + 1;
+    float d;
+    const int izf = fast_index(kk, r, &d);
+    const float vf = table_term<GRID>(S, r, min(izf, kNFMX));
+    const int iz = fabsf(d) > 0.499f ? table_index_near_boundary(kk, r.zfl, r.zs, reclo[base + k], recd + (base + k))
+                                     : izf;
+    if (iz > kNFMX) {
+      atomicOr(err, 2);
+      c -= vf;
+    } else if (iz != izf) {
+      c += table_term<GRID>(S, r, iz) - vf;
+    }
+  }
+  return c;
 }
 
 // Sum over the records [lo, hi) of one grid at global point g of the lane:
 // the records pass through the warp's shared-memory buffer kBatch at a time,
 // the next batch already loaded into registers while the current one is used.
-// The FP64 path adds record by record in record order; the mixed path adds
-// the records in pairs (one FP32 sum per pair into the Kahan sum).
+// The FP64 path adds record by record in record order; the mixed path sums
+// each batch in FP32 (four partial sums) and adds the batch to the Kahan sum.
 template <bool Plain, int GRID>
 __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs& a, const GridRec* __restrict__ rec,
                                             const GridRecD* __restrict__ recd, const GridRecLo* __restrict__ reclo,
@@ -332,25 +364,21 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
   GridRec* buf = S.wrec[warp];
   GridRec nxt;
   GridRecD nxtd;
-  GridRecLo nxtl;
   if (lo + sl < hi) {
     nxt = rec[lo + sl];
     if constexpr (Plain) nxtd = recd[lo + sl];
-    else nxtl = reclo[lo + sl];
   }
   for (int64_t base = lo; base < hi; base += kBatch) {
     __syncwarp();
     if (lane < kBatch) {
       buf[lane] = nxt;
       if constexpr (Plain) S.wrecd[warp][lane] = nxtd;
-      else S.wlo[warp][lane] = nxtl;
     }
     __syncwarp();
     const int cnt = (int)(hi - base < kBatch ? hi - base : kBatch);
     if (base + kBatch + sl < hi) {
       nxt = rec[base + kBatch + sl];
       if constexpr (Plain) nxtd = recd[base + kBatch + sl];
-      else nxtl = reclo[base + kBatch + sl];
     }
     if (!active) continue;
     if constexpr (Plain) {
@@ -373,12 +401,23 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
         }
       }
     } else {
-      for (int k = 0; k < cnt; k += 2) {
-        const int k1 = (k + 1 < cnt) ? k + 1 : k;
-        float v0 = contrib_mixed<GRID>(S, buf[k], S.wlo[warp][k], recd + (base + k), g, qmax, a.err);
-        float v1 = contrib_mixed<GRID>(S, buf[k1], S.wlo[warp][k1], recd + (base + k1), g, qmax, a.err);
-        acc.add(k1 != k ? v0 + v1 : v0);
+      // four FP32 partial sums per batch, one Kahan step per batch
+      unsigned fix = 0;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      if (cnt == kBatch) {
+#pragma unroll
+        for (int k = 0; k < kBatch; k += 4) {
+          s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
+          s1 += term_fast<GRID>(S, buf[k + 1], g, qmax, &fix, 2u << k);
+          s2 += term_fast<GRID>(S, buf[k + 2], g, qmax, &fix, 4u << k);
+          s3 += term_fast<GRID>(S, buf[k + 3], g, qmax, &fix, 8u << k);
+        }
+      } else {
+        for (int k = 0; k < cnt; ++k) s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
       }
+      float bsum = (s0 + s1) + (s2 + s3);
+      if (fix) bsum += fix_terms<GRID>(S, buf, base, reclo, recd, g, fix, a.err);
+      acc.add(bsum);
     }
   }
   __syncwarp();
