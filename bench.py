@@ -401,7 +401,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kt = {"ms_panel": 0.0, "ms_f4conv": 0.0, "launches": 0}
+    kt = {"ms_panel": 0.0, "ms_f4conv": 0.0, "ms_line_chain": 0.0, "ms_f4_chain": 0.0, "launches": 0}
     with Clocks() as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
@@ -479,7 +479,12 @@ def main():
                         "ms_per_step": e2e_ms},
                 "plain_fp64": plain, "jacobians": jacl, "cpu_baseline": cpu, "roofline": roof,
                 "clocks": clk.summary(),
-                "gpu_launches": int(kt["launches"])}
+                "gpu_launches": int(kt["launches"]),
+                # per step, from events on the library's two streams: the line chain
+                # and the far-wing chain run side by side before the panel kernel
+                "stages_ms": {"line_chain": kt["ms_line_chain"] / args.steps,
+                              "far_wing_chain": kt["ms_f4_chain"] / args.steps,
+                              "k_f4_conv": kt["ms_f4conv"] / args.steps, "k_panel": kt["ms_panel"] / args.steps}}
         print(json.dumps(line))
     h.close()
     if world > 1:

@@ -74,8 +74,10 @@ __global__ void k_f4_blockscan(int64_t* blocksum, int nblk, const LayerPlan* pla
 __global__ void k_f4_compact(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0,
                              const int64_t* blocksum, int nblk, int64_t* cidx, long long* vbits, long long* lbits,
                              int64_t* src, unsigned char* flags, int64_t* cut);
+__global__ void k_f4_next(const long long* vbits, const long long* lbits, const int64_t* ntot, int64_t stride,
+                          int* gnxt);
 __global__ void k_f4_walk(const LayerPlan* plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
-                          const int64_t* cidx, const long long* vbits, const long long* lbits,
+                          const int64_t* cidx, const long long* vbits, const long long* lbits, const int* gnxt,
                           const unsigned char* flags, const int64_t* ntot, const int64_t* cut, int4* groups,
                           int64_t* ngroups);
 __global__ void k_f4_groupsum(const LayerPlan* plans, int layer0, const F4Prep* prep, int64_t stride,

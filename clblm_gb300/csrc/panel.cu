@@ -311,9 +311,9 @@ __device__ __forceinline__ int fast_index(int k, const GridRec& r, float* d) {
 // terms with the reference's FP64 index.
 template <int GRID>
 __device__ __forceinline__ float term_fast(const PanelSmem<false>& S, const GridRec& r, int g, int qmax,
-                                           unsigned* fix, unsigned bit) {
+                                           unsigned* fix, unsigned bit, bool valid = true) {
   const int kk = g - r.g_lo + 1;
-  const bool hit = kk >= 1 && g <= r.g_hi && r.q <= qmax;
+  const bool hit = valid && kk >= 1 && g <= r.g_hi && r.q <= qmax;
   float d;
   int iz = fast_index(kk, r, &d);
   *fix |= (hit && (fabsf(d) > 0.499f || iz > kNFMX)) ? bit : 0u;
@@ -413,7 +413,13 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
           s3 += term_fast<GRID>(S, buf[k + 3], g, qmax, &fix, 8u << k);
         }
       } else {
-        for (int k = 0; k < cnt; ++k) s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
+        // a partial batch in groups of four; entries past cnt are masked
+        for (int k = 0; k < cnt; k += 4) {
+          s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
+          s1 += term_fast<GRID>(S, buf[k + 1], g, qmax, &fix, 2u << k, k + 1 < cnt);
+          s2 += term_fast<GRID>(S, buf[k + 2], g, qmax, &fix, 4u << k, k + 2 < cnt);
+          s3 += term_fast<GRID>(S, buf[k + 3], g, qmax, &fix, 8u << k, k + 3 < cnt);
+        }
       }
       float bsum = (s0 + s1) + (s2 + s3);
       if (fix) bsum += fix_terms<GRID>(S, buf, base, reclo, recd, g, fix, a.err);

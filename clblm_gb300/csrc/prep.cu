@@ -712,45 +712,71 @@ __global__ void k_f4_compact(const F4Prep* __restrict__ prep, int64_t stride, co
   }
 }
 
+// Next-group map of one layer's compacted far-wing stream.  Within a SHRINQ
+// call, a group that follows a group ending at line b has the limit
+// VLMT = VNU(b) + DVR4/2 and ends at the first line e > b whose successor
+// lies above VLMT, or at the call's last line (clblm_ODLAY_LineF4.f90:1529-
+// 1560).  gnxt[b] = (first j >= b+2 with VNU(j) > VLMT) - 1 over the whole
+// stream; a call takes min(gnxt[b], its last line).  Centres carry their
+// pressure shifts and need not be sorted, so the search is the reference's
+// linear one, one thread per line.
+__global__ void k_f4_next(const long long* __restrict__ vbits, const long long* __restrict__ lbits,
+                          const int64_t* __restrict__ ntot, int64_t stride, int* __restrict__ gnxt) {
+  const int layer = blockIdx.y;
+  const int64_t total = ntot[layer];
+  const long long* V = vbits + (int64_t)layer * stride;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < total; b += (int64_t)gridDim.x * blockDim.x) {
+    const long long lim = lbits[(int64_t)layer * stride + b];
+    int64_t j = b + 2;
+    while (j < total && V[j] <= lim) ++j;
+    gnxt[(int64_t)layer * stride + b] = (int)(j - 1);
+  }
+}
+
 // Group list of one layer: one CTA replays LINF4Q's record loop (records of
 // 250 lines appended to a buffer until it holds 1000, then SHRINQ over the
 // lines not yet shrunk, clblm_ODLAY_LineF4.f90:1355-1476 and :1516-1647).
-// Centres are compared through their bit patterns (positive centres order
-// like their binary64 images; a non-positive centre is rejected on the host).
 //
-// Within one SHRINQ call a group that follows a group ending at line b has
-// the limit VLMT = VNU(b) + DVR4/2 and ends at the first line e > b whose
-// successor lies above VLMT.  That end is computed for every b in parallel;
-// one thread then follows the chain from the first group through shared
-// memory, and the groups' flags and output slots come from block scans.
-// Each group records its stream range and how many lines it emits (a
-// non-CO2 line when a non-CO2 member has SP >= 1e-35, a CO2 line likewise),
-// which is what the buffer arithmetic of the record loop counts.
+// One SHRINQ call over m lines: the group ends form the chain e0, nxt(e0),
+// nxt(nxt(e0)), ... up to the call's last line, with nxt the capped
+// next-group map and e0 the end of the first group (VLMT = VNU(first) +
+// DVR4/2).  The chain is found in parallel: binary-lifting tables nxt^(2^k)
+// in shared memory, then every line v >= e0 descends greedily from e0 to the
+// last chain node <= v and is a group end when it lands on itself.  A block
+// scan ranks the ends and counts each line's non-CO2 / CO2 flags; a group
+// emits a non-CO2 line when one of its members has a non-CO2 line with
+// SP >= 1e-35, a CO2 line likewise, and a second scan gives the output slots
+// that the record loop's buffer arithmetic counts.
 constexpr int kWalkThreads = 256;
 constexpr int kWalkMax = 1280;  // lines of one SHRINQ call: < 1000 + one 250-line record
+constexpr int kWalkPer = kWalkMax / kWalkThreads;
+constexpr int kLift = 11;       // 2^11 > kWalkMax
+constexpr int kRecWin = 256;    // records whose stream offsets are staged at a time
 
-// exclusive block scan of one int per thread; returns the block total
-__device__ __forceinline__ int block_scan_excl(int v, int* warp_tot, int* out_excl) {
+// exclusive block scan of one value per thread; returns the block total
+template <typename T>
+__device__ __forceinline__ T block_scan_excl(T v, T* warp_tot, T* out_excl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int x = v;
+  T x = v;
   for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, o);
+    T y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
   if (lane == 31) warp_tot[warp] = x;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int w = 0; w < kWalkThreads / 32; ++w) {
-      int t = warp_tot[w];
-      warp_tot[w] = run;
-      run += t;
+  if (threadIdx.x < 32) {
+    T w = threadIdx.x < kWalkThreads / 32 ? warp_tot[threadIdx.x] : T(0);
+    T z = w;
+    for (int o = 1; o < kWalkThreads / 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, z, o);
+      if ((int)threadIdx.x >= o) z += y;
     }
-    warp_tot[kWalkThreads / 32] = run;
+    if (threadIdx.x < kWalkThreads / 32) warp_tot[threadIdx.x] = z - w;
+    if (threadIdx.x == kWalkThreads / 32 - 1) warp_tot[kWalkThreads / 32] = z;
   }
   __syncthreads();
   *out_excl = warp_tot[warp] + x - v;
-  int total = warp_tot[kWalkThreads / 32];
+  const T total = warp_tot[kWalkThreads / 32];
   __syncthreads();
   return total;
 }
@@ -758,17 +784,17 @@ __device__ __forceinline__ int block_scan_excl(int v, int* warp_tot, int* out_ex
 __global__ void __launch_bounds__(kWalkThreads)
     k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
               const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
-              const long long* __restrict__ lbits, const unsigned char* __restrict__ flags,
-              const int64_t* __restrict__ ntot, const int64_t* __restrict__ cut, int4* __restrict__ groups,
-              int64_t* __restrict__ ngroups) {
-  __shared__ long long sv[kWalkMax], sl[kWalkMax];
-  __shared__ short nxt[kWalkMax];          // group end following a group that ends at b
-  __shared__ short nxt2[kWalkMax], nxt3[kWalkMax], nxt4[kWalkMax];  // nxt applied 2, 3, 4 times
-  __shared__ short ends[kWalkMax];         // group ends of the call, in order
+              const long long* __restrict__ lbits, const int* __restrict__ gnxt,
+              const unsigned char* __restrict__ flags, const int64_t* __restrict__ ntot,
+              const int64_t* __restrict__ cut, int4* __restrict__ groups, int64_t* __restrict__ ngroups) {
+  __shared__ short up[kLift][kWalkMax];     // up[k][b]: nxt applied 2^k times
+  __shared__ short ends[kWalkMax];          // group ends of the call, in order
+  __shared__ short pc1[kWalkMax + 1], pc2[kWalkMax + 1];  // flag counts before each line
   __shared__ unsigned char sf[kWalkMax];
-  __shared__ int warp_tot[kWalkThreads / 32 + 1];
-  __shared__ int sh_ng;
-  constexpr int kPer = kWalkMax / kWalkThreads;  // lines (or groups) per thread in the scans
+  __shared__ int64_t civ[kRecWin + 1];      // stream offsets of records wbase .. wbase+kRecWin
+  __shared__ unsigned long long wt64[kWalkThreads / 32 + 1];
+  __shared__ int wt32[kWalkThreads / 32 + 1];
+  __shared__ int sh_e0, sh_K;
 
   const int layer = blockIdx.x;
   if (layer >= nlayers) return;
@@ -778,6 +804,7 @@ __global__ void __launch_bounds__(kWalkThreads)
   const int64_t* ci = cidx + (int64_t)layer * (stride + 1);
   const long long* V = vbits + (int64_t)layer * stride;
   const long long* Lm = lbits + (int64_t)layer * stride;
+  const int* GN = gnxt + (int64_t)layer * stride;
   const unsigned char* F = flags + (int64_t)layer * stride;
   int4* G = groups + (int64_t)layer * stride;
   const int64_t total = ntot[layer];
@@ -787,6 +814,7 @@ __global__ void __launch_bounds__(kWalkThreads)
   const int64_t R = 250;
   const int64_t nrec_total = (nlines_total + R - 1) / R;
   int64_t rec = P.f4_lo / R;
+  int64_t wbase = -(kRecWin + 2);  // no record staged yet
   int64_t IJ = 0, ILO = 1;  // 1-based buffer positions, as in LINF4Q
   int64_t u0 = 0;           // stream index of the first unshrunk line
   int64_t ng = 0, slot = 0;
@@ -796,11 +824,20 @@ __global__ void __launch_bounds__(kWalkThreads)
     if (rec >= nrec_total) {
       IEOF = true;
     } else {
+      if (rec + 1 > wbase + kRecWin) {  // stage the offsets of the next records
+        wbase = rec;
+        __syncthreads();
+        for (int k = tid; k <= kRecWin; k += kWalkThreads) {
+          int64_t t = (wbase + k) * R - P.f4_lo;
+          civ[k] = ci[t < 0 ? 0 : (t > n ? n : t)];
+        }
+        __syncthreads();
+      }
       int64_t tb = rec * R - P.f4_lo, te = tb + R;
+      const int64_t cb = civ[rec - wbase];
       rec++;
-      int64_t cb = ci[tb < 0 ? 0 : (tb > n ? n : tb)];
       int64_t ce;
-      if (te <= n) ce = ci[te];
+      if (te <= n) ce = civ[rec - wbase];
       else if (rec * R >= nlines_total || (has_cut && send <= ci[n])) ce = ci[n];
       else {  // lines beyond the prepared range would be needed
         status = 2;
@@ -823,75 +860,100 @@ __global__ void __launch_bounds__(kWalkThreads)
     int64_t nemit = 0;
     if (m > 0) {
       for (int i = tid; i < m; i += kWalkThreads) {
-        sv[i] = V[u0 + i];
-        sl[i] = Lm[u0 + i];
+        const int64_t e = GN[u0 + i];
+        up[0][i] = (short)((e < u1 - 1 ? e : u1 - 1) - u0);
         sf[i] = F[u0 + i];
       }
-      __syncthreads();
-      // the end of the group that starts at b+1 with VLMT = VNU(b) + DVR4/2:
-      // the first e > b with VNU(e+1) > VLMT, or the last line
-      for (int b = tid; b < m; b += kWalkThreads) {
-        const long long lim = sl[b];
-        int j = b + 2;
-        while (j < m && sv[j] <= lim) ++j;
-        nxt[b] = (short)(j - 1 < m - 1 ? j - 1 : m - 1);
-      }
-      __syncthreads();
-      // powers of the map, so that the chain below advances four groups per
-      // step with independent loads (nxt(m-1) = m-1 keeps chains at the end)
-      for (int b = tid; b < m; b += kWalkThreads) nxt2[b] = nxt[nxt[b]];
-      __syncthreads();
-      for (int b = tid; b < m; b += kWalkThreads) {
-        nxt3[b] = nxt[nxt2[b]];
-        nxt4[b] = nxt2[nxt2[b]];
-      }
-      __syncthreads();
       if (tid == 0) {
-        // the first group starts at the first unshrunk line, VLMT = VNU(ILO) + DVR4/2
-        const long long lim = sl[0];
-        int j = 1;
-        while (j < m && sv[j] <= lim) ++j;
-        int e = j - 1;
-        int k = 0;
-        ends[k++] = (short)e;
-        while (e < m - 1) {
-          const int a1 = nxt[e], a2 = nxt2[e], a3 = nxt3[e], a4 = nxt4[e];
-          ends[k++] = (short)a1;
-          if (a1 == m - 1) break;
-          ends[k++] = (short)a2;
-          if (a2 == m - 1) break;
-          ends[k++] = (short)a3;
-          if (a3 == m - 1) break;
-          ends[k++] = (short)a4;
-          e = a4;
-        }
-        sh_ng = k;
+        // the first group: VLMT = VNU(first) + DVR4/2
+        sh_e0 = (m == 1 || V[u0 + 1] > Lm[u0]) ? 0 : -1;
       }
       __syncthreads();
-      const int gcount = sh_ng;
-      // which kinds each group emits: OR of its members' flags, then the
-      // output slots by a scan of the emitted counts
-      int kind[kPer], cnt = 0;
-      for (int q = 0; q < kPer; ++q) {
-        const int g = tid * kPer + q;
+      if (tid == 0 && sh_e0 < 0) sh_e0 = up[0][0];
+      __syncthreads();
+      const int e0 = sh_e0;
+      // lifting tables until 2^K steps from e0 reach the last line
+      int K = 0;
+      while (K < kLift - 1 && up[K][e0] != m - 1) {
+        for (int i = tid; i < m; i += kWalkThreads) up[K + 1][i] = up[K][up[K][i]];
+        ++K;
+        __syncthreads();
+      }
+      // group ends: lines v >= e0 on the chain; thread t owns lines t*kWalkPer + q
+      bool on[kWalkPer];
+      {
+        int x[kWalkPer];
+#pragma unroll
+        for (int q = 0; q < kWalkPer; ++q) x[q] = e0;
+        for (int k = K; k >= 0; --k) {
+#pragma unroll
+          for (int q = 0; q < kWalkPer; ++q) {
+            const int v = tid * kWalkPer + q;
+            const int y = up[k][x[q]];
+            if (y <= v) x[q] = y;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kWalkPer; ++q) {
+          const int v = tid * kWalkPer + q;
+          on[q] = v < m && v >= e0 && x[q] == v;
+        }
+      }
+      // one scan: ends (bits 0-20), non-CO2 flags (21-41), CO2 flags (42-62)
+      unsigned long long mine = 0;
+#pragma unroll
+      for (int q = 0; q < kWalkPer; ++q) {
+        const int v = tid * kWalkPer + q;
+        const unsigned f = v < m ? sf[v] : 0u;
+        mine += (unsigned long long)on[q] + ((unsigned long long)(f & 1u) << 21) +
+                ((unsigned long long)((f >> 1) & 1u) << 42);
+      }
+      unsigned long long ex;
+      const unsigned long long tot = block_scan_excl<unsigned long long>(mine, wt64, &ex);
+      {
+        unsigned long long run = ex;
+#pragma unroll
+        for (int q = 0; q < kWalkPer; ++q) {
+          const int v = tid * kWalkPer + q;
+          if (v < m) {
+            pc1[v] = (short)((run >> 21) & 0x1FFFFF);
+            pc2[v] = (short)((run >> 42) & 0x1FFFFF);
+            if (on[q]) ends[run & 0x1FFFFF] = (short)v;
+            const unsigned f = sf[v];
+            run += (unsigned long long)on[q] + ((unsigned long long)(f & 1u) << 21) +
+                   ((unsigned long long)((f >> 1) & 1u) << 42);
+          }
+        }
+      }
+      if (tid == 0) {
+        pc1[m] = (short)((tot >> 21) & 0x1FFFFF);
+        pc2[m] = (short)((tot >> 42) & 0x1FFFFF);
+      }
+      __syncthreads();
+      const int gcount = (int)(tot & 0x1FFFFF);
+      // which kinds each group emits, then the output slots; thread t owns
+      // groups t*kWalkPer + q
+      int kind[kWalkPer], cnt = 0;
+#pragma unroll
+      for (int q = 0; q < kWalkPer; ++q) {
+        const int g = tid * kWalkPer + q;
         kind[q] = 0;
         if (g < gcount) {
-          const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g];
-          int f = 0;
-          for (int i = s0; i <= s1; ++i) f |= sf[i];
-          kind[q] = f & 3;
-          cnt += (f & 1) + ((f >> 1) & 1);
+          const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g] + 1;
+          kind[q] = (pc1[s1] > pc1[s0] ? 1 : 0) | (pc2[s1] > pc2[s0] ? 2 : 0);
+          cnt += (kind[q] & 1) + (kind[q] >> 1);
         }
       }
       int excl;
-      const int emitted = block_scan_excl(cnt, warp_tot, &excl);
+      const int emitted = block_scan_excl<int>(cnt, wt32, &excl);
       int run = (int)slot + excl;
-      for (int q = 0; q < kPer; ++q) {
-        const int g = tid * kPer + q;
+#pragma unroll
+      for (int q = 0; q < kWalkPer; ++q) {
+        const int g = tid * kWalkPer + q;
         if (g < gcount) {
           const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g];
           if (ng + g < stride) G[ng + g] = make_int4((int)(u0 + s0), (int)(u0 + s1), run, kind[q]);
-          run += (kind[q] & 1) + ((kind[q] >> 1) & 1);
+          run += (kind[q] & 1) + (kind[q] >> 1);
         }
       }
       ng += gcount;

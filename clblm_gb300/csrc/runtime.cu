@@ -80,23 +80,24 @@ struct clblm_handle {
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
   DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
   DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
-  DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp;
+  DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt;
   DevBuf rt[4], outbuf, imap[2];
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
   // per-call sums of the line-shape kernels' work and device time
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // f4 start/stop, panel start/stop
+  // f4 conv start/stop, panel start/stop, batch start, line chain done
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // the far-wing chain runs on a second stream, forked from and joined back
   // into `stream` within each OD batch
   cudaStream_t stream2 = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int64_t acc_fnq = 0, acc_f4q = 0;
-  double acc_ms_panel = 0., acc_ms_f4 = 0.;
+  double acc_ms_panel = 0., acc_ms_f4 = 0., acc_ms_line_chain = 0., acc_ms_f4_chain = 0.;
   void reset_call() {
     launches = 0;
     acc_fnq = acc_f4q = 0;
-    acc_ms_panel = acc_ms_f4 = 0.;
+    acc_ms_panel = acc_ms_f4 = acc_ms_line_chain = acc_ms_f4_chain = 0.;
   }
 };
 
@@ -688,6 +689,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   dim3 blk(256);
   // the continuum and the far-wing chain on the second stream, the line
   // chain on the handle's stream; k_panel waits for both
+  CUDA_TRY(h, cudaEventRecord(h->ev[4], h->stream));
   CUDA_TRY(h, cudaEventRecord(h->fork_ev, h->stream));
   CUDA_TRY(h, cudaStreamWaitEvent(h->stream2, h->fork_ev, 0));
   cudaStream_t st = h->stream2;
@@ -714,10 +716,13 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
                                                      h->f4src.as<int64_t>(), h->f4flag.as<unsigned char>(),
                                                      h->f4cut.as<int64_t>());
     h->launches++;
+    k_f4_next<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), 256, 0, st>>>(
+        h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4ntot.as<int64_t>(), f4stride, h->f4nxt.as<int>());
+    h->launches++;
     k_f4_walk<<<count, 256, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
-                                    h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4flag.as<unsigned char>(),
-                                    h->f4ntot.as<int64_t>(), h->f4cut.as<int64_t>(), h->f4grp.as<int4>(),
-                                    h->f4nout.as<int64_t>());
+                                    h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4nxt.as<int>(),
+                                    h->f4flag.as<unsigned char>(), h->f4ntot.as<int64_t>(), h->f4cut.as<int64_t>(),
+                                    h->f4grp.as<int4>(), h->f4nout.as<int64_t>());
     h->launches++;
     k_f4_groupsum<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), 256, 0, st>>>(
         dplans, first, h->f4prep.as<F4Prep>(), f4stride, h->f4src.as<int64_t>(), h->f4grp.as<int4>(),
@@ -812,6 +817,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     k_r4_radfac<<<dim3((maxb + 63) / 64, count), 64, 0, st>>>(dplans, first, h->bv1.as<double>(), h->bn.as<int>(),
                                                             h->bfac.as<double>());
   }
+  CUDA_TRY(h, cudaEventRecord(h->ev[5], st));
   CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
   size_t smem = panel_smem_bytes(plain);
   if (plain) {
@@ -890,6 +896,7 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
     CUDA_TRY(h, h->f4lb.ensure(sizeof(long long) * fs * count));
     CUDA_TRY(h, h->f4src.ensure(sizeof(int64_t) * fs * count));
     CUDA_TRY(h, h->f4flag.ensure(fs * count));
+    CUDA_TRY(h, h->f4nxt.ensure(sizeof(int) * fs * count));
     CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * count));
     CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * fs * count));
   }
@@ -961,11 +968,15 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
   if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
   if (err[0] & 4) return set_err(h, CLBLM_ERR_CUDA, "far-wing records: a shared-memory stage never arrived");
   {
-    float t0 = 0.f, t1 = 0.f;
+    float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
     CUDA_TRY(h, cudaEventElapsedTime(&t0, h->ev[0], h->ev[1]));
     CUDA_TRY(h, cudaEventElapsedTime(&t1, h->ev[2], h->ev[3]));
+    CUDA_TRY(h, cudaEventElapsedTime(&t2, h->ev[4], h->ev[5]));
+    CUDA_TRY(h, cudaEventElapsedTime(&t3, h->ev[4], h->ev[1]));
     h->acc_ms_f4 += t0;
     h->acc_ms_panel += t1;
+    h->acc_ms_line_chain += t2;
+    h->acc_ms_f4_chain += t3;
     for (int k = first; k < first + count; ++k) {
       h->acc_fnq += (int64_t)stats[k * kStatsPerLayer + 5];
       h->acc_f4q += (int64_t)stats[k * kStatsPerLayer + 6];
@@ -998,6 +1009,8 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
     last_stats->cnvf4q_steps = h->acc_f4q;
     last_stats->ms_panel = h->acc_ms_panel;
     last_stats->ms_f4conv = h->acc_ms_f4;
+    last_stats->ms_line_chain = h->acc_ms_line_chain;
+    last_stats->ms_f4_chain = h->acc_ms_f4_chain;
   }
   return CLBLM_OK;
 }
@@ -1094,7 +1107,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
+                    &h->f4cut,     &h->f4grp,    &h->f4nxt,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
                     &h->jblk};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();

@@ -194,6 +194,8 @@ typedef struct {
   int64_t cnvf4q_steps; /* sum of (far-wing record, R4 point) pairs (CNVF4Q)    */
   double  ms_panel;     /* device time of the panel kernel (R1/R2/R3 + combine) */
   double  ms_f4conv;    /* device time of the far-wing convolution kernel       */
+  double  ms_line_chain; /* batch start to the end of the line chain (stream 1) */
+  double  ms_f4_chain;  /* batch start to the end of the far-wing chain (stream 2) */
 } clblm_od_stats_t;
 
 typedef struct clblm_handle clblm_handle_t;
