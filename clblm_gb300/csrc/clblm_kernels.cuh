@@ -61,7 +61,7 @@ __global__ void k_scan_apply(const LinePrep* prep, int64_t stride, const int64_t
 __global__ void k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
                                const int* qpanel, int64_t stride, GridRec* rec, GridRecD* recd,
                                GridRecLo* reclo, const double* vnu_raw, unsigned long long* stats,
-                               double* alfvmax);
+                               double* alfvmax, int* aggmax, int* aggmin, int nagg);
 __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
 __global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);
@@ -87,8 +87,12 @@ struct F4RecD;
 __global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
                               int64_t* nmirror, unsigned long long* stats);
-__global__ void k_rec_bounds(const LayerPlan* plans, int layer0, const GridRec* rec, int64_t stride, int* pmax,
-                             int* smin);
+// running bounds of the line records, in blocks of kRecBlock records
+constexpr int kRecBlock = 256;
+constexpr int kRecNone = 0x7fffffff;
+__global__ void k_rec_carry(const LayerPlan* plans, int layer0, int* aggmax, int* aggmin, int nagg);
+__global__ void k_rec_bounds(const LayerPlan* plans, int layer0, const GridRec* rec, int64_t stride,
+                             const int* aggmax, const int* aggmin, int nagg, int* pmax, int* smin);
 __global__ void k_f4_bounds(const F4Rec* rec, int64_t rstride, const int64_t* nrec, int layer0, int* pmax,
                             int* smin);
 

@@ -41,15 +41,15 @@ struct PanelArgs {
 // FP32 form of the mixed path: 80 bytes, staged in shared memory in chunks.
 // Every coefficient is stored twice, as the (x, y) operand pair of the
 // packed FP32x2 arithmetic that evaluates two points at once.
-struct __align__(16) F4Rec {
-  int jmin, jmax;   // global R4 points J = m+1 in [jmin, jmax]
+struct __align__(16) F4Rec {  // the wing terms' operands fill the first 48 bytes
   float2 nmc;       // -mc: the grid point m nearest the line centre (exact in FP32)
   float2 x0;        // mc*DVR4 - XNUI, |x0| <= DVR4/2
-  float2 ralv2;     // 1 / ALFV^2
   float2 nfb0, fb2; // minus the pedestal: -fb0 + x^2 fb2 (CO2: fb0 = 2 F4BND,
                     // fb2 = F4BND/BOUND^2; else F4BND, 0)
-  float2 sa3, sb3;  // SIV*A3, SIV*B3
   float2 al2, sil;  // ALFL^2, SIL
+  float2 ralv2;     // 1 / ALFV^2
+  float2 sa3, sb3;  // SIV*A3, SIV*B3
+  int jmin, jmax;   // global R4 points J = m+1 in [jmin, jmax]
 };
 static_assert(sizeof(F4Rec) == 80, "far-wing record layout");
 // FP64 form (the FP64 path), 64 bytes

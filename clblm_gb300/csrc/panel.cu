@@ -740,6 +740,44 @@ template __global__ void k_panel<true>(PanelArgs);
 // reference's order (record order); the mixed path keeps four FP32 partial
 // sums per chunk (alternate records) and adds each chunk's total into a Kahan
 // sum.
+// FP32 terms of far-wing record r at a thread's two points (packed FP32x2):
+// Core: the point may lie within 64 ALFV of the line (the polynomial core of
+// CNVF4Q), else the Lorentzian wing is certain; Mask: the record's point
+// range [jmin, jmax] may exclude a point.
+template <bool Core, bool Mask>
+__device__ __forceinline__ float2 f4_term(const F4Rec& r, float2 Jm1, float2 dvr4, int JA, int JB) {
+  const float2 xm = __ffma2_rn(__fadd2_rn(Jm1, r.nmc), dvr4, r.x0);
+  const float2 xmsq = __fmul2_rn(xm, xm);
+  const float2 nfb = __ffma2_rn(xmsq, r.fb2, r.nfb0);
+  const float2 den = __fadd2_rn(xmsq, r.al2);
+  float2 f = make_float2(__fdividef(r.sil.x, den.x), __fdividef(r.sil.y, den.y));
+  if constexpr (Core) {
+    const float2 zvsq = __fmul2_rn(xmsq, r.ralv2);
+    const float2 core = __ffma2_rn(zvsq, r.sb3, r.sa3);
+    f.x = zvsq.x <= 4096.f ? core.x : f.x;
+    f.y = zvsq.y <= 4096.f ? core.y : f.y;
+  }
+  f = __fadd2_rn(f, nfb);
+  if constexpr (Mask) {
+    f.x = (JA >= r.jmin && JA <= r.jmax) ? f.x : 0.f;
+    f.y = (JB >= r.jmin && JB <= r.jmax) ? f.y : 0.f;
+  }
+  return f;
+}
+
+// Sum of the records S[0, cnt) at both points, two records per step
+template <bool Core, bool Mask>
+__device__ __forceinline__ float2 f4_chunk(const F4Rec* S, int cnt, float2 Jm1, float2 dvr4, int JA, int JB) {
+  float2 p0 = make_float2(0.f, 0.f), p1 = p0;
+  int k = 0;
+  for (; k + 2 <= cnt; k += 2) {
+    p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], Jm1, dvr4, JA, JB));
+    p1 = __fadd2_rn(p1, f4_term<Core, Mask>(S[k + 1], Jm1, dvr4, JA, JB));
+  }
+  if (k < cnt) p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], Jm1, dvr4, JA, JB));
+  return __fadd2_rn(p0, p1);
+}
+
 template <bool Plain>
 __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
   using Real = typename std::conditional<Plain, double, float>::type;
@@ -817,24 +855,6 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
     if (ZVSQ <= ZSQBND) return (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb;
     return d.sil / (d.al2 + XMSQ) - fb;
   };
-  // FP32 terms of record r at both points (packed FP32x2), before the range test
-  auto shape_f = [&](const F4Rec& r) -> float2 {
-    const float2 xm = __ffma2_rn(__fadd2_rn(Jm1, r.nmc), dvr4, r.x0);
-    const float2 xmsq = __fmul2_rn(xm, xm);
-    const float2 zvsq = __fmul2_rn(xmsq, r.ralv2);
-    const float2 nfb = __ffma2_rn(xmsq, r.fb2, r.nfb0);
-    const float2 core = __ffma2_rn(zvsq, r.sb3, r.sa3);
-    const float2 den = __fadd2_rn(xmsq, r.al2);
-    float2 f = make_float2(zvsq.x <= 4096.f ? core.x : __fdividef(r.sil.x, den.x),
-                           zvsq.y <= 4096.f ? core.y : __fdividef(r.sil.y, den.y));
-    return __fadd2_rn(f, nfb);
-  };
-  auto term_f = [&](const F4Rec& r) -> float2 {
-    float2 f = shape_f(r);
-    f.x = (JA >= r.jmin && JA <= r.jmax) ? f.x : 0.f;
-    f.y = (JB >= r.jmin && JB <= r.jmax) ? f.y : 0.f;
-    return f;
-  };
   const int tJlo = (int)m0 + 1;
   const int tJhi = (int)(m0 + kF4Tile < P.nptr4 ? m0 + kF4Tile : P.nptr4);
   for (int64_t c = 0; c < nchunk; ++c) {
@@ -863,26 +883,28 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
       }
     }
     if constexpr (!Plain) {
-      // a chunk whose records all span the tile's live points needs no range test
-      bool cov = true;
-      for (int k = threadIdx.x; k < cnt; k += kF4Threads) cov &= (S[k].jmin <= tJlo && S[k].jmax >= tJhi);
+      // A chunk whose records all span the tile's live points needs no range
+      // test.  One whose records all keep the tile beyond 64.064 ALFV (the
+      // tile's offsets from each line are monotone in J, so its end points
+      // bound them) takes the wing branch at every point: ZVSQ > 4096 with a
+      // margin well above the FP32 rounding of ZVSQ.
+      bool cov = true, wing = true;
+      for (int k = threadIdx.x; k < cnt; k += kF4Threads) {
+        const F4Rec& r = S[k];
+        cov &= (r.jmin <= tJlo && r.jmax >= tJhi);
+        const float xlo = fmaf((float)(tJlo - 1) + r.nmc.x, dvr4f, r.x0.x);
+        const float xhi = fmaf((float)(tJhi - 1) + r.nmc.x, dvr4f, r.x0.x);
+        const float c = 64.064f * rsqrtf(r.ralv2.x);
+        wing &= (xlo > c) || (xhi < -c);
+      }
       const bool full = __syncthreads_and(cov);
+      const bool wonly = __syncthreads_and(wing);
       if (liveA) {
-        float2 p0 = make_float2(0.f, 0.f), p1 = p0;
-        int k = 0;
-        if (full) {
-          for (; k + 2 <= cnt; k += 2) {
-            p0 = __fadd2_rn(p0, shape_f(S[k]));
-            p1 = __fadd2_rn(p1, shape_f(S[k + 1]));
-          }
-        } else {
-          for (; k + 2 <= cnt; k += 2) {
-            p0 = __fadd2_rn(p0, term_f(S[k]));
-            p1 = __fadd2_rn(p1, term_f(S[k + 1]));
-          }
-        }
-        if (k < cnt) p0 = __fadd2_rn(p0, term_f(S[k]));
-        const float2 t = __fadd2_rn(p0, p1);
+        float2 t;
+        if (full) t = wonly ? f4_chunk<false, false>(S, cnt, Jm1, dvr4, JA, JB)
+                            : f4_chunk<true, false>(S, cnt, Jm1, dvr4, JA, JB);
+        else t = wonly ? f4_chunk<false, true>(S, cnt, Jm1, dvr4, JA, JB)
+                       : f4_chunk<true, true>(S, cnt, Jm1, dvr4, JA, JB);
         kA.add(t.x);
         kB.add(t.y);
       }
@@ -917,7 +939,7 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
       for (int64_t i = n; i < n + nm; ++i) {
         const F4Rec& r = recs[i];
         if (J < r.jmin || J > r.jmax) continue;
-        const float2 t = term_f(r);  // lane x is point A, lane y point B
+        const float2 t = f4_term<true, true>(r, Jm1, dvr4, JA, JB);  // lane x is point A, lane y point B
         acc.add(q == 0 ? t.x : t.y);
       }
       R4[m] = acc.value();

@@ -283,7 +283,8 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
                                GridRec* __restrict__ rec, GridRecD* __restrict__ recd,
                                GridRecLo* __restrict__ reclo, const double* __restrict__ vnu_raw,
                                unsigned long long* __restrict__ stats,
-                               double* __restrict__ alfvmax) {
+                               double* __restrict__ alfvmax, int* __restrict__ aggmax, int* __restrict__ aggmin,
+                               int nagg) {
   int layer = blockIdx.y;
   const LayerPlan& P = plans[layer + layer0];
   int64_t n = P.line_hi - P.line_lo + 1;
@@ -297,9 +298,14 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
   double amax = 0.;
   unsigned long long bad = 0;
   unsigned long long steps = 0;  // CNVFNQ inner steps JMAX1-JMIN1+1 of the accepted lines
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    const LinePrep lp = prep[layer * stride + t];
-    int q = qpanel[layer * stride + t];
+  __shared__ int red[3][2][kRecBlock / 32];
+  // block-uniform loop: block b handles lines [kRecBlock*b', +kRecBlock) and
+  // writes their running-bound aggregates (max g_hi, min g_lo per grid)
+  for (int64_t base = blockIdx.x * (int64_t)kRecBlock; base < n; base += (int64_t)gridDim.x * kRecBlock) {
+    const int64_t t = base + threadIdx.x;
+    const bool live = t < n;
+    const LinePrep lp = live ? prep[layer * stride + t] : LinePrep{};
+    int q = live ? qpanel[layer * stride + t] : 0;
     GridRec g1, g2, g3;
     g1.g_lo = g2.g_lo = g3.g_lo = 1;
     g1.g_hi = g2.g_hi = g3.g_hi = 0;  // empty
@@ -309,7 +315,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
     g1.a0 = g1.a1 = g1.a2 = g2.a0 = g2.a1 = g2.a2 = g3.a0 = g3.a1 = g3.a2 = 0.f;
     GridRecD d1 = {0, 0, 0, 0, 0}, d2 = d1, d3 = d1;
     GridRecLo l1 = {0.f, 0.f}, l2 = l1, l3 = l1;
-    if (lp.fpanel >= 0 && q < P.npanels) {
+    if (live && lp.fpanel >= 0 && q < P.npanels) {
       // a line of a later record is read in the panel the previous record
       // ended in; dropping it there (HWF3*ALFV + VNU < VFT) is not modelled
       int64_t gi = P.line_lo + t;
@@ -383,16 +389,47 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
       amax = fmax(amax, 1. / lp.recalf);
     }
-    int64_t o = (int64_t)layer * stride * 3;
-    rec[o + t] = g1;
-    rec[o + stride + t] = g2;
-    rec[o + 2 * stride + t] = g3;
-    recd[o + t] = d1;
-    recd[o + stride + t] = d2;
-    recd[o + 2 * stride + t] = d3;
-    reclo[o + t] = l1;
-    reclo[o + stride + t] = l2;
-    reclo[o + 2 * stride + t] = l3;
+    if (live) {
+      int64_t o = (int64_t)layer * stride * 3;
+      rec[o + t] = g1;
+      rec[o + stride + t] = g2;
+      rec[o + 2 * stride + t] = g3;
+      recd[o + t] = d1;
+      recd[o + stride + t] = d2;
+      recd[o + 2 * stride + t] = d3;
+      reclo[o + t] = l1;
+      reclo[o + stride + t] = l2;
+      reclo[o + 2 * stride + t] = l3;
+    }
+    {
+      const GridRec* gg[3] = {&g1, &g2, &g3};
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int k = 0; k < 3; ++k) {
+        const bool ne = gg[k]->g_hi >= gg[k]->g_lo;  // empty records do not bound
+        int mx = ne ? gg[k]->g_hi : -1, mn = ne ? gg[k]->g_lo : kRecNone;
+        for (int off = 16; off > 0; off >>= 1) {
+          mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+          mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+        }
+        if (lane == 0) {
+          red[k][0][warp] = mx;
+          red[k][1][warp] = mn;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        int mx = -1, mn = kRecNone;
+        for (int w = 0; w < kRecBlock / 32; ++w) {
+          mx = max(mx, red[k][0][w]);
+          mn = min(mn, red[k][1][w]);
+        }
+        const int64_t a = ((int64_t)layer * 3 + k) * nagg + base / kRecBlock;
+        aggmax[a] = mx;
+        aggmin[a] = mn;
+      }
+      __syncthreads();
+    }
   }
   for (int off = 16; off > 0; off >>= 1) amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, off));
   unsigned long long b = bad;
@@ -1190,55 +1227,107 @@ __global__ void k_f4_bounds(const F4Rec* __restrict__ rec, int64_t rstride, cons
 // g_lo from the right over the convolution records, so that the records that
 // touch a range [g0, g1] of grid points form the contiguous index range found
 // by two binary searches.  Empty records (g_hi < g_lo) touch nothing.
-__global__ void k_rec_bounds(const LayerPlan* __restrict__ plans, int layer0, const GridRec* __restrict__ rec,
-                             int64_t stride, int* __restrict__ pmax, int* __restrict__ smin) {
-  const int layer = blockIdx.x / 3, grid = blockIdx.x % 3;
+// Running bounds of each grid's records in record order: pm[i] = max g_hi
+// over records 0..i, sm[i] = min g_lo over records i..n-1 (empty records are
+// skipped).  The 256-record block aggregates come from k_line_records; one
+// CTA per (layer, grid) turns them into exclusive carries, then one CTA per
+// block scans its records with the carries.
+__global__ void k_rec_carry(const LayerPlan* __restrict__ plans, int layer0, int* __restrict__ aggmax,
+                            int* __restrict__ aggmin, int nagg) {
+  const int layer = blockIdx.x / 3;
   const LayerPlan& P = plans[layer + layer0];
   const int64_t n = P.line_hi - P.line_lo + 1;
-  const int64_t o = ((int64_t)layer * 3 + grid) * stride;
-  const GridRec* R = rec + o;
-  int* pm = pmax + o;
-  int* sm = smin + o;
-  const int T = blockDim.x;
-  const int64_t chunk = (n + T - 1) / T;
-  const int64_t b = threadIdx.x * chunk, e = min(n, b + chunk);
-  __shared__ int shmax[1024], shmin[1024];
-  const int kNone = 0x7fffffff;
-  int mx = -1, mn = kNone;
-  for (int64_t i = b; i < e; ++i) {
-    const int lo = R[i].g_lo, hi = R[i].g_hi;
-    if (hi >= lo) {
-      mx = max(mx, hi);
-      mn = min(mn, lo);
+  const int nb = (int)((n + kRecBlock - 1) / kRecBlock);
+  int* am = aggmax + (int64_t)blockIdx.x * nagg;
+  int* an = aggmin + (int64_t)blockIdx.x * nagg;
+  __shared__ int wt[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // exclusive prefix max, chunk by chunk
+  int carry = -1;
+  for (int c0 = 0; c0 < nb; c0 += blockDim.x) {
+    const int i = c0 + threadIdx.x;
+    const int v = i < nb ? am[i] : -1;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x = max(x, y);
+    }
+    if (lane == 31) wt[warp] = x;
+    __syncthreads();
+    int pre = carry;
+    for (int w = 0; w < warp; ++w) pre = max(pre, wt[w]);
+    int ex = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) ex = -1;
+    if (i < nb) am[i] = max(pre, ex);
+    int tot = carry;
+    for (int w = 0; w < nw; ++w) tot = max(tot, wt[w]);
+    __syncthreads();
+    carry = tot;
+  }
+  // exclusive suffix min, chunk by chunk from the end
+  carry = kRecNone;
+  for (int c1 = nb; c1 > 0; c1 -= blockDim.x) {
+    const int i = c1 - 1 - threadIdx.x;  // thread 0 takes the last element of the chunk
+    const int v = i >= 0 ? an[i] : kRecNone;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x = min(x, y);
+    }
+    if (lane == 31) wt[warp] = x;
+    __syncthreads();
+    int pre = carry;
+    for (int w = 0; w < warp; ++w) pre = min(pre, wt[w]);
+    int ex = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) ex = kRecNone;
+    if (i >= 0) an[i] = min(pre, ex);
+    int tot = carry;
+    for (int w = 0; w < nw; ++w) tot = min(tot, wt[w]);
+    __syncthreads();
+    carry = tot;
+  }
+}
+
+__global__ void __launch_bounds__(kRecBlock)
+    k_rec_bounds(const LayerPlan* __restrict__ plans, int layer0, const GridRec* __restrict__ rec, int64_t stride,
+                 const int* __restrict__ aggmax, const int* __restrict__ aggmin, int nagg, int* __restrict__ pmax,
+                 int* __restrict__ smin) {
+  const int layer = blockIdx.y / 3;
+  const LayerPlan& P = plans[layer + layer0];
+  const int64_t n = P.line_hi - P.line_lo + 1;
+  const int64_t base = (int64_t)blockIdx.x * kRecBlock;
+  if (base >= n) return;
+  const int64_t o = (int64_t)blockIdx.y * stride;
+  const int64_t i = base + threadIdx.x;
+  const bool live = i < n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ int wmax[kRecBlock / 32], wmin[kRecBlock / 32];
+  int hi = -1, lo = kRecNone;
+  if (live) {
+    const GridRec r = rec[o + i];
+    if (r.g_hi >= r.g_lo) {
+      hi = r.g_hi;
+      lo = r.g_lo;
     }
   }
-  shmax[threadIdx.x] = mx;
-  shmin[threadIdx.x] = mn;
+  // inclusive prefix max within the warp, inclusive suffix min within the warp
+  int x = hi, y = lo;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int a = __shfl_up_sync(0xffffffffu, x, d);
+    const int b = __shfl_down_sync(0xffffffffu, y, d);
+    if (lane >= d) x = max(x, a);
+    if (lane + d < 32) y = min(y, b);
+  }
+  if (lane == 31) wmax[warp] = x;
+  if (lane == 0) wmin[warp] = y;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = -1;
-    for (int t = 0; t < T; ++t) {
-      int v = shmax[t];
-      shmax[t] = run;  // exclusive prefix max
-      run = max(run, v);
-    }
-    run = kNone;
-    for (int t = T - 1; t >= 0; --t) {
-      int v = shmin[t];
-      shmin[t] = run;  // exclusive suffix min
-      run = min(run, v);
-    }
-  }
-  __syncthreads();
-  int run = shmax[threadIdx.x];
-  for (int64_t i = b; i < e; ++i) {
-    if (R[i].g_hi >= R[i].g_lo) run = max(run, R[i].g_hi);
-    pm[i] = run;
-  }
-  run = shmin[threadIdx.x];
-  for (int64_t i = e - 1; i >= b; --i) {
-    if (R[i].g_hi >= R[i].g_lo) run = min(run, R[i].g_lo);
-    sm[i] = run;
+  int cm = aggmax[(int64_t)blockIdx.y * nagg + blockIdx.x];
+  for (int w = 0; w < warp; ++w) cm = max(cm, wmax[w]);
+  int cn = aggmin[(int64_t)blockIdx.y * nagg + blockIdx.x];
+  for (int w = warp + 1; w < kRecBlock / 32; ++w) cn = min(cn, wmin[w]);
+  if (live) {
+    pmax[o + i] = max(cm, x);
+    smin[o + i] = min(cn, y);
   }
 }
 

@@ -80,7 +80,7 @@ struct clblm_handle {
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
   DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
   DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
-  DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt;
+  DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt, ragg;
   DevBuf rt[4], outbuf, imap[2];
   std::string errmsg;
   clblm_od_stats_t last{};
@@ -774,14 +774,20 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   h->launches++;
   k_scan_apply<<<dim3(nblk, count), 256, 0, st>>>(h->prep.as<LinePrep>(), lstride, h->nlines_d.as<int64_t>() + first,
                                                    h->blockmax.as<int>(), nblk, h->qpanel.as<int>());
+  const int nagg = (int)((lstride + kRecBlock - 1) / kRecBlock);
   h->launches++;
-  k_line_records<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
+  k_line_records<<<dim3((unsigned)std::min<int64_t>(nagg, 8192), count), kRecBlock, 0, st>>>(
       dplans, first, h->vft.as<double>(), h->prep.as<LinePrep>(), h->qpanel.as<int>(), lstride, h->rec.as<GridRec>(),
       h->recd.as<GridRecD>(), h->reclo.as<GridRecLo>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(),
-      h->alfvmax.as<double>());
+      h->alfvmax.as<double>(), h->ragg.as<int>(), h->ragg.as<int>() + (int64_t)3 * count * nagg, nagg);
   h->launches++;
-  k_rec_bounds<<<3 * count, 1024, 0, st>>>(dplans, first, h->rec.as<GridRec>(), lstride, h->gpm.as<int>(),
-                                           h->gsm.as<int>());
+  k_rec_carry<<<3 * count, 1024, 0, st>>>(dplans, first, h->ragg.as<int>(),
+                                          h->ragg.as<int>() + (int64_t)3 * count * nagg, nagg);
+  h->launches++;
+  k_rec_bounds<<<dim3(nagg, 3 * count), kRecBlock, 0, st>>>(dplans, first, h->rec.as<GridRec>(), lstride,
+                                                            h->ragg.as<int>(),
+                                                            h->ragg.as<int>() + (int64_t)3 * count * nagg, nagg,
+                                                            h->gpm.as<int>(), h->gsm.as<int>());
   int maxp = 0;
   for (int k = 0; k < count; ++k) maxp = std::max(maxp, hps[first + k].P.npanels);
   h->launches++;
@@ -876,6 +882,7 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
   CUDA_TRY(h, h->gpm.ensure(sizeof(int) * ls * 3 * count));
   CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * ls * 3 * count));
   CUDA_TRY(h, h->gsm.ensure(sizeof(int) * ls * 3 * count));
+  CUDA_TRY(h, h->ragg.ensure(sizeof(int) * 2 * 3 * count * ((ls + kRecBlock - 1) / kRecBlock)));
   CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * ps * count));
   CUDA_TRY(h, h->od.ensure(real * odt));
   CUDA_TRY(h, h->r4.ensure(real * r4t));
@@ -1107,7 +1114,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->f4nxt,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
+                    &h->f4cut,     &h->f4grp,    &h->f4nxt,   &h->ragg,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
                     &h->jblk};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
