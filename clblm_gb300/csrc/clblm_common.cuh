@@ -38,6 +38,7 @@ constexpr int kTIPSNMOL = 9;
 struct LayerPlan {
   // grid
   double v1, v2, dv, dvr2, dvr3, alfav, alfmax, bound, vbot, vtop, vft0;
+  double wavdxf, rdv;             // DV/DXF1 (CNVFNQ's WAVDXF) and 1/DV (estimates only)
   double pave, tave, wtot, xkt, xkt0, betacr, tratio, rhorat, pavp0, pavp2;
   double ln_tratio;               // log(T/296): (T/296)^n = exp(n log(T/296))
   int mixed;                      // 1: FP32 for strengths and shape coefficients
@@ -75,6 +76,8 @@ struct LinePrep {
   double vnu;      // shifted centre
   double sp;       // SP(I) after the T correction
   double recalf;   // 1 / ALFV
+  double alfv;     // ALFV
+  double bhwdxf;   // BHWDXF = HWDXF / ZSLOPE of CNVFNQ
   double zetai;
   int iz;          // IZETA
   int fpanel;      // first panel whose MAX1 fits the line (-1: rejected)

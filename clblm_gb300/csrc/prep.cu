@@ -53,11 +53,18 @@ __device__ __forceinline__ float radfn_f(float XVI, float XKT) {
   return XVI;
 }
 
-// Does panel p (origin vft) take the line: JMAX1 <= MAX1 (CNVFNQ :2176-2181).
-__device__ __forceinline__ bool fits_panel(double vnu, double vft, double dv, double bhwdxf, int max1) {
-  double ZINT = (vnu - vft) / dv;
-  int JMAX1 = (int)(ZINT + bhwdxf + 1.5);
-  return JMAX1 <= max1;
+// Does panel p (origin vft) take the line: JMAX1 <= MAX1 (CNVFNQ :2176-2181),
+// JMAX1 = INT(ZINT + BHWDXF + 1.5) with ZINT = (VNU - VFT)/DV.  The quotient
+// is first formed with the reciprocal of DV, which stays within a few units
+// in the last place of the exact quotient (about 5e-16 |a|); only when the
+// argument lies within 1e-12 + 1e-13 |a| of an integer, where truncation
+// could differ, is it redone with the reference's division.
+__device__ __forceinline__ bool fits_panel(double vnu, double vft, double dv, double rdv, double bhwdxf, int max1) {
+  const double d = vnu - vft;
+  double a = d * rdv + bhwdxf + 1.5;
+  const double fl = floor(a), tol = 1e-12 + 1e-13 * fabs(a);
+  if (a - fl < tol || fl + 1. - a < tol) a = d / dv + bhwdxf + 1.5;
+  return (int)a <= max1;
 }
 
 __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
@@ -74,6 +81,8 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     r.vnu = 0.;
     r.sp = 0.;
     r.recalf = 0.;
+    r.alfv = 0.;
+    r.bhwdxf = 0.;
     r.zetai = 0.;
     r.iz = 0;
     r.fpanel = -1;
@@ -157,16 +166,17 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             r.recalf = RECALF;
             r.zetai = ZETA;
             r.iz = IZ;
-            // first panel p with JMAX1 <= MAX1
-            double WAVDXF = P.dv / kDXF1;
+            // first panel p with JMAX1 <= MAX1 (the estimate only starts the search)
             double HWDXF = kHWF1 / kDXF1;
-            double ZSLOPE = RECALF * WAVDXF;
+            double ZSLOPE = RECALF * P.wavdxf;
             double BHWDXF = HWDXF / ZSLOPE;
-            double est = ((VNU - vft[0]) / P.dv + BHWDXF + 1.5 - (double)P.max1) / (double)kPanelPts;
+            r.alfv = ALFV;
+            r.bhwdxf = BHWDXF;
+            double est = ((VNU - vft[0]) * P.rdv + BHWDXF + 1.5 - (double)P.max1) * (1. / kPanelPts);
             int p = est > 0. ? (int)est : 0;
             if (p > P.npanels) p = P.npanels;
-            while (p > 0 && fits_panel(VNU, vft[p - 1], P.dv, BHWDXF, P.max1)) p--;
-            while (p < P.npanels && !fits_panel(VNU, vft[p], P.dv, BHWDXF, P.max1)) p++;
+            while (p > 0 && fits_panel(VNU, vft[p - 1], P.dv, P.rdv, BHWDXF, P.max1)) p--;
+            while (p < P.npanels && !fits_panel(VNU, vft[p], P.dv, P.rdv, BHWDXF, P.max1)) p++;
             r.fpanel = p;  // == npanels: never convolved
           }
         }
@@ -323,8 +333,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
         int64_t rs = (gi / 250) * 250;  // first line of this line's record
         int qr = 0;
         if (rs - 1 >= P.line_lo) qr = max(0, qpanel[layer * stride + (rs - 1 - P.line_lo)]);
-        double alfv = 1. / lp.recalf;
-        if (qr > 0 && qr < P.npanels && kHWF3 * alfv + lp.vnu < vft[qr]) bad++;
+        if (qr > 0 && qr < P.npanels && kHWF3 * lp.alfv + lp.vnu < vft[qr]) bad++;
       }
       double DEPTHA = lp.sp * lp.recalf;
       int IZM = lp.iz;
@@ -351,7 +360,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       }
       double ZSLOPE = lp.recalf * WAVDXF;
       double ZINT = (lp.vnu - vft[q]) / P.dv;
-      double BHWDXF = HWDXF / ZSLOPE;
+      double BHWDXF = lp.bhwdxf;  // HWDXF / ZSLOPE
       int JMAX1 = (int)(ZINT + BHWDXF + 1.5);
       int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
       if (JMAX1 >= JMIN1) steps += (unsigned long long)(JMAX1 - JMIN1 + 1);
@@ -387,7 +396,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       l1 = {(float)(ZF1L - (double)g1.zfl), zs_lo};
       l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
       l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
-      amax = fmax(amax, 1. / lp.recalf);
+      amax = fmax(amax, lp.alfv);
     }
     if (live) {
       int64_t o = (int64_t)layer * stride * 3;

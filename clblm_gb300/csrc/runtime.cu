@@ -429,6 +429,8 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.v1 = V1;
   P.v2 = V2;
   P.dv = DV;
+  P.wavdxf = DV / kDXF1;
+  P.rdv = 1. / DV;
   P.dvr2 = (kDXF2 / kDXF1) * DV;
   P.dvr3 = (kDXF3 / kDXF1) * DV;
   P.alfav = ALFAV;
