@@ -22,7 +22,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_gpu_stream",
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
-           "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc")
+           "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -67,6 +67,9 @@ def lib():
                                          P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_jac.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + \
             [C.c_void_p] * 5 + [C.c_int64, C.c_int32]
+        L.clblm_gpu_batch_size.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t),
+                                           P(C.c_int64), P(C.c_double)]
+        L.clblm_gpu_batch.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t), C.c_int32]
         L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
                                        P(C.c_int64), C.c_char_p, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
@@ -200,6 +203,65 @@ def _jac_methods():
 
 
 Handle.jac_size, Handle.jac, Handle.jac_device = _jac_methods()
+
+
+def _profiles(cols, jacs):
+    arr = (T.clblm_profile_t * len(cols))()
+    keep = []
+    for i, (c, j) in enumerate(zip(cols, jacs)):
+        cs, js = c.struct(), j.struct()
+        keep += [cs, js]
+        arr[i].col = C.pointer(cs)
+        arr[i].jac = C.pointer(js)
+    return arr, keep
+
+
+def _batch_methods():
+    def batch_size(self, cols, ctrl, jacs):
+        """Points and DVout of every profile's spectra."""
+        arr, keep = _profiles(cols, jacs)
+        n = len(cols)
+        npts, dv = (C.c_int64 * n)(), (C.c_double * n)()
+        self._check(lib().clblm_gpu_batch_size(self.h, arr, n, C.byref(ctrl), npts, dv))
+        return list(npts), list(dv)
+
+    def batch(self, cols, ctrl, jacs):
+        """Radiance and Jacobians of many profiles in one call (the scene loop
+        of the reference's main program): a list of dicts as Handle.jac."""
+        npts, dvs = self.batch_size(cols, ctrl, jacs)
+        arr, keep = _profiles(cols, jacs)
+        outs = []
+        for i, c in enumerate(cols):
+            n, nl = npts[i], c.nlay
+            o = {"rad": np.empty(n), "dtsfc": np.empty(n), "demis": np.empty(n),
+                 "dtlev": np.empty((nl + 1, n)), "dqlev": np.empty((nl + 1, n)), "v1": c.v1, "dv": dvs[i]}
+            for f, k in (("rad", "rad"), ("dr_dtlev", "dtlev"), ("dr_dqlev", "dqlev"), ("dr_dtskin", "dtsfc"),
+                         ("dr_demis", "demis")):
+                setattr(arr[i], f, o[k].ctypes.data_as(C.POINTER(C.c_double)))
+            arr[i].cap = n
+            outs.append(o)
+        self._check(lib().clblm_gpu_batch(self.h, arr, len(cols), C.byref(ctrl), T.CLBLM_OUT_HOST))
+        return outs
+
+    def batch_device(self, cols, ctrl, jacs, outs, graph=False):
+        """The same into device buffers: outs[i] = dict of device addresses
+        (rad, dtlev, dqlev, dtsfc, demis; 0 for none) and cap; with graph=True
+        the launches are captured once and replayed for the same batch.
+        Returns the per-profile status codes."""
+        arr, keep = _profiles(cols, jacs)
+        for i, o in enumerate(outs):
+            for f, k in (("rad", "rad"), ("dr_dtlev", "dtlev"), ("dr_dqlev", "dqlev"), ("dr_dtskin", "dtsfc"),
+                         ("dr_demis", "demis")):
+                setattr(arr[i], f, C.cast(C.c_void_p(o.get(k) or None), C.POINTER(C.c_double)))
+            arr[i].cap = o["cap"]
+        flags = T.CLBLM_OUT_DEVICE | (T.CLBLM_BATCH_GRAPH if graph else 0)
+        self._check(lib().clblm_gpu_batch(self.h, arr, len(cols), C.byref(ctrl), flags))
+        return [arr[i].status for i in range(len(cols))]
+
+    return batch_size, batch, batch_device
+
+
+Handle.batch_size, Handle.batch, Handle.batch_device = _batch_methods()
 
 
 def noScattJacob(handle, col, ctrl, jac):

@@ -71,6 +71,15 @@ class clblm_jac_t(C.Structure):
     _fields_ = [("plev", _dp), ("qlev", _dp), ("jac_mol", C.c_int32), ("do_temp", C.c_int32)]
 
 
+class clblm_profile_t(C.Structure):
+    _fields_ = [("col", C.POINTER(clblm_column_t)), ("jac", C.POINTER(clblm_jac_t)),
+                ("rad", _dp), ("dr_dtlev", _dp), ("dr_dqlev", _dp), ("dr_dtskin", _dp), ("dr_demis", _dp),
+                ("cap", C.c_int64), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
+CLBLM_BATCH_GRAPH = 0x10
+
+
 class JacProfile:
     """Level pressures and Jacobian-molecule mixing ratios (level 0 at the
     surface) and the clblm_jac_t view of them."""

@@ -11,15 +11,20 @@ namespace clblm {
 constexpr int kMaxJacLayers = 128;
 
 // One layer OD of a Jacobian block: where the OD pipeline left it, how it
-// maps onto the block's uniform grid, and its slot (variant * nlay + layer)
-// in the block's OD array.
+// maps onto its block's uniform grid, and where its row of the block's OD
+// array [variant][layer][point] lies.  Jobs of several blocks (of several
+// profiles) can share one launch.
 struct JacJob {
-  InterpSpec spec;   // layer grid -> uniform grid (map: general ratio)
-  int2* map;         // per-point (iIn, IP) of a general-ratio spec
-  int64_t od_off;    // OD of the layer in the pipeline's OD buffer (Real)
-  int64_t n_in;      // points of the layer OD
-  int slot;
-  int build_map;     // 1: this job builds the map (other jobs of the layer read it)
+  InterpSpec spec;        // layer grid -> uniform grid (map: general ratio)
+  int2* map;              // per-point (iIn, IP) of a general-ratio spec
+  const int64_t* blk_j1;  // the block's interpolation blocks (start J1, wavenumber Vo)
+  const double* blk_vo;
+  int64_t od_off;         // OD of the layer in the pipeline's OD buffer (Real)
+  int64_t n_in;           // points of the layer OD
+  int64_t nout;           // points of the block
+  int64_t dst_off;        // first element of the job's row in the output (Real)
+  int nblk;               // interpolation blocks of the block
+  int build_map;          // 1: this job builds the map (other jobs of the layer read it)
 };
 
 struct JacArgs {
@@ -35,10 +40,9 @@ struct JacArgs {
   int64_t off;             // first output point of the block
 };
 
-__global__ void k_interp_map_jobs(const JacJob* jobs, int njob, const int64_t* blk_j1, const double* blk_vo,
-                                  int nblk, int64_t nout);
+__global__ void k_interp_map_jobs(const JacJob* jobs, int njob);
 template <bool Plain>
-__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, int64_t nout, void* out);
+__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out);
 template <bool Plain>
 __global__ void k_jac(JacArgs a);
 

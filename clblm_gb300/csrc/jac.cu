@@ -24,15 +24,17 @@
 
 namespace clblm {
 
-__global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob, const int64_t* __restrict__ blk_j1,
-                                  const double* __restrict__ blk_vo, int nblk, int64_t nout) {
+// grid (blocks of 64 interpolation blocks, jobs); each job its own block list
+__global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob) {
   const int j = blockIdx.y;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= njob || b >= nblk) return;
+  if (j >= njob || b >= jobs[j].nblk) return;
   const InterpSpec& s = jobs[j].spec;
   if (!jobs[j].build_map) return;
   int2* map = jobs[j].map;
-  const double Vo = blk_vo[b];
+  const int64_t* blk_j1 = jobs[j].blk_j1;
+  const int64_t nout = jobs[j].nout;
+  const double Vo = jobs[j].blk_vo[b];
   int64_t iIn = (int64_t)__dadd_rn(__ddiv_rn(__dadd_rn(Vo, -s.v1), s.dvin), 1.00001);
   double Vi = __dadd_rn(s.v1, __dmul_rn((double)(iIn - 1), s.dvin));
   double P = __ddiv_rn(__dadd_rn(Vo, -Vi), s.dvin);
@@ -58,13 +60,15 @@ __device__ __forceinline__ Real od_ext_t(const Real* x, int64_t n, int64_t i) {
   return (Real)0;
 }
 
+// grid (points of the longest block, jobs)
 template <bool Plain>
-__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, int64_t nout, void* out) {
+__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out) {
   using Real = typename std::conditional<Plain, double, float>::type;
   const int j = blockIdx.y;
   const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (j >= njob || I > nout) return;
+  if (j >= njob) return;
   const JacJob& jb = jobs[j];
+  if (I > jb.nout) return;
   const Real* x = reinterpret_cast<const Real*>(od_all) + jb.od_off;
   const Stencil<Real> st = interp_stencil<Real>(jb.spec, I);  // FP32 weights in the mixed path
   Real v = 0;
@@ -72,11 +76,11 @@ __global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, int6
   else
 #pragma unroll
     for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext_t(x, jb.n_in, st.i[k]);
-  reinterpret_cast<Real*>(out)[(int64_t)jb.slot * nout + (I - 1)] = v;
+  reinterpret_cast<Real*>(out)[jb.dst_off + (I - 1)] = v;
 }
 
-template __global__ void k_od_jobs<false>(const JacJob*, int, const void*, int64_t, void*);
-template __global__ void k_od_jobs<true>(const JacJob*, int, const void*, int64_t, void*);
+template __global__ void k_od_jobs<false>(const JacJob*, int, const void*, void*);
+template __global__ void k_od_jobs<true>(const JacJob*, int, const void*, void*);
 
 // ---- the per-point recurrence (Jacobians, down-looking branch) ------------
 template <typename Real>

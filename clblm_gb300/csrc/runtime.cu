@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -32,11 +34,16 @@ namespace {
 
 thread_local std::string g_create_err;
 
+// bumped whenever a device buffer is freed or moved: a captured launch
+// sequence that holds buffer addresses is only replayed while it is unchanged
+std::atomic<uint64_t> g_buf_gen{0};
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
   cudaError_t ensure(size_t n) {
     if (n <= bytes) return cudaSuccess;
+    g_buf_gen++;
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
@@ -46,7 +53,10 @@ struct DevBuf {
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      g_buf_gen++;
+      cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -57,6 +67,10 @@ struct DevBuf {
 };
 
 }  // namespace
+
+namespace {
+struct BatchGraph;
+}
 
 struct clblm_handle {
   int device = 0;
@@ -82,6 +96,10 @@ struct clblm_handle {
   DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt, ragg;
   DevBuf rt[4], outbuf, imap[2];
+  // batched profiles: captured launch sequences of recent batches
+  std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
+  uint64_t bgraph_clock = 0;
+  bool panel_attr_set[2] = {false, false};
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
@@ -829,12 +847,18 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
   size_t smem = panel_smem_bytes(plain);
   if (plain) {
-    CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (!h->panel_attr_set[1]) {
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      h->panel_attr_set[1] = true;
+    }
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
     k_panel<true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
   } else {
-    CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (!h->panel_attr_set[0]) {
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      h->panel_attr_set[0] = true;
+    }
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
     k_panel<false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
@@ -844,10 +868,35 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   return CLBLM_OK;
 }
 
-// Sizes the workspace for layers [first, first+count) and uploads their plans.
-int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t* lstride,
-                  int64_t* f4stride, int64_t* pstride, int64_t* od_total) {
-  int64_t ls = 1, fs = 1, ps = 1, odt = 0, r4t = 0, vftt = 0;
+// Per-batch workspace sizes: products of the batch's strides and layer count.
+struct WsDims {
+  int64_t lsc = 0;     // line stride x layers
+  int64_t fsc = 0;     // far-wing line stride x layers
+  int64_t psc = 0;     // panels x layers
+  int64_t cnt = 0;     // layers
+  int64_t odt = 0;     // OD points (padded)
+  int64_t r4t = 0;     // R4 points (padded)
+  int64_t nblk4c = 0;  // far-wing scan blocks x layers
+  int64_t smaxc = 0;   // first-fit scan blocks x layers
+  int64_t raggc = 0;   // record-bound aggregates
+  void max_with(const WsDims& o) {
+    lsc = std::max(lsc, o.lsc);
+    fsc = std::max(fsc, o.fsc);
+    psc = std::max(psc, o.psc);
+    cnt = std::max(cnt, o.cnt);
+    odt = std::max(odt, o.odt);
+    r4t = std::max(r4t, o.r4t);
+    nblk4c = std::max(nblk4c, o.nblk4c);
+    smaxc = std::max(smaxc, o.smaxc);
+    raggc = std::max(raggc, o.raggc);
+  }
+};
+
+// Strides of the layers [first, first+count) and their offsets in the
+// per-batch buffers (OD, R4, ABSRB).
+WsDims batch_dims(std::vector<HostPlan>& hps, int first, int count, int64_t* lstride, int64_t* f4stride,
+                  int64_t* pstride) {
+  int64_t ls = 1, fs = 1, ps = 1, odt = 0, r4t = 0;
   for (int k = 0; k < count; ++k) {
     LayerPlan& P = hps[first + k].P;
     ls = std::max<int64_t>(ls, P.line_hi - P.line_lo + 1);
@@ -856,16 +905,6 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
   }
   ls = pad256(ls);
   fs = pad256(fs);
-  int nL = (int)hps.size();
-  // offsets of every layer's slices (all layers share the vft/plan arrays)
-  int64_t blkt = 0;
-  for (int k = 0; k < nL; ++k) {
-    LayerPlan& P = hps[k].P;
-    P.vft_off = vftt;
-    vftt += pad256((int64_t)hps[k].vft.size());
-    P.blk_off = blkt;
-    blkt += hps[k].blk_v1.size();
-  }
   for (int k = 0; k < count; ++k) {
     LayerPlan& P = hps[first + k].P;
     P.od_off = odt;
@@ -874,90 +913,130 @@ int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int co
     r4t += pad256(P.nptr4 + 8);
     P.abs_off = (int64_t)k * (kNABSRB + 8);
   }
-  size_t real = plain ? 8 : 4;
+  WsDims d;
+  d.lsc = ls * count;
+  d.fsc = fs * count;
+  d.psc = ps * count;
+  d.cnt = count;
+  d.odt = odt;
+  d.r4t = r4t;
+  d.nblk4c = ((fs + 1 + 1023) / 1024) * count;
+  d.smaxc = ((ls + 1023) / 1024) * count;
+  d.raggc = 2 * 3 * count * ((ls + kRecBlock - 1) / kRecBlock);
+  *lstride = ls;
+  *f4stride = fs;
+  *pstride = ps;
+  return d;
+}
+
+// Buffers of one OD batch (sized by d) and of all nL planned layers.
+int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
+  const size_t real = plain ? 8 : 4;
   CUDA_TRY(h, h->plans.ensure(sizeof(LayerPlan) * nL));
   CUDA_TRY(h, h->vft.ensure(sizeof(double) * vftt));
-  CUDA_TRY(h, h->prep.ensure(sizeof(LinePrep) * ls * count));
-  CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * ls * count));
-  CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * ls * 3 * count));
-  CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * ls * 3 * count));
-  CUDA_TRY(h, h->gpm.ensure(sizeof(int) * ls * 3 * count));
-  CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * ls * 3 * count));
-  CUDA_TRY(h, h->gsm.ensure(sizeof(int) * ls * 3 * count));
-  CUDA_TRY(h, h->ragg.ensure(sizeof(int) * 2 * 3 * count * ((ls + kRecBlock - 1) / kRecBlock)));
-  CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * ps * count));
-  CUDA_TRY(h, h->od.ensure(real * odt));
-  CUDA_TRY(h, h->r4.ensure(real * r4t));
-  CUDA_TRY(h, h->absrb.ensure(sizeof(double) * (kNABSRB + 8) * count));
+  CUDA_TRY(h, h->prep.ensure(sizeof(LinePrep) * d.lsc));
+  CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * d.lsc));
+  CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * d.lsc * 3));
+  CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * d.lsc * 3));
+  CUDA_TRY(h, h->gpm.ensure(sizeof(int) * d.lsc * 3));
+  CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * d.lsc * 3));
+  CUDA_TRY(h, h->gsm.ensure(sizeof(int) * d.lsc * 3));
+  CUDA_TRY(h, h->ragg.ensure(sizeof(int) * d.raggc));
+  CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * d.psc));
+  CUDA_TRY(h, h->od.ensure(real * d.odt));
+  CUDA_TRY(h, h->r4.ensure(real * d.r4t));
+  CUDA_TRY(h, h->absrb.ensure(sizeof(double) * (kNABSRB + 8) * d.cnt));
   CUDA_TRY(h, h->stats.ensure(sizeof(unsigned long long) * kStatsPerLayer * nL));
   CUDA_TRY(h, h->alfvmax.ensure(sizeof(double) * nL));
-  CUDA_TRY(h, h->blockmax.ensure(sizeof(int) * ((ls + 1023) / 1024) * count));
+  CUDA_TRY(h, h->blockmax.ensure(sizeof(int) * d.smaxc));
   CUDA_TRY(h, h->nlines_d.ensure(sizeof(int64_t) * nL));
-  CUDA_TRY(h, h->f4prep.ensure(sizeof(F4Prep) * fs * count));
-  CUDA_TRY(h, h->f4sh.ensure(sizeof(ShrunkLine) * fs * count));
+  CUDA_TRY(h, h->f4prep.ensure(sizeof(F4Prep) * d.fsc));
+  CUDA_TRY(h, h->f4sh.ensure(sizeof(ShrunkLine) * d.fsc));
   CUDA_TRY(h, h->f4nout.ensure(sizeof(int64_t) * 2 * nL));
-  {
-    int64_t nblk4 = (fs + 1 + 1023) / 1024;
-    CUDA_TRY(h, h->f4blk.ensure(sizeof(int64_t) * nblk4 * count));
-    CUDA_TRY(h, h->f4ntot.ensure(sizeof(int64_t) * count));
-    CUDA_TRY(h, h->f4cidx.ensure(sizeof(int64_t) * (fs + 1) * count));
-    CUDA_TRY(h, h->f4vb.ensure(sizeof(long long) * fs * count));
-    CUDA_TRY(h, h->f4lb.ensure(sizeof(long long) * fs * count));
-    CUDA_TRY(h, h->f4src.ensure(sizeof(int64_t) * fs * count));
-    CUDA_TRY(h, h->f4flag.ensure(fs * count));
-    CUDA_TRY(h, h->f4nxt.ensure(sizeof(int) * fs * count));
-    CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * count));
-    CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * fs * count));
-  }
-  CUDA_TRY(h, h->f4rec.ensure(sizeof(F4Rec) * (fs + 4096) * count));
-  CUDA_TRY(h, h->f4recd.ensure(sizeof(F4RecD) * (fs + 4096) * count));
+  CUDA_TRY(h, h->f4blk.ensure(sizeof(int64_t) * d.nblk4c));
+  CUDA_TRY(h, h->f4ntot.ensure(sizeof(int64_t) * d.cnt));
+  CUDA_TRY(h, h->f4cidx.ensure(sizeof(int64_t) * (d.fsc + d.cnt)));
+  CUDA_TRY(h, h->f4vb.ensure(sizeof(long long) * d.fsc));
+  CUDA_TRY(h, h->f4lb.ensure(sizeof(long long) * d.fsc));
+  CUDA_TRY(h, h->f4src.ensure(sizeof(int64_t) * d.fsc));
+  CUDA_TRY(h, h->f4flag.ensure(d.fsc));
+  CUDA_TRY(h, h->f4nxt.ensure(sizeof(int) * d.fsc));
+  CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * d.cnt));
+  CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * d.fsc));
+  CUDA_TRY(h, h->f4rec.ensure(sizeof(F4Rec) * (d.fsc + 4096 * d.cnt)));
+  CUDA_TRY(h, h->f4recd.ensure(sizeof(F4RecD) * (d.fsc + 4096 * d.cnt)));
   CUDA_TRY(h, h->f4nrec.ensure(sizeof(int64_t) * nL));
   CUDA_TRY(h, h->f4nmir.ensure(sizeof(int64_t) * nL));
-  CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (fs + 4096) * count));
-  CUDA_TRY(h, h->f4sm.ensure(sizeof(int) * (fs + 4096) * count));
+  CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
+  CUDA_TRY(h, h->f4sm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
   CUDA_TRY(h, h->err.ensure(sizeof(int) * 4));
   CUDA_TRY(h, h->pblk.ensure(sizeof(int) * vftt));
   CUDA_TRY(h, h->bv1.ensure(sizeof(double) * (blkt + 1)));
   CUDA_TRY(h, h->bn.ensure(sizeof(int) * (blkt + 1)));
   CUDA_TRY(h, h->bm0.ensure(sizeof(int64_t) * (blkt + 1)));
   CUDA_TRY(h, h->bfac.ensure(sizeof(double) * (kLIMOUT4 + 2) * (blkt + 1)));
-  {
-    std::vector<int> pb(vftt, 0), bn(blkt + 1, 0);
-    std::vector<double> bv(blkt + 1, 0.);
-    std::vector<int64_t> bm(blkt + 1, 0);
-    for (int k = 0; k < nL; ++k) {
-      const HostPlan& hp = hps[k];
-      std::copy(hp.panel_blk.begin(), hp.panel_blk.end(), pb.begin() + hp.P.vft_off);
-      std::copy(hp.blk_v1.begin(), hp.blk_v1.end(), bv.begin() + hp.P.blk_off);
-      std::copy(hp.blk_n.begin(), hp.blk_n.end(), bn.begin() + hp.P.blk_off);
-      std::copy(hp.blk_m0.begin(), hp.blk_m0.end(), bm.begin() + hp.P.blk_off);
-    }
-    cudaStream_t st0 = h->stream;
-    CUDA_TRY(h, cudaMemcpyAsync(h->pblk.p, pb.data(), sizeof(int) * vftt, cudaMemcpyHostToDevice, st0));
-    CUDA_TRY(h, cudaMemcpyAsync(h->bv1.p, bv.data(), sizeof(double) * (blkt + 1), cudaMemcpyHostToDevice, st0));
-    CUDA_TRY(h, cudaMemcpyAsync(h->bn.p, bn.data(), sizeof(int) * (blkt + 1), cudaMemcpyHostToDevice, st0));
-    CUDA_TRY(h, cudaMemcpyAsync(h->bm0.p, bm.data(), sizeof(int64_t) * (blkt + 1), cudaMemcpyHostToDevice, st0));
-    CUDA_TRY(h, cudaStreamSynchronize(st0));  // host vectors go out of scope
+  return CLBLM_OK;
+}
+
+// Offsets of every planned layer's panel and far-wing block tables.
+void table_offsets(std::vector<HostPlan>& hps, int64_t* vftt, int64_t* blkt) {
+  int64_t v = 0, b = 0;
+  for (auto& hp : hps) {
+    hp.P.vft_off = v;
+    v += pad256((int64_t)hp.vft.size());
+    hp.P.blk_off = b;
+    b += hp.blk_v1.size();
   }
+  *vftt = v;
+  *blkt = b;
+}
+
+// Uploads the plans and tables of all layers (after the offsets are set);
+// zeroes the counters and error flags.
+int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int64_t blkt) {
+  const int nL = (int)hps.size();
+  std::vector<int> pb(vftt, 0), bn(blkt + 1, 0);
+  std::vector<double> bv(blkt + 1, 0.);
+  std::vector<int64_t> bm(blkt + 1, 0);
   std::vector<LayerPlan> plans(nL);
   std::vector<double> vft(vftt, 0.);
   std::vector<int64_t> nl(nL, 0);
   for (int k = 0; k < nL; ++k) {
-    plans[k] = hps[k].P;
-    std::copy(hps[k].vft.begin(), hps[k].vft.end(), vft.begin() + hps[k].P.vft_off);
-    nl[k] = hps[k].P.line_hi - hps[k].P.line_lo + 1;
+    const HostPlan& hp = hps[k];
+    std::copy(hp.panel_blk.begin(), hp.panel_blk.end(), pb.begin() + hp.P.vft_off);
+    std::copy(hp.blk_v1.begin(), hp.blk_v1.end(), bv.begin() + hp.P.blk_off);
+    std::copy(hp.blk_n.begin(), hp.blk_n.end(), bn.begin() + hp.P.blk_off);
+    std::copy(hp.blk_m0.begin(), hp.blk_m0.end(), bm.begin() + hp.P.blk_off);
+    plans[k] = hp.P;
+    std::copy(hp.vft.begin(), hp.vft.end(), vft.begin() + hp.P.vft_off);
+    nl[k] = hp.P.line_hi - hp.P.line_lo + 1;
   }
   cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(h->pblk.p, pb.data(), sizeof(int) * vftt, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->bv1.p, bv.data(), sizeof(double) * (blkt + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->bn.p, bn.data(), sizeof(int) * (blkt + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->bm0.p, bm.data(), sizeof(int64_t) * (blkt + 1), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->plans.p, plans.data(), sizeof(LayerPlan) * nL, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->vft.p, vft.data(), sizeof(double) * vftt, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->nlines_d.p, nl.data(), sizeof(int64_t) * nL, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemsetAsync(h->stats.p, 0, sizeof(unsigned long long) * kStatsPerLayer * nL, st));
   CUDA_TRY(h, cudaMemsetAsync(h->alfvmax.p, 0, sizeof(double) * nL, st));
   CUDA_TRY(h, cudaMemsetAsync(h->err.p, 0, sizeof(int) * 4, st));
-  *lstride = ls;
-  *f4stride = fs;
-  *pstride = ps;
-  *od_total = odt;
+  CUDA_TRY(h, cudaStreamSynchronize(st));  // the host vectors go out of scope
+  return CLBLM_OK;
+}
+
+// Sizes the workspace for layers [first, first+count) and uploads all plans.
+int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t* lstride,
+                  int64_t* f4stride, int64_t* pstride, int64_t* od_total) {
+  const WsDims d = batch_dims(hps, first, count, lstride, f4stride, pstride);
+  int64_t vftt, blkt;
+  table_offsets(hps, &vftt, &blkt);
+  int rc = ensure_workspace(h, d, (int)hps.size(), vftt, blkt, plain);
+  if (rc) return rc;
+  rc = upload_plans(h, hps, vftt, blkt);
+  if (rc) return rc;
+  *od_total = d.odt;
   return CLBLM_OK;
 }
 
@@ -1123,6 +1202,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   for (auto& b : h->imap) b.release();
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
+  h->bgraphs.clear();
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->stream2) {
@@ -1905,23 +1985,26 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
         jb.build_map = (owner == j && jb.spec.kind != 0 && jb.spec.itype < 0) ? 1 : 0;
         jb.od_off = P.od_off;
         jb.n_in = P.nsamp;
-        jb.slot = js.job_var[j] * nl + js.job_lay[j];
+        jb.nout = nlim;
+        jb.dst_off = (int64_t)(js.job_var[j] * nl + js.job_lay[j]) * nlim;
+        jb.blk_j1 = dj1;
+        jb.blk_vo = dvo;
+        jb.nblk = nbt;
       }
       CUDA_TRY(h, cudaMemcpyAsync(h->jjobs.p, jobs.data(), sizeof(JacJob) * count, cudaMemcpyHostToDevice,
                                   h->stream));
       h->launches += 2;
-      k_interp_map_jobs<<<dim3((unsigned)((nbt + 63) / 64), count), 64, 0, h->stream>>>(
-          h->jjobs.as<JacJob>(), count, dj1, dvo, nbt, nlim);
+      k_interp_map_jobs<<<dim3((unsigned)((nbt + 63) / 64), count), 64, 0, h->stream>>>(h->jjobs.as<JacJob>(), count);
       {
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_interp_map_jobs: %s", cudaGetErrorString(e));
       }
       if (plain)
         k_od_jobs<true><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
-            h->jjobs.as<JacJob>(), count, h->od.p, nlim, h->jod.p);
+            h->jjobs.as<JacJob>(), count, h->od.p, h->jod.p);
       else
         k_od_jobs<false><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
-            h->jjobs.as<JacJob>(), count, h->od.p, nlim, h->jod.p);
+            h->jjobs.as<JacJob>(), count, h->od.p, h->jod.p);
       {
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_od_jobs: %s", cudaGetErrorString(e));
@@ -1988,6 +2071,617 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   }
   h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
+}  // extern "C"
+
+// ---- batched profiles -------------------------------------------------------
+//
+// The scene loop of the reference (app/clblm_main.f90:115-200, RT_Jac and
+// noScattJacob per scene) over a batch: the ODLAY calls of every profile's
+// Jacobian blocks are planned on the host in the reference's order (the
+// sticky JRAD runs through them), then the OD jobs of consecutive blocks --
+// of any profiles -- share the OD pipeline's launches, their ODs land in
+// per-block slabs, and each block's recurrence runs once its slab is full.
+// Nothing between the first launch and the final check waits on the host,
+// so the launch sequence can be captured into a CUDA graph.
+namespace {
+
+struct BProfile {
+  JacSetup js;
+  std::vector<double> dvn, dvf;
+  std::vector<JacBlock> blocks;
+  int nl = 0;
+  int64_t npts = 0;
+  int status = CLBLM_OK;
+  int64_t prof_off = 0;   // its layer/level arrays in jprof (doubles)
+  int64_t stage_off = 0;  // host outputs: its first double in the staging buffer
+};
+
+struct BUnit {              // one noScattJacob block of one profile
+  int prof = 0;
+  double v1 = 0.;
+  int64_t nlim = 0, point0 = 0;
+  int job0 = 0, njob = 0;
+  int64_t jod_off = 0;      // its OD slab [variant][layer][point] in jod (Real)
+  int64_t map_off = 0;      // its maps in jmap (int2)
+  int64_t blk_off = 0;      // its interpolation blocks in jblk
+  int nblk = 0;
+  int wave = 0;
+};
+
+struct BChunk {             // one launch of the OD pipeline
+  int first = 0, count = 0, wave = 0;
+  int64_t ls = 0, fs = 0, ps = 0;
+  int unit_end = 0;         // units whose jobs all ran by the end of this chunk
+  int64_t nmax = 1;         // longest block among the chunk's jobs
+  int bmax = 1;             // most interpolation blocks among them
+};
+
+constexpr size_t kBatchWsBudget = (size_t)24 << 30;
+constexpr size_t kBatchWaveBudget = (size_t)32 << 30;
+
+uint64_t fnv(uint64_t s, const void* p, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) {
+    s ^= b[i];
+    s *= 1099511628211ull;
+  }
+  return s;
+}
+
+// every input value, the output pointers, the controls and the JRAD state
+uint64_t batch_signature(const clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_rt_ctrl_t* ctrl,
+                         int flags) {
+  uint64_t s = 1469598103934665603ull;
+  s = fnv(s, &n, sizeof n);
+  s = fnv(s, ctrl, sizeof *ctrl);
+  s = fnv(s, &flags, sizeof flags);
+  s = fnv(s, &h->jrad, sizeof h->jrad);
+  const int fp = h->first_pass_jrad ? 1 : 0;
+  s = fnv(s, &fp, sizeof fp);
+  for (int i = 0; i < n; ++i) {
+    const clblm_profile_t& P = prof[i];
+    const double* outs[5] = {P.rad, P.dr_dtlev, P.dr_dqlev, P.dr_dtskin, P.dr_demis};
+    s = fnv(s, outs, sizeof outs);
+    s = fnv(s, &P.cap, sizeof P.cap);
+    const clblm_column_t* c = P.col;
+    const clblm_jac_t* j = P.jac;
+    if (!c || !j || c->nlay < 1 || c->nmol < 1) {
+      s = fnv(s, "-", 1);
+      continue;
+    }
+    const size_t nl = (size_t)c->nlay, nm = (size_t)c->nmol;
+    s = fnv(s, &c->nlay, sizeof c->nlay);
+    s = fnv(s, &c->nmol, sizeof c->nmol);
+    if (c->mol_id) s = fnv(s, c->mol_id, sizeof(int32_t) * nm);
+    for (const double* a : {c->pave, c->tave, c->tbot, c->ttop, c->wtot, c->wtot_down})
+      if (a) s = fnv(s, a, sizeof(double) * nl);
+    if (c->w) s = fnv(s, c->w, sizeof(double) * nl * nm);
+    const double sc[4] = {c->v1, c->v2, c->tskin, c->emis};
+    s = fnv(s, sc, sizeof sc);
+    if (j->plev) s = fnv(s, j->plev, sizeof(double) * (nl + 1));
+    if (j->qlev) s = fnv(s, j->qlev, sizeof(double) * (nl + 1));
+    s = fnv(s, &j->jac_mol, sizeof j->jac_mol);
+    s = fnv(s, &j->do_temp, sizeof j->do_temp);
+  }
+  return s;
+}
+
+// Host plan of a batch: profiles, blocks (units), OD jobs, chunks and waves.
+struct BatchPlan {
+  std::vector<BProfile> profs;
+  std::vector<BUnit> units;
+  std::vector<HostPlan> hps;
+  std::vector<int> job_prof;
+  std::vector<BChunk> chunks;
+  std::vector<int64_t> j1;
+  std::vector<double> vo;
+  std::vector<double> prof_arr;
+  int jr_after = 0;
+  bool fp_after = false;
+  int64_t jod_max = 0, map_max = 0;  // per wave (elements)
+  int64_t vftt = 0, blkt = 0;        // panel / far-wing block table sizes
+  std::vector<JacJob> jobs;          // device job table (addresses of the slabs and maps)
+};
+
+// A captured batch: its launch sequence, the host tables it reads (uploaded
+// again before each replay: other calls reuse the same device tables), and
+// the buffer generation its addresses belong to.
+struct BatchGraph {
+  uint64_t sig = 0, gen = 0, last_use = 0;
+  cudaGraphExec_t exec = nullptr;
+  BatchPlan plan;
+  std::vector<int> prof_status;
+  ~BatchGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+constexpr size_t kBatchGraphs = 8;
+
+// Uploads a planned batch's tables: plans, panel and block tables, job
+// table, interpolation blocks and profile arrays; zeroes the counters.
+int batch_upload(clblm_handle* h, BatchPlan& bp) {
+  if (!bp.hps.empty()) {
+    int rc = upload_plans(h, bp.hps, bp.vftt, bp.blkt);
+    if (rc) return rc;
+  }
+  if (!bp.jobs.empty())
+    CUDA_TRY(h, cudaMemcpyAsync(h->jjobs.p, bp.jobs.data(), sizeof(JacJob) * bp.jobs.size(), cudaMemcpyHostToDevice,
+                                h->stream));
+  if (!bp.j1.empty()) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->jblk.p, bp.j1.data(), 8 * bp.j1.size(), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->jblk.as<unsigned char>() + 8 * bp.j1.size(), bp.vo.data(), 8 * bp.vo.size(),
+                                cudaMemcpyHostToDevice, h->stream));
+  }
+  if (!bp.prof_arr.empty())
+    CUDA_TRY(h, cudaMemcpyAsync(h->jprof.p, bp.prof_arr.data(), sizeof(double) * bp.prof_arr.size(),
+                                cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return CLBLM_OK;
+}
+
+int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_rt_ctrl_t* ctrl, bool plain,
+               BatchPlan* bp) {
+  const size_t real = plain ? 8 : 4;
+  bp->profs.resize(n);
+  int jr = h->jrad;
+  bool fp = h->first_pass_jrad;
+  for (int i = 0; i < n; ++i) {
+    BProfile& pr = bp->profs[i];
+    const clblm_column_t* col = prof[i].col;
+    const clblm_jac_t* jac = prof[i].jac;
+    const int jr0 = jr;
+    const bool fp0 = fp;
+    const size_t units0 = bp->units.size(), jobs0 = bp->hps.size();
+    int rc = jac_setup(h, col, ctrl, jac, &pr.js, &pr.dvn, &pr.dvf);
+    if (!rc) rc = jac_block_list(h, col, ctrl, pr.js, pr.dvn, pr.dvf, &pr.blocks);
+    int64_t npts = 0;
+    for (size_t b = 0; !rc && b < pr.blocks.size(); ++b) {
+      std::vector<HostPlan> hps;
+      int64_t nlim;
+      rc = jac_plan_block(h, ctrl, jac, pr.js, pr.dvn, pr.dvf, pr.blocks[b].v1, pr.blocks[b].v2, &jr, &fp, &hps,
+                          &nlim);
+      if (!rc && nlim != pr.blocks[b].n) rc = set_err(h, CLBLM_ERR_GRID, "Jacobian block length changed");
+      if (rc) break;
+      BUnit u;
+      u.prof = i;
+      u.v1 = pr.blocks[b].v1;
+      u.nlim = nlim;
+      u.point0 = npts;
+      u.job0 = (int)bp->hps.size();
+      u.njob = (int)hps.size();
+      npts += nlim;
+      for (auto& hp : hps) {
+        bp->hps.push_back(std::move(hp));
+        bp->job_prof.push_back(i);
+      }
+      bp->units.push_back(u);
+    }
+    if (!rc && prof[i].cap < npts) rc = set_err(h, CLBLM_ERR_CAPACITY, "profile %d needs %lld points", i,
+                                                 (long long)npts);
+    if (rc) {  // the profile makes no ODLAY call: drop what was planned for it
+      pr.status = rc;
+      bp->units.resize(units0);
+      bp->hps.resize(jobs0);
+      bp->job_prof.resize(jobs0);
+      jr = jr0;
+      fp = fp0;
+      continue;
+    }
+    pr.nl = col->nlay;
+    pr.npts = npts;
+    // layer and level arrays: tlay, tlev, amf_down, wtot, dT_dTup, dT_dTlo, dW_dQup, dW_dQlo
+    const int nl = pr.nl;
+    std::vector<double> tlev(nl + 1), amfd(nl), dTu(nl), dTl(nl), dWu(nl), dWl(nl);
+    for (int l = 0; l < nl; ++l) {
+      tlev[l] = col->tbot[l];
+      amfd[l] = col->wtot_down[l] / col->wtot[l];
+    }
+    tlev[nl] = col->ttop[nl - 1];
+    level2layer_h(jac->plev, tlev.data(), col->tave, pr.js.imol >= 0 ? jac->qlev : nullptr, nl, dTu.data(),
+                  dTl.data(), dWu.data(), dWl.data());
+    pr.prof_off = (int64_t)bp->prof_arr.size();
+    auto& a = bp->prof_arr;
+    a.insert(a.end(), col->tave, col->tave + nl);
+    a.insert(a.end(), tlev.begin(), tlev.end());
+    a.insert(a.end(), amfd.begin(), amfd.end());
+    a.insert(a.end(), col->wtot, col->wtot + nl);
+    for (auto* v : {&dTu, &dTl, &dWu, &dWl}) a.insert(a.end(), v->begin(), v->end());
+  }
+  bp->jr_after = jr;
+  bp->fp_after = fp;
+  // interpolation blocks of every unit (interpSpectrum's general branch)
+  for (auto& u : bp->units) {
+    const double dvb = bp->profs[u.prof].js.dvb;
+    const double TOL = 1.e-8;
+    const double V2out = u.v1 + (double)(u.nlim - 1) * dvb;
+    double Vo = u.v1;
+    u.blk_off = (int64_t)bp->j1.size();
+    while (Vo < V2out + TOL) {
+      int64_t J1 = (int64_t)((Vo - u.v1) / dvb + 1.001);
+      int64_t J2 = std::min<int64_t>(u.nlim, J1 + 2400 - 1);
+      bp->j1.push_back(J1);
+      bp->vo.push_back(Vo);
+      Vo = u.v1 + (double)J2 * dvb;
+      if ((int64_t)bp->j1.size() - u.blk_off > u.nlim / 2400 + 8)
+        return set_err(h, CLBLM_ERR_GRID, "interpolation blocks");
+    }
+    u.nblk = (int)((int64_t)bp->j1.size() - u.blk_off);
+  }
+  // waves of units whose OD slabs and maps fit the wave budget
+  {
+    int wave = 0;
+    int64_t jod = 0, map = 0;
+    for (auto& u : bp->units) {
+      const BProfile& pr = bp->profs[u.prof];
+      const int64_t uj = (int64_t)pr.js.nvar * pr.nl * u.nlim, um = (int64_t)u.njob * u.nlim;
+      if ((jod > 0 || map > 0) && (size_t)(jod + uj) * real + (size_t)(map + um) * 8 > kBatchWaveBudget) {
+        wave++;
+        jod = map = 0;
+      }
+      u.wave = wave;
+      u.jod_off = jod;
+      u.map_off = map;
+      jod += uj;
+      map += um;
+      bp->jod_max = std::max(bp->jod_max, jod);
+      bp->map_max = std::max(bp->map_max, map);
+    }
+  }
+  // chunks of consecutive jobs within a wave, sized to the workspace budget
+  {
+    const int njob = (int)bp->hps.size();
+    std::vector<int> job_wave(njob, 0), job_unit(njob, 0);
+    for (size_t k = 0; k < bp->units.size(); ++k)
+      for (int j = 0; j < bp->units[k].njob; ++j) {
+        job_wave[bp->units[k].job0 + j] = bp->units[k].wave;
+        job_unit[bp->units[k].job0 + j] = (int)k;
+      }
+    for (int first = 0; first < njob;) {
+      BChunk c;
+      c.first = first;
+      c.wave = job_wave[first];
+      size_t bytes = 0;
+      while (first + c.count < njob && job_wave[first + c.count] == c.wave) {
+        const LayerPlan& P = bp->hps[first + c.count].P;
+        size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
+                   (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+        if (c.count > 0 && bytes + b > kBatchWsBudget) break;
+        bytes += b;
+        c.count++;
+      }
+      for (int j = c.first; j < first + c.count; ++j) {
+        c.nmax = std::max(c.nmax, bp->units[job_unit[j]].nlim);
+        c.bmax = std::max(c.bmax, bp->units[job_unit[j]].nblk);
+      }
+      first += c.count;
+      // units complete once their last job has run
+      const int last_unit = job_unit[first - 1];
+      c.unit_end = (first == njob || job_unit[first] != last_unit) ? last_unit + 1 : last_unit;
+      bp->chunks.push_back(c);
+    }
+  }
+  return CLBLM_OK;
+}
+
+// Launches of a planned batch (no host waits, capturable).
+int batch_enqueue(clblm_handle* h, BatchPlan& bp, const clblm_profile_t* prof, const clblm_rt_ctrl_t* ctrl,
+                  bool plain, bool dev_out) {
+  const size_t real = plain ? 8 : 4;
+  const double* dprof = h->jprof.as<double>();
+  double* stage = h->outbuf.as<double>();
+  int unit_done = 0;
+  for (const BChunk& c : bp.chunks) {
+    int rc = run_od_batch(h, bp.hps, c.first, c.count, plain, c.ls, c.fs, c.ps);
+    if (rc) return rc;
+    JacJob* jobs = h->jjobs.as<JacJob>() + c.first;
+    const int64_t nmax = c.nmax;
+    const int bmax = c.bmax;
+    h->launches += 2;
+    k_interp_map_jobs<<<dim3((unsigned)((bmax + 63) / 64), c.count), 64, 0, h->stream>>>(jobs, c.count);
+    if (plain)
+      k_od_jobs<true><<<dim3((unsigned)((nmax + 255) / 256), c.count), 256, 0, h->stream>>>(jobs, c.count, h->od.p,
+                                                                                             h->jod.p);
+    else
+      k_od_jobs<false><<<dim3((unsigned)((nmax + 255) / 256), c.count), 256, 0, h->stream>>>(jobs, c.count, h->od.p,
+                                                                                              h->jod.p);
+    {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "batch OD gather: %s", cudaGetErrorString(e));
+    }
+    // recurrences of the blocks whose ODs are complete
+    for (; unit_done < c.unit_end; ++unit_done) {
+      const BUnit& U = bp.units[unit_done];
+      const BProfile& pr = bp.profs[U.prof];
+      const clblm_profile_t& po = prof[U.prof];
+      const int nl = pr.nl;
+      const double* pa = dprof + pr.prof_off;
+      JacArgs a;
+      std::memset(&a, 0, sizeof a);
+      a.jod = h->jod.as<unsigned char>() + real * U.jod_off;
+      a.nlay = nl;
+      a.vT = pr.js.vT;
+      a.vW = pr.js.vW;
+      a.vM = pr.js.vM;
+      a.nout = U.nlim;
+      a.v1 = U.v1;
+      a.dv = pr.js.dvb;
+      a.tlay = pa;
+      a.tlev = pa + nl;
+      a.amf_down = pa + 2 * nl + 1;
+      a.wtot = pa + 3 * nl + 1;
+      a.dT_dTup = pa + 4 * nl + 1;
+      a.dT_dTlo = pa + 5 * nl + 1;
+      a.dW_dQup = pa + 6 * nl + 1;
+      a.dW_dQlo = pa + 7 * nl + 1;
+      a.tsfc = po.col->tskin;
+      a.emis = po.col->emis;
+      a.lin_in_tau = ctrl->lin_in_tau;
+      a.do_temp = po.jac->do_temp;
+      if (dev_out) {
+        a.rad = po.rad;
+        a.dtsfc = po.dr_dtskin;
+        a.demis = po.dr_demis;
+        a.dtlev = po.dr_dtlev;
+        a.dqlev = po.dr_dqlev;
+        a.ld = po.cap;
+      } else {
+        double* b = stage + pr.stage_off;
+        const int64_t np = pr.npts;
+        a.rad = po.rad ? b : nullptr;
+        a.dtsfc = po.dr_dtskin ? b + np : nullptr;
+        a.demis = po.dr_demis ? b + 2 * np : nullptr;
+        a.dtlev = po.dr_dtlev ? b + 3 * np : nullptr;
+        a.dqlev = po.dr_dqlev ? b + 3 * np + (int64_t)(nl + 1) * np : nullptr;
+        a.ld = np;
+      }
+      a.off = U.point0;
+      h->launches++;
+      if (plain) k_jac<true><<<(unsigned)((U.nlim + 127) / 128), 128, 0, h->stream>>>(a);
+      else k_jac<false><<<(unsigned)((U.nlim + 127) / 128), 128, 0, h->stream>>>(a);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "batch k_jac: %s", cudaGetErrorString(e));
+    }
+  }
+  return CLBLM_OK;
+}
+
+// Error flags and counters of every OD job of the batch, after it ran; a
+// failing job fails its profile.  Returns the first failing profile's code.
+int batch_check(clblm_handle* h, const std::vector<int>& job_prof, std::vector<int>* status) {
+  const int nL = (int)job_prof.size();
+  int err[4];
+  std::vector<unsigned long long> stats((size_t)kStatsPerLayer * nL);
+  std::vector<int64_t> nout(2 * (size_t)nL);
+  CUDA_TRY(h, cudaMemcpyAsync(err, h->err.p, sizeof err, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(stats.data(), h->stats.p, sizeof(unsigned long long) * stats.size(),
+                              cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(nout.data(), h->f4nout.p, sizeof(int64_t) * nout.size(), cudaMemcpyDeviceToHost,
+                              h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  CUDA_TRY(h, cudaGetLastError());
+  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "more than %d radiation-term segments in a panel", kMaxSeg);
+  if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
+  if (err[0] & 4) return set_err(h, CLBLM_ERR_CUDA, "far-wing records: a shared-memory stage never arrived");
+  int first_bad = CLBLM_OK;
+  for (int k = 0; k < nL; ++k) {
+    const unsigned long long* s = &stats[(size_t)k * kStatsPerLayer];
+    h->acc_fnq += (int64_t)s[5];
+    h->acc_f4q += (int64_t)s[6];
+    int rc = CLBLM_OK;
+    if (s[4]) rc = set_err(h, CLBLM_ERR_UNSUPPORTED, "profile %d: %llu lines need isotopologue/line-coupling "
+                           "rules that are not on this path", job_prof[k], s[4]);
+    else if (nout[2 * k] == -2)
+      rc = set_err(h, CLBLM_ERR_UNSUPPORTED, "profile %d: far-wing line window ends outside the prepared range",
+                   job_prof[k]);
+    else if (nout[2 * k] < 0)
+      rc = set_err(h, CLBLM_ERR_RANGE, "profile %d: a SHRINQ call longer than the walk buffer", job_prof[k]);
+    if (rc) {
+      int& st = (*status)[job_prof[k]];
+      if (st == CLBLM_OK) st = rc;
+      if (first_bad == CLBLM_OK) first_bad = rc;
+    }
+  }
+  return first_bad;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clblm_gpu_batch_size(clblm_handle_t* h, const clblm_profile_t* prof, int32_t n, const clblm_rt_ctrl_t* ctrl,
+                         int64_t* npts, double* dv) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!prof || n < 0 || !ctrl) return set_err(h, CLBLM_ERR_ARG, "bad batch");
+  int first_bad = CLBLM_OK;
+  for (int i = 0; i < n; ++i) {
+    int rc = clblm_gpu_jac_size(h, prof[i].col, ctrl, prof[i].jac, npts ? npts + i : nullptr, dv ? dv + i : nullptr);
+    if (rc && first_bad == CLBLM_OK) first_bad = rc;
+  }
+  return first_bad;
+}
+
+int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const clblm_rt_ctrl_t* ctrl, int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!prof || n < 0 || !ctrl) return set_err(h, CLBLM_ERR_ARG, "bad batch");
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  const bool dev_out = (flags & CLBLM_OUT_DEVICE) != 0;
+  const bool graph = (flags & CLBLM_BATCH_GRAPH) != 0;
+  if (graph && !dev_out) return set_err(h, CLBLM_ERR_ARG, "CLBLM_BATCH_GRAPH needs device outputs");
+  const bool plain = ctrl->od.precision == CLBLM_PREC_PLAIN;
+  h->reset_call();
+  uint64_t sig = 0;
+  if (graph) {
+    sig = batch_signature(h, prof, n, ctrl, flags);
+    // graphs whose buffers have moved since their capture are dropped
+    auto& gs = h->bgraphs;
+    gs.erase(std::remove_if(gs.begin(), gs.end(), [](const std::shared_ptr<BatchGraph>& g) {
+               return g->gen != g_buf_gen.load();
+             }), gs.end());
+    for (auto& g : gs) {
+      if (g->sig != sig) continue;  // the same batch again: replay its launches
+      g->last_use = ++h->bgraph_clock;
+      int rc = batch_upload(h, g->plan);
+      if (rc) return rc;
+      CUDA_TRY(h, cudaGraphLaunch(g->exec, h->stream));
+      std::vector<int> status = g->prof_status;
+      rc = batch_check(h, g->plan.job_prof, &status);
+      for (int i = 0; i < n; ++i) prof[i].status = status[i];
+      h->jrad = g->plan.jr_after;
+      h->first_pass_jrad = g->plan.fp_after;
+      h->last.launches = h->launches;
+      if (rc) return rc;
+      for (int i = 0; i < n; ++i)
+        if (status[i]) return status[i];
+      return CLBLM_OK;
+    }
+  }
+  BatchPlan bp;
+  int rc = batch_plan(h, prof, n, ctrl, plain, &bp);
+  if (rc) return rc;
+  if (bp.hps.empty()) {  // no profile could be planned
+    int first_bad = CLBLM_OK;
+    for (int i = 0; i < n; ++i) {
+      prof[i].status = bp.profs[i].status;
+      if (prof[i].status && first_bad == CLBLM_OK) first_bad = prof[i].status;
+    }
+    return first_bad;
+  }
+  // workspace: the largest chunk, every job's plan, the waves' slabs
+  table_offsets(bp.hps, &bp.vftt, &bp.blkt);
+  WsDims dmax;
+  for (BChunk& c : bp.chunks) dmax.max_with(batch_dims(bp.hps, c.first, c.count, &c.ls, &c.fs, &c.ps));
+  const int njob = (int)bp.hps.size();
+  const size_t real = plain ? 8 : 4;
+  rc = ensure_workspace(h, dmax, njob, bp.vftt, bp.blkt, plain);
+  if (rc) return rc;
+  CUDA_TRY(h, h->jod.ensure(real * (size_t)std::max<int64_t>(bp.jod_max, 1)));
+  CUDA_TRY(h, h->jmap.ensure(sizeof(int2) * (size_t)std::max<int64_t>(bp.map_max, 1)));
+  CUDA_TRY(h, h->jjobs.ensure(sizeof(JacJob) * (size_t)std::max(njob, 1)));
+  CUDA_TRY(h, h->jblk.ensure(16 * (bp.j1.size() + 1)));
+  CUDA_TRY(h, h->jprof.ensure(sizeof(double) * (bp.prof_arr.size() + 1)));
+  // host outputs: one staging area for all profiles
+  int64_t stage = 0;
+  for (auto& pr : bp.profs) {
+    pr.stage_off = stage;
+    if (!dev_out && pr.status == CLBLM_OK) stage += pr.npts * (3 + 2 * (int64_t)(pr.nl + 1));
+  }
+  if (!dev_out) CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * (size_t)std::max<int64_t>(stage, 1)));
+  // job table: every OD job's grid map and slab row
+  {
+    std::vector<JacJob>& jobs = bp.jobs;
+    jobs.assign(njob, JacJob{});
+    int2* dmap = h->jmap.as<int2>();
+    const int64_t* dj1 = h->jblk.as<int64_t>();
+    const double* dvo = reinterpret_cast<const double*>(h->jblk.as<unsigned char>() + 8 * bp.j1.size());
+    for (const BUnit& U : bp.units) {
+      const BProfile& pr = bp.profs[U.prof];
+      for (int q = 0; q < U.njob; ++q) {
+        const int j = U.job0 + q;
+        const LayerPlan& P = bp.hps[j].P;
+        JacJob& jb = jobs[j];
+        jb.spec = interp_spec(P.v1, P.dv, P.nsamp, U.v1, pr.js.dvb, U.nlim);
+        const int il = pr.js.job_lay[q];
+        int owner = q;
+        for (int r = 0; r < q; ++r)
+          if (pr.js.job_lay[r] == il && bp.hps[U.job0 + r].P.dv == P.dv &&
+              bp.hps[U.job0 + r].P.nsamp == P.nsamp) {
+            owner = r;
+            break;
+          }
+        jb.map = dmap + U.map_off + (int64_t)owner * U.nlim;
+        jb.spec.map = jb.map;
+        jb.build_map = (owner == q && jb.spec.kind != 0 && jb.spec.itype < 0) ? 1 : 0;
+        jb.od_off = P.od_off;
+        jb.n_in = P.nsamp;
+        jb.nout = U.nlim;
+        jb.dst_off = U.jod_off + (int64_t)(pr.js.job_var[q] * pr.nl + pr.js.job_lay[q]) * U.nlim;
+        jb.blk_j1 = dj1 + U.blk_off;
+        jb.blk_vo = dvo + U.blk_off;
+        jb.nblk = U.nblk;
+      }
+    }
+  }
+  rc = batch_upload(h, bp);
+  if (rc) return rc;
+  // launches: directly, or captured into a graph that the handle keeps
+  std::shared_ptr<BatchGraph> bg;
+  if (graph) {
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    rc = batch_enqueue(h, bp, prof, ctrl, plain, dev_out);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "batch capture: %s", cudaGetErrorString(e));
+    bg = std::make_shared<BatchGraph>();
+    e = cudaGraphInstantiate(&bg->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      bg->exec = nullptr;
+      return set_err(h, CLBLM_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    }
+    CUDA_TRY(h, cudaGraphLaunch(bg->exec, h->stream));
+  } else {
+    rc = batch_enqueue(h, bp, prof, ctrl, plain, dev_out);
+    if (rc) return rc;
+  }
+  std::vector<int> status(n);
+  for (int i = 0; i < n; ++i) status[i] = bp.profs[i].status;
+  const std::vector<int> plan_status = status;
+  rc = batch_check(h, bp.job_prof, &status);
+  h->jrad = bp.jr_after;
+  h->first_pass_jrad = bp.fp_after;
+  if (bg) {  // keep the graph (the least recently used one leaves a full cache)
+    auto& gs = h->bgraphs;
+    if (gs.size() >= kBatchGraphs) {
+      auto old = std::min_element(gs.begin(), gs.end(), [](const std::shared_ptr<BatchGraph>& a,
+                                                           const std::shared_ptr<BatchGraph>& b) {
+        return a->last_use < b->last_use;
+      });
+      gs.erase(old);
+    }
+    bg->sig = sig;
+    bg->gen = g_buf_gen.load();
+    bg->last_use = ++h->bgraph_clock;
+    bg->prof_status = plan_status;
+    bg->plan = std::move(bp);
+    gs.push_back(std::move(bg));
+  }
+  // host outputs
+  if (!dev_out) {
+    const double* sb = h->outbuf.as<double>();
+    for (int i = 0; i < n; ++i) {
+      const BProfile& pr = bp.profs[i];
+      if (pr.status != CLBLM_OK) continue;
+      const int64_t np = pr.npts;
+      const double* b = sb + pr.stage_off;
+      const clblm_profile_t& po = prof[i];
+      auto row = [&](double* dst, const double* src) -> cudaError_t {
+        return dst ? cudaMemcpyAsync(dst, src, sizeof(double) * np, cudaMemcpyDeviceToHost, h->stream) : cudaSuccess;
+      };
+      CUDA_TRY(h, row(po.rad, b));
+      CUDA_TRY(h, row(po.dr_dtskin, b + np));
+      CUDA_TRY(h, row(po.dr_demis, b + 2 * np));
+      if (po.dr_dtlev)
+        CUDA_TRY(h, cudaMemcpy2DAsync(po.dr_dtlev, sizeof(double) * po.cap, b + 3 * np, sizeof(double) * np,
+                                      sizeof(double) * np, pr.nl + 1, cudaMemcpyDeviceToHost, h->stream));
+      if (po.dr_dqlev)
+        CUDA_TRY(h, cudaMemcpy2DAsync(po.dr_dqlev, sizeof(double) * po.cap, b + 3 * np + (int64_t)(pr.nl + 1) * np,
+                                      sizeof(double) * np, sizeof(double) * np, pr.nl + 1, cudaMemcpyDeviceToHost,
+                                      h->stream));
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  }
+  for (int i = 0; i < n; ++i) prof[i].status = status[i];
+  h->last.launches = h->launches;
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i)
+    if (status[i]) return status[i];
   return CLBLM_OK;
 }
 

@@ -287,6 +287,45 @@ int clblm_gpu_jac(clblm_handle_t *h, const clblm_column_t *col,
                   double *dr_dtskin, double *dr_demis, int64_t cap,
                   int32_t flags);
 
+/* ---- many profiles in one call ----------------------------------------------
+ *
+ * The scene loop of the reference's main program (app/clblm_main.f90:115-200:
+ * RT_Jac, clblm_Drivers.f90:559, and through it one noScattJacob per scene,
+ * with the SAVEd JRAD carried from scene to scene) for a batch of profiles
+ * of uneven layer counts and spectral windows.  The layer ODs of all profiles'
+ * Jacobian blocks are planned on the host in the reference's call order,
+ * then share the OD pipeline's launches (a launch covers layers of several
+ * profiles), and every block's recurrence runs as soon as its ODs are on the
+ * device.  Results equal clblm_gpu_jac called on each profile in turn with
+ * the same handle.
+ *
+ * With CLBLM_BATCH_GRAPH in `flags` (device outputs only), the launch
+ * sequence of the batch is captured once into a CUDA graph that the handle
+ * keeps; a later call with the same batch (same inputs, same output
+ * pointers, same JRAD state) replays the graph instead of launching again. */
+typedef struct {
+  const clblm_column_t *col;  /* the profile's layers and window             */
+  const clblm_jac_t *jac;     /* level profile of the Jacobians              */
+  double *rad, *dr_dtlev, *dr_dqlev, *dr_dtskin, *dr_demis;
+                              /* outputs as in clblm_gpu_jac (any may be NULL)*/
+  int64_t cap;                /* capacity of each output spectrum           */
+  int32_t status;             /* written by the call: CLBLM_OK or the code  */
+  int32_t reserved;
+} clblm_profile_t;
+
+#define CLBLM_BATCH_GRAPH 0x10
+
+/* Points and DVout of each profile's spectra (npts[n], dv[n]). */
+int clblm_gpu_batch_size(clblm_handle_t *h, const clblm_profile_t *prof,
+                         int32_t n, const clblm_rt_ctrl_t *ctrl,
+                         int64_t *npts, double *dv);
+/* Radiance and Jacobians of n profiles.  Returns CLBLM_OK when every
+ * profile succeeded, else the first failing profile's code; each profile's
+ * own code is in prof[i].status.  flags: CLBLM_OUT_HOST or CLBLM_OUT_DEVICE,
+ * optionally | CLBLM_BATCH_GRAPH. */
+int clblm_gpu_batch(clblm_handle_t *h, clblm_profile_t *prof, int32_t n,
+                    const clblm_rt_ctrl_t *ctrl, int32_t flags);
+
 /* Lines of an LNFL line file (TAPE3) as read by RDLIN (clblm_ODLAY.f90:
  * 2645-2700) through CLBLM_LineData (clblm_LineData.f90:52-161): Fortran
  * unformatted records (4-byte length markers), the file header, the optional
