@@ -2198,7 +2198,7 @@ struct BatchGraph {
     if (exec) cudaGraphExecDestroy(exec);
   }
 };
-constexpr size_t kBatchGraphs = 8;
+constexpr size_t kBatchGraphs = 16;
 
 // Uploads a planned batch's tables: plans, panel and block tables, job
 // table, interpolation blocks and profile arrays; zeroes the counters.

@@ -81,12 +81,15 @@ def temperature(z_km):
 
 
 def atmosphere(nlay, p_top, v1, v2, mols=SEVEN, p_sfc=1013.0, scale_height=7.0,
-               other_vmr=OTHER_VMR, emis=0.98):
-    """Layered nadir column, layer 0 at the surface."""
+               other_vmr=OTHER_VMR, emis=0.98, dt_lev=None):
+    """Layered nadir column, layer 0 at the surface; dt_lev [nlay+1] (K) is
+    added to the level temperatures of the lapse profile."""
     k = np.arange(nlay + 1)
     p_lev = p_sfc * (p_top / p_sfc) ** (k / nlay)
     z_lev = -scale_height * np.log(p_lev / p_sfc)
     t_lev = temperature(z_lev)
+    if dt_lev is not None:
+        t_lev = t_lev + np.asarray(dt_lev, dtype=np.float64)
     pave = np.sqrt(p_lev[:-1] * p_lev[1:])
     tave = 0.5 * (t_lev[:-1] + t_lev[1:])
     zmid = 0.5 * (z_lev[:-1] + z_lev[1:])
@@ -136,6 +139,25 @@ def config2():
     """config 1's atmosphere and lines over 600-1100 cm-1."""
     lines, col, cont = config1()
     return lines.window(600.0, 1100.0), col.with_window(600.0, 1100.0), cont
+
+
+def config3(n_profiles=256, n_lines=500000):
+    """Batched profiles: layer counts uniform on 20..100, level temperatures
+    of the config 1 lapse profile plus N(0, 3 K), each with its own window of
+    log-uniform width 10..1000 cm-1 inside 500-2500 cm-1, config 1's lines.
+    Returns the lines, the continuum and lists of columns and Jacobian
+    profiles (radiance + T and H2O Jacobians for each)."""
+    lines, _, cont = config1(n_lines)
+    rng = np.random.default_rng(3)
+    cols, jacs = [], []
+    for _ in range(n_profiles):
+        nlay = int(rng.integers(20, 101))
+        width = 10.0 ** rng.uniform(1.0, 3.0)
+        v1 = float(np.round(rng.uniform(500.0, 2500.0 - width), 3))
+        col = atmosphere(nlay, 0.1, v1, float(np.round(v1 + width, 3)), dt_lev=rng.normal(0.0, 3.0, nlay + 1))
+        cols.append(col)
+        jacs.append(jac_profile(col))
+    return lines, cont, cols, jacs
 
 
 def config4(n_lines=3000000):

@@ -301,8 +301,11 @@ int clblm_gpu_jac(clblm_handle_t *h, const clblm_column_t *col,
  *
  * With CLBLM_BATCH_GRAPH in `flags` (device outputs only), the launch
  * sequence of the batch is captured once into a CUDA graph that the handle
- * keeps; a later call with the same batch (same inputs, same output
- * pointers, same JRAD state) replays the graph instead of launching again. */
+ * keeps (for its last 16 batches); a later call with the same batch (same
+ * inputs, same output pointers, same JRAD state) uploads the batch's tables
+ * again and replays the graph instead of launching kernel by kernel.  A
+ * graph is dropped when any of the handle's device buffers has moved since
+ * its capture. */
 typedef struct {
   const clblm_column_t *col;  /* the profile's layers and window             */
   const clblm_jac_t *jac;     /* level profile of the Jacobians              */
