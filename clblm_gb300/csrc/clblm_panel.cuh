@@ -59,7 +59,9 @@ struct F4RecD {
 };
 constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv (two per thread)
 constexpr int kF4Threads = kF4Tile / 2;
-constexpr int kF4Chunk = 256;    // records per shared-memory stage
+constexpr int kF4Group = 32;     // records per FP32 partial sum of the mixed path
+// records per shared-memory stage of k_f4_conv: the variants the autotuner
+// times (64, 128, 256)
 
 struct F4Args {
   const LayerPlan* plans;
@@ -81,7 +83,7 @@ __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* bl
 
 template <bool Plain>
 __global__ void k_panel(PanelArgs a);
-template <bool Plain>
+template <bool Plain, int CHUNK>
 __global__ void k_f4_conv(F4Args a);
 
 }  // namespace clblm

@@ -734,12 +734,15 @@ template __global__ void k_panel<true>(PanelArgs);
 // that reach any point of the tile are one index range: from the first record
 // whose running max of JMAX reaches the tile's first point to the first one
 // whose running min of JMIN (from the right) passes its last point.  That
-// range streams through shared memory in chunks of kF4Chunk records, one bulk
+// range streams through shared memory in chunks of CHUNK records, one bulk
 // copy per chunk into two alternating stages; every thread then evaluates all
-// records of the chunk at its own point.  The FP64 path adds the terms in the
-// reference's order (record order); the mixed path keeps four FP32 partial
-// sums per chunk (alternate records) and adds each chunk's total into a Kahan
-// sum.
+// records of the chunk at its two points.  The FP64 path adds the terms in
+// the reference's order (record order); the mixed path sums groups of
+// kF4Group records (two packed partial sums over alternate records) and adds
+// each group's total into a Kahan sum.  Groups start at the tile's first
+// record, so the records per stage (CHUNK, a multiple of kF4Group, chosen by
+// the autotuner) do not change the result.
+
 // FP32 terms of far-wing record r at a thread's two points (packed FP32x2):
 // Core: the point may lie within 64 ALFV of the line (the polynomial core of
 // CNVF4Q), else the Lorentzian wing is certain; Mask: the record's point
@@ -778,11 +781,12 @@ __device__ __forceinline__ float2 f4_chunk(const F4Rec* S, int cnt, float2 Jm1, 
   return __fadd2_rn(p0, p1);
 }
 
-template <bool Plain>
+template <bool Plain, int CHUNK>
 __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
+  static_assert(CHUNK % kF4Group == 0, "groups of the FP32 sums lie within a chunk");
   using Real = typename std::conditional<Plain, double, float>::type;
   using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
-  __shared__ __align__(128) Rec stage[2][kF4Chunk];
+  __shared__ __align__(128) Rec stage[2][CHUNK];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ int64_t rng[2];
 
@@ -825,10 +829,10 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
   }
   __syncthreads();
   const int64_t lo = rng[0], hi = rng[1];
-  const int64_t nchunk = (hi - lo + kF4Chunk - 1) / kF4Chunk;
+  const int64_t nchunk = (hi - lo + CHUNK - 1) / CHUNK;
   auto issue = [&](int64_t c) {  // thread 0: chunk c into stage c&1
-    const int64_t r0 = lo + c * kF4Chunk;
-    const int64_t nr = hi - r0 < kF4Chunk ? hi - r0 : (int64_t)kF4Chunk;
+    const int64_t r0 = lo + c * CHUNK;
+    const int64_t nr = hi - r0 < CHUNK ? hi - r0 : (int64_t)CHUNK;
     const uint32_t bytes = (uint32_t)(nr * (int64_t)sizeof(Rec));
     mbar_arrive_expect_tx(&bar[c & 1], bytes);
     bulk_g2s(&stage[c & 1][0], recs + r0, bytes, &bar[c & 1]);
@@ -871,8 +875,8 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
       break;
     }
     const Rec* S = stage[c & 1];
-    const int64_t left = hi - (lo + c * kF4Chunk);
-    const int cnt = (int)(left < kF4Chunk ? left : kF4Chunk);
+    const int64_t left = hi - (lo + c * CHUNK);
+    const int cnt = (int)(left < CHUNK ? left : CHUNK);
     if (liveA) {
       if constexpr (Plain) {
         for (int k = 0; k < cnt; ++k) {
@@ -900,13 +904,17 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
       const bool full = __syncthreads_and(cov);
       const bool wonly = __syncthreads_and(wing);
       if (liveA) {
-        float2 t;
-        if (full) t = wonly ? f4_chunk<false, false>(S, cnt, Jm1, dvr4, JA, JB)
-                            : f4_chunk<true, false>(S, cnt, Jm1, dvr4, JA, JB);
-        else t = wonly ? f4_chunk<false, true>(S, cnt, Jm1, dvr4, JA, JB)
-                       : f4_chunk<true, true>(S, cnt, Jm1, dvr4, JA, JB);
-        kA.add(t.x);
-        kB.add(t.y);
+        for (int g0 = 0; g0 < cnt; g0 += kF4Group) {
+          const F4Rec* G = S + g0;
+          const int gc = cnt - g0 < kF4Group ? cnt - g0 : kF4Group;
+          float2 t;
+          if (full) t = wonly ? f4_chunk<false, false>(G, gc, Jm1, dvr4, JA, JB)
+                              : f4_chunk<true, false>(G, gc, Jm1, dvr4, JA, JB);
+          else t = wonly ? f4_chunk<false, true>(G, gc, Jm1, dvr4, JA, JB)
+                         : f4_chunk<true, true>(G, gc, Jm1, dvr4, JA, JB);
+          kA.add(t.x);
+          kB.add(t.y);
+        }
       }
     }
     __syncthreads();  // stage c&1 is free for chunk c+2
@@ -947,7 +955,11 @@ __global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
   }
 }
 
-template __global__ void k_f4_conv<false>(F4Args);
-template __global__ void k_f4_conv<true>(F4Args);
+template __global__ void k_f4_conv<false, 64>(F4Args);
+template __global__ void k_f4_conv<false, 128>(F4Args);
+template __global__ void k_f4_conv<false, 256>(F4Args);
+template __global__ void k_f4_conv<true, 64>(F4Args);
+template __global__ void k_f4_conv<true, 128>(F4Args);
+template __global__ void k_f4_conv<true, 256>(F4Args);
 
 }  // namespace clblm

@@ -300,7 +300,6 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
   int64_t n = P.line_hi - P.line_lo + 1;
   const double* vft = vft_all + P.vft_off;
   double WAVDXF = P.dv / kDXF1;
-  double HWDXF = kHWF1 / kDXF1;
   double DVR2 = (kDXF2 / kDXF1) * P.dv;
   double DVR3 = (kDXF3 / kDXF1) * P.dv;
   double CONF2 = P.dv / DVR2;
@@ -840,7 +839,7 @@ __global__ void __launch_bounds__(kWalkThreads)
   __shared__ int64_t civ[kRecWin + 1];      // stream offsets of records wbase .. wbase+kRecWin
   __shared__ unsigned long long wt64[kWalkThreads / 32 + 1];
   __shared__ int wt32[kWalkThreads / 32 + 1];
-  __shared__ int sh_e0, sh_K;
+  __shared__ int sh_e0;
 
   const int layer = blockIdx.x;
   if (layer >= nlayers) return;

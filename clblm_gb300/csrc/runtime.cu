@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -70,7 +71,20 @@ struct DevBuf {
 
 namespace {
 struct BatchGraph;
-}
+
+// Launch shapes chosen by timing the variants on the handle's first real
+// work; none of them changes a result (each variant computes every value
+// with the same operations in the same order).  -1: not chosen yet.
+struct Tuner {
+  int f4[2] = {-1, -1};   // k_f4_conv records per stage: 64 / 128 / 256 (index), per precision
+  int rt[2] = {-1, -1};   // k_rt_layer threads per block: 128 / 256 / 512
+  int jac[2] = {-1, -1};  // k_jac threads per block: 64 / 128
+  bool on = true;         // CLBLM_AUTOTUNE=0: the defaults, no timing
+};
+constexpr int kF4StageRecords[3] = {64, 128, 256};
+constexpr int kRtThreads[3] = {128, 256, 512};
+constexpr int kJacThreads[2] = {64, 128};
+}  // namespace
 
 struct clblm_handle {
   int device = 0;
@@ -100,6 +114,8 @@ struct clblm_handle {
   std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
   uint64_t bgraph_clock = 0;
   bool panel_attr_set[2] = {false, false};
+  Tuner tune;
+  bool last_plain = false;  // precision of the last OD / radiance / Jacobian call
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
@@ -700,12 +716,56 @@ struct Batch {
 
 int64_t pad256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
+// The fastest of n launch variants on the work at hand: each variant runs once
+// to warm up and once timed on `st`.  The launches must be repeatable (they
+// do not write what they read).  While `st` is being captured into a graph
+// the default variant is used and nothing is chosen.
+template <typename F>
+int tune_pick(clblm_handle* h, cudaStream_t st, int n, int def, F launch, int* slot, int* use) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(h, cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {
+    *use = def;
+    return CLBLM_OK;
+  }
+  if (!h->tune.on) {
+    *slot = *use = def;
+    return CLBLM_OK;
+  }
+  cudaEvent_t a = nullptr, b = nullptr;
+  CUDA_TRY(h, cudaEventCreate(&a));
+  CUDA_TRY(h, cudaEventCreate(&b));
+  float best = 0.f;
+  int bi = def;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    launch(i);
+    e = cudaEventRecord(a, st);
+    launch(i);
+    if (e == cudaSuccess) e = cudaEventRecord(b, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess && (i == 0 || ms < best)) {
+      best = ms;
+      bi = i;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "tuning: %s", cudaGetErrorString(e));
+  *slot = *use = bi;
+  return CLBLM_OK;
+}
+
 // Runs the OD pipeline for `count` layers whose plans are already uploaded at
 // plans[first..]; OD of layer k lands at od + P.od_off (Real).
 int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t lstride,
                  int64_t f4stride, int64_t pstride) {
   const LayerPlan* dplans = h->plans.as<const LayerPlan>();
   LineIn li = line_in(h);
+  h->last_plain = plain;
   dim3 blk(256);
   // the continuum and the far-wing chain on the second stream, the line
   // chain on the handle's stream; k_panel waits for both
@@ -773,10 +833,25 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     fa.r4_all = h->r4.p;
     fa.err = h->err.as<int>();
     dim3 grid((unsigned)((maxr4 + 2 + kF4Tile - 1) / kF4Tile), count);
+    auto f4 = [&](int v) {  // records per stage: 64, 128, 256
+      if (plain) {
+        if (v == 0) k_f4_conv<true, 64><<<grid, kF4Threads, 0, st>>>(fa);
+        else if (v == 1) k_f4_conv<true, 128><<<grid, kF4Threads, 0, st>>>(fa);
+        else k_f4_conv<true, 256><<<grid, kF4Threads, 0, st>>>(fa);
+      } else {
+        if (v == 0) k_f4_conv<false, 64><<<grid, kF4Threads, 0, st>>>(fa);
+        else if (v == 1) k_f4_conv<false, 128><<<grid, kF4Threads, 0, st>>>(fa);
+        else k_f4_conv<false, 256><<<grid, kF4Threads, 0, st>>>(fa);
+      }
+    };
+    int tv = h->tune.f4[plain ? 1 : 0];
+    if (tv < 0) {
+      int rc = tune_pick(h, st, 3, 2, f4, &h->tune.f4[plain ? 1 : 0], &tv);
+      if (rc) return rc;
+    }
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-    if (plain) k_f4_conv<true><<<grid, kF4Threads, 0, st>>>(fa);
-    else k_f4_conv<false><<<grid, kF4Threads, 0, st>>>(fa);
+    f4(tv);
     CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   }
   CUDA_TRY(h, cudaEventRecord(h->join_ev, st));
@@ -1131,6 +1206,15 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
     delete h;
     return CLBLM_ERR_CUDA;
   }
+  // CLBLM_AUTOTUNE=0: default launch shapes; CLBLM_F4_STAGE_RECORDS=64|128|256:
+  // that stage size for the far-wing kernel
+  if (const char* e = std::getenv("CLBLM_AUTOTUNE"))
+    if (e[0] == '0') h->tune.on = false;
+  if (const char* e = std::getenv("CLBLM_F4_STAGE_RECORDS")) {
+    const int v = std::atoi(e);
+    for (int k = 0; k < 3; ++k)
+      if (kF4StageRecords[k] == v) h->tune.f4[0] = h->tune.f4[1] = k;
+  }
   for (auto& e : h->ev) {
     if (cudaEventCreate(&e) != cudaSuccess) {
       g_create_err = "cannot create CUDA events";
@@ -1357,6 +1441,10 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
 int clblm_gpu_od_stats(const clblm_handle_t* h, clblm_od_stats_t* stats) {
   if (!h || !stats) return CLBLM_ERR_ARG;
   *stats = h->last;
+  const int p = h->last_plain ? 1 : 0;
+  stats->f4_stage_records = h->tune.f4[p] >= 0 ? kF4StageRecords[h->tune.f4[p]] : 0;
+  stats->rt_threads = h->tune.rt[p] >= 0 ? kRtThreads[h->tune.rt[p]] : 0;
+  stats->jac_threads = h->tune.jac[p] >= 0 ? kJacThreads[h->tune.jac[p]] : 0;
   return CLBLM_OK;
 }
 
@@ -1533,10 +1621,19 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       a.vf1 = (float)P.dv;
       a.xs0 = (float)(col->v1 * (kRADCN2 / col->tskin));
       a.xs1 = (float)(in_dv * (kRADCN2 / col->tskin));
-      unsigned grid = (unsigned)((a.n_out + 255) / 256);
+      auto rt = [&](int v) {
+        const int nt = kRtThreads[v];
+        const unsigned grid = (unsigned)((a.n_out + nt - 1) / nt);
+        if (plain) k_rt_layer<true><<<grid, nt, 0, h->stream>>>(a);
+        else k_rt_layer<false><<<grid, nt, 0, h->stream>>>(a);
+      };
+      int tv = h->tune.rt[plain ? 1 : 0];
+      if (tv < 0) {
+        rc = tune_pick(h, h->stream, 3, 1, rt, &h->tune.rt[plain ? 1 : 0], &tv);
+        if (rc) return rc;
+      }
       h->launches++;
-      if (plain) k_rt_layer<true><<<grid, 256, 0, h->stream>>>(a);
-      else k_rt_layer<false><<<grid, 256, 0, h->stream>>>(a);
+      rt(tv);
       CUDA_TRY(h, cudaGetLastError());
       cur = 1 - cur;
     }
@@ -1667,6 +1764,26 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
 
 // ---- Jacobians of the nadir radiance (noScattJacob) --------------------------
 namespace {
+
+// k_jac over the block's points with the tuned block size
+int launch_jac(clblm_handle* h, const JacArgs& a, bool plain) {
+  auto jac = [&](int v) {
+    const int nt = kJacThreads[v];
+    const unsigned grid = (unsigned)((a.nout + nt - 1) / nt);
+    if (plain) k_jac<true><<<grid, nt, 0, h->stream>>>(a);
+    else k_jac<false><<<grid, nt, 0, h->stream>>>(a);
+  };
+  int tv = h->tune.jac[plain ? 1 : 0];
+  if (tv < 0) {
+    int rc = tune_pick(h, h->stream, 2, 1, jac, &h->tune.jac[plain ? 1 : 0], &tv);
+    if (rc) return rc;
+  }
+  h->launches++;
+  jac(tv);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_jac: %s", cudaGetErrorString(e));
+  return CLBLM_OK;
+}
 
 // level2layer, clblm_noScattJac.f90:1208-1279, for one molecule (level l+1
 // is the top of layer l)
@@ -2042,13 +2159,8 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     a.demis = o_dem;
     a.ld = ld;
     a.off = total;
-    h->launches++;
-    if (plain) k_jac<true><<<(unsigned)((nlim + 127) / 128), 128, 0, h->stream>>>(a);
-    else k_jac<false><<<(unsigned)((nlim + 127) / 128), 128, 0, h->stream>>>(a);
-    {
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_jac: %s", cudaGetErrorString(e));
-    }
+    rc = launch_jac(h, a, plain);
+    if (rc) return rc;
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     total += nlim;
   }
@@ -2438,11 +2550,8 @@ int batch_enqueue(clblm_handle* h, BatchPlan& bp, const clblm_profile_t* prof, c
         a.ld = np;
       }
       a.off = U.point0;
-      h->launches++;
-      if (plain) k_jac<true><<<(unsigned)((U.nlim + 127) / 128), 128, 0, h->stream>>>(a);
-      else k_jac<false><<<(unsigned)((U.nlim + 127) / 128), 128, 0, h->stream>>>(a);
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "batch k_jac: %s", cudaGetErrorString(e));
+      int rc2 = launch_jac(h, a, plain);
+      if (rc2) return rc2;
     }
   }
   return CLBLM_OK;

@@ -196,6 +196,13 @@ typedef struct {
   double  ms_f4conv;    /* device time of the far-wing convolution kernel       */
   double  ms_line_chain; /* batch start to the end of the line chain (stream 1) */
   double  ms_f4_chain;  /* batch start to the end of the far-wing chain (stream 2) */
+  /* launch shapes the autotuner chose for the handle (0: not chosen yet); no
+   * choice changes a result.  CLBLM_AUTOTUNE=0 in the environment keeps the
+   * defaults (256, 256, 128). */
+  int32_t f4_stage_records; /* far-wing records per shared-memory stage     */
+  int32_t rt_threads;       /* threads per block of the layer recurrence     */
+  int32_t jac_threads;      /* threads per block of the Jacobian recurrence  */
+  int32_t reserved;
 } clblm_od_stats_t;
 
 typedef struct clblm_handle clblm_handle_t;
