@@ -23,6 +23,7 @@ UNITS = {
     "panel.cu": [],
     "rt.cu": [],
     "jac.cu": [],
+    "scan.cu": [],
     "tape3.cpp": [],
     "runtime.cu": [],
 }
@@ -63,7 +64,9 @@ def build(force=False, verbose_ptxas=False):
         for _, log in results:
             sys.stderr.write(log)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", str(tmp), "-lcudart"]
+    cudalib = str(Path(nvcc()).resolve().parent.parent / "lib64")
+    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", str(tmp), "-lcudart", "-L", cudalib,
+           "-lcufft", "-Xlinker", "-rpath," + cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

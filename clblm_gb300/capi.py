@@ -22,7 +22,8 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_gpu_stream",
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
-           "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch")
+           "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
+           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -70,6 +71,10 @@ def lib():
         L.clblm_gpu_batch_size.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t),
                                            P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_batch.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t), C.c_int32]
+        L.clblm_gpu_fftscn_size.argtypes = [P(T.clblm_scan_t), C.c_double, C.c_double, C.c_int64, P(C.c_double),
+                                            P(C.c_double), P(C.c_int64)]
+        L.clblm_gpu_fftscn.argtypes = [C.c_void_p, P(T.clblm_scan_t), C.c_void_p, C.c_double, C.c_double, C.c_int64,
+                                       C.c_void_p, C.c_int64, C.c_int32]
         L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
                                        P(C.c_int64), C.c_char_p, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
@@ -267,6 +272,36 @@ Handle.batch_size, Handle.batch, Handle.batch_device = _batch_methods()
 def noScattJacob(handle, col, ctrl, jac):
     """Radiance and level Jacobians of a nadir column (clblm_noScattJac.f90:20)."""
     return handle.jac(col, ctrl, jac)
+
+
+def fftscn_size(scan, v1, dv, n):
+    """(V1S, DV, points) of the scanned spectrum (host arithmetic)."""
+    v1s, dvs, ns = C.c_double(), C.c_double(), C.c_int64()
+    rc = lib().clblm_gpu_fftscn_size(C.byref(scan), v1, dv, n, C.byref(v1s), C.byref(dvs), C.byref(ns))
+    if rc:
+        raise ClblmError(rc, "FFTSCN size")
+    return v1s.value, dvs.value, ns.value
+
+
+def _scan_methods():
+    def fftscn(self, scan, spect, v1, dv):
+        """clblm_FFTSCN of a binary64 spectrum on v1 + i*dv: (scanned, V1S, DV)."""
+        spect = np.ascontiguousarray(spect, dtype=np.float64)
+        v1s, dvs, ns = fftscn_size(scan, v1, dv, len(spect))
+        out = np.empty(ns)
+        self._check(lib().clblm_gpu_fftscn(self.h, C.byref(scan), spect.ctypes.data_as(C.c_void_p), v1, dv,
+                                           len(spect), out.ctypes.data_as(C.c_void_p), ns, T.CLBLM_OUT_HOST))
+        return out, v1s, dvs
+
+    def fftscn_device(self, scan, dspect, n, v1, dv, dout, cap):
+        """The same on device buffers (addresses)."""
+        self._check(lib().clblm_gpu_fftscn(self.h, C.byref(scan), C.c_void_p(dspect), v1, dv, n, C.c_void_p(dout),
+                                           cap, T.CLBLM_OUT_DEVICE))
+
+    return fftscn, fftscn_device
+
+
+Handle.fftscn, Handle.fftscn_device = _scan_methods()
 
 
 def read_tape3(path, v1=-1e30, v2=1e30):

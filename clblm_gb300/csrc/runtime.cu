@@ -8,6 +8,7 @@
 // :2349-2360 and :2496, the record logic of RDLIN :2571-2798) so that the
 // device kernels see the same panel origins, index limits and line ranges.
 #include <cuda_runtime.h>
+#include <cufft.h>
 
 #include <algorithm>
 #include <atomic>
@@ -28,6 +29,7 @@
 #include "clblm_ref_tables.h"
 #include "clblm_jac.cuh"
 #include "clblm_rt.cuh"
+#include "clblm_scan.cuh"
 
 using namespace clblm;
 
@@ -116,6 +118,12 @@ struct clblm_handle {
   bool panel_attr_set[2] = {false, false};
   Tuner tune;
   bool last_plain = false;  // precision of the last OD / radiance / Jacobian call
+  // FFT scan: cuFFT plans of the last transform size, the transform buffer
+  // and the per-record path differences
+  int64_t scan_n = 0;
+  cufftHandle scan_fwd = 0, scan_inv = 0;
+  bool scan_plans = false;
+  DevBuf scan_buf, scan_x0, scan_io;
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
@@ -1287,6 +1295,13 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   h->bgraphs.clear();
+  if (h->scan_plans) {
+    cufftDestroy(h->scan_fwd);
+    cufftDestroy(h->scan_inv);
+  }
+  h->scan_buf.release();
+  h->scan_x0.release();
+  h->scan_io.release();
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->stream2) {
@@ -2791,6 +2806,250 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
   if (rc) return rc;
   for (int i = 0; i < n; ++i)
     if (status[i]) return status[i];
+  return CLBLM_OK;
+}
+
+}  // extern "C"
+
+// ---- FFT instrument-function scan --------------------------------------------
+//
+// clblm_FFTSCN_struct (clblm_FFT.f90:352-844) for the scanning functions with
+// an analytic apodization (functID 2..8: triangle, Gaussian, sinc**2, sinc,
+// Beer, Hamming, Hanning; IVX = 1, which the reference takes whenever the
+// calculation range exceeds CRATIO half widths), the boxcar alone
+// (functID 1), pre-boxing with or without deconvolution, output on the scan
+// grid.  The host arithmetic below follows the reference's FP64 operations.
+namespace {
+
+// C, CRATIO, CLIMIT of the scanning functions, clblm_FFT.f90:108-131
+constexpr double kScanC[14] = {0.0, 2.0, 0.849322, 2.257609, 3.314800, 2.100669, 2.195676,
+                               2.0, 2.570274, 2.367714, 2.071759, -3.3, -2.5, 3.314800};
+constexpr double kScanCRatio[14] = {0.0, 40., 10., 40., 160., 20., 20., 20., 40., 40., 20., 100., 10., 1e308};
+constexpr double kScanCLimit[14] = {1., 2., 3., 40., 160., 20., 20., 20., 40., 40., 20., 100., 10., 160.};
+
+struct ScanPlan {
+  int jfn = 0;
+  double A = 0.;
+  double V1Z = 0., V2Z = 0., DV = 0.;
+  int64_t ltotal = 0, n1 = 0;   // loaded points, first input point (1-based)
+  int M = 0;                    // pre-boxing: points per mean (0: none)
+  int64_t ktotal = 0;
+  int nrec = 0;                 // records of 65536 points of the transform
+  bool fft = false, deconv = false;
+  double deconv_a = 0.;
+  int64_t N1 = 0, ntotal = 0;   // output: first point (1-based) and count
+  double V1S = 0.;
+};
+
+// LoadSpect's / Boxcar's record count: fourfold padding to a power of two
+// (clblm_FFT.f90:1160-1186, :902-925)
+int scan_records(int64_t lt) {
+  const double ardata = (double)lt / (double)kScanRecord;
+  const int64_t lrdata = (ardata - (double)(int64_t)ardata == 0.0) ? (int64_t)ardata : (int64_t)(ardata + 1.0);
+  const double power = std::log((double)lrdata) / std::log(2.0);
+  const int ip = (int)power;
+  const int e = (power - (double)ip == 0.0) ? ip + 2 : ip + 3;
+  return e < 30 ? (1 << e) : -1;
+}
+
+int scan_plan(clblm_handle* h, const clblm_scan_t* sc, double v1c, double dv, int64_t np, ScanPlan* p) {
+  auto bad = [&](int code, const char* msg) { return h ? set_err(h, code, "%s", msg) : code; };
+  if (!sc || !(dv > 0.) || np < 2) return bad(CLBLM_ERR_ARG, "FFTSCN: bad spectrum");
+  const double v2c = v1c + dv * (double)(np - 1);
+  const double fill = sc->padding, hwhm = sc->hwhm;
+  if (fill < 0. || fill > 1.) return bad(CLBLM_ERR_ARG, "FFTSCN: FILL value is out of range");
+  const int jfn = sc->funct_id - 1;
+  bool prebox = false, deconv = false;
+  double boxhw = 0.;
+  if (jfn == 0) {
+    prebox = true;
+    boxhw = hwhm;
+  } else if (jfn >= 1 && jfn <= 7) {
+    if (sc->prebox_hw > 0.) {
+      prebox = true;
+      deconv = sc->deconv_prebox != 0;
+      boxhw = sc->prebox_hw;
+    }
+  } else {
+    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: scanning functions 9..14 and deconvolution only are not on this path");
+  }
+  if (!(hwhm > 0.)) return bad(CLBLM_ERR_ARG, "FFTSCN: HWHM must be positive");
+  p->jfn = jfn;
+  p->A = jfn > 0 ? kScanC[jfn] * hwhm : 0.;
+  const double V1out = sc->v1out, V2out = sc->v2out;
+  if (V1out >= V2out) return bad(CLBLM_ERR_ARG, "FFTSCN: Initial V >= final V");
+  if (V1out >= v2c || V2out <= v1c) return bad(CLBLM_ERR_ARG, "FFTSCN: V1out to V2out is outside the data range");
+  double V1Z = V1out - hwhm * kScanCLimit[jfn];
+  double V2Z = V2out + hwhm * kScanCLimit[jfn];
+  V1Z = v1c + (double)(int64_t)((V1Z - v1c) / dv) * dv;
+  V2Z = v1c + (double)(int64_t)((V2Z - v1c) / dv + 1.01) * dv;
+  if (V1Z < v1c) V1Z = v1c;
+  if (V2Z > v2c) V2Z = v2c;
+  if ((V2Z - V1Z) / hwhm < kScanCLimit[jfn]) return bad(CLBLM_ERR_RANGE, "FFTSCN: insufficient data");
+  const double DVN = 2. * hwhm / 12.;
+  if (dv > DVN && jfn != 0)
+    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: input grid coarser than 2*HWHM/12 (interpolation not on this path)");
+  if (jfn != 0 && !((V2Z - V1Z) / hwhm > kScanCRatio[jfn]))
+    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: apodization from the scanning function's transform (IVX = -1) "
+                                      "is not on this path");
+  // LoadSpect
+  int64_t lt = (int64_t)((V2Z - V1Z) / dv + 1.1);
+  V2Z = V1Z + dv * (double)(lt - 1);
+  p->n1 = (int64_t)((V1Z - v1c) / dv + 1.00001);
+  if (p->n1 < 1 || p->n1 - 1 + lt > np) return bad(CLBLM_ERR_RANGE, "FFTSCN: ran out of data");
+  p->ltotal = lt;
+  p->nrec = scan_records(lt);
+  double DV = dv;
+  p->M = 0;
+  p->deconv = false;
+  if (prebox) {
+    const int M = (int)(2.0 * boxhw / DV);
+    if (M >= 2) {
+      V1Z = V1Z + DV * (double)(M - 1) / 2.0;
+      p->ktotal = lt / M;
+      DV = (double)M * DV;
+      V2Z = V1Z + DV * (double)(p->ktotal - 1);
+      p->M = M;
+      p->nrec = scan_records(p->ktotal);
+      p->deconv = deconv;
+      p->deconv_a = DV;
+      lt = p->ktotal;
+    }
+  }
+  if (p->nrec < 0) return bad(CLBLM_ERR_RANGE, "FFTSCN: transform too large");
+  p->fft = jfn != 0 || p->deconv;
+  p->V1Z = V1Z;
+  p->V2Z = V2Z;
+  p->DV = DV;
+  int64_t N1 = (int64_t)((V1out - V1Z) / DV);
+  double V1S = V1Z + (double)(N1 - 1) * DV;
+  if (V1S < V1Z) {
+    N1 = 1;
+    V1S = V1Z;
+  }
+  int64_t N2 = (int64_t)((V2out - V1Z) / DV + 3.01);
+  const double V2S = V1Z + (double)(N2 - 1) * DV;
+  if (V2S > V2Z) N2 = (int64_t)((V2Z - V1Z) / DV + 1.01);
+  p->N1 = N1;
+  p->ntotal = N2 - N1 + 1;
+  p->V1S = V1S;
+  if (p->ntotal < 1 || N1 - 1 + p->ntotal > (int64_t)p->nrec * kScanRecord)
+    return bad(CLBLM_ERR_RANGE, "FFTSCN: output outside the transform");
+  return CLBLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clblm_gpu_fftscn_size(const clblm_scan_t* scan, double v1, double dv, int64_t n, double* v1s, double* dvs,
+                          int64_t* ns) {
+  ScanPlan p;
+  int rc = scan_plan(nullptr, scan, v1, dv, n, &p);
+  if (rc) return rc;
+  if (v1s) *v1s = p.V1S;
+  if (dvs) *dvs = p.DV;
+  if (ns) *ns = p.ntotal;
+  return CLBLM_OK;
+}
+
+int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* spect, double v1, double dv,
+                     int64_t n, double* out, int64_t cap, int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  if (!spect || !out) return set_err(h, CLBLM_ERR_ARG, "FFTSCN: null spectrum or output");
+  ScanPlan p;
+  int rc = scan_plan(h, scan, v1, dv, n, &p);
+  if (rc) return rc;
+  if (cap < p.ntotal) return set_err(h, CLBLM_ERR_CAPACITY, "FFTSCN: output needs %lld points", (long long)p.ntotal);
+  h->reset_call();
+  const bool dev = flags == CLBLM_OUT_DEVICE;
+  const int64_t N = (int64_t)p.nrec * kScanRecord;
+  cudaStream_t st = h->stream;
+  // the input spectrum's used span on the device
+  const double* din = spect;
+  int64_t off = p.n1 - 1;
+  if (!dev) {
+    CUDA_TRY(h, h->scan_io.ensure(sizeof(double) * (size_t)std::max<int64_t>(p.ltotal, p.ntotal)));
+    CUDA_TRY(h, cudaMemcpyAsync(h->scan_io.p, spect + off, sizeof(double) * p.ltotal, cudaMemcpyHostToDevice, st));
+    din = h->scan_io.as<double>();
+    off = 0;
+  }
+  // transform buffer: N reals, in place as N/2+1 complex
+  CUDA_TRY(h, h->scan_buf.ensure(sizeof(double2) * (size_t)(N / 2 + 1)));
+  double* x = h->scan_buf.as<double>();
+  const unsigned grid = (unsigned)std::min<int64_t>((N + 255) / 256, 152 * 32);
+  h->launches++;
+  k_scan_load<<<grid, 256, 0, st>>>(din, off, p.ltotal, p.M, p.ktotal, scan->padding, x, N);
+  CUDA_TRY(h, cudaGetLastError());
+  if (p.fft) {
+    if (!h->scan_plans || h->scan_n != N) {
+      if (h->scan_plans) {
+        cufftDestroy(h->scan_fwd);
+        cufftDestroy(h->scan_inv);
+        h->scan_plans = false;
+      }
+      if (N > (int64_t)1 << 30 || cufftPlan1d(&h->scan_fwd, (int)N, CUFFT_D2Z, 1) != CUFFT_SUCCESS)
+        return set_err(h, CLBLM_ERR_OOM, "FFTSCN: no cuFFT plan for %lld points", (long long)N);
+      if (cufftPlan1d(&h->scan_inv, (int)N, CUFFT_Z2D, 1) != CUFFT_SUCCESS) {
+        cufftDestroy(h->scan_fwd);
+        return set_err(h, CLBLM_ERR_OOM, "FFTSCN: no cuFFT plan for %lld points", (long long)N);
+      }
+      h->scan_plans = true;
+      h->scan_n = N;
+    }
+    if (cufftSetStream(h->scan_fwd, st) != CUFFT_SUCCESS || cufftSetStream(h->scan_inv, st) != CUFFT_SUCCESS)
+      return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: cufftSetStream");
+    if (cufftExecD2Z(h->scan_fwd, x, reinterpret_cast<cufftDoubleComplex*>(x)) != CUFFT_SUCCESS)
+      return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: forward transform");
+    // path differences at the start of every record, accumulated as
+    // Scnfnt leaves X after each record (X0 + 32768*DX)
+    ScanArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.jfn = p.jfn;
+    a.A = p.A;
+    a.DX = 1.0 / ((double)((int64_t)kScanRecord * p.nrec) * p.DV);
+    a.nhalf = N / 2;
+    std::vector<double> x0(p.nrec);
+    double X = 0.;
+    for (int j = 0; j < p.nrec; ++j) {
+      x0[j] = X;
+      if (p.jfn == 4 && a.nedge < kScanMaxEdges) {  // the rectangle's interpolated end point
+        const double alen = 1.0 / p.A;
+        int64_t nn = (int64_t)((alen - X) / a.DX) + 1;
+        double r = (alen - X) / a.DX + 1.0 - (double)nn;
+        if (r <= 0.5) {
+          r = r + 1.0;
+          nn = nn - 1;
+        }
+        if (nn >= 1 && nn <= kScanHalf - 1) {
+          a.edge_k[a.nedge] = (int64_t)j * kScanHalf + nn;
+          a.edge_v[a.nedge] = r - 0.5;
+          a.nedge++;
+        }
+      }
+      X = X + (double)kScanRecord * a.DX / 2.0;
+    }
+    CUDA_TRY(h, h->scan_x0.ensure(sizeof(double) * (size_t)p.nrec));
+    CUDA_TRY(h, cudaMemcpyAsync(h->scan_x0.p, x0.data(), sizeof(double) * p.nrec, cudaMemcpyHostToDevice, st));
+    a.X0 = h->scan_x0.as<double>();
+    a.deconv = p.deconv ? 1 : 0;
+    a.deconv_a = p.deconv_a;
+    h->launches++;
+    k_scan_apod<<<grid, 256, 0, st>>>(a, reinterpret_cast<double2*>(x));
+    CUDA_TRY(h, cudaGetLastError());
+    if (cufftExecZ2D(h->scan_inv, reinterpret_cast<cufftDoubleComplex*>(x), x) != CUFFT_SUCCESS)
+      return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: inverse transform");
+    CUDA_TRY(h, cudaStreamSynchronize(st));  // x0 goes out of scope
+  }
+  double* dst = dev ? out : h->scan_io.as<double>();
+  h->launches++;
+  k_scan_out<<<(unsigned)std::min<int64_t>((p.ntotal + 255) / 256, 152 * 32), 256, 0, st>>>(
+      x, p.N1 - 1, p.ntotal, p.fft ? 1.0 / (double)N : 1.0, dst);
+  CUDA_TRY(h, cudaGetLastError());
+  if (!dev) CUDA_TRY(h, cudaMemcpyAsync(out, dst, sizeof(double) * p.ntotal, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  h->last.launches = h->launches;
   return CLBLM_OK;
 }
 

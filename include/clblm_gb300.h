@@ -336,6 +336,39 @@ int clblm_gpu_batch_size(clblm_handle_t *h, const clblm_profile_t *prof,
 int clblm_gpu_batch(clblm_handle_t *h, clblm_profile_t *prof, int32_t n,
                     const clblm_rt_ctrl_t *ctrl, int32_t flags);
 
+/* ---- instrument-function scan ----------------------------------------------
+ *
+ * clblm_FFTSCN (clblm_FFT.f90:308-844): a spectrum on a uniform grid
+ * convolved with a scanning function through Fourier transforms, as the
+ * post-processing of RT_Jac (postProc_scan) applies it.  On this path: the
+ * scanning functions whose apodization the reference computes analytically
+ * (functID 2..8: triangle, Gaussian, sinc**2, sinc, Beer, Hamming, Hanning;
+ * the reference takes that branch whenever the calculation range exceeds
+ * CRATIO half widths), the boxcar alone (functID 1), pre-boxing with or
+ * without its deconvolution; the result stays on the scan grid.  The
+ * reference's transform is zero-padded (FILL) to four times the next power
+ * of two of its 65536-point records; this one is the same size. */
+typedef struct {
+  int32_t funct_id;      /* 1: boxcar only; 2..8: triangle, Gaussian, sinc**2,
+                          * sinc, Beer, Hamming, Hanning                      */
+  int32_t deconv_prebox; /* 1: deconvolve the pre-boxing                     */
+  double  hwhm;          /* functHWHM [cm-1] (sinc: 1/(3.3148 * OPD))        */
+  double  padding;       /* FILL in [0, 1]: 0 for radiance, 1 transmittance  */
+  double  prebox_hw;     /* preBoxHW [cm-1]; <= 0: no pre-boxing             */
+  double  v1out, v2out;  /* requested limits [cm-1]                          */
+} clblm_scan_t;
+
+/* Grid of the scanned spectrum of a spectrum on v1 + i*dv, i < n: first
+ * wavenumber V1S, spacing (dv, or M*dv after pre-boxing) and points.  Host
+ * arithmetic only. */
+int clblm_gpu_fftscn_size(const clblm_scan_t *scan, double v1, double dv,
+                          int64_t n, double *v1s, double *dvs, int64_t *ns);
+/* The scanned spectrum into out[cap]; spect and out are host buffers, or
+ * device buffers with CLBLM_OUT_DEVICE.  binary64 throughout. */
+int clblm_gpu_fftscn(clblm_handle_t *h, const clblm_scan_t *scan,
+                     const double *spect, double v1, double dv, int64_t n,
+                     double *out, int64_t cap, int32_t flags);
+
 /* Lines of an LNFL line file (TAPE3) as read by RDLIN (clblm_ODLAY.f90:
  * 2645-2700) through CLBLM_LineData (clblm_LineData.f90:52-161): Fortran
  * unformatted records (4-byte length markers), the file header, the optional
