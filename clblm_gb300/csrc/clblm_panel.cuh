@@ -35,7 +35,16 @@ struct PanelArgs {
   const int* pmax_g;         // per grid: running max of g_hi over the records
   const int* smin_g;         // per grid: running min (from the right) of g_lo
   int* err;
+  // radiation-term segments of panels with more than kMaxSeg of them (low
+  // wavenumbers at coarse DV): slots of kSegSlot entries claimed by atomics
+  int* seg_next;             // next free slot
+  int seg_slots;             // slots in the pool
+  int* seg_pool_start;       // [slot][kSegSlot + 1]
+  double* seg_pool_v;        // [slot][kSegSlot]
+  double* seg_pool_d;
 };
+constexpr int kSegSlot = kNLIM1 + 1;  // at most one segment per point of a panel
+constexpr int kSegPoolSlots = 4096;
 
 // far-wing pseudo-line prepared for the convolution (CNVF4Q per-line set-up),
 // FP32 form of the mixed path: 80 bytes, staged in shared memory in chunks.

@@ -117,7 +117,7 @@ struct PanelSmem<false> : PanelTiles {
   float r2[kR2Pts];      // R2 p-frame 0..615
   int seg_start[kMaxSeg + 1];
   float segf_v[kMaxSeg], segf_d[kMaxSeg];
-  int nseg;
+  int nseg, seg_slot;  // seg_slot >= 0: the segments are in that pool slot
 };
 template <>
 struct PanelSmem<true> : PanelTiles {
@@ -130,7 +130,7 @@ struct PanelSmem<true> : PanelTiles {
   double r2[kR2Pts];
   int seg_start[kMaxSeg + 1];
   double seg_v[kMaxSeg], seg_d[kMaxSeg];
-  int nseg;
+  int nseg, seg_slot;
 };
 
 size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArg
   // units 0..kTiles3-1: 32 new points each; unit kTiles3: the 8 old points
   static_assert(kTiles3 + 1 < kPanelWarps, "the last warp has no R3 unit");
   if (warp == kPanelWarps - 1 && lane == 0) {  // idle in the R3 phase: radiation-term segments (panelOut, JRAD = 0)
-    int ns = 0;
+    int ns = 0, slot = -1;
     if (P.jrad == 0) {
       const int NLO = kNSHIFT + 1;
       double XKT = P.tave / kRADCN2;
@@ -559,13 +559,50 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArg
             S.segf_v[ns] = (float)RADVI;
             S.segf_d[ns] = (float)RDEL;
           }
+        } else {
+          if (slot < 0) {  // more segments than shared memory holds: move to a pool slot
+            slot = atomicAdd(a.seg_next, 1);
+            if (slot >= a.seg_slots) {
+              atomicOr(a.err, 1);
+              slot = -1;
+              ns = 0;
+              break;
+            }
+            int* gs = a.seg_pool_start + (int64_t)slot * (kSegSlot + 1);
+            double* gv = a.seg_pool_v + (int64_t)slot * kSegSlot;
+            double* gd = a.seg_pool_d + (int64_t)slot * kSegSlot;
+            for (int q = 0; q < kMaxSeg; ++q) {
+              gs[q] = S.seg_start[q];
+              if constexpr (Plain) {
+                gv[q] = S.seg_v[q];
+                gd[q] = S.seg_d[q];
+              } else {
+                gv[q] = S.segf_v[q];
+                gd[q] = S.segf_d[q];
+              }
+            }
+          }
+          if (ns >= kSegSlot) {  // cannot happen: a segment spans at least one point
+            atomicOr(a.err, 1);
+            ns = 0;
+            break;
+          }
+          a.seg_pool_start[(int64_t)slot * (kSegSlot + 1) + ns] = N1;
+          if constexpr (Plain) {
+            a.seg_pool_v[(int64_t)slot * kSegSlot + ns] = RADVI;
+            a.seg_pool_d[(int64_t)slot * kSegSlot + ns] = RDEL;
+          } else {  // the values the mixed path uses are FP32
+            a.seg_pool_v[(int64_t)slot * kSegSlot + ns] = (float)RADVI;
+            a.seg_pool_d[(int64_t)slot * kSegSlot + ns] = (float)RDEL;
+          }
         }
         ns++;
       } while (N2 < NHI);
-      if (ns > kMaxSeg) atomicOr(a.err, 1);
-      S.seg_start[min(ns, kMaxSeg)] = NHI + 1;
+      if (slot >= 0) a.seg_pool_start[(int64_t)slot * (kSegSlot + 1) + ns] = NHI + 1;
+      else S.seg_start[ns] = NHI + 1;
     }
-    S.nseg = min(ns, kMaxSeg);
+    S.nseg = ns;
+    S.seg_slot = slot;
   }
   for (int u = warp; u <= kTiles3; u += kPanelWarps) {
     const bool old = (u == kTiles3);
@@ -703,19 +740,31 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArg
         else v = X03 * R2[J2 - 1] + X02 * R2[J2] + X01 * R2[J2 + 1] + X00 * R2[J2 + 2];
         acc.add(v);
         Real val = acc.value();
-        if (P.jrad == 0) {
+        if (P.jrad == 0 && S.nseg > 0) {
           // segment of J: largest s with seg_start[s] <= J
+          const int slot = S.seg_slot;
+          const int* ss = slot < 0 ? S.seg_start : a.seg_pool_start + (int64_t)slot * (kSegSlot + 1);
           int s0 = 0, s1 = S.nseg;
           while (s1 - s0 > 1) {
             int m = (s0 + s1) >> 1;
-            if (S.seg_start[m] <= J) s0 = m;
+            if (ss[m] <= J) s0 = m;
             else s1 = m;
           }
-          if constexpr (Plain) {
-            double f = S.seg_v[s0] + (double)(J - S.seg_start[s0]) * S.seg_d[s0];
-            val = val * f;
+          if (slot < 0) {
+            if constexpr (Plain) {
+              double f = S.seg_v[s0] + (double)(J - S.seg_start[s0]) * S.seg_d[s0];
+              val = val * f;
+            } else {
+              val *= fmaf((float)(J - S.seg_start[s0]), S.segf_d[s0], S.segf_v[s0]);
+            }
           } else {
-            val *= fmaf((float)(J - S.seg_start[s0]), S.segf_d[s0], S.segf_v[s0]);
+            const double gv = a.seg_pool_v[(int64_t)slot * kSegSlot + s0];
+            const double gd = a.seg_pool_d[(int64_t)slot * kSegSlot + s0];
+            if constexpr (Plain) {
+              val = val * (gv + (double)(J - ss[s0]) * gd);
+            } else {
+              val *= fmaf((float)(J - ss[s0]), (float)gd, (float)gv);
+            }
           }
         }
         od[(int64_t)kPanelPts * p + (J - kNSHIFT - 1)] = val;

@@ -111,6 +111,7 @@ struct clblm_handle {
   DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
   DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt, ragg;
+  DevBuf segpool;  // radiation-term segments of panels with more than kMaxSeg
   DevBuf rt[4], outbuf, imap[2];
   // batched profiles: captured launch sequences of recent batches
   std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
@@ -920,6 +921,18 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.smin_g = h->gsm.as<int>();
   pa.err = h->err.as<int>();
   {
+    // (allocated with the workspace, before any capture)
+    const size_t start_b = sizeof(int) * (size_t)kSegPoolSlots * (kSegSlot + 1);
+    const size_t val_b = sizeof(double) * (size_t)kSegPoolSlots * kSegSlot;
+    unsigned char* b = h->segpool.as<unsigned char>();
+    pa.seg_next = reinterpret_cast<int*>(b);
+    pa.seg_slots = kSegPoolSlots;
+    pa.seg_pool_start = reinterpret_cast<int*>(b + 256);
+    pa.seg_pool_v = reinterpret_cast<double*>(b + 256 + start_b);
+    pa.seg_pool_d = reinterpret_cast<double*>(b + 256 + start_b + val_b);
+    CUDA_TRY(h, cudaMemsetAsync(pa.seg_next, 0, sizeof(int), st));
+  }
+  {
     int maxb = 1;
     for (int k = 0; k < count; ++k) maxb = std::max(maxb, hps[first + k].P.nblk4);
     h->launches++;
@@ -1053,6 +1066,8 @@ int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
   CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
   CUDA_TRY(h, h->f4sm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
   CUDA_TRY(h, h->err.ensure(sizeof(int) * 4));
+  CUDA_TRY(h, h->segpool.ensure(256 + (sizeof(int) * (kSegSlot + 1) + 2 * sizeof(double) * kSegSlot) *
+                                          (size_t)kSegPoolSlots));
   CUDA_TRY(h, h->pblk.ensure(sizeof(int) * vftt));
   CUDA_TRY(h, h->bv1.ensure(sizeof(double) * (blkt + 1)));
   CUDA_TRY(h, h->bn.ensure(sizeof(int) * (blkt + 1)));
@@ -1135,7 +1150,8 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
   CUDA_TRY(h, cudaMemcpyAsync(nout.data(), h->f4nout.p, sizeof(int64_t) * 2 * nL, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   CUDA_TRY(h, cudaGetLastError());
-  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "more than %d radiation-term segments in a panel", kMaxSeg);
+  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "radiation-term segments: more than %d panels of a batch "
+                                 "need more than %d", kSegPoolSlots, kMaxSeg);
   if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
   if (err[0] & 4) return set_err(h, CLBLM_ERR_CUDA, "far-wing records: a shared-memory stage never arrived");
   {
@@ -1287,7 +1303,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
                     &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
                     &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
                     &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->f4nxt,   &h->ragg,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
+                    &h->f4cut,     &h->f4grp,    &h->f4nxt,   &h->ragg,  &h->segpool,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
                     &h->jblk};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : h->rt) b.release();
@@ -2586,7 +2602,8 @@ int batch_check(clblm_handle* h, const std::vector<int>& job_prof, std::vector<i
                               h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   CUDA_TRY(h, cudaGetLastError());
-  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "more than %d radiation-term segments in a panel", kMaxSeg);
+  if (err[0] & 1) return set_err(h, CLBLM_ERR_RANGE, "radiation-term segments: more than %d panels of a batch "
+                                 "need more than %d", kSegPoolSlots, kMaxSeg);
   if (err[0] & 2) return set_err(h, CLBLM_ERR_RANGE, "shape-table index beyond NFMX");
   if (err[0] & 4) return set_err(h, CLBLM_ERR_CUDA, "far-wing records: a shared-memory stage never arrived");
   int first_bad = CLBLM_OK;
