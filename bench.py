@@ -345,6 +345,76 @@ def batch_leg(cont, steps, per_call=16):
     return res
 
 
+def config4_leg(steps):
+    """Broadband case: 3,000,000 lines on 10-3500 cm-1, 100 layers 1013 to
+    0.01 hPa, synthetic continuum.  The nadir radiance (mixed timed, FP64
+    once), its FFT scans to instrument resolution (sinc of maximum OPD
+    0.8 cm, and the Gaussian of the same half width), and radiance plus the
+    T and ln q(H2O) Jacobians of all 101 levels (noScattJacob, mixed)."""
+    import torch
+    from clblm_gb300 import capi, synth
+    from clblm_gb300 import capi_types as T
+    lines, col, cont = synth.config4()
+    h = capi.Handle(lines, cont)
+    res = {"workload": "3,000,000 lines, 10-3500 cm-1, 100 layers 1013-0.01 hPa: nadir radiance, FFT scans "
+                       "(sinc OPD 0.8 cm; Gaussian), radiance + dR/dT and dR/dln q(H2O) of every level"}
+    rad = {}
+    for name, prec, k in (("mixed", T.CLBLM_PREC_MIXED, steps), ("plain", T.CLBLM_PREC_PLAIN, 1)):
+        ctrl = T.rt_ctrl(precision=prec)
+        n, dv = h.rt_size(col, ctrl)
+        out = torch.empty(n, dtype=torch.float64, device="cuda")
+        h.rt_mode2_device(col, ctrl, out.data_ptr(), n)  # warm-up (workspace, tuning)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            h.rt_mode2_device(col, ctrl, out.data_ptr(), n)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / k
+        st = h.stats()  # the last call's per-stream stage times (all OD batches)
+        lp = layer_points(h, col, ctrl)
+        res["radiance_" + name] = {"ms": ms, "value": lp / (ms * 1e-3), "unit": UNIT, "layer_points": lp,
+                                   "stages_ms": {"line_chain": st["ms_line_chain"],
+                                                 "far_wing_chain": st["ms_f4_chain"],
+                                                 "k_f4_conv": st["ms_f4conv"], "k_panel": st["ms_panel"]}}
+        res["radiance_points"], res["dv"] = n, dv
+        rad[name] = out
+    m, p = rad["mixed"], rad["plain"]
+    res["max_rel_rad_diff_mixed_vs_plain"] = float(((m - p).abs() / p.abs()).max())
+    res["radiance_speedup_mixed_vs_plain"] = res["radiance_plain"]["ms"] / res["radiance_mixed"]["ms"]
+    # instrument-function scans of the mixed radiance, on the device
+    hw = 1.0 / (0.8 * 3.314800)
+    for name, fid in (("sinc", 5), ("gaussian", 3)):
+        sc = T.scan_struct(fid, hw, 20.0, 3490.0)
+        v1s, dvs, ns = capi.fftscn_size(sc, col.v1, res["dv"], len(m))
+        o = torch.empty(ns, dtype=torch.float64, device="cuda")
+        h.fftscn_device(sc, m.data_ptr(), len(m), col.v1, res["dv"], o.data_ptr(), ns)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            h.fftscn_device(sc, m.data_ptr(), len(m), col.v1, res["dv"], o.data_ptr(), ns)
+        torch.cuda.synchronize()
+        res["scan_" + name] = {"ms": (time.perf_counter() - t0) * 1e3 / 3, "hwhm": hw, "points": ns, "dv": dvs}
+    del rad
+    # radiance + Jacobians (mixed; FP64 too when asked: about half a minute)
+    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_MIXED, grid_type=1)
+    prof = synth.jac_profile(col)
+    n, dv = h.jac_size(col, ctrl, prof)
+    nl = col.nlay
+    o = {key: torch.empty(shape, dtype=torch.float64, device="cuda")
+         for key, shape in (("rad", n), ("dtlev", (nl + 1, n)), ("dqlev", (nl + 1, n)), ("dtsfc", n), ("demis", n))}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h.jac_device(col, ctrl, prof, o["rad"].data_ptr(), o["dtlev"].data_ptr(), o["dqlev"].data_ptr(),
+                 o["dtsfc"].data_ptr(), o["demis"].data_ptr(), n)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    res["jacobians_mixed"] = {"ms": ms, "points": n, "dv": dv, "value": n * nl / (ms * 1e-3), "unit": UNIT}
+    del o
+    h.close()
+    torch.cuda.empty_cache()
+    return res
+
+
 def profile_case(args):
     """A bounded case for ncu captures of one kernel: the OD of one layer of the
     60-layer column over a narrower window (the full line list stays on the
@@ -400,6 +470,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 GPU leg")
     ap.add_argument("--no-jac", action="store_true", help="skip the Jacobian leg (600-1100 cm-1)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-profiles leg (256 profiles)")
+    ap.add_argument("--no-config4", action="store_true", help="skip the broadband leg (3 M lines, 100 layers)")
     ap.add_argument("--profile-layer", type=int, default=None,
                     help="profiling case: the OD of this one layer of the column, three calls, no JSON line")
     ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
@@ -543,6 +614,9 @@ def main():
     batl = None
     if not args.no_batch:
         batl = batch_leg(cont, 1)
+    c4 = None
+    if not args.no_config4:
+        c4 = config4_leg(2)
     roof = roofline(work, kt, args.steps, ms)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -555,7 +629,7 @@ def main():
                            "l2": "inputs larger than L2, no flush"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": e2e_ms},
-                "plain_fp64": plain, "jacobians": jacl, "batched_profiles": batl, "cpu_baseline": cpu, "roofline": roof,
+                "plain_fp64": plain, "jacobians": jacl, "batched_profiles": batl, "broadband": c4, "cpu_baseline": cpu, "roofline": roof,
                 "clocks": clk.summary(),
                 "gpu_launches": int(kt["launches"]),
                 # per step, from events on the library's two streams: the line chain

@@ -725,6 +725,19 @@ struct Batch {
 
 int64_t pad256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
+// Bytes of OD-pipeline workspace one batch of layers may take: half of the
+// device memory free at the call (the layers of a batch share launches, and
+// every batch replays the far-wing walk's serial record loop, so fewer,
+// larger batches are faster), between 8 and 96 GB.  The estimate per layer
+// is the sum of the per-line and per-point buffers.
+size_t od_batch_budget() {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return (size_t)24 << 30;
+  const size_t lo = (size_t)8 << 30, hi = (size_t)96 << 30;
+  const size_t half = free_b / 2;
+  return half < lo ? lo : (half > hi ? hi : half);
+}
+
 // The fastest of n launch variants on the work at hand: each variant runs once
 // to warm up and once timed on `st`.  The launches must be repeatable (they
 // do not write what they read).  While `st` is being captured into a graph
@@ -1589,7 +1602,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
   for (int il = 0; il < n; ++il) maxn = std::max(maxn, rp.grid_n[il]);
   for (auto& b : h->rt) CUDA_TRY(h, b.ensure(real * (maxn + 8)));
   // layers in batches sized to the workspace budget
-  const size_t budget = (size_t)24 << 30;
+  const size_t budget = od_batch_budget();
   int cur = 0;  // ping-pong index of the merged spectra
   for (int first = 0; first < n;) {
     int count = 0;
@@ -2061,7 +2074,7 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
   int jr = h->jrad;
   bool fp = h->first_pass_jrad;
   int64_t total = 0;
-  const size_t budget = (size_t)24 << 30;
+  const size_t budget = od_batch_budget();
   for (auto& blk : blocks) {
     std::vector<HostPlan> hps;
     int64_t nlim;
