@@ -345,7 +345,7 @@ def batch_leg(cont, steps, per_call=16):
     return res
 
 
-def config4_leg(steps):
+def config4_leg(steps, fp64_jacobians=False):
     """Broadband case: 3,000,000 lines on 10-3500 cm-1, 100 layers 1013 to
     0.01 hPa, synthetic continuum.  The nadir radiance (mixed timed, FP64
     once), its FFT scans to instrument resolution (sinc of maximum OPD
@@ -396,20 +396,33 @@ def config4_leg(steps):
         res["scan_" + name] = {"ms": (time.perf_counter() - t0) * 1e3 / 3, "hwhm": hw, "points": ns, "dv": dvs}
     del rad
     # radiance + Jacobians (mixed; FP64 too when asked: about half a minute)
-    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_MIXED, grid_type=1)
     prof = synth.jac_profile(col)
-    n, dv = h.jac_size(col, ctrl, prof)
     nl = col.nlay
-    o = {key: torch.empty(shape, dtype=torch.float64, device="cuda")
-         for key, shape in (("rad", n), ("dtlev", (nl + 1, n)), ("dqlev", (nl + 1, n)), ("dtsfc", n), ("demis", n))}
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    h.jac_device(col, ctrl, prof, o["rad"].data_ptr(), o["dtlev"].data_ptr(), o["dqlev"].data_ptr(),
-                 o["dtsfc"].data_ptr(), o["demis"].data_ptr(), n)
-    torch.cuda.synchronize()
-    ms = (time.perf_counter() - t0) * 1e3
-    res["jacobians_mixed"] = {"ms": ms, "points": n, "dv": dv, "value": n * nl / (ms * 1e-3), "unit": UNIT}
-    del o
+    jrad = {}
+    for name, prec in (("mixed", T.CLBLM_PREC_MIXED), ("plain", T.CLBLM_PREC_PLAIN)):
+        if name == "plain" and not fp64_jacobians:
+            continue
+        ctrl = T.rt_ctrl(precision=prec, grid_type=1)
+        n, dv = h.jac_size(col, ctrl, prof)
+        o = {key: torch.empty(shape, dtype=torch.float64, device="cuda")
+             for key, shape in (("rad", n), ("dtlev", (nl + 1, n)), ("dqlev", (nl + 1, n)), ("dtsfc", n),
+                                ("demis", n))}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.jac_device(col, ctrl, prof, o["rad"].data_ptr(), o["dtlev"].data_ptr(), o["dqlev"].data_ptr(),
+                     o["dtsfc"].data_ptr(), o["demis"].data_ptr(), n)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
+        res["jacobians_" + name] = {"ms": ms, "points": n, "dv": dv, "value": n * nl / (ms * 1e-3), "unit": UNIT}
+        jrad[name] = o["rad"]
+        del o
+    if "plain" in jrad:
+        m, p = jrad["mixed"], jrad["plain"]
+        res["jacobian_leg_max_rel_rad_diff_mixed_vs_plain"] = float(((m - p).abs() / p.abs()).max())
+        tm = res["radiance_mixed"]["ms"] + res["jacobians_mixed"]["ms"]
+        tp = res["radiance_plain"]["ms"] + res["jacobians_plain"]["ms"]
+        res["speedup_radiance_plus_jacobians_mixed_vs_plain"] = tp / tm
+    del jrad
     h.close()
     torch.cuda.empty_cache()
     return res
@@ -471,6 +484,8 @@ def main():
     ap.add_argument("--no-jac", action="store_true", help="skip the Jacobian leg (600-1100 cm-1)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-profiles leg (256 profiles)")
     ap.add_argument("--no-config4", action="store_true", help="skip the broadband leg (3 M lines, 100 layers)")
+    ap.add_argument("--broadband-fp64-jacobians", action="store_true",
+                    help="also time the broadband Jacobians in FP64 (about half a minute more)")
     ap.add_argument("--profile-layer", type=int, default=None,
                     help="profiling case: the OD of this one layer of the column, three calls, no JSON line")
     ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
@@ -616,7 +631,7 @@ def main():
         batl = batch_leg(cont, 1)
     c4 = None
     if not args.no_config4:
-        c4 = config4_leg(2)
+        c4 = config4_leg(2, fp64_jacobians=args.broadband_fp64_jacobians)
     roof = roofline(work, kt, args.steps, ms)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
