@@ -632,11 +632,18 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           else
             SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
         }
-        double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
-        double ALFA0I = alfa * TMPCOR;
-        double HWHMSI = hwhm * TMPCOR;
-        r.alfa = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
-        r.alfd = VNU * P.alfd1[m];
+        if (P.mixed) {  // widths set no index or group: FP32
+          const float TMPCOR = __expf(lines.tmpalf[i] * (float)P.ln_tratio);  // (T/296)^n
+          const float rs = (float)P.rhoslf[m];
+          r.alfa = ((float)alfa * TMPCOR) * ((float)P.rhorat - rs) + ((float)hwhm * TMPCOR) * rs;
+          r.alfd = (float)VNU * (float)P.alfd1[m];
+        } else {
+          double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
+          double ALFA0I = alfa * TMPCOR;
+          double HWHMSI = hwhm * TMPCOR;
+          r.alfa = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
+          r.alfd = VNU * P.alfd1[m];
+        }
         r.sp = SUI * (1. + 0. * P.pavp2);
         r.vnu = VNU;
         r.mol = m;
@@ -1085,53 +1092,84 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
 // the global far-wing grid V1R4 + (J-1)*DVR4.  Lines at 0 < vnu <= 25 cm-1
 // also get a Van Vleck-Weisskopf mirror record at -vnu (:480-487), appended
 // after the direct records.
+// CNVF4Q's per-line set-up (clblm_ODLAY_LineF4.f90:218-283).  The point
+// range JMIN..JMAX and the offset of the nearest grid point take the
+// reference's FP64 arithmetic in both paths; the mixed path forms the
+// coefficients, which set no index, in FP32 and writes no FP64 record.
+template <bool Mixed>
 __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, F4Rec* r, F4RecD* d) {
   const double ZSQBND = 64. * 64.;
   const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
   const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
   const double RECPI = 1. / (2. * asin(1.));
-  double ALFADI = L.alfd, ALFALI = L.alfa;
-  double ZETAI = ALFALI / (ALFALI + ALFADI);
-  int IZ = (int)(100. * ZETAI + kONEPL);
-  double ZETDIF = 100. * ZETAI - (double)(IZ - 1);
-  double ALFAVI = (c_AVRAT[IZ - 1] + ZETDIF * (c_AVRAT[IZ] - c_AVRAT[IZ - 1])) * (ALFALI + ALFADI);
-  double RALFVI = 1. / ALFAVI;
-  double SIL = L.sp * RECPI * ALFALI;
-  double SIV = (ALFALI * RALFVI) * L.sp * RECPI * RALFVI;
-  double XNUI = VNUI - P.v1r4;
+  const double XNUI = VNUI - P.v1r4;
   int JMIN = (int)((XNUI - P.bound4) / P.dvr4 + 2.);
   if (JMIN < 1) JMIN = 1;
   int JMAX = (int)((XNUI + P.bound4) / P.dvr4 + 1.);
   if (JMAX > (int)P.nptr4) JMAX = (int)P.nptr4;
-  double ALFLI2 = ALFALI * ALFALI;
-  double ALFVI2 = ALFAVI * ALFAVI;
-  double BNDSQ = P.bound4 * P.bound4;
-  double F4BND = SIL / (ALFLI2 + BNDSQ);
+  const double BNDSQ = P.bound4 * P.bound4;
   const bool co2 = (L.mol == 2);
-  r->jmin = d->jmin = JMIN;
-  r->jmax = d->jmax = JMAX;
-  d->co2 = co2;
-  d->pad = 0;
+  r->jmin = JMIN;
+  r->jmax = JMAX;
   // FP32 distances are taken from the grid point nearest the line centre, so
   // that points near the centre do not lose digits to cancellation
   const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
   auto pair = [](double v) { return make_float2((float)v, (float)v); };
+  auto pairf = [](float v) { return make_float2(v, v); };
   r->nmc = pair(-(double)mc);
   r->x0 = pair((double)mc * P.dvr4 - XNUI);
-  r->sil = pair(SIL);
-  r->al2 = pair(ALFLI2);
-  r->ralv2 = pair(1. / ALFVI2);
-  r->sa3 = pair(SIV * A3);
-  r->sb3 = pair(SIV * B3);
-  // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
-  r->nfb0 = pair(co2 ? -2. * F4BND : -F4BND);
-  r->fb2 = pair(co2 ? F4BND / BNDSQ : 0.);
-  d->xnui = XNUI;
-  d->sil = SIL;
-  d->siv = SIV;
-  d->fbnd = F4BND;
-  d->al2 = ALFLI2;
-  d->alv2 = ALFVI2;
+  if constexpr (Mixed) {
+    const float ALFADI = (float)L.alfd, ALFALI = (float)L.alfa;
+    const float ZETAI = ALFALI / (ALFALI + ALFADI);
+    int IZ = (int)(100.f * ZETAI + (float)kONEPL);
+    IZ = IZ < 1 ? 1 : (IZ > 101 ? 101 : IZ);
+    const float ZETDIF = 100.f * ZETAI - (float)(IZ - 1);
+    const float a0 = (float)c_AVRAT[IZ - 1], a1 = (float)c_AVRAT[IZ];
+    const float ALFAVI = (a0 + ZETDIF * (a1 - a0)) * (ALFALI + ALFADI);
+    const float RALFVI = 1.f / ALFAVI;
+    const float SP = (float)L.sp, rpi = (float)RECPI;
+    const float SIL = SP * rpi * ALFALI;
+    const float SIV = (ALFALI * RALFVI) * SP * rpi * RALFVI;
+    const float ALFLI2 = ALFALI * ALFALI, ALFVI2 = ALFAVI * ALFAVI;
+    const float F4BND = SIL / (ALFLI2 + (float)BNDSQ);
+    r->sil = pairf(SIL);
+    r->al2 = pairf(ALFLI2);
+    r->ralv2 = pairf(1.f / ALFVI2);
+    r->sa3 = pairf(SIV * (float)A3);
+    r->sb3 = pairf(SIV * (float)B3);
+    // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
+    r->nfb0 = pairf(co2 ? -2.f * F4BND : -F4BND);
+    r->fb2 = pairf(co2 ? F4BND / (float)BNDSQ : 0.f);
+  } else {
+    const double ALFADI = L.alfd, ALFALI = L.alfa;
+    const double ZETAI = ALFALI / (ALFALI + ALFADI);
+    const int IZ = (int)(100. * ZETAI + kONEPL);
+    const double ZETDIF = 100. * ZETAI - (double)(IZ - 1);
+    const double ALFAVI = (c_AVRAT[IZ - 1] + ZETDIF * (c_AVRAT[IZ] - c_AVRAT[IZ - 1])) * (ALFALI + ALFADI);
+    const double RALFVI = 1. / ALFAVI;
+    const double SIL = L.sp * RECPI * ALFALI;
+    const double SIV = (ALFALI * RALFVI) * L.sp * RECPI * RALFVI;
+    const double ALFLI2 = ALFALI * ALFALI;
+    const double ALFVI2 = ALFAVI * ALFAVI;
+    const double F4BND = SIL / (ALFLI2 + BNDSQ);
+    r->sil = pair(SIL);
+    r->al2 = pair(ALFLI2);
+    r->ralv2 = pair(1. / ALFVI2);
+    r->sa3 = pair(SIV * A3);
+    r->sb3 = pair(SIV * B3);
+    r->nfb0 = pair(co2 ? -2. * F4BND : -F4BND);
+    r->fb2 = pair(co2 ? F4BND / BNDSQ : 0.);
+    d->jmin = JMIN;
+    d->jmax = JMAX;
+    d->co2 = co2;
+    d->pad = 0;
+    d->xnui = XNUI;
+    d->sil = SIL;
+    d->siv = SIV;
+    d->fbnd = F4BND;
+    d->al2 = ALFLI2;
+    d->alv2 = ALFVI2;
+  }
 }
 
 __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
@@ -1150,7 +1188,8 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     const ShrunkLine L = S[i];
     F4Rec r;
     F4RecD d;
-    f4_record(P, L, L.vnu, &r, &d);
+    if (P.mixed) f4_record<true>(P, L, L.vnu, &r, &d);
+    else f4_record<false>(P, L, L.vnu, &r, &d);
     // lines beyond the last point's reach, or without strength, add nothing
     if (L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) {
       r.jmin = d.jmin = 1 << 30;
@@ -1158,7 +1197,7 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     }
     if (r.jmax >= r.jmin) steps += (unsigned long long)(r.jmax - r.jmin + 1);
     R[i] = r;
-    D[i] = d;
+    if (!P.mixed) D[i] = d;
   }
   for (int o = 16; o > 0; o >>= 1) steps += __shfl_down_sync(0xffffffffu, steps, o);
   if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 6], steps);
@@ -1170,10 +1209,11 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
       if (!(L.vnu > 0. && L.vnu <= 25.) || L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) continue;
       F4Rec r;
       F4RecD d;
-      f4_record(P, L, -L.vnu, &r, &d);
+      if (P.mixed) f4_record<true>(P, L, -L.vnu, &r, &d);
+      else f4_record<false>(P, L, -L.vnu, &r, &d);
       if (r.jmax >= r.jmin && n + nm < rstride) {
         R[n + nm] = r;
-        D[n + nm] = d;
+        if (!P.mixed) D[n + nm] = d;
         nm++;
         atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 6], (unsigned long long)(r.jmax - r.jmin + 1));
       }
