@@ -23,7 +23,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
-           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn")
+           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -75,6 +75,8 @@ def lib():
                                             P(C.c_double), P(C.c_int64)]
         L.clblm_gpu_fftscn.argtypes = [C.c_void_p, P(T.clblm_scan_t), C.c_void_p, C.c_double, C.c_double, C.c_int64,
                                        C.c_void_p, C.c_int64, C.c_int32]
+        L.clblm_gpu_layer_amounts.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [P(C.c_double)] * 4 + \
+            [C.c_double] + [P(C.c_double)] * 5
         L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
                                        P(C.c_int64), C.c_char_p, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
@@ -302,6 +304,24 @@ def _scan_methods():
 
 
 Handle.fftscn, Handle.fftscn_device = _scan_methods()
+
+
+def _layer_amounts(self, z, p, t, den, earth_radius=6371.23):
+    """Layer Pave, Tave, Wtot, W [nlay, nmol] and secant of a nadir path
+    between the levels of a profile (rayTraceAndLayerPack: ALAYER + FPACK)."""
+    z, p, t = (np.ascontiguousarray(a, dtype=np.float64) for a in (z, p, t))
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    nlev, nmol = den.shape
+    nl = nlev - 1
+    out = {k: np.zeros(nl) for k in ("pave", "tave", "wtot", "secant")}
+    out["w"] = np.zeros((nl, nmol))
+    self._check(lib().clblm_gpu_layer_amounts(self.h, nlev, nmol, _dp(z), _dp(p), _dp(t), _dp(den), earth_radius,
+                                              _dp(out["pave"]), _dp(out["tave"]), _dp(out["wtot"]), _dp(out["w"]),
+                                              _dp(out["secant"])))
+    return out
+
+
+Handle.layer_amounts = _layer_amounts
 
 
 def read_tape3(path, v1=-1e30, v2=1e30):

@@ -87,6 +87,12 @@ struct F4RecD;
 __global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
                               int64_t* nmirror, unsigned long long* stats);
+// layer averages and amounts of a nadir path (ALAYER + FPACK)
+constexpr int kMaxLayerMol = 64;
+__global__ void k_layer_amounts(int nlev, int nmol, const double* z, const double* p, const double* t,
+                                const double* den, double re, double* pave, double* tave, double* wtot, double* w,
+                                double* secant, int* err);
+
 // running bounds of the line records, in blocks of kRecBlock records
 constexpr int kRecBlock = 256;
 constexpr int kRecNone = 0x7fffffff;

@@ -1380,3 +1380,111 @@ __global__ void __launch_bounds__(kRecBlock)
 }
 
 }  // namespace clblm
+
+namespace clblm {
+
+// ---- layer averages and amounts of a nadir path ---------------------------
+// ALAYER (clblm_AtmPath.f90:3000-3246) for a vertical path between the
+// profile's levels -- every sine of incidence 0, so the refraction ratios
+// drop out and the weights of the quadratic rule come from the radii alone
+// -- then FPACK's density-weighted averages (:3279-3483), one thread per
+// layer in FP64 with every operation rounded on its own (this file is
+// compiled without contraction), as the reference's unoptimised build.
+__global__ void k_layer_amounts(int nlev, int nmol, const double* __restrict__ z, const double* __restrict__ p,
+                                const double* __restrict__ t, const double* __restrict__ den, double re,
+                                double* __restrict__ pave, double* __restrict__ tave, double* __restrict__ wtot,
+                                double* __restrict__ w, double* __restrict__ secant, int* __restrict__ err) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nlev - 1) return;
+  const double EPSILN = 1.0E-5, DELTAS = 5.0;
+  const double GCAIR = 1.0E-3 * 8.314472E+07 / 6.02214199E+23;
+  double dena[kMaxLayerMol], denb[kMaxLayerMol], hden[kMaxLayerMol], amt[kMaxLayerMol];
+  const double Z1 = z[j], Z2 = z[j + 1];
+  double H1 = Z1, R1 = re + H1;
+  const double DHMIN = DELTAS * DELTAS / (2.0 * R1);
+  double COSAI1 = -1.0;
+  double X1 = -R1 * COSAI1;
+  double DSDX1 = 1.0 / (1.0 - 0.0);
+  double PA = p[j], PB = p[j + 1];
+  if (PB == PA) {
+    atomicOr(err, 1);
+    return;
+  }
+  const double TA = t[j], TB = t[j + 1];
+  double RHOA = PA / (GCAIR * TA), RHOB = PB / (GCAIR * TB);
+  const double DZ = Z2 - Z1;
+  const double HP = -DZ / log(PB / PA);
+  const double HRHO = fabs(RHOB / RHOA - 1.0) >= EPSILN ? -DZ / log(RHOB / RHOA) : 1.0E30;
+  for (int k = 0; k < nmol; ++k) {
+    dena[k] = den[(int64_t)j * nmol + k];
+    denb[k] = den[(int64_t)(j + 1) * nmol + k];
+    amt[k] = 0.;
+    if ((dena[k] == 0.0 || denb[k] == 0.0) || fabs(1.0 - dena[k] / denb[k]) <= EPSILN) hden[k] = 0.0;
+    else hden[k] = -DZ / log(denb[k] / dena[k]);
+  }
+  double ppsum = 0., tpsum = 0., rhopsm = 0., S = 0.;
+  for (int step = 0; step < 1 << 20; ++step) {  // the layer in steps of DELTAS (bounded)
+    double DH = -DELTAS * COSAI1;
+    if (DH < DHMIN) DH = DHMIN;
+    double H3 = H1 + DH;
+    if (H3 > Z2) H3 = Z2;
+    DH = H3 - H1;
+    const double R3 = re + H3;
+    const double H2 = H1 + DH / 2.0;
+    const double R2 = re + H2;
+    const double COSAI2 = -sqrt(1.0 - 0.0), COSAI3 = -sqrt(1.0 - 0.0);
+    const double X2 = -R2 * COSAI2, X3 = -R3 * COSAI3;
+    const double D31 = X3 - X1, D32 = X3 - X2, D21 = X2 - X1;
+    double W1, W2, W3;
+    if (D32 == 0.0 || D21 == 0.0) {
+      W1 = 0.5 * D31;
+      W2 = 0.0;
+      W3 = 0.5 * D31;
+    } else {
+      W1 = (2.0 - D32 / D21) * D31 / 6.0;
+      W2 = D31 * D31 * D31 / (D32 * D21 * 6.0);
+      W3 = (2.0 - D21 / D32) * D31 / 6.0;
+    }
+    const double DSDX2 = 1.0 / (1.0 - 0.0), DSDX3 = 1.0 / (1.0 - 0.0);
+    const double DS = W1 * DSDX1 + W2 * DSDX2 + W3 * DSDX3;
+    S = S + DS;
+    const double DSDZ = DS / DH;
+    PB = PA * exp(-DH / HP);
+    RHOB = RHOA * exp(-DH / HRHO);
+    if ((DH / HRHO) >= EPSILN) {
+      ppsum = ppsum + DSDZ * (HP / (1.0 + HP / HRHO)) * (PA * RHOA - PB * RHOB);
+      tpsum = tpsum + DSDZ * HP * (PA - PB) / GCAIR;
+      rhopsm = rhopsm + DSDZ * HRHO * (RHOA - RHOB);
+    } else {
+      ppsum = ppsum + 0.5 * DS * (PA * RHOA + PB * RHOB);
+      tpsum = tpsum + 0.5 * DS * (PA + PB) / GCAIR;
+      rhopsm = rhopsm + 0.5 * DS * (RHOA + RHOB);
+    }
+    for (int k = 0; k < nmol; ++k) {
+      const double d0 = den[(int64_t)j * nmol + k], d1 = den[(int64_t)(j + 1) * nmol + k];
+      if (hden[k] == 0.0 || fabs(DH / hden[k]) < EPSILN) {
+        denb[k] = d0 + (d1 - d0) * (H3 - Z1) / DZ;
+        amt[k] = amt[k] + 0.5 * (dena[k] + denb[k]) * DS * 1.0E5;
+      } else {
+        denb[k] = d0 * exp(-(H3 - Z1) / hden[k]);
+        amt[k] = amt[k] + DSDZ * hden[k] * (dena[k] - denb[k]) * 1.0E5;
+      }
+    }
+    PA = PB;
+    RHOA = RHOB;
+    for (int k = 0; k < nmol; ++k) dena[k] = denb[k];
+    if (!(H3 < Z2)) break;
+    H1 = H3;
+    R1 = R3;
+    COSAI1 = COSAI3;
+    X1 = X3;
+    DSDX1 = DSDX3;
+  }
+  pave[j] = ppsum / rhopsm;
+  tave[j] = tpsum / rhopsm;
+  wtot[j] = rhopsm * 1.0E+5;
+  secant[j] = S / (Z2 - Z1);
+  for (int k = 0; k < nmol; ++k) w[(int64_t)j * nmol + k] = amt[k];
+}
+
+}  // namespace clblm

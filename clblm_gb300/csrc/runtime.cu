@@ -3084,3 +3084,48 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
 }
 
 }  // extern "C"
+
+// ---- layer averages and amounts of a nadir path -------------------------------
+extern "C" int clblm_gpu_layer_amounts(clblm_handle_t* h, int32_t nlev, int32_t nmol, const double* z,
+                                       const double* p, const double* t, const double* den, double earth_radius,
+                                       double* pave, double* tave, double* wtot, double* w, double* secant) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (nlev < 2 || nmol < 0 || nmol > kMaxLayerMol || !z || !p || !t || (nmol > 0 && (!den || !w)) || !pave ||
+      !tave || !wtot || !secant || !(earth_radius > 0.))
+    return set_err(h, CLBLM_ERR_ARG, "layer amounts: bad profile (2 levels or more, at most %d molecules)",
+                   kMaxLayerMol);
+  for (int i = 0; i + 1 < nlev; ++i)
+    if (!(z[i + 1] > z[i])) return set_err(h, CLBLM_ERR_ARG, "layer amounts: altitudes must increase");
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  const int nl = nlev - 1;
+  const size_t nin = (size_t)nlev * (3 + (size_t)nmol), nout = (size_t)nl * (4 + (size_t)nmol);
+  CUDA_TRY(h, h->scan_io.ensure(sizeof(double) * (nin + nout) + 64));
+  double* d = h->scan_io.as<double>();
+  double *dz = d, *dp = d + nlev, *dt = d + 2 * nlev, *dden = d + 3 * nlev;
+  double* o = d + nin;
+  double *opa = o, *ota = o + nl, *owt = o + 2 * nl, *osc = o + 3 * nl, *ow = o + 4 * nl;
+  int* derr = reinterpret_cast<int*>(o + nout);
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(dz, z, sizeof(double) * nlev, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(dp, p, sizeof(double) * nlev, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(dt, t, sizeof(double) * nlev, cudaMemcpyHostToDevice, st));
+  if (nmol > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(dden, den, sizeof(double) * nlev * nmol, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemsetAsync(derr, 0, sizeof(int), st));
+  h->reset_call();
+  h->launches++;
+  k_layer_amounts<<<(nl + 63) / 64, 64, 0, st>>>(nlev, nmol, dz, dp, dt, dden, earth_radius, opa, ota, owt, ow, osc,
+                                                 derr);
+  CUDA_TRY(h, cudaGetLastError());
+  int err = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(pave, opa, sizeof(double) * nl, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(tave, ota, sizeof(double) * nl, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(wtot, owt, sizeof(double) * nl, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(secant, osc, sizeof(double) * nl, cudaMemcpyDeviceToHost, st));
+  if (nmol > 0) CUDA_TRY(h, cudaMemcpyAsync(w, ow, sizeof(double) * nl * nmol, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err) return set_err(h, CLBLM_ERR_ARG, "layer amounts: pressures in adjoining levels must differ");
+  h->last.launches = h->launches;
+  return CLBLM_OK;
+}

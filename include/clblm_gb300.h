@@ -336,6 +336,26 @@ int clblm_gpu_batch_size(clblm_handle_t *h, const clblm_profile_t *prof,
 int clblm_gpu_batch(clblm_handle_t *h, clblm_profile_t *prof, int32_t n,
                     const clblm_rt_ctrl_t *ctrl, int32_t flags);
 
+/* ---- layer averages and amounts of a nadir path ------------------------------
+ *
+ * The layer parameters ODLAY takes (Pave, Tave, Wtot, W per molecule) from a
+ * level profile, as rayTraceAndLayerPack (clblm_AtmPath.f90:1135-1301)
+ * forms them for a path seen straight down from its top level to its bottom
+ * level with the layer boundaries at the profile's levels: ALAYER's
+ * integration (:3000-3246) in steps of DELTAS = 5 km with exponential
+ * interpolation of pressure, air density and each absorber's density, then
+ * FPACK's density-weighted pressure and temperature (:3279-3483).  Runs on
+ * the device in binary64, one thread per layer.  Inputs (host): nlev levels
+ * in ascending altitude, z [km], p [mb], t [K], den [nlev*nmol] number
+ * densities [molec/cm3] (level-major), earth radius [km].  Outputs (host,
+ * nlev-1 layers): pave [mb], tave [K], wtot and w [(nlev-1)*nmol]
+ * [molec/cm2], secant (the path length over the layer thickness: 1). */
+int clblm_gpu_layer_amounts(clblm_handle_t *h, int32_t nlev, int32_t nmol,
+                            const double *z, const double *p, const double *t,
+                            const double *den, double earth_radius,
+                            double *pave, double *tave, double *wtot,
+                            double *w, double *secant);
+
 /* ---- instrument-function scan ----------------------------------------------
  *
  * clblm_FFTSCN (clblm_FFT.f90:308-844): a spectrum on a uniform grid

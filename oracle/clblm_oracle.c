@@ -2461,3 +2461,123 @@ int ocl_jac_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
   free(dvf);
   return rc;
 }
+
+/* ---- layer averages and amounts of a nadir path ---------------------------
+ *
+ * ALAYER (clblm_AtmPath.f90:3000-3246) for a vertical path (initial sine of
+ * the incidence angle 0, so CPATH = 0, every sine 0, cosines -1, and the
+ * refraction ratios drop out), traced upward layer by layer between the
+ * profile's levels (path levels = RT boundaries = profile levels), then
+ * FPACK (:3279-3483) with one path layer per output layer and, for a
+ * downward view (H1 > H2), no zeroing of amounts.  Steps of DELTAS = 5 km
+ * (at least DELTAS^2/(2 R1)); within a step P and the air density follow
+ * exponentials of their layer scale heights and each absorber an
+ * exponential of its own, or a straight line when its end values are equal
+ * to EPSILN or one is zero. */
+int ocl_layer_amounts(int nlev, int nmol, const double *z, const double *p, const double *t, const double *den,
+                      double re, double *pave, double *tave, double *wtot, double *w, double *secant) {
+  const double EPSILN = 1.0E-5, DELTAS = 5.0;
+  const double GCAIR = 1.0E-3 * 8.314472E+07 / 6.02214199E+23;
+  if (nlev < 2 || nmol < 0) return CLBLM_ERR_ARG;
+  double *dena = (double *)malloc(sizeof(double) * (nmol > 0 ? nmol : 1));
+  double *denb = (double *)malloc(sizeof(double) * (nmol > 0 ? nmol : 1));
+  double *hden = (double *)malloc(sizeof(double) * (nmol > 0 ? nmol : 1));
+  int rc = CLBLM_OK;
+  for (int j = 0; j + 1 < nlev && rc == CLBLM_OK; ++j) {
+    double ppsum = 0., tpsum = 0., rhopsm = 0., S = 0.;
+    for (int k = 0; k < nmol; ++k) w[(size_t)j * nmol + k] = 0.;
+    const double Z1 = z[j], Z2 = z[j + 1];
+    double H1 = Z1, R1 = re + H1;
+    const double DHMIN = DELTAS * DELTAS / (2.0 * R1);
+    double COSAI1 = -1.0;
+    double X1 = -R1 * COSAI1;
+    double DSDX1 = 1.0 / (1.0 - 0.0);
+    double PA = p[j], PB = p[j + 1];
+    if (PB == PA) {
+      rc = CLBLM_ERR_ARG;  /* "PRESSURES IN ADJOINING LAYERS MUST DIFFER" */
+      break;
+    }
+    const double TA = t[j], TB = t[j + 1];
+    double RHOA = PA / (GCAIR * TA), RHOB = PB / (GCAIR * TB);
+    const double DZ = Z2 - Z1;
+    const double HP = -DZ / log(PB / PA);
+    const double HRHO = fabs(RHOB / RHOA - 1.0) >= EPSILN ? -DZ / log(RHOB / RHOA) : 1.0E30;
+    for (int k = 0; k < nmol; ++k) {
+      dena[k] = den[(size_t)j * nmol + k];
+      denb[k] = den[(size_t)(j + 1) * nmol + k];
+      if ((dena[k] == 0.0 || denb[k] == 0.0) || fabs(1.0 - dena[k] / denb[k]) <= EPSILN) hden[k] = 0.0;
+      else hden[k] = -DZ / log(denb[k] / dena[k]);
+    }
+    for (;;) {
+      double DH = -DELTAS * COSAI1;
+      if (DH < DHMIN) DH = DHMIN;
+      double H3 = H1 + DH;
+      if (H3 > Z2) H3 = Z2;
+      DH = H3 - H1;
+      const double R3 = re + H3;
+      const double H2 = H1 + DH / 2.0;
+      const double R2 = re + H2;
+      const double COSAI2 = -sqrt(1.0 - 0.0), COSAI3 = -sqrt(1.0 - 0.0);
+      const double X2 = -R2 * COSAI2, X3 = -R3 * COSAI3;
+      const double D31 = X3 - X1, D32 = X3 - X2, D21 = X2 - X1;
+      double W1, W2, W3;
+      if (D32 == 0.0 || D21 == 0.0) {
+        W1 = 0.5 * D31;
+        W2 = 0.0;
+        W3 = 0.5 * D31;
+      } else {
+        W1 = (2.0 - D32 / D21) * D31 / 6.0;
+        W2 = D31 * D31 * D31 / (D32 * D21 * 6.0);
+        W3 = (2.0 - D21 / D32) * D31 / 6.0;
+      }
+      const double DSDX2 = 1.0 / (1.0 - 0.0), DSDX3 = 1.0 / (1.0 - 0.0);
+      const double DS = W1 * DSDX1 + W2 * DSDX2 + W3 * DSDX3;
+      S = S + DS;
+      const double DSDZ = DS / DH;
+      PB = PA * exp(-DH / HP);
+      RHOB = RHOA * exp(-DH / HRHO);
+      if ((DH / HRHO) >= EPSILN) {
+        ppsum = ppsum + DSDZ * (HP / (1.0 + HP / HRHO)) * (PA * RHOA - PB * RHOB);
+        tpsum = tpsum + DSDZ * HP * (PA - PB) / GCAIR;
+        rhopsm = rhopsm + DSDZ * HRHO * (RHOA - RHOB);
+      } else {
+        ppsum = ppsum + 0.5 * DS * (PA * RHOA + PB * RHOB);
+        tpsum = tpsum + 0.5 * DS * (PA + PB) / GCAIR;
+        rhopsm = rhopsm + 0.5 * DS * (RHOA + RHOB);
+      }
+      for (int k = 0; k < nmol; ++k) {
+        double *amt = &w[(size_t)j * nmol + k];
+        if (hden[k] == 0.0 || fabs(DH / hden[k]) < EPSILN) {
+          denb[k] = den[(size_t)j * nmol + k] + (den[(size_t)(j + 1) * nmol + k] - den[(size_t)j * nmol + k]) *
+                                                    (H3 - Z1) / DZ;
+          *amt = *amt + 0.5 * (dena[k] + denb[k]) * DS * 1.0E5;
+        } else {
+          denb[k] = den[(size_t)j * nmol + k] * exp(-(H3 - Z1) / hden[k]);
+          *amt = *amt + DSDZ * hden[k] * (dena[k] - denb[k]) * 1.0E5;
+        }
+      }
+      PA = PB;
+      RHOA = RHOB;
+      for (int k = 0; k < nmol; ++k) dena[k] = denb[k];
+      if (H3 < Z2) {
+        H1 = H3;
+        R1 = R3;
+        COSAI1 = COSAI3;
+        X1 = X3;
+        DSDX1 = DSDX3;
+      } else {
+        break;
+      }
+    }
+    /* FPACK: density-weighted pressure and temperature, air column in cm,
+     * effective secant */
+    pave[j] = ppsum / rhopsm;
+    tave[j] = tpsum / rhopsm;
+    wtot[j] = rhopsm * 1.0E+5;
+    secant[j] = S / (Z2 - Z1);
+  }
+  free(dena);
+  free(denb);
+  free(hden);
+  return rc;
+}

@@ -65,6 +65,14 @@ int ocl_jac_point(const double *viewOD, const double *downOD, const double *amfV
                   const double *dT_dTlo, double *dRad_dTlev, double *dRad_dTau, double *rad,
                   double *dRad_dTsfc, double *dRad_dEmis);
 
+/* Layer averages and amounts of a nadir path between the profile's levels
+ * (ALAYER + FPACK, clblm_AtmPath.f90:3000-3483): z [km], p [mb], t [K] at
+ * nlev levels (ascending z), den [nlev*nmol] number densities [molec/cm3];
+ * out per layer: pave, tave, wtot (air column, molec/cm2), w [nlay*nmol]
+ * (molec/cm2), secant. */
+int ocl_layer_amounts(int nlev, int nmol, const double *z, const double *p, const double *t, const double *den,
+                      double re, double *pave, double *tave, double *wtot, double *w, double *secant);
+
 /* Building blocks exposed for known-answer tests. */
 void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg,
                       double *xver); /* each [3001] */

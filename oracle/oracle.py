@@ -66,6 +66,7 @@ def lib():
         L.ocl_jac_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
                                     P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + [P(C.c_double)] * 5 + [
                                     C.c_int64, P(C.c_int64), P(C.c_double), C.c_int]
+        L.ocl_layer_amounts.argtypes = [C.c_int, C.c_int] + [P(C.c_double)] * 4 + [C.c_double] + [P(C.c_double)] * 5
         L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
                                                                                     P(C.c_double), P(C.c_int)]
@@ -218,3 +219,19 @@ def contnm_h2o(cont, v1, v2, pave, tave, wtot, wk1, jrad=0, xself=1.0, xfrgn=1.0
     if rc:
         raise OracleError(rc, "contnm_h2o")
     return v1abs.value, out[:npt.value].copy()
+
+
+def layer_amounts(z, p, t, den, re=6371.23):
+    """ALAYER + FPACK for a nadir path between the profile's levels: dict of
+    pave, tave, wtot, w [nlay, nmol], secant."""
+    z, p, t = (np.ascontiguousarray(a, dtype=np.float64) for a in (z, p, t))
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    nlev, nmol = den.shape
+    nl = nlev - 1
+    out = {k: np.zeros(nl) for k in ("pave", "tave", "wtot", "secant")}
+    out["w"] = np.zeros((nl, nmol))
+    rc = lib().ocl_layer_amounts(nlev, nmol, _dp(z), _dp(p), _dp(t), _dp(den), float(re), _dp(out["pave"]),
+                                 _dp(out["tave"]), _dp(out["wtot"]), _dp(out["w"]), _dp(out["secant"]))
+    if rc:
+        raise OracleError(rc, "layer amounts")
+    return out
