@@ -60,6 +60,7 @@ struct LayerPlan {
   int contnm;                     // 1: continuum on
   int jac_mol;                    // icflg: molecule whose continuum derivative term is added
   double v1abs, v2abs, dvabs, xself, xfrgn, wk1, h2o_fac;
+  double xco2c;                   // XCO2C: scale of the CO2 continuum (0: none)
   int nptabs;
   // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
   int sel[kTIPSNMOL + 1];

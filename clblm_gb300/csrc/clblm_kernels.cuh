@@ -29,6 +29,10 @@ struct ContIn {
   const double* for_absco_ref;
   const double* self_texp;
   double ref_press, ref_temp;
+  // CO2 continuum: FRNCO2's S(5003), TDEP_BANDHEAD(1196:1220), CONTNM's XFACCO2(500)
+  const double* co2_s;
+  const double* co2_tdep;
+  const double* co2_xfac;
 };
 
 // LINF4Q-corrected line (before SHRINQ)

@@ -17,6 +17,10 @@ Tables extracted (reference file:line):
     src/clblm_src/clblm_ODLAY_TIPS.f90:424-2254
   * isotopologue-1 molecular masses of molecules 1-9:
     src/common/clblm_ConstParam.f90:263-290
+  * CO2 continuum (mt_ckd 2.5): FRNCO2's coefficients S(1:5003) on -4 to
+    10000 cm-1 at 2 cm-1 and its band-head temperature exponents
+    TDEP_BANDHEAD(1196:1220), src/clblm_src/clblm_ODLAY_Continuum.f90:1333-2511;
+    CONTNM's XFACCO2(500) scaling for 2000-2998 cm-1, :145-204
 
 Run (in a tree where the reference is mounted):
     python clblm_gb300/csrc/gen_ref_tables.py /root/reference > clblm_gb300/csrc/clblm_ref_tables.h
@@ -80,6 +84,22 @@ def _masses(src):
     return out
 
 
+def _data_block(src, start_pat, data_pat, count):
+    """The values of a DATA statement (after start_pat) with `count` entries."""
+    st = re.search(start_pat, src, re.I)
+    if not st:
+        raise SystemExit("%s not found" % start_pat)
+    # comments first: they hold slashes of their own (the "!DATA F0000/" labels)
+    text = "\n".join(line.split("!")[0] for line in src[st.start():].splitlines())
+    m = re.search(data_pat, text, re.S | re.I)
+    if not m:
+        raise SystemExit("%s: data not found" % data_pat)
+    vals = _numbers(m.group(1).replace("&", " "))
+    if len(vals) != count:
+        raise SystemExit("%s: %d values, want %d" % (data_pat, len(vals), count))
+    return vals
+
+
 def main(ref_root):
     ref = Path(ref_root)
     common = (ref / "src/clblm_src/clblm_ODLAY_CommonSub.f90").read_text(errors="replace")
@@ -121,6 +141,12 @@ def main(ref_root):
     lines.append("")
     # clblm_ConstParam.f90:263-290
     emit("CLBLM_ISO1_MASS", _masses(const), per=9)
+    # clblm_ODLAY_Continuum.f90: FRNCO2 (:1333-2511) and CONTNM's XFACCO2 (:145-204)
+    cont = (ref / "src/clblm_src/clblm_ODLAY_Continuum.f90").read_text(errors="replace")
+    emit("CLBLM_CO2_S", _data_block(cont, r"SUBROUTINE\s+FRNCO2", r"DATA\s+S\(1:5003\)\s*/(.*?)/", 5003))
+    emit("CLBLM_CO2_TDEP", _data_block(cont, r"SUBROUTINE\s+FRNCO2",
+                                       r"data\s*\(tdep_bandhead\(i\),i=1196,1220\)\s*/(.*?)/", 25))
+    emit("CLBLM_XFACCO2", _data_block(cont, r"SUBROUTINE\s+CONTNM", r"DATA\s+XFACCO2\s*/(.*?)/", 500), per=8)
     lines.append("#endif")
     sys.stdout.write("\n".join(lines) + "\n")
 

@@ -493,18 +493,11 @@ __global__ void k_panel_ranges(const LayerPlan* __restrict__ plans, int layer0, 
 // One thread per ABSRB point I (1-based).  The four table coefficients the
 // 4-point interpolation (myxint) needs are rebuilt per point exactly as
 // mt_ckd_h2o_absco builds sh2o_coeff/fh2o_coeff.
-__global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, ContIn cont, double* __restrict__ absrb_all) {
-  const LayerPlan& P = plans[blockIdx.y + layer0];
-  double* ABSRB = absrb_all + P.abs_off;  // ABSRB[I], I = 1..N_ABSRB
-  int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (I > kNABSRB + 7) return;
-  ABSRB[I] = 0.;
-  if (I == 1) ABSRB[0] = 0.;
-  if (I > kNABSRB) return;
-  if (!P.contnm) return;
-  if (!((P.v2 > -20.0) && (P.v1 < 20000.) && ((P.xself > 0.) || (P.xfrgn > 0.)))) return;
+// H2O continuum at ABSRB point I (1-based): MT_CKD self + foreign through
+// myxint, plus the icflg term of the H2O Jacobian OD
+__device__ double h2o_continuum(const LayerPlan& P, const ContIn& cont, int I) {
+  if (!((P.v2 > -20.0) && (P.v1 < 20000.) && ((P.xself > 0.) || (P.xfrgn > 0.)))) return 0.;
   int ncoeffin = cont.n;
-  if (I > (int)((P.v2abs - P.v1abs) / P.dvabs + 1)) return;  // beyond NPTABS: nothing to add
   const double dvc = (cont.v1 + cont.dv) - cont.v1;
   // i1, i2 bracket [V1ABS - 2 dvc, V2ABS + 2 dvc] (mt_ckd_h2o_module.f90:106-117):
   // the reference's forward scans, as binary searches over the monotone grid
@@ -540,7 +533,7 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
   if (ILO < ist) ILO = ist;
   int IHI = (int)((V2A - dvc - P.v1abs) / P.dvabs + onemi);
   if (IHI > lst) IHI = lst;
-  if (I < ILO || I > IHI) return;
+  if (I < ILO || I > IHI) return 0.;
   double xkt = P.tave / kRADCN2;
   double rho_rat = (P.pave / cont.ref_press) * (cont.ref_temp / P.tave);
   double VI = P.v1abs + P.dvabs * (double)(I - 1);
@@ -588,6 +581,88 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
     double c = cself - cfrgn_aj;
     ab = ab + c;
   }
+  return ab;
+}
+
+// CO2 continuum at ABSRB point I: the CO2 block of CONTNM
+// (clblm_ODLAY_Continuum.f90:408-451) with FRNCO2 (:1333-1410) -- mt_ckd 2.5
+// coefficients on -4 .. 10000 cm-1 at 2 cm-1, the band head scaled by
+// (T/246)^TDEP, XFACCO2 over 2000-2998 cm-1, times W(CO2) RHOAVE 1e-20 XCO2C
+// (and RADFN when JRAD = 1) -- through XINT; 0 where XINT does not reach I.
+// XINT's last stencil can read C(NPTC+1), which FRNCO2 never sets: taken as 0.
+__device__ double co2_continuum(const LayerPlan& P, const ContIn& cont, int I, bool* hit) {
+  *hit = false;
+  if (!((P.v2 > -20.0) && (P.v1 < 10000.) && P.xco2c > 0.) || !cont.co2_s) return 0.;
+  const double P0 = 1013., T0 = 296.;
+  const double RHOAVE = (P.pave / P0) * (T0 / P.tave);
+  const double XKT = P.tave / kRADCN2;
+  const double WCO2 = P.wk[2] * RHOAVE * 1.0E-20 * P.xco2c;
+  const double V1S = -4.0, DVS = 2.0;
+  const int NPTS = 5003;
+  const double DVC = DVS;
+  double V1C = P.v1abs - DVC, V2C = P.v2abs + DVC;
+  const int I1 = (V1C < V1S) ? -1 : (int)((V1C - V1S) / DVS + 0.01);
+  V1C = V1S + DVS * (double)(I1 - 1);
+  const int I2 = (int)((V2C - V1S) / DVS + 0.01);
+  int NPTC = I2 - I1 + 3;
+  if (NPTC > NPTS) NPTC = NPTS + 4;
+  V2C = V1C + DVS * (double)(NPTC - 1);
+  // XINT(V1C, V2C, DVC, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS), ONEPL/ONEMI
+  const double RECDVA = 1. / DVC;
+  int ILO = (int)((V1C + DVC - P.v1abs) / P.dvabs + 1. + kONEMI);
+  if (ILO < 1) ILO = 1;
+  int IHI = (int)((V2C - DVC - P.v1abs) / P.dvabs + kONEMI);
+  if (IHI > P.nptabs) IHI = P.nptabs;
+  if (I < ILO || I > IHI) return 0.;
+  *hit = true;
+  const double trat = P.tave / 246.;
+  auto coef = [&](int J) -> double {  // C(J), J = 1 .. NPTC
+    if (J < 1 || J > NPTC) return 0.;
+    const int Ii = I1 + (J - 1);
+    double c = 0.;
+    if (Ii >= 1 && Ii <= NPTS) {
+      double tcor = 1.;
+      if (Ii >= 1196 && Ii <= 1220) tcor = pow(trat, cont.co2_tdep[Ii - 1196]);
+      c = tcor * cont.co2_s[Ii - 1];
+    }
+    const double VJ = V1C + DVC * (double)(J - 1);
+    double CFAC = 1.;
+    if (VJ >= 2000. && VJ <= 2998.) {
+      const int JFAC = (int)((VJ - 1998.) / 2. + 0.00001);
+      CFAC = cont.co2_xfac[JFAC - 1];
+    }
+    c = CFAC * c;
+    double v = c * WCO2;
+    if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+    return v;
+  };
+  const double VI = P.v1abs + P.dvabs * (double)(I - 1);
+  const int J = (int)((VI - V1C) * RECDVA + kONEPL);
+  const double VJ = V1C + DVC * (double)(J - 1);
+  const double Pp = RECDVA * (VI - VJ);
+  const double C = (3. - 2. * Pp) * Pp * Pp;
+  const double B = 0.5 * Pp * (1. - Pp);
+  const double B1 = B * (1. - Pp);
+  const double B2 = B * Pp;
+  const double CONTI = -coef(J - 1) * B1 + coef(J) * (1. - C + B2) + coef(J + 1) * (C + B1) - coef(J + 2) * B2;
+  return CONTI * 1.0;
+}
+
+__global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, ContIn cont, double* __restrict__ absrb_all) {
+  const LayerPlan& P = plans[blockIdx.y + layer0];
+  double* ABSRB = absrb_all + P.abs_off;  // ABSRB[I], I = 1..N_ABSRB
+  int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (I > kNABSRB + 7) return;
+  ABSRB[I] = 0.;
+  if (I == 1) ABSRB[0] = 0.;
+  if (I > kNABSRB) return;
+  if (!P.contnm) return;
+  if (I > (int)((P.v2abs - P.v1abs) / P.dvabs + 1)) return;  // beyond NPTABS: nothing to add
+  // the H2O block adds to ABSRB first, then the CO2 block (XINT)
+  double ab = h2o_continuum(P, cont, I);
+  bool hit;
+  const double co2 = co2_continuum(P, cont, I, &hit);
+  if (hit) ab = ab + co2;
   ABSRB[I] = ab;
 }
 

@@ -97,7 +97,7 @@ struct clblm_handle {
   std::vector<int32_t> h_iflg, h_mol;
   double shiftmax = 0.;
   bool has_cont = false;
-  DevBuf cont_self, cont_for, cont_texp;
+  DevBuf cont_self, cont_for, cont_texp, cont_co2;
   ContIn cont{};
   DevBuf tabs;  // shape tables
   ShapeTabs shape{};
@@ -610,6 +610,7 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
     P.xfrgn = c->xfrgn;
     P.wk1 = P.wk[1];
     P.h2o_fac = P.wk[1] / lay->wtot;
+    P.xco2c = c->xco2c;
   }
   // returned spectrum: DVout interpolation, clblm_ODLAY.f90:571-604
   double outputDV = DV;
@@ -1286,6 +1287,18 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
         h->cont.self_texp = h->cont_texp.as<double>();
         h->cont.ref_press = cont->ref_press;
         h->cont.ref_temp = cont->ref_temp;
+        // the CO2 continuum's tables (data of the reference's source)
+        if (h->cont_co2.ensure(sizeof(double) * (5003 + 25 + 500))) {
+          rc = CLBLM_ERR_OOM;
+        } else {
+          double* d = h->cont_co2.as<double>();
+          cudaMemcpy(d, CLBLM_CO2_S, sizeof(double) * 5003, cudaMemcpyHostToDevice);
+          cudaMemcpy(d + 5003, CLBLM_CO2_TDEP, sizeof(double) * 25, cudaMemcpyHostToDevice);
+          cudaMemcpy(d + 5028, CLBLM_XFACCO2, sizeof(double) * 500, cudaMemcpyHostToDevice);
+          h->cont.co2_s = d;
+          h->cont.co2_tdep = d + 5003;
+          h->cont.co2_xfac = d + 5028;
+        }
         h->has_cont = true;
       }
     }

@@ -127,6 +127,10 @@ typedef struct {
   int32_t jac_mol;     /* HITRAN number whose continuum derivative term CONTNM
                         * adds (icflg, clblm_ODLAY.f90:436-438,
                         * clblm_ODLAY_Continuum.f90:394-401); 0: none          */
+  int32_t reserved;
+  double  xco2c;       /* XCO2C, scale of the CO2 continuum (mt_ckd 2.5, CONTNM
+                        * clblm_ODLAY_Continuum.f90:408-451); the reference's
+                        * default is 1, 0 leaves it out                        */
 } clblm_od_ctrl_t;
 
 /* A layered column seen in nadir from the top of the atmosphere, with the

@@ -535,6 +535,55 @@ static int contnm_h2o(ocl_session *s, const clblm_cont_t *C, int JRAD, double V1
 }
 
 /* ======================================================================
+ * CO2 continuum: the CO2 block of CONTNM (clblm_ODLAY_Continuum.f90:408-451)
+ * with FRNCO2 (:1333-1410): mt_ckd 2.5 coefficients on -4 .. 10000 cm-1 at
+ * 2 cm-1 (band head 2386-2434 cm-1 scaled by (T/246)^TDEP), XFACCO2 for
+ * 2000-2998 cm-1, times W(CO2) * RHOAVE * 1e-20 * XCO2C (and RADFN when JRAD
+ * = 1), XINT onto ABSRB after the H2O block.  XINT's last stencil can read
+ * C(NPTC+1), which FRNCO2 never sets; it is taken as 0 here.
+ * ====================================================================== */
+static void contnm_co2(int JRAD, double V1ABS, double V2ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/,
+                       double XCO2C, double V1, double V2, double PAVE, double TAVE, double WKCO2) {
+  if (!((V2 > -20.0) && (V1 < 10000.) && XCO2C > 0.)) return;
+  const double P0 = 1013., T0 = 296.;
+  const double RHOAVE = (PAVE / P0) * (T0 / TAVE);
+  const double XKT = TAVE / RADCN2;
+  const double WCO2 = WKCO2 * RHOAVE * 1.0E-20 * XCO2C;
+  const double V1S = -4.0, DVS = 2.0;
+  const int NPTS = 5003;
+  const double trat = TAVE / 246.;
+  const double DVC = DVS;
+  double V1C = V1ABS - DVC, V2C = V2ABS + DVC;
+  int I1 = (V1C < V1S) ? -1 : (int)((V1C - V1S) / DVS + 0.01);
+  V1C = V1S + DVS * (double)(I1 - 1);
+  int I2 = (int)((V2C - V1S) / DVS + 0.01);
+  int NPTC = I2 - I1 + 3;
+  if (NPTC > NPTS) NPTC = NPTS + 4;
+  V2C = V1C + DVS * (double)(NPTC - 1);
+  double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double)); /* 1-based, C(NPTC+1..) = 0 */
+  for (int J = 1; J <= NPTC; ++J) {
+    const int I = I1 + (J - 1);
+    double c = 0.;
+    if (I >= 1 && I <= NPTS) {
+      double tcor = 1.;
+      if (I >= 1196 && I <= 1220) tcor = pow(trat, CLBLM_CO2_TDEP[I - 1196]);
+      c = tcor * CLBLM_CO2_S[I - 1];
+    }
+    const double VJ = V1C + DVC * (double)(J - 1);
+    double CFAC = 1.;
+    if (VJ >= 2000. && VJ <= 2998.) {
+      const int JFAC = (int)((VJ - 1998.) / 2. + 0.00001);
+      CFAC = CLBLM_XFACCO2[JFAC - 1];
+    }
+    c = CFAC * c;
+    C[J] = c * WCO2;
+    if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+  }
+  xint(V1C, V2C, DVC, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+  free(C);
+}
+
+/* ======================================================================
  * Far-wing (function 4) lines: the TAPE9 scratch file as records in memory.
  * LINF4Q clblm_ODLAY_LineF4.f90:647-1266 (RDLNFL :1355-1476),
  * SHRINQ :1516-1647, LBLF4Q :25-182, CNVF4Q :187-494, RDLN4Q :554-640.
@@ -1605,6 +1654,7 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
       free(ABSRBb);
       return rc;
     }
+    contnm_co2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xco2c, V1, V2, PAVE, TAVE, M.WK[2]);
   }
   double ALFAV4 = 64. * g->sample * DV;
   double DVR4 = ALFAV4 / g->sample;
@@ -2580,4 +2630,14 @@ int ocl_layer_amounts(int nlev, int nmol, const double *z, const double *p, cons
   free(denb);
   free(hden);
   return rc;
+}
+
+/* The CO2 block of CONTNM alone, onto a zeroed ABSRB (1-based, nptabs
+ * points on v1abs + (i-1)*dvabs), for the known-answer tests. */
+int ocl_contnm_co2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xco2c,
+                   double v1, double v2, double pave, double tave, double wkco2) {
+  if (nptabs < 1 || nptabs > N_ABSRB - 4) return CLBLM_ERR_RANGE;
+  for (int i = 0; i <= nptabs; ++i) absrb[i] = 0.;
+  contnm_co2(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xco2c, v1, v2, pave, tave, wkco2);
+  return CLBLM_OK;
 }

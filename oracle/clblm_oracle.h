@@ -84,6 +84,9 @@ int ocl_tips_scor(int mol, double t, double *scor);
 int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double v1, double v2, double pave,
                    double tave, double wtot, double wk1, double xself, double xfrgn,
                    double *absrb, double *v1abs, int *nptabs);
+/* The CO2 block of CONTNM alone (ABSRB 1-based, [nptabs + 1]) */
+int ocl_contnm_co2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xco2c,
+                   double v1, double v2, double pave, double tave, double wkco2);
 int ocl_interp_spectrum(const double *in, double dvin, double v1in,
                         int64_t nin, double *out, double dvout, double v1out,
                         int64_t nout);

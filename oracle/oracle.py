@@ -66,6 +66,8 @@ def lib():
         L.ocl_jac_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
                                     P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + [P(C.c_double)] * 5 + [
                                     C.c_int64, P(C.c_int64), P(C.c_double), C.c_int]
+        L.ocl_contnm_co2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
+            [C.c_double] * 6
         L.ocl_layer_amounts.argtypes = [C.c_int, C.c_int] + [P(C.c_double)] * 4 + [C.c_double] + [P(C.c_double)] * 5
         L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
@@ -235,3 +237,13 @@ def layer_amounts(z, p, t, den, re=6371.23):
     if rc:
         raise OracleError(rc, "layer amounts")
     return out
+
+
+def contnm_co2(jrad, v1abs, dvabs, nptabs, xco2c, v1, v2, pave, tave, wkco2):
+    """ABSRB(1..nptabs) of the CO2 continuum alone (1-based array, [0] unused)."""
+    a = np.zeros(nptabs + 8)
+    v2abs = v1abs + dvabs * (nptabs - 1)
+    rc = lib().ocl_contnm_co2(jrad, v1abs, v2abs, dvabs, nptabs, _dp(a), xco2c, v1, v2, pave, tave, wkco2)
+    if rc:
+        raise OracleError(rc, "contnm_co2")
+    return a

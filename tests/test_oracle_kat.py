@@ -159,3 +159,34 @@ def test_interp_general_ratio_linear_within_phase_step(oracle_mod):
     want = 3.0 + 2.0 * np.arange(nout) * dvout / dvin
     inner = slice(2, nout - 3)
     assert np.max(np.abs(out[inner] - want[inner])) <= 2.0 / 200 + 1e-9
+
+
+def test_co2_continuum_at_table_nodes():
+    """At T = 246 K (band-head factor 1) and ABSRB points on FRNCO2's 2 cm-1
+    nodes, XINT returns the node value: S(I) * XFACCO2 * W(CO2) RHOAVE 1e-20
+    (clblm_ODLAY_Continuum.f90:408-451, :1333-1410)."""
+    from pathlib import Path
+    txt = (Path(__file__).resolve().parents[1] / "clblm_gb300/csrc/clblm_ref_tables.h").read_text()
+
+    def table(name, n):
+        body = txt.split("static const double %s[%d] = {" % (name, n))[1].split("};")[0]
+        return np.array([float(x) for x in body.replace("\n", " ").split(",") if x.strip()])
+
+    S = table("CLBLM_CO2_S", 5003)
+    XF = table("CLBLM_XFACCO2", 500)
+    pave, tave, wco2 = 500.0, 246.0, 3e21
+    v1abs, dvabs, n = 1996.0, 1.0, 1010
+    a = oracle_mod_contnm(0, v1abs, dvabs, n, 1.0, 2000.0, 3000.0, pave, tave, wco2)
+    rho = (pave / 1013.) * (296. / tave)
+    w = wco2 * rho * 1e-20
+    for v in (2000.0, 2100.0, 2386.0, 2400.0, 2434.0, 2998.0):
+        i = int(round((v - v1abs) / dvabs)) + 1
+        idx = int(round((v + 4.0) / 2.0)) + 1         # FRNCO2 index I: V = -4 + 2 (I - 1)
+        jfac = int((v - 1998.) / 2. + 0.00001)
+        want = S[idx - 1] * XF[jfac - 1] * w
+        assert a[i] == pytest.approx(want, rel=1e-13), v
+
+
+def oracle_mod_contnm(*args):
+    from oracle import oracle as O
+    return O.contnm_co2(*args)
