@@ -39,9 +39,17 @@ struct LayerPlan {
   // grid
   double v1, v2, dv, dvr2, dvr3, alfav, alfmax, bound, vbot, vtop, vft0;
   double wavdxf, rdv;             // DV/DXF1 (CNVFNQ's WAVDXF) and 1/DV (estimates only)
+  double conf2, conf3;            // CNVFNQ's CONF2 = DV/DVR2, CONF3 = DV/DVR3
+  double omconf2, omconf3;        // 1 - CONF2, 1 - CONF3
   double pave, tave, wtot, xkt, xkt0, betacr, tratio, rhorat, pavp0, pavp2;
   double ln_tratio;               // log(T/296): (T/296)^n = exp(n log(T/296))
   int mixed;                      // 1: FP32 for strengths and shape coefficients
+  // FP32 copies of the layer scalars the mixed path's strengths and widths use
+  float xkt_f, betacr_f, betacr4_f, beta_f, ln_tratio_f, rhorat_f;
+  // largest floats <= -1.001 and <= -0.999: for a float EPP, (double)EPP <= -1.001
+  // and (double)EPP > -0.999 are EPP <= epp_abs_f and EPP > epp_neg_f
+  float epp_abs_f, epp_neg_f;
+  double spfac;                   // 1 + 0*PAVP2, the SP factor of LNCORQ/LINF4Q
   double dptmn, dptfc;
   int jrad, ilnflg, max1, max2, max3, nalfmax, nbound;
   int npanels, nhi_last;          // panels and NHI of the last panel
@@ -65,6 +73,8 @@ struct LayerPlan {
   // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
   int sel[kTIPSNMOL + 1];
   double wk[kTIPSNMOL + 1], scor[kTIPSNMOL + 1], rhoslf[kTIPSNMOL + 1], alfd1[kTIPSNMOL + 1];
+  double rhodif[kTIPSNMOL + 1];   // RHORAT - RHOSLF(m)
+  float scor_f[kTIPSNMOL + 1], rhoslf_f[kTIPSNMOL + 1], alfd1_f[kTIPSNMOL + 1];
   // offsets of this layer's slices inside the shared per-call buffers
   int64_t vft_off;     // VFT of panel p at vft_off + p
   int64_t od_off;      // OD output
@@ -83,6 +93,39 @@ struct LinePrep {
   int iz;          // IZETA
   int fpanel;      // first panel whose MAX1 fits the line (-1: rejected)
 };
+
+#ifdef __CUDACC__
+// CNVFNQ's set-up of one line read in panel q (clblm_ODLAY.f90:2127-2166):
+// ZSLOPE, ZINT, JMIN1/JMAX1, the grid shifts J2SHFT/J3SHFT and ZFkL of the
+// three grids.  Every double operation is rounded on its own, as in the
+// reference's unoptimised build; the explicit _rn forms give the same values
+// in every translation unit whatever its contraction flags, so the record
+// set-up and the gather's exact-index fix-up agree bit for bit.
+struct CnvfnqSetup {
+  double zslope, zint, zf[3];
+  int jmin1, jmax1, j2shft, j3shft;
+};
+__device__ __forceinline__ CnvfnqSetup cnvfnq_setup(const LayerPlan& P, double vft_q, double vnu, double recalf,
+                                                    double bhwdxf) {
+  CnvfnqSetup s;
+  // WAVDXF = DV/DXF1, CONF2 = DV/DVR2, CONF3 = DV/DVR3 and 1 - CONFk are the
+  // layer's, formed once on the host with the same operations
+  const double CONF2 = P.conf2, CONF3 = P.conf3;
+  s.zslope = __dmul_rn(recalf, P.wavdxf);
+  const double ZINT = __ddiv_rn(__dsub_rn(vnu, vft_q), P.dv);
+  s.zint = ZINT;
+  s.jmax1 = (int)__dadd_rn(__dadd_rn(ZINT, bhwdxf), 1.5);
+  s.jmin1 = (int)__dadd_rn(__dsub_rn(ZINT, bhwdxf), 1.5);
+  const double RSHFT = ZINT < 0.0 ? -0.5 : 0.5;
+  s.j2shft = (int)__dadd_rn(__dmul_rn(ZINT, P.omconf2), RSHFT);
+  s.j3shft = (int)__dadd_rn(__dmul_rn(ZINT, P.omconf3), RSHFT);
+  const int JMIN2 = s.jmin1 - s.j2shft, JMIN3 = s.jmin1 - s.j3shft;
+  s.zf[0] = __dmul_rn(__dsub_rn((double)(s.jmin1 - 2), ZINT), s.zslope);
+  s.zf[1] = __dmul_rn(__dsub_rn((double)(JMIN2 - 2), __dmul_rn(ZINT, CONF2)), s.zslope);
+  s.zf[2] = __dmul_rn(__dsub_rn((double)(JMIN3 - 2), __dmul_rn(ZINT, CONF3)), s.zslope);
+  return s;
+}
+#endif
 
 // One line's contribution on one of the three nested grids, in global
 // coordinates of that grid (index 0 at VFT of panel 0).

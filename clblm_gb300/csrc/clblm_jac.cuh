@@ -41,6 +41,9 @@ struct JacArgs {
 };
 
 __global__ void k_interp_map_jobs(const JacJob* jobs, int njob);
+// k_od_jobs: threads per CTA and output points per CTA
+constexpr int kOdJobThreads = 256;
+constexpr int kOdJobPoints = 2048;
 template <bool Plain>
 __global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out);
 template <bool Plain>

@@ -18,8 +18,9 @@ struct PanelArgs {
   int layer0;
   const double* vft_all;
   const GridRec* rec;
-  const GridRecD* recd;
+  const GridRecD* recd;       // FP64 records (FP64 path only)
   const GridRecLo* reclo;
+  const LinePrep* prep;       // the lines (the mixed path's rare FP64 index)
   int64_t stride;
   const int64_t* ranges;     // per panel: candidate record windows of R1, R2, R3
   int64_t panel_stride;
@@ -91,7 +92,7 @@ __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* bl
                             double* blk_fac);
 
 template <bool Plain>
-__global__ void k_panel(PanelArgs a);
+__global__ void k_panel(const __grid_constant__ PanelArgs a);
 template <bool Plain, int CHUNK>
 __global__ void k_f4_conv(F4Args a);
 

@@ -60,23 +60,58 @@ __device__ __forceinline__ Real od_ext_t(const Real* x, int64_t n, int64_t i) {
   return (Real)0;
 }
 
-// grid (points of the longest block, jobs)
+// grid (kOdJobPoints-point slices of the longest block, jobs).  A general-
+// ratio job reads per point its (iIn, IP) and the 201-point coefficients of
+// IP: those four are staged in shared memory, interleaved, since lanes with
+// different IP would serialise on the constant cache.
 template <bool Plain>
-__global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out) {
+__global__ void __launch_bounds__(kOdJobThreads) k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out) {
   using Real = typename std::conditional<Plain, double, float>::type;
+  using Real4 = typename std::conditional<Plain, double4, float4>::type;
+  __shared__ Real4 ia[203];
   const int j = blockIdx.y;
-  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j >= njob) return;
   const JacJob& jb = jobs[j];
-  if (I > jb.nout) return;
+  const int64_t nout = jb.nout;
+  const int64_t I0 = (int64_t)blockIdx.x * kOdJobPoints;
+  if (I0 >= nout) return;  // the whole CTA, before its barrier
   const Real* x = reinterpret_cast<const Real*>(od_all) + jb.od_off;
-  const Stencil<Real> st = interp_stencil<Real>(jb.spec, I);  // FP32 weights in the mixed path
-  Real v = 0;
-  if (st.n == 1) v = od_ext_t(x, jb.n_in, st.i[0]);
-  else
+  Real* o = reinterpret_cast<Real*>(out) + jb.dst_off;
+  const int64_t n_in = jb.n_in;
+  const int64_t Iend = min(nout, I0 + kOdJobPoints);
+  const bool general = jb.spec.kind != 0 && jb.spec.itype < 0;
+  if (general) {  // CTA-uniform
+    for (int k = threadIdx.x; k < 203; k += blockDim.x) {
+      Real4 c;
+      c.x = ia_coef<Real>(0, k);
+      c.y = ia_coef<Real>(1, k);
+      c.z = ia_coef<Real>(2, k);
+      c.w = ia_coef<Real>(3, k);
+      ia[k] = c;
+    }
+    __syncthreads();
+    const int2* map = jb.spec.map;
+    for (int64_t I = I0 + threadIdx.x + 1; I <= Iend; I += blockDim.x) {
+      const int2 mp = map[I - 1];
+      const int64_t i = mp.x;
+      const Real4 c = ia[mp.y];
+      Real v = c.x * od_ext_t(x, n_in, i - 1);
+      v += c.y * od_ext_t(x, n_in, i);
+      v += c.z * od_ext_t(x, n_in, i + 1);
+      v += c.w * od_ext_t(x, n_in, i + 2);
+      o[I - 1] = v;
+    }
+    return;
+  }
+  for (int64_t I = I0 + threadIdx.x + 1; I <= Iend; I += blockDim.x) {
+    const Stencil<Real> st = interp_stencil<Real>(jb.spec, I);  // FP32 weights in the mixed path
+    Real v = 0;
+    if (st.n == 1) v = od_ext_t(x, n_in, st.i[0]);
+    else
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext_t(x, jb.n_in, st.i[k]);
-  reinterpret_cast<Real*>(out)[jb.dst_off + (I - 1)] = v;
+      for (int k = 0; k < 4; ++k) v += st.w[k] * od_ext_t(x, n_in, st.i[k]);
+    o[I - 1] = v;
+  }
 }
 
 template __global__ void k_od_jobs<false>(const JacJob*, int, const void*, void*);

@@ -54,8 +54,10 @@ struct SumD {
 // FP32 argument lies within 1e-3 of a rounding boundary it is redone in
 // float-float (ZFL and ZSLOPE as hi + lo pairs, products and sums with their
 // exact errors, about 1e-8 absolute), and within 1e-7 of the boundary after
-// that, in FP64 from the record.
-__device__ __noinline__ int table_index_near_boundary(int k, float zfl, float zs, GridRecLo lo, const GridRecD* rd) {
+// that, in FP64 with ZFL and ZSLOPE formed again from the line record `rec`
+// of this CTA's layer, as CNVFNQ's set-up forms them.
+__device__ __noinline__ int table_index_near_boundary(int k, float zfl, float zs, GridRecLo lo, const PanelArgs* pa,
+                                                      int64_t rec, int q, int grid) {
   const float kf = (float)k;
   const float p = kf * zs;
   const float pe = fmaf(kf, zs, -p);                // kf*zs = p + pe exactly
@@ -67,7 +69,11 @@ __device__ __noinline__ int table_index_near_boundary(int k, float zfl, float zs
   const float n = rintf(a);
   const float dd = (a - n) + al;                    // |ZF| - n
   if (fabsf(fabsf(dd) - 0.5f) < 1e-7f) {
-    const double zf64 = fma((double)k, rd->zs, rd->zfl);
+    // ZFkL and ZSLOPE in FP64 from the line, as the record set-up forms them
+    const LayerPlan& P = pa->plans[blockIdx.y + pa->layer0];
+    const LinePrep L = pa->prep[(int64_t)blockIdx.y * pa->stride + rec];
+    const CnvfnqSetup cs = cnvfnq_setup(P, pa->vft_all[P.vft_off + q], L.vnu, L.recalf, L.bhwdxf);
+    const double zf64 = fma((double)k, cs.zslope, cs.zf[grid - 1]);
     return (int)(fabs(zf64) + 1.5);
   }
   return (int)n + 1 + (dd >= 0.5f ? 1 : (dd < -0.5f ? -1 : 0));
@@ -326,8 +332,7 @@ __device__ __forceinline__ float term_fast(const PanelSmem<false>& S, const Grid
 // the FP64-exact index replaces the FP32-index one (both hits by construction)
 template <int GRID>
 __device__ __forceinline__ float fix_terms(const PanelSmem<false>& S, const GridRec* buf, int64_t base,
-                                        const GridRecLo* __restrict__ reclo, const GridRecD* __restrict__ recd,
-                                        int g, unsigned fix, int* err) {
+                                        const GridRecLo* __restrict__ reclo, const PanelArgs& a, int g, unsigned fix) {
   float c = 0.f;
   while (fix) {
     const int k = __ffs(fix) - 1;
@@ -337,10 +342,11 @@ __device__ __forceinline__ float fix_terms(const PanelSmem<false>& S, const Grid
     float d;
     const int izf = fast_index(kk, r, &d);
     const float vf = table_term<GRID>(S, r, min(izf, kNFMX));
-    const int iz = fabsf(d) > 0.499f ? table_index_near_boundary(kk, r.zfl, r.zs, reclo[base + k], recd + (base + k))
-                                     : izf;
+    const int iz = fabsf(d) > 0.499f
+                       ? table_index_near_boundary(kk, r.zfl, r.zs, reclo[base + k], &a, base + k, r.q, GRID)
+                       : izf;
     if (iz > kNFMX) {
-      atomicOr(err, 2);
+      atomicOr(a.err, 2);
       c -= vf;
     } else if (iz != izf) {
       c += table_term<GRID>(S, r, iz) - vf;
@@ -422,7 +428,7 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
         }
       }
       float bsum = (s0 + s1) + (s2 + s3);
-      if (fix) bsum += fix_terms<GRID>(S, buf, base, reclo, recd, g, fix, a.err);
+      if (fix) bsum += fix_terms<GRID>(S, buf, base, reclo, a, g, fix);
       acc.add(bsum);
     }
   }
@@ -430,7 +436,7 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
 }
 
 template <bool Plain>
-__global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArgs a) {
+__global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __grid_constant__ PanelArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -469,7 +475,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArg
   const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
   const GridRec* rec2 = rec1 + a.stride;
   const GridRec* rec3 = rec2 + a.stride;
-  const GridRecD* rd1 = a.recd + (int64_t)layer * a.stride * 3;
+  const GridRecD* rd1 = Plain ? a.recd + (int64_t)layer * a.stride * 3 : nullptr;  // FP64 path only
   const GridRecD* rd2 = rd1 + a.stride;
   const GridRecD* rd3 = rd2 + a.stride;
   const GridRecLo* rl1 = a.reclo + (int64_t)layer * a.stride * 3;
@@ -773,8 +779,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(PanelArg
   }
 }
 
-template __global__ void k_panel<false>(PanelArgs);
-template __global__ void k_panel<true>(PanelArgs);
+template __global__ void k_panel<false>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<true>(const __grid_constant__ PanelArgs);
 
 // ---------------------------------------------------------------------------
 // Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1 (CNVF4Q).

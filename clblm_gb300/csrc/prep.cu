@@ -299,11 +299,6 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
   const LayerPlan& P = plans[layer + layer0];
   int64_t n = P.line_hi - P.line_lo + 1;
   const double* vft = vft_all + P.vft_off;
-  double WAVDXF = P.dv / kDXF1;
-  double DVR2 = (kDXF2 / kDXF1) * P.dv;
-  double DVR3 = (kDXF3 / kDXF1) * P.dv;
-  double CONF2 = P.dv / DVR2;
-  double CONF3 = P.dv / DVR3;
   double amax = 0.;
   unsigned long long bad = 0;
   unsigned long long steps = 0;  // CNVFNQ inner steps JMAX1-JMIN1+1 of the accepted lines
@@ -357,21 +352,14 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
         interp_coef(c_CGAUSS, IZM, ZETDIF, DEPTHA, &STRDA);
         interp_coef(c_CER, IZM, ZETDIF, DEPTHA, &STRVRA);
       }
-      double ZSLOPE = lp.recalf * WAVDXF;
-      double ZINT = (lp.vnu - vft[q]) / P.dv;
-      double BHWDXF = lp.bhwdxf;  // HWDXF / ZSLOPE
-      int JMAX1 = (int)(ZINT + BHWDXF + 1.5);
-      int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
+      // BHWDXF = HWDXF / ZSLOPE comes with the line
+      const CnvfnqSetup cs = cnvfnq_setup(P, vft[q], lp.vnu, lp.recalf, lp.bhwdxf);
+      const double ZSLOPE = cs.zslope;
+      const int JMAX1 = cs.jmax1, JMIN1 = cs.jmin1, J2SHFT = cs.j2shft, J3SHFT = cs.j3shft;
       if (JMAX1 >= JMIN1) steps += (unsigned long long)(JMAX1 - JMIN1 + 1);
-      double RSHFT = 0.5;
-      if (ZINT < 0.0) RSHFT = -RSHFT;
-      int J2SHFT = (int)(ZINT * (1. - CONF2) + RSHFT);
-      int J3SHFT = (int)(ZINT * (1. - CONF3) + RSHFT);
-      int JMIN2 = JMIN1 - J2SHFT;
-      int JMIN3 = JMIN1 - J3SHFT;
-      double ZF1L = ((double)(JMIN1 - 2) - ZINT) * ZSLOPE;
-      double ZF2L = ((double)(JMIN2 - 2) - ZINT * CONF2) * ZSLOPE;
-      double ZF3L = ((double)(JMIN3 - 2) - ZINT * CONF3) * ZSLOPE;
+      const int JMIN2 = JMIN1 - J2SHFT;
+      const int JMIN3 = JMIN1 - J3SHFT;
+      const double ZF1L = cs.zf[0], ZF2L = cs.zf[1], ZF3L = cs.zf[2];
       // global indices: grid k point J of panel q is kPanel_k * q + J - 1
       g1.g_lo = kPanelPts * q + JMIN1 - 1;
       g1.g_hi = kPanelPts * q + JMAX1 - 1;
@@ -402,9 +390,11 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       rec[o + t] = g1;
       rec[o + stride + t] = g2;
       rec[o + 2 * stride + t] = g3;
-      recd[o + t] = d1;
-      recd[o + stride + t] = d2;
-      recd[o + 2 * stride + t] = d3;
+      if (!P.mixed) {  // the mixed gather redoes its rare exact indices from the line itself
+        recd[o + t] = d1;
+        recd[o + stride + t] = d2;
+        recd[o + 2 * stride + t] = d3;
+      }
       reclo[o + t] = l1;
       reclo[o + stride + t] = l2;
       reclo[o + 2 * stride + t] = l3;

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/clblm_gb300.h"
@@ -146,7 +147,12 @@ struct clblm_handle {
 
 namespace {
 
+// Set on host planning threads: their errors are only returned; the failing
+// plan is redone on the calling thread, which records the message.
+thread_local bool tl_quiet_err = false;
+
 int set_err(clblm_handle* h, int code, const char* fmt, ...) {
+  if (tl_quiet_err) return code;
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -446,6 +452,23 @@ void line_range(const clblm_handle* h, double VBOT, double VTOP, int64_t* lo, in
   }
 }
 
+// The largest float at or below x.
+float float_at_or_below(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = std::nextafter(f, -HUGE_VALF);
+  return f;
+}
+
+// The sticky JRAD after one ODLAY call (clblm_ODLAY.f90:349-352, OPDPTH
+// :877-878): the control's value on the first pass, then the state, dropped
+// to 0 for V1/kT < 5 unless it is -1.
+int jrad_step(int jrad_state, bool first_pass, int jrad_ctrl, double V1, double tave) {
+  int JRAD = first_pass ? jrad_ctrl : jrad_state;
+  const double XKT = tave / kRADCN2;
+  if (((V1 / XKT) < 5.) && (JRAD != -1)) JRAD = 0;
+  return JRAD;
+}
+
 int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g, const clblm_od_ctrl_t* c,
                int jrad_state, bool first_pass, HostPlan* hp, int* jrad_after) {
   if (!lay || !g || !c) return set_err(h, CLBLM_ERR_ARG, "null argument");
@@ -463,10 +486,8 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   double ALFAV = g->sample * std::max(g->dv_normal, g->dv_narrow);
   double DV = g->dv_normal;
   if (!(std::fabs(g->dv_normal - g->dv_narrow) / g->dv_normal > 0.2)) DV = g->dv_narrow;
-  // sticky JRAD, clblm_ODLAY.f90:349-352 and OPDPTH :877-878
-  int JRAD = first_pass ? c->jrad : jrad_state;
-  double XKT = lay->tave / kRADCN2;
-  if (((V1 / XKT) < 5.) && (JRAD != -1)) JRAD = 0;
+  const int JRAD = jrad_step(jrad_state, first_pass, c->jrad, V1, lay->tave);
+  const double XKT = lay->tave / kRADCN2;
   *jrad_after = JRAD;
   if (JRAD != 0 && JRAD != 1) return set_err(h, CLBLM_ERR_UNSUPPORTED, "JRAD=%d is not on this path", JRAD);
   P.v1 = V1;
@@ -476,6 +497,10 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.rdv = 1. / DV;
   P.dvr2 = (kDXF2 / kDXF1) * DV;
   P.dvr3 = (kDXF3 / kDXF1) * DV;
+  P.conf2 = DV / P.dvr2;
+  P.conf3 = DV / P.dvr3;
+  P.omconf2 = 1. - P.conf2;
+  P.omconf3 = 1. - P.conf3;
   P.alfav = ALFAV;
   P.alfmax = 4. * ALFAV;
   P.nalfmax = (int)(P.alfmax / DV);
@@ -500,9 +525,12 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.tratio = lay->tave / kT0;
   P.ln_tratio = std::log(P.tratio);
   P.mixed = c->precision == CLBLM_PREC_PLAIN ? 0 : 1;
+  P.epp_abs_f = float_at_or_below(-1.001);
+  P.epp_neg_f = float_at_or_below(-0.999);
   P.rhorat = (lay->pave / kP0) * (kT0 / lay->tave);
   P.pavp0 = lay->pave / kP0;
   P.pavp2 = P.pavp0 * P.pavp0;
+  P.spfac = 1. + 0. * P.pavp2;
   P.jrad = JRAD;
   P.ilnflg = c->line_rejec ? 0 : -1;
   P.dptmn = c->dptmin;
@@ -524,6 +552,10 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
     P.scor[m] = q296 / qt;
     P.rhoslf[m] = P.rhorat * P.wk[m] / lay->wtot;
     P.alfd1[m] = std::sqrt(FAD * lay->tave / CLBLM_ISO1_MASS[m - 1]);
+    P.rhodif[m] = P.rhorat - P.rhoslf[m];
+    P.scor_f[m] = (float)P.scor[m];
+    P.rhoslf_f[m] = (float)P.rhoslf[m];
+    P.alfd1_f[m] = (float)P.alfd1[m];
   }
   // panels: VFT advanced by 2400 DV until VFT + (NHI-1) DV > V2 (panelOut)
   hp->vft.clear();
@@ -588,6 +620,12 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.beta = kRADCN2 / lay->tave;
   P.beta0 = kRADCN2 / kT0;
   P.betacr4 = P.beta - P.beta0;
+  P.xkt_f = (float)P.xkt;
+  P.betacr_f = (float)P.betacr;
+  P.betacr4_f = (float)P.betacr4;
+  P.beta_f = (float)P.beta;
+  P.ln_tratio_f = (float)P.ln_tratio;
+  P.rhorat_f = (float)P.rhorat;
   P.f4_lo = lower_bound_h(h->h_vnu, 0, h->nlines, P.v1l4);
   if (P.f4_lo < h->nlines && !(h->h_vnu[P.f4_lo] - h->shiftmax * P.rhorat > 0.))
     return set_err(h, CLBLM_ERR_UNSUPPORTED, "line centres at or below 0 cm-1 are not on this path");
@@ -726,15 +764,27 @@ struct Batch {
 
 int64_t pad256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
+// Workspace bytes of one layer OD in a batch: the per-line buffers of the
+// line chain and of the far-wing chain (the FP64 records only on the FP64
+// path), the OD and R4 grids.
+size_t od_job_bytes(const LayerPlan& P, bool plain) {
+  const size_t per_line = sizeof(LinePrep) + sizeof(int) + 3 * (sizeof(GridRec) + sizeof(GridRecLo) + 2 * sizeof(int)) +
+                          (plain ? 3 * sizeof(GridRecD) : 0);
+  const size_t per_f4 = sizeof(F4Prep) + sizeof(ShrunkLine) + 4 * sizeof(int64_t) + 1 + sizeof(int) + sizeof(int4) +
+                        sizeof(F4Rec) + 2 * sizeof(int) + (plain ? sizeof(F4RecD) : 0);
+  const size_t real = plain ? 8 : 4;
+  return (size_t)(P.line_hi - P.line_lo + 1) * per_line + (size_t)(P.f4_hi - P.f4_lo) * per_f4 +
+         (size_t)(P.nsamp + P.nptr4) * real;
+}
+
 // Bytes of OD-pipeline workspace one batch of layers may take: half of the
 // device memory free at the call (the layers of a batch share launches, and
 // every batch replays the far-wing walk's serial record loop, so fewer,
-// larger batches are faster), between 8 and 96 GB.  The estimate per layer
-// is the sum of the per-line and per-point buffers.
+// larger batches are faster), between 8 and 160 GB.
 size_t od_batch_budget() {
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return (size_t)24 << 30;
-  const size_t lo = (size_t)8 << 30, hi = (size_t)96 << 30;
+  const size_t lo = (size_t)8 << 30, hi = (size_t)160 << 30;
   const size_t half = free_b / 2;
   return half < lo ? lo : (half > hi ? hi : half);
 }
@@ -919,6 +969,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.rec = h->rec.as<GridRec>();
   pa.recd = h->recd.as<GridRecD>();
   pa.reclo = h->reclo.as<GridRecLo>();
+  pa.prep = h->prep.as<LinePrep>();
   pa.stride = lstride;
   pa.ranges = h->ranges.as<int64_t>();
   pa.panel_stride = pstride;
@@ -1047,7 +1098,8 @@ int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
   CUDA_TRY(h, h->prep.ensure(sizeof(LinePrep) * d.lsc));
   CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * d.lsc));
   CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * d.lsc * 3));
-  CUDA_TRY(h, h->recd.ensure(sizeof(GridRecD) * d.lsc * 3));
+  // FP64 records: the FP64 path only
+  CUDA_TRY(h, h->recd.ensure(plain ? sizeof(GridRecD) * d.lsc * 3 : 256));
   CUDA_TRY(h, h->gpm.ensure(sizeof(int) * d.lsc * 3));
   CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * d.lsc * 3));
   CUDA_TRY(h, h->gsm.ensure(sizeof(int) * d.lsc * 3));
@@ -1074,7 +1126,7 @@ int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
   CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * d.cnt));
   CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * d.fsc));
   CUDA_TRY(h, h->f4rec.ensure(sizeof(F4Rec) * (d.fsc + 4096 * d.cnt)));
-  CUDA_TRY(h, h->f4recd.ensure(sizeof(F4RecD) * (d.fsc + 4096 * d.cnt)));
+  CUDA_TRY(h, h->f4recd.ensure(plain ? sizeof(F4RecD) * (d.fsc + 4096 * d.cnt) : 256));
   CUDA_TRY(h, h->f4nrec.ensure(sizeof(int64_t) * nL));
   CUDA_TRY(h, h->f4nmir.ensure(sizeof(int64_t) * nL));
   CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
@@ -1621,9 +1673,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
     int count = 0;
     size_t bytes = 0;
     while (first + count < n) {
-      const LayerPlan& P = rp.hps[first + count].P;
-      size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
-                 (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+      const size_t b = od_job_bytes(rp.hps[first + count].P, plain);
       if (count > 0 && bytes + b > budget) break;
       bytes += b;
       count++;
@@ -2012,6 +2062,64 @@ int jac_block_list(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ct
   return CLBLM_OK;
 }
 
+// The plans of every block of one profile (jac_plan_block per block), the
+// blocks spread over host threads.  The sticky JRAD each block starts from
+// depends only on the blocks' V1 and the layers' temperatures, so it is
+// replayed first and the blocks are then independent.  A failing block is
+// planned again on the calling thread, which records its message; the first
+// failing block's code is returned, as the sequential loop would.
+int jac_plan_blocks(clblm_handle* h, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac, const JacSetup& js,
+                    const std::vector<double>& dvn, const std::vector<double>& dvf,
+                    const std::vector<JacBlock>& blocks, int* jr, bool* fp, std::vector<std::vector<HostPlan>>* plans,
+                    std::vector<int64_t>* nlims) {
+  const size_t nb = blocks.size();
+  const int njob = (int)js.job_var.size();
+  const int nl = (int)dvn.size();
+  std::vector<int> jr0(nb);
+  std::vector<char> fp0(nb);
+  int r = *jr;
+  bool f = *fp;
+  for (size_t b = 0; b < nb; ++b) {
+    jr0[b] = r;
+    fp0[b] = f ? 1 : 0;
+    for (int j = 0; j < njob; ++j) {
+      r = jrad_step(r, f, ctrl->od.jrad, blocks[b].v1, js.lays[(size_t)js.job_var[j] * nl + js.job_lay[j]].tave);
+      f = false;
+    }
+  }
+  plans->assign(nb, std::vector<HostPlan>());
+  nlims->assign(nb, 0);
+  std::vector<int> rcs(nb, CLBLM_OK);
+  std::atomic<size_t> next{0};
+  auto work = [&](bool quiet) {
+    tl_quiet_err = quiet;
+    for (size_t b; (b = next.fetch_add(1)) < nb;) {
+      int jb = jr0[b];
+      bool fb = fp0[b] != 0;
+      rcs[b] = jac_plan_block(h, ctrl, jac, js, dvn, dvf, blocks[b].v1, blocks[b].v2, &jb, &fb, &(*plans)[b],
+                              &(*nlims)[b]);
+    }
+    tl_quiet_err = false;
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>(nb, std::min(16u, hw));
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < nt; ++t) pool.emplace_back(work, true);
+  work(true);
+  for (auto& t : pool) t.join();
+  for (size_t b = 0; b < nb; ++b) {
+    if (rcs[b] == CLBLM_OK) continue;
+    int jb = jr0[b];
+    bool fb = fp0[b] != 0;
+    const int rc = jac_plan_block(h, ctrl, jac, js, dvn, dvf, blocks[b].v1, blocks[b].v2, &jb, &fb, &(*plans)[b],
+                                  &(*nlims)[b]);
+    return rc ? rc : rcs[b];
+  }
+  *jr = r;
+  *fp = f;
+  return CLBLM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -2125,9 +2233,7 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
       int count = 0;
       size_t bytes = 0;
       while (first + count < njob) {
-        const LayerPlan& P = hps[first + count].P;
-        size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
-                   (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+        const size_t b = od_job_bytes(hps[first + count].P, plain);
         if (count > 0 && bytes + b > budget) break;
         bytes += b;
         count++;
@@ -2174,10 +2280,12 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
         if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "k_interp_map_jobs: %s", cudaGetErrorString(e));
       }
       if (plain)
-        k_od_jobs<true><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
+        k_od_jobs<true><<<dim3((unsigned)((nlim + kOdJobPoints - 1) / kOdJobPoints), count), kOdJobThreads, 0,
+                          h->stream>>>(
             h->jjobs.as<JacJob>(), count, h->od.p, h->jod.p);
       else
-        k_od_jobs<false><<<dim3((unsigned)((nlim + 255) / 256), count), 256, 0, h->stream>>>(
+        k_od_jobs<false><<<dim3((unsigned)((nlim + kOdJobPoints - 1) / kOdJobPoints), count), kOdJobThreads, 0,
+                           h->stream>>>(
             h->jjobs.as<JacJob>(), count, h->od.p, h->jod.p);
       {
         cudaError_t e = cudaGetLastError();
@@ -2407,12 +2515,13 @@ int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_
     int rc = jac_setup(h, col, ctrl, jac, &pr.js, &pr.dvn, &pr.dvf);
     if (!rc) rc = jac_block_list(h, col, ctrl, pr.js, pr.dvn, pr.dvf, &pr.blocks);
     int64_t npts = 0;
+    std::vector<std::vector<HostPlan>> bplans;
+    std::vector<int64_t> nlims;
+    if (!rc) rc = jac_plan_blocks(h, ctrl, jac, pr.js, pr.dvn, pr.dvf, pr.blocks, &jr, &fp, &bplans, &nlims);
     for (size_t b = 0; !rc && b < pr.blocks.size(); ++b) {
-      std::vector<HostPlan> hps;
-      int64_t nlim;
-      rc = jac_plan_block(h, ctrl, jac, pr.js, pr.dvn, pr.dvf, pr.blocks[b].v1, pr.blocks[b].v2, &jr, &fp, &hps,
-                          &nlim);
-      if (!rc && nlim != pr.blocks[b].n) rc = set_err(h, CLBLM_ERR_GRID, "Jacobian block length changed");
+      std::vector<HostPlan>& hps = bplans[b];
+      const int64_t nlim = nlims[b];
+      if (nlim != pr.blocks[b].n) rc = set_err(h, CLBLM_ERR_GRID, "Jacobian block length changed");
       if (rc) break;
       BUnit u;
       u.prof = i;
@@ -2514,9 +2623,7 @@ int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_
       c.wave = job_wave[first];
       size_t bytes = 0;
       while (first + c.count < njob && job_wave[first + c.count] == c.wave) {
-        const LayerPlan& P = bp->hps[first + c.count].P;
-        size_t b = (size_t)(P.line_hi - P.line_lo + 1) * 300 + (size_t)(P.f4_hi - P.f4_lo) * 220 +
-                   (size_t)P.nsamp * real + (size_t)P.nptr4 * real;
+        const size_t b = od_job_bytes(bp->hps[first + c.count].P, plain);
         if (c.count > 0 && bytes + b > kBatchWsBudget) break;
         bytes += b;
         c.count++;
@@ -2551,11 +2658,11 @@ int batch_enqueue(clblm_handle* h, BatchPlan& bp, const clblm_profile_t* prof, c
     h->launches += 2;
     k_interp_map_jobs<<<dim3((unsigned)((bmax + 63) / 64), c.count), 64, 0, h->stream>>>(jobs, c.count);
     if (plain)
-      k_od_jobs<true><<<dim3((unsigned)((nmax + 255) / 256), c.count), 256, 0, h->stream>>>(jobs, c.count, h->od.p,
-                                                                                             h->jod.p);
+      k_od_jobs<true><<<dim3((unsigned)((nmax + kOdJobPoints - 1) / kOdJobPoints), c.count), kOdJobThreads, 0,
+                        h->stream>>>(jobs, c.count, h->od.p, h->jod.p);
     else
-      k_od_jobs<false><<<dim3((unsigned)((nmax + 255) / 256), c.count), 256, 0, h->stream>>>(jobs, c.count, h->od.p,
-                                                                                              h->jod.p);
+      k_od_jobs<false><<<dim3((unsigned)((nmax + kOdJobPoints - 1) / kOdJobPoints), c.count), kOdJobThreads, 0,
+                         h->stream>>>(jobs, c.count, h->od.p, h->jod.p);
     {
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "batch OD gather: %s", cudaGetErrorString(e));
@@ -2745,19 +2852,25 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
     const double* dvo = reinterpret_cast<const double*>(h->jblk.as<unsigned char>() + 8 * bp.j1.size());
     for (const BUnit& U : bp.units) {
       const BProfile& pr = bp.profs[U.prof];
+      std::vector<int> first_of(pr.nl, -1);  // the unit's first job of each layer
       for (int q = 0; q < U.njob; ++q) {
         const int j = U.job0 + q;
         const LayerPlan& P = bp.hps[j].P;
         JacJob& jb = jobs[j];
         jb.spec = interp_spec(P.v1, P.dv, P.nsamp, U.v1, pr.js.dvb, U.nlim);
         const int il = pr.js.job_lay[q];
+        auto same = [&](int r) {
+          return pr.js.job_lay[r] == il && bp.hps[U.job0 + r].P.dv == P.dv && bp.hps[U.job0 + r].P.nsamp == P.nsamp;
+        };
         int owner = q;
-        for (int r = 0; r < q; ++r)
-          if (pr.js.job_lay[r] == il && bp.hps[U.job0 + r].P.dv == P.dv &&
-              bp.hps[U.job0 + r].P.nsamp == P.nsamp) {
-            owner = r;
-            break;
-          }
+        if (first_of[il] < 0) first_of[il] = q;
+        else if (same(first_of[il])) owner = first_of[il];
+        else
+          for (int r = 0; r < q; ++r)
+            if (same(r)) {
+              owner = r;
+              break;
+            }
         jb.map = dmap + U.map_off + (int64_t)owner * U.nlim;
         jb.spec.map = jb.map;
         jb.build_map = (owner == q && jb.spec.kind != 0 && jb.spec.itype < 0) ? 1 : 0;
