@@ -59,6 +59,9 @@ struct LayerPlan {
   int64_t first_rec_end;          // first line index after the first record read
   // far wing
   double dvr4, bound4, v1r4, v2r4st, v1l4, v2l4, beta, beta0, betacr4;
+  double recpi;                   // 1/(2 ASIN(1)) of CNVF4Q
+  double rdvr4;                   // 1/DVR4 (the mixed records' nearest grid point only)
+  float bndsq_f;                  // BOUND**2 (mixed records)
   int64_t nptr4;                  // R4 points on the global far-wing grid
   int nblk4;                      // LBLF4Q blocks of <= 2500 points along the panels
   int64_t blk_off;                // this layer's block table: v1r4 / npt / m0 at blk_off + b
@@ -89,7 +92,7 @@ struct LinePrep {
   double recalf;   // 1 / ALFV
   double alfv;     // ALFV
   double bhwdxf;   // BHWDXF = HWDXF / ZSLOPE of CNVFNQ
-  double zetai;
+  double zetdif;   // ZETDIF = 100*ZETA - (IZETA-1)
   int iz;          // IZETA
   int fpanel;      // first panel whose MAX1 fits the line (-1: rejected)
 };
@@ -148,7 +151,13 @@ struct GridRecLo {
 
 // Far-wing pseudo line after SHRINQ (LINE_SHRINK, clblm_LineData.f90:88-94).
 struct ShrunkLine {
-  double vnu, sp, alfa, alfd, spp;
+  double vnu, sp;
+  // binary64 ALFA, ALFD, SPP on the FP64 path; on the mixed path f[0..3] =
+  // ALFA, ALFD, SP, SPP as floats (they set no index)
+  union {
+    double d[3];
+    float f[6];
+  } w;
   int mol;
   int pad;
 };

@@ -37,7 +37,13 @@ struct ContIn {
 
 // LINF4Q-corrected line (before SHRINQ)
 struct F4Prep {
-  double vnu, sp, alfa, alfd;
+  double vnu, sp;
+  // widths: binary64 ALFA, ALFD on the FP64 path; on the mixed path, where
+  // they set no index or group, f[0..2] = ALFA, ALFD, SP as floats
+  union {
+    double d[2];
+    float f[4];
+  } w;
   int mol, pass;
 };
 
@@ -55,6 +61,7 @@ struct ShapeTabs {
 extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
 // FP32 copies of CF1, CF2, CF3, CGAUSS, CER (mixed-path shape coefficients)
 extern __constant__ float c_SHAPEf[5][102];
+extern __constant__ float c_AVRATf[102];
 __global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const double* vft_all, LinePrep* out,
                             int64_t out_stride, unsigned long long* stats);
 __global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,

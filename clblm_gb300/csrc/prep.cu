@@ -24,6 +24,7 @@ namespace clblm {
 
 __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
 __constant__ float c_SHAPEf[5][102];
+__constant__ float c_AVRATf[102];
 // MaxISOTPL_smass, clblm_ConstParam.f90:246-251 (molecules 1..9)
 __constant__ int c_MAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
 
@@ -67,6 +68,21 @@ __device__ __forceinline__ bool fits_panel(double vnu, double vft, double dv, do
   return (int)a <= max1;
 }
 
+// The same decision, first in FP32 from the binary64 difference d = VNU - VFT:
+// the FP32 argument lies within 4e-7 (|d/DV| + BHWDXF + 1.5) of the exact one,
+// so farther than 1e-2 + 1e-6 (|d/DV| + BHWDXF) from MAX1 + 1 it decides
+// JMAX1 <= MAX1 (INT truncates: INT(a) <= MAX1 is a < MAX1 + 1 for MAX1 >= 0);
+// nearer, fits_panel decides.
+__device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rdv_f, float bhwdxf_f, double dv,
+                                                double rdv, double bhwdxf, int max1) {
+  const double d = vnu - vft;
+  const float dr = (float)d * rdv_f;
+  const float a = dr + bhwdxf_f + 1.5f;
+  const float lim = (float)(max1 + 1);
+  if (fabsf(a - lim) > 1e-2f + 1e-6f * (fabsf(dr) + bhwdxf_f)) return a < lim;
+  return fits_panel(vnu, vft, dv, rdv, bhwdxf, max1);
+}
+
 __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                             const double* __restrict__ vft_all, LinePrep* __restrict__ out,
                             int64_t out_stride, unsigned long long* __restrict__ stats) {
@@ -83,7 +99,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     r.recalf = 0.;
     r.alfv = 0.;
     r.bhwdxf = 0.;
-    r.zetai = 0.;
+    r.zetdif = 0.;
     r.iz = 0;
     r.fpanel = -1;
     int iflg = lines.iflg[i];
@@ -111,7 +127,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
       double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
-      double ALFL = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
+      double ALFL = ALFA0I * P.rhodif[m] + HWHMSI * P.rhoslf[m];  // RHODIF = RHORAT - RHOSLF
       double ALFAD = VNU * P.alfd1[m];
       double ZETA = ALFL / (ALFL + ALFAD);
       double FZETA = 100. * ZETA;
@@ -134,28 +150,38 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
         // HWF3*ALFV + VNU < VFT: the line cannot reach the panel it is read
         // in.  Lines of the first record are read with panel 0; k_line_records
         // checks that no later line would be dropped at its own read panel.
-        if (kHWF3 * ALFV + VNU < vft[0]) ok = false;
+        // (ALFV > 0: the sum is at least VNU, so only VNU < VFT can drop.)
+        if (VNU < vft[0] && kHWF3 * ALFV + VNU < vft[0]) ok = false;
         if (ok) {
           double RECALF = 1. / ALFV;
-          double EPP = (double)lines.epp[i];
-          if (EPP <= -1.001) EPP = fabs(EPP);
+          const float EPP0 = lines.epp[i];
+          double SP;
           if (P.mixed) {
             // strengths set no index: FP32 (RADFN when JRAD = 1, SCOR, the
-            // lower-state Boltzmann factor and the stimulated-emission term)
+            // lower-state Boltzmann factor and the stimulated-emission term);
+            // EPP's tests are the binary64 ones, exactly
             float sui = (float)SUI;
-            if (P.jrad == 1) sui *= radfn_f((float)lines.vnu[i], (float)P.xkt);
-            if (EPP > -0.999)
-              sui = sui * (float)P.scor[m] * __expf(-(float)EPP * (float)P.betacr) *
-                    (1.f + __expf(-(float)VNU / (float)P.xkt));
+            if (P.jrad == 1) sui *= radfn_f((float)lines.vnu[i], P.xkt_f);
+            const float EPP = EPP0 <= P.epp_abs_f ? fabsf(EPP0) : EPP0;
+            if (EPP > P.epp_neg_f)
+              sui = sui * P.scor_f[m] * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
             SUI = sui;
+            SP = SUI;  // SUI*(1 + 0*PAVP2)
+            // SPEAK = SUI/ALFV > 0 unless SUI = 0 (SUI >= 1e-45, 1/ALFV > 1:
+            // no underflow), so with DPTMIN = 0 the test is SUI = 0
+            if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
+              if (P.dptmn == 0. ? sui == 0.f : SUI * RECALF <= P.dptmn) ok = false;
+            }
           } else {
+            double EPP = (double)EPP0;
+            if (EPP <= -1.001) EPP = fabs(EPP);
             if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
             if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
-          }
-          double SP = SUI * (1. + 0. * P.pavp2);
-          if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
-            double SPEAK = SUI * RECALF;
-            if (SPEAK <= P.dptmn) ok = false;  // DPTFAC == 0 on this path
+            SP = SUI * P.spfac;
+            if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
+              double SPEAK = SUI * RECALF;
+              if (SPEAK <= P.dptmn) ok = false;  // DPTFAC == 0 on this path
+            }
           }
           if (ok) {
             lincnt++;
@@ -164,7 +190,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             r.vnu = VNU;
             r.sp = SP;
             r.recalf = RECALF;
-            r.zetai = ZETA;
+            r.zetdif = ZETDIF;
             r.iz = IZ;
             // first panel p with JMAX1 <= MAX1 (the estimate only starts the search)
             double HWDXF = kHWF1 / kDXF1;
@@ -172,11 +198,12 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             double BHWDXF = HWDXF / ZSLOPE;
             r.alfv = ALFV;
             r.bhwdxf = BHWDXF;
-            double est = ((VNU - vft[0]) * P.rdv + BHWDXF + 1.5 - (double)P.max1) * (1. / kPanelPts);
-            int p = est > 0. ? (int)est : 0;
+            const float rdv_f = (float)P.rdv, bh_f = (float)BHWDXF;
+            const float est = ((float)(VNU - vft[0]) * rdv_f + bh_f + 1.5f - (float)P.max1) * (1.f / kPanelPts);
+            int p = est > 0.f ? (int)fminf(est, 2.e9f) : 0;
             if (p > P.npanels) p = P.npanels;
-            while (p > 0 && fits_panel(VNU, vft[p - 1], P.dv, P.rdv, BHWDXF, P.max1)) p--;
-            while (p < P.npanels && !fits_panel(VNU, vft[p], P.dv, P.rdv, BHWDXF, P.max1)) p++;
+            while (p > 0 && fits_panel_fast(VNU, vft[p - 1], rdv_f, bh_f, P.dv, P.rdv, BHWDXF, P.max1)) p--;
+            while (p < P.npanels && !fits_panel_fast(VNU, vft[p], rdv_f, bh_f, P.dv, P.rdv, BHWDXF, P.max1)) p++;
             r.fpanel = p;  // == npanels: never convolved
           }
         }
@@ -327,30 +354,31 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
         int64_t rs = (gi / 250) * 250;  // first line of this line's record
         int qr = 0;
         if (rs - 1 >= P.line_lo) qr = max(0, qpanel[layer * stride + (rs - 1 - P.line_lo)]);
-        if (qr > 0 && qr < P.npanels && kHWF3 * lp.alfv + lp.vnu < vft[qr]) bad++;
+        // (ALFV > 0: only VNU < VFT can drop the line)
+        if (qr > 0 && qr < P.npanels && lp.vnu < vft[qr] && kHWF3 * lp.alfv + lp.vnu < vft[qr]) bad++;
       }
       double DEPTHA = lp.sp * lp.recalf;
       int IZM = lp.iz;
-      double ZETDIF = 100. * lp.zetai - (double)(IZM - 1);
-      double STRFA1, STRFA2, STRFA3, STRDA, STRVRA;
+      double ZETDIF = lp.zetdif;  // 100*ZETA - (IZ-1)
+      double STRFA1 = 0., STRFA2 = 0., STRFA3 = 0., STRDA = 0., STRVRA = 0.;
+      float c[5];  // the same, FP32 (mixed path)
       if (P.mixed) {  // shape coefficients set no index: FP32
         const float zd = (float)ZETDIF, de = (float)DEPTHA;
-        float c[5];
         for (int q5 = 0; q5 < 5; ++q5) {
           const float* T = c_SHAPEf[q5];
           c[q5] = de * (T[IZM - 1] + zd * (T[IZM] - T[IZM - 1]));
         }
-        STRFA1 = c[0];
-        STRFA2 = c[1];
-        STRFA3 = c[2];
-        STRDA = c[3];
-        STRVRA = c[4];
       } else {
         interp_coef(c_CF1, IZM, ZETDIF, DEPTHA, &STRFA1);
         interp_coef(c_CF2, IZM, ZETDIF, DEPTHA, &STRFA2);
         interp_coef(c_CF3, IZM, ZETDIF, DEPTHA, &STRFA3);
         interp_coef(c_CGAUSS, IZM, ZETDIF, DEPTHA, &STRDA);
         interp_coef(c_CER, IZM, ZETDIF, DEPTHA, &STRVRA);
+        c[0] = (float)STRFA1;
+        c[1] = (float)STRFA2;
+        c[2] = (float)STRFA3;
+        c[3] = (float)STRDA;
+        c[4] = (float)STRVRA;
       }
       // BHWDXF = HWDXF / ZSLOPE comes with the line
       const CnvfnqSetup cs = cnvfnq_setup(P, vft[q], lp.vnu, lp.recalf, lp.bhwdxf);
@@ -371,14 +399,16 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       g2.zfl = (float)ZF2L;
       g3.zfl = (float)ZF3L;
       g1.zs = g2.zs = g3.zs = (float)ZSLOPE;
-      g1.a0 = (float)STRFA1;
-      g1.a1 = (float)STRDA;
-      g1.a2 = (float)STRVRA;
-      g2.a0 = (float)STRFA2;
-      g3.a0 = (float)STRFA3;
-      d1 = {ZF1L, ZSLOPE, STRFA1, STRDA, STRVRA};
-      d2 = {ZF2L, ZSLOPE, STRFA2, 0., 0.};
-      d3 = {ZF3L, ZSLOPE, STRFA3, 0., 0.};
+      g1.a0 = c[0];
+      g1.a1 = c[3];
+      g1.a2 = c[4];
+      g2.a0 = c[1];
+      g3.a0 = c[2];
+      if (!P.mixed) {
+        d1 = {ZF1L, ZSLOPE, STRFA1, STRDA, STRVRA};
+        d2 = {ZF2L, ZSLOPE, STRFA2, 0., 0.};
+        d3 = {ZF3L, ZSLOPE, STRFA3, 0., 0.};
+      }
       const float zs_lo = (float)(ZSLOPE - (double)g1.zs);
       l1 = {(float)(ZF1L - (double)g1.zfl), zs_lo};
       l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
@@ -667,7 +697,8 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
     int64_t i = P.f4_lo + t;
     F4Prep r;
     r.pass = 0;
-    r.vnu = r.sp = r.alfa = r.alfd = 0.;
+    r.vnu = r.sp = 0.;
+    r.w.d[0] = r.w.d[1] = 0.;
     r.mol = 0;
     int iflg = lines.iflg[i];
     int molf = lines.mol[i];
@@ -683,33 +714,39 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
     if (ok) {
       double SUI = (double)lines.sp[i] * P.wk[m];
       if (SUI != 0. && !(lines.vnu[i] < P.v1l4)) {
-        double alfa = (double)lines.alfa[i];
-        double hwhm = (double)lines.hwhm[i];
-        if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
-        double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
-        double EPP = (double)lines.epp[i];
-        if (VNU == 0.) SUI = 2. * SUI;
-        if (EPP <= -1.001) EPP = fabs(EPP);
-        if (EPP > -0.999) {
-          if (P.mixed)
-            SUI = (float)SUI * (float)P.scor[m] * __expf(-(float)EPP * (float)P.betacr4) *
-                  (1.f + __expf(-(float)VNU * (float)P.beta));
-          else
-            SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
-        }
-        if (P.mixed) {  // widths set no index or group: FP32
-          const float TMPCOR = __expf(lines.tmpalf[i] * (float)P.ln_tratio);  // (T/296)^n
-          const float rs = (float)P.rhoslf[m];
-          r.alfa = ((float)alfa * TMPCOR) * ((float)P.rhorat - rs) + ((float)hwhm * TMPCOR) * rs;
-          r.alfd = (float)VNU * (float)P.alfd1[m];
+        const float alfa_in = lines.alfa[i], hwhm_in = lines.hwhm[i];
+        const double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
+        const float EPP0 = lines.epp[i];
+        if (P.mixed) {
+          // FP32 throughout but for the centre: strengths and widths set no
+          // index or group.  EPP's tests are the binary64 ones, exactly.
+          float sui = (float)SUI;
+          if (VNU == 0.) sui = 2.f * sui;
+          const float EPP = EPP0 <= P.epp_abs_f ? fabsf(EPP0) : EPP0;
+          const float vf = (float)VNU;
+          if (EPP > P.epp_neg_f) sui = sui * P.scor_f[m] * __expf(-EPP * P.betacr4_f) * (1.f + __expf(-vf * P.beta_f));
+          float alfa = alfa_in;
+          if (m == 7) alfa = (float)(((double)alfa_in - 0.21 * (double)hwhm_in) / (1.0 - 0.21));
+          const float TMPCOR = __expf(lines.tmpalf[i] * P.ln_tratio_f);  // (T/296)^n
+          const float rs = P.rhoslf_f[m];
+          r.w.f[0] = (alfa * TMPCOR) * (P.rhorat_f - rs) + (hwhm_in * TMPCOR) * rs;
+          r.w.f[1] = vf * P.alfd1_f[m];
+          r.w.f[2] = sui;
+          r.sp = (double)sui;  // SP = SUI*(1 + 0*PAVP2) = SUI
         } else {
+          double alfa = (double)alfa_in, hwhm = (double)hwhm_in;
+          if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
+          double EPP = (double)EPP0;
+          if (VNU == 0.) SUI = 2. * SUI;
+          if (EPP <= -1.001) EPP = fabs(EPP);
+          if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
           double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
           double ALFA0I = alfa * TMPCOR;
           double HWHMSI = hwhm * TMPCOR;
-          r.alfa = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
-          r.alfd = VNU * P.alfd1[m];
+          r.w.d[0] = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
+          r.w.d[1] = VNU * P.alfd1[m];
+          r.sp = SUI * P.spfac;
         }
-        r.sp = SUI * (1. + 0. * P.pavp2);
         r.vnu = VNU;
         r.mol = m;
         r.pass = 1;
@@ -1105,8 +1142,50 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
   const int64_t* S = src + (int64_t)layer * stride;
   const F4Prep* pr = prep + (int64_t)layer * stride;
   ShrunkLine* O = out + (int64_t)layer * stride;
+  const bool mixed = plans[layer + layer0].mixed != 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
     const int4 gr = G[g];
+    int slot = gr.z;
+    if (mixed) {
+      // the centre VNU = SUMV/SUMS sets the record's point range: binary64 in
+      // the reference's order; the widths and the FP32 strength set no index
+      double SUMS = 0., SUMV = 0., SUMS2 = 0., SUMV2 = 0.;
+      float SAL = 0.f, SAD = 0.f, SAL2 = 0.f, SAD2 = 0.f;
+      for (int u = gr.x; u <= gr.y; ++u) {
+        const F4Prep& r = pr[S[u]];
+        const bool weak = r.sp < 1.0e-35;
+        const double sp = weak ? 0.0 : r.sp;
+        const float spf = weak ? 0.f : r.w.f[2];
+        if (r.mol != 2) {
+          SUMV = SUMV + r.vnu * sp;
+          SUMS = SUMS + sp;
+          SAL = SAL + spf * r.w.f[0];
+          SAD = SAD + spf * r.w.f[1];
+        } else {
+          SUMV2 = SUMV2 + r.vnu * sp;
+          SUMS2 = SUMS2 + sp;
+          SAL2 = SAL2 + spf * r.w.f[0];
+          SAD2 = SAD2 + spf * r.w.f[1];
+        }
+      }
+      for (int k = 0; k < 2; ++k) {
+        const double ss = k ? SUMS2 : SUMS;
+        if (!(ss > 0.)) continue;
+        ShrunkLine L;
+        L.vnu = (k ? SUMV2 : SUMV) / ss;
+        L.sp = ss;
+        const float sf = (float)ss;
+        L.w.f[0] = (k ? SAL2 : SAL) / sf;
+        L.w.f[1] = (k ? SAD2 : SAD) / sf;
+        L.w.f[2] = sf;
+        L.w.f[3] = 0.f;  // SUMC: zero
+        L.w.f[4] = L.w.f[5] = 0.f;
+        L.mol = k ? 2 : 0;
+        L.pad = 0;
+        O[slot++] = L;
+      }
+      continue;
+    }
     double SUMAL = 0., SUMAD = 0., SUMS = 0., SUMV = 0., SUMC = 0.;
     double SUMAL2 = 0., SUMAD2 = 0., SUMS2 = 0., SUMV2 = 0., SUMC2 = 0.;
     for (int u = gr.x; u <= gr.y; ++u) {
@@ -1115,25 +1194,24 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
       if (r.mol != 2) {
         SUMV = SUMV + r.vnu * sp;
         SUMS = SUMS + sp;
-        SUMAL = SUMAL + sp * r.alfa;
-        SUMAD = SUMAD + sp * r.alfd;
+        SUMAL = SUMAL + sp * r.w.d[0];
+        SUMAD = SUMAD + sp * r.w.d[1];
         SUMC = SUMC + 0.;
       } else {
         SUMV2 = SUMV2 + r.vnu * sp;
         SUMS2 = SUMS2 + sp;
-        SUMAL2 = SUMAL2 + sp * r.alfa;
-        SUMAD2 = SUMAD2 + sp * r.alfd;
+        SUMAL2 = SUMAL2 + sp * r.w.d[0];
+        SUMAD2 = SUMAD2 + sp * r.w.d[1];
         SUMC2 = SUMC2 + 0.;
       }
     }
-    int slot = gr.z;
     if (SUMS > 0.) {
       ShrunkLine L;
       L.sp = SUMS;
-      L.alfa = SUMAL / SUMS;
-      L.alfd = SUMAD / SUMS;
+      L.w.d[0] = SUMAL / SUMS;
+      L.w.d[1] = SUMAD / SUMS;
       L.vnu = SUMV / SUMS;
-      L.spp = SUMC;
+      L.w.d[2] = SUMC;
       L.mol = 0;
       L.pad = 0;
       O[slot++] = L;
@@ -1141,10 +1219,10 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
     if (SUMS2 > 0.) {
       ShrunkLine L;
       L.sp = SUMS2;
-      L.alfa = SUMAL2 / SUMS2;
-      L.alfd = SUMAD2 / SUMS2;
+      L.w.d[0] = SUMAL2 / SUMS2;
+      L.w.d[1] = SUMAD2 / SUMS2;
       L.vnu = SUMV2 / SUMS2;
-      L.spp = SUMC2;
+      L.w.d[2] = SUMC2;
       L.mol = 2;
       L.pad = 0;
       O[slot++] = L;
@@ -1166,37 +1244,37 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
   const double ZSQBND = 64. * 64.;
   const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
   const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
-  const double RECPI = 1. / (2. * asin(1.));
+  const double RECPI = P.recpi;
   const double XNUI = VNUI - P.v1r4;
   int JMIN = (int)((XNUI - P.bound4) / P.dvr4 + 2.);
   if (JMIN < 1) JMIN = 1;
   int JMAX = (int)((XNUI + P.bound4) / P.dvr4 + 1.);
   if (JMAX > (int)P.nptr4) JMAX = (int)P.nptr4;
-  const double BNDSQ = P.bound4 * P.bound4;
   const bool co2 = (L.mol == 2);
   r->jmin = JMIN;
   r->jmax = JMAX;
-  // FP32 distances are taken from the grid point nearest the line centre, so
-  // that points near the centre do not lose digits to cancellation
-  const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
   auto pair = [](double v) { return make_float2((float)v, (float)v); };
   auto pairf = [](float v) { return make_float2(v, v); };
-  r->nmc = pair(-(double)mc);
-  r->x0 = pair((double)mc * P.dvr4 - XNUI);
   if constexpr (Mixed) {
-    const float ALFADI = (float)L.alfd, ALFALI = (float)L.alfa;
+    // FP32 distances are taken from a grid point mc near the line centre, so
+    // that points near the centre do not lose digits to cancellation (mc is
+    // this path's own choice: the product with 1/DVR4 serves)
+    const int mc = (int)floor(XNUI * P.rdvr4 + 0.5);
+    r->nmc = pairf((float)(-mc));
+    r->x0 = pair((double)mc * P.dvr4 - XNUI);
+    const float ALFALI = L.w.f[0], ALFADI = L.w.f[1];
     const float ZETAI = ALFALI / (ALFALI + ALFADI);
     int IZ = (int)(100.f * ZETAI + (float)kONEPL);
     IZ = IZ < 1 ? 1 : (IZ > 101 ? 101 : IZ);
     const float ZETDIF = 100.f * ZETAI - (float)(IZ - 1);
-    const float a0 = (float)c_AVRAT[IZ - 1], a1 = (float)c_AVRAT[IZ];
+    const float a0 = c_AVRATf[IZ - 1], a1 = c_AVRATf[IZ];
     const float ALFAVI = (a0 + ZETDIF * (a1 - a0)) * (ALFALI + ALFADI);
     const float RALFVI = 1.f / ALFAVI;
-    const float SP = (float)L.sp, rpi = (float)RECPI;
+    const float SP = L.w.f[2], rpi = (float)(1. / 3.14159265358979323846);
     const float SIL = SP * rpi * ALFALI;
     const float SIV = (ALFALI * RALFVI) * SP * rpi * RALFVI;
     const float ALFLI2 = ALFALI * ALFALI, ALFVI2 = ALFAVI * ALFAVI;
-    const float F4BND = SIL / (ALFLI2 + (float)BNDSQ);
+    const float F4BND = SIL / (ALFLI2 + P.bndsq_f);
     r->sil = pairf(SIL);
     r->al2 = pairf(ALFLI2);
     r->ralv2 = pairf(1.f / ALFVI2);
@@ -1204,9 +1282,13 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
     r->sb3 = pairf(SIV * (float)B3);
     // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
     r->nfb0 = pairf(co2 ? -2.f * F4BND : -F4BND);
-    r->fb2 = pairf(co2 ? F4BND / (float)BNDSQ : 0.f);
+    r->fb2 = pairf(co2 ? F4BND / P.bndsq_f : 0.f);
   } else {
-    const double ALFADI = L.alfd, ALFALI = L.alfa;
+    const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
+    r->nmc = pair(-(double)mc);
+    r->x0 = pair((double)mc * P.dvr4 - XNUI);
+    const double BNDSQ = P.bound4 * P.bound4;
+    const double ALFALI = L.w.d[0], ALFADI = L.w.d[1];
     const double ZETAI = ALFALI / (ALFALI + ALFADI);
     const int IZ = (int)(100. * ZETAI + kONEPL);
     const double ZETDIF = 100. * ZETAI - (double)(IZ - 1);
@@ -1256,7 +1338,7 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     if (P.mixed) f4_record<true>(P, L, L.vnu, &r, &d);
     else f4_record<false>(P, L, L.vnu, &r, &d);
     // lines beyond the last point's reach, or without strength, add nothing
-    if (L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) {
+    if (L.vnu >= VNULST || (L.sp == 0. && (P.mixed ? L.w.f[3] == 0.f : L.w.d[2] == 0.))) {
       r.jmin = d.jmin = 1 << 30;
       r.jmax = d.jmax = -1;
     }
@@ -1271,7 +1353,9 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     int64_t nm = 0;
     for (int64_t i = 0; i < n && S[i].vnu <= 25. + 1.; ++i) {
       const ShrunkLine L = S[i];
-      if (!(L.vnu > 0. && L.vnu <= 25.) || L.vnu >= VNULST || (L.sp == 0. && L.spp == 0.)) continue;
+      if (!(L.vnu > 0. && L.vnu <= 25.) || L.vnu >= VNULST ||
+          (L.sp == 0. && (P.mixed ? L.w.f[3] == 0.f : L.w.d[2] == 0.)))
+        continue;
       F4Rec r;
       F4RecD d;
       if (P.mixed) f4_record<true>(P, L, -L.vnu, &r, &d);

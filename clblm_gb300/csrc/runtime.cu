@@ -322,6 +322,9 @@ int upload_tables(clblm_handle* h) {
     for (int q = 0; q < 5; ++q)
       for (int i = 0; i < 102; ++i) sf[q][i] = (float)src[q][i];
     CUDA_TRY(h, cudaMemcpyToSymbol(c_SHAPEf, sf, sizeof sf));
+    float af[102];
+    for (int i = 0; i < 102; ++i) af[i] = (float)CLBLM_AVRAT[i];
+    CUDA_TRY(h, cudaMemcpyToSymbol(c_AVRATf, af, sizeof af));
   }
   rt_upload_interp_coef(h->stream);
   return CLBLM_OK;
@@ -626,6 +629,9 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.beta_f = (float)P.beta;
   P.ln_tratio_f = (float)P.ln_tratio;
   P.rhorat_f = (float)P.rhorat;
+  P.recpi = 1. / (2. * std::asin(1.));
+  P.rdvr4 = 1. / P.dvr4;
+  P.bndsq_f = (float)(P.bound4 * P.bound4);
   P.f4_lo = lower_bound_h(h->h_vnu, 0, h->nlines, P.v1l4);
   if (P.f4_lo < h->nlines && !(h->h_vnu[P.f4_lo] - h->shiftmax * P.rhorat > 0.))
     return set_err(h, CLBLM_ERR_UNSUPPORTED, "line centres at or below 0 cm-1 are not on this path");
