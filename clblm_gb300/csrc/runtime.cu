@@ -47,13 +47,12 @@ struct DevBuf {
   size_t bytes = 0;
   cudaError_t ensure(size_t n) {
     if (n <= bytes) return cudaSuccess;
+    release();
     g_buf_gen++;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
     size_t want = n + n / 8 + 256;
     cudaError_t e = cudaMalloc(&p, want);
     if (e == cudaSuccess) bytes = want;
+    else p = nullptr;
     return e;
   }
   void release() {
@@ -118,6 +117,19 @@ struct clblm_handle {
   std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
   uint64_t bgraph_clock = 0;
   bool panel_attr_set[2] = {false, false};
+  // every device buffer of the handle but the line list
+  std::vector<DevBuf*> buffers() {
+    std::vector<DevBuf*> v = {&cont_self, &cont_for, &cont_texp, &cont_co2, &tabs,    &plans,   &vft,    &prep,    &qpanel,
+                              &rec,       &recd,     &ranges,    &od,      &r4,      &absrb,  &stats,   &alfvmax,
+                              &blockmax,  &nlines_d, &f4prep,    &f4sh,    &f4nout,  &f4rec,  &f4recd,  &f4nrec,
+                              &f4nmir,    &f4pm,     &f4sm,      &err,     &outbuf,  &pblk,   &bv1,     &bn,
+                              &bm0,       &bfac,     &f4blk,     &f4ntot,  &f4cidx,  &f4vb,   &f4lb,    &f4src,
+                              &f4flag,    &f4cut,    &f4grp,     &f4nxt,   &ragg,    &segpool, &gpm,    &gsm,
+                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk};
+    for (auto& b : rt) v.push_back(&b);
+    for (auto& b : imap) v.push_back(&b);
+    return v;
+  }
   Tuner tune;
   bool last_plain = false;  // precision of the last OD / radiance / Jacobian call
   // FFT scan: cuFFT plans of the last transform size, the transform buffer
@@ -783,16 +795,23 @@ size_t od_job_bytes(const LayerPlan& P, bool plain) {
          (size_t)(P.nsamp + P.nptr4) * real;
 }
 
-// Bytes of OD-pipeline workspace one batch of layers may take: half of the
-// device memory free at the call (the layers of a batch share launches, and
-// every batch replays the far-wing walk's serial record loop, so fewer,
-// larger batches are faster), between 8 and 160 GB.
-size_t od_batch_budget() {
+// Bytes of OD-pipeline workspace one batch of layers may take: 60 % of the
+// device memory free at the call plus what the library's own buffers hold
+// already (the layers of a batch share launches, and every batch replays the
+// far-wing walk's serial record loop, so fewer, larger batches are faster),
+// between 8 and 192 GB.  CLBLM_OD_BUDGET_GB=<GB> sets it instead.
+size_t od_batch_budget(clblm_handle* h) {
+  if (const char* e = std::getenv("CLBLM_OD_BUDGET_GB")) {
+    const double gb = std::atof(e);
+    if (gb > 0.) return (size_t)(gb * (double)((size_t)1 << 30));
+  }
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return (size_t)24 << 30;
-  const size_t lo = (size_t)8 << 30, hi = (size_t)160 << 30;
-  const size_t half = free_b / 2;
-  return half < lo ? lo : (half > hi ? hi : half);
+  size_t held = 0;
+  for (const DevBuf* b : h->buffers()) held += b->bytes;
+  const size_t lo = (size_t)8 << 30, hi = (size_t)192 << 30;
+  const size_t b = (free_b + held) / 10 * 6;
+  return b < lo ? lo : (b > hi ? hi : b);
 }
 
 // The fastest of n launch variants on the work at hand: each variant runs once
@@ -1381,17 +1400,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& b : h->lines) b.release();
-  DevBuf* bufs[] = {&h->cont_self, &h->cont_for, &h->cont_texp, &h->tabs,    &h->plans,  &h->vft,     &h->prep,
-                    &h->qpanel,    &h->rec,      &h->recd,      &h->ranges,  &h->od,     &h->r4,      &h->absrb,
-                    &h->stats,     &h->alfvmax,  &h->blockmax,  &h->nlines_d, &h->f4prep, &h->f4sh,
-                    &h->f4nout,    &h->f4rec,    &h->f4recd,    &h->f4nrec,  &h->f4nmir, &h->f4pm,    &h->f4sm,
-                    &h->err,       &h->outbuf,   &h->pblk,      &h->bv1,     &h->bn,     &h->bm0,     &h->bfac,
-                    &h->f4blk,     &h->f4ntot,   &h->f4cidx,    &h->f4vb,    &h->f4lb,   &h->f4src,   &h->f4flag,
-                    &h->f4cut,     &h->f4grp,    &h->f4nxt,   &h->ragg,  &h->segpool,    &h->gpm,       &h->gsm,      &h->reclo,     &h->jprof,   &h->jod,    &h->jmap,    &h->jjobs,
-                    &h->jblk};
-  for (DevBuf* b : bufs) b->release();
-  for (auto& b : h->rt) b.release();
-  for (auto& b : h->imap) b.release();
+  for (DevBuf* b : h->buffers()) b->release();
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   h->bgraphs.clear();
@@ -1673,7 +1682,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
   for (int il = 0; il < n; ++il) maxn = std::max(maxn, rp.grid_n[il]);
   for (auto& b : h->rt) CUDA_TRY(h, b.ensure(real * (maxn + 8)));
   // layers in batches sized to the workspace budget
-  const size_t budget = od_batch_budget();
+  const size_t budget = od_batch_budget(h);
   int cur = 0;  // ping-pong index of the merged spectra
   for (int first = 0; first < n;) {
     int count = 0;
@@ -2201,7 +2210,7 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
   int jr = h->jrad;
   bool fp = h->first_pass_jrad;
   int64_t total = 0;
-  const size_t budget = od_batch_budget();
+  const size_t budget = od_batch_budget(h);
   for (auto& blk : blocks) {
     std::vector<HostPlan> hps;
     int64_t nlim;
@@ -2402,8 +2411,8 @@ struct BChunk {             // one launch of the OD pipeline
   int bmax = 1;             // most interpolation blocks among them
 };
 
-constexpr size_t kBatchWsBudget = (size_t)24 << 30;
-constexpr size_t kBatchWaveBudget = (size_t)32 << 30;
+// of the OD budget: half for one chunk's OD workspace, a quarter for a
+// wave's OD slabs and maps
 
 uint64_t fnv(uint64_t s, const void* p, size_t n) {
   const unsigned char* b = static_cast<const unsigned char*>(p);
@@ -2576,6 +2585,8 @@ int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_
   }
   bp->jr_after = jr;
   bp->fp_after = fp;
+  const size_t budget = od_batch_budget(h);
+  const size_t ws_budget = budget / 2, wave_budget = budget / 4;
   // interpolation blocks of every unit (interpSpectrum's general branch)
   for (auto& u : bp->units) {
     const double dvb = bp->profs[u.prof].js.dvb;
@@ -2601,7 +2612,7 @@ int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_
     for (auto& u : bp->units) {
       const BProfile& pr = bp->profs[u.prof];
       const int64_t uj = (int64_t)pr.js.nvar * pr.nl * u.nlim, um = (int64_t)u.njob * u.nlim;
-      if ((jod > 0 || map > 0) && (size_t)(jod + uj) * real + (size_t)(map + um) * 8 > kBatchWaveBudget) {
+      if ((jod > 0 || map > 0) && (size_t)(jod + uj) * real + (size_t)(map + um) * 8 > wave_budget) {
         wave++;
         jod = map = 0;
       }
@@ -2630,7 +2641,7 @@ int batch_plan(clblm_handle* h, const clblm_profile_t* prof, int n, const clblm_
       size_t bytes = 0;
       while (first + c.count < njob && job_wave[first + c.count] == c.wave) {
         const size_t b = od_job_bytes(bp->hps[first + c.count].P, plain);
-        if (c.count > 0 && bytes + b > kBatchWsBudget) break;
+        if (c.count > 0 && bytes + b > ws_budget) break;
         bytes += b;
         c.count++;
       }
