@@ -55,7 +55,20 @@ struct ShapeTabs {
   const double* t1d;   // F1, FG, XVER interleaved [3*NFMX]
   const double* t2d;
   const double* t3d;
+  const void* mixed;   // MixedTables: the mixed path's shared-memory image
 };
+
+// The mixed path's shape tables as k_panel holds them in shared memory, in
+// the layout of their global image, so that one bulk copy stages them (each
+// array padded to a multiple of 16 bytes)
+constexpr int kNFMXp = (kNFMX + 3) & ~3;
+struct alignas(16) MixedTables {
+  float2 t1ab[kNFMXp];  // R1 tables F1, FG
+  float t1c[kNFMXp];    // R1 table XVER
+  float t2[kNFMXp];
+  float t3[kNFMXp];
+};
+static_assert(sizeof(MixedTables) % 16 == 0, "a bulk copy moves multiples of 16 bytes");
 
 // kernels of prep.cu (FP64, no FMA contraction)
 extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];

@@ -114,10 +114,9 @@ struct PanelTiles {
 template <>
 struct PanelSmem<false> : PanelTiles {
   float absf[kAbsStage];
-  float2 t1ab[kNFMX];    // R1 tables F1, FG
-  float t1c[kNFMX];      // R1 table XVER
-  float t2[kNFMX];
-  float t3[kNFMX];
+  MixedTables tab;       // shape tables (one bulk copy)
+  uint64_t tab_bar;      // completes the table copy
+  float4 cw[4];          // Lagrange weights of the R3->R2 and R2->R1 combine by point offset
   float r3n[kR3Pts];     // R3 p-frame 0..160, lines of panels <= p
   float r3o[8];          // R3 p-frame 0..7, lines of panels <= p-1
   float r2[kR2Pts];      // R2 p-frame 0..615
@@ -138,6 +137,9 @@ struct PanelSmem<true> : PanelTiles {
   double seg_v[kMaxSeg], seg_d[kMaxSeg];
   int nseg, seg_slot;
 };
+
+// three CTAs of the mixed path per SM (228 KB, 1 KB reserved per CTA)
+static_assert(3 * (sizeof(PanelSmem<false>) + 1024) <= 228 * 1024, "mixed k_panel: three CTAs per SM");
 
 size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
 
@@ -291,12 +293,12 @@ __device__ __forceinline__ void tile_ranges(const int* __restrict__ pm, const in
 template <int GRID>
 __device__ __forceinline__ float table_term(const PanelSmem<false>& S, const GridRec& r, int iz) {
   if constexpr (GRID == 1) {
-    const float2 ab = S.t1ab[iz - 1];
-    return fmaf(r.a0, ab.x, fmaf(r.a1, ab.y, r.a2 * S.t1c[iz - 1]));
+    const float2 ab = S.tab.t1ab[iz - 1];
+    return fmaf(r.a0, ab.x, fmaf(r.a1, ab.y, r.a2 * S.tab.t1c[iz - 1]));
   } else if constexpr (GRID == 2) {
-    return r.a0 * S.t2[iz - 1];
+    return r.a0 * S.tab.t2[iz - 1];
   } else {
-    return r.a0 * S.t3[iz - 1];
+    return r.a0 * S.tab.t3[iz - 1];
   }
 }
 
@@ -461,16 +463,25 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
       S.t2[i] = a.tabs.t2d[i];
       S.t3[i] = a.tabs.t3d[i];
     }
+    __syncthreads();
   } else {
-    for (int i = tid; i < kNFMX; i += blockDim.x) {
-      const float4 t = a.tabs.t1f[i];
-      S.t1ab[i] = make_float2(t.x, t.y);
-      S.t1c[i] = t.z;
-      S.t2[i] = a.tabs.t2f[i];
-      S.t3[i] = a.tabs.t3f[i];
+    // one bulk copy of the table image; the CTA waits for it just before its
+    // first gather
+    if (tid == 0) {
+      mbar_init(&S.tab_bar, 1);
+      mbar_fence_init();
+      mbar_arrive_expect_tx(&S.tab_bar, (uint32_t)sizeof(MixedTables));
+      bulk_g2s(&S.tab, a.tabs.mixed, (uint32_t)sizeof(MixedTables), &S.tab_bar);
+    }
+    if (tid < 4) {  // combine weights of offsets 0..3 (0: the point itself)
+      const float X00 = -7.f / 128.f, X01 = 105.f / 128.f, X02 = 35.f / 128.f, X03 = -5.f / 128.f;
+      const float X10 = -1.f / 16.f, X11 = 9.f / 16.f;
+      S.cw[tid] = tid == 0 ? make_float4(0.f, 1.f, 0.f, 0.f)
+                  : tid == 1 ? make_float4(X00, X01, X02, X03)
+                  : tid == 2 ? make_float4(X10, X11, X11, X10)
+                             : make_float4(X03, X02, X01, X00);
     }
   }
-  __syncthreads();
 
   const GridRec* rec1 = a.rec + (int64_t)layer * a.stride * 3;
   const GridRec* rec2 = rec1 + a.stride;
@@ -536,6 +547,16 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
   tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, kTiles2, S.lo2, S.hi2);
   tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, kTiles3, S.lo3, S.hi3);
   __syncthreads();
+  if constexpr (!Plain) {  // the tables have landed (bounded wait; the error flag otherwise)
+    const bool ok = mbar_wait_bounded(&S.tab_bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(a.err, 4);
+        mbar_wait_bounded(&S.tab_bar, 0);  // let the copy land before the CTA leaves
+      }
+      return;
+    }
+  }
 
   // ---- R3: line sums on p-frame points 0..160 (new) and 0..7 (old) ----
   // units 0..kTiles3-1: 32 new points each; unit kTiles3: the 8 old points
@@ -711,10 +732,15 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
         if (inloop || extra || fromOld) {
           const Real* R3 = fromOld ? S.r3o : S.r3n;
           int J3 = (Jg - 1) / 4 + 1;
-          if (off == 0) v = R3[J3];
-          else if (off == 1) v = X00 * R3[J3 - 1] + X01 * R3[J3] + X02 * R3[J3 + 1] + X03 * R3[J3 + 2];
-          else if (off == 2) v = X10 * (R3[J3 - 1] + R3[J3 + 2]) + X11 * (R3[J3] + R3[J3 + 1]);
-          else v = X03 * R3[J3 - 1] + X02 * R3[J3] + X01 * R3[J3 + 1] + X00 * R3[J3 + 2];
+          if constexpr (Plain) {  // the reference's sums
+            if (off == 0) v = R3[J3];
+            else if (off == 1) v = X00 * R3[J3 - 1] + X01 * R3[J3] + X02 * R3[J3 + 1] + X03 * R3[J3 + 2];
+            else if (off == 2) v = X10 * (R3[J3 - 1] + R3[J3 + 2]) + X11 * (R3[J3] + R3[J3 + 1]);
+            else v = X03 * R3[J3 - 1] + X02 * R3[J3] + X01 * R3[J3 + 1] + X00 * R3[J3 + 2];
+          } else {  // one weighted sum for every offset (offset 0 weighs the point alone)
+            const float4 w = S.cw[off];
+            v = fmaf(w.x, R3[J3 - 1], fmaf(w.y, R3[J3], fmaf(w.z, R3[J3 + 1], w.w * R3[J3 + 2])));
+          }
         }
         acc.add(v);
         S.r2[J] = acc.value();
@@ -740,10 +766,15 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
         int J2 = (Jg - 1) / 4 + 1;
         const Real* R2 = S.r2;
         Real v;
-        if (off == 0) v = R2[J2];
-        else if (off == 1) v = X00 * R2[J2 - 1] + X01 * R2[J2] + X02 * R2[J2 + 1] + X03 * R2[J2 + 2];
-        else if (off == 2) v = X10 * (R2[J2 - 1] + R2[J2 + 2]) + X11 * (R2[J2] + R2[J2 + 1]);
-        else v = X03 * R2[J2 - 1] + X02 * R2[J2] + X01 * R2[J2 + 1] + X00 * R2[J2 + 2];
+        if constexpr (Plain) {  // the reference's sums
+          if (off == 0) v = R2[J2];
+          else if (off == 1) v = X00 * R2[J2 - 1] + X01 * R2[J2] + X02 * R2[J2 + 1] + X03 * R2[J2 + 2];
+          else if (off == 2) v = X10 * (R2[J2 - 1] + R2[J2 + 2]) + X11 * (R2[J2] + R2[J2 + 1]);
+          else v = X03 * R2[J2 - 1] + X02 * R2[J2] + X01 * R2[J2 + 1] + X00 * R2[J2 + 2];
+        } else {  // one weighted sum for every offset (offset 0 weighs the point alone)
+          const float4 w = S.cw[off];
+          v = fmaf(w.x, R2[J2 - 1], fmaf(w.y, R2[J2], fmaf(w.z, R2[J2 + 1], w.w * R2[J2 + 2])));
+        }
         acc.add(v);
         Real val = acc.value();
         if (P.jrad == 0 && S.nseg > 0) {

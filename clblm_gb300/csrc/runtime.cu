@@ -284,7 +284,7 @@ int upload_tables(clblm_handle* h) {
   std::vector<double> F1, F2, F3, FG, XV;
   shape_tables(F1, F2, F3, FG, XV);
   const int N = kNFMX;
-  size_t bytes = N * sizeof(float4) + 2 * N * sizeof(float) + 5 * N * sizeof(double) + 1024;
+  size_t bytes = N * sizeof(float4) + 2 * N * sizeof(float) + 5 * N * sizeof(double) + sizeof(MixedTables) + 2048;
   CUDA_TRY(h, h->tabs.ensure(bytes));
   std::vector<unsigned char> host(bytes, 0);
   size_t off = 0;
@@ -313,6 +313,15 @@ int upload_tables(clblm_handle* h) {
   size_t o4 = put(t1d.data(), 3 * N * sizeof(double));
   size_t o5 = put(t2d.data(), N * sizeof(double));
   size_t o6 = put(t3d.data(), N * sizeof(double));
+  std::unique_ptr<MixedTables> mt(new MixedTables());
+  std::memset(mt.get(), 0, sizeof(MixedTables));
+  for (int i = 0; i < N; ++i) {
+    mt->t1ab[i] = make_float2(t1f[i].x, t1f[i].y);
+    mt->t1c[i] = t1f[i].z;
+    mt->t2[i] = t2f[i];
+    mt->t3[i] = t3f[i];
+  }
+  size_t o7 = put(mt.get(), sizeof(MixedTables));
   if (off > h->tabs.bytes) return set_err(h, CLBLM_ERR_ARG, "table layout");
   CUDA_TRY(h, cudaMemcpy(h->tabs.p, host.data(), off, cudaMemcpyHostToDevice));
   unsigned char* b = h->tabs.as<unsigned char>();
@@ -322,6 +331,7 @@ int upload_tables(clblm_handle* h) {
   h->shape.t1d = reinterpret_cast<const double*>(b + o4);
   h->shape.t2d = reinterpret_cast<const double*>(b + o5);
   h->shape.t3d = reinterpret_cast<const double*>(b + o6);
+  h->shape.mixed = b + o7;
   CUDA_TRY(h, cudaMemcpyToSymbol(c_AVRAT, CLBLM_AVRAT, sizeof CLBLM_AVRAT));
   CUDA_TRY(h, cudaMemcpyToSymbol(c_CGAUSS, CLBLM_CGAUSS, sizeof CLBLM_CGAUSS));
   CUDA_TRY(h, cudaMemcpyToSymbol(c_CF1, CLBLM_CF1, sizeof CLBLM_CF1));
