@@ -71,19 +71,25 @@ def fp32_peak_tflops():
 
 
 def load_traffic():
-    """DRAM bytes per algorithmic step of each line-shape kernel, from the ncu
-    capture summarised in profiles/ (None before one exists)."""
-    f = ROOT / "profiles" / "dram_traffic.json"
+    """DRAM bytes per output point of each kernel, from the ncu capture whose
+    summary profiles/dram_traffic.txt holds (lines `kernel bytes_per_point`;
+    a kernel without a line reports traffic null)."""
+    out = {}
     try:
-        return json.loads(f.read_text())
-    except Exception:
-        return {}
+        for line in (ROOT / "profiles" / "dram_traffic.txt").read_text().splitlines():
+            f = line.split()
+            if len(f) == 2 and not line.startswith("#"):
+                out[f[0]] = float(f[1])
+    except (OSError, ValueError):
+        pass
+    return out
 
 
-def roofline(work, kt, steps, ms_step):
+def roofline(work, kt, steps, ms_step, points):
     """Roofline of the dominant line-shape kernel: algorithmic FLOPs of one
     launch (the call's step counts) over its CUDA-event time on the library's
-    stream, averaged over the timed steps."""
+    stream, averaged over the timed steps; `points` (the launch's output
+    points) scales the measured DRAM bytes per point to the launch."""
     peak, mhz = fp32_peak_tflops()
     traffic = load_traffic()
     kernels = {
@@ -93,10 +99,10 @@ def roofline(work, kt, steps, ms_step):
     out = {}
     for name, (flop, ms, nstep) in kernels.items():
         ach = flop / (ms * 1e-3) / 1e12 if ms > 0 else None
-        bps = traffic.get(name)
+        bpp = traffic.get(name)
         out[name] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if ach else None,
-                     "traffic": bps * nstep if bps is not None else None,
+                     "traffic": bpp * points if bpp is not None else None,
                      "ms_per_launch": ms, "share_of_step": ms / ms_step, "flop_per_launch": flop}
     top = max(out, key=lambda k: out[k]["ms_per_launch"])
     r = dict(out[top])
@@ -648,7 +654,7 @@ def main():
     c4 = None
     if not args.no_config4:
         c4 = config4_leg(2, fp64_jacobians=args.broadband_fp64_jacobians)
-    roof = roofline(work, kt, args.steps, ms)
+    roof = roofline(work, kt, args.steps, ms, lp)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
