@@ -1125,55 +1125,96 @@ WsDims batch_dims(std::vector<HostPlan>& hps, int first, int count, int64_t* lst
   return d;
 }
 
-// Buffers of one OD batch (sized by d) and of all nL planned layers.
-int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
+// Buffers of one OD batch (sized by d) and of all nL planned layers: the
+// first error, or success.
+cudaError_t ws_alloc(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
   const size_t real = plain ? 8 : 4;
-  CUDA_TRY(h, h->plans.ensure(sizeof(LayerPlan) * nL));
-  CUDA_TRY(h, h->vft.ensure(sizeof(double) * vftt));
-  CUDA_TRY(h, h->prep.ensure(sizeof(LinePrep) * d.lsc));
-  CUDA_TRY(h, h->qpanel.ensure(sizeof(int) * d.lsc));
-  CUDA_TRY(h, h->rec.ensure(sizeof(GridRec) * d.lsc * 3));
+  cudaError_t e = cudaSuccess;
+#define WS_ENSURE(x)                       \
+  do {                                     \
+    if ((e = (x)) != cudaSuccess) return e; \
+  } while (0)
+  WS_ENSURE(h->plans.ensure(sizeof(LayerPlan) * nL));
+  WS_ENSURE(h->vft.ensure(sizeof(double) * vftt));
+  WS_ENSURE(h->prep.ensure(sizeof(LinePrep) * d.lsc));
+  WS_ENSURE(h->qpanel.ensure(sizeof(int) * d.lsc));
+  WS_ENSURE(h->rec.ensure(sizeof(GridRec) * d.lsc * 3));
   // FP64 records: the FP64 path only
-  CUDA_TRY(h, h->recd.ensure(plain ? sizeof(GridRecD) * d.lsc * 3 : 256));
-  CUDA_TRY(h, h->gpm.ensure(sizeof(int) * d.lsc * 3));
-  CUDA_TRY(h, h->reclo.ensure(sizeof(GridRecLo) * d.lsc * 3));
-  CUDA_TRY(h, h->gsm.ensure(sizeof(int) * d.lsc * 3));
-  CUDA_TRY(h, h->ragg.ensure(sizeof(int) * d.raggc));
-  CUDA_TRY(h, h->ranges.ensure(sizeof(int64_t) * 6 * d.psc));
-  CUDA_TRY(h, h->od.ensure(real * d.odt));
-  CUDA_TRY(h, h->r4.ensure(real * d.r4t));
-  CUDA_TRY(h, h->absrb.ensure(sizeof(double) * (kNABSRB + 8) * d.cnt));
-  CUDA_TRY(h, h->stats.ensure(sizeof(unsigned long long) * kStatsPerLayer * nL));
-  CUDA_TRY(h, h->alfvmax.ensure(sizeof(double) * nL));
-  CUDA_TRY(h, h->blockmax.ensure(sizeof(int) * d.smaxc));
-  CUDA_TRY(h, h->nlines_d.ensure(sizeof(int64_t) * nL));
-  CUDA_TRY(h, h->f4prep.ensure(sizeof(F4Prep) * d.fsc));
-  CUDA_TRY(h, h->f4sh.ensure(sizeof(ShrunkLine) * d.fsc));
-  CUDA_TRY(h, h->f4nout.ensure(sizeof(int64_t) * 2 * nL));
-  CUDA_TRY(h, h->f4blk.ensure(sizeof(int64_t) * d.nblk4c));
-  CUDA_TRY(h, h->f4ntot.ensure(sizeof(int64_t) * d.cnt));
-  CUDA_TRY(h, h->f4cidx.ensure(sizeof(int64_t) * (d.fsc + d.cnt)));
-  CUDA_TRY(h, h->f4vb.ensure(sizeof(long long) * d.fsc));
-  CUDA_TRY(h, h->f4lb.ensure(sizeof(long long) * d.fsc));
-  CUDA_TRY(h, h->f4src.ensure(sizeof(int64_t) * d.fsc));
-  CUDA_TRY(h, h->f4flag.ensure(d.fsc));
-  CUDA_TRY(h, h->f4nxt.ensure(sizeof(int) * d.fsc));
-  CUDA_TRY(h, h->f4cut.ensure(sizeof(int64_t) * d.cnt));
-  CUDA_TRY(h, h->f4grp.ensure(sizeof(int4) * d.fsc));
-  CUDA_TRY(h, h->f4rec.ensure(sizeof(F4Rec) * (d.fsc + 4096 * d.cnt)));
-  CUDA_TRY(h, h->f4recd.ensure(plain ? sizeof(F4RecD) * (d.fsc + 4096 * d.cnt) : 256));
-  CUDA_TRY(h, h->f4nrec.ensure(sizeof(int64_t) * nL));
-  CUDA_TRY(h, h->f4nmir.ensure(sizeof(int64_t) * nL));
-  CUDA_TRY(h, h->f4pm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
-  CUDA_TRY(h, h->f4sm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
-  CUDA_TRY(h, h->err.ensure(sizeof(int) * 4));
-  CUDA_TRY(h, h->segpool.ensure(256 + (sizeof(int) * (kSegSlot + 1) + 2 * sizeof(double) * kSegSlot) *
+  WS_ENSURE(h->recd.ensure(plain ? sizeof(GridRecD) * d.lsc * 3 : 256));
+  WS_ENSURE(h->gpm.ensure(sizeof(int) * d.lsc * 3));
+  WS_ENSURE(h->reclo.ensure(sizeof(GridRecLo) * d.lsc * 3));
+  WS_ENSURE(h->gsm.ensure(sizeof(int) * d.lsc * 3));
+  WS_ENSURE(h->ragg.ensure(sizeof(int) * d.raggc));
+  WS_ENSURE(h->ranges.ensure(sizeof(int64_t) * 6 * d.psc));
+  WS_ENSURE(h->od.ensure(real * d.odt));
+  WS_ENSURE(h->r4.ensure(real * d.r4t));
+  WS_ENSURE(h->absrb.ensure(sizeof(double) * (kNABSRB + 8) * d.cnt));
+  WS_ENSURE(h->stats.ensure(sizeof(unsigned long long) * kStatsPerLayer * nL));
+  WS_ENSURE(h->alfvmax.ensure(sizeof(double) * nL));
+  WS_ENSURE(h->blockmax.ensure(sizeof(int) * d.smaxc));
+  WS_ENSURE(h->nlines_d.ensure(sizeof(int64_t) * nL));
+  WS_ENSURE(h->f4prep.ensure(sizeof(F4Prep) * d.fsc));
+  WS_ENSURE(h->f4sh.ensure(sizeof(ShrunkLine) * d.fsc));
+  WS_ENSURE(h->f4nout.ensure(sizeof(int64_t) * 2 * nL));
+  WS_ENSURE(h->f4blk.ensure(sizeof(int64_t) * d.nblk4c));
+  WS_ENSURE(h->f4ntot.ensure(sizeof(int64_t) * d.cnt));
+  WS_ENSURE(h->f4cidx.ensure(sizeof(int64_t) * (d.fsc + d.cnt)));
+  WS_ENSURE(h->f4vb.ensure(sizeof(long long) * d.fsc));
+  WS_ENSURE(h->f4lb.ensure(sizeof(long long) * d.fsc));
+  WS_ENSURE(h->f4src.ensure(sizeof(int64_t) * d.fsc));
+  WS_ENSURE(h->f4flag.ensure(d.fsc));
+  WS_ENSURE(h->f4nxt.ensure(sizeof(int) * d.fsc));
+  WS_ENSURE(h->f4cut.ensure(sizeof(int64_t) * d.cnt));
+  WS_ENSURE(h->f4grp.ensure(sizeof(int4) * d.fsc));
+  WS_ENSURE(h->f4rec.ensure(sizeof(F4Rec) * (d.fsc + 4096 * d.cnt)));
+  WS_ENSURE(h->f4recd.ensure(plain ? sizeof(F4RecD) * (d.fsc + 4096 * d.cnt) : 256));
+  WS_ENSURE(h->f4nrec.ensure(sizeof(int64_t) * nL));
+  WS_ENSURE(h->f4nmir.ensure(sizeof(int64_t) * nL));
+  WS_ENSURE(h->f4pm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
+  WS_ENSURE(h->f4sm.ensure(sizeof(int) * (d.fsc + 4096 * d.cnt)));
+  WS_ENSURE(h->err.ensure(sizeof(int) * 4));
+  WS_ENSURE(h->segpool.ensure(256 + (sizeof(int) * (kSegSlot + 1) + 2 * sizeof(double) * kSegSlot) *
                                           (size_t)kSegPoolSlots));
-  CUDA_TRY(h, h->pblk.ensure(sizeof(int) * vftt));
-  CUDA_TRY(h, h->bv1.ensure(sizeof(double) * (blkt + 1)));
-  CUDA_TRY(h, h->bn.ensure(sizeof(int) * (blkt + 1)));
-  CUDA_TRY(h, h->bm0.ensure(sizeof(int64_t) * (blkt + 1)));
-  CUDA_TRY(h, h->bfac.ensure(sizeof(double) * (kLIMOUT4 + 2) * (blkt + 1)));
+  WS_ENSURE(h->pblk.ensure(sizeof(int) * vftt));
+  WS_ENSURE(h->bv1.ensure(sizeof(double) * (blkt + 1)));
+  WS_ENSURE(h->bn.ensure(sizeof(int) * (blkt + 1)));
+  WS_ENSURE(h->bm0.ensure(sizeof(int64_t) * (blkt + 1)));
+  WS_ENSURE(h->bfac.ensure(sizeof(double) * (kLIMOUT4 + 2) * (blkt + 1)));
+#undef WS_ENSURE
+  return e;
+}
+
+// The buffers ws_alloc sizes: scratch of one batch, nothing in them outlives it.
+std::vector<DevBuf*> ws_buffers(clblm_handle* h) {
+  return {&h->plans,  &h->vft,    &h->prep,   &h->qpanel,   &h->rec,    &h->recd,   &h->gpm,    &h->reclo,
+          &h->gsm,    &h->ragg,   &h->ranges, &h->od,       &h->r4,     &h->absrb,  &h->stats,  &h->alfvmax,
+          &h->blockmax, &h->nlines_d, &h->f4prep, &h->f4sh, &h->f4nout, &h->f4blk, &h->f4ntot, &h->f4cidx,
+          &h->f4vb,   &h->f4lb,   &h->f4src,  &h->f4flag,   &h->f4nxt,  &h->f4cut,  &h->f4grp,  &h->f4rec,
+          &h->f4recd, &h->f4nrec, &h->f4nmir, &h->f4pm,     &h->f4sm,   &h->err,    &h->segpool, &h->pblk,
+          &h->bv1,    &h->bn,     &h->bm0,    &h->bfac};
+}
+
+// Frees every work buffer of the handle (all but the line list, the shape
+// tables and the continuum tables): only between calls, when none holds data.
+void release_work(clblm_handle* h) {
+  for (DevBuf* b : h->buffers())
+    if (b != &h->tabs && b != &h->cont_self && b != &h->cont_for && b != &h->cont_texp && b != &h->cont_co2)
+      b->release();
+}
+
+// ws_alloc; when the device is out of memory (buffers a previous call grew
+// for another shape hold it), the batch buffers are freed and allocated
+// afresh once.
+int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
+  cudaError_t e = ws_alloc(h, d, nL, vftt, blkt, plain);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    for (DevBuf* b : ws_buffers(h)) b->release();
+    e = ws_alloc(h, d, nL, vftt, blkt, plain);
+  }
+  if (e != cudaSuccess)
+    return set_err(h, e == cudaErrorMemoryAllocation ? CLBLM_ERR_OOM : CLBLM_ERR_CUDA, "OD workspace: %s",
+                   cudaGetErrorString(e));
   return CLBLM_OK;
 }
 
@@ -1690,7 +1731,22 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
   size_t real = plain ? 8 : 4;
   int64_t maxn = rp.n0;
   for (int il = 0; il < n; ++il) maxn = std::max(maxn, rp.grid_n[il]);
-  for (auto& b : h->rt) CUDA_TRY(h, b.ensure(real * (maxn + 8)));
+  {  // merged spectra (out of memory: the handle's work buffers are freed, then once more)
+    auto alloc = [&]() -> cudaError_t {
+      for (auto& b : h->rt) {
+        const cudaError_t e = b.ensure(real * (maxn + 8));
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    };
+    cudaError_t e = alloc();
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      release_work(h);
+      e = alloc();
+    }
+    CUDA_TRY(h, e);
+  }
   // layers in batches sized to the workspace budget
   const size_t budget = od_batch_budget(h);
   int cur = 0;  // ping-pong index of the merged spectra
@@ -2229,9 +2285,22 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     if (nlim != blk.n) return set_err(h, CLBLM_ERR_GRID, "Jacobian block length changed");
     const int njob = (int)hps.size();
     // the block's ODs on the uniform grid, [variant][layer][point]
-    CUDA_TRY(h, h->jod.ensure(real * (size_t)js.nvar * nl * nlim));
-    CUDA_TRY(h, h->jmap.ensure(sizeof(int2) * (size_t)njob * nlim));
-    CUDA_TRY(h, h->jjobs.ensure(sizeof(JacJob) * (size_t)njob));
+    {  // (out of memory: the batch scratch and the block buffers, dead here, are freed, then once more)
+      auto alloc = [&]() -> cudaError_t {
+        cudaError_t e = h->jod.ensure(real * (size_t)js.nvar * nl * nlim);
+        if (e == cudaSuccess) e = h->jmap.ensure(sizeof(int2) * (size_t)njob * nlim);
+        if (e == cudaSuccess) e = h->jjobs.ensure(sizeof(JacJob) * (size_t)njob);
+        return e;
+      };
+      cudaError_t e = alloc();
+      if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        for (DevBuf* b : ws_buffers(h)) b->release();
+        for (DevBuf* b : {&h->jod, &h->jmap, &h->jjobs}) b->release();
+        e = alloc();
+      }
+      CUDA_TRY(h, e);
+    }
     // output-grid blocks of interpSpectrum's general branch (shared by all jobs)
     std::vector<int64_t> j1;
     std::vector<double> vo;
@@ -2856,20 +2925,36 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
   for (BChunk& c : bp.chunks) dmax.max_with(batch_dims(bp.hps, c.first, c.count, &c.ls, &c.fs, &c.ps));
   const int njob = (int)bp.hps.size();
   const size_t real = plain ? 8 : 4;
-  rc = ensure_workspace(h, dmax, njob, bp.vftt, bp.blkt, plain);
-  if (rc) return rc;
-  CUDA_TRY(h, h->jod.ensure(real * (size_t)std::max<int64_t>(bp.jod_max, 1)));
-  CUDA_TRY(h, h->jmap.ensure(sizeof(int2) * (size_t)std::max<int64_t>(bp.map_max, 1)));
-  CUDA_TRY(h, h->jjobs.ensure(sizeof(JacJob) * (size_t)std::max(njob, 1)));
-  CUDA_TRY(h, h->jblk.ensure(16 * (bp.j1.size() + 1)));
-  CUDA_TRY(h, h->jprof.ensure(sizeof(double) * (bp.prof_arr.size() + 1)));
   // host outputs: one staging area for all profiles
   int64_t stage = 0;
   for (auto& pr : bp.profs) {
     pr.stage_off = stage;
     if (!dev_out && pr.status == CLBLM_OK) stage += pr.npts * (3 + 2 * (int64_t)(pr.nl + 1));
   }
-  if (!dev_out) CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * (size_t)std::max<int64_t>(stage, 1)));
+  // every buffer of the batch; when the device is out of memory (buffers a
+  // previous call grew for another shape hold it), all of the handle's work
+  // buffers are freed and the batch's allocated afresh once
+  auto alloc = [&]() -> cudaError_t {
+    cudaError_t e = ws_alloc(h, dmax, njob, bp.vftt, bp.blkt, plain);
+    if (e == cudaSuccess) e = h->jod.ensure(real * (size_t)std::max<int64_t>(bp.jod_max, 1));
+    if (e == cudaSuccess) e = h->jmap.ensure(sizeof(int2) * (size_t)std::max<int64_t>(bp.map_max, 1));
+    if (e == cudaSuccess) e = h->jjobs.ensure(sizeof(JacJob) * (size_t)std::max(njob, 1));
+    if (e == cudaSuccess) e = h->jblk.ensure(16 * (bp.j1.size() + 1));
+    if (e == cudaSuccess) e = h->jprof.ensure(sizeof(double) * (bp.prof_arr.size() + 1));
+    if (e == cudaSuccess && !dev_out) e = h->outbuf.ensure(sizeof(double) * (size_t)std::max<int64_t>(stage, 1));
+    return e;
+  };
+  {
+    cudaError_t e = alloc();
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      release_work(h);
+      e = alloc();
+    }
+    if (e != cudaSuccess)
+      return set_err(h, e == cudaErrorMemoryAllocation ? CLBLM_ERR_OOM : CLBLM_ERR_CUDA, "batch buffers: %s",
+                     cudaGetErrorString(e));
+  }
   // job table: every OD job's grid map and slab row
   {
     std::vector<JacJob>& jobs = bp.jobs;
