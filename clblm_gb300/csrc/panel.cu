@@ -104,8 +104,9 @@ constexpr int kPanelWarps = kPanelThreads / 32;
 // record index range [lo, hi) of every tile, one 32-record staging buffer
 // per warp, and the panel's XINT set-up
 constexpr int kBatch = 16;  // records per staging batch of a warp
+// (ranges are kept per 16-point half tile: half tile 2t + h is lanes 16h..16h+15 of tile t)
 struct PanelTiles {
-  int lo1[kTiles1], hi1[kTiles1], lo2[kTiles2], hi2[kTiles2], lo3[kTiles3], hi3[kTiles3];
+  int lo1[2 * kTiles1], hi1[2 * kTiles1], lo2[2 * kTiles2], hi2[2 * kTiles2], lo3[2 * kTiles3], hi3[2 * kTiles3];
   GridRec wrec[kPanelWarps][kBatch];
   XintPanel X;
 };
@@ -262,29 +263,30 @@ __global__ void k_r4_radfac(const LayerPlan* __restrict__ plans, int layer0, con
   } while (N2 < NPTR4);
 }
 
-// Record ranges of the T tiles [G0 + 32t, G0 + 32t + 31] of one grid from the
-// running max of g_hi (pm) and min of g_lo (sm) over the panel's candidate
-// window [w0, w1): lo(t) = first record with pm >= G0 + 32t, hi(t) = first
-// record with sm > G0 + 32t + 31 (w1 when there is none).  Both running
-// bounds are monotone, so each tile boundary is crossed by exactly one
-// record of the window (the first one for boundaries at or below its value),
-// and that record writes it.
-__device__ __forceinline__ long long floordiv32(long long x) { return x >> 5; }  // arithmetic shift: floor
+// Record ranges of the T half tiles [G0 + 16t, G0 + 16t + 15] of one grid
+// from the running max of g_hi (pm) and min of g_lo (sm) over the panel's
+// candidate window [w0, w1): lo(t) = first record with pm >= G0 + 16t,
+// hi(t) = first record with sm > G0 + 16t + 15 (w1 when there is none).
+// Both running bounds are monotone, so each tile boundary is crossed by
+// exactly one record of the window (the first one for boundaries at or below
+// its value), and that record writes it.  The 32-point tile t is half tiles
+// 2t and 2t + 1: its range is [lo(2t), hi(2t + 1)).
+__device__ __forceinline__ long long floordiv16(long long x) { return x >> 4; }  // arithmetic shift: floor
 __device__ __forceinline__ void tile_ranges(const int* __restrict__ pm, const int* __restrict__ sm, int64_t w0,
                                             int64_t w1, int G0, int T, int* lo, int* hi) {
   const long long g0 = G0;
   for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
-    // lo: tiles t with prev < G0 + 32 t <= cur
+    // lo: tiles t with prev < G0 + 16 t <= cur
     const long long cur = pm[i];
     const long long prev = (i == w0) ? LLONG_MIN / 4 : (long long)pm[i - 1];
-    long long ta = (prev < g0) ? 0 : floordiv32(prev - g0) + 1;
-    long long tb = (cur < g0) ? -1 : min(floordiv32(cur - g0), (long long)T - 1);
+    long long ta = (prev < g0) ? 0 : floordiv16(prev - g0) + 1;
+    long long tb = (cur < g0) ? -1 : min(floordiv16(cur - g0), (long long)T - 1);
     for (long long t = ta; t <= tb; ++t) lo[t] = (int)i;
-    // hi: tiles t with prev <= G0 + 32 t + 31 < cur
+    // hi: tiles t with prev <= G0 + 16 t + 15 < cur
     const long long curs = sm[i];
     const long long prevs = (i == w0) ? LLONG_MIN / 4 : (long long)sm[i - 1];
-    ta = (prevs - g0 - 31 <= 0) ? 0 : floordiv32(prevs - g0);
-    tb = (curs - g0 - 32 < 0) ? -1 : min(floordiv32(curs - g0 - 32), (long long)T - 1);
+    ta = (prevs - g0 - 15 <= 0) ? 0 : floordiv16(prevs - g0);
+    tb = (curs - g0 - 16 < 0) ? -1 : min(floordiv16(curs - g0 - 16), (long long)T - 1);
     for (long long t = ta; t <= tb; ++t) hi[t] = (int)i;
   }
 }
@@ -357,39 +359,44 @@ __device__ __forceinline__ float fix_terms(const PanelSmem<false>& S, const Grid
   return c;
 }
 
-// Sum over the records [lo, hi) of one grid at global point g of the lane:
-// the records pass through the warp's shared-memory buffer kBatch at a time,
-// the next batch already loaded into registers while the current one is used.
-// The FP64 path adds record by record in record order; the mixed path sums
-// each batch in FP32 (four partial sums) and adds the batch to the Kahan sum.
+// Sum over the records [lo, hi) of one grid at global point g of the lane.
+// FP64 path: [lo, hi) is the warp's 32-point tile's; the records pass through
+// the warp's shared-memory buffer kBatch at a time (the next batch already in
+// registers) and are added one by one in record order.  Mixed path: [lo, hi)
+// is the lane's 16-point half tile's, so each half warp sums only the records
+// that reach its half (narrow lines reach a few points: a 32-point range
+// would pair most records with lanes they miss); the halves stage
+// kHalfBatch records each, every batch is summed in FP32 (four partial sums)
+// and added to the Kahan sum.
+constexpr int kHalfBatch = kBatch / 2;
 template <bool Plain, int GRID>
 __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs& a, const GridRec* __restrict__ rec,
                                             const GridRecD* __restrict__ recd, const GridRecLo* __restrict__ reclo,
                                             int64_t lo, int64_t hi, int g, bool active, int qmax,
                                             typename std::conditional<Plain, SumD, KahanF>::type& acc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int sl = lane & (kBatch - 1);
-  GridRec* buf = S.wrec[warp];
-  GridRec nxt;
-  GridRecD nxtd;
-  if (lo + sl < hi) {
-    nxt = rec[lo + sl];
-    if constexpr (Plain) nxtd = recd[lo + sl];
-  }
-  for (int64_t base = lo; base < hi; base += kBatch) {
-    __syncwarp();
-    if (lane < kBatch) {
-      buf[lane] = nxt;
-      if constexpr (Plain) S.wrecd[warp][lane] = nxtd;
+  if constexpr (Plain) {
+    const int sl = lane & (kBatch - 1);
+    GridRec* buf = S.wrec[warp];
+    GridRec nxt;
+    GridRecD nxtd;
+    if (lo + sl < hi) {
+      nxt = rec[lo + sl];
+      nxtd = recd[lo + sl];
     }
-    __syncwarp();
-    const int cnt = (int)(hi - base < kBatch ? hi - base : kBatch);
-    if (base + kBatch + sl < hi) {
-      nxt = rec[base + kBatch + sl];
-      if constexpr (Plain) nxtd = recd[base + kBatch + sl];
-    }
-    if (!active) continue;
-    if constexpr (Plain) {
+    for (int64_t base = lo; base < hi; base += kBatch) {
+      __syncwarp();
+      if (lane < kBatch) {
+        buf[lane] = nxt;
+        S.wrecd[warp][lane] = nxtd;
+      }
+      __syncwarp();
+      const int cnt = (int)(hi - base < kBatch ? hi - base : kBatch);
+      if (base + kBatch + sl < hi) {
+        nxt = rec[base + kBatch + sl];
+        nxtd = recd[base + kBatch + sl];
+      }
+      if (!active) continue;
       for (int k = 0; k < cnt; ++k) {
         const GridRec r = buf[k];
         if (g < r.g_lo || g > r.g_hi || r.q > qmax) continue;
@@ -408,29 +415,44 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
           acc.add(d.a0 * S.t3[iz - 1]);
         }
       }
-    } else {
-      // four FP32 partial sums per batch, one Kahan step per batch
+    }
+  } else {
+    const int half = lane >> 4, hl = lane & 15;
+    GridRec* hb = S.wrec[warp] + half * kHalfBatch;
+    // a half warp without an active lane sums nothing
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    const int n = ((act >> (16 * half)) & 0xFFFFu) ? (int)(hi - lo) : 0;
+    const int nmax = max(n, __shfl_xor_sync(0xffffffffu, n, 16));  // the warp's batch loop
+    GridRec nxt = {};
+    if (hl < kHalfBatch && hl < n) nxt = rec[lo + hl];
+    for (int b = 0; b < nmax; b += kHalfBatch) {
+      __syncwarp();
+      if (hl < kHalfBatch) hb[hl] = nxt;
+      __syncwarp();
+      const int cnt = min(n - b, kHalfBatch);
+      if (hl < kHalfBatch && b + kHalfBatch + hl < n) nxt = rec[lo + b + kHalfBatch + hl];
+      if (!active || cnt <= 0) continue;
       unsigned fix = 0;
       float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-      if (cnt == kBatch) {
+      if (cnt == kHalfBatch) {
 #pragma unroll
-        for (int k = 0; k < kBatch; k += 4) {
-          s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
-          s1 += term_fast<GRID>(S, buf[k + 1], g, qmax, &fix, 2u << k);
-          s2 += term_fast<GRID>(S, buf[k + 2], g, qmax, &fix, 4u << k);
-          s3 += term_fast<GRID>(S, buf[k + 3], g, qmax, &fix, 8u << k);
+        for (int k = 0; k < kHalfBatch; k += 4) {
+          s0 += term_fast<GRID>(S, hb[k], g, qmax, &fix, 1u << k);
+          s1 += term_fast<GRID>(S, hb[k + 1], g, qmax, &fix, 2u << k);
+          s2 += term_fast<GRID>(S, hb[k + 2], g, qmax, &fix, 4u << k);
+          s3 += term_fast<GRID>(S, hb[k + 3], g, qmax, &fix, 8u << k);
         }
       } else {
         // a partial batch in groups of four; entries past cnt are masked
         for (int k = 0; k < cnt; k += 4) {
-          s0 += term_fast<GRID>(S, buf[k], g, qmax, &fix, 1u << k);
-          s1 += term_fast<GRID>(S, buf[k + 1], g, qmax, &fix, 2u << k, k + 1 < cnt);
-          s2 += term_fast<GRID>(S, buf[k + 2], g, qmax, &fix, 4u << k, k + 2 < cnt);
-          s3 += term_fast<GRID>(S, buf[k + 3], g, qmax, &fix, 8u << k, k + 3 < cnt);
+          s0 += term_fast<GRID>(S, hb[k], g, qmax, &fix, 1u << k);
+          s1 += term_fast<GRID>(S, hb[k + 1], g, qmax, &fix, 2u << k, k + 1 < cnt);
+          s2 += term_fast<GRID>(S, hb[k + 2], g, qmax, &fix, 4u << k, k + 2 < cnt);
+          s3 += term_fast<GRID>(S, hb[k + 3], g, qmax, &fix, 8u << k, k + 3 < cnt);
         }
       }
       float bsum = (s0 + s1) + (s2 + s3);
-      if (fix) bsum += fix_terms<GRID>(S, buf, base, reclo, a, g, fix);
+      if (fix) bsum += fix_terms<GRID>(S, hb, lo + b, reclo, a, g, fix);
       acc.add(bsum);
     }
   }
@@ -499,9 +521,9 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
   // ---- record range of every 32-point tile of the three grids ----
   const int nT1 = (NHI - kNSHIFT + 31) / 32;
   const int G01 = kPanelPts * p + kNSHIFT, G02 = kPanelR2 * p - 1, G03 = kPanelR3 * p - 1;
-  for (int t = tid; t < kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
-  for (int t = tid; t < kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
-  for (int t = tid; t < kTiles3; t += blockDim.x) S.lo3[t] = S.hi3[t] = (int)rg[5];
+  for (int t = tid; t < 2 * kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
+  for (int t = tid; t < 2 * kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
+  for (int t = tid; t < 2 * kTiles3; t += blockDim.x) S.lo3[t] = S.hi3[t] = (int)rg[5];
   if (tid == 0) {  // XINT set-up of the panel (once, in FP64)
     XintPanel& X = S.X;
     const double DVR3 = 16. * dv;
@@ -543,9 +565,9 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
     const double* AB = a.absrb_all + P.abs_off;  // 1-based
     for (int i = tid; i < S.X.nab; i += blockDim.x) S.absf[i] = (float)AB[S.X.ab0 + i];
   }
-  if (nT1 > 0) tile_ranges(pm1, sm1, rg[0], rg[1], G01, nT1, S.lo1, S.hi1);
-  tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, kTiles2, S.lo2, S.hi2);
-  tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, kTiles3, S.lo3, S.hi3);
+  if (nT1 > 0) tile_ranges(pm1, sm1, rg[0], rg[1], G01, 2 * nT1, S.lo1, S.hi1);
+  tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, 2 * kTiles2, S.lo2, S.hi2);
+  tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, 2 * kTiles3, S.lo3, S.hi3);
   __syncthreads();
   if constexpr (!Plain) {  // the tables have landed (bounded wait; the error flag otherwise)
     const bool ok = mbar_wait_bounded(&S.tab_bar, 0);
@@ -638,7 +660,9 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
     const int qmax = old ? p - 1 : p;
     const int g = kPanelR3 * p + J3 - 1;
     const int t = old ? 0 : u;
-    const int64_t lo = S.lo3[t], hi = max(S.lo3[t], S.hi3[t]);
+    // the FP64 path: the 32-point tile's range; mixed: the lane's half tile's
+    const int h0 = 2 * t + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * t + 1 : h0;
+    const int64_t lo = S.lo3[h0], hi = max(S.lo3[h0], S.hi3[h1]);
     Acc acc;
     gather_grid<Plain, 3>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
     if (active) {
@@ -721,7 +745,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
       bool active = J >= 5 && J < kR2Pts;
       int g = kPanelR2 * p + J - 1;
       Acc acc;
-      gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[tile], max(S.lo2[tile], S.hi2[tile]), g, active, p, acc);
+      const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
+      gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[h0], max(S.lo2[h0], S.hi2[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 1) & 3;
         int Jg = J - off;
@@ -759,7 +784,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
       bool active = J <= NHI;
       int g = kPanelPts * p + J - 1;
       Acc acc;
-      gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[tile], max(S.lo1[tile], S.hi1[tile]), g, active, p, acc);
+      const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
+      gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[h0], max(S.lo1[h0], S.hi1[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 33) & 3;
         int Jg = J - off;
