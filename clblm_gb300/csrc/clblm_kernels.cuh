@@ -100,10 +100,16 @@ __global__ void k_f4_compact(const F4Prep* prep, int64_t stride, const LayerPlan
                              int64_t* src, unsigned char* flags, int64_t* cut);
 __global__ void k_f4_next(const long long* vbits, const long long* lbits, const int64_t* ntot, int64_t stride,
                           int* gnxt);
-__global__ void k_f4_walk(const LayerPlan* plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
-                          const int64_t* cidx, const long long* vbits, const long long* lbits, const int* gnxt,
-                          const unsigned char* flags, const int64_t* ntot, const int64_t* cut, int4* groups,
-                          int64_t* ngroups);
+// PF: lines per thread of the next SHRINQ call loaded ahead (5: all; for a
+// batch of at most one CTA per SM, where each layer's walk is latency-bound)
+// (declared with the definition's __restrict__ qualifiers: a template's
+// declaration and definition must agree for the launch to find the kernel)
+template <int PF>
+__global__ void k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total,
+                          int64_t stride, const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
+                          const long long* __restrict__ lbits, const int* __restrict__ gnxt,
+                          const unsigned char* __restrict__ flags, const int64_t* __restrict__ ntot,
+                          const int64_t* __restrict__ cut, int4* __restrict__ groups, int64_t* __restrict__ ngroups);
 __global__ void k_f4_groupsum(const LayerPlan* plans, int layer0, const F4Prep* prep, int64_t stride,
                               const int64_t* src, const int4* groups, const int64_t* ngroups, ShrunkLine* out);
 struct F4Rec;

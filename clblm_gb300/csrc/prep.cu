@@ -935,12 +935,14 @@ __device__ __forceinline__ T block_scan_excl(T v, T* warp_tot, T* out_excl) {
   return total;
 }
 
+template <int kWalkPf>
 __global__ void __launch_bounds__(kWalkThreads)
     k_f4_walk(const LayerPlan* __restrict__ plans, int layer0, int nlayers, int64_t nlines_total, int64_t stride,
               const int64_t* __restrict__ cidx, const long long* __restrict__ vbits,
               const long long* __restrict__ lbits, const int* __restrict__ gnxt,
               const unsigned char* __restrict__ flags, const int64_t* __restrict__ ntot,
               const int64_t* __restrict__ cut, int4* __restrict__ groups, int64_t* __restrict__ ngroups) {
+  // (a template: declared with the same qualifiers in clblm_kernels.cuh)
   __shared__ short up[kLift][kWalkMax];     // up[k][b]: nxt applied 2^k times
   __shared__ short ends[kWalkMax];          // group ends of the call, in order
   __shared__ short pc1[kWalkMax + 1], pc2[kWalkMax + 1];  // flag counts before each line
@@ -974,6 +976,11 @@ __global__ void __launch_bounds__(kWalkThreads)
   int64_t ng = 0, slot = 0;
   int status = 0;
   bool IEOF = false;
+  // prefetched map, flags and first-group test operands of the call at pf_base
+  int pf_gn[kWalkPf];
+  unsigned char pf_f[kWalkPf];
+  long long pf_v1 = 0, pf_lm = 0;
+  int64_t pf_base = -1;
   for (;;) {  // every thread runs the (uniform) record loop
     if (rec >= nrec_total) {
       IEOF = true;
@@ -1013,14 +1020,37 @@ __global__ void __launch_bounds__(kWalkThreads)
     }
     int64_t nemit = 0;
     if (m > 0) {
-      for (int i = tid; i < m; i += kWalkThreads) {
-        const int64_t e = GN[u0 + i];
-        up[0][i] = (short)((e < u1 - 1 ? e : u1 - 1) - u0);
-        sf[i] = F[u0 + i];
+      // this call's next-group map and flags: from the registers the previous
+      // call filled when it started here, else from memory
+      const bool have = (pf_base == u0);
+#pragma unroll
+      for (int k = 0; k < kWalkPer; ++k) {
+        const int i = tid + k * kWalkThreads;
+        if (i < m) {
+          const bool pf = have && k < kWalkPf;
+          const int64_t e = pf ? (int64_t)pf_gn[k < kWalkPf ? k : 0] : (int64_t)GN[u0 + i];
+          up[0][i] = (short)((e < u1 - 1 ? e : u1 - 1) - u0);
+          sf[i] = pf ? pf_f[k < kWalkPf ? k : 0] : F[u0 + i];
+        }
       }
       if (tid == 0) {
         // the first group: VLMT = VNU(first) + DVR4/2
-        sh_e0 = (m == 1 || V[u0 + 1] > Lm[u0]) ? 0 : -1;
+        const bool split = m == 1 || (have ? pf_v1 > pf_lm : V[u0 + 1] > Lm[u0]);
+        sh_e0 = split ? 0 : -1;
+      }
+      // the next call starts at u1: its loads overlap this call's work
+      pf_base = u1;
+#pragma unroll
+      for (int k = 0; k < kWalkPf; ++k) {
+        const int64_t i = u1 + tid + k * kWalkThreads;
+        if (i < total) {
+          pf_gn[k] = GN[i];
+          pf_f[k] = F[i];
+        }
+      }
+      if (tid == 0) {
+        pf_v1 = u1 + 1 < total ? V[u1 + 1] : 0;
+        pf_lm = u1 < total ? Lm[u1] : 0;
       }
       __syncthreads();
       if (tid == 0 && sh_e0 < 0) sh_e0 = up[0][0];
@@ -1129,6 +1159,15 @@ __global__ void __launch_bounds__(kWalkThreads)
     ngroups[2 * (layer + layer0) + 1] = slot;
   }
 }
+
+#define CLBLM_WALK_ARGS                                                                                       \
+  const LayerPlan* __restrict__, int, int, int64_t, int64_t, const int64_t* __restrict__,                     \
+      const long long* __restrict__, const long long* __restrict__, const int* __restrict__,                  \
+      const unsigned char* __restrict__, const int64_t* __restrict__, const int64_t* __restrict__,            \
+      int4* __restrict__, int64_t* __restrict__
+template __global__ void k_f4_walk<2>(CLBLM_WALK_ARGS);
+template __global__ void k_f4_walk<kWalkPer>(CLBLM_WALK_ARGS);
+#undef CLBLM_WALK_ARGS
 
 // Sums of each group in the reference's order (SHRINQ :1563-1637): non-CO2
 // members into one pseudo-line, CO2 members into another, written to the

@@ -117,6 +117,7 @@ struct clblm_handle {
   std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
   uint64_t bgraph_clock = 0;
   bool panel_attr_set[2] = {false, false};
+  int nsm = 1;  // SMs of the device
   // every device buffer of the handle but the line list
   std::vector<DevBuf*> buffers() {
     std::vector<DevBuf*> v = {&cont_self, &cont_for, &cont_texp, &cont_co2, &tabs,    &plans,   &vft,    &prep,    &qpanel,
@@ -907,10 +908,18 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     k_f4_next<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), 256, 0, st>>>(
         h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4ntot.as<int64_t>(), f4stride, h->f4nxt.as<int>());
     h->launches++;
-    k_f4_walk<<<count, 256, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
-                                    h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4nxt.as<int>(),
-                                    h->f4flag.as<unsigned char>(), h->f4ntot.as<int64_t>(), h->f4cut.as<int64_t>(),
-                                    h->f4grp.as<int4>(), h->f4nout.as<int64_t>());
+    // one CTA per layer: with at most one per SM each walk is latency-bound and
+    // loads the whole next call ahead; with more, occupancy counts and it loads two lines per thread
+    if (count <= h->nsm)
+      k_f4_walk<5><<<count, 256, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
+                                         h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4nxt.as<int>(),
+                                         h->f4flag.as<unsigned char>(), h->f4ntot.as<int64_t>(),
+                                         h->f4cut.as<int64_t>(), h->f4grp.as<int4>(), h->f4nout.as<int64_t>());
+    else
+      k_f4_walk<2><<<count, 256, 0, st>>>(dplans, first, count, h->nlines, f4stride, h->f4cidx.as<int64_t>(),
+                                         h->f4vb.as<long long>(), h->f4lb.as<long long>(), h->f4nxt.as<int>(),
+                                         h->f4flag.as<unsigned char>(), h->f4ntot.as<int64_t>(),
+                                         h->f4cut.as<int64_t>(), h->f4grp.as<int4>(), h->f4nout.as<int64_t>());
     h->launches++;
     k_f4_groupsum<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), 256, 0, st>>>(
         dplans, first, h->f4prep.as<F4Prep>(), f4stride, h->f4src.as<int64_t>(), h->f4grp.as<int4>(),
@@ -1367,7 +1376,8 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
     delete h;
     return rc;
   }
-  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     g_create_err = "cannot use CUDA device";
     delete h;
     return CLBLM_ERR_CUDA;
