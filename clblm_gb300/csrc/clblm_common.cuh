@@ -72,6 +72,7 @@ struct LayerPlan {
   int jac_mol;                    // icflg: molecule whose continuum derivative term is added
   double v1abs, v2abs, dvabs, xself, xfrgn, wk1, h2o_fac;
   double xco2c;                   // XCO2C: scale of the CO2 continuum (0: none)
+  double xn2cn;                   // XN2CN: scale of the N2 continua (0: none)
   int nptabs;
   // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
   int sel[kTIPSNMOL + 1];
@@ -138,7 +139,7 @@ struct __align__(16) GridRec {
   float zfl, zs;    // ZFkL and ZSLOPE (FP32 copies for the mixed path)
   float a0, a1, a2; // strengths: R1 -> STRFA1, STRDA, STRVRA; R2/R3 -> STRFA2/3
 };
-// exact FP64 copies for the plain path and the mixed path's index fix-up
+// exact FP64 copies (the FP64 path)
 struct GridRecD {
   double zfl, zs, a0, a1, a2;
 };

@@ -33,6 +33,11 @@ struct ContIn {
   const double* co2_s;
   const double* co2_tdep;
   const double* co2_xfac;
+  // N2 continua: xn2_r's C_296, SF_296, C_220, SF_220 (4 x 73), n2_ver_1's
+  // xn2_272, xn2_228, a_h2o (3 x 230), n2_overtone1's xn2 (201)
+  const double* n2r;
+  const double* n2f;
+  const double* n2o1;
 };
 
 // LINF4Q-corrected line (before SHRINQ)

@@ -21,6 +21,11 @@ Tables extracted (reference file:line):
     10000 cm-1 at 2 cm-1 and its band-head temperature exponents
     TDEP_BANDHEAD(1196:1220), src/clblm_src/clblm_ODLAY_Continuum.f90:1333-2511;
     CONTNM's XFACCO2(500) scaling for 2000-2998 cm-1, :145-204
+  * N2 continua: the pure-rotation band's C and SF at 296 K and 220 K
+    (xn2_r, 73 points on -10..350 cm-1), the fundamental's coefficients at
+    272 K and 228 K and the H2O efficiencies (n2_ver_1, 230 points from
+    1993.8 cm-1), the first overtone's coefficients (n2_overtone1, 201
+    points from 4325 cm-1)
 
 Run (in a tree where the reference is mounted):
     python clblm_gb300/csrc/gen_ref_tables.py /root/reference > clblm_gb300/csrc/clblm_ref_tables.h
@@ -147,6 +152,14 @@ def main(ref_root):
     emit("CLBLM_CO2_TDEP", _data_block(cont, r"SUBROUTINE\s+FRNCO2",
                                        r"data\s*\(tdep_bandhead\(i\),i=1196,1220\)\s*/(.*?)/", 25))
     emit("CLBLM_XFACCO2", _data_block(cont, r"SUBROUTINE\s+CONTNM", r"DATA\s+XFACCO2\s*/(.*?)/", 500), per=8)
+    # N2 continua: xn2_r (:2533-2681), n2_ver_1 (:2696-2945), n2_overtone1 (:2948-3056)
+    for name, pat in (("C_296", r"DATA\s+C_296\(1:73\)\s*/(.*?)/"), ("SF_296", r"DATA\s+sf_296\s*/(.*?)/"),
+                      ("C_220", r"DATA\s+C_220\(1:73\)\s*/(.*?)/"), ("SF_220", r"DATA\s+sf_220\s*/(.*?)/")):
+        emit("CLBLM_N2R_" + name, _data_block(cont, r"SUBROUTINE\s+xn2_r", pat, 73))
+    for name in ("xn2_272", "xn2_228", "a_h2o"):
+        emit("CLBLM_N2F_" + name.upper(),
+             _data_block(cont, r"subroutine\s+n2_ver_1", r"DATA\s+%s\s*/(.*?)/" % name, 230))
+    emit("CLBLM_N2O1_XN2", _data_block(cont, r"subroutine\s+n2_overtone1", r"DATA\s+xn2\s*/(.*?)/", 201))
     lines.append("#endif")
     sys.stdout.write("\n".join(lines) + "\n")
 

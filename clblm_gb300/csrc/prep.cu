@@ -668,6 +668,143 @@ __device__ double co2_continuum(const LayerPlan& P, const ContIn& cont, int I, b
   return CONTI * 1.0;
 }
 
+// The grid of a continuum table routine on V1S + (i-1)*DVS, i = 1..NPTS, over
+// [V1ABS - DVS, V2ABS + DVS] (the set-up FRNCO2, xn2_r, n2_ver_1 and
+// n2_overtone1 share, clblm_ODLAY_Continuum.f90:2566-2580).
+struct ContGrid {
+  double v1c, v2c, dvc;
+  int nptc, i1;
+};
+__device__ __forceinline__ ContGrid cont_grid(const LayerPlan& P, double V1S, double DVS, int NPTS) {
+  ContGrid g;
+  g.dvc = DVS;
+  double V1C = P.v1abs - DVS, V2C = P.v2abs + DVS;
+  g.i1 = (V1C < V1S) ? -1 : (int)((V1C - V1S) / DVS + 0.01);
+  V1C = V1S + DVS * (double)(g.i1 - 1);
+  const int I2 = (int)((V2C - V1S) / DVS + 0.01);
+  g.nptc = I2 - g.i1 + 3;
+  if (g.nptc > NPTS) g.nptc = NPTS + 4;
+  g.v1c = V1C;
+  g.v2c = V1C + DVS * (double)(g.nptc - 1);
+  return g;
+}
+
+// What XINT(V1C, V2C, DVC, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS) adds at
+// ABSRB point I (clblm_Spectrum.f90:874-915); *hit when I is in its range.
+// coef(J) gives C(J), J = 1..NPTC, and 0 outside (XINT's last stencil can
+// reach C(NPTC+1) with a zero weight).
+template <typename F>
+__device__ __forceinline__ double xint_at(const LayerPlan& P, int I, const ContGrid& g, F coef, bool* hit) {
+  *hit = false;
+  const double RECDVA = 1. / g.dvc;
+  int ILO = (int)((g.v1c + g.dvc - P.v1abs) / P.dvabs + 1. + kONEMI);
+  if (ILO < 1) ILO = 1;
+  int IHI = (int)((g.v2c - g.dvc - P.v1abs) / P.dvabs + kONEMI);
+  if (IHI > P.nptabs) IHI = P.nptabs;
+  if (I < ILO || I > IHI) return 0.;
+  *hit = true;
+  const double VI = P.v1abs + P.dvabs * (double)(I - 1);
+  const int J = (int)((VI - g.v1c) * RECDVA + kONEPL);
+  const double VJ = g.v1c + g.dvc * (double)(J - 1);
+  const double Pp = RECDVA * (VI - VJ);
+  const double C = (3. - 2. * Pp) * Pp * Pp;
+  const double B = 0.5 * Pp * (1. - Pp);
+  const double B1 = B * (1. - Pp);
+  const double B2 = B * Pp;
+  const double CONTI = -coef(J - 1) * B1 + coef(J) * (1. - C + B2) + coef(J + 1) * (C + B1) - coef(J + 2) * B2;
+  return CONTI * 1.0;
+}
+
+// The N2 collision-induced continua of CONTNM (clblm_ODLAY_Continuum.f90:
+// 805-990) at ABSRB point I, added in the reference's order after the CO2
+// block: pure rotation (xn2_r :2533-2681), fundamental (n2_ver_1 :2696-2945),
+// first overtone (n2_overtone1 :2948-3056).  Amounts as CONTNM's prologue
+// (:287-300): x_vmr_h2o = W(H2O)/Wtot, x_vmr_o2 = W(O2)/Wtot, x_vmr_n2 the
+// rest, Wn2 = x_vmr_n2 Wtot (0 for the molecule-derivative OD).
+__device__ double n2_continuum(const LayerPlan& P, const ContIn& cont, int I, double ab) {
+  if (!(P.xn2cn > 0.) || !cont.n2r) return ab;
+  const double P0 = 1013., XLOSMT = 2.68675E+19;
+  const double XKT = P.tave / kRADCN2;
+  const double amagat = (P.pave / P0) * (273. / P.tave);
+  const double x_vmr_h2o = P.wk[1] / P.wtot, x_vmr_o2 = P.wk[7] / P.wtot;
+  const double x_vmr_n2 = 1. - x_vmr_h2o - x_vmr_o2;
+  const double Wn2 = P.jac_mol > 0 ? 0. : x_vmr_n2 * P.wtot;
+  bool hit;
+  if ((P.v2 > -10.0) && (P.v1 < 350.)) {  // pure rotation
+    const ContGrid g = cont_grid(P, -10., 5.0, 73);
+    const double xo2 = 0.21, xn2 = 0.79, a_h2o = 1.;
+    const double tfac = (P.tave - 296.) / (220. - 296.);
+    const double tau_fac = P.xn2cn * (Wn2 / XLOSMT) * amagat;
+    const double* C296 = cont.n2r;
+    const double *SF296 = C296 + 73, *C220 = C296 + 146, *SF220 = C296 + 219;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      double c0 = 0., c1 = 0.;
+      if (Ii >= 1 && Ii <= 73) {
+        c0 = C296[Ii - 1] * pow(C220[Ii - 1] / C296[Ii - 1], tfac);
+        const double sf_T = SF296[Ii - 1] * pow(SF220[Ii - 1] / SF296[Ii - 1], tfac);
+        c1 = (sf_T - 1.) * (xn2) / (xo2);
+      }
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      double v = tau_fac * c0 * (x_vmr_n2 + c1 * x_vmr_o2 + a_h2o * x_vmr_h2o);
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if ((P.v2 > 2001.77) && (P.v1 < 2897.59)) {  // fundamental
+    const ContGrid g = cont_grid(P, 1993.803434, 3.981461525, 230);
+    const double T = P.tave;
+    const double xtfac = ((1. / T) - (1. / 272.)) / ((1. / 228.) - (1. / 272.));
+    const double xt_lin = (T - 272.) / (228. - 272.);
+    const double a_o2 = 1.294 - 0.4545 * T / 296.;
+    const double tau_fac = P.xn2cn * (Wn2 / XLOSMT) * amagat;
+    const double* X272 = cont.n2f;
+    const double *X228 = X272 + 230, *AH2O = X272 + 460;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      double cn0 = 0., cn1 = 0., cn2 = 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      if (Ii >= 1 && Ii <= 230) {
+        const double x272 = X272[Ii - 1], x228 = X228[Ii - 1];
+        double c;
+        if ((x272 > 0.) && (x228 > 0.)) c = x272 * pow(x228 / x272, xtfac);
+        else c = x272 + (x228 - x272) * xt_lin;
+        c = c / VJ;
+        cn0 = c;
+        cn1 = a_o2 * c;
+        cn2 = (9. / 7.) * AH2O[Ii - 1] * c;
+      }
+      double v = tau_fac * (x_vmr_n2 * cn0 + x_vmr_o2 * cn1 + x_vmr_h2o * cn2);
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if ((P.v2 > 4340.0) && (P.v1 < 4910.)) {  // first overtone
+    const ContGrid g = cont_grid(P, 4325.0, 3.0, 201);
+    const double a_o2 = 1., a_h2o = 1.;
+    const double tau_fac = P.xn2cn * (Wn2 / XLOSMT) * amagat * (x_vmr_n2 + a_o2 * x_vmr_o2 + a_h2o * x_vmr_h2o);
+    const double* XN = cont.n2o1;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 201) ? XN[Ii - 1] / VJ : 0.;
+      double v = tau_fac * c0;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  return ab;
+}
+
 __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, ContIn cont, double* __restrict__ absrb_all) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
   double* ABSRB = absrb_all + P.abs_off;  // ABSRB[I], I = 1..N_ABSRB
@@ -678,11 +815,13 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
   if (I > kNABSRB) return;
   if (!P.contnm) return;
   if (I > (int)((P.v2abs - P.v1abs) / P.dvabs + 1)) return;  // beyond NPTABS: nothing to add
-  // the H2O block adds to ABSRB first, then the CO2 block (XINT)
+  // the H2O block adds to ABSRB first, then the CO2 block, then the N2
+  // blocks (XINT each)
   double ab = h2o_continuum(P, cont, I);
   bool hit;
   const double co2 = co2_continuum(P, cont, I, &hit);
   if (hit) ab = ab + co2;
+  ab = n2_continuum(P, cont, I, ab);
   ABSRB[I] = ab;
 }
 

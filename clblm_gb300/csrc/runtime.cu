@@ -678,6 +678,7 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
     P.wk1 = P.wk[1];
     P.h2o_fac = P.wk[1] / lay->wtot;
     P.xco2c = c->xco2c;
+    P.xn2cn = c->xn2cn;
   }
   // returned spectrum: DVout interpolation, clblm_ODLAY.f90:571-604
   double outputDV = DV;
@@ -1425,17 +1426,35 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
         h->cont.self_texp = h->cont_texp.as<double>();
         h->cont.ref_press = cont->ref_press;
         h->cont.ref_temp = cont->ref_temp;
-        // the CO2 continuum's tables (data of the reference's source)
-        if (h->cont_co2.ensure(sizeof(double) * (5003 + 25 + 500))) {
+        // the CO2 and N2 continua's tables (data of the reference's source)
+        const size_t n_co2 = 5003 + 25 + 500, n_n2 = 4 * 73 + 3 * 230 + 201;
+        if (h->cont_co2.ensure(sizeof(double) * (n_co2 + n_n2))) {
           rc = CLBLM_ERR_OOM;
         } else {
+          std::vector<double> t;
+          t.reserve(n_co2 + n_n2);
+          auto add = [&t](const double* a, size_t n) { t.insert(t.end(), a, a + n); };
+          add(CLBLM_CO2_S, 5003);
+          add(CLBLM_CO2_TDEP, 25);
+          add(CLBLM_XFACCO2, 500);
+          add(CLBLM_N2R_C_296, 73);
+          add(CLBLM_N2R_SF_296, 73);
+          add(CLBLM_N2R_C_220, 73);
+          add(CLBLM_N2R_SF_220, 73);
+          add(CLBLM_N2F_XN2_272, 230);
+          add(CLBLM_N2F_XN2_228, 230);
+          add(CLBLM_N2F_A_H2O, 230);
+          add(CLBLM_N2O1_XN2, 201);
           double* d = h->cont_co2.as<double>();
-          cudaMemcpy(d, CLBLM_CO2_S, sizeof(double) * 5003, cudaMemcpyHostToDevice);
-          cudaMemcpy(d + 5003, CLBLM_CO2_TDEP, sizeof(double) * 25, cudaMemcpyHostToDevice);
-          cudaMemcpy(d + 5028, CLBLM_XFACCO2, sizeof(double) * 500, cudaMemcpyHostToDevice);
+          if (cudaMemcpy(d, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = set_err(h, CLBLM_ERR_CUDA, "continuum tables");
+          }
           h->cont.co2_s = d;
           h->cont.co2_tdep = d + 5003;
           h->cont.co2_xfac = d + 5028;
+          h->cont.n2r = d + n_co2;
+          h->cont.n2f = d + n_co2 + 4 * 73;
+          h->cont.n2o1 = d + n_co2 + 4 * 73 + 3 * 230;
         }
         h->has_cont = true;
       }

@@ -131,6 +131,10 @@ typedef struct {
   double  xco2c;       /* XCO2C, scale of the CO2 continuum (mt_ckd 2.5, CONTNM
                         * clblm_ODLAY_Continuum.f90:408-451); the reference's
                         * default is 1, 0 leaves it out                        */
+  double  xn2cn;       /* XN2CN, scale of the N2 collision-induced continua
+                        * (pure rotation, fundamental, first overtone: CONTNM
+                        * clblm_ODLAY_Continuum.f90:805-990); the reference's
+                        * default is 1, 0 leaves them out                      */
 } clblm_od_ctrl_t;
 
 /* A layered column seen in nadir from the top of the atmosphere, with the

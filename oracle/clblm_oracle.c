@@ -584,6 +584,121 @@ static void contnm_co2(int JRAD, double V1ABS, double V2ABS, double DVABS, int N
 }
 
 /* ======================================================================
+ * N2 collision-induced continua: the nitrogen blocks of CONTNM
+ * (clblm_ODLAY_Continuum.f90:805-990) with xn2_r (:2533-2681), n2_ver_1
+ * (:2696-2945) and n2_overtone1 (:2948-3056), each on its own coarse grid,
+ * XINT'd onto ABSRB in that order after the CO2 block.  The amounts follow
+ * CONTNM's prologue (:287-300): x_vmr_h2o = W(H2O)/Wtot, x_vmr_o2 =
+ * W(O2)/Wtot, x_vmr_n2 = 1 - both, Wn2 = x_vmr_n2*Wtot (0 for the molecule
+ * derivative OD, icflg > 0), amagat = (P/1013)(273/T).
+ * ====================================================================== */
+/* the coarse grid of a table routine on V1S + (i-1)*DVS, i = 1..NPTS
+ * (the grid set-up xn2_r, n2_ver_1 and n2_overtone1 share with FRNCO2) */
+static void cont_table_grid(double V1S, double DVS, int NPTS, double V1ABS, double V2ABS, double *V1C, double *V2C,
+                            int *NPTC, int *I1) {
+  const double DVC = DVS;
+  double v1c = V1ABS - DVC, v2c = V2ABS + DVC;
+  int i1 = (v1c < V1S) ? -1 : (int)((v1c - V1S) / DVS + 0.01);
+  v1c = V1S + DVS * (double)(i1 - 1);
+  int i2 = (int)((v2c - V1S) / DVS + 0.01);
+  int nptc = i2 - i1 + 3;
+  if (nptc > NPTS) nptc = NPTS + 4;
+  v2c = v1c + DVS * (double)(nptc - 1);
+  *V1C = v1c;
+  *V2C = v2c;
+  *NPTC = nptc;
+  *I1 = i1;
+}
+
+static void contnm_n2(int JRAD, double V1ABS, double V2ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/,
+                      double XN2CN, double V1, double V2, double PAVE, double TAVE, double WTOT, double WKH2O,
+                      double WKO2, int icflg) {
+  if (!(XN2CN > 0.)) return;
+  const double P0 = 1013., XLOSMT = 2.68675E+19;
+  const double XKT = TAVE / RADCN2;
+  const double amagat = (PAVE / P0) * (273. / TAVE);
+  const double x_vmr_h2o = WKH2O / WTOT, x_vmr_o2 = WKO2 / WTOT;
+  const double x_vmr_n2 = 1. - x_vmr_h2o - x_vmr_o2;
+  const double Wn2 = icflg > 0 ? 0. : x_vmr_n2 * WTOT;
+  double V1C, V2C;
+  int NPTC, I1;
+  /* pure rotation band, -10 .. 350 cm-1 (xn2_r: C and SF at 296 K and 220 K) */
+  if ((V2 > -10.0) && (V1 < 350.)) {
+    const double V1S = -10., DVS = 5.0;
+    const int NPTS = 73;
+    const double xo2 = 0.21, xn2 = 0.79, a_h2o = 1.;
+    const double tfac = (TAVE - 296.) / (220. - 296.);
+    const double tau_fac = XN2CN * (Wn2 / XLOSMT) * amagat;
+    cont_table_grid(V1S, DVS, NPTS, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      double c0 = 0., c1 = 0.;
+      if (I >= 1 && I <= NPTS) {
+        c0 = CLBLM_N2R_C_296[I - 1] * pow(CLBLM_N2R_C_220[I - 1] / CLBLM_N2R_C_296[I - 1], tfac);
+        const double sf_T = CLBLM_N2R_SF_296[I - 1] * pow(CLBLM_N2R_SF_220[I - 1] / CLBLM_N2R_SF_296[I - 1], tfac);
+        c1 = (sf_T - 1.) * (xn2) / (xo2);
+      }
+      const double VJ = V1C + DVS * (double)(J - 1);
+      C[J] = tau_fac * c0 * (x_vmr_n2 + c1 * x_vmr_o2 + a_h2o * x_vmr_h2o);
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, DVS, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  /* fundamental, 2001.77 .. 2897.59 cm-1 (n2_ver_1: 272 K and 228 K, O2 and H2O partners) */
+  if ((V2 > 2001.77) && (V1 < 2897.59)) {
+    const double V1S = 1993.803434, DVS = 3.981461525;
+    const int NPTS = 230;
+    const double T = TAVE;
+    const double xtfac = ((1. / T) - (1. / 272.)) / ((1. / 228.) - (1. / 272.));
+    const double xt_lin = (T - 272.) / (228. - 272.);
+    const double a_o2 = 1.294 - 0.4545 * T / 296.;
+    const double tau_fac = XN2CN * (Wn2 / XLOSMT) * amagat;
+    cont_table_grid(V1S, DVS, NPTS, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      double cn0 = 0., cn1 = 0., cn2 = 0.;
+      const double VJ = V1C + DVS * (double)(J - 1);
+      if (I >= 1 && I <= NPTS) {
+        const double x272 = CLBLM_N2F_XN2_272[I - 1], x228 = CLBLM_N2F_XN2_228[I - 1];
+        double c;
+        if ((x272 > 0.) && (x228 > 0.)) c = x272 * pow(x228 / x272, xtfac);  /* log in 1/T */
+        else c = x272 + (x228 - x272) * xt_lin;                                /* linear */
+        c = c / VJ;  /* the radiation field removed */
+        cn0 = c;
+        cn1 = a_o2 * c;
+        cn2 = (9. / 7.) * CLBLM_N2F_A_H2O[I - 1] * c;
+      }
+      C[J] = tau_fac * (x_vmr_n2 * cn0 + x_vmr_o2 * cn1 + x_vmr_h2o * cn2);
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, DVS, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  /* first overtone, 4340 .. 4910 cm-1 (n2_overtone1, no temperature dependence) */
+  if ((V2 > 4340.0) && (V1 < 4910.)) {
+    const double V1S = 4325.0, DVS = 3.0;
+    const int NPTS = 201;
+    const double a_o2 = 1., a_h2o = 1.;
+    const double tau_fac = XN2CN * (Wn2 / XLOSMT) * amagat * (x_vmr_n2 + a_o2 * x_vmr_o2 + a_h2o * x_vmr_h2o);
+    cont_table_grid(V1S, DVS, NPTS, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      double c0 = 0.;
+      const double VJ = V1C + DVS * (double)(J - 1);
+      if (I >= 1 && I <= NPTS) c0 = CLBLM_N2O1_XN2[I - 1] / VJ;
+      C[J] = tau_fac * c0;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, DVS, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+}
+
+/* ======================================================================
  * Far-wing (function 4) lines: the TAPE9 scratch file as records in memory.
  * LINF4Q clblm_ODLAY_LineF4.f90:647-1266 (RDLNFL :1355-1476),
  * SHRINQ :1516-1647, LBLF4Q :25-182, CNVF4Q :187-494, RDLN4Q :554-640.
@@ -1655,6 +1770,8 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
       return rc;
     }
     contnm_co2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xco2c, V1, V2, PAVE, TAVE, M.WK[2]);
+    contnm_n2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xn2cn, V1, V2, PAVE, TAVE, lay->wtot, M.WK[1],
+              M.WK[7], ctrl->jac_mol);
   }
   double ALFAV4 = 64. * g->sample * DV;
   double DVR4 = ALFAV4 / g->sample;
@@ -2640,4 +2757,10 @@ int ocl_contnm_co2(int jrad, double v1abs, double v2abs, double dvabs, int nptab
   for (int i = 0; i <= nptabs; ++i) absrb[i] = 0.;
   contnm_co2(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xco2c, v1, v2, pave, tave, wkco2);
   return CLBLM_OK;
+}
+
+int ocl_contnm_n2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xn2cn,
+                  double v1, double v2, double pave, double tave, double wtot, double wkh2o, double wko2, int icflg) {
+  contnm_n2(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xn2cn, v1, v2, pave, tave, wtot, wkh2o, wko2, icflg);
+  return 0;
 }

@@ -87,6 +87,10 @@ int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double v1, double v2, double
 /* The CO2 block of CONTNM alone (ABSRB 1-based, [nptabs + 1]) */
 int ocl_contnm_co2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xco2c,
                    double v1, double v2, double pave, double tave, double wkco2);
+/* The N2 blocks of CONTNM alone (ABSRB 1-based, [nptabs + 1]); icflg > 0:
+ * the molecule-derivative OD, where CONTNM sets Wn2 = 0 */
+int ocl_contnm_n2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xn2cn,
+                  double v1, double v2, double pave, double tave, double wtot, double wkh2o, double wko2, int icflg);
 int ocl_interp_spectrum(const double *in, double dvin, double v1in,
                         int64_t nin, double *out, double dvout, double v1out,
                         int64_t nout);

@@ -68,6 +68,8 @@ def lib():
                                     C.c_int64, P(C.c_int64), P(C.c_double), C.c_int]
         L.ocl_contnm_co2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
             [C.c_double] * 6
+        L.ocl_contnm_n2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
+            [C.c_double] * 8 + [C.c_int]
         L.ocl_layer_amounts.argtypes = [C.c_int, C.c_int] + [P(C.c_double)] * 4 + [C.c_double] + [P(C.c_double)] * 5
         L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
@@ -237,6 +239,17 @@ def layer_amounts(z, p, t, den, re=6371.23):
     if rc:
         raise OracleError(rc, "layer amounts")
     return out
+
+
+def contnm_n2(jrad, v1abs, dvabs, nptabs, xn2cn, v1, v2, pave, tave, wtot, wkh2o=0.0, wko2=0.0, icflg=0):
+    """ABSRB(1..nptabs) of the N2 continua alone (1-based array, [0] unused)."""
+    a = np.zeros(nptabs + 8)
+    v2abs = v1abs + dvabs * (nptabs - 1)
+    rc = lib().ocl_contnm_n2(jrad, v1abs, v2abs, dvabs, nptabs, _dp(a), xn2cn, v1, v2, pave, tave, wtot, wkh2o, wko2,
+                             icflg)
+    if rc:
+        raise OracleError(rc, "contnm_n2")
+    return a
 
 
 def contnm_co2(jrad, v1abs, dvabs, nptabs, xco2c, v1, v2, pave, tave, wkco2):

@@ -16,11 +16,11 @@ def _layer_case(n_lines, v1, v2, seed, mols=(1,), pave=1013.25, tave=296.0, wabs
     return lines, col
 
 
-def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision=T.CLBLM_PREC_MIXED):
+def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision=T.CLBLM_PREC_MIXED, xn2cn=1.0):
     dn, df, _ = gpu_lib.setDV(col)
     lay = col.layer(0)
     g = T.grid_struct(col.v1, col.v2, dn[0], df[0])
-    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off)
+    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off, xn2cn=xn2cn)
     h = gpu_lib.Handle(lines, cont)
     od, dv = h.odlay(lay, g, ctrl)
     st = h.stats()
@@ -71,6 +71,28 @@ def test_reference_mtckd_table(gpu_lib, oracle_mod, mtckd, precision, tol, layer
     od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=mtckd, contnm_off=0, precision=precision)
     rel = np.max(np.abs(od - ref) / np.abs(ref))
     assert rel <= tol, rel
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+@pytest.mark.parametrize("window", [(150.0, 250.0), (2050.0, 2150.0)])
+def test_n2_continua(gpu_lib, oracle_mod, precision, tol, window):
+    """The N2 collision-induced continua (pure rotation below 350 cm-1, the
+    fundamental at 2000-2900 cm-1) on a water-rich lower layer of the
+    broadband atmosphere with a sparse line list, against the oracle (there
+    the N2 part reaches 13 % and 2e-5 of the OD); on the FP64 path also the
+    N2 part itself (XN2CN = 1 minus XN2CN = 0) against the oracle's."""
+    lines, col, cont = synth.config4(n_lines=3000)
+    col = col.sub([2]).with_window(*window)
+    od1, ref1 = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0, precision=precision)
+    rel = np.max(np.abs(od1 - ref1) / np.abs(ref1))
+    assert rel <= tol, rel
+    if precision == T.CLBLM_PREC_PLAIN:
+        od0, ref0 = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0, precision=precision,
+                             xn2cn=0.0)
+        dref = ref1 - ref0
+        assert np.max(dref) > 0.0
+        err = np.max(np.abs((od1 - od0) - dref)) / np.max(dref)
+        assert err <= 1e-6, err
 
 
 def test_od_from_tape3_file_is_identical(gpu_lib, tmp_path):

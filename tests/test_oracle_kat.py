@@ -187,6 +187,52 @@ def test_co2_continuum_at_table_nodes():
         assert a[i] == pytest.approx(want, rel=1e-13), v
 
 
+def _ref_table(name, n):
+    from pathlib import Path
+    txt = (Path(__file__).resolve().parents[1] / "clblm_gb300/csrc/clblm_ref_tables.h").read_text()
+    body = txt.split("static const double %s[%d] = {" % (name, n))[1].split("};")[0]
+    return np.array([float(x) for x in body.replace("\n", " ").split(",") if x.strip()])
+
+
+def test_n2_rotation_continuum_at_table_nodes():
+    """At T = 296 K (temperature factor 1) and ABSRB points on xn2_r's 5 cm-1
+    nodes, XINT returns the node value C_296 * XN2CN (Wn2/XLOSMT) amagat
+    (x_n2 + f_o2 x_o2 + x_h2o), f_o2 = (SF_296 - 1) 0.79/0.21
+    (clblm_ODLAY_Continuum.f90:805-860, :2533-2600)."""
+    from oracle import oracle as O
+    C296 = _ref_table("CLBLM_N2R_C_296", 73)
+    SF296 = _ref_table("CLBLM_N2R_SF_296", 73)
+    pave, tave, wtot, wh2o, wo2 = 700.0, 296.0, 1.5e24, 4.0e21, 3.1e23
+    v1abs, dvabs, n = 17.0, 1.0, 330
+    a = O.contnm_n2(0, v1abs, dvabs, n, 1.0, 20.0, 340.0, pave, tave, wtot, wh2o, wo2)
+    xh, xo = wh2o / wtot, wo2 / wtot
+    xn = 1. - xh - xo
+    tau = (xn * wtot / 2.68675e19) * (pave / 1013.) * (273. / tave)
+    for v in (25.0, 50.0, 100.0, 200.0, 300.0, 335.0):
+        i = int(round((v - v1abs) / dvabs)) + 1
+        k = int(round((v + 10.0) / 5.0))              # xn2_r node: V = -10 + 5 (I - 1)
+        fo2 = (SF296[k] - 1.) * 0.79 / 0.21
+        want = tau * C296[k] * (xn + fo2 * xo + xh)
+        assert a[i] == pytest.approx(want, rel=1e-13), v
+
+
+def test_n2_continuum_linear_and_absent_for_derivative_od():
+    """The N2 blocks scale exactly with XN2CN, vanish for the molecule
+    derivative OD (CONTNM sets Wn2 = 0 when icflg > 0) and add nothing
+    outside their bands (rotation < 350, fundamental 2001.77-2897.59 cm-1)."""
+    from oracle import oracle as O
+    args = (700.0, 250.0, 1.5e24, 4.0e21, 0.0)
+    v1abs, dvabs, n = 1997.0, 1.0, 1000
+    a1 = O.contnm_n2(1, v1abs, dvabs, n, 1.0, 2000.0, 2990.0, *args)
+    a2 = O.contnm_n2(1, v1abs, dvabs, n, 2.0, 2000.0, 2990.0, *args)
+    assert np.max(a1) > 0
+    np.testing.assert_array_equal(a2, 2.0 * a1)
+    a0 = O.contnm_n2(1, v1abs, dvabs, n, 1.0, 2000.0, 2990.0, *args, icflg=1)
+    assert not np.any(a0)
+    gap = O.contnm_n2(1, 497.0, 1.0, 1000, 1.0, 500.0, 1490.0, *args)
+    assert not np.any(gap)
+
+
 def oracle_mod_contnm(*args):
     from oracle import oracle as O
     return O.contnm_co2(*args)
