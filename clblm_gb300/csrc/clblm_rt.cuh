@@ -18,6 +18,7 @@ struct InterpSpec {
   double v1, dvin, dvout, ratio;
   int64_t nin;
   const int2* map;  // itype < 0: (iIn, IP) of each output point, replayed by k_interp_map
+  int dec;          // dvin > dvout (formed on the host: no binary64 compare per point)
 };
 
 struct RtLayerArgs {
@@ -40,6 +41,9 @@ struct RtLayerArgs {
   // FP32 set-up of the mixed path: v/kT = x0 + (i-1)*x1 on the OD grid
   float xt0, xt1, xb0, xb1, xa0, xa1, vf0, vf1;
   float xs0, xs1;      // surface: v/kT_skin on the merged-input grid
+  // FP32 copies of the scalars above the mixed path uses (formed on the host:
+  // a conversion per point would run on the FP64 unit)
+  float scal_up_f, scal_dn_f, emis_f, omemis_f, vs0, vs1;  // vs: V on the merged-input grid
 };
 
 // 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365),
@@ -84,16 +88,18 @@ __device__ __forceinline__ Stencil<W> interp_stencil(const InterpSpec& s, int64_
     return st;
   }
   if (s.itype > 0) {  // fixed ratio n/(n+1) or (n+1)/n
-    int64_t g = (I - 1) / s.len_out;
-    int NL = (int)((I - 1) % s.len_out) + 1;
+    // (32-bit arithmetic: a spectrum holds fewer than 2^31 points)
+    const int I0 = (int)(I - 1);
+    const int g = I0 / s.len_out;
+    const int NL = I0 - g * s.len_out + 1;
     if (NL == 1) {
-      st.i[0] = 1 + g * s.len_in;
+      st.i[0] = 1 + (int64_t)g * s.len_in;
       st.w[0] = 1.;
       st.n = 1;
       return st;
     }
-    int64_t iIn = NL - s.len_in + (g + 1) * (int64_t)s.len_in;
-    if (s.dvin > s.dvout) iIn -= 1;
+    int64_t iIn = NL - s.len_in + (int64_t)(g + 1) * s.len_in;
+    if (s.dec) iIn -= 1;
     st.i[0] = iIn - 1;
     st.i[1] = iIn;
     st.i[2] = iIn + 1;

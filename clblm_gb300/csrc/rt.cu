@@ -133,7 +133,7 @@ __device__ __forceinline__ void layer_terms_d(const RtLayerArgs& a, int64_t i, d
 
 __device__ __forceinline__ void layer_terms_f(const RtLayerArgs& a, int64_t i, float out[4]) {
   const float odf = reinterpret_cast<const float*>(a.od)[i - 1];
-  const float odA = odf * (float)a.scal_up, odB = odf * (float)a.scal_dn;
+  const float odA = odf * a.scal_up_f, odB = odf * a.scal_dn_f;
   const float TA = expf(-odA), TB = expf(-odB);
   const float aA = -expm1f(-odA), aB = -expm1f(-odB);
   const float fi = (float)(i - 1);
@@ -202,11 +202,14 @@ __global__ void k_rt_layer(RtLayerArgs a) {
             return planck_d(v, a.tskin / kRADCN2) * a.emis;
           } else {
             float fj = (float)(j - 1);
-            float vf = fmaf(fj, (float)a.mr.dvin, (float)a.v1);
-            return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * (float)a.emis;
+            float vf = fmaf(fj, a.vs1, a.vs0);
+            return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * a.emis_f;
           }
         };
-        auto sf = [&](int64_t) -> Real { return (Real)(1.0 - a.emis); };
+        auto sf = [&](int64_t) -> Real {
+          if constexpr (Plain) return 1.0 - a.emis;
+          else return a.omemis_f;
+        };
         r = ext_at<Real>(sr, a.mr.nin, st.i[k]);
         f = ext_at<Real>(sf, a.mr.nin, st.i[k]);
       } else {

@@ -704,6 +704,7 @@ InterpSpec interp_spec(double v1in, double dvin, int64_t nin, double v1out, doub
     return s;
   }
   s.kind = 1;
+  s.dec = dvin > dvout ? 1 : 0;
   bool sameV1 = std::fabs(v1in - v1out) < EPS;
   double dvRatio = dvout / dvin;
   if (std::fabs(dvout - dvin) < TOL) dvRatio = 1.;
@@ -1838,6 +1839,12 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       a.vf1 = (float)P.dv;
       a.xs0 = (float)(col->v1 * (kRADCN2 / col->tskin));
       a.xs1 = (float)(in_dv * (kRADCN2 / col->tskin));
+      a.scal_up_f = (float)a.scal_up;
+      a.scal_dn_f = (float)a.scal_dn;
+      a.emis_f = (float)a.emis;
+      a.omemis_f = (float)(1.0 - a.emis);
+      a.vs0 = (float)a.v1;
+      a.vs1 = (float)a.mr.dvin;
       auto rt = [&](int v) {
         const int nt = kRtThreads[v];
         const unsigned grid = (unsigned)((a.n_out + nt - 1) / nt);
