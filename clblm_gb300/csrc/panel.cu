@@ -859,20 +859,26 @@ template __global__ void k_panel<true>(const __grid_constant__ PanelArgs);
 // Core: the point may lie within 64 ALFV of the line (the polynomial core of
 // CNVF4Q), else the Lorentzian wing is certain; Mask: the record's point
 // range [jmin, jmax] may exclude a point.
+__device__ __forceinline__ float rcp_approx(float x) {  // PTX rcp.approx: relative error < 2^-23
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <bool Core, bool Mask>
 __device__ __forceinline__ float2 f4_term(const F4Rec& r, float2 Jm1, float2 dvr4, int JA, int JB) {
   const float2 xm = __ffma2_rn(__fadd2_rn(Jm1, r.nmc), dvr4, r.x0);
   const float2 xmsq = __fmul2_rn(xm, xm);
   const float2 nfb = __ffma2_rn(xmsq, r.fb2, r.nfb0);
   const float2 den = __fadd2_rn(xmsq, r.al2);
-  float2 f = make_float2(__fdividef(r.sil.x, den.x), __fdividef(r.sil.y, den.y));
+  // the Lorentzian wing SIL / (AL2 + XM^2) and the pedestal in one packed FMA
+  float2 f = __ffma2_rn(r.sil, make_float2(rcp_approx(den.x), rcp_approx(den.y)), nfb);
   if constexpr (Core) {
     const float2 zvsq = __fmul2_rn(xmsq, r.ralv2);
-    const float2 core = __ffma2_rn(zvsq, r.sb3, r.sa3);
+    const float2 core = __fadd2_rn(__ffma2_rn(zvsq, r.sb3, r.sa3), nfb);
     f.x = zvsq.x <= 4096.f ? core.x : f.x;
     f.y = zvsq.y <= 4096.f ? core.y : f.y;
   }
-  f = __fadd2_rn(f, nfb);
   if constexpr (Mask) {
     f.x = (JA >= r.jmin && JA <= r.jmax) ? f.x : 0.f;
     f.y = (JB >= r.jmin && JB <= r.jmax) ? f.y : 0.f;
@@ -894,7 +900,7 @@ __device__ __forceinline__ float2 f4_chunk(const F4Rec* S, int cnt, float2 Jm1, 
 }
 
 template <bool Plain, int CHUNK>
-__global__ void __launch_bounds__(kF4Threads) k_f4_conv(F4Args a) {
+__global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a) {
   static_assert(CHUNK % kF4Group == 0, "groups of the FP32 sums lie within a chunk");
   using Real = typename std::conditional<Plain, double, float>::type;
   using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
