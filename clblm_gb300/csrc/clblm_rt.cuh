@@ -124,8 +124,9 @@ __device__ __forceinline__ Stencil<W> interp_stencil(const InterpSpec& s, int64_
 void rt_upload_interp_coef(cudaStream_t st);
 __global__ void k_interp_map(InterpSpec s, const int64_t* blk_j1, const double* blk_vo, int nblk, int64_t nout,
                              int2* map);
+constexpr int kRtMaxThreads = 512;  // largest k_rt_layer block the autotuner times
 template <bool Plain>
-__global__ void k_rt_layer(RtLayerArgs a);
+__global__ void __launch_bounds__(kRtMaxThreads) k_rt_layer(RtLayerArgs a);
 template <bool Plain>
 __global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_out, double* out);
 

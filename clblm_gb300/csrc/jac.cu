@@ -126,7 +126,7 @@ __device__ __forceinline__ Real dev_exp(Real x) {
 
 // planckFnDrv, clblm_EMLAY.f90:45-70
 template <typename Real>
-__device__ __forceinline__ void planck_drv_t(double V, Real T, Real* B, Real* dB) {
+__device__ __forceinline__ void planck_drv_t(Real V, Real T, Real* B, Real* dB) {
   const Real RC1 = (Real)kRADCN1, RC2 = (Real)kRADCN2;
   Real XKT = T / RC2;
   if (XKT <= (Real)1.e-6) {
@@ -162,22 +162,47 @@ template <bool Plain>
 __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   const int64_t iv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (iv >= a.nout) return;
   const int N2 = a.nlay;
   constexpr int M = kMaxJacLayers + 2;
+  // mixed path: FP32 copies of the profile's per-layer arrays, converted once
+  // per block (a conversion from binary64 runs on the FP64 unit)
+  enum { kAmf, kTlev, kTlay, kTup, kTlo, kQup, kQlo, kRt100, kNc };
+  __shared__ float s_c[Plain ? 1 : kNc][Plain ? 1 : M];
+  if constexpr (!Plain) {
+    for (int l = threadIdx.x; l <= N2; l += blockDim.x) {
+      const bool lay = l < N2;
+      auto cv = [&](const double* arr, bool in) { return in && arr ? (float)arr[l] : 0.f; };
+      s_c[kTlev][l] = cv(a.tlev, true);
+      s_c[kAmf][l] = cv(a.amf_down, lay);
+      s_c[kTlay][l] = cv(a.tlay, lay);
+      s_c[kTup][l] = cv(a.dT_dTup, lay);
+      s_c[kTlo][l] = cv(a.dT_dTlo, lay);
+      s_c[kQup][l] = cv(a.dW_dQup, lay);
+      s_c[kQlo][l] = cv(a.dW_dQlo, lay);
+      s_c[kRt100][l] = lay && a.tlay ? 100.f / (float)a.tlay[l] : 0.f;
+    }
+    __syncthreads();
+  }
+  // per-layer value c of layer (or level) i: binary64 on the FP64 path
+  auto lc = [&](int c, const double* arr, int i) -> Real {
+    if constexpr (Plain) return arr[i];
+    else return s_c[c][i];
+  };
+  if (iv >= a.nout) return;
   Real viewOD[M], downOD[M], Bbar[M], dBbar[M], Blev[M], dBlev[M], cumTxA[M], cumTxB2[M];
   Real dRad_dT_up[M], dRad_dT_dn[M], dRad_dTbar[M], dRad_dTau[M], dRad_dTlev[M];
   const Real* jod = reinterpret_cast<const Real*>(a.jod);
   const double vn = a.v1 + (double)iv * a.dv;
+  const Real vr = (Real)vn;  // the point's wavenumber in the working precision, converted once
   for (int l = 1; l <= N2; ++l) {
     viewOD[l] = jod[(int64_t)(l - 1) * a.nout + iv];
-    downOD[l] = viewOD[l] * (Real)a.amf_down[l - 1];
+    downOD[l] = viewOD[l] * lc(kAmf, a.amf_down, l - 1);
   }
   if (a.lin_in_tau != 0)
-    for (int lv = 1; lv <= N2 + 1; ++lv) planck_drv_t<Real>(vn, (Real)a.tlev[lv - 1], &Blev[lv], &dBlev[lv]);
-  for (int l = 1; l <= N2; ++l) planck_drv_t<Real>(vn, (Real)a.tlay[l - 1], &Bbar[l], &dBbar[l]);
+    for (int lv = 1; lv <= N2 + 1; ++lv) planck_drv_t<Real>(vr, lc(kTlev, a.tlev, lv - 1), &Blev[lv], &dBlev[lv]);
+  for (int l = 1; l <= N2; ++l) planck_drv_t<Real>(vr, lc(kTlay, a.tlay, l - 1), &Bbar[l], &dBbar[l]);
   Real Bsfc, dBsfc;
-  planck_drv_t<Real>(vn, (Real)a.tsfc, &Bsfc, &dBsfc);
+  planck_drv_t<Real>(vr, (Real)a.tsfc, &Bsfc, &dBsfc);
   Real rad = 0;
   for (int l = 1; l <= N2; ++l) dRad_dTau[l] = dRad_dTbar[l] = 0;
   for (int l = 1; l <= N2 + 1; ++l) dRad_dT_up[l] = dRad_dT_dn[l] = dRad_dTlev[l] = 0;
@@ -203,7 +228,7 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
     }
     for (int l = N2; l >= 1; --l) {
       dTran = cumTxB2[l] - cumTxB2[l + 1];
-      const Real amf = (Real)a.amf_down[l - 1];
+      const Real amf = lc(kAmf, a.amf_down, l - 1);
       if (lit != 0) {
         rlin_t(downOD[l], &dbavgdb, &dbavgdbdod);
         if (lit == 2) {
@@ -272,8 +297,8 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
       for (int lv = 1; lv <= N2 + 1; ++lv) dRad_dTlev[lv] = dRad_dT_up[lv] + dRad_dT_dn[lv] * rsfc;
     if (lit == 0 || lit == 1)
       for (int l = N2; l >= 1; --l) {
-        dRad_dTlev[l + 1] = dRad_dTlev[l + 1] + dRad_dTbar[l] * (Real)a.dT_dTup[l - 1];
-        dRad_dTlev[l] = dRad_dTlev[l] + dRad_dTbar[l] * (Real)a.dT_dTlo[l - 1];
+        dRad_dTlev[l + 1] = dRad_dTlev[l + 1] + dRad_dTbar[l] * lc(kTup, a.dT_dTup, l - 1);
+        dRad_dTlev[l] = dRad_dTlev[l] + dRad_dTbar[l] * lc(kTlo, a.dT_dTlo, l - 1);
       }
   }
   const int64_t o = a.off + iv;
@@ -296,11 +321,11 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
         dTau_dT = dTau_dT - dTau_dW * fac;
       } else {
         // (wp - m) / (0.01 Wtot) * (Wtot / T) = (wp - m) * 100 / T
-        dTau_dT = (tp - m) - (wp - m) * (100.f / (float)a.tlay[il]);
+        dTau_dT = (tp - m) - (wp - m) * s_c[kRt100][il];
       }
       const Real dRaddT = dRad_dTau[il + 1] * dTau_dT;
-      const Real up = dRaddT * (Real)a.dT_dTup[il];
-      lo = lo + dRaddT * (Real)a.dT_dTlo[il] + dRad_dTlev[il + 1];
+      const Real up = dRaddT * lc(kTup, a.dT_dTup, il);
+      lo = lo + dRaddT * lc(kTlo, a.dT_dTlo, il) + dRad_dTlev[il + 1];
       a.dtlev[(int64_t)il * a.ld + o] = (double)lo;
       if (il == N2 - 1) a.dtlev[(int64_t)N2 * a.ld + o] = (double)(up + dRad_dTlev[il + 2]);
       lo = up;
@@ -311,8 +336,8 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
     Real lo = 0;
     for (int il = 0; il < N2; ++il) {
       const Real dRad_dW = dRad_dTau[il + 1] * jod[((int64_t)a.vM * N2 + il) * a.nout + iv];
-      const Real up = dRad_dW * (Real)a.dW_dQup[il];
-      lo = lo + dRad_dW * (Real)a.dW_dQlo[il];
+      const Real up = dRad_dW * lc(kQup, a.dW_dQup, il);
+      lo = lo + dRad_dW * lc(kQlo, a.dW_dQlo, il);
       a.dqlev[(int64_t)il * a.ld + o] = (double)lo;
       if (il == N2 - 1) a.dqlev[(int64_t)N2 * a.ld + o] = (double)up;
       lo = up;

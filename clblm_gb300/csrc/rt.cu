@@ -13,6 +13,8 @@
 // per output point instead of materialising the interpolated arrays.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "clblm_common.cuh"
 #include "clblm_kernels.cuh"
 #include "clblm_panel.cuh"
@@ -136,7 +138,7 @@ __device__ __forceinline__ void layer_terms_f(const RtLayerArgs& a, int64_t i, f
   const float odA = odf * a.scal_up_f, odB = odf * a.scal_dn_f;
   const float TA = expf(-odA), TB = expf(-odB);
   const float aA = -expm1f(-odA), aB = -expm1f(-odB);
-  const float fi = (float)(i - 1);
+  const float fi = (float)(int)(i - 1);  // 32-bit conversion: a 64-bit one runs on the FP64 unit
   const float vf = fmaf(fi, a.vf1, a.vf0);
   const float cv3 = (float)kRADCN1 * vf * vf * vf;
   const float Bt = planck_f(fmaf(fi, a.xt1, a.xt0), cv3);
@@ -183,10 +185,47 @@ __device__ __forceinline__ void layer_terms_ext(const RtLayerArgs& a, int64_t j,
 }
 
 template <bool Plain>
-__global__ void k_rt_layer(RtLayerArgs a) {
+__global__ void __launch_bounds__(kRtMaxThreads) k_rt_layer(RtLayerArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
-  int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (I > a.n_out) return;
+  // layer terms of the CTA's OD-grid range, each evaluated once (a layer grid
+  // coarser than the merge grid feeds every OD point into up to four
+  // neighbouring output points' stencils)
+  constexpr int kCap = kRtMaxThreads + 8;
+  __shared__ Real sh_t[4][kCap];
+  __shared__ int sh_lo, sh_hi;
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const bool live = I <= a.n_out;
+  const bool share = a.ly.kind == 1 && a.ly.itype != 0;  // four-point stencils: uniform over the launch
+  Stencil<Real> sl;
+  sl.n = 0;
+  if (live) sl = interp_stencil<Real>(a.ly, I);
+  int64_t jlo = 0;
+  bool staged = false;
+  if (share) {
+    if (threadIdx.x == 0) {
+      sh_lo = INT_MAX;
+      sh_hi = INT_MIN;
+    }
+    __syncthreads();
+    if (live) {
+      atomicMin(&sh_lo, (int)sl.i[0]);
+      atomicMax(&sh_hi, (int)(sl.n == 4 ? sl.i[3] : sl.i[0]));  // stencils hold 1 or 4 points
+    }
+    __syncthreads();
+    jlo = sh_lo;
+    const int64_t nr = (int64_t)sh_hi - jlo + 1;
+    staged = nr <= kCap;  // uniform over the CTA
+    if (staged) {
+      for (int64_t r = threadIdx.x; r < nr; r += blockDim.x) {
+        Real t[4];
+        layer_terms_ext<Plain>(a, jlo + r, t);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) sh_t[c][r] = t[c];
+      }
+      __syncthreads();
+    }
+  }
+  if (!live) return;
   // merged radiance and reflectance at I
   Real R = 0, F = 0;
   {
@@ -201,7 +240,7 @@ __global__ void k_rt_layer(RtLayerArgs a) {
             double v = a.v1 + (double)(j - 1) * a.mr.dvin;
             return planck_d(v, a.tskin / kRADCN2) * a.emis;
           } else {
-            float fj = (float)(j - 1);
+            float fj = (float)(int)(j - 1);
             float vf = fmaf(fj, a.vs1, a.vs0);
             return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * a.emis_f;
           }
@@ -231,15 +270,24 @@ __global__ void k_rt_layer(RtLayerArgs a) {
   }
   Real L[4];
   {
-    const Stencil<Real> st = interp_stencil<Real>(a.ly, I);
+    const Stencil<Real>& st = sl;
+    // the terms at OD-grid index j: from the CTA's staged range, or evaluated here
+    auto terms = [&](int64_t j, Real t[4]) {
+      if (staged) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) t[c] = sh_t[c][j - jlo];
+      } else {
+        layer_terms_ext<Plain>(a, j, t);
+      }
+    };
     if (st.n == 1) {
-      layer_terms_ext<Plain>(a, st.i[0], L);
+      terms(st.i[0], L);
     } else {
       for (int c = 0; c < 4; ++c) L[c] = 0;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         Real t[4];
-        layer_terms_ext<Plain>(a, st.i[k], t);
+        terms(st.i[k], t);
         for (int c = 0; c < 4; ++c) L[c] += st.w[k] * t[c];
       }
     }

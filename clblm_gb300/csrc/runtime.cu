@@ -84,7 +84,7 @@ struct Tuner {
   bool on = true;         // CLBLM_AUTOTUNE=0: the defaults, no timing
 };
 constexpr int kF4StageRecords[3] = {64, 128, 256};
-constexpr int kRtThreads[3] = {128, 256, 512};
+constexpr int kRtThreads[3] = {128, 256, kRtMaxThreads};
 constexpr int kJacThreads[2] = {64, 128};
 }  // namespace
 
