@@ -70,6 +70,14 @@ def fp32_peak_tflops():
     return 152 * 128 * 2 * mhz * 1e6 / 1e12, mhz
 
 
+def hbm_peak_gbs():
+    """Measured copy bandwidth of the GB300s (GB/s), else the 6.8 TB/s fallback."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
 def load_traffic():
     """DRAM bytes per output point of each kernel, from the ncu capture whose
     summary profiles/dram_traffic.txt holds (lines `kernel bytes_per_point`;
@@ -104,7 +112,17 @@ def roofline(work, kt, steps, ms_step, points):
                      "frac": ach / peak if ach else None,
                      "traffic": bpp * points if bpp is not None else None,
                      "ms_per_launch": ms, "share_of_step": ms / ms_step, "flop_per_launch": flop}
-    top = max(out, key=lambda k: out[k]["ms_per_launch"])
+    if kt.get("ms_rt", 0) > 0 and work.get("rt_bytes", 0) > 0:
+        # the layer recurrence (one launch per layer): algorithmic bytes over
+        # its device time, against the measured copy bandwidth
+        hbm = hbm_peak_gbs()
+        ms_rt = kt["ms_rt"] / steps
+        ach = work["rt_bytes"] / (ms_rt * 1e-3) / 1e9
+        out["k_rt_layer"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "traffic": None, "ms_per_launch": ms_rt, "share_of_step": ms_rt / ms_step,
+                             "bytes_per_step": work["rt_bytes"], "launches_per_step": work.get("layers"),
+                             "peak_source": "hbm_gbs of MEASURED_PEAKS.json (burst copy)"}
+    top = max((k for k in out if out[k]["bound"] == "fp32"), key=lambda k: out[k]["ms_per_launch"])
     r = dict(out[top])
     r["kernel"] = top
     r["peak_source"] = ("nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x %.0f MHz (sm_max_mhz of "
@@ -584,7 +602,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kt = {"ms_panel": 0.0, "ms_f4conv": 0.0, "ms_line_chain": 0.0, "ms_f4_chain": 0.0, "launches": 0}
+    kt = {"ms_panel": 0.0, "ms_f4conv": 0.0, "ms_line_chain": 0.0, "ms_f4_chain": 0.0, "ms_rt": 0.0,
+          "launches": 0}
     with Clocks() as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
@@ -595,7 +614,7 @@ def main():
                 kt[k] += st[k]
         ev1.record(stream)
         torch.cuda.synchronize()
-    work = h.stats()
+    work = dict(h.stats(), layers=col.nlay)
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, "cuda")
     value = replica_value(lp, world, ms)
 
@@ -673,7 +692,8 @@ def main():
                 # and the far-wing chain run side by side before the panel kernel
                 "stages_ms": {"line_chain": kt["ms_line_chain"] / args.steps,
                               "far_wing_chain": kt["ms_f4_chain"] / args.steps,
-                              "k_f4_conv": kt["ms_f4conv"] / args.steps, "k_panel": kt["ms_panel"] / args.steps}}
+                              "k_f4_conv": kt["ms_f4conv"] / args.steps, "k_panel": kt["ms_panel"] / args.steps,
+                              "k_rt_layer": kt["ms_rt"] / args.steps}}
         print(json.dumps(line))
     h.close()
     if world > 1:

@@ -126,7 +126,7 @@ class clblm_od_stats_t(C.Structure):
                 ("cnvf4q_steps", C.c_int64), ("ms_panel", C.c_double), ("ms_f4conv", C.c_double),
                 ("ms_line_chain", C.c_double), ("ms_f4_chain", C.c_double),
                 ("f4_stage_records", C.c_int32), ("rt_threads", C.c_int32), ("jac_threads", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("ms_rt", C.c_double), ("rt_bytes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

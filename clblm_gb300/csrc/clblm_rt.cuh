@@ -126,7 +126,7 @@ __global__ void k_interp_map(InterpSpec s, const int64_t* blk_j1, const double* 
                              int2* map);
 constexpr int kRtMaxThreads = 512;  // largest k_rt_layer block the autotuner times
 template <bool Plain>
-__global__ void __launch_bounds__(kRtMaxThreads) k_rt_layer(RtLayerArgs a);
+__global__ void __launch_bounds__(kRtMaxThreads, Plain ? 1 : 2) k_rt_layer(RtLayerArgs a);
 template <bool Plain>
 __global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_out, double* out);
 

@@ -185,7 +185,7 @@ __device__ __forceinline__ void layer_terms_ext(const RtLayerArgs& a, int64_t j,
 }
 
 template <bool Plain>
-__global__ void __launch_bounds__(kRtMaxThreads) k_rt_layer(RtLayerArgs a) {
+__global__ void __launch_bounds__(kRtMaxThreads, Plain ? 1 : 2) k_rt_layer(RtLayerArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
   // layer terms of the CTA's OD-grid range, each evaluated once (a layer grid
   // coarser than the merge grid feeds every OD point into up to four

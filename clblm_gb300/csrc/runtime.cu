@@ -144,17 +144,20 @@ struct clblm_handle {
   int64_t launches = 0;  // kernels launched by the current call
   // per-call sums of the line-shape kernels' work and device time
   // f4 conv start/stop, panel start/stop, batch start, line chain done
-  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // batch timing: far-wing kernel, panel kernel, line chain (0-5); layer recurrence (6, 7)
+  cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // the far-wing chain runs on a second stream, forked from and joined back
   // into `stream` within each OD batch
   cudaStream_t stream2 = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int64_t acc_fnq = 0, acc_f4q = 0;
-  double acc_ms_panel = 0., acc_ms_f4 = 0., acc_ms_line_chain = 0., acc_ms_f4_chain = 0.;
+  double acc_ms_panel = 0., acc_ms_f4 = 0., acc_ms_line_chain = 0., acc_ms_f4_chain = 0., acc_ms_rt = 0.;
+  int64_t acc_rt_bytes = 0;
   void reset_call() {
     launches = 0;
     acc_fnq = acc_f4q = 0;
-    acc_ms_panel = acc_ms_f4 = acc_ms_line_chain = acc_ms_f4_chain = 0.;
+    acc_ms_panel = acc_ms_f4 = acc_ms_line_chain = acc_ms_f4_chain = acc_ms_rt = 0.;
+    acc_rt_bytes = 0;
   }
 };
 
@@ -1351,6 +1354,8 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
     last_stats->ms_f4conv = h->acc_ms_f4;
     last_stats->ms_line_chain = h->acc_ms_line_chain;
     last_stats->ms_f4_chain = h->acc_ms_f4_chain;
+    last_stats->ms_rt = h->acc_ms_rt;  // radiance calls add the batch's recurrence after this
+    last_stats->rt_bytes = h->acc_rt_bytes;
   }
   return CLBLM_OK;
 }
@@ -1794,6 +1799,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
     if (rc) return rc;
     rc = run_od_batch(h, rp.hps, first, count, plain, ls, fs, ps);
     if (rc) return rc;
+    CUDA_TRY(h, cudaEventRecord(h->ev[6], h->stream));
     for (int il = first; il < first + count; ++il) {
       const LayerPlan& P = rp.hps[il].P;
       RtLayerArgs a;
@@ -1859,10 +1865,21 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       h->launches++;
       rt(tv);
       CUDA_TRY(h, cudaGetLastError());
+      // algorithmic bytes: the layer OD, the merged radiance and reflectance
+      // in (none from the surface) and out
+      h->acc_rt_bytes += (int64_t)real * (P.nsamp + (il == 0 ? 0 : 2 * in_n) + 2 * a.n_out);
       cur = 1 - cur;
     }
+    CUDA_TRY(h, cudaEventRecord(h->ev[7], h->stream));
     rc = check_batch(h, rp.hps, first, count, &h->last);
     if (rc) return rc;
+    {
+      float t = 0.f;
+      CUDA_TRY(h, cudaEventElapsedTime(&t, h->ev[6], h->ev[7]));
+      h->acc_ms_rt += t;
+      h->last.ms_rt = h->acc_ms_rt;
+      h->last.rt_bytes = h->acc_rt_bytes;
+    }
     first += count;
   }
   // binary64 radiance out

@@ -211,6 +211,10 @@ typedef struct {
   int32_t rt_threads;       /* threads per block of the layer recurrence     */
   int32_t jac_threads;      /* threads per block of the Jacobian recurrence  */
   int32_t reserved;
+  /* radiance calls: device time of the layer recurrence launches and their
+   * algorithmic bytes (layer OD, merged spectra in and out), summed */
+  double  ms_rt;
+  int64_t rt_bytes;
 } clblm_od_stats_t;
 
 typedef struct clblm_handle clblm_handle_t;
