@@ -121,7 +121,7 @@ __device__ __forceinline__ Stencil<W> interp_stencil(const InterpSpec& s, int64_
   return st;
 }
 
-void rt_upload_interp_coef(cudaStream_t st);
+cudaError_t rt_upload_interp_coef(cudaStream_t st);
 __global__ void k_interp_map(InterpSpec s, const int64_t* blk_j1, const double* blk_vo, int nblk, int64_t nout,
                              int2* map);
 constexpr int kRtMaxThreads = 512;  // largest k_rt_layer block the autotuner times

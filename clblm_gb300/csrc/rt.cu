@@ -43,6 +43,7 @@ __global__ void k_interp_map(InterpSpec s, const int64_t* __restrict__ blk_j1, c
   double Vi = __dadd_rn(s.v1, __dmul_rn((double)(iIn - 1), s.dvin));
   double P = __ddiv_rn(__dadd_rn(Vo, -Vi), s.dvin);
   const int64_t J1 = blk_j1[b];
+  if (J1 < 1 || J1 > nout) return;  // a block start off the output grid writes nothing
   const int64_t J2 = min(nout, J1 + 2400 - 1);
   for (int64_t J = J1; J <= J2; ++J) {
     int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
@@ -322,7 +323,7 @@ __global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_o
 template __global__ void k_od_out<false>(const void*, int64_t, InterpSpec, int64_t, double*);
 template __global__ void k_od_out<true>(const void*, int64_t, InterpSpec, int64_t, double*);
 
-void rt_upload_interp_coef(cudaStream_t st) {
+cudaError_t rt_upload_interp_coef(cudaStream_t st) {
   double a1[203], a2[203], a3[203], a4[203];
   const double XNUMCF = 201.;
   for (int IP = 0; IP <= 202; ++IP) {
@@ -333,10 +334,11 @@ void rt_upload_interp_coef(cudaStream_t st) {
     a3[IP] = PP * (3.0 - 2.0 * P) + P / 2.0 * ((1.0 - P) * (1.0 - P));
     a4[IP] = -PP / 2 * (1.0 - P);
   }
-  cudaMemcpyToSymbolAsync(c_IA1, a1, sizeof a1, 0, cudaMemcpyHostToDevice, st);
-  cudaMemcpyToSymbolAsync(c_IA2, a2, sizeof a2, 0, cudaMemcpyHostToDevice, st);
-  cudaMemcpyToSymbolAsync(c_IA3, a3, sizeof a3, 0, cudaMemcpyHostToDevice, st);
-  cudaMemcpyToSymbolAsync(c_IA4, a4, sizeof a4, 0, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_IA1, a1, sizeof a1, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_IA2, a2, sizeof a2, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_IA3, a3, sizeof a3, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_IA4, a4, sizeof a4, 0, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
   static float af[4][203];  // staged by the copy before it returns (pageable source)
   for (int IP = 0; IP <= 202; ++IP) {
     af[0][IP] = (float)a1[IP];
@@ -344,7 +346,7 @@ void rt_upload_interp_coef(cudaStream_t st) {
     af[2][IP] = (float)a3[IP];
     af[3][IP] = (float)a4[IP];
   }
-  cudaMemcpyToSymbolAsync(c_IAf, af, sizeof af, 0, cudaMemcpyHostToDevice, st);
+  return cudaMemcpyToSymbolAsync(c_IAf, af, sizeof af, 0, cudaMemcpyHostToDevice, st);
 }
 
 }  // namespace clblm

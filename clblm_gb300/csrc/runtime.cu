@@ -352,7 +352,7 @@ int upload_tables(clblm_handle* h) {
     for (int i = 0; i < 102; ++i) af[i] = (float)CLBLM_AVRAT[i];
     CUDA_TRY(h, cudaMemcpyToSymbol(c_AVRATf, af, sizeof af));
   }
-  rt_upload_interp_coef(h->stream);
+  CUDA_TRY(h, rt_upload_interp_coef(h->stream));
   return CLBLM_OK;
 }
 
@@ -1927,7 +1927,8 @@ unsigned char* g_noalloc_ptr[kNoAllocMaxDevices];
 
 // Once per device, with that device current: the device address of the
 // scratch array (its host-side name is only a stand-in) and the 201-point
-// interpolation coefficients in constant memory.
+// interpolation coefficients in constant memory.  The device counts as set up
+// only when both succeeded.
 cudaError_t noalloc_setup(int dev, unsigned char** ptr) {
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (g_noalloc_ptr[dev]) {
@@ -1937,7 +1938,8 @@ cudaError_t noalloc_setup(int dev, unsigned char** ptr) {
   void* p = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  rt_upload_interp_coef(0);
+  e = rt_upload_interp_coef(0);
+  if (e != cudaSuccess) return e;
   e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) return e;
   g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
@@ -1945,13 +1947,34 @@ cudaError_t noalloc_setup(int dev, unsigned char** ptr) {
   return cudaSuccess;
 }
 
-bool is_device_pointer(const void* p) {
+// Device memory of device `dev` (or managed memory); host memory and memory of
+// another GPU are refused.
+bool is_device_pointer(const void* p, int dev) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
+}
+
+// interpSpectrum's block starts J1 and their wavenumbers Vo (the outer loop
+// of the general-ratio branch, clblm_Spectrum.f90:528-535), formed on the
+// device by one thread with every operation rounded on its own, as the host
+// loop of clblm_gpu_od forms them; `nb` blocks, counted by the same loop on
+// the host.  Nothing is copied from host memory.
+__global__ void k_noalloc_blocks(double v1, double dvout, int64_t nout, int nb, int64_t* __restrict__ j1,
+                                 double* __restrict__ vo) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double Vo = v1;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t J1 = (int64_t)__dadd_rn(__ddiv_rn(__dadd_rn(Vo, -v1), dvout), 1.001);
+    const int64_t J2 = min(nout, J1 + 2400 - 1);
+    j1[b] = J1;
+    vo[b] = Vo;
+    Vo = __dadd_rn(v1, __dmul_rn((double)J2, dvout));
+  }
 }
 
 }  // namespace
@@ -1963,15 +1986,14 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
   if (nout > CLBLM_NOALLOC_MAX_POINTS) return CLBLM_ERR_CAPACITY;
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return CLBLM_ERR_NO_DEVICE;
-  if (!is_device_pointer(d_in) || !is_device_pointer(d_out)) return CLBLM_ERR_ARG;
+  if (!is_device_pointer(d_in, dev) || !is_device_pointer(d_out, dev)) return CLBLM_ERR_ARG;
   unsigned char* base = nullptr;
   if (noalloc_setup(dev, &base) != cudaSuccess) return CLBLM_ERR_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   InterpSpec s = interp_spec(v1, dvin, nin, v1, dvout, nout);
   if (s.kind != 0 && s.itype < 0) {
-    // block starts of interpSpectrum's outer loop, as build_interp_map
-    int64_t j1[kNoAllocBlocks];
-    double vo[kNoAllocBlocks];
+    // number of blocks of interpSpectrum's outer loop, as build_interp_map
+    // counts them; the device forms the block starts themselves
     int nb = 0;
     const double TOL = 1.e-8;
     double V2out = v1 + (double)(nout - 1) * dvout;
@@ -1980,8 +2002,6 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
       if (nb >= kNoAllocBlocks) return CLBLM_ERR_GRID;
       int64_t J1 = (int64_t)((Vo - v1) / dvout + 1.001);
       int64_t J2 = std::min<int64_t>(nout, J1 + 2400 - 1);
-      j1[nb] = J1;
-      vo[nb] = Vo;
       ++nb;
       Vo = v1 + (double)J2 * dvout;
     }
@@ -1991,9 +2011,8 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
     if (cudaMemsetAsync(map, 0, sizeof(int2) * (size_t)nout, st) != cudaSuccess) return CLBLM_ERR_CUDA;
     int64_t* dj1 = reinterpret_cast<int64_t*>(base + kNoAllocMapBytes);
     double* dvo = reinterpret_cast<double*>(base + kNoAllocMapBytes + 8 * (size_t)kNoAllocBlocks);
-    // the host tables are staged by the copies before they return
-    if (cudaMemcpyAsync(dj1, j1, 8 * (size_t)nb, cudaMemcpyHostToDevice, st) != cudaSuccess) return CLBLM_ERR_CUDA;
-    if (cudaMemcpyAsync(dvo, vo, 8 * (size_t)nb, cudaMemcpyHostToDevice, st) != cudaSuccess) return CLBLM_ERR_CUDA;
+    k_noalloc_blocks<<<1, 32, 0, st>>>(v1, dvout, nout, nb, dj1, dvo);
+    if (cudaGetLastError() != cudaSuccess) return CLBLM_ERR_CUDA;
     k_interp_map<<<(unsigned)((nb + 63) / 64), 64, 0, st>>>(s, dj1, dvo, nb, nout, map);
     if (cudaGetLastError() != cudaSuccess) return CLBLM_ERR_CUDA;
     s.map = map;
