@@ -504,7 +504,13 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   if (!(g->v2 > g->v1) || !(g->dv_normal > 0.) || !(g->dv_narrow > 0.) || !(g->sample > 0.))
     return set_err(h, CLBLM_ERR_GRID, "bad grid (v1 %.6f v2 %.6f dv %.3g/%.3g)", g->v1, g->v2, g->dv_normal,
                    g->dv_narrow);
-  if (!(lay->pave > 0.) || !(lay->tave > 0.) || !(lay->wtot > 0.)) return set_err(h, CLBLM_ERR_ARG, "bad layer");
+  if (!(lay->pave > 0.) || !(lay->tave > 0.) || !(lay->wtot > 0.) || !std::isfinite(lay->pave) ||
+      !std::isfinite(lay->tave) || !std::isfinite(lay->wtot))
+    return set_err(h, CLBLM_ERR_ARG, "bad layer (P %g, T %g, Wtot %g)", lay->pave, lay->tave, lay->wtot);
+  if (lay->nmol < 0 || (lay->nmol > 0 && (!lay->mol_id || !lay->w)))
+    return set_err(h, CLBLM_ERR_ARG, "bad layer molecules");
+  for (int i = 0; i < lay->nmol; ++i)
+    if (!std::isfinite(lay->w[i])) return set_err(h, CLBLM_ERR_ARG, "layer amount %d is not finite", i);
   if (c->line_off) return set_err(h, CLBLM_ERR_UNSUPPORTED, "lineOff is not on this path");
   if (c->dptmin != 0. || c->dptfac != 0.)
     return set_err(h, CLBLM_ERR_UNSUPPORTED, "line rejection thresholds DPTMIN/DPTFAC != 0 are not on this path");
@@ -1514,8 +1520,21 @@ void* clblm_gpu_stream(const clblm_handle_t* h) { return h ? (void*)h->stream : 
 
 int clblm_setdv(const clblm_column_t* col, double sample, double alfal0, double alfal0_fine, int32_t grid_type,
                 double dv_user, double* dv_normal, double* dv_narrow, double* dv_out) {
-  if (!col || col->nlay < 1 || !dv_normal || !dv_narrow) return CLBLM_ERR_ARG;
+  if (!col || col->nlay < 1 || !dv_normal || !dv_narrow || !col->pave || !col->tave || !col->wtot ||
+      (col->nmol > 0 && (!col->mol_id || !col->w)))
+    return CLBLM_ERR_ARG;
   const int n = col->nlay;
+  // layer pressures, temperatures and amounts: positive and finite (the
+  // reference would carry a NaN into every DV); the window finite
+  if (!std::isfinite(col->v1) || !std::isfinite(col->v2) || !(sample > 0.) || !std::isfinite(sample))
+    return CLBLM_ERR_ARG;
+  for (int il = 0; il < n; ++il) {
+    if (!(col->pave[il] > 0.) || !(col->tave[il] > 0.) || !(col->wtot[il] > 0.) || !std::isfinite(col->pave[il]) ||
+        !std::isfinite(col->tave[il]) || !std::isfinite(col->wtot[il]))
+      return CLBLM_ERR_ARG;
+    for (int m = 0; m < col->nmol; ++m)
+      if (!std::isfinite(col->w[(size_t)il * col->nmol + m])) return CLBLM_ERR_ARG;
+  }
   double V1 = col->v1, V2 = col->v2;
   double Vbar = 0.5 * (V1 + V2);
   if (V2 < V1) Vbar = V1;
@@ -1673,6 +1692,19 @@ struct RtPlan {
   int jrad_after = 0;
 };
 
+// Level temperatures, the downwelling path's columns and the surface of a
+// radiance column: finite, temperatures and columns positive, emissivity in
+// [0, 1].
+int check_column_rt(clblm_handle* h, const clblm_column_t* col) {
+  for (int il = 0; il < col->nlay; ++il)
+    if (!(col->tbot[il] > 0.) || !(col->ttop[il] > 0.) || !(col->wtot_down[il] > 0.) ||
+        !std::isfinite(col->tbot[il]) || !std::isfinite(col->ttop[il]) || !std::isfinite(col->wtot_down[il]))
+      return set_err(h, CLBLM_ERR_ARG, "bad column: layer %d level temperatures or downwelling column", il);
+  if (!(col->tskin > 0.) || !std::isfinite(col->tskin) || !(col->emis >= 0. && col->emis <= 1.))
+    return set_err(h, CLBLM_ERR_ARG, "bad surface (Tskin %g, emissivity %g)", col->tskin, col->emis);
+  return CLBLM_OK;
+}
+
 int plan_column(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, RtPlan* rp) {
   if (!col || !ctrl || col->nlay < 1) return set_err(h, CLBLM_ERR_ARG, "bad column");
   const int n = col->nlay;
@@ -1681,7 +1713,7 @@ int plan_column(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_
   int rc = clblm_setdv(col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, ctrl->grid_type, ctrl->dv_user, dvn.data(),
                        dvf.data(), &dvo);
   if (rc == CLBLM_ERR_DV_RATIO) return set_err(h, rc, "layer DV ratio > 2.5");
-  if (rc) return set_err(h, rc, "setDV failed");
+  if (rc) return set_err(h, rc, "setDV: bad column (layer P, T, amounts or window)");
   rp->hps.resize(n);
   rp->layers.resize(n);
   int jr = h->jrad;
@@ -1751,6 +1783,7 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
   if (!h) return CLBLM_ERR_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
   if (!col || !col->tbot || !col->ttop || !col->wtot_down) return set_err(h, CLBLM_ERR_ARG, "bad column");
+  if (int rc0 = check_column_rt(h, col)) return rc0;
   RtPlan rp;
   int rc = plan_column(h, col, ctrl, &rp);
   if (rc == CLBLM_OK || rc == CLBLM_ERR_UNSUPPORTED) {
@@ -2085,6 +2118,8 @@ int jac_setup(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t*
   if (col->nlay > kMaxJacLayers) return set_err(h, CLBLM_ERR_UNSUPPORTED, "more than %d layers", kMaxJacLayers);
   if (ctrl->grid_type != 1)
     return set_err(h, CLBLM_ERR_GRID, "noScattJacob: spectral grid is not uniform (gridType 1)");
+  if (!col->tbot || !col->ttop || !col->wtot_down) return set_err(h, CLBLM_ERR_ARG, "bad column");
+  if (int rc0 = check_column_rt(h, col)) return rc0;
   const int nl = col->nlay, nmol = col->nmol;
   if (jac->jac_mol > 0) {
     for (int k = 0; k < nmol; ++k)
@@ -2096,7 +2131,7 @@ int jac_setup(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t*
   int rc = clblm_setdv(col, ctrl->sample, ctrl->alfal0, ctrl->alfal0_fine, 1, ctrl->dv_user, dvn->data(),
                        dvf->data(), &js->dvb);
   if (rc == CLBLM_ERR_DV_RATIO) return set_err(h, rc, "layer DV ratio > 2.5");
-  if (rc) return set_err(h, rc, "setDV failed");
+  if (rc) return set_err(h, rc, "setDV: bad column (layer P, T, amounts or window)");
   if (!(js->dvb > 0.)) return set_err(h, CLBLM_ERR_GRID, "noScattJacob: DVout not set");
   js->nvar = 1;
   if (jac->do_temp) {
