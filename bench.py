@@ -12,10 +12,12 @@ Metric: layer-spectral-points/s = sum over layers of the layer-grid points
                    list is copied in from pinned host memory and the radiance
                    copied back to pinned host memory inside every step
   plain            the FP64 GPU path on the same column (reported beside)
-  cpu_baseline     the FP64 CPU restatement of the reference on a bounded
-                   sample of layers of the same column
+  cpu_baseline     the FP64 CPU restatement of the reference on the whole
+                   column, all host threads (and one thread on six layers);
+                   every GPU radiance of the run is compared with its radiance
+                   (max_rel_err_vs_oracle)
   --impl reference the reference's CPU path (the FP64 restatement, all host
-                   threads) on a bounded sample of the same workload
+                   threads) on the whole column every step
 
 Inputs are larger than L2 (the line list alone is 20 MB, the per-layer
 working set of a few layers exceeds 129 MB), so no extra L2 flush is done.
@@ -111,6 +113,9 @@ def roofline(work, kt, steps, ms_step, points):
         out[name] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if ach else None,
                      "traffic": bpp * points if bpp is not None else None,
+                     "traffic_source": ("scaled from a stored ncu capture: DRAM bytes per output point "
+                                        "(profiles/dram_traffic.txt) x this launch's points"
+                                        if bpp is not None else None),
                      "ms_per_launch": ms, "share_of_step": ms / ms_step, "flop_per_launch": flop}
     if kt.get("ms_rt", 0) > 0 and work.get("rt_bytes", 0) > 0:
         # the layer recurrence (one launch per layer): algorithmic bytes over
@@ -129,6 +134,35 @@ def roofline(work, kt, steps, ms_step, points):
                         "MEASURED_PEAKS.json, which holds no FP32 figure)" % mhz)
     r["others"] = {k: v for k, v in out.items() if k != top}
     return r
+
+
+def od_points(v1, v2, dv_normal, dv_narrow):
+    """Points ODLAY returns for one layer on its own grid: the grid choice of
+    clblm_ODLAY.f90:443-457 (DVnarrow when within 20 %) and panelOut's panel
+    rule (:2349-2360): panels of 2400 points from VFT = V1 - 32 DV until the
+    panel reaching V2, whose NHI is cut there (one more point when the cut
+    falls short of V2).  The same arithmetic as clblm_gpu_od_size; binary64
+    throughout, with no fused operations."""
+    dv = dv_normal if abs(dv_normal - dv_narrow) / dv_normal > 0.2 else dv_narrow
+    vft = v1 - 32.0 * dv
+    nhi0 = 2401 + 32 - 1
+    n = 0
+    while True:
+        if vft + (nhi0 - 1) * dv > v2:
+            nhi = int((v2 - vft) / dv + 1.0)
+            if vft + (nhi - 1) * dv < v2:
+                nhi += 1
+            return n + nhi - 33 + 1
+        n += nhi0 - 33 + 1
+        vft = vft + 2400.0 * dv
+
+
+def layer_points_host(col, ctrl):
+    """Sum over layers of the points ODLAY returns on each layer grid, from
+    setDV (the oracle's, no device) and the panel rule (od_points)."""
+    from oracle import oracle as O
+    dn, df, _ = O.Session().setdv(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, ctrl.grid_type, ctrl.dv_user)
+    return sum(od_points(col.v1, col.v2, dn[il], df[il]) for il in range(col.nlay))
 
 
 def layer_points(h, col, ctrl):
@@ -207,7 +241,6 @@ def pinned_lines(lines):
 
 
 CPU_LAYERS = list(range(28, 34))     # single-thread sample: 6 adjacent layers
-REF_LAYERS = list(range(20, 36))     # reference arm (all threads): 16 adjacent layers
 
 
 def cpu_sample_column(col, layers=CPU_LAYERS):
@@ -216,29 +249,25 @@ def cpu_sample_column(col, layers=CPU_LAYERS):
     return col.sub(layers)
 
 
-def run_cpu(lines, col, cont, ctrl, threads, layers=CPU_LAYERS):
+def run_cpu(lines, col, cont, ctrl, threads, layers=None):
+    """The FP64 restatement of the reference's path on `threads` host threads
+    (layer ODs in parallel, the merge's per-point loops in parallel): the
+    radiance of `col` (or of its `layers`), its sub-column and the time."""
     from oracle import oracle as O
     s = O.Session()
-    sub = cpu_sample_column(col, layers)
+    sub = col if layers is None else cpu_sample_column(col, layers)
     t0 = time.perf_counter()
-    s.rt_mode2(lines, sub, ctrl, cont, nthreads=threads)
+    rad, _ = s.rt_mode2(lines, sub, ctrl, cont, nthreads=threads)
     dt = time.perf_counter() - t0
-    return sub, dt
+    return sub, dt, rad
 
 
-def sample_points(col, ctrl):
-    from clblm_gb300 import capi_types as T
-    from oracle import oracle as O
-    s = O.Session()
-    dn, df, do = s.setdv(col, ctrl.sample, ctrl.alfal0, ctrl.alfal0_fine, ctrl.grid_type, ctrl.dv_user)
-    tot = 0
-    for il in range(col.nlay):
-        dv = dn[il] if abs(dn[il] - df[il]) / dn[il] > 0.2 else df[il]
-        # points ODLAY returns (panel rule); computed by the oracle's size query
-        g = T.grid_struct(col.v1, col.v2, dn[il], df[il], do, ctrl.sample, ctrl.alfal0)
-        n = int(np.ceil((col.v2 - col.v1) / dv + 1.0))
-        tot += n
-    return tot
+def rel_err(got, ref):
+    """Largest relative difference |got - ref| / |ref| over the spectrum."""
+    got, ref = np.asarray(got, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    if got.shape != ref.shape:
+        return None
+    return float(np.max(np.abs(got - ref) / np.abs(ref)))
 
 
 def jacobian_leg(cont, steps):
@@ -513,6 +542,13 @@ def profile_column(args):
     h.close()
 
 
+def config_of(col, lines, lp, npts, world):
+    """The workload's `config` object, the same in both arms."""
+    return {"workload": WORKLOAD, "layers": col.nlay, "lines": lines.n, "layer_points_per_step": int(lp),
+            "radiance_points": int(npts), "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2, no flush"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -524,8 +560,8 @@ def main():
     ap.add_argument("--no-jac", action="store_true", help="skip the Jacobian leg (600-1100 cm-1)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-profiles leg (256 profiles)")
     ap.add_argument("--no-config4", action="store_true", help="skip the broadband leg (3 M lines, 100 layers)")
-    ap.add_argument("--broadband-fp64-jacobians", action="store_true",
-                    help="also time the broadband Jacobians in FP64 (about half a minute more)")
+    ap.add_argument("--no-broadband-fp64-jacobians", action="store_true",
+                    help="skip the FP64 timing of the broadband Jacobians (about 20 s)")
     ap.add_argument("--profile-layer", type=int, default=None,
                     help="profiling case: the OD of this one layer of the column, three calls, no JSON line")
     ap.add_argument("--window", type=float, nargs=2, default=(1000.0, 1200.0),
@@ -556,24 +592,26 @@ def main():
         from oracle import oracle as O
         O.build()
         threads = os.cpu_count() or 1
-        # each step: the reference path on the sample column (all host threads)
+        pctrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN)
+        lp = layer_points_host(col, ctrl)
+        # each step: the reference path on the whole column, all host threads
+        # (one warm-up step: the CPU path has no state to warm)
         for _ in range(min(args.warmup, 1)):
-            run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), threads, REF_LAYERS)
+            run_cpu(lines, col, cont, pctrl, threads)
         times = []
-        sub = None
+        rad = None
         for _ in range(args.steps):
-            sub, dt = run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), threads, REF_LAYERS)
+            _, dt, rad = run_cpu(lines, col, cont, pctrl, threads)
             times.append(dt)
-        pts = sample_points(sub, ctrl)
-        v = pts / float(np.mean(times))
+        v = lp / float(np.mean(times))
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded)",
-                "config": {"workload": WORKLOAD, "sample": "layers %d-%d of the column" % (REF_LAYERS[0], REF_LAYERS[-1])},
+                "data": "synthetic (seeded, workload distributions)",
+                "config": config_of(col, lines, lp, len(rad), world),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": "layers %d-%d of the 60-layer column, full 500-2500 cm-1, OpenMP over layers"
-                                           % (REF_LAYERS[0], REF_LAYERS[-1])},
+                                 "sample": "the whole 60-layer column, 500-2500 cm-1, every step: layer ODs "
+                                           "OpenMP-parallel over layers, the merge's per-point loops OpenMP-parallel"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -655,14 +693,27 @@ def main():
         plain["max_rel_rad_diff_mixed_vs_plain"] = float(((rad_dev - r64).abs() / r64.abs()).max().item())
 
     cpu = None
+    oracle_err = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         O.build()
-        sub, dt = run_cpu(lines, col, cont, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), 1)
-        pts = sample_points(sub, ctrl)
-        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "layers %d-%d of the column, full 500-2500 cm-1, one thread (%.1f s)"
-                         % (CPU_LAYERS[0], CPU_LAYERS[-1], dt)}
+        threads = os.cpu_count() or 1
+        pctrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN)
+        _, dt_all, rad_ref = run_cpu(lines, col, cont, pctrl, threads)
+        sub, dt1, _ = run_cpu(lines, col, cont, pctrl, 1, CPU_LAYERS)
+        pts1 = layer_points_host(sub, ctrl)
+        cpu = {"value": lp / dt_all, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "the whole 60-layer column, 500-2500 cm-1, once (%.1f s; layer ODs OpenMP-parallel over "
+                         "layers, the merge's per-point loops OpenMP-parallel)" % dt_all,
+               "single_core": {"value": pts1 / dt1, "unit": UNIT, "cores": 1,
+                               "sample": "layers %d-%d of the column, full 500-2500 cm-1, one thread (%.1f s)"
+                                         % (CPU_LAYERS[0], CPU_LAYERS[-1], dt1)}}
+        # every radiance of this run against the FP64 oracle's, whole column
+        oracle_err = {"mixed": rel_err(rad_dev.cpu().numpy(), rad_ref),
+                      "plain_fp64": rel_err(r64.cpu().numpy(), rad_ref) if plain is not None else None,
+                      "e2e_mixed": rel_err(rad_host, rad_ref),
+                      "what": "max over the 5.5 M radiance points of |GPU - oracle| / |oracle|, whole column; "
+                              "bounds 1e-4 (mixed) and 1e-8 (FP64)"}
 
     jacl = None
     if not args.no_jac:
@@ -672,17 +723,15 @@ def main():
         batl = batch_leg(cont, 1)
     c4 = None
     if not args.no_config4:
-        c4 = config4_leg(2, fp64_jacobians=args.broadband_fp64_jacobians)
+        c4 = config4_leg(2, fp64_jacobians=not args.no_broadband_fp64_jacobians)
     roof = roofline(work, kt, args.steps, ms, lp)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32 (mixed: FP32 line shape + Kahan, FP64 index math)",
                 "data": "synthetic (seeded, workload distributions)",
-                "config": {"workload": WORKLOAD, "layers": col.nlay, "lines": lines.n,
-                           "layer_points_per_step": lp, "radiance_points": npts,
-                           "parallelism": "replicas" if world > 1 else "single GPU",
-                           "l2": "inputs larger than L2, no flush"},
+                "config": config_of(col, lines, lp, npts, world),
+                "max_rel_err_vs_oracle": oracle_err,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": e2e_ms},
                 "plain_fp64": plain, "jacobians": jacl, "batched_profiles": batl, "broadband": c4, "cpu_baseline": cpu, "roofline": roof,

@@ -23,7 +23,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
-           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts")
+           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts", "clblm_gpu_od_lines")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -60,6 +60,8 @@ def lib():
         L.clblm_gpu_od.argtypes = [C.c_void_p, P(T.clblm_layer_t), P(T.clblm_grid_t), P(T.clblm_od_ctrl_t),
                                    C.c_void_p, C.c_int64, C.c_int32]
         L.clblm_gpu_od_stats.argtypes = [C.c_void_p, P(T.clblm_od_stats_t)]
+        L.clblm_gpu_od_lines.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_int32), C.c_int64,
+                                         P(C.c_int64)] + [P(C.c_double)] * 4 + [P(C.c_int32), C.c_int64]
         L.clblm_gpu_rt_mode2_size.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t),
                                               P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), C.c_void_p,
@@ -147,6 +149,27 @@ class Handle:
         """Layer OD written to a device buffer (e.g. torch tensor data_ptr())."""
         self._check(lib().clblm_gpu_od(self.h, C.byref(layer), C.byref(grid), C.byref(ctrl), C.c_void_p(dptr),
                                        cap, T.CLBLM_OUT_DEVICE))
+
+    def od_lines(self):
+        """Line selection of the last odlay call (clblm_gpu_od_lines): dict of
+        line_lo, line_panel [n_lines] (panel that convolved each line of the
+        window, -1 rejected) and the far-wing pseudo-lines shr_vnu, shr_sp,
+        shr_alfl, shr_alfd, shr_mol in TAPE9 order."""
+        lo, nl, ns = C.c_int64(), C.c_int64(), C.c_int64()
+        z = C.c_int64(0)
+        self._check(lib().clblm_gpu_od_lines(self.h, C.byref(lo), C.byref(nl), None, 0, C.byref(ns), None, None, None,
+                                             None, None, 0))
+        n, m = nl.value, ns.value
+        out = {"line_lo": lo.value, "line_panel": np.zeros(n, dtype=np.int32)}
+        for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd"):
+            out[k] = np.zeros(m)
+        out["shr_mol"] = np.zeros(m, dtype=np.int32)
+        i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        self._check(lib().clblm_gpu_od_lines(self.h, C.byref(lo), C.byref(nl), i32(out["line_panel"]), n,
+                                             C.byref(ns), _dp(out["shr_vnu"]), _dp(out["shr_sp"]),
+                                             _dp(out["shr_alfl"]), _dp(out["shr_alfd"]), i32(out["shr_mol"]), m))
+        del z
+        return out
 
     def stats(self):
         s = T.clblm_od_stats_t()

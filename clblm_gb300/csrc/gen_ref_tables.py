@@ -28,7 +28,7 @@ Tables extracted (reference file:line):
     points from 4325 cm-1)
 
 Run (in a tree where the reference is mounted):
-    python clblm_gb300/csrc/gen_ref_tables.py /root/reference > clblm_gb300/csrc/clblm_ref_tables.h
+    python clblm_gb300/csrc/gen_ref_tables.py <CLBLM source root> > clblm_gb300/csrc/clblm_ref_tables.h
 The generated header is committed; the build never needs the reference.
 """
 import re
@@ -165,4 +165,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_ref_tables.py <CLBLM source root>  (the directory holding src/)")
+    main(sys.argv[1])

@@ -153,7 +153,14 @@ struct clblm_handle {
   int64_t acc_fnq = 0, acc_f4q = 0;
   double acc_ms_panel = 0., acc_ms_f4 = 0., acc_ms_line_chain = 0., acc_ms_f4_chain = 0., acc_ms_rt = 0.;
   int64_t acc_rt_bytes = 0;
+  // the last clblm_gpu_od call's layer in the workspace (clblm_gpu_od_lines)
+  struct {
+    bool valid = false;
+    bool plain = false;
+    int64_t lstride = 0, f4stride = 0, line_lo = 0, nlines = 0;
+  } last_od;
   void reset_call() {
+    last_od.valid = false;
     launches = 0;
     acc_fnq = acc_f4q = 0;
     acc_ms_panel = acc_ms_f4 = acc_ms_line_chain = acc_ms_f4_chain = acc_ms_rt = 0.;
@@ -1647,6 +1654,11 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
   if (rc) return rc;
   const LayerPlan& P = hps[0].P;
   int64_t n = hps[0].n_out;
+  h->last_od.plain = plain;
+  h->last_od.lstride = ls;
+  h->last_od.f4stride = fs;
+  h->last_od.line_lo = P.line_lo;
+  h->last_od.nlines = P.line_hi >= P.line_lo ? P.line_hi - P.line_lo + 1 : 0;
   double* dst = out;
   if (flags != CLBLM_OUT_DEVICE) {
     CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * n));
@@ -1664,7 +1676,50 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
     CUDA_TRY(h, cudaMemcpyAsync(out, dst, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
   rc = check_batch(h, hps, 0, 1, &h->last);
   h->last.launches = h->launches;
+  h->last_od.valid = rc == CLBLM_OK;
   return rc;
+}
+
+int clblm_gpu_od_lines(clblm_handle_t* h, int64_t* line_lo, int64_t* n_lines, int32_t* line_panel, int64_t line_cap,
+                       int64_t* n_shrunk, double* shr_vnu, double* shr_sp, double* shr_alfl, double* shr_alfd,
+                       int32_t* shr_mol, int64_t shr_cap) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!h->last_od.valid) return set_err(h, CLBLM_ERR_ARG, "no clblm_gpu_od call to report on");
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  const int64_t n = h->last_od.nlines;
+  int64_t nout[2];
+  CUDA_TRY(h, cudaMemcpy(nout, h->f4nout.p, sizeof nout, cudaMemcpyDeviceToHost));
+  const int64_t nsh = nout[1];
+  if (line_lo) *line_lo = h->last_od.line_lo;
+  if (n_lines) *n_lines = n;
+  if (n_shrunk) *n_shrunk = nsh;
+  if (line_panel) {
+    if (line_cap < n) return set_err(h, CLBLM_ERR_CAPACITY, "line panels need %lld entries", (long long)n);
+    std::vector<LinePrep> prep(n);
+    std::vector<int> q(n);
+    int npanels = h->last.npanels > 0 ? (int)h->last.npanels : 0;
+    if (n) {
+      CUDA_TRY(h, cudaMemcpy(prep.data(), h->prep.p, sizeof(LinePrep) * n, cudaMemcpyDeviceToHost));
+      CUDA_TRY(h, cudaMemcpy(q.data(), h->qpanel.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    }
+    // convolved in panel q when LNCORQ kept it and its deferral stays within
+    // the layer's panels (the rule k_line_records applies)
+    for (int64_t i = 0; i < n; ++i) line_panel[i] = (prep[i].fpanel >= 0 && q[i] < npanels) ? q[i] : -1;
+  }
+  if (shr_vnu || shr_sp || shr_alfl || shr_alfd || shr_mol) {
+    if (shr_cap < nsh) return set_err(h, CLBLM_ERR_CAPACITY, "far-wing lines need %lld entries", (long long)nsh);
+    std::vector<ShrunkLine> sh(nsh);
+    if (nsh) CUDA_TRY(h, cudaMemcpy(sh.data(), h->f4sh.p, sizeof(ShrunkLine) * nsh, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < nsh; ++i) {
+      const ShrunkLine& L = sh[i];
+      if (shr_vnu) shr_vnu[i] = L.vnu;
+      if (shr_sp) shr_sp[i] = h->last_od.plain ? L.sp : (double)L.w.f[2];
+      if (shr_alfl) shr_alfl[i] = h->last_od.plain ? L.w.d[0] : (double)L.w.f[0];
+      if (shr_alfd) shr_alfd[i] = h->last_od.plain ? L.w.d[1] : (double)L.w.f[1];
+      if (shr_mol) shr_mol[i] = L.mol;
+    }
+  }
+  return CLBLM_OK;
 }
 
 int clblm_gpu_od_stats(const clblm_handle_t* h, clblm_od_stats_t* stats) {

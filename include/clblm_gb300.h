@@ -266,6 +266,25 @@ void *clblm_gpu_stream(const clblm_handle_t *h);
 /* Counters of the last clblm_gpu_od (or of the last layer of clblm_gpu_rt_mode2). */
 int clblm_gpu_od_stats(const clblm_handle_t *h, clblm_od_stats_t *stats);
 
+/* Line selection of the last clblm_gpu_od call, as the reference's own
+ * bookkeeping holds it:
+ *  - per line of the layer's line window [*line_lo, *line_lo + *n_lines)
+ *    (indices of the line list), the 0-based panel whose CNVFNQ pass
+ *    convolved it, -1 when LNCORQ rejected it (RDLIN's record window and
+ *    LNCORQ's selection, clblm_ODLAY.f90:2624-2696 and 1566-2041; a line
+ *    that does not fit panel p's MAX1 is deferred to the next one, CNVFNQ
+ *    :2135-2140);
+ *  - the far-wing pseudo-lines SHRINQ writes to TAPE9
+ *    (clblm_ODLAY_LineF4.f90:1516-1647), in file order: centre, strength,
+ *    Lorentz and Doppler half widths, molecule flag (2: CO2, else 0).
+ * Output pointers may be NULL (the counts alone); line_cap and shr_cap are
+ * their capacities.  Refused (CLBLM_ERR_ARG) when the handle's last call was
+ * not a successful clblm_gpu_od. */
+int clblm_gpu_od_lines(clblm_handle_t *h, int64_t *line_lo, int64_t *n_lines,
+                       int32_t *line_panel, int64_t line_cap, int64_t *n_shrunk,
+                       double *shr_vnu, double *shr_sp, double *shr_alfl,
+                       double *shr_alfd, int32_t *shr_mol, int64_t shr_cap);
+
 /* Size of the nadir upwelling radiance spectrum of a column: the final merge
  * grid of mode2_lookDn_mergeUp. */
 int clblm_gpu_rt_mode2_size(clblm_handle_t *h, const clblm_column_t *col,

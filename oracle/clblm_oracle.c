@@ -62,6 +62,12 @@ struct ocl_session {
   int interp_ready;
   double IA1[203], IA2[203], IA3[203], IA4[203];
   char err[256];
+  /* line bookkeeping of the next ocl_odlay call (ocl_set_trace): the panel
+   * whose CNVFNQ pass convolved each line, and the TAPE9 pseudo-lines */
+  int32_t *tr_panel;
+  double *tr_vnu, *tr_sp, *tr_alfl, *tr_alfd;
+  int32_t *tr_mol;
+  int64_t tr_cap, *tr_nshr;
 };
 
 static int fail(ocl_session *s, int code, const char *fmt, ...) {
@@ -1188,8 +1194,10 @@ static int hiracq(ocl_session *s, hirac_args *a) {
   double PAVP0 = PAVE / P0;
   double PAVP2 = PAVP0 * PAVP0;
 
-  /* RDLIN state */
-  int64_t rec = 0;
+  /* RDLIN state; bufb: line-list index of the buffer's first line, panel_no:
+   * panels written so far (the trace) */
+  int64_t rec = 0, bufb = 0;
+  int panel_no = 0;
   int IEOF = 0, ILO = 0, IHI = -999, IDATA = 0, IPANEL = 0;
   int ISTOP = 0;
 
@@ -1208,6 +1216,7 @@ static int hiracq(ocl_session *s, hirac_args *a) {
       int64_t b = rec_first(rec), e = rec_end(a->F, rec);
       int NREC = (int)(e - b);
       double VMIN = L->vnu[b];
+      bufb = b;
       rec++;
       for (int i = 1; i <= NREC; ++i) {
         int64_t k = b + i - 1;
@@ -1350,6 +1359,7 @@ static int hiracq(ocl_session *s, hirac_args *a) {
             IPANEL = 1;
             goto L40;
           }
+          if (s->tr_panel) s->tr_panel[bufb + I - 1] = panel_no;
           int JMIN1 = (int)(ZINT - BHWDXF + 1.5);
           double RSHFT = 0.5;
           if (ZINT < 0.0) RSHFT = -RSHFT;
@@ -1485,6 +1495,7 @@ static int hiracq(ocl_session *s, hirac_args *a) {
       }
       a->numTotPoints += NLIM;
       if (a->st) a->st->npanels++;
+      panel_no++;
       VFT = VFT + (double)(NLIM1 - 1) * DV;
       if (ISTOP != 1) {
         for (int jj = NLIM1; jj <= MAX1; ++jj) R1[jj - NLIM1 + 1] = R1[jj];
@@ -1713,17 +1724,41 @@ static int sticky_jrad(ocl_session *s, const clblm_layer_t *lay, const clblm_gri
   return s->jrad;
 }
 
-int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
-              const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, double *out, int64_t cap, int64_t *nsamp,
-              double *dv_used, clblm_od_stats_t *st) {
-  if (!s || !L || !lay || !g || !ctrl) return CLBLM_ERR_ARG;
+static int odlay_checked(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
+                         const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, double *out, int64_t cap,
+                         int64_t *nsamp, double *dv_used, clblm_od_stats_t *st) {
+  if (!L || !lay || !g || !ctrl) return CLBLM_ERR_ARG;
   s->err[0] = 0;
   double DV, ALFAV;
   if (od_grid(g, &DV, &ALFAV)) return fail(s, CLBLM_ERR_GRID, "bad grid");
   for (int64_t i = 1; i < L->n; ++i)
     if (L->vnu[i] < L->vnu[i - 1]) return fail(s, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
   int JRAD = sticky_jrad(s, lay, g, ctrl);
+  if (s->tr_panel)
+    for (int64_t i = 0; i < L->n; ++i) s->tr_panel[i] = -1;
   return odlay_core(s, L, C, lay, g, ctrl, JRAD, out, cap, nsamp, dv_used, st);
+}
+
+int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
+              const clblm_grid_t *g, const clblm_od_ctrl_t *ctrl, double *out, int64_t cap, int64_t *nsamp,
+              double *dv_used, clblm_od_stats_t *st) {
+  if (!s) return CLBLM_ERR_ARG;
+  int rc = odlay_checked(s, L, C, lay, g, ctrl, out, cap, nsamp, dv_used, st);
+  s->tr_panel = NULL; /* the trace covers one call only */
+  s->tr_nshr = NULL;
+  return rc;
+}
+
+void ocl_set_trace(ocl_session *s, int32_t *line_panel, double *shr_vnu, double *shr_sp, double *shr_alfl,
+                   double *shr_alfd, int32_t *shr_mol, int64_t shr_cap, int64_t *n_shr) {
+  s->tr_panel = line_panel;
+  s->tr_vnu = shr_vnu;
+  s->tr_sp = shr_sp;
+  s->tr_alfl = shr_alfl;
+  s->tr_alfd = shr_alfd;
+  s->tr_mol = shr_mol;
+  s->tr_cap = shr_cap;
+  s->tr_nshr = n_shr;
 }
 
 static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, const clblm_layer_t *lay,
@@ -1792,6 +1827,19 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
     return rc;
   }
   stl.nshrunk = T9.nlines;
+  if (s->tr_nshr) { /* the TAPE9 pseudo-lines, in file order */
+    int64_t k = 0;
+    for (int r = 0; r < T9.nrec; ++r)
+      for (int i = 1; i <= T9.rec[r].n; ++i, ++k) {
+        if (k >= s->tr_cap) continue;
+        s->tr_vnu[k] = T9.rec[r].VNU[i];
+        s->tr_sp[k] = T9.rec[r].SP[i];
+        s->tr_alfl[k] = T9.rec[r].ALFA[i];
+        s->tr_alfd[k] = T9.rec[r].EPP[i];
+        s->tr_mol[k] = T9.rec[r].MOL[i];
+      }
+    *s->tr_nshr = k;
+  }
 
   /* size of the output, then HIRACQ */
   int64_t sizeOfBuffer = (int64_t)ceil((V2 - V1) / DV + 1.);
@@ -1981,8 +2029,10 @@ void ocl_rlin(double od, double *hlf) {
 }
 
 static void layer_emis(double *em, double Ta, double Tb, double Tave, const double *tx, const double *od,
-                       int linInTau, double V1, double DV, int64_t n) {
+                       int linInTau, double V1, double DV, int64_t n, int nthreads) {
   double XKTA = Ta / RADCN2, XKTB = Tb / RADCN2, XKT = Tave / RADCN2;
+  /* every point on its own: the same values whatever the thread count */
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
   for (int64_t ip = 1; ip <= n; ++ip) {
     double odvi = od[ip - 1];
     double abso = 1 - tx[ip - 1];
@@ -2090,8 +2140,11 @@ static int rt_mode2_impl(ocl_session *s, const clblm_lines_t *L, const clblm_con
   }
   ensure_tables(s);
   interp_coef(s);
+  /* the upper layers (finest grids, most points) first, so that the largest
+   * ODs do not start last */
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
-  for (int il = 0; il < n; ++il) {
+  for (int k = 0; k < n; ++k) {
+    const int il = n - 1 - k;
     ocl_session loc = *s; /* tables and coefficients are read-only from here */
     int64_t capn = (int64_t)ceil((V2 - V1) / (dvn[il] < dvf[il] ? dvn[il] : dvf[il]) + 16.);
     ods[il] = (double *)malloc(sizeof(double) * (size_t)capn);
@@ -2124,6 +2177,7 @@ static int rt_mode2_impl(ocl_session *s, const clblm_lines_t *L, const clblm_con
     spect_set(&EU, V1, dvl, ns);
     spect_set(&ED, V1, dvl, ns);
     double *odA = (double *)malloc(sizeof(double) * (size_t)ns), *odB = (double *)malloc(sizeof(double) * (size_t)ns);
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
     for (int64_t k = 0; k < ns; ++k) {
       odA[k] = od[k] * scalUp;
       odA[k] = odA[k] * 1.0;
@@ -2132,9 +2186,11 @@ static int rt_mode2_impl(ocl_session *s, const clblm_lines_t *L, const clblm_con
       TA.v[k] = exp(-odA[k]);
       TB.v[k] = exp(-odB[k]);
     }
-    layer_emis(ED.v, col->tbot[il], col->ttop[il], col->tave[il], TB.v, odB, ctrl->lin_in_tau, V1, dvl, ns);
+    layer_emis(ED.v, col->tbot[il], col->ttop[il], col->tave[il], TB.v, odB, ctrl->lin_in_tau, V1, dvl, ns,
+               nthreads);
     if (ctrl->lin_in_tau != 0)
-      layer_emis(EU.v, col->ttop[il], col->tbot[il], col->tave[il], TA.v, odA, ctrl->lin_in_tau, V1, dvl, ns);
+      layer_emis(EU.v, col->ttop[il], col->tbot[il], col->tave[il], TA.v, odA, ctrl->lin_in_tau, V1, dvl, ns,
+                 nthreads);
     else
       memcpy(EU.v, ED.v, sizeof(double) * (size_t)ns);
     free(odA);
@@ -2142,8 +2198,11 @@ static int rt_mode2_impl(ocl_session *s, const clblm_lines_t *L, const clblm_con
     spect_t *arr[6] = {&R, &Rf, &TA, &TB, &EU, &ED};
     rc = to_finest(s, arr, 6);
     if (rc) break;
-    for (int64_t k = 0; k < R.n; ++k) R.v[k] = EU.v[k] + TA.v[k] * (R.v[k] + ED.v[k] * Rf.v[k]);
-    for (int64_t k = 0; k < Rf.n; ++k) Rf.v[k] = TA.v[k] * TB.v[k] * Rf.v[k];
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t k = 0; k < R.n; ++k) {
+      R.v[k] = EU.v[k] + TA.v[k] * (R.v[k] + ED.v[k] * Rf.v[k]);
+      Rf.v[k] = TA.v[k] * TB.v[k] * Rf.v[k];
+    }
   }
   if (!rc) {
     if (npts) *npts = R.n;

@@ -112,3 +112,67 @@ def test_od_from_tape3_file_is_identical(gpu_lib, tmp_path):
     h1.close()
     h2.close()
     assert np.array_equal(a, b)
+
+
+def _selection(gpu_lib, oracle_mod, lines, col, cont, precision, contnm_off=0):
+    """OD, the per-line panel of every line of the layer's window and the
+    far-wing pseudo-lines, from the library and the oracle."""
+    dn, df, _ = gpu_lib.setDV(col)
+    lay = col.layer(0)
+    g = T.grid_struct(col.v1, col.v2, dn[0], df[0])
+    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off)
+    h = gpu_lib.Handle(lines, cont)
+    try:
+        od, dv = h.odlay(lay, g, ctrl)
+        sel = h.od_lines()
+    finally:
+        h.close()
+    ref, dvr, sr, tr = oracle_mod.Session().odlay_trace(lines, lay, g, ctrl, cont)
+    return od, ref, sel, tr, sr
+
+
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+@pytest.mark.parametrize("case", ["config0", "config1_top", "config1_surface", "config4_lowest"])
+def test_line_selection_bit_exact(gpu_lib, oracle_mod, case, precision):
+    """Line selection and panel index ranges equal the reference's bookkeeping
+    line by line: every line of the window is convolved in the same panel (or
+    rejected by both), so each panel's line range is the same; the far-wing
+    pseudo-lines SHRINQ forms are the same lines in the same order (FP64 path:
+    bit for bit; mixed: the same groups, whose binary64 centres agree to
+    1e-12 and whose FP32 strengths and widths agree to 1e-6)."""
+    if case == "config0":
+        lines, col = synth.config0()
+        cont = None
+        contnm_off = 1
+    elif case.startswith("config1"):
+        lines, col, cont = synth.config1(n_lines=100000)
+        col = col.sub([59 if case.endswith("top") else 0]).with_window(1000.0, 1100.0)
+        contnm_off = 0
+    else:  # the lowest layer of the broadband column at 10-60 cm-1: far-wing mirror lines
+        lines, col, cont = synth.config4(n_lines=300000)
+        col = col.sub([0]).with_window(10.0, 60.0)
+        contnm_off = 0
+    od, ref, sel, tr, sr = _selection(gpu_lib, oracle_mod, lines, col, cont, precision, contnm_off)
+    lo, lp = sel["line_lo"], sel["line_panel"]
+    want = tr["line_panel"]
+    assert np.array_equal(lp, want[lo:lo + len(lp)])
+    assert np.all(want[:lo] == -1) and np.all(want[lo + len(lp):] == -1)
+    assert (lp >= 0).sum() == sr["lincnt"]
+    # per-panel line ranges follow: first and last line of each panel
+    for q in range(int(sr["npanels"])):
+        idx = np.nonzero(lp == q)[0]
+        widx = np.nonzero(want == q)[0]
+        assert len(idx) == len(widx)
+        if len(idx):
+            assert idx[0] + lo == widx[0] and idx[-1] + lo == widx[-1]
+    assert len(sel["shr_vnu"]) == len(tr["shr_vnu"]) == sr["nshrunk"]
+    assert np.array_equal(sel["shr_mol"], tr["shr_mol"])
+    if precision == T.CLBLM_PREC_PLAIN:
+        for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd"):
+            assert np.array_equal(sel[k], tr[k]), k
+    else:
+        np.testing.assert_allclose(sel["shr_vnu"], tr["shr_vnu"], rtol=1e-12, atol=0)
+        for k in ("shr_sp", "shr_alfl", "shr_alfd"):
+            np.testing.assert_allclose(sel[k], tr[k], rtol=1e-6, atol=0)
+    tol = 1e-9 if precision == T.CLBLM_PREC_PLAIN else 1e-5
+    assert np.max(np.abs(od - ref) / np.abs(ref)) <= tol

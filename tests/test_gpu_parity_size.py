@@ -1,0 +1,148 @@
+"""Parity at the workloads' own sizes: the GPU path against the FP64 oracle
+on full-width sub-columns and whole spectral windows, not on slices.
+
+  * the 60-layer column (500,000 lines): full 500-2500 cm-1 radiance of the
+    ten uppermost layers (the finest grids, 5.4 M points) and of twelve
+    middle layers;
+  * the Jacobian workload: radiance and level T / ln q(H2O) Jacobians over
+    the whole 600-1100 cm-1 window (the 120,000 lines there) on six layers
+    at the bottom and six at the top of the column;
+  * a dozen of the 256 batched profiles (every 21st), each through
+    clblm_gpu_batch, against the oracle's noScattJacob;
+  * the broadband column (3,000,000 lines): the three lowest layers at
+    10-60 cm-1, where the far-wing mirror lines of CNVF4Q are active.
+
+Bounds: radiance 1e-4 relative per point (mixed) and 1e-8 (FP64).
+Jacobians, per point: |got - want| <= JAC_RTOL |want| + JAC_ATOL * max|want|
+over the level's own spectrum.  The mixed path forms dtau/dT as the
+reference does, tau(T+1) - tau(T) - (Wtot/T) [tau(1.01 W) - tau(W)] / 0.01,
+a difference of FP32-compensated ODs whose relative error is eps <= 1e-6:
+its absolute error is about 2 eps tau (1 + 100/T) < 3 eps tau, against a
+typical |dtau/dT| of 1e-2 tau, so 3e-4 of the derivative where it is
+typical (JAC_RTOL 1e-3 leaves room for the chain rule's sums) and, where
+dtau/dT crosses zero inside a line, 3 eps tau |dR/dtau| absolute, which is
+about 3e-4 of the level's largest Jacobian (JAC_ATOL).  FP64: 1e-9 and
+1e-10.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from clblm_gb300 import capi_types as T
+from clblm_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+JAC_TOL = {T.CLBLM_PREC_MIXED: (1e-3, 3e-4), T.CLBLM_PREC_PLAIN: (1e-9, 1e-10)}
+RAD_TOL = {T.CLBLM_PREC_MIXED: 1e-4, T.CLBLM_PREC_PLAIN: 1e-8}
+
+
+def _rad_err(got, want):
+    assert got.shape == want.shape
+    return float(np.max(np.abs(got - want) / np.abs(want)))
+
+
+def _jac_check(got, want, precision, what):
+    """The per-point bound of the module docstring, level by level; levels
+    that are not finite in the oracle (level2layer's log ratio of equal
+    mixing ratios) must be non-finite in both."""
+    rt, at = JAC_TOL[precision]
+    g2, w2 = np.atleast_2d(got), np.atleast_2d(want)
+    assert g2.shape == w2.shape, what
+    worst = 0.0
+    for lev in range(w2.shape[0]):
+        w, g = w2[lev], g2[lev]
+        if not np.all(np.isfinite(w)):
+            assert not np.all(np.isfinite(g)), (what, lev)
+            continue
+        scale = np.max(np.abs(w))
+        excess = np.abs(g - w) / (rt * np.abs(w) + at * scale + 1e-300)
+        worst = max(worst, float(np.max(excess)))
+    assert worst <= 1.0, (what, worst)
+    return worst
+
+
+@pytest.fixture(scope="module")
+def config1():
+    return synth.config1()
+
+
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+@pytest.mark.parametrize("layers", [(50, 60), (20, 32)])
+def test_config1_radiance_full_width(gpu_lib, oracle_mod, config1, precision, layers):
+    lines, col, cont = config1
+    sub = col.sub(list(range(*layers)))
+    ctrl = T.rt_ctrl(precision=precision)
+    h = gpu_lib.Handle(lines, cont)
+    try:
+        got, dv = h.rt_mode2(sub, ctrl)
+    finally:
+        h.close()
+    want, dvw = oracle_mod.Session().rt_mode2(lines, sub, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), cont,
+                                             nthreads=THREADS)
+    assert dv == dvw and len(got) == len(want) > 1_000_000
+    err = _rad_err(got, want)
+    assert err <= RAD_TOL[precision], err
+
+
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+@pytest.mark.parametrize("first", [0, 54])
+def test_config2_jacobians_whole_window(gpu_lib, oracle_mod, config1, precision, first):
+    lines, col, cont = config1
+    lines = lines.window(600.0, 1100.0)
+    full = col.with_window(600.0, 1100.0)
+    sub = full.sub(list(range(first, first + 6)))
+    prof = synth.jac_profile(full).sub(first, 6)
+    ctrl = T.rt_ctrl(precision=precision, grid_type=1)
+    h = gpu_lib.Handle(lines, cont)
+    try:
+        got = h.jac(sub, ctrl, prof)
+    finally:
+        h.close()
+    want = oracle_mod.jac_mode2(oracle_mod.Session(), lines, sub, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN,
+                                                                            grid_type=1), prof, cont,
+                                nthreads=THREADS)
+    assert got["dv"] == want["dv"] and len(got["rad"]) == len(want["rad"]) > 100_000
+    assert _rad_err(got["rad"], want["rad"]) <= RAD_TOL[precision]
+    for k in ("dtlev", "dqlev", "dtsfc", "demis"):
+        _jac_check(got[k], want[k], precision, k)
+
+
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+def test_config3_dozen_profiles(gpu_lib, oracle_mod, precision):
+    lines, cont, cols, jacs = synth.config3()
+    ctrl = T.rt_ctrl(precision=precision, grid_type=1)
+    octrl = T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN, grid_type=1)
+    for i in range(0, 252, 21):
+        # a handle per profile, as the oracle starts a fresh process per
+        # profile (the sticky JRAD would otherwise run from profile to profile)
+        h = gpu_lib.Handle(lines, cont)
+        try:
+            got = h.batch([cols[i]], ctrl, [jacs[i]])[0]
+        finally:
+            h.close()
+        want = oracle_mod.jac_mode2(oracle_mod.Session(), lines, cols[i], octrl, jacs[i], cont, nthreads=THREADS)
+        assert got["dv"] == want["dv"] and len(got["rad"]) == len(want["rad"]), i
+        err = _rad_err(got["rad"], want["rad"])
+        assert err <= RAD_TOL[precision], (i, err)
+        for k in ("dtlev", "dqlev", "dtsfc", "demis"):
+            _jac_check(got[k], want[k], precision, (i, k))
+
+
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+def test_config4_lowest_layers_far_wing_mirror(gpu_lib, oracle_mod, precision):
+    lines, col, cont = synth.config4()
+    sub = col.sub([0, 1, 2]).with_window(10.0, 60.0)
+    ctrl = T.rt_ctrl(precision=precision)
+    h = gpu_lib.Handle(lines, cont)
+    try:
+        got, dv = h.rt_mode2(sub, ctrl)
+    finally:
+        h.close()
+    want, dvw = oracle_mod.Session().rt_mode2(lines, sub, T.rt_ctrl(precision=T.CLBLM_PREC_PLAIN), cont,
+                                             nthreads=THREADS)
+    assert dv == dvw and len(got) == len(want)
+    err = _rad_err(got, want)
+    assert err <= RAD_TOL[precision], err
