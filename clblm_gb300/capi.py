@@ -61,7 +61,8 @@ def lib():
                                    C.c_void_p, C.c_int64, C.c_int32]
         L.clblm_gpu_od_stats.argtypes = [C.c_void_p, P(T.clblm_od_stats_t)]
         L.clblm_gpu_od_lines.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_int32), C.c_int64,
-                                         P(C.c_int64)] + [P(C.c_double)] * 4 + [P(C.c_int32), C.c_int64]
+                                         P(C.c_int64)] + [P(C.c_double)] * 4 + [P(C.c_int32), P(C.c_int64),
+                                                                                 C.c_int64]
         L.clblm_gpu_rt_mode2_size.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t),
                                               P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), C.c_void_p,
@@ -156,19 +157,19 @@ class Handle:
         window, -1 rejected) and the far-wing pseudo-lines shr_vnu, shr_sp,
         shr_alfl, shr_alfd, shr_mol in TAPE9 order."""
         lo, nl, ns = C.c_int64(), C.c_int64(), C.c_int64()
-        z = C.c_int64(0)
         self._check(lib().clblm_gpu_od_lines(self.h, C.byref(lo), C.byref(nl), None, 0, C.byref(ns), None, None, None,
-                                             None, None, 0))
+                                             None, None, None, 0))
         n, m = nl.value, ns.value
         out = {"line_lo": lo.value, "line_panel": np.zeros(n, dtype=np.int32)}
         for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd"):
             out[k] = np.zeros(m)
         out["shr_mol"] = np.zeros(m, dtype=np.int32)
+        out["shr_last"] = np.zeros(m, dtype=np.int64)
         i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
         self._check(lib().clblm_gpu_od_lines(self.h, C.byref(lo), C.byref(nl), i32(out["line_panel"]), n,
                                              C.byref(ns), _dp(out["shr_vnu"]), _dp(out["shr_sp"]),
-                                             _dp(out["shr_alfl"]), _dp(out["shr_alfd"]), i32(out["shr_mol"]), m))
-        del z
+                                             _dp(out["shr_alfl"]), _dp(out["shr_alfd"]), i32(out["shr_mol"]),
+                                             out["shr_last"].ctypes.data_as(C.POINTER(C.c_int64)), m))
         return out
 
     def stats(self):

@@ -157,7 +157,7 @@ struct clblm_handle {
   struct {
     bool valid = false;
     bool plain = false;
-    int64_t lstride = 0, f4stride = 0, line_lo = 0, nlines = 0;
+    int64_t lstride = 0, f4stride = 0, line_lo = 0, nlines = 0, f4_lo = 0;
   } last_od;
   void reset_call() {
     last_od.valid = false;
@@ -1659,6 +1659,7 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
   h->last_od.f4stride = fs;
   h->last_od.line_lo = P.line_lo;
   h->last_od.nlines = P.line_hi >= P.line_lo ? P.line_hi - P.line_lo + 1 : 0;
+  h->last_od.f4_lo = P.f4_lo;
   double* dst = out;
   if (flags != CLBLM_OUT_DEVICE) {
     CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * n));
@@ -1682,7 +1683,7 @@ int clblm_gpu_od(clblm_handle_t* h, const clblm_layer_t* layer, const clblm_grid
 
 int clblm_gpu_od_lines(clblm_handle_t* h, int64_t* line_lo, int64_t* n_lines, int32_t* line_panel, int64_t line_cap,
                        int64_t* n_shrunk, double* shr_vnu, double* shr_sp, double* shr_alfl, double* shr_alfd,
-                       int32_t* shr_mol, int64_t shr_cap) {
+                       int32_t* shr_mol, int64_t* shr_last, int64_t shr_cap) {
   if (!h) return CLBLM_ERR_ARG;
   if (!h->last_od.valid) return set_err(h, CLBLM_ERR_ARG, "no clblm_gpu_od call to report on");
   if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
@@ -1706,7 +1707,7 @@ int clblm_gpu_od_lines(clblm_handle_t* h, int64_t* line_lo, int64_t* n_lines, in
     // the layer's panels (the rule k_line_records applies)
     for (int64_t i = 0; i < n; ++i) line_panel[i] = (prep[i].fpanel >= 0 && q[i] < npanels) ? q[i] : -1;
   }
-  if (shr_vnu || shr_sp || shr_alfl || shr_alfd || shr_mol) {
+  if (shr_vnu || shr_sp || shr_alfl || shr_alfd || shr_mol || shr_last) {
     if (shr_cap < nsh) return set_err(h, CLBLM_ERR_CAPACITY, "far-wing lines need %lld entries", (long long)nsh);
     std::vector<ShrunkLine> sh(nsh);
     if (nsh) CUDA_TRY(h, cudaMemcpy(sh.data(), h->f4sh.p, sizeof(ShrunkLine) * nsh, cudaMemcpyDeviceToHost));
@@ -1717,6 +1718,24 @@ int clblm_gpu_od_lines(clblm_handle_t* h, int64_t* line_lo, int64_t* n_lines, in
       if (shr_alfl) shr_alfl[i] = h->last_od.plain ? L.w.d[0] : (double)L.w.f[0];
       if (shr_alfd) shr_alfd[i] = h->last_od.plain ? L.w.d[1] : (double)L.w.f[1];
       if (shr_mol) shr_mol[i] = L.mol;
+    }
+    if (shr_last) {
+      // each group (first and last member in the compacted order, first
+      // output slot) gives its one or two pseudo-lines the line-list index
+      // of its last member
+      const int64_t ng = nout[0];
+      std::vector<int4> grp(ng > 0 ? ng : 0);
+      std::vector<int64_t> src(h->last_od.f4stride);
+      if (ng > 0) CUDA_TRY(h, cudaMemcpy(grp.data(), h->f4grp.p, sizeof(int4) * ng, cudaMemcpyDeviceToHost));
+      if (!src.empty())
+        CUDA_TRY(h, cudaMemcpy(src.data(), h->f4src.p, sizeof(int64_t) * src.size(), cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < nsh; ++i) shr_last[i] = -1;
+      for (int64_t g = 0; g < ng; ++g) {
+        const int64_t s0 = grp[g].z, s1 = g + 1 < ng ? grp[g + 1].z : nsh;
+        const int64_t u = grp[g].y;
+        const int64_t line = (u >= 0 && u < (int64_t)src.size()) ? h->last_od.f4_lo + src[u] : -1;
+        for (int64_t k = s0; k < s1 && k < nsh; ++k) shr_last[k] = line;
+      }
     }
   }
   return CLBLM_OK;

@@ -276,14 +276,17 @@ int clblm_gpu_od_stats(const clblm_handle_t *h, clblm_od_stats_t *stats);
  *    :2135-2140);
  *  - the far-wing pseudo-lines SHRINQ writes to TAPE9
  *    (clblm_ODLAY_LineF4.f90:1516-1647), in file order: centre, strength,
- *    Lorentz and Doppler half widths, molecule flag (2: CO2, else 0).
+ *    Lorentz and Doppler half widths, molecule flag (2: CO2, else 0), and
+ *    the line-list index of the last line of the group it was summed from
+ *    (which lines merge).
  * Output pointers may be NULL (the counts alone); line_cap and shr_cap are
  * their capacities.  Refused (CLBLM_ERR_ARG) when the handle's last call was
  * not a successful clblm_gpu_od. */
 int clblm_gpu_od_lines(clblm_handle_t *h, int64_t *line_lo, int64_t *n_lines,
                        int32_t *line_panel, int64_t line_cap, int64_t *n_shrunk,
                        double *shr_vnu, double *shr_sp, double *shr_alfl,
-                       double *shr_alfd, int32_t *shr_mol, int64_t shr_cap);
+                       double *shr_alfd, int32_t *shr_mol, int64_t *shr_last,
+                       int64_t shr_cap);
 
 /* Size of the nadir upwelling radiance spectrum of a column: the final merge
  * grid of mode2_lookDn_mergeUp. */

@@ -67,6 +67,7 @@ struct ocl_session {
   int32_t *tr_panel;
   double *tr_vnu, *tr_sp, *tr_alfl, *tr_alfd;
   int32_t *tr_mol;
+  int64_t *tr_last;
   int64_t tr_cap, *tr_nshr;
 };
 
@@ -715,6 +716,9 @@ typedef struct {
   int n;
   double VNU[SHR_MAX + 1], SP[SHR_MAX + 1], ALFA[SHR_MAX + 1], EPP[SHR_MAX + 1], SPP[SHR_MAX + 1];
   int MOL[SHR_MAX + 1];
+  /* bookkeeping for the trace: line-list index of each buffered line, and of
+   * the last line of the group each shrunk line was summed from */
+  int64_t IDX[SHR_MAX + 1], LAST[SHR_MAX + 1];
 } shrunk_rec;
 
 typedef struct {
@@ -752,6 +756,7 @@ static void shrinq(shrunk_rec *S, int *ILO, int *IHI, double DVR4) {
       S->EPP[J] = S->EPP[I];
       S->SPP[J] = S->SPP[I];
       S->MOL[J] = S->MOL[I];
+      S->LAST[J] = S->IDX[I];
       if (S->MOL[J] != 2) S->MOL[J] = 0;
       goto L10;
     }
@@ -781,6 +786,7 @@ static void shrinq(shrunk_rec *S, int *ILO, int *IHI, double DVR4) {
       S->VNU[J] = SUMV / SUMS;
       S->SPP[J] = SUMC;
       S->MOL[J] = 0;
+      S->LAST[J] = S->IDX[I];
       SUMAL = SUMAD = SUMS = SUMV = SUMC = 0.;
     }
     if (SUMS2 > 0.) {
@@ -790,6 +796,7 @@ static void shrinq(shrunk_rec *S, int *ILO, int *IHI, double DVR4) {
       S->EPP[J] = SUMAD2 / SUMS2;
       S->VNU[J] = SUMV2 / SUMS2;
       S->MOL[J] = 2;
+      S->LAST[J] = S->IDX[I];
       S->SPP[J] = SUMC2;
       SUMAL2 = SUMAD2 = SUMS2 = SUMV2 = SUMC2 = 0.;
     }
@@ -851,6 +858,7 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
         if (SUI == 0.) continue;
         if (L->vnu[i] < VLO) continue;
         IJ = IJ + 1;
+        S->IDX[IJ] = i;
         S->VNU[IJ] = L->vnu[i] + RHORAT * pshift;
         S->ALFA[IJ] = alfa;
         S->EPP[IJ] = (double)L->epp[i];
@@ -1750,8 +1758,9 @@ int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C, con
 }
 
 void ocl_set_trace(ocl_session *s, int32_t *line_panel, double *shr_vnu, double *shr_sp, double *shr_alfl,
-                   double *shr_alfd, int32_t *shr_mol, int64_t shr_cap, int64_t *n_shr) {
+                   double *shr_alfd, int32_t *shr_mol, int64_t *shr_last, int64_t shr_cap, int64_t *n_shr) {
   s->tr_panel = line_panel;
+  s->tr_last = shr_last;
   s->tr_vnu = shr_vnu;
   s->tr_sp = shr_sp;
   s->tr_alfl = shr_alfl;
@@ -1837,6 +1846,7 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
         s->tr_alfl[k] = T9.rec[r].ALFA[i];
         s->tr_alfd[k] = T9.rec[r].EPP[i];
         s->tr_mol[k] = T9.rec[r].MOL[i];
+        s->tr_last[k] = T9.rec[r].LAST[i];
       }
     *s->tr_nshr = k;
   }

@@ -42,10 +42,10 @@ int ocl_odlay(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,
  * per line of the list, the 0-based panel whose CNVFNQ pass convolved it
  * (-1: not read, or rejected by LNCORQ); shr_* (capacity shr_cap) get the
  * far-wing pseudo-lines SHRINQ wrote to TAPE9 in file order (centre,
- * strength, Lorentz and Doppler half widths, molecule flag), their count in
- * *n_shr.  NULL pointers: no trace. */
+ * strength, Lorentz and Doppler half widths, molecule flag, line-list index
+ * of the last line of the group), their count in *n_shr.  NULL pointers: no trace. */
 void ocl_set_trace(ocl_session *s, int32_t *line_panel, double *shr_vnu, double *shr_sp, double *shr_alfl,
-                   double *shr_alfd, int32_t *shr_mol, int64_t shr_cap, int64_t *n_shr);
+                   double *shr_alfd, int32_t *shr_mol, int64_t *shr_last, int64_t shr_cap, int64_t *n_shr);
 
 /* mode2_lookDn_mergeUp thermal nadir radiance. */
 int ocl_rt_mode2(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t *C,

@@ -46,8 +46,8 @@ def lib():
         L.ocl_odlay.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_layer_t),
                                 P(T.clblm_grid_t), P(T.clblm_od_ctrl_t), P(C.c_double), C.c_int64,
                                 P(C.c_int64), P(C.c_double), P(T.clblm_od_stats_t)]
-        L.ocl_set_trace.argtypes = [C.c_void_p, P(C.c_int32)] + [P(C.c_double)] * 4 + [P(C.c_int32), C.c_int64,
-                                                                                     P(C.c_int64)]
+        L.ocl_set_trace.argtypes = [C.c_void_p, P(C.c_int32)] + [P(C.c_double)] * 4 + [P(C.c_int32), P(C.c_int64),
+                                                                                     C.c_int64, P(C.c_int64)]
         L.ocl_rt_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
                                    P(T.clblm_rt_ctrl_t), P(C.c_double), C.c_int64, P(C.c_int64),
                                    P(C.c_double)]
@@ -129,16 +129,18 @@ class Session:
         none) and the TAPE9 pseudo-lines shr_vnu, shr_sp, shr_alfl, shr_alfd,
         shr_mol."""
         shr_cap = shr_cap or lines.n + 16
-        tr = {"line_panel": np.full(lines.n, -1, dtype=np.int32), "shr_mol": np.zeros(shr_cap, dtype=np.int32)}
+        tr = {"line_panel": np.full(lines.n, -1, dtype=np.int32), "shr_mol": np.zeros(shr_cap, dtype=np.int32),
+              "shr_last": np.zeros(shr_cap, dtype=np.int64)}
         for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd"):
             tr[k] = np.zeros(shr_cap)
         ns = C.c_int64()
         i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
         lib().ocl_set_trace(self.h, i32(tr["line_panel"]), _dp(tr["shr_vnu"]), _dp(tr["shr_sp"]),
-                            _dp(tr["shr_alfl"]), _dp(tr["shr_alfd"]), i32(tr["shr_mol"]), shr_cap, C.byref(ns))
+                            _dp(tr["shr_alfl"]), _dp(tr["shr_alfd"]), i32(tr["shr_mol"]),
+                            tr["shr_last"].ctypes.data_as(C.POINTER(C.c_int64)), shr_cap, C.byref(ns))
         od, dv, st = self.odlay(lines, layer, grid, ctrl, cont)
         m = ns.value
-        for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd", "shr_mol"):
+        for k in ("shr_vnu", "shr_sp", "shr_alfl", "shr_alfd", "shr_mol", "shr_last"):
             tr[k] = tr[k][:m].copy()
         return od, dv, st, tr
 

@@ -13,16 +13,22 @@ on full-width sub-columns and whole spectral windows, not on slices.
     10-60 cm-1, where the far-wing mirror lines of CNVF4Q are active.
 
 Bounds: radiance 1e-4 relative per point (mixed) and 1e-8 (FP64).
-Jacobians, per point: |got - want| <= JAC_RTOL |want| + JAC_ATOL * max|want|
-over the level's own spectrum.  The mixed path forms dtau/dT as the
-reference does, tau(T+1) - tau(T) - (Wtot/T) [tau(1.01 W) - tau(W)] / 0.01,
-a difference of FP32-compensated ODs whose relative error is eps <= 1e-6:
-its absolute error is about 2 eps tau (1 + 100/T) < 3 eps tau, against a
-typical |dtau/dT| of 1e-2 tau, so 3e-4 of the derivative where it is
-typical (JAC_RTOL 1e-3 leaves room for the chain rule's sums) and, where
-dtau/dT crosses zero inside a line, 3 eps tau |dR/dtau| absolute, which is
-about 3e-4 of the level's largest Jacobian (JAC_ATOL).  FP64: 1e-9 and
-1e-10.
+Jacobians, per point and level l:
+    |got - want| <= JAC_RTOL |want| + JAC_ATOL S_l,
+    S_l = max(max|want_l|, 1e-6 max over all levels |want|).
+Where the bound comes from (mixed path): the reference forms dtau/dT as
+tau(T+1) - tau(T) - (Wtot/T) [tau(1.01 W) - tau(W)] / 0.01, a difference of
+ODs whose relative error is eps <= 1e-6, so its absolute error is at most
+2 eps tau (1 + 100/T) < 3 eps tau.  A layer's OD changes by no less than
+about 2.3e-3 per K at its line peaks (the Doppler width's T^1/2 at 217 K),
+so the error is at most ~1.3e-3 of the level's largest Jacobian wherever it
+falls (JAC_ATOL, with room for level2layer's two-layer sums, whose
+cancellation where the H2O mixing ratio reaches its floor amplifies it), and
+about 3e-4 of the value itself where dtau/dT is typical (JAC_RTOL 1e-3).
+Levels below an opaque lower atmosphere have Jacobians of 1e-40 to 1e-320,
+below FP32's range, where the mixed path returns 0: S_l's floor at 1e-6 of
+the column's largest Jacobian makes those levels count as zero.  FP64: the
+same form with 1e-9 and 1e-10.
 """
 import os
 
@@ -35,7 +41,8 @@ from clblm_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 THREADS = os.cpu_count() or 1
-JAC_TOL = {T.CLBLM_PREC_MIXED: (1e-3, 3e-4), T.CLBLM_PREC_PLAIN: (1e-9, 1e-10)}
+JAC_TOL = {T.CLBLM_PREC_MIXED: (1e-3, 2.5e-3), T.CLBLM_PREC_PLAIN: (1e-9, 1e-10)}
+JAC_FLOOR = 1e-6
 RAD_TOL = {T.CLBLM_PREC_MIXED: 1e-4, T.CLBLM_PREC_PLAIN: 1e-8}
 
 
@@ -51,16 +58,20 @@ def _jac_check(got, want, precision, what):
     rt, at = JAC_TOL[precision]
     g2, w2 = np.atleast_2d(got), np.atleast_2d(want)
     assert g2.shape == w2.shape, what
-    worst = 0.0
+    fin = [bool(np.all(np.isfinite(w))) for w in w2]
+    top = max((float(np.max(np.abs(w))) for w, f in zip(w2, fin) if f), default=0.0)
+    worst, where = 0.0, None
     for lev in range(w2.shape[0]):
         w, g = w2[lev], g2[lev]
-        if not np.all(np.isfinite(w)):
+        if not fin[lev]:
             assert not np.all(np.isfinite(g)), (what, lev)
             continue
-        scale = np.max(np.abs(w))
+        scale = max(float(np.max(np.abs(w))), JAC_FLOOR * top)
         excess = np.abs(g - w) / (rt * np.abs(w) + at * scale + 1e-300)
-        worst = max(worst, float(np.max(excess)))
-    assert worst <= 1.0, (what, worst)
+        i = int(np.argmax(excess))
+        if excess[i] > worst:
+            worst, where = float(excess[i]), (lev, i, float(w[i]), float(g[i]), scale, top)
+    assert worst <= 1.0, (what, worst, where)
     return worst
 
 
