@@ -21,29 +21,44 @@ struct InterpSpec {
   int dec;          // dvin > dvout (formed on the host: no binary64 compare per point)
 };
 
-struct RtLayerArgs {
-  int64_t n_out;
+// One layer of a run of k_rt_segment: its OD grid, the map of that grid onto
+// the run's merge grid and the scalars of its layer terms.
+struct RtSegLayer {
+  InterpSpec ly;       // layer OD grid -> the run's merge grid
+  const void* od;
+  int64_t n_od;
+  double v1, dv_od;    // the OD grid
+  double scal_up, scal_dn;
+  double tbot, ttop, tave;
+  // FP32 set-up of the mixed path on the OD grid: v = vf0 + (i-1) vf1 and
+  // v/kT = x0 + (i-1) x1 for the top, bottom and mean temperatures (formed
+  // on the host: a conversion per point would run on the FP64 unit)
+  float xt0, xt1, xb0, xb1, xa0, xa1, vf0, vf1;
+  float scal_up_f, scal_dn_f;
+  // 1: this layer's bottom temperature is the previous layer's top and both
+  // layers are on the run's grid (the mixed path reuses that Planck value)
+  int bot_is_prev_top;
+  int pad;
+};
+static_assert(sizeof(RtSegLayer) % 8 == 0, "RtSegLayer is staged in 8-byte words");
+constexpr int kRtSegMaxLayers = 32;  // layers per k_rt_segment launch (a longer run takes several)
+
+struct RtSegArgs {
+  int64_t n_out;       // points of the run's merge grid
   double v1;
-  InterpSpec mr;       // merged radiance/reflectance: previous grid -> this layer's grid
-  InterpSpec ly;       // layer OD grid -> this layer's grid
+  InterpSpec mr;       // merged radiance/reflectance: previous grid -> this grid
   const void* rad_in;
   const void* refl_in;
   void* rad_out;
   void* refl_out;
-  const void* od;
-  int64_t n_od;
-  double dv_od;
-  double scal_up, scal_dn;
-  double tbot, ttop, tave;
+  double* final_out;   // the column's last run: binary64 radiance here instead
+  const RtSegLayer* lay;  // [nlay], device memory
+  int nlay;
   int lin_in_tau;
   int first;           // merged spectra come from the surface
   double tskin, emis;
-  // FP32 set-up of the mixed path: v/kT = x0 + (i-1)*x1 on the OD grid
-  float xt0, xt1, xb0, xb1, xa0, xa1, vf0, vf1;
   float xs0, xs1;      // surface: v/kT_skin on the merged-input grid
-  // FP32 copies of the scalars above the mixed path uses (formed on the host:
-  // a conversion per point would run on the FP64 unit)
-  float scal_up_f, scal_dn_f, emis_f, omemis_f, vs0, vs1;  // vs: V on the merged-input grid
+  float emis_f, omemis_f, vs0, vs1;  // vs: V on the merged-input grid
 };
 
 // 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365),
@@ -124,9 +139,9 @@ __device__ __forceinline__ Stencil<W> interp_stencil(const InterpSpec& s, int64_
 cudaError_t rt_upload_interp_coef(cudaStream_t st);
 __global__ void k_interp_map(InterpSpec s, const int64_t* blk_j1, const double* blk_vo, int nblk, int64_t nout,
                              int2* map);
-constexpr int kRtMaxThreads = 512;  // largest k_rt_layer block the autotuner times
+constexpr int kRtMaxThreads = 512;  // largest k_rt_segment block the autotuner times
 template <bool Plain>
-__global__ void __launch_bounds__(kRtMaxThreads, Plain ? 1 : 2) k_rt_layer(RtLayerArgs a);
+__global__ void __launch_bounds__(kRtMaxThreads) k_rt_segment(const __grid_constant__ RtSegArgs a);
 template <bool Plain>
 __global__ void k_od_out(const void* od, int64_t n_in, InterpSpec s, int64_t n_out, double* out);
 

@@ -1,5 +1,6 @@
-// rt.cu -- nadir upwelling radiance: one kernel launch per layer of the
-// upward merge of mode2_lookDn_mergeUp (clblm_noScattRT.f90:1340-1466).
+// rt.cu -- nadir upwelling radiance: the upward merge of
+// mode2_lookDn_mergeUp (clblm_noScattRT.f90:1340-1466), one kernel launch per
+// run of layers that share a merge grid.
 //
 // Per output point of the layer's merge grid:
 //   TxA = exp(-tau_A), TxB = exp(-tau_B)  with tau_A, tau_B the reference-path
@@ -92,23 +93,24 @@ __device__ __forceinline__ double hlf_d(double od) {
   return 1. / (od)-1. / (tex - 1.);
 }
 
-// layer terms at OD-grid point i: TxA, TxB, EmUp, EmDn
-__device__ __forceinline__ void layer_terms_d(const RtLayerArgs& a, int64_t i, double out[4]) {
-  const double od = reinterpret_cast<const double*>(a.od)[i - 1];
-  const double v = a.v1 + (double)(i - 1) * a.dv_od;
-  double odA = od * a.scal_up;
+// Layer terms at OD-grid point j of layer L, from its OD value `od`: TxA,
+// TxB, EmUp, EmDn (layerMerge_mode2 :1640-1762 with layerEmis).
+__device__ __forceinline__ void layer_terms_d(const RtSegLayer& L, int lin_in_tau, int64_t j, double od,
+                                              double out[4]) {
+  const double v = L.v1 + (double)(j - 1) * L.dv_od;
+  double odA = od * L.scal_up;
   odA = odA * 1.0;
-  double odB = od * a.scal_dn;
+  double odB = od * L.scal_dn;
   odB = odB * 1.0;
   double TA = exp(-odA), TB = exp(-odB);
-  double XKTA_up = a.ttop / kRADCN2, XKTA_dn = a.tbot / kRADCN2, XKT = a.tave / kRADCN2;
-  double XKTB_up = a.tbot / kRADCN2, XKTB_dn = a.ttop / kRADCN2;
+  double XKTA_up = L.ttop / kRADCN2, XKTA_dn = L.tbot / kRADCN2, XKT = L.tave / kRADCN2;
+  double XKTB_up = L.tbot / kRADCN2, XKTB_dn = L.ttop / kRADCN2;
   double EU, ED;
   {  // down: Ta = Tbot, Tb = Ttop over path B
     double abso = 1 - TB;
-    double hlf = a.lin_in_tau ? hlf_d(odB) : 0.;
-    if (a.lin_in_tau == 0) ED = abso * planck_d(v, XKT);
-    else if (a.lin_in_tau == 1) {
+    double hlf = lin_in_tau ? hlf_d(odB) : 0.;
+    if (lin_in_tau == 0) ED = abso * planck_d(v, XKT);
+    else if (lin_in_tau == 1) {
       double bba = planck_d(v, XKTA_dn), bb = planck_d(v, XKT);
       ED = abso * (bba + 2 * (bb - bba) * hlf);
     } else {
@@ -116,11 +118,11 @@ __device__ __forceinline__ void layer_terms_d(const RtLayerArgs& a, int64_t i, d
       ED = abso * (bba + (bbb - bba) * hlf);
     }
   }
-  if (a.lin_in_tau == 0) EU = ED;
+  if (lin_in_tau == 0) EU = ED;
   else {  // up: Ta = Ttop, Tb = Tbot over path A
     double abso = 1 - TA;
     double hlf = hlf_d(odA);
-    if (a.lin_in_tau == 1) {
+    if (lin_in_tau == 1) {
       double bba = planck_d(v, XKTA_up), bb = planck_d(v, XKT);
       EU = abso * (bba + 2 * (bb - bba) * hlf);
     } else {
@@ -134,99 +136,127 @@ __device__ __forceinline__ void layer_terms_d(const RtLayerArgs& a, int64_t i, d
   out[3] = ED;
 }
 
-__device__ __forceinline__ void layer_terms_f(const RtLayerArgs& a, int64_t i, float out[4]) {
-  const float odf = reinterpret_cast<const float*>(a.od)[i - 1];
-  const float odA = odf * a.scal_up_f, odB = odf * a.scal_dn_f;
-  const float TA = expf(-odA), TB = expf(-odB);
-  const float aA = -expm1f(-odA), aB = -expm1f(-odB);
-  const float fi = (float)(int)(i - 1);  // 32-bit conversion: a 64-bit one runs on the FP64 unit
-  const float vf = fmaf(fi, a.vf1, a.vf0);
-  const float cv3 = (float)kRADCN1 * vf * vf * vf;
-  const float Bt = planck_f(fmaf(fi, a.xt1, a.xt0), cv3);
-  const float Bb = planck_f(fmaf(fi, a.xb1, a.xb0), cv3);
-  const float Ba = planck_f(fmaf(fi, a.xa1, a.xa0), cv3);
-  float EU, ED;
-  if (a.lin_in_tau == 0) {
-    ED = aB * Ba;
-    EU = ED;
-  } else if (a.lin_in_tau == 1) {
-    ED = aB * (Bb + 2.f * (Ba - Bb) * hlf_f(odB));
-    EU = aA * (Bt + 2.f * (Ba - Bt) * hlf_f(odA));
-  } else {
-    ED = aB * (Bb + (Bt - Bb) * hlf_f(odB));
-    EU = aA * (Bt + (Bb - Bt) * hlf_f(odA));
+// Mixed path: e^x - 1 for x <= 0 or a Planck argument x > 0: the Taylor
+// series (relative error below 4e-10) where |x| < 1/4 and the difference
+// would cancel, else the hardware exponential (ex2.approx, relative error
+// about 1e-6 here) minus 1.
+__device__ __forceinline__ float expm1_mixed(float x) {
+  if (fabsf(x) < 0.25f) {
+    float p = fmaf(x, 1.f / 5040.f, 1.f / 720.f);
+    p = fmaf(x, p, 1.f / 120.f);
+    p = fmaf(x, p, 1.f / 24.f);
+    p = fmaf(x, p, 1.f / 6.f);
+    p = fmaf(x, p, 0.5f);
+    return fmaf(x * x, p, x);
   }
-  out[0] = TA;
-  out[1] = TB;
+  return __expf(x) - 1.f;
+}
+
+// Transmittance T = e^-od and absorptance 1 - T of one path, and rlin's
+// linear-in-tau weight 1/od - 1/(e^od - 1) = (a - od T) / (od a) from them
+// (the series below od = 0.1, 1/od above 20).
+struct PathF {
+  float T, a, hlf;
+};
+__device__ __forceinline__ PathF path_f(float od, bool with_hlf) {
+  PathF p;
+  p.T = __expf(-od);
+  p.a = od < 0.25f ? -expm1_mixed(-od) : 1.f - p.T;
+  p.hlf = 0.f;
+  if (with_hlf) {
+    if (od < 0.1f) {
+      const float o2 = od * od;
+      p.hlf = 0.5f + od * (-1.f / 12.f + o2 * (1.f / 720.f - o2 * (1.f / 30240.f)));
+    } else if (od > 20.f) {
+      p.hlf = __fdividef(1.f, od);
+    } else {
+      p.hlf = __fdividef(fmaf(-od, p.T, p.a), od * p.a);
+    }
+  }
+  return p;
+}
+
+__device__ __forceinline__ float planck_fast(float x /* v/kT */, float cv3) {
+  return __fdividef(cv3, expm1_mixed(x));
+}
+
+// The mixed path's terms.  `Bb` (the Planck function at the layer's bottom
+// temperature) is passed in when the previous layer of the run had it at its
+// top (the same level temperature), else it is formed here (Bb < 0).
+__device__ __forceinline__ void layer_terms_f(const RtSegLayer& L, int lin_in_tau, int64_t j, float odf,
+                                              float out[4], float* Bt_out = nullptr, float Bb = -1.f) {
+  const float odA = odf * L.scal_up_f, odB = odf * L.scal_dn_f;
+  const bool lin = lin_in_tau != 0;
+  const PathF A = path_f(odA, lin), B = path_f(odB, lin);
+  const float fi = (float)(int)(j - 1);  // 32-bit conversion: a 64-bit one runs on the FP64 unit
+  const float vf = fmaf(fi, L.vf1, L.vf0);
+  const float cv3 = (float)kRADCN1 * vf * vf * vf;
+  const float Ba = planck_fast(fmaf(fi, L.xa1, L.xa0), cv3);
+  float EU, ED;
+  if (lin_in_tau == 0) {
+    ED = B.a * Ba;
+    EU = ED;
+    if (Bt_out) *Bt_out = -1.f;
+  } else {
+    const float Bt = planck_fast(fmaf(fi, L.xt1, L.xt0), cv3);
+    if (Bb < 0.f) Bb = planck_fast(fmaf(fi, L.xb1, L.xb0), cv3);
+    if (lin_in_tau == 1) {
+      ED = B.a * fmaf(2.f * (Ba - Bb), B.hlf, Bb);
+      EU = A.a * fmaf(2.f * (Ba - Bt), A.hlf, Bt);
+    } else {
+      ED = B.a * fmaf(Bt - Bb, B.hlf, Bb);
+      EU = A.a * fmaf(Bb - Bt, A.hlf, Bt);
+    }
+    if (Bt_out) *Bt_out = Bt;
+  }
+  out[0] = A.T;
+  out[1] = B.T;
   out[2] = EU;
   out[3] = ED;
 }
 
-template <bool Plain>
-__device__ __forceinline__ void layer_terms(const RtLayerArgs& a, int64_t i,
-                                            typename std::conditional<Plain, double, float>::type out[4]) {
-  if constexpr (Plain) layer_terms_d(a, i, out);
-  else layer_terms_f(a, i, out);
-}
-
-// layer terms at OD-grid index j, with interpSpectrum's linear extension by
-// two points past either end
+// the terms at OD-grid index j of layer L, with interpSpectrum's linear
+// extension by two points past either end
 template <bool Plain, typename Real>
-__device__ __forceinline__ void layer_terms_ext(const RtLayerArgs& a, int64_t j, Real t[4]) {
-  if (j >= 1 && j <= a.n_od) {
-    layer_terms<Plain>(a, j, t);
+__device__ __forceinline__ void layer_terms_ext(const RtSegLayer& L, int lin_in_tau, int64_t j, Real t[4]) {
+  const Real* od = reinterpret_cast<const Real*>(L.od);
+  auto at = [&](int64_t k, Real o[4]) {
+    if constexpr (Plain) layer_terms_d(L, lin_in_tau, k, od[k - 1], o);
+    else layer_terms_f(L, lin_in_tau, k, od[k - 1], o);
+  };
+  if (j >= 1 && j <= L.n_od) {
+    at(j, t);
     return;
   }
   Real lo[4], hi[4];
-  const int64_t jl = j < 1 ? 1 : a.n_od, jm = j < 1 ? 2 : a.n_od - 1;
-  layer_terms<Plain>(a, jl, lo);
-  layer_terms<Plain>(a, jm, hi);
-  const bool ext = (j == 0 || j == -1 || j == a.n_od + 1 || j == a.n_od + 2);
+  const int64_t jl = j < 1 ? 1 : L.n_od, jm = j < 1 ? 2 : L.n_od - 1;
+  at(jl, lo);
+  at(jm, hi);
+  const bool ext = (j == 0 || j == -1 || j == L.n_od + 1 || j == L.n_od + 2);
   for (int c = 0; c < 4; ++c) t[c] = ext ? (Real)2 * lo[c] - hi[c] : (Real)0;
 }
 
+// One run of consecutive layers whose merge grid is the same (the layer loop
+// of mode2_lookDn_mergeUp, :1340-1466, between two refinements of the grid
+// by interpToFinestGrid).  One thread per point of the run's grid: the
+// merged radiance R and reflectance F are read once (interpolated from the
+// previous grid with interpSpectrum's stencil, or the surface terms), the
+// run's layers are merged in registers,
+//   R <- EmUp + TxA (R + EmDn F),   F <- TxA TxB F        (:1782-1794),
+// and R, F are written once (binary64 R alone after the column's last
+// layer).  A layer on the run's grid reads its OD at the point itself; a
+// coarser one brings its four terms to the point with its stencil, as the
+// reference interpolates TxA, TxB, EmUp and EmDn.  Memory traffic per point:
+// one OD value per layer plus R and F in and out once per run.
 template <bool Plain>
-__global__ void __launch_bounds__(kRtMaxThreads, Plain ? 1 : 2) k_rt_layer(RtLayerArgs a) {
+__global__ void __launch_bounds__(kRtMaxThreads) k_rt_segment(const __grid_constant__ RtSegArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
-  // layer terms of the CTA's OD-grid range, each evaluated once (a layer grid
-  // coarser than the merge grid feeds every OD point into up to four
-  // neighbouring output points' stencils)
-  constexpr int kCap = kRtMaxThreads + 8;
-  __shared__ Real sh_t[4][kCap];
-  __shared__ int sh_lo, sh_hi;
+  __shared__ RtSegLayer sl[kRtSegMaxLayers];
+  for (int k = threadIdx.x; k < a.nlay * (int)(sizeof(RtSegLayer) / 8); k += blockDim.x)
+    reinterpret_cast<uint64_t*>(sl)[k] = reinterpret_cast<const uint64_t*>(a.lay)[k];
+  __syncthreads();
   const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const bool live = I <= a.n_out;
-  const bool share = a.ly.kind == 1 && a.ly.itype != 0;  // four-point stencils: uniform over the launch
-  Stencil<Real> sl;
-  sl.n = 0;
-  if (live) sl = interp_stencil<Real>(a.ly, I);
-  int64_t jlo = 0;
-  bool staged = false;
-  if (share) {
-    if (threadIdx.x == 0) {
-      sh_lo = INT_MAX;
-      sh_hi = INT_MIN;
-    }
-    __syncthreads();
-    if (live) {
-      atomicMin(&sh_lo, (int)sl.i[0]);
-      atomicMax(&sh_hi, (int)(sl.n == 4 ? sl.i[3] : sl.i[0]));  // stencils hold 1 or 4 points
-    }
-    __syncthreads();
-    jlo = sh_lo;
-    const int64_t nr = (int64_t)sh_hi - jlo + 1;
-    staged = nr <= kCap;  // uniform over the CTA
-    if (staged) {
-      for (int64_t r = threadIdx.x; r < nr; r += blockDim.x) {
-        Real t[4];
-        layer_terms_ext<Plain>(a, jlo + r, t);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) sh_t[c][r] = t[c];
-      }
-      __syncthreads();
-    }
-  }
-  if (!live) return;
+  if (I > a.n_out) return;
   // merged radiance and reflectance at I
   Real R = 0, F = 0;
   {
@@ -269,39 +299,52 @@ __global__ void __launch_bounds__(kRtMaxThreads, Plain ? 1 : 2) k_rt_layer(RtLay
       }
     }
   }
-  Real L[4];
-  {
-    const Stencil<Real>& st = sl;
-    // the terms at OD-grid index j: from the CTA's staged range, or evaluated here
-    auto terms = [&](int64_t j, Real t[4]) {
-      if (staged) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) t[c] = sh_t[c][j - jlo];
+  // the run's layers; the next layer's OD on the run's grid is loaded while
+  // the current one is merged
+  Real nxt = 0;
+  if (a.nlay > 0 && sl[0].ly.kind == 0) nxt = reinterpret_cast<const Real*>(sl[0].od)[I - 1];
+  float Bprev = -1.f;  // mixed: the Planck function at the previous layer's top
+  for (int l = 0; l < a.nlay; ++l) {
+    const RtSegLayer& L = sl[l];
+    const Real cur = nxt;
+    if (l + 1 < a.nlay && sl[l + 1].ly.kind == 0) nxt = reinterpret_cast<const Real*>(sl[l + 1].od)[I - 1];
+    Real T[4];
+    if (L.ly.kind == 0) {
+      if constexpr (Plain) {
+        layer_terms_d(L, a.lin_in_tau, I, cur, T);
       } else {
-        layer_terms_ext<Plain>(a, j, t);
+        const float bb = L.bot_is_prev_top ? Bprev : -1.f;
+        layer_terms_f(L, a.lin_in_tau, I, cur, T, &Bprev, bb);
       }
-    };
-    if (st.n == 1) {
-      terms(st.i[0], L);
     } else {
-      for (int c = 0; c < 4; ++c) L[c] = 0;
+      Bprev = -1.f;
+      const Stencil<Real> st = interp_stencil<Real>(L.ly, I);
+      if (st.n == 1) {
+        layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[0], T);
+      } else {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        Real t[4];
-        terms(st.i[k], t);
-        for (int c = 0; c < 4; ++c) L[c] += st.w[k] * t[c];
+        for (int c = 0; c < 4; ++c) T[c] = 0;
+        for (int k = 0; k < 4; ++k) {
+          Real t[4];
+          layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[k], t);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) T[c] += st.w[k] * t[c];
+        }
       }
     }
+    R = T[2] + T[0] * (R + T[3] * F);
+    F = T[0] * T[1] * F;
   }
-  const Real TA = L[0], TB = L[1], EU = L[2], ED = L[3];
-  Real* rout = reinterpret_cast<Real*>(a.rad_out);
-  Real* fout = reinterpret_cast<Real*>(a.refl_out);
-  rout[I - 1] = EU + TA * (R + ED * F);
-  fout[I - 1] = TA * TB * F;
+  if (a.final_out) {
+    a.final_out[I - 1] = (double)R;
+  } else {
+    reinterpret_cast<Real*>(a.rad_out)[I - 1] = R;
+    reinterpret_cast<Real*>(a.refl_out)[I - 1] = F;
+  }
 }
 
-template __global__ void k_rt_layer<false>(RtLayerArgs);
-template __global__ void k_rt_layer<true>(RtLayerArgs);
+template __global__ void k_rt_segment<false>(const __grid_constant__ RtSegArgs);
+template __global__ void k_rt_segment<true>(const __grid_constant__ RtSegArgs);
 
 // DVout interpolation of a layer OD (ODLAY_nonStruct :582-598) and the
 // conversion of the device OD to binary64.

@@ -79,7 +79,7 @@ struct BatchGraph;
 // with the same operations in the same order).  -1: not chosen yet.
 struct Tuner {
   int f4[2] = {-1, -1};   // k_f4_conv records per stage: 64 / 128 / 256 (index), per precision
-  int rt[2] = {-1, -1};   // k_rt_layer threads per block: 128 / 256 / 512
+  int rt[2] = {-1, -1};   // k_rt_segment threads per block: 128 / 256 / 512
   int jac[2] = {-1, -1};  // k_jac threads per block: 64 / 128
   bool on = true;         // CLBLM_AUTOTUNE=0: the defaults, no timing
 };
@@ -113,6 +113,9 @@ struct clblm_handle {
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt, ragg;
   DevBuf segpool;  // radiation-term segments of panels with more than kMaxSeg
   DevBuf rt[4], outbuf, imap[2];
+  DevBuf rtseg;                  // layer tables of the radiance runs (RtSegLayer)
+  std::vector<DevBuf> rt_lymap;  // maps of layers coarser than their merge grid by a general ratio
+  std::vector<RtSegLayer> rtseg_host;
   // batched profiles: captured launch sequences of recent batches
   std::vector<std::shared_ptr<BatchGraph>> bgraphs;  // (deleter bound where BatchGraph is complete)
   uint64_t bgraph_clock = 0;
@@ -129,6 +132,8 @@ struct clblm_handle {
                               &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk};
     for (auto& b : rt) v.push_back(&b);
     for (auto& b : imap) v.push_back(&b);
+    v.push_back(&rtseg);
+    for (auto& b : rt_lymap) v.push_back(&b);
     return v;
   }
   Tuner tune;
@@ -1889,6 +1894,9 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
     }
     CUDA_TRY(h, e);
   }
+  // the column's last run writes the binary64 radiance here
+  CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * nfinal));
+  double* final_dst = flags == CLBLM_OUT_DEVICE ? rad : h->outbuf.as<double>();
   // layers in batches sized to the workspace budget
   const size_t budget = od_batch_budget(h);
   int cur = 0;  // ping-pong index of the merged spectra
@@ -1907,53 +1915,80 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
     rc = run_od_batch(h, rp.hps, first, count, plain, ls, fs, ps);
     if (rc) return rc;
     CUDA_TRY(h, cudaEventRecord(h->ev[6], h->stream));
+    // the layer tables of this batch: each layer's grid, its map onto the
+    // merge grid and the scalars of its terms
+    h->rtseg_host.assign(count, RtSegLayer{});
+    int nlymap = 0;
     for (int il = first; il < first + count; ++il) {
       const LayerPlan& P = rp.hps[il].P;
-      RtLayerArgs a;
+      RtSegLayer& L = h->rtseg_host[il - first];
+      std::memset(&L, 0, sizeof L);
+      // layer spectra on the OD grid (DV, nsamp) or the DVout grid
+      const double odv = rp.hps[il].dv_out;
+      const int64_t onn = rp.hps[il].n_out;
+      if (std::fabs(odv - P.dv) >= 2.220446049250313e-16)
+        return set_err(h, CLBLM_ERR_UNSUPPORTED, "uniform DVout grids in the radiance path are not on this path");
+      L.ly = interp_spec(col->v1, odv, onn, col->v1, rp.grid_dv[il], rp.grid_n[il]);
+      if (L.ly.kind != 0 && L.ly.itype < 0) {  // a coarser layer by a general ratio: its own map
+        if ((int)h->rt_lymap.size() <= nlymap) h->rt_lymap.resize(nlymap + 1);
+        rc = build_interp_map(h, &L.ly, rp.grid_n[il], &h->rt_lymap[nlymap++]);
+        if (rc) return rc;
+      }
+      L.od = plain ? (const void*)(h->od.as<double>() + P.od_off) : (const void*)(h->od.as<float>() + P.od_off);
+      L.n_od = P.nsamp;
+      L.v1 = col->v1;
+      L.dv_od = P.dv;
+      L.scal_up = col->wtot[il] / col->wtot[il];
+      L.scal_dn = col->wtot_down[il] / col->wtot[il];
+      L.tbot = col->tbot[il];
+      L.ttop = col->ttop[il];
+      L.tave = col->tave[il];
+      L.xt0 = (float)(col->v1 * (kRADCN2 / col->ttop[il]));
+      L.xt1 = (float)(P.dv * (kRADCN2 / col->ttop[il]));
+      L.xb0 = (float)(col->v1 * (kRADCN2 / col->tbot[il]));
+      L.xb1 = (float)(P.dv * (kRADCN2 / col->tbot[il]));
+      L.xa0 = (float)(col->v1 * (kRADCN2 / col->tave[il]));
+      L.xa1 = (float)(P.dv * (kRADCN2 / col->tave[il]));
+      L.vf0 = (float)col->v1;
+      L.vf1 = (float)P.dv;
+      L.scal_up_f = (float)L.scal_up;
+      L.scal_dn_f = (float)L.scal_dn;
+      // the same level temperature, on the same OD grid as the previous layer
+      L.bot_is_prev_top = (il > first && col->tbot[il] == col->ttop[il - 1] && L.ly.kind == 0 &&
+                           h->rtseg_host[il - first - 1].ly.kind == 0 && P.dv == rp.hps[il - 1].P.dv)
+                              ? 1 : 0;
+    }
+    CUDA_TRY(h, h->rtseg.ensure(sizeof(RtSegLayer) * (size_t)count));
+    CUDA_TRY(h, cudaMemcpyAsync(h->rtseg.p, h->rtseg_host.data(), sizeof(RtSegLayer) * (size_t)count,
+                                cudaMemcpyHostToDevice, h->stream));
+    // runs: consecutive layers on one merge grid, at most kRtSegMaxLayers
+    for (int il = first; il < first + count;) {
+      int je = il + 1;
+      while (je < first + count && je - il < kRtSegMaxLayers && rp.grid_n[je] == rp.grid_n[il] &&
+             rp.grid_dv[je] == rp.grid_dv[il])
+        ++je;
+      RtSegArgs a;
       std::memset(&a, 0, sizeof a);
-      double in_dv = il == 0 ? rp.dv0 : rp.grid_dv[il - 1];
-      int64_t in_n = il == 0 ? rp.n0 : rp.grid_n[il - 1];
+      const double in_dv = il == 0 ? rp.dv0 : rp.grid_dv[il - 1];
+      const int64_t in_n = il == 0 ? rp.n0 : rp.grid_n[il - 1];
       a.n_out = rp.grid_n[il];
       a.v1 = col->v1;
       a.mr = interp_spec(col->v1, in_dv, in_n, col->v1, rp.grid_dv[il], rp.grid_n[il]);
       rc = build_interp_map(h, &a.mr, a.n_out, &h->imap[0]);
       if (rc) return rc;
-      // layer spectra on the OD grid (DV, nsamp) or the DVout grid
-      double odv = rp.hps[il].dv_out;
-      int64_t onn = rp.hps[il].n_out;
-      if (std::fabs(odv - P.dv) >= 2.220446049250313e-16)
-        return set_err(h, CLBLM_ERR_UNSUPPORTED, "uniform DVout grids in the radiance path are not on this path");
-      a.ly = interp_spec(col->v1, odv, onn, col->v1, rp.grid_dv[il], rp.grid_n[il]);
-      rc = build_interp_map(h, &a.ly, a.n_out, &h->imap[1]);
-      if (rc) return rc;
       a.rad_in = h->rt[cur * 2].p;
       a.refl_in = h->rt[cur * 2 + 1].p;
       a.rad_out = h->rt[(1 - cur) * 2].p;
       a.refl_out = h->rt[(1 - cur) * 2 + 1].p;
-      a.od = plain ? (const void*)(h->od.as<double>() + P.od_off) : (const void*)(h->od.as<float>() + P.od_off);
-      a.n_od = P.nsamp;
-      a.dv_od = P.dv;
-      a.scal_up = col->wtot[il] / col->wtot[il];
-      a.scal_dn = col->wtot_down[il] / col->wtot[il];
-      a.tbot = col->tbot[il];
-      a.ttop = col->ttop[il];
-      a.tave = col->tave[il];
+      a.final_out = je == n ? final_dst : nullptr;
+      a.lay = h->rtseg.as<RtSegLayer>() + (il - first);
+      a.nlay = je - il;
       a.lin_in_tau = ctrl->lin_in_tau;
       a.first = il == 0;
       a.tskin = col->tskin;
       a.emis = col->emis;
-      a.xt0 = (float)(col->v1 * (kRADCN2 / col->ttop[il]));
-      a.xt1 = (float)(P.dv * (kRADCN2 / col->ttop[il]));
-      a.xb0 = (float)(col->v1 * (kRADCN2 / col->tbot[il]));
-      a.xb1 = (float)(P.dv * (kRADCN2 / col->tbot[il]));
-      a.xa0 = (float)(col->v1 * (kRADCN2 / col->tave[il]));
-      a.xa1 = (float)(P.dv * (kRADCN2 / col->tave[il]));
-      a.vf0 = (float)col->v1;
-      a.vf1 = (float)P.dv;
       a.xs0 = (float)(col->v1 * (kRADCN2 / col->tskin));
       a.xs1 = (float)(in_dv * (kRADCN2 / col->tskin));
-      a.scal_up_f = (float)a.scal_up;
-      a.scal_dn_f = (float)a.scal_dn;
       a.emis_f = (float)a.emis;
       a.omemis_f = (float)(1.0 - a.emis);
       a.vs0 = (float)a.v1;
@@ -1961,8 +1996,8 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       auto rt = [&](int v) {
         const int nt = kRtThreads[v];
         const unsigned grid = (unsigned)((a.n_out + nt - 1) / nt);
-        if (plain) k_rt_layer<true><<<grid, nt, 0, h->stream>>>(a);
-        else k_rt_layer<false><<<grid, nt, 0, h->stream>>>(a);
+        if (plain) k_rt_segment<true><<<grid, nt, 0, h->stream>>>(a);
+        else k_rt_segment<false><<<grid, nt, 0, h->stream>>>(a);
       };
       int tv = h->tune.rt[plain ? 1 : 0];
       if (tv < 0) {
@@ -1972,10 +2007,12 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       h->launches++;
       rt(tv);
       CUDA_TRY(h, cudaGetLastError());
-      // algorithmic bytes: the layer OD, the merged radiance and reflectance
-      // in (none from the surface) and out
-      h->acc_rt_bytes += (int64_t)real * (P.nsamp + (il == 0 ? 0 : 2 * in_n) + 2 * a.n_out);
-      cur = 1 - cur;
+      // algorithmic bytes: every layer's OD, the merged radiance and
+      // reflectance in (none from the surface) and out once per run
+      for (int k = il; k < je; ++k) h->acc_rt_bytes += (int64_t)real * rp.hps[k].P.nsamp;
+      h->acc_rt_bytes += (int64_t)real * (il == 0 ? 0 : 2 * in_n) + (je == n ? 8 : 2 * (int64_t)real) * a.n_out;
+      if (je != n) cur = 1 - cur;
+      il = je;
     }
     CUDA_TRY(h, cudaEventRecord(h->ev[7], h->stream));
     rc = check_batch(h, rp.hps, first, count, &h->last);
@@ -1989,18 +2026,8 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
     }
     first += count;
   }
-  // binary64 radiance out
-  CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * nfinal));
-  InterpSpec same;
-  std::memset(&same, 0, sizeof same);
-  same.kind = 0;
-  double* dst = flags == CLBLM_OUT_DEVICE ? rad : h->outbuf.as<double>();
-  h->launches++;
-  if (plain) k_od_out<true><<<(unsigned)((nfinal + 255) / 256), 256, 0, h->stream>>>(h->rt[cur * 2].p, nfinal, same, nfinal, dst);
-  else k_od_out<false><<<(unsigned)((nfinal + 255) / 256), 256, 0, h->stream>>>(h->rt[cur * 2].p, nfinal, same, nfinal, dst);
-  CUDA_TRY(h, cudaGetLastError());
   if (flags != CLBLM_OUT_DEVICE)
-    CUDA_TRY(h, cudaMemcpyAsync(rad, dst, sizeof(double) * nfinal, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(rad, final_dst, sizeof(double) * nfinal, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   h->last.launches = h->launches;
   return CLBLM_OK;
