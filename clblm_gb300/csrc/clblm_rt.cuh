@@ -38,10 +38,16 @@ struct RtSegLayer {
   // 1: this layer's bottom temperature is the previous layer's top and both
   // layers are on the run's grid (the mixed path reuses that Planck value)
   int bot_is_prev_top;
-  int pad;
+  // mixed path on the run's grid: v/kT = v * k for the mean, top and bottom
+  // temperatures (k = RADCN2 / T)
+  float ka, kt, kb;
 };
 static_assert(sizeof(RtSegLayer) % 8 == 0, "RtSegLayer is staged in 8-byte words");
 constexpr int kRtSegMaxLayers = 32;  // layers per k_rt_segment launch (a longer run takes several)
+// consecutive points per thread of k_rt_segment (1 or 4; four points per
+// thread, with 16-byte accesses, measured slower on GB300: 3.2 against 2.6 ms
+// for the 60-layer column)
+constexpr int kRtPts = 1;
 
 struct RtSegArgs {
   int64_t n_out;       // points of the run's merge grid
@@ -59,6 +65,7 @@ struct RtSegArgs {
   double tskin, emis;
   float xs0, xs1;      // surface: v/kT_skin on the merged-input grid
   float emis_f, omemis_f, vs0, vs1;  // vs: V on the merged-input grid
+  float vr0, vr1;      // mixed: V = vr0 + (I-1) vr1 on the run's grid
 };
 
 // 201-point interpolation coefficients of interpSpectrum (clblm_Spectrum.f90:350-365),

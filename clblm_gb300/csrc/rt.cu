@@ -180,6 +180,57 @@ __device__ __forceinline__ float planck_fast(float x /* v/kT */, float cv3) {
   return __fdividef(cv3, expm1_mixed(x));
 }
 
+// The mixed path's merge of one layer on the run's own grid, branch-free but
+// for the Planck argument's rare series: transmittance T = e^-od and
+// absorptance a = 1 - T of the viewing (A) and downwelling (B) paths, with
+// rlin's weight hlf = 1/od - 1/(e^od - 1) = (a - od T) / (od a) from them, as
+// series (a to od^7, hlf to od^7) below od = 1/4 where the differences
+// cancel; the Planck functions at the layer's mean and top temperatures (the
+// bottom one passed in when the previous layer's top is the same level,
+// Bb >= 0); then R <- EmUp + TA (R + EmDn F), F <- TA TB F.
+__device__ __forceinline__ void path_lean(float od, float* T, float* a, float* hlf) {
+  *T = __expf(-od);
+  const float o2 = od * od;
+  float p = fmaf(-od, 1.f / 7.f, 1.f);
+  p = fmaf(-od * (1.f / 6.f), p, 1.f);
+  p = fmaf(-od * (1.f / 5.f), p, 1.f);
+  p = fmaf(-od * (1.f / 4.f), p, 1.f);
+  p = fmaf(-od * (1.f / 3.f), p, 1.f);
+  p = fmaf(-od * 0.5f, p, 1.f);
+  const float as = od * p;  // 1 - e^-od, od < 1/4
+  const float hs = fmaf(od, fmaf(o2, fmaf(o2, fmaf(o2, 1.f / 1209600.f, -1.f / 30240.f), 1.f / 720.f), -1.f / 12.f), 0.5f);
+  const bool small = od < 0.25f;
+  *a = small ? as : 1.f - *T;
+  *hlf = small ? hs : __fdividef(fmaf(-od, *T, *a), od * *a);
+}
+__device__ __forceinline__ void merge_lean(float od, float su, float sd, float ka, float kt, float kb, float vf,
+                                           float cv3, int lin_in_tau, float* Bprev, bool share, float* R,
+                                           float* F) {
+  float TA, aA, hA, TB, aB, hB;
+  path_lean(od * su, &TA, &aA, &hA);
+  path_lean(od * sd, &TB, &aB, &hB);
+  const float Ba = planck_fast(vf * ka, cv3);
+  float EU, ED;
+  if (lin_in_tau == 0) {
+    ED = aB * Ba;
+    EU = ED;
+    *Bprev = -1.f;
+  } else {
+    const float Bt = planck_fast(vf * kt, cv3);
+    const float Bb = share ? *Bprev : planck_fast(vf * kb, cv3);
+    if (lin_in_tau == 1) {
+      ED = aB * fmaf(2.f * (Ba - Bb), hB, Bb);
+      EU = aA * fmaf(2.f * (Ba - Bt), hA, Bt);
+    } else {
+      ED = aB * fmaf(Bt - Bb, hB, Bb);
+      EU = aA * fmaf(Bb - Bt, hA, Bt);
+    }
+    *Bprev = Bt;
+  }
+  *R = fmaf(TA, fmaf(ED, *F, *R), EU);
+  *F = TA * TB * *F;
+}
+
 // The mixed path's terms.  `Bb` (the Planck function at the layer's bottom
 // temperature) is passed in when the previous layer of the run had it at its
 // top (the same level temperature), else it is formed here (Bb < 0).
@@ -236,18 +287,103 @@ __device__ __forceinline__ void layer_terms_ext(const RtSegLayer& L, int lin_in_
   for (int c = 0; c < 4; ++c) t[c] = ext ? (Real)2 * lo[c] - hi[c] : (Real)0;
 }
 
+// merged radiance and reflectance entering a run at point I: from the
+// previous grid through interpSpectrum's stencil, or the surface terms
+template <bool Plain, typename Real>
+__device__ __forceinline__ void merged_at(const RtSegArgs& a, int64_t I, Real* R, Real* F) {
+  const Stencil<Real> st = interp_stencil<Real>(a.mr, I);
+  Real r0 = 0, f0 = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (k >= st.n) break;
+    Real r, f;
+    if (a.first) {
+      auto sr = [&](int64_t j) -> Real {
+        if constexpr (Plain) {
+          double v = a.v1 + (double)(j - 1) * a.mr.dvin;
+          return planck_d(v, a.tskin / kRADCN2) * a.emis;
+        } else {
+          float fj = (float)(int)(j - 1);
+          float vf = fmaf(fj, a.vs1, a.vs0);
+          return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * a.emis_f;
+        }
+      };
+      auto sf = [&](int64_t) -> Real {
+        if constexpr (Plain) return 1.0 - a.emis;
+        else return a.omemis_f;
+      };
+      r = ext_at<Real>(sr, a.mr.nin, st.i[k]);
+      f = ext_at<Real>(sf, a.mr.nin, st.i[k]);
+    } else {
+      const Real* rin = reinterpret_cast<const Real*>(a.rad_in);
+      const Real* fin = reinterpret_cast<const Real*>(a.refl_in);
+      auto gr = [&](int64_t j) -> Real { return rin[j - 1]; };
+      auto gf = [&](int64_t j) -> Real { return fin[j - 1]; };
+      r = ext_at<Real>(gr, a.mr.nin, st.i[k]);
+      f = ext_at<Real>(gf, a.mr.nin, st.i[k]);
+    }
+    if (st.n == 1) {
+      r0 = r;
+      f0 = f;
+    } else {
+      r0 += st.w[k] * r;
+      f0 += st.w[k] * f;
+    }
+  }
+  *R = r0;
+  *F = f0;
+}
+
+// kRtPts consecutive values x[I0-1 ..] of a spectrum whose first element is
+// 256-byte aligned; I0 - 1 is a multiple of kRtPts, so with four points a
+// full group is one 16-byte (FP32) or two 16-byte (FP64) accesses
+template <typename Real>
+__device__ __forceinline__ void load_pts(const Real* x, int64_t I0, int np, Real v[kRtPts]) {
+  if (kRtPts == 4 && np == kRtPts) {
+    if constexpr (sizeof(Real) == 4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(x + (I0 - 1)));
+      v[0] = q.x, v[kRtPts > 1 ? 1 : 0] = q.y, v[kRtPts > 2 ? 2 : 0] = q.z, v[kRtPts > 3 ? 3 : 0] = q.w;
+    } else {
+      const double2 q0 = __ldg(reinterpret_cast<const double2*>(x + (I0 - 1)));
+      const double2 q1 = __ldg(reinterpret_cast<const double2*>(x + (I0 + 1)));
+      v[0] = q0.x, v[kRtPts > 1 ? 1 : 0] = q0.y, v[kRtPts > 2 ? 2 : 0] = q1.x, v[kRtPts > 3 ? 3 : 0] = q1.y;
+    }
+  } else {
+#pragma unroll
+    for (int p = 0; p < kRtPts; ++p) v[p] = p < np ? x[I0 - 1 + p] : (Real)0;
+  }
+}
+template <typename Real>
+__device__ __forceinline__ void store_pts(Real* x, int64_t I0, int np, const Real v[kRtPts]) {
+  if (kRtPts == 4 && np == kRtPts) {
+    if constexpr (sizeof(Real) == 4) {
+      *reinterpret_cast<float4*>(x + (I0 - 1)) =
+          make_float4(v[0], v[kRtPts > 1 ? 1 : 0], v[kRtPts > 2 ? 2 : 0], v[kRtPts > 3 ? 3 : 0]);
+    } else {
+      *reinterpret_cast<double2*>(x + (I0 - 1)) = make_double2(v[0], v[kRtPts > 1 ? 1 : 0]);
+      *reinterpret_cast<double2*>(x + (I0 + 1)) = make_double2(v[kRtPts > 2 ? 2 : 0], v[kRtPts > 3 ? 3 : 0]);
+    }
+  } else {
+#pragma unroll
+    for (int p = 0; p < kRtPts; ++p)
+      if (p < np) x[I0 - 1 + p] = v[p];
+  }
+}
+
 // One run of consecutive layers whose merge grid is the same (the layer loop
 // of mode2_lookDn_mergeUp, :1340-1466, between two refinements of the grid
-// by interpToFinestGrid).  One thread per point of the run's grid: the
-// merged radiance R and reflectance F are read once (interpolated from the
-// previous grid with interpSpectrum's stencil, or the surface terms), the
-// run's layers are merged in registers,
+// by interpToFinestGrid).  kRtPts consecutive points of the run's grid per
+// thread: the merged radiance R and reflectance F are read once
+// (interpolated from the previous grid with interpSpectrum's stencil, or
+// the surface terms), the run's layers are merged in registers,
 //   R <- EmUp + TxA (R + EmDn F),   F <- TxA TxB F        (:1782-1794),
 // and R, F are written once (binary64 R alone after the column's last
-// layer).  A layer on the run's grid reads its OD at the point itself; a
-// coarser one brings its four terms to the point with its stencil, as the
-// reference interpolates TxA, TxB, EmUp and EmDn.  Memory traffic per point:
-// one OD value per layer plus R and F in and out once per run.
+// layer).  A layer on the run's grid reads its OD at the points themselves,
+// one 16-byte load per layer and thread (the next layer's is in flight while
+// the current one is merged); a coarser one brings its four terms to each
+// point with its stencil, as the reference interpolates TxA, TxB, EmUp and
+// EmDn.  Memory traffic per point: one OD value per layer plus R and F in
+// and out once per run.
 template <bool Plain>
 __global__ void __launch_bounds__(kRtMaxThreads) k_rt_segment(const __grid_constant__ RtSegArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
@@ -255,91 +391,74 @@ __global__ void __launch_bounds__(kRtMaxThreads) k_rt_segment(const __grid_const
   for (int k = threadIdx.x; k < a.nlay * (int)(sizeof(RtSegLayer) / 8); k += blockDim.x)
     reinterpret_cast<uint64_t*>(sl)[k] = reinterpret_cast<const uint64_t*>(a.lay)[k];
   __syncthreads();
-  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (I > a.n_out) return;
-  // merged radiance and reflectance at I
-  Real R = 0, F = 0;
-  {
-    const Stencil<Real> st = interp_stencil<Real>(a.mr, I);
+  const int64_t I0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRtPts + 1;
+  if (I0 > a.n_out) return;
+  const int np = (int)min((int64_t)kRtPts, a.n_out - I0 + 1);
+  Real R[kRtPts], F[kRtPts];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (k >= st.n) break;
-      Real r, f;
-      if (a.first) {
-        auto sr = [&](int64_t j) -> Real {
-          if constexpr (Plain) {
-            double v = a.v1 + (double)(j - 1) * a.mr.dvin;
-            return planck_d(v, a.tskin / kRADCN2) * a.emis;
-          } else {
-            float fj = (float)(int)(j - 1);
-            float vf = fmaf(fj, a.vs1, a.vs0);
-            return planck_f(fmaf(fj, a.xs1, a.xs0), (float)kRADCN1 * vf * vf * vf) * a.emis_f;
-          }
-        };
-        auto sf = [&](int64_t) -> Real {
-          if constexpr (Plain) return 1.0 - a.emis;
-          else return a.omemis_f;
-        };
-        r = ext_at<Real>(sr, a.mr.nin, st.i[k]);
-        f = ext_at<Real>(sf, a.mr.nin, st.i[k]);
-      } else {
-        const Real* rin = reinterpret_cast<const Real*>(a.rad_in);
-        const Real* fin = reinterpret_cast<const Real*>(a.refl_in);
-        auto gr = [&](int64_t j) -> Real { return rin[j - 1]; };
-        auto gf = [&](int64_t j) -> Real { return fin[j - 1]; };
-        r = ext_at<Real>(gr, a.mr.nin, st.i[k]);
-        f = ext_at<Real>(gf, a.mr.nin, st.i[k]);
-      }
-      if (st.n == 1) {
-        R = r;
-        F = f;
-      } else {
-        R += st.w[k] * r;
-        F += st.w[k] * f;
-      }
-    }
+  for (int p = 0; p < kRtPts; ++p) {
+    R[p] = F[p] = 0;
+    if (p < np) merged_at<Plain>(a, I0 + p, &R[p], &F[p]);
   }
-  // the run's layers; the next layer's OD on the run's grid is loaded while
-  // the current one is merged
-  Real nxt = 0;
-  if (a.nlay > 0 && sl[0].ly.kind == 0) nxt = reinterpret_cast<const Real*>(sl[0].od)[I - 1];
-  float Bprev = -1.f;  // mixed: the Planck function at the previous layer's top
+  Real nxt[kRtPts];
+  if (a.nlay > 0 && sl[0].ly.kind == 0) load_pts(reinterpret_cast<const Real*>(sl[0].od), I0, np, nxt);
+  float Bprev[kRtPts];  // mixed: the Planck function at the previous layer's top
+  float vfp[kRtPts], cv3p[kRtPts];  // mixed: wavenumber and RADCN1 v^3 of the points (the run's grid)
+#pragma unroll
+  for (int p = 0; p < kRtPts; ++p) {
+    Bprev[p] = -1.f;
+    const float fi = (float)(int)(I0 + p - 1);
+    vfp[p] = fmaf(fi, a.vr1, a.vr0);
+    cv3p[p] = (float)kRADCN1 * vfp[p] * vfp[p] * vfp[p];
+  }
   for (int l = 0; l < a.nlay; ++l) {
     const RtSegLayer& L = sl[l];
-    const Real cur = nxt;
-    if (l + 1 < a.nlay && sl[l + 1].ly.kind == 0) nxt = reinterpret_cast<const Real*>(sl[l + 1].od)[I - 1];
-    Real T[4];
-    if (L.ly.kind == 0) {
-      if constexpr (Plain) {
-        layer_terms_d(L, a.lin_in_tau, I, cur, T);
-      } else {
-        const float bb = L.bot_is_prev_top ? Bprev : -1.f;
-        layer_terms_f(L, a.lin_in_tau, I, cur, T, &Bprev, bb);
-      }
-    } else {
-      Bprev = -1.f;
-      const Stencil<Real> st = interp_stencil<Real>(L.ly, I);
-      if (st.n == 1) {
-        layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[0], T);
-      } else {
+    Real cur[kRtPts];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) T[c] = 0;
-        for (int k = 0; k < 4; ++k) {
-          Real t[4];
-          layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[k], t);
+    for (int p = 0; p < kRtPts; ++p) cur[p] = nxt[p];
+    if (l + 1 < a.nlay && sl[l + 1].ly.kind == 0)
+      load_pts(reinterpret_cast<const Real*>(sl[l + 1].od), I0, np, nxt);
 #pragma unroll
-          for (int c = 0; c < 4; ++c) T[c] += st.w[k] * t[c];
+    for (int p = 0; p < kRtPts; ++p) {
+      if (p >= np) break;
+      const int64_t I = I0 + p;
+      Real T[4];
+      if (L.ly.kind == 0) {
+        if constexpr (Plain) {
+          layer_terms_d(L, a.lin_in_tau, I, cur[p], T);
+        } else {
+          merge_lean(cur[p], L.scal_up_f, L.scal_dn_f, L.ka, L.kt, L.kb, vfp[p], cv3p[p], a.lin_in_tau, &Bprev[p],
+                     L.bot_is_prev_top != 0 && Bprev[p] >= 0.f, &R[p], &F[p]);
+          continue;
+        }
+      } else {
+        Bprev[p] = -1.f;
+        const Stencil<Real> st = interp_stencil<Real>(L.ly, I);
+        if (st.n == 1) {
+          layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[0], T);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) T[c] = 0;
+          for (int k = 0; k < 4; ++k) {
+            Real t[4];
+            layer_terms_ext<Plain>(L, a.lin_in_tau, st.i[k], t);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) T[c] += st.w[k] * t[c];
+          }
         }
       }
+      R[p] = T[2] + T[0] * (R[p] + T[3] * F[p]);
+      F[p] = T[0] * T[1] * F[p];
     }
-    R = T[2] + T[0] * (R + T[3] * F);
-    F = T[0] * T[1] * F;
   }
   if (a.final_out) {
-    a.final_out[I - 1] = (double)R;
+    double out[kRtPts];
+#pragma unroll
+    for (int p = 0; p < kRtPts; ++p) out[p] = (double)R[p];
+    store_pts(a.final_out, I0, np, out);
   } else {
-    reinterpret_cast<Real*>(a.rad_out)[I - 1] = R;
-    reinterpret_cast<Real*>(a.refl_out)[I - 1] = F;
+    store_pts(reinterpret_cast<Real*>(a.rad_out), I0, np, R);
+    store_pts(reinterpret_cast<Real*>(a.refl_out), I0, np, F);
   }
 }
 

@@ -1953,6 +1953,9 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       L.vf1 = (float)P.dv;
       L.scal_up_f = (float)L.scal_up;
       L.scal_dn_f = (float)L.scal_dn;
+      L.ka = (float)(kRADCN2 / col->tave[il]);
+      L.kt = (float)(kRADCN2 / col->ttop[il]);
+      L.kb = (float)(kRADCN2 / col->tbot[il]);
       // the same level temperature, on the same OD grid as the previous layer
       L.bot_is_prev_top = (il > first && col->tbot[il] == col->ttop[il - 1] && L.ly.kind == 0 &&
                            h->rtseg_host[il - first - 1].ly.kind == 0 && P.dv == rp.hps[il - 1].P.dv)
@@ -1993,9 +1996,12 @@ int clblm_gpu_rt_mode2(clblm_handle_t* h, const clblm_column_t* col, const clblm
       a.omemis_f = (float)(1.0 - a.emis);
       a.vs0 = (float)a.v1;
       a.vs1 = (float)a.mr.dvin;
+      a.vr0 = (float)col->v1;
+      a.vr1 = (float)rp.grid_dv[il];
       auto rt = [&](int v) {
         const int nt = kRtThreads[v];
-        const unsigned grid = (unsigned)((a.n_out + nt - 1) / nt);
+        const int64_t per_cta = (int64_t)nt * kRtPts;
+        const unsigned grid = (unsigned)((a.n_out + per_cta - 1) / per_cta);
         if (plain) k_rt_segment<true><<<grid, nt, 0, h->stream>>>(a);
         else k_rt_segment<false><<<grid, nt, 0, h->stream>>>(a);
       };
