@@ -312,8 +312,7 @@ def jacobian_leg(cont, steps):
         # max |mixed - FP64| over the largest |FP64| Jacobian of all levels
         # (levels under an opaque lower atmosphere have Jacobians near 1e-50,
         # below FP32's range, so a per-level ratio says nothing); levels that
-        # are not finite in FP64 (level2layer's log ratio of equal mixing
-        # ratios) are left out
+        # are not finite in FP64, if any, are left out
         ok = torch.isfinite(p[key]).all(dim=1)
         scale = p[key][ok].abs().max()
         d = (m[key][ok] - p[key][ok]).abs().max()
@@ -323,6 +322,63 @@ def jacobian_leg(cont, steps):
     res["workload"] = ("60-layer column, 120k lines, 600-1100 cm-1: radiance + dR/dT and dR/dln q(H2O) of all "
                        "61 levels (noScattJacob, 100000-point blocks, uniform DV)")
     res["speedup_mixed_vs_plain"] = res["plain"]["ms_per_step"] / res["mixed"]["ms_per_step"]
+    h.close()
+    return res
+
+
+def autograd_leg(cont, steps):
+    """The radiance of the 60-layer column over 600-1100 cm-1 as a
+    differentiable function of its level profile (torch.autograd): forward
+    (layers from the levels by ALAYER + FPACK, then the radiance alone) and
+    backward (the vector-Jacobian product of clblm_gpu_jac_vjp: the layer ODs
+    formed again block by block and every block's derivatives reduced against
+    the gradient), mixed path; the backward's agreement with the dense
+    Jacobians contracted with the same gradient (one FP64 call each)."""
+    import torch
+    from clblm_gb300 import capi, synth, torch_ops
+    from clblm_gb300 import capi_types as T
+    lines, col, _ = synth.config1()
+    lines, col = lines.window(600.0, 1100.0), col.with_window(600.0, 1100.0)
+    h = capi.Handle(lines, cont)
+    ctrl = T.rt_ctrl(precision=T.CLBLM_PREC_MIXED, grid_type=1)
+    p = torch_ops.RadianceProblem.from_column(h, ctrl, col)
+    t0, q0 = p.levels(np.append(col.tbot, col.ttop[-1]))
+    ts = torch.tensor(col.tskin, dtype=torch.float64, device="cuda")
+    em = torch.tensor(col.emis, dtype=torch.float64, device="cuda")
+
+    def step():
+        t = t0.clone().requires_grad_()
+        q = q0.clone().requires_grad_()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        rad = torch_ops.nadir_radiance(p, t, q, ts, em)
+        torch.cuda.synchronize()
+        b = time.perf_counter()
+        rad.sum().backward()
+        torch.cuda.synchronize()
+        c = time.perf_counter()
+        return (b - a) * 1e3, (c - b) * 1e3, len(rad), t.grad
+
+    step()  # warm-up
+    fw, bw = [], []
+    for _ in range(steps):
+        f_ms, b_ms, n, gt = step()
+        fw.append(f_ms)
+        bw.append(b_ms)
+    res = {"workload": "60-layer column, 120k lines, 600-1100 cm-1: radiance of the level profile (forward) and "
+                       "the gradient of its sum with respect to the 61 level temperatures and ln q(H2O), Tskin "
+                       "and emissivity (backward: vector-Jacobian product, no stored Jacobian)",
+           "points": n, "forward_ms": float(np.min(fw)), "backward_ms": float(np.min(bw)),
+           "forward_plus_backward_ms": float(np.min(fw) + np.min(bw)), "steps": steps}
+    # against the dense Jacobians (FP64 both)
+    c0, prof0 = p.state(np.append(col.tbot, col.ttop[-1]), q0.cpu().numpy(), col.tskin, col.emis)
+    pc = T.clblm_rt_ctrl_t.from_buffer_copy(p.ctrl)
+    pc.od.precision = T.CLBLM_PREC_PLAIN
+    g = np.random.default_rng(0).standard_normal(n)
+    dense = h.jac(c0, pc, prof0)
+    v = h.jac_vjp(c0, pc, prof0, g)
+    want = dense["dtlev"] @ g
+    res["fp64_vjp_vs_dense_jacobians_max_rel"] = float(np.max(np.abs(v["g_tlev"] - want) / np.abs(want)))
     h.close()
     return res
 
@@ -721,6 +777,7 @@ def main():
     jacl = None
     if not args.no_jac:
         jacl = jacobian_leg(cont, max(1, min(args.steps, 3)))
+        jacl["autograd"] = autograd_leg(cont, max(1, min(args.steps, 3)))
     batl = None
     if not args.no_batch:
         batl = batch_leg(cont, 1)

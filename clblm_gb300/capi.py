@@ -23,7 +23,8 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
-           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts", "clblm_gpu_od_lines")
+           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts", "clblm_gpu_od_lines",
+           "clblm_gpu_jac_vjp")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -71,6 +72,8 @@ def lib():
                                          P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_jac.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t)] + \
             [C.c_void_p] * 5 + [C.c_int64, C.c_int32]
+        L.clblm_gpu_jac_vjp.argtypes = [C.c_void_p, P(T.clblm_column_t), P(T.clblm_rt_ctrl_t), P(T.clblm_jac_t),
+                                        C.c_void_p, C.c_int64] + [P(C.c_double)] * 4 + [C.c_int32]
         L.clblm_gpu_batch_size.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t),
                                            P(C.c_int64), P(C.c_double)]
         L.clblm_gpu_batch.argtypes = [C.c_void_p, P(T.clblm_profile_t), C.c_int32, P(T.clblm_rt_ctrl_t), C.c_int32]
@@ -230,10 +233,29 @@ def _jac_methods():
                                         C.c_void_p(dtsfc or None), C.c_void_p(demis or None), cap,
                                         T.CLBLM_OUT_DEVICE))
 
-    return jac_size, jac, jac_device
+    def jac_vjp(self, col, ctrl, jac, g, n=None):
+        """Sums over the spectrum of g times each Jacobian (clblm_gpu_jac_vjp):
+        dict of g_tlev [nlay+1], g_qlev [nlay+1], g_tskin, g_emis.  `g` is a
+        numpy array (host) or a device address with its length `n`."""
+        nl = col.nlay
+        out = {"g_tlev": np.zeros(nl + 1), "g_qlev": np.zeros(nl + 1)}
+        ts, em = C.c_double(), C.c_double()
+        cs, js = col.struct(), jac.struct()
+        if isinstance(g, np.ndarray):
+            g = np.ascontiguousarray(g, dtype=np.float64)
+            ptr, n, flags = g.ctypes.data_as(C.c_void_p), len(g), T.CLBLM_OUT_HOST
+        else:
+            ptr, flags = C.c_void_p(g), T.CLBLM_OUT_DEVICE
+        self._check(lib().clblm_gpu_jac_vjp(self.h, C.byref(cs), C.byref(ctrl), C.byref(js), ptr, n,
+                                            _dp(out["g_tlev"]), _dp(out["g_qlev"]), C.byref(ts), C.byref(em),
+                                            flags))
+        out["g_tskin"], out["g_emis"] = ts.value, em.value
+        return out
+
+    return jac_size, jac, jac_device, jac_vjp
 
 
-Handle.jac_size, Handle.jac, Handle.jac_device = _jac_methods()
+Handle.jac_size, Handle.jac, Handle.jac_device, Handle.jac_vjp = _jac_methods()
 
 
 def _profiles(cols, jacs):

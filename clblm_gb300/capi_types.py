@@ -90,8 +90,8 @@ def scan_struct(funct_id, hwhm, v1out, v2out, padding=0.0, prebox_hw=-1.0, decon
 
 
 class JacProfile:
-    """Level pressures and Jacobian-molecule mixing ratios (level 0 at the
-    surface) and the clblm_jac_t view of them."""
+    """Level pressures [mb] and Jacobian-molecule number densities [molec/cm3]
+    (level 0 at the surface) and the clblm_jac_t view of them."""
 
     def __init__(self, plev, qlev, jac_mol=1, do_temp=1):
         self.plev = np.ascontiguousarray(plev, dtype=np.float64)
@@ -270,7 +270,8 @@ class Column:
         return layer_struct(self.mol_id, self.w[il], self.wtot[il], self.pave[il], self.tave[il],
                             lay_no=il + 1)
 
-    LEVEL_FIELDS = ("p_lev", "q_h2o_lev")  # optional level profiles ([nlay+1], level 0 at the bottom)
+    # optional level profiles ([nlay+1, ...], level 0 at the bottom)
+    LEVEL_FIELDS = ("p_lev", "q_h2o_lev", "z_lev", "vmr_lev")
 
     def sub(self, layers):
         idx = np.asarray(layers)

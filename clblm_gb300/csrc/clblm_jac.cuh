@@ -38,7 +38,17 @@ struct JacArgs {
   double *rad, *dtlev, *dqlev, *dtsfc, *demis;  // outputs (any may be null)
   int64_t ld;              // row length of the level-major outputs
   int64_t off;             // first output point of the block
+  // vector-Jacobian product instead of the outputs above: g[off + i] is the
+  // cotangent of the radiance at point i; each CTA writes the g-weighted sums
+  // of its points' level T and ln q derivatives, dR/dTskin and dR/demis to
+  // part[blockIdx.x][0 .. 2 (nlay + 1) + 2)
+  const double* g;
+  double* part;
 };
+constexpr int kJacMaxWarps = 4;  // warps of the largest k_jac block (128 threads)
+// slots of a CTA's partial sums: level T derivatives [0, nlay], level ln q
+// derivatives [nlay + 1, 2 nlay + 1], then dR/dTskin and dR/demis
+__host__ __device__ constexpr int jac_vjp_slots(int nlay) { return 2 * (nlay + 1) + 2; }
 
 __global__ void k_interp_map_jobs(const JacJob* jobs, int njob);
 // k_od_jobs: threads per CTA and output points per CTA
@@ -48,5 +58,7 @@ template <bool Plain>
 __global__ void k_od_jobs(const JacJob* jobs, int njob, const void* od_all, void* out);
 template <bool Plain>
 __global__ void k_jac(JacArgs a);
+// acc[k] += the CTAs' partial sums part[c][k], c = 0 .. nctas-1 in order
+__global__ void k_vjp_accum(const double* part, int nctas, int nslot, double* acc);
 
 }  // namespace clblm

@@ -158,12 +158,28 @@ __device__ __forceinline__ void rlin_t(Real od, Real* hlf, Real* dhlf) {
   }
 }
 
+__device__ __forceinline__ double warp_sum_d(double v) {
+  // butterfly: every lane ends with the same sum, added in the same order
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
 template <bool Plain>
 __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
   using Real = typename std::conditional<Plain, double, float>::type;
-  const int64_t iv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t iv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int N2 = a.nlay;
   constexpr int M = kMaxJacLayers + 2;
+  // vector-Jacobian product: per warp, the g-weighted sums of every slot
+  const bool vjp = a.g != nullptr;
+  __shared__ double s_vjp[kJacMaxWarps][jac_vjp_slots(kMaxJacLayers)];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nslot = jac_vjp_slots(N2);
+  if (vjp) {
+    for (int k = lane; k < nslot; k += 32) s_vjp[warp][k] = 0.;
+    __syncwarp();
+  }
   // mixed path: FP32 copies of the profile's per-layer arrays, converted once
   // per block (a conversion from binary64 runs on the FP64 unit)
   enum { kAmf, kTlev, kTlay, kTup, kTlo, kQup, kQlo, kRt100, kNc };
@@ -188,7 +204,23 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
     if constexpr (Plain) return arr[i];
     else return s_c[c][i];
   };
-  if (iv >= a.nout) return;
+  // past the block's end: nothing to write; for the product, every lane takes
+  // part in the warp sums, with the last point and a zero weight
+  const bool live = iv < a.nout;
+  if (!live) {
+    if (!vjp) return;
+    iv = a.nout - 1;
+  }
+  const double gval = vjp && live ? a.g[a.off + iv] : 0.;
+  // one output value: written, or weighted by g and summed over the warp
+  auto put = [&](double* dst, int64_t idx, int slot, Real val) {
+    if (vjp) {
+      const double v = warp_sum_d((double)val * gval);
+      if (lane == 0) s_vjp[warp][slot] = v;
+    } else if (dst) {
+      dst[idx] = (double)val;
+    }
+  };
   Real viewOD[M], downOD[M], Bbar[M], dBbar[M], Blev[M], dBlev[M], cumTxA[M], cumTxB2[M];
   Real dRad_dT_up[M], dRad_dT_dn[M], dRad_dTbar[M], dRad_dTau[M], dRad_dTlev[M];
   const Real* jod = reinterpret_cast<const Real*>(a.jod);
@@ -302,11 +334,11 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
       }
   }
   const int64_t o = a.off + iv;
-  if (a.rad) a.rad[o] = (double)rad;
-  if (a.dtsfc) a.dtsfc[o] = (double)dRad_dTsfc;
-  if (a.demis) a.demis[o] = (double)dRad_dEmis;
+  if (a.rad && !vjp) a.rad[o] = (double)rad;
+  put(a.dtsfc, o, 2 * N2 + 2, dRad_dTsfc);
+  put(a.demis, o, 2 * N2 + 3, dRad_dEmis);
   // drv_LevelTemp: dTau/dT = [tau(T+1) - tau(T)] - (Wtot/T) dTau/dWtot
-  if (dT && a.dtlev && a.vT >= 0) {
+  if (dT && (a.dtlev || vjp) && a.vT >= 0) {
     Real lo = 0;
     for (int il = 0; il < N2; ++il) {
       const Real m = jod[(int64_t)il * a.nout + iv];
@@ -326,23 +358,40 @@ __global__ void __launch_bounds__(128) k_jac(JacArgs a) {
       const Real dRaddT = dRad_dTau[il + 1] * dTau_dT;
       const Real up = dRaddT * lc(kTup, a.dT_dTup, il);
       lo = lo + dRaddT * lc(kTlo, a.dT_dTlo, il) + dRad_dTlev[il + 1];
-      a.dtlev[(int64_t)il * a.ld + o] = (double)lo;
-      if (il == N2 - 1) a.dtlev[(int64_t)N2 * a.ld + o] = (double)(up + dRad_dTlev[il + 2]);
+      put(a.dtlev, (int64_t)il * a.ld + o, il, lo);
+      if (il == N2 - 1) put(a.dtlev, (int64_t)N2 * a.ld + o, N2, up + dRad_dTlev[il + 2]);
       lo = up;
     }
   }
   // drv_LevelConc: dTau/dln W = the OD of the molecule alone
-  if (a.dqlev && a.vM >= 0) {
+  if ((a.dqlev || vjp) && a.vM >= 0) {
     Real lo = 0;
     for (int il = 0; il < N2; ++il) {
       const Real dRad_dW = dRad_dTau[il + 1] * jod[((int64_t)a.vM * N2 + il) * a.nout + iv];
       const Real up = dRad_dW * lc(kQup, a.dW_dQup, il);
       lo = lo + dRad_dW * lc(kQlo, a.dW_dQlo, il);
-      a.dqlev[(int64_t)il * a.ld + o] = (double)lo;
-      if (il == N2 - 1) a.dqlev[(int64_t)N2 * a.ld + o] = (double)up;
+      put(a.dqlev, (int64_t)il * a.ld + o, N2 + 1 + il, lo);
+      if (il == N2 - 1) put(a.dqlev, (int64_t)N2 * a.ld + o, 2 * N2 + 1, up);
       lo = up;
     }
   }
+  if (vjp) {  // the CTA's sums, warp by warp in order
+    __syncthreads();
+    const int nw = (int)(blockDim.x >> 5);
+    for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+      double sum = 0.;
+      for (int w = 0; w < nw; ++w) sum += s_vjp[w][k];
+      a.part[(int64_t)blockIdx.x * nslot + k] = sum;
+    }
+  }
+}
+
+__global__ void k_vjp_accum(const double* __restrict__ part, int nctas, int nslot, double* __restrict__ acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nslot) return;
+  double sum = acc[k];
+  for (int c = 0; c < nctas; ++c) sum += part[(int64_t)c * nslot + k];
+  acc[k] = sum;
 }
 
 template __global__ void k_jac<false>(JacArgs);

@@ -110,6 +110,7 @@ struct clblm_handle {
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
   DevBuf reclo;     // low parts of the records' ZFL/ZSLOPE
   DevBuf jprof, jod, jmap, jjobs, jblk;  // Jacobians: profiles, block ODs, maps, jobs, grid blocks
+  DevBuf jvjp;                          // vector-Jacobian product: CTA partial sums and the totals
   DevBuf f4blk, f4ntot, f4cidx, f4vb, f4lb, f4src, f4flag, f4cut, f4grp, f4nxt, ragg;
   DevBuf segpool;  // radiation-term segments of panels with more than kMaxSeg
   DevBuf rt[4], outbuf, imap[2];
@@ -129,7 +130,7 @@ struct clblm_handle {
                               &f4nmir,    &f4pm,     &f4sm,      &err,     &outbuf,  &pblk,   &bv1,     &bn,
                               &bm0,       &bfac,     &f4blk,     &f4ntot,  &f4cidx,  &f4vb,   &f4lb,    &f4src,
                               &f4flag,    &f4cut,    &f4grp,     &f4nxt,   &ragg,    &segpool, &gpm,    &gsm,
-                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk};
+                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk,    &jvjp};
     for (auto& b : rt) v.push_back(&b);
     for (auto& b : imap) v.push_back(&b);
     v.push_back(&rtseg);
@@ -2166,7 +2167,7 @@ extern "C" int clblm_gpu_interp_spectrum_noalloc(const double* d_in, int64_t nin
 namespace {
 
 // k_jac over the block's points with the tuned block size
-int launch_jac(clblm_handle* h, const JacArgs& a, bool plain) {
+int launch_jac(clblm_handle* h, const JacArgs& a, bool plain, int* grid_used = nullptr) {
   auto jac = [&](int v) {
     const int nt = kJacThreads[v];
     const unsigned grid = (unsigned)((a.nout + nt - 1) / nt);
@@ -2174,10 +2175,14 @@ int launch_jac(clblm_handle* h, const JacArgs& a, bool plain) {
     else k_jac<false><<<grid, nt, 0, h->stream>>>(a);
   };
   int tv = h->tune.jac[plain ? 1 : 0];
-  if (tv < 0) {
+  // the product's partial sums are written once per launch (the variants'
+  // grids differ), so it is timed only for the plain outputs
+  if (tv < 0 && !a.g) {
     int rc = tune_pick(h, h->stream, 2, 1, jac, &h->tune.jac[plain ? 1 : 0], &tv);
     if (rc) return rc;
   }
+  if (tv < 0) tv = 1;
+  if (grid_used) *grid_used = (int)((a.nout + kJacThreads[tv] - 1) / kJacThreads[tv]);
   h->launches++;
   jac(tv);
   cudaError_t e = cudaGetLastError();
@@ -2225,7 +2230,6 @@ int jac_setup(clblm_handle* h, const clblm_column_t* col, const clblm_rt_ctrl_t*
   if (col->nlay > kMaxJacLayers) return set_err(h, CLBLM_ERR_UNSUPPORTED, "more than %d layers", kMaxJacLayers);
   if (ctrl->grid_type != 1)
     return set_err(h, CLBLM_ERR_GRID, "noScattJacob: spectral grid is not uniform (gridType 1)");
-  if (!col->tbot || !col->ttop || !col->wtot_down) return set_err(h, CLBLM_ERR_ARG, "bad column");
   if (int rc0 = check_column_rt(h, col)) return rc0;
   const int nl = col->nlay, nmol = col->nmol;
   if (jac->jac_mol > 0) {
@@ -2436,9 +2440,23 @@ int clblm_gpu_jac_size(clblm_handle_t* h, const clblm_column_t* col, const clblm
   return CLBLM_OK;
 }
 
-int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac,
-                  double* rad, double* dr_dtlev, double* dr_dqlev, double* dr_dtskin, double* dr_demis, int64_t cap,
-                  int32_t flags) {
+}  // extern "C"
+
+namespace {
+
+// The product of clblm_gpu_jac_vjp: the cotangent g of the radiance (npts
+// values, device or host memory) and the host array that receives the
+// g-weighted sums of the Jacobians (jac_vjp_slots(nlay) values).
+struct JacVjp {
+  const double* g = nullptr;
+  int64_t n = 0;
+  bool g_dev = false;
+  double* acc = nullptr;
+};
+
+int jac_impl(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac,
+             double* rad, double* dr_dtlev, double* dr_dqlev, double* dr_dtskin, double* dr_demis, int64_t cap,
+             int32_t flags, const JacVjp* vjp) {
   if (!h) return CLBLM_ERR_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
   JacSetup js;
@@ -2451,8 +2469,17 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
   std::vector<JacBlock> blocks;
   rc = jac_block_list(h, col, ctrl, js, dvn, dvf, &blocks);
   if (rc) return rc;
-  int64_t npts = 0;
-  for (auto& b : blocks) npts += b.n;
+  int64_t npts = 0, nmax = 0;
+  for (auto& b : blocks) {
+    npts += b.n;
+    nmax = std::max(nmax, b.n);
+  }
+  if (vjp) {
+    if (vjp->n != npts) return set_err(h, CLBLM_ERR_ARG, "the cotangent has %lld points, the spectrum %lld",
+                                       (long long)vjp->n, (long long)npts);
+    rad = dr_dtlev = dr_dqlev = dr_dtskin = dr_demis = nullptr;
+    cap = npts;
+  }
   if (cap < npts) return set_err(h, CLBLM_ERR_CAPACITY, "Jacobian spectra need %lld points", (long long)npts);
   h->reset_call();
   // layer and level profiles
@@ -2486,6 +2513,27 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     o_dem = dr_demis ? b + 2 * npts : nullptr;
     o_dtl = dr_dtlev ? b + 3 * npts : nullptr;
     o_dql = dr_dqlev ? b + 3 * npts + (size_t)(nl + 1) * npts : nullptr;
+  }
+  // the product: the cotangent on the device, the CTAs' partial sums of a
+  // block (the smallest tuned block, 64 threads, has the most CTAs) and the
+  // running totals
+  const int nslot = jac_vjp_slots(nl);
+  const double* d_g = nullptr;
+  double *d_part = nullptr, *d_acc = nullptr;
+  if (vjp) {
+    if (vjp->g_dev) {
+      d_g = vjp->g;
+    } else {
+      CUDA_TRY(h, h->outbuf.ensure(sizeof(double) * (size_t)npts));
+      CUDA_TRY(h, cudaMemcpyAsync(h->outbuf.p, vjp->g, sizeof(double) * (size_t)npts, cudaMemcpyHostToDevice,
+                                  h->stream));
+      d_g = h->outbuf.as<double>();
+    }
+    const int64_t ctas = (nmax + kJacThreads[0] - 1) / kJacThreads[0];
+    CUDA_TRY(h, h->jvjp.ensure(sizeof(double) * (size_t)nslot * (size_t)(ctas + 1)));
+    d_acc = h->jvjp.as<double>();
+    d_part = d_acc + nslot;
+    CUDA_TRY(h, cudaMemsetAsync(d_acc, 0, sizeof(double) * (size_t)nslot, h->stream));
   }
   int jr = h->jrad;
   bool fp = h->first_pass_jrad;
@@ -2632,13 +2680,26 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     a.demis = o_dem;
     a.ld = ld;
     a.off = total;
-    rc = launch_jac(h, a, plain);
+    a.g = d_g;
+    a.part = d_part;
+    int grid = 0;
+    rc = launch_jac(h, a, plain, &grid);
     if (rc) return rc;
+    if (vjp) {
+      h->launches++;
+      k_vjp_accum<<<(unsigned)((nslot + 127) / 128), 128, 0, h->stream>>>(d_part, grid, nslot, d_acc);
+      CUDA_TRY(h, cudaGetLastError());
+    }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     total += nlim;
   }
   h->first_pass_jrad = fp;
   h->jrad = jr;
+  if (vjp) {
+    CUDA_TRY(h, cudaMemcpy(vjp->acc, d_acc, sizeof(double) * (size_t)nslot, cudaMemcpyDeviceToHost));
+    h->last.launches = h->launches;
+    return CLBLM_OK;
+  }
   if (!dev) {
     auto row = [&](double* dst, const double* src) -> cudaError_t {
       return dst && src ? cudaMemcpyAsync(dst, src, sizeof(double) * npts, cudaMemcpyDeviceToHost, h->stream)
@@ -2656,6 +2717,37 @@ int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_c
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   }
   h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clblm_gpu_jac(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl, const clblm_jac_t* jac,
+                  double* rad, double* dr_dtlev, double* dr_dqlev, double* dr_dtskin, double* dr_demis, int64_t cap,
+                  int32_t flags) {
+  return jac_impl(h, col, ctrl, jac, rad, dr_dtlev, dr_dqlev, dr_dtskin, dr_demis, cap, flags, nullptr);
+}
+
+int clblm_gpu_jac_vjp(clblm_handle_t* h, const clblm_column_t* col, const clblm_rt_ctrl_t* ctrl,
+                      const clblm_jac_t* jac, const double* g, int64_t n, double* g_tlev, double* g_qlev,
+                      double* g_tskin, double* g_emis, int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!g || !col || col->nlay < 1) return set_err(h, CLBLM_ERR_ARG, "bad cotangent or column");
+  const int nl = col->nlay;
+  std::vector<double> acc(jac_vjp_slots(nl), 0.);
+  JacVjp v;
+  v.g = g;
+  v.n = n;
+  v.g_dev = flags == CLBLM_OUT_DEVICE;
+  v.acc = acc.data();
+  const int rc = jac_impl(h, col, ctrl, jac, nullptr, nullptr, nullptr, nullptr, nullptr, 0, CLBLM_OUT_DEVICE, &v);
+  if (rc) return rc;
+  if (g_tlev) std::copy(acc.begin(), acc.begin() + nl + 1, g_tlev);
+  if (g_qlev) std::copy(acc.begin() + nl + 1, acc.begin() + 2 * nl + 2, g_qlev);
+  if (g_tskin) *g_tskin = acc[2 * nl + 2];
+  if (g_emis) *g_emis = acc[2 * nl + 3];
   return CLBLM_OK;
 }
 

@@ -105,15 +105,31 @@ def atmosphere(nlay, p_top, v1, v2, mols=SEVEN, p_sfc=1013.0, scale_height=7.0,
     col = Column(mols, pave, tave, t_lev[:-1], t_lev[1:], w, wair, SECANT_DIFFUSE * wair,
                  v1, v2, t_lev[0], emis)
     col.p_lev = p_lev
+    col.z_lev = z_lev
     col.q_h2o_lev = np.maximum(1.0e-2 * np.exp(-z_lev / 2.0), 4.0e-6)
+    # volume mixing ratios of every absorber at the levels [nlay+1, nmol]
+    col.vmr_lev = np.stack([col.q_h2o_lev if m == 1 else np.full(nlay + 1, other_vmr) for m in mols], axis=1)
     return col
 
 
+# Boltzmann's constant in the units of level2layer's air density P/(T k)
+# with P in mb (clblm_noScattJac.f90:1243-1244)
+BOLTZ_MB = 1.3806503E-19
+
+
+def level_density(p_lev, t_lev, vmr_lev):
+    """Number density [molec/cm3] of an absorber at levels: vmr P/(k T), the
+    level concentrations the reference's Jacobians take (viewPath%Q,
+    densityOnPathLevel, clblm_AtmPath.f90:1278,1306-1313)."""
+    return np.asarray(vmr_lev) * np.asarray(p_lev) / (np.asarray(t_lev) * BOLTZ_MB)
+
+
 def jac_profile(col, jac_mol=1, do_temp=1):
-    """Level pressures and H2O mixing ratios of a column made by atmosphere(),
-    as the Jacobian inputs (level 0 at the surface)."""
+    """Level pressures and H2O number densities of a column made by
+    atmosphere(), as the Jacobian inputs (level 0 at the surface)."""
     from .capi_types import JacProfile
-    return JacProfile(col.p_lev, col.q_h2o_lev, jac_mol=jac_mol, do_temp=do_temp)
+    t_lev = np.append(col.tbot, col.ttop[-1])
+    return JacProfile(col.p_lev, level_density(col.p_lev, t_lev, col.q_h2o_lev), jac_mol=jac_mol, do_temp=do_temp)
 
 
 # ---- the benchmark workloads --------------------------------------------

@@ -165,7 +165,12 @@ typedef struct {
  * column's tbot[0..nlay-1] and ttop[nlay-1]. */
 typedef struct {
   const double *plev;   /* [nlay+1] level pressure, mbar                       */
-  const double *qlev;   /* [nlay+1] volume mixing ratio of jac_mol at levels   */
+  const double *qlev;   /* [nlay+1] number density of jac_mol at the levels,
+                         * molec/cm3: the path's level concentrations that
+                         * noScattJacob hands to level2layer (viewPath%Q,
+                         * clblm_noScattJac.f90:162-167, from
+                         * densityOnPathLevel, clblm_AtmPath.f90:1278); the
+                         * molecule Jacobians are per unit of its logarithm  */
   int32_t jac_mol;      /* HITRAN number of the Jacobian molecule (1: H2O);
                          * 0: no molecule Jacobian                              */
   int32_t do_temp;      /* 1: level-temperature Jacobians                      */
@@ -327,6 +332,26 @@ int clblm_gpu_jac(clblm_handle_t *h, const clblm_column_t *col,
                   double *rad, double *dr_dtlev, double *dr_dqlev,
                   double *dr_dtskin, double *dr_demis, int64_t cap,
                   int32_t flags);
+
+/* Vector-Jacobian product of the same radiance: for a cotangent g on the
+ * grid of clblm_gpu_jac_size (n points; device memory with CLBLM_OUT_DEVICE
+ * in flags, else host), the sums over the spectrum of g times each
+ * Jacobian of clblm_gpu_jac:
+ *   g_tlev [nlay+1]  sum_i g_i dR_i/dT of each level
+ *   g_qlev [nlay+1]  sum_i g_i dR_i/d ln q of each level (jac->jac_mol)
+ *   g_tskin, g_emis  sum_i g_i dR_i/dTskin, sum_i g_i dR_i/demis
+ * (host memory; any may be NULL).  It runs noScattJacob's layer ODs block by
+ * block as clblm_gpu_jac does and reduces every block's derivatives against
+ * g on the device as they are formed, so no (nlay+1) x n Jacobian is stored:
+ * the backward pass of a gradient through the radiance.  The sums are formed
+ * in a fixed order (per CTA, then CTA by CTA and block by block), so a call
+ * repeats bit for bit.  No counterpart routine in the reference, whose
+ * Jacobians (clblm_noScattJac.f90:346-716, 899-1203) it contracts. */
+int clblm_gpu_jac_vjp(clblm_handle_t *h, const clblm_column_t *col,
+                      const clblm_rt_ctrl_t *ctrl, const clblm_jac_t *jac,
+                      const double *g, int64_t n, double *g_tlev,
+                      double *g_qlev, double *g_tskin, double *g_emis,
+                      int32_t flags);
 
 /* ---- many profiles in one call ----------------------------------------------
  *

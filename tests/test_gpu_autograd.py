@@ -1,6 +1,8 @@
-"""The torch.autograd binding of the radiance Jacobians (GPU): the backward
-pass applies the analytic Jacobians, checked against central finite
-differences of the radiance computed through the same C-ABI."""
+"""The radiance as a differentiable function of the level profile (GPU):
+clblm_gpu_jac_vjp against clblm_gpu_jac's Jacobians contracted with the same
+cotangent, the torch.autograd binding at states other than the profile's
+own, and the gradient against central finite differences of the forward
+pass (levels -> ALAYER/FPACK layers -> radiance)."""
 import numpy as np
 import pytest
 
@@ -10,97 +12,116 @@ from clblm_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _problem(gpu_lib, mtckd, col=None, precision=T.CLBLM_PREC_PLAIN, first=10):
+def _problem(gpu_lib, mtckd, precision=T.CLBLM_PREC_PLAIN, first=10, nl=3, window=(1000.0, 1002.0)):
     from clblm_gb300 import torch_ops
     lines, full, _ = synth.config1(n_lines=20000)
-    nl = 3
-    c = col if col is not None else full.sub(list(range(first, first + nl))).with_window(1000.0, 1002.0)
-    prof = synth.jac_profile(full).sub(first, nl)
+    col = full.sub(list(range(first, first + nl))).with_window(*window)
     h = gpu_lib.Handle(lines, mtckd)
     ctrl = T.rt_ctrl(precision=precision, grid_type=1, lin_in_tau=1)
-    return torch_ops.RadianceProblem(h, c, ctrl, prof), c, prof, h
+    return torch_ops.RadianceProblem.from_column(h, ctrl, col), col, h
 
 
-def _radiance(gpu_lib, mtckd, col):
-    p, _, _, h = _problem(gpu_lib, mtckd, col)
-    out = h.jac(col, p.ctrl, p.prof)
-    h.close()
-    return out["rad"]
+def _tlev(col):
+    return np.append(col.tbot, col.ttop[-1])
 
 
-def test_backward_is_jacobian_transpose(gpu_lib, mtckd):
+@pytest.mark.parametrize("precision,rtol", [(T.CLBLM_PREC_PLAIN, 1e-10), (T.CLBLM_PREC_MIXED, 1e-9)])
+def test_vjp_is_jacobian_transpose(gpu_lib, mtckd, precision, rtol):
+    """The product reduces exactly the derivatives clblm_gpu_jac writes; the
+    whole 600-1100 cm-1 window of six layers, several 100000-point blocks."""
+    p, col, h = _problem(gpu_lib, mtckd, precision, first=30, nl=6, window=(600.0, 1100.0))
+    try:
+        c, prof = p.state(_tlev(col), np.log(col.vmr_lev[:, 0]), col.tskin, col.emis)
+        ref = h.jac(c, p.ctrl, prof)
+        n = len(ref["rad"])
+        assert n > 200000
+        g = np.random.default_rng(5).standard_normal(n)
+        got = h.jac_vjp(c, p.ctrl, prof, g)
+        again = h.jac_vjp(c, p.ctrl, prof, g)
+    finally:
+        h.close()
+    for k, j in (("g_tlev", "dtlev"), ("g_qlev", "dqlev")):
+        np.testing.assert_allclose(got[k], ref[j] @ g, rtol=rtol, atol=0, err_msg=k)
+        assert np.array_equal(got[k], again[k])  # a fixed summation order
+    assert got["g_tskin"] == pytest.approx(float(ref["dtsfc"] @ g), rel=rtol)
+    assert got["g_emis"] == pytest.approx(float(ref["demis"] @ g), rel=rtol)
+
+
+def test_autograd_at_a_perturbed_state(gpu_lib, mtckd):
+    """Forward at a state other than the profile's own (the layers are formed
+    from the level tensors); backward equals the Jacobians at that state
+    contracted with the incoming gradient."""
     import torch
     from clblm_gb300 import torch_ops
-    p, c, prof, h = _problem(gpu_lib, mtckd)
-    t, q, ts, em = [x.requires_grad_() for x in p.levels()]
-    rad = torch_ops.NadirRadiance.apply(t, q, ts, em, p)
-    ref = h.jac(c, p.ctrl, prof)
-    np.testing.assert_allclose(rad.detach().cpu().numpy(), ref["rad"], rtol=1e-12)
-    g = torch.rand_like(rad)
-    (rad * g).sum().backward()
+    p, col, h = _problem(gpu_lib, mtckd)
+    try:
+        t0, q0 = p.levels(_tlev(col))
+        t = (t0 + torch.tensor([1.5, -0.7, 2.0, 0.3], dtype=torch.float64, device="cuda")).requires_grad_()
+        q = (q0 + 0.05).requires_grad_()
+        ts = torch.tensor(col.tskin + 1.0, dtype=torch.float64, device="cuda", requires_grad=True)
+        em = torch.tensor(0.95, dtype=torch.float64, device="cuda", requires_grad=True)
+        rad = torch_ops.nadir_radiance(p, t, q, ts, em)
+        c, prof = p.state(t.detach().cpu().numpy(), q.detach().cpu().numpy(), float(ts), float(em))
+        ref = h.jac(c, p.ctrl, prof)
+        np.testing.assert_allclose(rad.detach().cpu().numpy(), ref["rad"], rtol=1e-12)
+        c0, prof0 = p.state(_tlev(col), np.log(col.vmr_lev[:, 0]), col.tskin, col.emis)
+        base = h.jac(c0, p.ctrl, prof0)["rad"]
+        assert len(base) == len(ref["rad"])  # one grid for every state
+        assert np.max(np.abs(ref["rad"] / base - 1)) > 1e-3  # the state moved the radiance
+        g = torch.rand_like(rad)
+        (rad * g).sum().backward()
+    finally:
+        h.close()
     gn = g.cpu().numpy()
     np.testing.assert_allclose(t.grad.cpu().numpy(), ref["dtlev"] @ gn, rtol=1e-10)
     np.testing.assert_allclose(q.grad.cpu().numpy(), ref["dqlev"] @ gn, rtol=1e-10)
     assert float(ts.grad) == pytest.approx(float(ref["dtsfc"] @ gn), rel=1e-10)
     assert float(em.grad) == pytest.approx(float(ref["demis"] @ gn), rel=1e-10)
-    h.close()
 
 
-def _shift_col(c, **kw):
-    a = dict(mol_id=c.mol_id, pave=c.pave, tave=c.tave, tbot=c.tbot, ttop=c.ttop, w=c.w, wtot=c.wtot,
-             wtot_down=c.wtot_down, v1=c.v1, v2=c.v2, tskin=c.tskin, emis=c.emis)
-    a.update(kw)
-    return T.Column(**a)
-
-
-def test_surface_derivatives_match_central_differences(gpu_lib, mtckd):
+def test_gradient_against_central_differences(gpu_lib, mtckd):
+    """Directional derivatives of sum(g * radiance) by central differences of
+    the forward pass (0.01 K in the level temperatures, 1e-4 in ln q, 0.01 K
+    in Tskin, 1e-4 in the emissivity) against the gradient.  The reference's
+    dtau/dT is a 1 K forward difference with the Wtot/T correction and its
+    dtau/dln q keeps the self-broadening fixed, and its level maps linearise
+    ALAYER's integrals, so the level terms agree to a few per cent; the
+    surface terms are exact derivatives."""
+    import torch
+    from clblm_gb300 import torch_ops
     # layers 40-42 (a few hPa): thin enough that the surface is seen
-    p, c, prof, h = _problem(gpu_lib, mtckd, first=40)
-    ref = h.jac(c, p.ctrl, prof)
-    h.close()
-    for key, field, step in (("dtsfc", "tskin", 0.01), ("demis", "emis", 1e-4)):
-        rp = _radiance(gpu_lib, mtckd, _shift_col(c, **{field: getattr(c, field) + step}))
-        rm = _radiance(gpu_lib, mtckd, _shift_col(c, **{field: getattr(c, field) - step}))
-        fd = (rp - rm) / (2 * step)
-        scale = np.max(np.abs(ref[key]))
-        assert np.max(np.abs(fd - ref[key])) <= 1e-5 * scale, key
+    p, col, h = _problem(gpu_lib, mtckd, first=40)
+    try:
+        t0, q0 = p.levels(_tlev(col))
+        ts0, em0 = col.tskin, col.emis
+        rng = np.random.default_rng(11)
+        gvec = None
 
+        def f(t, q, ts, em):
+            nonlocal gvec
+            r = torch_ops.nadir_radiance(p, t, q, ts, em)
+            if gvec is None:
+                gvec = torch.tensor(rng.uniform(0.5, 1.5, len(r)), dtype=torch.float64, device="cuda")
+            return (r * gvec).sum()
 
-def _level_shift(c, prof, k, dT=0.0, dlnq=0.0):
-    """The column after level k's temperature or ln q moves, carried into the
-    layers through level2layer's own maps (the reference's linearisation)."""
-    sys_ = __import__("test_oracle_jac")
-    tlev = np.append(c.tbot, c.ttop[-1])
-    dTu, dTl, dWu, dWl = sys_._level2layer(prof.plev, tlev, c.tave, prof.qlev)
-    tave, w = c.tave.copy(), c.w.copy()
-    tlev2 = tlev.copy()
-    tlev2[k] += dT
-    ih = int(np.where(c.mol_id == 1)[0][0])
-    if k < c.nlay:  # layer k has level k at its bottom
-        tave[k] += dTl[k] * dT
-        w[k, ih] *= np.exp(dWl[k] * dlnq)
-    if k > 0:       # layer k-1 has level k at its top
-        tave[k - 1] += dTu[k - 1] * dT
-        w[k - 1, ih] *= np.exp(dWu[k - 1] * dlnq)
-    return _shift_col(c, tave=tave, w=w, tbot=tlev2[:-1], ttop=tlev2[1:], tskin=c.tskin)
-
-
-def test_level_derivatives_against_central_differences(gpu_lib, mtckd):
-    """Central differences in level T (0.01 K) and ln q (1e-4) against the
-    analytic Jacobians.  The reference's dTau/dT is a 1 K forward difference
-    and its dTau/dln q leaves the self-broadening unchanged, so the agreement
-    is that of those approximations (a few per cent), not of rounding."""
-    p, c, prof, h = _problem(gpu_lib, mtckd)
-    ref = h.jac(c, p.ctrl, prof)
-    h.close()
-    worst = {}
-    for k in range(1, c.nlay + 1):
-        for key, kw, step in (("dtlev", "dT", 0.01), ("dqlev", "dlnq", 1e-4)):
-            rp = _radiance(gpu_lib, mtckd, _level_shift(c, prof, k, **{kw: step}))
-            rm = _radiance(gpu_lib, mtckd, _level_shift(c, prof, k, **{kw: -step}))
-            fd = (rp - rm) / (2 * step)
-            a = ref[key][k]
-            err = np.linalg.norm(fd - a) / np.linalg.norm(fd)
-            worst[key, k] = err
+        t = t0.clone().requires_grad_()
+        q = q0.clone().requires_grad_()
+        ts = torch.tensor(ts0, dtype=torch.float64, device="cuda", requires_grad=True)
+        em = torch.tensor(em0, dtype=torch.float64, device="cuda", requires_grad=True)
+        f(t, q, ts, em).backward()
+        worst = {}
+        for name, grad, step, shift in (
+                ("t_lev", t.grad, 0.01, lambda s, d: (t0 + s * d, q0, ts0, em0)),
+                ("lnq_lev", q.grad, 1e-4, lambda s, d: (t0, q0 + s * d, ts0, em0))):
+            d = torch.tensor(rng.choice([-1.0, 1.0], len(t0)), dtype=torch.float64, device="cuda")
+            fd = (f(*shift(step, d)) - f(*shift(-step, d))).item() / (2 * step)
+            an = float((grad * d).sum())
+            worst[name] = abs(fd - an) / abs(fd)
+        for name, grad, step, x0 in (("tskin", ts.grad, 0.01, ts0), ("emis", em.grad, 1e-4, em0)):
+            args = lambda s: (t0, q0, x0 + s, em0) if name == "tskin" else (t0, q0, ts0, x0 + s)
+            fd = (f(*args(step)) - f(*args(-step))).item() / (2 * step)
+            assert float(grad) == pytest.approx(fd, rel=1e-5), name
+    finally:
+        h.close()
     print("relative differences", worst)
     assert max(worst.values()) <= 0.1, worst
