@@ -91,7 +91,10 @@ size_t panel_smem_bytes(bool plain);
 __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* blk_v1, const int* blk_n,
                             double* blk_fac);
 
-template <bool Plain>
+// k_panel in one pass (kPanelAll), or the line sums (kPanelLines) and the far
+// wings, continuum, combine and radiation term (kPanelWings) in two
+constexpr int kPanelAll = 0, kPanelLines = 1, kPanelWings = 2;
+template <bool Plain, int Part>
 __global__ void k_panel(const __grid_constant__ PanelArgs a);
 template <bool Plain, int CHUNK>
 __global__ void k_f4_conv(F4Args a);

@@ -459,8 +459,14 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
   __syncwarp();
 }
 
-template <bool Plain>
+template <bool Plain, int Part>
 __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __grid_constant__ PanelArgs a) {
+  // Part: kPanelAll, or the line sums alone (kPanelLines: the far wings and
+  // the continuum are not yet known), or the rest alone (kPanelWings: R4 and
+  // ABSRB through XINT, the R3->R2->R1 combine and the radiation term, added
+  // to the OD the line pass wrote).  Every step is linear in R3, R2 and R1,
+  // so the two passes give the one-pass OD up to FP32 rounding.
+  constexpr bool kLines = Part != kPanelWings, kWings = Part != kPanelLines;
   using Real = typename std::conditional<Plain, double, float>::type;
   using Acc = typename std::conditional<Plain, SumD, KahanF>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
   } else {
     // one bulk copy of the table image; the CTA waits for it just before its
     // first gather
-    if (tid == 0) {
+    if (kLines && tid == 0) {
       mbar_init(&S.tab_bar, 1);
       mbar_fence_init();
       mbar_arrive_expect_tx(&S.tab_bar, (uint32_t)sizeof(MixedTables));
@@ -565,11 +571,13 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
     const double* AB = a.absrb_all + P.abs_off;  // 1-based
     for (int i = tid; i < S.X.nab; i += blockDim.x) S.absf[i] = (float)AB[S.X.ab0 + i];
   }
-  if (nT1 > 0) tile_ranges(pm1, sm1, rg[0], rg[1], G01, 2 * nT1, S.lo1, S.hi1);
-  tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, 2 * kTiles2, S.lo2, S.hi2);
-  tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, 2 * kTiles3, S.lo3, S.hi3);
+  if (kLines) {
+    if (nT1 > 0) tile_ranges(pm1, sm1, rg[0], rg[1], G01, 2 * nT1, S.lo1, S.hi1);
+    tile_ranges(pm1 + a.stride, sm1 + a.stride, rg[2], rg[3], G02, 2 * kTiles2, S.lo2, S.hi2);
+    tile_ranges(pm1 + 2 * a.stride, sm1 + 2 * a.stride, rg[4], rg[5], G03, 2 * kTiles3, S.lo3, S.hi3);
+  }
   __syncthreads();
-  if constexpr (!Plain) {  // the tables have landed (bounded wait; the error flag otherwise)
+  if constexpr (!Plain && kLines) {  // the tables have landed (bounded wait; the error flag otherwise)
     const bool ok = mbar_wait_bounded(&S.tab_bar, 0);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
@@ -664,8 +672,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
     const int h0 = 2 * t + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * t + 1 : h0;
     const int64_t lo = S.lo3[h0], hi = max(S.lo3[h0], S.hi3[h1]);
     Acc acc;
-    gather_grid<Plain, 3>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
-    if (active) {
+    if (kLines) gather_grid<Plain, 3>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
+    if (active && kWings) {
       // far wings (R4) and continuum (ABSRB) interpolated into R3 (XINT).
       // The R4 block LBLF4Q held when XINT reached the point: this panel's
       // for N1R3 = 6..155, the previous panel's for the carried points 1..5
@@ -727,6 +735,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
         }
       }
       acc.add(extra);
+    }
+    if (active) {
       if (old) S.r3o[J3] = acc.value();
       else S.r3n[J3] = acc.value();
     }
@@ -746,7 +756,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
       int g = kPanelR2 * p + J - 1;
       Acc acc;
       const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
-      gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[h0], max(S.lo2[h0], S.hi2[h1]), g, active, p, acc);
+      if (kLines)
+        gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[h0], max(S.lo2[h0], S.hi2[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 1) & 3;
         int Jg = J - off;
@@ -785,7 +796,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
       int g = kPanelPts * p + J - 1;
       Acc acc;
       const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
-      gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[h0], max(S.lo1[h0], S.hi1[h1]), g, active, p, acc);
+      if (kLines)
+        gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[h0], max(S.lo1[h0], S.hi1[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 33) & 3;
         int Jg = J - off;
@@ -830,14 +842,17 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
             }
           }
         }
-        od[(int64_t)kPanelPts * p + (J - kNSHIFT - 1)] = val;
+        Real* o = od + (int64_t)kPanelPts * p + (J - kNSHIFT - 1);
+        if constexpr (Part == kPanelWings) *o += val;
+        else *o = val;
       }
     }
   }
 }
 
-template __global__ void k_panel<false>(const __grid_constant__ PanelArgs);
-template __global__ void k_panel<true>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<false, kPanelLines>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<false, kPanelWings>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<true, kPanelAll>(const __grid_constant__ PanelArgs);
 
 // ---------------------------------------------------------------------------
 // Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1 (CNVF4Q).

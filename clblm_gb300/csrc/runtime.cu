@@ -151,7 +151,8 @@ struct clblm_handle {
   // per-call sums of the line-shape kernels' work and device time
   // f4 conv start/stop, panel start/stop, batch start, line chain done
   // batch timing: far-wing kernel, panel kernel, line chain (0-5); layer recurrence (6, 7)
-  cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // (8, 9: the mixed path's second panel pass)
+  cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // the far-wing chain runs on a second stream, forked from and joined back
   // into `stream` within each OD batch
   cudaStream_t stream2 = nullptr;
@@ -1073,26 +1074,43 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
                                                             h->bfac.as<double>());
   }
   CUDA_TRY(h, cudaEventRecord(h->ev[5], st));
-  CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
   size_t smem = panel_smem_bytes(plain);
   if (plain) {
+    // FP64: one pass once R4 and ABSRB are ready
+    CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));
     if (!h->panel_attr_set[1]) {
-      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true, kPanelAll>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
       h->panel_attr_set[1] = true;
     }
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-    k_panel<true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    k_panel<true, kPanelAll><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
   } else {
+    // mixed: the line sums run beside the far-wing chain, then, once R4 and
+    // ABSRB are ready, a second pass adds the far wings and the continuum
+    // through XINT and the combine (the OD is linear in R3, R2 and R1)
     if (!h->panel_attr_set[0]) {
-      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelLines>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelWings>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
       h->panel_attr_set[0] = true;
     }
-    h->launches++;
+    h->launches += 2;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-    k_panel<false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    k_panel<false, kPanelLines><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
+    // the radiation-term pool is claimed again by the second pass
+    CUDA_TRY(h, cudaMemsetAsync(pa.seg_next, 0, sizeof(int), st));
+    CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
+    k_panel<false, kPanelWings><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
   }
-  CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
   CUDA_TRY(h, cudaGetLastError());
   return CLBLM_OK;
 }
@@ -1333,6 +1351,9 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
     float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
     CUDA_TRY(h, cudaEventElapsedTime(&t0, h->ev[0], h->ev[1]));
     CUDA_TRY(h, cudaEventElapsedTime(&t1, h->ev[2], h->ev[3]));
+    float t1b = 0.f;
+    CUDA_TRY(h, cudaEventElapsedTime(&t1b, h->ev[8], h->ev[9]));
+    t1 += t1b;
     CUDA_TRY(h, cudaEventElapsedTime(&t2, h->ev[4], h->ev[5]));
     CUDA_TRY(h, cudaEventElapsedTime(&t3, h->ev[4], h->ev[1]));
     h->acc_ms_f4 += t0;
