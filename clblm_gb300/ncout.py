@@ -17,14 +17,21 @@ layout of this package's level-major Jacobian arrays.
 File names follow writeRadiance (:1342-1462) and writeJacobians
 (:1668-1908): root name, product, `_mono`, the observer altitude and view
 angle when set, `_sNNN`, `.nc`, with the default root names of
-clblm_Config.f90:255-259.
+clblm_Config.f90:255-259.  The layer OD file of writeOD (:1914-2016) is
+`od` + altitude/angle + `_sNNN_LLL.nc` with variable `layerOD`; the
+transmittance files of writeTransmittance (:1469-1666) are
+`tx-total_<mono|convolved>..._sNNN.nc` and, per layer of a profile,
+`tx-prfl_<mono|convolved>..._sNNN_LLL.nc`, with variable `transmittance`.
 """
 from pathlib import Path
 
 import numpy as np
 from scipy.io import netcdf_file
 
+ROOT_OD = "od"          # clblm_Config.f90:255
 ROOT_RAD = "rad"        # clblm_Config.f90:256
+ROOT_TXTOT = "tx-total"  # clblm_Config.f90:257
+ROOT_TXPRFL = "tx-prfl"  # clblm_Config.f90:258
 ROOT_JAC = "drad-d"     # clblm_Config.f90:259
 
 
@@ -52,7 +59,21 @@ def jacobian_name(jac, scene_no=1, obs_alt=None, view_ang=None, root=ROOT_JAC):
     return "%s%s_mono%s_s%03d.nc" % (root, jac, _alt_ang(obs_alt, view_ang), scene_no)
 
 
-def _write(path, var, data, dims, v1, v2, dv, product, scene_no, uid, scene_file):
+def od_name(lay_no, scene_no=1, obs_alt=None, view_ang=None, root=ROOT_OD):
+    """The layer OD file's name (writeOD :1968-1980): no `_mono` tag."""
+    return "%s%s_s%03d_%03d.nc" % (root, _alt_ang(obs_alt, view_ang), scene_no, lay_no)
+
+
+def transmittance_name(scene_no=1, lay_no=None, convolved=False, obs_alt=None, view_ang=None):
+    """The total (lay_no None) or profile-layer transmittance file's name
+    (writeTransmittance :1535, :1554, :1611, :1626)."""
+    kind = "_convolved" if convolved else "_mono"
+    if lay_no is None:
+        return "%s%s%s_s%03d.nc" % (ROOT_TXTOT, kind, _alt_ang(obs_alt, view_ang), scene_no)
+    return "%s%s%s_s%03d_%03d.nc" % (ROOT_TXPRFL, kind, _alt_ang(obs_alt, view_ang), scene_no, lay_no)
+
+
+def _write(path, var, data, dims, v1, v2, dv, product, scene_no, uid, scene_file, spect_type="Monochromatic"):
     data = np.ascontiguousarray(data, dtype=np.float64)
     f = netcdf_file(str(path), "w", version=2)
     try:
@@ -62,7 +83,7 @@ def _write(path, var, data, dims, v1, v2, dv, product, scene_no, uid, scene_file
         f.UID = np.int32(uid)
         f.sceneNumber = np.int32(scene_no)
         f.productName = _pad(product, 32)
-        f.spectralDataType = _pad("Monochromatic", 32)
+        f.spectralDataType = _pad(spect_type, 32)
         f.V1 = np.float64(v1)
         f.V2 = np.float64(v2)
         f.DV = np.float64(dv)
@@ -104,6 +125,29 @@ def write_jacobians(directory, v1, dv, dtlev=None, dqlev=None, dtsfc=None, demis
         path = Path(directory) / jacobian_name(tag, scene_no, obs_alt, view_ang)
         out.append(_write(path, var, arr, dims, v1, v2, dv, "Concentration_Jacobians", scene_no, uid, scene_file))
     return out
+
+
+def write_od(directory, od, v1, dv, lay_no, scene_no=1, uid=0, scene_file="", obs_alt=None, view_ang=None):
+    """A layer's monochromatic optical depth (ODLAY's monoOD) as writeOD
+    writes it: `layerOD` on numPoints, product Layer_OD.  Returns the path."""
+    od = np.asarray(od, dtype=np.float64)
+    v2 = v1 + dv * (len(od) - 1)
+    path = Path(directory) / od_name(lay_no, scene_no, obs_alt, view_ang)
+    return _write(path, "layerOD", od, ("numPoints",), v1, v2, dv, "Layer_OD", scene_no, uid, scene_file)
+
+
+def write_transmittance(directory, tx, v1, dv, scene_no=1, lay_no=None, convolved=False, uid=0, scene_file="",
+                        obs_alt=None, view_ang=None):
+    """A total transmittance (lay_no None: product Total_transmittance) or
+    one layer of a transmittance profile (Transmittance_profile), on its own
+    grid, monochromatic or convolved, as writeTransmittance writes them
+    (TxFlag 1, -1 with a scanning function, 2, -2).  Returns the path."""
+    tx = np.asarray(tx, dtype=np.float64)
+    v2 = v1 + dv * (len(tx) - 1)
+    path = Path(directory) / transmittance_name(scene_no, lay_no, convolved, obs_alt, view_ang)
+    product = "Total_transmittance" if lay_no is None else "Transmittance_profile"
+    return _write(path, "transmittance", tx, ("numPoints",), v1, v2, dv, product, scene_no, uid, scene_file,
+                  "Convolved" if convolved else "Monochromatic")
 
 
 def read(path):

@@ -75,3 +75,48 @@ def test_gpu_results_round_trip(gpu_lib, mtckd, tmp_path):
                               ("dRad_dT", "dRad_dH2O", "dRad_dTskin", "dRad_dEmis")):
         _, v = ncout.read(path)
         np.testing.assert_array_equal(v[var], r[key])
+
+
+def test_od_and_transmittance_names():
+    # writeOD: root, altitude/angle, _sNNN_LLL (no _mono)
+    assert ncout.od_name(7, 2) == "od_s002_007.nc"
+    assert ncout.od_name(12, 1, obs_alt=705.0, view_ang=0.0) == "od_a705km-o000deg_s001_012.nc"
+    assert ncout.transmittance_name(3) == "tx-total_mono_s003.nc"
+    assert ncout.transmittance_name(3, convolved=True) == "tx-total_convolved_s003.nc"
+    assert ncout.transmittance_name(3, lay_no=14) == "tx-prfl_mono_s003_014.nc"
+    assert ncout.transmittance_name(1, lay_no=2, convolved=True, view_ang=40.0) == "tx-prfl_convolvedo040deg_s001_002.nc"
+
+
+def test_od_and_transmittance_files(tmp_path):
+    od = np.geomspace(1e-4, 3.0, 777)
+    p = ncout.write_od(tmp_path, od, 600.0, 0.005, lay_no=5, scene_no=2, uid=9)
+    assert p.name == "od_s002_005.nc" and p.read_bytes()[:4] == b"CDF\x02"
+    attrs, v = ncout.read(p)
+    assert attrs["productName"].rstrip() == "Layer_OD" and attrs["spectralDataType"].rstrip() == "Monochromatic"
+    assert attrs["NSAMP"] == 777 and attrs["V2"] == 600.0 + 0.005 * 776
+    np.testing.assert_array_equal(v["layerOD"], od)
+    tx = np.exp(-od)
+    p = ncout.write_transmittance(tmp_path, tx, 600.0, 0.005, scene_no=2)
+    attrs, v = ncout.read(p)
+    assert p.name == "tx-total_mono_s002.nc" and attrs["productName"].rstrip() == "Total_transmittance"
+    np.testing.assert_array_equal(v["transmittance"], tx)
+    p = ncout.write_transmittance(tmp_path, tx, 600.0, 0.005, scene_no=2, lay_no=4, convolved=True)
+    attrs, _ = ncout.read(p)
+    assert attrs["productName"].rstrip() == "Transmittance_profile"
+    assert attrs["spectralDataType"].rstrip() == "Convolved"
+
+
+@pytest.mark.gpu
+def test_gpu_od_file_round_trip(gpu_lib, tmp_path):
+    """A layer OD of clblm_gpu_od written as writeOD's file and read back."""
+    from clblm_gb300 import capi_types as T
+    from clblm_gb300 import synth
+    lines, col = synth.config0()
+    dn, df, _ = gpu_lib.setDV(col)
+    h = gpu_lib.Handle(lines)
+    od, dv = h.odlay(col.layer(0), T.grid_struct(col.v1, col.v2, dn[0], df[0]), T.od_ctrl(contnm_off=1))
+    h.close()
+    p = ncout.write_od(tmp_path, od, col.v1, dv, lay_no=1)
+    attrs, v = ncout.read(p)
+    np.testing.assert_array_equal(v["layerOD"], od)
+    assert attrs["DV"] == dv and attrs["NSAMP"] == len(od)
