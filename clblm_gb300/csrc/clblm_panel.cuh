@@ -98,5 +98,10 @@ template <bool Plain, int Part>
 __global__ void k_panel(const __grid_constant__ PanelArgs a);
 template <bool Plain, int CHUNK>
 __global__ void k_f4_conv(F4Args a);
+// RSYM of the first panel of every layer whose panel origin is at or below
+// 0 cm-1, as a correction of the OD the panel kernel wrote (one CTA per layer
+// of the batch; others return at once)
+template <bool Plain>
+__global__ void k_rsym(const __grid_constant__ PanelArgs a);
 
 }  // namespace clblm

@@ -144,7 +144,10 @@ static_assert(3 * (sizeof(PanelSmem<false>) + 1024) <= 228 * 1024, "mixed k_pane
 
 size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
 
-// RADFNI, clblm_ODLAY_CommonSub.f90:379-508 (FP64)
+// RADFNI, clblm_ODLAY_CommonSub.f90:379-508 (FP64).  *VINEW carries the end
+// of the previous interval: when the caller passes it negative (the first
+// call of a panel or block whose start lies within one step of zero), its
+// magnitude is taken as the end of this interval as it is.
 __device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, double* RDEL, double* RDLAST) {
   const double FACT1 = 3.0E-03;
   double XVI = VI;
@@ -162,14 +165,24 @@ __device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, dou
   }
   double RADFNI = *RDLAST;
   int INTVLS = 1;
+  // the next interval's end: VI + step rounded to whole DVI, or |VINEW| as passed
+  auto advance = [&](double step) {
+    if (*VINEW >= 0.0) {
+      *VINEW = VI + step;
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+      *VINEW = VI + DVI * (double)INTVLS;
+    } else {
+      *VINEW = fabs(*VINEW);
+      INTVLS = (int)((*VINEW - VI) / DVI);
+      if (INTVLS < 1) INTVLS = 1;
+    }
+  };
   double RDNEXT;
   if (XKT > 0.0) {
     double XVIOKT = XVI / XKT;
     if (XVIOKT <= 0.01) {
-      *VINEW = VI + FACT1 * 0.5 * XVI;
-      INTVLS = (int)((*VINEW - VI) / DVI);
-      if (INTVLS < 1) INTVLS = 1;
-      *VINEW = VI + DVI * (double)INTVLS;
+      advance(FACT1 * 0.5 * XVI);
       double XVINEW = *VINEW;
       double XVINEWOKT = XVINEW / XKT;
       RDNEXT = 0.5 * XVINEWOKT * XVINEW;
@@ -177,26 +190,17 @@ __device__ double radfni_d(double VI, double DVI, double XKT, double* VINEW, dou
       double E = exp(-XVIOKT);
       double XMINUS = 1. - E, XPLUS = 1. + E;
       double CVIKT = XVIOKT * E;
-      *VINEW = VI + FACT1 * XVI / (1. + (CVIKT / XMINUS + CVIKT / XPLUS));
-      INTVLS = (int)((*VINEW - VI) / DVI);
-      if (INTVLS < 1) INTVLS = 1;
-      *VINEW = VI + DVI * (double)INTVLS;
+      advance(FACT1 * XVI / (1. + (CVIKT / XMINUS + CVIKT / XPLUS)));
       double XVINEW = *VINEW;
       double XVINEWOKT = XVINEW / XKT;
       double EN = exp(-XVINEWOKT);
       RDNEXT = XVINEW * (1. - EN) / (1. + EN);
     } else {
-      *VINEW = VI + (FACT1 * XVI);
-      INTVLS = (int)((*VINEW - VI) / DVI);
-      if (INTVLS < 1) INTVLS = 1;
-      *VINEW = VI + DVI * (double)INTVLS;
+      advance(FACT1 * XVI);
       RDNEXT = *VINEW;
     }
   } else {
-    *VINEW = VI + (FACT1 * XVI);
-    INTVLS = (int)((*VINEW - VI) / DVI);
-    if (INTVLS < 1) INTVLS = 1;
-    *VINEW = VI + DVI * (double)INTVLS;
+    advance(FACT1 * XVI);
     RDNEXT = *VINEW;
   }
   *RDEL = (RDNEXT - RADFNI) / (double)INTVLS;
@@ -853,6 +857,236 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
 template __global__ void k_panel<false, kPanelLines>(const __grid_constant__ PanelArgs);
 template __global__ void k_panel<false, kPanelWings>(const __grid_constant__ PanelArgs);
 template __global__ void k_panel<true, kPanelAll>(const __grid_constant__ PanelArgs);
+
+// ---------------------------------------------------------------------------
+// RSYM (clblm_ODLAY.f90:3020-3085): when a layer's first panel starts at or
+// below 0 cm-1 (VFT = V1 - 32 DV <= 0, a window starting within 32 DV of
+// zero), HIRACQ folds the line sums of that panel about zero on each of R1,
+// R2 and R3 before XINT and panelOut (:1440-1450): the negative-frequency part
+// of a line near zero is added, by four-point interpolation, to the mirrored
+// positive frequencies.  The fold is linear and touches only the points
+// within 2 IP of the panel's start (IP <= 33 on R1, <= 9 on R2, <= 3 on R3),
+// so it is applied here as a correction after the panel kernel: one CTA per
+// layer forms, in binary64 and in the reference's line order, the line sums
+// of the panel-0 lines at those points, folds them as RSYM does, and carries
+// the difference through panelOut's R3->R2->R1 combine and radiation term
+// into the OD points it reaches.
+constexpr int kRsymLo = -2;                          // first p-frame point held
+constexpr int kRsymN1 = 70 - kRsymLo + 1, kRsymN2 = 22 - kRsymLo + 1, kRsymN3 = 10 - kRsymLo + 1;  // R1, R2, R3
+__device__ __forceinline__ int rsym_n(int k) { return k == 0 ? kRsymN1 : (k == 1 ? kRsymN2 : kRsymN3); }
+constexpr int kRsymOut = 176;                        // R1 points carried: 1 .. kRsymOut
+
+// RSYM on R (p-frame, R[J] = r[J - kRsymLo]) with spacing DVk, as the
+// reference steps it (in place, reading the values of earlier steps)
+__device__ void rsym_fold(double* r, int nr, double DVk, double VFT) {
+  auto R = [&](int J) -> double& { return r[min(max(J - kRsymLo, 0), nr - 1)]; };
+  int IP = (int)((-VFT / DVk) + 1. - .000001);
+  IP = IP + 1;
+  double P = ((double)(IP - 1) + VFT / DVk) * 2.;
+  const double PST = P;
+  if (P > 1.) P = P - 1.;
+  const double WN1 = -P * (P - 1.) * (P - 2.) / 6.;
+  const double W0 = (P * P - 1.) * (P - 2.) / 2.;
+  const double W1 = -P * (P + 1.) * (P - 2.) / 2.;
+  const double W2 = P * (P * P - 1.) / 6.;
+  int K = IP;
+  const int IPMAX = IP + IP - 1;
+  double B1, B2, C1, C2;
+  if (PST > 1.) {
+    B1 = R(IP - 2);
+    B2 = R(IP - 1);
+    C1 = R(K);
+    for (int I = IP; I <= IPMAX; ++I) {
+      K = K - 1;
+      C2 = C1;
+      if (K < 1) return;
+      C1 = R(K);
+      R(K) = R(K) + WN1 * R(I + 1) + W0 * R(I) + W1 * B2 + W2 * B1;
+      B1 = B2;
+      B2 = R(I);
+      if (K <= 2) continue;
+      R(I) = R(I) + WN1 * C2 + W0 * C1 + W1 * R(K - 1) + W2 * R(K - 2);
+    }
+    return;
+  }
+  C1 = R(IP);
+  C2 = R(IP + 1);
+  B2 = R(IP - 1);
+  for (int I = IP; I <= IPMAX; ++I) {
+    K = K - 1;
+    B1 = B2;
+    B2 = R(I);
+    if (K <= 1) return;
+    R(I) = R(I) + WN1 * C2 + W0 * C1 + W1 * R(K) + W2 * R(K - 1);
+    C2 = C1;
+    C1 = R(K);
+    R(K) = R(K) + WN1 * R(I + 2) + W0 * R(I + 1) + W1 * B2 + W2 * B1;
+  }
+}
+
+template <bool Plain>
+__global__ void __launch_bounds__(256) k_rsym(const __grid_constant__ PanelArgs a) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  const int layer = blockIdx.x;
+  const LayerPlan& P = a.plans[layer + a.layer0];
+  const double* vft = a.vft_all + P.vft_off;
+  const double VFT = vft[0];
+  if (!(VFT <= 0.)) return;  // the first panel starts above zero: nothing to fold
+  const int tid = threadIdx.x;
+  const double dv = P.dv, DVR2 = P.dvr2, DVR3 = P.dvr3;
+  // the panel-0 line sums at the points RSYM reads, then their folds
+  __shared__ double sR[3][kRsymN1];
+  __shared__ double sF[3][kRsymN1];
+  // the chunk's panel-0 lines that reach those points, in line order
+  struct RSet {
+    double zf[3], zs, str[5];
+    int jmin1, jmax1, j2, j3;
+  };
+  __shared__ RSet set[256];
+  __shared__ int warp_cnt[8], chunk_cnt, more;
+  for (int k = tid; k < 3 * kRsymN1; k += blockDim.x) (&sR[0][0])[k] = 0.;
+  // global index ranges of the held points (panel 0: g = J - 1 on every grid)
+  const int glo = kRsymLo - 1;
+  const int ghi[3] = {kRsymLo + kRsymN1 - 2, kRsymLo + kRsymN2 - 2, kRsymLo + kRsymN3 - 2};  // g = J - 1
+  const int64_t nrec = P.line_hi - P.line_lo + 1;
+  const GridRec* rec = a.rec + (int64_t)layer * a.stride * 3;
+  const LinePrep* prep = a.prep + (int64_t)layer * a.stride;
+  // records are in line order and their panel never decreases: panel 0 is a
+  // prefix of them
+  for (int64_t base = 0;; base += blockDim.x) {
+    if (tid == 0) more = 0;
+    __syncthreads();
+    const int64_t t = base + tid;
+    bool hit = false;
+    if (t < nrec) {
+      const GridRec& r1 = rec[t];
+      if (r1.q <= 0) more = 1;
+      if (r1.q == 0 && prep[t].fpanel >= 0) {
+        for (int k = 0; k < 3; ++k) {
+          const GridRec& r = rec[(int64_t)k * a.stride + t];
+          hit |= r.g_lo <= r.g_hi && r.g_lo <= ghi[k] && r.g_hi >= glo;
+        }
+      }
+    }
+    // ordered compaction of the chunk's lines
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    const int lane = tid & 31, warp = tid >> 5;
+    if (lane == 0) warp_cnt[warp] = __popc(bal);
+    __syncthreads();
+    if (tid == 0) {
+      int run = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        const int c = warp_cnt[w];
+        warp_cnt[w] = run;
+        run += c;
+      }
+      chunk_cnt = run;
+    }
+    __syncthreads();
+    if (hit) {
+      const int slot = warp_cnt[warp] + __popc(bal & ((1u << lane) - 1u));
+      const LinePrep L = prep[t];
+      const CnvfnqSetup cs = cnvfnq_setup(P, VFT, L.vnu, L.recalf, L.bhwdxf);
+      RSet& e = set[slot];
+      for (int k = 0; k < 3; ++k) e.zf[k] = cs.zf[k];
+      e.zs = cs.zslope;
+      e.jmin1 = cs.jmin1;
+      e.jmax1 = cs.jmax1;
+      e.j2 = cs.j2shft;
+      e.j3 = cs.j3shft;
+      // CNVFNQ's strengths (:2117-2125): DEPTHA times the zeta-interpolated
+      // CF1, CF2, CF3, CGAUSS, CER
+      const double DEPTHA = L.sp * L.recalf, ZD = L.zetdif;
+      const double* tabs[5] = {c_CF1, c_CGAUSS, c_CER, c_CF2, c_CF3};
+      for (int k = 0; k < 5; ++k)
+        e.str[k] = DEPTHA * (tabs[k][L.iz - 1] + ZD * (tabs[k][L.iz] - tabs[k][L.iz - 1]));
+    }
+    __syncthreads();
+    // each held point adds the chunk's lines in their order
+    const int cnt = chunk_cnt;
+    for (int k = tid; k < kRsymN1 + kRsymN2 + kRsymN3; k += blockDim.x) {
+      const int grid = k < kRsymN1 ? 0 : (k < kRsymN1 + kRsymN2 ? 1 : 2);
+      const int i = grid == 0 ? k : (grid == 1 ? k - kRsymN1 : k - kRsymN1 - kRsymN2);
+      const int J = kRsymLo + i;
+      double acc = sR[grid][i];
+      for (int q = 0; q < cnt; ++q) {
+        const RSet& e = set[q];
+        const int J1 = J + (grid == 0 ? 0 : (grid == 1 ? e.j2 : e.j3));
+        if (J1 < e.jmin1 || J1 > e.jmax1) continue;
+        const double zf = fma((double)(J1 - e.jmin1 + 1), e.zs, e.zf[grid]);
+        const int iz = (int)(fabs(zf) + 1.5);
+        if (iz > kNFMX) continue;
+        if (grid == 0) {
+          const double* T = a.tabs.t1d + 3 * (iz - 1);
+          acc = acc + e.str[0] * T[0] + e.str[1] * T[1] + e.str[2] * T[2];
+        } else if (grid == 1) {
+          acc = acc + e.str[3] * a.tabs.t2d[iz - 1];
+        } else {
+          acc = acc + e.str[4] * a.tabs.t3d[iz - 1];
+        }
+      }
+      sR[grid][i] = acc;
+    }
+    __syncthreads();
+    if (!more) break;
+  }
+  if (tid != 0) return;
+  // the folds and their differences
+  for (int k = 0; k < 3; ++k) {
+    for (int i = 0; i < rsym_n(k); ++i) sF[k][i] = sR[k][i];
+    rsym_fold(sF[k], rsym_n(k), k == 0 ? dv : (k == 1 ? DVR2 : DVR3), VFT);
+    for (int i = 0; i < rsym_n(k); ++i) sF[k][i] -= sR[k][i];
+  }
+  auto d1 = [&](int J) { return (J >= kRsymLo && J < kRsymLo + kRsymN1) ? sF[0][J - kRsymLo] : 0.; };
+  auto d2 = [&](int J) { return (J >= kRsymLo && J < kRsymLo + kRsymN2) ? sF[1][J - kRsymLo] : 0.; };
+  auto d3 = [&](int J) { return (J >= kRsymLo && J < kRsymLo + kRsymN3) ? sF[2][J - kRsymLo] : 0.; };
+  // panelOut of the first panel (N1R2 = 1: LIMLO = 5), linear in the sums
+  const double X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
+  const double X10 = -1. / 16., X11 = 9. / 16.;
+  auto comb = [&](auto f, int Jc, int off) -> double {
+    if (off == 0) return f(Jc);
+    if (off == 1) return X00 * f(Jc - 1) + X01 * f(Jc) + X02 * f(Jc + 1) + X03 * f(Jc + 2);
+    if (off == 2) return X10 * (f(Jc - 1) + f(Jc + 2)) + X11 * (f(Jc) + f(Jc + 1));
+    return X03 * f(Jc - 1) + X02 * f(Jc) + X01 * f(Jc + 1) + X00 * f(Jc + 2);
+  };
+  const bool last = P.npanels == 1;
+  const int NHI = last ? P.nhi_last : (kNLIM1 + kNSHIFT - 1);
+  const int LIMLO = 5, LIMHI = NHI / 4 + 1;
+  const int lastJg = LIMLO + ((LIMHI - LIMLO) / 4) * 4;
+  constexpr int kD2 = kRsymOut / 4 + 4;
+  double dr2[kD2 + 1];  // R2 differences 0 .. kD2 after the R3 combine
+  for (int J = 0; J <= kD2; ++J) {
+    double v = d2(J);
+    const int off = (J - 1) & 3, Jg = J - off;
+    const bool inloop = LIMLO <= LIMHI && Jg >= LIMLO && Jg <= LIMHI;
+    const bool extra = last && LIMLO <= LIMHI && Jg == lastJg + 4 && off <= 1;
+    if (J >= 5 && (inloop || extra)) v += comb(d3, (Jg - 1) / 4 + 1, off);
+    dr2[J] = v;
+  }
+  auto f2 = [&](int J) { return (J >= 0 && J <= kD2) ? dr2[J] : 0.; };
+  // radiation term of the first panel (JRAD = 0), as the panel kernel forms it
+  const double XKT = P.tave / kRADCN2;
+  double VITST = VFT + (double)kNSHIFT * dv - dv, RDLAST = -1.;
+  int N2 = kNSHIFT, N1 = N2 + 1;
+  double RADVI = 1., RDEL = 0.;
+  Real* od = reinterpret_cast<Real*>(a.od_all) + P.od_off;
+  for (int J = kNSHIFT + 1; J <= min(NHI, kRsymOut); ++J) {
+    while (P.jrad == 0 && J > N2) {  // (a segment may be empty: RADFNI's first interval near zero)
+      N1 = N2 + 1;
+      const double VI = VFT + (double)(N1 - 1) * dv;
+      RADVI = radfni_d(VI, dv, XKT, &VITST, &RDEL, &RDLAST);
+      N2 = (int)((VITST - VFT) / dv + 0.001);
+      if (N2 > NHI) N2 = NHI;
+    }
+    const int off = (J - kNSHIFT - 1) & 3, Jg = J - off;
+    double v = d1(J) + comb(f2, (Jg - 1) / 4 + 1, off);
+    if (P.jrad == 0) v = v * (RADVI + (double)(J - N1) * RDEL);
+    od[J - kNSHIFT - 1] += (Real)v;
+  }
+}
+
+template __global__ void k_rsym<false>(const __grid_constant__ PanelArgs);
+template __global__ void k_rsym<true>(const __grid_constant__ PanelArgs);
 
 // ---------------------------------------------------------------------------
 // Far wings: R4 on the grid V1R4 + m*DVR4, m = 0 .. nptr4-1 (CNVF4Q).

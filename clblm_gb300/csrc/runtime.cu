@@ -563,8 +563,6 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.vft0 = V1 - (double)kNSHIFT * DV;
   P.vbot = V1 - P.bound;
   P.vtop = V2 + P.bound;
-  if (!(P.vft0 > 0.))
-    return set_err(h, CLBLM_ERR_UNSUPPORTED, "panels below 0 cm-1 (RSYM folding) are not on this path");
   P.pave = lay->pave;
   P.tave = lay->tave;
   P.wtot = lay->wtot;
@@ -1110,6 +1108,14 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
     k_panel<false, kPanelWings><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
     CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
+  }
+  // RSYM: the first panel of a layer whose panel origin is at or below 0 cm-1
+  bool fold = false;
+  for (int k = 0; k < count; ++k) fold |= !(hps[first + k].P.vft0 > 0.);
+  if (fold) {
+    h->launches++;
+    if (plain) k_rsym<true><<<count, 256, 0, st>>>(pa);
+    else k_rsym<false><<<count, 256, 0, st>>>(pa);
   }
   CUDA_TRY(h, cudaGetLastError());
   return CLBLM_OK;

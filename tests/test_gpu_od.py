@@ -182,3 +182,19 @@ def test_line_selection_bit_exact(gpu_lib, oracle_mod, case, precision):
             np.testing.assert_allclose(sel[k], tr[k], rtol=2e-6, atol=0, err_msg=k)
     tol = 1e-9 if precision == T.CLBLM_PREC_PLAIN else 1e-5
     assert np.max(np.abs(od - ref) / np.abs(ref)) <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+@pytest.mark.parametrize("v2", [12.0, 60.0])
+def test_window_starting_at_zero_rsym(gpu_lib, oracle_mod, precision, tol, v2):
+    """A window starting at 0.0005 cm-1: the first panel's origin
+    VFT = V1 - 32 DV lies below zero, where HIRACQ folds the panel's line
+    sums about zero (RSYM, clblm_ODLAY.f90:3020-3085); one panel (v2 = 12)
+    and three (v2 = 60), lines from 0.02 cm-1, the MT_CKD-style continuum."""
+    lines = synth.line_list(6000, 0.02, 90.0, seed=9, mols=(1,))
+    cont = synth.continuum()
+    col = T.Column(np.array([1], np.int32), [1013.25], [296.0], [296.0], [296.0], np.array([[1e22]]), [2.479e24],
+                   [1.67 * 2.479e24], 0.0005, v2, 296.0, 1.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
