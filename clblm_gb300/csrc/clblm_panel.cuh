@@ -87,7 +87,7 @@ struct F4Args {
   int* err;                 // bit 2: a shared-memory stage never arrived
 };
 
-size_t panel_smem_bytes(bool plain);
+size_t panel_smem_bytes(bool plain, bool wings = false);  // wings: the mixed far-wing pass
 __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* blk_v1, const int* blk_n,
                             double* blk_fac);
 

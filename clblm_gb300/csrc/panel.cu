@@ -111,12 +111,12 @@ struct PanelTiles {
   XintPanel X;
 };
 
-// mixed path: under 74 KB, so that three CTAs share an SM
+// mixed path: under 74 KB, so that three CTAs of the line pass share an SM.
+// The shape tables come last: the far-wing pass, which reads no line, is
+// launched with the bytes before them alone.
 template <>
 struct PanelSmem<false> : PanelTiles {
   float absf[kAbsStage];
-  MixedTables tab;       // shape tables (one bulk copy)
-  uint64_t tab_bar;      // completes the table copy
   float4 cw[4];          // Lagrange weights of the R3->R2 and R2->R1 combine by point offset
   float r3n[kR3Pts];     // R3 p-frame 0..160, lines of panels <= p
   float r3o[8];          // R3 p-frame 0..7, lines of panels <= p-1
@@ -124,7 +124,12 @@ struct PanelSmem<false> : PanelTiles {
   int seg_start[kMaxSeg + 1];
   float segf_v[kMaxSeg], segf_d[kMaxSeg];
   int nseg, seg_slot;  // seg_slot >= 0: the segments are in that pool slot
+  uint64_t tab_bar;      // completes the table copy
+  MixedTables tab;       // shape tables (one bulk copy)
 };
+// bytes of PanelSmem<false> before the shape tables
+constexpr size_t kWingsSmem = sizeof(PanelSmem<false>) - sizeof(MixedTables);
+static_assert(kWingsSmem % 16 == 0, "the tables start on a 16-byte boundary");
 template <>
 struct PanelSmem<true> : PanelTiles {
   GridRecD wrecd[kPanelWarps][kBatch];
@@ -142,7 +147,9 @@ struct PanelSmem<true> : PanelTiles {
 // three CTAs of the mixed path per SM (228 KB, 1 KB reserved per CTA)
 static_assert(3 * (sizeof(PanelSmem<false>) + 1024) <= 228 * 1024, "mixed k_panel: three CTAs per SM");
 
-size_t panel_smem_bytes(bool plain) { return plain ? sizeof(PanelSmem<true>) : sizeof(PanelSmem<false>); }
+size_t panel_smem_bytes(bool plain, bool wings) {
+  return plain ? sizeof(PanelSmem<true>) : (wings ? kWingsSmem : sizeof(PanelSmem<false>));
+}
 
 // RADFNI, clblm_ODLAY_CommonSub.f90:379-508 (FP64).  *VINEW carries the end
 // of the previous interval: when the caller passes it negative (the first
@@ -464,7 +471,8 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
 }
 
 template <bool Plain, int Part>
-__global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __grid_constant__ PanelArgs a) {
+__global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWings ? 6 : 3))
+    k_panel(const __grid_constant__ PanelArgs a) {
   // Part: kPanelAll, or the line sums alone (kPanelLines: the far wings and
   // the continuum are not yet known), or the rest alone (kPanelWings: R4 and
   // ABSRB through XINT, the R3->R2->R1 combine and the radiation term, added
@@ -530,6 +538,18 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
 
   // ---- record range of every 32-point tile of the three grids ----
   const int nT1 = (NHI - kNSHIFT + 31) / 32;
+  // the far-wing pass adds to the OD the line pass wrote: its loads are
+  // issued here, ahead of the R3 and R2 phases
+  constexpr int kT1PerWarp = (kTiles1 + kPanelWarps - 1) / kPanelWarps;
+  float od_pre[Part == kPanelWings ? kT1PerWarp : 1];
+  if constexpr (Part == kPanelWings) {
+    const float* od = reinterpret_cast<const float*>(a.od_all) + P.od_off + (int64_t)kPanelPts * p;
+#pragma unroll
+    for (int i = 0; i < kT1PerWarp; ++i) {
+      const int J = kNSHIFT + 1 + (warp + i * kPanelWarps) * 32 + lane;
+      od_pre[i] = (warp + i * kPanelWarps < nT1 && J <= NHI) ? od[J - kNSHIFT - 1] : 0.f;
+    }
+  }
   const int G01 = kPanelPts * p + kNSHIFT, G02 = kPanelR2 * p - 1, G03 = kPanelR3 * p - 1;
   for (int t = tid; t < 2 * kTiles1; t += blockDim.x) S.lo1[t] = S.hi1[t] = (int)rg[1];
   for (int t = tid; t < 2 * kTiles2; t += blockDim.x) S.lo2[t] = S.hi2[t] = (int)rg[3];
@@ -794,7 +814,8 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
     const Real X00 = -7. / 128., X01 = 105. / 128., X02 = 35. / 128., X03 = -5. / 128.;
     const Real X10 = -1. / 16., X11 = 9. / 16.;
     Real* od = reinterpret_cast<Real*>(a.od_all) + P.od_off;
-    for (int tile = warp; tile < nT1; tile += kPanelWarps) {
+    // one 32-point tile; `prev`: the OD the line pass wrote (far-wing pass)
+    auto r1_tile = [&](int tile, float prev) {
       int J = kNSHIFT + 1 + tile * 32 + lane;  // p-frame R1 index, 33..
       bool active = J <= NHI;
       int g = kPanelPts * p + J - 1;
@@ -847,9 +868,16 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : 3) k_panel(const __
           }
         }
         Real* o = od + (int64_t)kPanelPts * p + (J - kNSHIFT - 1);
-        if constexpr (Part == kPanelWings) *o += val;
+        if constexpr (Part == kPanelWings) *o = prev + val;
         else *o = val;
       }
+    };
+    if constexpr (Part == kPanelWings) {
+#pragma unroll
+      for (int i = 0; i < kT1PerWarp; ++i)
+        if (warp + i * kPanelWarps < nT1) r1_tile(warp + i * kPanelWarps, od_pre[i]);
+    } else {
+      for (int tile = warp; tile < nT1; tile += kPanelWarps) r1_tile(tile, 0.f);
     }
   }
 }

@@ -1095,7 +1095,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
       CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelLines>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
       CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelWings>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+                                       (int)panel_smem_bytes(false, true)));
       h->panel_attr_set[0] = true;
     }
     h->launches += 2;
@@ -1106,7 +1106,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     // the radiation-term pool is claimed again by the second pass
     CUDA_TRY(h, cudaMemsetAsync(pa.seg_next, 0, sizeof(int), st));
     CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
-    k_panel<false, kPanelWings><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    // without the shape tables: six CTAs of the far-wing pass share an SM
+    k_panel<false, kPanelWings><<<dim3(maxp, count), kPanelThreads, panel_smem_bytes(false, true), st>>>(pa);
     CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
   }
   // RSYM: the first panel of a layer whose panel origin is at or below 0 cm-1
