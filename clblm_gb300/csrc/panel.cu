@@ -1,21 +1,22 @@
 // panel.cu -- hot kernels of the layer optical depth and nadir radiance.
 //
-//   k_panel<Plain>   one CTA per (layer, panel of 2400 points): the three
+//   k_panel<Plain, Part>  one CTA per (layer, panel of 2400 points): the three
 //                    nested Voigt sub-function grids R3 (16 DV), R2 (4 DV) and
 //                    R1 (DV) gathered from the per-line records (CNVFNQ,
 //                    clblm_ODLAY.f90:2067-2258), far-wing and continuum
 //                    interpolation into R3 (XINT, clblm_Spectrum.f90:874-915),
 //                    the R3->R2->R1 4-point interpolation and the radiation
-//                    term (panelOut, clblm_ODLAY.f90:2289-2493).
+//                    term (panelOut, clblm_ODLAY.f90:2289-2493).  The FP64
+//                    path runs it in one launch (kPanelAll); the mixed path
+//                    in two: the line sums (kPanelLines) beside the far-wing
+//                    chain, then R4 and the continuum (kPanelWings).
 //   k_f4_conv<Plain> far-wing function 4 on the DVR4 grid (CNVF4Q,
 //                    clblm_ODLAY_LineF4.f90:187-494): two points per thread
 //                    (packed FP32x2 in the mixed path), records streamed
 //                    through shared memory by bulk copies.
-//   k_rt_layer<...>  one layer of the upward merge of mode2_lookDn_mergeUp
-//                    (layerMerge_mode2, clblm_noScattRT.f90:1704-1794) with
-//                    layerEmis (clblm_EMLAY.f90:104-178) and the
-//                    interpolation to the finest grid (interpSpectrum,
-//                    clblm_Spectrum.f90:326-620) folded into the load.
+//   k_rsym<Plain>    RSYM's fold about 0 cm-1 of the first panel of a window
+//                    starting within 32 DV of zero (clblm_ODLAY.f90:3020-3085),
+//                    applied as a binary64 correction after k_panel.
 //
 // Mixed path: table look-ups, products and sums in FP32 with Kahan-
 // compensated accumulation; every table index is the reference's FP64 index
