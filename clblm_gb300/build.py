@@ -24,6 +24,7 @@ UNITS = {
     "rt.cu": [],
     "jac.cu": [],
     "scan.cu": [],
+    "scanfn.cu": [],
     "tape3.cpp": [],
     "runtime.cu": [],
 }

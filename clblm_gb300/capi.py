@@ -23,8 +23,8 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_setdv", "clblm_gpu_od_size", "clblm_gpu_od", "clblm_gpu_od_stats",
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
-           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_layer_amounts", "clblm_gpu_od_lines",
-           "clblm_gpu_jac_vjp")
+           "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_scanfn_size", "clblm_gpu_scanfn",
+           "clblm_gpu_layer_amounts", "clblm_gpu_od_lines", "clblm_gpu_jac_vjp")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -80,6 +80,10 @@ def lib():
         L.clblm_gpu_fftscn_size.argtypes = [P(T.clblm_scan_t), C.c_double, C.c_double, C.c_int64, P(C.c_double),
                                             P(C.c_double), P(C.c_int64)]
         L.clblm_gpu_fftscn.argtypes = [C.c_void_p, P(T.clblm_scan_t), C.c_void_p, C.c_double, C.c_double, C.c_int64,
+                                       C.c_void_p, C.c_int64, C.c_int32]
+        L.clblm_gpu_scanfn_size.argtypes = [P(T.clblm_scanfn_t), C.c_double, C.c_double, C.c_int64, P(C.c_double),
+                                            P(C.c_double), P(C.c_int64)]
+        L.clblm_gpu_scanfn.argtypes = [C.c_void_p, P(T.clblm_scanfn_t), C.c_void_p, C.c_double, C.c_double, C.c_int64,
                                        C.c_void_p, C.c_int64, C.c_int32]
         L.clblm_gpu_layer_amounts.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [P(C.c_double)] * 4 + \
             [C.c_double] + [P(C.c_double)] * 5
@@ -350,6 +354,36 @@ def _scan_methods():
 
 
 Handle.fftscn, Handle.fftscn_device = _scan_methods()
+
+
+def scanfn_size(scan, v1, dv, n):
+    """(V1out, DVout, NPout) of the wavenumber-space scan (host arithmetic)."""
+    v1o, dvo, no = C.c_double(), C.c_double(), C.c_int64()
+    rc = lib().clblm_gpu_scanfn_size(C.byref(scan), v1, dv, n, C.byref(v1o), C.byref(dvo), C.byref(no))
+    if rc:
+        raise ClblmError(rc, "SCANFN size")
+    return v1o.value, dvo.value, no.value
+
+
+def _scanfn_methods():
+    def scanfn(self, scan, spect, v1, dv):
+        """clblm_SCANFN of a binary64 spectrum on v1 + i*dv: (scanned, V1out, DVout)."""
+        spect = np.ascontiguousarray(spect, dtype=np.float64)
+        v1o, dvo, no = scanfn_size(scan, v1, dv, len(spect))
+        out = np.empty(max(no, 1))
+        self._check(lib().clblm_gpu_scanfn(self.h, C.byref(scan), spect.ctypes.data_as(C.c_void_p), v1, dv,
+                                           len(spect), out.ctypes.data_as(C.c_void_p), no, T.CLBLM_OUT_HOST))
+        return out[:no], v1o, dvo
+
+    def scanfn_device(self, scan, dspect, n, v1, dv, dout, cap):
+        """The same on device buffers (addresses)."""
+        self._check(lib().clblm_gpu_scanfn(self.h, C.byref(scan), C.c_void_p(dspect), v1, dv, n, C.c_void_p(dout),
+                                           cap, T.CLBLM_OUT_DEVICE))
+
+    return scanfn, scanfn_device
+
+
+Handle.scanfn, Handle.scanfn_device = _scanfn_methods()
 
 
 def _layer_amounts(self, z, p, t, den, earth_radius=6371.23):

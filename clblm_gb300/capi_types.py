@@ -89,6 +89,15 @@ def scan_struct(funct_id, hwhm, v1out, v2out, padding=0.0, prebox_hw=-1.0, decon
     return clblm_scan_t(funct_id, deconv_prebox, hwhm, padding, prebox_hw, v1out, v2out)
 
 
+class clblm_scanfn_t(C.Structure):
+    _fields_ = [("funct_id", C.c_int32), ("reserved", C.c_int32), ("hwhm", C.c_double), ("v1out", C.c_double),
+                ("v2out", C.c_double), ("dvout", C.c_double)]
+
+
+def scanfn_struct(funct_id, hwhm, v1out, v2out, dvout=0.0):
+    return clblm_scanfn_t(funct_id, 0, hwhm, v1out, v2out, dvout)
+
+
 class JacProfile:
     """Level pressures [mb] and Jacobian-molecule number densities [molec/cm3]
     (level 0 at the surface) and the clblm_jac_t view of them."""

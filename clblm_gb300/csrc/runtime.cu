@@ -31,6 +31,7 @@
 #include "clblm_jac.cuh"
 #include "clblm_rt.cuh"
 #include "clblm_scan.cuh"
+#include "clblm_scanfn.cuh"
 
 using namespace clblm;
 
@@ -145,6 +146,7 @@ struct clblm_handle {
   cufftHandle scan_fwd = 0, scan_inv = 0;
   bool scan_plans = false;
   DevBuf scan_buf, scan_x0, scan_io;
+  DevBuf sf_ws, sf_io;  // SCANFN: workspace, host input/output staging
   std::string errmsg;
   clblm_od_stats_t last{};
   int64_t launches = 0;  // kernels launched by the current call
@@ -1544,6 +1546,8 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   h->scan_buf.release();
   h->scan_x0.release();
   h->scan_io.release();
+  h->sf_ws.release();
+  h->sf_io.release();
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->stream2) {
@@ -3651,6 +3655,58 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
   CUDA_TRY(h, cudaGetLastError());
   if (!dev) CUDA_TRY(h, cudaMemcpyAsync(out, dst, sizeof(double) * p.ntotal, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
+  h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
+}  // extern "C"
+
+// ---- wavenumber-space instrument scan (clblm_SCANFN) -------------------------
+extern "C" {
+
+int clblm_gpu_scanfn_size(const clblm_scanfn_t* sc, double v1, double dv, int64_t n, double* v1o, double* dvo,
+                          int64_t* no) {
+  if (!sc) return CLBLM_ERR_ARG;
+  SfPlan p;
+  std::string msg;
+  const int rc = sf_plan(sc->funct_id, sc->hwhm, sc->v1out, sc->v2out, sc->dvout, v1, dv, n, &p, &msg);
+  if (rc) return rc;
+  if (v1o) *v1o = p.v1_out;
+  if (dvo) *dvo = p.dv_out;
+  if (no) *no = p.n_out;
+  return CLBLM_OK;
+}
+
+int clblm_gpu_scanfn(clblm_handle_t* h, const clblm_scanfn_t* sc, const double* spect, double v1, double dv,
+                     int64_t n, double* out, int64_t cap, int32_t flags) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!sc || !spect || !out) return set_err(h, CLBLM_ERR_ARG, "SCANFN: null argument");
+  if (flags != CLBLM_OUT_HOST && flags != CLBLM_OUT_DEVICE) return set_err(h, CLBLM_ERR_ARG, "SCANFN: bad flags");
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  SfPlan p;
+  std::string msg;
+  const int rc = sf_plan(sc->funct_id, sc->hwhm, sc->v1out, sc->v2out, sc->dvout, v1, dv, n, &p, &msg);
+  if (rc) return set_err(h, rc, "%s", msg.c_str());
+  if (cap < p.n_out) return set_err(h, CLBLM_ERR_CAPACITY, "SCANFN: output needs %lld points", (long long)p.n_out);
+  h->reset_call();
+  const bool dev = flags == CLBLM_OUT_DEVICE;
+  cudaStream_t st = h->stream;
+  const double* din = spect;
+  double* dout = out;
+  if (!dev) {
+    CUDA_TRY(h, h->sf_io.ensure(sizeof(double) * (size_t)(n + std::max<int64_t>(p.n_out, 1)) + 256));
+    double* io = h->sf_io.as<double>();
+    CUDA_TRY(h, cudaMemcpyAsync(io, spect, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+    din = io;
+    dout = io + n;
+  }
+  CUDA_TRY(h, h->sf_ws.ensure(std::max<size_t>(p.ws_bytes, 256)));
+  int launches = 0;
+  CUDA_TRY(h, sf_launch(p, din, dout, h->sf_ws.as<unsigned char>(), st, &launches));
+  h->launches += launches;
+  if (!dev && p.n_out > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(out, dout, sizeof(double) * (size_t)p.n_out, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));  // the plan's tables are read by the copies above
   h->last.launches = h->launches;
   return CLBLM_OK;
 }

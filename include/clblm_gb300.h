@@ -448,6 +448,46 @@ int clblm_gpu_fftscn(clblm_handle_t *h, const clblm_scan_t *scan,
                      const double *spect, double v1, double dv, int64_t n,
                      double *out, int64_t cap, int32_t flags);
 
+/* ---- wavenumber-space instrument scan -------------------------------------
+ *
+ * clblm_SCANFN_array (clblm_ScanFilter.f90:33-67 and the driver :70-544):
+ * the scan postProc_scan applies when the post-processing asks for no FFT
+ * (clblm_PostProc.f90:273-281), and the pre-box smoothing of the radiance
+ * and Jacobians (functID 1 with the box half width, clblm_noScattRT.f90:468,
+ * :522, clblm_noScattJac.f90:1372).  As in the reference: a spectrum coarser
+ * than HWHM/12 is first interpolated to HWHM/12 (clblm_INTERP, four-point
+ * tabulated coefficients); functions 2..5 shrink it to means of up to 120
+ * points per HWHM/12 (SHRKSC) and add each point's tabulated function
+ * (nearest of the table at 0.02 HWHM) into the output (CONVSC); function 1
+ * averages it over boxes of width 2*HWHM with fractional end points
+ * (CNVRCT).  The output starts at V1out, on DVout (functions 2..5: HWHM over
+ * HWHM/DVout; function 1: the nearest whole multiple of the input spacing),
+ * and ends at the first point at or past V2out as panelOutput counts it.
+ * HWHM <= 0 returns the spectrum unchanged; function 1 with fewer than two
+ * input points per output point returns the (interpolated) spectrum.
+ * Errors: functID outside -5..5 or -1..-3 given as a first zero
+ * (CLBLM_ERR_ARG, the reference STOPs); a function wider than the
+ * reference's 5000-point buffer R1 (CLBLM_ERR_UNSUPPORTED). */
+typedef struct {
+  int32_t funct_id;  /* functID: 1 rectangle, 2 triangle, 3 Gaussian, 4 sinc**2,
+                      * 5 sinc; -4, -5: hwhm is the first zero crossing.  0 is
+                      * the triangle, as the reference's SIGN makes it       */
+  int32_t reserved;
+  double  hwhm;      /* functHWHM [cm-1]                                      */
+  double  v1out, v2out; /* V1out, V2out [cm-1]                                */
+  double  dvout;     /* DVout [cm-1]; 0: the function's default sampling      */
+} clblm_scanfn_t;
+
+/* Grid of the scan of a spectrum on v1 + i*dv, i < n: first wavenumber,
+ * spacing and points (NPout).  Host arithmetic only. */
+int clblm_gpu_scanfn_size(const clblm_scanfn_t *scan, double v1, double dv,
+                          int64_t n, double *v1o, double *dvo, int64_t *npout);
+/* The scanned spectrum into out[cap]; spect and out are host buffers, or
+ * device buffers with CLBLM_OUT_DEVICE.  binary64 throughout. */
+int clblm_gpu_scanfn(clblm_handle_t *h, const clblm_scanfn_t *scan,
+                     const double *spect, double v1, double dv, int64_t n,
+                     double *out, int64_t cap, int32_t flags);
+
 /* Lines of an LNFL line file (TAPE3) as read by RDLIN (clblm_ODLAY.f90:
  * 2645-2700) through CLBLM_LineData (clblm_LineData.f90:52-161): Fortran
  * unformatted records (4-byte length markers), the file header, the optional

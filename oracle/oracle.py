@@ -76,6 +76,14 @@ def lib():
         L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
                                                                                     P(C.c_double), P(C.c_int)]
+        L.ocl_scanfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_int, C.c_double,
+                                 C.c_double, C.c_double, C.c_double, P(P(C.c_double)), P(C.c_int64),
+                                 P(C.c_double), P(C.c_double)]
+        L.ocl_sf_interp.restype = C.c_int64
+        L.ocl_sf_interp.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_double, C.c_double,
+                                    C.c_double, P(P(C.c_double))]
+        L.ocl_sf_table.argtypes = [C.c_int, P(C.c_double)]
+        L.ocl_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -283,3 +291,44 @@ def contnm_co2(jrad, v1abs, dvabs, nptabs, xco2c, v1, v2, pave, tave, wkco2):
     if rc:
         raise OracleError(rc, "contnm_co2")
     return a
+
+
+def scanfn(spect, v1, dv, funct_id, hwhm, v1out, v2out, dvout=0.0):
+    """clblm_SCANFN_array (clblm_ScanFilter.f90:33-67): (out, v1, dv) of the
+    wavenumber-space scan of `spect` on v1 + i*dv.  funct_id 1..5
+    (rectangle, triangle, Gaussian, sinc**2, sinc; negative: a sinc or
+    sinc**2 given by its first zero), dvout <= 0: the function's default
+    sampling."""
+    sp = np.ascontiguousarray(spect, dtype=np.float64)
+    out = C.POINTER(C.c_double)()
+    n, v1o, dvo = C.c_int64(), C.c_double(), C.c_double()
+    rc = lib().ocl_scanfn(_dp(sp), v1, dv, len(sp), funct_id, hwhm, v1out, v2out, dvout, C.byref(out), C.byref(n),
+                          C.byref(v1o), C.byref(dvo))
+    if rc:
+        raise OracleError(rc, "SCANFN: %s" % {-1: "invalid functID", -2: "beyond the reference's buffers",
+                                              -3: "no data"}.get(rc, "failed"))
+    try:
+        res = np.ctypeslib.as_array(out, shape=(n.value,)).copy() if n.value > 0 else np.zeros(0)
+    finally:
+        lib().ocl_free(out)
+    return res, v1o.value, dvo.value
+
+
+def sf_interp(spect, v1, dv, v1out, v2out, dvout):
+    """clblm_INTERP (clblm_ScanFilter.f90:1975-2316), four-point scheme."""
+    sp = np.ascontiguousarray(spect, dtype=np.float64)
+    out = C.POINTER(C.c_double)()
+    n = lib().ocl_sf_interp(_dp(sp), v1, dv, len(sp), v1out, v2out, dvout, C.byref(out))
+    if n < 0:
+        raise OracleError(int(n), "INTERP: no data")
+    try:
+        return np.ctypeslib.as_array(out, shape=(n,)).copy()
+    finally:
+        lib().ocl_free(out)
+
+
+def sf_table(jfn):
+    """SCANFN's function table XF(1..NFMAX) of JFN 1..4 (index 0 unused)."""
+    xf = np.zeros(6020)
+    lib().ocl_sf_table(jfn, _dp(xf))
+    return xf
