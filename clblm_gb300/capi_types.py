@@ -82,11 +82,14 @@ CLBLM_BATCH_GRAPH = 0x10
 
 class clblm_scan_t(C.Structure):
     _fields_ = [("funct_id", C.c_int32), ("deconv_prebox", C.c_int32), ("hwhm", C.c_double),
-                ("padding", C.c_double), ("prebox_hw", C.c_double), ("v1out", C.c_double), ("v2out", C.c_double)]
+                ("padding", C.c_double), ("prebox_hw", C.c_double), ("v1out", C.c_double), ("v2out", C.c_double),
+                ("dvout", C.c_double), ("parms", C.c_double * 3)]
 
 
-def scan_struct(funct_id, hwhm, v1out, v2out, padding=0.0, prebox_hw=-1.0, deconv_prebox=0):
-    return clblm_scan_t(funct_id, deconv_prebox, hwhm, padding, prebox_hw, v1out, v2out)
+def scan_struct(funct_id, hwhm, v1out, v2out, padding=0.0, prebox_hw=-1.0, deconv_prebox=0, dvout=0.0,
+                parms=(0.0, 0.0, 0.0)):
+    return clblm_scan_t(funct_id, deconv_prebox, hwhm, padding, prebox_hw, v1out, v2out, dvout,
+                        (C.c_double * 3)(*parms))
 
 
 class clblm_scanfn_t(C.Structure):

@@ -77,6 +77,15 @@ struct SfPlan {
 int sf_plan(int funct_id, double hwhm, double v1out, double v2out, double dvout, double v1, double dv, int64_t n,
             SfPlan* p, std::string* msg);
 
+// Intpdr (clblm_FFT.f90:2392-2443): [vv1, vv2] pulled inside the data on
+// v1 + i*dv (i < n) by whole steps of dvv, then the plan of clblm_INTERP
+// onto *v1_new + j*dvv (p->n_sp points, workspace p->ws_bytes).
+int sf_plan_intpdr(double vv1, double vv2, double dvv, double v1, double dv, int64_t n, SfPlan* p, double* v1_new,
+                   std::string* msg);
+// That interpolation of the device spectrum `in` into `out` (p.n_sp points).
+cudaError_t sf_launch_interp(const SfPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
+                             int* launches);
+
 // The scan of the device spectrum `in` (n points) into `out` (p.n_out
 // points) with the workspace `ws` (p.ws_bytes).  `upload` copies the plan's
 // tables with cudaMemcpyAsync from host memory that stays valid until the

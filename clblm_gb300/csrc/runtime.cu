@@ -145,7 +145,7 @@ struct clblm_handle {
   int64_t scan_n = 0;
   cufftHandle scan_fwd = 0, scan_inv = 0;
   bool scan_plans = false;
-  DevBuf scan_buf, scan_x0, scan_io;
+  DevBuf scan_buf, scan_buf2, scan_x0, scan_io;
   DevBuf sf_ws, sf_io;  // SCANFN: workspace, host input/output staging
   std::string errmsg;
   clblm_od_stats_t last{};
@@ -1546,6 +1546,7 @@ int clblm_gpu_destroy(clblm_handle_t* h) {
   h->scan_buf.release();
   h->scan_x0.release();
   h->scan_io.release();
+  h->scan_buf2.release();
   h->sf_ws.release();
   h->sf_io.release();
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
@@ -3419,22 +3420,28 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
 
 // ---- FFT instrument-function scan --------------------------------------------
 //
-// clblm_FFTSCN_struct (clblm_FFT.f90:352-844) for the scanning functions with
-// an analytic apodization (functID 2..8: triangle, Gaussian, sinc**2, sinc,
-// Beer, Hamming, Hanning; IVX = 1, which the reference takes whenever the
-// calculation range exceeds CRATIO half widths), the boxcar alone
-// (functID 1), pre-boxing with or without deconvolution, output on the scan
-// grid.  The host arithmetic below follows the reference's FP64 operations.
+// clblm_FFTSCN_struct (clblm_FFT.f90:352-844): functID 1 (the boxcar alone),
+// 2..11 and 14 (triangle, Gaussian, sinc**2, sinc, Beer, Hamming, Hanning,
+// Norton-Beer weak/medium/strong, Kiruna), 102..114 (the scan of a spectrum
+// pre-boxed outside, and the deconvolution of that boxing), -1 (the
+// deconvolution alone); the apodization computed analytically (IVX = 1) or
+// as the transform of the sampled scanning function (IVX = -1) as the
+// calculation range decides; pre-boxing with or without its deconvolution;
+// a spectrum coarser than 2*HWHM/12 interpolated first and the result
+// interpolated onto DVOUT > 0 (Intpdr, clblm_INTERP).  The host arithmetic
+// below follows the reference's FP64 operations.
 namespace {
 
 // C, CRATIO, CLIMIT of the scanning functions, clblm_FFT.f90:108-131
 constexpr double kScanC[14] = {0.0, 2.0, 0.849322, 2.257609, 3.314800, 2.100669, 2.195676,
                                2.0, 2.570274, 2.367714, 2.071759, -3.3, -2.5, 3.314800};
-constexpr double kScanCRatio[14] = {0.0, 40., 10., 40., 160., 20., 20., 20., 40., 40., 20., 100., 10., 1e308};
+constexpr double kScanCRatio[14] = {0.0, 40., 10., 40., 160., 20., 20., 20., 40., 40., 20., 100., 10.,
+                                    1.7976931348623157e308};  // huge(1.): REAL is binary64 in the reference's build
 constexpr double kScanCLimit[14] = {1., 2., 3., 40., 160., 20., 20., 20., 40., 40., 20., 100., 10., 160.};
 
 struct ScanPlan {
   int jfn = 0;
+  int ivx = 0;                  // 1: analytic apodization, -1: the scanning function's transform, 0: none
   double A = 0.;
   double V1Z = 0., V2Z = 0., DV = 0.;
   int64_t ltotal = 0, n1 = 0;   // loaded points, first input point (1-based)
@@ -3443,8 +3450,16 @@ struct ScanPlan {
   int nrec = 0;                 // records of 65536 points of the transform
   bool fft = false, deconv = false;
   double deconv_a = 0.;
-  int64_t N1 = 0, ntotal = 0;   // output: first point (1-based) and count
+  int64_t N1 = 0, ntotal = 0;   // scan grid: first point (1-based) and count
   double V1S = 0.;
+  double parms[3] = {0., 0., 0.};
+  // a coarse input interpolated onto 2*HWHM/12 first, and the result
+  // interpolated onto DVOUT
+  bool pre = false, post = false;
+  SfPlan pre_plan, post_plan;
+  // the output grid
+  double v1_out = 0., dv_out = 0.;
+  int64_t n_out = 0;
 };
 
 // LoadSpect's / Boxcar's record count: fourfold padding to a power of two
@@ -3461,43 +3476,76 @@ int scan_records(int64_t lt) {
 int scan_plan(clblm_handle* h, const clblm_scan_t* sc, double v1c, double dv, int64_t np, ScanPlan* p) {
   auto bad = [&](int code, const char* msg) { return h ? set_err(h, code, "%s", msg) : code; };
   if (!sc || !(dv > 0.) || np < 2) return bad(CLBLM_ERR_ARG, "FFTSCN: bad spectrum");
-  const double v2c = v1c + dv * (double)(np - 1);
+  double v2c = v1c + dv * (double)(np - 1);
   const double fill = sc->padding, hwhm = sc->hwhm;
   if (fill < 0. || fill > 1.) return bad(CLBLM_ERR_ARG, "FFTSCN: FILL value is out of range");
-  const int jfn = sc->funct_id - 1;
-  bool prebox = false, deconv = false;
-  double boxhw = 0.;
+  const int fid = sc->funct_id;
+  if (!((fid >= 1 && fid <= 14) || (fid >= 102 && fid <= 114) || fid == -1))
+    return bad(CLBLM_ERR_ARG, "FFTSCN: Value for functID must be in between [1,14] or [102,114] (or -1)");
+  int jfn = fid - 1;
+  bool prebox = false, deconv = false, deconv_only = false, deconv_fixed = false;
+  double boxhw = 0., deconv_hw = 0.;
   if (jfn == 0) {
     prebox = true;
     boxhw = hwhm;
-  } else if (jfn >= 1 && jfn <= 7) {
+  } else if (jfn >= 1 && jfn <= 13) {
     if (sc->prebox_hw > 0.) {
       prebox = true;
       deconv = sc->deconv_prebox != 0;
       boxhw = sc->prebox_hw;
     }
-  } else {
-    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: scanning functions 9..14 and deconvolution only are not on this path");
+  } else if (jfn >= 101 && jfn <= 113) {  // pre-boxed outside: the scan and the deconvolution
+    jfn -= 100;
+    deconv = deconv_fixed = true;
+    deconv_hw = sc->prebox_hw;
+  } else {  // -1: the deconvolution alone
+    deconv_only = deconv = deconv_fixed = true;
+    jfn = 0;
+    deconv_hw = sc->prebox_hw;
   }
   if (!(hwhm > 0.)) return bad(CLBLM_ERR_ARG, "FFTSCN: HWHM must be positive");
   p->jfn = jfn;
-  p->A = jfn > 0 ? kScanC[jfn] * hwhm : 0.;
+  for (int k = 0; k < 3; ++k) p->parms[k] = sc->parms[k];
+  if (jfn > 0) {
+    if (!(kScanC[jfn] > 0.))
+      return bad(CLBLM_ERR_ARG, "FFTSCN: for this scanning function (Brault, Kaiser-Bessel) the reference "
+                                "requires the interferometer optical path difference and stops");
+    p->A = kScanC[jfn] * hwhm;
+  }
   const double V1out = sc->v1out, V2out = sc->v2out;
   if (V1out >= V2out) return bad(CLBLM_ERR_ARG, "FFTSCN: Initial V >= final V");
   if (V1out >= v2c || V2out <= v1c) return bad(CLBLM_ERR_ARG, "FFTSCN: V1out to V2out is outside the data range");
-  double V1Z = V1out - hwhm * kScanCLimit[jfn];
-  double V2Z = V2out + hwhm * kScanCLimit[jfn];
-  V1Z = v1c + (double)(int64_t)((V1Z - v1c) / dv) * dv;
-  V2Z = v1c + (double)(int64_t)((V2Z - v1c) / dv + 1.01) * dv;
+  double V1Z, V2Z;
+  if (deconv_only) {
+    V1Z = v1c;
+    V2Z = v2c;
+  } else {
+    V1Z = V1out - hwhm * kScanCLimit[jfn];
+    V2Z = V2out + hwhm * kScanCLimit[jfn];
+    V1Z = v1c + (double)(int64_t)((V1Z - v1c) / dv) * dv;
+    V2Z = v1c + (double)(int64_t)((V2Z - v1c) / dv + 1.01) * dv;
+  }
   if (V1Z < v1c) V1Z = v1c;
   if (V2Z > v2c) V2Z = v2c;
   if ((V2Z - V1Z) / hwhm < kScanCLimit[jfn]) return bad(CLBLM_ERR_RANGE, "FFTSCN: insufficient data");
   const double DVN = 2. * hwhm / 12.;
-  if (dv > DVN && jfn != 0)
-    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: input grid coarser than 2*HWHM/12 (interpolation not on this path)");
-  if (jfn != 0 && !((V2Z - V1Z) / hwhm > kScanCRatio[jfn]))
-    return bad(CLBLM_ERR_UNSUPPORTED, "FFTSCN: apodization from the scanning function's transform (IVX = -1) "
-                                      "is not on this path");
+  if (dv > DVN && jfn != 0) {  // onto 2*HWHM/12 first (Intpdr)
+    std::string msg;
+    double vv1 = 0.;
+    const int rc = sf_plan_intpdr(V1Z, V2Z, DVN, v1c, dv, np, &p->pre_plan, &vv1, &msg);
+    if (rc) return h ? set_err(h, rc, "FFTSCN: %s", msg.c_str()) : rc;
+    p->pre = true;
+    v1c = vv1;
+    dv = DVN;
+    np = p->pre_plan.n_sp;
+    v2c = v1c + dv * (double)(np - 1);
+    V1Z = v1c;
+    V2Z = v2c;
+  }
+  p->ivx = jfn == 0 ? 0 : ((V2Z - V1Z) / hwhm > kScanCRatio[jfn] ? 1 : -1);
+  if (p->ivx == -1 && jfn >= 8 && jfn <= 10)
+    return bad(CLBLM_ERR_ARG, "FFTSCN: Norton-Beer apodization not yet implemented in spectral domain (as the "
+                              "reference, which stops)");
   // LoadSpect
   int64_t lt = (int64_t)((V2Z - V1Z) / dv + 1.1);
   V2Z = V1Z + dv * (double)(lt - 1);
@@ -3522,6 +3570,10 @@ int scan_plan(clblm_handle* h, const clblm_scan_t* sc, double v1c, double dv, in
       lt = p->ktotal;
     }
   }
+  if (deconv_fixed) {
+    p->deconv = true;
+    p->deconv_a = deconv_hw;
+  }
   if (p->nrec < 0) return bad(CLBLM_ERR_RANGE, "FFTSCN: transform too large");
   p->fft = jfn != 0 || p->deconv;
   p->V1Z = V1Z;
@@ -3541,6 +3593,20 @@ int scan_plan(clblm_handle* h, const clblm_scan_t* sc, double v1c, double dv, in
   p->V1S = V1S;
   if (p->ntotal < 1 || N1 - 1 + p->ntotal > (int64_t)p->nrec * kScanRecord)
     return bad(CLBLM_ERR_RANGE, "FFTSCN: output outside the transform");
+  p->v1_out = V1S;
+  p->dv_out = DV;
+  p->n_out = p->ntotal;
+  if (sc->dvout > 0.) {  // onto the requested grid (Intpdr)
+    if (p->ntotal < 8) return bad(CLBLM_ERR_RANGE, "FFTSCN: too few scanned points to interpolate");
+    std::string msg;
+    double vv1 = 0.;
+    const int rc = sf_plan_intpdr(V1out, V2out, sc->dvout, V1S, DV, p->ntotal, &p->post_plan, &vv1, &msg);
+    if (rc) return h ? set_err(h, rc, "FFTSCN: %s", msg.c_str()) : rc;
+    p->post = true;
+    p->v1_out = vv1;
+    p->dv_out = sc->dvout;
+    p->n_out = p->post_plan.n_sp;
+  }
   return CLBLM_OK;
 }
 
@@ -3553,9 +3619,9 @@ int clblm_gpu_fftscn_size(const clblm_scan_t* scan, double v1, double dv, int64_
   ScanPlan p;
   int rc = scan_plan(nullptr, scan, v1, dv, n, &p);
   if (rc) return rc;
-  if (v1s) *v1s = p.V1S;
-  if (dvs) *dvs = p.DV;
-  if (ns) *ns = p.ntotal;
+  if (v1s) *v1s = p.v1_out;
+  if (dvs) *dvs = p.dv_out;
+  if (ns) *ns = p.n_out;
   return CLBLM_OK;
 }
 
@@ -3564,29 +3630,45 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
   if (!h) return CLBLM_ERR_ARG;
   if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
   if (!spect || !out) return set_err(h, CLBLM_ERR_ARG, "FFTSCN: null spectrum or output");
+  if (flags != CLBLM_OUT_HOST && flags != CLBLM_OUT_DEVICE) return set_err(h, CLBLM_ERR_ARG, "FFTSCN: bad flags");
   ScanPlan p;
   int rc = scan_plan(h, scan, v1, dv, n, &p);
   if (rc) return rc;
-  if (cap < p.ntotal) return set_err(h, CLBLM_ERR_CAPACITY, "FFTSCN: output needs %lld points", (long long)p.ntotal);
+  if (cap < p.n_out) return set_err(h, CLBLM_ERR_CAPACITY, "FFTSCN: output needs %lld points", (long long)p.n_out);
   h->reset_call();
   const bool dev = flags == CLBLM_OUT_DEVICE;
   const int64_t N = (int64_t)p.nrec * kScanRecord;
   cudaStream_t st = h->stream;
-  // the input spectrum's used span on the device
+  // host staging: the input and the final output
   const double* din = spect;
-  int64_t off = p.n1 - 1;
   if (!dev) {
-    CUDA_TRY(h, h->scan_io.ensure(sizeof(double) * (size_t)std::max<int64_t>(p.ltotal, p.ntotal)));
-    CUDA_TRY(h, cudaMemcpyAsync(h->scan_io.p, spect + off, sizeof(double) * p.ltotal, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(h, h->scan_io.ensure(sizeof(double) * (size_t)(n + std::max<int64_t>(p.n_out, 1))));
+    CUDA_TRY(h, cudaMemcpyAsync(h->scan_io.p, spect, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
     din = h->scan_io.as<double>();
-    off = 0;
   }
+  double* dfinal = dev ? out : h->scan_io.as<double>() + n;
+  // auxiliary device memory: the interpolated input and its workspace, the
+  // scan grid before the output interpolation and its workspace
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t a_pre = p.pre ? al(sizeof(double) * (size_t)p.pre_plan.n_sp) : 0;
+  const size_t a_prews = p.pre ? al(p.pre_plan.ws_bytes) : 0;
+  const size_t a_scan = p.post ? al(sizeof(double) * (size_t)p.ntotal) : 0;
+  const size_t a_postws = p.post ? al(p.post_plan.ws_bytes) : 0;
+  CUDA_TRY(h, h->sf_ws.ensure(std::max<size_t>(a_pre + a_prews + a_scan + a_postws, 256)));
+  unsigned char* aux = h->sf_ws.as<unsigned char>();
+  int launches = 0;
+  if (p.pre) {
+    double* sp = reinterpret_cast<double*>(aux);
+    CUDA_TRY(h, sf_launch_interp(p.pre_plan, din, sp, aux + a_pre, st, &launches));
+    din = sp;
+  }
+  h->launches += launches;
   // transform buffer: N reals, in place as N/2+1 complex
   CUDA_TRY(h, h->scan_buf.ensure(sizeof(double2) * (size_t)(N / 2 + 1)));
   double* x = h->scan_buf.as<double>();
   const unsigned grid = (unsigned)std::min<int64_t>((N + 255) / 256, 152 * 32);
   h->launches++;
-  k_scan_load<<<grid, 256, 0, st>>>(din, off, p.ltotal, p.M, p.ktotal, scan->padding, x, N);
+  k_scan_load<<<grid, 256, 0, st>>>(din, p.n1 - 1, p.ltotal, p.M, p.ktotal, scan->padding, x, N);
   CUDA_TRY(h, cudaGetLastError());
   if (p.fft) {
     if (!h->scan_plans || h->scan_n != N) {
@@ -3608,11 +3690,25 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
       return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: cufftSetStream");
     if (cufftExecD2Z(h->scan_fwd, x, reinterpret_cast<cufftDoubleComplex*>(x)) != CUFFT_SUCCESS)
       return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: forward transform");
+    if (p.ivx == -1) {
+      // the scanning function sampled at DV, transformed; its first
+      // coefficient (the area) normalises it
+      CUDA_TRY(h, h->scan_buf2.ensure(sizeof(double2) * (size_t)(N / 2 + 1)));
+      double* y = h->scan_buf2.as<double>();
+      h->launches += 2;
+      k_scan_sfn<<<grid, 256, 0, st>>>(p.jfn, p.A, p.DV, N, p.parms[0], p.parms[1], p.parms[2], y);
+      CUDA_TRY(h, cudaGetLastError());
+      if (cufftExecD2Z(h->scan_fwd, y, reinterpret_cast<cufftDoubleComplex*>(y)) != CUFFT_SUCCESS)
+        return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: transform of the scanning function");
+      k_scan_mulnum<<<grid, 256, 0, st>>>(reinterpret_cast<const double2*>(y), N / 2,
+                                          reinterpret_cast<double2*>(x));
+      CUDA_TRY(h, cudaGetLastError());
+    }
     // path differences at the start of every record, accumulated as
     // Scnfnt leaves X after each record (X0 + 32768*DX)
     ScanArgs a;
     std::memset(&a, 0, sizeof a);
-    a.jfn = p.jfn;
+    a.jfn = p.ivx == 1 ? p.jfn : 0;  // the analytic apodization, or none (done above)
     a.A = p.A;
     a.DX = 1.0 / ((double)((int64_t)kScanRecord * p.nrec) * p.DV);
     a.nhalf = N / 2;
@@ -3620,7 +3716,7 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
     double X = 0.;
     for (int j = 0; j < p.nrec; ++j) {
       x0[j] = X;
-      if (p.jfn == 4 && a.nedge < kScanMaxEdges) {  // the rectangle's interpolated end point
+      if (a.jfn == 4 && a.nedge < kScanMaxEdges) {  // the rectangle's interpolated end point
         const double alen = 1.0 / p.A;
         int64_t nn = (int64_t)((alen - X) / a.DX) + 1;
         double r = (alen - X) / a.DX + 1.0 - (double)nn;
@@ -3636,24 +3732,31 @@ int clblm_gpu_fftscn(clblm_handle_t* h, const clblm_scan_t* scan, const double* 
       }
       X = X + (double)kScanRecord * a.DX / 2.0;
     }
-    CUDA_TRY(h, h->scan_x0.ensure(sizeof(double) * (size_t)p.nrec));
-    CUDA_TRY(h, cudaMemcpyAsync(h->scan_x0.p, x0.data(), sizeof(double) * p.nrec, cudaMemcpyHostToDevice, st));
-    a.X0 = h->scan_x0.as<double>();
     a.deconv = p.deconv ? 1 : 0;
     a.deconv_a = p.deconv_a;
-    h->launches++;
-    k_scan_apod<<<grid, 256, 0, st>>>(a, reinterpret_cast<double2*>(x));
-    CUDA_TRY(h, cudaGetLastError());
+    if (a.jfn > 0 || a.deconv) {
+      CUDA_TRY(h, h->scan_x0.ensure(sizeof(double) * (size_t)p.nrec));
+      CUDA_TRY(h, cudaMemcpyAsync(h->scan_x0.p, x0.data(), sizeof(double) * p.nrec, cudaMemcpyHostToDevice, st));
+      a.X0 = h->scan_x0.as<double>();
+      h->launches++;
+      k_scan_apod<<<grid, 256, 0, st>>>(a, reinterpret_cast<double2*>(x));
+      CUDA_TRY(h, cudaGetLastError());
+    }
     if (cufftExecZ2D(h->scan_inv, reinterpret_cast<cufftDoubleComplex*>(x), x) != CUFFT_SUCCESS)
       return set_err(h, CLBLM_ERR_CUDA, "FFTSCN: inverse transform");
     CUDA_TRY(h, cudaStreamSynchronize(st));  // x0 goes out of scope
   }
-  double* dst = dev ? out : h->scan_io.as<double>();
+  double* dscan = p.post ? reinterpret_cast<double*>(aux + a_pre + a_prews) : dfinal;
   h->launches++;
   k_scan_out<<<(unsigned)std::min<int64_t>((p.ntotal + 255) / 256, 152 * 32), 256, 0, st>>>(
-      x, p.N1 - 1, p.ntotal, p.fft ? 1.0 / (double)N : 1.0, dst);
+      x, p.N1 - 1, p.ntotal, p.fft ? 1.0 / (double)N : 1.0, dscan);
   CUDA_TRY(h, cudaGetLastError());
-  if (!dev) CUDA_TRY(h, cudaMemcpyAsync(out, dst, sizeof(double) * p.ntotal, cudaMemcpyDeviceToHost, st));
+  if (p.post) {
+    launches = 0;
+    CUDA_TRY(h, sf_launch_interp(p.post_plan, dscan, dfinal, aux + a_pre + a_prews + a_scan, st, &launches));
+    h->launches += launches;
+  }
+  if (!dev) CUDA_TRY(h, cudaMemcpyAsync(out, dfinal, sizeof(double) * p.n_out, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
   h->last.launches = h->launches;
   return CLBLM_OK;

@@ -260,6 +260,45 @@ static int sf_plan_interp(double V1, double V2, double DVO, double v1, double dv
   return CLBLM_OK;
 }
 
+int sf_plan_intpdr(double vv1, double vv2, double dvv, double v1, double dv, int64_t n, SfPlan* p, double* v1_new,
+                   std::string* msg) {
+  *p = SfPlan();
+  if (!(dvv > 0.) || !(dv > 0.) || n < 8) {
+    *msg = "Intpdr: bad grid";
+    return CLBLM_ERR_ARG;
+  }
+  // the requested limits pulled inside the data by whole steps (Intpdr, clblm_FFT.f90:2392-2443)
+  const double V1C = v1, V2C = v1 + dv * (double)(n - 1);
+  if (vv1 < V1C) {
+    const double AN = (V1C - vv1) / dvv;
+    vv1 = AN == (double)(int64_t)AN ? vv1 + dvv * (double)(int64_t)AN : vv1 + dvv * (double)((int64_t)AN + 1);
+  }
+  if (vv2 > V2C) {
+    const double AN = (vv2 - V2C) / dvv;
+    vv2 = AN == (double)(int64_t)AN ? vv2 - dvv * (double)(int64_t)AN : vv2 - dvv * (double)((int64_t)AN + 1);
+  }
+  p->interp = true;
+  p->dvint = dvv;
+  p->n_in = n;
+  const int rc = sf_plan_interp(vv1, vv2, dvv, v1, dv, n, p, msg);
+  if (rc) return rc;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  p->o_seg = take(sizeof(SfSeg) * std::max<size_t>(p->segs.size(), 1));
+  p->o_coef = take(sizeof(double) * p->coef.size());
+  p->ws_bytes = off;
+  p->kind = 2;
+  p->n_out = p->n_sp;
+  p->v1_out = vv1;
+  p->dv_out = dvv;
+  *v1_new = vv1;
+  return CLBLM_OK;
+}
+
 int sf_plan(int funct_id, double functHWHM, double v1out, double v2out, double dvout, double v1, double dv, int64_t n,
             SfPlan* p, std::string* msg) {
   *p = SfPlan();
@@ -771,6 +810,29 @@ __global__ void k_sf_rect(SfRectArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+cudaError_t sf_launch_interp(const SfPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
+                             int* launches) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * (size_t)p.n_sp, st);
+  if (e != cudaSuccess || p.segs.empty()) return e;
+  SfSeg* segs = reinterpret_cast<SfSeg*>(ws + p.o_seg);
+  double* coef = reinterpret_cast<double*>(ws + p.o_coef);
+  if ((e = cudaMemcpyAsync(segs, p.segs.data(), sizeof(SfSeg) * p.segs.size(), cudaMemcpyHostToDevice, st)))
+    return e;
+  if ((e = cudaMemcpyAsync(coef, p.coef.data(), sizeof(double) * p.coef.size(), cudaMemcpyHostToDevice, st)))
+    return e;
+  SfInterpArgs ia;
+  ia.segs = segs;
+  ia.nseg = (int)p.segs.size();
+  ia.in = in;
+  ia.n_in = p.n_in;
+  ia.coef = coef;
+  ia.vratio = p.vratio;
+  ia.out = out;
+  ++*launches;
+  k_sf_interp<<<(ia.nseg + 63) / 64, 64, 0, st>>>(ia);
+  return cudaGetLastError();
+}
+
 cudaError_t sf_launch(const SfPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
                       int* launches) {
   cudaError_t e;

@@ -419,22 +419,30 @@ int clblm_gpu_layer_amounts(clblm_handle_t *h, int32_t nlev, int32_t nmol,
  *
  * clblm_FFTSCN (clblm_FFT.f90:308-844): a spectrum on a uniform grid
  * convolved with a scanning function through Fourier transforms, as the
- * post-processing of RT_Jac (postProc_scan) applies it.  On this path: the
- * scanning functions whose apodization the reference computes analytically
- * (functID 2..8: triangle, Gaussian, sinc**2, sinc, Beer, Hamming, Hanning;
- * the reference takes that branch whenever the calculation range exceeds
- * CRATIO half widths), the boxcar alone (functID 1), pre-boxing with or
- * without its deconvolution; the result stays on the scan grid.  The
- * reference's transform is zero-padded (FILL) to four times the next power
- * of two of its 65536-point records; this one is the same size. */
+ * post-processing of RT_Jac (postProc_scan) applies it.  functID 1: the
+ * boxcar alone; 2..11: triangle, Gaussian, sinc**2, sinc, Beer, Hamming,
+ * Hanning, Norton-Beer weak, medium, strong; 14: Kiruna (two sincs, parms
+ * = offset, weight at 0, weight at the offset); 102..114: the scan of a
+ * spectrum boxed outside (prebox_hw) and the deconvolution of that box; -1:
+ * that deconvolution alone.  The apodization is computed analytically when
+ * the calculation range exceeds CRATIO half widths, else as the transform of
+ * the sampled scanning function (Kiruna always); pre-boxing with or without
+ * its deconvolution.  A spectrum coarser than 2*HWHM/12 is interpolated onto
+ * it first and, with dvout > 0, the result onto V1out..V2out at dvout
+ * (Intpdr: clblm_INTERP's four-point scheme).  functID 12, 13 (Brault,
+ * Kaiser-Bessel) need an optical path difference the reference does not
+ * take: CLBLM_ERR_ARG, as it stops.  The reference's transform is
+ * zero-padded (FILL) to four times the next power of two of its 65536-point
+ * records; this one is the same size. */
 typedef struct {
-  int32_t funct_id;      /* 1: boxcar only; 2..8: triangle, Gaussian, sinc**2,
-                          * sinc, Beer, Hamming, Hanning                      */
+  int32_t funct_id;      /* functID, as above                                */
   int32_t deconv_prebox; /* 1: deconvolve the pre-boxing                     */
   double  hwhm;          /* functHWHM [cm-1] (sinc: 1/(3.3148 * OPD))        */
   double  padding;       /* FILL in [0, 1]: 0 for radiance, 1 transmittance  */
   double  prebox_hw;     /* preBoxHW [cm-1]; <= 0: no pre-boxing             */
   double  v1out, v2out;  /* requested limits [cm-1]                          */
+  double  dvout;         /* DVOUT [cm-1]; <= 0: the scan grid                */
+  double  parms[3];      /* functParams: PARM1..PARM3 (Kiruna)               */
 } clblm_scan_t;
 
 /* Grid of the scanned spectrum of a spectrum on v1 + i*dv, i < n: first

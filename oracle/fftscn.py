@@ -14,10 +14,17 @@ the record size inside), so the scan is the circular convolution of the
 FILL-padded spectrum with the unit-area scanning function.  Any correct FFT
 gives the same values up to rounding; numpy's is used here.
 
-Covered: functID 1 (boxcar only) and 2..8 (triangle, Gaussian, sinc**2,
-sinc, Beer, Hamming, Hanning) with the apodization computed analytically
-(IVX = 1: (V2Z-V1Z)/HWHM > CRATIO), optional pre-boxing with deconvolution,
-output on the scan grid (DVOUT <= 0).
+Covered: functID 1 (boxcar only), 2..11 and 14 (triangle, Gaussian,
+sinc**2, sinc, Beer, Hamming, Hanning, Norton-Beer weak/medium/strong,
+Kiruna) with the apodization computed analytically (IVX = 1: (V2Z-V1Z)/HWHM
+> CRATIO) or as the transform of the sampled scanning function (IVX = -1,
+Scntrn :2097-2163), optional pre-boxing with deconvolution, the
+deconvolution of an external pre-boxing (functID 102..114) or alone
+(functID -1), the interpolation of a spectrum coarser than 2*HWHM/12 before
+the scan and onto DVOUT after it (Intpdr :2392-2443, clblm_INTERP through
+the C oracle).  As in the reference, Brault and Kaiser-Bessel (functID 12,
+13) stop for want of an optical path difference, and the Norton-Beer
+functions have no spectral-domain form (IVX = -1 stops).
 """
 import math
 
@@ -66,7 +73,9 @@ def apodization(jfn, A, dv, nrec, deconv_a=None):
     for j in range(nrec):
         x = X0 + kk * DX  # X = X0 + (L+1)*DX/2: round((L+1)*DX)/2 = round(k*DX)
         sl = slice(j * half, (j + 1) * half)
-        if jfn == 1:    # triangle: sinc**2
+        if jfn == 0:    # no scanning function (the deconvolution alone)
+            h = np.ones_like(x)
+        elif jfn == 1:    # triangle: sinc**2
             z = PI * x * A
             with np.errstate(invalid="ignore", divide="ignore"):
                 h = np.where(x == 0, 1.0, (np.sin(z) / z) ** 2)
@@ -91,6 +100,15 @@ def apodization(jfn, A, dv, nrec, deconv_a=None):
             h = np.where(x < 1.0 / A, 0.53835685 * (1.0 + 0.857504 * np.cos(PI * x * A)), 0.0)
         elif jfn == 7:  # Hanning
             h = np.where(x < 1.0 / A, 0.5 * (1.0 + np.cos(PI * x * A)), 0.0)
+        elif jfn in (8, 9, 10):  # Norton-Beer weak, medium, strong (:1774-1813)
+            u = 1.0 - (x * A) ** 2
+            if jfn == 8:
+                f = 0.384093 - 0.087577 * u + 0.703484 * u ** 2
+            elif jfn == 9:
+                f = 0.152442 - 0.136176 * u + 0.983734 * u ** 2
+            else:
+                f = 0.045355 + 0.554883 * u ** 2 + 0.399782 * u ** 4
+            h = np.where(x < 1.0 / A, f, 0.0)
         else:
             raise ScanError("scanning function %d is not covered" % jfn)
         H[sl] = h
@@ -105,7 +123,80 @@ def apodization(jfn, A, dv, nrec, deconv_a=None):
     return H, D
 
 
-def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.0, deconv_prebox=False):
+def scanning_function(jfn, A, x, parms=(0.0, 0.0, 0.0)):
+    """The scanning function of JFN at wavenumber offsets x (Scnfnt with
+    IAPSC = -1, :1499-1921): triangle, Gaussian, sinc**2, sinc, Beer,
+    Hamming, Hanning, Kiruna."""
+    PI = 2.0 * math.asin(1.0)
+    x = np.asarray(x, dtype=np.float64)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        if jfn == 1:
+            return np.where(x > A, 0.0, 1.0 - x / A)
+        if jfn == 2:
+            return np.exp(-np.minimum(0.5 * (x / A) ** 2, ARGMIN))
+        if jfn == 3:
+            z = PI * x / A
+            return np.where(x != 0, (np.sin(z) / z) ** 2, 1.0)
+        if jfn == 4:
+            z = 2.0 * PI * x / A
+            return np.where(x != 0, np.sin(z) / z, 1.0)
+        if jfn == 5:
+            u = 2.0 * PI * x / A
+            return np.where(u >= 0.5, 15. * ((3.0 - u ** 2) * np.sin(u) - 3.0 * u * np.cos(u)) / (u ** 5),
+                            1.0 - 15.0 / 210 * u ** 2)
+        if jfn in (6, 7):
+            c = 0.428752 if jfn == 6 else 0.5
+            u = 2.0 * PI * x / A
+            f = np.sin(u) / u + c * (np.sin(u + PI) / (u + PI) + np.sin(u - PI) / (u - PI))
+            f = np.where(u == 0, 1.0, f)
+            return np.where(np.abs(u) == PI, c, f)
+        if jfn == 13:
+            u1 = 2.0 * PI * x / A
+            u2 = 2.0 * PI * (x - parms[0]) / A
+            f1 = np.where(u1 == 0.0, 1.0, np.sin(u1) / u1)
+            f2 = np.where(u2 == 0.0, 1.0, np.sin(u2) / u2)
+            return parms[1] * f1 + parms[2] * f2
+    raise ScanError("scanning function %d has no spectral-domain form" % jfn)
+
+
+def numeric_apodization(jfn, A, dv, nrec, parms=(0.0, 0.0, 0.0)):
+    """IVX = -1 (Scntrn :2097-2163): the scanning function sampled at DV in
+    the transform's circular layout, transformed, over its first coefficient
+    (its area).  The symmetric functions hold f(g DV) at g < N/2 and
+    f((N-g) DV) above; the asymmetric Kiruna function's negative blocks are
+    written as the reference writes them, from X = VSAVE + DV downwards and
+    reversed: block J (of 65536 points, counted from the end) holds
+    f(((2J-2)*65536 - (N-g) + 2) DV)."""
+    lpts = LPTSMX
+    n = nrec * lpts
+    g = np.arange(n, dtype=np.int64)
+    if jfn == 13:
+        ng = n - g
+        J = (ng + lpts - 1) // lpts
+        xneg = ((2 * J - 2) * lpts - ng + 2).astype(np.float64) * dv
+        x = np.where(g < n // 2, g.astype(np.float64) * dv, xneg)
+    else:
+        x = np.minimum(g, n - g).astype(np.float64) * dv
+    F = np.fft.rfft(scanning_function(jfn, A, x, parms))
+    return F / F[0].real
+
+
+def intpdr(spect, v1c, dv, vv1, vv2, dvv):
+    """Intpdr (:2392-2443): the requested limits pulled inside the data by
+    whole steps, then clblm_INTERP onto vv1 + j*dvv.  Returns (spectrum, V1)."""
+    from oracle import oracle as O
+    v2c = v1c + dv * (len(spect) - 1)
+    if vv1 < v1c:
+        an = (v1c - vv1) / dvv
+        vv1 = vv1 + dvv * int(an) if an == int(an) else vv1 + dvv * (int(an) + 1)
+    if vv2 > v2c:
+        an = (vv2 - v2c) / dvv
+        vv2 = vv2 - dvv * int(an) if an == int(an) else vv2 - dvv * (int(an) + 1)
+    return O.sf_interp(spect, v1c, dv, vv1, vv2, dvv), vv1
+
+
+def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.0, deconv_prebox=False,
+           dvout=0.0, parms=(0.0, 0.0, 0.0)):
     """clblm_FFTSCN_struct (:352-844) for the cases above.  Returns
     (scanned spectrum, V1S, DV) on the scan grid."""
     spect = np.asarray(spect, dtype=np.float64)
@@ -113,7 +204,11 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
     v2c = v1c + dv * (np_in - 1)
     if not (0.0 <= fill <= 1.0):
         raise ScanError("FILL out of range")
+    if not (1 <= funct_id <= 14 or 102 <= funct_id <= 114 or funct_id == -1):
+        raise ScanError("functID must be in [1,14] or [102,114], or -1")
     jfn = funct_id - 1
+    deconv_only = False
+    deconv_hw = None
     if jfn == 0:
         do_prebox, do_deconv, boxcar_hw = True, False, hwhm
     elif 1 <= jfn <= 13:
@@ -121,8 +216,13 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
             do_prebox, do_deconv, boxcar_hw = False, False, 0.0
         else:
             do_prebox, do_deconv, boxcar_hw = True, bool(deconv_prebox), prebox_hw
-    else:
-        raise ScanError("functID %d is not covered" % funct_id)
+    elif 101 <= jfn <= 113:  # pre-boxed outside: the scan and the deconvolution
+        jfn -= 100
+        do_prebox, do_deconv, boxcar_hw, deconv_hw = False, True, 0.0, prebox_hw
+    else:  # -1: the deconvolution alone
+        deconv_only = True
+        jfn = 0
+        do_prebox, do_deconv, boxcar_hw, deconv_hw = False, True, 0.0, prebox_hw
     if jfn > 0:
         if C[jfn] <= 0:
             raise ScanError("scanning function needs an optical path difference")
@@ -132,10 +232,13 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
     if v1out >= v2out or v1out >= v2c or v2out <= v1c:
         raise ScanError("V1out..V2out outside the data")
     # limits of the internal calculation (:527-578)
-    V1Z = v1out - hwhm * CLIMIT[jfn]
-    V2Z = v2out + hwhm * CLIMIT[jfn]
-    V1Z = v1c + float(int((V1Z - v1c) / dv)) * dv
-    V2Z = v1c + float(int((V2Z - v1c) / dv + 1.01)) * dv
+    if deconv_only:
+        V1Z, V2Z = v1c, v2c
+    else:
+        V1Z = v1out - hwhm * CLIMIT[jfn]
+        V2Z = v2out + hwhm * CLIMIT[jfn]
+        V1Z = v1c + float(int((V1Z - v1c) / dv)) * dv
+        V2Z = v1c + float(int((V2Z - v1c) / dv + 1.01)) * dv
     if V1Z < v1c:
         V1Z = v1c
     if V2Z > v2c:
@@ -143,10 +246,17 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
     if (V2Z - V1Z) / hwhm < CLIMIT[jfn]:
         raise ScanError("insufficient data for an accurate calculation")
     DVN = 2.0 * hwhm / MDVHW
-    if dv > DVN and jfn != 0:
-        raise ScanError("input grid coarser than 2*HWHM/12: the interpolation step is not covered")
-    if jfn != 0 and not ((V2Z - V1Z) / hwhm > CRATIO[jfn]):
-        raise ScanError("apodization from the scanning function's transform (IVX = -1) is not covered")
+    if dv > DVN and jfn != 0:  # a coarse grid: onto 2*HWHM/12 first (:592-610)
+        spect, v1c = intpdr(spect, v1c, dv, V1Z, V2Z, DVN)
+        dv = DVN
+        np_in = len(spect)
+        v2c = v1c + dv * (np_in - 1)
+        V1Z, V2Z = v1c, v2c
+    ivx = 1 if (V2Z - V1Z) / hwhm > CRATIO[jfn] else -1
+    if jfn == 0:
+        ivx = 0
+    if ivx == -1 and jfn in (8, 9, 10):
+        raise ScanError("Norton-Beer apodization has no spectral-domain form (IVX = -1)")
     # LoadSpect (:1113-1290)
     ltotal = int((V2Z - V1Z) / dv + 1.1)
     V2Z = V1Z + dv * (ltotal - 1)
@@ -179,12 +289,15 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
             deconv_a = DV
         else:
             do_deconv = False
+    if deconv_hw is not None:
+        deconv_a = deconv_hw
     if not do_deconv:
         deconv_a = None
     if jfn != 0 or do_deconv:
         F = np.fft.rfft(x)
-        H, D = apodization(jfn, A, DV, nrec, deconv_a)
-        F = F * H
+        H, D = apodization(jfn if ivx == 1 else 0, A, DV, nrec, deconv_a)
+        if jfn != 0:
+            F = F * (H if ivx == 1 else numeric_apodization(jfn, A, DV, nrec, parms))
         if D is not None:
             F = F * D
         x = np.fft.irfft(F, n=nrec * LPTSMX)
@@ -199,4 +312,8 @@ def fftscn(spect, v1c, dv, funct_id, hwhm, v1out, v2out, fill=0.0, prebox_hw=-1.
     if V2S > V2Z:
         N2 = int((V2Z - V1Z) / DV + 1.01)
     ntotal = N2 - N1 + 1
-    return x[N1 - 1:N1 - 1 + ntotal].copy(), V1S, DV
+    out = x[N1 - 1:N1 - 1 + ntotal].copy()
+    if dvout > 0:  # onto the requested grid (:804-820)
+        out, V1S = intpdr(out, V1S, DV, v1out, v2out, dvout)
+        DV = dvout
+    return out, V1S, DV

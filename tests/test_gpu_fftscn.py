@@ -36,6 +36,32 @@ def test_scan_matches_oracle(gpu_lib, funct_id, prebox, deconv, fill):
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-11 * np.abs(want).max())
 
 
+@pytest.mark.parametrize("funct_id,hw,a,b,prebox,dvout,dv", [
+    (9, 0.3, 1030.0, 1070.0, -1.0, 0.0, 0.002),     # Norton-Beer weak
+    (10, 0.3, 1030.0, 1070.0, -1.0, 0.0, 0.002),    # Norton-Beer medium
+    (11, 0.3, 1030.0, 1070.0, -1.0, 0.0, 0.002),    # Norton-Beer strong
+    (2, 4.0, 1040.0, 1060.0, -1.0, 0.0, 0.002),     # triangle from its transform (IVX = -1)
+    (3, 12.0, 1040.0, 1060.0, -1.0, 0.0, 0.002),    # Gaussian, IVX = -1
+    (14, 0.1, 1030.0, 1070.0, -1.0, 0.0, 0.002),    # Kiruna (asymmetric, IVX = -1)
+    (3, 0.3, 1030.0, 1070.0, -1.0, 0.0, 0.1),       # a coarse input, interpolated first
+    (5, 0.3771, 1030.0, 1070.0, -1.0, 0.01, 0.002), # onto DVOUT
+    (103, 0.3, 1030.0, 1070.0, 0.01, 0.0, 0.002),   # boxed outside: scan + deconvolution
+    (-1, 0.3, 1030.0, 1070.0, 0.01, 0.0, 0.002),    # the deconvolution alone
+])
+def test_scan_options_match_oracle(gpu_lib, funct_id, hw, a, b, prebox, dvout, dv):
+    x, v1, dv = _spectrum(dv=dv)
+    parms = (0.05, 0.9, 0.1)
+    want, v1s, dvs = S.fftscn(x, v1, dv, funct_id, hw, a, b, prebox_hw=prebox, dvout=dvout, parms=parms)
+    h = gpu_lib.Handle(*_lines())
+    try:
+        got, g1, gdv = h.fftscn(T.scan_struct(funct_id, hw, a, b, prebox_hw=prebox, dvout=dvout, parms=parms), x,
+                                v1, dv)
+    finally:
+        h.close()
+    assert (g1, gdv, len(got)) == (v1s, dvs, len(want))
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-11 * np.abs(want).max())
+
+
 def test_scan_large_transform(gpu_lib):
     """4.2 M input points, 3.2 M of them loaded: a 2^24-point transform (256
     records of 65536; the sinc rectangle ends inside a later record)."""
