@@ -57,7 +57,8 @@ class clblm_od_ctrl_t(C.Structure):
     _fields_ = [("jrad", C.c_int32), ("line_rejec", C.c_int32), ("dptmin", C.c_double),
                 ("dptfac", C.c_double), ("xself", C.c_double), ("xfrgn", C.c_double),
                 ("contnm_off", C.c_int32), ("line_off", C.c_int32), ("precision", C.c_int32),
-                ("jac_mol", C.c_int32), ("reserved", C.c_int32), ("xco2c", C.c_double), ("xn2cn", C.c_double)]
+                ("jac_mol", C.c_int32), ("reserved", C.c_int32), ("xco2c", C.c_double), ("xn2cn", C.c_double),
+                ("xo3cn", C.c_double), ("xo2cn", C.c_double), ("xrayl", C.c_double)]
 
 
 class clblm_column_t(C.Structure):
@@ -234,11 +235,14 @@ def grid_struct(v1, v2, dv_normal, dv_narrow, dv_out=-999.9, sample=4.0, alfal0=
 
 
 def od_ctrl(precision=CLBLM_PREC_MIXED, jrad=1, line_rejec=1, dptmin=0.0, dptfac=0.0,
-            xself=1.0, xfrgn=1.0, contnm_off=0, line_off=0, jac_mol=0, xco2c=1.0, xn2cn=1.0):
+            xself=1.0, xfrgn=1.0, contnm_off=0, line_off=0, jac_mol=0, xco2c=1.0, xn2cn=1.0, xo3cn=1.0,
+            xo2cn=1.0, xrayl=1.0):
+    """CLBLM_OD_Ctrl with the reference's defaults (clblm_Config.f90:88-110)."""
     c = clblm_od_ctrl_t()
     c.jrad, c.line_rejec, c.dptmin, c.dptfac = jrad, line_rejec, dptmin, dptfac
     c.xself, c.xfrgn, c.contnm_off, c.line_off = xself, xfrgn, contnm_off, line_off
     c.precision, c.jac_mol, c.xco2c, c.xn2cn = precision, jac_mol, xco2c, xn2cn
+    c.xo3cn, c.xo2cn, c.xrayl = xo3cn, xo2cn, xrayl
     return c
 
 

@@ -73,6 +73,7 @@ struct LayerPlan {
   double v1abs, v2abs, dvabs, xself, xfrgn, wk1, h2o_fac;
   double xco2c;                   // XCO2C: scale of the CO2 continuum (0: none)
   double xn2cn;                   // XN2CN: scale of the N2 continua (0: none)
+  double xo3cn, xo2cn, xrayl;      // XO3CN, XO2CN, XRAYL: O3 and O2 continua, Rayleigh (0: none)
   int nptabs;
   // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
   int sel[kTIPSNMOL + 1];

@@ -38,6 +38,11 @@ struct ContIn {
   const double* n2r;
   const double* n2f;
   const double* n2o1;
+  // O3 continua: XO3CHP's X, Y, Z (3 x 3150), O3HHT0/1/2 (3 x 2687), O3HHUV
+  // (133); O2 continua: o2_ver_1's XO2, XO2T (2 x 103), O2INF1 (483), O2INF3
+  // (261), O2_vis (1488), O2FUV (1512)
+  const double* o3;
+  const double* o2;
 };
 
 // LINF4Q-corrected line (before SHRINQ)

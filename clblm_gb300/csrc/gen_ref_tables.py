@@ -26,6 +26,14 @@ Tables extracted (reference file:line):
     272 K and 228 K and the H2O efficiencies (n2_ver_1, 230 points from
     1993.8 cm-1), the first overtone's coefficients (n2_overtone1, 201
     points from 4325 cm-1)
+  * O3 continua: Chappuis X, Y, Z (XO3CHP, 3150 points from 8920 cm-1),
+    Hartley-Huggins at 0 C and its linear and quadratic temperature
+    coefficients (O3HHT0/1/2, 2687 points from 27370 cm-1), the UV
+    (O3HHUV, 133 points from 40800 cm-1)
+  * O2 continua: the fundamental's XO2, XO2T (o2_ver_1, 103 points from
+    1340 cm-1), the 1.27 um band (O2INF1, 483 from 7536), the A band
+    (O2INF3, 261 from 12961.5), the visible (O2_vis, 1488 from 15000), the
+    far UV (O2FUV, 1512 from 56740)
 
 Run (in a tree where the reference is mounted):
     python clblm_gb300/csrc/gen_ref_tables.py <CLBLM source root> > clblm_gb300/csrc/clblm_ref_tables.h
@@ -39,9 +47,10 @@ NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[EeDd][-+]?\d+)?"
 
 
 def _numbers(text):
+    """The values of a DATA list, a repeat count N*value expanded."""
     out = []
-    for tok in re.findall(NUM, text):
-        out.append(tok.replace("D", "E").replace("d", "e"))
+    for rep, tok in re.findall(r"(?:(\d+)\s*\*\s*)?(%s)" % NUM, text):
+        out.extend([tok.replace("D", "E").replace("d", "e")] * (int(rep) if rep else 1))
     return out
 
 
@@ -105,6 +114,26 @@ def _data_block(src, start_pat, data_pat, count):
     return vals
 
 
+def _data_segments(src, start_pat, name, count):
+    """An array filled by segments DATA (NAME(I),I= a, b)/.../ after start_pat."""
+    st = re.search(start_pat, src, re.I)
+    if not st:
+        raise SystemExit("%s not found" % start_pat)
+    end = re.search(r"END\s+SUBROUTINE", src[st.end():], re.I)
+    text = "\n".join(line.split("!")[0] for line in src[st.start():st.end() + end.start()].splitlines())
+    vals = [None] * count
+    for m in re.finditer(r"DATA\s*\(\s*%s\s*\(\s*I\s*\)\s*,\s*I\s*=\s*(\d+)\s*,\s*(\d+)\s*\)\s*/(.*?)/" % name,
+                         text, re.S | re.I):
+        a, b = int(m.group(1)), int(m.group(2))
+        seg = _numbers(m.group(3).replace("&", " "))
+        if len(seg) != b - a + 1:
+            raise SystemExit("%s(%d:%d): %d values" % (name, a, b, len(seg)))
+        vals[a - 1:b] = seg
+    if any(v is None for v in vals):
+        raise SystemExit("%s: %d of %d values" % (name, sum(v is not None for v in vals), count))
+    return vals
+
+
 def main(ref_root):
     ref = Path(ref_root)
     common = (ref / "src/clblm_src/clblm_ODLAY_CommonSub.f90").read_text(errors="replace")
@@ -160,6 +189,20 @@ def main(ref_root):
         emit("CLBLM_N2F_" + name.upper(),
              _data_block(cont, r"subroutine\s+n2_ver_1", r"DATA\s+%s\s*/(.*?)/" % name, 230))
     emit("CLBLM_N2O1_XN2", _data_block(cont, r"subroutine\s+n2_overtone1", r"DATA\s+xn2\s*/(.*?)/", 201))
+    # O3 continua: XO3CHP (:3061-5205), O3HHT0/1/2 (:5210-7085), O3HHUV (:7090-7175)
+    for name in ("X", "Y", "Z"):
+        emit("CLBLM_O3CHP_" + name, _data_segments(cont, r"SUBROUTINE\s+XO3CHP", name, 3150))
+    for sub in ("O3HHT0", "O3HHT1", "O3HHT2"):
+        emit("CLBLM_" + sub, _data_block(cont, r"SUBROUTINE\s+%s\b" % sub, r"DATA\s+S\(1:2687\)\s*/(.*?)/", 2687))
+    emit("CLBLM_O3HHUV", _data_block(cont, r"SUBROUTINE\s+O3HHUV", r"DATA\s+S\(1:133\)\s*/(.*?)/", 133))
+    # O2 continua: o2_ver_1 (:7180-7310), O2INF1 (:7327-7488), O2INF3 (:7573-7682),
+    # O2_vis (:7699-8090), O2FUV (:8257-8770)
+    emit("CLBLM_O2F_XO2", _data_block(cont, r"subroutine\s+o2_ver_1", r"DATA\s+xo2\(1:103\)\s*/(.*?)/", 103))
+    emit("CLBLM_O2F_XO2T", _data_block(cont, r"subroutine\s+o2_ver_1", r"DATA\s+xo2t\(1:103\)\s*/(.*?)/", 103))
+    emit("CLBLM_O2INF1", _data_block(cont, r"SUBROUTINE\s+O2INF1", r"DATA\s+xo2inf1\(1:483\)\s*/(.*?)/", 483))
+    emit("CLBLM_O2INF3", _data_block(cont, r"SUBROUTINE\s+O2INF3", r"DATA\s+xo2inf3\s*/(.*?)/", 261))
+    emit("CLBLM_O2VIS", _data_block(cont, r"SUBROUTINE\s+O2_vis", r"DATA\s+S\(1:1488\)\s*/(.*?)/", 1488))
+    emit("CLBLM_O2FUV", _data_block(cont, r"SUBROUTINE\s+O2FUV", r"DATA\s+S\(1:1512\)\s*/(.*?)/", 1512))
     lines.append("#endif")
     sys.stdout.write("\n".join(lines) + "\n")
 

@@ -675,15 +675,17 @@ struct ContGrid {
   double v1c, v2c, dvc;
   int nptc, i1;
 };
-__device__ __forceinline__ ContGrid cont_grid(const LayerPlan& P, double V1S, double DVS, int NPTS) {
+// (NPTS < 0: no cap; eps: O2FUV rounds its indices with 1e-5)
+__device__ __forceinline__ ContGrid cont_grid(const LayerPlan& P, double V1S, double DVS, int NPTS,
+                                              double eps = 0.01) {
   ContGrid g;
   g.dvc = DVS;
   double V1C = P.v1abs - DVS, V2C = P.v2abs + DVS;
-  g.i1 = (V1C < V1S) ? -1 : (int)((V1C - V1S) / DVS + 0.01);
+  g.i1 = (V1C < V1S) ? -1 : (int)((V1C - V1S) / DVS + eps);
   V1C = V1S + DVS * (double)(g.i1 - 1);
-  const int I2 = (int)((V2C - V1S) / DVS + 0.01);
+  const int I2 = (int)((V2C - V1S) / DVS + eps);
   g.nptc = I2 - g.i1 + 3;
-  if (g.nptc > NPTS) g.nptc = NPTS + 4;
+  if (NPTS >= 0 && g.nptc > NPTS) g.nptc = NPTS + 4;
   g.v1c = V1C;
   g.v2c = V1C + DVS * (double)(g.nptc - 1);
   return g;
@@ -693,14 +695,17 @@ __device__ __forceinline__ ContGrid cont_grid(const LayerPlan& P, double V1S, do
 // ABSRB point I (clblm_Spectrum.f90:874-915); *hit when I is in its range.
 // coef(J) gives C(J), J = 1..NPTC, and 0 outside (XINT's last stencil can
 // reach C(NPTC+1) with a zero weight).
+// (n1, n2: the ABSRB range pre_xint gives, clblm_Spectrum.f90:917-936;
+// 1..NPTABS otherwise)
 template <typename F>
-__device__ __forceinline__ double xint_at(const LayerPlan& P, int I, const ContGrid& g, F coef, bool* hit) {
+__device__ __forceinline__ double xint_at(const LayerPlan& P, int I, const ContGrid& g, F coef, bool* hit,
+                                          int n1 = 1, int n2 = INT_MAX) {
   *hit = false;
   const double RECDVA = 1. / g.dvc;
   int ILO = (int)((g.v1c + g.dvc - P.v1abs) / P.dvabs + 1. + kONEMI);
-  if (ILO < 1) ILO = 1;
+  if (ILO < n1) ILO = n1;
   int IHI = (int)((g.v2c - g.dvc - P.v1abs) / P.dvabs + kONEMI);
-  if (IHI > P.nptabs) IHI = P.nptabs;
+  if (IHI > min(P.nptabs, n2)) IHI = min(P.nptabs, n2);
   if (I < ILO || I > IHI) return 0.;
   *hit = true;
   const double VI = P.v1abs + P.dvabs * (double)(I - 1);
@@ -805,6 +810,277 @@ __device__ double n2_continuum(const LayerPlan& P, const ContIn& cont, int I, do
   return ab;
 }
 
+// pre_xint (clblm_Spectrum.f90:917-936): the ABSRB points [ist, last] of a
+// table that covers v1ss..v2ss
+__device__ __forceinline__ void pre_xint(const LayerPlan& P, double v1ss, double v2ss, int* ist, int* last) {
+  const int nb1 = (int)(2. + (v1ss - P.v1abs) / P.dvabs + 1.e-5);
+  *ist = max(1, nb1);
+  const int nb2 = (int)(1. + (v2ss - P.v1abs) / P.dvabs + 1.e-5);
+  *last = min(P.nptabs, nb2);
+}
+
+// The O3 continua of CONTNM at ABSRB point I, added after the CO2 block in
+// the reference's order (clblm_ODLAY_Continuum.f90:453-566): the Chappuis
+// band with its quadratic temperature dependence (XO3CHP :3061-5205), the
+// Hartley-Huggins band with its temperature coefficients (O3HHT0/1/2
+// :5210-7085), kept below 40800 cm-1 where the UV part (O3HHUV :7090-7175)
+// takes over -- the reference saves and restores ABSRB on either side, so
+// neither adds there.
+__device__ double o3_continuum(const LayerPlan& P, const ContIn& cont, int I, double ab) {
+  if (!(P.xo3cn > 0.) || !cont.o3) return ab;
+  const double XKT = P.tave / kRADCN2;
+  const double* CX = cont.o3;
+  const double *CY = CX + 3150, *CZ = CX + 6300;
+  const double* HT0 = CX + 9450;
+  const double *HT1 = HT0 + 2687, *HT2 = HT0 + 2 * 2687, *HUV = HT0 + 3 * 2687;
+  bool hit;
+  if (P.v2 > 8920.0 && P.v1 <= 24665.0) {  // Chappuis (diffuse ozone)
+    const ContGrid g = cont_grid(P, 8920.0, 5.0, 3150);
+    const double WO3 = P.wk[3] * 1.0E-20 * P.xo3cn;
+    const double DT = P.tave - 273.15;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      if (Ii < 1 || Ii > 3150) return 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = CX[Ii - 1] / VJ, c1 = CY[Ii - 1] / VJ, c2 = CZ[Ii - 1] / VJ;
+      double v = (c0 + (c1 + c2 * DT) * DT) * WO3;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 27370. && P.v1 < 40800.) {  // Hartley-Huggins
+    const ContGrid g = cont_grid(P, 27370., 5., 2687);
+    const double WO3 = P.wk[3] * 1.E-20 * P.xo3cn;
+    const double TC = P.tave - 273.15;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      double c0 = 0., ct1 = 0., ct2 = 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      if (Ii >= 1 && Ii <= 2687) {
+        c0 = HT0[Ii - 1] / VJ;
+        ct1 = HT1[Ii - 1];
+        ct2 = HT2[Ii - 1];
+      }
+      double v = c0 * WO3;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v * (1. + ct1 * TC + ct2 * TC * TC);
+    };
+    const double VJlast = g.v1c + g.dvc * (double)(g.nptc - 1);
+    bool keep = true;
+    if (VJlast > 40815. && P.v2 > 40800.) {
+      const int I_FIX = (int)((40800. - P.v1abs) / P.dvabs + 1.001);
+      keep = I < I_FIX;
+    }
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit && keep) ab = ab + d;
+  }
+  if (P.v2 > 40800. && P.v1 < 54000.) {  // UV Hartley-Huggins
+    const ContGrid g = cont_grid(P, 40800., 100., 133);
+    const double WO3 = P.wk[3] * P.xo3cn;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      if (Ii < 1 || Ii > 133) return 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      double v = (HUV[Ii - 1] / VJ) * WO3;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    bool keep = true;
+    if (P.v1 < 40800.) keep = I >= (int)((40800. - P.v1abs) / P.dvabs + 1.001);
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit && keep) ab = ab + d;
+  }
+  return ab;
+}
+
+// HERTDA and HERPRS (clblm_ODLAY_Continuum.f90:8164-8253): the Herzberg band
+// at V and its pressure term
+__device__ __forceinline__ double herzberg(double V, double T, double Pr) {
+  double HERZ = 0.0;
+  if (V > 36000.00) {
+    double CORR = 0.;
+    if (V <= 40000.) CORR = ((40000. - V) / 4000.) * 7.917E-27;
+    const double YRATIO = V / 48811.0;
+    const double L = log(YRATIO);
+    HERZ = 6.884E-04 * (YRATIO)*exp(-69.738 * (L * L)) - CORR;
+  }
+  const double PO = 1013., TO = 273.16;
+  return HERZ * (1. + .83 * (Pr / PO) * (TO / T));
+}
+
+// The O2 continua of CONTNM at ABSRB point I, in the reference's order after
+// the O3 blocks (clblm_ODLAY_Continuum.f90:568-803): the collision-induced
+// fundamental (o2_ver_1 :7180-7310), the 1.27 um band (O2INF1 :7327-7488),
+// the 1.06 um band (O2INF2 :7494-7560), the A band (O2INF3 :7573-7682, over
+// pre_xint's range), the visible (O2_vis :7699-8090), the Herzberg band
+// (O2HERZ :8095-8145) and the far UV (O2FUV :8257-8770, pre_xint's range).
+__device__ double o2_continuum(const LayerPlan& P, const ContIn& cont, int I, double ab) {
+  if (!(P.xo2cn > 0.) || !cont.o2) return ab;
+  const double P0 = 1013., T0 = 296., XLOSMT = 2.68675E+19;
+  const double XKT = P.tave / kRADCN2;
+  const double RHOAVE = (P.pave / P0) * (T0 / P.tave);
+  const double amagat = (P.pave / P0) * (273. / P.tave);
+  const double x_vmr_h2o = P.wk[1] / P.wtot, x_vmr_o2 = P.wk[7] / P.wtot;
+  const double x_vmr_n2 = 1. - x_vmr_h2o - x_vmr_o2;
+  const double* XO2 = cont.o2;
+  const double *XO2T = XO2 + 103, *INF1 = XO2 + 206, *INF3 = INF1 + 483, *VIS = INF3 + 261, *FUV = VIS + 1488;
+  bool hit;
+  if (P.v2 > 1340.0 && P.v1 < 1850.) {  // fundamental
+    const ContGrid g = cont_grid(P, 1340.000, 5.000, 103);
+    const double tau_fac = P.xo2cn * P.wk[7] * 1.e-20 * amagat;
+    const double xktfac = (1. / 296.) - (1. / P.tave);
+    const double factor = (1.e+20 / XLOSMT);
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 103) ? factor * XO2[Ii - 1] * exp(XO2T[Ii - 1] * xktfac) / VJ : 0.;
+      double v = tau_fac * c0;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 7536.0 && P.v1 < 8500.) {  // 1.27 um
+    const ContGrid g = cont_grid(P, 7536.000, 2.000, 483);
+    const double a_o2 = 1. / 0.446, a_n2 = 0.3 / 0.446, a_h2o = 1.;
+    const double tau_fac =
+        P.xo2cn * (P.wk[7] / XLOSMT) * amagat * (a_o2 * x_vmr_o2 + a_n2 * x_vmr_n2 + a_h2o * x_vmr_h2o);
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 483) ? INF1[Ii - 1] / VJ : 0.;
+      double v = tau_fac * c0;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 9100.0 && P.v1 < 11000.) {  // 1.06 um: two damped Lorentzians on their own grid
+    const double V1S = 9100., V2S = 11000., DVS = 2.;
+    ContGrid g;
+    g.dvc = DVS;
+    double V1C = P.v1abs - DVS, V2C = P.v2abs + DVS;
+    if (V1C < V1S) V1C = V1S - 2. * DVS;
+    if (V2C > V2S) V2C = V2S + 2. * DVS;
+    g.nptc = (int)((V2C - V1C) / DVS + 3.01);
+    g.v1c = V1C;
+    g.v2c = V1C + DVS * (double)(g.nptc - 1);
+    g.i1 = 1;
+    const double WO2 = P.xo2cn * (P.wk[7] * 1.e-20) * RHOAVE;
+    const double ADJWO2 = (P.wk[7] / P.wtot) * (1. / 0.209) * WO2;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      double c0 = 0.;
+      if (VJ > V1S && VJ < V2S) {
+        const double V1_osc = 9375., HW1 = 58.96, V2_osc = 9439., HW2 = 45.04, S1 = 1.166E-04, S2 = 3.086E-05;
+        const double DV1 = VJ - V1_osc, DV2 = VJ - V2_osc;
+        const double DAMP1 = DV1 < 0.0 ? exp(DV1 / 176.1) : 1.0;
+        const double DAMP2 = DV2 < 0.0 ? exp(DV2 / 176.1) : 1.0;
+        const double q1 = DV1 / HW1, q2 = DV2 / HW2;
+        const double O2INF =
+            0.31831 * (((S1 * DAMP1 / HW1) / (1. + q1 * q1)) + ((S2 * DAMP2 / HW2) / (1. + q2 * q2))) * 1.054;
+        c0 = O2INF / VJ;
+      }
+      double v = c0 * ADJWO2;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 12961.5 && P.v1 < 13221.5) {  // A band
+    const ContGrid g = cont_grid(P, 12961.5, 1.0, 261);
+    const double tau_fac = P.xo2cn * (P.wk[7] / XLOSMT) * amagat;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 261) ? INF3[Ii - 1] / VJ : 0.;
+      double v = tau_fac * c0;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    int ist, last;
+    pre_xint(P, 12961.5, 13221.5, &ist, &last);
+    const double d = xint_at(P, I, g, coef, &hit, ist, last);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 15000.0 && P.v1 < 29870.) {  // visible
+    const ContGrid g = cont_grid(P, 15000.0, 10.0, 1488);
+    const double WO2 = P.wk[7] * 1.e-20 * ((P.pave / 1013.) * (273. / P.tave)) * P.xo2cn;
+    const double ADJWO2 = (P.wk[7] / P.wtot) * WO2;
+    const double q = 55. * 273. / 296.;
+    const double factor = 1. / ((XLOSMT * 1.e-20 * (q * q)) * 89.5);
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 1488) ? factor * VIS[Ii - 1] / VJ : 0.;
+      double v = c0 * ADJWO2;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 36000.0) {  // Herzberg
+    const ContGrid g = cont_grid(P, 36000., 10., -1);
+    const double WO2 = P.wk[7] * 1.e-20 * P.xo2cn;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      if (Ii < 1) return 0.;
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      double v = (herzberg(VJ, P.tave, P.pave) / VJ) * WO2;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    const double d = xint_at(P, I, g, coef, &hit);
+    if (hit) ab = ab + d;
+  }
+  if (P.v2 > 56740.0) {  // far UV
+    const ContGrid g = cont_grid(P, 56740.0, 20.0, 1512, 1.e-5);
+    const double WO2 = P.wk[7] * 1.e-20 * P.xo2cn;
+    auto coef = [&](int J) -> double {
+      if (J < 1 || J > g.nptc) return 0.;
+      const int Ii = g.i1 + (J - 1);
+      const double VJ = g.v1c + g.dvc * (double)(J - 1);
+      const double c0 = (Ii >= 1 && Ii <= 1512) ? FUV[Ii - 1] / VJ : 0.;
+      double v = c0 * WO2;
+      if (P.jrad == 1) v = v * radfn_d(VJ, XKT);
+      return v;
+    };
+    int ist, last;
+    pre_xint(P, 56740.0, 86960.0, &ist, &last);
+    const double d = xint_at(P, I, g, coef, &hit, ist, last);
+    if (hit) ab = ab + d;
+  }
+  return ab;
+}
+
+// Rayleigh extinction of CONTNM (clblm_ODLAY_Continuum.f90:993-1060), IAERSL
+// = 0, at ABSRB point I: added after every continuum, on ABSRB's own grid.
+__device__ __forceinline__ double rayleigh(const LayerPlan& P, int I, double ab) {
+  if (!(P.v2 >= 820. && P.xrayl > 0.)) return ab;
+  const double conv_cm2mol = P.xrayl * 1.E-20 / (2.68675e-1 * 1.e5);
+  const double vrayleigh = P.v1abs + (double)(I - 1) * P.dvabs;
+  const double x = vrayleigh / 1.e4;
+  double ray_ext = (x * x * x / (9.38076E2 - 10.8426 * (x * x))) * (P.wtot * conv_cm2mol);
+  if (P.jrad == 1) ray_ext = ray_ext * x;
+  else if (P.jrad == 0) ray_ext = ray_ext / 1.e4;
+  return ab + ray_ext;
+}
+
 __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, ContIn cont, double* __restrict__ absrb_all) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
   double* ABSRB = absrb_all + P.abs_off;  // ABSRB[I], I = 1..N_ABSRB
@@ -815,13 +1091,16 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
   if (I > kNABSRB) return;
   if (!P.contnm) return;
   if (I > (int)((P.v2abs - P.v1abs) / P.dvabs + 1)) return;  // beyond NPTABS: nothing to add
-  // the H2O block adds to ABSRB first, then the CO2 block, then the N2
-  // blocks (XINT each)
+  // the H2O block adds to ABSRB first, then the CO2, O3, O2 and N2 blocks
+  // (XINT each), then the Rayleigh extinction
   double ab = h2o_continuum(P, cont, I);
   bool hit;
   const double co2 = co2_continuum(P, cont, I, &hit);
   if (hit) ab = ab + co2;
+  ab = o3_continuum(P, cont, I, ab);
+  ab = o2_continuum(P, cont, I, ab);
   ab = n2_continuum(P, cont, I, ab);
+  ab = rayleigh(P, I, ab);
   ABSRB[I] = ab;
 }
 

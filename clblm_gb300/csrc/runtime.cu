@@ -702,6 +702,9 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
     P.h2o_fac = P.wk[1] / lay->wtot;
     P.xco2c = c->xco2c;
     P.xn2cn = c->xn2cn;
+    P.xo3cn = c->xo3cn;
+    P.xo2cn = c->xo2cn;
+    P.xrayl = c->xrayl;
   }
   // returned spectrum: DVout interpolation, clblm_ODLAY.f90:571-604
   double outputDV = DV;
@@ -1483,7 +1486,8 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
         h->cont.ref_temp = cont->ref_temp;
         // the CO2 and N2 continua's tables (data of the reference's source)
         const size_t n_co2 = 5003 + 25 + 500, n_n2 = 4 * 73 + 3 * 230 + 201;
-        if (h->cont_co2.ensure(sizeof(double) * (n_co2 + n_n2))) {
+        const size_t n_o3 = 3 * 3150 + 3 * 2687 + 133, n_o2 = 2 * 103 + 483 + 261 + 1488 + 1512;
+        if (h->cont_co2.ensure(sizeof(double) * (n_co2 + n_n2 + n_o3 + n_o2))) {
           rc = CLBLM_ERR_OOM;
         } else {
           std::vector<double> t;
@@ -1500,6 +1504,19 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
           add(CLBLM_N2F_XN2_228, 230);
           add(CLBLM_N2F_A_H2O, 230);
           add(CLBLM_N2O1_XN2, 201);
+          add(CLBLM_O3CHP_X, 3150);
+          add(CLBLM_O3CHP_Y, 3150);
+          add(CLBLM_O3CHP_Z, 3150);
+          add(CLBLM_O3HHT0, 2687);
+          add(CLBLM_O3HHT1, 2687);
+          add(CLBLM_O3HHT2, 2687);
+          add(CLBLM_O3HHUV, 133);
+          add(CLBLM_O2F_XO2, 103);
+          add(CLBLM_O2F_XO2T, 103);
+          add(CLBLM_O2INF1, 483);
+          add(CLBLM_O2INF3, 261);
+          add(CLBLM_O2VIS, 1488);
+          add(CLBLM_O2FUV, 1512);
           double* d = h->cont_co2.as<double>();
           if (cudaMemcpy(d, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
             rc = set_err(h, CLBLM_ERR_CUDA, "continuum tables");
@@ -1510,6 +1527,8 @@ int clblm_gpu_create(const clblm_lines_t* lines, const clblm_cont_t* cont, int d
           h->cont.n2r = d + n_co2;
           h->cont.n2f = d + n_co2 + 4 * 73;
           h->cont.n2o1 = d + n_co2 + 4 * 73 + 3 * 230;
+          h->cont.o3 = d + n_co2 + n_n2;
+          h->cont.o2 = d + n_co2 + n_n2 + n_o3;
         }
         h->has_cont = true;
       }

@@ -135,6 +135,13 @@ typedef struct {
                         * (pure rotation, fundamental, first overtone: CONTNM
                         * clblm_ODLAY_Continuum.f90:805-990); the reference's
                         * default is 1, 0 leaves them out                      */
+  double  xo3cn;       /* XO3CN, scale of the O3 continua (Chappuis, Hartley-
+                        * Huggins, UV: :453-566); default 1, 0 leaves them out */
+  double  xo2cn;       /* XO2CN, scale of the O2 continua (fundamental, 1.27 um,
+                        * 1.06 um, A band, visible, Herzberg, far UV: :568-803);
+                        * default 1, 0 leaves them out                          */
+  double  xrayl;       /* XRAYL, scale of Rayleigh extinction (v2 >= 820 cm-1:
+                        * :993-1060); default 1, 0 leaves it out               */
 } clblm_od_ctrl_t;
 
 /* A layered column seen in nadir from the top of the atmosphere, with the

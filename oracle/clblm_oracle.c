@@ -617,6 +617,276 @@ static void cont_table_grid(double V1S, double DVS, int NPTS, double V1ABS, doub
   *I1 = i1;
 }
 
+/* ======================================================================
+ * O3 continua: the ozone blocks of CONTNM (clblm_ODLAY_Continuum.f90:
+ * 453-566), after the CO2 block: Chappuis (XO3CHP :3061-5205) with its
+ * quadratic temperature dependence, Hartley-Huggins (O3HHT0/1/2
+ * :5210-7085) and its UV part (O3HHUV :7090-7175), with the reference's
+ * save/restore of ABSRB (ABSBSV) on either side of 40800 cm-1.
+ * ====================================================================== */
+/* the grid of a table routine; eps: O2FUV rounds its indices with 1e-5;
+ * NPTS < 0: no cap (O2HERZ) */
+static void cont_table_grid_eps(double V1S, double DVS, int NPTS, double eps, double V1ABS, double V2ABS, double *V1C,
+                                double *V2C, int *NPTC, int *I1) {
+  const double DVC = DVS;
+  double v1c = V1ABS - DVC, v2c = V2ABS + DVC;
+  int i1 = (v1c < V1S) ? -1 : (int)((v1c - V1S) / DVS + eps);
+  v1c = V1S + DVS * (double)(i1 - 1);
+  int i2 = (int)((v2c - V1S) / DVS + eps);
+  int nptc = i2 - i1 + 3;
+  if (NPTS >= 0 && nptc > NPTS) nptc = NPTS + 4;
+  v2c = v1c + DVS * (double)(nptc - 1);
+  *V1C = v1c;
+  *V2C = v2c;
+  *NPTC = nptc;
+  *I1 = i1;
+}
+
+static void contnm_o3(int JRAD, double V1ABS, double V2ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/,
+                      double XO3CN, double V1, double V2, double TAVE, double WKO3) {
+  if (!(XO3CN > 0.)) return;
+  const double XKT = TAVE / RADCN2;
+  double V1C, V2C, VJ = 0.;
+  int NPTC, I1;
+  double *ABSBSV = (double *)calloc((size_t)NPTABS + 8, sizeof(double));
+  if (V2 > 8920.0 && V1 <= 24665.0) { /* Chappuis */
+    cont_table_grid_eps(8920.0, 5.0, 3150, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO3 = WKO3 * 1.0E-20 * XO3CN, DT = TAVE - 273.15;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      if (I < 1 || I > 3150) continue;
+      VJ = V1C + 5.0 * (double)(J - 1);
+      const double c0 = CLBLM_O3CHP_X[I - 1] / VJ, c1 = CLBLM_O3CHP_Y[I - 1] / VJ, c2 = CLBLM_O3CHP_Z[I - 1] / VJ;
+      C[J] = (c0 + (c1 + c2 * DT) * DT) * WO3;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, 5.0, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 27370. && V1 < 40800.) { /* Hartley-Huggins */
+    cont_table_grid_eps(27370., 5., 2687, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO3 = WKO3 * 1.E-20 * XO3CN, TC = TAVE - 273.15;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      double c0 = 0., ct1 = 0., ct2 = 0.;
+      VJ = V1C + 5. * (double)(J - 1);
+      if (I >= 1 && I <= 2687) {
+        c0 = CLBLM_O3HHT0[I - 1] / VJ;
+        ct1 = CLBLM_O3HHT1[I - 1];
+        ct2 = CLBLM_O3HHT2[I - 1];
+      }
+      C[J] = c0 * WO3;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+      C[J] = C[J] * (1. + ct1 * TC + ct2 * TC * TC);
+    }
+    int I_FIX = 0;
+    const int fix = VJ > 40815. && V2 > 40800;
+    if (fix) {
+      I_FIX = (int)((40800. - V1ABS) / DVABS + 1.001);
+      for (int I = I_FIX; I <= NPTABS; ++I) ABSBSV[I] = ABSRB[I];
+    }
+    xint(V1C, V2C, 5., C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    if (fix)
+      for (int I = I_FIX; I <= NPTABS; ++I) ABSRB[I] = ABSBSV[I];
+    free(C);
+  }
+  if (V2 > 40800. && V1 < 54000.) { /* UV */
+    cont_table_grid_eps(40800., 100., 133, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO3 = WKO3 * XO3CN;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      if (I < 1 || I > 133) continue;
+      VJ = V1C + 100. * (double)(J - 1);
+      C[J] = (CLBLM_O3HHUV[I - 1] / VJ) * WO3;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    int I_FIX = 0;
+    if (V1 < 40800) {
+      I_FIX = (int)((40800. - V1ABS) / DVABS + 1.001);
+      for (int I = 1; I <= I_FIX - 1; ++I) ABSBSV[I] = ABSRB[I];
+    }
+    xint(V1C, V2C, 100., C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    if (V1 < 40800)
+      for (int I = 1; I <= I_FIX - 1; ++I) ABSRB[I] = ABSBSV[I];
+    free(C);
+  }
+  free(ABSBSV);
+}
+
+/* ======================================================================
+ * O2 continua: the oxygen blocks of CONTNM (clblm_ODLAY_Continuum.f90:
+ * 568-803), after the O3 blocks: the collision-induced fundamental
+ * (o2_ver_1 :7180-7310), the 1.27 um band (O2INF1 :7327-7488), the 1.06 um
+ * band (O2INF2 :7494-7560), the A band (O2INF3 :7573-7682) and the far UV
+ * (O2FUV :8257-8770) over pre_xint's ranges (clblm_Spectrum.f90:917-936),
+ * the visible (O2_vis :7699-8090) and the Herzberg band (O2HERZ, HERTDA,
+ * HERPRS :8095-8253).
+ * ====================================================================== */
+static void pre_xint_range(double v1ss, double v2ss, double v1abs, double dvabs, int nptabs, int *ist, int *last) {
+  const int nb1 = (int)(2. + (v1ss - v1abs) / dvabs + 1.e-5);
+  *ist = nb1 > 1 ? nb1 : 1;
+  const int nb2 = (int)(1. + (v2ss - v1abs) / dvabs + 1.e-5);
+  *last = nb2 < nptabs ? nb2 : nptabs;
+}
+
+static void contnm_o2(int JRAD, double V1ABS, double V2ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/,
+                      double XO2CN, double V1, double V2, double PAVE, double TAVE, double WTOT, double WKH2O,
+                      double WKO2) {
+  if (!(XO2CN > 0.)) return;
+  const double P0 = 1013., T0 = 296., XLOSMT = 2.68675E+19;
+  const double XKT = TAVE / RADCN2;
+  const double RHOAVE = (PAVE / P0) * (T0 / TAVE);
+  const double amagat = (PAVE / P0) * (273. / TAVE);
+  const double x_vmr_h2o = WKH2O / WTOT, x_vmr_o2 = WKO2 / WTOT;
+  const double x_vmr_n2 = 1. - x_vmr_h2o - x_vmr_o2;
+  double V1C, V2C;
+  int NPTC, I1;
+  if (V2 > 1340.0 && V1 < 1850.) { /* fundamental */
+    cont_table_grid_eps(1340.000, 5.000, 103, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double tau_fac = XO2CN * WKO2 * 1.e-20 * amagat;
+    const double xktfac = (1. / 296.) - (1. / TAVE), factor = (1.e+20 / XLOSMT);
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      const double VJ = V1C + 5.000 * (double)(J - 1);
+      const double c0 =
+          (I >= 1 && I <= 103) ? factor * CLBLM_O2F_XO2[I - 1] * exp(CLBLM_O2F_XO2T[I - 1] * xktfac) / VJ : 0.;
+      C[J] = tau_fac * c0;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, 5.000, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 7536.0 && V1 < 8500.) { /* 1.27 um */
+    cont_table_grid_eps(7536.000, 2.000, 483, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double a_o2 = 1. / 0.446, a_n2 = 0.3 / 0.446, a_h2o = 1.;
+    const double tau_fac = XO2CN * (WKO2 / XLOSMT) * amagat * (a_o2 * x_vmr_o2 + a_n2 * x_vmr_n2 + a_h2o * x_vmr_h2o);
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      const double VJ = V1C + 2.000 * (double)(J - 1);
+      C[J] = tau_fac * ((I >= 1 && I <= 483) ? CLBLM_O2INF1[I - 1] / VJ : 0.);
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, 2.000, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 9100.0 && V1 < 11000.) { /* 1.06 um */
+    const double V1S = 9100., V2S = 11000., DVS = 2.;
+    V1C = V1ABS - DVS;
+    V2C = V2ABS + DVS;
+    if (V1C < V1S) V1C = V1S - 2. * DVS;
+    if (V2C > V2S) V2C = V2S + 2. * DVS;
+    NPTC = (int)((V2C - V1C) / DVS + 3.01);
+    V2C = V1C + DVS * (double)(NPTC - 1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO2 = XO2CN * (WKO2 * 1.e-20) * RHOAVE;
+    const double ADJWO2 = (WKO2 / WTOT) * (1. / 0.209) * WO2;
+    for (int J = 1; J <= NPTC; ++J) {
+      const double VJ = V1C + DVS * (double)(J - 1);
+      double c0 = 0.;
+      if (VJ > V1S && VJ < V2S) {
+        const double V1_osc = 9375., HW1 = 58.96, V2_osc = 9439., HW2 = 45.04, S1 = 1.166E-04, S2 = 3.086E-05;
+        const double DV1 = VJ - V1_osc, DV2 = VJ - V2_osc;
+        const double DAMP1 = DV1 < 0.0 ? exp(DV1 / 176.1) : 1.0;
+        const double DAMP2 = DV2 < 0.0 ? exp(DV2 / 176.1) : 1.0;
+        const double q1 = DV1 / HW1, q2 = DV2 / HW2;
+        c0 = 0.31831 * (((S1 * DAMP1 / HW1) / (1. + q1 * q1)) + ((S2 * DAMP2 / HW2) / (1. + q2 * q2))) * 1.054 / VJ;
+      }
+      C[J] = c0 * ADJWO2;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, DVS, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 12961.5 && V1 < 13221.5) { /* A band */
+    cont_table_grid_eps(12961.5, 1.0, 261, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double tau_fac = XO2CN * (WKO2 / XLOSMT) * amagat;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      const double VJ = V1C + 1.0 * (double)(J - 1);
+      C[J] = tau_fac * ((I >= 1 && I <= 261) ? CLBLM_O2INF3[I - 1] / VJ : 0.);
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    int ist, last;
+    pre_xint_range(12961.5, 13221.5, V1ABS, DVABS, NPTABS, &ist, &last);
+    xint(V1C, V2C, 1.0, C, 1.0, V1ABS, DVABS, ABSRB, ist, last);
+    free(C);
+  }
+  if (V2 > 15000.0 && V1 < 29870.) { /* visible */
+    cont_table_grid_eps(15000.0, 10.0, 1488, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO2 = WKO2 * 1.e-20 * ((PAVE / 1013.) * (273. / TAVE)) * XO2CN;
+    const double ADJWO2 = (WKO2 / WTOT) * WO2;
+    const double q = 55. * 273. / 296.;
+    const double factor = 1. / ((XLOSMT * 1.e-20 * (q * q)) * 89.5);
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      const double VJ = V1C + 10.0 * (double)(J - 1);
+      C[J] = ((I >= 1 && I <= 1488) ? factor * CLBLM_O2VIS[I - 1] / VJ : 0.) * ADJWO2;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, 10.0, C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 36000.0) { /* Herzberg */
+    cont_table_grid_eps(36000., 10., -1, 0.01, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO2 = WKO2 * 1.e-20 * XO2CN;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      if (I < 1) continue;
+      const double VJ = V1C + 10. * (double)(J - 1);
+      double HERZ = 0.0;
+      if (VJ > 36000.00) {
+        double CORR = 0.;
+        if (VJ <= 40000.) CORR = ((40000. - VJ) / 4000.) * 7.917E-27;
+        const double YRATIO = VJ / 48811.0, L = log(YRATIO);
+        HERZ = 6.884E-04 * (YRATIO)*exp(-69.738 * (L * L)) - CORR;
+      }
+      HERZ = HERZ * (1. + .83 * (PAVE / 1013.) * (273.16 / TAVE));
+      C[J] = (HERZ / VJ) * WO2;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    xint(V1C, V2C, 10., C, 1.0, V1ABS, DVABS, ABSRB, 1, NPTABS);
+    free(C);
+  }
+  if (V2 > 56740.0) { /* far UV */
+    cont_table_grid_eps(56740.0, 20.0, 1512, 1.e-5, V1ABS, V2ABS, &V1C, &V2C, &NPTC, &I1);
+    double *C = (double *)calloc((size_t)NPTC + 4, sizeof(double));
+    const double WO2 = WKO2 * 1.e-20 * XO2CN;
+    for (int J = 1; J <= NPTC; ++J) {
+      const int I = I1 + (J - 1);
+      const double VJ = V1C + 20.0 * (double)(J - 1);
+      C[J] = ((I >= 1 && I <= 1512) ? CLBLM_O2FUV[I - 1] / VJ : 0.) * WO2;
+      if (JRAD == 1) C[J] = C[J] * ocl_radfn(VJ, XKT);
+    }
+    int ist, last;
+    pre_xint_range(56740.0, 86960.0, V1ABS, DVABS, NPTABS, &ist, &last);
+    xint(V1C, V2C, 20.0, C, 1.0, V1ABS, DVABS, ABSRB, ist, last);
+    free(C);
+  }
+}
+
+/* Rayleigh extinction of CONTNM (clblm_ODLAY_Continuum.f90:993-1060), IAERSL = 0 */
+static void contnm_rayl(int JRAD, double V1ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/, double XRAYL,
+                        double V2, double WTOT) {
+  if (!(V2 >= 820. && XRAYL > 0.)) return;
+  const double conv_cm2mol = XRAYL * 1.E-20 / (2.68675e-1 * 1.e5);
+  for (int i = 1; i <= NPTABS; ++i) {
+    const double vrayleigh = V1ABS + (double)(i - 1) * DVABS;
+    const double x = vrayleigh / 1.e4;
+    double ray_ext = (x * x * x / (9.38076E2 - 10.8426 * (x * x))) * (WTOT * conv_cm2mol);
+    if (JRAD == 1) ray_ext = ray_ext * x;
+    else if (JRAD == 0) ray_ext = ray_ext / 1.e4;
+    ABSRB[i] = ABSRB[i] + ray_ext;
+  }
+}
+
 static void contnm_n2(int JRAD, double V1ABS, double V2ABS, double DVABS, int NPTABS, double *ABSRB /*1-based*/,
                       double XN2CN, double V1, double V2, double PAVE, double TAVE, double WTOT, double WKH2O,
                       double WKO2, int icflg) {
@@ -1814,8 +2084,12 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
       return rc;
     }
     contnm_co2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xco2c, V1, V2, PAVE, TAVE, M.WK[2]);
+    contnm_o3(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xo3cn, V1, V2, TAVE, M.WK[3]);
+    contnm_o2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xo2cn, V1, V2, PAVE, TAVE, lay->wtot, M.WK[1],
+              M.WK[7]);
     contnm_n2(JRAD, V1ABS, V2ABS, DVABS, NPTABS, ABSRBb, ctrl->xn2cn, V1, V2, PAVE, TAVE, lay->wtot, M.WK[1],
               M.WK[7], ctrl->jac_mol);
+    contnm_rayl(JRAD, V1ABS, DVABS, NPTABS, ABSRBb, ctrl->xrayl, V2, lay->wtot);
   }
   double ALFAV4 = 64. * g->sample * DV;
   double DVR4 = ALFAV4 / g->sample;
@@ -2826,6 +3100,16 @@ int ocl_contnm_co2(int jrad, double v1abs, double v2abs, double dvabs, int nptab
   for (int i = 0; i <= nptabs; ++i) absrb[i] = 0.;
   contnm_co2(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xco2c, v1, v2, pave, tave, wkco2);
   return CLBLM_OK;
+}
+
+int ocl_contnm_o3o2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xo3cn,
+                    double xo2cn, double xrayl, double v1, double v2, double pave, double tave, double wtot,
+                    double wkh2o, double wko3, double wko2) {
+  if (nptabs < 1 || nptabs > N_ABSRB - 4) return CLBLM_ERR_RANGE;
+  contnm_o3(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xo3cn, v1, v2, tave, wko3);
+  contnm_o2(jrad, v1abs, v2abs, dvabs, nptabs, absrb, xo2cn, v1, v2, pave, tave, wtot, wkh2o, wko2);
+  contnm_rayl(jrad, v1abs, dvabs, nptabs, absrb, xrayl, v2, wtot);
+  return 0;
 }
 
 int ocl_contnm_n2(int jrad, double v1abs, double v2abs, double dvabs, int nptabs, double *absrb, double xn2cn,

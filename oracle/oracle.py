@@ -76,6 +76,8 @@ def lib():
         L.ocl_jac_point.argtypes = [P(C.c_double)] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int] + [P(C.c_double)] * 7
         L.ocl_contnm_h2o.argtypes = [P(T.clblm_cont_t), C.c_int] + [C.c_double] * 8 + [P(C.c_double),
                                                                                     P(C.c_double), P(C.c_int)]
+        L.ocl_contnm_o3o2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
+            [C.c_double] * 11
         L.ocl_scanfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_int, C.c_double,
                                  C.c_double, C.c_double, C.c_double, P(P(C.c_double)), P(C.c_int64),
                                  P(C.c_double), P(C.c_double)]
@@ -332,3 +334,16 @@ def sf_table(jfn):
     xf = np.zeros(6020)
     lib().ocl_sf_table(jfn, _dp(xf))
     return xf
+
+
+def contnm_o3o2(jrad, v1abs, dvabs, nptabs, v1, v2, pave, tave, wtot, wkh2o, wko3, wko2, xo3cn=1.0, xo2cn=1.0,
+                xrayl=1.0):
+    """CONTNM's O3 and O2 blocks and the Rayleigh extinction on ABSRB
+    (1-based, v1abs + (i-1)*dvabs), alone."""
+    a = np.zeros(nptabs + 8)
+    v2abs = v1abs + dvabs * (nptabs - 1)
+    rc = lib().ocl_contnm_o3o2(jrad, v1abs, v2abs, dvabs, nptabs, _dp(a), xo3cn, xo2cn, xrayl, v1, v2, pave, tave,
+                               wtot, wkh2o, wko3, wko2)
+    if rc:
+        raise OracleError(rc, "contnm_o3o2")
+    return a

@@ -16,11 +16,12 @@ def _layer_case(n_lines, v1, v2, seed, mols=(1,), pave=1013.25, tave=296.0, wabs
     return lines, col
 
 
-def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision=T.CLBLM_PREC_MIXED, xn2cn=1.0):
+def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision=T.CLBLM_PREC_MIXED, xn2cn=1.0,
+             **scales):
     dn, df, _ = gpu_lib.setDV(col)
     lay = col.layer(0)
     g = T.grid_struct(col.v1, col.v2, dn[0], df[0])
-    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off, xn2cn=xn2cn)
+    ctrl = T.od_ctrl(precision=precision, contnm_off=contnm_off, xn2cn=xn2cn, **scales)
     h = gpu_lib.Handle(lines, cont)
     od, dv = h.odlay(lay, g, ctrl)
     st = h.stats()
@@ -93,6 +94,48 @@ def test_n2_continua(gpu_lib, oracle_mod, precision, tol, window):
         assert np.max(dref) > 0.0
         err = np.max(np.abs((od1 - od0) - dref)) / np.max(dref)
         assert err <= 1e-6, err
+
+
+def _o2_atmosphere():
+    """The broadband atmosphere's levels with H2O, CO2, O3 and O2 at 0.21."""
+    col = synth.atmosphere(100, 0.01, 10.0, 3500.0, mols=(1, 2, 3, 7))
+    col.w[:, 3] *= 0.21 / synth.OTHER_VMR
+    return col
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+@pytest.mark.parametrize("window,what", [
+    ((1400.0, 1500.0), "xo2cn"),      # O2 collision-induced fundamental
+    ((7600.0, 7700.0), "xo2cn"),      # O2 1.27 um
+    ((9300.0, 9400.0), "xo2cn"),      # O2 1.06 um (and the O3 Chappuis band)
+    ((13000.0, 13100.0), "xo2cn"),    # O2 A band, over pre_xint's range
+    ((20000.0, 20100.0), "xo3cn"),    # O3 Chappuis (and the O2 visible)
+    ((27300.0, 27450.0), "xo3cn"),    # O3 Hartley-Huggins from its first point
+    ((40700.0, 40900.0), "xo3cn"),    # Hartley-Huggins handing over to the UV at 40800 cm-1
+    ((38000.0, 38100.0), "xo2cn"),    # O2 Herzberg
+    ((57000.0, 57100.0), "xo2cn"),    # O2 far UV, over pre_xint's range
+    ((2500.0, 2600.0), "xrayl"),      # Rayleigh extinction
+])
+def test_o3_o2_rayleigh_continua(gpu_lib, oracle_mod, precision, tol, window, what):
+    """The O3 and O2 continua and Rayleigh extinction of CONTNM on a lower
+    layer of the broadband atmosphere with O2 at 0.21, in windows where each
+    band lives, against the oracle; on the FP64 path also that continuum
+    alone (scale 1 minus scale 0) against the oracle's, which pins it where
+    lines or other continua would hide it."""
+    lines, _, cont = synth.config4(n_lines=3000)
+    col = _o2_atmosphere().sub([2]).with_window(*window)
+    od1, ref1 = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0, precision=precision)
+    rel = np.max(np.abs(od1 - ref1) / np.abs(ref1))
+    assert rel <= tol, rel
+    if precision == T.CLBLM_PREC_PLAIN:  # the part alone: below the mixed path's FP32 noise at line centres
+        od0, ref0 = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=0, precision=precision,
+                             **{what: 0.0})
+        dref = ref1 - ref0
+        assert np.max(np.abs(dref)) > 0.0
+        # to 1e-6 of the part, or to binary64 rounding of the whole OD where
+        # the part is that small (Rayleigh: 3e-6 beside line centres of 1e7)
+        err = np.max(np.abs((od1 - od0) - dref))
+        assert err <= max(1e-6 * np.max(np.abs(dref)), 1e-13 * np.max(np.abs(ref1))), err
 
 
 def test_od_from_tape3_file_is_identical(gpu_lib, tmp_path):
