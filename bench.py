@@ -436,7 +436,12 @@ def batch_leg(cont, steps, per_call=16):
     res = {"workload": "256 profiles, 20-100 layers, windows 10-1000 cm-1 in 500-2500, radiance + dR/dT and "
                        "dR/dln q(H2O) of every level (clblm_gpu_batch, %d profiles per call, CUDA graphs)" % per_call,
            "profiles": len(cols), "points": int(sum(sum(ns) for ns in sizes)), "layer_points_per_step": int(lp),
-           "ms_per_step": ms, "value": lp / (ms * 1e-3), "unit": UNIT, "steps": steps}
+           "ms_per_step": ms, "value": lp / (ms * 1e-3), "unit": UNIT, "steps": steps,
+           # each layer's OD is formed four times on the Jacobian grid: the
+           # viewing path, T + 1 K, Wtot * 1.01 and the H2O-only layer
+           # (drv_LevelTemp, drv_LevelConc), besides the Jacobian recurrence
+           "od_layer_points_per_step": int(4 * lp), "od_value": 4 * lp / (ms * 1e-3),
+           "od_note": "layer OD points formed per second: 4 ODs per layer (viewing, T+1 K, Wtot*1.01, H2O alone)"}
     # agreement with FP64 on the first call's profiles (the calls share the
     # pool: the first call runs again before its radiances are kept)
     step(which=0)
