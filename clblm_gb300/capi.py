@@ -24,7 +24,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
            "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_scanfn_size", "clblm_gpu_scanfn",
-           "clblm_gpu_layer_amounts", "clblm_gpu_od_lines", "clblm_gpu_jac_vjp")
+           "clblm_gpu_layer_amounts", "clblm_gpu_od_lines", "clblm_gpu_jac_vjp", "clblm_gpu_filter")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -85,6 +85,8 @@ def lib():
                                             P(C.c_double), P(C.c_int64)]
         L.clblm_gpu_scanfn.argtypes = [C.c_void_p, P(T.clblm_scanfn_t), C.c_void_p, C.c_double, C.c_double, C.c_int64,
                                        C.c_void_p, C.c_int64, C.c_int32]
+        L.clblm_gpu_filter.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32,
+                                       P(C.c_double), P(C.c_double), P(C.c_int32), P(C.c_double), P(C.c_double)]
         L.clblm_gpu_layer_amounts.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [P(C.c_double)] * 4 + \
             [C.c_double] + [P(C.c_double)] * 5
         L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
@@ -456,3 +458,25 @@ def interp_spectrum_noalloc(d_in, nin, v1, dvin, d_out, nout, dvout, stream=0):
                                                  dvout, C.c_void_p(stream))
     if rc:
         raise ClblmError(rc, "clblm_gpu_interp_spectrum_noalloc")
+
+
+def _filter_method():
+    def filter(self, spect, v1, dv, channels):
+        """clblm_FLTRFN for every channel: `channels` is a list of (start_freq,
+        delta_freq, values); returns the channels' filtered values."""
+        spect = np.ascontiguousarray(spect, dtype=np.float64)
+        sf = np.array([c[0] for c in channels], dtype=np.float64)
+        df = np.array([c[1] for c in channels], dtype=np.float64)
+        ns = np.array([len(c[2]) for c in channels], dtype=np.int32)
+        vals = np.ascontiguousarray(np.concatenate([np.asarray(c[2], dtype=np.float64) for c in channels]))
+        out = np.zeros(len(channels))
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(lib().clblm_gpu_filter(self.h, spect.ctypes.data_as(C.c_void_p), v1, dv, len(spect),
+                                           len(channels), dp(sf), dp(df), ns.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           dp(vals), dp(out)))
+        return out
+
+    return filter
+
+
+Handle.filter = _filter_method()

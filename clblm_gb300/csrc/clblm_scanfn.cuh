@@ -93,4 +93,37 @@ cudaError_t sf_launch_interp(const SfPlan& p, const double* in, double* out, uns
 cudaError_t sf_launch(const SfPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
                       int* launches);
 
+// ---- spectral response functions: clblm_FLTRFN for every channel ----------
+constexpr int kFltMaxPoints = 3001;  // NFLTPT, clblm_ConstParam.f90:99
+
+// One panel of a channel's integral: CNVFLT's points IMIN..IMAX of the
+// panel whose S(1) is spectrum point g0, at V1I
+struct FltPanel {
+  int64_t g0;
+  double v1i;
+  int imin, imax;
+};
+struct FltChan {
+  int p0, np;         // its panels
+  int64_t xf_off;     // its filter values (endpoints halved) in the device table
+  int nptf;
+  double v1f, dvf, sumflt;  // V1F and DVF as the panel loop takes them; the filter's area
+};
+struct FltPlan {
+  std::vector<FltChan> ch;
+  std::vector<FltPanel> pan;
+  std::vector<double> xf;
+  double dvi = 0.;    // the spectrum's spacing (DVI = DVC)
+  size_t ws_bytes = 0, o_ch = 0, o_pan = 0, o_xf = 0, o_out = 0;
+};
+// The plan of FLTRFN's panel loop for every channel (host, the reference's
+// binary64 order).  Returns 0 or an error code with a message.
+int flt_plan(int nchan, const double* start_freq, const double* delta_freq, const int32_t* nsamp,
+             const double* filt, double v1, double dv, int64_t n, FltPlan* p, std::string* msg);
+// The channels' sums RFILTR of the device spectrum `in` into the device
+// array out[nchan] (workspace p.ws_bytes); the filter output is
+// (RFILTR * DVC) / SUMFLT.
+cudaError_t flt_launch(const FltPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
+                       int* launches);
+
 }  // namespace clblm

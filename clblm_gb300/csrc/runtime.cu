@@ -3835,6 +3835,35 @@ int clblm_gpu_scanfn(clblm_handle_t* h, const clblm_scanfn_t* sc, const double* 
 
 }  // extern "C"
 
+// ---- spectral response functions (clblm_FLTRFN) ------------------------------
+extern "C" int clblm_gpu_filter(clblm_handle_t* h, const double* spect, double v1, double dv, int64_t n,
+                                int32_t nchan, const double* start_freq, const double* delta_freq,
+                                const int32_t* nsamp, const double* filt, double* out) {
+  if (!h) return CLBLM_ERR_ARG;
+  if (!spect || !out) return set_err(h, CLBLM_ERR_ARG, "FLTRFN: null spectrum or output");
+  if (cudaSetDevice(h->device) != cudaSuccess) return set_err(h, CLBLM_ERR_CUDA, "cudaSetDevice");
+  FltPlan p;
+  std::string msg;
+  const int rc = flt_plan(nchan, start_freq, delta_freq, nsamp, filt, v1, dv, n, &p, &msg);
+  if (rc) return set_err(h, rc, "%s", msg.c_str());
+  h->reset_call();
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, h->sf_io.ensure(sizeof(double) * (size_t)n + 256));
+  CUDA_TRY(h, h->sf_ws.ensure(std::max<size_t>(p.ws_bytes, 256)));
+  double* din = h->sf_io.as<double>();
+  CUDA_TRY(h, cudaMemcpyAsync(din, spect, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+  double* dsum = reinterpret_cast<double*>(h->sf_ws.as<unsigned char>() + p.o_out);
+  int launches = 0;
+  CUDA_TRY(h, flt_launch(p, din, dsum, h->sf_ws.as<unsigned char>(), st, &launches));
+  h->launches += launches;
+  std::vector<double> rf(p.ch.size());
+  CUDA_TRY(h, cudaMemcpyAsync(rf.data(), dsum, sizeof(double) * rf.size(), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  for (size_t c = 0; c < rf.size(); ++c) out[c] = (rf[c] * dv) / p.ch[c].sumflt;  // (RFILTR*DVC)/SUMFLT
+  h->last.launches = h->launches;
+  return CLBLM_OK;
+}
+
 // ---- layer averages and amounts of a nadir path -------------------------------
 extern "C" int clblm_gpu_layer_amounts(clblm_handle_t* h, int32_t nlev, int32_t nmol, const double* z,
                                        const double* p, const double* t, const double* den, double earth_radius,

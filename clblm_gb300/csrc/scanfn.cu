@@ -953,4 +953,151 @@ cudaError_t sf_launch(const SfPlan& p, const double* in, double* out, unsigned c
 #undef SF_TRY
 }
 
+// ---------------------------------------------------------------------------
+// FLTRFN (clblm_ScanFilter.f90:1702-1897): per channel, the filter's
+// endpoints halved, its area SUMFLT, then panelInput from V1F to V2F and
+// CNVFLT (:1901-1969) on every panel.  The host forms the panels' V1I and
+// point ranges as the reference does; one CTA per channel adds the points'
+// terms and reduces them in a fixed order.
+int flt_plan(int nchan, const double* start_freq, const double* delta_freq, const int32_t* nsamp,
+             const double* filt, double v1, double dv, int64_t n, FltPlan* p, std::string* msg) {
+  *p = FltPlan();
+  if (nchan < 1 || !start_freq || !delta_freq || !nsamp || !filt || !(dv > 0.) || n < 1) {
+    *msg = "FLTRFN: bad channels or spectrum";
+    return CLBLM_ERR_ARG;
+  }
+  int64_t off = 0;
+  for (int c = 0; c < nchan; ++c) {
+    const int NPTF = nsamp[c];
+    if (NPTF < 1 || NPTF > kFltMaxPoints) {
+      *msg = "FLTRFN: NPTS > NFLTPT limit (or no filter values)";
+      return CLBLM_ERR_ARG;
+    }
+    double V1F = start_freq[c], DVF = delta_freq[c];
+    if (!std::isfinite(V1F) || !std::isfinite(DVF) || DVF == 0.) {
+      *msg = "FLTRFN: bad filter grid";
+      return CLBLM_ERR_ARG;
+    }
+    if (V1F < 0) {  // the reference returns without a value
+      *msg = "FLTRFN: a negative V1F leaves the reference's filter output unset";
+      return CLBLM_ERR_ARG;
+    }
+    if (DVF < 0.) {  // V1F is the centre
+      DVF = std::fabs(DVF);
+      if ((NPTF - 1) % 2 != 0) {
+        *msg = "FLTRFN: Use of V1F as center frequency requires odd number of points";
+        return CLBLM_ERR_ARG;
+      }
+      V1F = V1F - DVF * (double)((std::abs(NPTF) - 1) / 2);
+    }
+    const double V2F = V1F + DVF * (double)(NPTF - 1);
+    FltChan ch;
+    ch.xf_off = off;
+    ch.nptf = NPTF;
+    ch.v1f = V1F;
+    ch.dvf = DVF;
+    std::vector<double> XF(filt + off, filt + off + NPTF);
+    off += NPTF;
+    XF[0] = 0.5 * XF[0];
+    XF[NPTF - 1] = 0.5 * XF[NPTF - 1];
+    double SUMFLT = 0.0;
+    for (int i = 0; i < NPTF; ++i) SUMFLT = SUMFLT + XF[i];
+    SUMFLT = SUMFLT * DVF;
+    ch.sumflt = SUMFLT;
+    p->xf.insert(p->xf.end(), XF.begin(), XF.end());
+    ch.p0 = (int)p->pan.size();
+    SfReader rd{v1, dv, n};
+    rd.processed_v2 = v1 - dv;
+    for (;;) {
+      double V1I, V2I, DVI;
+      int NNI, IHI, IDATA;
+      int64_t g0;
+      if (!rd.read(0, V1F, V2F, &V1I, &V2I, &DVI, &NNI, &g0, &IHI, &IDATA)) break;
+      const int ILO = 1;
+      int IMIN = std::max((int)((V1F - V1I) / DVI + 1.0001), ILO);
+      int IMAX = std::min((int)((V2F + V1F - V1I) / DVI + 1.0001), IHI);
+      const double XIF0 = (V1I - V1F) / DVF + 1.0001, XDVIF = DVI / DVF;
+      if ((int)(XIF0 + XDVIF * (double)IMAX) + 1 > NPTF) {
+        for (int i = IMAX - 1; i >= IMIN; --i)
+          if ((int)(XIF0 + XDVIF * (double)i) + 1 <= NPTF) {
+            IMAX = i;
+            break;
+          }
+      }
+      if (IMAX >= IMIN && (int)(XIF0 + XDVIF * (double)IMAX) + 1 > NPTF) {
+        *msg = "CNVFLT: Subscript is greater than the upper bound of XF";
+        return CLBLM_ERR_RANGE;
+      }
+      p->pan.push_back(FltPanel{g0, V1I, IMIN, IMAX});
+      if (IDATA == 1) break;
+    }
+    ch.np = (int)p->pan.size() - ch.p0;
+    p->ch.push_back(ch);
+  }
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t r = o;
+    o += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  p->o_ch = take(sizeof(FltChan) * p->ch.size());
+  p->o_pan = take(sizeof(FltPanel) * std::max<size_t>(p->pan.size(), 1));
+  p->o_xf = take(sizeof(double) * p->xf.size());
+  p->o_out = take(sizeof(double) * p->ch.size());
+  p->ws_bytes = o;
+  p->dvi = dv;
+  return CLBLM_OK;
+}
+
+constexpr int kFltThreads = 256;
+
+__global__ void __launch_bounds__(kFltThreads) k_flt(const FltChan* __restrict__ chans,
+                                                    const FltPanel* __restrict__ pans,
+                                                    const double* __restrict__ xf_all, const double* __restrict__ sp,
+                                                    double dvi, double* __restrict__ out) {
+  const FltChan ch = chans[blockIdx.x];
+  const double* XF = xf_all + ch.xf_off - 1;  // XF(1..NPTF)
+  const double V1F = ch.v1f, DVF = ch.dvf;
+  const double XDVIF = __ddiv_rn(dvi, DVF);
+  double acc = 0.;
+  for (int q = 0; q < ch.np; ++q) {
+    const FltPanel pn = pans[ch.p0 + q];
+    const double XIF0 = __dadd_rn(__ddiv_rn(__dsub_rn(pn.v1i, V1F), DVF), 1.0001);
+    for (int I = pn.imin + (int)threadIdx.x; I <= pn.imax; I += blockDim.x) {
+      const int IFL = (int)__dadd_rn(XIF0, __dmul_rn(XDVIF, (double)I));
+      const double v2s = __dadd_rn(pn.v1i, __dmul_rn((double)I, dvi));
+      const double vxf1 = __dadd_rn(V1F, __dmul_rn((double)(IFL - 1), DVF));
+      const double vxf2 = __dadd_rn(V1F, __dmul_rn((double)IFL, DVF));
+      const double pw = __ddiv_rn(__dsub_rn(vxf2, v2s), __dsub_rn(vxf2, vxf1));
+      const double w = __dadd_rn(__dmul_rn(pw, XF[IFL]), __dmul_rn(__dsub_rn(1., pw), XF[IFL + 1]));
+      acc = __dadd_rn(acc, __dmul_rn(sp[pn.g0 + I - 1], w));
+    }
+  }
+  // fixed-order reduction: a call repeats bit for bit
+  __shared__ double red[kFltThreads];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int sN = kFltThreads / 2; sN > 0; sN >>= 1) {
+    if ((int)threadIdx.x < sN) red[threadIdx.x] = __dadd_rn(red[threadIdx.x], red[threadIdx.x + sN]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+cudaError_t flt_launch(const FltPlan& p, const double* in, double* out, unsigned char* ws, cudaStream_t st,
+                       int* launches) {
+  cudaError_t e;
+  FltChan* dch = reinterpret_cast<FltChan*>(ws + p.o_ch);
+  FltPanel* dpan = reinterpret_cast<FltPanel*>(ws + p.o_pan);
+  double* dxf = reinterpret_cast<double*>(ws + p.o_xf);
+  if ((e = cudaMemcpyAsync(dch, p.ch.data(), sizeof(FltChan) * p.ch.size(), cudaMemcpyHostToDevice, st))) return e;
+  if (!p.pan.empty() &&
+      (e = cudaMemcpyAsync(dpan, p.pan.data(), sizeof(FltPanel) * p.pan.size(), cudaMemcpyHostToDevice, st)))
+    return e;
+  if ((e = cudaMemcpyAsync(dxf, p.xf.data(), sizeof(double) * p.xf.size(), cudaMemcpyHostToDevice, st))) return e;
+  ++*launches;
+  k_flt<<<(unsigned)p.ch.size(), kFltThreads, 0, st>>>(dch, dpan, dxf, in, p.dvi, out);
+  return cudaGetLastError();
+}
+
 }  // namespace clblm

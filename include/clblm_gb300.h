@@ -503,6 +503,23 @@ int clblm_gpu_scanfn(clblm_handle_t *h, const clblm_scanfn_t *scan,
                      const double *spect, double v1, double dv, int64_t n,
                      double *out, int64_t cap, int32_t flags);
 
+/* ---- spectral response (filter) functions ---------------------------------
+ *
+ * clblm_FLTRFN (clblm_ScanFilter.f90:1702-1897, CNVFLT :1901-1969) for each
+ * channel of a sensor's filter functions, as postProc_filter applies them
+ * (clblm_PostProc.f90:289-336): the spectrum on v1 + i*dv (host buffer)
+ * integrated against channel c's nsamp[c] filter values filt[...] on
+ * start_freq[c] + j*delta_freq[c] (delta_freq < 0: start_freq is the centre
+ * of an odd count), the filter's end values halved, over the filter's area;
+ * out[c] on the host.  The channels' values follow one another in filt.
+ * Errors as the reference stops: more than 3001 values (NFLTPT), an even
+ * count about a centre, a filter point past its last value; a negative
+ * start_freq, for which the reference returns no value, is CLBLM_ERR_ARG. */
+int clblm_gpu_filter(clblm_handle_t *h, const double *spect, double v1, double dv,
+                     int64_t n, int32_t nchan, const double *start_freq,
+                     const double *delta_freq, const int32_t *nsamp,
+                     const double *filt, double *out);
+
 /* Lines of an LNFL line file (TAPE3) as read by RDLIN (clblm_ODLAY.f90:
  * 2645-2700) through CLBLM_LineData (clblm_LineData.f90:52-161): Fortran
  * unformatted records (4-byte length markers), the file header, the optional

@@ -78,6 +78,8 @@ def lib():
                                                                                     P(C.c_double), P(C.c_int)]
         L.ocl_contnm_o3o2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
             [C.c_double] * 11
+        L.ocl_fltrfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_double, C.c_double, C.c_int,
+                                 P(C.c_double), C.c_int, P(C.c_double)]
         L.ocl_scanfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_int, C.c_double,
                                  C.c_double, C.c_double, C.c_double, P(P(C.c_double)), P(C.c_int64),
                                  P(C.c_double), P(C.c_double)]
@@ -347,3 +349,14 @@ def contnm_o3o2(jrad, v1abs, dvabs, nptabs, v1, v2, pave, tave, wtot, wkh2o, wko
     if rc:
         raise OracleError(rc, "contnm_o3o2")
     return a
+
+
+def fltrfn(spect, v1, dv, v1f, dvf, xf, nfltpt=3001):
+    """clblm_FLTRFN (clblm_ScanFilter.f90:1702-1897) of one channel."""
+    sp = np.ascontiguousarray(spect, dtype=np.float64)
+    x = np.ascontiguousarray(xf, dtype=np.float64)
+    out = C.c_double()
+    rc = lib().ocl_fltrfn(_dp(sp), v1, dv, len(sp), v1f, dvf, len(x), _dp(x), nfltpt, C.byref(out))
+    if rc:
+        raise OracleError(rc, "FLTRFN")
+    return out.value

@@ -550,3 +550,74 @@ L60:
 }
 
 void ocl_free(void* p) { free(p); }
+
+/* clblm_FLTRFN (clblm_ScanFilter.f90:1702-1897) with CNVFLT (:1901-1969): the
+ * spectrum integrated against one filter function xf[0..nptf-1] on v1f +
+ * j*dvf (dvf < 0: v1f is the centre of an odd number of points), over the
+ * filter's area.  Returns 0, -1 (v1f < 0: the reference returns without a
+ * value), -2 (an even count about a centre, or more than nfltpt points,
+ * where the reference stops), -3 (a filter point beyond XF: its STOP). */
+int ocl_fltrfn(const double* sp, double v1, double dv, int64_t n, double v1f, double dvf, int nptf,
+               const double* xf_in, int nfltpt, double* out) {
+  SfSpec s = {sp, v1, dv, n};
+  if (nptf < 1 || nptf > nfltpt) return -2;
+  if (v1f < 0) return -1;
+  double DVF = dvf, V1F = v1f;
+  const int NPTF = nptf;
+  if (DVF < 0.) {
+    DVF = fabs(DVF);
+    if ((NPTF - 1) % 2 != 0) return -2;
+    const int half = (abs(NPTF) - 1) / 2;
+    V1F = v1f - DVF * (double)half;
+  }
+  double* XF = (double*)malloc(sizeof(double) * (size_t)(NPTF + 2));
+  for (int i = 1; i <= NPTF; ++i) XF[i] = xf_in[i - 1];
+  const double DVC = s.dv;
+  const double V2F = V1F + DVF * (double)(NPTF - 1);
+  XF[1] = 0.5 * XF[1];
+  XF[NPTF] = 0.5 * XF[NPTF];
+  double SUMFLT = 0.0;
+  for (int i = 1; i <= NPTF; ++i) SUMFLT = SUMFLT + XF[i];
+  SUMFLT = SUMFLT * DVF;
+  double RFILTR = 0.0;
+  SfIn st = {0, s.v1 - s.dv};
+  double* S = (double*)malloc(sizeof(double) * 4651);
+  int rc = 0;
+  for (;;) {
+    double V1I, V2I, DVI;
+    int NNI, ILO, IHI, IEOFSC, IDATA;
+    sf_panel_input(S, 0, &V1I, &V2I, &DVI, &NNI, V1F, V2F, &ILO, &IHI, &IEOFSC, &IDATA, &s, &st);
+    if (IEOFSC != 1) break;
+    /* CNVFLT */
+    int IMIN = (int)((V1F - V1I) / DVI + 1.0001);
+    if (IMIN < ILO) IMIN = ILO;
+    int IMAX = (int)((V2F + V1F - V1I) / DVI + 1.0001);
+    if (IMAX > IHI) IMAX = IHI;
+    const double XIF0 = (V1I - V1F) / DVF + 1.0001;
+    const double XDVIF = DVI / DVF;
+    if ((int)(XIF0 + XDVIF * (double)IMAX) + 1 > NPTF) {
+      for (int i = IMAX - 1; i >= IMIN; --i)
+        if ((int)(XIF0 + XDVIF * (double)i) + 1 <= NPTF) {
+          IMAX = i;
+          break;
+        }
+    }
+    if (IMAX >= IMIN && (int)(XIF0 + XDVIF * (double)IMAX) + 1 > NPTF) {
+      rc = -3;
+      break;
+    }
+    for (int I = IMIN; I <= IMAX; ++I) {
+      const int IFL = (int)(XIF0 + XDVIF * (double)I);
+      const double v2s = V1I + (double)I * DVI;
+      const double vxf1 = V1F + (double)(IFL - 1) * DVF, vxf2 = V1F + (double)IFL * DVF;
+      const double p = (vxf2 - v2s) / (vxf2 - vxf1);
+      RFILTR = RFILTR + S[I] * (p * XF[IFL] + (1. - p) * XF[IFL + 1]);
+    }
+    if (IDATA == 1) break;
+  }
+  free(S);
+  free(XF);
+  if (rc) return rc;
+  *out = (RFILTR * DVC) / SUMFLT;
+  return 0;
+}

@@ -77,3 +77,27 @@ def test_plan_grid_matches_oracle(oracle_mod):
                             assert (len(ref[0]), ref[1], ref[2]) == (got[2], got[0], got[1])
                         n_cases += 1
     assert n_cases == 540
+
+
+def test_filter_keeps_a_constant_and_a_line(oracle_mod):
+    """FLTRFN over a smooth filter keeps a constant and a straight line
+    through the filter's centre to 2e-5 (its trapezoid edges and the
+    reference's one-point shift of the spectrum's grid against the
+    filter's)."""
+    v1, dv, n = 900.0, 0.001, 200001
+    v = v1 + dv * np.arange(n)
+    g = np.exp(-np.linspace(-3, 3, 61) ** 2)
+    assert oracle_mod.fltrfn(np.full(n, 3.0), v1, dv, 1000.0, -0.1, g) == pytest.approx(3.0, rel=2e-5)
+    assert oracle_mod.fltrfn(1 + (v - 1000) / 100, v1, dv, 1000.0, -0.1, g) == pytest.approx(1.0, rel=2e-5)
+
+
+def test_filter_stops_where_the_reference_does(oracle_mod):
+    """A filter whose last point falls exactly on the first point of a
+    2400-point input panel leaves CNVFLT no point to keep in that panel: the
+    reference stops (subscript beyond XF); so do the oracle and the library."""
+    from clblm_gb300 import capi
+    v1, dv, n = 900.0, 0.001, 200001
+    with pytest.raises(oracle_mod.OracleError):
+        oracle_mod.fltrfn(np.full(n, 3.0), v1, dv, 950.0, 0.5, np.ones(21))
+    with pytest.raises(oracle_mod.OracleError):
+        oracle_mod.fltrfn(np.full(n, 3.0), v1, dv, 950.0, -0.5, np.ones(20))  # even count about a centre
