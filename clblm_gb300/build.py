@@ -26,6 +26,7 @@ UNITS = {
     "scan.cu": [],
     "scanfn.cu": [],
     "tape3.cpp": [],
+    "path.cpp": [],
     "runtime.cu": [],
 }
 

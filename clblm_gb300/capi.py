@@ -24,7 +24,7 @@ EXPORTS = ("clblm_gpu_create", "clblm_gpu_set_lines", "clblm_gpu_destroy", "clbl
            "clblm_gpu_rt_mode2_size", "clblm_gpu_rt_mode2", "clblm_gpu_jac_size", "clblm_gpu_jac",
            "clblm_tape3_read", "clblm_gpu_interp_spectrum_noalloc", "clblm_gpu_batch_size", "clblm_gpu_batch",
            "clblm_gpu_fftscn_size", "clblm_gpu_fftscn", "clblm_gpu_scanfn_size", "clblm_gpu_scanfn",
-           "clblm_gpu_layer_amounts", "clblm_gpu_od_lines", "clblm_gpu_jac_vjp", "clblm_gpu_filter")
+           "clblm_gpu_layer_amounts", "clblm_gpu_od_lines", "clblm_gpu_jac_vjp", "clblm_gpu_filter", "clblm_path")
 
 NOALLOC_MAX_POINTS = 1 << 20  # CLBLM_NOALLOC_MAX_POINTS
 
@@ -89,6 +89,7 @@ def lib():
                                        P(C.c_double), P(C.c_double), P(C.c_int32), P(C.c_double), P(C.c_double)]
         L.clblm_gpu_layer_amounts.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [P(C.c_double)] * 4 + \
             [C.c_double] + [P(C.c_double)] * 5
+        L.clblm_path.argtypes = [P(T.clblm_path_in_t), P(T.clblm_path_t), C.c_char_p, C.c_int32]
         L.clblm_tape3_read.argtypes = [C.c_char_p, C.c_double, C.c_double, P(T.clblm_lines_t), C.c_int64,
                                        P(C.c_int64), C.c_char_p, C.c_int32]
         L.clblm_gpu_interp_spectrum_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_double,
@@ -422,6 +423,45 @@ def read_tape3(path, v1=-1e30, v2=1e30):
     if rc:
         raise ClblmError(rc, err.value.decode())
     return lines
+
+
+def path(z, p, t, den, obs_alt, view_ang, z_rt=None, h2o=0, o2=-1, earth_radius=6371.23, v_refrac=1000.0,
+         zero_abs_amt=0, cap=None):
+    """calculatePath (clblm_AtmPath.f90:871-964): the layers of the line of
+    sight from an observer at obs_alt [km] at zenith angle view_ang [deg]
+    through the level profile (z [km], p [mb], t [K], den [nlev, nmol]
+    number densities), with the RT boundaries z_rt (default: the profile's
+    levels).  Returns (layers, geometry): layers holds the path's levels
+    (z, p, t, q [nlay+1, nmol]) and layers (pave, tave, wtot, w [nlay,
+    nmol], secant, ipath); geometry the standard form (hobs, hend, angle,
+    phi, hmin, len) and the traced ray's range, beta, bendng, phi_end.
+    Host code, no device needed."""
+    z, p, t = (np.ascontiguousarray(a, dtype=np.float64) for a in (z, p, t))
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    nlev, nmol = den.shape
+    zr = np.ascontiguousarray(z if z_rt is None else z_rt, dtype=np.float64)
+    cap = nlev + len(zr) + 4 if cap is None else int(cap)
+    o = dict(z=np.zeros(cap + 1), p=np.zeros(cap + 1), t=np.zeros(cap + 1), q=np.zeros((cap + 1) * max(nmol, 1)),
+             pave=np.zeros(cap), tave=np.zeros(cap), wtot=np.zeros(cap), w=np.zeros(cap * max(nmol, 1)),
+             secant=np.zeros(cap), ipath=np.zeros(cap, dtype=np.int32))
+    pin = T.clblm_path_in_t(nlev, nmol, _dp(z), _dp(p), _dp(t), _dp(den), h2o, o2, earth_radius, obs_alt, view_ang,
+                            v_refrac, len(zr), _dp(zr), zero_abs_amt)
+    pout = T.clblm_path_t()
+    pout.cap = cap
+    for k in ("z", "p", "t", "q", "pave", "tave", "wtot", "w", "secant"):
+        setattr(pout, k, _dp(o[k]))
+    pout.ipath = o["ipath"].ctypes.data_as(C.POINTER(C.c_int32))
+    err = C.create_string_buffer(512)
+    rc = lib().clblm_path(C.byref(pin), C.byref(pout), err, 512)
+    if rc:
+        raise ClblmError(rc, err.value.decode())
+    n = pout.nlay
+    layers = dict(z=o["z"][:n + 1], p=o["p"][:n + 1], t=o["t"][:n + 1], q=o["q"][:(n + 1) * nmol].reshape(n + 1, nmol),
+                  pave=o["pave"][:n], tave=o["tave"][:n], wtot=o["wtot"][:n], w=o["w"][:n * nmol].reshape(n, nmol),
+                  secant=o["secant"][:n], ipath=o["ipath"][:n])
+    geom = {k: getattr(pout, k) for k in ("hobs", "hend", "angle", "phi", "hmin", "len", "range", "beta", "bendng",
+                                          "phi_end")}
+    return layers, geom
 
 
 def setDV(col, sample=4.0, alfal0=0.04, alfal0_fine=0.005, grid_type=0, dv_user=-1.0):

@@ -102,6 +102,21 @@ def scanfn_struct(funct_id, hwhm, v1out, v2out, dvout=0.0):
     return clblm_scanfn_t(funct_id, 0, hwhm, v1out, v2out, dvout)
 
 
+class clblm_path_in_t(C.Structure):
+    _fields_ = [("nlev", C.c_int32), ("nmol", C.c_int32), ("z", C.POINTER(C.c_double)),
+                ("p", C.POINTER(C.c_double)), ("t", C.POINTER(C.c_double)), ("den", C.POINTER(C.c_double)),
+                ("h2o", C.c_int32), ("o2", C.c_int32), ("earth_radius", C.c_double), ("obs_alt", C.c_double),
+                ("view_ang", C.c_double), ("v_refrac", C.c_double), ("nrt", C.c_int32),
+                ("z_rt", C.POINTER(C.c_double)), ("zero_abs_amt", C.c_int32)]
+
+
+class clblm_path_t(C.Structure):
+    _fields_ = [("cap", C.c_int32), ("nlay", C.c_int32)] + \
+        [(f, C.POINTER(C.c_double)) for f in ("z", "p", "t", "q", "pave", "tave", "wtot", "w", "secant")] + \
+        [("ipath", C.POINTER(C.c_int32))] + [(f, C.c_double) for f in ("hobs", "hend", "angle", "phi", "hmin")] + \
+        [("len", C.c_int32)] + [(f, C.c_double) for f in ("range", "beta", "bendng", "phi_end")]
+
+
 class JacProfile:
     """Level pressures [mb] and Jacobian-molecule number densities [molec/cm3]
     (level 0 at the surface) and the clblm_jac_t view of them."""

@@ -422,6 +422,69 @@ int clblm_gpu_layer_amounts(clblm_handle_t *h, int32_t nlev, int32_t nmol,
                             double *pave, double *tave, double *wtot,
                             double *w, double *secant);
 
+/* ---- the line of sight: slant and refracted paths --------------------------
+ *
+ * calculatePath (clblm_AtmPath.f90:871-964) for an observer at obs_alt
+ * looking at zenith angle view_ang through a level profile: the refractive
+ * index of each level at v_refrac (refractiveIndex :977-1004), the path in
+ * standard form (standardPathGeometry :1010-1131: FSCGEO's case 2A with
+ * H2 at the bottom of the profile looking down and at its top looking up,
+ * retried towards the top when the ray cannot reach the bottom; FNDHMN's
+ * tangent height; REDUCE above the profile), the merge of the profile's
+ * levels with the RT boundaries z_rt and the path's ends (AMERGE, altitudes
+ * within 5e-4 km snapped together), the ray traced through every merged
+ * layer with refraction (RFPATH, ALAYER's steps of DELTAS = 5 km), and the
+ * merged layers packed into the RT layers (FPACK: density-weighted pressure
+ * and temperature, the air and absorber columns, the secant, IPATH; with
+ * zero_abs_amt = 1 absorbers above 99.9% of their column zeroed on an
+ * upward path and the path cut where all of them are).  Layers below a
+ * tangent point are traversed twice: IPATH 2, amounts of one traversal, as
+ * the reference keeps them.  The densities at the path's levels follow
+ * densityOnPathLevel (:1306-1355).  Host code in binary64 with the
+ * reference's order of operations; needs no device.
+ *
+ * Errors (message in errbuf): CLBLM_ERR_ARG for bad sizes or pointers, for
+ * a geometry FSCGEO rejects (the path above the profile, a downward path
+ * from the ground, an upward path from above its end, a ray meeting the
+ * ground) and where the reference STOPs (FNDHMN not converging, AMERGE's
+ * HMIN above the profile, equal pressures at adjacent path levels, FPACK's
+ * level count); CLBLM_ERR_CAPACITY when the layers do not fit cap. */
+typedef struct {
+  int32_t nlev, nmol;        /* profile levels (ascending altitude) and absorbers */
+  const double *z, *p, *t;   /* [nlev] km, mb, K */
+  const double *den;         /* [nlev*nmol] number densities [molec/cm3], level-major */
+  int32_t h2o, o2;           /* the columns of den that hold H2O and O2, or -1 */
+  double earth_radius;       /* km */
+  double obs_alt;            /* observer altitude [km] */
+  double view_ang;           /* zenith angle of the line of sight at the observer [deg] */
+  double v_refrac;           /* wavenumber of the refractive index [cm-1] */
+  int32_t nrt;               /* RT boundaries */
+  const double *z_rt;        /* [nrt] km, ascending */
+  int32_t zero_abs_amt;      /* zeroAbsAmt: 1 zeroes the last 0.1% of upward columns */
+} clblm_path_in_t;
+
+typedef struct {
+  int32_t cap;               /* in: layers the arrays below hold */
+  int32_t nlay;              /* out: layers of the path, bottom up */
+  double *z, *p, *t;         /* [cap+1] the path's levels (zRT, pRT, T) */
+  double *q;                 /* [(cap+1)*nmol] densities at them, or NULL */
+  double *pave, *tave;       /* [cap] mb, K */
+  double *wtot;              /* [cap] air column [molec/cm2] */
+  double *w;                 /* [cap*nmol] absorber columns [molec/cm2] */
+  double *secant;            /* [cap] path length over the layer's thickness */
+  int32_t *ipath;            /* [cap] 1 down, 2 below the tangent point, 3 up */
+  /* out: the path in standard form as the reference keeps it (Hobs, Hend,
+   * ANGLE, PHI, HMIN, LEN of CLBLM_PathGeom), and RFPATH's results: the
+   * path length, the earth-centred angle, the bending [deg] and the zenith
+   * angle at hend from the traced ray. */
+  double hobs, hend, angle, phi, hmin;
+  int32_t len;
+  double range, beta, bendng, phi_end;
+} clblm_path_t;
+
+int clblm_path(const clblm_path_in_t *in, clblm_path_t *out, char *errbuf,
+               int32_t errlen);
+
 /* ---- instrument-function scan ----------------------------------------------
  *
  * clblm_FFTSCN (clblm_FFT.f90:308-844): a spectrum on a uniform grid

@@ -78,6 +78,9 @@ def lib():
                                                                                     P(C.c_double), P(C.c_int)]
         L.ocl_contnm_o3o2.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)] + \
             [C.c_double] * 11
+        L.ocl_path_amounts.argtypes = [C.c_int, C.c_int] + [P(C.c_double)] * 4 + [C.c_int, C.c_int] + \
+            [C.c_double] * 4 + [C.c_int, P(C.c_double), C.c_int, C.c_int, P(C.c_int)] + [P(C.c_double)] * 9 + \
+            [P(C.c_int), P(C.c_double)]
         L.ocl_fltrfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_double, C.c_double, C.c_int,
                                  P(C.c_double), C.c_int, P(C.c_double)]
         L.ocl_scanfn.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, C.c_int, C.c_double,
@@ -360,3 +363,41 @@ def fltrfn(spect, v1, dv, v1f, dvf, xf, nfltpt=3001):
     if rc:
         raise OracleError(rc, "FLTRFN")
     return out.value
+
+
+PATH_ERRORS = {-1: "bad arguments", -2: "impossible geometry (FSCGEO)", -3: "AMERGE", -4: "equal pressures",
+               -5: "capacity", -6: "FPACK", -7: "zeroAbsAmt cut in the first layer"}
+
+
+def path_amounts(z, p, t, den, h_obs, view_ang, z_rt=None, h2o=0, o2=-1, re=6371.23, xvbar=1000.0,
+                 zero_abs_amt=0):
+    """calculatePath (clblm_AtmPath.f90:871-964) for an observer at h_obs
+    [km] looking at zenith angle view_ang [deg]: the output layers' dict
+    (zlev, plev, tlev, qlev [nlay+1, nmol], pave, tave, wtot, w [nlay,
+    nmol], secant, ipath) and the geometry (Hobs, Hend, ANGLE, PHI, HMIN,
+    LEN as standardPathGeometry leaves them; RFPATH's RANGE, BETA, BENDNG
+    and PHI_END)."""
+    z, p, t = (np.ascontiguousarray(a, dtype=np.float64) for a in (z, p, t))
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    nlev, nmol = den.shape
+    zr = np.ascontiguousarray(z if z_rt is None else z_rt, dtype=np.float64)
+    cap = nlev + len(zr) + 4
+    zl, pl, tl = np.zeros(cap + 1), np.zeros(cap + 1), np.zeros(cap + 1)
+    ql = np.zeros((cap + 1) * max(nmol, 1))
+    pave, tave, wtot, sec = np.zeros(cap), np.zeros(cap), np.zeros(cap), np.zeros(cap)
+    w = np.zeros(cap * max(nmol, 1))
+    ipath = np.zeros(cap, dtype=np.int32)
+    geom = np.zeros(10)
+    n = C.c_int()
+    rc = lib().ocl_path_amounts(nlev, nmol, _dp(z), _dp(p), _dp(t), _dp(den), h2o, o2, re, h_obs, view_ang, xvbar,
+                                len(zr), _dp(zr), zero_abs_amt, cap, C.byref(n), _dp(zl), _dp(pl), _dp(tl), _dp(ql),
+                                _dp(pave), _dp(tave), _dp(wtot), _dp(w), _dp(sec),
+                                ipath.ctypes.data_as(C.POINTER(C.c_int)), _dp(geom))
+    if rc:
+        raise OracleError(rc, "path: " + PATH_ERRORS.get(rc, "failed"))
+    k = n.value
+    out = dict(zlev=zl[:k + 1], plev=pl[:k + 1], tlev=tl[:k + 1], qlev=ql[:(k + 1) * nmol].reshape(k + 1, nmol),
+               pave=pave[:k], tave=tave[:k], wtot=wtot[:k], w=w[:k * nmol].reshape(k, nmol), secant=sec[:k],
+               ipath=ipath[:k])
+    names = ("Hobs", "Hend", "ANGLE", "PHI", "HMIN", "LEN", "RANGE", "BETA", "BENDNG", "PHI_END")
+    return out, dict(zip(names, geom))

@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 
 STRUCTS = ("clblm_lines_t", "clblm_cont_t", "clblm_layer_t", "clblm_grid_t", "clblm_od_ctrl_t", "clblm_column_t",
            "clblm_jac_t", "clblm_rt_ctrl_t", "clblm_od_stats_t", "clblm_profile_t", "clblm_scan_t",
-           "clblm_scanfn_t")
+           "clblm_scanfn_t", "clblm_path_in_t", "clblm_path_t")
 
 
 def _gcc():
