@@ -31,7 +31,17 @@ constexpr int kPanelR3 = kNLIM3 - 1;     // 150
 constexpr double kHWF1 = 4., kHWF2 = 16., kHWF3 = 64.;
 constexpr double kDXF1 = 0.002, kDXF2 = 0.008, kDXF3 = 0.032;
 constexpr int kLIMOUT4 = 2500;           // clblm_ODLAY_LineF4.f90:86
-constexpr int kTIPSNMOL = 9;
+constexpr int kMaxMol = 47;              // MXMOL: HITRAN molecules 1..47
+constexpr int kMaxIso = 10;              // isotopologues of a molecule at most
+
+// The constants of one isotopologue of a selected molecule in one layer
+// (MOLEC, clblm_ODLAY_CommonSub.f90:201-264): TIPS_2003's SCOR(m,iso), the
+// Doppler factor ALFD1(m,iso), and the molecule's self-density ratio RHOSLF
+// with RHORAT - RHOSLF; FP32 copies for the mixed path.
+struct IsoRow {
+  double scor, alfd1, rhoslf, rhodif;
+  float scor_f, alfd1_f, rhoslf_f, pad;
+};
 
 // Per-layer plan, filled on the host (exact FP64 restatement of the scalar
 // set-up of ODLAY_nonStruct, OPDPTH and HIRACQ) and read by the kernels.
@@ -75,11 +85,13 @@ struct LayerPlan {
   double xn2cn;                   // XN2CN: scale of the N2 continua (0: none)
   double xo3cn, xo2cn, xrayl;      // XO3CN, XO2CN, XRAYL: O3 and O2 continua, Rayleigh (0: none)
   int nptabs;
-  // molecules (index = HITRAN number, 0..kTIPSNMOL); sel=0: not selected
-  int sel[kTIPSNMOL + 1];
-  double wk[kTIPSNMOL + 1], scor[kTIPSNMOL + 1], rhoslf[kTIPSNMOL + 1], alfd1[kTIPSNMOL + 1];
-  double rhodif[kTIPSNMOL + 1];   // RHORAT - RHOSLF(m)
-  float scor_f[kTIPSNMOL + 1], rhoslf_f[kTIPSNMOL + 1], alfd1_f[kTIPSNMOL + 1];
+  // molecules (index = HITRAN number, 0..kMaxMol): the column amounts WK(m),
+  // and the row of isotopologue 1 of a selected molecule in this layer's
+  // IsoRow table at iso_off (isotopologue iso at mrow[m] + iso - 1); -1: the
+  // molecule is not selected
+  double wk[kMaxMol + 1];
+  int16_t mrow[kMaxMol + 1];
+  int64_t iso_off;
   // offsets of this layer's slices inside the shared per-call buffers
   int64_t vft_off;     // VFT of panel p at vft_off + p
   int64_t od_off;      // OD output

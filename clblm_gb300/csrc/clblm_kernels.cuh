@@ -85,8 +85,8 @@ extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], 
 // FP32 copies of CF1, CF2, CF3, CGAUSS, CER (mixed-path shape coefficients)
 extern __constant__ float c_SHAPEf[5][102];
 extern __constant__ float c_AVRATf[102];
-__global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const double* vft_all, LinePrep* out,
-                            int64_t out_stride, unsigned long long* stats);
+__global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const IsoRow* iso_tab,
+                            const double* vft_all, LinePrep* out, int64_t out_stride, unsigned long long* stats);
 __global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,
                                 int nblk_stride);
 __global__ void k_scan_blocks(int* blockmax, int nblk_stride, const int64_t* nlines, int nlayers);
@@ -99,8 +99,8 @@ __global__ void k_line_records(const LayerPlan* plans, int layer0, const double*
 __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
 __global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);
-__global__ void k_f4_prep(const LayerPlan* plans, int layer0, LineIn lines, F4Prep* out, int64_t stride,
-                          unsigned long long* stats);
+__global__ void k_f4_prep(const LayerPlan* plans, int layer0, LineIn lines, const IsoRow* iso_tab, F4Prep* out,
+                          int64_t stride, unsigned long long* stats);
 __global__ void k_f4_count(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0, int64_t* blocksum,
                            int nblk);
 __global__ void k_f4_blockscan(int64_t* blocksum, int nblk, const LayerPlan* plans, int layer0, int nlayers,

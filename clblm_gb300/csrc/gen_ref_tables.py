@@ -12,11 +12,14 @@ Tables extracted (reference file:line):
     (102 entries each over zeta = 0, 0.01, ..., 1.01):
     src/clblm_src/clblm_ODLAY_CommonSub.f90:43-185
   * TIPS temperature grid Tdat(119):  src/clblm_src/clblm_ODLAY_TIPS.f90:16-29
-  * TIPS Q(T) for isotopologue 1 of HITRAN molecules 1-9 (H2O, CO2, O3, N2O,
-    CO, CH4, O2, NO, SO2): the ``QofT( 1,J)`` DATA blocks of QT_H2O ... QT_SO2,
-    src/clblm_src/clblm_ODLAY_TIPS.f90:424-2254
-  * isotopologue-1 molecular masses of molecules 1-9:
-    src/common/clblm_ConstParam.f90:263-290
+  * TIPS Q(T): every ``QofT(k,J)`` DATA row of the 45 QT_* routines
+    (src/clblm_src/clblm_ODLAY_TIPS.f90:421-5442), and for each HITRAN
+    molecule 1-47 and isotopologue the row TIPS_2003's dispatch (:57-419)
+    reads: the isotopologue's own, the first isotopologue's where the
+    dispatch falls back to it (HNO3, HF, HCl, HBr, HI, N2, COF2), none where
+    it sets Q = 1 (O, CH3OH, SO3)
+  * the number of isotopologues of each molecule (MaxISOTPL_smass) and their
+    molecular masses (isotpl_mass): src/common/clblm_ConstParam.f90:246-420
   * CO2 continuum (mt_ckd 2.5): FRNCO2's coefficients S(1:5003) on -4 to
     10000 cm-1 at 2 cm-1 and its band-head temperature exponents
     TDEP_BANDHEAD(1196:1220), src/clblm_src/clblm_ODLAY_Continuum.f90:1333-2511;
@@ -74,27 +77,64 @@ def _tips_grid(src):
     return vals
 
 
-def _tips_iso1(src, mol):
-    start = re.search(r"Subroutine\s+QT_%s\b" % mol, src, re.I)
-    if not start:
-        raise SystemExit("QT_%s not found" % mol)
-    rest = src[start.end():]
-    m = re.search(r"data\s*\(QofT\(\s*1,J\),J=1,119\)\s*/(.*?)/", rest, re.S | re.I)
-    body = "\n".join(line.split("!")[0] for line in m.group(1).splitlines())
-    vals = _numbers(body.replace("&", " "))
-    if len(vals) != 119:
-        raise SystemExit("QT_%s iso1: %d values" % (mol, len(vals)))
+def _tips_all(src, maxiso):
+    """(rows, rowmap): the Q(T) rows of all QT_* routines in file order, and
+    rowmap[mol-1][iso-1] = the row TIPS_2003 interpolates for (mol, iso);
+    -1 where it takes Q = 1."""
+    subs = [(m.group(1), m.start()) for m in re.finditer(r"Subroutine\s+QT_(\w+)\s*\(", src, re.I)]
+    rows, first = [], {}
+    for k, (name, pos) in enumerate(subs):
+        body = src[pos:subs[k + 1][1] if k + 1 < len(subs) else len(src)]
+        nrow = int(re.search(r"dimension\s+xgj\(\s*(\d+)\)", body, re.I).group(1))
+        first[name.upper()] = (len(rows), nrow)
+        for j in range(1, nrow + 1):
+            m = re.search(r"data\s*\(QofT\(\s*%d\s*,\s*J\)\s*,\s*J=1,119\)\s*/(.*?)/" % j, body, re.S | re.I)
+            text = "\n".join(line.split("!")[0] for line in m.group(1).splitlines())
+            vals = _numbers(text.replace("&", " "))
+            if len(vals) != 119:
+                raise SystemExit("QT_%s row %d: %d values" % (name, j, len(vals)))
+            rows.append(vals)
+    disp = src[src.index("Subroutine TIPS_2003"):subs[0][1]]
+    rowmap = []
+    for mol in range(1, 48):
+        blk = re.search(r"IF\s*\(\s*MOL\s*\.EQ\.\s*%d\s*\)\s*THEN(.*?)go to 100" % mol, disp, re.I | re.S)
+        call = re.search(r"CALL\s+QT_(\w+)\s*\(", blk.group(1), re.I)
+        if not call:
+            if not re.search(r"QT\s*=\s*1", blk.group(1), re.I):
+                raise SystemExit("molecule %d: no TIPS routine and no Q = 1" % mol)
+            rowmap.append([-1] * maxiso[mol - 1])
+            continue
+        base, nrow = first[call.group(1).upper()]
+        own = nrow
+        g = re.search(r"IF\s*\(\s*ISO\.EQ\.1\s*(\.OR\.\s*ISO\s*\.EQ\.\s*2)?\s*\)", blk.group(1), re.I)
+        if g:
+            own = 2 if g.group(1) else 1
+        elif maxiso[mol - 1] > nrow:
+            raise SystemExit("molecule %d: %d isotopologues, %d TIPS rows" % (mol, maxiso[mol - 1], nrow))
+        rowmap.append([base + (iso - 1 if iso <= own else 0) for iso in range(1, maxiso[mol - 1] + 1)])
+    return rows, rowmap
+
+
+def _maxiso(src):
+    m = re.search(r"MaxISOTPL_smass\(MXMOL\)\s*=\s*\[(.*?)\]", src, re.S)
+    text = "\n".join(line.split("!")[0] for line in m.group(1).splitlines())
+    vals = [int(v) for v in re.findall(r"\d+", text.replace("&", " "))]
+    if len(vals) != 47:
+        raise SystemExit("MaxISOTPL_smass: %d values" % len(vals))
     return vals
 
 
-def _masses(src):
+def _masses_all(src, maxiso):
     out = []
-    for m_id in range(1, 10):
-        m = re.search(r"data\s*\(isotpl_mass\(%d,i\),i=1,\d+\)\s*&?\s*&?\s*/\s*(%s)" % (m_id, NUM),
-                      src, re.S | re.I)
+    for m_id in range(1, 48):
+        m = re.search(r"data\s*\(isotpl_mass\(%d,i\),i=1,(\d+)\)\s*&?\s*&?\s*/(.*?)/" % m_id, src, re.S | re.I)
         if not m:
-            raise SystemExit("mass of molecule %d not found" % m_id)
-        out.append(m.group(1))
+            raise SystemExit("masses of molecule %d not found" % m_id)
+        text = "\n".join(line.split("!")[0] for line in m.group(2).splitlines())
+        vals = _numbers(text.replace("&", " "))
+        if len(vals) != int(m.group(1)) or len(vals) < maxiso[m_id - 1]:
+            raise SystemExit("masses of molecule %d: %d values" % (m_id, len(vals)))
+        out.append(vals[:maxiso[m_id - 1]])
     return out
 
 
@@ -161,20 +201,37 @@ def main(ref_root):
         emit("CLBLM_" + name, _fortran_array(common, name))
     # clblm_ODLAY_TIPS.f90:16-29
     emit("CLBLM_TIPS_TDAT", _tips_grid(tips), per=8)
-    mols = ("H2O", "CO2", "O3", "N2O", "CO", "CH4", "O2", "NO", "SO2")
-    lines.append("/* TIPS Q(T) of isotopologue 1, HITRAN molecules 1..9 (%s) */" % ", ".join(mols))
-    lines.append("#define CLBLM_TIPS_NMOL 9")
-    lines.append("static const double CLBLM_TIPS_Q_ISO1[9][119] = {")
-    for mol in mols:
-        vals = _tips_iso1(tips, mol)
-        lines.append("  { /* %s */" % mol)
+    # MaxISOTPL_smass and isotpl_mass, clblm_ConstParam.f90:246-420
+    maxiso = _maxiso(const)
+    lines.append("#define CLBLM_MXMOL 47   /* MXMOL */")
+    lines.append("#define CLBLM_MXISO 10   /* isotopologues of a molecule at most */")
+    lines.append("static const int CLBLM_MAXISO[47] = {")
+    lines.append("    " + ", ".join(str(v) for v in maxiso) + ",")
+    lines.append("};")
+    lines.append("")
+    lines.append("/* molecular mass of (molecule, isotopologue); 0: no such isotopologue */")
+    lines.append("static const double CLBLM_ISO_MASS[47][10] = {")
+    for vals in _masses_all(const, maxiso):
+        lines.append("    {" + ", ".join(vals + ["0."] * (10 - len(vals))) + "},")
+    lines.append("};")
+    lines.append("")
+    rows, rowmap = _tips_all(tips, maxiso)
+    lines.append("/* TIPS Q(T) rows of the QT_* routines, in file order */")
+    lines.append("#define CLBLM_TIPS_NQ %d" % len(rows))
+    lines.append("static const double CLBLM_TIPS_Q[%d][119] = {" % len(rows))
+    for vals in rows:
+        lines.append("  {")
         for i in range(0, len(vals), 6):
             lines.append("    " + ", ".join(vals[i:i + 6]) + ",")
         lines.append("  },")
     lines.append("};")
     lines.append("")
-    # clblm_ConstParam.f90:263-290
-    emit("CLBLM_ISO1_MASS", _masses(const), per=9)
+    lines.append("/* the row of CLBLM_TIPS_Q for (molecule, isotopologue); -1: Q = 1; -2: no such isotopologue */")
+    lines.append("static const int CLBLM_TIPS_QROW[47][10] = {")
+    for r in rowmap:
+        lines.append("    {" + ", ".join(str(v) for v in r + [-2] * (10 - len(r))) + "},")
+    lines.append("};")
+    lines.append("")
     # clblm_ODLAY_Continuum.f90: FRNCO2 (:1333-2511) and CONTNM's XFACCO2 (:145-204)
     cont = (ref / "src/clblm_src/clblm_ODLAY_Continuum.f90").read_text(errors="replace")
     emit("CLBLM_CO2_S", _data_block(cont, r"SUBROUTINE\s+FRNCO2", r"DATA\s+S\(1:5003\)\s*/(.*?)/", 5003))

@@ -25,8 +25,10 @@ namespace clblm {
 __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], c_CF3[102], c_CER[102];
 __constant__ float c_SHAPEf[5][102];
 __constant__ float c_AVRATf[102];
-// MaxISOTPL_smass, clblm_ConstParam.f90:246-251 (molecules 1..9)
-__constant__ int c_MAXISO[10] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2};
+// MaxISOTPL_smass, clblm_ConstParam.f90:246-251 (index: HITRAN molecule 0..47)
+__constant__ int c_MAXISO[kMaxMol + 1] = {0, 6, 10, 9, 5, 6, 4, 3, 3, 2, 1, 2, 2, 3, 2, 4, 4, 2,
+                                          2,  5, 3, 2, 2, 3, 2, 1, 3, 2, 1, 2, 1, 3, 1, 1,
+                                          1,  2, 1, 2, 2, 1, 2, 1, 1, 1, 1, 2, 4, 1};
 
 __device__ __forceinline__ double radfn_d(double VI, double XKT) {
   // RADFN, clblm_ODLAY_CommonSub.f90:293-323
@@ -84,8 +86,8 @@ __device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rd
 }
 
 __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
-                            const double* __restrict__ vft_all, LinePrep* __restrict__ out,
-                            int64_t out_stride, unsigned long long* __restrict__ stats) {
+                            const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
+                            LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
   int64_t n = P.line_hi - P.line_lo + 1;
   LinePrep* o = out + (int64_t)blockIdx.y * out_stride;
@@ -107,9 +109,9 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     int m = molf % 100;
     int iso = (molf % 1000) / 100;
     if (iso == 0) iso = 10;
-    bool ok = iflg >= 0 && m >= 1 && m <= kTIPSNMOL && P.sel[m];
+    bool ok = iflg >= 0 && m >= 1 && m <= kMaxMol && P.mrow[m] >= 0;
     if (ok && iso > c_MAXISO[m]) ok = false;
-    if (ok && (iso != 1 || iflg == 1 || iflg == 3)) {
+    if (ok && (iflg == 1 || iflg == 3)) {
       bad++;
       ok = false;
     }
@@ -120,15 +122,18 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     }
     if (ok) {
       nlin++;
+      const IsoRow& R = iso_tab[P.iso_off + P.mrow[m] + iso - 1];
       double alfa0 = (double)lines.alfa[i];
       double hwhms = (double)lines.hwhm[i];
+      // air-broadened widths of O2 and N2 to foreign widths (RDLIN :2728-2745)
       if (m == 7) alfa0 = (alfa0 - 0.21 * hwhms) / (1.0 - 0.21);
+      if (m == 22) alfa0 = (alfa0 - 0.79 * hwhms) / (1.0 - 0.79);
       double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
       double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
-      double ALFL = ALFA0I * P.rhodif[m] + HWHMSI * P.rhoslf[m];  // RHODIF = RHORAT - RHOSLF
-      double ALFAD = VNU * P.alfd1[m];
+      double ALFL = ALFA0I * R.rhodif + HWHMSI * R.rhoslf;  // RHODIF = RHORAT - RHOSLF
+      double ALFAD = VNU * R.alfd1;
       double ZETA = ALFL / (ALFL + ALFAD);
       double FZETA = 100. * ZETA;
       int IZ = (int)(FZETA + kONEPL);
@@ -164,7 +169,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             if (P.jrad == 1) sui *= radfn_f((float)lines.vnu[i], P.xkt_f);
             const float EPP = EPP0 <= P.epp_abs_f ? fabsf(EPP0) : EPP0;
             if (EPP > P.epp_neg_f)
-              sui = sui * P.scor_f[m] * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
+              sui = sui * R.scor_f * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
             SUI = sui;
             SP = SUI;  // SUI*(1 + 0*PAVP2)
             // SPEAK = SUI/ALFV > 0 unless SUI = 0 (SUI >= 1e-45, 1/ALFV > 1:
@@ -176,7 +181,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             double EPP = (double)EPP0;
             if (EPP <= -1.001) EPP = fabs(EPP);
             if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
-            if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
+            if (EPP > -0.999) SUI = SUI * R.scor * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
             SP = SUI * P.spfac;
             if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
               double SPEAK = SUI * RECALF;
@@ -1105,8 +1110,9 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
 }
 
 // ---- far-wing lines: LINF4Q per-line corrections --------------------------
-__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines, F4Prep* __restrict__ out,
-                          int64_t stride, unsigned long long* __restrict__ stats) {
+__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+                          const IsoRow* __restrict__ iso_tab, F4Prep* __restrict__ out, int64_t stride,
+                          unsigned long long* __restrict__ stats) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
   int64_t n = P.f4_hi - P.f4_lo;
   F4Prep* o = out + (int64_t)blockIdx.y * stride;
@@ -1123,15 +1129,16 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
     int m = molf % 100;
     int iso = (molf % 1000) / 100;
     if (iso == 0) iso = 10;
-    bool ok = iflg >= 0 && m >= 1 && m <= kTIPSNMOL && P.sel[m];
+    bool ok = iflg >= 0 && m >= 1 && m <= kMaxMol && P.mrow[m] >= 0;
     if (ok && iso > c_MAXISO[m]) ok = false;
-    if (ok && (iso != 1 || iflg == 1 || iflg == 3)) {
+    if (ok && (iflg == 1 || iflg == 3)) {
       bad++;
       ok = false;
     }
     if (ok) {
       double SUI = (double)lines.sp[i] * P.wk[m];
       if (SUI != 0. && !(lines.vnu[i] < P.v1l4)) {
+        const IsoRow& R = iso_tab[P.iso_off + P.mrow[m] + iso - 1];
         const float alfa_in = lines.alfa[i], hwhm_in = lines.hwhm[i];
         const double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
         const float EPP0 = lines.epp[i];
@@ -1142,27 +1149,29 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           if (VNU == 0.) sui = 2.f * sui;
           const float EPP = EPP0 <= P.epp_abs_f ? fabsf(EPP0) : EPP0;
           const float vf = (float)VNU;
-          if (EPP > P.epp_neg_f) sui = sui * P.scor_f[m] * __expf(-EPP * P.betacr4_f) * (1.f + __expf(-vf * P.beta_f));
+          if (EPP > P.epp_neg_f) sui = sui * R.scor_f * __expf(-EPP * P.betacr4_f) * (1.f + __expf(-vf * P.beta_f));
           float alfa = alfa_in;
           if (m == 7) alfa = (float)(((double)alfa_in - 0.21 * (double)hwhm_in) / (1.0 - 0.21));
+          if (m == 22) alfa = (float)(((double)alfa_in - 0.79 * (double)hwhm_in) / (1.0 - 0.79));
           const float TMPCOR = __expf(lines.tmpalf[i] * P.ln_tratio_f);  // (T/296)^n
-          const float rs = P.rhoslf_f[m];
+          const float rs = R.rhoslf_f;
           r.w.f[0] = (alfa * TMPCOR) * (P.rhorat_f - rs) + (hwhm_in * TMPCOR) * rs;
-          r.w.f[1] = vf * P.alfd1_f[m];
+          r.w.f[1] = vf * R.alfd1_f;
           r.w.f[2] = sui;
           r.sp = (double)sui;  // SP = SUI*(1 + 0*PAVP2) = SUI
         } else {
           double alfa = (double)alfa_in, hwhm = (double)hwhm_in;
           if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
+          if (m == 22) alfa = (alfa - 0.79 * hwhm) / (1.0 - 0.79);
           double EPP = (double)EPP0;
           if (VNU == 0.) SUI = 2. * SUI;
           if (EPP <= -1.001) EPP = fabs(EPP);
-          if (EPP > -0.999) SUI = SUI * P.scor[m] * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
+          if (EPP > -0.999) SUI = SUI * R.scor * exp(-EPP * P.betacr4) * (1. + exp(-VNU * P.beta));
           double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
           double ALFA0I = alfa * TMPCOR;
           double HWHMSI = hwhm * TMPCOR;
-          r.w.d[0] = ALFA0I * (P.rhorat - P.rhoslf[m]) + HWHMSI * P.rhoslf[m];
-          r.w.d[1] = VNU * P.alfd1[m];
+          r.w.d[0] = ALFA0I * (P.rhorat - R.rhoslf) + HWHMSI * R.rhoslf;
+          r.w.d[1] = VNU * R.alfd1;
           r.sp = SUI * P.spfac;
         }
         r.vnu = VNU;

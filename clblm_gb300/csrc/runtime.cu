@@ -106,6 +106,7 @@ struct clblm_handle {
   int jrad = 0;
   // workspace
   DevBuf plans, vft, prep, qpanel, rec, recd, ranges, od, r4, absrb, stats, alfvmax, blockmax, nlines_d;
+  DevBuf isotab;  // isotopologue rows of the planned layers
   DevBuf f4prep, f4sh, f4nout, f4rec, f4recd, f4nrec, f4nmir, f4pm, f4sm, err;
   DevBuf pblk, bv1, bn, bm0, bfac;
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
@@ -131,7 +132,7 @@ struct clblm_handle {
                               &f4nmir,    &f4pm,     &f4sm,      &err,     &outbuf,  &pblk,   &bv1,     &bn,
                               &bm0,       &bfac,     &f4blk,     &f4ntot,  &f4cidx,  &f4vb,   &f4lb,    &f4src,
                               &f4flag,    &f4cut,    &f4grp,     &f4nxt,   &ragg,    &segpool, &gpm,    &gsm,
-                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk,    &jvjp};
+                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk,    &jvjp,   &isotab};
     for (auto& b : rt) v.push_back(&b);
     for (auto& b : imap) v.push_back(&b);
     v.push_back(&rtseg);
@@ -419,6 +420,7 @@ struct HostPlan {
   std::vector<double> blk_v1;       // block origins V1R4
   std::vector<int> blk_n;           // NPTR4 of each block
   std::vector<int64_t> blk_m0;      // origin on the global far-wing grid
+  std::vector<IsoRow> iso;          // isotopologue rows of the selected molecules
   double dv_out;    // DV of the returned spectrum
   int64_t n_out;    // points of the returned spectrum
 };
@@ -586,25 +588,38 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   if (JRAD != 1) P.dptmn = c->dptmin / radfn_h(V2, lay->tave / kRADCN2);
   P.dptfc = c->dptfac;
   // molecules: MOLEC clblm_ODLAY_CommonSub.f90:201-264 with TIPS_2003
+  // (clblm_ODLAY_TIPS.f90:57-419) for every isotopologue of each molecule
   const double FLN2 = std::log(2.);
   const double FAD = FLN2 * 2. * kAVOGAD * kBOLTZ / (kCLIGHT * kCLIGHT);
+  for (int m = 0; m <= kMaxMol; ++m) P.mrow[m] = -1;
+  hp->iso.clear();
   for (int i = 0; i < lay->nmol; ++i) {
     int m = lay->mol_id[i];
-    if (m < 1 || m > kTIPSNMOL)
-      return set_err(h, CLBLM_ERR_UNSUPPORTED, "molecule %d: the partition-sum tables carry molecules 1-9", m);
+    if (m < 1 || m > kMaxMol) return set_err(h, CLBLM_ERR_ARG, "molecule %d: HITRAN molecules are 1-47", m);
+    if (P.mrow[m] >= 0) return set_err(h, CLBLM_ERR_ARG, "molecule %d selected twice", m);
     if (!(lay->tave >= 70. && lay->tave <= 3000.))
       return set_err(h, CLBLM_ERR_RANGE, "TIPS: temperature %.3f K outside 70-3000 K", lay->tave);
-    P.sel[m] = 1;
     P.wk[m] = lay->w[i];
-    double q296 = tips_interp(296., CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[m - 1], 119);
-    double qt = tips_interp(lay->tave, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[m - 1], 119);
-    P.scor[m] = q296 / qt;
-    P.rhoslf[m] = P.rhorat * P.wk[m] / lay->wtot;
-    P.alfd1[m] = std::sqrt(FAD * lay->tave / CLBLM_ISO1_MASS[m - 1]);
-    P.rhodif[m] = P.rhorat - P.rhoslf[m];
-    P.scor_f[m] = (float)P.scor[m];
-    P.rhoslf_f[m] = (float)P.rhoslf[m];
-    P.alfd1_f[m] = (float)P.alfd1[m];
+    P.mrow[m] = (int16_t)hp->iso.size();
+    const double rhoslf = P.rhorat * P.wk[m] / lay->wtot;
+    for (int iso = 1; iso <= CLBLM_MAXISO[m - 1]; ++iso) {
+      IsoRow r{};
+      const int row = CLBLM_TIPS_QROW[m - 1][iso - 1];
+      if (row < 0) {
+        r.scor = 1.0;  // Q = 1 at both temperatures (O, CH3OH, SO3)
+      } else {
+        double q296 = tips_interp(296., CLBLM_TIPS_TDAT, CLBLM_TIPS_Q[row], 119);
+        double qt = tips_interp(lay->tave, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q[row], 119);
+        r.scor = q296 / qt;
+      }
+      r.alfd1 = std::sqrt(FAD * lay->tave / CLBLM_ISO_MASS[m - 1][iso - 1]);
+      r.rhoslf = rhoslf;
+      r.rhodif = P.rhorat - rhoslf;
+      r.scor_f = (float)r.scor;
+      r.alfd1_f = (float)r.alfd1;
+      r.rhoslf_f = (float)r.rhoslf;
+      hp->iso.push_back(r);
+    }
   }
   // panels: VFT advanced by 2400 DV until VFT + (NHI-1) DV > V2 (panelOut)
   hp->vft.clear();
@@ -915,7 +930,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   // far wings
   h->launches++;
   k_f4_prep<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
-      dplans, first, li, h->f4prep.as<F4Prep>(), f4stride, h->stats.as<unsigned long long>());
+      dplans, first, li, h->isotab.as<const IsoRow>(), h->f4prep.as<F4Prep>(), f4stride,
+      h->stats.as<unsigned long long>());
   {
     // LINF4Q record loop + SHRINQ: count, compact, walk, group sums
     int nblk4 = (int)((f4stride + 1 + 1023) / 1024);
@@ -1004,7 +1020,8 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   // line centres
   h->launches++;
   k_line_prep<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
-      dplans, first, li, h->vft.as<double>(), h->prep.as<LinePrep>(), lstride, h->stats.as<unsigned long long>());
+      dplans, first, li, h->isotab.as<const IsoRow>(), h->vft.as<double>(), h->prep.as<LinePrep>(), lstride,
+      h->stats.as<unsigned long long>());
   int nblk = (int)((lstride + 1023) / 1024);
   h->launches++;
   k_scan_blockmax<<<dim3(nblk, count), 256, 0, st>>>(h->prep.as<LinePrep>(), lstride, h->nlines_d.as<int64_t>() + first,
@@ -1190,7 +1207,8 @@ WsDims batch_dims(std::vector<HostPlan>& hps, int first, int count, int64_t* lst
 
 // Buffers of one OD batch (sized by d) and of all nL planned layers: the
 // first error, or success.
-cudaError_t ws_alloc(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
+cudaError_t ws_alloc(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, int64_t isot,
+                     bool plain) {
   const size_t real = plain ? 8 : 4;
   cudaError_t e = cudaSuccess;
 #define WS_ENSURE(x)                       \
@@ -1198,6 +1216,7 @@ cudaError_t ws_alloc(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
     if ((e = (x)) != cudaSuccess) return e; \
   } while (0)
   WS_ENSURE(h->plans.ensure(sizeof(LayerPlan) * nL));
+  WS_ENSURE(h->isotab.ensure(sizeof(IsoRow) * (size_t)std::max<int64_t>(isot, 1)));
   WS_ENSURE(h->vft.ensure(sizeof(double) * vftt));
   WS_ENSURE(h->prep.ensure(sizeof(LinePrep) * d.lsc));
   WS_ENSURE(h->qpanel.ensure(sizeof(int) * d.lsc));
@@ -1254,7 +1273,7 @@ std::vector<DevBuf*> ws_buffers(clblm_handle* h) {
           &h->blockmax, &h->nlines_d, &h->f4prep, &h->f4sh, &h->f4nout, &h->f4blk, &h->f4ntot, &h->f4cidx,
           &h->f4vb,   &h->f4lb,   &h->f4src,  &h->f4flag,   &h->f4nxt,  &h->f4cut,  &h->f4grp,  &h->f4rec,
           &h->f4recd, &h->f4nrec, &h->f4nmir, &h->f4pm,     &h->f4sm,   &h->err,    &h->segpool, &h->pblk,
-          &h->bv1,    &h->bn,     &h->bm0,    &h->bfac};
+          &h->bv1,    &h->bn,     &h->bm0,    &h->bfac,   &h->isotab};
 }
 
 // Frees every work buffer of the handle (all but the line list, the shape
@@ -1268,12 +1287,13 @@ void release_work(clblm_handle* h) {
 // ws_alloc; when the device is out of memory (buffers a previous call grew
 // for another shape hold it), the batch buffers are freed and allocated
 // afresh once.
-int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, bool plain) {
-  cudaError_t e = ws_alloc(h, d, nL, vftt, blkt, plain);
+int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int64_t blkt, int64_t isot,
+                     bool plain) {
+  cudaError_t e = ws_alloc(h, d, nL, vftt, blkt, isot, plain);
   if (e == cudaErrorMemoryAllocation) {
     cudaGetLastError();
     for (DevBuf* b : ws_buffers(h)) b->release();
-    e = ws_alloc(h, d, nL, vftt, blkt, plain);
+    e = ws_alloc(h, d, nL, vftt, blkt, isot, plain);
   }
   if (e != cudaSuccess)
     return set_err(h, e == cudaErrorMemoryAllocation ? CLBLM_ERR_OOM : CLBLM_ERR_CUDA, "OD workspace: %s",
@@ -1281,22 +1301,26 @@ int ensure_workspace(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
   return CLBLM_OK;
 }
 
-// Offsets of every planned layer's panel and far-wing block tables.
-void table_offsets(std::vector<HostPlan>& hps, int64_t* vftt, int64_t* blkt) {
-  int64_t v = 0, b = 0;
+// Offsets of every planned layer's panel, far-wing block and isotopologue
+// tables.
+void table_offsets(std::vector<HostPlan>& hps, int64_t* vftt, int64_t* blkt, int64_t* isot) {
+  int64_t v = 0, b = 0, r = 0;
   for (auto& hp : hps) {
     hp.P.vft_off = v;
     v += pad256((int64_t)hp.vft.size());
     hp.P.blk_off = b;
     b += hp.blk_v1.size();
+    hp.P.iso_off = r;
+    r += hp.iso.size();
   }
   *vftt = v;
   *blkt = b;
+  *isot = r;
 }
 
 // Uploads the plans and tables of all layers (after the offsets are set);
 // zeroes the counters and error flags.
-int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int64_t blkt) {
+int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int64_t blkt, int64_t isot) {
   const int nL = (int)hps.size();
   std::vector<int> pb(vftt, 0), bn(blkt + 1, 0);
   std::vector<double> bv(blkt + 1, 0.);
@@ -1304,8 +1328,10 @@ int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int6
   std::vector<LayerPlan> plans(nL);
   std::vector<double> vft(vftt, 0.);
   std::vector<int64_t> nl(nL, 0);
+  std::vector<IsoRow> iso(std::max<int64_t>(isot, 1));
   for (int k = 0; k < nL; ++k) {
     const HostPlan& hp = hps[k];
+    std::copy(hp.iso.begin(), hp.iso.end(), iso.begin() + hp.P.iso_off);
     std::copy(hp.panel_blk.begin(), hp.panel_blk.end(), pb.begin() + hp.P.vft_off);
     std::copy(hp.blk_v1.begin(), hp.blk_v1.end(), bv.begin() + hp.P.blk_off);
     std::copy(hp.blk_n.begin(), hp.blk_n.end(), bn.begin() + hp.P.blk_off);
@@ -1320,6 +1346,7 @@ int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int6
   CUDA_TRY(h, cudaMemcpyAsync(h->bn.p, bn.data(), sizeof(int) * (blkt + 1), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->bm0.p, bm.data(), sizeof(int64_t) * (blkt + 1), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->plans.p, plans.data(), sizeof(LayerPlan) * nL, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(h->isotab.p, iso.data(), sizeof(IsoRow) * iso.size(), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->vft.p, vft.data(), sizeof(double) * vftt, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(h->nlines_d.p, nl.data(), sizeof(int64_t) * nL, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemsetAsync(h->stats.p, 0, sizeof(unsigned long long) * kStatsPerLayer * nL, st));
@@ -1333,11 +1360,11 @@ int upload_plans(clblm_handle* h, std::vector<HostPlan>& hps, int64_t vftt, int6
 int prepare_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int count, bool plain, int64_t* lstride,
                   int64_t* f4stride, int64_t* pstride, int64_t* od_total) {
   const WsDims d = batch_dims(hps, first, count, lstride, f4stride, pstride);
-  int64_t vftt, blkt;
-  table_offsets(hps, &vftt, &blkt);
-  int rc = ensure_workspace(h, d, (int)hps.size(), vftt, blkt, plain);
+  int64_t vftt, blkt, isot;
+  table_offsets(hps, &vftt, &blkt, &isot);
+  int rc = ensure_workspace(h, d, (int)hps.size(), vftt, blkt, isot, plain);
   if (rc) return rc;
-  rc = upload_plans(h, hps, vftt, blkt);
+  rc = upload_plans(h, hps, vftt, blkt, isot);
   if (rc) return rc;
   *od_total = d.odt;
   return CLBLM_OK;
@@ -2911,7 +2938,7 @@ struct BatchPlan {
   int jr_after = 0;
   bool fp_after = false;
   int64_t jod_max = 0, map_max = 0;  // per wave (elements)
-  int64_t vftt = 0, blkt = 0;        // panel / far-wing block table sizes
+  int64_t vftt = 0, blkt = 0, isot = 0;  // panel / far-wing block / isotopologue table sizes
   std::vector<JacJob> jobs;          // device job table (addresses of the slabs and maps)
 };
 
@@ -2933,7 +2960,7 @@ constexpr size_t kBatchGraphs = 16;
 // table, interpolation blocks and profile arrays; zeroes the counters.
 int batch_upload(clblm_handle* h, BatchPlan& bp) {
   if (!bp.hps.empty()) {
-    int rc = upload_plans(h, bp.hps, bp.vftt, bp.blkt);
+    int rc = upload_plans(h, bp.hps, bp.vftt, bp.blkt, bp.isot);
     if (rc) return rc;
   }
   if (!bp.jobs.empty())
@@ -3278,7 +3305,7 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
     return first_bad;
   }
   // workspace: the largest chunk, every job's plan, the waves' slabs
-  table_offsets(bp.hps, &bp.vftt, &bp.blkt);
+  table_offsets(bp.hps, &bp.vftt, &bp.blkt, &bp.isot);
   WsDims dmax;
   for (BChunk& c : bp.chunks) dmax.max_with(batch_dims(bp.hps, c.first, c.count, &c.ls, &c.fs, &c.ps));
   const int njob = (int)bp.hps.size();
@@ -3293,7 +3320,7 @@ int clblm_gpu_batch(clblm_handle_t* h, clblm_profile_t* prof, int32_t n, const c
   // previous call grew for another shape hold it), all of the handle's work
   // buffers are freed and the batch's allocated afresh once
   auto alloc = [&]() -> cudaError_t {
-    cudaError_t e = ws_alloc(h, dmax, njob, bp.vftt, bp.blkt, plain);
+    cudaError_t e = ws_alloc(h, dmax, njob, bp.vftt, bp.blkt, bp.isot, plain);
     if (e == cudaSuccess) e = h->jod.ensure(real * (size_t)std::max<int64_t>(bp.jod_max, 1));
     if (e == cudaSuccess) e = h->jmap.ensure(sizeof(int2) * (size_t)std::max<int64_t>(bp.map_max, 1));
     if (e == cudaSuccess) e = h->jjobs.ensure(sizeof(JacJob) * (size_t)std::max(njob, 1));

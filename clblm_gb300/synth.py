@@ -33,9 +33,17 @@ AIR_COLUMN_PER_HPA = 100.0 / (9.80665 * 28.964e-3 / 6.02214199e23) / 1.0e4  # mo
 SECANT_DIFFUSE = 1.67  # clblm_ConstParam.f90:124
 
 
-def line_list(n, v1, v2, seed, mols=(1,)):
+# isotopologues of each HITRAN molecule 1..47 (MaxISOTPL_smass, clblm_ConstParam.f90:246-251)
+MAXISO = (6, 10, 9, 5, 6, 4, 3, 3, 2, 1, 2, 2, 3, 2, 4, 4, 2, 2, 5, 3, 2, 2, 3, 2,
+          1, 3, 2, 1, 2, 1, 3, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1, 1, 1, 1, 2, 4, 1)
+
+
+def line_list(n, v1, v2, seed, mols=(1,), isotopologues=False):
     """n lines on [v1, v2] with the workload distributions; molecules drawn
-    uniformly from `mols` (HITRAN numbers, isotopologue 1)."""
+    uniformly from `mols` (HITRAN numbers), isotopologue 1, or with
+    isotopologues=True each molecule's isotopologues drawn uniformly (the
+    line file's MOL field is molecule + 100 * isotopologue, 10 written as 0)
+    and O2 and N2 given self widths near their air widths."""
     rng = np.random.Generator(np.random.PCG64(seed))
     vnu = np.sort(rng.uniform(v1, v2, n))
     sp = 10.0 ** rng.uniform(-26.0, -19.0, n)
@@ -45,7 +53,16 @@ def line_list(n, v1, v2, seed, mols=(1,)):
     epp = rng.uniform(0.0, 3000.0, n)
     pshift = rng.uniform(-0.005, 0.005, n)
     mols = np.asarray(mols, dtype=np.int32)
-    mol = mols[rng.integers(0, len(mols), n)] + 100
+    m = mols[rng.integers(0, len(mols), n)]
+    mol = m + 100
+    if isotopologues:
+        iso = 1 + np.floor(rng.uniform(0.0, 1.0, n) * np.asarray(MAXISO)[m - 1]).astype(np.int32)
+        mol = m + 100 * (iso % 10)
+        # O2 and N2: self widths near the air widths, as in HITRAN, so that
+        # the reference's foreign width (air - vmr * self) / (1 - vmr) stays
+        # positive
+        o2n2 = (m == 7) | (m == 22)
+        hwhm = np.where(o2n2, alfa * rng.uniform(0.8, 1.2, n), hwhm)
     return Lines(vnu=vnu, sp=sp.astype(np.float32), alfa=alfa.astype(np.float32),
                  epp=epp.astype(np.float32), mol=mol.astype(np.int32),
                  hwhm=hwhm.astype(np.float32), tmpalf=tmpalf.astype(np.float32),

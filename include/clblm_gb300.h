@@ -93,7 +93,9 @@ typedef struct {
  * the arguments of ODLAY_nonStruct, clblm_ODLAY.f90:129-177. */
 typedef struct {
   int32_t        nmol;
-  const int32_t *mol_id;   /* HITRAN molecule numbers of the selected absorbers */
+  const int32_t *mol_id;   /* HITRAN molecule numbers (1-47) of the selected
+                            * absorbers; lines of every isotopologue count, each
+                            * with its own TIPS_2003 partition sums and mass */
   const double  *w;        /* [nmol] column amounts [molec/cm2]                */
   double         wtot;     /* total column incl. broadeners [molec/cm2]        */
   double         pave;     /* mbar */

@@ -364,16 +364,23 @@ static double atob(double aa, const double *Aarr, const double *Barr, int npt) {
 #undef B
 }
 
-static int tips_qt(int mol, double T, double *qt) {
-  if (mol < 1 || mol > CLBLM_TIPS_NMOL) return -1;
+/* TIPS_2003's Q(T) of (mol, iso): the QT_* table TIPS_2003 dispatches to
+ * (clblm_ODLAY_TIPS.f90:57-419), Q = 1 for O, CH3OH and SO3 */
+static int tips_qt(int mol, int iso, double T, double *qt) {
+  if (mol < 1 || mol > CLBLM_MXMOL || iso < 1 || iso > CLBLM_MAXISO[mol - 1]) return -1;
+  const int row = CLBLM_TIPS_QROW[mol - 1][iso - 1];
+  if (row == -1) {
+    *qt = 1.0;
+    return 0;
+  }
   if (T < 70. || T > 3000.) return -2;
-  *qt = atob(T, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q_ISO1[mol - 1], NT);
+  *qt = atob(T, CLBLM_TIPS_TDAT, CLBLM_TIPS_Q[row], NT);
   return 0;
 }
 
-int ocl_tips_scor(int mol, double t, double *scor) {
+int ocl_tips_scor(int mol, int iso, double t, double *scor) {
   double q296, qt;
-  if (tips_qt(mol, 296., &q296) || tips_qt(mol, t, &qt)) return CLBLM_ERR_RANGE;
+  if (tips_qt(mol, iso, 296., &q296) || tips_qt(mol, iso, t, &qt)) return CLBLM_ERR_RANGE;
   if (q296 <= 0. || qt <= 0.) return CLBLM_ERR_RANGE;
   *scor = q296 / qt;
   return 0;
@@ -381,15 +388,15 @@ int ocl_tips_scor(int mol, double t, double *scor) {
 
 /* ======================================================================
  * Per-layer molecular constants: MOLEC clblm_ODLAY_CommonSub.f90:201-264
- * (isotopologue 1 only: the line list carries iso 1 of molecules 1-7).
+ * with TIPS_2003, for every isotopologue of the selected molecules.
  * ====================================================================== */
 typedef struct {
   int nsel;
   int sel[64];          /* selected HITRAN molecule numbers */
   double WK[MXMOL + 1]; /* WK(m), clblm_ODLAY.f90:393-397 */
-  double SCOR[CLBLM_TIPS_NMOL + 1]; /* SCOR(m,1) */
+  double SCOR[MXMOL + 1][CLBLM_MXISO + 1]; /* SCOR(m,iso) */
   double RHOSLF[MXMOL + 1];
-  double ALFD1[CLBLM_TIPS_NMOL + 1]; /* ALFD1(m,1) */
+  double ALFD1[MXMOL + 1][CLBLM_MXISO + 1]; /* ALFD1(m,iso) */
 } molec_t;
 
 static int is_selected(const molec_t *M, int m) {
@@ -404,14 +411,15 @@ static int molec(ocl_session *s, molec_t *M, const clblm_layer_t *lay, double PA
   double RHORAT = (PAVE / P0) * (TEMP0 / TAVE);
   for (int i = 0; i < M->nsel; ++i) {
     int imol = M->sel[i];
-    if (imol < 1 || imol > CLBLM_TIPS_NMOL)
-      return fail(s, CLBLM_ERR_UNSUPPORTED, "molecule %d: TIPS/mass tables carry molecules 1-9", imol);
-    double scor;
-    if (ocl_tips_scor(imol, TAVE, &scor))
-      return fail(s, CLBLM_ERR_RANGE, "TIPS: temperature %.3f outside 70-3000 K", TAVE);
-    M->SCOR[imol] = scor;
+    if (imol < 1 || imol > MXMOL) return fail(s, CLBLM_ERR_ARG, "molecule %d: HITRAN molecules are 1-47", imol);
+    for (int iso = 1; iso <= MAXISO[imol - 1]; ++iso) {
+      double scor;
+      if (ocl_tips_scor(imol, iso, TAVE, &scor))
+        return fail(s, CLBLM_ERR_RANGE, "TIPS: temperature %.3f outside 70-3000 K", TAVE);
+      M->SCOR[imol][iso] = scor;
+      M->ALFD1[imol][iso] = sqrt(FAD * TAVE / CLBLM_ISO_MASS[imol - 1][iso - 1]);
+    }
     M->RHOSLF[imol] = RHORAT * M->WK[imol] / lay->wtot;
-    M->ALFD1[imol] = sqrt(FAD * TAVE / CLBLM_ISO1_MASS[imol - 1]);
   }
   return 0;
 }
@@ -1116,10 +1124,6 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
         if (!is_selected(M, M_)) continue;
         if (M_ > MXMOL || M_ < 1) continue;
         if (ISO > MAXISO[M_ - 1]) continue;
-        if (ISO != 1) {
-          free(S);
-          return fail(s, CLBLM_ERR_UNSUPPORTED, "isotopologue %d of molecule %d", ISO, M_);
-        }
         double alfa = (double)L->alfa[i];
         double pshift = (double)L->pshift[i];
         if (M_ == 7 && L->iflg[i] >= 0) alfa = (alfa - 0.21 * (double)L->hwhm[i]) / (1.0 - 0.21);
@@ -1136,12 +1140,12 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
         if (S->VNU[IJ] == 0.) SUI = 2. * SUI;
         if (S->EPP[IJ] <= -1.001) S->EPP[IJ] = fabs(S->EPP[IJ]);
         if (S->EPP[IJ] > -0.999)
-          SUI = SUI * M->SCOR[M_] * exp(-S->EPP[IJ] * BETACR) * (1. + exp(-S->VNU[IJ] * BETA));
+          SUI = SUI * M->SCOR[M_][ISO] * exp(-S->EPP[IJ] * BETACR) * (1. + exp(-S->VNU[IJ] * BETA));
         double TMPCOR = pow(TRATIO, (double)L->tmpalf[i]);
         double ALFA0I = S->ALFA[IJ] * TMPCOR;
         double HWHMSI = (double)L->hwhm[i] * TMPCOR;
         S->ALFA[IJ] = ALFA0I * (RHORAT - M->RHOSLF[M_]) + HWHMSI * M->RHOSLF[M_];
-        S->EPP[IJ] = S->VNU[IJ] * M->ALFD1[M_];
+        S->EPP[IJ] = S->VNU[IJ] * M->ALFD1[M_][ISO];
         S->SP[IJ] = SUI * (1. + 0. * (PAVE / P0) * (PAVE / P0));
         S->SPP[IJ] = SUI * 0. * (PAVE / P0);
         if (S->VNU[IJ] > VHI) {
@@ -1541,10 +1545,6 @@ static int hiracq(ocl_session *s, hirac_args *a) {
       if (!is_selected(M, m)) goto L25;
       if (m > MXMOL || m < 1) goto L25;
       if (ISO > MAXISO[m - 1]) goto L25;
-      if (ISO != 1) {
-        rc = fail(s, CLBLM_ERR_UNSUPPORTED, "isotopologue %d of molecule %d", ISO, m);
-        goto done;
-      }
       if (IFLAG == 1 || IFLAG == 3) {
         rc = fail(s, CLBLM_ERR_UNSUPPORTED, "line coupling (IFLG=%d)", IFLAG);
         goto done;
@@ -1560,7 +1560,7 @@ static int hiracq(ocl_session *s, hirac_args *a) {
         double ALFA0I = B->ALFA0[I] * TMPCOR;
         double HWHMSI = B->HWHMS[I] * TMPCOR;
         double ALFL = ALFA0I * (RHORAT - M->RHOSLF[m]) + HWHMSI * M->RHOSLF[m];
-        double ALFAD = B->VNU[I] * M->ALFD1[m];
+        double ALFAD = B->VNU[I] * M->ALFD1[m][ISO];
         double ZETA = ALFL / (ALFL + ALFAD);
         B->ZETAI[I] = ZETA;
         double FZETA = 100. * ZETA;
@@ -1581,7 +1581,7 @@ static int hiracq(ocl_session *s, hirac_args *a) {
         B->RECALF[I] = 1. / ALFV;
         if (B->EPP[I] <= -1.001) B->EPP[I] = fabs(B->EPP[I]);
         if (B->EPP[I] > -0.999)
-          SUI = SUI * M->SCOR[m] * exp(-B->EPP[I] * BETACR) * (1. + exp(-B->VNU[I] / XKT));
+          SUI = SUI * M->SCOR[m][ISO] * exp(-B->EPP[I] * BETACR) * (1. + exp(-B->VNU[I] / XKT));
         B->SP[I] = SUI * (1. + 0. * PAVP2);
         double SPPI = SUI * 0. * PAVP0;
         B->SPPSP[I] = SPPI / B->SP[I];

@@ -88,7 +88,7 @@ void ocl_shape_tables(double *f1, double *f2, double *f3, double *fg,
 double ocl_radfn(double vi, double xkt);
 double ocl_planck(double v, double xkt);
 void ocl_rlin(double od, double *hlf);
-int ocl_tips_scor(int mol, double t, double *scor);
+int ocl_tips_scor(int mol, int iso, double t, double *scor);
 /* ABSRB(1..5050) of the H2O continuum on OPDPTH's 1 cm-1 grid starting at *v1abs */
 int ocl_contnm_h2o(const clblm_cont_t *C, int jrad, double v1, double v2, double pave,
                    double tave, double wtot, double wk1, double xself, double xfrgn,

@@ -62,7 +62,7 @@ def lib():
         L.ocl_planck.restype = C.c_double
         L.ocl_planck.argtypes = [C.c_double, C.c_double]
         L.ocl_rlin.argtypes = [C.c_double, P(C.c_double)]
-        L.ocl_tips_scor.argtypes = [C.c_int, C.c_double, P(C.c_double)]
+        L.ocl_tips_scor.argtypes = [C.c_int, C.c_int, C.c_double, P(C.c_double)]
         L.ocl_interp_spectrum.argtypes = [P(C.c_double), C.c_double, C.c_double, C.c_int64, P(C.c_double),
                                           C.c_double, C.c_double, C.c_int64]
         L.ocl_jac_mode2.argtypes = [C.c_void_p, P(T.clblm_lines_t), P(T.clblm_cont_t), P(T.clblm_column_t),
@@ -231,9 +231,9 @@ def rlin(od):
     return h.value
 
 
-def tips_scor(mol, t):
+def tips_scor(mol, t, iso=1):
     s = C.c_double()
-    rc = lib().ocl_tips_scor(int(mol), float(t), C.byref(s))
+    rc = lib().ocl_tips_scor(int(mol), int(iso), float(t), C.byref(s))
     if rc:
         raise OracleError(rc, "tips")
     return s.value

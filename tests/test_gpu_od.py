@@ -8,8 +8,9 @@ from clblm_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _layer_case(n_lines, v1, v2, seed, mols=(1,), pave=1013.25, tave=296.0, wabs=1e22, wtot=2.479e24):
-    lines = synth.line_list(n_lines, v1, v2, seed=seed, mols=mols)
+def _layer_case(n_lines, v1, v2, seed, mols=(1,), pave=1013.25, tave=296.0, wabs=1e22, wtot=2.479e24,
+                isotopologues=False):
+    lines = synth.line_list(n_lines, v1, v2, seed=seed, mols=mols, isotopologues=isotopologues)
     mol = np.array(mols, np.int32)
     w = np.full((1, len(mols)), wabs)
     col = T.Column(mol, [pave], [tave], [tave], [tave], w, [wtot], [1.67 * wtot], v1, v2, tave, 1.0)
@@ -37,6 +38,21 @@ def _compare(gpu_lib, oracle_mod, lines, col, cont=None, contnm_off=1, precision
 @pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
 def test_config0_full(gpu_lib, oracle_mod, precision, tol):
     lines, col = synth.config0()
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+def test_isotopologues_and_molecules_past_nine(gpu_lib, oracle_mod, precision, tol):
+    """Lines of every isotopologue of H2O, CO2, O3 and O2 and of HNO3, OCS,
+    N2 (foreign width from the air width), O, CH3OH and SO3 (Q = 1): each
+    isotopologue's partition-sum ratio and Doppler mass"""
+    mols = (1, 2, 3, 7, 12, 19, 22, 34, 39, 47)
+    lines, col = _layer_case(30000, 600.0, 700.0, seed=11, mols=mols, pave=400.0, tave=240.0, wabs=1e17,
+                             isotopologues=True)
+    iso = (lines.mol // 100) % 10
+    assert len(set(iso.tolist())) == 10  # isotopologues 1-9 and 10 (written as 0)
     od, ref = _compare(gpu_lib, oracle_mod, lines, col, precision=precision)
     rel = np.max(np.abs(od - ref) / np.abs(ref))
     assert rel <= tol, rel

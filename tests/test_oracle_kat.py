@@ -41,15 +41,41 @@ def test_continuum_at_table_nodes(oracle_mod, mtckd, pave, tave, jrad):
         assert got == pytest.approx(want, rel=1e-13), nu
 
 
+MAXISO = (6, 10, 9, 5, 6, 4, 3, 3, 2, 1, 2, 2, 3, 2, 4, 4, 2, 2, 5, 3, 2, 2, 3, 2,
+          1, 3, 2, 1, 2, 1, 3, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1, 1, 1, 1, 2, 4, 1)
+Q_ONE = (34, 39, 47)  # O, CH3OH, SO3: TIPS_2003 takes Q = 1
+
+
 def test_tips_ratio_is_one_at_296(oracle_mod):
-    for mol in range(1, 10):
-        assert oracle_mod.tips_scor(mol, 296.0) == 1.0
+    for mol in range(1, 48):
+        for iso in range(1, MAXISO[mol - 1] + 1):
+            assert oracle_mod.tips_scor(mol, 296.0, iso) == 1.0, (mol, iso)
 
 
 def test_tips_ratio_decreases_with_temperature(oracle_mod):
-    for mol in range(1, 10):
-        s = [oracle_mod.tips_scor(mol, t) for t in np.arange(150.0, 351.0, 10.0)]
-        assert np.all(np.diff(s) < 0), mol
+    for mol in range(1, 48):
+        for iso in range(1, MAXISO[mol - 1] + 1):
+            s = [oracle_mod.tips_scor(mol, t, iso) for t in np.arange(150.0, 351.0, 10.0)]
+            if mol in Q_ONE:
+                assert np.all(np.array(s) == 1.0)
+            else:
+                assert np.all(np.diff(s) < 0), (mol, iso)
+
+
+def test_tips_fallbacks_to_the_first_isotopologue(oracle_mod):
+    """TIPS_2003 reads isotopologue 1's table for HNO3 2, HF 2, HCl 3-4,
+    HBr 3-4, HI 2, N2 2 and COF2 2 (clblm_ODLAY_TIPS.f90:150-260)"""
+    for mol, isos in ((12, (2,)), (14, (2,)), (15, (3, 4)), (16, (3, 4)), (17, (2,)), (22, (2,)), (29, (2,))):
+        for t in (200.0, 250.0, 310.0):
+            for iso in isos:
+                assert oracle_mod.tips_scor(mol, t, iso) == oracle_mod.tips_scor(mol, t, 1)
+    # HCl 2 and HBr 2 have tables of their own
+    assert oracle_mod.tips_scor(15, 250.0, 2) != oracle_mod.tips_scor(15, 250.0, 1)
+    assert oracle_mod.tips_scor(16, 250.0, 2) != oracle_mod.tips_scor(16, 250.0, 1)
+    # a classical rotor's Q ~ T^(3/2) (CH4) and T (CO): the ratio's slope
+    for mol, expo in ((6, 1.5), (5, 1.0)):
+        s = oracle_mod.tips_scor(mol, 250.0, 2)
+        assert s == pytest.approx((296.0 / 250.0) ** expo, rel=0.03), mol
 
 
 def test_planck(oracle_mod):
