@@ -184,8 +184,14 @@ class Lines:
     def subset(self, lo, hi):
         return Lines(**{name: getattr(self, name)[lo:hi] for name, _ in self.FIELDS})
 
+    def keys(self):
+        """The centres as sort keys: a coefficient record (IFLG < 0, after a
+        coupled line) takes its line's centre."""
+        k = np.where(self.iflg >= 0, self.vnu, -np.inf)
+        return np.maximum.accumulate(k) if self.n else k
+
     def window(self, v1, v2):
-        lo, hi = np.searchsorted(self.vnu, [v1, v2])
+        lo, hi = np.searchsorted(self.keys(), [v1, v2])
         return self.subset(int(lo), int(hi))
 
     def struct(self):

@@ -61,6 +61,12 @@ struct LayerPlan {
   float epp_abs_f, epp_neg_f;
   double spfac;                   // 1 + 0*PAVP2, the SP factor of LNCORQ/LINF4Q
   double dptmn, dptfc;
+  // line coupling: the interval of the coefficient temperatures TEMPLC =
+  // 200, 250, 296, 340 K that LNCORQ (:1713-1721, lower node lc_ilc) and
+  // LINF4Q (clblm_ODLAY_LineF4.f90:860-866, upper node lc4_ilc) interpolate
+  // in, 1 / its width and TAVE minus the node (1-based node numbers)
+  int lc_ilc, lc4_ilc;
+  double lc_rectlc, lc_tmpdif, lc4_rectlc, lc4_tmpdif;
   int jrad, ilnflg, max1, max2, max3, nalfmax, nbound;
   int npanels, nhi_last;          // panels and NHI of the last panel
   int64_t nsamp;                  // R1 points output
@@ -109,7 +115,15 @@ struct LinePrep {
   double zetdif;   // ZETDIF = 100*ZETA - (IZETA-1)
   int iz;          // IZETA
   int fpanel;      // first panel whose MAX1 fits the line (-1: rejected)
+  double sppsp;    // SPPSP = SPP / SP of a coupled line (line coupling), else 0
 };
+
+// A grid record of a coupled line carries this bit in its panel number q: the
+// panel kernel's fast sums skip it and add it with its dispersion term
+constexpr int kCplBit = 1 << 30;
+// CNVFNQ's CLC1..3 = 4, 16, 64 over NX - 1 (clblm_ODLAY.f90:2117-2119)
+constexpr double kCLC1 = 4. / (double)(kNFPTS - 1), kCLC2 = 16. / (double)(kNFPTS - 1),
+                 kCLC3 = 64. / (double)(kNFPTS - 1);
 
 #ifdef __CUDACC__
 // CNVFNQ's set-up of one line read in panel q (clblm_ODLAY.f90:2127-2166):

@@ -48,6 +48,7 @@ struct ContIn {
 // LINF4Q-corrected line (before SHRINQ)
 struct F4Prep {
   double vnu, sp;
+  double spp;  // SPP = SUI * Y * PAVP0 of a coupled line (line coupling), else 0
   // widths: binary64 ALFA, ALFD on the FP64 path; on the mixed path, where
   // they set no index or group, f[0..2] = ALFA, ALFD, SP as floats
   union {
@@ -94,7 +95,7 @@ __global__ void k_scan_apply(const LinePrep* prep, int64_t stride, const int64_t
                              int nblk_stride, int* qpanel);
 __global__ void k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
                                const int* qpanel, int64_t stride, GridRec* rec, GridRecD* recd,
-                               GridRecLo* reclo, const double* vnu_raw, unsigned long long* stats,
+                               GridRecLo* reclo, double* cpl, unsigned long long* stats,
                                double* alfvmax, int* aggmax, int* aggmin, int nagg);
 __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
@@ -126,7 +127,7 @@ struct F4Rec;
 struct F4RecD;
 __global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
-                              int64_t* nmirror, unsigned long long* stats);
+                              int64_t* nmirror, unsigned long long* stats, double* cpl);
 // layer averages and amounts of a nadir path (ALAYER + FPACK)
 constexpr int kMaxLayerMol = 64;
 __global__ void k_layer_amounts(int nlev, int nmol, const double* z, const double* p, const double* t,

@@ -21,6 +21,7 @@ struct PanelArgs {
   const GridRecD* recd;       // FP64 records (FP64 path only)
   const GridRecLo* reclo;
   const LinePrep* prep;       // the lines (the mixed path's rare FP64 index)
+  const double* cpl;          // SPPSP of the coupled lines (records flagged with kCplBit)
   int64_t stride;
   const int64_t* ranges;     // per panel: candidate record windows of R1, R2, R3
   int64_t panel_stride;
@@ -85,7 +86,14 @@ struct F4Args {
   const int* smin_jmin;     // running min (from the right) of jmin
   void* r4_all;
   int* err;                 // bit 2: a shared-memory stage never arrived
+  const double* cpl;        // DPTRAT of each record (line coupling; 0: uncoupled)
 };
+
+// line coupling in the far wings: the coupled records of each layer in
+// record order, then their dispersion terms added to R4
+__global__ void k_f4_cpl_list(const F4Args a, int64_t* list, int64_t* nlist);
+template <bool Plain>
+__global__ void k_f4_cpl(const F4Args a, const int64_t* list, const int64_t* nlist);
 
 size_t panel_smem_bytes(bool plain, bool wings = false);  // wings: the mixed far-wing pass
 __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* blk_v1, const int* blk_n,

@@ -371,6 +371,37 @@ __device__ __forceinline__ float fix_terms(const PanelSmem<false>& S, const Grid
   return c;
 }
 
+// The terms of the coupled records (bits of m) at point g (mixed path): the
+// shape with the exact index, plus its dispersion term, the shape times
+// CLCk * DPTRAT * ZF (CNVFNQ's line-coupling loop, clblm_ODLAY.f90:2195-2239)
+template <int GRID>
+__device__ __forceinline__ float cpl_terms(const PanelSmem<false>& S, const GridRec* buf, int64_t base,
+                                        const GridRecLo* __restrict__ reclo, const PanelArgs& a, int g, int qmax,
+                                        unsigned m) {
+  const float clc = GRID == 1 ? (float)kCLC1 : (GRID == 2 ? (float)kCLC2 : (float)kCLC3);
+  float c = 0.f;
+  while (m) {
+    const int k = __ffs(m) - 1;
+    m &= m - 1;
+    const GridRec r = buf[k];
+    const int q = r.q & ~kCplBit;
+    const int kk = g - r.g_lo + 1;
+    if (kk < 1 || g > r.g_hi || q > qmax) continue;
+    float d;
+    int iz = fast_index(kk, r, &d);
+    if (fabsf(d) > 0.499f) iz = table_index_near_boundary(kk, r.zfl, r.zs, reclo[base + k], &a, base + k, q, GRID);
+    if (iz > kNFMX) {
+      atomicOr(a.err, 2);
+      continue;
+    }
+    const float v = table_term<GRID>(S, r, iz);
+    const float zf = fmaf((float)kk, r.zs, r.zfl);
+    const float dpt = (float)a.cpl[(int64_t)blockIdx.y * a.stride + base + k];
+    c += v + (v * (clc * dpt)) * zf;
+  }
+  return c;
+}
+
 // Sum over the records [lo, hi) of one grid at global point g of the lane.
 // FP64 path: [lo, hi) is the warp's 32-point tile's; the records pass through
 // the warp's shared-memory buffer kBatch at a time (the next batch already in
@@ -411,20 +442,29 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
       if (!active) continue;
       for (int k = 0; k < cnt; ++k) {
         const GridRec r = buf[k];
-        if (g < r.g_lo || g > r.g_hi || r.q > qmax) continue;
+        if (g < r.g_lo || g > r.g_hi || (r.q & ~kCplBit) > qmax) continue;
         const GridRecD& d = S.wrecd[warp][k];
-        const int iz = (int)(fabs(fma((double)(g - r.g_lo + 1), d.zs, d.zfl)) + 1.5);
+        const double zf = fma((double)(g - r.g_lo + 1), d.zs, d.zfl);
+        const int iz = (int)(fabs(zf) + 1.5);
         if (iz > kNFMX) {
           atomicOr(a.err, 2);
           continue;
         }
+        // a coupled line adds its dispersion term: the strengths times CLCk
+        // times DPTRAT, the shape times ZF (clblm_ODLAY.f90:2195-2239)
+        const double dpt = (r.q & kCplBit) ? a.cpl[(int64_t)blockIdx.y * a.stride + base + k] : 0.;
         if constexpr (GRID == 1) {
           const double* T = S.t1 + 3 * (iz - 1);
           acc.add(d.a0 * T[0] + d.a1 * T[1] + d.a2 * T[2]);
+          if (dpt != 0.)
+            acc.add((((d.a0 * kCLC1) * dpt) * T[0] + ((d.a1 * kCLC1) * dpt) * T[1] + ((d.a2 * kCLC1) * dpt) * T[2]) *
+                    zf);
         } else if constexpr (GRID == 2) {
           acc.add(d.a0 * S.t2[iz - 1]);
+          if (dpt != 0.) acc.add((((d.a0 * kCLC2) * dpt) * S.t2[iz - 1]) * zf);
         } else {
           acc.add(d.a0 * S.t3[iz - 1]);
+          if (dpt != 0.) acc.add((((d.a0 * kCLC3) * dpt) * S.t3[iz - 1]) * zf);
         }
       }
     }
@@ -440,6 +480,8 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
     for (int b = 0; b < nmax; b += kHalfBatch) {
       __syncwarp();
       if (hl < kHalfBatch) hb[hl] = nxt;
+      // the batch's coupled records: term_fast skips them (q carries kCplBit)
+      const unsigned cpl_bits = __ballot_sync(0xffffffffu, hl < kHalfBatch && (nxt.q & kCplBit) != 0);
       __syncwarp();
       const int cnt = min(n - b, kHalfBatch);
       if (hl < kHalfBatch && b + kHalfBatch + hl < n) nxt = rec[lo + b + kHalfBatch + hl];
@@ -465,6 +507,8 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
       }
       float bsum = (s0 + s1) + (s2 + s3);
       if (fix) bsum += fix_terms<GRID>(S, hb, lo + b, reclo, a, g, fix);
+      const unsigned cm = (cpl_bits >> (16 * half)) & ((1u << cnt) - 1u);
+      if (cm) bsum += cpl_terms<GRID>(S, hb, lo + b, reclo, a, g, qmax, cm);
       acc.add(bsum);
     }
   }
@@ -968,7 +1012,7 @@ __global__ void __launch_bounds__(256) k_rsym(const __grid_constant__ PanelArgs 
   __shared__ double sF[3][kRsymN1];
   // the chunk's panel-0 lines that reach those points, in line order
   struct RSet {
-    double zf[3], zs, str[5];
+    double zf[3], zs, str[5], cpl;
     int jmin1, jmax1, j2, j3;
   };
   __shared__ RSet set[256];
@@ -989,8 +1033,9 @@ __global__ void __launch_bounds__(256) k_rsym(const __grid_constant__ PanelArgs 
     bool hit = false;
     if (t < nrec) {
       const GridRec& r1 = rec[t];
-      if (r1.q <= 0) more = 1;
-      if (r1.q == 0 && prep[t].fpanel >= 0) {
+      const int q1 = r1.q & ~kCplBit;
+      if (q1 <= 0) more = 1;
+      if (q1 == 0 && prep[t].fpanel >= 0) {
         for (int k = 0; k < 3; ++k) {
           const GridRec& r = rec[(int64_t)k * a.stride + t];
           hit |= r.g_lo <= r.g_hi && r.g_lo <= ghi[k] && r.g_hi >= glo;
@@ -1029,6 +1074,7 @@ __global__ void __launch_bounds__(256) k_rsym(const __grid_constant__ PanelArgs 
       const double* tabs[5] = {c_CF1, c_CGAUSS, c_CER, c_CF2, c_CF3};
       for (int k = 0; k < 5; ++k)
         e.str[k] = DEPTHA * (tabs[k][L.iz - 1] + ZD * (tabs[k][L.iz] - tabs[k][L.iz - 1]));
+      e.cpl = L.sppsp;
     }
     __syncthreads();
     // each held point adds the chunk's lines in their order
@@ -1048,10 +1094,15 @@ __global__ void __launch_bounds__(256) k_rsym(const __grid_constant__ PanelArgs 
         if (grid == 0) {
           const double* T = a.tabs.t1d + 3 * (iz - 1);
           acc = acc + e.str[0] * T[0] + e.str[1] * T[1] + e.str[2] * T[2];
+          if (e.cpl != 0.)  // line coupling's dispersion term
+            acc = acc + (e.str[0] * kCLC1 * e.cpl * T[0] + e.str[1] * kCLC1 * e.cpl * T[1] +
+                         e.str[2] * kCLC1 * e.cpl * T[2]) * zf;
         } else if (grid == 1) {
           acc = acc + e.str[3] * a.tabs.t2d[iz - 1];
+          if (e.cpl != 0.) acc = acc + e.str[3] * kCLC2 * e.cpl * a.tabs.t2d[iz - 1] * zf;
         } else {
           acc = acc + e.str[4] * a.tabs.t3d[iz - 1];
+          if (e.cpl != 0.) acc = acc + e.str[4] * kCLC3 * e.cpl * a.tabs.t3d[iz - 1] * zf;
         }
       }
       sR[grid][i] = acc;
@@ -1350,6 +1401,104 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
     }
   }
 }
+
+// ---- line coupling in the far wings -----------------------------------------
+// CNVF4Q adds XM * DPTRAT * F4FN for a coupled record on top of its F4FN
+// (clblm_ODLAY_LineF4.f90:366, 414-417, 450-453); k_f4_conv has added F4FN
+// for every record, these kernels add the rest.  Coupled records are rare:
+// one CTA per layer lists them in record order, then each R4 point adds
+// their terms in that order.
+__global__ void k_f4_cpl_list(const F4Args a, int64_t* __restrict__ list, int64_t* __restrict__ nlist) {
+  const int layer = blockIdx.x;
+  const int64_t n = a.nrec[layer + a.layer0] + a.nmirror[layer + a.layer0];
+  const double* C = a.cpl + (int64_t)layer * a.stride;
+  int64_t* L = list + (int64_t)layer * a.stride;
+  __shared__ int wcnt[32];
+  __shared__ int chunk_tot;
+  __shared__ int64_t run;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) run = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < n; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const bool hit = i < n && C[i] != 0.;
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) wcnt[warp] = __popc(bal);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int r = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        const int v = wcnt[w];
+        wcnt[w] = r;
+        r += v;
+      }
+      chunk_tot = r;
+    }
+    __syncthreads();
+    if (hit) L[run + wcnt[warp] + __popc(bal & ((1u << lane) - 1u))] = i;
+    __syncthreads();
+    if (threadIdx.x == 0) run += chunk_tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) nlist[layer + a.layer0] = run;
+}
+
+template <bool Plain>
+__global__ void k_f4_cpl(const F4Args a, const int64_t* list, const int64_t* nlist) {
+  using Real = typename std::conditional<Plain, double, float>::type;
+  const int layer = blockIdx.y;
+  const LayerPlan& P = a.plans[layer + a.layer0];
+  const int64_t nc = nlist[layer + a.layer0];
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (nc == 0 || m >= P.nptr4) return;
+  const int J = (int)m + 1;
+  const int64_t* Lc = list + (int64_t)layer * a.stride;
+  const double* C = a.cpl + (int64_t)layer * a.stride;
+  double acc = 0.;
+  bool any = false;
+  if constexpr (Plain) {
+    const F4RecD* R = a.recd + (int64_t)layer * a.stride;
+    const double ZSQBND = 64. * 64.;
+    const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
+    const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
+    const double bnd2 = P.bound4 * P.bound4;
+    for (int64_t k = 0; k < nc; ++k) {
+      const int64_t i = Lc[k];
+      const F4RecD d = R[i];
+      if (J < d.jmin || J > d.jmax) continue;
+      const double XM = (double)m * P.dvr4 - d.xnui;
+      const double XMSQ = XM * XM;
+      const double ZVSQ = XMSQ / d.alv2;
+      const double fb = d.co2 ? (2. - XMSQ / bnd2) * d.fbnd : d.fbnd;
+      const double F4FN = ZVSQ <= ZSQBND ? (d.siv * A3 + ZVSQ * (d.siv * B3)) - fb : d.sil / (d.al2 + XMSQ) - fb;
+      acc = acc + XM * C[i] * F4FN;
+      any = true;
+    }
+  } else {
+    const F4Rec* R = a.rec + (int64_t)layer * a.stride;
+    const float dvr4 = (float)P.dvr4;
+    for (int64_t k = 0; k < nc; ++k) {
+      const int64_t i = Lc[k];
+      const F4Rec& r = R[i];
+      if (J < r.jmin || J > r.jmax) continue;
+      // F4FN as k_f4_conv forms it, at this one point
+      const float xm = fmaf((float)(J - 1) + r.nmc.x, dvr4, r.x0.x);
+      const float xmsq = xm * xm;
+      const float nfb = fmaf(xmsq, r.fb2.x, r.nfb0.x);
+      float f = fmaf(r.sil.x, rcp_approx(xmsq + r.al2.x), nfb);
+      const float zvsq = xmsq * r.ralv2.x;
+      if (zvsq <= 4096.f) f = fmaf(zvsq, r.sb3.x, r.sa3.x) + nfb;
+      acc += (double)((xm * (float)C[i]) * f);
+      any = true;
+    }
+  }
+  if (any) {
+    Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
+    R4[m] = R4[m] + (Real)acc;
+  }
+}
+template __global__ void k_f4_cpl<false>(const F4Args, const int64_t*, const int64_t*);
+template __global__ void k_f4_cpl<true>(const F4Args, const int64_t*, const int64_t*);
 
 template __global__ void k_f4_conv<false, 64>(F4Args);
 template __global__ void k_f4_conv<false, 128>(F4Args);

@@ -85,6 +85,34 @@ __device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rd
   return fits_panel(vnu, vft, dv, rdv, bhwdxf, max1);
 }
 
+// The coupling coefficients of a coupled line (IFLG 1: Y and G; IFLG 3:
+// GAMMA1 and GAMMA2) at the layer's temperature, from the record k after it:
+// A(1..4) = VNU, ALFA, the bits of MOL read as a float, TMPALF and B(1..4) =
+// SP, EPP, HWHM, PSHIFT hold them at TEMPLC = 200, 250, 296, 340 K (LNCORQ
+// clblm_ODLAY.f90:1822-1846; RDLIN's O2/N2 width rule applies to the record
+// as to any).  LNCORQ interpolates from the lower node ilc, LINF4Q
+// (clblm_ODLAY_LineF4.f90:963-984) from the upper one (upper = true).
+__device__ void lc_coefs(const LineIn& L, int64_t k, int ilc, double rectlc, double tmpdif, bool upper, double* a,
+                         double* b) {
+  double alfa = (double)L.alfa[k];
+  const int m = L.mol[k] % 100;
+  if (m == 7 && L.iflg[k] >= 0) alfa = (alfa - 0.21 * (double)L.hwhm[k]) / (1.0 - 0.21);
+  if (m == 22 && L.iflg[k] >= 0) alfa = (alfa - 0.79 * (double)L.hwhm[k]) / (1.0 - 0.79);
+  const double A[5] = {0., L.vnu[k], alfa, (double)__int_as_float(L.mol[k]), (double)L.tmpalf[k]};
+  const double B[5] = {0., (double)L.sp[k], (double)L.epp[k], (double)L.hwhm[k], (double)L.pshift[k]};
+  if (!upper) {
+    const double SLOPEA = (A[ilc + 1] - A[ilc]) * rectlc;
+    const double SLOPEB = (B[ilc + 1] - B[ilc]) * rectlc;
+    *a = A[ilc] + SLOPEA * tmpdif;
+    *b = B[ilc] + SLOPEB * tmpdif;
+  } else {
+    const double SLOPEY = (A[ilc] - A[ilc - 1]) * rectlc;
+    const double SLOPEG = (B[ilc] - B[ilc - 1]) * rectlc;
+    *a = A[ilc] + SLOPEY * tmpdif;
+    *b = B[ilc] + SLOPEG * tmpdif;
+  }
+}
+
 __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                             const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
                             LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats) {
@@ -104,6 +132,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     r.zetdif = 0.;
     r.iz = 0;
     r.fpanel = -1;
+    r.sppsp = 0.;
     int iflg = lines.iflg[i];
     int molf = lines.mol[i];
     int m = molf % 100;
@@ -111,10 +140,6 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     if (iso == 0) iso = 10;
     bool ok = iflg >= 0 && m >= 1 && m <= kMaxMol && P.mrow[m] >= 0;
     if (ok && iso > c_MAXISO[m]) ok = false;
-    if (ok && (iflg == 1 || iflg == 3)) {
-      bad++;
-      ok = false;
-    }
     double SUI = 0.;
     if (ok) {
       SUI = (double)lines.sp[i] * P.wk[m];
@@ -123,6 +148,12 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     if (ok) {
       nlin++;
       const IsoRow& R = iso_tab[P.iso_off + P.mrow[m] + iso - 1];
+      // line coupling: Y, G (IFLG 1) or GAMMA1, GAMMA2 (IFLG 3)
+      double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
+      if ((iflg == 1 || iflg == 3) && i + 1 < lines.n) {
+        if (iflg == 1) lc_coefs(lines, i + 1, P.lc_ilc, P.lc_rectlc, P.lc_tmpdif, false, &YI, &GI);
+        else lc_coefs(lines, i + 1, P.lc_ilc, P.lc_rectlc, P.lc_tmpdif, false, &GAMMA1, &GAMMA2);
+      }
       double alfa0 = (double)lines.alfa[i];
       double hwhms = (double)lines.hwhm[i];
       // air-broadened widths of O2 and N2 to foreign widths (RDLIN :2728-2745)
@@ -133,6 +164,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
       double ALFL = ALFA0I * R.rhodif + HWHMSI * R.rhoslf;  // RHODIF = RHORAT - RHOSLF
+      if (iflg == 3) ALFL = ALFL * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);  // reduced widths
       double ALFAD = VNU * R.alfd1;
       double ZETA = ALFL / (ALFL + ALFAD);
       double FZETA = 100. * ZETA;
@@ -171,7 +203,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             if (EPP > P.epp_neg_f)
               sui = sui * R.scor_f * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
             SUI = sui;
-            SP = SUI;  // SUI*(1 + 0*PAVP2)
+            SP = iflg == 1 ? SUI * (1. + GI * P.pavp2) : SUI;  // SUI*(1 + G*PAVP2)
             // SPEAK = SUI/ALFV > 0 unless SUI = 0 (SUI >= 1e-45, 1/ALFV > 1:
             // no underflow), so with DPTMIN = 0 the test is SUI = 0
             if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
@@ -182,12 +214,14 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             if (EPP <= -1.001) EPP = fabs(EPP);
             if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
             if (EPP > -0.999) SUI = SUI * R.scor * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
-            SP = SUI * P.spfac;
+            SP = SUI * (1. + GI * P.pavp2);
             if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
               double SPEAK = SUI * RECALF;
               if (SPEAK <= P.dptmn) ok = false;  // DPTFAC == 0 on this path
             }
           }
+          // SPPSP = SPP / SP, SPP = SUI * Y * PAVP0 (:1938-1940)
+          if (iflg == 1) r.sppsp = (SUI * YI * P.pavp0) / SP;
           if (ok) {
             lincnt++;
             nminus += nmin;
@@ -323,7 +357,7 @@ __device__ __forceinline__ void interp_coef(const double* tab, int IZM, double Z
 __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vft_all,
                                const LinePrep* __restrict__ prep, const int* __restrict__ qpanel, int64_t stride,
                                GridRec* __restrict__ rec, GridRecD* __restrict__ recd,
-                               GridRecLo* __restrict__ reclo, const double* __restrict__ vnu_raw,
+                               GridRecLo* __restrict__ reclo, double* __restrict__ cpl,
                                unsigned long long* __restrict__ stats,
                                double* __restrict__ alfvmax, int* __restrict__ aggmax, int* __restrict__ aggmin,
                                int nagg) {
@@ -419,6 +453,12 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
       l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
       amax = fmax(amax, lp.alfv);
+      if (lp.sppsp != 0.) {  // a coupled line: its records go the exact way
+        g1.q |= kCplBit;
+        g2.q |= kCplBit;
+        g3.q |= kCplBit;
+        cpl[(int64_t)layer * stride + t] = lp.sppsp;
+      }
     }
     if (live) {
       int64_t o = (int64_t)layer * stride * 3;
@@ -1121,7 +1161,7 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
     int64_t i = P.f4_lo + t;
     F4Prep r;
     r.pass = 0;
-    r.vnu = r.sp = 0.;
+    r.vnu = r.sp = r.spp = 0.;
     r.w.d[0] = r.w.d[1] = 0.;
     r.mol = 0;
     int iflg = lines.iflg[i];
@@ -1131,14 +1171,17 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
     if (iso == 0) iso = 10;
     bool ok = iflg >= 0 && m >= 1 && m <= kMaxMol && P.mrow[m] >= 0;
     if (ok && iso > c_MAXISO[m]) ok = false;
-    if (ok && (iflg == 1 || iflg == 3)) {
-      bad++;
-      ok = false;
-    }
     if (ok) {
       double SUI = (double)lines.sp[i] * P.wk[m];
       if (SUI != 0. && !(lines.vnu[i] < P.v1l4)) {
         const IsoRow& R = iso_tab[P.iso_off + P.mrow[m] + iso - 1];
+        // line coupling: G scales the strength, Y gives SPP (IFLG 1);
+        // GAMMA1, GAMMA2 reduce the width (IFLG 3)
+        double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
+        if ((iflg == 1 || iflg == 3) && i + 1 < lines.n) {
+          if (iflg == 1) lc_coefs(lines, i + 1, P.lc4_ilc, P.lc4_rectlc, P.lc4_tmpdif, true, &YI, &GI);
+          else lc_coefs(lines, i + 1, P.lc4_ilc, P.lc4_rectlc, P.lc4_tmpdif, true, &GAMMA1, &GAMMA2);
+        }
         const float alfa_in = lines.alfa[i], hwhm_in = lines.hwhm[i];
         const double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
         const float EPP0 = lines.epp[i];
@@ -1156,9 +1199,16 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           const float TMPCOR = __expf(lines.tmpalf[i] * P.ln_tratio_f);  // (T/296)^n
           const float rs = R.rhoslf_f;
           r.w.f[0] = (alfa * TMPCOR) * (P.rhorat_f - rs) + (hwhm_in * TMPCOR) * rs;
+          if (iflg == 3) r.w.f[0] = r.w.f[0] * (float)(1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
           r.w.f[1] = vf * R.alfd1_f;
+          if (iflg == 1) {
+            r.sp = (double)sui * (1. + GI * P.pavp2);  // SP = SUI*(1 + G*PAVP2)
+            r.spp = (double)sui * YI * P.pavp0;       // SPP = SUI*Y*PAVP0
+            sui = (float)r.sp;
+          } else {
+            r.sp = (double)sui;  // SP = SUI*(1 + 0*PAVP2) = SUI
+          }
           r.w.f[2] = sui;
-          r.sp = (double)sui;  // SP = SUI*(1 + 0*PAVP2) = SUI
         } else {
           double alfa = (double)alfa_in, hwhm = (double)hwhm_in;
           if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
@@ -1171,8 +1221,10 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           double ALFA0I = alfa * TMPCOR;
           double HWHMSI = hwhm * TMPCOR;
           r.w.d[0] = ALFA0I * (P.rhorat - R.rhoslf) + HWHMSI * R.rhoslf;
+          if (iflg == 3) r.w.d[0] = r.w.d[0] * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
           r.w.d[1] = VNU * R.alfd1;
-          r.sp = SUI * P.spfac;
+          r.sp = SUI * (1. + GI * P.pavp2);
+          r.spp = SUI * YI * P.pavp0;
         }
         r.vnu = VNU;
         r.mol = m;
@@ -1284,10 +1336,13 @@ __global__ void k_f4_compact(const F4Prep* __restrict__ prep, int64_t stride, co
       vbits[(int64_t)layer * stride + c] = __double_as_longlong(r.vnu);
       lbits[(int64_t)layer * stride + c] = __double_as_longlong(r.vnu + half);
       src[(int64_t)layer * stride + c] = t;
-      // SHRINQ zeroes SP < 1e-35; a group emits a non-CO2 / CO2 line when
-      // its strength sum of that kind is positive
+      // SHRINQ zeroes SP < 1e-35 (and SPP with it); a coupled line (SPP
+      // still nonzero) is a record of its own (4), else a group emits a
+      // non-CO2 / CO2 line when its strength sum of that kind is positive
       bool strong = !(r.sp < 1.0e-35);
-      flags[(int64_t)layer * stride + c] = (unsigned char)((strong && r.mol != 2 ? 1 : 0) | (strong && r.mol == 2 ? 2 : 0));
+      const bool coupled = strong && r.spp != 0.;
+      flags[(int64_t)layer * stride + c] =
+          (unsigned char)(coupled ? 4 : ((strong && r.mol != 2 ? 1 : 0) | (strong && r.mol == 2 ? 2 : 0)));
       if (r.vnu > P.v2l4) atomicMin((unsigned long long*)&cut[layer], (unsigned long long)c);
     }
   }
@@ -1373,6 +1428,7 @@ __global__ void __launch_bounds__(kWalkThreads)
   __shared__ short up[kLift][kWalkMax];     // up[k][b]: nxt applied 2^k times
   __shared__ short ends[kWalkMax];          // group ends of the call, in order
   __shared__ short pc1[kWalkMax + 1], pc2[kWalkMax + 1];  // flag counts before each line
+  __shared__ short pc4[kWalkMax + 1];                      // coupled lines before each line
   __shared__ unsigned char sf[kWalkMax];
   __shared__ int64_t civ[kRecWin + 1];      // stream offsets of records wbase .. wbase+kRecWin
   __shared__ unsigned long long wt64[kWalkThreads / 32 + 1];
@@ -1510,14 +1566,18 @@ __global__ void __launch_bounds__(kWalkThreads)
           on[q] = v < m && v >= e0 && x[q] == v;
         }
       }
-      // one scan: ends (bits 0-20), non-CO2 flags (21-41), CO2 flags (42-62)
+      // one scan, 16 bits a count (m <= kWalkMax < 2^16): ends, non-CO2
+      // flags, CO2 flags, coupled lines
+      auto packed = [](bool e, unsigned f) {
+        return (unsigned long long)e + ((unsigned long long)(f & 1u) << 16) +
+               ((unsigned long long)((f >> 1) & 1u) << 32) + ((unsigned long long)((f >> 2) & 1u) << 48);
+      };
       unsigned long long mine = 0;
 #pragma unroll
       for (int q = 0; q < kWalkPer; ++q) {
         const int v = tid * kWalkPer + q;
         const unsigned f = v < m ? sf[v] : 0u;
-        mine += (unsigned long long)on[q] + ((unsigned long long)(f & 1u) << 21) +
-                ((unsigned long long)((f >> 1) & 1u) << 42);
+        mine += packed(on[q], f);
       }
       unsigned long long ex;
       const unsigned long long tot = block_scan_excl<unsigned long long>(mine, wt64, &ex);
@@ -1527,32 +1587,34 @@ __global__ void __launch_bounds__(kWalkThreads)
         for (int q = 0; q < kWalkPer; ++q) {
           const int v = tid * kWalkPer + q;
           if (v < m) {
-            pc1[v] = (short)((run >> 21) & 0x1FFFFF);
-            pc2[v] = (short)((run >> 42) & 0x1FFFFF);
-            if (on[q]) ends[run & 0x1FFFFF] = (short)v;
-            const unsigned f = sf[v];
-            run += (unsigned long long)on[q] + ((unsigned long long)(f & 1u) << 21) +
-                   ((unsigned long long)((f >> 1) & 1u) << 42);
+            pc1[v] = (short)((run >> 16) & 0xFFFF);
+            pc2[v] = (short)((run >> 32) & 0xFFFF);
+            pc4[v] = (short)((run >> 48) & 0xFFFF);
+            if (on[q]) ends[run & 0xFFFF] = (short)v;
+            run += packed(on[q], sf[v]);
           }
         }
       }
       if (tid == 0) {
-        pc1[m] = (short)((tot >> 21) & 0x1FFFFF);
-        pc2[m] = (short)((tot >> 42) & 0x1FFFFF);
+        pc1[m] = (short)((tot >> 16) & 0xFFFF);
+        pc2[m] = (short)((tot >> 32) & 0xFFFF);
+        pc4[m] = (short)((tot >> 48) & 0xFFFF);
       }
       __syncthreads();
-      const int gcount = (int)(tot & 0x1FFFFF);
-      // which kinds each group emits, then the output slots; thread t owns
-      // groups t*kWalkPer + q
-      int kind[kWalkPer], cnt = 0;
+      const int gcount = (int)(tot & 0xFFFF);
+      // which kinds each group emits, then the output slots (its coupled
+      // lines first, then its sums); thread t owns groups t*kWalkPer + q
+      int kind[kWalkPer], ncp[kWalkPer], cnt = 0;
 #pragma unroll
       for (int q = 0; q < kWalkPer; ++q) {
         const int g = tid * kWalkPer + q;
         kind[q] = 0;
+        ncp[q] = 0;
         if (g < gcount) {
           const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g] + 1;
           kind[q] = (pc1[s1] > pc1[s0] ? 1 : 0) | (pc2[s1] > pc2[s0] ? 2 : 0);
-          cnt += (kind[q] & 1) + (kind[q] >> 1);
+          ncp[q] = pc4[s1] - pc4[s0];
+          cnt += (kind[q] & 1) + (kind[q] >> 1) + ncp[q];
         }
       }
       int excl;
@@ -1564,7 +1626,7 @@ __global__ void __launch_bounds__(kWalkThreads)
         if (g < gcount) {
           const int s0 = g == 0 ? 0 : ends[g - 1] + 1, s1 = ends[g];
           if (ng + g < stride) G[ng + g] = make_int4((int)(u0 + s0), (int)(u0 + s1), run, kind[q]);
-          run += (kind[q] & 1) + (kind[q] >> 1);
+          run += (kind[q] & 1) + (kind[q] >> 1) + ncp[q];
         }
       }
       ng += gcount;
@@ -1620,6 +1682,20 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
       for (int u = gr.x; u <= gr.y; ++u) {
         const F4Prep& r = pr[S[u]];
         const bool weak = r.sp < 1.0e-35;
+        if (!weak && r.spp != 0.) {  // a coupled line is not shrunk (SHRINQ :1566-1578)
+          ShrunkLine L;
+          L.vnu = r.vnu;
+          L.sp = r.sp;
+          L.w.f[0] = r.w.f[0];
+          L.w.f[1] = r.w.f[1];
+          L.w.f[2] = r.w.f[2];
+          L.w.f[3] = (float)r.spp;
+          L.w.f[4] = L.w.f[5] = 0.f;
+          L.mol = r.mol == 2 ? 2 : 0;
+          L.pad = 0;
+          O[slot++] = L;
+          continue;
+        }
         const double sp = weak ? 0.0 : r.sp;
         const float spf = weak ? 0.f : r.w.f[2];
         if (r.mol != 2) {
@@ -1656,6 +1732,18 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
     double SUMAL2 = 0., SUMAD2 = 0., SUMS2 = 0., SUMV2 = 0., SUMC2 = 0.;
     for (int u = gr.x; u <= gr.y; ++u) {
       const F4Prep& r = pr[S[u]];
+      if (!(r.sp < 1.0e-35) && r.spp != 0.) {  // a coupled line is not shrunk (SHRINQ :1566-1578)
+        ShrunkLine L;
+        L.vnu = r.vnu;
+        L.sp = r.sp;
+        L.w.d[0] = r.w.d[0];
+        L.w.d[1] = r.w.d[1];
+        L.w.d[2] = r.spp;
+        L.mol = r.mol == 2 ? 2 : 0;
+        L.pad = 0;
+        O[slot++] = L;
+        continue;
+      }
       double sp = r.sp < 1.0e-35 ? 0.0 : r.sp;
       if (r.mol != 2) {
         SUMV = SUMV + r.vnu * sp;
@@ -1705,8 +1793,10 @@ __global__ void k_f4_groupsum(const LayerPlan* __restrict__ plans, int layer0, c
 // range JMIN..JMAX and the offset of the nearest grid point take the
 // reference's FP64 arithmetic in both paths; the mixed path forms the
 // coefficients, which set no index, in FP32 and writes no FP64 record.
+// *dpt: CNVF4Q's DPTRAT = SPP / (SP * ALFV) of a coupled line (the mirror
+// record of a line below 25 cm-1 takes -SPP), else 0 (:366)
 template <bool Mixed>
-__device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, F4Rec* r, F4RecD* d) {
+__device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, F4Rec* r, F4RecD* d, double* dpt) {
   const double ZSQBND = 64. * 64.;
   const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
   const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
@@ -1749,6 +1839,8 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
     // CNVF4Q's CO2 pedestal (2 - x^2/BOUND^2) F4BND, else F4BND
     r->nfb0 = pairf(co2 ? -2.f * F4BND : -F4BND);
     r->fb2 = pairf(co2 ? F4BND / P.bndsq_f : 0.f);
+    const float spp = VNUI == L.vnu ? L.w.f[3] : -L.w.f[3];
+    *dpt = spp != 0.f ? (double)(spp / (SP * ALFAVI)) : 0.;
   } else {
     const int mc = (int)floor(XNUI / P.dvr4 + 0.5);
     r->nmc = pair(-(double)mc);
@@ -1782,13 +1874,16 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
     d->fbnd = F4BND;
     d->al2 = ALFLI2;
     d->alv2 = ALFVI2;
+    const double spp = VNUI == L.vnu ? L.w.d[2] : -L.w.d[2];
+    *dpt = spp != 0. ? spp / (L.sp * ALFAVI) : 0.;
   }
 }
 
 __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
                               int64_t stride, const int64_t* __restrict__ nsh, F4Rec* __restrict__ rec,
                               F4RecD* __restrict__ recd, int64_t rstride, int64_t* __restrict__ nrec,
-                              int64_t* __restrict__ nmirror, unsigned long long* __restrict__ stats) {
+                              int64_t* __restrict__ nmirror, unsigned long long* __restrict__ stats,
+                              double* __restrict__ cpl) {
   const int layer = blockIdx.y;
   const LayerPlan& P = plans[layer + layer0];
   const int64_t n = nsh[2 * (layer + layer0)] < 0 ? 0 : nsh[2 * (layer + layer0) + 1];
@@ -1801,8 +1896,10 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
     const ShrunkLine L = S[i];
     F4Rec r;
     F4RecD d;
-    if (P.mixed) f4_record<true>(P, L, L.vnu, &r, &d);
-    else f4_record<false>(P, L, L.vnu, &r, &d);
+    double dpt;
+    if (P.mixed) f4_record<true>(P, L, L.vnu, &r, &d, &dpt);
+    else f4_record<false>(P, L, L.vnu, &r, &d, &dpt);
+    if (cpl) cpl[(int64_t)layer * rstride + i] = dpt;
     // lines beyond the last point's reach, or without strength, add nothing
     if (L.vnu >= VNULST || (L.sp == 0. && (P.mixed ? L.w.f[3] == 0.f : L.w.d[2] == 0.))) {
       r.jmin = d.jmin = 1 << 30;
@@ -1824,11 +1921,13 @@ __global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, c
         continue;
       F4Rec r;
       F4RecD d;
-      if (P.mixed) f4_record<true>(P, L, -L.vnu, &r, &d);
-      else f4_record<false>(P, L, -L.vnu, &r, &d);
+      double dpt;
+      if (P.mixed) f4_record<true>(P, L, -L.vnu, &r, &d, &dpt);
+      else f4_record<false>(P, L, -L.vnu, &r, &d, &dpt);
       if (r.jmax >= r.jmin && n + nm < rstride) {
         R[n + nm] = r;
         if (!P.mixed) D[n + nm] = d;
+        if (cpl) cpl[(int64_t)layer * rstride + n + nm] = dpt;
         nm++;
         atomicAdd(&stats[(layer + layer0) * kStatsPerLayer + 6], (unsigned long long)(r.jmax - r.jmin + 1));
       }

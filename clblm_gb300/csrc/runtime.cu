@@ -94,7 +94,11 @@ struct clblm_handle {
   cudaStream_t stream = nullptr;
   int64_t nlines = 0;
   DevBuf lines[9];
+  DevBuf vkey;  // the centres as sort keys (h_vnu)
+  // line centres as sort keys: a coefficient record (IFLG < 0) takes its
+  // line's centre, so that the keys ascend
   std::vector<double> h_vnu;
+  bool has_cpl = false;  // the list holds coupled lines (IFLG 1 or 3)
   std::vector<int32_t> h_iflg, h_mol;
   double shiftmax = 0.;
   bool has_cont = false;
@@ -107,6 +111,8 @@ struct clblm_handle {
   // workspace
   DevBuf plans, vft, prep, qpanel, rec, recd, ranges, od, r4, absrb, stats, alfvmax, blockmax, nlines_d;
   DevBuf isotab;  // isotopologue rows of the planned layers
+  DevBuf linecpl;  // SPPSP of the coupled lines, per line of each layer
+  DevBuf f4cpl, f4cpll, f4ncpl;  // far wings: DPTRAT per record, the coupled records' list and counts
   DevBuf f4prep, f4sh, f4nout, f4rec, f4recd, f4nrec, f4nmir, f4pm, f4sm, err;
   DevBuf pblk, bv1, bn, bm0, bfac;
   DevBuf gpm, gsm;  // per grid record bounds of the panel kernel
@@ -132,7 +138,8 @@ struct clblm_handle {
                               &f4nmir,    &f4pm,     &f4sm,      &err,     &outbuf,  &pblk,   &bv1,     &bn,
                               &bm0,       &bfac,     &f4blk,     &f4ntot,  &f4cidx,  &f4vb,   &f4lb,    &f4src,
                               &f4flag,    &f4cut,    &f4grp,     &f4nxt,   &ragg,    &segpool, &gpm,    &gsm,
-                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk,    &jvjp,   &isotab};
+                              &reclo,     &jprof,    &jod,       &jmap,    &jjobs,   &jblk,    &jvjp,   &isotab,
+                              &linecpl,   &f4cpl,    &f4cpll,    &f4ncpl};
     for (auto& b : rt) v.push_back(&b);
     for (auto& b : imap) v.push_back(&b);
     v.push_back(&rtseg);
@@ -377,11 +384,21 @@ int load_lines(clblm_handle* h, const clblm_lines_t* L) {
   if (!L || L->n < 0 || (L->n > 0 && (!L->vnu || !L->sp || !L->alfa || !L->epp || !L->mol || !L->hwhm ||
                                       !L->tmpalf || !L->pshift || !L->iflg)))
     return set_err(h, CLBLM_ERR_ARG, "bad line list");
-  for (int64_t i = 1; i < L->n; ++i)
-    if (L->vnu[i] < L->vnu[i - 1]) return set_err(h, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+  // the lines (IFLG >= 0) must be sorted; a record with IFLG < 0 (the
+  // coupling coefficients after a coupled line) carries no centre
   int64_t n = L->n;
+  h->h_vnu.assign(n, 0.);
+  h->has_cpl = false;
+  double key = -1e300;
+  for (int64_t i = 0; i < n; ++i) {
+    if (L->iflg[i] >= 0) {
+      if (L->vnu[i] < key) return set_err(h, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+      key = L->vnu[i];
+    }
+    if (L->iflg[i] == 1 || L->iflg[i] == 3) h->has_cpl = true;
+    h->h_vnu[i] = key;
+  }
   h->nlines = n;
-  h->h_vnu.assign(L->vnu, L->vnu + n);
   h->h_iflg.assign(L->iflg, L->iflg + n);
   h->h_mol.assign(L->mol, L->mol + n);
   double sm = 0.;
@@ -393,6 +410,9 @@ int load_lines(clblm_handle* h, const clblm_lines_t* L) {
     CUDA_TRY(h, h->lines[k].ensure(std::max<size_t>(1, n * esz[k])));
     if (n) CUDA_TRY(h, cudaMemcpyAsync(h->lines[k].p, src[k], n * esz[k], cudaMemcpyHostToDevice, h->stream));
   }
+  CUDA_TRY(h, h->vkey.ensure(std::max<size_t>(1, n * sizeof(double))));
+  if (n)
+    CUDA_TRY(h, cudaMemcpyAsync(h->vkey.p, h->h_vnu.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return CLBLM_OK;
 }
@@ -582,6 +602,29 @@ int plan_layer(clblm_handle* h, const clblm_layer_t* lay, const clblm_grid_t* g,
   P.pavp0 = lay->pave / kP0;
   P.pavp2 = P.pavp0 * P.pavp0;
   P.spfac = 1. + 0. * P.pavp2;
+  {
+    // line-coupling temperature intervals: LNCORQ's lower node (the last of
+    // the first three below TAVE) and LINF4Q's upper node (the first at or
+    // above TAVE, between the second and the fourth)
+    static const double TEMPLC[5] = {0., 200.0, 250.0, 296.0, 340.0};
+    const double T = lay->tave;
+    int ilc = 1;
+    for (int il = 1; il <= 3; ++il) {
+      ilc = il;
+      if (T < TEMPLC[ilc + 1]) break;
+    }
+    P.lc_ilc = ilc;
+    P.lc_rectlc = 1.0 / (TEMPLC[ilc + 1] - TEMPLC[ilc]);
+    P.lc_tmpdif = T - TEMPLC[ilc];
+    int ilc4;
+    for (ilc4 = 1; ilc4 <= 4; ++ilc4)
+      if (T <= TEMPLC[ilc4]) break;
+    if (ilc4 == 1) ilc4 = 2;
+    if (ilc4 == 5) ilc4 = 4;
+    P.lc4_ilc = ilc4;
+    P.lc4_rectlc = 1.0 / (TEMPLC[ilc4] - TEMPLC[ilc4 - 1]);
+    P.lc4_tmpdif = T - TEMPLC[ilc4];
+  }
   P.jrad = JRAD;
   P.ilnflg = c->line_rejec ? 0 : -1;
   P.dptmn = c->dptmin;
@@ -974,7 +1017,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   k_f4_lineinit<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
       dplans, first, h->f4sh.as<ShrunkLine>(), f4stride, h->f4nout.as<int64_t>(), h->f4rec.as<F4Rec>(),
       h->f4recd.as<F4RecD>(), rstride, h->f4nrec.as<int64_t>(), h->f4nmir.as<int64_t>(),
-      h->stats.as<unsigned long long>());
+      h->stats.as<unsigned long long>(), h->has_cpl ? h->f4cpl.as<double>() : nullptr);
   h->launches++;
   k_f4_bounds<<<count, 1024, 0, st>>>(h->f4rec.as<F4Rec>(), rstride, h->f4nrec.as<int64_t>(), first,
                                       h->f4pm.as<int>(), h->f4sm.as<int>());
@@ -993,6 +1036,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     fa.smin_jmin = h->f4sm.as<int>();
     fa.r4_all = h->r4.p;
     fa.err = h->err.as<int>();
+    fa.cpl = h->f4cpl.as<const double>();
     dim3 grid((unsigned)((maxr4 + 2 + kF4Tile - 1) / kF4Tile), count);
     auto f4 = [&](int v) {  // records per stage: 64, 128, 256
       if (plain) {
@@ -1013,6 +1057,14 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
     f4(tv);
+    if (h->has_cpl) {  // the coupled records' dispersion terms
+      h->launches += 2;
+      k_f4_cpl_list<<<count, 1024, 0, st>>>(fa, h->f4cpll.as<int64_t>(), h->f4ncpl.as<int64_t>());
+      dim3 gc((unsigned)((maxr4 + 255) / 256), count);
+      if (plain) k_f4_cpl<true><<<gc, 256, 0, st>>>(fa, h->f4cpll.as<int64_t>(), h->f4ncpl.as<int64_t>());
+      else k_f4_cpl<false><<<gc, 256, 0, st>>>(fa, h->f4cpll.as<int64_t>(), h->f4ncpl.as<int64_t>());
+      CUDA_TRY(h, cudaGetLastError());
+    }
     CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   }
   CUDA_TRY(h, cudaEventRecord(h->join_ev, st));
@@ -1035,7 +1087,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   h->launches++;
   k_line_records<<<dim3((unsigned)std::min<int64_t>(nagg, 8192), count), kRecBlock, 0, st>>>(
       dplans, first, h->vft.as<double>(), h->prep.as<LinePrep>(), h->qpanel.as<int>(), lstride, h->rec.as<GridRec>(),
-      h->recd.as<GridRecD>(), h->reclo.as<GridRecLo>(), h->lines[0].as<double>(), h->stats.as<unsigned long long>(),
+      h->recd.as<GridRecD>(), h->reclo.as<GridRecLo>(), h->linecpl.as<double>(), h->stats.as<unsigned long long>(),
       h->alfvmax.as<double>(), h->ragg.as<int>(), h->ragg.as<int>() + (int64_t)3 * count * nagg, nagg);
   h->launches++;
   k_rec_carry<<<3 * count, 1024, 0, st>>>(dplans, first, h->ragg.as<int>(),
@@ -1048,7 +1100,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   int maxp = 0;
   for (int k = 0; k < count; ++k) maxp = std::max(maxp, hps[first + k].P.npanels);
   h->launches++;
-  k_panel_ranges<<<dim3((maxp + 127) / 128, count), 128, 0, st>>>(dplans, first, h->lines[0].as<double>(),
+  k_panel_ranges<<<dim3((maxp + 127) / 128, count), 128, 0, st>>>(dplans, first, h->vkey.as<double>(),
                                                                    h->alfvmax.as<double>(), h->shiftmax,
                                                                    h->ranges.as<int64_t>(), pstride);
   PanelArgs pa;
@@ -1059,6 +1111,7 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   pa.recd = h->recd.as<GridRecD>();
   pa.reclo = h->reclo.as<GridRecLo>();
   pa.prep = h->prep.as<LinePrep>();
+  pa.cpl = h->linecpl.as<const double>();
   pa.stride = lstride;
   pa.ranges = h->ranges.as<int64_t>();
   pa.panel_stride = pstride;
@@ -1217,6 +1270,10 @@ cudaError_t ws_alloc(clblm_handle* h, const WsDims& d, int nL, int64_t vftt, int
   } while (0)
   WS_ENSURE(h->plans.ensure(sizeof(LayerPlan) * nL));
   WS_ENSURE(h->isotab.ensure(sizeof(IsoRow) * (size_t)std::max<int64_t>(isot, 1)));
+  WS_ENSURE(h->linecpl.ensure(h->has_cpl ? sizeof(double) * d.lsc : 256));
+  WS_ENSURE(h->f4cpl.ensure(h->has_cpl ? sizeof(double) * (d.fsc + 4096 * d.cnt) : 256));
+  WS_ENSURE(h->f4cpll.ensure(h->has_cpl ? sizeof(int64_t) * (d.fsc + 4096 * d.cnt) : 256));
+  WS_ENSURE(h->f4ncpl.ensure(sizeof(int64_t) * std::max(nL, 1)));
   WS_ENSURE(h->vft.ensure(sizeof(double) * vftt));
   WS_ENSURE(h->prep.ensure(sizeof(LinePrep) * d.lsc));
   WS_ENSURE(h->qpanel.ensure(sizeof(int) * d.lsc));
@@ -1273,7 +1330,8 @@ std::vector<DevBuf*> ws_buffers(clblm_handle* h) {
           &h->blockmax, &h->nlines_d, &h->f4prep, &h->f4sh, &h->f4nout, &h->f4blk, &h->f4ntot, &h->f4cidx,
           &h->f4vb,   &h->f4lb,   &h->f4src,  &h->f4flag,   &h->f4nxt,  &h->f4cut,  &h->f4grp,  &h->f4rec,
           &h->f4recd, &h->f4nrec, &h->f4nmir, &h->f4pm,     &h->f4sm,   &h->err,    &h->segpool, &h->pblk,
-          &h->bv1,    &h->bn,     &h->bm0,    &h->bfac,   &h->isotab};
+          &h->bv1,    &h->bn,     &h->bm0,    &h->bfac,   &h->isotab, &h->linecpl, &h->f4cpl, &h->f4cpll,
+          &h->f4ncpl};
 }
 
 // Frees every work buffer of the handle (all but the line list, the shape
@@ -1406,8 +1464,8 @@ int check_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int coun
   }
   for (int k = first; k < first + count; ++k) {
     const unsigned long long* s = &stats[k * kStatsPerLayer];
-    if (s[4]) return set_err(h, CLBLM_ERR_UNSUPPORTED, "layer %d: %llu lines need isotopologue/line-coupling/drop "
-                             "rules that are not on this path", k + 1, s[4]);
+    if (s[4]) return set_err(h, CLBLM_ERR_UNSUPPORTED, "layer %d: %llu lines have widths outside the Voigt tables or "
+                             "would be dropped at a later record's panel, rules not on this path", k + 1, s[4]);
     if (nout[2 * k] == -2)
       return set_err(h, CLBLM_ERR_UNSUPPORTED, "far-wing line window: no line above V2L4 within the prepared range");
     if (nout[2 * k] < 0)
@@ -3226,8 +3284,8 @@ int batch_check(clblm_handle* h, const std::vector<int>& job_prof, std::vector<i
     h->acc_fnq += (int64_t)s[5];
     h->acc_f4q += (int64_t)s[6];
     int rc = CLBLM_OK;
-    if (s[4]) rc = set_err(h, CLBLM_ERR_UNSUPPORTED, "profile %d: %llu lines need isotopologue/line-coupling "
-                           "rules that are not on this path", job_prof[k], s[4]);
+    if (s[4]) rc = set_err(h, CLBLM_ERR_UNSUPPORTED, "profile %d: %llu lines have widths outside the Voigt "
+                           "tables or would be dropped at a later record's panel", job_prof[k], s[4]);
     else if (nout[2 * k] == -2)
       rc = set_err(h, CLBLM_ERR_UNSUPPORTED, "profile %d: far-wing line window ends outside the prepared range",
                    job_prof[k]);

@@ -69,6 +69,53 @@ def line_list(n, v1, v2, seed, mols=(1,), isotopologues=False):
                  pshift=pshift.astype(np.float32), iflg=np.zeros(n, np.int32))
 
 
+# temperatures of the line-coupling coefficients (LNCORQ's TEMPLC)
+TEMPLC = (200.0, 250.0, 296.0, 340.0)
+
+
+def with_coupling(lines, idx, iflg=1, a=(0.02, 0.015, 0.01, 0.008), b=(1.0e-3, 8.0e-4, 5.0e-4, 4.0e-4)):
+    """The line list with line-coupling coefficients for the lines idx: each
+    gets IFLG = iflg (1: first-order coupling Y and second-order G; 3:
+    reduced widths GAMMA1, GAMMA2; one value, or one per line) and is
+    followed by a coefficient record
+    (IFLG -1) holding a = Y or GAMMA1 at the four TEMPLC in VNU, ALFA, MOL
+    (the bits of a float) and TMPALF, and b = G or GAMMA2 in SP, EPP, HWHM
+    and PSHIFT, as LNFL writes them (LNCORQ clblm_ODLAY.f90:1822-1832).
+    a and b: four values, or one row of four per line."""
+    from .capi_types import Lines
+    idx = np.asarray(idx, dtype=np.int64)
+    order = np.argsort(idx, kind="stable")
+    idx = idx[order]
+    m = len(idx)
+    iflg = np.broadcast_to(np.asarray(iflg, dtype=np.int32), (m,))[order] if np.ndim(iflg) else np.full(m, iflg, np.int32)
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    a = a[order] if a.ndim == 2 else a
+    b = b[order] if b.ndim == 2 else b
+    a = np.broadcast_to(np.asarray(a, dtype=np.float64), (m, 4))
+    b = np.broadcast_to(np.asarray(b, dtype=np.float64), (m, 4))
+    total = lines.n + m
+    pos = idx + np.arange(m) + 1              # the coefficient records in the new list
+    keep = np.ones(total, bool)
+    keep[pos] = False
+    out = {}
+    for name, dt in Lines.FIELDS:
+        arr = np.zeros(total, dtype=dt)
+        arr[keep] = getattr(lines, name)
+        out[name] = arr
+    out["iflg"][pos - 1] = iflg
+    out["iflg"][pos] = -1
+    out["vnu"][pos] = a[:, 0]
+    out["alfa"][pos] = a[:, 1].astype(np.float32)
+    out["mol"][pos] = a[:, 2].astype(np.float32).view(np.int32)
+    out["tmpalf"][pos] = a[:, 3].astype(np.float32)
+    out["sp"][pos] = b[:, 0].astype(np.float32)
+    out["epp"][pos] = b[:, 1].astype(np.float32)
+    out["hwhm"][pos] = b[:, 2].astype(np.float32)
+    out["pshift"][pos] = b[:, 3].astype(np.float32)
+    return Lines(**out)
+
+
 def continuum(seed=7):
     """Smooth synthetic self/foreign coefficients on the MT_CKD 10 cm-1 grid."""
     rng = np.random.Generator(np.random.PCG64(1000 + seed))

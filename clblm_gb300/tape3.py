@@ -38,8 +38,9 @@ def write_tape3(path, lines, title="CLBLM GB300"):
             sumstr[m - 1] = float(lines.sp[sel].astype(np.float64).sum())
     zeros = np.zeros(64, np.int32)
     nblocks = (n + NLINEREC - 1) // NLINEREC
+    key = lines.keys()  # the line centres; a coupling-coefficient record takes its line's
     header = (hlinid + bmolid + molcnt.tobytes() + zeros.tobytes() + zeros.tobytes() + sumstr.tobytes()
-              + struct.pack("<i", len(mols)) + struct.pack("<ff", float(lines.vnu[0]), float(lines.vnu[-1]))
+              + struct.pack("<i", len(mols)) + struct.pack("<ff", float(key[0]), float(key[-1]))
               + struct.pack("<iiiii", n, 0, 0, nblocks, nblocks) + _chars("") + _chars(""))
     with open(path, "wb") as f:
         _record(f, header)
@@ -58,5 +59,5 @@ def write_tape3(path, lines, title="CLBLM GB300"):
                     + np.zeros(3 * MXBRDMOL * NLINEREC, "<f4").tobytes()
                     + np.zeros(NLINEREC, "<f4").tobytes())
             assert len(body) == 4 * _BLOCK_WORDS  # 39*250 words, VNU two per line
-            _record(f, struct.pack("<ddii", float(lines.vnu[lo]), float(lines.vnu[hi - 1]), k, len(body) // 4))
+            _record(f, struct.pack("<ddii", float(key[lo]), float(key[hi - 1]), k, len(body) // 4))
             _record(f, body)

@@ -64,7 +64,7 @@ enum {
 
 /* Line list in structure-of-arrays form with TAPE3 precision
  * (INPUT_BLOCK, clblm_LineData.f90:52-64): vnu is binary64, the rest binary32
- * or int32.  Lines must be sorted by vnu (ascending). */
+ * or int32.  Lines (iflg >= 0) must be sorted by vnu (ascending). */
 typedef struct {
   int64_t        n;
   const double  *vnu;     /* line centre [cm-1]                                */
@@ -75,7 +75,14 @@ typedef struct {
   const float   *hwhm;    /* self-broadened HWHM at 296 K [cm-1/atm]           */
   const float   *tmpalf;  /* temperature exponent of the widths                */
   const float   *pshift;  /* pressure shift [cm-1/atm]                         */
-  const int32_t *iflg;    /* line-coupling flag; lines with iflg < 0 skipped   */
+  const int32_t *iflg;    /* line-coupling flag: 0 a plain line; 1 a coupled line
+                           * (first-order Y, second-order G), 3 one with
+                           * reduced widths (GAMMA1, GAMMA2); < 0 the record
+                           * after a coupled line holding its coefficients at
+                           * 200, 250, 296, 340 K in VNU, ALFA, MOL (float
+                           * bits), TMPALF and SP, EPP, HWHM, PSHIFT, as LNFL
+                           * writes them; such records are not lines and need
+                           * not be sorted */
 } clblm_lines_t;
 
 /* MT_CKD-style H2O continuum coefficient table on a uniform grid

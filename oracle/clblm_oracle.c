@@ -425,6 +425,30 @@ static int molec(ocl_session *s, molec_t *M, const clblm_layer_t *lay, double PA
 }
 
 /* ======================================================================
+ * Line coupling: the first-order coupling coefficient Y and the second-order
+ * G (IFLG 1), or the width reductions GAMMA1, GAMMA2 (IFLG 3), at the four
+ * temperatures TEMPLC, carried in the line-file record after the coupled
+ * line (LNCORQ clblm_ODLAY.f90:1822-1846, LINF4Q clblm_ODLAY_LineF4.f90:
+ * 960-984): A(1..4) = VNU, ALFA, the bits of MOL read as a float, TMPALF;
+ * B(1..4) = SP, EPP, HWHM, PSHIFT.
+ * ====================================================================== */
+static const double TEMPLC[5] = {0., 200.0, 250.0, 296.0, 340.0};
+
+static void lc_record(double vnu, double sp, double alfa, double epp, int32_t mol, double hwhm, double tmpalf,
+                      double pshift, double A[5], double Bc[5]) {
+  float amol;
+  memcpy(&amol, &mol, sizeof amol);
+  A[1] = vnu;
+  Bc[1] = sp;
+  A[2] = alfa;
+  Bc[2] = epp;
+  A[3] = (double)amol;
+  Bc[3] = hwhm;
+  A[4] = tmpalf;
+  Bc[4] = pshift;
+}
+
+/* ======================================================================
  * XINT, clblm_Spectrum.f90:874-915 (ONEPL/ONEMI of clblm_ConstParam).
  * A and R3 are 1-based.
  * ====================================================================== */
@@ -1083,10 +1107,24 @@ static void shrinq(shrunk_rec *S, int *ILO, int *IHI, double DVR4) {
   *IHI = J;
 }
 
+/* The line file: its records of 250 entries, and the centres as the block
+ * headers' VMIN/VMAX see them (a coupling-coefficient record, IFLG < 0,
+ * carries no centre: it takes its line's). */
 typedef struct {
   const clblm_lines_t *L;
   int64_t nrec;
+  double *key;
 } linefile_t;
+
+static double *line_keys(const clblm_lines_t *L) {
+  double *k = (double *)malloc(sizeof(double) * (size_t)(L->n > 0 ? L->n : 1));
+  double run = -1e300;
+  for (int64_t i = 0; i < L->n; ++i) {
+    if (L->iflg[i] >= 0) run = L->vnu[i];
+    k[i] = run;
+  }
+  return k;
+}
 
 static int64_t rec_first(int64_t r) { return r * CLBLM_LINES_PER_RECORD; }
 static int64_t rec_end(const linefile_t *F, int64_t r) {
@@ -1103,12 +1141,22 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
   double BETA = RADCN2 / TAVE, BETA0 = RADCN2 / TEMP0, BETACR = BETA - BETA0;
   double VLO = V1L4, VHI = V2L4;
   (void)WTOT;
+  const double PAVP0 = PAVE / P0, PAVP2 = PAVP0 * PAVP0;
+  /* LINF4Q's coupling-temperature interval (:860-866): the first TEMPLC at
+   * or above TAVE, between the second and the fourth */
+  int ILC;
+  for (ILC = 1; ILC <= 4; ++ILC)
+    if (TAVE <= TEMPLC[ILC]) break;
+  if (ILC == 1) ILC = 2;
+  if (ILC == 5) ILC = 4;
+  const double RECTLC = 1.0 / (TEMPLC[ILC] - TEMPLC[ILC - 1]);
+  const double TMPDIF = TAVE - TEMPLC[ILC];
   shrunk_rec *S = (shrunk_rec *)calloc(1, sizeof(shrunk_rec));
   int IJ = 0, ILO = 1, IHI = 0, IEOF = 0;
   int64_t rec = 0;
   for (;;) { /* label 30: RDLNFL */
     /* RDLNFL: skip records with VMAX < VLO */
-    while (rec < F->nrec && L->vnu[rec_end(F, rec) - 1] < VLO) rec++;
+    while (rec < F->nrec && F->key[rec_end(F, rec) - 1] < VLO) rec++;
     if (rec >= F->nrec) {
       IEOF = 1;
       goto L60;
@@ -1132,6 +1180,27 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
         if (SUI == 0.) continue;
         if (L->vnu[i] < VLO) continue;
         IJ = IJ + 1;
+        double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
+        const int IFLAG = L->iflg[i];
+        if ((IFLAG == 1 || IFLAG == 3) && i + 1 < L->n) {
+          double A[5], Bc[5];
+          const int64_t k = i + 1;
+          double alfa1 = (double)L->alfa[k];
+          const int m1 = L->mol[k] % 100;
+          if (m1 == 7 && L->iflg[k] >= 0) alfa1 = (alfa1 - 0.21 * (double)L->hwhm[k]) / (1.0 - 0.21);
+          if (m1 == 22 && L->iflg[k] >= 0) alfa1 = (alfa1 - 0.79 * (double)L->hwhm[k]) / (1.0 - 0.79);
+          lc_record(L->vnu[k], (double)L->sp[k], alfa1, (double)L->epp[k], L->mol[k], (double)L->hwhm[k],
+                    (double)L->tmpalf[k], (double)L->pshift[k], A, Bc);
+          const double SLOPEY = (A[ILC] - A[ILC - 1]) * RECTLC;
+          const double SLOPEG = (Bc[ILC] - Bc[ILC - 1]) * RECTLC;
+          if (IFLAG == 1) {
+            YI = A[ILC] + SLOPEY * TMPDIF;
+            GI = Bc[ILC] + SLOPEG * TMPDIF;
+          } else {
+            GAMMA1 = A[ILC] + SLOPEY * TMPDIF;
+            GAMMA2 = Bc[ILC] + SLOPEG * TMPDIF;
+          }
+        }
         S->IDX[IJ] = i;
         S->VNU[IJ] = L->vnu[i] + RHORAT * pshift;
         S->ALFA[IJ] = alfa;
@@ -1145,9 +1214,10 @@ static int linf4q(ocl_session *s, const linefile_t *F, const molec_t *M, double 
         double ALFA0I = S->ALFA[IJ] * TMPCOR;
         double HWHMSI = (double)L->hwhm[i] * TMPCOR;
         S->ALFA[IJ] = ALFA0I * (RHORAT - M->RHOSLF[M_]) + HWHMSI * M->RHOSLF[M_];
+        if (IFLAG == 3) S->ALFA[IJ] = S->ALFA[IJ] * (1.0 - GAMMA1 * PAVP0 - GAMMA2 * PAVP2);
         S->EPP[IJ] = S->VNU[IJ] * M->ALFD1[M_][ISO];
-        S->SP[IJ] = SUI * (1. + 0. * (PAVE / P0) * (PAVE / P0));
-        S->SPP[IJ] = SUI * 0. * (PAVE / P0);
+        S->SP[IJ] = SUI * (1. + GI * PAVP2);
+        S->SPP[IJ] = SUI * YI * PAVP0;
         if (S->VNU[IJ] > VHI) {
           IEOF = 1;
           goto L60;
@@ -1475,6 +1545,15 @@ static int hiracq(ocl_session *s, hirac_args *a) {
   double RHORAT = (PAVE / P0) * (TEMP0 / TAVE);
   double PAVP0 = PAVE / P0;
   double PAVP2 = PAVP0 * PAVP0;
+  /* LNCORQ's coupling-temperature interval (:1713-1721): the last TEMPLC
+   * below TAVE among the first three */
+  int ILC = 1;
+  for (int IL = 1; IL <= 3; ++IL) {
+    ILC = IL;
+    if (TAVE < TEMPLC[ILC + 1]) break;
+  }
+  const double RECTLC = 1.0 / (TEMPLC[ILC + 1] - TEMPLC[ILC]);
+  const double TMPDIF = TAVE - TEMPLC[ILC];
 
   /* RDLIN state; bufb: line-list index of the buffer's first line, panel_no:
    * panels written so far (the trace) */
@@ -1490,14 +1569,14 @@ static int hiracq(ocl_session *s, hirac_args *a) {
     {
       IDATA = 0;
       if (ILO <= 0) rec = 0;
-      while (rec < a->F->nrec && L->vnu[rec_end(a->F, rec) - 1] < VBOT) rec++;
+      while (rec < a->F->nrec && a->F->key[rec_end(a->F, rec) - 1] < VBOT) rec++;
       if (rec >= a->F->nrec) {
         IEOF = 1;
         goto L80;
       }
       int64_t b = rec_first(rec), e = rec_end(a->F, rec);
       int NREC = (int)(e - b);
-      double VMIN = L->vnu[b];
+      double VMIN = a->F->key[b];
       bufb = b;
       rec++;
       for (int i = 1; i <= NREC; ++i) {
@@ -1514,6 +1593,26 @@ static int hiracq(ocl_session *s, hirac_args *a) {
         int m = B->MOL[i] % 100;
         if (m == 7 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.21 * B->HWHMS[i]) / (1.0 - 0.21);
         if (m == 22 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.79 * B->HWHMS[i]) / (1.0 - 0.79);
+      }
+      {
+        /* the coupling coefficients of the block's last line: the next line
+         * of the list (the reference's buffer would hold a stale record) */
+        const int i = NREC + 1;
+        const int64_t k = e < L->n ? e : L->n - 1;
+        B->IFLG[i] = L->iflg[k];
+        B->VNU[i] = L->vnu[k];
+        B->SP[i] = (double)L->sp[k];
+        B->ALFA0[i] = (double)L->alfa[k];
+        B->EPP[i] = (double)L->epp[k];
+        B->MOL[i] = L->mol[k];
+        B->HWHMS[i] = (double)L->hwhm[k];
+        B->TMPALF[i] = (double)L->tmpalf[k];
+        B->PSHIFT[i] = (double)L->pshift[k];
+        const int m = B->MOL[i] % 100;
+        if (m == 7 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.21 * B->HWHMS[i]) / (1.0 - 0.21);
+        if (m == 22 && B->IFLG[i] >= 0) B->ALFA0[i] = (B->ALFA0[i] - 0.79 * B->HWHMS[i]) / (1.0 - 0.79);
+        if (e >= L->n) B->SP[i] = B->VNU[i] = B->ALFA0[i] = B->EPP[i] = B->HWHMS[i] = B->TMPALF[i] = B->PSHIFT[i] = 0.;
+        if (e >= L->n) B->MOL[i] = 0;
       }
       ILO = 1;
       int IJ = 0;
@@ -1545,21 +1644,33 @@ static int hiracq(ocl_session *s, hirac_args *a) {
       if (!is_selected(M, m)) goto L25;
       if (m > MXMOL || m < 1) goto L25;
       if (ISO > MAXISO[m - 1]) goto L25;
-      if (IFLAG == 1 || IFLAG == 3) {
-        rc = fail(s, CLBLM_ERR_UNSUPPORTED, "line coupling (IFLG=%d)", IFLAG);
-        goto done;
-      }
       B->MOL[I] = m;
       {
         double SUI = B->SP[I] * M->WK[m];
         if (JRAD == 1) SUI = SUI * ocl_radfn(B->VNU[I], XKT);
         if (SUI == 0.) goto L25;
         NLIN++;
+        double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
+        if (IFLAG == 1 || IFLAG == 3) {
+          double A[5], Bc[5];
+          lc_record(B->VNU[I + 1], B->SP[I + 1], B->ALFA0[I + 1], B->EPP[I + 1], B->MOL[I + 1], B->HWHMS[I + 1],
+                    B->TMPALF[I + 1], B->PSHIFT[I + 1], A, Bc);
+          const double SLOPEA = (A[ILC + 1] - A[ILC]) * RECTLC;
+          const double SLOPEB = (Bc[ILC + 1] - Bc[ILC]) * RECTLC;
+          if (IFLAG == 1) {
+            YI = A[ILC] + SLOPEA * TMPDIF;
+            GI = Bc[ILC] + SLOPEB * TMPDIF;
+          } else {
+            GAMMA1 = A[ILC] + SLOPEA * TMPDIF;
+            GAMMA2 = Bc[ILC] + SLOPEB * TMPDIF;
+          }
+        }
         B->VNU[I] = B->VNU[I] + RHORAT * B->PSHIFT[I];
         double TMPCOR = pow(TRATIO, B->TMPALF[I]);
         double ALFA0I = B->ALFA0[I] * TMPCOR;
         double HWHMSI = B->HWHMS[I] * TMPCOR;
         double ALFL = ALFA0I * (RHORAT - M->RHOSLF[m]) + HWHMSI * M->RHOSLF[m];
+        if (IFLAG == 3) ALFL = ALFL * (1.0 - GAMMA1 * PAVP0 - GAMMA2 * PAVP2);
         double ALFAD = B->VNU[I] * M->ALFD1[m][ISO];
         double ZETA = ALFL / (ALFL + ALFAD);
         B->ZETAI[I] = ZETA;
@@ -1582,8 +1693,8 @@ static int hiracq(ocl_session *s, hirac_args *a) {
         if (B->EPP[I] <= -1.001) B->EPP[I] = fabs(B->EPP[I]);
         if (B->EPP[I] > -0.999)
           SUI = SUI * M->SCOR[m][ISO] * exp(-B->EPP[I] * BETACR) * (1. + exp(-B->VNU[I] / XKT));
-        B->SP[I] = SUI * (1. + 0. * PAVP2);
-        double SPPI = SUI * 0. * PAVP0;
+        B->SP[I] = SUI * (1. + GI * PAVP2);
+        double SPPI = SUI * YI * PAVP0;
         B->SPPSP[I] = SPPI / B->SP[I];
         B->EPP[I] = 0.0;
         if (IFLAG == 0 && (a->ILNFLG == 0 || a->ILNFLG == 1)) {
@@ -1608,8 +1719,9 @@ static int hiracq(ocl_session *s, hirac_args *a) {
     /* ---- label 70: CNVFNQ ---- */
   L70:
     {
-      double CLC1 = 4. / ((double)(NX1 - 1));
-      (void)CLC1;
+      const double CLC1 = 4. / ((double)(NX1 - 1));
+      const double CLC2 = 16. / ((double)(NX1 - 1));
+      const double CLC3 = 64. / ((double)(NX1 - 1));
       double WAVDXF = DV / DXF1;
       double HWDXF = HWF1 / DXF1;
       double CONF2 = DV / DVR2;
@@ -1670,6 +1782,29 @@ static int hiracq(ocl_session *s, hirac_args *a) {
             R3[J3] = R3[J3] + STRFA3 * F3[IZ3];
             R2[J2] = R2[J2] + STRFA2 * F2[IZ2];
             R1[J1] = R1[J1] + STRFA1 * F1[IZ1] + STRDA * FG[IZ1] + STRVRA * XVER[IZ1];
+          }
+          if (B->SPPSP[I] != 0.) {
+            /* line coupling (:2195-2239): the dispersion term, the shape
+             * times the distance ZF from the centre */
+            const double DPTRAT = B->SPPSP[I];
+            STRFA3 = STRFA3 * CLC3 * DPTRAT;
+            STRFA2 = STRFA2 * CLC2 * DPTRAT;
+            STRFA1 = STRFA1 * CLC1 * DPTRAT;
+            STRDA = STRDA * CLC1 * DPTRAT;
+            STRVRA = STRVRA * CLC1 * DPTRAT;
+            for (int J1 = JMIN1; J1 <= JMAX1; ++J1) {
+              int J2 = J1 - J2SHFT;
+              int J3 = J1 - J3SHFT;
+              ZF3L = ZF3L + ZSLOPE;
+              ZF2L = ZF2L + ZSLOPE;
+              ZF1L = ZF1L + ZSLOPE;
+              int IZ3 = (int)(fabs(ZF3L) + 1.5);
+              int IZ2 = (int)(fabs(ZF2L) + 1.5);
+              int IZ1 = (int)(fabs(ZF1L) + 1.5);
+              R3[J3] = R3[J3] + STRFA3 * F3[IZ3] * ZF3L;
+              R2[J2] = R2[J2] + STRFA2 * F2[IZ2] * ZF2L;
+              R1[J1] = R1[J1] + (STRFA1 * F1[IZ1] + STRDA * FG[IZ1] + STRVRA * XVER[IZ1]) * ZF1L;
+            }
           }
         }
         ILAST = IHI;
@@ -2009,8 +2144,14 @@ static int odlay_checked(ocl_session *s, const clblm_lines_t *L, const clblm_con
   s->err[0] = 0;
   double DV, ALFAV;
   if (od_grid(g, &DV, &ALFAV)) return fail(s, CLBLM_ERR_GRID, "bad grid");
-  for (int64_t i = 1; i < L->n; ++i)
-    if (L->vnu[i] < L->vnu[i - 1]) return fail(s, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+  {
+    double run = -1e300;
+    for (int64_t i = 0; i < L->n; ++i) {
+      if (L->iflg[i] < 0) continue;  /* coupling coefficients: no centre */
+      if (L->vnu[i] < run) return fail(s, CLBLM_ERR_UNSORTED, "line list not sorted at %lld", (long long)i);
+      run = L->vnu[i];
+    }
+  }
   int JRAD = sticky_jrad(s, lay, g, ctrl);
   if (s->tr_panel)
     for (int64_t i = 0; i < L->n; ++i) s->tr_panel[i] = -1;
@@ -2101,12 +2242,14 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
   linefile_t F;
   F.L = L;
   F.nrec = (L->n + CLBLM_LINES_PER_RECORD - 1) / CLBLM_LINES_PER_RECORD;
+  F.key = line_keys(L);
   tape9_t T9;
   memset(&T9, 0, sizeof T9);
   rc = linf4q(s, &F, &M, V1L4, V2L4, DVR4, PAVE, TAVE, lay->wtot, &T9);
   if (rc) {
     free(ABSRBb);
     free(T9.rec);
+    free(F.key);
     return rc;
   }
   stl.nshrunk = T9.nlines;
@@ -2159,6 +2302,7 @@ static int odlay_core(ocl_session *s, const clblm_lines_t *L, const clblm_cont_t
   rc = hiracq(s, &a);
   free(ABSRBb);
   free(T9.rec);
+  free(F.key);
   if (rc) {
     free(buf);
     return rc;

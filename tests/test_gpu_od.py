@@ -243,6 +243,48 @@ def test_line_selection_bit_exact(gpu_lib, oracle_mod, case, precision):
     assert np.max(np.abs(od - ref) / np.abs(ref)) <= tol
 
 
+def _coupled(lines, every, seed):
+    """every `every`-th line coupled: IFLG 1 with Y and G of either sign
+    and size, every fifth of them IFLG 3 (reduced widths)"""
+    rng = np.random.default_rng(seed)
+    idx = np.arange(3, lines.n, every)
+    m = len(idx)
+    iflg = np.where(np.arange(m) % 5 == 4, 3, 1)
+    t4 = np.array(synth.TEMPLC)
+    y = rng.uniform(-0.05, 0.05, (m, 1)) * (1.0 + 0.3 * (296.0 - t4) / 100.0)
+    g = rng.uniform(-0.01, 0.01, (m, 1)) * (1.0 + 0.2 * (296.0 - t4) / 100.0)
+    return synth.with_coupling(lines, idx, iflg=iflg, a=np.abs(y) * (iflg[:, None] == 3) + y * (iflg[:, None] == 1),
+                               b=np.abs(g) * (iflg[:, None] == 3) + g * (iflg[:, None] == 1))
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+@pytest.mark.parametrize("tave", [215.0, 288.0])
+def test_line_coupling(gpu_lib, oracle_mod, precision, tol, tave):
+    """Coupled H2O and CO2 lines (each followed by its coefficient record):
+    the dispersion term on the three line-centre grids, G and the reduced
+    widths, coupled far-wing lines kept out of SHRINQ's groups and their
+    dispersion term in CNVF4Q, lines outside the window through the wings"""
+    lines = _coupled(synth.line_list(20000, 550.0, 750.0, seed=5, mols=(1, 2)), 13, seed=6)
+    col = T.Column(np.array([1, 2], np.int32), [400.0], [tave], [tave], [tave], np.array([[3e17, 3e17]]), [2.479e24],
+                   [1.67 * 2.479e24], 600.0, 700.0, tave, 1.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
+
+
+@pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
+def test_line_coupling_near_zero(gpu_lib, oracle_mod, precision, tol):
+    """Coupled O2-like lines from 0.02 cm-1 in a window starting near zero:
+    the dispersion term in the folded first panel (RSYM) and in the far
+    wings' Van Vleck-Weisskopf mirror records (SPP negated)"""
+    lines = _coupled(synth.line_list(3000, 0.02, 90.0, seed=10, mols=(7,), isotopologues=True), 7, seed=11)
+    col = T.Column(np.array([7], np.int32), [1013.25], [296.0], [296.0], [296.0], np.array([[5e18]]), [2.479e24],
+                   [1.67 * 2.479e24], 0.0005, 60.0, 296.0, 1.0)
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, precision=precision)
+    rel = np.max(np.abs(od - ref) / np.abs(ref))
+    assert rel <= tol, rel
+
+
 @pytest.mark.parametrize("precision,tol", [(T.CLBLM_PREC_MIXED, 1e-5), (T.CLBLM_PREC_PLAIN, 1e-9)])
 @pytest.mark.parametrize("v2", [12.0, 60.0])
 def test_window_starting_at_zero_rsym(gpu_lib, oracle_mod, precision, tol, v2):
