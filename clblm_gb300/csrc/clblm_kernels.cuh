@@ -86,8 +86,14 @@ extern __constant__ double c_AVRAT[102], c_CGAUSS[102], c_CF1[102], c_CF2[102], 
 // FP32 copies of CF1, CF2, CF3, CGAUSS, CER (mixed-path shape coefficients)
 extern __constant__ float c_SHAPEf[5][102];
 extern __constant__ float c_AVRATf[102];
-__global__ void k_line_prep(const LayerPlan* plans, int layer0, LineIn lines, const IsoRow* iso_tab,
-                            const double* vft_all, LinePrep* out, int64_t out_stride, unsigned long long* stats);
+// Cpl: the line list holds coupled lines (IFLG 1 or 3) with their coefficient
+// records.  (A template kernel's declaration repeats its definition's
+// parameter qualifiers exactly: nvcc takes a difference in __restrict__ for
+// another template, whose explicit instantiation then has no device code.)
+template <bool Cpl>
+__global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+                            const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
+                            LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats);
 __global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,
                                 int nblk_stride);
 __global__ void k_scan_blocks(int* blockmax, int nblk_stride, const int64_t* nlines, int nlayers);
@@ -100,8 +106,10 @@ __global__ void k_line_records(const LayerPlan* plans, int layer0, const double*
 __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double* vnu_raw, const double* alfvmax,
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
 __global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);
-__global__ void k_f4_prep(const LayerPlan* plans, int layer0, LineIn lines, const IsoRow* iso_tab, F4Prep* out,
-                          int64_t stride, unsigned long long* stats);
+template <bool Cpl>
+__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+                          const IsoRow* __restrict__ iso_tab, F4Prep* __restrict__ out, int64_t stride,
+                          unsigned long long* __restrict__ stats);
 __global__ void k_f4_count(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0, int64_t* blocksum,
                            int nblk);
 __global__ void k_f4_blockscan(int64_t* blocksum, int nblk, const LayerPlan* plans, int layer0, int nlayers,

@@ -102,7 +102,10 @@ __global__ void k_r4_radfac(const LayerPlan* plans, int layer0, const double* bl
 // k_panel in one pass (kPanelAll), or the line sums (kPanelLines) and the far
 // wings, continuum, combine and radiation term (kPanelWings) in two
 constexpr int kPanelAll = 0, kPanelLines = 1, kPanelWings = 2;
-template <bool Plain, int Part>
+// Cpl: the line list holds coupled lines, whose grid records carry kCplBit
+// (the branch-free sums of the mixed path skip them; they are added with
+// their dispersion term); without it the line sums stay as lean as before
+template <bool Plain, int Part, bool Cpl>
 __global__ void k_panel(const __grid_constant__ PanelArgs a);
 template <bool Plain, int CHUNK>
 __global__ void k_f4_conv(F4Args a);

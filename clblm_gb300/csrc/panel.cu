@@ -1,6 +1,6 @@
 // panel.cu -- hot kernels of the layer optical depth and nadir radiance.
 //
-//   k_panel<Plain, Part>  one CTA per (layer, panel of 2400 points): the three
+//   k_panel<Plain, Part, Cpl>  one CTA per (layer, panel of 2400 points): the three
 //                    nested Voigt sub-function grids R3 (16 DV), R2 (4 DV) and
 //                    R1 (DV) gathered from the per-line records (CNVFNQ,
 //                    clblm_ODLAY.f90:2067-2258), far-wing and continuum
@@ -412,7 +412,7 @@ __device__ __forceinline__ float cpl_terms(const PanelSmem<false>& S, const Grid
 // kHalfBatch records each, every batch is summed in FP32 (four partial sums)
 // and added to the Kahan sum.
 constexpr int kHalfBatch = kBatch / 2;
-template <bool Plain, int GRID>
+template <bool Plain, int GRID, bool Cpl>
 __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs& a, const GridRec* __restrict__ rec,
                                             const GridRecD* __restrict__ recd, const GridRecLo* __restrict__ reclo,
                                             int64_t lo, int64_t hi, int g, bool active, int qmax,
@@ -442,7 +442,7 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
       if (!active) continue;
       for (int k = 0; k < cnt; ++k) {
         const GridRec r = buf[k];
-        if (g < r.g_lo || g > r.g_hi || (r.q & ~kCplBit) > qmax) continue;
+        if (g < r.g_lo || g > r.g_hi || (Cpl ? (r.q & ~kCplBit) : r.q) > qmax) continue;
         const GridRecD& d = S.wrecd[warp][k];
         const double zf = fma((double)(g - r.g_lo + 1), d.zs, d.zfl);
         const int iz = (int)(fabs(zf) + 1.5);
@@ -452,7 +452,7 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
         }
         // a coupled line adds its dispersion term: the strengths times CLCk
         // times DPTRAT, the shape times ZF (clblm_ODLAY.f90:2195-2239)
-        const double dpt = (r.q & kCplBit) ? a.cpl[(int64_t)blockIdx.y * a.stride + base + k] : 0.;
+        const double dpt = (Cpl && (r.q & kCplBit)) ? a.cpl[(int64_t)blockIdx.y * a.stride + base + k] : 0.;
         if constexpr (GRID == 1) {
           const double* T = S.t1 + 3 * (iz - 1);
           acc.add(d.a0 * T[0] + d.a1 * T[1] + d.a2 * T[2]);
@@ -481,7 +481,8 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
       __syncwarp();
       if (hl < kHalfBatch) hb[hl] = nxt;
       // the batch's coupled records: term_fast skips them (q carries kCplBit)
-      const unsigned cpl_bits = __ballot_sync(0xffffffffu, hl < kHalfBatch && (nxt.q & kCplBit) != 0);
+      unsigned cpl_bits = 0;
+      if constexpr (Cpl) cpl_bits = __ballot_sync(0xffffffffu, hl < kHalfBatch && (nxt.q & kCplBit) != 0);
       __syncwarp();
       const int cnt = min(n - b, kHalfBatch);
       if (hl < kHalfBatch && b + kHalfBatch + hl < n) nxt = rec[lo + b + kHalfBatch + hl];
@@ -507,15 +508,17 @@ __device__ __forceinline__ void gather_grid(PanelSmem<Plain>& S, const PanelArgs
       }
       float bsum = (s0 + s1) + (s2 + s3);
       if (fix) bsum += fix_terms<GRID>(S, hb, lo + b, reclo, a, g, fix);
-      const unsigned cm = (cpl_bits >> (16 * half)) & ((1u << cnt) - 1u);
-      if (cm) bsum += cpl_terms<GRID>(S, hb, lo + b, reclo, a, g, qmax, cm);
+      if constexpr (Cpl) {
+        const unsigned cm = (cpl_bits >> (16 * half)) & ((1u << cnt) - 1u);
+        if (cm) bsum += cpl_terms<GRID>(S, hb, lo + b, reclo, a, g, qmax, cm);
+      }
       acc.add(bsum);
     }
   }
   __syncwarp();
 }
 
-template <bool Plain, int Part>
+template <bool Plain, int Part, bool Cpl>
 __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWings ? 6 : 3))
     k_panel(const __grid_constant__ PanelArgs a) {
   // Part: kPanelAll, or the line sums alone (kPanelLines: the far wings and
@@ -741,7 +744,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWing
     const int h0 = 2 * t + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * t + 1 : h0;
     const int64_t lo = S.lo3[h0], hi = max(S.lo3[h0], S.hi3[h1]);
     Acc acc;
-    if (kLines) gather_grid<Plain, 3>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
+    if (kLines) gather_grid<Plain, 3, Cpl>(S, a, rec3, rd3, rl3, lo, hi, g, active, qmax, acc);
     if (active && kWings) {
       // far wings (R4) and continuum (ABSRB) interpolated into R3 (XINT).
       // The R4 block LBLF4Q held when XINT reached the point: this panel's
@@ -826,7 +829,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWing
       Acc acc;
       const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
       if (kLines)
-        gather_grid<Plain, 2>(S, a, rec2, rd2, rl2, S.lo2[h0], max(S.lo2[h0], S.hi2[h1]), g, active, p, acc);
+        gather_grid<Plain, 2, Cpl>(S, a, rec2, rd2, rl2, S.lo2[h0], max(S.lo2[h0], S.hi2[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 1) & 3;
         int Jg = J - off;
@@ -867,7 +870,7 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWing
       Acc acc;
       const int h0 = 2 * tile + (Plain ? 0 : (lane >> 4)), h1 = Plain ? 2 * tile + 1 : h0;
       if (kLines)
-        gather_grid<Plain, 1>(S, a, rec1, rd1, rl1, S.lo1[h0], max(S.lo1[h0], S.hi1[h1]), g, active, p, acc);
+        gather_grid<Plain, 1, Cpl>(S, a, rec1, rd1, rl1, S.lo1[h0], max(S.lo1[h0], S.hi1[h1]), g, active, p, acc);
       if (active) {
         int off = (J - 33) & 3;
         int Jg = J - off;
@@ -927,9 +930,11 @@ __global__ void __launch_bounds__(kPanelThreads, Plain ? 1 : (Part == kPanelWing
   }
 }
 
-template __global__ void k_panel<false, kPanelLines>(const __grid_constant__ PanelArgs);
-template __global__ void k_panel<false, kPanelWings>(const __grid_constant__ PanelArgs);
-template __global__ void k_panel<true, kPanelAll>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<false, kPanelLines, false>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<false, kPanelLines, true>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<false, kPanelWings, false>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<true, kPanelAll, false>(const __grid_constant__ PanelArgs);
+template __global__ void k_panel<true, kPanelAll, true>(const __grid_constant__ PanelArgs);
 
 // ---------------------------------------------------------------------------
 // RSYM (clblm_ODLAY.f90:3020-3085): when a layer's first panel starts at or

@@ -85,6 +85,30 @@ __device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rd
   return fits_panel(vnu, vft, dv, rdv, bhwdxf, max1);
 }
 
+// A(k) and B(k) of the coefficient record k (node k = 1..4), loaded one
+// field at a time (no local array: these kernels keep their registers)
+__device__ __forceinline__ double lc_a(const LineIn& L, int64_t k, int node) {
+  switch (node) {
+    case 1: return L.vnu[k];
+    case 2: {
+      double alfa = (double)L.alfa[k];
+      const int m = L.mol[k] % 100;
+      if (m == 7 && L.iflg[k] >= 0) alfa = (alfa - 0.21 * (double)L.hwhm[k]) / (1.0 - 0.21);
+      if (m == 22 && L.iflg[k] >= 0) alfa = (alfa - 0.79 * (double)L.hwhm[k]) / (1.0 - 0.79);
+      return alfa;
+    }
+    case 3: return (double)__int_as_float(L.mol[k]);
+    default: return (double)L.tmpalf[k];
+  }
+}
+__device__ __forceinline__ double lc_b(const LineIn& L, int64_t k, int node) {
+  switch (node) {
+    case 1: return (double)L.sp[k];
+    case 2: return (double)L.epp[k];
+    case 3: return (double)L.hwhm[k];
+    default: return (double)L.pshift[k];
+  }
+}
 // The coupling coefficients of a coupled line (IFLG 1: Y and G; IFLG 3:
 // GAMMA1 and GAMMA2) at the layer's temperature, from the record k after it:
 // A(1..4) = VNU, ALFA, the bits of MOL read as a float, TMPALF and B(1..4) =
@@ -92,27 +116,26 @@ __device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rd
 // clblm_ODLAY.f90:1822-1846; RDLIN's O2/N2 width rule applies to the record
 // as to any).  LNCORQ interpolates from the lower node ilc, LINF4Q
 // (clblm_ODLAY_LineF4.f90:963-984) from the upper one (upper = true).
-__device__ void lc_coefs(const LineIn& L, int64_t k, int ilc, double rectlc, double tmpdif, bool upper, double* a,
-                         double* b) {
-  double alfa = (double)L.alfa[k];
-  const int m = L.mol[k] % 100;
-  if (m == 7 && L.iflg[k] >= 0) alfa = (alfa - 0.21 * (double)L.hwhm[k]) / (1.0 - 0.21);
-  if (m == 22 && L.iflg[k] >= 0) alfa = (alfa - 0.79 * (double)L.hwhm[k]) / (1.0 - 0.79);
-  const double A[5] = {0., L.vnu[k], alfa, (double)__int_as_float(L.mol[k]), (double)L.tmpalf[k]};
-  const double B[5] = {0., (double)L.sp[k], (double)L.epp[k], (double)L.hwhm[k], (double)L.pshift[k]};
+__device__ __forceinline__ void lc_coefs(const LineIn& L, int64_t k, int ilc, double rectlc, double tmpdif,
+                                         bool upper, double* a, double* b) {
   if (!upper) {
-    const double SLOPEA = (A[ilc + 1] - A[ilc]) * rectlc;
-    const double SLOPEB = (B[ilc + 1] - B[ilc]) * rectlc;
-    *a = A[ilc] + SLOPEA * tmpdif;
-    *b = B[ilc] + SLOPEB * tmpdif;
+    const double a0 = lc_a(L, k, ilc), a1 = lc_a(L, k, ilc + 1);
+    const double b0 = lc_b(L, k, ilc), b1 = lc_b(L, k, ilc + 1);
+    const double SLOPEA = (a1 - a0) * rectlc;
+    const double SLOPEB = (b1 - b0) * rectlc;
+    *a = a0 + SLOPEA * tmpdif;
+    *b = b0 + SLOPEB * tmpdif;
   } else {
-    const double SLOPEY = (A[ilc] - A[ilc - 1]) * rectlc;
-    const double SLOPEG = (B[ilc] - B[ilc - 1]) * rectlc;
-    *a = A[ilc] + SLOPEY * tmpdif;
-    *b = B[ilc] + SLOPEG * tmpdif;
+    const double a1 = lc_a(L, k, ilc), a0 = lc_a(L, k, ilc - 1);
+    const double b1 = lc_b(L, k, ilc), b0 = lc_b(L, k, ilc - 1);
+    const double SLOPEY = (a1 - a0) * rectlc;
+    const double SLOPEG = (b1 - b0) * rectlc;
+    *a = a1 + SLOPEY * tmpdif;
+    *b = b1 + SLOPEG * tmpdif;
   }
 }
 
+template <bool Cpl>
 __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                             const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
                             LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats) {
@@ -150,21 +173,30 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
       const IsoRow& R = iso_tab[P.iso_off + P.mrow[m] + iso - 1];
       // line coupling: Y, G (IFLG 1) or GAMMA1, GAMMA2 (IFLG 3)
       double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
-      if ((iflg == 1 || iflg == 3) && i + 1 < lines.n) {
-        if (iflg == 1) lc_coefs(lines, i + 1, P.lc_ilc, P.lc_rectlc, P.lc_tmpdif, false, &YI, &GI);
-        else lc_coefs(lines, i + 1, P.lc_ilc, P.lc_rectlc, P.lc_tmpdif, false, &GAMMA1, &GAMMA2);
+      if (Cpl && (iflg == 1 || iflg == 3) && i + 1 < lines.n) {
+        double ca, cb;
+        lc_coefs(lines, i + 1, P.lc_ilc, P.lc_rectlc, P.lc_tmpdif, false, &ca, &cb);
+        if (iflg == 1) {
+          YI = ca;
+          GI = cb;
+        } else {
+          GAMMA1 = ca;
+          GAMMA2 = cb;
+        }
       }
       double alfa0 = (double)lines.alfa[i];
       double hwhms = (double)lines.hwhm[i];
       // air-broadened widths of O2 and N2 to foreign widths (RDLIN :2728-2745)
-      if (m == 7) alfa0 = (alfa0 - 0.21 * hwhms) / (1.0 - 0.21);
-      if (m == 22) alfa0 = (alfa0 - 0.79 * hwhms) / (1.0 - 0.79);
+      if (m == 7 || m == 22) {
+        const double rvmr = m == 7 ? 0.21 : 0.79;
+        alfa0 = (alfa0 - rvmr * hwhms) / (1.0 - rvmr);
+      }
       double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
       double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
       double ALFL = ALFA0I * R.rhodif + HWHMSI * R.rhoslf;  // RHODIF = RHORAT - RHOSLF
-      if (iflg == 3) ALFL = ALFL * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);  // reduced widths
+      if (Cpl && iflg == 3) ALFL = ALFL * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);  // reduced widths
       double ALFAD = VNU * R.alfd1;
       double ZETA = ALFL / (ALFL + ALFAD);
       double FZETA = 100. * ZETA;
@@ -203,7 +235,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             if (EPP > P.epp_neg_f)
               sui = sui * R.scor_f * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
             SUI = sui;
-            SP = iflg == 1 ? SUI * (1. + GI * P.pavp2) : SUI;  // SUI*(1 + G*PAVP2)
+            SP = (Cpl && iflg == 1) ? SUI * (1. + GI * P.pavp2) : SUI;  // SUI*(1 + G*PAVP2)
             // SPEAK = SUI/ALFV > 0 unless SUI = 0 (SUI >= 1e-45, 1/ALFV > 1:
             // no underflow), so with DPTMIN = 0 the test is SUI = 0
             if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
@@ -214,14 +246,14 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             if (EPP <= -1.001) EPP = fabs(EPP);
             if (P.jrad == 1) SUI = SUI * radfn_d(lines.vnu[i], P.xkt);
             if (EPP > -0.999) SUI = SUI * R.scor * exp(-EPP * P.betacr) * (1. + exp(-VNU / P.xkt));
-            SP = SUI * (1. + GI * P.pavp2);
+            SP = Cpl ? SUI * (1. + GI * P.pavp2) : SUI * P.spfac;
             if (iflg == 0 && (P.ilnflg == 0 || P.ilnflg == 1)) {
               double SPEAK = SUI * RECALF;
               if (SPEAK <= P.dptmn) ok = false;  // DPTFAC == 0 on this path
             }
           }
           // SPPSP = SPP / SP, SPP = SUI * Y * PAVP0 (:1938-1940)
-          if (iflg == 1) r.sppsp = (SUI * YI * P.pavp0) / SP;
+          if (Cpl && iflg == 1) r.sppsp = (SUI * YI * P.pavp0) / SP;
           if (ok) {
             lincnt++;
             nminus += nmin;
@@ -267,6 +299,12 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     }
   }
 }
+template __global__ void k_line_prep<false>(const LayerPlan* __restrict__, int, LineIn, const IsoRow* __restrict__,
+                                           const double* __restrict__, LinePrep* __restrict__, int64_t,
+                                           unsigned long long* __restrict__);
+template __global__ void k_line_prep<true>(const LayerPlan* __restrict__, int, LineIn, const IsoRow* __restrict__,
+                                          const double* __restrict__, LinePrep* __restrict__, int64_t,
+                                          unsigned long long* __restrict__);
 
 // ---- prefix maximum of fpanel over a layer's line range -------------------
 constexpr int kScanBlock = 1024;
@@ -453,7 +491,9 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
       l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
       amax = fmax(amax, lp.alfv);
-      if (lp.sppsp != 0.) {  // a coupled line: its records go the exact way
+      // a coupled line (SPPSP != 0, tested on the bits: no FP64 compare) has
+      // its records go the exact way
+      if ((__double_as_longlong(lp.sppsp) << 1) != 0) {
         g1.q |= kCplBit;
         g2.q |= kCplBit;
         g3.q |= kCplBit;
@@ -1150,6 +1190,7 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
 }
 
 // ---- far-wing lines: LINF4Q per-line corrections --------------------------
+template <bool Cpl>
 __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                           const IsoRow* __restrict__ iso_tab, F4Prep* __restrict__ out, int64_t stride,
                           unsigned long long* __restrict__ stats) {
@@ -1178,9 +1219,16 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
         // line coupling: G scales the strength, Y gives SPP (IFLG 1);
         // GAMMA1, GAMMA2 reduce the width (IFLG 3)
         double YI = 0., GI = 0., GAMMA1 = 0., GAMMA2 = 0.;
-        if ((iflg == 1 || iflg == 3) && i + 1 < lines.n) {
-          if (iflg == 1) lc_coefs(lines, i + 1, P.lc4_ilc, P.lc4_rectlc, P.lc4_tmpdif, true, &YI, &GI);
-          else lc_coefs(lines, i + 1, P.lc4_ilc, P.lc4_rectlc, P.lc4_tmpdif, true, &GAMMA1, &GAMMA2);
+        if (Cpl && (iflg == 1 || iflg == 3) && i + 1 < lines.n) {
+          double ca, cb;
+          lc_coefs(lines, i + 1, P.lc4_ilc, P.lc4_rectlc, P.lc4_tmpdif, true, &ca, &cb);
+          if (iflg == 1) {
+            YI = ca;
+            GI = cb;
+          } else {
+            GAMMA1 = ca;
+            GAMMA2 = cb;
+          }
         }
         const float alfa_in = lines.alfa[i], hwhm_in = lines.hwhm[i];
         const double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
@@ -1194,14 +1242,16 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           const float vf = (float)VNU;
           if (EPP > P.epp_neg_f) sui = sui * R.scor_f * __expf(-EPP * P.betacr4_f) * (1.f + __expf(-vf * P.beta_f));
           float alfa = alfa_in;
-          if (m == 7) alfa = (float)(((double)alfa_in - 0.21 * (double)hwhm_in) / (1.0 - 0.21));
-          if (m == 22) alfa = (float)(((double)alfa_in - 0.79 * (double)hwhm_in) / (1.0 - 0.79));
+          if (m == 7 || m == 22) {
+            const double rvmr = m == 7 ? 0.21 : 0.79;
+            alfa = (float)(((double)alfa_in - rvmr * (double)hwhm_in) / (1.0 - rvmr));
+          }
           const float TMPCOR = __expf(lines.tmpalf[i] * P.ln_tratio_f);  // (T/296)^n
           const float rs = R.rhoslf_f;
           r.w.f[0] = (alfa * TMPCOR) * (P.rhorat_f - rs) + (hwhm_in * TMPCOR) * rs;
-          if (iflg == 3) r.w.f[0] = r.w.f[0] * (float)(1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
+          if (Cpl && iflg == 3) r.w.f[0] = r.w.f[0] * (float)(1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
           r.w.f[1] = vf * R.alfd1_f;
-          if (iflg == 1) {
+          if (Cpl && iflg == 1) {
             r.sp = (double)sui * (1. + GI * P.pavp2);  // SP = SUI*(1 + G*PAVP2)
             r.spp = (double)sui * YI * P.pavp0;       // SPP = SUI*Y*PAVP0
             sui = (float)r.sp;
@@ -1211,8 +1261,10 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           r.w.f[2] = sui;
         } else {
           double alfa = (double)alfa_in, hwhm = (double)hwhm_in;
-          if (m == 7) alfa = (alfa - 0.21 * hwhm) / (1.0 - 0.21);
-          if (m == 22) alfa = (alfa - 0.79 * hwhm) / (1.0 - 0.79);
+          if (m == 7 || m == 22) {
+            const double rvmr = m == 7 ? 0.21 : 0.79;
+            alfa = (alfa - rvmr * hwhm) / (1.0 - rvmr);
+          }
           double EPP = (double)EPP0;
           if (VNU == 0.) SUI = 2. * SUI;
           if (EPP <= -1.001) EPP = fabs(EPP);
@@ -1221,10 +1273,10 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
           double ALFA0I = alfa * TMPCOR;
           double HWHMSI = hwhm * TMPCOR;
           r.w.d[0] = ALFA0I * (P.rhorat - R.rhoslf) + HWHMSI * R.rhoslf;
-          if (iflg == 3) r.w.d[0] = r.w.d[0] * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
+          if (Cpl && iflg == 3) r.w.d[0] = r.w.d[0] * (1.0 - GAMMA1 * P.pavp0 - GAMMA2 * P.pavp2);
           r.w.d[1] = VNU * R.alfd1;
-          r.sp = SUI * (1. + GI * P.pavp2);
-          r.spp = SUI * YI * P.pavp0;
+          r.sp = Cpl ? SUI * (1. + GI * P.pavp2) : SUI * P.spfac;
+          if (Cpl) r.spp = SUI * YI * P.pavp0;
         }
         r.vnu = VNU;
         r.mol = m;
@@ -1236,6 +1288,10 @@ __global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineI
   for (int off = 16; off > 0; off >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, off);
   if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&stats[(blockIdx.y + layer0) * kStatsPerLayer + 4], bad);
 }
+template __global__ void k_f4_prep<false>(const LayerPlan* __restrict__, int, LineIn, const IsoRow* __restrict__,
+                                         F4Prep* __restrict__, int64_t, unsigned long long* __restrict__);
+template __global__ void k_f4_prep<true>(const LayerPlan* __restrict__, int, LineIn, const IsoRow* __restrict__,
+                                        F4Prep* __restrict__, int64_t, unsigned long long* __restrict__);
 
 // ---- LINF4Q record loop with SHRINQ, in parallel pieces -------------------
 // The reference appends the corrected lines of each 250-line record to a

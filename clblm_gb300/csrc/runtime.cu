@@ -972,9 +972,16 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   k_continuum<<<dim3((kNABSRB + 255) / 256, count), blk, 0, st>>>(dplans, first, h->cont, h->absrb.as<double>());
   // far wings
   h->launches++;
-  k_f4_prep<<<dim3((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count), blk, 0, st>>>(
-      dplans, first, li, h->isotab.as<const IsoRow>(), h->f4prep.as<F4Prep>(), f4stride,
-      h->stats.as<unsigned long long>());
+  {
+    const dim3 g4((unsigned)std::min<int64_t>((f4stride + 255) / 256, 4096), count);
+    if (h->has_cpl)
+      k_f4_prep<true><<<g4, blk, 0, st>>>(dplans, first, li, h->isotab.as<const IsoRow>(), h->f4prep.as<F4Prep>(),
+                                          f4stride, h->stats.as<unsigned long long>());
+    else
+      k_f4_prep<false><<<g4, blk, 0, st>>>(dplans, first, li, h->isotab.as<const IsoRow>(), h->f4prep.as<F4Prep>(),
+                                           f4stride, h->stats.as<unsigned long long>());
+    CUDA_TRY(h, cudaGetLastError());  // the chain after it reads what it writes
+  }
   {
     // LINF4Q record loop + SHRINQ: count, compact, walk, group sums
     int nblk4 = (int)((f4stride + 1 + 1023) / 1024);
@@ -1071,9 +1078,16 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
   st = h->stream;
   // line centres
   h->launches++;
-  k_line_prep<<<dim3((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count), blk, 0, st>>>(
-      dplans, first, li, h->isotab.as<const IsoRow>(), h->vft.as<double>(), h->prep.as<LinePrep>(), lstride,
-      h->stats.as<unsigned long long>());
+  {
+    const dim3 gl((unsigned)std::min<int64_t>((lstride + 255) / 256, 8192), count);
+    if (h->has_cpl)
+      k_line_prep<true><<<gl, blk, 0, st>>>(dplans, first, li, h->isotab.as<const IsoRow>(), h->vft.as<double>(),
+                                            h->prep.as<LinePrep>(), lstride, h->stats.as<unsigned long long>());
+    else
+      k_line_prep<false><<<gl, blk, 0, st>>>(dplans, first, li, h->isotab.as<const IsoRow>(), h->vft.as<double>(),
+                                             h->prep.as<LinePrep>(), lstride, h->stats.as<unsigned long long>());
+    CUDA_TRY(h, cudaGetLastError());  // the chain after it reads what it writes
+  }
   int nblk = (int)((lstride + 1023) / 1024);
   h->launches++;
   k_scan_blockmax<<<dim3(nblk, count), 256, 0, st>>>(h->prep.as<LinePrep>(), lstride, h->nlines_d.as<int64_t>() + first,
@@ -1152,13 +1166,16 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     // FP64: one pass once R4 and ABSRB are ready
     CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));
     if (!h->panel_attr_set[1]) {
-      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true, kPanelAll>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true, kPanelAll, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<true, kPanelAll, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
       h->panel_attr_set[1] = true;
     }
     h->launches++;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-    k_panel<true, kPanelAll><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    if (h->has_cpl) k_panel<true, kPanelAll, true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    else k_panel<true, kPanelAll, false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
     CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
     CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
     CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
@@ -1167,22 +1184,25 @@ int run_od_batch(clblm_handle* h, std::vector<HostPlan>& hps, int first, int cou
     // ABSRB are ready, a second pass adds the far wings and the continuum
     // through XINT and the combine (the OD is linear in R3, R2 and R1)
     if (!h->panel_attr_set[0]) {
-      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelLines>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelWings>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)panel_smem_bytes(false, true)));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelLines, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelLines, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CUDA_TRY(h, cudaFuncSetAttribute(k_panel<false, kPanelWings, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem_bytes(false, true)));
       h->panel_attr_set[0] = true;
     }
     h->launches += 2;
     CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-    k_panel<false, kPanelLines><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    if (h->has_cpl) k_panel<false, kPanelLines, true><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
+    else k_panel<false, kPanelLines, false><<<dim3(maxp, count), kPanelThreads, smem, st>>>(pa);
     CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
     CUDA_TRY(h, cudaStreamWaitEvent(st, h->join_ev, 0));  // R4 and ABSRB are ready
     // the radiation-term pool is claimed again by the second pass
     CUDA_TRY(h, cudaMemsetAsync(pa.seg_next, 0, sizeof(int), st));
     CUDA_TRY(h, cudaEventRecord(h->ev[8], st));
     // without the shape tables: six CTAs of the far-wing pass share an SM
-    k_panel<false, kPanelWings><<<dim3(maxp, count), kPanelThreads, panel_smem_bytes(false, true), st>>>(pa);
+    k_panel<false, kPanelWings, false><<<dim3(maxp, count), kPanelThreads, panel_smem_bytes(false, true), st>>>(pa);
     CUDA_TRY(h, cudaEventRecord(h->ev[9], st));
   }
   // RSYM: the first panel of a layer whose panel origin is at or below 0 cm-1
