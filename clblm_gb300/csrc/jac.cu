@@ -39,6 +39,7 @@ __global__ void k_interp_map_jobs(const JacJob* __restrict__ jobs, int njob) {
   double Vi = __dadd_rn(s.v1, __dmul_rn((double)(iIn - 1), s.dvin));
   double P = __ddiv_rn(__dadd_rn(Vo, -Vi), s.dvin);
   const int64_t J1 = blk_j1[b];
+  if (J1 < 1 || J1 > nout) return;  // a block start off the output grid writes nothing
   const int64_t J2 = min(nout, J1 + 2400 - 1);
   for (int64_t J = J1; J <= J2; ++J) {
     int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
