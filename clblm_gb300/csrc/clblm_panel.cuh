@@ -68,8 +68,9 @@ struct F4RecD {
   int jmin, jmax, co2, pad;
   double xnui, sil, siv, fbnd, al2, alv2;
 };
-constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv (two per thread)
-constexpr int kF4Threads = kF4Tile / 2;
+constexpr int kF4Tile = 256;     // R4 points per CTA of k_f4_conv
+constexpr int kF4Pts = 4;        // points per thread: a record read from shared memory serves four
+constexpr int kF4Threads = kF4Tile / kF4Pts;
 constexpr int kF4Group = 32;     // records per FP32 partial sum of the mixed path
 // records per shared-memory stage of k_f4_conv: the variants the autotuner
 // times (64, 128, 256)

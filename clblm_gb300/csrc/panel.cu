@@ -1182,7 +1182,8 @@ template __global__ void k_rsym<true>(const __grid_constant__ PanelArgs);
 // whose running min of JMIN (from the right) passes its last point.  That
 // range streams through shared memory in chunks of CHUNK records, one bulk
 // copy per chunk into two alternating stages; every thread then evaluates all
-// records of the chunk at its two points.  The FP64 path adds the terms in
+// records of the chunk at its kF4Pts points (m0 + t + i kF4Threads), each
+// record's fields loaded once for all of them.  The FP64 path adds the terms in
 // the reference's order (record order); the mixed path sums groups of
 // kF4Group records (two packed partial sums over alternate records) and adds
 // each group's total into a Kahan sum.  Groups start at the tile's first
@@ -1220,21 +1221,31 @@ __device__ __forceinline__ float2 f4_term(const F4Rec& r, float2 Jm1, float2 dvr
   return f;
 }
 
-// Sum of the records S[0, cnt) at both points, two records per step
+// Sum of the records S[0, cnt) at the thread's four points (pairs AB and
+// CD), two records per step: each point's sum runs over alternate records in
+// two partial sums, whatever the number of points a thread holds
 template <bool Core, bool Mask>
-__device__ __forceinline__ float2 f4_chunk(const F4Rec* S, int cnt, float2 Jm1, float2 dvr4, int JA, int JB) {
-  float2 p0 = make_float2(0.f, 0.f), p1 = p0;
+__device__ __forceinline__ void f4_chunk(const F4Rec* S, int cnt, float2 JmAB, float2 JmCD, float2 dvr4, int JA,
+                                         int JB, int JC, int JD, float2* tAB, float2* tCD) {
+  float2 p0 = make_float2(0.f, 0.f), p1 = p0, q0 = p0, q1 = p0;
   int k = 0;
   for (; k + 2 <= cnt; k += 2) {
-    p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], Jm1, dvr4, JA, JB));
-    p1 = __fadd2_rn(p1, f4_term<Core, Mask>(S[k + 1], Jm1, dvr4, JA, JB));
+    p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], JmAB, dvr4, JA, JB));
+    q0 = __fadd2_rn(q0, f4_term<Core, Mask>(S[k], JmCD, dvr4, JC, JD));
+    p1 = __fadd2_rn(p1, f4_term<Core, Mask>(S[k + 1], JmAB, dvr4, JA, JB));
+    q1 = __fadd2_rn(q1, f4_term<Core, Mask>(S[k + 1], JmCD, dvr4, JC, JD));
   }
-  if (k < cnt) p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], Jm1, dvr4, JA, JB));
-  return __fadd2_rn(p0, p1);
+  if (k < cnt) {
+    p0 = __fadd2_rn(p0, f4_term<Core, Mask>(S[k], JmAB, dvr4, JA, JB));
+    q0 = __fadd2_rn(q0, f4_term<Core, Mask>(S[k], JmCD, dvr4, JC, JD));
+  }
+  *tAB = __fadd2_rn(p0, p1);
+  *tCD = __fadd2_rn(q0, q1);
 }
 
 template <bool Plain, int CHUNK>
-__global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a) {
+__global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 16) k_f4_conv(F4Args a) {
+  static_assert(kF4Pts == 4, "the thread's points are the pairs AB and CD");
   static_assert(CHUNK % kF4Group == 0, "groups of the FP32 sums lie within a chunk");
   using Real = typename std::conditional<Plain, double, float>::type;
   using Rec = typename std::conditional<Plain, F4RecD, F4Rec>::type;
@@ -1246,9 +1257,9 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
   const LayerPlan& P = a.plans[layer + a.layer0];
   const int64_t m0 = (int64_t)blockIdx.x * kF4Tile;
   if (m0 >= P.nptr4 + 2) return;  // whole CTA: no barrier has been set up yet
-  // the thread's two points: m0 + t and m0 + t + kF4Threads
-  const int64_t mA = m0 + threadIdx.x, mB = mA + kF4Threads;
-  const int JA = (int)mA + 1, JB = (int)mB + 1;
+  // the thread's four points: m0 + t + i kF4Threads, i = 0..3
+  const int64_t mA = m0 + threadIdx.x, mB = mA + kF4Threads, mC = mB + kF4Threads, mD = mC + kF4Threads;
+  const int JA = (int)mA + 1, JB = (int)mB + 1, JC = (int)mC + 1, JD = (int)mD + 1;
   Real* R4 = reinterpret_cast<Real*>(a.r4_all) + P.r4_off;
   const int64_t n = a.nrec[layer + a.layer0];
   const int64_t nm = a.nmirror[layer + a.layer0];
@@ -1291,16 +1302,18 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
   };
   if (threadIdx.x == 0 && nchunk > 0) issue(0);
 
-  const bool liveA = mA < P.nptr4, liveB = mB < P.nptr4;
-  const float2 Jm1 = make_float2((float)(JA - 1), (float)(JB - 1));  // exact: J < 2^24
+  const bool liveA = mA < P.nptr4;
+  const int64_t ms[kF4Pts] = {mA, mB, mC, mD};
+  const float2 JmAB = make_float2((float)(JA - 1), (float)(JB - 1));  // exact: J < 2^24
+  const float2 JmCD = make_float2((float)(JC - 1), (float)(JD - 1));
   const float dvr4f = (float)P.dvr4;
   const float2 dvr4 = make_float2(dvr4f, dvr4f);
   const double ZSQBND = 64. * 64.;
   const double A3 = (1. + 2. * ZSQBND) / ((1. + ZSQBND) * (1. + ZSQBND));
   const double B3 = -1. / ((1. + ZSQBND) * (1. + ZSQBND));
   const double bnd2 = P.bound4 * P.bound4;
-  double accA = 0., accB = 0.;  // FP64 path
-  KahanF kA, kB;                // mixed path: chunk totals
+  double acc[kF4Pts] = {0., 0., 0., 0.};  // FP64 path
+  KahanF kacc[kF4Pts];                     // mixed path: chunk totals
   bool failed = false;
   // FP64 term of record d at point m, in the reference's operations
   auto term_d = [&](const F4RecD& d, int64_t m) -> double {
@@ -1333,8 +1346,11 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
       if constexpr (Plain) {
         for (int k = 0; k < cnt; ++k) {
           const F4RecD& d = S[k];
-          if (JA >= d.jmin && JA <= d.jmax) accA += term_d(d, mA);
-          if (liveB && JB >= d.jmin && JB <= d.jmax) accB += term_d(d, mB);
+#pragma unroll
+          for (int q = 0; q < kF4Pts; ++q) {
+            const int J = (int)ms[q] + 1;
+            if (ms[q] < P.nptr4 && J >= d.jmin && J <= d.jmax) acc[q] += term_d(d, ms[q]);
+          }
         }
       }
     }
@@ -1359,13 +1375,18 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
         for (int g0 = 0; g0 < cnt; g0 += kF4Group) {
           const F4Rec* G = S + g0;
           const int gc = cnt - g0 < kF4Group ? cnt - g0 : kF4Group;
-          float2 t;
-          if (full) t = wonly ? f4_chunk<false, false>(G, gc, Jm1, dvr4, JA, JB)
-                              : f4_chunk<true, false>(G, gc, Jm1, dvr4, JA, JB);
-          else t = wonly ? f4_chunk<false, true>(G, gc, Jm1, dvr4, JA, JB)
-                         : f4_chunk<true, true>(G, gc, Jm1, dvr4, JA, JB);
-          kA.add(t.x);
-          kB.add(t.y);
+          float2 tAB, tCD;
+          if (full) {
+            if (wonly) f4_chunk<false, false>(G, gc, JmAB, JmCD, dvr4, JA, JB, JC, JD, &tAB, &tCD);
+            else f4_chunk<true, false>(G, gc, JmAB, JmCD, dvr4, JA, JB, JC, JD, &tAB, &tCD);
+          } else {
+            if (wonly) f4_chunk<false, true>(G, gc, JmAB, JmCD, dvr4, JA, JB, JC, JD, &tAB, &tCD);
+            else f4_chunk<true, true>(G, gc, JmAB, JmCD, dvr4, JA, JB, JC, JD, &tAB, &tCD);
+          }
+          kacc[0].add(tAB.x);
+          kacc[1].add(tAB.y);
+          kacc[2].add(tCD.x);
+          kacc[3].add(tCD.y);
         }
       }
     }
@@ -1378,8 +1399,8 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
   if (failed) return;
   // the reference's R4 is zero past NPTR4 (LBLF4Q :91-94); mirror records of
   // lines below 25 cm-1 follow the direct ones
-  const int64_t ms[2] = {mA, mB};
-  for (int q = 0; q < 2; ++q) {
+#pragma unroll
+  for (int q = 0; q < kF4Pts; ++q) {
     const int64_t m = ms[q];
     if (m >= P.nptr4 + 2) continue;
     if (m >= P.nptr4) {
@@ -1388,21 +1409,23 @@ __global__ void __launch_bounds__(kF4Threads, Plain ? 1 : 8) k_f4_conv(F4Args a)
     }
     const int J = (int)m + 1;
     if constexpr (Plain) {
-      double acc = q == 0 ? accA : accB;
+      double s = acc[q];
       for (int64_t i = n; i < n + nm; ++i) {
         const F4RecD& d = recs[i];
-        if (J >= d.jmin && J <= d.jmax) acc += term_d(d, m);
+        if (J >= d.jmin && J <= d.jmax) s += term_d(d, m);
       }
-      R4[m] = acc;
+      R4[m] = s;
     } else {
-      KahanF& acc = q == 0 ? kA : kB;
+      KahanF& s = kacc[q];
+      const float2 Jm = q < 2 ? JmAB : JmCD;
+      const int J0 = q < 2 ? JA : JC, J1 = q < 2 ? JB : JD;
       for (int64_t i = n; i < n + nm; ++i) {
         const F4Rec& r = recs[i];
         if (J < r.jmin || J > r.jmax) continue;
-        const float2 t = f4_term<true, true>(r, Jm1, dvr4, JA, JB);  // lane x is point A, lane y point B
-        acc.add(q == 0 ? t.x : t.y);
+        const float2 t = f4_term<true, true>(r, Jm, dvr4, J0, J1);  // lane x is the pair's first point
+        s.add((q & 1) == 0 ? t.x : t.y);
       }
-      R4[m] = acc.value();
+      R4[m] = s.value();
     }
   }
 }
