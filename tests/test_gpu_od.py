@@ -67,6 +67,26 @@ def test_continuum_and_seven_absorbers(gpu_lib, oracle_mod):
     assert rel <= 1e-5, rel
 
 
+@pytest.mark.parametrize("precision", [T.CLBLM_PREC_MIXED, T.CLBLM_PREC_PLAIN])
+@pytest.mark.parametrize("v1,v2,contnm_off", [(1000.0, 1010.0, 1), (1000.0, 1010.0, 0), (720.0, 730.0, 1)])
+def test_window_without_line_centres(gpu_lib, oracle_mod, precision, v1, v2, contnm_off):
+    """A window that no line centre reaches: far from every line the OD is
+    zero, or the continuum alone; 20-30 cm-1 past the last line only the far
+    wings (BOUND4 = 25 cm-1) reach it"""
+    lines, col = _layer_case(5000, 600.0, 700.0, seed=4, wabs=1e21)
+    col = col.with_window(v1, v2)
+    cont = synth.continuum() if contnm_off == 0 else None
+    od, ref = _compare(gpu_lib, oracle_mod, lines, col, cont=cont, contnm_off=contnm_off, precision=precision)
+    st_zero = v1 >= 1000.0 and contnm_off == 1
+    if st_zero:
+        assert np.all(od == 0.0) and np.all(ref == 0.0)
+    else:
+        assert np.max(np.abs(ref)) > 0.0
+        tol = 1e-5 if precision == T.CLBLM_PREC_MIXED else 1e-9
+        rel = np.max(np.abs(od - ref)) / np.max(np.abs(ref))
+        assert rel <= tol, rel
+
+
 @pytest.mark.parametrize("layer", [0, 30, 59])
 def test_config1_layers_narrow_window(gpu_lib, oracle_mod, layer):
     lines, col, cont = synth.config1(n_lines=50000)
