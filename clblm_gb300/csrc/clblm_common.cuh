@@ -7,6 +7,7 @@
 // VFT of panel p, the array limits MAX1..MAX3, the far-wing grid, ...
 #pragma once
 #include <cstdint>
+#include "clblm_fpconv.cuh"
 
 namespace clblm {
 
@@ -145,15 +146,17 @@ __device__ __forceinline__ CnvfnqSetup cnvfnq_setup(const LayerPlan& P, double v
   s.zslope = __dmul_rn(recalf, P.wavdxf);
   const double ZINT = __ddiv_rn(__dsub_rn(vnu, vft_q), P.dv);
   s.zint = ZINT;
-  s.jmax1 = (int)__dadd_rn(__dadd_rn(ZINT, bhwdxf), 1.5);
-  s.jmin1 = (int)__dadd_rn(__dsub_rn(ZINT, bhwdxf), 1.5);
+  // INT truncations and the integer-to-binary64 conversions are exact
+  // integer arithmetic (clblm_fpconv.cuh): the binary64 pipe keeps the sums
+  s.jmax1 = f64_to_i32_trunc(__dadd_rn(__dadd_rn(ZINT, bhwdxf), 1.5));
+  s.jmin1 = f64_to_i32_trunc(__dadd_rn(__dsub_rn(ZINT, bhwdxf), 1.5));
   const double RSHFT = ZINT < 0.0 ? -0.5 : 0.5;
-  s.j2shft = (int)__dadd_rn(__dmul_rn(ZINT, P.omconf2), RSHFT);
-  s.j3shft = (int)__dadd_rn(__dmul_rn(ZINT, P.omconf3), RSHFT);
+  s.j2shft = f64_to_i32_trunc(__dadd_rn(__dmul_rn(ZINT, P.omconf2), RSHFT));
+  s.j3shft = f64_to_i32_trunc(__dadd_rn(__dmul_rn(ZINT, P.omconf3), RSHFT));
   const int JMIN2 = s.jmin1 - s.j2shft, JMIN3 = s.jmin1 - s.j3shft;
-  s.zf[0] = __dmul_rn(__dsub_rn((double)(s.jmin1 - 2), ZINT), s.zslope);
-  s.zf[1] = __dmul_rn(__dsub_rn((double)(JMIN2 - 2), __dmul_rn(ZINT, CONF2)), s.zslope);
-  s.zf[2] = __dmul_rn(__dsub_rn((double)(JMIN3 - 2), __dmul_rn(ZINT, CONF3)), s.zslope);
+  s.zf[0] = __dmul_rn(__dsub_rn(i32_to_f64(s.jmin1 - 2), ZINT), s.zslope);
+  s.zf[1] = __dmul_rn(__dsub_rn(i32_to_f64(JMIN2 - 2), __dmul_rn(ZINT, CONF2)), s.zslope);
+  s.zf[2] = __dmul_rn(__dsub_rn(i32_to_f64(JMIN3 - 2), __dmul_rn(ZINT, CONF3)), s.zslope);
   return s;
 }
 #endif

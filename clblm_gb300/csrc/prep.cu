@@ -17,6 +17,7 @@
 //   k_f4_count/compact/walk/groupsum  the LINF4Q record loop with SHRINQ
 //                    (:959-1234, :1516-1647)
 #include "clblm_common.cuh"
+#include "clblm_fpconv.cuh"
 #include "clblm_kernels.cuh"
 #include "clblm_panel.cuh"
 
@@ -78,7 +79,7 @@ __device__ __forceinline__ bool fits_panel(double vnu, double vft, double dv, do
 __device__ __forceinline__ bool fits_panel_fast(double vnu, double vft, float rdv_f, float bhwdxf_f, double dv,
                                                 double rdv, double bhwdxf, int max1) {
   const double d = vnu - vft;
-  const float dr = (float)d * rdv_f;
+  const float dr = f64_to_f32(d) * rdv_f;
   const float a = dr + bhwdxf_f + 1.5f;
   const float lim = (float)(max1 + 1);
   if (fabsf(a - lim) > 1e-2f + 1e-6f * (fabsf(dr) + bhwdxf_f)) return a < lim;
@@ -165,7 +166,7 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
     if (ok && iso > c_MAXISO[m]) ok = false;
     double SUI = 0.;
     if (ok) {
-      SUI = (double)lines.sp[i] * P.wk[m];
+      SUI = f32_to_f64(lines.sp[i]) * P.wk[m];
       if (SUI == 0.) ok = false;
     }
     if (ok) {
@@ -184,15 +185,17 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
           GAMMA2 = cb;
         }
       }
-      double alfa0 = (double)lines.alfa[i];
-      double hwhms = (double)lines.hwhm[i];
+      // the line's FP32 fields widened in integer arithmetic (exact, as the
+      // hardware conversion, without its binary64 pipe)
+      double alfa0 = f32_to_f64(lines.alfa[i]);
+      double hwhms = f32_to_f64(lines.hwhm[i]);
       // air-broadened widths of O2 and N2 to foreign widths (RDLIN :2728-2745)
       if (m == 7 || m == 22) {
         const double rvmr = m == 7 ? 0.21 : 0.79;
         alfa0 = (alfa0 - rvmr * hwhms) / (1.0 - rvmr);
       }
-      double VNU = lines.vnu[i] + P.rhorat * (double)lines.pshift[i];
-      double TMPCOR = exp((double)lines.tmpalf[i] * P.ln_tratio);  // (T/296)^n
+      double VNU = lines.vnu[i] + P.rhorat * f32_to_f64(lines.pshift[i]);
+      double TMPCOR = exp(f32_to_f64(lines.tmpalf[i]) * P.ln_tratio);  // (T/296)^n
       double ALFA0I = alfa0 * TMPCOR;
       double HWHMSI = hwhms * TMPCOR;
       double ALFL = ALFA0I * R.rhodif + HWHMSI * R.rhoslf;  // RHODIF = RHORAT - RHOSLF
@@ -200,12 +203,12 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
       double ALFAD = VNU * R.alfd1;
       double ZETA = ALFL / (ALFL + ALFAD);
       double FZETA = 100. * ZETA;
-      int IZ = (int)(FZETA + kONEPL);
+      int IZ = f64_to_i32_trunc(FZETA + kONEPL);
       if (!(IZ >= 1 && IZ <= 101)) {
         bad++;
         ok = false;
       } else {
-        double ZETDIF = FZETA - (double)(IZ - 1);
+        double ZETDIF = FZETA - i32_to_f64(IZ - 1);
         double ALFV = (c_AVRAT[IZ - 1] + ZETDIF * (c_AVRAT[IZ] - c_AVRAT[IZ - 1])) * (ALFL + ALFAD);
         int nmin = 0, npl = 0;
         if (ALFV < P.dv) {
@@ -229,12 +232,12 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             // strengths set no index: FP32 (RADFN when JRAD = 1, SCOR, the
             // lower-state Boltzmann factor and the stimulated-emission term);
             // EPP's tests are the binary64 ones, exactly
-            float sui = (float)SUI;
-            if (P.jrad == 1) sui *= radfn_f((float)lines.vnu[i], P.xkt_f);
+            float sui = f64_to_f32(SUI);
+            if (P.jrad == 1) sui *= radfn_f(f64_to_f32(lines.vnu[i]), P.xkt_f);
             const float EPP = EPP0 <= P.epp_abs_f ? fabsf(EPP0) : EPP0;
             if (EPP > P.epp_neg_f)
-              sui = sui * R.scor_f * __expf(-EPP * P.betacr_f) * (1.f + __expf(-(float)VNU / P.xkt_f));
-            SUI = sui;
+              sui = sui * R.scor_f * __expf(-EPP * P.betacr_f) * (1.f + __expf(-f64_to_f32(VNU) / P.xkt_f));
+            SUI = f32_to_f64(sui);
             SP = (Cpl && iflg == 1) ? SUI * (1. + GI * P.pavp2) : SUI;  // SUI*(1 + G*PAVP2)
             // SPEAK = SUI/ALFV > 0 unless SUI = 0 (SUI >= 1e-45, 1/ALFV > 1:
             // no underflow), so with DPTMIN = 0 the test is SUI = 0
@@ -269,8 +272,8 @@ __global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, Lin
             double BHWDXF = HWDXF / ZSLOPE;
             r.alfv = ALFV;
             r.bhwdxf = BHWDXF;
-            const float rdv_f = (float)P.rdv, bh_f = (float)BHWDXF;
-            const float est = ((float)(VNU - vft[0]) * rdv_f + bh_f + 1.5f - (float)P.max1) * (1.f / kPanelPts);
+            const float rdv_f = f64_to_f32(P.rdv), bh_f = f64_to_f32(BHWDXF);
+            const float est = (f64_to_f32(VNU - vft[0]) * rdv_f + bh_f + 1.5f - (float)P.max1) * (1.f / kPanelPts);
             int p = est > 0.f ? (int)fminf(est, 2.e9f) : 0;
             if (p > P.npanels) p = P.npanels;
             while (p > 0 && fits_panel_fast(VNU, vft[p - 1], rdv_f, bh_f, P.dv, P.rdv, BHWDXF, P.max1)) p--;
@@ -440,7 +443,7 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       double STRFA1 = 0., STRFA2 = 0., STRFA3 = 0., STRDA = 0., STRVRA = 0.;
       float c[5];  // the same, FP32 (mixed path)
       if (P.mixed) {  // shape coefficients set no index: FP32
-        const float zd = (float)ZETDIF, de = (float)DEPTHA;
+        const float zd = f64_to_f32(ZETDIF), de = f64_to_f32(DEPTHA);
         for (int q5 = 0; q5 < 5; ++q5) {
           const float* T = c_SHAPEf[q5];
           c[q5] = de * (T[IZM - 1] + zd * (T[IZM] - T[IZM - 1]));
@@ -472,10 +475,13 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
       g2.g_hi = kPanelR2 * q + (JMAX1 - J2SHFT) - 1;
       g3.g_lo = kPanelR3 * q + JMIN3 - 1;
       g3.g_hi = kPanelR3 * q + (JMAX1 - J3SHFT) - 1;
-      g1.zfl = (float)ZF1L;
-      g2.zfl = (float)ZF2L;
-      g3.zfl = (float)ZF3L;
-      g1.zs = g2.zs = g3.zs = (float)ZSLOPE;
+      // FP32 copies and their residuals (the float-float index near a
+      // rounding boundary), converted in integer arithmetic
+      float lo1, lo2, lo3, zs_lo;
+      g1.zfl = f64_to_f32_split(ZF1L, &lo1);
+      g2.zfl = f64_to_f32_split(ZF2L, &lo2);
+      g3.zfl = f64_to_f32_split(ZF3L, &lo3);
+      g1.zs = g2.zs = g3.zs = f64_to_f32_split(ZSLOPE, &zs_lo);
       g1.a0 = c[0];
       g1.a1 = c[3];
       g1.a2 = c[4];
@@ -486,10 +492,9 @@ __global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, 
         d2 = {ZF2L, ZSLOPE, STRFA2, 0., 0.};
         d3 = {ZF3L, ZSLOPE, STRFA3, 0., 0.};
       }
-      const float zs_lo = (float)(ZSLOPE - (double)g1.zs);
-      l1 = {(float)(ZF1L - (double)g1.zfl), zs_lo};
-      l2 = {(float)(ZF2L - (double)g2.zfl), zs_lo};
-      l3 = {(float)(ZF3L - (double)g3.zfl), zs_lo};
+      l1 = {lo1, zs_lo};
+      l2 = {lo2, zs_lo};
+      l3 = {lo3, zs_lo};
       amax = fmax(amax, lp.alfv);
       // a coupled line (SPPSP != 0, tested on the bits: no FP64 compare) has
       // its records go the exact way
