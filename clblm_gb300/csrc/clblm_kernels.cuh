@@ -90,16 +90,22 @@ extern __constant__ float c_AVRATf[102];
 // records.  (A template kernel's declaration repeats its definition's
 // parameter qualifiers exactly: nvcc takes a difference in __restrict__ for
 // another template, whose explicit instantiation then has no device code.)
+// The two per-line set-up kernels are bound by the binary64 pipe and wait on
+// its results: three CTAs of 256 threads per SM (80 registers) keep more
+// warps in flight than the two their register use would allow.
+constexpr int kSetupThreads = 256, kSetupMinBlocks = 3;
 template <bool Cpl>
-__global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
-                            const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
-                            LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats);
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+    k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines, const IsoRow* __restrict__ iso_tab,
+                const double* __restrict__ vft_all, LinePrep* __restrict__ out, int64_t out_stride,
+                unsigned long long* __restrict__ stats);
 __global__ void k_scan_blockmax(const LinePrep* prep, int64_t stride, const int64_t* nlines, int* blockmax,
                                 int nblk_stride);
 __global__ void k_scan_blocks(int* blockmax, int nblk_stride, const int64_t* nlines, int nlayers);
 __global__ void k_scan_apply(const LinePrep* prep, int64_t stride, const int64_t* nlines, const int* blockmax,
                              int nblk_stride, int* qpanel);
-__global__ void k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+    k_line_records(const LayerPlan* plans, int layer0, const double* vft_all, const LinePrep* prep,
                                const int* qpanel, int64_t stride, GridRec* rec, GridRecD* recd,
                                GridRecLo* reclo, double* cpl, unsigned long long* stats,
                                double* alfvmax, int* aggmax, int* aggmin, int nagg);

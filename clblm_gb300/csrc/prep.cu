@@ -137,7 +137,8 @@ __device__ __forceinline__ void lc_coefs(const LineIn& L, int64_t k, int ilc, do
 }
 
 template <bool Cpl>
-__global__ void k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+    k_line_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                             const IsoRow* __restrict__ iso_tab, const double* __restrict__ vft_all,
                             LinePrep* __restrict__ out, int64_t out_stride, unsigned long long* __restrict__ stats) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
@@ -395,7 +396,8 @@ __device__ __forceinline__ void interp_coef(const double* tab, int IZM, double Z
   *out = DEPTHA * (tab[IZM - 1] + ZETDIF * (tab[IZM] - tab[IZM - 1]));
 }
 
-__global__ void k_line_records(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vft_all,
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+    k_line_records(const LayerPlan* __restrict__ plans, int layer0, const double* __restrict__ vft_all,
                                const LinePrep* __restrict__ prep, const int* __restrict__ qpanel, int64_t stride,
                                GridRec* __restrict__ rec, GridRecD* __restrict__ recd,
                                GridRecLo* __restrict__ reclo, double* __restrict__ cpl,
