@@ -139,7 +139,8 @@ __global__ void k_f4_groupsum(const LayerPlan* plans, int layer0, const F4Prep* 
                               const int64_t* src, const int4* groups, const int64_t* ngroups, ShrunkLine* out);
 struct F4Rec;
 struct F4RecD;
-__global__ void k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
+__global__ void __launch_bounds__(kSetupThreads, 3)
+    k_f4_lineinit(const LayerPlan* plans, int layer0, const ShrunkLine* sh, int64_t stride,
                               const int64_t* nsh, F4Rec* rec, F4RecD* recd, int64_t rstride, int64_t* nrec,
                               int64_t* nmirror, unsigned long long* stats, double* cpl);
 // layer averages and amounts of a nadir path (ALAYER + FPACK)

@@ -1942,7 +1942,8 @@ __device__ void f4_record(const LayerPlan& P, const ShrunkLine& L, double VNUI, 
   }
 }
 
-__global__ void k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
+__global__ void __launch_bounds__(kSetupThreads, 3)
+    k_f4_lineinit(const LayerPlan* __restrict__ plans, int layer0, const ShrunkLine* __restrict__ sh,
                               int64_t stride, const int64_t* __restrict__ nsh, F4Rec* __restrict__ rec,
                               F4RecD* __restrict__ recd, int64_t rstride, int64_t* __restrict__ nrec,
                               int64_t* __restrict__ nmirror, unsigned long long* __restrict__ stats,
