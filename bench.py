@@ -124,8 +124,13 @@ def roofline(work, kt, steps, ms_step, points):
         hbm = hbm_peak_gbs()
         ms_rt = kt["ms_rt"] / steps
         ach = work["rt_bytes"] / (ms_rt * 1e-3) / 1e9
+        bpp = traffic.get("k_rt_segment")
         out["k_rt_segment"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                               "traffic": None, "ms_per_step": ms_rt, "share_of_step": ms_rt / ms_step,
+                               "traffic": bpp * points if bpp is not None else None,
+                               "traffic_source": ("scaled from a stored ncu capture: DRAM bytes per layer point "
+                                                  "(profiles/dram_traffic.txt) x this step's layer points"
+                                                  if bpp is not None else None),
+                               "ms_per_step": ms_rt, "share_of_step": ms_rt / ms_step,
                                "bytes_per_step": work["rt_bytes"],
                                "bytes_counted": "every layer's OD once, the merged radiance and reflectance in and "
                                                 "out once per run of layers on one merge grid",
