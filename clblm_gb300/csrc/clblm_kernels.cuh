@@ -113,7 +113,8 @@ __global__ void k_panel_ranges(const LayerPlan* plans, int layer0, const double*
                                double shiftmax, int64_t* ranges, int64_t panel_stride);
 __global__ void k_continuum(const LayerPlan* plans, int layer0, ContIn cont, double* absrb_all);
 template <bool Cpl>
-__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+__global__ void __launch_bounds__(kSetupThreads, 4)
+    k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                           const IsoRow* __restrict__ iso_tab, F4Prep* __restrict__ out, int64_t stride,
                           unsigned long long* __restrict__ stats);
 __global__ void k_f4_count(const F4Prep* prep, int64_t stride, const LayerPlan* plans, int layer0, int64_t* blocksum,

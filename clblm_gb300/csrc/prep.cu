@@ -1198,7 +1198,8 @@ __global__ void k_continuum(const LayerPlan* __restrict__ plans, int layer0, Con
 
 // ---- far-wing lines: LINF4Q per-line corrections --------------------------
 template <bool Cpl>
-__global__ void k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
+__global__ void __launch_bounds__(kSetupThreads, 4)
+    k_f4_prep(const LayerPlan* __restrict__ plans, int layer0, LineIn lines,
                           const IsoRow* __restrict__ iso_tab, F4Prep* __restrict__ out, int64_t stride,
                           unsigned long long* __restrict__ stats) {
   const LayerPlan& P = plans[blockIdx.y + layer0];
