@@ -46,6 +46,21 @@ __global__ void k_interp_map(InterpSpec s, const int64_t* __restrict__ blk_j1, c
   const int64_t J1 = blk_j1[b];
   if (J1 < 1 || J1 > nout) return;  // a block start off the output grid writes nothing
   const int64_t J2 = min(nout, J1 + 2400 - 1);
+  if (s.ratio < 0.999) {
+    // P < 1 on entry to every step, so P + RATIO < 1.999: a carry is INT(P)
+    // = 1 and INT(iIn + P) = iIn + 1, and P - 1 is exact (the same values,
+    // with a shorter chain of dependent binary64 operations per step)
+    for (int64_t J = J1; J <= J2; ++J) {
+      int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
+      map[J - 1] = make_int2((int)iIn, IP < 0 ? 0 : (IP > 202 ? 202 : IP));
+      P = __dadd_rn(P, s.ratio);
+      if (P >= 1.0) {
+        iIn += 1;
+        P = __dadd_rn(P, -1.0);
+      }
+    }
+    return;
+  }
   for (int64_t J = J1; J <= J2; ++J) {
     int IP = (int)__dadd_rn(__dmul_rn(P, 201.), 1.00001);
     map[J - 1] = make_int2((int)iIn, IP < 0 ? 0 : (IP > 202 ? 202 : IP));
